@@ -1,0 +1,329 @@
+/*
+ * phx_fluid.h -- C ABI of the GB300 (sm_103a) GRMHD fluid hot path.
+ *
+ * This is the drop-in boundary for the fluid update of phoebus (lanl/phoebus).
+ * Every entry point below replaces one Parthenon task of the reference fluid
+ * package (file:line cited beside each declaration, paths relative to the
+ * phoebus source tree).  The C++ shim in phx_parthenon_shim.hpp keeps the
+ * reference's task signatures and forwards to these functions.
+ *
+ * Conventions
+ *   - All arrays are caller-owned DEVICE memory, FP64, structure-of-arrays:
+ *     field(v, k, j, i) = base[v * var_stride + (k * n2t + j) * n1t + i],
+ *     with i fastest.  n1t = nx1 + 2 ng, n2t = nx2 + 2 ng (1 when ndim < 2),
+ *     n3t = nx3 + 2 ng (1 when ndim < 3).  This is Parthenon's per-variable
+ *     View layout, so packs can be passed through without copies.
+ *   - Index ranges (phx_range) are inclusive, in ghost-inclusive indices,
+ *     exactly like Parthenon's IndexRange.
+ *   - Every call is asynchronous on the given CUDA stream (cudaStream_t passed
+ *     as void*; NULL = legacy default stream).  Nothing is allocated inside a
+ *     call; scratch lives in the phx_ctx or in caller-owned block fields.
+ *   - Device code never traps.  Per-zone failures are written as the
+ *     reference's fail flags (1.0 success / 0.0 failure).  Conditions the
+ *     reference aborts on (an unbracketed con2prim root) are recorded in the
+ *     context's sticky error word, read with phx_ctx_check().
+ */
+#ifndef PHX_FLUID_H_
+#define PHX_FLUID_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PHX_ABI_VERSION 1
+
+/* ---- variable indices ------------------------------------------------- */
+/* Primitive block (prim[PHX_NPRIM][N]).  The first PHX_NRECON entries are the
+ * reconstructed variables, in the order the reference registers them
+ * (fluid.cpp:272-286: density, velocity(3), energy, bfield(3), pressure,
+ * gamma1).  The reference takes its flux (conserved) indices from this same
+ * map (riemann.hpp:240-245). */
+enum {
+  PHX_PRHO = 0,  /* rest-mass density rho                           */
+  PHX_PVEL = 1,  /* W v^i (3 entries, normal-observer 3-velocity * W) */
+  PHX_PENG = 4,  /* internal energy density u = rho * eps            */
+  PHX_PB = 5,    /* B^i (3 entries)                                  */
+  PHX_PPRS = 8,  /* pressure                                         */
+  PHX_PGM1 = 9,  /* gamma1 = bulk modulus / pressure                 */
+  PHX_PTMP = 10, /* temperature                                      */
+  PHX_PMU = 11,  /* c2p_mu: last con2prim root (warm-start guess)    */
+  PHX_NPRIM = 12,
+  PHX_NRECON = 10
+};
+/* Conserved block (cons[PHX_NCONS][N]), densitized by sqrt(gamma). */
+enum {
+  PHX_CRHO = 0, /* D = sqrt(gamma) rho W            */
+  PHX_CMOM = 1, /* S_i (3 entries)                  */
+  PHX_CENG = 4, /* tau (Valencia energy)            */
+  PHX_CB = 5,   /* sqrt(gamma) B^i (3 entries)      */
+  PHX_NCONS = 8
+};
+
+typedef enum {
+  PHX_OK = 0,
+  PHX_ERR_INVALID_ARG = 1,
+  PHX_ERR_UNBRACKETED = 2, /* con2prim root not bracketed (reference aborts) */
+  PHX_ERR_NAN_INPUT = 3,
+  PHX_ERR_TIMEOUT = 4,     /* a bounded device wait gave up                */
+  PHX_ERR_CUDA = 5,
+  PHX_ERR_NO_DEVICE = 6,
+  PHX_ERR_CAPACITY = 7,    /* request larger than a fixed-size buffer      */
+  PHX_ERR_UNSUPPORTED = 8
+} phx_status;
+
+typedef enum { /* reconstruction.hpp:23 ReconType */
+  PHX_RECON_CONSTANT = 0,
+  PHX_RECON_LINEAR = 1, /* PLM, MC limiter with alpha = 1.5            */
+  PHX_RECON_WENO5Z = 2, /* WENO5-Z blended with MC (alpha = 2)         */
+  PHX_RECON_MP5 = 3
+} phx_recon;
+
+typedef enum { PHX_RIEMANN_LLF = 0, PHX_RIEMANN_HLL = 1 } phx_riemann; /* riemann.hpp:30 */
+
+typedef enum { PHX_GEOM_MINKOWSKI = 0, PHX_GEOM_FMKS = 1 } phx_geom_kind;
+
+typedef enum { /* fixup.hpp FloorFlag */
+  PHX_FLOOR_CONSTANT_RHO_SIE = 0,
+  PHX_FLOOR_EXPX1_RHO_SIE = 1,
+  PHX_FLOOR_EXPX1_RHO_U = 2,
+  PHX_FLOOR_X1_RHO_SIE = 3,
+  PHX_FLOOR_R_RHO_SIE = 4
+} phx_floor_type;
+
+typedef struct {
+  int s, e; /* inclusive, ghost-inclusive */
+} phx_range;
+
+/* Physics parameters: the fluid, fixup and eos package Params the hot path
+ * reads (fluid.cpp:53-136, fixup.cpp:48-280, eos_phoebus.cpp:73-95).  Fill
+ * with phx_params_default() and override. */
+typedef struct {
+  /* ideal-gas EOS (singularity-eos IdealGas in scale-free units) */
+  double gm1;  /* Gamma - 1 */
+  double Cv;
+  double rho_min_eos, sie_min_eos; /* eos/rho_min, eos/sie_min (default 0) */
+  /* con2prim (fluid.cpp:76-94) */
+  double c2p_tol;
+  int c2p_max_iter;
+  double c2p_floor_scale_fac;
+  int c2p_fail_on_floors;
+  int c2p_fail_on_ceilings;
+  /* reconstruction / Riemann solver / timestep */
+  int recon;   /* phx_recon   */
+  int riemann; /* phx_riemann */
+  double cfl;
+  int mhd;     /* fluid/mhd: 1 = B evolved (FluxCT applied) */
+  /* fixup package */
+  int enable_floors, enable_ceilings, enable_mhd_floors, enable_c2p_fixup;
+  int c2p_failure_strategy_floors; /* 0 = interpolate (default), 1 = floors */
+  int floor_type;                  /* phx_floor_type */
+  double rho0_floor, sie0_floor, rho_exp_floor, sie_exp_floor;
+  double gam0_ceiling, sie0_ceiling;         /* ConstantGamSie ceilings */
+  double bsqorho0_ceiling, bsqou0_ceiling;   /* ConstantBsqRat ceilings */
+} phx_params;
+
+/* Geometry.  Minkowski is constant-folded into the kernels.  FMKS
+ * (Modified<SphericalKerrSchild, McKinneyGammieRyan>, fmks.hpp:44) is read
+ * from axisymmetric per-block tables, the layout of the reference's cached
+ * geometry (cached_system.hpp:474-560 with geometry/axisymmetric = true).
+ * Each location table holds PHX_GEOM_NLOC values per (j, i):
+ *   alpha, beta^1..3, gcov (10, symmetric, Flatten2 order), gamcon (6,
+ *   symmetric), sqrt(gamma).
+ * Cell-centre derivative table: dlnalpha/dX^1..3 (3), dg_{mu nu}/dX^1..3
+ * (10 x 3).  Tables are filled by phx_geometry_fill_fmks or by the caller. */
+enum {
+  PHX_G_ALPHA = 0,
+  PHX_G_BETA = 1,
+  PHX_G_GCOV = 4,
+  PHX_G_GAMCON = 14,
+  PHX_G_DETGAM = 20,
+  PHX_GEOM_NLOC = 21,
+  PHX_GD_DALPHA = 0,
+  PHX_GD_DG = 3,
+  PHX_GEOM_NDER = 33
+};
+
+typedef struct {
+  int kind; /* phx_geom_kind */
+  /* FMKS parameters (fmks.cpp:37-88 defaults in phx_geometry_default) */
+  double a, hslope, poly_xt, poly_alpha, x0, smooth, hexp_br, hexp_nsq, hexp_csq;
+  int derefine_poles;
+  /* tables (device pointers; NULL for Minkowski).  Leading dimension is
+   * the variable, then j, then i. */
+  double *cent;  /* [PHX_GEOM_NLOC][n2t][n1t]     cell centres (and X3 faces)   */
+  double *face1; /* [PHX_GEOM_NLOC][n2t][n1t + 1] X1 faces                      */
+  double *face2; /* [PHX_GEOM_NLOC][n2t + 1][n1t] X2 faces                      */
+  double *deriv; /* [PHX_GEOM_NDER][n2t][n1t]     cell-centre derivatives       */
+} phx_geometry;
+
+/* One meshblock.  Coordinates are Parthenon UniformCartesian:
+ * Xf(i) = (xmin - ng dx) + i dx, Xc(i) = (xmin - ng dx) + (i + 1/2) dx for
+ * active dimensions (xmin is the interior lower edge); an inactive
+ * dimension has a single zone with Xc = xmin + dx/2. */
+typedef struct {
+  int nx1, nx2, nx3; /* interior zones (1 for inactive dimensions) */
+  int ng;            /* ghost zones per side (4 for WENO5-Z / MP5)  */
+  int ndim;          /* 1, 2 or 3 */
+  long long var_stride; /* elements between variables; 0 = n1t*n2t*n3t */
+  double x1min, x2min, x3min;
+  double dx1, dx2, dx3;
+  double *prim;     /* [PHX_NPRIM][N]                                   */
+  double *cons;     /* [PHX_NCONS][N]                                   */
+  double *flux;     /* [3][PHX_NCONS][N]  flux(d, m, k, j, i)           */
+  double *face_sig; /* [3][N] face signal speed                        */
+  double *cell_sig; /* [3][N] cell signal speed                        */
+  double *fail;     /* [N]    1.0 = con2prim success, 0.0 = failure     */
+  double *src;      /* [4][N] geometric sources for S_1..3 and tau      */
+  double *emf;      /* [3][N] FluxCT edge EMFs (scratch)                */
+  double *dudt;     /* [PHX_NCONS][N] right-hand side (scratch)         */
+  const phx_geometry *geom; /* NULL = Minkowski */
+} phx_block;
+
+/* con2prim statistics, accumulated on the device by every con2prim call
+ * (the reference's CON2PRIM_STATISTICS histogram, con2prim_statistics.hpp). */
+#define PHX_C2P_HIST 128
+typedef struct {
+  unsigned long long zones;
+  unsigned long long iterations;     /* sum of root-find iterations      */
+  unsigned long long residual_evals; /* sum of residual evaluations      */
+  unsigned long long failures;       /* zones flagged fail = 0.0         */
+  unsigned long long unbracketed;    /* zones whose root was not bracketed */
+  unsigned long long learned_accepted; /* learned brackets that bracketed */
+  unsigned long long hist[PHX_C2P_HIST]; /* iteration-count histogram     */
+} phx_c2p_stats;
+
+typedef struct phx_ctx phx_ctx;
+
+/* ---- context ----------------------------------------------------------- */
+phx_status phx_ctx_create(int device, phx_ctx **out);
+phx_status phx_ctx_destroy(phx_ctx *ctx);
+/* Synchronise the device and return (and clear) the sticky error word. */
+phx_status phx_ctx_check(phx_ctx *ctx);
+/* Copy (and optionally reset) the device-side con2prim statistics. */
+phx_status phx_ctx_c2p_stats(phx_ctx *ctx, phx_c2p_stats *out, int reset);
+const char *phx_status_string(phx_status s);
+/* Human-readable detail of the last host-side error in this thread. */
+const char *phx_last_error(void);
+int phx_abi_version(void);
+/* Build flavour: 1 when compiled without FMA contraction (bit-exact parity
+ * build), 0 for the production build. */
+int phx_build_exact(void);
+
+void phx_params_default(phx_params *p);
+void phx_geometry_default(phx_geometry *g, int kind);
+
+/* ---- hot-path entry points -------------------------------------------- */
+
+/* fluid::PrimitiveToConservedRegion (fluid.cpp:368-449).  Writes cons and
+ * cell_sig over the range. */
+phx_status phx_prim_to_con(phx_ctx *ctx, const phx_params *p, const phx_block *b,
+                           phx_range ib, phx_range jb, phx_range kb, void *stream);
+
+/* fluid::ConservedToPrimitiveRegion with the robust solver
+ * (fluid.cpp:451-517, con2prim_robust.hpp:299-453).  Reads cons and the
+ * c2p_mu guess, writes prims, fail, cell_sig and (when bounds were applied)
+ * cons. */
+phx_status phx_con_to_prim(phx_ctx *ctx, const phx_params *p, const phx_block *b,
+                           phx_range ib, phx_range jb, phx_range kb, void *stream);
+
+/* Same as phx_con_to_prim, but the starting bracket comes from the learned
+ * guess network loaded into ctx (phx_mlp_set_weights).  The FP64 root find
+ * and its fallback to the reference bracket are unchanged. */
+phx_status phx_con_to_prim_learned(phx_ctx *ctx, const phx_params *p, const phx_block *b,
+                                   phx_range ib, phx_range jb, phx_range kb,
+                                   void *stream);
+
+/* fluid::CalculateFluxes (fluid.cpp:659-773): reconstruction + LLF/HLL.
+ * Writes flux(d, m) and face_sig(d) on every face the reference's divergence
+ * and FluxCT read. */
+phx_status phx_calculate_fluxes(phx_ctx *ctx, const phx_params *p, const phx_block *b,
+                                void *stream);
+
+/* fluid::FluxCT (fluid.cpp:775-841). */
+phx_status phx_flux_ct(phx_ctx *ctx, const phx_params *p, const phx_block *b,
+                       void *stream);
+
+/* fluid::CalculateFluidSourceTerms (fluid.cpp:566-657) over nblocks blocks
+ * (a MeshData pack).  Writes src. */
+phx_status phx_calculate_fluid_source_terms(phx_ctx *ctx, const phx_params *p,
+                                            const phx_block *blocks, int nblocks,
+                                            void *stream);
+
+/* Stage glue of PhoebusDriver::RungeKuttaStage (phoebus_driver.cpp:547-577):
+ * dudt = FluxDivergence + src (SumData), cons0 = beta cons0 + (1-beta) base
+ * (AverageIndependentData), out = cons0 + beta dt dudt (UpdateIndependentData).
+ * base may equal cons0 (first stage); out may equal base. */
+phx_status phx_update_stage(phx_ctx *ctx, const phx_block *b, const double *cons_base,
+                            double *cons_out, double beta, double dt, void *stream);
+
+/* Periodic ghost fill of nvar variables starting at field (Parthenon's
+ * periodic boundary exchange for a single block). */
+phx_status phx_fill_ghosts_periodic(phx_ctx *ctx, const phx_block *b, double *field,
+                                    int nvar, void *stream);
+
+/* fluid::EstimateTimestepBlock (fluid.cpp:899-944).  use_face_speeds selects
+ * the reference's second form.  The result (cfl * min dt) is written to
+ * *dt_out_device (device memory) without synchronising. */
+phx_status phx_estimate_timestep(phx_ctx *ctx, const phx_params *p, const phx_block *b,
+                                 int use_face_speeds, double *dt_out_device,
+                                 void *stream);
+
+/* fixup::ConservedToPrimitiveFixup (fixup_c2p.cpp:44-356), interior zones. */
+phx_status phx_c2p_fixup(phx_ctx *ctx, const phx_params *p, const phx_block *b,
+                         void *stream);
+
+/* fixup::ApplyFloors (fixup.cpp:285-687), range as in the reference. */
+phx_status phx_apply_floors(phx_ctx *ctx, const phx_params *p, const phx_block *b,
+                            phx_range ib, phx_range jb, phx_range kb, void *stream);
+
+/* Fill the FMKS geometry tables of g for block b (cached_system.hpp:560-640
+ * "analytic" branch: point evaluations and finite-difference derivatives). */
+phx_status phx_geometry_fill_fmks(phx_ctx *ctx, const phx_geometry *g, const phx_block *b,
+                                  void *stream);
+
+/* One full RK stage for one block with periodic boundaries, in the order
+ * of PhoebusDriver::RungeKuttaStage (phoebus_driver.cpp:204-738): sources,
+ * fluxes, FluxCT, divergence + SumData + Average + Update, con2prim over the
+ * entire block, [c2p fixup, floors], ghost exchange of the conserved
+ * variables, con2prim over the entire block again, [c2p fixup, floors].
+ * b->cons is the stage input (prims consistent with it), cons_base the state
+ * at the start of the step, cons_out receives the stage result (it may alias
+ * cons_base); on return the prims are consistent with cons_out.  Heun RK2:
+ * stage 1 (beta = 1) cons = base -> out = second buffer; stage 2
+ * (beta = 1/2) cons = second buffer -> out = base. */
+phx_status phx_stage(phx_ctx *ctx, const phx_params *p, const phx_block *b,
+                     const double *cons_base, double *cons_out, double beta, double dt,
+                     int use_learned_guess, void *stream);
+
+/* Batched uneven meshblocks: the same stage over nblocks independent
+ * (periodic) blocks of mixed sizes, each kernel phase one persistent launch
+ * walking a device work list.  cons_base[n] / cons_out[n] per block. */
+phx_status phx_stage_batched(phx_ctx *ctx, const phx_params *p, const phx_block *blocks,
+                             int nblocks, const double *const *cons_base,
+                             double *const *cons_out, double beta, double dt,
+                             int use_learned_guess, void *stream);
+
+/* ---- learned con2prim guess (no reference counterpart) ---------------- */
+/* Network 6 -> 64 -> 64 -> 64 -> 2, GELU, BF16 weights, FP32 accumulate. */
+#define PHX_MLP_IN 6
+#define PHX_MLP_HID 64
+#define PHX_MLP_OUT 2
+#define PHX_MLP_NPARAM (PHX_MLP_IN * PHX_MLP_HID + PHX_MLP_HID + \
+                        2 * (PHX_MLP_HID * PHX_MLP_HID + PHX_MLP_HID) + \
+                        PHX_MLP_HID * PHX_MLP_OUT + PHX_MLP_OUT)
+/* Load FP32 master parameters (host memory, PHX_MLP_NPARAM floats). */
+phx_status phx_mlp_set_weights(phx_ctx *ctx, const float *params_host);
+phx_status phx_mlp_get_weights(phx_ctx *ctx, float *params_host);
+
+/* ---- measurement probe -------------------------------------------------- */
+/* Time a dependent-chain-free FP64 FMA loop and report FLOP/s (2 per FMA).
+ * Used to measure the FP64 roofline of the device the library runs on. */
+phx_status phx_probe_fp64_peak(phx_ctx *ctx, double *flops_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PHX_FLUID_H_ */

@@ -1,0 +1,175 @@
+"""ctypes wrapper of the CPU oracle (oracle/phx_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg, as the checker.  The product never loads it.
+
+The task functions mirror phoebus_gb300.fluid.FluidContext on host (numpy)
+Blocks, so a parity test runs the same sequence on both sides.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent.parent
+import sys  # noqa: E402
+
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+from phoebus_gb300 import abi  # noqa: E402  (struct layouts only)
+from phoebus_gb300.block import Block  # noqa: E402
+
+LIB = ROOT / "oracle" / "_build" / "libphx_oracle.so"
+SRC = ROOT / "oracle" / "phx_oracle.cpp"
+
+
+def build(force: bool = False) -> Path:
+    LIB.parent.mkdir(exist_ok=True)
+    hdr = ROOT / "include" / "phx_fluid.h"
+    if force or not LIB.exists() or LIB.stat().st_mtime < max(SRC.stat().st_mtime, hdr.stat().st_mtime):
+        subprocess.run(["g++", "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-o",
+                        str(LIB), str(SRC)], check=True)
+    return LIB
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(str(LIB))
+        P, B, R = C.POINTER(abi.Params), C.POINTER(abi.BlockS), abi.Range
+        L.orc_prim_to_con.argtypes = [P, B, R, R, R]
+        L.orc_prim_to_con.restype = None
+        L.orc_con_to_prim.argtypes = [P, B, R, R, R, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_con_to_prim.restype = C.c_longlong
+        L.orc_calculate_fluxes.argtypes = [P, B]
+        L.orc_calculate_fluxes.restype = None
+        L.orc_flux_ct.argtypes = [B]
+        L.orc_flux_ct.restype = None
+        L.orc_sources.argtypes = [P, B]
+        L.orc_sources.restype = None
+        L.orc_flux_divergence.argtypes = [P, B]
+        L.orc_flux_divergence.restype = None
+        L.orc_update.argtypes = [P, B, C.c_void_p, C.c_void_p, C.c_double, C.c_double]
+        L.orc_update.restype = None
+        L.orc_fill_ghosts_periodic.argtypes = [B, C.c_void_p, C.c_int]
+        L.orc_fill_ghosts_periodic.restype = None
+        L.orc_estimate_timestep.argtypes = [P, B, C.c_int]
+        L.orc_estimate_timestep.restype = C.c_double
+        L.orc_geometry_fill_fmks.argtypes = [C.POINTER(abi.Geometry), B]
+        L.orc_geometry_fill_fmks.restype = None
+        L.orc_fmks_point.argtypes = [C.POINTER(abi.Geometry), C.c_double, C.c_double, C.c_double, C.c_void_p]
+        L.orc_fmks_point.restype = None
+        _lib = L
+    return _lib
+
+
+def _r(r):
+    return abi.Range(int(r[0]), int(r[1]))
+
+
+def set_threads(n: int | None):
+    if n:
+        os.environ["OMP_NUM_THREADS"] = str(n)
+
+
+class Oracle:
+    """The reference tasks on host Blocks (numpy arrays)."""
+
+    def __init__(self):
+        self.L = lib()
+
+    def PrimitiveToConserved(self, p, b: Block, ib=None, jb=None, kb=None):
+        e = b.entire()
+        s = b.struct()
+        self.L.orc_prim_to_con(C.byref(p), C.byref(s), _r(ib or e[0]), _r(jb or e[1]), _r(kb or e[2]))
+
+    def ConservedToPrimitive(self, p, b: Block, ib=None, jb=None, kb=None, iters=None, guess=None):
+        """Returns the number of unbracketed zones.  iters: optional int32
+        array shaped like one field, receiving iteration counts."""
+        e = b.entire()
+        s = b.struct()
+        it = iters.ctypes.data if iters is not None else None
+        gs = guess.ctypes.data if guess is not None else None
+        ev = C.c_longlong()
+        n = self.L.orc_con_to_prim(C.byref(p), C.byref(s), _r(ib or e[0]), _r(jb or e[1]), _r(kb or e[2]), it, gs,
+                                   C.byref(ev))
+        self.last_evals = ev.value
+        return n
+
+    def CalculateFluxes(self, p, b: Block):
+        s = b.struct()
+        self.L.orc_calculate_fluxes(C.byref(p), C.byref(s))
+
+    def FluxCT(self, p, b: Block):
+        if not p.mhd or b.ndim == 1:
+            return
+        s = b.struct()
+        self.L.orc_flux_ct(C.byref(s))
+
+    def CalculateFluidSourceTerms(self, p, b: Block):
+        s = b.struct()
+        self.L.orc_sources(C.byref(p), C.byref(s))
+
+    def FluxDivergence(self, p, b: Block):
+        s = b.struct()
+        self.L.orc_flux_divergence(C.byref(p), C.byref(s))
+
+    def Update(self, p, b: Block, base, out, beta, dt):
+        s = b.struct()
+        self.L.orc_update(C.byref(p), C.byref(s), base.ctypes.data, out.ctypes.data, beta, dt)
+
+    def FillGhostsPeriodic(self, b: Block, field, nvar):
+        s = b.struct()
+        self.L.orc_fill_ghosts_periodic(C.byref(s), field.ctypes.data, nvar)
+
+    def EstimateTimestepBlock(self, p, b: Block, use_face_speeds: bool) -> float:
+        s = b.struct()
+        return self.L.orc_estimate_timestep(C.byref(p), C.byref(s), int(use_face_speeds))
+
+    def GeometryFillFMKS(self, b: Block):
+        g = b.geom.struct()
+        s = b.struct()
+        self.L.orc_geometry_fill_fmks(C.byref(g), C.byref(s))
+
+    def fmks_point(self, g, X1, X2, X3=0.0):
+        out = np.zeros(abi.GEOM_NLOC)
+        self.L.orc_fmks_point(C.byref(g), X1, X2, X3, out.ctypes.data)
+        return out
+
+    # ---- composite sequences (same order as the GPU host API)
+    def Initialize(self, p, b: Block):
+        self.PrimitiveToConserved(p, b)
+        self.FillGhostsPeriodic(b, b["cons"], abi.NCONS if p.mhd else 5)
+        return self.ConservedToPrimitive(p, b)
+
+    def Stage(self, p, b: Block, base, out, beta, dt):
+        """PhoebusDriver::RungeKuttaStage for one periodic block: sources,
+        fluxes, FluxCT, divergence + update, con2prim (entire), ghost
+        exchange, con2prim (entire).  b['cons'] is the stage input."""
+        self.CalculateFluidSourceTerms(p, b)
+        self.CalculateFluxes(p, b)
+        self.FluxCT(p, b)
+        self.FluxDivergence(p, b)
+        self.Update(p, b, base, out, beta, dt)
+        cons_in = b.arrays["cons"]
+        b.arrays["cons"] = out
+        unbr = self.ConservedToPrimitive(p, b)
+        self.FillGhostsPeriodic(b, out, abi.NCONS if p.mhd else 5)
+        unbr += self.ConservedToPrimitive(p, b)
+        b.arrays["cons"] = cons_in
+        return unbr
+
+    def rk2_step(self, p, b: Block, cons_stage, dt):
+        base = b.arrays["cons"]
+        self.Stage(p, b, base, cons_stage, 1.0, dt)
+        b.arrays["cons"] = cons_stage
+        self.Stage(p, b, base, base, 0.5, dt)
+        b.arrays["cons"] = base

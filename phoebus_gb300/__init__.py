@@ -1,0 +1,12 @@
+"""GB300-native (sm_103a) GRMHD fluid hot path of phoebus.
+
+Hand-written FP64 CUDA kernels behind the C ABI of include/phx_fluid.h:
+reconstruction (PLM, WENO5-Z, MP5) + LLF/HLL Riemann fluxes, the robust
+con2prim root find, geometric source terms and the RK stage glue, for
+Minkowski and FMKS (cached, axisymmetric) geometry.  `fluid` is the host API
+mirroring the reference task names; `states` makes seeded initial states.
+"""
+from . import abi  # noqa: F401
+from .block import Block, GeomTables  # noqa: F401
+
+__all__ = ["abi", "Block", "GeomTables"]

@@ -1,0 +1,185 @@
+"""ctypes mirror of include/phx_fluid.h and loader of the sm_103a libraries.
+
+The structures here are byte-for-byte the C structs of the header; the same
+definitions describe host arrays (numpy) and device arrays (torch CUDA
+tensors), since the ABI only sees pointers.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+LIBDIR = PKG / "_lib"
+
+# ---- constants (phx_fluid.h)
+PRHO, PVEL, PENG, PB, PPRS, PGM1, PTMP, PMU = 0, 1, 4, 5, 8, 9, 10, 11
+NPRIM, NRECON = 12, 10
+CRHO, CMOM, CENG, CB = 0, 1, 4, 5
+NCONS = 8
+RECON = {"constant": 0, "linear": 1, "weno5": 2, "weno5z": 2, "mp5": 3}
+RIEMANN = {"llf": 0, "hll": 1}
+GEOM_MINKOWSKI, GEOM_FMKS = 0, 1
+FLOOR = {"ConstantRhoSie": 0, "ExpX1RhoSie": 1, "ExpX1RhoU": 2, "X1RhoSie": 3, "RRhoSie": 4}
+G_ALPHA, G_BETA, G_GCOV, G_GAMCON, G_DETGAM, GEOM_NLOC = 0, 1, 4, 14, 20, 21
+GD_DALPHA, GD_DG, GEOM_NDER = 0, 3, 33
+C2P_HIST = 128
+MLP_IN, MLP_HID, MLP_OUT = 6, 64, 2
+MLP_NPARAM = MLP_IN * MLP_HID + MLP_HID + 2 * (MLP_HID * MLP_HID + MLP_HID) + MLP_HID * 2 + 2
+
+STATUS = {0: "ok", 1: "invalid argument", 2: "con2prim root not bracketed", 3: "NaN input",
+          4: "device wait timed out", 5: "CUDA error", 6: "no CUDA device", 7: "capacity", 8: "unsupported"}
+
+
+class Range(C.Structure):
+    _fields_ = [("s", C.c_int), ("e", C.c_int)]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("gm1", C.c_double), ("Cv", C.c_double), ("rho_min_eos", C.c_double), ("sie_min_eos", C.c_double),
+        ("c2p_tol", C.c_double), ("c2p_max_iter", C.c_int), ("c2p_floor_scale_fac", C.c_double),
+        ("c2p_fail_on_floors", C.c_int), ("c2p_fail_on_ceilings", C.c_int),
+        ("recon", C.c_int), ("riemann", C.c_int), ("cfl", C.c_double), ("mhd", C.c_int),
+        ("enable_floors", C.c_int), ("enable_ceilings", C.c_int), ("enable_mhd_floors", C.c_int),
+        ("enable_c2p_fixup", C.c_int), ("c2p_failure_strategy_floors", C.c_int), ("floor_type", C.c_int),
+        ("rho0_floor", C.c_double), ("sie0_floor", C.c_double), ("rho_exp_floor", C.c_double),
+        ("sie_exp_floor", C.c_double), ("gam0_ceiling", C.c_double), ("sie0_ceiling", C.c_double),
+        ("bsqorho0_ceiling", C.c_double), ("bsqou0_ceiling", C.c_double),
+    ]
+
+
+class Geometry(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int), ("a", C.c_double), ("hslope", C.c_double), ("poly_xt", C.c_double),
+        ("poly_alpha", C.c_double), ("x0", C.c_double), ("smooth", C.c_double), ("hexp_br", C.c_double),
+        ("hexp_nsq", C.c_double), ("hexp_csq", C.c_double), ("derefine_poles", C.c_int),
+        ("cent", C.c_void_p), ("face1", C.c_void_p), ("face2", C.c_void_p), ("deriv", C.c_void_p),
+    ]
+
+
+class BlockS(C.Structure):
+    _fields_ = [
+        ("nx1", C.c_int), ("nx2", C.c_int), ("nx3", C.c_int), ("ng", C.c_int), ("ndim", C.c_int),
+        ("var_stride", C.c_longlong),
+        ("x1min", C.c_double), ("x2min", C.c_double), ("x3min", C.c_double),
+        ("dx1", C.c_double), ("dx2", C.c_double), ("dx3", C.c_double),
+        ("prim", C.c_void_p), ("cons", C.c_void_p), ("flux", C.c_void_p), ("face_sig", C.c_void_p),
+        ("cell_sig", C.c_void_p), ("fail", C.c_void_p), ("src", C.c_void_p), ("emf", C.c_void_p),
+        ("dudt", C.c_void_p), ("geom", C.POINTER(Geometry)),
+    ]
+
+
+class C2PStats(C.Structure):
+    _fields_ = [("zones", C.c_ulonglong), ("iterations", C.c_ulonglong), ("residual_evals", C.c_ulonglong),
+                ("failures", C.c_ulonglong), ("unbracketed", C.c_ulonglong),
+                ("learned_accepted", C.c_ulonglong), ("hist", C.c_ulonglong * C2P_HIST)]
+
+
+class PhxError(RuntimeError):
+    """Raised when an entry point returns a non-OK phx_status."""
+
+    def __init__(self, status: int, detail: str):
+        super().__init__(f"phx status {status} ({STATUS.get(status, '?')}): {detail}")
+        self.status = status
+
+
+_LIBS: dict[str, C.CDLL] = {}
+
+_P = C.c_void_p
+_SIGS = {
+    "phx_ctx_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
+    "phx_ctx_destroy": (C.c_int, [_P]),
+    "phx_ctx_check": (C.c_int, [_P]),
+    "phx_ctx_c2p_stats": (C.c_int, [_P, C.POINTER(C2PStats), C.c_int]),
+    "phx_status_string": (C.c_char_p, [C.c_int]),
+    "phx_last_error": (C.c_char_p, []),
+    "phx_abi_version": (C.c_int, []),
+    "phx_build_exact": (C.c_int, []),
+    "phx_params_default": (None, [C.POINTER(Params)]),
+    "phx_geometry_default": (None, [C.POINTER(Geometry), C.c_int]),
+    "phx_prim_to_con": (C.c_int, [_P, C.POINTER(Params), C.POINTER(BlockS), Range, Range, Range, _P]),
+    "phx_con_to_prim": (C.c_int, [_P, C.POINTER(Params), C.POINTER(BlockS), Range, Range, Range, _P]),
+    "phx_con_to_prim_learned": (C.c_int, [_P, C.POINTER(Params), C.POINTER(BlockS), Range, Range, Range, _P]),
+    "phx_calculate_fluxes": (C.c_int, [_P, C.POINTER(Params), C.POINTER(BlockS), _P]),
+    "phx_flux_ct": (C.c_int, [_P, C.POINTER(Params), C.POINTER(BlockS), _P]),
+    "phx_calculate_fluid_source_terms": (C.c_int, [_P, C.POINTER(Params), C.POINTER(BlockS), C.c_int, _P]),
+    "phx_update_stage": (C.c_int, [_P, C.POINTER(BlockS), _P, _P, C.c_double, C.c_double, _P]),
+    "phx_fill_ghosts_periodic": (C.c_int, [_P, C.POINTER(BlockS), _P, C.c_int, _P]),
+    "phx_estimate_timestep": (C.c_int, [_P, C.POINTER(Params), C.POINTER(BlockS), C.c_int, _P, _P]),
+    "phx_c2p_fixup": (C.c_int, [_P, C.POINTER(Params), C.POINTER(BlockS), _P]),
+    "phx_apply_floors": (C.c_int, [_P, C.POINTER(Params), C.POINTER(BlockS), Range, Range, Range, _P]),
+    "phx_geometry_fill_fmks": (C.c_int, [_P, C.POINTER(Geometry), C.POINTER(BlockS), _P]),
+    "phx_stage": (C.c_int, [_P, C.POINTER(Params), C.POINTER(BlockS), _P, _P, C.c_double, C.c_double,
+                            C.c_int, _P]),
+    "phx_stage_batched": (C.c_int, [_P, C.POINTER(Params), C.POINTER(BlockS), C.c_int, _P, _P, C.c_double,
+                                    C.c_double, C.c_int, _P]),
+    "phx_mlp_set_weights": (C.c_int, [_P, C.POINTER(C.c_float)]),
+    "phx_mlp_get_weights": (C.c_int, [_P, C.POINTER(C.c_float)]),
+    "phx_probe_fp64_peak": (C.c_int, [_P, C.POINTER(C.c_double)]),
+}
+
+
+def exported_symbols() -> list[str]:
+    """Every entry point include/phx_fluid.h declares (kept in sync by a test)."""
+    return sorted(_SIGS)
+
+
+def lib_path(exact: bool = False) -> Path:
+    return LIBDIR / ("libphx_fluid_exact.so" if exact else "libphx_fluid.so")
+
+
+def load(exact: bool = False) -> C.CDLL:
+    """Load the CUDA library.  Fails loudly if it was not built: there is no
+    CPU fallback for the hot path."""
+    key = "exact" if exact else "fast"
+    if key in _LIBS:
+        return _LIBS[key]
+    path = lib_path(exact)
+    if not path.exists():
+        raise RuntimeError(f"{path} is missing: run `python -c 'import __graft_entry__ as g; g.build()'` "
+                           "(the fluid hot path has no CPU fallback)")
+    lib = C.CDLL(str(path))
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIBS[key] = lib
+    return lib
+
+
+def check(lib: C.CDLL, status: int) -> None:
+    if status != 0:
+        raise PhxError(status, lib.phx_last_error().decode())
+
+
+def default_params(lib: C.CDLL | None = None, **over) -> Params:
+    p = Params()
+    # same defaults as phx_params_default (fluid.cpp:53-136, fixup.cpp:48-280)
+    p.gm1, p.Cv = 4.0 / 3.0 - 1.0, 1.0
+    p.c2p_tol, p.c2p_max_iter, p.c2p_floor_scale_fac = 1.0e-8, 20, 1.0
+    p.recon, p.riemann, p.cfl, p.mhd = RECON["linear"], RIEMANN["hll"], 0.8, 1
+    p.floor_type, p.rho_exp_floor, p.sie_exp_floor = 0, -2.0, -1.0
+    p.gam0_ceiling, p.sie0_ceiling, p.bsqorho0_ceiling, p.bsqou0_ceiling = 1000.0, 100.0, 50.0, 2500.0
+    for k, v in over.items():
+        if k == "recon" and isinstance(v, str):
+            v = RECON[v]
+        if k == "riemann" and isinstance(v, str):
+            v = RIEMANN[v]
+        if k == "floor_type" and isinstance(v, str):
+            v = FLOOR[v]
+        if k == "Gamma":
+            k, v = "gm1", v - 1.0
+        setattr(p, k, v)
+    return p
+
+
+def default_geometry(kind: int, **over) -> Geometry:
+    g = Geometry()
+    g.kind = kind
+    g.a, g.hslope, g.poly_xt, g.poly_alpha, g.x0, g.smooth = 0.0, 0.3, 0.82, 14.0, 0.0, 0.5
+    g.hexp_br, g.hexp_nsq, g.hexp_csq, g.derefine_poles = 1.0e30, 4.0, 4.0, 1
+    for k, v in over.items():
+        setattr(g, k, v)
+    return g

@@ -1,0 +1,530 @@
+// phx_api.cu -- the extern "C" entry points of phx_fluid.h.
+//
+// Host-side validation, parameter resolution (the fixup package defaults of
+// fixup.cpp:120-180), and dispatch to the kernels.  All calls are
+// asynchronous on the caller's stream; nothing is allocated per call.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "phx_kernels.cuh"
+
+struct phx_ctx {
+  int device;
+  phx::DevStats *stats;        // device
+  unsigned int *err;           // device sticky error word
+  unsigned long long *dt_scr;  // device scratch for the dt reduction
+  float *mlp_w;                // device FP32 parameters of the learned guess (or null)
+  int mlp_loaded;
+};
+
+namespace {
+thread_local std::string g_last_error;
+
+phx_status fail(phx_status s, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return s;
+}
+
+phx_status cuda_status(const char *where) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(PHX_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
+  return PHX_OK;
+}
+
+phx::Par make_par(const phx_params &p) {
+  phx::Par d{};
+  d.gm1 = p.gm1;
+  d.Cv = p.Cv;
+  d.rho_min_eos = p.rho_min_eos;
+  d.sie_min_eos = p.sie_min_eos;
+  d.c2p_tol = p.c2p_tol;
+  d.c2p_max_iter = p.c2p_max_iter;
+  d.fsf = p.c2p_floor_scale_fac;
+  d.fail_on_floors = p.c2p_fail_on_floors;
+  d.fail_on_ceilings = p.c2p_fail_on_ceilings;
+  d.mhd = p.mhd;
+  if (p.enable_floors || p.enable_c2p_fixup || (p.enable_mhd_floors && p.mhd)) {
+    d.floor_type = p.floor_type;
+    d.r0 = p.rho0_floor;
+    d.s0 = p.sie0_floor;
+    d.ralpha = p.rho_exp_floor;
+    d.salpha = p.sie_exp_floor;
+    d.enable_floors = 1;
+  } else {  // Floors(): ConstantRhoSie with -max (fixup.hpp:75-78)
+    d.floor_type = PHX_FLOOR_CONSTANT_RHO_SIE;
+    d.r0 = -phx::kDBLMAX;
+    d.s0 = -phx::kDBLMAX;
+    d.ralpha = d.salpha = 0.0;
+    d.enable_floors = 0;
+  }
+  if (p.enable_ceilings) {
+    d.g0 = p.gam0_ceiling;
+    d.smax0 = p.sie0_ceiling;
+  } else {
+    d.g0 = phx::kDBLMAX;
+    d.smax0 = phx::kDBLMAX;
+  }
+  d.enable_mhd_floors = (p.enable_mhd_floors && p.mhd) ? 1 : 0;
+  if (d.enable_mhd_floors) {
+    d.bsqorho0 = p.bsqorho0_ceiling;
+    d.bsqou0 = p.bsqou0_ceiling;
+  } else {
+    d.bsqorho0 = phx::kDBLMAX;
+    d.bsqou0 = phx::kDBLMAX;
+  }
+  d.recon = p.recon;
+  d.riemann = p.riemann;
+  d.cfl = p.cfl;
+  d.c2p_fixup = p.enable_c2p_fixup;
+  d.strategy_floors = p.c2p_failure_strategy_floors;
+  return d;
+}
+
+phx_status check_params(const phx_params *p) {
+  if (!p) return fail(PHX_ERR_INVALID_ARG, "params is NULL");
+  if (p->recon < PHX_RECON_CONSTANT || p->recon > PHX_RECON_MP5)
+    return fail(PHX_ERR_INVALID_ARG, "invalid recon %d", p->recon);
+  if (p->riemann != PHX_RIEMANN_LLF && p->riemann != PHX_RIEMANN_HLL)
+    return fail(PHX_ERR_INVALID_ARG, "invalid riemann solver %d (choose llf or hll)", p->riemann);
+  if (!(p->c2p_floor_scale_fac <= 1. && p->c2p_floor_scale_fac > 0.))
+    return fail(PHX_ERR_INVALID_ARG, "fluid/c2p_floor_scale_fac must be between 0 and 1!");
+  if (p->c2p_max_iter < 0) return fail(PHX_ERR_INVALID_ARG, "c2p_max_iter < 0");
+  return PHX_OK;
+}
+
+phx_status make_view(const phx_block *b, phx::BView &v) {
+  if (!b) return fail(PHX_ERR_INVALID_ARG, "block is NULL");
+  if (b->ndim < 1 || b->ndim > 3) return fail(PHX_ERR_INVALID_ARG, "ndim must be 1..3");
+  if (b->ng < 3) return fail(PHX_ERR_INVALID_ARG, "ng must be >= 3 (got %d)", b->ng);
+  if (b->nx1 < 1 || b->nx2 < 1 || b->nx3 < 1) return fail(PHX_ERR_INVALID_ARG, "nx must be >= 1");
+  if ((b->ndim < 2 && b->nx2 != 1) || (b->ndim < 3 && b->nx3 != 1))
+    return fail(PHX_ERR_INVALID_ARG, "inactive dimensions must have nx = 1");
+  if (!b->prim || !b->cons) return fail(PHX_ERR_INVALID_ARG, "prim/cons pointers are NULL");
+  v.ndim = b->ndim;
+  v.ng = b->ng;
+  v.nx1 = b->nx1;
+  v.nx2 = b->nx2;
+  v.nx3 = b->nx3;
+  v.n1t = b->nx1 + 2 * b->ng;
+  v.n2t = b->ndim >= 2 ? b->nx2 + 2 * b->ng : 1;
+  v.n3t = b->ndim >= 3 ? b->nx3 + 2 * b->ng : 1;
+  const long long N = (long long)v.n1t * v.n2t * v.n3t;
+  v.vs = b->var_stride ? b->var_stride : N;
+  if (v.vs < N) return fail(PHX_ERR_INVALID_ARG, "var_stride smaller than the block");
+  const double xmin[3] = {b->x1min, b->x2min, b->x3min};
+  const double dx[3] = {b->dx1, b->dx2, b->dx3};
+  for (int d = 0; d < 3; d++) {
+    v.dx[d] = dx[d];
+    v.x0[d] = d < b->ndim ? xmin[d] - b->ng * dx[d] : xmin[d];
+  }
+  v.prim = b->prim;
+  v.cons = b->cons;
+  v.flux = b->flux;
+  v.face_sig = b->face_sig;
+  v.cell_sig = b->cell_sig;
+  v.fail = b->fail;
+  v.src = b->src;
+  v.emf = b->emf;
+  v.dudt = b->dudt;
+  v.fmks = 0;
+  v.gcent = v.gface1 = v.gface2 = v.gderiv = nullptr;
+  if (b->geom && b->geom->kind == PHX_GEOM_FMKS) {
+    if (!b->geom->cent || !b->geom->face1 || !b->geom->face2 || !b->geom->deriv)
+      return fail(PHX_ERR_INVALID_ARG, "FMKS geometry tables are NULL");
+    v.fmks = 1;
+    v.gcent = b->geom->cent;
+    v.gface1 = b->geom->face1;
+    v.gface2 = b->geom->face2;
+    v.gderiv = b->geom->deriv;
+  }
+  return PHX_OK;
+}
+
+phx_status check_range(const phx::BView &v, phx_range ib, phx_range jb, phx_range kb, phx::Range3 &r) {
+  if (ib.s < 0 || ib.e >= v.n1t || jb.s < 0 || jb.e >= v.n2t || kb.s < 0 || kb.e >= v.n3t)
+    return fail(PHX_ERR_INVALID_ARG, "index range outside the block");
+  r = {ib.s, ib.e, jb.s, jb.e, kb.s, kb.e};
+  return PHX_OK;
+}
+
+phx::Range3 entire(const phx::BView &v) { return {0, v.n1t - 1, 0, v.n2t - 1, 0, v.n3t - 1}; }
+phx::Range3 interior(const phx::BView &v) {
+  return {v.ng, v.ng + v.nx1 - 1, v.ndim >= 2 ? v.ng : 0, v.ndim >= 2 ? v.ng + v.nx2 - 1 : 0,
+          v.ndim >= 3 ? v.ng : 0, v.ndim >= 3 ? v.ng + v.nx3 - 1 : 0};
+}
+
+inline cudaStream_t S(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+phx_status ctx_device(phx_ctx *ctx) {
+  if (!ctx) return fail(PHX_ERR_INVALID_ARG, "ctx is NULL");
+  int cur = -1;
+  cudaGetDevice(&cur);
+  if (cur != ctx->device) {
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return fail(PHX_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
+  }
+  return PHX_OK;
+}
+}  // namespace
+
+namespace phx {
+void launch_fluxes_err(const Par &p, const BView &b, unsigned int *err, cudaStream_t s);
+}
+
+extern "C" {
+
+int phx_abi_version(void) { return PHX_ABI_VERSION; }
+
+int phx_build_exact(void) {
+#ifdef PHX_EXACT
+  return 1;
+#else
+  return 0;
+#endif
+}
+
+const char *phx_status_string(phx_status s) {
+  switch (s) {
+  case PHX_OK: return "ok";
+  case PHX_ERR_INVALID_ARG: return "invalid argument";
+  case PHX_ERR_UNBRACKETED: return "con2prim root not bracketed";
+  case PHX_ERR_NAN_INPUT: return "NaN input";
+  case PHX_ERR_TIMEOUT: return "device wait timed out";
+  case PHX_ERR_CUDA: return "CUDA error";
+  case PHX_ERR_NO_DEVICE: return "no CUDA device";
+  case PHX_ERR_CAPACITY: return "request exceeds a fixed capacity";
+  case PHX_ERR_UNSUPPORTED: return "unsupported";
+  }
+  return "unknown status";
+}
+
+const char *phx_last_error(void) { return g_last_error.c_str(); }
+
+void phx_params_default(phx_params *p) {
+  std::memset(p, 0, sizeof(*p));
+  p->gm1 = 4.0 / 3.0 - 1.0;
+  p->Cv = 1.0;
+  p->rho_min_eos = 0.0;
+  p->sie_min_eos = 0.0;
+  p->c2p_tol = 1.e-8;       // fluid.cpp:76
+  p->c2p_max_iter = 20;     // fluid.cpp:79
+  p->c2p_floor_scale_fac = 1.0;
+  p->recon = PHX_RECON_LINEAR;  // fluid.cpp:96
+  p->riemann = PHX_RIEMANN_HLL; // fluid.cpp:119
+  p->cfl = 0.8;                 // fluid.cpp:63
+  p->mhd = 1;
+  p->floor_type = PHX_FLOOR_CONSTANT_RHO_SIE;
+  p->rho_exp_floor = -2.0;
+  p->sie_exp_floor = -1.0;
+  p->gam0_ceiling = 1000.0;
+  p->sie0_ceiling = 100.0;
+  p->bsqorho0_ceiling = 50.0;
+  p->bsqou0_ceiling = 2500.0;
+}
+
+void phx_geometry_default(phx_geometry *g, int kind) {
+  std::memset(g, 0, sizeof(*g));
+  g->kind = kind;
+  g->a = 0.0;
+  g->hslope = 0.3;       // fmks.cpp:41-47
+  g->poly_xt = 0.82;
+  g->poly_alpha = 14.0;
+  g->x0 = 0.0;
+  g->smooth = 0.5;
+  g->hexp_br = 1.e30;
+  g->hexp_nsq = 4.0;
+  g->hexp_csq = 4.0;
+  g->derefine_poles = 1;
+}
+
+phx_status phx_ctx_create(int device, phx_ctx **out) {
+  if (!out) return fail(PHX_ERR_INVALID_ARG, "out is NULL");
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return fail(PHX_ERR_NO_DEVICE, "no CUDA device available");
+  }
+  if (device < 0 || device >= n) return fail(PHX_ERR_INVALID_ARG, "device %d out of range", device);
+  if (cudaSetDevice(device) != cudaSuccess) return cuda_status("cudaSetDevice");
+  phx_ctx *c = new phx_ctx{};
+  c->device = device;
+  if (cudaMalloc(&c->stats, sizeof(phx::DevStats)) != cudaSuccess ||
+      cudaMalloc(&c->err, sizeof(unsigned int)) != cudaSuccess ||
+      cudaMalloc(&c->dt_scr, sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMalloc(&c->mlp_w, sizeof(float) * PHX_MLP_NPARAM) != cudaSuccess) {
+    phx_status s = cuda_status("cudaMalloc");
+    phx_ctx_destroy(c);
+    return s;
+  }
+  cudaMemset(c->stats, 0, sizeof(phx::DevStats));
+  cudaMemset(c->err, 0, sizeof(unsigned int));
+  cudaMemset(c->mlp_w, 0, sizeof(float) * PHX_MLP_NPARAM);
+  phx_status s = cuda_status("ctx init");
+  if (s != PHX_OK) {
+    phx_ctx_destroy(c);
+    return s;
+  }
+  *out = c;
+  return PHX_OK;
+}
+
+phx_status phx_ctx_destroy(phx_ctx *ctx) {
+  if (!ctx) return PHX_OK;
+  cudaSetDevice(ctx->device);
+  cudaFree(ctx->stats);
+  cudaFree(ctx->err);
+  cudaFree(ctx->dt_scr);
+  cudaFree(ctx->mlp_w);
+  delete ctx;
+  return PHX_OK;
+}
+
+phx_status phx_ctx_check(phx_ctx *ctx) {
+  phx_status s = ctx_device(ctx);
+  if (s != PHX_OK) return s;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return fail(PHX_ERR_CUDA, "device error: %s", cudaGetErrorString(e));
+  unsigned int w = 0;
+  cudaMemcpy(&w, ctx->err, sizeof(w), cudaMemcpyDeviceToHost);
+  cudaMemset(ctx->err, 0, sizeof(unsigned int));
+  if (w & phx::ERR_TIMEOUT) return fail(PHX_ERR_TIMEOUT, "a bounded device wait gave up");
+  if (w & phx::ERR_UNBRACKETED) return fail(PHX_ERR_UNBRACKETED, "Aborting with unbracketed root.");
+  if (w & phx::ERR_BOUNDS) return fail(PHX_ERR_INVALID_ARG, "device index check failed");
+  return cuda_status("phx_ctx_check");
+}
+
+phx_status phx_ctx_c2p_stats(phx_ctx *ctx, phx_c2p_stats *out, int reset) {
+  phx_status s = ctx_device(ctx);
+  if (s != PHX_OK) return s;
+  if (!out) return fail(PHX_ERR_INVALID_ARG, "out is NULL");
+  static_assert(sizeof(phx::DevStats) == sizeof(phx_c2p_stats), "stats layout");
+  if (cudaMemcpy(out, ctx->stats, sizeof(*out), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return cuda_status("stats copy");
+  if (reset) cudaMemset(ctx->stats, 0, sizeof(phx::DevStats));
+  return cuda_status("stats");
+}
+
+phx_status phx_prim_to_con(phx_ctx *ctx, const phx_params *p, const phx_block *b, phx_range ib,
+                           phx_range jb, phx_range kb, void *stream) {
+  phx_status s;
+  if ((s = ctx_device(ctx)) || (s = check_params(p))) return s;
+  phx::BView v;
+  if ((s = make_view(b, v))) return s;
+  if (!b->cell_sig) return fail(PHX_ERR_INVALID_ARG, "cell_sig is NULL");
+  phx::Range3 r;
+  if ((s = check_range(v, ib, jb, kb, r))) return s;
+  phx::launch_p2c(make_par(*p), v, r, S(stream));
+  return cuda_status("phx_prim_to_con");
+}
+
+static phx_status c2p_common(phx_ctx *ctx, const phx_params *p, const phx_block *b, phx_range ib,
+                             phx_range jb, phx_range kb, void *stream, bool learned) {
+  phx_status s;
+  if ((s = ctx_device(ctx)) || (s = check_params(p))) return s;
+  phx::BView v;
+  if ((s = make_view(b, v))) return s;
+  if (!b->fail || !b->cell_sig) return fail(PHX_ERR_INVALID_ARG, "fail/cell_sig is NULL");
+  phx::Range3 r;
+  if ((s = check_range(v, ib, jb, kb, r))) return s;
+  if (learned && !ctx->mlp_loaded) return fail(PHX_ERR_INVALID_ARG, "no learned-guess weights loaded");
+  phx::launch_c2p(make_par(*p), v, r, ctx->stats, ctx->err, learned ? ctx->mlp_w : nullptr, S(stream));
+  return cuda_status("phx_con_to_prim");
+}
+
+phx_status phx_con_to_prim(phx_ctx *ctx, const phx_params *p, const phx_block *b, phx_range ib,
+                           phx_range jb, phx_range kb, void *stream) {
+  return c2p_common(ctx, p, b, ib, jb, kb, stream, false);
+}
+
+phx_status phx_con_to_prim_learned(phx_ctx *ctx, const phx_params *p, const phx_block *b,
+                                   phx_range ib, phx_range jb, phx_range kb, void *stream) {
+  return c2p_common(ctx, p, b, ib, jb, kb, stream, true);
+}
+
+phx_status phx_calculate_fluxes(phx_ctx *ctx, const phx_params *p, const phx_block *b, void *stream) {
+  phx_status s;
+  if ((s = ctx_device(ctx)) || (s = check_params(p))) return s;
+  phx::BView v;
+  if ((s = make_view(b, v))) return s;
+  if (!b->flux || !b->face_sig) return fail(PHX_ERR_INVALID_ARG, "flux/face_sig is NULL");
+  phx::launch_fluxes_err(make_par(*p), v, ctx->err, S(stream));
+  return cuda_status("phx_calculate_fluxes");
+}
+
+phx_status phx_flux_ct(phx_ctx *ctx, const phx_params *p, const phx_block *b, void *stream) {
+  phx_status s;
+  if ((s = ctx_device(ctx)) || (s = check_params(p))) return s;
+  phx::BView v;
+  if ((s = make_view(b, v))) return s;
+  if (!p->mhd || b->ndim == 1) return PHX_OK;  // fluid.cpp:779-784
+  if (!b->flux || !b->emf) return fail(PHX_ERR_INVALID_ARG, "flux/emf is NULL");
+  phx::launch_fluxct(v, S(stream));
+  return cuda_status("phx_flux_ct");
+}
+
+phx_status phx_calculate_fluid_source_terms(phx_ctx *ctx, const phx_params *p, const phx_block *blocks,
+                                            int nblocks, void *stream) {
+  phx_status s;
+  if ((s = ctx_device(ctx)) || (s = check_params(p))) return s;
+  if (nblocks < 0 || (nblocks > 0 && !blocks)) return fail(PHX_ERR_INVALID_ARG, "bad block list");
+  const phx::Par par = make_par(*p);
+  for (int n = 0; n < nblocks; n++) {
+    phx::BView v;
+    if ((s = make_view(&blocks[n], v))) return s;
+    if (!blocks[n].src) return fail(PHX_ERR_INVALID_ARG, "src is NULL");
+    phx::launch_sources(par, v, S(stream));
+  }
+  return cuda_status("phx_calculate_fluid_source_terms");
+}
+
+phx_status phx_update_stage(phx_ctx *ctx, const phx_block *b, const double *cons_base, double *cons_out,
+                            double beta, double dt, void *stream) {
+  phx_status s;
+  if ((s = ctx_device(ctx))) return s;
+  phx::BView v;
+  if ((s = make_view(b, v))) return s;
+  if (!b->flux) return fail(PHX_ERR_INVALID_ARG, "flux is NULL");
+  if (cons_out && !cons_base) return fail(PHX_ERR_INVALID_ARG, "cons_base is NULL");
+  phx::Par par{};
+  par.mhd = 1;
+  phx::launch_update(par, v, cons_base, cons_out, beta, dt, S(stream));
+  return cuda_status("phx_update_stage");
+}
+
+phx_status phx_fill_ghosts_periodic(phx_ctx *ctx, const phx_block *b, double *field, int nvar, void *stream) {
+  phx_status s;
+  if ((s = ctx_device(ctx))) return s;
+  phx::BView v;
+  if ((s = make_view(b, v))) return s;
+  if (!field || nvar < 0) return fail(PHX_ERR_INVALID_ARG, "bad field");
+  if (b->nx1 < b->ng || (b->ndim >= 2 && b->nx2 < b->ng) || (b->ndim >= 3 && b->nx3 < b->ng))
+    return fail(PHX_ERR_INVALID_ARG, "periodic exchange needs nx >= ng");
+  phx::launch_ghost_periodic(v, field, nvar, S(stream));
+  return cuda_status("phx_fill_ghosts_periodic");
+}
+
+phx_status phx_estimate_timestep(phx_ctx *ctx, const phx_params *p, const phx_block *b, int use_face_speeds,
+                                 double *dt_out_device, void *stream) {
+  phx_status s;
+  if ((s = ctx_device(ctx)) || (s = check_params(p))) return s;
+  phx::BView v;
+  if ((s = make_view(b, v))) return s;
+  if (!dt_out_device || !b->cell_sig || (use_face_speeds && !b->face_sig))
+    return fail(PHX_ERR_INVALID_ARG, "dt_out/cell_sig/face_sig is NULL");
+  phx::launch_dt(make_par(*p), v, use_face_speeds, ctx->dt_scr, dt_out_device, S(stream));
+  return cuda_status("phx_estimate_timestep");
+}
+
+phx_status phx_c2p_fixup(phx_ctx *ctx, const phx_params *p, const phx_block *b, void *stream) {
+  (void)ctx; (void)p; (void)b; (void)stream;
+  return fail(PHX_ERR_UNSUPPORTED, "phx_c2p_fixup: not built yet");
+}
+
+phx_status phx_apply_floors(phx_ctx *ctx, const phx_params *p, const phx_block *b, phx_range ib, phx_range jb,
+                            phx_range kb, void *stream) {
+  (void)ctx; (void)p; (void)b; (void)ib; (void)jb; (void)kb; (void)stream;
+  return fail(PHX_ERR_UNSUPPORTED, "phx_apply_floors: not built yet");
+}
+
+phx_status phx_geometry_fill_fmks(phx_ctx *ctx, const phx_geometry *g, const phx_block *b, void *stream) {
+  phx_status s;
+  if ((s = ctx_device(ctx))) return s;
+  if (!g || g->kind != PHX_GEOM_FMKS) return fail(PHX_ERR_INVALID_ARG, "geometry must be FMKS");
+  if (!g->cent || !g->face1 || !g->face2 || !g->deriv) return fail(PHX_ERR_INVALID_ARG, "tables are NULL");
+  phx::BView v;
+  phx_block bb = *b;
+  bb.geom = nullptr;
+  if ((s = make_view(&bb, v))) return s;
+  phx::launch_geom_fmks(*g, v, S(stream));
+  return cuda_status("phx_geometry_fill_fmks");
+}
+
+phx_status phx_stage(phx_ctx *ctx, const phx_params *p, const phx_block *b, const double *cons_base,
+                     double *cons_out, double beta, double dt, int use_learned_guess, void *stream) {
+  phx_status s;
+  if ((s = ctx_device(ctx)) || (s = check_params(p))) return s;
+  phx::BView v;
+  if ((s = make_view(b, v))) return s;
+  if (!b->flux || !b->face_sig || !b->cell_sig || !b->fail || !b->src || !cons_base || !cons_out)
+    return fail(PHX_ERR_INVALID_ARG, "stage needs flux, face_sig, cell_sig, fail, src, cons_base, cons_out");
+  if (p->mhd && b->ndim > 1 && !b->emf) return fail(PHX_ERR_INVALID_ARG, "emf is NULL");
+  if (b->nx1 < b->ng || (b->ndim >= 2 && b->nx2 < b->ng) || (b->ndim >= 3 && b->nx3 < b->ng))
+    return fail(PHX_ERR_INVALID_ARG, "periodic exchange needs nx >= ng");
+  if (use_learned_guess && !ctx->mlp_loaded) return fail(PHX_ERR_INVALID_ARG, "no learned-guess weights loaded");
+  const phx::Par par = make_par(*p);
+  cudaStream_t st = S(stream);
+  phx::launch_sources(par, v, st);                      // CalculateFluidSourceTerms
+  phx::launch_fluxes_err(par, v, ctx->err, st);         // CalculateFluxes
+  if (p->mhd && b->ndim > 1) phx::launch_fluxct(v, st);  // FluxCT
+  phx::launch_update(par, v, cons_base, cons_out, beta, dt, st);
+  phx::BView vo = v;  // the stage result: con2prim reads cons_out
+  vo.cons = cons_out;
+  const float *w = use_learned_guess ? ctx->mlp_w : nullptr;
+  phx::launch_c2p(par, vo, entire(vo), ctx->stats, ctx->err, w, st);  // FillDerived (MeshData)
+  phx::launch_ghost_periodic(vo, cons_out, p->mhd ? PHX_NCONS : 5, st);  // boundary exchange
+  phx::launch_c2p(par, vo, entire(vo), ctx->stats, ctx->err, w, st);  // FillDerived (block)
+  return cuda_status("phx_stage");
+}
+
+phx_status phx_stage_batched(phx_ctx *ctx, const phx_params *p, const phx_block *blocks, int nblocks,
+                             const double *const *cons_base, double *const *cons_out, double beta, double dt,
+                             int use_learned_guess, void *stream) {
+  (void)ctx; (void)p; (void)blocks; (void)nblocks; (void)cons_base; (void)cons_out; (void)beta; (void)dt;
+  (void)use_learned_guess; (void)stream;
+  return fail(PHX_ERR_UNSUPPORTED, "phx_stage_batched: not built yet");
+}
+
+phx_status phx_mlp_set_weights(phx_ctx *ctx, const float *params_host) {
+  phx_status s;
+  if ((s = ctx_device(ctx))) return s;
+  if (!params_host) return fail(PHX_ERR_INVALID_ARG, "params is NULL");
+  if (cudaMemcpy(ctx->mlp_w, params_host, sizeof(float) * PHX_MLP_NPARAM, cudaMemcpyHostToDevice) != cudaSuccess)
+    return cuda_status("mlp weights");
+  ctx->mlp_loaded = 1;
+  return PHX_OK;
+}
+
+phx_status phx_mlp_get_weights(phx_ctx *ctx, float *params_host) {
+  phx_status s;
+  if ((s = ctx_device(ctx))) return s;
+  if (!params_host) return fail(PHX_ERR_INVALID_ARG, "params is NULL");
+  if (cudaMemcpy(params_host, ctx->mlp_w, sizeof(float) * PHX_MLP_NPARAM, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return cuda_status("mlp weights");
+  return PHX_OK;
+}
+
+phx_status phx_probe_fp64_peak(phx_ctx *ctx, double *flops_out) {
+  phx_status s;
+  if ((s = ctx_device(ctx))) return s;
+  if (!flops_out) return fail(PHX_ERR_INVALID_ARG, "flops_out is NULL");
+  double *d = nullptr;
+  // the probe's output word lives in the dt scratch (never read back)
+  d = reinterpret_cast<double *>(ctx->dt_scr);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int nthreads = 0;
+  const int iters = 4096;
+  phx::launch_fp64_probe(d, 64, 0, &nthreads);  // warm-up
+  cudaEventRecord(e0, 0);
+  phx::launch_fp64_probe(d, iters, 0, &nthreads);
+  cudaEventRecord(e1, 0);
+  cudaEventSynchronize(e1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *flops_out = 2.0 * 8.0 * (double)iters * nthreads / (ms * 1e-3);
+  return cuda_status("phx_probe_fp64_peak");
+}
+
+}  // extern "C"

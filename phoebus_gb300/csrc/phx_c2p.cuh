@@ -1,0 +1,320 @@
+// phx_c2p.cuh -- robust con2prim for one zone on the device
+// (con2prim_robust.hpp:46-453, root_find.hpp:27-167).
+//
+// The regula-falsi loop is warp-synchronous: every lane stays in the loop
+// until the warp's vote (__any_sync) says no lane is still iterating, so all
+// 32 lanes re-enter each iteration together and reconverge after it.
+#pragma once
+#include "phx_device.cuh"
+
+namespace phx {
+
+struct Residual {
+  double D, q, bsq, bsq_rpsq, rsq, rbsq, v0sq;
+  double x1, x2, x3;
+  double rho_floor, gam_max, e_max;
+  bool used_density_floor, used_energy_floor, used_energy_max, used_gamma_max;
+
+  __device__ __forceinline__ void init(const Par &p) {
+    double garbage = 0.0;
+    rho_floor = 0.0;
+    get_floors(p, x1, x2, x3, rho_floor, garbage);
+    gam_max = p.g0;
+    e_max = p.smax0;
+    rho_floor *= p.fsf;
+    used_density_floor = used_energy_floor = used_energy_max = used_gamma_max = false;
+  }
+  __device__ __forceinline__ double x_mu(double mu) const { return ratio(1.0, 1.0 + mu * bsq); }
+  __device__ __forceinline__ double rbarsq_mu(double mu, double x) const {
+    return x * (x * rsq + mu * (1.0 + x) * rbsq);
+  }
+  __device__ __forceinline__ double qbar_mu(double mu, double x) const {
+    const double mux = mu * x;
+    return q - 0.5 * (bsq + mux * mux * bsq_rpsq);
+  }
+  __device__ __forceinline__ double vhatsq_mu(double mu, double rbarsq) {
+    const double vsq_trial = mu * mu * rbarsq;
+    if (vsq_trial > v0sq) {
+      used_gamma_max = true;
+      return v0sq;
+    }
+    used_gamma_max = false;
+    return vsq_trial;
+  }
+  __device__ __forceinline__ double iWhat_mu(double vhatsq) const { return sqrt(1.0 - vhatsq); }
+  __device__ __forceinline__ double rhohat_mu(double iWhat) {
+    const double rho_trial = D * iWhat;
+    if (rho_trial <= rho_floor) {
+      used_density_floor = true;
+      return rho_floor;
+    }
+    used_density_floor = false;
+    return rho_trial;
+  }
+  __device__ __forceinline__ double ehat_mu(const Par &p, double mu, double qbar, double rbarsq,
+                                            double vhatsq, double What) {
+    double rho = rhohat_mu(ratio(1.0, What));
+    double e_floor;
+    get_floors(p, x1, x2, x3, rho, e_floor);
+    e_floor *= p.fsf;
+    const double ehat_trial = What * (qbar - mu * rbarsq) + vhatsq * What * ratio(What, 1.0 + What);
+    used_energy_floor = false;
+    used_energy_max = false;
+    if (ehat_trial <= e_floor) {
+      used_energy_floor = true;
+      return e_floor;
+    } else if (ehat_trial > e_max) {
+      used_energy_max = true;
+      return e_max;
+    }
+    return ehat_trial;
+  }
+  __device__ __forceinline__ double operator()(const Par &p, double mu) {
+    const double x = x_mu(mu);
+    const double rbarsq = rbarsq_mu(mu, x);
+    const double qbar = qbar_mu(mu, x);
+    const double vhatsq = vhatsq_mu(mu, rbarsq);
+    const double iWhat = iWhat_mu(vhatsq);
+    const double What = ratio(1.0, iWhat);
+    const double rhohat = rhohat_mu(iWhat);
+    const double ehat = ehat_mu(p, mu, qbar, rbarsq, vhatsq, What);
+    const double Phat = eos_P_rho_sie(p, rhohat, ehat);
+    const double hhat = rhohat * (1.0 + ehat) + Phat;
+    const double ahat = Phat / make_positive(hhat - Phat);
+    const double nua = (1.0 + ahat) * (1.0 + ehat) * iWhat;
+    const double nub = (1.0 + ahat) * (1.0 + qbar - mu * rbarsq);
+    const double nuhat = fmax(nua, nub);
+    const double muhat = 1.0 / (nuhat + mu * rbarsq);
+    return mu - muhat;
+  }
+  __device__ __forceinline__ bool used_bounds() const {
+    return used_density_floor || used_energy_floor || used_energy_max || used_gamma_max;
+  }
+};
+
+// Outcome of one zone (written back by the caller).
+struct C2POut {
+  int iterations;
+  int evals;
+  bool success;
+  bool bracketed;
+  bool nan_input;
+};
+
+// Setup of the inversion (con2prim_robust.hpp:303-366).  Returns false when
+// the input is NaN (the reference returns failure before touching prims).
+template <bool MINK>
+__device__ __forceinline__ bool c2p_setup(const Par &p, const Pt &g, const double U[PHX_NCONS],
+                                          double x1, double x2, double x3, Residual &res,
+                                          double rcon[3], double rcov[3], double bu[3],
+                                          double Bprim[3], double &bdotr) {
+  const int num_nans = isnan(U[PHX_CRHO]) + isnan(U[PHX_CMOM]) + isnan(U[PHX_CENG]);
+  if (num_nans > 0) return false;
+  const double gdet = MINK ? 1.0 : g.detgam;
+  const double igdet = 1.0 / gdet;
+  double rhoflr = 0.0, epsflr;
+  get_floors(p, x1, x2, x3, rhoflr, epsflr);
+  rhoflr *= p.fsf;
+  const double gam_max = p.g0;
+  const double D = U[PHX_CRHO] * igdet;
+  const double tau = U[PHX_CENG] * igdet;
+  const double q = ratio(tau, D);
+  double bsq = 0.0, bsq_rpsq = 0.0, rbsq = 0.0, rsq;
+  bdotr = 0.0;
+  rcov[0] = ratio(U[PHX_CMOM], U[PHX_CRHO]);
+  rcov[1] = ratio(U[PHX_CMOM + 1], U[PHX_CRHO]);
+  rcov[2] = ratio(U[PHX_CMOM + 2], U[PHX_CRHO]);
+  if constexpr (MINK) {
+    rcon[0] = rcov[0];
+    rcon[1] = rcov[1];
+    rcon[2] = rcov[2];
+    rsq = rcon[0] * rcov[0] + rcon[1] * rcov[1] + rcon[2] * rcov[2];
+  } else {
+    rsq = 0.0;
+#pragma unroll
+    for (int ii = 0; ii < 3; ii++) {
+      rcon[ii] = 0.0;
+#pragma unroll
+      for (int jj = 0; jj < 3; jj++) rcon[ii] += g.gamcon[ii][jj] * rcov[jj];
+      rsq += rcon[ii] * rcov[ii];
+    }
+  }
+  bu[0] = bu[1] = bu[2] = 0.0;
+  if (p.mhd) {
+#pragma unroll
+    for (int ii = 0; ii < 3; ii++) Bprim[ii] = U[PHX_CB + ii] * igdet;
+    const double sD = 1.0 / sqrt(fmax(D, rhoflr));
+#pragma unroll
+    for (int ii = 0; ii < 3; ii++) {
+      bu[ii] = Bprim[ii] * sD;
+      bdotr += bu[ii] * rcov[ii];
+    }
+    bsq = dot_sp<MINK>(g, bu, bu);
+    bsq = fmax(0.0, bsq);
+    rbsq = bdotr * bdotr;
+    bsq_rpsq = bsq * rsq - rbsq;
+  }
+  const double zsq = rsq / 1.0;  // h0sq_ = 1
+  const double v0sq = fmin(zsq / (1.0 + zsq), 1.0 - 1.0 / (gam_max * gam_max));
+  res.D = D;
+  res.q = q;
+  res.bsq = bsq;
+  res.bsq_rpsq = bsq_rpsq;
+  res.rsq = rsq;
+  res.rbsq = rbsq;
+  res.v0sq = v0sq;
+  res.x1 = x1;
+  res.x2 = x2;
+  res.x3 = x3;
+  res.init(p);
+  return true;
+}
+
+// refine_bracket + regula_falsi (root_find.hpp:42-58, 110-167), vote-driven.
+// valid = this lane owns a zone.  Returns mu; iterations/evals/bracketed
+// through out.  lo/hi: starting bracket ([0, 1] in the reference).
+__device__ __forceinline__ double regula_falsi_warp(const Par &p, Residual &res, bool valid,
+                                                   double a, double b, double guess, C2POut &out) {
+  const double tol = p.c2p_tol;
+  const int max_iter = p.c2p_max_iter;
+  double ya = 0.0, yb = 0.0;
+  int evals = 0;
+  bool bracketed = true;
+  if (valid) {
+    if (a <= guess && b >= guess) {
+      ya = res(p, guess);
+      yb = res(p, b);
+      evals += 2;
+      if (ya * yb > 0.0) {
+        yb = ya;
+        b = guess;
+        ya = res(p, a);
+        evals++;
+      } else {
+        a = guess;
+      }
+    } else {
+      ya = res(p, a);
+      yb = res(p, b);
+      evals += 2;
+    }
+    bracketed = !(ya * yb > 0.0);
+  }
+  int it = 0;
+  double sign = (ya < 0 ? 1.0 : -1.0);
+  ya *= sign;
+  yb *= sign;
+  int b1 = 0, b2 = 0;
+  bool active = valid && bracketed && (b - a > 2.0 * tol) && (it < max_iter);
+  while (__any_sync(0xffffffffu, active)) {
+    if (active) {
+      const double c = (a * yb - b * ya) / (yb - ya);
+      if (c == a) {
+        b = a;
+      } else if (c == b) {
+        a = b;
+      } else {
+        const double yc = sign * res(p, c);
+        evals++;
+        if (yc > 0.0) {
+          b = c;
+          yb = yc;
+          b1++;
+          ya *= (b1 > 1 ? 0.5 : 1.0);
+          b2 = 0;
+        } else if (yc < 0.0) {
+          a = c;
+          ya = yc;
+          b2++;
+          yb *= (b2 > 1 ? 0.5 : 1.0);
+          b1 = 0;
+        } else {
+          a = c;
+          b = c;
+        }
+      }
+      it++;
+      active = (b - a > 2.0 * tol) && (it < max_iter);
+    }
+  }
+  out.iterations = it;
+  out.evals = evals;
+  out.bracketed = bracketed;
+  if (!bracketed) return guess;
+  return 0.5 * (a + b);
+}
+
+// Unwrap mu into primitives (con2prim_robust.hpp:381-452).
+// prim[] receives PHX_NPRIM values (B slots only when mhd), U[] may be
+// rewritten by p2c when bounds were used; sig[3] receives signal speeds.
+template <bool MINK>
+__device__ __forceinline__ void c2p_finish(const Par &p, const Pt &g, Residual &res, double mu,
+                                           const double rcon[3], const double bu_in[3],
+                                           const double Bprim[3], double bdotr,
+                                           double prim[PHX_NPRIM], double U[PHX_NCONS],
+                                           double sig[3], bool &used_bounds_out) {
+  prim[PHX_PMU] = mu;
+  const double x = res.x_mu(mu);
+  const double rbarsq = res.rbarsq_mu(mu, x);
+  const double vsq = res.vhatsq_mu(mu, rbarsq);
+  const double iW = res.iWhat_mu(vsq);
+  prim[PHX_PRHO] = res.rhohat_mu(iW);
+  const double qbar = res.qbar_mu(mu, x);
+  const double W = 1.0 / iW;
+  double eng = res.ehat_mu(p, mu, qbar, rbarsq, vsq, W);
+  prim[PHX_PTMP] = eos_T_rho_sie(p, prim[PHX_PRHO], eng);
+  eng *= prim[PHX_PRHO];
+  prim[PHX_PENG] = eng;
+  prim[PHX_PPRS] = eos_P_rho_T(p, prim[PHX_PRHO], prim[PHX_PTMP]);
+  prim[PHX_PGM1] = eos_bmod_rho_T(p, prim[PHX_PRHO], prim[PHX_PTMP]) / prim[PHX_PPRS];
+  double vel[3];
+#pragma unroll
+  for (int ii = 0; ii < 3; ii++) {
+    vel[ii] = W * mu * x * (rcon[ii] + mu * bdotr * bu_in[ii]);
+    prim[PHX_PVEL + ii] = vel[ii];
+  }
+  double bu[3] = {0.0, 0.0, 0.0};
+  if (p.mhd) {
+#pragma unroll
+    for (int ii = 0; ii < 3; ii++) {
+      prim[PHX_PB + ii] = Bprim[ii];
+      bu[ii] = Bprim[ii];
+    }
+  }
+  used_bounds_out = res.used_bounds();
+  if (used_bounds_out) {
+    double S[3], bcons[3], Dn, taun;
+    const double gdet = MINK ? 1.0 : g.detgam;
+    p2c<MINK>(prim[PHX_PRHO], vel, bu, prim[PHX_PENG], prim[PHX_PPRS], prim[PHX_PGM1], g, gdet,
+              Dn, S, bcons, taun, sig);
+    U[PHX_CRHO] = Dn;
+    U[PHX_CENG] = taun;
+#pragma unroll
+    for (int ii = 0; ii < 3; ii++) U[PHX_CMOM + ii] = S[ii];
+  } else {
+#pragma unroll
+    for (int m = 0; m < 3; m++) vel[m] *= iW;
+    double bsq = 0.0;
+    if (p.mhd) {
+      double bdotv;
+      if constexpr (MINK) {
+        bsq = bu[0] * bu[0] + bu[1] * bu[1] + bu[2] * bu[2];
+        bdotv = bu[0] * vel[0] + bu[1] * vel[1] + bu[2] * vel[2];
+      } else {
+        bdotv = 0.0;
+#pragma unroll
+        for (int m = 0; m < 3; m++)
+#pragma unroll
+          for (int n = 0; n < 3; n++) {
+            bsq += bu[m] * bu[n] * g.gcov[m + 1][n + 1];
+            bdotv += bu[m] * vel[n] * g.gcov[m + 1][n + 1];
+          }
+      }
+      bsq = iW * iW * bsq + bdotv * bdotv;
+    }
+    signal_speeds<MINK>(prim[PHX_PRHO], prim[PHX_PENG], prim[PHX_PPRS], bsq, vel, vsq,
+                        prim[PHX_PGM1], g, sig);
+  }
+}
+
+}  // namespace phx

@@ -1,0 +1,512 @@
+// phx_device.cuh -- per-zone FP64 physics of the phoebus fluid hot path, on
+// the device.
+//
+// Every function follows the operation order of the phoebus source it cites
+// (paths relative to the phoebus tree), so that the exact build (nvcc
+// -fmad=false) reproduces a CPU build without FMA contraction bit for bit.
+// Minkowski is folded at compile time: with gcov = diag(-1,1,1,1), lapse 1,
+// shift 0, each metric contraction of the reference reduces to the same
+// sequence of roundings on its nonzero terms (x * 1 = x, s + (+-0) = s), so the
+// folded form is bit-identical for finite states and saves most of the FP64
+// work of the general contraction.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/phx_fluid.h"
+
+namespace phx {
+
+// ------------------------------------------------------------ robust.hpp
+constexpr double kSMALL = 10 * 2.2250738585072014e-308;  // 10 * DBL_MIN
+constexpr double kEPS = 10 * 2.220446049250313e-16;      // 10 * DBL_EPSILON
+constexpr double kDBLMAX = 1.7976931348623157e308;
+
+__device__ __forceinline__ double make_positive(double v) { return fmax(v, kEPS); }
+__device__ __forceinline__ double make_bounded(double v, double vmin, double vmax) {
+  return fmin(fmax(v, vmin + kEPS), vmax * (1.0 - kEPS));
+}
+__device__ __forceinline__ double ratio(double a, double b) {
+  const double sgn = b >= 0 ? 1.0 : -1.0;
+  return a / (b + sgn * kSMALL);
+}
+
+// ---------------------------------------------------------- parameters
+// Device copy of the fluid / fixup / eos params (phx_params), with the
+// fixup package's defaults already resolved (fixup.cpp:120-180).
+struct Par {
+  double gm1, Cv;
+  double rho_min_eos, sie_min_eos;
+  double c2p_tol;
+  int c2p_max_iter;
+  double fsf;  // c2p_floor_scale_fac
+  int fail_on_floors, fail_on_ceilings;
+  int mhd;
+  int floor_type;
+  double r0, s0, ralpha, salpha;
+  double g0, smax0;
+  double bsqorho0, bsqou0;
+  int recon, riemann;
+  double cfl;
+  int c2p_fixup, strategy_floors, enable_floors, enable_mhd_floors;
+};
+
+// ------------------------------------------------ singularity-eos IdealGas
+__device__ __forceinline__ double eos_P_rho_sie(const Par &p, double rho, double sie) {
+  return fmax(0.0, p.gm1 * rho * sie);
+}
+__device__ __forceinline__ double eos_T_rho_sie(const Par &p, double rho, double sie) {
+  return fmax(0.0, sie / p.Cv);
+}
+__device__ __forceinline__ double eos_P_rho_T(const Par &p, double rho, double T) {
+  return fmax(0.0, p.gm1 * rho * p.Cv * T);
+}
+__device__ __forceinline__ double eos_bmod_rho_T(const Par &p, double rho, double T) {
+  return fmax(0.0, (p.gm1 + 1) * p.gm1 * rho * p.Cv * T);
+}
+
+// ------------------------------------------------------- fixup.hpp Bounds
+__device__ __forceinline__ void get_floors(const Par &p, double x1, double x2, double x3,
+                                           double &rflr, double &sflr) {
+  switch (p.floor_type) {
+  case PHX_FLOOR_CONSTANT_RHO_SIE:
+    rflr = p.r0;
+    sflr = p.s0;
+    break;
+  case PHX_FLOOR_EXPX1_RHO_SIE:
+    rflr = p.r0 * exp(p.ralpha * x1);
+    sflr = p.s0 * exp(p.salpha * x1);
+    break;
+  case PHX_FLOOR_EXPX1_RHO_U: {
+    double scratch = p.r0 * exp(p.ralpha * x1);
+    sflr = p.s0 * exp(p.salpha * x1) / fmax(rflr, scratch);
+    rflr = scratch;
+  } break;
+  case PHX_FLOOR_X1_RHO_SIE:
+    rflr = p.r0 * fmin(1.0, pow(x1, p.ralpha));
+    sflr = p.s0 * fmin(1.0, pow(x1, p.salpha));
+    break;
+  default: {
+    double r = sqrt(x1 * x1 + x2 * x2 + x3 * x3);
+    rflr = p.r0 * fmin(1.0, pow(r, p.ralpha));
+    sflr = p.s0 * fmin(1.0, pow(r, p.salpha));
+  } break;
+  }
+  rflr = fmax(rflr, p.rho_min_eos);
+  sflr = fmax(sflr, p.sie_min_eos);
+}
+
+// ------------------------------------------------------------ block view
+struct BView {
+  int n1t, n2t, n3t, ndim, ng, nx1, nx2, nx3;
+  long long vs;
+  double x0[3], dx[3];
+  double *prim, *cons, *flux, *face_sig, *cell_sig, *fail, *src, *emf, *dudt;
+  const double *gcent, *gface1, *gface2, *gderiv;
+  int fmks;
+  __device__ __forceinline__ long long idx(int k, int j, int i) const {
+    return ((long long)k * n2t + j) * n1t + i;
+  }
+  __device__ __forceinline__ double Xc(int d, int ix) const { return x0[d] + (ix + 0.5) * dx[d]; }
+  __device__ __forceinline__ double Xf(int d, int ix) const { return x0[d] + ix * dx[d]; }
+  __device__ __forceinline__ int is() const { return ng; }
+  __device__ __forceinline__ int ie() const { return ng + nx1 - 1; }
+  __device__ __forceinline__ int js() const { return ndim >= 2 ? ng : 0; }
+  __device__ __forceinline__ int je() const { return ndim >= 2 ? ng + nx2 - 1 : 0; }
+  __device__ __forceinline__ int ks() const { return ndim >= 3 ? ng : 0; }
+  __device__ __forceinline__ int ke() const { return ndim >= 3 ? ng + nx3 - 1 : 0; }
+};
+
+// ------------------------------------------------------------- geometry
+// Point geometry (values at a cell centre or a face).
+struct Pt {
+  double alpha, beta[3], gcov[4][4], gamcon[3][3], detgam;
+};
+
+__device__ __forceinline__ int flat2(int m, int n) {
+  // Flatten2 (geometry_utils.hpp:180-185): symmetric 4x4 packing
+  const int lo = m < n ? m : n, hi = m < n ? n : m;
+  return hi * (hi + 1) / 2 + lo;
+}
+
+// loc: 0 = centre (and X3 face), 1 = X1 face, 2 = X2 face
+__device__ __forceinline__ void load_pt(const BView &b, int loc, int j, int i, Pt &p) {
+  const double *t;
+  long long pitch, off;
+  if (loc == 1) {
+    t = b.gface1;
+    pitch = (long long)b.n2t * (b.n1t + 1);
+    off = (long long)j * (b.n1t + 1) + i;
+  } else if (loc == 2) {
+    t = b.gface2;
+    pitch = (long long)(b.n2t + 1) * b.n1t;
+    off = (long long)j * b.n1t + i;
+  } else {
+    t = b.gcent;
+    pitch = (long long)b.n2t * b.n1t;
+    off = (long long)j * b.n1t + i;
+  }
+  p.alpha = __ldg(t + PHX_G_ALPHA * pitch + off);
+#pragma unroll
+  for (int d = 0; d < 3; d++) p.beta[d] = __ldg(t + (PHX_G_BETA + d) * pitch + off);
+#pragma unroll
+  for (int m = 0; m < 4; m++)
+#pragma unroll
+    for (int n = 0; n < 4; n++) p.gcov[m][n] = __ldg(t + (PHX_G_GCOV + flat2(m, n)) * pitch + off);
+#pragma unroll
+  for (int m = 0; m < 3; m++)
+#pragma unroll
+    for (int n = 0; n < 3; n++) p.gamcon[m][n] = __ldg(t + (PHX_G_GAMCON + flat2(m, n)) * pitch + off);
+  p.detgam = __ldg(t + PHX_G_DETGAM * pitch + off);
+}
+
+// sum_{m,n} gcov[m+1][n+1] a[m] b[n], in the reference's loop order.
+template <bool MINK>
+__device__ __forceinline__ double dot_sp(const Pt &g, const double a[3], const double b[3]) {
+  if constexpr (MINK) {
+    return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+  } else {
+    double s = 0.0;
+#pragma unroll
+    for (int m = 0; m < 3; m++)
+#pragma unroll
+      for (int n = 0; n < 3; n++) s += g.gcov[m + 1][n + 1] * a[m] * b[n];
+    return s;
+  }
+}
+
+// ------------------------------------------------- relativity_utils.hpp
+template <bool MINK>
+__device__ __forceinline__ double lorentz(const Pt &g, const double v[3]) {
+  return sqrt(1. + dot_sp<MINK>(g, v, v));
+}
+
+// ---------------------------------------------------------- prim2con.hpp
+// signal_speeds (prim2con.hpp:24-46); ndim entries written.
+template <bool MINK>
+__device__ __forceinline__ void signal_speeds(double rho, double u, double p, double bsq,
+                                              const double v[3], double vsq, double gam1,
+                                              const Pt &g, double *sig) {
+  const double rho_rel = rho + u + p;
+  const double vasq = bsq / (rho_rel + bsq);
+  double cssq = gam1 * p / rho_rel;
+  cssq += vasq - cssq * vasq;
+  const double alpha = MINK ? 1.0 : g.alpha;
+  const double vcoff = alpha / (1.0 - vsq * cssq);
+#pragma unroll
+  for (int m = 0; m < 3; m++) {
+    const double gmm = MINK ? 1.0 : g.gamcon[m][m];
+    const double vpm = sqrt(cssq * (1.0 - vsq) * (gmm * (1.0 - vsq * cssq) - v[m] * v[m] * (1.0 - cssq)));
+    double vp = vcoff * (v[m] * (1.0 - cssq) + vpm);
+    double vm = vcoff * (v[m] * (1.0 - cssq) - vpm);
+    if constexpr (!MINK) {
+      vp -= g.beta[m];
+      vm -= g.beta[m];
+    }
+    sig[m] = fmax(fabs(vp), fabs(vm));
+  }
+}
+
+// p2c (prim2con.hpp:48-102)
+template <bool MINK>
+__device__ __forceinline__ void p2c(double rho, const double vp[3], const double b[3], double u,
+                                    double p, double gam1, const Pt &g, double gdet, double &D,
+                                    double S[3], double bcons[3], double &tau, double *sig) {
+  const double W = lorentz<MINK>(g, vp);
+  const double iW = 1.0 / W;
+  double v[3] = {vp[0] * iW, vp[1] * iW, vp[2] * iW};
+  double vsq, Bsq, Bdotv;
+  if constexpr (MINK) {
+    // the reference accumulates the three sums interleaved; each is independent
+    vsq = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+    Bsq = b[0] * b[0] + b[1] * b[1] + b[2] * b[2];
+    Bdotv = b[0] * v[0] + b[1] * v[1] + b[2] * v[2];
+  } else {
+    vsq = 0.0;
+    Bsq = 0.0;
+    Bdotv = 0.0;
+#pragma unroll
+    for (int ii = 0; ii < 3; ii++)
+#pragma unroll
+      for (int jj = 0; jj < 3; jj++) {
+        vsq += g.gcov[ii + 1][jj + 1] * v[ii] * v[jj];
+        Bsq += g.gcov[ii + 1][jj + 1] * b[ii] * b[jj];
+        Bdotv += g.gcov[ii + 1][jj + 1] * b[ii] * v[jj];
+      }
+  }
+  const double b0 = W * Bdotv;
+  const double alpha = MINK ? 1.0 : g.alpha;
+  double bcon[4];
+  bcon[0] = W * Bdotv / alpha;
+#pragma unroll
+  for (int m = 0; m < 3; m++) {
+    if constexpr (MINK)
+      bcon[m + 1] = b[m] * iW + Bdotv * W * v[m];
+    else
+      bcon[m + 1] = b[m] * iW + Bdotv * W * (v[m] - g.beta[m] / alpha);
+  }
+  const double bsq = Bsq * iW * iW + Bdotv * Bdotv;
+  double bcov[3];
+#pragma unroll
+  for (int m = 0; m < 3; m++) {
+    if constexpr (MINK) {
+      bcov[m] = bcon[m + 1];
+    } else {
+      bcov[m] = 0.0;
+#pragma unroll
+      for (int n = 0; n < 4; n++) bcov[m] += g.gcov[m + 1][n] * bcon[n];
+    }
+  }
+  D = gdet * rho * W;
+  const double rho_rel = (rho + u + p + bsq) * W * W;
+#pragma unroll
+  for (int m = 0; m < 3; m++) {
+    double vcov;
+    if constexpr (MINK) {
+      vcov = v[m];
+    } else {
+      vcov = 0.0;
+#pragma unroll
+      for (int n = 0; n < 3; n++) vcov += g.gcov[m + 1][n + 1] * v[n];
+    }
+    S[m] = gdet * (rho_rel * vcov - b0 * bcov[m]);
+    bcons[m] = gdet * b[m];
+  }
+  tau = gdet * (rho_rel - (p + 0.5 * bsq) - b0 * b0) - D;
+  if (sig != nullptr) signal_speeds<MINK>(rho, u, p, bsq, v, vsq, gam1, g, sig);
+}
+
+// -------------------------------------------------- reconstruction.hpp
+__device__ __forceinline__ double mc(double dm, double dp, double alpha) {
+  const double dc = (dm * dp > 0.0) * 0.5 * (dm + dp);
+  return copysign(fmin(fabs(dc), alpha * fmin(fabs(dm), fabs(dp))), dc);
+}
+__device__ __forceinline__ void recon_plm(double qm, double q0, double qp, double &ql, double &qr) {
+  double dq = qp - q0;
+  dq = mc(q0 - qm, dq, 1.5);
+  ql = q0 + 0.5 * dq;
+  qr = q0 - 0.5 * dq;
+}
+__device__ __forceinline__ void recon_weno5z(double q0, double q1, double q2, double q3, double q4,
+                                             double &ql, double &qr) {
+  constexpr double a00 = 1.0 / 3.0, a01 = -7.0 / 6.0, a02 = 11.0 / 6.0;
+  constexpr double a10 = -1.0 / 6.0, a11 = 5.0 / 6.0, a12 = 1.0 / 3.0;
+  constexpr double a20 = 1.0 / 3.0, a21 = 5.0 / 6.0, a22 = -1.0 / 6.0;
+  constexpr double g0 = 0.1, g1 = 0.6, g2 = 0.3;
+  constexpr double eps = 1e-100;
+  constexpr double t13 = 13.0 / 3.0;
+  double a = q0 - 2 * q1 + q2;
+  double b = q0 - 4.0 * q1 + 3.0 * q2;
+  double beta0 = t13 * a * a + b * b + eps;
+  a = q1 - 2.0 * q2 + q3;
+  b = q3 - q1;
+  double beta1 = t13 * a * a + b * b + eps;
+  a = q2 - 2.0 * q3 + q4;
+  b = q4 - 4.0 * q3 + 3.0 * q2;
+  double beta2 = t13 * a * a + b * b + eps;
+  const double tau5 = fabs(beta2 - beta0);
+  beta0 = (beta0 + tau5) / beta0;
+  beta1 = (beta1 + tau5) / beta1;
+  beta2 = (beta2 + tau5) / beta2;
+  double w0 = g0 * beta0 + eps;
+  double w1 = g1 * beta1 + eps;
+  double w2 = g2 * beta2 + eps;
+  double wsum = 1.0 / (w0 + w1 + w2);
+  ql = w0 * (a00 * q0 + a01 * q1 + a02 * q2);
+  ql += w1 * (a10 * q1 + a11 * q2 + a12 * q3);
+  ql += w2 * (a20 * q2 + a21 * q3 + a22 * q4);
+  ql *= wsum;
+  const double alpha_l = 3.0 * wsum * w0 * w1 * w2 / (g2 * w0 * w1 + g1 * w0 * w2 + g0 * w1 * w2) + eps;
+  w0 = g0 * beta2 + eps;
+  w1 = g1 * beta1 + eps;
+  w2 = g2 * beta0 + eps;
+  wsum = 1.0 / (w0 + w1 + w2);
+  qr = w0 * (a00 * q4 + a01 * q3 + a02 * q2);
+  qr += w1 * (a10 * q3 + a11 * q2 + a12 * q1);
+  qr += w2 * (a20 * q2 + a21 * q1 + a22 * q0);
+  qr *= wsum;
+  const double alpha_r = 3.0 * wsum * w0 * w1 * w2 / (g2 * w0 * w1 + g1 * w0 * w2 + g0 * w1 * w2) + eps;
+  double dq = q3 - q2;
+  dq = mc(q2 - q1, dq, 2.0);
+  const double alpha_lin = 2.0 * alpha_l * alpha_r / (alpha_l + alpha_r);
+  ql = alpha_lin * ql + (1.0 - alpha_lin) * (q2 + 0.5 * dq);
+  qr = alpha_lin * qr + (1.0 - alpha_lin) * (q2 - 0.5 * dq);
+}
+__device__ __forceinline__ double minmod(double a, double b) {
+  return a * b > 0.0 ? (fabs(a) < fabs(b) ? a : b) : 0.0;
+}
+__device__ __forceinline__ double mp5_subcalc(double Fjm2, double Fjm1, double Fj, double Fjp1,
+                                              double Fjp2) {
+  constexpr double alpha = 4.0, epsm = 1.e-12;
+  double f = 2.0 * Fjm2 - 13.0 * Fjm1 + 47.0 * Fj + 27.0 * Fjp1 - 3.0 * Fjp2;
+  f /= 60.0;
+  const double fMP = Fj + minmod(Fjp1 - Fj, alpha * (Fj - Fjm1));
+  if ((f - Fj) * (f - fMP) <= epsm) return f;
+  const double d2m = Fjm2 + Fj - 2.0 * Fjm1;
+  const double d2 = Fjm1 + Fjp1 - 2.0 * Fj;
+  const double d2p = Fj + Fjp2 - 2.0 * Fjp1;
+  double scrh1 = minmod(4.0 * d2 - d2p, 4.0 * d2p - d2);
+  double scrh2 = minmod(d2, d2p);
+  const double dMMp = minmod(scrh1, scrh2);
+  scrh1 = minmod(4.0 * d2m - d2, 4.0 * d2 - d2m);
+  scrh2 = minmod(d2, d2m);
+  const double dMMm = minmod(scrh1, scrh2);
+  const double fUL = Fj + alpha * (Fj - Fjm1);
+  const double fAV = 0.5 * (Fj + Fjp1);
+  const double fMD = fAV - 0.5 * dMMp;
+  const double fLC = 0.5 * (3.0 * Fj - Fjm1) + 4.0 / 3.0 * dMMm;
+  scrh1 = fmin(Fj, Fjp1);
+  scrh1 = fmin(scrh1, fMD);
+  scrh2 = fmin(Fj, fUL);
+  scrh2 = fmin(scrh2, fLC);
+  const double Fmin = fmax(scrh1, scrh2);
+  scrh1 = fmax(Fj, Fjp1);
+  scrh1 = fmax(scrh1, fMD);
+  scrh2 = fmax(Fj, fUL);
+  scrh2 = fmax(scrh2, fLC);
+  const double Fmax = fmin(scrh1, scrh2);
+  return f + minmod(Fmin - f, Fmax - f);  // Median(f, Fmin, Fmax)
+}
+
+// 5-point (or 3-point) reconstruction of one variable.  ql = value at the
+// upper face of the cell, qr = value at its lower face.
+template <int RECON>
+__device__ __forceinline__ void recon(double qm2, double qm1, double q0, double qp1, double qp2,
+                                      double &ql, double &qr) {
+  if constexpr (RECON == PHX_RECON_WENO5Z) {
+    recon_weno5z(qm2, qm1, q0, qp1, qp2, ql, qr);
+  } else if constexpr (RECON == PHX_RECON_MP5) {
+    ql = mp5_subcalc(qm2, qm1, q0, qp1, qp2);
+    qr = mp5_subcalc(qp2, qp1, q0, qm1, qm2);
+  } else if constexpr (RECON == PHX_RECON_LINEAR) {
+    recon_plm(qm1, q0, qp1, ql, qr);
+  } else {
+    ql = q0;
+    qr = q0;
+  }
+}
+
+// ------------------------------------------------------- riemann.hpp
+struct Face {
+  Pt g;          // face geometry (unused for Minkowski)
+  double gdet;   // DetG: 1 for Minkowski, alpha * detgam from the cache
+  double gammadet;
+  double gdd;
+  double X1, X2, X3;
+};
+
+// prim_to_flux (riemann.hpp:88-209) for face direction DIR (0-based).
+template <bool MINK, int DIR>
+__device__ __forceinline__ void prim_to_flux(const Par &par, const Face &f, const double q[PHX_NRECON],
+                                             double &vm, double &vp, double U[PHX_NCONS],
+                                             double F[PHX_NCONS], double sie_max, double gam_max) {
+  const Pt &g = f.g;
+  double rho_floor = q[PHX_PRHO];
+  double sie_floor;
+  get_floors(par, f.X1, f.X2, f.X3, rho_floor, sie_floor);
+  const double rho = fmax(q[PHX_PRHO], rho_floor);
+  double vpcon[3] = {q[PHX_PVEL], q[PHX_PVEL + 1], q[PHX_PVEL + 2]};
+  double W = lorentz<MINK>(g, vpcon);
+  if (W > gam_max) {
+    const double rescale = sqrt((gam_max * gam_max - 1.) / (W * W - 1.));
+#pragma unroll
+    for (int ii = 0; ii < 3; ii++) vpcon[ii] *= rescale;
+  }
+  double vcon[3] = {vpcon[0] / W, vpcon[1] / W, vpcon[2] / W};
+  double Bcon[3] = {0.0, 0.0, 0.0};
+  const double qe = q[PHX_PENG];
+  const double u = (qe / rho > sie_floor ? (qe / rho > sie_max ? rho * sie_max : qe) : rho * sie_floor);
+  const double P = fmax(q[PHX_PPRS], 0.0);
+  const double gamma1 = q[PHX_PGM1];
+  if (par.mhd) {
+    Bcon[0] = q[PHX_PB];
+    Bcon[1] = q[PHX_PB + 1];
+    Bcon[2] = q[PHX_PB + 2];
+  }
+  double vsq, Bdotv, BdotB;
+  if constexpr (MINK) {
+    vsq = vcon[0] * vcon[0] + vcon[1] * vcon[1] + vcon[2] * vcon[2];
+    Bdotv = Bcon[0] * vcon[0] + Bcon[1] * vcon[1] + Bcon[2] * vcon[2];
+    BdotB = Bcon[0] * Bcon[0] + Bcon[1] * Bcon[1] + Bcon[2] * Bcon[2];
+  } else {
+    vsq = 0.0;
+    Bdotv = 0.0;
+    BdotB = 0.0;
+#pragma unroll
+    for (int m = 0; m < 3; m++)
+#pragma unroll
+      for (int n = 0; n < 3; n++) {
+        vsq += g.gcov[m + 1][n + 1] * vcon[m] * vcon[n];
+        Bdotv += g.gcov[m + 1][n + 1] * Bcon[m] * vcon[n];
+        BdotB += g.gcov[m + 1][n + 1] * Bcon[m] * Bcon[n];
+      }
+  }
+  const double vsq_max = 1.0 - 1.0 / (gam_max * gam_max);
+  if (vsq > vsq_max) {
+    double scale = vsq_max / vsq;
+    vsq *= scale;
+    scale = sqrt(scale);
+    Bdotv *= scale;
+#pragma unroll
+    for (int m = 0; m < 3; m++) vcon[m] *= scale;
+  }
+  W = 1.0 / sqrt(1 - vsq);
+  const double vel = vcon[DIR];
+  const double alpha = MINK ? 1.0 : g.alpha;
+  double vtil;
+  if constexpr (MINK)
+    vtil = vel;
+  else
+    vtil = vel - g.beta[DIR] / alpha;
+  U[PHX_CRHO] = rho * W;
+  F[PHX_CRHO] = U[PHX_CRHO] * vtil;
+  const double b0 = W * Bdotv;
+  const double bsq = (BdotB + b0 * b0) / (W * W);
+  const double rhohWsq = (rho + u + P) * W * W;
+  const double bsqWsq = bsq * W * W;
+  const double ptot = P + 0.5 * bsq;
+#pragma unroll
+  for (int m = 0; m < 3; m++) {
+    double bcovm, vcovm;
+    if constexpr (MINK) {
+      // gcov[m+1][0] = 0: first term is +-0; then only n = m+1 survives
+      bcovm = Bcon[m] / W + b0 * vcon[m];
+      vcovm = vcon[m];
+    } else {
+      bcovm = g.gcov[m + 1][0] * b0 / alpha;
+      vcovm = 0.0;
+#pragma unroll
+      for (int n = 1; n < 4; n++) {
+        bcovm += g.gcov[m + 1][n] * (Bcon[n - 1] / W + b0 * (vcon[n - 1] - g.beta[n - 1] / alpha));
+        vcovm += g.gcov[m + 1][n] * vcon[n - 1];
+      }
+    }
+    U[PHX_CMOM + m] = (rhohWsq + bsqWsq) * vcovm - b0 * bcovm;
+    F[PHX_CMOM + m] = U[PHX_CMOM + m] * vtil + ptot * (double)(DIR == m) - bcovm * Bcon[DIR] / W;
+  }
+  U[PHX_CENG] = rhohWsq + bsqWsq - ptot - b0 * b0 - U[PHX_CRHO];
+  F[PHX_CENG] = U[PHX_CENG] * vtil + ptot * vel - Bdotv * Bcon[DIR];
+#pragma unroll
+  for (int m = 0; m < 3; m++) {
+    U[PHX_CB + m] = Bcon[m];
+    if constexpr (MINK)
+      F[PHX_CB + m] = U[PHX_CB + m] * vtil - Bcon[DIR] * vcon[m];
+    else
+      F[PHX_CB + m] = U[PHX_CB + m] * vtil - Bcon[DIR] * (vcon[m] - g.beta[m] / alpha);
+  }
+  const double vasq = bsqWsq / make_positive(rhohWsq + bsqWsq);
+  const double cssq = make_bounded(gamma1 * P * W * W / make_positive(rhohWsq), 0.0, 1.0);
+  const double cmsq = make_bounded(cssq + vasq * (1.0 - cssq), 0.0, 1.0);
+  const double vcoff = alpha / (1.0 - vsq * cmsq);
+  const double v0 = vel * (1.0 - cmsq);
+  const double gdd = MINK ? 1.0 : f.gdd;
+  const double vpm = sqrt(make_positive(cmsq * (1.0 - vsq) * (gdd * (1.0 - vsq * cmsq) - vel * v0)));
+  vp = vcoff * (v0 + vpm);
+  vm = vcoff * (v0 - vpm);
+  if constexpr (!MINK) {
+    vp -= g.beta[DIR];
+    vm -= g.beta[DIR];
+  }
+}
+
+}  // namespace phx

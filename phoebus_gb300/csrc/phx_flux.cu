@@ -1,0 +1,310 @@
+// phx_flux.cu -- fluid::CalculateFluxes (fluid.cpp:659-773) as fused
+// reconstruction + Riemann kernels, one launch per direction.
+//
+// The reference reconstructs every variable into ql/qr arrays (K1) and then
+// solves one Riemann problem per face (K2).  Here each face's two states are
+// produced and consumed in registers:
+//   X1: a warp owns one (k, j) pencil.  Lane 0 stages the pencil's 10
+//       primitive rows in shared memory with cp.async.bulk (TMA bulk copies
+//       completing on an mbarrier); lanes reconstruct consecutive cells and
+//       the left state of face i (the upper-face value of cell i-1) moves to
+//       lane i with __shfl_up_sync.
+//   X2, X3: a thread sweeps a segment of faces along the direction with the
+//       5-point stencil window and the previous cell's upper-face state held
+//       in registers; consecutive lanes are consecutive i (coalesced).
+// Faces computed, per direction d: along d [s, e+1]; transverse active
+// directions [s-1, e+1].  These are all the faces FluxDivergence, FluxCT and
+// EstimateTimestep read.
+#include "phx_kernels.cuh"
+
+namespace phx {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+// Riemann solve + store for one face (riemann.hpp:256-301).
+template <bool MINK, int DIR>
+__device__ __forceinline__ void face_flux(const Par &p, const BView &b, int k, int j, int i,
+                                          const double ql[PHX_NRECON], const double qr[PHX_NRECON]) {
+  Face f;
+  if constexpr (!MINK) {
+    load_pt(b, DIR == 0 ? 1 : (DIR == 1 ? 2 : 0), j, i, f.g);
+    f.gdet = f.g.alpha * f.g.detgam;
+    f.gammadet = f.g.detgam;
+    f.gdd = f.g.gamcon[DIR][DIR];
+  }
+  f.X1 = DIR == 0 ? b.Xf(0, i) : b.Xc(0, i);
+  f.X2 = DIR == 1 ? b.Xf(1, j) : b.Xc(1, j);
+  f.X3 = DIR == 2 ? b.Xf(2, k) : b.Xc(2, k);
+  const double gam_max = p.g0, sie_max = p.smax0;
+  double Ul[PHX_NCONS], Fl[PHX_NCONS], Ur[PHX_NCONS], Fr[PHX_NCONS];
+  double vml, vpl, vmr, vpr;
+  prim_to_flux<MINK, DIR>(p, f, ql, vml, vpl, Ul, Fl, sie_max, gam_max);
+  prim_to_flux<MINK, DIR>(p, f, qr, vmr, vpr, Ur, Fr, sie_max, gam_max);
+  const double gdet = MINK ? 1.0 : f.gdet;
+  const double gammadet = MINK ? 1.0 : f.gammadet;
+  const long long id = b.idx(k, j, i);
+  double *fx = b.flux + (long long)DIR * PHX_NCONS * b.vs + id;
+  const int ncons = p.mhd ? PHX_NCONS : 5;
+  double sig;
+  if (p.riemann == PHX_RIEMANN_LLF) {
+    const double cmax = fmax(fmax(-vml, vpl), fmax(-vmr, vpr));
+#pragma unroll
+    for (int m = 0; m < PHX_NCONS; m++)
+      if (m < ncons) fx[m * b.vs] = 0.5 * ((Fl[m] + Fr[m]) * gdet - cmax * ((Ur[m] - Ul[m]) * gammadet));
+    sig = cmax;
+  } else {
+    const double cl = fmin(fmin(vml, vmr), 0.0);
+    const double cr = fmax(fmax(vpl, vpr), 0.0);
+    const double crcl = cr * cl;
+    const double inv_cr_cl = ratio(1.0, cr - cl);
+#pragma unroll
+    for (int m = 0; m < PHX_NCONS; m++)
+      if (m < ncons)
+        fx[m * b.vs] = ((cr * Fl[m] - cl * Fr[m]) * gdet + crcl * (Ur[m] - Ul[m]) * gammadet) * inv_cr_cl;
+    sig = fmax(-cl, cr);
+  }
+  b.face_sig[(long long)DIR * b.vs + id] = sig;
+}
+
+// ------------------------------------------------------------------ X1
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned phase) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+constexpr int X1_WARPS = 4;
+constexpr long long MBAR_SPIN_LIMIT = 1ll << 26;
+
+// One warp per (k, j) pencil; pencils enumerated over the transverse box.
+template <int RECON, bool MINK>
+__global__ void __launch_bounds__(32 * X1_WARPS)
+    k_flux_x1(Par p, BView b, int jlo, int nj, int klo, int npencil, int use_tma, unsigned int *err) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bars[X1_WARPS];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n1t = b.n1t;
+  double *row = reinterpret_cast<double *>(smem_raw) + (long long)warp * PHX_NRECON * n1t;
+  const int pencil = blockIdx.x * X1_WARPS + warp;
+  if (use_tma) {
+    if (lane == 0) mbar_init(&bars[warp], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    __syncwarp();
+  }
+  if (pencil >= npencil) return;  // whole warp leaves together
+  const int j = jlo + pencil % nj;
+  const int k = klo + pencil / nj;
+  const long long base = b.idx(k, j, 0);
+  if (use_tma) {
+    if (lane == 0) {
+      const unsigned bytes = (unsigned)(n1t * sizeof(double));
+      mbar_expect_tx(&bars[warp], bytes * PHX_NRECON);
+#pragma unroll 1
+      for (int v = 0; v < PHX_NRECON; v++) bulk_g2s(row + v * n1t, b.prim + v * b.vs + base, bytes, &bars[warp]);
+    }
+    long long spins = 0;
+    while (!mbar_try_wait(&bars[warp], 0)) {
+      if (++spins > MBAR_SPIN_LIMIT) {
+        if (lane == 0) atomicOr(err, ERR_TIMEOUT);
+        return;
+      }
+    }
+  } else {
+    for (int v = 0; v < PHX_NRECON; v++)
+      for (int i = lane; i < n1t; i += 32) row[v * n1t + i] = b.prim[v * b.vs + base + i];
+    __syncwarp();
+  }
+  const int c0 = b.is() - 1, c1 = b.ie() + 1;  // cells reconstructed
+  double carry[PHX_NRECON];
+#pragma unroll
+  for (int v = 0; v < PHX_NRECON; v++) carry[v] = 0.0;
+  for (int cbase = c0; cbase <= c1; cbase += 32) {
+    const int c = cbase + lane;
+    const bool have = c <= c1;
+    double ql[PHX_NRECON], qr[PHX_NRECON];
+#pragma unroll
+    for (int v = 0; v < PHX_NRECON; v++) {
+      const double *r = row + v * n1t;
+      if (have) {
+        if constexpr (RECON == PHX_RECON_WENO5Z || RECON == PHX_RECON_MP5)
+          recon<RECON>(r[c - 2], r[c - 1], r[c], r[c + 1], r[c + 2], ql[v], qr[v]);
+        else if constexpr (RECON == PHX_RECON_LINEAR)
+          recon<RECON>(0.0, r[c - 1], r[c], r[c + 1], 0.0, ql[v], qr[v]);
+        else
+          recon<RECON>(0.0, 0.0, r[c], 0.0, 0.0, ql[v], qr[v]);
+      } else {
+        ql[v] = qr[v] = 0.0;
+      }
+    }
+    double left[PHX_NRECON];
+#pragma unroll
+    for (int v = 0; v < PHX_NRECON; v++) {
+      const double up = __shfl_up_sync(FULL, ql[v], 1);
+      left[v] = lane == 0 ? carry[v] : up;
+      carry[v] = __shfl_sync(FULL, ql[v], 31);
+    }
+    // face c: left state from cell c-1, right state from cell c
+    if (have && c >= b.is()) face_flux<MINK, 0>(p, b, k, j, c, left, qr);
+  }
+}
+
+// ------------------------------------------------------------- sweeps
+// Thread = (transverse a, transverse c, segment).  DIR 1: a = i, c = k;
+// DIR 2: a = i, c = j; DIR 0 (fallback for X1): a = j, c = k.
+template <int RECON, bool MINK, int DIR>
+__global__ void __launch_bounds__(128)
+    k_flux_sweep(Par p, BView b, int alo, int na, int clo, int nc, int f0, int nface, int seg,
+                 int nseg) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long total = (long long)na * nc * nseg;
+  if (t >= total) return;
+  const int a = alo + (int)(t % na);
+  const long long q = t / na;
+  const int s = (int)(q % nseg);
+  const int cc = clo + (int)(q / nseg);
+  const int fbeg = f0 + s * seg;
+  const int fend = min(f0 + nface - 1, fbeg + seg - 1);
+  if (fbeg > fend) return;
+  // position along the sweep direction -> (k, j, i)
+  auto kji = [&](int x, int &k, int &j, int &i) {
+    if constexpr (DIR == 0) {
+      i = x;
+      j = a;
+      k = cc;
+    } else if constexpr (DIR == 1) {
+      i = a;
+      j = x;
+      k = cc;
+    } else {
+      i = a;
+      j = cc;
+      k = x;
+    }
+  };
+  long long stride;
+  if constexpr (DIR == 0)
+    stride = 1;
+  else if constexpr (DIR == 1)
+    stride = b.n1t;
+  else
+    stride = (long long)b.n1t * b.n2t;
+  int k0, j0, i0;
+  kji(fbeg - 1, k0, j0, i0);
+  const double *pc = b.prim + b.idx(k0, j0, i0);  // cell fbeg-1
+  const long long vs = b.vs;
+  double w[PHX_NRECON][5];
+#pragma unroll
+  for (int v = 0; v < PHX_NRECON; v++)
+#pragma unroll
+    for (int o = 0; o < 4; o++) w[v][o + 1] = pc[v * vs + (o - 2) * stride];  // cells x-2..x+1
+  double prev_ql[PHX_NRECON];
+  for (int x = fbeg - 1; x <= fend; x++) {
+    const double *pn = pc + (long long)(x - (fbeg - 1)) * stride;
+    double ql[PHX_NRECON], qr[PHX_NRECON];
+#pragma unroll
+    for (int v = 0; v < PHX_NRECON; v++) {
+#pragma unroll
+      for (int o = 0; o < 4; o++) w[v][o] = w[v][o + 1];
+      w[v][4] = pn[v * vs + 2 * stride];
+      recon<RECON>(w[v][0], w[v][1], w[v][2], w[v][3], w[v][4], ql[v], qr[v]);
+    }
+    if (x >= fbeg) {
+      int k, j, i;
+      kji(x, k, j, i);
+      face_flux<MINK, DIR>(p, b, k, j, i, prev_ql, qr);
+    }
+#pragma unroll
+    for (int v = 0; v < PHX_NRECON; v++) prev_ql[v] = ql[v];
+  }
+}
+
+template <int RECON, bool MINK, int DIR>
+static void launch_sweep(const Par &p, const BView &b, int alo, int na, int clo, int nc, int f0,
+                         int nface, cudaStream_t s) {
+  const int target = 32;
+  const int nseg = (nface + target - 1) / target;
+  const int seg = (nface + nseg - 1) / nseg;
+  const long long total = (long long)na * nc * nseg;
+  const int T = 128;
+  k_flux_sweep<RECON, MINK, DIR><<<(unsigned)((total + T - 1) / T), T, 0, s>>>(p, b, alo, na, clo, nc,
+                                                                            f0, nface, seg, nseg);
+}
+
+template <int RECON, bool MINK>
+static void launch_fluxes_t(const Par &p, const BView &b, unsigned int *err, cudaStream_t s) {
+  const int ndim = b.ndim;
+  const int dk = ndim == 3 ? 1 : 0, dj = ndim > 1 ? 1 : 0;
+  const int is = b.ng, ie = b.ng + b.nx1 - 1;
+  const int js = dj ? b.ng : 0, je = dj ? b.ng + b.nx2 - 1 : 0;
+  const int ks = dk ? b.ng : 0, ke = dk ? b.ng + b.nx3 - 1 : 0;
+  // X1 faces: i in [is, ie+1]; j in [js-dj, je+dj]; k in [ks-dk, ke+dk]
+  {
+    const int jlo = js - dj, nj = je - js + 1 + 2 * dj;
+    const int klo = ks - dk, nk = ke - ks + 1 + 2 * dk;
+    const int npencil = nj * nk;
+    const size_t smem = (size_t)X1_WARPS * PHX_NRECON * b.n1t * sizeof(double);
+    const bool aligned = (b.n1t % 2 == 0) && (b.vs % 2 == 0) &&
+                         ((reinterpret_cast<uintptr_t>(b.prim) & 15) == 0);
+    if (smem <= 200 * 1024) {
+      auto kern = k_flux_x1<RECON, MINK>;
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      kern<<<(npencil + X1_WARPS - 1) / X1_WARPS, 32 * X1_WARPS, smem, s>>>(p, b, jlo, nj, klo, npencil,
+                                                                          aligned ? 1 : 0, err);
+    } else {
+      launch_sweep<RECON, MINK, 0>(p, b, jlo, nj, klo, nk, is, ie - is + 2, s);
+    }
+  }
+  if (ndim >= 2) {  // X2 faces: j in [js, je+1]; i in [is-1, ie+1]; k in [ks-dk, ke+dk]
+    launch_sweep<RECON, MINK, 1>(p, b, is - 1, ie - is + 3, ks - dk, ke - ks + 1 + 2 * dk, js,
+                                 je - js + 2, s);
+  }
+  if (ndim >= 3) {  // X3 faces: k in [ks, ke+1]; i in [is-1, ie+1]; j in [js-1, je+1]
+    launch_sweep<RECON, MINK, 2>(p, b, is - 1, ie - is + 3, js - 1, je - js + 3, ks, ke - ks + 2, s);
+  }
+}
+
+void launch_fluxes_err(const Par &p, const BView &b, unsigned int *err, cudaStream_t s) {
+  const bool mink = !b.fmks;
+  switch (p.recon) {
+  case PHX_RECON_WENO5Z:
+    mink ? launch_fluxes_t<PHX_RECON_WENO5Z, true>(p, b, err, s)
+         : launch_fluxes_t<PHX_RECON_WENO5Z, false>(p, b, err, s);
+    break;
+  case PHX_RECON_MP5:
+    mink ? launch_fluxes_t<PHX_RECON_MP5, true>(p, b, err, s) : launch_fluxes_t<PHX_RECON_MP5, false>(p, b, err, s);
+    break;
+  case PHX_RECON_LINEAR:
+    mink ? launch_fluxes_t<PHX_RECON_LINEAR, true>(p, b, err, s)
+         : launch_fluxes_t<PHX_RECON_LINEAR, false>(p, b, err, s);
+    break;
+  default:
+    mink ? launch_fluxes_t<PHX_RECON_CONSTANT, true>(p, b, err, s)
+         : launch_fluxes_t<PHX_RECON_CONSTANT, false>(p, b, err, s);
+    break;
+  }
+}
+
+}  // namespace phx

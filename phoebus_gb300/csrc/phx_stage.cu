@@ -1,0 +1,330 @@
+// phx_stage.cu -- stage glue around the flux and con2prim kernels:
+//   FluxCT (fluid.cpp:775-841), geometric sources (fluid.cpp:566-657 with
+//   tmunu.hpp:62-131), FluxDivergence + SumData + Average/UpdateIndependentData
+//   (phoebus_driver.cpp:547-577), periodic ghost exchange, and
+//   EstimateTimestepBlock (fluid.cpp:899-944) as an on-device min-reduction.
+#include "phx_kernels.cuh"
+
+namespace phx {
+
+__device__ __forceinline__ double &FX(const BView &b, int d, int m, long long id) {
+  return b.flux[((long long)d * PHX_NCONS + m) * b.vs + id];
+}
+
+// ---------------------------------------------------------------- FluxCT
+__global__ void k_emf3d(BView b, int is, int js, int ks, int ni, int nj, long long n) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = is + (int)(t % ni);
+  const int j = js + (int)((t / ni) % nj);
+  const int k = ks + (int)(t / ((long long)ni * nj));
+  const long long id = b.idx(k, j, i);
+  const long long dk = (long long)b.n1t * b.n2t, dj = b.n1t;
+  const int B1 = PHX_CB, B2 = PHX_CB + 1, B3 = PHX_CB + 2;
+  b.emf[id] = 0.25 * (FX(b, 1, B3, id) + FX(b, 1, B3, id - dk) - FX(b, 2, B2, id) - FX(b, 2, B2, id - dj));
+  b.emf[b.vs + id] = -0.25 * (FX(b, 0, B3, id) + FX(b, 0, B3, id - dk) - FX(b, 2, B1, id) - FX(b, 2, B1, id - 1));
+  b.emf[2 * b.vs + id] = 0.25 * (FX(b, 0, B2, id) + FX(b, 0, B2, id - dj) - FX(b, 1, B1, id) - FX(b, 1, B1, id - 1));
+}
+__global__ void k_ctflux3d(BView b, int is, int js, int ks, int ni, int nj, long long n) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = is + (int)(t % ni);
+  const int j = js + (int)((t / ni) % nj);
+  const int k = ks + (int)(t / ((long long)ni * nj));
+  const long long id = b.idx(k, j, i);
+  const long long dk = (long long)b.n1t * b.n2t, dj = b.n1t;
+  const double *e0 = b.emf, *e1 = b.emf + b.vs, *e2 = b.emf + 2 * b.vs;
+  const int B1 = PHX_CB, B2 = PHX_CB + 1, B3 = PHX_CB + 2;
+  FX(b, 0, B1, id) = 0.0;
+  FX(b, 0, B2, id) = 0.5 * (e2[id] + e2[id + dj]);
+  FX(b, 0, B3, id) = -0.5 * (e1[id] + e1[id + dk]);
+  FX(b, 1, B1, id) = -0.5 * (e2[id] + e2[id + 1]);
+  FX(b, 1, B2, id) = 0.0;
+  FX(b, 1, B3, id) = 0.5 * (e0[id] + e0[id + dk]);
+  FX(b, 2, B1, id) = 0.5 * (e1[id] + e1[id + 1]);
+  FX(b, 2, B2, id) = -0.5 * (e0[id] + e0[id + dj]);
+  FX(b, 2, B3, id) = 0.0;
+}
+__global__ void k_emf2d(BView b, int is, int js, int ni, long long n) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = is + (int)(t % ni);
+  const int j = js + (int)(t / ni);
+  const long long id = b.idx(0, j, i), dj = b.n1t;
+  const int B1 = PHX_CB, B2 = PHX_CB + 1;
+  b.emf[id] = 0.25 * (FX(b, 0, B2, id) + FX(b, 0, B2, id - dj) - FX(b, 1, B1, id) - FX(b, 1, B1, id - 1));
+}
+__global__ void k_ctflux2d(BView b, int is, int js, int ni, long long n) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = is + (int)(t % ni);
+  const int j = js + (int)(t / ni);
+  const long long id = b.idx(0, j, i), dj = b.n1t;
+  const int B1 = PHX_CB, B2 = PHX_CB + 1;
+  FX(b, 0, B1, id) = 0.0;
+  FX(b, 0, B2, id) = 0.5 * (b.emf[id] + b.emf[id + dj]);
+  FX(b, 1, B1, id) = -0.5 * (b.emf[id] + b.emf[id + 1]);
+  FX(b, 1, B2, id) = 0.0;
+}
+
+void launch_fluxct(const BView &b, cudaStream_t s) {
+  const int T = 256;
+  if (b.ndim == 3) {
+    const int ni = b.nx1 + 1, nj = b.nx2 + 1, nk = b.nx3 + 1;
+    const long long n = (long long)ni * nj * nk;
+    const unsigned g = (unsigned)((n + T - 1) / T);
+    k_emf3d<<<g, T, 0, s>>>(b, b.ng, b.ng, b.ng, ni, nj, n);
+    k_ctflux3d<<<g, T, 0, s>>>(b, b.ng, b.ng, b.ng, ni, nj, n);
+  } else if (b.ndim == 2) {
+    const int ni = b.nx1 + 1, nj = b.nx2 + 1;
+    const long long n = (long long)ni * nj;
+    const unsigned g = (unsigned)((n + T - 1) / T);
+    k_emf2d<<<g, T, 0, s>>>(b, b.ng, b.ng, ni, n);
+    k_ctflux2d<<<g, T, 0, s>>>(b, b.ng, b.ng, ni, n);
+  }
+}
+
+// -------------------------------------- FluxDivergence + RK2 stage update
+// dudt = -(A1 dF1 + A2 dF2 + A3 dF3) / V (+ src for S_i, tau);
+// u0 = beta u0 + (1 - beta) base; out = u0 + (beta dt) dudt.
+__global__ void __launch_bounds__(256) k_update(BView b, const double *base, double *out, double beta,
+                                                double bdt, double A1, double A2, double A3,
+                                                double V, int ncons, long long n) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int ni = b.nx1, nj = b.ndim >= 2 ? b.nx2 : 1;
+  const int i = b.ng + (int)(t % ni);
+  const int j = (b.ndim >= 2 ? b.ng : 0) + (int)((t / ni) % nj);
+  const int k = (b.ndim >= 3 ? b.ng : 0) + (int)(t / ((long long)ni * nj));
+  const long long id = b.idx(k, j, i);
+  const long long dk = (long long)b.n1t * b.n2t, dj = b.n1t;
+  for (int m = 0; m < ncons; m++) {
+    double du = (A1 * FX(b, 0, m, id + 1) - A1 * FX(b, 0, m, id));
+    if (b.ndim >= 2) du += A2 * FX(b, 1, m, id + dj) - A2 * FX(b, 1, m, id);
+    if (b.ndim == 3) du += A3 * FX(b, 2, m, id + dk) - A3 * FX(b, 2, m, id);
+    double r = -du / V;
+    if (m >= 1 && m <= 4 && b.src != nullptr) r = r + b.src[(m - 1) * b.vs + id];
+    const long long vid = m * b.vs + id;
+    if (b.dudt != nullptr) b.dudt[vid] = r;
+    if (out != nullptr) {
+      double u0 = b.cons[vid];
+      u0 = beta * u0 + (1 - beta) * base[vid];
+      b.cons[vid] = u0;
+      out[vid] = u0 + bdt * r;
+    }
+  }
+}
+
+void launch_update(const Par &p, const BView &b, const double *base, double *out, double beta,
+                   double dt, cudaStream_t s) {
+  const double dx1 = b.dx[0], dx2 = b.dx[1], dx3 = b.dx[2];
+  const double A1 = dx2 * dx3, A2 = dx1 * dx3, A3 = dx1 * dx2, V = dx1 * dx2 * dx3;
+  const long long n = (long long)b.nx1 * (b.ndim >= 2 ? b.nx2 : 1) * (b.ndim >= 3 ? b.nx3 : 1);
+  const int T = 256;
+  k_update<<<(unsigned)((n + T - 1) / T), T, 0, s>>>(b, base, out, beta, beta * dt, A1, A2, A3, V,
+                                                    p.mhd ? PHX_NCONS : 5, n);
+}
+
+// ------------------------------------------------ periodic ghost exchange
+__device__ __forceinline__ int wrap(int x, int ng, int n) {
+  if (x < ng) return x + n;
+  if (x >= ng + n) return x - n;
+  return x;
+}
+__global__ void __launch_bounds__(256) k_ghost(BView b, double *field, int nvar, long long n) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = (int)(t % b.n1t);
+  const int j = (int)((t / b.n1t) % b.n2t);
+  const int k = (int)(t / ((long long)b.n1t * b.n2t));
+  const int si = wrap(i, b.ng, b.nx1);
+  const int sj = b.ndim >= 2 ? wrap(j, b.ng, b.nx2) : j;
+  const int sk = b.ndim >= 3 ? wrap(k, b.ng, b.nx3) : k;
+  if (si == i && sj == j && sk == k) return;
+  const long long d = b.idx(k, j, i), src = b.idx(sk, sj, si);
+  for (int v = 0; v < nvar; v++) field[v * b.vs + d] = field[v * b.vs + src];
+}
+
+void launch_ghost_periodic(const BView &b, double *field, int nvar, cudaStream_t s) {
+  const long long n = (long long)b.n1t * b.n2t * b.n3t;
+  const int T = 256;
+  k_ghost<<<(unsigned)((n + T - 1) / T), T, 0, s>>>(b, field, nvar, n);
+}
+
+// ------------------------------------------------------------ timestep
+__global__ void k_dt_init(unsigned long long *scratch) { *scratch = 0x7ff0000000000000ull; }
+__global__ void __launch_bounds__(256) k_dt(BView b, int use_face, unsigned long long *scratch, long long n) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double v = 1.7976931348623157e308;
+  if (t < n) {
+    const int ni = b.nx1, nj = b.ndim >= 2 ? b.nx2 : 1;
+    const int i = b.ng + (int)(t % ni);
+    const int j = (b.ndim >= 2 ? b.ng : 0) + (int)((t / ni) % nj);
+    const int k = (b.ndim >= 3 ? b.ng : 0) + (int)(t / ((long long)ni * nj));
+    const long long id = b.idx(k, j, i);
+    double ldt = 0.0;
+    for (int d = 0; d < b.ndim; d++) {
+      double ms = b.cell_sig[d * b.vs + id];
+      if (use_face) {
+        const long long off = d == 0 ? 1 : (d == 1 ? (long long)b.n1t : (long long)b.n1t * b.n2t);
+        ms = fmax(ms, fmax(b.face_sig[d * b.vs + id], b.face_sig[d * b.vs + id + off]));
+      }
+      ldt += ms / b.dx[d];
+    }
+    v = 1.0 / (ldt + 1.e-50);
+  }
+  // positive doubles order like their bit patterns
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+  __shared__ double sm[8];
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) v = fmin(v, sm[w]);
+    if (!(v >= 0.0)) v = 1.7976931348623157e308;  // all-NaN block: skipped, like the serial min
+    atomicMin(scratch, (unsigned long long)__double_as_longlong(v));
+  }
+}
+__global__ void k_dt_final(const unsigned long long *scratch, double cfl, double *out) {
+  *out = cfl * __longlong_as_double((long long)*scratch);
+}
+
+void launch_dt(const Par &p, const BView &b, int use_face, unsigned long long *scratch, double *dt_out,
+               cudaStream_t s) {
+  const long long n = (long long)b.nx1 * (b.ndim >= 2 ? b.nx2 : 1) * (b.ndim >= 3 ? b.nx3 : 1);
+  const int T = 256;
+  k_dt_init<<<1, 1, 0, s>>>(scratch);
+  k_dt<<<(unsigned)((n + T - 1) / T), T, 0, s>>>(b, use_face, scratch, n);
+  k_dt_final<<<1, 1, 0, s>>>(scratch, p.cfl, dt_out);
+}
+
+// ------------------------------------------------------------- sources
+template <bool MINK>
+__global__ void __launch_bounds__(128) k_sources(Par p, BView b, long long n) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int ni = b.nx1, nj = b.ndim >= 2 ? b.nx2 : 1;
+  const int i = b.ng + (int)(t % ni);
+  const int j = (b.ndim >= 2 ? b.ng : 0) + (int)((t / ni) % nj);
+  const int k = (b.ndim >= 3 ? b.ng : 0) + (int)(t / ((long long)ni * nj));
+  const long long id = b.idx(k, j, i);
+  const long long vs = b.vs;
+  const double *P = b.prim + id;
+  const double rho = P[PHX_PRHO * vs], uu = P[PHX_PENG * vs], Pr = P[PHX_PPRS * vs];
+  const double vp[3] = {P[PHX_PVEL * vs], P[(PHX_PVEL + 1) * vs], P[(PHX_PVEL + 2) * vs]};
+  double bf[3] = {0.0, 0.0, 0.0};
+  if (p.mhd) {
+    bf[0] = P[PHX_PB * vs];
+    bf[1] = P[(PHX_PB + 1) * vs];
+    bf[2] = P[(PHX_PB + 2) * vs];
+  }
+  if constexpr (MINK) {
+    // All metric derivatives vanish: every source is exactly +0 for a finite
+    // stress-energy tensor, NaN otherwise (as in the reference's arithmetic).
+    const double chk = rho + uu + Pr + vp[0] + vp[1] + vp[2] + bf[0] + bf[1] + bf[2];
+    const double z = isfinite(chk) ? 0.0 : __longlong_as_double(0x7ff8000000000000ll);
+    for (int l = 0; l < 4; l++) b.src[l * vs + id] = z;
+  } else {
+    Pt g;
+    load_pt(b, 0, j, i, g);
+    double vsqw = 0.;
+    for (int ii = 0; ii < 3; ii++)
+      for (int jj = 0; jj < 3; jj++) vsqw += g.gcov[ii + 1][jj + 1] * vp[ii] * vp[jj];
+    const double W = sqrt(1. + vsqw);
+    double Bdotv = 0.0, Bsq = 0.0;
+    for (int ii = 0; ii < 3; ii++)
+      for (int jj = 0; jj < 3; jj++) {
+        Bdotv += bf[ii] * (vp[jj] / W) * g.gcov[ii + 1][jj + 1];
+        Bsq += bf[ii] * bf[jj] * g.gcov[ii + 1][jj + 1];
+      }
+    const double iW = ratio(1., W);
+    const double alpha = g.alpha;
+    double u[4], bb[4];
+    u[0] = ratio(W, fabs(alpha));
+    bb[0] = u[0] * Bdotv;
+    for (int l = 1; l < 4; ++l) {
+      u[l] = vp[l - 1] - u[0] * g.beta[l - 1];
+      bb[l] = iW * (bf[l - 1] + alpha * bb[0] * u[l]);
+    }
+    const double bsq = Bsq * iW * iW + Bdotv * Bdotv;
+    double gi[4][4];
+    {
+      double alpha2 = g.alpha;
+      alpha2 *= alpha2;
+      gi[0][0] = -ratio(1, alpha2);
+      for (int mu = 0; mu < 3; mu++) gi[mu + 1][0] = gi[0][mu + 1] = ratio(g.beta[mu], alpha2);
+      for (int mu = 0; mu < 3; mu++)
+        for (int nu = 0; nu < 3; nu++) {
+          gi[mu + 1][nu + 1] = g.gamcon[mu][nu];
+          gi[mu + 1][nu + 1] -= gi[0][mu + 1] * gi[0][nu + 1] * alpha2;
+        }
+    }
+    const double A = rho + uu + Pr + bsq;
+    const double Bt = Pr + 0.5 * bsq;
+    double T[4][4];
+    for (int mu = 0; mu < 4; mu++)
+      for (int nu = 0; nu < 4; nu++) T[mu][nu] = A * u[mu] * u[nu] + Bt * gi[mu][nu] - bb[mu] * bb[nu];
+    const double gdet = g.alpha * g.detgam;
+    const long long pitch = (long long)b.n2t * b.n1t, off = (long long)j * b.n1t + i;
+    double dg[4][4][4];
+    for (int mu = 0; mu < 4; mu++)
+      for (int nu = 0; nu < 4; nu++) {
+        dg[mu][nu][0] = 0.0;
+        for (int s = 1; s < 4; s++) dg[mu][nu][s] = __ldg(b.gderiv + (PHX_GD_DG + 3 * flat2(mu, nu) + s - 1) * pitch + off);
+      }
+    // Gamma[a][b][c] = 0.5 (dg[b][a][c] + dg[c][a][b] - dg[b][c][a]) is formed on the fly
+    auto gam = [&](int a, int bb_, int c) { return 0.5 * (dg[bb_][a][c] + dg[c][a][bb_] - dg[bb_][c][a]); };
+    for (int l = 0; l < 3; l++) {
+      double src_mom = 0.0;
+      for (int m = 0; m < 4; m++)
+        for (int nn = 0; nn < 4; nn++) src_mom += T[m][nn] * (dg[nn][l + 1][m] - gam(l + 1, nn, m));
+      b.src[l * vs + id] = gdet * src_mom;
+    }
+    double TGam = 0.0;
+    const double inv_alpha2 = ratio(1, alpha * alpha);
+    const double gcon0[4] = {-inv_alpha2, inv_alpha2 * g.beta[0], inv_alpha2 * g.beta[1], inv_alpha2 * g.beta[2]};
+    for (int m = 0; m < 4; m++)
+      for (int nn = 0; nn < 4; nn++) {
+        double gam0 = 0;
+        for (int r = 0; r < 4; r++) gam0 += gcon0[r] * gam(r, m, nn);
+        TGam += T[m][nn] * gam0;
+      }
+    double Ta = 0.0;
+    double da[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int d = 1; d < 4; d++) da[d] = __ldg(b.gderiv + (PHX_GD_DALPHA + d - 1) * pitch + off);
+    for (int m = 0; m < 4; m++) Ta += T[m][0] * da[m];
+    b.src[3 * vs + id] = gdet * alpha * (Ta - TGam);
+  }
+}
+
+void launch_sources(const Par &p, const BView &b, cudaStream_t s) {
+  const long long n = (long long)b.nx1 * (b.ndim >= 2 ? b.nx2 : 1) * (b.ndim >= 3 ? b.nx3 : 1);
+  const int T = 128;
+  if (b.fmks)
+    k_sources<false><<<(unsigned)((n + T - 1) / T), T, 0, s>>>(p, b, n);
+  else
+    k_sources<true><<<(unsigned)((n + T - 1) / T), T, 0, s>>>(p, b, n);
+}
+
+// ------------------------------------------------------- FP64 peak probe
+// Independent FMA chains (8 per thread) so the pipe, not latency, limits.
+__global__ void __launch_bounds__(256) k_fp64_probe(double *out, int iters) {
+  double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-3, a2 = a0 + 2e-3, a3 = a0 + 3e-3;
+  double a4 = a0 + 4e-3, a5 = a0 + 5e-3, a6 = a0 + 6e-3, a7 = a0 + 7e-3;
+  const double m = 0.999999999, c = 1e-12;
+  for (int it = 0; it < iters; it++) {
+    a0 = fma(a0, m, c); a1 = fma(a1, m, c); a2 = fma(a2, m, c); a3 = fma(a3, m, c);
+    a4 = fma(a4, m, c); a5 = fma(a5, m, c); a6 = fma(a6, m, c); a7 = fma(a7, m, c);
+  }
+  const double r = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+  if (r == 12345.678) out[0] = r;  // keep the chains alive
+}
+void launch_fp64_probe(double *out, int iters, cudaStream_t s, int *nthreads_out) {
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = nsm * 8;
+  k_fp64_probe<<<blocks, 256, 0, s>>>(out, iters);
+  *nthreads_out = blocks * 256;
+}
+
+}  // namespace phx

@@ -1,0 +1,164 @@
+"""Host API of the GB300 fluid hot path, mirroring the reference's tasks.
+
+The functions keep the names and argument meaning of the phoebus fluid
+package tasks (fluid.hpp:27-69) and forward to the C ABI of phx_fluid.h:
+
+    PrimitiveToConserved(Region)   fluid.cpp:359-449
+    ConservedToPrimitive(Region)   fluid.cpp:451-517 (robust solver)
+    CalculateFluxes                fluid.cpp:659-773
+    FluxCT                         fluid.cpp:775-841
+    CalculateFluidSourceTerms      fluid.cpp:566-657
+    EstimateTimestepBlock          fluid.cpp:899-944
+plus the RK stage glue of PhoebusDriver::RungeKuttaStage.  Errors follow the
+reference: invalid configuration raises (PARTHENON_THROW), an unbracketed
+con2prim root raises on the next check (PARTHENON_FAIL aborts the run).
+All work runs on the GPU; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+from . import abi
+from .block import Block
+
+
+def _stream(stream):
+    if stream is None:
+        import torch
+
+        return torch.cuda.current_stream().cuda_stream
+    return getattr(stream, "cuda_stream", stream)
+
+
+def _rng(r):
+    return abi.Range(int(r[0]), int(r[1]))
+
+
+class FluidContext:
+    """A phx_ctx on one device, plus the calls that use it."""
+
+    def __init__(self, device: int = 0, exact: bool = False):
+        self.lib = abi.load(exact)
+        self.exact = exact
+        h = C.c_void_p()
+        abi.check(self.lib, self.lib.phx_ctx_create(device, C.byref(h)))
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if self.h:
+            self.lib.phx_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ok(self, st):
+        abi.check(self.lib, st)
+
+    # ---- context
+    def check(self):
+        """Synchronise; raise on a sticky device error (e.g. an unbracketed root)."""
+        self._ok(self.lib.phx_ctx_check(self.h))
+
+    def c2p_stats(self, reset: bool = False) -> dict:
+        s = abi.C2PStats()
+        self._ok(self.lib.phx_ctx_c2p_stats(self.h, C.byref(s), int(reset)))
+        return {"zones": s.zones, "iterations": s.iterations, "residual_evals": s.residual_evals,
+                "failures": s.failures, "unbracketed": s.unbracketed, "learned_accepted": s.learned_accepted,
+                "hist": list(s.hist)}
+
+    # ---- tasks
+    def PrimitiveToConserved(self, p: abi.Params, b: Block, ib=None, jb=None, kb=None, stream=None):
+        e = b.entire()
+        ib, jb, kb = ib or e[0], jb or e[1], kb or e[2]
+        s = b.struct()
+        self._ok(self.lib.phx_prim_to_con(self.h, C.byref(p), C.byref(s), _rng(ib), _rng(jb), _rng(kb),
+                                          _stream(stream)))
+
+    def ConservedToPrimitive(self, p: abi.Params, b: Block, ib=None, jb=None, kb=None, learned=False,
+                             stream=None):
+        e = b.entire()
+        ib, jb, kb = ib or e[0], jb or e[1], kb or e[2]
+        s = b.struct()
+        fn = self.lib.phx_con_to_prim_learned if learned else self.lib.phx_con_to_prim
+        self._ok(fn(self.h, C.byref(p), C.byref(s), _rng(ib), _rng(jb), _rng(kb), _stream(stream)))
+
+    def CalculateFluxes(self, p: abi.Params, b: Block, stream=None):
+        s = b.struct()
+        self._ok(self.lib.phx_calculate_fluxes(self.h, C.byref(p), C.byref(s), _stream(stream)))
+
+    def FluxCT(self, p: abi.Params, b: Block, stream=None):
+        s = b.struct()
+        self._ok(self.lib.phx_flux_ct(self.h, C.byref(p), C.byref(s), _stream(stream)))
+
+    def CalculateFluidSourceTerms(self, p: abi.Params, blocks, stream=None):
+        blocks = blocks if isinstance(blocks, (list, tuple)) else [blocks]
+        arr = (abi.BlockS * len(blocks))(*[b.struct() for b in blocks])
+        self._ok(self.lib.phx_calculate_fluid_source_terms(self.h, C.byref(p), arr, len(blocks), _stream(stream)))
+
+    def UpdateStage(self, b: Block, cons_base, cons_out, beta: float, dt: float, stream=None):
+        from .block import _ptr
+
+        s = b.struct()
+        self._ok(self.lib.phx_update_stage(self.h, C.byref(s), _ptr(cons_base), _ptr(cons_out), beta, dt,
+                                           _stream(stream)))
+
+    def FillGhostsPeriodic(self, b: Block, field, nvar: int, stream=None):
+        from .block import _ptr
+
+        s = b.struct()
+        self._ok(self.lib.phx_fill_ghosts_periodic(self.h, C.byref(s), _ptr(field), nvar, _stream(stream)))
+
+    def EstimateTimestepBlock(self, p: abi.Params, b: Block, use_face_speeds: bool, out=None, stream=None):
+        """Returns cfl * min dt (a 1-element device tensor; no host sync)."""
+        import torch
+
+        if out is None:
+            out = torch.zeros(1, dtype=torch.float64, device=f"cuda:{self.device}")
+        s = b.struct()
+        self._ok(self.lib.phx_estimate_timestep(self.h, C.byref(p), C.byref(s), int(use_face_speeds),
+                                                out.data_ptr(), _stream(stream)))
+        return out
+
+    def GeometryFillFMKS(self, b: Block, stream=None):
+        assert b.geom is not None
+        g = b.geom.struct()
+        s = b.struct()
+        self._ok(self.lib.phx_geometry_fill_fmks(self.h, C.byref(g), C.byref(s), _stream(stream)))
+
+    def Stage(self, p: abi.Params, b: Block, cons_base, cons_out, beta: float, dt: float, learned=False,
+              stream=None):
+        from .block import _ptr
+
+        s = b.struct()
+        self._ok(self.lib.phx_stage(self.h, C.byref(p), C.byref(s), _ptr(cons_base), _ptr(cons_out), beta, dt,
+                                    int(learned), _stream(stream)))
+
+    def probe_fp64_peak(self) -> float:
+        v = C.c_double()
+        self._ok(self.lib.phx_probe_fp64_peak(self.h, C.byref(v)))
+        return v.value
+
+    # ---- composite helpers
+    def Initialize(self, p: abi.Params, b: Block, stream=None):
+        """Mesh initialisation after a problem generator wrote the prims:
+        PrimitiveToConserved (entire), periodic ghost exchange of the
+        conserved variables, FillDerived (con2prim, entire)."""
+        self.PrimitiveToConserved(p, b, stream=stream)
+        self.FillGhostsPeriodic(b, b["cons"], abi.NCONS if p.mhd else 5, stream=stream)
+        self.ConservedToPrimitive(p, b, stream=stream)
+
+
+def rk2_step(ctx: FluidContext, p: abi.Params, b: Block, cons_stage, dt: float, learned=False, stream=None):
+    """One Heun RK2 step (rk2 LowStorageIntegrator: beta = 1, 1/2).  b['cons']
+    holds U^n on entry and U^{n+1} on exit; cons_stage is the second buffer."""
+    base = b["cons"]
+    ctx.Stage(p, b, base, cons_stage, 1.0, dt, learned, stream)
+    b2 = Block(b.nx, b.ng, b.ndim, b.xmin, b.dx, backend=b.backend, device=b.device, arrays=dict(b.arrays),
+               geom=b.geom)
+    b2.arrays["cons"] = cons_stage
+    ctx.Stage(p, b2, base, base, 0.5, dt, learned, stream)

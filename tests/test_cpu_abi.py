@@ -1,0 +1,76 @@
+"""CPU-side checks of the C ABI: the libraries build, load, and export every
+entry point include/phx_fluid.h declares; the ctypes mirror matches the
+header.  No compute calls (no GPU here)."""
+import re
+import subprocess
+from pathlib import Path
+
+import pytest
+
+from phoebus_gb300 import abi
+
+ROOT = Path(__file__).resolve().parent.parent
+HEADER = ROOT / "include" / "phx_fluid.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(phx_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_and_ctypes_agree():
+    assert declared_functions() == abi.exported_symbols()
+
+
+@pytest.mark.parametrize("exact", [False, True])
+def test_library_exports_every_symbol(built, exact):
+    path = abi.lib_path(exact)
+    assert path.exists()
+    out = subprocess.run(["nm", "-D", "--defined-only", str(path)], capture_output=True, text=True, check=True).stdout
+    syms = {line.split()[-1] for line in out.splitlines() if line.strip()}
+    missing = [f for f in declared_functions() if f not in syms]
+    assert not missing, f"not exported: {missing}"
+
+
+def test_library_loads_without_gpu(built):
+    # dlopen + symbol binding works without a device; only pure host calls.
+    lib = abi.load(False)
+    assert lib.phx_abi_version() == 1
+    assert lib.phx_build_exact() == 0
+    assert abi.load(True).phx_build_exact() == 1
+    p = abi.Params()
+    lib.phx_params_default(p)
+    ref = abi.default_params()
+    for name, _ in abi.Params._fields_:
+        assert getattr(p, name) == getattr(ref, name), name
+    g = abi.Geometry()
+    lib.phx_geometry_default(g, abi.GEOM_FMKS)
+    gr = abi.default_geometry(abi.GEOM_FMKS)
+    for name in ("hslope", "poly_xt", "poly_alpha", "smooth", "hexp_br", "derefine_poles"):
+        assert getattr(g, name) == getattr(gr, name), name
+    assert lib.phx_status_string(2) == b"con2prim root not bracketed"
+
+
+def test_struct_sizes_match_header(built, tmp_path):
+    """Compile a tiny C program against the header and compare sizeof/offsets
+    with the ctypes mirror."""
+    import ctypes as C
+
+    src = tmp_path / "sz.c"
+    fields = {"phx_params": abi.Params, "phx_block": abi.BlockS, "phx_geometry": abi.Geometry,
+              "phx_c2p_stats": abi.C2PStats}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void){"]
+    for cname, cls in fields.items():
+        lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
+        for fname, _ in cls._fields_:
+            lines.append(f'printf("{cname}.{fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines.append("return 0;}")
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "sz"
+    subprocess.run(["gcc", "-o", str(exe), str(src)], check=True)
+    out = dict(l.rsplit(" ", 1) for l in subprocess.run([str(exe)], capture_output=True, text=True).stdout.splitlines())
+    for cname, cls in fields.items():
+        assert int(out[cname]) == C.sizeof(cls), cname
+        for fname, _ in cls._fields_:
+            assert int(out[f"{cname}.{fname}"]) == getattr(cls, fname).offset, f"{cname}.{fname}"
