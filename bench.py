@@ -1,0 +1,371 @@
+"""Benchmark of the GRMHD fluid hot path on one GB300 (per rank).
+
+Workload: the 256^3 single-meshblock shear layer (Minkowski, ideal gas
+Gamma = 5/3, WENO5-Z + HLL, MHD, periodic), seeded synthetic state.  One
+bench step = one full Heun RK2 timestep of the reference's stage sequence
+(two stages: sources, fluxes, FluxCT, divergence + update, con2prim over the
+whole block, ghost exchange, con2prim again; then the face-speed timestep
+estimate).  The metric is zone-updates/s: interior zones advanced one full
+RK2 timestep per second.
+
+  value      device-resident state, CUDA events around K steps
+  e2e        the same steps through the C ABI with the state in pinned host
+             memory: every step copies prims + cons to the device, runs, and
+             copies prims + cons back, all inside the timed region
+  roofline   CalculateFluxes (the dominant kernels): algorithmic bytes per
+             launch / measured launch time vs the measured HBM copy peak; an
+             FP64 section relates the same launches to the measured FP64 peak
+  cpu_baseline  the oracle (CPU restatement of the reference path) timed on
+             a 64^3 sample of the same state with all host threads
+
+--impl reference runs the reference's CPU path (the oracle port) on the host
+cores: each step is one RK2 timestep of a 64^3 sample of the same state.
+Multi-GPU: independent replicas (one block per rank, weak scaling); the only
+cross-rank operations are the timing barriers.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "GRMHD zone-updates/s on 1 GB300; con2prim zones/s learned-guess vs plain @1e-10"
+UNIT = "zone-updates/s"
+LAUNCHES_PER_STAGE = 10  # sources 1, fluxes 3, FluxCT 2, update 1, con2prim 2, ghosts 1
+LAUNCHES_DT = 3
+
+
+def parse():
+    a = argparse.ArgumentParser()
+    a.add_argument("--gpus", type=int, default=1)
+    a.add_argument("--steps", type=int, default=5)
+    a.add_argument("--warmup", type=int, default=3)
+    a.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    a.add_argument("--n", type=int, default=256)
+    a.add_argument("--cpu-n", type=int, default=64)
+    a.add_argument("--exact", action="store_true", help="time the parity (no-FMA) build")
+    a.add_argument("--no-e2e", action="store_true")
+    a.add_argument("--no-cpu", action="store_true")
+    return a.parse_args()
+
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        if args.impl == "ours":
+            import torch
+
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(ws, v, device=None):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        import statistics
+
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measured_peaks():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def flux_bytes(n, ng=4):
+    """Algorithmic HBM bytes of one CalculateFluxes call (three launches) on
+    an n^3 block: each direction reads the 10 reconstructed primitives of
+    every cell its stencils touch and writes 8 fluxes + 1 signal speed per
+    face it computes."""
+    n1t = n + 2 * ng
+    t = n + 2  # transverse face range [s-1, e+1]
+    cells = n1t * t * t  # stencil cells per direction (full pencil, +-1 layer)
+    faces = (n + 1) * t * t
+    return 3 * (10 * cells + 9 * faces) * 8
+
+
+def cpu_baseline(args, threads):
+    """Oracle RK2 timestep on a cpu_n^3 sample of the workload."""
+    import numpy as np
+
+    from oracle.oracle import Oracle
+    from phoebus_gb300 import abi, states
+
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    o = Oracle()
+    hb, par = states.kelvin_helmholtz(n=args.cpu_n)
+    p = abi.default_params(**par)
+    o.Initialize(p, hb)
+    dt = 0.5 * o.EstimateTimestepBlock(p, hb, False)
+    cs = np.zeros_like(hb["cons"])
+    o.rk2_step(p, hb, cs, dt)  # warm-up
+    times = []
+    for _ in range(max(1, min(args.steps, 3))):
+        t0 = time.perf_counter()
+        o.rk2_step(p, hb, cs, dt)
+        o.EstimateTimestepBlock(p, hb, True)
+        times.append(time.perf_counter() - t0)
+    t = min(times)
+    return args.cpu_n ** 3 / t, t
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    import numpy as np
+
+    from oracle.oracle import Oracle
+    from phoebus_gb300 import abi, states
+
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    o = Oracle()
+    hb, par = states.kelvin_helmholtz(n=args.cpu_n)
+    p = abi.default_params(**par)
+    o.Initialize(p, hb)
+    dt = 0.5 * o.EstimateTimestepBlock(p, hb, False)
+    cs = np.zeros_like(hb["cons"])
+    for _ in range(args.warmup):
+        o.rk2_step(p, hb, cs, dt)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.rk2_step(p, hb, cs, dt)
+        o.EstimateTimestepBlock(p, hb, True)
+    el = time.perf_counter() - t0
+    v = args.cpu_n ** 3 * args.steps / el
+    sample = f"{args.cpu_n}^3 sample of the {args.n}^3 shear layer, one RK2 step per bench step"
+    out = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": f"shear layer {args.n}^3 WENO5-Z+HLL MHD RK2 (reference CPU path on a "
+                                  f"{args.cpu_n}^3 sample)", "n": args.n, "sample_n": args.cpu_n},
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+    import numpy as np
+    import torch
+
+    from phoebus_gb300 import abi, states
+    from phoebus_gb300.fluid import FluidContext
+
+    dev = f"cuda:{local}"
+    torch.cuda.set_device(local)
+    n = args.n
+    hb, par = states.kelvin_helmholtz(n=n)
+    p = abi.default_params(**par)
+    db = hb.to_device(dev)
+    ctx = FluidContext(local, exact=args.exact)
+    stream = torch.cuda.current_stream()
+    ctx.Initialize(p, db)
+    dt = 0.5 * ctx.EstimateTimestepBlock(p, db, False).item()
+    base = db["cons"]
+    second = torch.zeros_like(base)
+    dt_out = torch.zeros(1, dtype=torch.float64, device=dev)
+
+    def step(block):
+        b0 = block["cons"]
+        ctx.Stage(p, block, b0, second, 1.0, dt)
+        block.arrays["cons"] = second
+        ctx.Stage(p, block, b0, b0, 0.5, dt)
+        block.arrays["cons"] = b0
+        ctx.EstimateTimestepBlock(p, block, True, out=dt_out)
+
+    for _ in range(args.warmup):
+        step(db)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    barrier(ws)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step(db)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(ws)
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    ms = max_over_ranks(ws, ms, dev)
+    zones = n ** 3
+    value = ws * zones / (ms * 1e-3)
+
+    # dominant kernels: CalculateFluxes (three launches), timed live
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 3
+    torch.cuda.synchronize()
+    f0.record(stream)
+    for _ in range(reps):
+        ctx.CalculateFluxes(p, db)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    flux_ms = f0.elapsed_time(f1) / reps
+    hbm_peak, peak_src = measured_peaks()
+    fb = flux_bytes(n)
+    achieved = fb / (flux_ms * 1e-3) / 1e9
+    fp64_peak = ctx.probe_fp64_peak()
+    prof = ROOT / "profiles" / "flux_fp64_per_zone.json"
+    fp64 = None
+    if prof.exists():
+        d = json.loads(prof.read_text())
+        flops = d["fp64_flops_per_call_per_zone"] * zones
+        fp64 = {"achieved_tflops": flops / (flux_ms * 1e-3) / 1e12, "peak_tflops": fp64_peak / 1e12,
+                "frac": flops / (flux_ms * 1e-3) / fp64_peak, "flops_source": d["source"],
+                "peak_source": "measured in-process (phx_probe_fp64_peak)"}
+    traffic = None
+    tf = ROOT / "profiles" / "flux_dram_traffic.json"
+    if tf.exists():
+        traffic = json.loads(tf.read_text()).get("bytes_per_call_scaled")
+
+    # end to end through the C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        h_prim = torch.empty(db["prim"].shape, dtype=torch.float64, pin_memory=True)
+        h_cons = torch.empty(db["cons"].shape, dtype=torch.float64, pin_memory=True)
+        h_prim.copy_(db["prim"])
+        h_cons.copy_(db["cons"])
+        o_prim = torch.empty_like(h_prim).pin_memory()
+        o_cons = torch.empty_like(h_cons).pin_memory()
+        torch.cuda.synchronize()
+        barrier(ws)
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        g0.record(stream)
+        for _ in range(args.steps):
+            db["prim"].copy_(h_prim, non_blocking=True)
+            db["cons"].copy_(h_cons, non_blocking=True)
+            step(db)
+            o_prim.copy_(db["prim"], non_blocking=True)
+            o_cons.copy_(db["cons"], non_blocking=True)
+        g1.record(stream)
+        torch.cuda.synchronize()
+        barrier(ws)
+        ems = max_over_ranks(ws, g0.elapsed_time(g1) / args.steps, dev)
+        nb = (h_prim.numel() + h_cons.numel()) * 8
+        e2e = {"value": ws * zones / (ems * 1e-3), "unit": UNIT, "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb,
+               "ms_per_step": ems}
+    ctx.check()
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        v, t = cpu_baseline(args, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"oracle RK2 step on a {args.cpu_n}^3 sample of the same state ({t:.2f} s/step)"}
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": f"shear layer {n}^3 single block, Minkowski, Gamma 5/3, WENO5-Z + HLL, MHD, "
+                                   "periodic; one RK2 timestep (2 stages + timestep estimate) per step",
+                       "n": n, "ng": 4, "rk_stages_per_step": 2, "zone_stages_per_s": 2 * value,
+                       "l2": "inputs larger than L2 (state ~%.1f GB)" % (db.N * 60 * 8 / 1e9),
+                       "parallelism": f"replicas x{ws}", "build": "exact" if args.exact else "production"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "traffic": traffic, "kernel": "CalculateFluxes (x1/x2/x3)",
+                         "peak_source": peak_src, "algorithmic_bytes": fb, "launch_ms": flux_ms,
+                         "note": "FP64-pipe bound on GB300; see fp64"},
+            "fp64": fp64,
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "e2e": e2e,
+            "gpu_launches": args.steps * (2 * LAUNCHES_PER_STAGE + LAUNCHES_DT),
+        }
+        print(json.dumps(out), flush=True)
+    ctx.close()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()
