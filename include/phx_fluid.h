@@ -271,6 +271,26 @@ phx_status phx_estimate_timestep(phx_ctx *ctx, const phx_params *p, const phx_bl
                                  int use_face_speeds, double *dt_out_device,
                                  void *stream);
 
+/* Allocation-free variant of phx_estimate_timestep.  It has no counterpart in
+ * the reference.  It is for callers that cannot allocate device memory (and so
+ * cannot create a phx_ctx, which calls cudaMalloc): hosts whose device memory
+ * all comes from their own pool and that forbid libraries from allocating, or
+ * loops that must not risk the device synchronisation an allocation can cause
+ * mid-step.  Same inputs, output and result as phx_estimate_timestep; it uses
+ * the current device and calls no cudaMalloc, cudaFree or allocating routine.
+ * Its scratch is a file-scope __device__ array of PHX_DT_STATIC_MAX_PARTIALS
+ * doubles (512 KiB) that every device loading the library keeps until exit,
+ * so blocks with more than PHX_DT_STATIC_MAX_ZONES interior zones are
+ * rejected with PHX_ERR_CAPACITY.  The first call on each device looks up the
+ * array's device address (cudaGetSymbolAddress); make that first call before
+ * any stream capture.  All calls share the array: calls that overlap on the
+ * GPU (different streams, concurrent host threads) race on it. */
+#define PHX_DT_STATIC_MAX_PARTIALS 65536
+#define PHX_DT_STATIC_MAX_ZONES (65536LL * 256LL)
+phx_status phx_estimate_timestep_static(const phx_params *p, const phx_block *b,
+                                        int use_face_speeds, double *dt_out_device,
+                                        void *stream);
+
 /* fixup::ConservedToPrimitiveFixup (fixup_c2p.cpp:44-356), interior zones. */
 phx_status phx_c2p_fixup(phx_ctx *ctx, const phx_params *p, const phx_block *b,
                          void *stream);

@@ -108,6 +108,7 @@ _SIGS = {
     "phx_update_stage": (C.c_int, [_P, C.POINTER(BlockS), _P, _P, C.c_double, C.c_double, _P]),
     "phx_fill_ghosts_periodic": (C.c_int, [_P, C.POINTER(BlockS), _P, C.c_int, _P]),
     "phx_estimate_timestep": (C.c_int, [_P, C.POINTER(Params), C.POINTER(BlockS), C.c_int, _P, _P]),
+    "phx_estimate_timestep_static": (C.c_int, [C.POINTER(Params), C.POINTER(BlockS), C.c_int, _P, _P]),
     "phx_c2p_fixup": (C.c_int, [_P, C.POINTER(Params), C.POINTER(BlockS), _P]),
     "phx_apply_floors": (C.c_int, [_P, C.POINTER(Params), C.POINTER(BlockS), Range, Range, Range, _P]),
     "phx_geometry_fill_fmks": (C.c_int, [_P, C.POINTER(Geometry), C.POINTER(BlockS), _P]),
