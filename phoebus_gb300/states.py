@@ -12,6 +12,8 @@ gas, computed as the EOS does.
 """
 from __future__ import annotations
 
+import math
+
 import numpy as np
 
 from . import abi
@@ -173,3 +175,142 @@ def uneven_block_sizes(nblocks: int = 1024, seed: int = SEED + 3, sizes=(16, 32,
     u = uniform(seed, 99, nblocks)
     edges = np.cumsum(probs)
     return [int(sizes[int(np.searchsorted(edges, x, side="right"))]) for x in u]
+
+
+def linear_modes_2d(n: int = 64, ng: int = 4, amp: float = 1.0e-5, gam: float = 1.333333333333333333):
+    """Problem generator linear_modes (pgen/linear_modes.cpp:21-307) for the
+    2D hydro sound mode on [0, 1]^2 (the regression deck inputs/linear_modes.pin
+    with nx = 64, fluid/mhd = true, hydro_modes/physics = hydro): primitives set
+    on the entire block from the analytic mode at each cell's own coordinates
+    (ghosts included, as the reference does).  Returns (block, params, tlim)
+    with tlim = one wave period, which the generator writes over parthenon/time/tlim."""
+    kk = 2.0 * np.pi
+    omega_im = 3.8780661653218766
+    drho, dug, du1, du2 = 0.5804294924639213, 0.7739059899518947, 0.1791244302079596, 0.1791244302079596
+    dx = 1.0 / n
+    b = Block((n, n, 1), ng, 2, (0.0, 0.0, -1.0), (dx, dx, 2.0)).alloc()
+    x0 = 0.0 - ng * dx
+    xs = x0 + (np.arange(b.n1t) + 0.5) * dx
+    ys = x0 + (np.arange(b.n2t) + 0.5) * dx
+    Y, X = np.meshgrid(ys, xs, indexing="ij")
+    # the C library's cos (as the reference's std::cos), not numpy's vectorised one
+    arg = kk * X + kk * Y
+    mode = amp * np.array([math.cos(a) for a in arg.ravel()]).reshape(arg.shape)
+    rho = 1.0 + drho * mode
+    ug = 1.0 + dug * mode
+    gm1 = gam - 1.0
+    Pg = (gam - 1.0) * ug
+    T = np.maximum(0.0, (ug / rho) / 1.0)
+    bmod = np.maximum(0.0, (gm1 + 1) * gm1 * rho * 1.0 * T)
+    pr = b.arrays["prim"]
+    pr[abi.PRHO, 0] = rho
+    pr[abi.PENG, 0] = ug
+    pr[abi.PPRS, 0] = Pg
+    pr[abi.PTMP, 0] = T
+    pr[abi.PGM1, 0] = bmod / Pg
+    pr[abi.PVEL, 0] = 0.0 + du1 * mode
+    pr[abi.PVEL + 1, 0] = 0.0 + du2 * mode
+    pr[abi.PVEL + 2, 0] = 0.0
+    pr[abi.PB:abi.PB + 3, 0] = 0.0
+    par = dict(Gamma=gam, recon="linear", riemann="hll", cfl=0.4, c2p_tol=1.0e-12, c2p_max_iter=100, mhd=1)
+    tlim = 2.0 * np.pi / omega_im
+    return b, par, tlim
+
+
+class TimeControl:
+    """PhoebusDriver::Step (phoebus_driver.cpp:121-143) and Parthenon's
+    EvolutionDriver timestep control: dt_0 from the cell-speed estimate after
+    initialisation; the first step uses dt_init_fact * dt; afterwards the new
+    estimate (growth_cap = True also limits growth to 2x per step, a variant of
+    the driver the reference's linear-modes gold does not match); every step
+    is clipped to end at tlim."""
+
+    def __init__(self, tlim: float, dt0: float, dt_init_fact: float = 1.0, growth_cap: bool = False):
+        self.tlim, self.time, self.ncycle = tlim, 0.0, 0
+        self.dt_init_fact = dt_init_fact
+        self.growth_cap = growth_cap
+        big = np.finfo(np.float64).max
+        self.dt = min(big, dt0)
+        if self.time < self.tlim and (self.tlim - self.time) < self.dt:
+            self.dt = self.tlim - self.time
+
+    def keep_going(self):
+        return self.time < self.tlim
+
+    def begin_step(self) -> float:
+        dt = min(self.dt, 1.0e300)
+        dt *= self.dt_init_fact
+        self.dt_init_fact = 1.0
+        if self.time + dt > self.tlim:
+            dt = self.tlim - self.time
+        self.dt = dt
+        return dt
+
+    def end_step(self, new_dt: float):
+        self.ncycle += 1
+        self.time += self.dt
+        if self.growth_cap and self.dt < 0.1 * np.finfo(np.float64).max:
+            self.dt *= 2.0
+            self.dt = min(self.dt, new_dt)
+        else:
+            self.dt = new_dt
+        if self.time < self.tlim and (self.tlim - self.time) < self.dt:
+            self.dt = self.tlim - self.time
+
+
+def p2c2p_fmks(n: int = 512, ng: int = 4):
+    """Problem generator p2c2p (pgen/p2c2p.cpp:21-136) on its deck
+    inputs/p2c2p.pin: a 1D FMKS block, X1 in [1, 2] (r in [e, e^2]), one X2
+    zone on [-1, 1], a = 0.9375, derefine_poles = false, Gamma = 5/3, MHD.
+    Primitives are smooth functions of X1 set on the entire block.  Returns
+    (block with FMKS parameters, params, analytic functions)."""
+    from .block import GeomTables
+
+    dx = 1.0 / n
+    b = Block((n, 1, 1), ng, 1, (1.0, -1.0, -1.0), (dx, 2.0, 2.0)).alloc()
+    g = abi.default_geometry(abi.GEOM_FMKS, a=0.9375, derefine_poles=0, x0=min(1.0, max(0.0, 1.0 - ng * dx)))
+    b.geom = GeomTables(g, b.n1t, b.n2t).alloc()
+    x = (1.0 - ng * dx) + (np.arange(b.n1t) + 0.5) * dx
+    f = {
+        "rho": lambda x: 1.0 + 0.3 * np.sin(x), "u": lambda x: 1.0 + 0.3 * np.cos(x),
+        "v1": lambda x: 0.5 + 0.2 * np.sin(x - 0.3), "v2": lambda x: 0.3 + 0.2 * np.cos(x - 0.2),
+        "v3": lambda x: 0.4 + 0.3 * np.sin(x + 0.1), "b1": lambda x: 0.3 + 0.1 * np.sin(x),
+        "b2": lambda x: 0.4 + 0.2 * np.cos(x), "b3": lambda x: 0.5 + 0.3 * np.sin(x - 0.1),
+    }
+    gm1 = 5.0 / 3.0 - 1.0
+    pr = b.arrays["prim"]
+    rho, u = f["rho"](x), f["u"](x)
+    pr[abi.PRHO, 0, 0] = rho
+    pr[abi.PENG, 0, 0] = u
+    for d, k in enumerate(("v1", "v2", "v3")):
+        pr[abi.PVEL + d, 0, 0] = f[k](x)
+    for d, k in enumerate(("b1", "b2", "b3")):
+        pr[abi.PB + d, 0, 0] = f[k](x)
+    sie = u / rho
+    P = np.maximum(0.0, gm1 * rho * sie)
+    T = np.maximum(0.0, sie / 1.0)
+    pr[abi.PPRS, 0, 0] = P
+    pr[abi.PTMP, 0, 0] = T
+    pr[abi.PGM1, 0, 0] = np.maximum(0.0, (gm1 + 1) * gm1 * rho * 1.0 * T) / P
+    par = dict(Gamma=5.0 / 3.0, recon="weno5z", riemann="hll", cfl=0.8, c2p_tol=1.0e-14, c2p_max_iter=100, mhd=1)
+    return b, par, f, x
+
+
+def fmks_random_block(nx=(12, 10, 4), seed: int = SEED + 5, ng: int = 4, r=(2.0, 20.0), x2=(0.1, 0.9),
+                      a: float = 0.9375, derefine_poles: int = 1, Gamma: float = 4.0 / 3.0):
+    """A block of FMKS coordinates (X1 = ln r, X2 in (0, 1), X3 = phi) holding
+    per-zone random primitives, with FMKS table storage attached."""
+    from .block import GeomTables
+
+    n1, n2, n3 = nx
+    x1min, x1max = np.log(r[0]), np.log(r[1])
+    dx = ((x1max - x1min) / n1, (x2[1] - x2[0]) / n2, 2.0 * np.pi / n3)
+    b = Block(nx, ng, 3, (x1min, x2[0], 0.0), dx).alloc()
+    g = abi.default_geometry(abi.GEOM_FMKS, a=a, derefine_poles=derefine_poles, x0=x1min - ng * dx[0])
+    b.geom = GeomTables(g, b.n1t, b.n2t).alloc()
+    N = n1 * n2 * n3
+    rho, wv, P, B = random_zones_prims(N, seed, W=(1.0, 3.0), sigma=(1e-3, 1.0))
+    shp = (n3, n2, n1)
+    _set_interior(b, rho.reshape(shp), [w.reshape(shp) for w in wv], P.reshape(shp), [x.reshape(shp) for x in B],
+                  Gamma - 1.0)
+    return b
