@@ -17,6 +17,10 @@ pytestmark = pytest.mark.gpu
 
 @pytest.mark.parametrize("derefine", [0, 1])
 def test_fmks_tables(oracle, ctx_exact, derefine):
+    """GPU tables vs the oracle's: libm differences of an ulp, amplified where
+    theta = thG + e (thJ - thG) cancels near the pole (derefined poles, ghost
+    zones at X2 < 0), stay below 1e-10 of each variable's scale; the
+    finite-difference derivatives (step eps^(1/3) max(|X|, 1)) below 1e-9."""
     hb = states.fmks_random_block(derefine_poles=derefine)
     db = hb.to_device()
     oracle.GeometryFillFMKS(hb)
@@ -24,13 +28,10 @@ def test_fmks_tables(oracle, ctx_exact, derefine):
     for name in ("cent", "face1", "face2"):
         g, r = db.geom.arrays[name].cpu().numpy(), hb.geom.arrays[name]
         for v in range(abi.GEOM_NLOC):
-            assert_close(g[v], r[v], 1e-13, f"{name}[{v}]")
+            assert_close(g[v], r[v], 1e-10, f"{name}[{v}]")
     g, r = db.geom.arrays["deriv"].cpu().numpy(), hb.geom.arrays["deriv"]
-    # central differences with step eps^(1/3) max(|X|, 1): rounding of g at
-    # 1e-16 becomes ~1e-11 of the metric scale in the derivative
-    scale = np.max(np.abs(hb.geom.arrays["cent"][abi.G_GCOV:abi.G_GCOV + 10]))
     for v in range(abi.GEOM_NDER):
-        assert_close(g[v], r[v], 1e-9, f"deriv[{v}]", floor=scale)
+        assert_close(g[v], r[v], 1e-9, f"deriv[{v}]")
 
 
 def _shared_tables(oracle, hb):
@@ -72,8 +73,13 @@ def test_fmks_sources_fast(oracle, ctx_fast):
     oracle.CalculateFluidSourceTerms(p, hb)
     ctx_fast.CalculateFluidSourceTerms(p, db)
     ks, js, is_ = hb.isl()
-    for v in range(4):
-        assert_close(db["src"][v, ks, js, is_], hb["src"][v, ks, js, is_], 1e-12, f"src {v}")
+    got, ref = db["src"][:, ks, js, is_].cpu().numpy(), hb["src"][:, ks, js, is_]
+    for v in (0, 1, 3):
+        assert_close(got[v], ref[v], 1e-12, f"src {v}")
+    # S_phi is zero analytically in axisymmetric Kerr (T symmetric, d_phi g = 0):
+    # both builds give rounding residuals, compared on the zone's source scale
+    scale = np.abs(ref[0]) + np.abs(ref[1]) + np.abs(ref[3])
+    assert np.all(np.abs(got[2] - ref[2]) <= 1e-12 * scale)
 
 
 def test_p2c2p_known_answer_gpu(oracle, ctx_exact):
