@@ -4,6 +4,9 @@
 // The regula-falsi loop is warp-synchronous: every lane stays in the loop
 // until the warp's vote (__any_sync) says no lane is still iterating, so all
 // 32 lanes re-enter each iteration together and reconverge after it.
+// In the production build the residual's divisions use the Newton-refined
+// hardware reciprocal (rcp_p / ratio_p); the exact build divides as the
+// reference does.
 #pragma once
 #include "phx_device.cuh"
 
@@ -24,7 +27,7 @@ struct Residual {
     rho_floor *= p.fsf;
     used_density_floor = used_energy_floor = used_energy_max = used_gamma_max = false;
   }
-  __device__ __forceinline__ double x_mu(double mu) const { return ratio(1.0, 1.0 + mu * bsq); }
+  __device__ __forceinline__ double x_mu(double mu) const { return ratio_p(1.0, 1.0 + mu * bsq); }
   __device__ __forceinline__ double rbarsq_mu(double mu, double x) const {
     return x * (x * rsq + mu * (1.0 + x) * rbsq);
   }
@@ -53,11 +56,11 @@ struct Residual {
   }
   __device__ __forceinline__ double ehat_mu(const Par &p, double mu, double qbar, double rbarsq,
                                             double vhatsq, double What) {
-    double rho = rhohat_mu(ratio(1.0, What));
+    double rho = rhohat_mu(ratio_p(1.0, What));
     double e_floor;
     get_floors(p, x1, x2, x3, rho, e_floor);
     e_floor *= p.fsf;
-    const double ehat_trial = What * (qbar - mu * rbarsq) + vhatsq * What * ratio(What, 1.0 + What);
+    const double ehat_trial = What * (qbar - mu * rbarsq) + vhatsq * What * ratio_p(What, 1.0 + What);
     used_energy_floor = false;
     used_energy_max = false;
     if (ehat_trial <= e_floor) {
@@ -75,16 +78,16 @@ struct Residual {
     const double qbar = qbar_mu(mu, x);
     const double vhatsq = vhatsq_mu(mu, rbarsq);
     const double iWhat = iWhat_mu(vhatsq);
-    const double What = ratio(1.0, iWhat);
+    const double What = ratio_p(1.0, iWhat);
     const double rhohat = rhohat_mu(iWhat);
     const double ehat = ehat_mu(p, mu, qbar, rbarsq, vhatsq, What);
     const double Phat = eos_P_rho_sie(p, rhohat, ehat);
     const double hhat = rhohat * (1.0 + ehat) + Phat;
-    const double ahat = Phat / make_positive(hhat - Phat);
+    const double ahat = div_p(Phat, make_positive(hhat - Phat));
     const double nua = (1.0 + ahat) * (1.0 + ehat) * iWhat;
     const double nub = (1.0 + ahat) * (1.0 + qbar - mu * rbarsq);
     const double nuhat = fmax(nua, nub);
-    const double muhat = 1.0 / (nuhat + mu * rbarsq);
+    const double muhat = rcp_p(nuhat + mu * rbarsq);
     return mu - muhat;
   }
   __device__ __forceinline__ bool used_bounds() const {

@@ -31,6 +31,47 @@ __device__ __forceinline__ double ratio(double a, double b) {
   return a / (b + sgn * kSMALL);
 }
 
+// 1/x from the hardware reciprocal seed and two Newton steps (accurate to an
+// ulp or two for normal x; callers guarantee a normal, finite argument).
+__device__ __forceinline__ double rcp_nr(double x) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  double e = fma(-x, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-x, r, 1.0);
+  return fma(r, e, r);
+}
+// biased exponent of a double, on the integer pipe
+__device__ __forceinline__ int dexp(double x) { return (__double2hiint(x) >> 20) & 0x7ff; }
+
+// 1/x for the production build (IEEE division in the exact build); falls back
+// to the division when x is outside the normal range the Newton form handles.
+__device__ __forceinline__ double rcp_p(double x) {
+#ifdef PHX_EXACT
+  return 1.0 / x;
+#else
+  const int e = dexp(x);
+  return (e >= 16 && e <= 2030) ? rcp_nr(x) : 1.0 / x;
+#endif
+}
+// a / b: IEEE division in the exact build, a * rcp_p(b) in the production build
+__device__ __forceinline__ double div_p(double a, double b) {
+#ifdef PHX_EXACT
+  return a / b;
+#else
+  return a * rcp_p(b);
+#endif
+}
+// robust::ratio with the production-build reciprocal
+__device__ __forceinline__ double ratio_p(double a, double b) {
+#ifdef PHX_EXACT
+  return ratio(a, b);
+#else
+  const double sgn = b >= 0 ? 1.0 : -1.0;
+  return a * rcp_p(b + sgn * kSMALL);
+#endif
+}
+
 // ---------------------------------------------------------- parameters
 // Device copy of the fluid / fixup / eos params (phx_params), with the
 // fixup package's defaults already resolved (fixup.cpp:120-180).
@@ -332,6 +373,81 @@ __device__ __forceinline__ void recon_weno5z(double q0, double q1, double q2, do
   ql = alpha_lin * ql + (1.0 - alpha_lin) * (q2 + 0.5 * dq);
   qr = alpha_lin * qr + (1.0 - alpha_lin) * (q2 - 0.5 * dq);
 }
+// ---- production-build WENO5-Z: same mathematics, fewer FP64 instructions.
+// WENO5-Z as reconstruction.hpp:127-183, rearranged: the nonlinear weights
+// are gamma_k (1 + tau5 / beta_k), normalised by their sum; the three 1/beta_k
+// come from one reciprocal of beta0 beta1 beta2, the two weight sums and the
+// two denominators of alpha_l, alpha_r (on normalised weights) from one
+// reciprocal each.  Four reciprocals instead of eight divisions.  Every
+// intermediate stays in the normal range for |q| < 1e50; outside it (checked
+// on the exponents) the reference sequence is used.
+__device__ __forceinline__ void recon_weno5z_fast(double q0, double q1, double q2, double q3, double q4,
+                                                  double &ql, double &qr) {
+  constexpr double a00 = 1.0 / 3.0, a01 = -7.0 / 6.0, a02 = 11.0 / 6.0;
+  constexpr double a10 = -1.0 / 6.0, a11 = 5.0 / 6.0, a12 = 1.0 / 3.0;
+  constexpr double a20 = 1.0 / 3.0, a21 = 5.0 / 6.0, a22 = -1.0 / 6.0;
+  constexpr double g0 = 0.1, g1 = 0.6, g2 = 0.3;
+  constexpr double eps = 1e-100;
+  constexpr double t13 = 13.0 / 3.0;
+  double a = q0 - 2 * q1 + q2;
+  double b = q0 - 4.0 * q1 + 3.0 * q2;
+  const double beta0 = t13 * a * a + b * b + eps;
+  a = q1 - 2.0 * q2 + q3;
+  b = q3 - q1;
+  const double beta1 = t13 * a * a + b * b + eps;
+  a = q2 - 2.0 * q3 + q4;
+  b = q4 - 4.0 * q3 + 3.0 * q2;
+  const double beta2 = t13 * a * a + b * b + eps;
+  const double tau5 = fabs(beta2 - beta0);
+  const double b01 = beta0 * beta1;
+  const double prod = b01 * beta2;
+  const int ep = dexp(prod);
+  if (ep < 16 || ep > 2030) {  // outside [~1e-303, ~1e303]: reference sequence
+    recon_weno5z(q0, q1, q2, q3, q4, ql, qr);
+    return;
+  }
+  const double rp = rcp_nr(prod);
+  const double t = beta2 * rp;
+  const double bp0 = fma(tau5, beta1 * t, 1.0);
+  const double bp1 = fma(tau5, beta0 * t, 1.0);
+  const double bp2 = fma(tau5, b01 * rp, 1.0);
+  double wl0 = fma(g0, bp0, eps), wl1 = fma(g1, bp1, eps), wl2 = fma(g2, bp2, eps);
+  double wr0 = fma(g0, bp2, eps), wr2 = fma(g2, bp0, eps);
+  const double Sl = wl0 + wl1 + wl2, Sr = wr0 + wl1 + wr2;
+  const double SS = Sl * Sr;
+  if (dexp(SS) > 2030) {
+    recon_weno5z(q0, q1, q2, q3, q4, ql, qr);
+    return;
+  }
+  const double rS = rcp_nr(SS);
+  const double isl = Sr * rS, isr = Sl * rS;
+  wl0 *= isl;
+  const double wm_l = wl1 * isl;
+  wl2 *= isl;
+  wr0 *= isr;
+  const double wm_r = wl1 * isr;
+  wr2 *= isr;
+  ql = wl0 * (a00 * q0 + a01 * q1 + a02 * q2) + wm_l * (a10 * q1 + a11 * q2 + a12 * q3) +
+       wl2 * (a20 * q2 + a21 * q3 + a22 * q4);
+  qr = wr0 * (a00 * q4 + a01 * q3 + a02 * q2) + wm_r * (a10 * q3 + a11 * q2 + a12 * q1) +
+       wr2 * (a20 * q2 + a21 * q1 + a22 * q0);
+  const double Dl = g2 * wl0 * wm_l + g1 * wl0 * wl2 + g0 * wm_l * wl2;
+  const double Dr = g2 * wr0 * wm_r + g1 * wr0 * wr2 + g0 * wm_r * wr2;
+  const double DD = Dl * Dr;
+  if (dexp(DD) < 16) {
+    recon_weno5z(q0, q1, q2, q3, q4, ql, qr);
+    return;
+  }
+  const double rD = rcp_nr(DD);
+  const double alpha_l = 3.0 * wl0 * wm_l * wl2 * (Dr * rD) + eps;
+  const double alpha_r = 3.0 * wr0 * wm_r * wr2 * (Dl * rD) + eps;
+  double dq = q3 - q2;
+  dq = mc(q2 - q1, dq, 2.0);
+  const double alpha_lin = 2.0 * alpha_l * alpha_r * rcp_nr(alpha_l + alpha_r);
+  ql = alpha_lin * ql + (1.0 - alpha_lin) * (q2 + 0.5 * dq);
+  qr = alpha_lin * qr + (1.0 - alpha_lin) * (q2 - 0.5 * dq);
+}
+
 __device__ __forceinline__ double minmod(double a, double b) {
   return a * b > 0.0 ? (fabs(a) < fabs(b) ? a : b) : 0.0;
 }
@@ -374,7 +490,11 @@ template <int RECON>
 __device__ __forceinline__ void recon(double qm2, double qm1, double q0, double qp1, double qp2,
                                       double &ql, double &qr) {
   if constexpr (RECON == PHX_RECON_WENO5Z) {
+#ifdef PHX_EXACT
     recon_weno5z(qm2, qm1, q0, qp1, qp2, ql, qr);
+#else
+    recon_weno5z_fast(qm2, qm1, q0, qp1, qp2, ql, qr);
+#endif
   } else if constexpr (RECON == PHX_RECON_MP5) {
     ql = mp5_subcalc(qm2, qm1, q0, qp1, qp2);
     qr = mp5_subcalc(qp2, qp1, q0, qm1, qm2);
@@ -412,7 +532,12 @@ __device__ __forceinline__ void prim_to_flux(const Par &par, const Face &f, cons
 #pragma unroll
     for (int ii = 0; ii < 3; ii++) vpcon[ii] *= rescale;
   }
+#ifdef PHX_EXACT
   double vcon[3] = {vpcon[0] / W, vpcon[1] / W, vpcon[2] / W};
+#else
+  const double iW0 = 1.0 / W;
+  double vcon[3] = {vpcon[0] * iW0, vpcon[1] * iW0, vpcon[2] * iW0};
+#endif
   double Bcon[3] = {0.0, 0.0, 0.0};
   const double qe = q[PHX_PENG];
   const double u = (qe / rho > sie_floor ? (qe / rho > sie_max ? rho * sie_max : qe) : rho * sie_floor);
@@ -450,7 +575,14 @@ __device__ __forceinline__ void prim_to_flux(const Par &par, const Face &f, cons
 #pragma unroll
     for (int m = 0; m < 3; m++) vcon[m] *= scale;
   }
+#ifdef PHX_EXACT
   W = 1.0 / sqrt(1 - vsq);
+#else
+  // production build: W = 1/s with s = sqrt(1 - v^2); divisions by W and W^2
+  // become products with s and s^2
+  const double sW = sqrt(1 - vsq);
+  W = 1.0 / sW;
+#endif
   const double vel = vcon[DIR];
   const double alpha = MINK ? 1.0 : g.alpha;
   double vtil;
@@ -461,28 +593,38 @@ __device__ __forceinline__ void prim_to_flux(const Par &par, const Face &f, cons
   U[PHX_CRHO] = rho * W;
   F[PHX_CRHO] = U[PHX_CRHO] * vtil;
   const double b0 = W * Bdotv;
+#ifdef PHX_EXACT
   const double bsq = (BdotB + b0 * b0) / (W * W);
+#else
+  const double bsq = (BdotB + b0 * b0) * (sW * sW);
+#endif
   const double rhohWsq = (rho + u + P) * W * W;
   const double bsqWsq = bsq * W * W;
   const double ptot = P + 0.5 * bsq;
 #pragma unroll
   for (int m = 0; m < 3; m++) {
     double bcovm, vcovm;
+#ifdef PHX_EXACT
+#define PHX_DIV_W(x) ((x) / W)
+#else
+#define PHX_DIV_W(x) ((x) * sW)
+#endif
     if constexpr (MINK) {
       // gcov[m+1][0] = 0: first term is +-0; then only n = m+1 survives
-      bcovm = Bcon[m] / W + b0 * vcon[m];
+      bcovm = PHX_DIV_W(Bcon[m]) + b0 * vcon[m];
       vcovm = vcon[m];
     } else {
       bcovm = g.gcov[m + 1][0] * b0 / alpha;
       vcovm = 0.0;
 #pragma unroll
       for (int n = 1; n < 4; n++) {
-        bcovm += g.gcov[m + 1][n] * (Bcon[n - 1] / W + b0 * (vcon[n - 1] - g.beta[n - 1] / alpha));
+        bcovm += g.gcov[m + 1][n] * (PHX_DIV_W(Bcon[n - 1]) + b0 * (vcon[n - 1] - g.beta[n - 1] / alpha));
         vcovm += g.gcov[m + 1][n] * vcon[n - 1];
       }
     }
     U[PHX_CMOM + m] = (rhohWsq + bsqWsq) * vcovm - b0 * bcovm;
-    F[PHX_CMOM + m] = U[PHX_CMOM + m] * vtil + ptot * (double)(DIR == m) - bcovm * Bcon[DIR] / W;
+    F[PHX_CMOM + m] = U[PHX_CMOM + m] * vtil + ptot * (double)(DIR == m) - PHX_DIV_W(bcovm * Bcon[DIR]);
+#undef PHX_DIV_W
   }
   U[PHX_CENG] = rhohWsq + bsqWsq - ptot - b0 * b0 - U[PHX_CRHO];
   F[PHX_CENG] = U[PHX_CENG] * vtil + ptot * vel - Bdotv * Bcon[DIR];

@@ -4,11 +4,10 @@
 // The reference reconstructs every variable into ql/qr arrays (K1) and then
 // solves one Riemann problem per face (K2).  Here each face's two states are
 // produced and consumed in registers:
-//   X1: a warp owns one (k, j) pencil.  Lane 0 stages the pencil's 10
-//       primitive rows in shared memory with cp.async.bulk (TMA bulk copies
-//       completing on an mbarrier); lanes reconstruct consecutive cells and
-//       the left state of face i (the upper-face value of cell i-1) moves to
-//       lane i with __shfl_up_sync.
+//   X1: a CTA stages four (k, j) pencils' 10 primitive rows in shared memory
+//       with cp.async.bulk (TMA bulk copies completing on an mbarrier); lanes
+//       reconstruct consecutive cells and the left state of face i (the
+//       upper-face value of cell i-1) moves to lane i with __shfl_up_sync.
 //   X2, X3: a thread sweeps a segment of faces along the direction with the
 //       5-point stencil window and the previous cell's upper-face state held
 //       in registers; consecutive lanes are consecutive i (coalesced).
@@ -96,58 +95,72 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned by
       : "memory");
 }
 
-constexpr int X1_WARPS = 4;
+constexpr int X1_WARPS = 4;    // warps per CTA
+constexpr int X1_PENCILS = 4;  // (k, j) pencils staged per CTA
 constexpr long long MBAR_SPIN_LIMIT = 1ll << 26;
 
-// One warp per (k, j) pencil; pencils enumerated over the transverse box.
+// A CTA stages X1_PENCILS pencils (10 primitive rows each) in shared memory
+// with TMA bulk copies completing on one mbarrier.  Its warps then walk the
+// pencils' cells as one flattened list [pencil][cell is-1 .. ie+1] in chunks
+// of 32 cells that overlap by one: lane L reconstructs its cell, takes the
+// upper-face state of the cell on its left from lane L-1 (__shfl_up_sync) and
+// solves the Riemann problem of its lower face; lane 0 only supplies its
+// state to lane 1 (its own face belongs to the previous chunk's lane 31).
 template <int RECON, bool MINK>
 __global__ void __launch_bounds__(32 * X1_WARPS)
     k_flux_x1(Par p, BView b, int jlo, int nj, int klo, int npencil, int use_tma, unsigned int *err) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  __shared__ __align__(8) uint64_t bars[X1_WARPS];
+  __shared__ __align__(8) uint64_t bar;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n1t = b.n1t;
-  double *row = reinterpret_cast<double *>(smem_raw) + (long long)warp * PHX_NRECON * n1t;
-  const int pencil = blockIdx.x * X1_WARPS + warp;
+  double *rows = reinterpret_cast<double *>(smem_raw);
+  const int p0 = blockIdx.x * X1_PENCILS;
+  const int np = min(X1_PENCILS, npencil - p0);
   if (use_tma) {
-    if (lane == 0) mbar_init(&bars[warp], 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    __syncwarp();
-  }
-  if (pencil >= npencil) return;  // whole warp leaves together
-  const int j = jlo + pencil % nj;
-  const int k = klo + pencil / nj;
-  const long long base = b.idx(k, j, 0);
-  if (use_tma) {
-    if (lane == 0) {
-      const unsigned bytes = (unsigned)(n1t * sizeof(double));
-      mbar_expect_tx(&bars[warp], bytes * PHX_NRECON);
-#pragma unroll 1
-      for (int v = 0; v < PHX_NRECON; v++) bulk_g2s(row + v * n1t, b.prim + v * b.vs + base, bytes, &bars[warp]);
+    if (threadIdx.x == 0) {
+      mbar_init(&bar, 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const unsigned bytes = (unsigned)(n1t * sizeof(double));
+    if (threadIdx.x == 0) mbar_expect_tx(&bar, bytes * PHX_NRECON * np);
+    __syncthreads();
+    if (threadIdx.x < np * PHX_NRECON) {  // one bulk copy per (pencil, variable) row
+      const int pp = threadIdx.x / PHX_NRECON, v = threadIdx.x % PHX_NRECON;
+      const int pen = p0 + pp;
+      const long long base = b.idx(klo + pen / nj, jlo + pen % nj, 0);
+      bulk_g2s(rows + (long long)(pp * PHX_NRECON + v) * n1t, b.prim + v * b.vs + base, bytes, &bar);
     }
     long long spins = 0;
-    while (!mbar_try_wait(&bars[warp], 0)) {
+    while (!mbar_try_wait(&bar, 0)) {
       if (++spins > MBAR_SPIN_LIMIT) {
-        if (lane == 0) atomicOr(err, ERR_TIMEOUT);
-        return;
+        if (threadIdx.x == 0) atomicOr(err, ERR_TIMEOUT);
+        return;  // every thread gives up on the same bounded wait
       }
     }
   } else {
-    for (int v = 0; v < PHX_NRECON; v++)
-      for (int i = lane; i < n1t; i += 32) row[v * n1t + i] = b.prim[v * b.vs + base + i];
-    __syncwarp();
+    for (int r = warp; r < np * PHX_NRECON; r += X1_WARPS) {
+      const int pp = r / PHX_NRECON, v = r % PHX_NRECON;
+      const int pen = p0 + pp;
+      const long long base = b.idx(klo + pen / nj, jlo + pen % nj, 0);
+      for (int i = lane; i < n1t; i += 32) rows[(long long)r * n1t + i] = b.prim[v * b.vs + base + i];
+    }
+    __syncthreads();
   }
-  const int c0 = b.is() - 1, c1 = b.ie() + 1;  // cells reconstructed
-  double carry[PHX_NRECON];
-#pragma unroll
-  for (int v = 0; v < PHX_NRECON; v++) carry[v] = 0.0;
-  for (int cbase = c0; cbase <= c1; cbase += 32) {
-    const int c = cbase + lane;
-    const bool have = c <= c1;
+  const int c0 = b.is() - 1;
+  const int ncell = b.ie() + 1 - c0 + 1;  // cells is-1 .. ie+1 per pencil
+  const int nslot = np * ncell;
+  const int nchunk = (nslot - 1 + 30) / 31;
+  for (int ch = warp; ch < nchunk; ch += X1_WARPS) {
+    const int slot = ch * 31 + lane;
+    const bool have = slot < nslot;
+    const int pp = have ? slot / ncell : 0;
+    const int c = c0 + (have ? slot % ncell : 0);
+    const double *prow = rows + (long long)pp * PHX_NRECON * n1t;
     double ql[PHX_NRECON], qr[PHX_NRECON];
 #pragma unroll
     for (int v = 0; v < PHX_NRECON; v++) {
-      const double *r = row + v * n1t;
+      const double *r = prow + v * n1t;
       if (have) {
         if constexpr (RECON == PHX_RECON_WENO5Z || RECON == PHX_RECON_MP5)
           recon<RECON>(r[c - 2], r[c - 1], r[c], r[c + 1], r[c + 2], ql[v], qr[v]);
@@ -161,13 +174,12 @@ __global__ void __launch_bounds__(32 * X1_WARPS)
     }
     double left[PHX_NRECON];
 #pragma unroll
-    for (int v = 0; v < PHX_NRECON; v++) {
-      const double up = __shfl_up_sync(FULL, ql[v], 1);
-      left[v] = lane == 0 ? carry[v] : up;
-      carry[v] = __shfl_sync(FULL, ql[v], 31);
+    for (int v = 0; v < PHX_NRECON; v++) left[v] = __shfl_up_sync(FULL, ql[v], 1);
+    // face of cell c: left state from cell c-1 (same pencil when c > is-1)
+    if (have && lane > 0 && c > c0) {
+      const int pen = p0 + pp;
+      face_flux<MINK, 0>(p, b, klo + pen / nj, jlo + pen % nj, c, left, qr);
     }
-    // face c: left state from cell c-1, right state from cell c
-    if (have && c >= b.is()) face_flux<MINK, 0>(p, b, k, j, c, left, qr);
   }
 }
 
@@ -265,14 +277,14 @@ static void launch_fluxes_t(const Par &p, const BView &b, unsigned int *err, cud
     const int jlo = js - dj, nj = je - js + 1 + 2 * dj;
     const int klo = ks - dk, nk = ke - ks + 1 + 2 * dk;
     const int npencil = nj * nk;
-    const size_t smem = (size_t)X1_WARPS * PHX_NRECON * b.n1t * sizeof(double);
+    const size_t smem = (size_t)X1_PENCILS * PHX_NRECON * b.n1t * sizeof(double);
     const bool aligned = (b.n1t % 2 == 0) && (b.vs % 2 == 0) &&
                          ((reinterpret_cast<uintptr_t>(b.prim) & 15) == 0);
     if (smem <= 200 * 1024) {
       auto kern = k_flux_x1<RECON, MINK>;
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      kern<<<(npencil + X1_WARPS - 1) / X1_WARPS, 32 * X1_WARPS, smem, s>>>(p, b, jlo, nj, klo, npencil,
-                                                                          aligned ? 1 : 0, err);
+      kern<<<(npencil + X1_PENCILS - 1) / X1_PENCILS, 32 * X1_WARPS, smem, s>>>(p, b, jlo, nj, klo, npencil,
+                                                                              aligned ? 1 : 0, err);
     } else {
       launch_sweep<RECON, MINK, 0>(p, b, jlo, nj, klo, nk, is, ie - is + 2, s);
     }
