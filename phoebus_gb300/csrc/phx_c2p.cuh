@@ -114,19 +114,28 @@ __device__ __forceinline__ bool c2p_setup(const Par &p, const Pt &g, const doubl
   const int num_nans = isnan(U[PHX_CRHO]) + isnan(U[PHX_CMOM]) + isnan(U[PHX_CENG]);
   if (num_nans > 0) return false;
   const double gdet = MINK ? 1.0 : g.detgam;
-  const double igdet = 1.0 / gdet;
+  const double igdet = rcp_p(gdet);
   double rhoflr = 0.0, epsflr;
   get_floors(p, x1, x2, x3, rhoflr, epsflr);
   rhoflr *= p.fsf;
   const double gam_max = p.g0;
   const double D = U[PHX_CRHO] * igdet;
   const double tau = U[PHX_CENG] * igdet;
-  const double q = ratio(tau, D);
+  const double q = ratio_p(tau, D);
   double bsq = 0.0, bsq_rpsq = 0.0, rbsq = 0.0, rsq;
   bdotr = 0.0;
+#ifdef PHX_EXACT
   rcov[0] = ratio(U[PHX_CMOM], U[PHX_CRHO]);
   rcov[1] = ratio(U[PHX_CMOM + 1], U[PHX_CRHO]);
   rcov[2] = ratio(U[PHX_CMOM + 2], U[PHX_CRHO]);
+#else
+  {
+    const double ic = ratio_p(1.0, U[PHX_CRHO]);
+    rcov[0] = U[PHX_CMOM] * ic;
+    rcov[1] = U[PHX_CMOM + 1] * ic;
+    rcov[2] = U[PHX_CMOM + 2] * ic;
+  }
+#endif
   if constexpr (MINK) {
     rcon[0] = rcov[0];
     rcon[1] = rcov[1];
@@ -146,7 +155,7 @@ __device__ __forceinline__ bool c2p_setup(const Par &p, const Pt &g, const doubl
   if (p.mhd) {
 #pragma unroll
     for (int ii = 0; ii < 3; ii++) Bprim[ii] = U[PHX_CB + ii] * igdet;
-    const double sD = 1.0 / sqrt(fmax(D, rhoflr));
+    const double sD = rcp_p(sqrt(fmax(D, rhoflr)));
 #pragma unroll
     for (int ii = 0; ii < 3; ii++) {
       bu[ii] = Bprim[ii] * sD;
@@ -158,7 +167,7 @@ __device__ __forceinline__ bool c2p_setup(const Par &p, const Pt &g, const doubl
     bsq_rpsq = bsq * rsq - rbsq;
   }
   const double zsq = rsq / 1.0;  // h0sq_ = 1
-  const double v0sq = fmin(zsq / (1.0 + zsq), 1.0 - 1.0 / (gam_max * gam_max));
+  const double v0sq = fmin(div_p(zsq, 1.0 + zsq), 1.0 - rcp_p(gam_max * gam_max));
   res.D = D;
   res.q = q;
   res.bsq = bsq;
@@ -211,7 +220,7 @@ __device__ __forceinline__ double regula_falsi_warp(const Par &p, Residual &res,
   bool active = valid && bracketed && (b - a > 2.0 * tol) && (it < max_iter);
   while (__any_sync(0xffffffffu, active)) {
     if (active) {
-      const double c = (a * yb - b * ya) / (yb - ya);
+      const double c = div_p(a * yb - b * ya, yb - ya);
       if (c == a) {
         b = a;
       } else if (c == b) {
@@ -263,13 +272,13 @@ __device__ __forceinline__ void c2p_finish(const Par &p, const Pt &g, Residual &
   const double iW = res.iWhat_mu(vsq);
   prim[PHX_PRHO] = res.rhohat_mu(iW);
   const double qbar = res.qbar_mu(mu, x);
-  const double W = 1.0 / iW;
+  const double W = rcp_p(iW);
   double eng = res.ehat_mu(p, mu, qbar, rbarsq, vsq, W);
   prim[PHX_PTMP] = eos_T_rho_sie(p, prim[PHX_PRHO], eng);
   eng *= prim[PHX_PRHO];
   prim[PHX_PENG] = eng;
   prim[PHX_PPRS] = eos_P_rho_T(p, prim[PHX_PRHO], prim[PHX_PTMP]);
-  prim[PHX_PGM1] = eos_bmod_rho_T(p, prim[PHX_PRHO], prim[PHX_PTMP]) / prim[PHX_PPRS];
+  prim[PHX_PGM1] = div_p(eos_bmod_rho_T(p, prim[PHX_PRHO], prim[PHX_PTMP]), prim[PHX_PPRS]);
   double vel[3];
 #pragma unroll
   for (int ii = 0; ii < 3; ii++) {

@@ -97,7 +97,7 @@ __device__ __forceinline__ double eos_P_rho_sie(const Par &p, double rho, double
   return fmax(0.0, p.gm1 * rho * sie);
 }
 __device__ __forceinline__ double eos_T_rho_sie(const Par &p, double rho, double sie) {
-  return fmax(0.0, sie / p.Cv);
+  return fmax(0.0, div_p(sie, p.Cv));
 }
 __device__ __forceinline__ double eos_P_rho_T(const Par &p, double rho, double T) {
   return fmax(0.0, p.gm1 * rho * p.Cv * T);
@@ -229,11 +229,11 @@ __device__ __forceinline__ void signal_speeds(double rho, double u, double p, do
                                               const double v[3], double vsq, double gam1,
                                               const Pt &g, double *sig) {
   const double rho_rel = rho + u + p;
-  const double vasq = bsq / (rho_rel + bsq);
-  double cssq = gam1 * p / rho_rel;
+  const double vasq = div_p(bsq, rho_rel + bsq);
+  double cssq = div_p(gam1 * p, rho_rel);
   cssq += vasq - cssq * vasq;
   const double alpha = MINK ? 1.0 : g.alpha;
-  const double vcoff = alpha / (1.0 - vsq * cssq);
+  const double vcoff = div_p(alpha, 1.0 - vsq * cssq);
 #pragma unroll
   for (int m = 0; m < 3; m++) {
     const double gmm = MINK ? 1.0 : g.gamcon[m][m];
@@ -254,7 +254,7 @@ __device__ __forceinline__ void p2c(double rho, const double vp[3], const double
                                     double p, double gam1, const Pt &g, double gdet, double &D,
                                     double S[3], double bcons[3], double &tau, double *sig) {
   const double W = lorentz<MINK>(g, vp);
-  const double iW = 1.0 / W;
+  const double iW = rcp_p(W);
   double v[3] = {vp[0] * iW, vp[1] * iW, vp[2] * iW};
   double vsq, Bsq, Bdotv;
   if constexpr (MINK) {

@@ -71,21 +71,30 @@ def test_con_to_prim_exact(oracle, ctx_exact, tol, maxit):
 
 
 def test_con_to_prim_fast(oracle, ctx_fast):
-    """Production build: prims within the con2prim tolerance, same flags."""
+    """Production build: the root mu agrees to the con2prim tolerance, fail
+    flags are identical, and the primitives differ by no more than two valid
+    solutions can: each is within the tolerance-induced deviation delta of
+    the exact root, measured here per variable as the oracle at tol against
+    the oracle at 1e-15 (the state's conditioning amplifies d mu into the
+    prims, ~W^2 for Lorentz factors up to 5)."""
     tol = 1e-10
     p = abi.default_params(Gamma=4.0 / 3.0, c2p_tol=tol, c2p_max_iter=100)
     hb = states.random_block(12, 9)
     oracle.PrimitiveToConserved(p, hb)
     db = hb.to_device()
+    tight = hb.to_host()
     oracle.ConservedToPrimitive(p, hb)
+    oracle.ConservedToPrimitive(abi.default_params(Gamma=4.0 / 3.0, c2p_tol=1e-15, c2p_max_iter=300), tight)
     ctx_fast.ConservedToPrimitive(p, db)
     ctx_fast.check()
     assert_bitwise(db["fail"], hb["fail"], "fail")
-    got, ref = db["prim"].cpu().numpy(), hb["prim"]
+    got, ref, exact = db["prim"].cpu().numpy(), hb["prim"], tight["prim"]
     # mu is the root itself: |mu_gpu - mu_cpu| <= 2 tol (both within tol of the root)
     assert np.max(np.abs(got[abi.PMU] - ref[abi.PMU])) <= 2 * tol
     for v in (abi.PRHO, abi.PENG, abi.PPRS, abi.PVEL, abi.PVEL + 1, abi.PVEL + 2):
-        assert_close(got[v], ref[v], 1e-8, f"prim {v}")
+        delta = np.max(np.abs(ref[v] - exact[v]) / np.abs(exact[v]))
+        err = np.max(np.abs(got[v] - ref[v]) / np.abs(ref[v]))
+        assert err <= 2.5 * delta + 1e-14, (v, err, delta)
 
 
 def test_con_to_prim_nan_and_guess(oracle, ctx_exact):
