@@ -1,0 +1,249 @@
+// phx_parthenon_shim.hpp -- the phoebus fluid task signatures over the C ABI.
+//
+// Header-only C++17.  It gives the functions phoebus's driver calls
+// (fluid.hpp:27-69, paths relative to the phoebus source tree) the same names,
+// signatures and error behaviour, and implements them with phx_fluid.h:
+//
+//   TaskStatus fluid::PrimitiveToConserved(MeshBlockData<Real> *)        fluid.cpp:359
+//   TaskStatus fluid::PrimitiveToConservedRegion(MeshBlockData<Real> *,
+//                                               ib, jb, kb)              fluid.cpp:368
+//   template <T> TaskStatus fluid::ConservedToPrimitive(T *)            fluid.cpp:469
+//   template <T> TaskStatus fluid::ConservedToPrimitiveRegion(T *, ...)  fluid.cpp:451
+//   template <T> TaskStatus fluid::ConservedToPrimitiveRobust(T *, ...)  fluid.cpp:477
+//   TaskStatus fluid::CalculateFluidSourceTerms(MeshData<Real> *,
+//                                              MeshData<Real> *)        fluid.cpp:566
+//   TaskStatus fluid::CalculateFluxes(MeshBlockData<Real> *)             fluid.cpp:659
+//   TaskStatus fluid::FluxCT(MeshBlockData<Real> *)                      fluid.cpp:775
+//   Real fluid::EstimateTimestepBlock(MeshBlockData<Real> *)             fluid.cpp:899
+//   template <T> using fluid::c2p_type = TaskStatus (*)(T *, ...)        fluid.hpp:65
+//
+// Parthenon is not part of this library, so the shim carries the few pieces
+// of it these tasks touch (MeshBlockData, MeshData, IndexRange, IndexDomain,
+// TaskStatus, the package Params) as small stand-ins in namespace parthenon.
+// Inside phoebus the same function bodies are written against the real
+// Parthenon types: a pack's variable Views provide the device pointers of
+// phx_block.
+//
+// Errors: configuration errors throw std::runtime_error (PARTHENON_THROW);
+// an unbracketed con2prim root is detected by phx_ctx_check() at the end of
+// ConservedToPrimitive and throws "Aborting with unbracketed root."
+// (root_find.hpp:115-118 aborts the run).
+#ifndef PHX_PARTHENON_SHIM_HPP_
+#define PHX_PARTHENON_SHIM_HPP_
+
+#include <cuda_runtime.h>
+
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "phx_fluid.h"
+
+namespace parthenon {
+using Real = double;
+enum class TaskStatus { fail, complete, incomplete, iterate, skip, waiting };
+enum class IndexDomain { entire, interior };
+struct IndexRange {
+  int s = 0;
+  int e = -1;
+};
+
+// Package parameters and execution resources the fluid tasks read.
+struct Mesh {
+  phx_params params{};      // "fluid", "fixup" and "eos" package Params
+  phx_geometry geometry{};  // "geometry" package (Minkowski or FMKS tables)
+  phx_ctx *ctx = nullptr;   // device context (the execution space)
+  void *stream = nullptr;   // CUDA stream the tasks run on
+  double *dt_device = nullptr;  // one device double for EstimateTimestepBlock
+  bool has_face_speeds = false; // fluid.cpp:911-941 switch
+  int ndim = 3;
+};
+
+template <typename T>
+class MeshBlockData;
+template <typename T>
+class MeshData;
+
+// One meshblock's fields (device pointers) and its mesh.
+template <>
+class MeshBlockData<Real> {
+ public:
+  MeshBlockData(Mesh *mesh, const phx_block &b) : mesh_(mesh), b_(b) { b_.geom = &mesh_->geometry; }
+  Mesh *GetMeshPointer() const { return mesh_; }
+  phx_block &Block() { return b_; }
+  const phx_block &Block() const { return b_; }
+  IndexRange GetBoundsI(IndexDomain d) const {
+    return d == IndexDomain::entire ? IndexRange{0, b_.nx1 + 2 * b_.ng - 1} : IndexRange{b_.ng, b_.ng + b_.nx1 - 1};
+  }
+  IndexRange GetBoundsJ(IndexDomain d) const {
+    if (b_.ndim < 2) return IndexRange{0, 0};
+    return d == IndexDomain::entire ? IndexRange{0, b_.nx2 + 2 * b_.ng - 1} : IndexRange{b_.ng, b_.ng + b_.nx2 - 1};
+  }
+  IndexRange GetBoundsK(IndexDomain d) const {
+    if (b_.ndim < 3) return IndexRange{0, 0};
+    return d == IndexDomain::entire ? IndexRange{0, b_.nx3 + 2 * b_.ng - 1} : IndexRange{b_.ng, b_.ng + b_.nx3 - 1};
+  }
+
+ private:
+  Mesh *mesh_;
+  phx_block b_;
+};
+
+// A pack of blocks (a MeshData partition).
+template <>
+class MeshData<Real> {
+ public:
+  MeshData(Mesh *mesh, std::vector<MeshBlockData<Real> *> blocks) : mesh_(mesh), blocks_(std::move(blocks)) {}
+  Mesh *GetMeshPointer() const { return mesh_; }
+  int NumBlocks() const { return static_cast<int>(blocks_.size()); }
+  MeshBlockData<Real> *GetBlockData(int n) const { return blocks_.at(n); }
+
+ private:
+  Mesh *mesh_;
+  std::vector<MeshBlockData<Real> *> blocks_;
+};
+}  // namespace parthenon
+
+namespace fluid {
+using parthenon::IndexDomain;
+using parthenon::IndexRange;
+using parthenon::Mesh;
+using parthenon::MeshBlockData;
+using parthenon::MeshData;
+using parthenon::Real;
+using parthenon::TaskStatus;
+
+template <typename T>
+using c2p_type = TaskStatus (*)(T *, const IndexRange &, const IndexRange &, const IndexRange &);
+using c2p_meshblock_type = c2p_type<MeshBlockData<Real>>;
+using c2p_mesh_type = c2p_type<MeshData<Real>>;
+
+namespace detail {
+inline void check(phx_status s, const char *where) {
+  if (s != PHX_OK)
+    throw std::runtime_error(std::string(where) + ": " + phx_status_string(s) + " (" + phx_last_error() + ")");
+}
+inline phx_range R(const IndexRange &r) { return phx_range{r.s, r.e}; }
+}  // namespace detail
+
+inline TaskStatus PrimitiveToConservedRegion(MeshBlockData<Real> *rc, const IndexRange &ib, const IndexRange &jb,
+                                             const IndexRange &kb) {
+  Mesh *m = rc->GetMeshPointer();
+  detail::check(phx_prim_to_con(m->ctx, &m->params, &rc->Block(), detail::R(ib), detail::R(jb), detail::R(kb),
+                                m->stream),
+                "PrimitiveToConservedRegion");
+  return TaskStatus::complete;
+}
+
+inline TaskStatus PrimitiveToConserved(MeshBlockData<Real> *rc) {
+  return PrimitiveToConservedRegion(rc, rc->GetBoundsI(IndexDomain::entire), rc->GetBoundsJ(IndexDomain::entire),
+                                    rc->GetBoundsK(IndexDomain::entire));
+}
+
+// The robust solver (con2prim_robust.hpp) on one block or on every block of
+// a pack.  An unbracketed root aborts, as in the reference.
+template <typename T>
+TaskStatus ConservedToPrimitiveRobust(T *rc, const IndexRange &ib, const IndexRange &jb, const IndexRange &kb);
+
+template <>
+inline TaskStatus ConservedToPrimitiveRobust<MeshBlockData<Real>>(MeshBlockData<Real> *rc, const IndexRange &ib,
+                                                                  const IndexRange &jb, const IndexRange &kb) {
+  Mesh *m = rc->GetMeshPointer();
+  detail::check(phx_con_to_prim(m->ctx, &m->params, &rc->Block(), detail::R(ib), detail::R(jb), detail::R(kb),
+                                m->stream),
+                "ConservedToPrimitiveRobust");
+  detail::check(phx_ctx_check(m->ctx), "ConservedToPrimitiveRobust");
+  return TaskStatus::complete;
+}
+
+template <>
+inline TaskStatus ConservedToPrimitiveRobust<MeshData<Real>>(MeshData<Real> *rc, const IndexRange &ib,
+                                                             const IndexRange &jb, const IndexRange &kb) {
+  Mesh *m = rc->GetMeshPointer();
+  for (int n = 0; n < rc->NumBlocks(); n++)
+    detail::check(phx_con_to_prim(m->ctx, &m->params, &rc->GetBlockData(n)->Block(), detail::R(ib), detail::R(jb),
+                                  detail::R(kb), m->stream),
+                  "ConservedToPrimitiveRobust");
+  detail::check(phx_ctx_check(m->ctx), "ConservedToPrimitiveRobust");
+  return TaskStatus::complete;
+}
+
+// fluid.cpp:68-75: the c2p Param is a function pointer; only the robust
+// solver is provided (c2p_method = "robust", the default).
+template <typename T>
+inline c2p_type<T> c2p_func() {
+  return ConservedToPrimitiveRobust<T>;
+}
+
+template <typename T>
+TaskStatus ConservedToPrimitiveRegion(T *rc, const IndexRange &ib, const IndexRange &jb, const IndexRange &kb) {
+  auto c2p = c2p_func<T>();
+  return c2p(rc, ib, jb, kb);
+}
+
+template <typename T>
+TaskStatus ConservedToPrimitive(T *rc);
+
+template <>
+inline TaskStatus ConservedToPrimitive<MeshBlockData<Real>>(MeshBlockData<Real> *rc) {
+  return ConservedToPrimitiveRegion(rc, rc->GetBoundsI(IndexDomain::entire), rc->GetBoundsJ(IndexDomain::entire),
+                                    rc->GetBoundsK(IndexDomain::entire));
+}
+
+template <>
+inline TaskStatus ConservedToPrimitive<MeshData<Real>>(MeshData<Real> *rc) {
+  // every block of a pack shares the index ranges of the first
+  MeshBlockData<Real> *b0 = rc->GetBlockData(0);
+  return ConservedToPrimitiveRegion(rc, b0->GetBoundsI(IndexDomain::entire), b0->GetBoundsJ(IndexDomain::entire),
+                                    b0->GetBoundsK(IndexDomain::entire));
+}
+
+// Sources go to rc_src's momentum and energy: with the conserved layout
+// (D, S_1..3, tau, B) the four source fields are cons + one variable.
+inline TaskStatus CalculateFluidSourceTerms(MeshData<Real> *rc, MeshData<Real> *rc_src) {
+  Mesh *m = rc->GetMeshPointer();
+  std::vector<phx_block> blocks;
+  for (int n = 0; n < rc->NumBlocks(); n++) {
+    phx_block b = rc->GetBlockData(n)->Block();
+    const phx_block &s = rc_src->GetBlockData(n)->Block();
+    const long long N = (long long)(b.nx1 + 2 * b.ng) * (b.ndim >= 2 ? b.nx2 + 2 * b.ng : 1) *
+                        (b.ndim >= 3 ? b.nx3 + 2 * b.ng : 1);
+    const long long vs = s.var_stride ? s.var_stride : N;
+    b.src = s.cons + vs;
+    blocks.push_back(b);
+  }
+  detail::check(phx_calculate_fluid_source_terms(m->ctx, &m->params, blocks.data(), (int)blocks.size(), m->stream),
+                "CalculateFluidSourceTerms");
+  return TaskStatus::complete;
+}
+
+inline TaskStatus CalculateFluxes(MeshBlockData<Real> *rc) {
+  Mesh *m = rc->GetMeshPointer();
+  detail::check(phx_calculate_fluxes(m->ctx, &m->params, &rc->Block(), m->stream), "CalculateFluxes");
+  return TaskStatus::complete;
+}
+
+inline TaskStatus FluxCT(MeshBlockData<Real> *rc) {
+  Mesh *m = rc->GetMeshPointer();
+  detail::check(phx_flux_ct(m->ctx, &m->params, &rc->Block(), m->stream), "FluxCT");
+  return TaskStatus::complete;
+}
+
+inline Real EstimateTimestepBlock(MeshBlockData<Real> *rc) {
+  Mesh *m = rc->GetMeshPointer();
+  if (!m->dt_device) throw std::runtime_error("EstimateTimestepBlock: Mesh::dt_device is not set");
+  detail::check(phx_estimate_timestep(m->ctx, &m->params, &rc->Block(), m->has_face_speeds ? 1 : 0, m->dt_device,
+                                      m->stream),
+                "EstimateTimestepBlock");
+  Real dt = 0.0;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(m->stream);
+  if (cudaMemcpyAsync(&dt, m->dt_device, sizeof(Real), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    throw std::runtime_error("EstimateTimestepBlock: copy of dt failed");
+  m->has_face_speeds = true;
+  return dt;
+}
+
+}  // namespace fluid
+
+#endif  // PHX_PARTHENON_SHIM_HPP_

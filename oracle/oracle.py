@@ -67,6 +67,10 @@ def lib() -> C.CDLL:
         L.orc_geometry_fill_fmks.restype = None
         L.orc_fmks_point.argtypes = [C.POINTER(abi.Geometry), C.c_double, C.c_double, C.c_double, C.c_void_p]
         L.orc_fmks_point.restype = None
+        L.orc_c2p_fixup.argtypes = [P, B]
+        L.orc_c2p_fixup.restype = None
+        L.orc_apply_floors.argtypes = [P, B, R, R, R]
+        L.orc_apply_floors.restype = C.c_longlong
         _lib = L
     return _lib
 
@@ -134,6 +138,15 @@ class Oracle:
         s = b.struct()
         return self.L.orc_estimate_timestep(C.byref(p), C.byref(s), int(use_face_speeds))
 
+    def ConservedToPrimitiveFixup(self, p, b: Block):
+        s = b.struct()
+        self.L.orc_c2p_fixup(C.byref(p), C.byref(s))
+
+    def ApplyFloors(self, p, b: Block, ib=None, jb=None, kb=None):
+        e = b.entire()
+        s = b.struct()
+        return self.L.orc_apply_floors(C.byref(p), C.byref(s), _r(ib or e[0]), _r(jb or e[1]), _r(kb or e[2]))
+
     def GeometryFillFMKS(self, b: Block):
         g = b.geom.struct()
         s = b.struct()
@@ -162,8 +175,12 @@ class Oracle:
         cons_in = b.arrays["cons"]
         b.arrays["cons"] = out
         unbr = self.ConservedToPrimitive(p, b)
+        self.ConservedToPrimitiveFixup(p, b)
+        self.ApplyFloors(p, b)
         self.FillGhostsPeriodic(b, out, abi.NCONS if p.mhd else 5)
         unbr += self.ConservedToPrimitive(p, b)
+        self.ConservedToPrimitiveFixup(p, b)
+        self.ApplyFloors(p, b)
         b.arrays["cons"] = cons_in
         return unbr
 

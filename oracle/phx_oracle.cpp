@@ -76,7 +76,8 @@ struct Bounds {
   Real g0, smax0;          // ceilings
   Real bsqorho0, bsqou0;   // MHD ceilings
   explicit Bounds(const phx_params &p) {
-    if (p.enable_floors) {
+    // fixup.cpp:124-133: c2p fixup and MHD floors force floors on
+    if (p.enable_floors || p.enable_c2p_fixup || (p.enable_mhd_floors && p.mhd)) {
       floor_type = p.floor_type;
       r0 = p.rho0_floor;
       s0 = p.sie0_floor;
@@ -1271,6 +1272,184 @@ void sources(const phx_params &par, const phx_block *blk) {
       }
 }
 
+
+// fixup_c2p.cpp:170-353 (ConservedToPrimitiveFixupImpl, fluid part) on the
+// interior.  Neighbour prims are read from a snapshot taken before the loop,
+// so the result does not depend on the order zones are fixed in.
+void c2p_fixup(const phx_params &par, const phx_block *blk) {
+  Blk B(blk);
+  Geom G(blk->geom, &B);
+  Bounds bounds(par);
+  EOS eos{par.gm1, par.Cv};
+  if (!par.enable_c2p_fixup) return;
+  const int ndim = B.ndim;
+  const bool mhd = par.mhd != 0;
+  std::vector<double> snap(blk->prim, blk->prim + (size_t)PHX_NPRIM * B.vs);
+  auto S = [&](int v, int k, int j, int i) { return snap[v * B.vs + B.idx(k, j, i)]; };
+  auto fl = [&](int k, int j, int i) { return blk->fail[B.idx(k, j, i)]; };
+  const int is = B.is(), ie = B.ie(), js = B.js(), je = B.je(), ks = B.ks(), ke = B.ke();
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int k = ks; k <= ke; k++)
+    for (int j = js; j <= je; j++)
+      for (int i = is; i <= ie; i++) {
+        if (fl(k, j, i) != 0.0) continue;
+        Real gamma_max, e_max;
+        bounds.GetCeilings(B.Xc(1, i), B.Xc(2, j), B.Xc(3, k), gamma_max, e_max);
+        auto fixv = [&](int iv, Real inv_mask_sum) {
+          Real s = fl(k, j, i - 1) * S(iv, k, j, i - 1) + fl(k, j, i + 1) * S(iv, k, j, i + 1);
+          if (ndim > 1) {
+            s += fl(k, j - 1, i) * S(iv, k, j - 1, i) + fl(k, j + 1, i) * S(iv, k, j + 1, i);
+            if (ndim == 3) s += fl(k - 1, j, i) * S(iv, k - 1, j, i) + fl(k + 1, j, i) * S(iv, k + 1, j, i);
+          }
+          return inv_mask_sum * s;
+        };
+        Real num_valid = fl(k, j, i - 1) + fl(k, j, i + 1);
+        if (ndim > 1) num_valid += fl(k, j - 1, i) + fl(k, j + 1, i);
+        if (ndim == 3) num_valid += fl(k - 1, j, i) + fl(k + 1, j, i);
+        if (num_valid > 0.5 && !par.c2p_failure_strategy_floors) {
+          const Real norm = 1.0 / num_valid;
+          B.P(PHX_PRHO, k, j, i) = fixv(PHX_PRHO, norm);
+          for (int pv = 0; pv < 3; pv++) B.P(PHX_PVEL + pv, k, j, i) = fixv(PHX_PVEL + pv, norm);
+          B.P(PHX_PENG, k, j, i) = fixv(PHX_PENG, norm);
+          B.P(PHX_PRHO, k, j, i) = std::max<Real>(B.P(PHX_PRHO, k, j, i), 100. * SMALL);
+          B.P(PHX_PENG, k, j, i) = std::max<Real>(B.P(PHX_PENG, k, j, i), 100. * SMALL);
+        } else {
+          B.P(PHX_PRHO, k, j, i) = 100. * SMALL;
+          B.P(PHX_PENG, k, j, i) = 100. * SMALL;
+          for (int ii = 0; ii < 3; ii++) B.P(PHX_PVEL + ii, k, j, i) = 0.;
+        }
+        GeomPt g;
+        G.at(CENT, k, j, i, g);
+        Real vpcon[3] = {B.P(PHX_PVEL, k, j, i), B.P(PHX_PVEL + 1, k, j, i), B.P(PHX_PVEL + 2, k, j, i)};
+        Real W = GetLorentzFactor(vpcon, g.gcov);
+        if (W > gamma_max) {
+          const Real rescale = std::sqrt(gamma_max * gamma_max - 1.) / (W * W - 1.);
+          for (int ii = 0; ii < 3; ii++) vpcon[ii] *= rescale;
+          for (int ii = 0; ii < 3; ii++) B.P(PHX_PVEL + ii, k, j, i) = vpcon[ii];
+          W = gamma_max;
+        }
+        Real &rho = B.P(PHX_PRHO, k, j, i);
+        B.P(PHX_PTMP, k, j, i) = eos.TemperatureFromDensityInternalEnergy(rho, ratio(B.P(PHX_PENG, k, j, i), rho));
+        B.P(PHX_PPRS, k, j, i) = eos.PressureFromDensityTemperature(rho, B.P(PHX_PTMP, k, j, i));
+        B.P(PHX_PGM1, k, j, i) =
+            ratio(eos.BulkModulusFromDensityTemperature(rho, B.P(PHX_PTMP, k, j, i)), B.P(PHX_PPRS, k, j, i));
+        Real bp[3] = {0.0, 0.0, 0.0};
+        if (mhd)
+          for (int ii = 0; ii < 3; ii++) bp[ii] = B.P(PHX_PB + ii, k, j, i);
+        Real Sv[3], bc[3], sig[3], D, tau;
+        p2c(rho, vpcon, bp, B.P(PHX_PENG, k, j, i), B.P(PHX_PPRS, k, j, i), B.P(PHX_PGM1, k, j, i), g.gcov,
+            g.gamcon, g.beta, g.alpha, g.detgam, D, Sv, bc, tau, sig);
+        B.U(PHX_CRHO, k, j, i) = D;
+        B.U(PHX_CENG, k, j, i) = tau;
+        for (int ii = 0; ii < 3; ii++) B.U(PHX_CMOM + ii, k, j, i) = Sv[ii];
+        for (int d = 0; d < ndim; d++) blk->cell_sig[d * B.vs + B.idx(k, j, i)] = sig[d];
+      }
+}
+
+// fixup.cpp:370-540 (ApplyFloorsImpl, fluid part) over the given range.
+// Returns the number of zones whose re-inversion failed (set to floors).
+long long apply_floors(const phx_params &par, const phx_block *blk, phx_range ib, phx_range jb, phx_range kb) {
+  Blk B(blk);
+  Geom G(blk->geom, &B);
+  Bounds bounds(par);
+  EOS eos{par.gm1, par.Cv};
+  if (!(par.enable_floors || par.enable_c2p_fixup || (par.enable_mhd_floors && par.mhd))) return 0;
+  const bool mhd_floors = par.enable_mhd_floors && par.mhd;
+  const bool mhd = par.mhd != 0;
+  long long nfail = 0;
+#pragma omp parallel for collapse(2) schedule(dynamic, 4) reduction(+ : nfail)
+  for (int k = kb.s; k <= kb.e; k++)
+    for (int j = jb.s; j <= jb.e; j++)
+      for (int i = ib.s; i <= ib.e; i++) {
+        auto P = [&](int v) -> Real & { return B.P(v, k, j, i); };
+        auto U = [&](int v) -> Real & { return B.U(v, k, j, i); };
+        const Real x1 = B.Xc(1, i), x2 = B.Xc(2, j), x3 = B.Xc(3, k);
+        Real rho_floor, sie_floor;
+        bounds.GetFloors(x1, x2, x3, rho_floor, sie_floor);
+        Real gamma_max, e_max;
+        bounds.GetCeilings(x1, x2, x3, gamma_max, e_max);
+        Real bsqorho_max, bsqou_max;
+        bounds.GetMHDCeilings(x1, x2, x3, bsqorho_max, bsqou_max);
+        Real rho_floor_max = rho_floor;
+        Real u_floor_max = rho_floor * sie_floor;
+        bool floor_applied = false, ceiling_applied = false;
+        GeomPt g;
+        G.at(CENT, k, j, i, g);
+        if (mhd_floors) {
+          Real Bsq = 0.0, Bdotv = 0.0;
+          const Real vp[3] = {P(PHX_PVEL), P(PHX_PVEL + 1), P(PHX_PVEL + 2)};
+          const Real bp[3] = {P(PHX_PB), P(PHX_PB + 1), P(PHX_PB + 2)};
+          const Real W = GetLorentzFactor(vp, g.gcov);
+          const Real iW = 1.0 / W;
+          for (int ii = 0; ii < 3; ii++)
+            for (int jj = 0; jj < 3; jj++) {
+              Bsq += g.gcov[ii + 1][jj + 1] * bp[ii] * bp[jj];
+              Bdotv += g.gcov[ii + 1][jj + 1] * bp[ii] * vp[jj];
+            }
+          Real bcon0 = W * Bdotv / g.alpha;
+          const Real bsq = (Bsq + g.alpha * g.alpha * bcon0 * bcon0) * iW * iW;
+          rho_floor_max = std::max<Real>(rho_floor_max, bsq / bsqorho_max);
+          u_floor_max = std::max<Real>(u_floor_max, bsq / bsqou_max);
+          rho_floor_max = std::max<Real>(rho_floor_max, std::max<Real>(P(PHX_PENG), u_floor_max) / e_max);
+        }
+        Real drho = rho_floor_max - P(PHX_PRHO);
+        Real du = u_floor_max - P(PHX_PENG);
+        if (drho > 0. || du > 0.) {
+          floor_applied = true;
+          drho = std::max<Real>(drho, du / sie_floor);
+          du = std::max<Real>(du, sie_floor * drho);
+        }
+        Real bp[3] = {0, 0, 0};
+        if (mhd)
+          for (int ii = 0; ii < 3; ii++) bp[ii] = P(PHX_PB + ii);
+        Real dS[3], dB[3], dcrho, dtau;
+        if (floor_applied) {
+          Real vp_normalobs[3] = {0, 0, 0};
+          Real dprs = eos.PressureFromDensityInternalEnergy(drho, ratio(du, drho));
+          // BulkModulusFromDensityInternalEnergy = (gm1 + 1) gm1 rho sie
+          Real dgm1 = ratio(std::max(0.0, (eos.gm1 + 1) * eos.gm1 * drho * ratio(du, drho)), dprs);
+          p2c(drho, vp_normalobs, bp, du, dprs, dgm1, g.gcov, g.gamcon, g.beta, g.alpha, g.detgam, dcrho, dS, dB,
+              dtau, nullptr);
+          U(PHX_CRHO) += dcrho;
+          for (int ii = 0; ii < 3; ii++) U(PHX_CMOM + ii) += dS[ii];
+          U(PHX_CENG) += dtau;
+          C2PResult r = con2prim_zone(B, G, eos, bounds, par, k, j, i, 0.0, false);
+          if (!r.success) {
+            nfail++;
+            P(PHX_PRHO) = drho;
+            for (int ii = 0; ii < 3; ii++) P(PHX_PVEL + ii) = vp_normalobs[ii];
+            P(PHX_PENG) = du;
+            P(PHX_PTMP) = eos.TemperatureFromDensityInternalEnergy(P(PHX_PRHO), P(PHX_PENG) / P(PHX_PRHO));
+            Real Dn, taun;
+            p2c(drho, vp_normalobs, bp, du, dprs, dgm1, g.gcov, g.gamcon, g.beta, g.alpha, g.detgam, Dn, dS, dB,
+                taun, nullptr);
+            U(PHX_CRHO) = Dn;
+            U(PHX_CENG) = taun;
+            for (int ii = 0; ii < 3; ii++) U(PHX_CMOM + ii) = dS[ii];
+          }
+        }
+        Real vpcon[3] = {P(PHX_PVEL), P(PHX_PVEL + 1), P(PHX_PVEL + 2)};
+        const Real W = GetLorentzFactor(vpcon, g.gcov);
+        if (W > gamma_max || P(PHX_PENG) / P(PHX_PRHO) > e_max) ceiling_applied = true;
+        if (ceiling_applied) {
+          const Real rescale = std::sqrt(gamma_max * gamma_max - 1.) / (W * W - 1.);
+          for (int ii = 0; ii < 3; ii++) vpcon[ii] *= rescale;
+          for (int ii = 0; ii < 3; ii++) P(PHX_PVEL + ii) = vpcon[ii];
+          Real Dn, taun;
+          p2c(P(PHX_PRHO), vpcon, bp, P(PHX_PENG), P(PHX_PPRS), P(PHX_PGM1), g.gcov, g.gamcon, g.beta, g.alpha,
+              g.detgam, Dn, dS, dB, taun, nullptr);
+          U(PHX_CRHO) = Dn;
+          U(PHX_CENG) = taun;
+          for (int ii = 0; ii < 3; ii++) U(PHX_CMOM + ii) = dS[ii];
+        }
+        if (floor_applied || ceiling_applied) {
+          P(PHX_PTMP) = eos.TemperatureFromDensityInternalEnergy(P(PHX_PRHO), ratio(P(PHX_PENG), P(PHX_PRHO)));
+          P(PHX_PPRS) = eos.PressureFromDensityTemperature(P(PHX_PRHO), P(PHX_PTMP));
+          P(PHX_PGM1) = ratio(eos.BulkModulusFromDensityTemperature(P(PHX_PRHO), P(PHX_PTMP)), P(PHX_PPRS));
+        }
+      }
+  return nfail;
+}
 }  // namespace orc
 
 using namespace orc;
@@ -1506,6 +1685,12 @@ void orc_fmks_point(const phx_geometry *g, double X1, double X2, double X3, doub
   for (int a = 0; a < 3; a++)
     for (int b = a; b < 3; b++) out21[PHX_G_GAMCON + flatten2s(a, b)] = gi[a][b];
   out21[PHX_G_DETGAM] = f.DetGamma(X1, X2, X3);
+}
+
+void orc_c2p_fixup(const phx_params *par, const phx_block *blk) { c2p_fixup(*par, blk); }
+
+long long orc_apply_floors(const phx_params *par, const phx_block *blk, phx_range ib, phx_range jb, phx_range kb) {
+  return apply_floors(*par, blk, ib, jb, kb);
 }
 
 }  // extern "C"

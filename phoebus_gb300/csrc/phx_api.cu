@@ -425,14 +425,26 @@ phx_status phx_estimate_timestep(phx_ctx *ctx, const phx_params *p, const phx_bl
 }
 
 phx_status phx_c2p_fixup(phx_ctx *ctx, const phx_params *p, const phx_block *b, void *stream) {
-  (void)ctx; (void)p; (void)b; (void)stream;
-  return fail(PHX_ERR_UNSUPPORTED, "phx_c2p_fixup: not built yet");
+  phx_status s;
+  if ((s = ctx_device(ctx)) || (s = check_params(p))) return s;
+  phx::BView v;
+  if ((s = make_view(b, v))) return s;
+  if (!b->fail || !b->cell_sig) return fail(PHX_ERR_INVALID_ARG, "fail/cell_sig is NULL");
+  phx::launch_c2p_fixup(make_par(*p), v, S(stream));
+  return cuda_status("phx_c2p_fixup");
 }
 
 phx_status phx_apply_floors(phx_ctx *ctx, const phx_params *p, const phx_block *b, phx_range ib, phx_range jb,
                             phx_range kb, void *stream) {
-  (void)ctx; (void)p; (void)b; (void)ib; (void)jb; (void)kb; (void)stream;
-  return fail(PHX_ERR_UNSUPPORTED, "phx_apply_floors: not built yet");
+  phx_status s;
+  if ((s = ctx_device(ctx)) || (s = check_params(p))) return s;
+  phx::BView v;
+  if ((s = make_view(b, v))) return s;
+  if (!b->cell_sig) return fail(PHX_ERR_INVALID_ARG, "cell_sig is NULL");
+  phx::Range3 r;
+  if ((s = check_range(v, ib, jb, kb, r))) return s;
+  phx::launch_floors(make_par(*p), v, r, ctx->stats, ctx->err, S(stream));
+  return cuda_status("phx_apply_floors");
 }
 
 phx_status phx_geometry_fill_fmks(phx_ctx *ctx, const phx_geometry *g, const phx_block *b, void *stream) {
@@ -470,8 +482,12 @@ phx_status phx_stage(phx_ctx *ctx, const phx_params *p, const phx_block *b, cons
   vo.cons = cons_out;
   const float *w = use_learned_guess ? ctx->mlp_w : nullptr;
   phx::launch_c2p(par, vo, entire(vo), ctx->stats, ctx->err, w, st);  // FillDerived (MeshData)
+  phx::launch_c2p_fixup(par, vo, st);                                  // ConservedToPrimitiveFixup
+  phx::launch_floors(par, vo, entire(vo), ctx->stats, ctx->err, st);    // ApplyFloors
   phx::launch_ghost_periodic(vo, cons_out, p->mhd ? PHX_NCONS : 5, st);  // boundary exchange
   phx::launch_c2p(par, vo, entire(vo), ctx->stats, ctx->err, w, st);  // FillDerived (block)
+  phx::launch_c2p_fixup(par, vo, st);
+  phx::launch_floors(par, vo, entire(vo), ctx->stats, ctx->err, st);
   return cuda_status("phx_stage");
 }
 

@@ -124,6 +124,17 @@ class FluidContext:
                                                 out.data_ptr(), _stream(stream)))
         return out
 
+    def ConservedToPrimitiveFixup(self, p: abi.Params, b: Block, stream=None):
+        s = b.struct()
+        self._ok(self.lib.phx_c2p_fixup(self.h, C.byref(p), C.byref(s), _stream(stream)))
+
+    def ApplyFloors(self, p: abi.Params, b: Block, ib=None, jb=None, kb=None, stream=None):
+        e = b.entire()
+        ib, jb, kb = ib or e[0], jb or e[1], kb or e[2]
+        s = b.struct()
+        self._ok(self.lib.phx_apply_floors(self.h, C.byref(p), C.byref(s), _rng(ib), _rng(jb), _rng(kb),
+                                           _stream(stream)))
+
     def GeometryFillFMKS(self, b: Block, stream=None):
         assert b.geom is not None
         g = b.geom.struct()
