@@ -236,6 +236,32 @@ phx_status phx_con_to_prim_learned(phx_ctx *ctx, const phx_params *p, const phx_
                                    phx_range ib, phx_range jb, phx_range kb,
                                    void *stream);
 
+/* prim2con::p2c (prim2con.hpp:25-102) over a list of independent zones, the
+ * generator of con2prim inputs and training pairs.  prim[PHX_NPRIM][n] ->
+ * cons[PHX_NCONS][n]; geom[PHX_GEOM_NLOC][n] as below (NULL = Minkowski);
+ * cell_sig[3][n] may be NULL. */
+phx_status phx_prim_to_con_zones(phx_ctx *ctx, const phx_params *p, long long n, const double *prim,
+                                 const double *geom, double *cons, double *cell_sig, void *stream);
+
+/* con2prim over a list of independent zones with per-zone geometry (the
+ * isolated-zone form of ConservedToPrimitiveRobust used to benchmark the
+ * inversion itself).  Arrays are SoA with stride n: cons[PHX_NCONS][n] (read;
+ * rewritten where bounds were applied), prim[PHX_NPRIM][n] (c2p_mu read as the
+ * guess, the rest written), geom[PHX_GEOM_NLOC][n] (point geometry as in the
+ * cell-centre table; NULL = Minkowski), fail[n], cell_sig[3][n] (may be NULL), coords[3][n]
+ * (X1..X3 for the floors; may be NULL = 0).  learned = 1 takes the starting
+ * bracket from the loaded network (phx_mlp_set_weights). */
+phx_status phx_con_to_prim_zones(phx_ctx *ctx, const phx_params *p, long long n, double *cons,
+                                 double *prim, const double *geom, double *fail,
+                                 double *cell_sig, const double *coords, int learned,
+                                 void *stream);
+
+/* Point FMKS geometry for a list of zones at coordinates (X1, X2): writes
+ * geom[PHX_GEOM_NLOC][n] as phx_geometry_fill_fmks does for cell centres. */
+phx_status phx_geometry_fmks_points(phx_ctx *ctx, const phx_geometry *g, long long n,
+                                    const double *x1, const double *x2, double *geom,
+                                    void *stream);
+
 /* fluid::CalculateFluxes (fluid.cpp:659-773): reconstruction + LLF/HLL.
  * Writes flux(d, m) and face_sig(d) on every face the reference's divergence
  * and FluxCT read. */
@@ -334,9 +360,65 @@ phx_status phx_stage_batched(phx_ctx *ctx, const phx_params *p, const phx_block 
 #define PHX_MLP_NPARAM (PHX_MLP_IN * PHX_MLP_HID + PHX_MLP_HID + \
                         2 * (PHX_MLP_HID * PHX_MLP_HID + PHX_MLP_HID) + \
                         PHX_MLP_HID * PHX_MLP_OUT + PHX_MLP_OUT)
-/* Load FP32 master parameters (host memory, PHX_MLP_NPARAM floats). */
+/* Parameter order (weights [out][in]): W1[64][6], b1[64], W2[64][64], b2[64],
+ * W3[64][64], b3[64], W4[2][64], b4[2].  GELU (tanh form) after each hidden
+ * layer.  Outputs: o0 = predicted ln(mu), o1 = ln(sigma) of its error, mu the
+ * con2prim unknown 1 / (h W).  The learned start is the bracket
+ * [e^{o0 - 3 s}, e^{o0 + 3 s}] (s = e^{o1}, clipped to [0, 1]) around
+ * m = e^{o0}; the root find evaluates f(m), then the outer end of the half
+ * that should hold the root, and starts the reference's Illinois iterations
+ * from that half if it changes sign -- otherwise from the reference's own
+ * [0, 1] + guess start.  Inference multiplies BF16 weights and activations on
+ * the tensor cores with FP32 accumulation. */
+
+/* Load FP32 master parameters (host memory, PHX_MLP_NPARAM floats); resets
+ * the optimiser state. */
 phx_status phx_mlp_set_weights(phx_ctx *ctx, const float *params_host);
 phx_status phx_mlp_get_weights(phx_ctx *ctx, float *params_host);
+
+/* The 6 FP32 network inputs of independent zones, x[6][n] (device), from the
+ * con2prim setup invariants of cons/geom/coords as in
+ * phx_con_to_prim_zones: log10 q / 4, log10 r^2 / 4, log10 b^2 / 4,
+ * (b.r)^2 / (b^2 r^2), v0^2, log10 D / 8 (q = tau / D, r_i = S_i / D,
+ * b^i = B^i / sqrt(D)). */
+phx_status phx_mlp_features_zones(phx_ctx *ctx, const phx_params *p, long long n, const double *cons,
+                                  const double *geom, const double *coords, float *x, void *stream);
+
+/* Network outputs out[2][n] for inputs x[6][n] (device), on the tensor cores. */
+phx_status phx_mlp_forward(phx_ctx *ctx, long long n, const float *x, float *out, void *stream);
+
+/* The learned start (m, lo, hi) per zone, bracket[3][n] (device, NaN where
+ * the con2prim setup rejects the zone): what phx_con_to_prim_zones with
+ * learned = 1 starts its root find from. */
+phx_status phx_mlp_bracket_zones(phx_ctx *ctx, const phx_params *p, long long n, const double *cons,
+                                 const double *geom, const double *coords, double *bracket, void *stream);
+
+/* Mean loss over n samples and its gradient for the loaded parameters:
+ * grad[PHX_MLP_NPARAM] and loss[1] (device; overwritten).  x[6][n], y[n]
+ * (device) with y = ln(mu) of the exact primitive state.  Loss: Gaussian
+ * negative log-likelihood 0.5 (y - o0)^2 e^{-2 o1} + o1.  The forward pass
+ * multiplies BF16-rounded weights and inputs; the gradient passes straight
+ * through the rounding. */
+phx_status phx_mlp_loss_grad(phx_ctx *ctx, long long n, const float *x, const float *y, float *grad,
+                             float *loss, void *stream);
+
+typedef struct phx_mlp_train_opts {
+  int batch;          /* samples per step (a multiple of 64 is best)   */
+  int epochs;         /* passes over the n samples (in order)          */
+  float lr, lr_min;   /* cosine schedule from lr to lr_min             */
+  float beta1, beta2, eps, weight_decay; /* AdamW (decay on weights)   */
+} phx_mlp_train_opts;
+
+void phx_mlp_train_opts_default(phx_mlp_train_opts *o);
+
+#define PHX_MLP_MAX_EPOCHS 1024
+
+/* Train the loaded parameters on n samples (x[6][n], y[n], device) with
+ * AdamW, floor(n / batch) steps per epoch, on the GPU; then pack the
+ * parameters for inference.  epoch_loss (host, may be NULL) receives the mean
+ * training loss of each epoch.  Synchronises the stream. */
+phx_status phx_mlp_train(phx_ctx *ctx, long long n, const float *x, const float *y, const phx_mlp_train_opts *o,
+                         float *epoch_loss, void *stream);
 
 /* ---- measurement probe -------------------------------------------------- */
 /* Time a dependent-chain-free FP64 FMA loop and report FLOP/s (2 per FMA).

@@ -71,6 +71,14 @@ def lib() -> C.CDLL:
         L.orc_c2p_fixup.restype = None
         L.orc_apply_floors.argtypes = [P, B, R, R, R]
         L.orc_apply_floors.restype = C.c_longlong
+        L.orc_prim_to_con_zones.argtypes = [P, C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_prim_to_con_zones.restype = None
+        L.orc_con_to_prim_zones.argtypes = [P, C.c_longlong] + [C.c_void_p] * 11
+        L.orc_con_to_prim_zones.restype = C.c_longlong
+        L.orc_c2p_features_zones.argtypes = [P, C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_c2p_features_zones.restype = None
+        L.orc_fmks_points.argtypes = [C.POINTER(abi.Geometry), C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_fmks_points.restype = None
         _lib = L
     return _lib
 
@@ -155,6 +163,53 @@ class Oracle:
     def fmks_point(self, g, X1, X2, X3=0.0):
         out = np.zeros(abi.GEOM_NLOC)
         self.L.orc_fmks_point(C.byref(g), X1, X2, X3, out.ctypes.data)
+        return out
+
+    # ---- independent zones (arrays [var][n], C-contiguous float64)
+    @staticmethod
+    def _p(a):
+        if a is None:
+            return None
+        assert a.dtype == np.float64 and a.flags.c_contiguous
+        return a.ctypes.data
+
+    def PrimitiveToConservedZones(self, p, prim, geom=None, cons=None, cell_sig=None):
+        n = prim.shape[1]
+        if cons is None:
+            cons = np.zeros((abi.NCONS, n))
+        self.L.orc_prim_to_con_zones(C.byref(p), n, self._p(prim), self._p(geom), self._p(cons), self._p(cell_sig))
+        return cons
+
+    def ConservedToPrimitiveZones(self, p, cons, prim, geom=None, fail=None, cell_sig=None, coords=None,
+                                  iters=None, guess=None, bracket=None):
+        """In place on prim (and cons where bounds applied).  Returns the
+        number of unbracketed zones; self.last_evals = residual evaluations,
+        self.last_accepted = learned brackets accepted.  bracket: optional
+        [3][n] learned starts (m, lo, hi)."""
+        n = cons.shape[1]
+        if fail is None:
+            fail = np.zeros(n)
+        ev, acc = C.c_longlong(), C.c_longlong()
+        it = iters.ctypes.data if iters is not None else None
+        r = self.L.orc_con_to_prim_zones(C.byref(p), n, self._p(cons), self._p(prim), self._p(geom), self._p(fail),
+                                         self._p(cell_sig), self._p(coords), it, self._p(guess), self._p(bracket),
+                                         C.byref(ev), C.byref(acc))
+        self.last_evals = ev.value
+        self.last_accepted = acc.value
+        return r
+
+    def C2PFeaturesZones(self, p, cons, geom=None, coords=None):
+        """The learned start's FP32 inputs [6][n]."""
+        n = cons.shape[1]
+        x = np.zeros((abi.MLP_IN, n), dtype=np.float32)
+        self.L.orc_c2p_features_zones(C.byref(p), n, self._p(cons), self._p(geom), self._p(coords), x.ctypes.data)
+        return x
+
+    def fmks_points(self, g, x1, x2):
+        n = x1.shape[0]
+        out = np.zeros((abi.GEOM_NLOC, n))
+        self.L.orc_fmks_points(C.byref(g), n, self._p(np.ascontiguousarray(x1)), self._p(np.ascontiguousarray(x2)),
+                               out.ctypes.data)
         return out
 
     # ---- composite sequences (same order as the GPU host API)

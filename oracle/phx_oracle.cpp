@@ -624,6 +624,12 @@ struct RootFind {
     refine_bracket(func, guess, a, b, ya, yb);
     bracketed = !(ya * yb > 0.0);
     if (!bracketed) return guess;
+    return iterate(func, a, b, ya, yb, tol);
+  }
+  // The Illinois iterations of regula_falsi (root_find.hpp:120-166) from a
+  // sign-changing bracket [a, b] with f(a) = ya, f(b) = yb.
+  template <typename F>
+  Real iterate(F &func, Real a, Real b, Real ya, Real yb, Real tol) {
     Real sign = (ya < 0 ? 1.0 : -1.0);
     ya *= sign;
     yb *= sign;
@@ -660,6 +666,37 @@ struct RootFind {
       iteration_count++;
     }
     return 0.5 * (a + b);
+  }
+  // Learned starting bracket (no reference counterpart).  m: predicted root
+  // in [lo, hi] (all in [0, 1]).  f(m) picks the half that should hold the
+  // root (f < 0 below the root, > 0 above it); one more evaluation at that
+  // half's outer end checks the sign change.  Accepted: the same Illinois
+  // iterations from that half.  Rejected: the reference's own start from
+  // [0, 1] refined by guess.
+  template <typename F>
+  Real regula_falsi_learned(F &func, Real m, Real lo, Real hi, Real tol, Real guess, bool &bracketed,
+                            bool &accepted) {
+    accepted = false;
+    if (!(lo >= 0.0 && lo <= m && m <= hi && hi <= 1.0))  // not a usable bracket (e.g. NaN)
+      return regula_falsi(func, 0.0, 1.0, tol, guess, bracketed);
+    Real a, b, ya, yb;
+    const Real ym = func(m);
+    if (ym > 0.0) {
+      a = lo;
+      b = m;
+      yb = ym;
+      ya = func(lo);
+    } else {
+      a = m;
+      b = hi;
+      ya = ym;
+      yb = func(hi);
+    }
+    evals += 2;
+    accepted = ya * yb <= 0.0;
+    if (!accepted) return regula_falsi(func, 0.0, 1.0, tol, guess, bracketed);
+    bracketed = true;
+    return iterate(func, a, b, ya, yb, tol);
   }
 };
 
@@ -750,18 +787,41 @@ struct C2PResult {
   bool bracketed;
   int iterations;
   int evals;
+  bool learned_accepted;
 };
 
-// con2prim_robust.hpp:299-453 for one zone.  x1..x3: cell-centre coordinates.
-C2PResult con2prim_zone(const Blk &B, const Geom &G, const EOS &eos, const Bounds &bounds,
-                        const phx_params &par, int k, int j, int i, Real guess_override,
-                        bool use_override) {
-  C2PResult res{false, true, 0, 0};
-  auto P = [&](int v) -> Real & { return B.P(v, k, j, i); };
-  auto U = [&](int v) -> Real & { return B.U(v, k, j, i); };
-  const Real x1 = B.Xc(1, i), x2 = B.Xc(2, j), x3 = B.Xc(3, k);
-  GeomPt g;
-  G.at(CENT, k, j, i, g);
+// Inputs of the learned con2prim start (no reference counterpart): scale-free
+// invariants of the inversion, each mapped to O(1).  log10 arguments are
+// bounded below so that zero momentum or field give finite values.
+// The arithmetic after the FP64 setup is FP32, as on the device.
+inline void c2p_features(Real D, Real q, Real rsq, Real bsq, Real rbsq, Real v0sq, float f[PHX_MLP_IN]) {
+  f[0] = std::log10((float)std::max(q, 1e-12)) * 0.25f;
+  f[1] = std::log10((float)std::max(rsq, 1e-12)) * 0.25f;
+  f[2] = std::log10((float)std::max(bsq, 1e-12)) * 0.25f;
+  f[3] = (float)rbsq / std::max((float)bsq * (float)rsq, 1e-30f);
+  f[4] = (float)v0sq;
+  f[5] = std::log10((float)std::max(D, 1e-30)) * 0.125f;
+}
+
+// One zone's primitive and conserved values: P[v * vs], U[v * vs].
+struct ZoneRef {
+  Real *Pz, *Uz;
+  long long vs;
+  Real &P(int v) const { return Pz[v * vs]; }
+  Real &U(int v) const { return Uz[v * vs]; }
+};
+
+// con2prim_robust.hpp:299-453 for one zone, given its metric g and its
+// cell-centre coordinates x1..x3 (used by the floors).  guess: the starting
+// value of the regula-falsi (the stored c2p_mu in the reference).  sig gets
+// the three cell signal speeds.
+C2PResult con2prim_core(const GeomPt &g, const EOS &eos, const Bounds &bounds, const phx_params &par,
+                        Real x1, Real x2, Real x3, const ZoneRef &z, Real guess, Real sig[3],
+                        const Real *learned = nullptr) {
+  C2PResult res{false, true, 0, 0, false};
+  auto P = [&](int v) -> Real & { return z.P(v); };
+  auto U = [&](int v) -> Real & { return z.U(v); };
+  sig[0] = sig[1] = sig[2] = 0.0;
   const Real gdet = g.detgam, lapse = g.alpha;
   const bool mhd = par.mhd != 0;
 
@@ -807,9 +867,10 @@ C2PResult con2prim_zone(const Blk &B, const Geom &G, const EOS &eos, const Bound
   Residual resid(D, q, bsq, bsq_rpsq, rsq, rbsq, v0sq, eos, bounds, x1, x2, x3,
                  par.c2p_floor_scale_fac);
   RootFind root(par.c2p_max_iter);
-  const Real guess = use_override ? guess_override : P(PHX_PMU);
   bool bracketed = true;
-  const Real mu = root.regula_falsi(resid, 0.0, 1.0, par.c2p_tol, guess, bracketed);
+  const Real mu = learned ? root.regula_falsi_learned(resid, learned[0], learned[1], learned[2], par.c2p_tol,
+                                                      guess, bracketed, res.learned_accepted)
+                          : root.regula_falsi(resid, 0.0, 1.0, par.c2p_tol, guess, bracketed);
   res.bracketed = bracketed;
   res.iterations = root.iteration_count;
   res.evals = root.evals;
@@ -836,7 +897,6 @@ C2PResult con2prim_zone(const Blk &B, const Geom &G, const EOS &eos, const Bound
   if (mhd)
     for (int ii = 0; ii < 3; ii++) bu[ii] = P(PHX_PB + ii);
 
-  Real sig[3];
   if (resid.used_bounds()) {
     Real S[3], bcons[3];
     Real Dn, taun;
@@ -860,9 +920,6 @@ C2PResult con2prim_zone(const Blk &B, const Geom &G, const EOS &eos, const Bound
     signal_speeds(P(PHX_PRHO), P(PHX_PENG), P(PHX_PPRS), bsq, vel, vsq, P(PHX_PGM1), lapse,
                   g.beta, g.gamcon, sig);
   }
-  const int ndim = B.ndim;
-  for (int d = 0; d < ndim; d++) B.b->cell_sig[d * B.vs + B.idx(k, j, i)] = sig[d];
-
   num_nans = std::isnan(U(PHX_CRHO)) + std::isnan(U(PHX_CMOM)) + std::isnan(U(PHX_CENG));
   if (!bracketed) return res;
   if (num_nans > 0) return res;
@@ -871,6 +928,23 @@ C2PResult con2prim_zone(const Blk &B, const Geom &G, const EOS &eos, const Bound
   if (par.c2p_fail_on_ceilings && resid.used_gamma_max_) return res;
   res.success = true;
   return res;
+}
+
+// The zone (k, j, i) of a block: metric from the block's geometry, the
+// floors at the cell centre, cell_sig for the active dimensions.
+C2PResult con2prim_zone(const Blk &B, const Geom &G, const EOS &eos, const Bounds &bounds,
+                        const phx_params &par, int k, int j, int i, Real guess_override,
+                        bool use_override) {
+  GeomPt g;
+  G.at(CENT, k, j, i, g);
+  const long long id = B.idx(k, j, i);
+  const ZoneRef z{B.b->prim + id, B.b->cons + id, B.vs};
+  const Real guess = use_override ? guess_override : z.P(PHX_PMU);
+  Real sig[3];
+  C2PResult r = con2prim_core(g, eos, bounds, par, B.Xc(1, i), B.Xc(2, j), B.Xc(3, k), z, guess, sig);
+  if (r.evals == 0) return r;  // NaN input: nothing written (con2prim_robust.hpp:308-309)
+  for (int d = 0; d < B.ndim; d++) B.b->cell_sig[d * B.vs + id] = sig[d];
+  return r;
 }
 
 // ------------------------------------------------- reconstruction.hpp
@@ -1513,6 +1587,145 @@ long long orc_con_to_prim(const phx_params *par, const phx_block *blk, phx_range
       }
   if (evals_total) *evals_total = ev;
   return unbr;
+}
+
+// Point geometry of zone q from geom [21][n] (null = Minkowski).
+static void zone_geom(const double *geom, long long n, long long q, GeomPt &g) {
+  if (!geom) {
+    Geom(nullptr, nullptr).at(CENT, 0, 0, 0, g);
+    return;
+  }
+  g.alpha = geom[PHX_G_ALPHA * n + q];
+  for (int d = 0; d < 3; d++) g.beta[d] = geom[(PHX_G_BETA + d) * n + q];
+  for (int mu = 0; mu < 4; mu++)
+    for (int nu = 0; nu < 4; nu++) g.gcov[mu][nu] = geom[(PHX_G_GCOV + flatten2(mu, nu)) * n + q];
+  for (int a = 0; a < 3; a++)
+    for (int b = 0; b < 3; b++) g.gamcon[a][b] = geom[(PHX_G_GAMCON + flatten2s(a, b)) * n + q];
+  g.detgam = geom[PHX_G_DETGAM * n + q];
+}
+
+// prim2con.hpp:25-102 over n independent zones (prim [12][n] -> cons [8][n]).
+void orc_prim_to_con_zones(const phx_params *par, long long n, const double *prim, const double *geom,
+                           double *cons, double *cell_sig) {
+  const bool mhd = par->mhd != 0;
+#pragma omp parallel for schedule(static)
+  for (long long q = 0; q < n; q++) {
+    GeomPt g;
+    zone_geom(geom, n, q, g);
+    auto P = [&](int v) { return prim[v * n + q]; };
+    Real S[3], bcons[3], sig[3];
+    const Real vel[] = {P(PHX_PVEL), P(PHX_PVEL + 1), P(PHX_PVEL + 2)};
+    Real bp[3] = {0.0, 0.0, 0.0};
+    if (mhd)
+      for (int d = 0; d < 3; ++d) bp[d] = P(PHX_PB + d);
+    Real D, tau;
+    p2c(P(PHX_PRHO), vel, bp, P(PHX_PENG), P(PHX_PPRS), P(PHX_PGM1), g.gcov, g.gamcon, g.beta, g.alpha, g.detgam,
+        D, S, bcons, tau, sig);
+    cons[PHX_CRHO * n + q] = D;
+    cons[PHX_CENG * n + q] = tau;
+    for (int d = 0; d < 3; ++d) cons[(PHX_CMOM + d) * n + q] = S[d];
+    if (mhd)
+      for (int d = 0; d < 3; ++d) cons[(PHX_CB + d) * n + q] = bcons[d];
+    if (cell_sig)
+      for (int d = 0; d < 3; d++) cell_sig[d * n + q] = sig[d];
+  }
+}
+
+// con2prim over n independent zones: cons/prim [var][n], geom [21][n] per
+// zone (null = Minkowski), coords [3][n] (null = 0; used by the floors),
+// fail [n], cell_sig [3][n] (null = not written).  The same per-zone
+// inversion as a block zone.  bracket [3][n] (optional): a learned start
+// (m, lo, hi) per zone for RootFind::regula_falsi_learned.
+long long orc_con_to_prim_zones(const phx_params *par, long long n, double *cons, double *prim,
+                                const double *geom, double *fail, double *cell_sig,
+                                const double *coords, int *iters, const double *guess,
+                                const double *bracket, long long *evals_total, long long *accepted_total) {
+  Bounds bounds(*par);
+  EOS eos{par->gm1, par->Cv};
+  long long unbr = 0, ev = 0, acc = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : unbr, ev, acc)
+  for (long long q = 0; q < n; q++) {
+    GeomPt g;
+    zone_geom(geom, n, q, g);
+    const ZoneRef z{prim + q, cons + q, n};
+    const Real x1 = coords ? coords[q] : 0.0, x2 = coords ? coords[n + q] : 0.0,
+               x3 = coords ? coords[2 * n + q] : 0.0;
+    Real sig[3];
+    Real lb[3];
+    if (bracket)
+      for (int c = 0; c < 3; c++) lb[c] = bracket[c * n + q];
+    C2PResult r = con2prim_core(g, eos, bounds, *par, x1, x2, x3, z, guess ? guess[q] : z.P(PHX_PMU), sig,
+                                bracket ? lb : nullptr);
+    acc += r.learned_accepted;
+    if (r.evals > 0 && cell_sig)
+      for (int d = 0; d < 3; d++) cell_sig[d * n + q] = sig[d];
+    fail[q] = r.success ? 1.0 : 0.0;
+    if (iters) iters[q] = r.iterations;
+    if (!r.bracketed) unbr++;
+    ev += r.evals;
+  }
+  if (evals_total) *evals_total = ev;
+  if (accepted_total) *accepted_total = acc;
+  return unbr;
+}
+
+void orc_fmks_point(const phx_geometry *g, double X1, double X2, double X3, double *out21);
+
+// The 6 FP32 inputs of the learned con2prim start, from the same setup
+// quantities as con2prim_robust.hpp:303-366 (D, q, r^2, b^2, (b.r)^2, v0^2).
+// Mirrors c2p_features on the device; no reference counterpart.
+void orc_c2p_features_zones(const phx_params *par, long long n, const double *cons, const double *geom,
+                            const double *coords, float *x) {
+  Bounds bounds(*par);
+#pragma omp parallel for schedule(static)
+  for (long long q = 0; q < n; q++) {
+    GeomPt g;
+    zone_geom(geom, n, q, g);
+    auto U = [&](int v) { return cons[v * n + q]; };
+    const Real x1 = coords ? coords[q] : 0.0, x2 = coords ? coords[n + q] : 0.0,
+               x3 = coords ? coords[2 * n + q] : 0.0;
+    const Real igdet = 1.0 / g.detgam;
+    Real rhoflr = 0.0, epsflr;
+    bounds.GetFloors(x1, x2, x3, rhoflr, epsflr);
+    rhoflr *= par->c2p_floor_scale_fac;
+    Real gam_max, eps_max;
+    bounds.GetCeilings(x1, x2, x3, gam_max, eps_max);
+    const Real D = U(PHX_CRHO) * igdet;
+    const Real qq = ratio(U(PHX_CENG) * igdet, D);
+    Real rcov[] = {ratio(U(PHX_CMOM), U(PHX_CRHO)), ratio(U(PHX_CMOM + 1), U(PHX_CRHO)),
+                   ratio(U(PHX_CMOM + 2), U(PHX_CRHO))};
+    Real rsq = 0.0, bsq = 0.0, bdotr = 0.0;
+    for (int ii = 0; ii < 3; ii++) {
+      Real rc = 0.0;
+      for (int jj = 0; jj < 3; jj++) rc += g.gamcon[ii][jj] * rcov[jj];
+      rsq += rc * rcov[ii];
+    }
+    if (par->mhd) {
+      Real bu[3];
+      const Real sD = 1.0 / std::sqrt(std::max(D, rhoflr));
+      for (int ii = 0; ii < 3; ii++) {
+        bu[ii] = U(PHX_CB + ii) * igdet * sD;
+        bdotr += bu[ii] * rcov[ii];
+      }
+      for (int ii = 0; ii < 3; ii++)
+        for (int jj = 0; jj < 3; jj++) bsq += g.gcov[ii + 1][jj + 1] * bu[ii] * bu[jj];
+      bsq = std::max(0.0, bsq);
+    }
+    const Real v0sq = std::min(rsq / (1.0 + rsq), 1.0 - 1.0 / (gam_max * gam_max));
+    float f[PHX_MLP_IN];
+    c2p_features(D, qq, rsq, bsq, bdotr * bdotr, v0sq, f);
+    for (int c = 0; c < PHX_MLP_IN; c++) x[c * n + q] = f[c];
+  }
+}
+
+// FMKS metric at n points (X1[q], X2[q]) into geom [21][n].
+void orc_fmks_points(const phx_geometry *g, long long n, const double *x1, const double *x2, double *geom) {
+#pragma omp parallel for schedule(static)
+  for (long long q = 0; q < n; q++) {
+    double out[PHX_GEOM_NLOC];
+    orc_fmks_point(g, x1[q], x2[q], 0.0, out);
+    for (int v = 0; v < PHX_GEOM_NLOC; v++) geom[v * n + q] = out[v];
+  }
 }
 
 void orc_calculate_fluxes(const phx_params *par, const phx_block *blk) {

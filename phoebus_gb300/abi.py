@@ -77,6 +77,20 @@ class C2PStats(C.Structure):
                 ("learned_accepted", C.c_ulonglong), ("hist", C.c_ulonglong * C2P_HIST)]
 
 
+class MlpTrainOpts(C.Structure):
+    _fields_ = [("batch", C.c_int), ("epochs", C.c_int), ("lr", C.c_float), ("lr_min", C.c_float),
+                ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float), ("weight_decay", C.c_float)]
+
+
+def default_train_opts(**over) -> MlpTrainOpts:
+    # same defaults as phx_mlp_train_opts_default
+    o = MlpTrainOpts(batch=4096, epochs=10, lr=3e-3, lr_min=0.0, beta1=0.9, beta2=0.999, eps=1e-8,
+                     weight_decay=1e-4)
+    for k, v in over.items():
+        setattr(o, k, v)
+    return o
+
+
 class PhxError(RuntimeError):
     """Raised when an entry point returns a non-OK phx_status."""
 
@@ -102,6 +116,15 @@ _SIGS = {
     "phx_prim_to_con": (C.c_int, [_P, C.POINTER(Params), C.POINTER(BlockS), Range, Range, Range, _P]),
     "phx_con_to_prim": (C.c_int, [_P, C.POINTER(Params), C.POINTER(BlockS), Range, Range, Range, _P]),
     "phx_con_to_prim_learned": (C.c_int, [_P, C.POINTER(Params), C.POINTER(BlockS), Range, Range, Range, _P]),
+    "phx_mlp_features_zones": (C.c_int, [_P, C.POINTER(Params), C.c_longlong, _P, _P, _P, _P, _P]),
+    "phx_mlp_forward": (C.c_int, [_P, C.c_longlong, _P, _P, _P]),
+    "phx_mlp_bracket_zones": (C.c_int, [_P, C.POINTER(Params), C.c_longlong, _P, _P, _P, _P, _P]),
+    "phx_mlp_loss_grad": (C.c_int, [_P, C.c_longlong, _P, _P, _P, _P, _P]),
+    "phx_mlp_train_opts_default": (None, [C.POINTER(MlpTrainOpts)]),
+    "phx_mlp_train": (C.c_int, [_P, C.c_longlong, _P, _P, C.POINTER(MlpTrainOpts), _P, _P]),
+    "phx_prim_to_con_zones": (C.c_int, [_P, C.POINTER(Params), C.c_longlong, _P, _P, _P, _P, _P]),
+    "phx_con_to_prim_zones": (C.c_int, [_P, C.POINTER(Params), C.c_longlong, _P, _P, _P, _P, _P, _P, C.c_int, _P]),
+    "phx_geometry_fmks_points": (C.c_int, [_P, C.POINTER(Geometry), C.c_longlong, _P, _P, _P, _P]),
     "phx_calculate_fluxes": (C.c_int, [_P, C.POINTER(Params), C.POINTER(BlockS), _P]),
     "phx_flux_ct": (C.c_int, [_P, C.POINTER(Params), C.POINTER(BlockS), _P]),
     "phx_calculate_fluid_source_terms": (C.c_int, [_P, C.POINTER(Params), C.POINTER(BlockS), C.c_int, _P]),

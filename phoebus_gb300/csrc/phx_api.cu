@@ -3,20 +3,25 @@
 // Host-side validation, parameter resolution (the fixup package defaults of
 // fixup.cpp:120-180), and dispatch to the kernels.  All calls are
 // asynchronous on the caller's stream; nothing is allocated per call.
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <string>
 
-#include "phx_kernels.cuh"
+#include "phx_mlp.cuh"
 
 struct phx_ctx {
   int device;
   phx::DevStats *stats;        // device
   unsigned int *err;           // device sticky error word
   unsigned long long *dt_scr;  // device scratch for the dt reduction
-  float *mlp_w;                // device FP32 parameters of the learned guess (or null)
+  float *mlp_w;                // device FP32 master parameters of the learned start
+  float *mlp_grad, *mlp_m, *mlp_v;  // device gradient and AdamW moments
+  float *mlp_loss;             // device per-epoch loss sums [PHX_MLP_MAX_EPOCHS]
+  phx::MlpPacked *mlp_packed;  // device BF16 fragments for inference
+  long long mlp_step;          // AdamW step count
   int mlp_loaded;
 };
 
@@ -260,7 +265,12 @@ phx_status phx_ctx_create(int device, phx_ctx **out) {
   if (cudaMalloc(&c->stats, sizeof(phx::DevStats)) != cudaSuccess ||
       cudaMalloc(&c->err, sizeof(unsigned int)) != cudaSuccess ||
       cudaMalloc(&c->dt_scr, sizeof(unsigned long long)) != cudaSuccess ||
-      cudaMalloc(&c->mlp_w, sizeof(float) * PHX_MLP_NPARAM) != cudaSuccess) {
+      cudaMalloc(&c->mlp_w, sizeof(float) * PHX_MLP_NPARAM) != cudaSuccess ||
+      cudaMalloc(&c->mlp_grad, sizeof(float) * PHX_MLP_NPARAM) != cudaSuccess ||
+      cudaMalloc(&c->mlp_m, sizeof(float) * PHX_MLP_NPARAM) != cudaSuccess ||
+      cudaMalloc(&c->mlp_v, sizeof(float) * PHX_MLP_NPARAM) != cudaSuccess ||
+      cudaMalloc(&c->mlp_loss, sizeof(float) * PHX_MLP_MAX_EPOCHS) != cudaSuccess ||
+      cudaMalloc(&c->mlp_packed, sizeof(phx::MlpPacked)) != cudaSuccess) {
     phx_status s = cuda_status("cudaMalloc");
     phx_ctx_destroy(c);
     return s;
@@ -268,6 +278,10 @@ phx_status phx_ctx_create(int device, phx_ctx **out) {
   cudaMemset(c->stats, 0, sizeof(phx::DevStats));
   cudaMemset(c->err, 0, sizeof(unsigned int));
   cudaMemset(c->mlp_w, 0, sizeof(float) * PHX_MLP_NPARAM);
+  cudaMemset(c->mlp_grad, 0, sizeof(float) * PHX_MLP_NPARAM);
+  cudaMemset(c->mlp_m, 0, sizeof(float) * PHX_MLP_NPARAM);
+  cudaMemset(c->mlp_v, 0, sizeof(float) * PHX_MLP_NPARAM);
+  cudaMemset(c->mlp_packed, 0, sizeof(phx::MlpPacked));
   phx_status s = cuda_status("ctx init");
   if (s != PHX_OK) {
     phx_ctx_destroy(c);
@@ -284,6 +298,11 @@ phx_status phx_ctx_destroy(phx_ctx *ctx) {
   cudaFree(ctx->err);
   cudaFree(ctx->dt_scr);
   cudaFree(ctx->mlp_w);
+  cudaFree(ctx->mlp_grad);
+  cudaFree(ctx->mlp_m);
+  cudaFree(ctx->mlp_v);
+  cudaFree(ctx->mlp_loss);
+  cudaFree(ctx->mlp_packed);
   delete ctx;
   return PHX_OK;
 }
@@ -336,7 +355,7 @@ static phx_status c2p_common(phx_ctx *ctx, const phx_params *p, const phx_block 
   phx::Range3 r;
   if ((s = check_range(v, ib, jb, kb, r))) return s;
   if (learned && !ctx->mlp_loaded) return fail(PHX_ERR_INVALID_ARG, "no learned-guess weights loaded");
-  phx::launch_c2p(make_par(*p), v, r, ctx->stats, ctx->err, learned ? ctx->mlp_w : nullptr, S(stream));
+  phx::launch_c2p(make_par(*p), v, r, ctx->stats, ctx->err, learned ? ctx->mlp_packed : nullptr, S(stream));
   return cuda_status("phx_con_to_prim");
 }
 
@@ -348,6 +367,43 @@ phx_status phx_con_to_prim(phx_ctx *ctx, const phx_params *p, const phx_block *b
 phx_status phx_con_to_prim_learned(phx_ctx *ctx, const phx_params *p, const phx_block *b,
                                    phx_range ib, phx_range jb, phx_range kb, void *stream) {
   return c2p_common(ctx, p, b, ib, jb, kb, stream, true);
+}
+
+phx_status phx_prim_to_con_zones(phx_ctx *ctx, const phx_params *p, long long n, const double *prim,
+                                 const double *geom, double *cons, double *cell_sig, void *stream) {
+  phx_status s;
+  if ((s = ctx_device(ctx)) || (s = check_params(p))) return s;
+  if (n < 0) return fail(PHX_ERR_INVALID_ARG, "n < 0");
+  if (n == 0) return PHX_OK;
+  if (!cons || !prim) return fail(PHX_ERR_INVALID_ARG, "cons/prim is NULL");
+  phx::launch_p2c_zones(make_par(*p), n, prim, geom, cons, cell_sig, S(stream));
+  return cuda_status("phx_prim_to_con_zones");
+}
+
+phx_status phx_con_to_prim_zones(phx_ctx *ctx, const phx_params *p, long long n, double *cons, double *prim,
+                                 const double *geom, double *fail_flag, double *cell_sig, const double *coords,
+                                 int learned, void *stream) {
+  phx_status s;
+  if ((s = ctx_device(ctx)) || (s = check_params(p))) return s;
+  if (n < 0) return fail(PHX_ERR_INVALID_ARG, "n < 0");
+  if (n == 0) return PHX_OK;
+  if (!cons || !prim || !fail_flag) return fail(PHX_ERR_INVALID_ARG, "cons/prim/fail is NULL");
+  if (learned && !ctx->mlp_loaded) return fail(PHX_ERR_INVALID_ARG, "no learned-guess weights loaded");
+  phx::launch_c2p_zones(make_par(*p), n, cons, prim, geom, fail_flag, cell_sig, coords, ctx->stats, ctx->err,
+                        learned ? ctx->mlp_packed : nullptr, S(stream));
+  return cuda_status("phx_con_to_prim_zones");
+}
+
+phx_status phx_geometry_fmks_points(phx_ctx *ctx, const phx_geometry *g, long long n, const double *x1,
+                                    const double *x2, double *geom, void *stream) {
+  phx_status s;
+  if ((s = ctx_device(ctx))) return s;
+  if (!g || g->kind != PHX_GEOM_FMKS) return fail(PHX_ERR_INVALID_ARG, "geometry must be FMKS");
+  if (n < 0) return fail(PHX_ERR_INVALID_ARG, "n < 0");
+  if (n == 0) return PHX_OK;
+  if (!x1 || !x2 || !geom) return fail(PHX_ERR_INVALID_ARG, "x1/x2/geom is NULL");
+  phx::launch_geom_points(*g, n, x1, x2, geom, S(stream));
+  return cuda_status("phx_geometry_fmks_points");
 }
 
 phx_status phx_calculate_fluxes(phx_ctx *ctx, const phx_params *p, const phx_block *b, void *stream) {
@@ -480,7 +536,7 @@ phx_status phx_stage(phx_ctx *ctx, const phx_params *p, const phx_block *b, cons
   phx::launch_update(par, v, cons_base, cons_out, beta, dt, st);
   phx::BView vo = v;  // the stage result: con2prim reads cons_out
   vo.cons = cons_out;
-  const float *w = use_learned_guess ? ctx->mlp_w : nullptr;
+  const phx::MlpPacked *w = use_learned_guess ? ctx->mlp_packed : nullptr;
   phx::launch_c2p(par, vo, entire(vo), ctx->stats, ctx->err, w, st);  // FillDerived (MeshData)
   phx::launch_c2p_fixup(par, vo, st);                                  // ConservedToPrimitiveFixup
   phx::launch_floors(par, vo, entire(vo), ctx->stats, ctx->err, st);    // ApplyFloors
@@ -505,6 +561,107 @@ phx_status phx_mlp_set_weights(phx_ctx *ctx, const float *params_host) {
   if (!params_host) return fail(PHX_ERR_INVALID_ARG, "params is NULL");
   if (cudaMemcpy(ctx->mlp_w, params_host, sizeof(float) * PHX_MLP_NPARAM, cudaMemcpyHostToDevice) != cudaSuccess)
     return cuda_status("mlp weights");
+  cudaMemset(ctx->mlp_grad, 0, sizeof(float) * PHX_MLP_NPARAM);
+  cudaMemset(ctx->mlp_m, 0, sizeof(float) * PHX_MLP_NPARAM);
+  cudaMemset(ctx->mlp_v, 0, sizeof(float) * PHX_MLP_NPARAM);
+  ctx->mlp_step = 0;
+  phx::launch_mlp_pack(ctx->mlp_w, ctx->mlp_packed, 0);
+  if ((s = cuda_status("mlp pack"))) return s;
+  if (cudaDeviceSynchronize() != cudaSuccess) return cuda_status("mlp pack");
+  ctx->mlp_loaded = 1;
+  return PHX_OK;
+}
+
+void phx_mlp_train_opts_default(phx_mlp_train_opts *o) {
+  o->batch = 4096;
+  o->epochs = 10;
+  o->lr = 3e-3f;
+  o->lr_min = 0.0f;
+  o->beta1 = 0.9f;
+  o->beta2 = 0.999f;
+  o->eps = 1e-8f;
+  o->weight_decay = 1e-4f;
+}
+
+phx_status phx_mlp_features_zones(phx_ctx *ctx, const phx_params *p, long long n, const double *cons,
+                                  const double *geom, const double *coords, float *x, void *stream) {
+  phx_status s;
+  if ((s = ctx_device(ctx)) || (s = check_params(p))) return s;
+  if (n < 0) return fail(PHX_ERR_INVALID_ARG, "n < 0");
+  if (n == 0) return PHX_OK;
+  if (!cons || !x) return fail(PHX_ERR_INVALID_ARG, "cons/x is NULL");
+  phx::launch_mlp_features(make_par(*p), n, cons, geom, coords, x, S(stream));
+  return cuda_status("phx_mlp_features_zones");
+}
+
+phx_status phx_mlp_forward(phx_ctx *ctx, long long n, const float *x, float *out, void *stream) {
+  phx_status s;
+  if ((s = ctx_device(ctx))) return s;
+  if (n < 0) return fail(PHX_ERR_INVALID_ARG, "n < 0");
+  if (n == 0) return PHX_OK;
+  if (!x || !out) return fail(PHX_ERR_INVALID_ARG, "x/out is NULL");
+  if (!ctx->mlp_loaded) return fail(PHX_ERR_INVALID_ARG, "no learned-guess weights loaded");
+  phx::launch_mlp_forward(ctx->mlp_packed, n, x, out, ctx->err, S(stream));
+  return cuda_status("phx_mlp_forward");
+}
+
+phx_status phx_mlp_bracket_zones(phx_ctx *ctx, const phx_params *p, long long n, const double *cons,
+                                 const double *geom, const double *coords, double *bracket, void *stream) {
+  phx_status s;
+  if ((s = ctx_device(ctx)) || (s = check_params(p))) return s;
+  if (n < 0) return fail(PHX_ERR_INVALID_ARG, "n < 0");
+  if (n == 0) return PHX_OK;
+  if (!cons || !bracket) return fail(PHX_ERR_INVALID_ARG, "cons/bracket is NULL");
+  if (!ctx->mlp_loaded) return fail(PHX_ERR_INVALID_ARG, "no learned-guess weights loaded");
+  phx::launch_mlp_bracket(make_par(*p), n, cons, geom, coords, ctx->mlp_packed, bracket, ctx->err, S(stream));
+  return cuda_status("phx_mlp_bracket_zones");
+}
+
+phx_status phx_mlp_loss_grad(phx_ctx *ctx, long long n, const float *x, const float *y, float *grad, float *loss,
+                             void *stream) {
+  phx_status s;
+  if ((s = ctx_device(ctx))) return s;
+  if (n <= 0) return fail(PHX_ERR_INVALID_ARG, "n must be positive");
+  if (!x || !y || !grad || !loss) return fail(PHX_ERR_INVALID_ARG, "x/y/grad/loss is NULL");
+  cudaStream_t st = S(stream);
+  cudaMemsetAsync(grad, 0, sizeof(float) * PHX_MLP_NPARAM, st);
+  cudaMemsetAsync(loss, 0, sizeof(float), st);
+  phx::launch_mlp_grad(ctx->mlp_w, x, y, n, 0, n, (float)(1.0 / (double)n), grad, loss, st);
+  return cuda_status("phx_mlp_loss_grad");
+}
+
+phx_status phx_mlp_train(phx_ctx *ctx, long long n, const float *x, const float *y, const phx_mlp_train_opts *o,
+                         float *epoch_loss, void *stream) {
+  phx_status s;
+  if ((s = ctx_device(ctx))) return s;
+  if (!x || !y || !o) return fail(PHX_ERR_INVALID_ARG, "x/y/opts is NULL");
+  if (o->batch <= 0 || o->epochs <= 0) return fail(PHX_ERR_INVALID_ARG, "batch and epochs must be positive");
+  if (o->epochs > PHX_MLP_MAX_EPOCHS) return fail(PHX_ERR_CAPACITY, "epochs > PHX_MLP_MAX_EPOCHS");
+  const long long steps = n / o->batch;
+  if (steps <= 0) return fail(PHX_ERR_INVALID_ARG, "n smaller than one batch");
+  cudaStream_t st = S(stream);
+  cudaMemsetAsync(ctx->mlp_loss, 0, sizeof(float) * o->epochs, st);
+  const long long total = steps * o->epochs;
+  const float inv_b = (float)(1.0 / (double)o->batch);
+  long long t = 0;
+  for (int e = 0; e < o->epochs; e++)
+    for (long long k = 0; k < steps; k++, t++) {
+      phx::launch_mlp_grad(ctx->mlp_w, x, y, n, k * o->batch, o->batch, inv_b, ctx->mlp_grad, ctx->mlp_loss + e, st);
+      const long long step = ++ctx->mlp_step;
+      const double lr = o->lr_min + 0.5 * (o->lr - o->lr_min) * (1.0 + cos(M_PI * (double)t / (double)total));
+      const double c1 = 1.0 / (1.0 - pow((double)o->beta1, (double)step));
+      const double c2 = 1.0 / (1.0 - pow((double)o->beta2, (double)step));
+      phx::launch_mlp_adamw(ctx->mlp_w, ctx->mlp_grad, ctx->mlp_m, ctx->mlp_v, (float)lr, o->beta1, o->beta2, o->eps,
+                            o->weight_decay, (float)c1, (float)c2, st);
+    }
+  phx::launch_mlp_pack(ctx->mlp_w, ctx->mlp_packed, st);
+  if ((s = cuda_status("phx_mlp_train"))) return s;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return cuda_status("phx_mlp_train");
+  if (epoch_loss) {
+    if (cudaMemcpy(epoch_loss, ctx->mlp_loss, sizeof(float) * o->epochs, cudaMemcpyDeviceToHost) != cudaSuccess)
+      return cuda_status("phx_mlp_train");
+    for (int e = 0; e < o->epochs; e++) epoch_loss[e] /= (float)steps;
+  }
   ctx->mlp_loaded = 1;
   return PHX_OK;
 }

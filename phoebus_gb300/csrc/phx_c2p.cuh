@@ -102,6 +102,7 @@ struct C2POut {
   bool success;
   bool bracketed;
   bool nan_input;
+  bool learned;  // the learned start was accepted
 };
 
 // Setup of the inversion (con2prim_robust.hpp:303-366).  Returns false when
@@ -182,17 +183,66 @@ __device__ __forceinline__ bool c2p_setup(const Par &p, const Pt &g, const doubl
   return true;
 }
 
+// Inputs of the learned con2prim start (no reference counterpart): scale-free
+// invariants of the inversion from the setup quantities, mapped to O(1) in
+// FP32: log10 q / 4, log10 r^2 / 4, log10 b^2 / 4, (b.r)^2 / (b^2 r^2),
+// v0^2, log10 D / 8 (log10 arguments bounded below by 1e-12, 1e-30).
+__device__ __forceinline__ void c2p_features(const Residual &r, float f[6]) {
+  f[0] = log10f((float)fmax(r.q, 1e-12)) * 0.25f;
+  f[1] = log10f((float)fmax(r.rsq, 1e-12)) * 0.25f;
+  f[2] = log10f((float)fmax(r.bsq, 1e-12)) * 0.25f;
+  f[3] = (float)r.rbsq / fmaxf((float)r.bsq * (float)r.rsq, 1e-30f);
+  f[4] = (float)r.v0sq;
+  f[5] = log10f((float)fmax(r.D, 1e-30)) * 0.125f;
+}
+
 // refine_bracket + regula_falsi (root_find.hpp:42-58, 110-167), vote-driven.
 // valid = this lane owns a zone.  Returns mu; iterations/evals/bracketed
 // through out.  lo/hi: starting bracket ([0, 1] in the reference).
+// LEARNED: lb = (m, lo, hi), a predicted root and bracket in [0, 1].  f(m)
+// picks the half that should hold the root (f < 0 below it, > 0 above), one
+// more evaluation checks that half's sign change; when it holds, the same
+// Illinois iterations start from that half, otherwise from the reference's
+// own start.  A bracket that is not ordered inside [0, 1] (e.g. NaN) is not
+// tried.
+template <bool LEARNED = false>
 __device__ __forceinline__ double regula_falsi_warp(const Par &p, Residual &res, bool valid,
-                                                   double a, double b, double guess, C2POut &out) {
+                                                   double a, double b, double guess, C2POut &out,
+                                                   const double *lb = nullptr) {
   const double tol = p.c2p_tol;
   const int max_iter = p.c2p_max_iter;
   double ya = 0.0, yb = 0.0;
   int evals = 0;
   bool bracketed = true;
-  if (valid) {
+  bool started = false;
+  out.learned = false;
+  if constexpr (LEARNED) {
+    if (valid && lb[1] >= 0.0 && lb[1] <= lb[0] && lb[0] <= lb[2] && lb[2] <= 1.0) {
+      double la, lbb, lya, lyb;
+      const double ym = res(p, lb[0]);
+      if (ym > 0.0) {
+        la = lb[1];
+        lbb = lb[0];
+        lyb = ym;
+        lya = res(p, la);
+      } else {
+        la = lb[0];
+        lbb = lb[2];
+        lya = ym;
+        lyb = res(p, lbb);
+      }
+      evals += 2;
+      if (lya * lyb <= 0.0) {
+        a = la;
+        b = lbb;
+        ya = lya;
+        yb = lyb;
+        started = true;
+        out.learned = true;
+      }
+    }
+  }
+  if (valid && !started) {
     if (a <= guess && b >= guess) {
       ya = res(p, guess);
       yb = res(p, b);

@@ -201,6 +201,22 @@ __device__ __forceinline__ void load_pt(const BView &b, int loc, int j, int i, P
   p.detgam = __ldg(t + PHX_G_DETGAM * pitch + off);
 }
 
+// Point geometry of zone q from a [PHX_GEOM_NLOC][pitch] table.
+__device__ __forceinline__ void load_pt_flat(const double *t, long long pitch, long long q, Pt &p) {
+  p.alpha = __ldg(t + PHX_G_ALPHA * pitch + q);
+#pragma unroll
+  for (int d = 0; d < 3; d++) p.beta[d] = __ldg(t + (PHX_G_BETA + d) * pitch + q);
+#pragma unroll
+  for (int m = 0; m < 4; m++)
+#pragma unroll
+    for (int n = 0; n < 4; n++) p.gcov[m][n] = __ldg(t + (PHX_G_GCOV + flat2(m, n)) * pitch + q);
+#pragma unroll
+  for (int m = 0; m < 3; m++)
+#pragma unroll
+    for (int n = 0; n < 3; n++) p.gamcon[m][n] = __ldg(t + (PHX_G_GAMCON + flat2(m, n)) * pitch + q);
+  p.detgam = __ldg(t + PHX_G_DETGAM * pitch + q);
+}
+
 // sum_{m,n} gcov[m+1][n+1] a[m] b[n], in the reference's loop order.
 template <bool MINK>
 __device__ __forceinline__ double dot_sp(const Pt &g, const double a[3], const double b[3]) {

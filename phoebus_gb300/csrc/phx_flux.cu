@@ -15,6 +15,7 @@
 // directions [s-1, e+1].  These are all the faces FluxDivergence, FluxCT and
 // EstimateTimestep read.
 #include "phx_kernels.cuh"
+#include "phx_bulk.cuh"
 
 namespace phx {
 
@@ -66,38 +67,8 @@ __device__ __forceinline__ void face_flux(const Par &p, const BView &b, int k, i
 }
 
 // ------------------------------------------------------------------ X1
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-               "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned phase) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(phase)
-      : "memory");
-  return ok != 0;
-}
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_u32(dst)),
-      "l"(src), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
-}
-
 constexpr int X1_WARPS = 4;    // warps per CTA
 constexpr int X1_PENCILS = 4;  // (k, j) pencils staged per CTA
-constexpr long long MBAR_SPIN_LIMIT = 1ll << 26;
 
 // A CTA stages X1_PENCILS pencils (10 primitive rows each) in shared memory
 // with TMA bulk copies completing on one mbarrier.  Its warps then walk the

@@ -236,7 +236,13 @@ __global__ void k_geom_deriv(FmksDev f, double x01, double dx1, double x02, doub
   }
 }
 
-void launch_geom_fmks(const phx_geometry &g, const BView &b, cudaStream_t s) {
+__global__ void k_geom_points(FmksDev f, long long n, const double *x1, const double *x2, double *t) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  f.point(x1[q], x2[q], t + q, n);
+}
+
+static FmksDev make_fmks(const phx_geometry &g) {
   FmksDev f;
   f.a = g.a;
   f.a2 = g.a * g.a;
@@ -250,6 +256,19 @@ void launch_geom_fmks(const phx_geometry &g, const BView &b, cudaStream_t s) {
   f.hexp_csq = g.hexp_csq;
   f.derefine_poles = g.derefine_poles;
   f.norm = 0.5 * M_PI * 1. / (1. + 1. / (f.alpha + 1.) * 1. / pow(f.xt, f.alpha));
+  return f;
+}
+
+void launch_geom_points(const phx_geometry &g, long long n, const double *x1, const double *x2, double *geom,
+                        cudaStream_t s) {
+  if (n <= 0) return;
+  const FmksDev f = make_fmks(g);
+  const int T = 128;
+  k_geom_points<<<(unsigned)((n + T - 1) / T), T, 0, s>>>(f, n, x1, x2, geom);
+}
+
+void launch_geom_fmks(const phx_geometry &g, const BView &b, cudaStream_t s) {
+  const FmksDev f = make_fmks(g);
   const int T = 128;
   auto grid = [&](long long n) { return (unsigned)((n + T - 1) / T); };
   const int n1t = b.n1t, n2t = b.n2t;

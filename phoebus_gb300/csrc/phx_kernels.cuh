@@ -17,19 +17,14 @@ struct DevStats {  // mirrors phx_c2p_stats
   unsigned long long hist[PHX_C2P_HIST];
 };
 
-// Optional learned starting bracket: per-zone [lo, hi] computed by the MLP.
-struct LearnedBracket {
-  const float *w;  // FP32 master parameters (PHX_MLP_NPARAM), or null
-  const void *wbf16;  // packed BF16 operand tiles for the tensor-core path
-};
-
 struct Range3 {
   int is, ie, js, je, ks, ke;
 };
 
 void launch_p2c(const Par &p, const BView &b, Range3 r, cudaStream_t s);
+struct MlpPacked;
 void launch_c2p(const Par &p, const BView &b, Range3 r, DevStats *stats, unsigned int *err,
-                const float *mlp_w, cudaStream_t s);
+                const MlpPacked *mlp, cudaStream_t s);
 void launch_fluxes(const Par &p, const BView &b, cudaStream_t s);
 void launch_fluxct(const BView &b, cudaStream_t s);
 void launch_sources(const Par &p, const BView &b, cudaStream_t s);
@@ -42,6 +37,25 @@ void launch_c2p_fixup(const Par &p, const BView &b, cudaStream_t s);
 void launch_floors(const Par &p, const BView &b, Range3 r, DevStats *stats, unsigned int *err,
                    cudaStream_t s);
 void launch_geom_fmks(const phx_geometry &g, const BView &b, cudaStream_t s);
+void launch_geom_points(const phx_geometry &g, long long n, const double *x1, const double *x2, double *geom,
+                        cudaStream_t s);
+void launch_p2c_zones(const Par &p, long long n, const double *prim, const double *geom, double *cons,
+                      double *cell_sig, cudaStream_t s);
+void launch_c2p_zones(const Par &p, long long n, double *cons, double *prim, const double *geom, double *fail,
+                      double *cell_sig, const double *coords, DevStats *stats, unsigned int *err,
+                      const MlpPacked *mlp, cudaStream_t s);
+void launch_mlp_bracket(const Par &p, long long n, const double *cons, const double *geom, const double *coords,
+                        const MlpPacked *mlp, double *bracket, unsigned int *err, cudaStream_t s);
+// learned-start network (phx_mlp.cu)
+void launch_mlp_pack(const float *theta, MlpPacked *out, cudaStream_t s);
+void launch_mlp_features(const Par &p, long long n, const double *cons, const double *geom, const double *coords,
+                         float *x, cudaStream_t s);
+void launch_mlp_forward(const MlpPacked *mlp, long long n, const float *x, float *out, unsigned int *err,
+                        cudaStream_t s);
+void launch_mlp_grad(const float *theta, const float *x, const float *y, long long stride, long long off,
+                     long long count, float inv_batch, float *grad, float *loss, cudaStream_t s);
+void launch_mlp_adamw(float *theta, float *grad, float *m, float *v, float lr, float b1, float b2, float eps,
+                      float wd, float c1, float c2, cudaStream_t s);
 void launch_fp64_probe(double *out, int iters, cudaStream_t s, int *nthreads_out);
 
 }  // namespace phx

@@ -30,6 +30,22 @@ def _stream(stream):
     return getattr(stream, "cuda_stream", stream)
 
 
+def _tp(t):
+    """Device pointer of a contiguous float64 CUDA tensor (None -> NULL)."""
+    if t is None:
+        return None
+    if not t.is_cuda or not t.is_contiguous() or t.dtype.itemsize != 8:
+        raise ValueError("expected a contiguous 8-byte CUDA tensor")
+    return t.data_ptr()
+
+
+def _tp4(t):
+    """Device pointer of a contiguous float32 CUDA tensor."""
+    if not t.is_cuda or not t.is_contiguous() or t.dtype.itemsize != 4:
+        raise ValueError("expected a contiguous 4-byte CUDA tensor")
+    return t.data_ptr()
+
+
 def _rng(r):
     return abi.Range(int(r[0]), int(r[1]))
 
@@ -86,6 +102,98 @@ class FluidContext:
         s = b.struct()
         fn = self.lib.phx_con_to_prim_learned if learned else self.lib.phx_con_to_prim
         self._ok(fn(self.h, C.byref(p), C.byref(s), _rng(ib), _rng(jb), _rng(kb), _stream(stream)))
+
+    # ---- independent zones: torch CUDA float64 tensors [var][n]
+    def PrimitiveToConservedZones(self, p: abi.Params, prim, geom=None, cons=None, cell_sig=None, stream=None):
+        import torch
+
+        n = prim.shape[1]
+        if cons is None:
+            cons = torch.zeros((abi.NCONS, n), dtype=torch.float64, device=prim.device)
+        self._ok(self.lib.phx_prim_to_con_zones(self.h, C.byref(p), n, _tp(prim), _tp(geom), _tp(cons),
+                                                _tp(cell_sig), _stream(stream)))
+        return cons
+
+    def ConservedToPrimitiveZones(self, p: abi.Params, cons, prim, geom=None, fail=None, cell_sig=None,
+                                  coords=None, learned=False, stream=None):
+        import torch
+
+        n = cons.shape[1]
+        if fail is None:
+            fail = torch.zeros(n, dtype=torch.float64, device=cons.device)
+        self._ok(self.lib.phx_con_to_prim_zones(self.h, C.byref(p), n, _tp(cons), _tp(prim), _tp(geom), _tp(fail),
+                                                _tp(cell_sig), _tp(coords), int(learned), _stream(stream)))
+        return fail
+
+    # ---- learned con2prim start
+    def mlp_set_weights(self, theta):
+        import numpy as np
+
+        t = np.ascontiguousarray(theta, dtype=np.float32)
+        assert t.size == abi.MLP_NPARAM
+        self._ok(self.lib.phx_mlp_set_weights(self.h, t.ctypes.data_as(C.POINTER(C.c_float))))
+
+    def mlp_get_weights(self):
+        import numpy as np
+
+        t = np.zeros(abi.MLP_NPARAM, dtype=np.float32)
+        self._ok(self.lib.phx_mlp_get_weights(self.h, t.ctypes.data_as(C.POINTER(C.c_float))))
+        return t
+
+    def MLPFeaturesZones(self, p: abi.Params, cons, geom=None, coords=None, x=None, stream=None):
+        import torch
+
+        n = cons.shape[1]
+        if x is None:
+            x = torch.empty((abi.MLP_IN, n), dtype=torch.float32, device=cons.device)
+        self._ok(self.lib.phx_mlp_features_zones(self.h, C.byref(p), n, _tp(cons), _tp(geom), _tp(coords),
+                                                 _tp4(x), _stream(stream)))
+        return x
+
+    def MLPForward(self, x, out=None, stream=None):
+        import torch
+
+        n = x.shape[1]
+        if out is None:
+            out = torch.empty((abi.MLP_OUT, n), dtype=torch.float32, device=x.device)
+        self._ok(self.lib.phx_mlp_forward(self.h, n, _tp4(x), _tp4(out), _stream(stream)))
+        return out
+
+    def MLPBracketZones(self, p: abi.Params, cons, geom=None, coords=None, out=None, stream=None):
+        import torch
+
+        n = cons.shape[1]
+        if out is None:
+            out = torch.empty((3, n), dtype=torch.float64, device=cons.device)
+        self._ok(self.lib.phx_mlp_bracket_zones(self.h, C.byref(p), n, _tp(cons), _tp(geom), _tp(coords),
+                                                _tp(out), _stream(stream)))
+        return out
+
+    def MLPLossGrad(self, x, y, stream=None):
+        import torch
+
+        grad = torch.empty(abi.MLP_NPARAM, dtype=torch.float32, device=x.device)
+        loss = torch.empty(1, dtype=torch.float32, device=x.device)
+        self._ok(self.lib.phx_mlp_loss_grad(self.h, x.shape[1], _tp4(x), _tp4(y), _tp4(grad), _tp4(loss),
+                                            _stream(stream)))
+        return loss, grad
+
+    def MLPTrain(self, x, y, opts: abi.MlpTrainOpts | None = None, stream=None):
+        """Returns the mean training loss of each epoch."""
+        opts = opts or abi.default_train_opts()
+        out = (C.c_float * opts.epochs)()
+        self._ok(self.lib.phx_mlp_train(self.h, x.shape[1], _tp4(x), _tp4(y), C.byref(opts), out, _stream(stream)))
+        return list(out)
+
+    def GeometryFMKSPoints(self, g: abi.Geometry, x1, x2, geom=None, stream=None):
+        import torch
+
+        n = x1.shape[0]
+        if geom is None:
+            geom = torch.empty((abi.GEOM_NLOC, n), dtype=torch.float64, device=x1.device)
+        self._ok(self.lib.phx_geometry_fmks_points(self.h, C.byref(g), n, _tp(x1), _tp(x2), _tp(geom),
+                                                   _stream(stream)))
+        return geom
 
     def CalculateFluxes(self, p: abi.Params, b: Block, stream=None):
         s = b.struct()

@@ -50,6 +50,11 @@ def test_library_loads_without_gpu(built):
     for name in ("hslope", "poly_xt", "poly_alpha", "smooth", "hexp_br", "derefine_poles"):
         assert getattr(g, name) == getattr(gr, name), name
     assert lib.phx_status_string(2) == b"con2prim root not bracketed"
+    o = abi.MlpTrainOpts()
+    lib.phx_mlp_train_opts_default(o)
+    ref_o = abi.default_train_opts()
+    for name, _ in abi.MlpTrainOpts._fields_:
+        assert getattr(o, name) == getattr(ref_o, name), name
 
 
 def test_struct_sizes_match_header(built, tmp_path):
@@ -59,7 +64,7 @@ def test_struct_sizes_match_header(built, tmp_path):
 
     src = tmp_path / "sz.c"
     fields = {"phx_params": abi.Params, "phx_block": abi.BlockS, "phx_geometry": abi.Geometry,
-              "phx_c2p_stats": abi.C2PStats}
+              "phx_c2p_stats": abi.C2PStats, "phx_mlp_train_opts": abi.MlpTrainOpts}
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void){"]
     for cname, cls in fields.items():
         lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
