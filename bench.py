@@ -18,6 +18,11 @@ RK2 timestep per second.
   cpu_baseline  the oracle (CPU restatement of the reference path) timed on
              a 64^3 sample of the same state with all host threads
 
+  c2p        con2prim over 5e7 independent FMKS Kerr-Schild zones at tolerance
+             1e-10: zones/s and root-find iterations with the reference's
+             start (plain) and with the learned start (network trained on
+             the GPU on 1e7 separately seeded pairs before timing)
+
 --impl reference runs the reference's CPU path (the oracle port) on the host
 cores: each step is one RK2 timestep of a 64^3 sample of the same state.
 Multi-GPU: independent replicas (one block per rank, weak scaling); the only
@@ -39,8 +44,24 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "GRMHD zone-updates/s on 1 GB300; con2prim zones/s learned-guess vs plain @1e-10"
 UNIT = "zone-updates/s"
-LAUNCHES_PER_STAGE = 10  # sources 1, fluxes 3, FluxCT 2, update 1, con2prim 2, ghosts 1
 LAUNCHES_DT = 3
+
+
+def c2p_launches(nzones: int, learned: bool = False) -> int:
+    """Kernel launches of one con2prim call: per chunk of C2P_CHUNK zones a
+    root-find launch and a retry launch (plus the bracket launch when
+    learned)."""
+    from phoebus_gb300 import abi
+
+    chunks = -(-nzones // abi.C2P_CHUNK)
+    return chunks * (3 if learned else 2)
+
+
+def stage_launches(n: int, ng: int = 4) -> int:
+    """Kernel launches of one RK stage on an n^3 periodic MHD block without
+    floors or fixups: sources 1, fluxes 3, FluxCT 2, update 1, ghosts 1, and
+    two con2prim calls over the entire block."""
+    return 8 + 2 * c2p_launches((n + 2 * ng) ** 3)
 
 
 def parse():
@@ -54,6 +75,10 @@ def parse():
     a.add_argument("--exact", action="store_true", help="time the parity (no-FMA) build")
     a.add_argument("--no-e2e", action="store_true")
     a.add_argument("--no-cpu", action="store_true")
+    a.add_argument("--no-c2p", action="store_true", help="skip the con2prim learned-vs-plain section")
+    a.add_argument("--c2p-zones", type=float, default=5e7)
+    a.add_argument("--train-pairs", type=float, default=1e7)
+    a.add_argument("--train-epochs", type=int, default=10)
     return a.parse_args()
 
 
@@ -160,6 +185,79 @@ def flux_bytes(n, ng=4):
     cells = n1t * t * t  # stencil cells per direction (full pencil, +-1 layer)
     faces = (n + 1) * t * t
     return 3 * (10 * cells + 9 * faces) * 8
+
+
+def bench_c2p(ctx, args, dev):
+    """Independent-zone con2prim at tolerance 1e-10 on seeded FMKS Kerr-Schild
+    zones (spin 0.9375): zones/s and FP64 root-find iterations per zone with
+    the reference's start (plain) and with the learned start, the network
+    trained first on the GPU on separately seeded pairs.  Each timed run
+    starts from c2p_mu = 0 (the plain start's guess) and the pristine
+    conserved state; the state (about 18 GB for 5e7 zones) is far larger
+    than L2."""
+    import torch
+
+    from phoebus_gb300 import abi, learned, states
+
+    N = int(args.c2p_zones)
+    p = abi.default_params(gm1=1.0 / 3.0)
+    p.c2p_tol, p.c2p_max_iter = 1e-10, 100
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    opts = abi.default_train_opts(epochs=args.train_epochs)
+    losses = learned.train(ctx, p, n=int(args.train_pairs), opts=opts, device=dev)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    prim = torch.empty((abi.NPRIM, N), dtype=torch.float64, device=dev)
+    cons = torch.empty((abi.NCONS, N), dtype=torch.float64, device=dev)
+    geom = torch.empty((abi.GEOM_NLOC, N), dtype=torch.float64, device=dev)
+    chunk = 10_000_000
+    for s0 in range(0, N, chunk):
+        m = min(chunk, N - s0)
+        pr, co, ge = learned.kerr_zone_set(ctx, p, m, states.SEED + 4, dev, start=s0)
+        prim[:, s0:s0 + m] = pr
+        cons[:, s0:s0 + m] = co
+        geom[:, s0:s0 + m] = ge
+        del pr, co, ge
+    cons0 = cons.clone()
+    fail = torch.empty(N, dtype=torch.float64, device=dev)
+    sig = torch.empty((3, N), dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream()
+    out = {}
+    for name, lrn in (("plain", False), ("learned", True)):
+        times = []
+        for rep in range(4):  # one untimed warm-up, three timed
+            prim[abi.PMU].zero_()
+            cons.copy_(cons0)
+            ctx.c2p_stats(reset=True)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ctx.ConservedToPrimitiveZones(p, cons, prim, geom, fail=fail, cell_sig=sig, learned=lrn)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if rep:
+                times.append(e0.elapsed_time(e1))
+            st = ctx.c2p_stats(reset=True)
+        ctx.check()
+        ms = sorted(times)[len(times) // 2]
+        out[name] = {"zones_per_s": N / (ms * 1e-3), "ms": ms, "iterations_per_zone": st["iterations"] / N,
+                     "residual_evals_per_zone": st["residual_evals"] / N, "failures": st["failures"],
+                     "unbracketed": st["unbracketed"], "gpu_launches": c2p_launches(N, lrn)}
+        if lrn:
+            out[name]["learned_accepted_frac"] = st["learned_accepted"] / N
+    del prim, cons, geom, cons0, fail, sig
+    torch.cuda.empty_cache()
+    out["learned_over_plain"] = out["learned"]["zones_per_s"] / out["plain"]["zones_per_s"]
+    out["zones"] = N
+    out["tolerance"] = 1e-10
+    out["workload"] = ("independent zones, FMKS Kerr-Schild a=0.9375 (no pole derefinement), r in [1.5, 50], "
+                       "theta in (0, pi), log10 rho in [-6, 0], log10 u/rho in [-4, 1], W in [1, 10], "
+                       "sigma in [1e-4, 1e2], ideal gas Gamma 4/3; cons from the library's prim2con")
+    out["training"] = {"pairs": int(args.train_pairs), "epochs": args.train_epochs, "batch": opts.batch,
+                       "seconds": t_train, "final_loss": losses[-1], "first_epoch_loss": losses[0],
+                       "optimizer": "AdamW, cosine lr 3e-3 -> 0"}
+    return out
 
 
 def cpu_baseline(args, threads):
@@ -331,6 +429,7 @@ def main():
         e2e = {"value": ws * zones / (ems * 1e-3), "unit": UNIT, "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb,
                "ms_per_step": ems}
     ctx.check()
+    c2p = None if args.no_c2p else bench_c2p(ctx, args, dev)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
@@ -354,10 +453,11 @@ def main():
                          "peak_source": peak_src, "algorithmic_bytes": fb, "launch_ms": flux_ms,
                          "note": "FP64-pipe bound on GB300; see fp64"},
             "fp64": fp64,
+            "c2p": c2p,
             "cpu_baseline": cpu,
             "clocks": clocks,
             "e2e": e2e,
-            "gpu_launches": args.steps * (2 * LAUNCHES_PER_STAGE + LAUNCHES_DT),
+            "gpu_launches": args.steps * (2 * stage_launches(n) + LAUNCHES_DT),
         }
         print(json.dumps(out), flush=True)
     ctx.close()

@@ -26,6 +26,7 @@ G_ALPHA, G_BETA, G_GCOV, G_GAMCON, G_DETGAM, GEOM_NLOC = 0, 1, 4, 14, 20, 21
 GD_DALPHA, GD_DG, GEOM_NDER = 0, 3, 33
 C2P_HIST = 128
 MLP_IN, MLP_HID, MLP_OUT = 6, 64, 2
+C2P_CHUNK = 1 << 21  # zones per con2prim chunk inside the library (launch accounting only)
 MLP_NPARAM = MLP_IN * MLP_HID + MLP_HID + 2 * (MLP_HID * MLP_HID + MLP_HID) + MLP_HID * 2 + 2
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "con2prim root not bracketed", 3: "NaN input",

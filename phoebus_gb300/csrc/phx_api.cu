@@ -21,6 +21,8 @@ struct phx_ctx {
   float *mlp_grad, *mlp_m, *mlp_v;  // device gradient and AdamW moments
   float *mlp_loss;             // device per-epoch loss sums [PHX_MLP_MAX_EPOCHS]
   phx::MlpPacked *mlp_packed;  // device BF16 fragments for inference
+  phx::C2PScratch c2p;         // device con2prim chunk scratch (brackets, retry list)
+  void *c2p_mem;               // its single allocation
   long long mlp_step;          // AdamW step count
   int mlp_loaded;
 };
@@ -168,6 +170,32 @@ phx::Range3 interior(const phx::BView &v) {
 
 inline cudaStream_t S(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// The con2prim chunk scratch as one allocation, 256-byte aligned pieces.
+size_t c2p_scratch_bytes() {
+  const size_t C = (size_t)phx::C2P_CHUNK;
+  return 256 * 9 + sizeof(double) * (3 * C + 4 * C) + sizeof(int) * (1 + C) + sizeof(unsigned long long) * C;
+}
+
+phx::C2PScratch c2p_scratch_carve(void *mem) {
+  const size_t C = (size_t)phx::C2P_CHUNK;
+  char *p = static_cast<char *>(mem);
+  auto take = [&](size_t bytes) {
+    char *r = p;
+    p += (bytes + 255) & ~size_t(255);
+    return r;
+  };
+  phx::C2PScratch s;
+  s.brk = reinterpret_cast<double *>(take(sizeof(double) * 3 * C));
+  s.count = reinterpret_cast<int *>(take(sizeof(int)));
+  s.idx = reinterpret_cast<int *>(take(sizeof(int) * C));
+  s.a = reinterpret_cast<double *>(take(sizeof(double) * C));
+  s.b = reinterpret_cast<double *>(take(sizeof(double) * C));
+  s.ya = reinterpret_cast<double *>(take(sizeof(double) * C));
+  s.yb = reinterpret_cast<double *>(take(sizeof(double) * C));
+  s.packed = reinterpret_cast<unsigned long long *>(take(sizeof(unsigned long long) * C));
+  return s;
+}
+
 phx_status ctx_device(phx_ctx *ctx) {
   if (!ctx) return fail(PHX_ERR_INVALID_ARG, "ctx is NULL");
   int cur = -1;
@@ -270,7 +298,8 @@ phx_status phx_ctx_create(int device, phx_ctx **out) {
       cudaMalloc(&c->mlp_m, sizeof(float) * PHX_MLP_NPARAM) != cudaSuccess ||
       cudaMalloc(&c->mlp_v, sizeof(float) * PHX_MLP_NPARAM) != cudaSuccess ||
       cudaMalloc(&c->mlp_loss, sizeof(float) * PHX_MLP_MAX_EPOCHS) != cudaSuccess ||
-      cudaMalloc(&c->mlp_packed, sizeof(phx::MlpPacked)) != cudaSuccess) {
+      cudaMalloc(&c->mlp_packed, sizeof(phx::MlpPacked)) != cudaSuccess ||
+      cudaMalloc(&c->c2p_mem, c2p_scratch_bytes()) != cudaSuccess) {
     phx_status s = cuda_status("cudaMalloc");
     phx_ctx_destroy(c);
     return s;
@@ -282,6 +311,7 @@ phx_status phx_ctx_create(int device, phx_ctx **out) {
   cudaMemset(c->mlp_m, 0, sizeof(float) * PHX_MLP_NPARAM);
   cudaMemset(c->mlp_v, 0, sizeof(float) * PHX_MLP_NPARAM);
   cudaMemset(c->mlp_packed, 0, sizeof(phx::MlpPacked));
+  c->c2p = c2p_scratch_carve(c->c2p_mem);
   phx_status s = cuda_status("ctx init");
   if (s != PHX_OK) {
     phx_ctx_destroy(c);
@@ -303,6 +333,7 @@ phx_status phx_ctx_destroy(phx_ctx *ctx) {
   cudaFree(ctx->mlp_v);
   cudaFree(ctx->mlp_loss);
   cudaFree(ctx->mlp_packed);
+  cudaFree(ctx->c2p_mem);
   delete ctx;
   return PHX_OK;
 }
@@ -355,7 +386,8 @@ static phx_status c2p_common(phx_ctx *ctx, const phx_params *p, const phx_block 
   phx::Range3 r;
   if ((s = check_range(v, ib, jb, kb, r))) return s;
   if (learned && !ctx->mlp_loaded) return fail(PHX_ERR_INVALID_ARG, "no learned-guess weights loaded");
-  phx::launch_c2p(make_par(*p), v, r, ctx->stats, ctx->err, learned ? ctx->mlp_packed : nullptr, S(stream));
+  phx::launch_c2p(make_par(*p), v, r, ctx->stats, ctx->err, learned ? ctx->mlp_packed : nullptr, ctx->c2p,
+                  S(stream));
   return cuda_status("phx_con_to_prim");
 }
 
@@ -390,7 +422,7 @@ phx_status phx_con_to_prim_zones(phx_ctx *ctx, const phx_params *p, long long n,
   if (!cons || !prim || !fail_flag) return fail(PHX_ERR_INVALID_ARG, "cons/prim/fail is NULL");
   if (learned && !ctx->mlp_loaded) return fail(PHX_ERR_INVALID_ARG, "no learned-guess weights loaded");
   phx::launch_c2p_zones(make_par(*p), n, cons, prim, geom, fail_flag, cell_sig, coords, ctx->stats, ctx->err,
-                        learned ? ctx->mlp_packed : nullptr, S(stream));
+                        learned ? ctx->mlp_packed : nullptr, ctx->c2p, S(stream));
   return cuda_status("phx_con_to_prim_zones");
 }
 
@@ -537,11 +569,11 @@ phx_status phx_stage(phx_ctx *ctx, const phx_params *p, const phx_block *b, cons
   phx::BView vo = v;  // the stage result: con2prim reads cons_out
   vo.cons = cons_out;
   const phx::MlpPacked *w = use_learned_guess ? ctx->mlp_packed : nullptr;
-  phx::launch_c2p(par, vo, entire(vo), ctx->stats, ctx->err, w, st);  // FillDerived (MeshData)
+  phx::launch_c2p(par, vo, entire(vo), ctx->stats, ctx->err, w, ctx->c2p, st);  // FillDerived (MeshData)
   phx::launch_c2p_fixup(par, vo, st);                                  // ConservedToPrimitiveFixup
   phx::launch_floors(par, vo, entire(vo), ctx->stats, ctx->err, st);    // ApplyFloors
   phx::launch_ghost_periodic(vo, cons_out, p->mhd ? PHX_NCONS : 5, st);  // boundary exchange
-  phx::launch_c2p(par, vo, entire(vo), ctx->stats, ctx->err, w, st);  // FillDerived (block)
+  phx::launch_c2p(par, vo, entire(vo), ctx->stats, ctx->err, w, ctx->c2p, st);  // FillDerived (block)
   phx::launch_c2p_fixup(par, vo, st);
   phx::launch_floors(par, vo, entire(vo), ctx->stats, ctx->err, st);
   return cuda_status("phx_stage");

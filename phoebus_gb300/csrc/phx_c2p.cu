@@ -2,6 +2,8 @@
 // (fluid.cpp:368-449 PrimitiveToConservedRegion, fluid.cpp:477-517
 // ConservedToPrimitiveRobust).  One zone per thread over the index box; the
 // con2prim loop exits on a warp vote.
+#include <cstdlib>
+
 #include "phx_mlp.cuh"
 
 namespace phx {
@@ -107,9 +109,12 @@ void launch_p2c_zones(const Par &p, long long n, const double *prim, const doubl
 // ----------------------------------------------------------- con2prim
 // One generic kernel over "zone accessors": a block index box (the
 // reference's ConservedToPrimitiveRegion) or a list of independent zones with
-// per-zone geometry.  LEARNED fuses the learned start: per warp, the setup
-// invariants of its 32 zones go through the tensor-core network, and the
-// resulting bracket starts the unchanged FP64 root find.
+// per-zone geometry.  The learned start runs as two kernels per chunk of
+// zones: k_mlp_bracket (setup invariants -> tensor-core network -> bracket
+// (m, lo, hi), 24 bytes per zone in a context scratch) and k_c2p<LEARNED>,
+// whose unchanged FP64 root find starts from that bracket.  Keeping the
+// network out of the root-find kernel keeps that kernel's instruction
+// footprint small (fused, the two codes thrashed the instruction cache).
 constexpr int C2P_THREADS = 128;
 constexpr int C2P_WARPS = C2P_THREADS / 32;
 
@@ -169,7 +174,7 @@ struct ListZones {
     x1 = coords ? coords[t] : 0.0;
     x2 = coords ? coords[n + t] : 0.0;
     x3 = coords ? coords[2 * n + t] : 0.0;
-    guess = prim[PHX_PMU * n + t];
+    guess = prim ? prim[PHX_PMU * n + t] : 0.0;
   }
   __device__ __forceinline__ void store(long long id, const Par &p, const double pr[PHX_NPRIM],
                                         const double U[PHX_NCONS], bool used_bounds, const double sig[3]) const {
@@ -191,145 +196,322 @@ struct ListZones {
   __device__ __forceinline__ void store_fail(long long id, double f) const { fail[id] = f; }
 };
 
-// Shared memory of the learned variant: packed weights + per-warp scratch.
-struct C2PLearnedSmem {
+// The learned start of zones t0 .. t0 + count - 1 into brk[3][count]
+// (NaN where the setup rejects the zone).  CTAs stage the packed weights
+// once and walk chunks of 128 zones; each warp runs the network for its 32.
+struct BracketSmem {
   MlpPacked w;
   uint32_t xs[C2P_WARPS][128];
   float os[C2P_WARPS][64];
 };
 
-// CTAs walk chunks of C2P_THREADS zones (grid-stride); with LEARNED the
-// weights are staged once per CTA.
-template <class Z, bool MINK, bool LEARNED>
-__global__ void __launch_bounds__(C2P_THREADS) k_c2p(Par p, Z zones, long long ntot, const MlpPacked *mlp,
-                                                      DevStats *stats, unsigned int *err) {
-  extern __shared__ __align__(16) unsigned char c2p_dyn[];
+template <class Z, bool MINK>
+__global__ void __launch_bounds__(C2P_THREADS) k_mlp_bracket(Par p, Z zones, long long t0, long long count,
+                                                             const MlpPacked *mlp, double *brk, unsigned int *err) {
+  extern __shared__ __align__(16) unsigned char brk_dyn[];
   __shared__ __align__(8) uint64_t bar;
+  BracketSmem *S = reinterpret_cast<BracketSmem *>(brk_dyn);
+  if (!mlp_stage_weights(&S->w, mlp, &bar, err)) return;
+  const int warp = threadIdx.x >> 5;
+  for (long long base = (long long)blockIdx.x * C2P_THREADS; base < count;
+       base += (long long)gridDim.x * C2P_THREADS) {
+    const long long q = base + threadIdx.x;
+    float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    bool ok = false;
+    if (q < count) {
+      long long id;
+      Pt g{};
+      double U[PHX_NCONS], x1, x2, x3, guess;
+      zones.template load<MINK>(t0 + q, id, g, U, x1, x2, x3, guess);
+      Residual res;
+      double rcon[3], rcov[3], bu[3], Bprim[3] = {0.0, 0.0, 0.0}, bdotr = 0.0;
+      ok = c2p_setup<MINK>(p, g, U, x1, x2, x3, res, rcon, rcov, bu, Bprim, bdotr);
+      if (ok) c2p_features(res, f);
+    }
+    float o0, o1;
+    mlp_warp_forward(S->w, f, S->xs[warp], S->os[warp], o0, o1);
+    if (q < count) {
+      double lb[3];
+      mlp_bracket(o0, o1, lb);
+      const double nan = __longlong_as_double(0x7ff8000000000000ll);
+      for (int c = 0; c < 3; c++) brk[c * count + q] = ok ? lb[c] : nan;
+    }
+  }
+}
+
+// Per-zone statistics into the block's shared counters.
+__device__ __forceinline__ void c2p_tally(unsigned int *s_hist, unsigned long long *s_cnt, const C2POut &out,
+                                          bool setup_ok, bool success) {
+  const int h = out.iterations < PHX_C2P_HIST ? out.iterations : PHX_C2P_HIST - 1;
+  atomicAdd(&s_hist[h], 1u);
+  atomicAdd(&s_cnt[0], (unsigned long long)out.iterations);
+  atomicAdd(&s_cnt[1], (unsigned long long)out.evals);
+  if (!success) atomicAdd(&s_cnt[2], 1ull);
+  if (setup_ok && !out.bracketed) atomicAdd(&s_cnt[3], 1ull);
+  atomicAdd(&s_cnt[4], 1ull);
+  if (out.learned) atomicAdd(&s_cnt[5], 1ull);
+}
+
+__device__ __forceinline__ void c2p_flush_stats(DevStats *stats, const unsigned int *s_hist,
+                                                const unsigned long long *s_cnt) {
+  __syncthreads();
+  for (int h = threadIdx.x; h < PHX_C2P_HIST; h += blockDim.x)
+    if (s_hist[h]) atomicAdd(&stats->hist[h], (unsigned long long)s_hist[h]);
+  if (threadIdx.x == 0) {
+    atomicAdd(&stats->iterations, s_cnt[0]);
+    atomicAdd(&stats->residual_evals, s_cnt[1]);
+    atomicAdd(&stats->failures, s_cnt[2]);
+    atomicAdd(&stats->unbracketed, s_cnt[3]);
+    atomicAdd(&stats->zones, s_cnt[4]);
+    atomicAdd(&stats->learned_accepted, s_cnt[5]);
+  }
+}
+
+// Finish one zone after its root find: unwrap mu, store, fail flag, stats.
+template <class Z, bool MINK>
+__device__ __forceinline__ void c2p_complete(const Par &p, const Z &zones, long long id, const Pt &g, Residual &res,
+                                             double mu, const double rcon[3], const double bu[3],
+                                             const double Bprim[3], double bdotr, double U[PHX_NCONS],
+                                             bool setup_ok, const C2POut &out, DevStats *stats, unsigned int *s_hist,
+                                             unsigned long long *s_cnt, unsigned int *err) {
+  bool success = false;
+  if (setup_ok) {
+    double prim[PHX_NPRIM], sig[3];
+    bool used_bounds;
+    c2p_finish<MINK>(p, g, res, mu, rcon, bu, Bprim, bdotr, prim, U, sig, used_bounds);
+    zones.store(id, p, prim, U, used_bounds, sig);
+    const int num_nans = isnan(U[PHX_CRHO]) + isnan(U[PHX_CMOM]) + isnan(U[PHX_CENG]);
+    success = out.bracketed && num_nans == 0;
+    if (p.fail_on_floors && (res.used_density_floor || res.used_energy_floor)) success = false;
+    if (p.fail_on_ceilings && res.used_gamma_max) success = false;
+    if (!out.bracketed) atomicOr(err, ERR_UNBRACKETED);
+  }
+  zones.store_fail(id, success ? 1.0 : 0.0);
+  if (stats) c2p_tally(s_hist, s_cnt, out, setup_ok, success);
+}
+
+// Zones whose root find is still running after the first kernel's iteration
+// cap: chunk offset and the saved RFState (it, evals, b1, b2 in 16/16/14/14
+// bits, then the sign and learned bits).
+struct RetryBuf {
+  int *count;
+  int *idx;
+  double *a, *b, *ya, *yb;
+  unsigned long long *packed;
+};
+
+__device__ __forceinline__ unsigned long long rf_pack(const RFState &s) {
+  return (unsigned long long)(s.it & 0xffff) | ((unsigned long long)(s.evals & 0xffff) << 16) |
+         ((unsigned long long)(s.b1 & 0x3fff) << 32) | ((unsigned long long)(s.b2 & 0x3fff) << 46) |
+         ((unsigned long long)(s.sign < 0.0) << 60) | ((unsigned long long)s.learned << 61);
+}
+__device__ __forceinline__ void rf_unpack(unsigned long long w, RFState &s) {
+  s.it = (int)(w & 0xffff);
+  s.evals = (int)((w >> 16) & 0xffff);
+  s.b1 = (int)((w >> 32) & 0x3fff);
+  s.b2 = (int)((w >> 46) & 0x3fff);
+  s.sign = ((w >> 60) & 1) ? -1.0 : 1.0;
+  s.learned = (w >> 61) & 1;
+  s.bracketed = true;
+}
+
+// con2prim of zones t0 .. t0 + count - 1, one zone per thread.  LEARNED:
+// the start bracket of zone t is brk[c * count + t - t0].  A lane that has
+// not converged after cap iterations saves its state to rb (warp-aggregated
+// append) and leaves the zone to k_c2p_retry, so that one slow zone does not
+// hold 31 finished lanes of its warp.
+template <class Z, bool MINK, bool LEARNED>
+__global__ void __launch_bounds__(C2P_THREADS) k_c2p(Par p, Z zones, long long t0, long long count,
+                                                      const double *brk, int cap, RetryBuf rb, DevStats *stats,
+                                                      unsigned int *err) {
   __shared__ unsigned int s_hist[PHX_C2P_HIST];
   __shared__ unsigned long long s_cnt[6];
   if (stats) {
     for (int h = threadIdx.x; h < PHX_C2P_HIST; h += blockDim.x) s_hist[h] = 0;
     if (threadIdx.x < 6) s_cnt[threadIdx.x] = 0;
-  }
-  C2PLearnedSmem *L = reinterpret_cast<C2PLearnedSmem *>(c2p_dyn);
-  if constexpr (LEARNED) {
-    if (!mlp_stage_weights(&L->w, mlp, &bar, err)) return;
-  } else {
     __syncthreads();
   }
-  const int warp = threadIdx.x >> 5;
-  for (long long base = (long long)blockIdx.x * C2P_THREADS; base < ntot;
-       base += (long long)gridDim.x * C2P_THREADS) {
-    const long long t = base + threadIdx.x;
-    const bool valid = t < ntot;
+  const long long q = (long long)blockIdx.x * C2P_THREADS + threadIdx.x;
+  const bool valid = q < count;
+  long long id = 0;
+  Pt g{};
+  double U[PHX_NCONS];
+  bool setup_ok = false;
+  Residual res;
+  double rcon[3], rcov[3], bu[3], Bprim[3] = {0.0, 0.0, 0.0}, bdotr = 0.0, guess = 0.0;
+  if (valid) {
+    double x1, x2, x3;
+    zones.template load<MINK>(t0 + q, id, g, U, x1, x2, x3, guess);
+    setup_ok = c2p_setup<MINK>(p, g, U, x1, x2, x3, res, rcon, rcov, bu, Bprim, bdotr);
+  }
+  const bool run = valid && setup_ok;
+  RFState st;
+  if constexpr (LEARNED) {
+    double lb[3] = {0.0, 0.0, 0.0};
+    if (valid) {
+      lb[0] = brk[q];
+      lb[1] = brk[count + q];
+      lb[2] = brk[2 * count + q];
+    }
+    rf_start<true>(p, res, run, 0.0, 1.0, guess, lb, st);
+  } else {
+    rf_start<false>(p, res, run, 0.0, 1.0, guess, nullptr, st);
+  }
+  rf_iterate(p, res, run, st, cap);
+  const bool defer = run && rf_running(p, st);
+  const unsigned m = __ballot_sync(0xffffffffu, defer);
+  if (m) {
+    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(rb.count, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (defer) {
+      const int pos = base + __popc(m & ((1u << lane) - 1u));
+      rb.idx[pos] = (int)q;
+      rb.a[pos] = st.a;
+      rb.b[pos] = st.b;
+      rb.ya[pos] = st.ya;
+      rb.yb[pos] = st.yb;
+      rb.packed[pos] = rf_pack(st);
+    }
+  }
+  if (valid && !defer) {
+    C2POut out{0, 0, false, true, false, false};
+    const double mu = rf_result(st, guess, out);
+    c2p_complete<Z, MINK>(p, zones, id, g, res, mu, rcon, bu, Bprim, bdotr, U, setup_ok, out, stats, s_hist, s_cnt,
+                          err);
+  }
+  if (stats) c2p_flush_stats(stats, s_hist, s_cnt);
+}
+
+// The deferred zones of a chunk: reload, set up again (the same
+// deterministic setup), restore the root-find state and iterate to the end.
+template <class Z, bool MINK>
+__global__ void __launch_bounds__(C2P_THREADS) k_c2p_retry(Par p, Z zones, long long t0, RetryBuf rb, DevStats *stats,
+                                                            unsigned int *err) {
+  __shared__ unsigned int s_hist[PHX_C2P_HIST];
+  __shared__ unsigned long long s_cnt[6];
+  if (stats) {
+    for (int h = threadIdx.x; h < PHX_C2P_HIST; h += blockDim.x) s_hist[h] = 0;
+    if (threadIdx.x < 6) s_cnt[threadIdx.x] = 0;
+    __syncthreads();
+  }
+  const int n = *rb.count;
+  for (long long base = (long long)blockIdx.x * C2P_THREADS; base < n; base += (long long)gridDim.x * C2P_THREADS) {
+    const long long k = base + threadIdx.x;
+    const bool valid = k < n;
     long long id = 0;
     Pt g{};
     double U[PHX_NCONS];
     bool setup_ok = false;
     Residual res;
     double rcon[3], rcov[3], bu[3], Bprim[3] = {0.0, 0.0, 0.0}, bdotr = 0.0, guess = 0.0;
+    RFState st{};
     if (valid) {
       double x1, x2, x3;
-      zones.template load<MINK>(t, id, g, U, x1, x2, x3, guess);
+      zones.template load<MINK>(t0 + rb.idx[k], id, g, U, x1, x2, x3, guess);
       setup_ok = c2p_setup<MINK>(p, g, U, x1, x2, x3, res, rcon, rcov, bu, Bprim, bdotr);
+      st.a = rb.a[k];
+      st.b = rb.b[k];
+      st.ya = rb.ya[k];
+      st.yb = rb.yb[k];
+      rf_unpack(rb.packed[k], st);
     }
-    C2POut out{0, 0, false, true, false, false};
-    double mu;
-    if constexpr (LEARNED) {
-      float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-      if (valid && setup_ok) c2p_features(res, f);
-      float o0, o1;
-      mlp_warp_forward(L->w, f, L->xs[warp], L->os[warp], o0, o1);
-      double lb[3];
-      mlp_bracket(o0, o1, lb);
-      mu = regula_falsi_warp<true>(p, res, valid && setup_ok, 0.0, 1.0, guess, out, lb);
-    } else {
-      mu = regula_falsi_warp<false>(p, res, valid && setup_ok, 0.0, 1.0, guess, out);
-    }
+    rf_iterate(p, res, valid && setup_ok, st, p.c2p_max_iter);
     if (valid) {
-      bool success = false;
-      if (setup_ok) {
-        double prim[PHX_NPRIM], sig[3];
-        bool used_bounds;
-        c2p_finish<MINK>(p, g, res, mu, rcon, bu, Bprim, bdotr, prim, U, sig, used_bounds);
-        zones.store(id, p, prim, U, used_bounds, sig);
-        const int num_nans = isnan(U[PHX_CRHO]) + isnan(U[PHX_CMOM]) + isnan(U[PHX_CENG]);
-        success = out.bracketed && num_nans == 0;
-        if (p.fail_on_floors && (res.used_density_floor || res.used_energy_floor)) success = false;
-        if (p.fail_on_ceilings && res.used_gamma_max) success = false;
-        if (!out.bracketed) atomicOr(err, ERR_UNBRACKETED);
-      }
-      zones.store_fail(id, success ? 1.0 : 0.0);
-      if (stats) {
-        const int h = out.iterations < PHX_C2P_HIST ? out.iterations : PHX_C2P_HIST - 1;
-        atomicAdd(&s_hist[h], 1u);
-        atomicAdd(&s_cnt[0], (unsigned long long)out.iterations);
-        atomicAdd(&s_cnt[1], (unsigned long long)out.evals);
-        if (!success) atomicAdd(&s_cnt[2], 1ull);
-        if (setup_ok && !out.bracketed) atomicAdd(&s_cnt[3], 1ull);
-        atomicAdd(&s_cnt[4], 1ull);
-        if (out.learned) atomicAdd(&s_cnt[5], 1ull);
-      }
+      C2POut out{0, 0, false, true, false, false};
+      const double mu = rf_result(st, guess, out);
+      c2p_complete<Z, MINK>(p, zones, id, g, res, mu, rcon, bu, Bprim, bdotr, U, setup_ok, out, stats, s_hist,
+                            s_cnt, err);
     }
   }
-  if (stats) {
-    __syncthreads();
-    for (int h = threadIdx.x; h < PHX_C2P_HIST; h += blockDim.x)
-      if (s_hist[h]) atomicAdd(&stats->hist[h], (unsigned long long)s_hist[h]);
-    if (threadIdx.x == 0) {
-      atomicAdd(&stats->iterations, s_cnt[0]);
-      atomicAdd(&stats->residual_evals, s_cnt[1]);
-      atomicAdd(&stats->failures, s_cnt[2]);
-      atomicAdd(&stats->unbracketed, s_cnt[3]);
-      atomicAdd(&stats->zones, s_cnt[4]);
-      atomicAdd(&stats->learned_accepted, s_cnt[5]);
-    }
-  }
+  if (stats) c2p_flush_stats(stats, s_hist, s_cnt);
 }
 
-// Plain launches cover the zones with one chunk per CTA; learned launches
-// cap the grid at a few CTAs per SM so that each CTA stages the weights once
-// for many chunks.
+static int num_sms() {
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  return nsm > 0 ? nsm : 1;
+}
+
 template <class Z, bool MINK>
-static void launch_c2p_any(const Par &p, const Z &z, long long n, const MlpPacked *mlp, DevStats *stats,
-                           unsigned int *err, cudaStream_t s) {
+static void launch_bracket_any(const Par &p, const Z &z, long long t0, long long count, const MlpPacked *mlp,
+                               double *brk, unsigned int *err, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_mlp_bracket<Z, MINK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sizeof(BracketSmem));
+    attr = true;
+  }
+  long long grid = (count + C2P_THREADS - 1) / C2P_THREADS;
+  const long long cap = (long long)num_sms() * 8;
+  if (grid > cap) grid = cap;
+  k_mlp_bracket<Z, MINK><<<(unsigned)grid, C2P_THREADS, sizeof(BracketSmem), s>>>(p, z, t0, count, mlp, brk, err);
+}
+
+// Zones per chunk of C2P_CHUNK; per chunk: [bracket launch], root-find
+// launch with an iteration cap, retry launch over the deferred zones.  The
+// caps default to a little above the mean iteration count of each start on
+// Kerr-Schild zones at tolerance 1e-10; PHX_C2P_CAP_PLAIN /
+// PHX_C2P_CAP_LEARNED in the environment override them (read once).
+static int cap_from_env(const char *name, int dflt) {
+  const char *v = getenv(name);
+  const int c = v ? atoi(v) : 0;
+  return c > 0 ? c : dflt;
+}
+
+template <class Z, bool MINK>
+static void launch_c2p_any(const Par &p, const Z &z, long long n, const MlpPacked *mlp, const C2PScratch &scr,
+                           DevStats *stats, unsigned int *err, cudaStream_t s) {
   if (n <= 0) return;
-  long long grid = (n + C2P_THREADS - 1) / C2P_THREADS;
-  if (mlp) {
-    static int nsm = 0;
-    if (!nsm) {
-      int dev = 0;
-      cudaGetDevice(&dev);
-      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-      cudaFuncSetAttribute(k_c2p<Z, MINK, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)sizeof(C2PLearnedSmem));
+  static const int cap_plain = cap_from_env("PHX_C2P_CAP_PLAIN", 12);
+  static const int cap_learned = cap_from_env("PHX_C2P_CAP_LEARNED", 6);
+  const int cap = mlp ? cap_learned : cap_plain;
+  RetryBuf rb{scr.count, scr.idx, scr.a, scr.b, scr.ya, scr.yb, scr.packed};
+  const unsigned retry_grid = (unsigned)num_sms() * 4;
+  for (long long t0 = 0; t0 < n; t0 += C2P_CHUNK) {
+    const long long m = n - t0 < C2P_CHUNK ? n - t0 : C2P_CHUNK;
+    const long long grid = (m + C2P_THREADS - 1) / C2P_THREADS;
+    cudaMemsetAsync(scr.count, 0, sizeof(int), s);
+    if (mlp) {
+      launch_bracket_any<Z, MINK>(p, z, t0, m, mlp, scr.brk, err, s);
+      k_c2p<Z, MINK, true><<<(unsigned)grid, C2P_THREADS, 0, s>>>(p, z, t0, m, scr.brk, cap, rb, stats, err);
+    } else {
+      k_c2p<Z, MINK, false><<<(unsigned)grid, C2P_THREADS, 0, s>>>(p, z, t0, m, nullptr, cap, rb, stats, err);
     }
-    const long long cap = (long long)nsm * 8;
-    if (grid > cap) grid = cap;
-    k_c2p<Z, MINK, true><<<(unsigned)grid, C2P_THREADS, sizeof(C2PLearnedSmem), s>>>(p, z, n, mlp, stats, err);
-  } else {
-    k_c2p<Z, MINK, false><<<(unsigned)grid, C2P_THREADS, 0, s>>>(p, z, n, nullptr, stats, err);
+    k_c2p_retry<Z, MINK><<<retry_grid, C2P_THREADS, 0, s>>>(p, z, t0, rb, stats, err);
   }
 }
 
 void launch_c2p(const Par &p, const BView &b, Range3 r, DevStats *stats, unsigned int *err,
-                const MlpPacked *mlp, cudaStream_t s) {
+                const MlpPacked *mlp, const C2PScratch &scr, cudaStream_t s) {
   const long long n = (long long)(r.ie - r.is + 1) * (r.je - r.js + 1) * (r.ke - r.ks + 1);
   const BoxZones z{b, r};
   if (b.fmks)
-    launch_c2p_any<BoxZones, false>(p, z, n, mlp, stats, err, s);
+    launch_c2p_any<BoxZones, false>(p, z, n, mlp, scr, stats, err, s);
   else
-    launch_c2p_any<BoxZones, true>(p, z, n, mlp, stats, err, s);
+    launch_c2p_any<BoxZones, true>(p, z, n, mlp, scr, stats, err, s);
 }
 
 void launch_c2p_zones(const Par &p, long long n, double *cons, double *prim, const double *geom, double *fail,
                       double *cell_sig, const double *coords, DevStats *stats, unsigned int *err,
-                      const MlpPacked *mlp, cudaStream_t s) {
+                      const MlpPacked *mlp, const C2PScratch &scr, cudaStream_t s) {
   const ListZones z{n, cons, prim, fail, cell_sig, geom, coords};
   if (geom)
-    launch_c2p_any<ListZones, false>(p, z, n, mlp, stats, err, s);
+    launch_c2p_any<ListZones, false>(p, z, n, mlp, scr, stats, err, s);
   else
-    launch_c2p_any<ListZones, true>(p, z, n, mlp, stats, err, s);
+    launch_c2p_any<ListZones, true>(p, z, n, mlp, scr, stats, err, s);
+}
+
+void launch_mlp_bracket(const Par &p, long long n, const double *cons, const double *geom, const double *coords,
+                        const MlpPacked *mlp, double *bracket, unsigned int *err, cudaStream_t s) {
+  if (n <= 0) return;
+  const ListZones z{n, const_cast<double *>(cons), nullptr, nullptr, nullptr, geom, coords};
+  if (geom)
+    launch_bracket_any<ListZones, false>(p, z, 0, n, mlp, bracket, err, s);
+  else
+    launch_bracket_any<ListZones, true>(p, z, 0, n, mlp, bracket, err, s);
 }
 
 }  // namespace phx

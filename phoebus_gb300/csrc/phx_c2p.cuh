@@ -196,26 +196,31 @@ __device__ __forceinline__ void c2p_features(const Residual &r, float f[6]) {
   f[5] = log10f((float)fmax(r.D, 1e-30)) * 0.125f;
 }
 
-// refine_bracket + regula_falsi (root_find.hpp:42-58, 110-167), vote-driven.
-// valid = this lane owns a zone.  Returns mu; iterations/evals/bracketed
-// through out.  lo/hi: starting bracket ([0, 1] in the reference).
-// LEARNED: lb = (m, lo, hi), a predicted root and bracket in [0, 1].  f(m)
-// picks the half that should hold the root (f < 0 below it, > 0 above), one
-// more evaluation checks that half's sign change; when it holds, the same
-// Illinois iterations start from that half, otherwise from the reference's
+// State of one zone's regula falsi (root_find.hpp:110-167) between
+// iterations: the bracket [a, b] with sign-normalised end values, the Illinois
+// counters, and the tallies.  Saving and restoring it resumes the same
+// sequence of operations.
+struct RFState {
+  double a, b, ya, yb, sign;
+  int it, evals, b1, b2;
+  bool bracketed, learned;
+};
+
+// Start: refine_bracket + check_bracket (root_find.hpp:42-58, 110-119) from
+// [a, b] and guess.  LEARNED: lb = (m, lo, hi), a predicted root and bracket
+// in [0, 1]; f(m) picks the half that should hold the root (f < 0 below it,
+// > 0 above), one more evaluation checks that half's sign change; when it
+// holds, the iterations start from that half, otherwise from the reference's
 // own start.  A bracket that is not ordered inside [0, 1] (e.g. NaN) is not
 // tried.
-template <bool LEARNED = false>
-__device__ __forceinline__ double regula_falsi_warp(const Par &p, Residual &res, bool valid,
-                                                   double a, double b, double guess, C2POut &out,
-                                                   const double *lb = nullptr) {
-  const double tol = p.c2p_tol;
-  const int max_iter = p.c2p_max_iter;
+template <bool LEARNED>
+__device__ __forceinline__ void rf_start(const Par &p, Residual &res, bool valid, double a, double b, double guess,
+                                         const double *lb, RFState &s) {
   double ya = 0.0, yb = 0.0;
   int evals = 0;
   bool bracketed = true;
   bool started = false;
-  out.learned = false;
+  s.learned = false;
   if constexpr (LEARNED) {
     if (valid && lb[1] >= 0.0 && lb[1] <= lb[0] && lb[0] <= lb[2] && lb[2] <= 1.0) {
       double la, lbb, lya, lyb;
@@ -238,7 +243,7 @@ __device__ __forceinline__ double regula_falsi_warp(const Par &p, Residual &res,
         ya = lya;
         yb = lyb;
         started = true;
-        out.learned = true;
+        s.learned = true;
       }
     }
   }
@@ -262,12 +267,33 @@ __device__ __forceinline__ double regula_falsi_warp(const Par &p, Residual &res,
     }
     bracketed = !(ya * yb > 0.0);
   }
-  int it = 0;
-  double sign = (ya < 0 ? 1.0 : -1.0);
-  ya *= sign;
-  yb *= sign;
-  int b1 = 0, b2 = 0;
-  bool active = valid && bracketed && (b - a > 2.0 * tol) && (it < max_iter);
+  s.sign = (ya < 0 ? 1.0 : -1.0);
+  s.a = a;
+  s.b = b;
+  s.ya = ya * s.sign;
+  s.yb = yb * s.sign;
+  s.it = 0;
+  s.b1 = s.b2 = 0;
+  s.evals = evals;
+  s.bracketed = bracketed;
+}
+
+// True while the zone still iterates (root_find.hpp:120 loop condition).
+__device__ __forceinline__ bool rf_running(const Par &p, const RFState &s) {
+  return s.bracketed && (s.b - s.a > 2.0 * p.c2p_tol) && (s.it < p.c2p_max_iter);
+}
+
+// The Illinois iterations (root_find.hpp:120-166), warp-synchronous: every
+// lane stays in the loop until the warp's vote says none is still
+// iterating.  A lane stops after cap iterations in total even if it has not
+// converged (rf_running stays true: the caller resumes it later).
+__device__ __forceinline__ void rf_iterate(const Par &p, Residual &res, bool valid, RFState &s, int cap) {
+  const double tol = p.c2p_tol;
+  const int max_iter = p.c2p_max_iter;
+  double a = s.a, b = s.b, ya = s.ya, yb = s.yb;
+  const double sign = s.sign;
+  int it = s.it, b1 = s.b1, b2 = s.b2, evals = s.evals;
+  bool active = valid && s.bracketed && (b - a > 2.0 * tol) && (it < max_iter) && (it < cap);
   while (__any_sync(0xffffffffu, active)) {
     if (active) {
       const double c = div_p(a * yb - b * ya, yb - ya);
@@ -296,14 +322,38 @@ __device__ __forceinline__ double regula_falsi_warp(const Par &p, Residual &res,
         }
       }
       it++;
-      active = (b - a > 2.0 * tol) && (it < max_iter);
+      active = (b - a > 2.0 * tol) && (it < max_iter) && (it < cap);
     }
   }
-  out.iterations = it;
-  out.evals = evals;
-  out.bracketed = bracketed;
-  if (!bracketed) return guess;
-  return 0.5 * (a + b);
+  s.a = a;
+  s.b = b;
+  s.ya = ya;
+  s.yb = yb;
+  s.it = it;
+  s.b1 = b1;
+  s.b2 = b2;
+  s.evals = evals;
+}
+
+__device__ __forceinline__ double rf_result(const RFState &s, double guess, C2POut &out) {
+  out.iterations = s.it;
+  out.evals = s.evals;
+  out.bracketed = s.bracketed;
+  out.learned = s.learned;
+  if (!s.bracketed) return guess;
+  return 0.5 * (s.a + s.b);
+}
+
+// refine_bracket + regula_falsi (root_find.hpp:42-58, 110-167) in one call.
+// valid = this lane owns a zone.  Returns mu; iterations/evals/bracketed
+// through out.  a/b: starting bracket ([0, 1] in the reference).
+template <bool LEARNED = false>
+__device__ __forceinline__ double regula_falsi_warp(const Par &p, Residual &res, bool valid, double a, double b,
+                                                   double guess, C2POut &out, const double *lb = nullptr) {
+  RFState s;
+  rf_start<LEARNED>(p, res, valid, a, b, guess, lb, s);
+  rf_iterate(p, res, valid, s, p.c2p_max_iter);
+  return rf_result(s, guess, out);
 }
 
 // Unwrap mu into primitives (con2prim_robust.hpp:381-452).

@@ -23,8 +23,19 @@ struct Range3 {
 
 void launch_p2c(const Par &p, const BView &b, Range3 r, cudaStream_t s);
 struct MlpPacked;
+// con2prim works in chunks of C2P_CHUNK zones; per chunk the context holds
+// the learned brackets [3][C2P_CHUNK] and the retry list of zones deferred
+// past the first kernel's iteration cap.
+constexpr long long C2P_CHUNK = 1ll << 21;
+struct C2PScratch {
+  double *brk;                  // [3][C2P_CHUNK]
+  int *count;                   // [1]
+  int *idx;                     // [C2P_CHUNK]
+  double *a, *b, *ya, *yb;      // [C2P_CHUNK] each
+  unsigned long long *packed;   // [C2P_CHUNK]
+};
 void launch_c2p(const Par &p, const BView &b, Range3 r, DevStats *stats, unsigned int *err,
-                const MlpPacked *mlp, cudaStream_t s);
+                const MlpPacked *mlp, const C2PScratch &scr, cudaStream_t s);
 void launch_fluxes(const Par &p, const BView &b, cudaStream_t s);
 void launch_fluxct(const BView &b, cudaStream_t s);
 void launch_sources(const Par &p, const BView &b, cudaStream_t s);
@@ -43,7 +54,7 @@ void launch_p2c_zones(const Par &p, long long n, const double *prim, const doubl
                       double *cell_sig, cudaStream_t s);
 void launch_c2p_zones(const Par &p, long long n, double *cons, double *prim, const double *geom, double *fail,
                       double *cell_sig, const double *coords, DevStats *stats, unsigned int *err,
-                      const MlpPacked *mlp, cudaStream_t s);
+                      const MlpPacked *mlp, const C2PScratch &scr, cudaStream_t s);
 void launch_mlp_bracket(const Par &p, long long n, const double *cons, const double *geom, const double *coords,
                         const MlpPacked *mlp, double *bracket, unsigned int *err, cudaStream_t s);
 // learned-start network (phx_mlp.cu)

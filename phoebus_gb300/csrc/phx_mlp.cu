@@ -129,62 +129,6 @@ void launch_mlp_forward(const MlpPacked *mlp, long long n, const float *x, float
   k_mlp_forward<<<(unsigned)grid, 128, sizeof(MlpFwdSmem), s>>>(mlp, n, x, out, err);
 }
 
-// The learned start (m, lo, hi) of independent zones, as the learned
-// con2prim kernel computes it before its root find: setup invariants ->
-// features -> network -> bracket.  NaN where the setup rejects the input.
-template <bool MINK>
-__global__ void __launch_bounds__(128) k_mlp_bracket(Par p, long long n, const double *cons, const double *geom,
-                                                     const double *coords, const MlpPacked *mlp, double *bracket,
-                                                     unsigned int *err) {
-  extern __shared__ __align__(16) unsigned char brk_dyn[];
-  __shared__ __align__(8) uint64_t bar;
-  MlpFwdSmem *S = reinterpret_cast<MlpFwdSmem *>(brk_dyn);
-  if (!mlp_stage_weights(&S->w, mlp, &bar, err)) return;
-  const int warp = threadIdx.x >> 5;
-  for (long long base = (long long)blockIdx.x * 128; base < n; base += (long long)gridDim.x * 128) {
-    const long long q = base + threadIdx.x;
-    float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    bool ok = false;
-    if (q < n) {
-      Pt g{};
-      if constexpr (!MINK) load_pt_flat(geom, n, q, g);
-      double U[PHX_NCONS];
-      for (int m = 0; m < PHX_NCONS; m++) U[m] = cons[m * n + q];
-      const double x1 = coords ? coords[q] : 0.0, x2 = coords ? coords[n + q] : 0.0,
-                   x3 = coords ? coords[2 * n + q] : 0.0;
-      Residual res;
-      double rcon[3], rcov[3], bu[3], Bprim[3] = {0.0, 0.0, 0.0}, bdotr = 0.0;
-      ok = c2p_setup<MINK>(p, g, U, x1, x2, x3, res, rcon, rcov, bu, Bprim, bdotr);
-      if (ok) c2p_features(res, f);
-    }
-    float o0, o1;
-    mlp_warp_forward(S->w, f, S->xs[warp], S->os[warp], o0, o1);
-    if (q < n) {
-      double lb[3];
-      mlp_bracket(o0, o1, lb);
-      const double nan = __longlong_as_double(0x7ff8000000000000ll);
-      for (int c = 0; c < 3; c++) bracket[c * n + q] = ok ? lb[c] : nan;
-    }
-  }
-}
-
-void launch_mlp_bracket(const Par &p, long long n, const double *cons, const double *geom, const double *coords,
-                        const MlpPacked *mlp, double *bracket, unsigned int *err, cudaStream_t s) {
-  if (n <= 0) return;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_mlp_bracket<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MlpFwdSmem));
-    cudaFuncSetAttribute(k_mlp_bracket<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MlpFwdSmem));
-    attr = true;
-  }
-  long long grid = (n + 127) / 128;
-  if (grid > 152 * 8) grid = 152 * 8;
-  if (geom)
-    k_mlp_bracket<false><<<(unsigned)grid, 128, sizeof(MlpFwdSmem), s>>>(p, n, cons, geom, coords, mlp, bracket, err);
-  else
-    k_mlp_bracket<true><<<(unsigned)grid, 128, sizeof(MlpFwdSmem), s>>>(p, n, cons, geom, coords, mlp, bracket, err);
-}
-
 // ------------------------------------------------------------------ training
 constexpr int TR_T = 64;         // samples per tile
 constexpr int TR_THREADS = 256;  // 16 x 16 threads, each a 4 x 4 block of a 64 x 64 product

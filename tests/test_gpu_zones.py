@@ -42,9 +42,17 @@ def test_fmks_points(ctx_fast, oracle, zones):
     z = zones["z"]
     got = host(ctx_fast.GeometryFMKSPoints(zones["g"], dev(z["x1"]), dev(z["x2"])))
     # CUDA and glibc transcendental functions differ by ulps; each quantity
-    # is compared on its own scale
+    # is compared on its own scale.  Near a pole an ulp of theta is a
+    # relative change ulp / theta of sin(theta), squared in the 1 / sin^2
+    # components: that amplification is allowed for.
+    x2 = z["x2"]
+    th = np.pi * x2 + 0.5 * (1.0 - 0.3) * np.sin(2.0 * np.pi * x2)
+    amp = 4.0 * np.finfo(float).eps / np.minimum(th, np.pi - th) ** 2
     for v in range(abi.GEOM_NLOC):
-        assert_close(got[v], zones["geom"][v], 1e-12, f"geom[{v}]")
+        ref = zones["geom"][v]
+        lim = 1e-12 * (np.abs(ref) + np.abs(ref).max()) + amp * np.abs(ref)
+        bad = ~(np.abs(got[v] - ref) <= lim)
+        assert not bad.any(), (v, np.argwhere(bad)[:3].ravel(), got[v][bad][:3], ref[bad][:3])
 
 
 @pytest.mark.parametrize("exact", [True, False])
