@@ -22,7 +22,8 @@
 // TaskStatus, the package Params) as small stand-ins in namespace parthenon.
 // Inside phoebus the same function bodies are written against the real
 // Parthenon types: a pack's variable Views provide the device pointers of
-// phx_block.
+// phx_block (the fluid fields of a block laid out as one [var][k][j][i]
+// allocation, or staged into one).
 //
 // Errors: configuration errors throw std::runtime_error (PARTHENON_THROW);
 // an unbracketed con2prim root is detected by phx_ctx_check() at the end of

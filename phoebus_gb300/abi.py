@@ -27,10 +27,12 @@ GD_DALPHA, GD_DG, GEOM_NDER = 0, 3, 33
 C2P_HIST = 128
 MLP_IN, MLP_HID, MLP_OUT = 6, 64, 2
 C2P_CHUNK = 1 << 21  # zones per con2prim chunk inside the library (launch accounting only)
+MLP_MAX_EPOCHS = 1024
 MLP_NPARAM = MLP_IN * MLP_HID + MLP_HID + 2 * (MLP_HID * MLP_HID + MLP_HID) + MLP_HID * 2 + 2
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "con2prim root not bracketed", 3: "NaN input",
-          4: "device wait timed out", 5: "CUDA error", 6: "no CUDA device", 7: "capacity", 8: "unsupported"}
+          4: "device wait timed out", 5: "CUDA error", 6: "no CUDA device",
+          7: "request exceeds a fixed capacity", 8: "unsupported"}
 
 
 class Range(C.Structure):

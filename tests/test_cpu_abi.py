@@ -79,3 +79,30 @@ def test_struct_sizes_match_header(built, tmp_path):
         assert int(out[cname]) == C.sizeof(cls), cname
         for fname, _ in cls._fields_:
             assert int(out[f"{cname}.{fname}"]) == getattr(cls, fname).offset, f"{cname}.{fname}"
+
+
+def _has_cuda():
+    try:
+        import torch
+
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+@pytest.mark.skipif(_has_cuda(), reason="checks the no-device path")
+def test_context_without_device_fails_loudly(built):
+    """No GPU: creating a context returns PHX_ERR_NO_DEVICE and the Python
+    layer raises; there is no CPU fallback."""
+    from phoebus_gb300.fluid import FluidContext
+
+    with pytest.raises(abi.PhxError) as e:
+        FluidContext(0)
+    assert e.value.status == 6 and "no CUDA device" in str(e.value)
+
+
+def test_status_strings(built):
+    lib = abi.load(False)
+    for code, text in abi.STATUS.items():
+        got = lib.phx_status_string(code).decode()
+        assert got == text, (code, got)
