@@ -344,13 +344,25 @@ phx_status phx_stage(phx_ctx *ctx, const phx_params *p, const phx_block *b,
                      const double *cons_base, double *cons_out, double beta, double dt,
                      int use_learned_guess, void *stream);
 
-/* Batched uneven meshblocks: the same stage over nblocks independent
- * (periodic) blocks of mixed sizes, each kernel phase one persistent launch
- * walking a device work list.  cons_base[n] / cons_out[n] per block. */
+/* Batched uneven meshblocks: the stage of phx_stage over nblocks independent
+ * (periodic) blocks of mixed sizes, with one persistent launch per phase
+ * walking a device work list of (block, index range) items, the whole stage
+ * replayed as a CUDA graph.  cons_base[n] / cons_out[n] per block.  The
+ * first call for a set of blocks and buffers builds a plan: device tables,
+ * work lists, tile shapes chosen by timing candidates (cached per process,
+ * and in the JSON file PHX_AUTOTUNE_CACHE names, if set) and the captured
+ * graph; later calls with the same blocks, buffers and params only update
+ * beta and dt in device memory and launch the graph.  Blocks must share ndim
+ * and geometry kind; c2p fixup / floors and the learned start are not
+ * supported here (PHX_ERR_UNSUPPORTED).  No counterpart in the reference,
+ * which launches every block's tasks separately. */
 phx_status phx_stage_batched(phx_ctx *ctx, const phx_params *p, const phx_block *blocks,
                              int nblocks, const double *const *cons_base,
                              double *const *cons_out, double beta, double dt,
                              int use_learned_guess, void *stream);
+
+/* Tile shapes and graph size of the most recent batched plan (0 if none). */
+phx_status phx_batch_info(phx_ctx *ctx, int *x1_cells, int *sweep_seg, int *graph_nodes);
 
 /* ---- learned con2prim guess (no reference counterpart) ---------------- */
 /* Network 6 -> 64 -> 64 -> 64 -> 2, GELU, BF16 weights, FP32 accumulate. */

@@ -142,6 +142,7 @@ _SIGS = {
                             C.c_int, _P]),
     "phx_stage_batched": (C.c_int, [_P, C.POINTER(Params), C.POINTER(BlockS), C.c_int, _P, _P, C.c_double,
                                     C.c_double, C.c_int, _P]),
+    "phx_batch_info": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "phx_mlp_set_weights": (C.c_int, [_P, C.POINTER(C.c_float)]),
     "phx_mlp_get_weights": (C.c_int, [_P, C.POINTER(C.c_float)]),
     "phx_probe_fp64_peak": (C.c_int, [_P, C.POINTER(C.c_double)]),

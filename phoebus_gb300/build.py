@@ -23,7 +23,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 LIB = PKG / "_lib"
 OBJ = PKG / "_build"
-SOURCES = ["phx_api.cu", "phx_c2p.cu", "phx_flux.cu", "phx_stage.cu", "phx_geometry.cu", "phx_mlp.cu", "phx_noalloc.cu", "phx_fixup.cu"]
+SOURCES = ["phx_api.cu", "phx_c2p.cu", "phx_flux.cu", "phx_stage.cu", "phx_geometry.cu", "phx_mlp.cu", "phx_noalloc.cu", "phx_fixup.cu", "phx_batch.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAVOURS = {
     "libphx_fluid.so": ["-fmad=true"],

@@ -9,6 +9,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "phx_mlp.cuh"
 
@@ -25,6 +26,7 @@ struct phx_ctx {
   void *c2p_mem;               // its single allocation
   long long mlp_step;          // AdamW step count
   int mlp_loaded;
+  phx::BatchCache *batch;      // plans of phx_stage_batched (host)
 };
 
 namespace {
@@ -47,7 +49,8 @@ phx_status cuda_status(const char *where) {
 }
 
 phx::Par make_par(const phx_params &p) {
-  phx::Par d{};
+  phx::Par d;
+  std::memset(&d, 0, sizeof(d));  // all bytes defined: batched plans compare Par bytewise
   d.gm1 = p.gm1;
   d.Cv = p.Cv;
   d.rho_min_eos = p.rho_min_eos;
@@ -312,6 +315,7 @@ phx_status phx_ctx_create(int device, phx_ctx **out) {
   cudaMemset(c->mlp_v, 0, sizeof(float) * PHX_MLP_NPARAM);
   cudaMemset(c->mlp_packed, 0, sizeof(phx::MlpPacked));
   c->c2p = c2p_scratch_carve(c->c2p_mem);
+  c->batch = phx::batch_cache_create();
   phx_status s = cuda_status("ctx init");
   if (s != PHX_OK) {
     phx_ctx_destroy(c);
@@ -334,6 +338,7 @@ phx_status phx_ctx_destroy(phx_ctx *ctx) {
   cudaFree(ctx->mlp_loss);
   cudaFree(ctx->mlp_packed);
   cudaFree(ctx->c2p_mem);
+  if (ctx->batch) phx::batch_cache_destroy(ctx->batch);
   delete ctx;
   return PHX_OK;
 }
@@ -582,9 +587,37 @@ phx_status phx_stage(phx_ctx *ctx, const phx_params *p, const phx_block *b, cons
 phx_status phx_stage_batched(phx_ctx *ctx, const phx_params *p, const phx_block *blocks, int nblocks,
                              const double *const *cons_base, double *const *cons_out, double beta, double dt,
                              int use_learned_guess, void *stream) {
-  (void)ctx; (void)p; (void)blocks; (void)nblocks; (void)cons_base; (void)cons_out; (void)beta; (void)dt;
-  (void)use_learned_guess; (void)stream;
-  return fail(PHX_ERR_UNSUPPORTED, "phx_stage_batched: not built yet");
+  phx_status s;
+  if ((s = ctx_device(ctx)) || (s = check_params(p))) return s;
+  if (!blocks || nblocks <= 0 || !cons_base || !cons_out) return fail(PHX_ERR_INVALID_ARG, "no blocks");
+  if (use_learned_guess)
+    return fail(PHX_ERR_UNSUPPORTED, "phx_stage_batched: the learned start runs on single blocks and zone lists");
+  if (p->enable_c2p_fixup || p->enable_floors || (p->enable_mhd_floors && p->mhd))
+    return fail(PHX_ERR_UNSUPPORTED, "phx_stage_batched: c2p fixup and floors run on single blocks (phx_stage)");
+  std::vector<phx::BView> views(nblocks);
+  for (int n = 0; n < nblocks; n++) {
+    const phx_block *b = &blocks[n];
+    if ((s = make_view(b, views[n]))) return fail(s, "block %d: %s", n, g_last_error.c_str());
+    if (!b->flux || !b->face_sig || !b->cell_sig || !b->fail || !b->src || !cons_base[n] || !cons_out[n])
+      return fail(PHX_ERR_INVALID_ARG, "block %d: stage needs flux, face_sig, cell_sig, fail, src, cons_base, "
+                                       "cons_out", n);
+    if (p->mhd && b->ndim > 1 && !b->emf) return fail(PHX_ERR_INVALID_ARG, "block %d: emf is NULL", n);
+    if (b->nx1 < b->ng || (b->ndim >= 2 && b->nx2 < b->ng) || (b->ndim >= 3 && b->nx3 < b->ng))
+      return fail(PHX_ERR_INVALID_ARG, "block %d: periodic exchange needs nx >= ng", n);
+    if (views[n].ndim != views[0].ndim || views[n].fmks != views[0].fmks)
+      return fail(PHX_ERR_INVALID_ARG, "blocks must share ndim and geometry kind");
+  }
+  const char *why = nullptr;
+  cudaError_t e = phx::batch_stage(ctx->batch, make_par(*p), blocks, views.data(), nblocks, cons_base, cons_out, beta,
+                                   dt, ctx->stats, ctx->err, S(stream), &why);
+  if (e != cudaSuccess) return fail(PHX_ERR_CUDA, "phx_stage_batched: %s", cudaGetErrorString(e));
+  return cuda_status("phx_stage_batched");
+}
+
+phx_status phx_batch_info(phx_ctx *ctx, int *x1_cells, int *sweep_seg, int *graph_nodes) {
+  if (!ctx || !x1_cells || !sweep_seg || !graph_nodes) return fail(PHX_ERR_INVALID_ARG, "NULL argument");
+  phx::batch_last_tuning(ctx->batch, x1_cells, sweep_seg, graph_nodes);
+  return PHX_OK;
 }
 
 phx_status phx_mlp_set_weights(phx_ctx *ctx, const float *params_host) {

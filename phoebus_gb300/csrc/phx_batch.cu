@@ -1,0 +1,366 @@
+// phx_batch.cu -- batched uneven meshblocks.
+//
+// One RK stage over many independent (periodic) blocks of mixed sizes, in
+// the order of PhoebusDriver::RungeKuttaStage (phoebus_driver.cpp:204-738):
+// each phase is ONE persistent launch over a device work list of
+// (block, index range) items covering every block, and the whole stage is
+// captured once as a CUDA graph and replayed.  A plan (device tables, work
+// lists, tuned tile shapes, graph) is built on the first call for a given set
+// of blocks and buffers and reused by later calls; beta and dt live in device
+// memory so the graph serves every step.
+//
+// Autotuner: before capture, the X1 flux kernel's tile (cells staged per
+// CTA, converted to pencils per block size) and the X2/X3 sweeps' segment
+// length are chosen by timing each candidate on the plan's own blocks.
+// Results are cached per (reconstruction, geometry, block-size mix) in the
+// process and, when PHX_AUTOTUNE_CACHE names a file, in that JSON file.
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <functional>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "phx_kernels.cuh"
+
+namespace phx {
+
+namespace {
+
+struct PhaseList {
+  WorkItem *d_items = nullptr;
+  int n = 0;
+};
+
+struct Tuning {
+  int x1_cells = 288;  // cells staged per X1 CTA (pencils x n1t)
+  int seg = 32;        // faces per thread along an X2/X3 sweep
+};
+
+std::mutex g_tune_mu;
+std::map<std::string, Tuning> g_tune;  // process-wide autotune results
+bool g_tune_loaded = false;
+
+void load_tune_file() {
+  if (g_tune_loaded) return;
+  g_tune_loaded = true;
+  const char *path = getenv("PHX_AUTOTUNE_CACHE");
+  if (!path) return;
+  std::ifstream f(path);
+  std::string line;
+  // one entry per line: "key": {"x1_cells": N, "seg": M},
+  while (std::getline(f, line)) {
+    const size_t k0 = line.find('"'), k1 = line.find('"', k0 + 1);
+    if (k0 == std::string::npos || k1 == std::string::npos) continue;
+    const std::string key = line.substr(k0 + 1, k1 - k0 - 1);
+    Tuning t;
+    const size_t a = line.find("\"x1_cells\":"), b = line.find("\"seg\":");
+    if (a == std::string::npos || b == std::string::npos) continue;
+    t.x1_cells = atoi(line.c_str() + a + 11);
+    t.seg = atoi(line.c_str() + b + 6);
+    if (t.x1_cells > 0 && t.seg > 0) g_tune[key] = t;
+  }
+}
+
+void save_tune_file() {
+  const char *path = getenv("PHX_AUTOTUNE_CACHE");
+  if (!path) return;
+  std::ofstream f(path);
+  f << "{\n";
+  size_t i = 0;
+  for (const auto &kv : g_tune) {
+    f << "  \"" << kv.first << "\": {\"x1_cells\": " << kv.second.x1_cells << ", \"seg\": " << kv.second.seg << "}"
+      << (++i < g_tune.size() ? "," : "") << "\n";
+  }
+  f << "}\n";
+}
+
+}  // namespace
+
+struct BatchPlan {
+  // identity
+  std::vector<phx_block> blocks;
+  std::vector<const double *> base;
+  std::vector<double *> out;
+  Par par;
+  // device state (one allocation for the tables)
+  void *mem = nullptr;
+  BView *views_in = nullptr, *views_out = nullptr;
+  const double **base_tab = nullptr;
+  double **out_tab = nullptr;
+  double *beta_dt = nullptr;
+  std::vector<void *> item_mem;  // work-list allocations
+  PhaseList sources, x1, x2, x3, fluxct, update, ghost, c2p;
+  size_t x1_smem = 0;
+  Tuning tune;
+  bool mink = true;
+  int ndim = 3;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph = nullptr;
+  ~BatchPlan() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    for (void *m : item_mem) cudaFree(m);
+    cudaFree(mem);
+  }
+};
+
+struct BatchCache {
+  std::vector<std::unique_ptr<BatchPlan>> plans;  // most recent last
+};
+
+BatchCache *batch_cache_create() { return new BatchCache(); }
+void batch_cache_destroy(BatchCache *c) { delete c; }
+
+// Items of size T over counts[b] indices per block.
+static std::vector<WorkItem> make_items(const std::vector<long long> &counts, long long T) {
+  std::vector<WorkItem> v;
+  for (size_t b = 0; b < counts.size(); b++)
+    for (long long f = 0; f < counts[b]; f += T) v.push_back(WorkItem{(int)b, 0, f, std::min(f + T, counts[b])});
+  return v;
+}
+
+static cudaError_t upload_items(BatchPlan &pl, PhaseList &ph, const std::vector<WorkItem> &items) {
+  ph.n = (int)items.size();
+  if (items.empty()) return cudaSuccess;
+  void *m = nullptr;
+  cudaError_t e = cudaMalloc(&m, sizeof(WorkItem) * items.size());
+  if (e != cudaSuccess) return e;
+  pl.item_mem.push_back(m);
+  ph.d_items = static_cast<WorkItem *>(m);
+  return cudaMemcpy(m, items.data(), sizeof(WorkItem) * items.size(), cudaMemcpyHostToDevice);
+}
+
+// X1 items: per block ceil(npencil / pencils) items of `pencils` pencils,
+// pencils = clamp(round(x1_cells / n1t), 1, 32) and the shared memory bound.
+static std::vector<WorkItem> x1_items(const std::vector<BView> &v, int x1_cells, size_t &smem) {
+  std::vector<WorkItem> items;
+  smem = 0;
+  for (size_t b = 0; b < v.size(); b++) {
+    int pen = (x1_cells + v[b].n1t / 2) / v[b].n1t;
+    pen = std::max(1, std::min(32, pen));
+    while (pen > 1 && (size_t)pen * PHX_NRECON * v[b].n1t * sizeof(double) > 200 * 1024) pen--;
+    smem = std::max(smem, (size_t)pen * PHX_NRECON * v[b].n1t * sizeof(double));
+    const int np = x1_npencil(v[b]);
+    for (int f = 0; f < np; f += pen) items.push_back(WorkItem{(int)b, 0, f, std::min(f + pen, np)});
+  }
+  return items;
+}
+
+static std::string tune_key(const Par &p, const std::vector<BView> &v, bool mink) {
+  std::map<int, int> sizes;
+  for (const BView &b : v) sizes[b.n1t * 1000000 + b.n2t * 1000 + b.n3t]++;
+  std::ostringstream k;
+  k << "recon" << p.recon << (mink ? "-mink" : "-fmks") << "-mhd" << p.mhd;
+  for (const auto &kv : sizes) k << "-" << kv.first << "x" << kv.second;
+  return k.str();
+}
+
+static float time_launch(cudaStream_t s, const std::function<void()> &fn, int reps) {
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  fn();  // warm-up
+  cudaEventRecord(a, s);
+  for (int r = 0; r < reps; r++) fn();
+  cudaEventRecord(b, s);
+  cudaEventSynchronize(b);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return ms / reps;
+}
+
+// Time the candidate tile shapes on the plan's blocks (flux outputs only are
+// written; the stage recomputes them).
+static Tuning autotune(BatchPlan &pl, const std::vector<BView> &v, unsigned int *err, cudaStream_t s) {
+  Tuning best;
+  float best_ms = 1e30f;
+  for (int cells : {96, 192, 288, 384, 576}) {
+    size_t smem;
+    std::vector<WorkItem> items = x1_items(v, cells, smem);
+    PhaseList ph;
+    if (upload_items(pl, ph, items) != cudaSuccess) break;
+    const float ms = time_launch(
+        s, [&] { launch_flux_x1_batched(pl.par, pl.mink, pl.views_in, ph.d_items, ph.n, 0, smem, err, s); }, 3);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best.x1_cells = cells;
+    }
+  }
+  best_ms = 1e30f;
+  for (int seg : {16, 32, 64}) {
+    float ms = 0.f;
+    for (int dir = 1; dir <= pl.ndim - 1; dir++) {
+      std::vector<long long> counts;
+      for (const BView &b : v) counts.push_back(sweep_threads(b, dir, seg));
+      PhaseList ph;
+      if (upload_items(pl, ph, make_items(counts, 128)) != cudaSuccess) break;
+      ms += time_launch(
+          s, [&] { launch_flux_sweep_batched(pl.par, pl.mink, dir, pl.views_in, ph.d_items, ph.n, 0, seg, s); }, 3);
+    }
+    if (ms < best_ms) {
+      best_ms = ms;
+      best.seg = seg;
+    }
+  }
+  return best;
+}
+
+// The stage's launches, in order (captured into the plan's graph).
+static void stage_launches(BatchPlan &pl, DevStats *stats, unsigned int *err, cudaStream_t s) {
+  const Par &p = pl.par;
+  launch_sources_batched(p, pl.mink, pl.views_in, pl.sources.d_items, pl.sources.n, 0, s);
+  launch_flux_x1_batched(p, pl.mink, pl.views_in, pl.x1.d_items, pl.x1.n, 0, pl.x1_smem, err, s);
+  if (pl.ndim >= 2) launch_flux_sweep_batched(p, pl.mink, 1, pl.views_in, pl.x2.d_items, pl.x2.n, 0, pl.tune.seg, s);
+  if (pl.ndim >= 3) launch_flux_sweep_batched(p, pl.mink, 2, pl.views_in, pl.x3.d_items, pl.x3.n, 0, pl.tune.seg, s);
+  if (p.mhd && pl.ndim > 1) launch_fluxct_batched(pl.ndim, pl.views_in, pl.fluxct.d_items, pl.fluxct.n, 0, s);
+  launch_update_batched(p, pl.views_in, pl.base_tab, pl.out_tab, pl.beta_dt, pl.update.d_items, pl.update.n, 0, s);
+  launch_c2p_batched(p, pl.mink, pl.views_out, pl.c2p.d_items, pl.c2p.n, 0, stats, err, s);
+  launch_ghost_batched(pl.views_out, p.mhd ? PHX_NCONS : 5, pl.ghost.d_items, pl.ghost.n, 0, s);
+  launch_c2p_batched(p, pl.mink, pl.views_out, pl.c2p.d_items, pl.c2p.n, 0, stats, err, s);
+}
+
+// Field-wise (phx_block has padding bytes the caller need not initialise).
+static bool same_block(const phx_block &a, const phx_block &b) {
+  if (a.nx1 != b.nx1 || a.nx2 != b.nx2 || a.nx3 != b.nx3 || a.ng != b.ng || a.ndim != b.ndim ||
+      a.var_stride != b.var_stride)
+    return false;
+  if (a.x1min != b.x1min || a.x2min != b.x2min || a.x3min != b.x3min || a.dx1 != b.dx1 || a.dx2 != b.dx2 ||
+      a.dx3 != b.dx3)
+    return false;
+  if (a.prim != b.prim || a.cons != b.cons || a.flux != b.flux || a.face_sig != b.face_sig ||
+      a.cell_sig != b.cell_sig || a.fail != b.fail || a.src != b.src || a.emf != b.emf || a.dudt != b.dudt ||
+      a.geom != b.geom)
+    return false;
+  if (a.geom && (a.geom->kind != b.geom->kind || a.geom->cent != b.geom->cent || a.geom->face1 != b.geom->face1 ||
+                 a.geom->face2 != b.geom->face2 || a.geom->deriv != b.geom->deriv))
+    return false;
+  return true;
+}
+
+static bool same_plan(const BatchPlan &pl, const phx_block *blocks, int n, const double *const *base,
+                      double *const *out, const Par &par) {
+  if ((int)pl.blocks.size() != n) return false;
+  if (memcmp(&pl.par, &par, sizeof(Par)) != 0) return false;  // Par is zero-filled before assignment
+  for (int i = 0; i < n; i++) {
+    if (!same_block(pl.blocks[i], blocks[i])) return false;
+    if (pl.base[i] != base[i] || pl.out[i] != out[i]) return false;
+  }
+  return true;
+}
+
+// Build (or find) the plan of this block set and launch its graph.
+// views: validated views of the blocks (cons = stage input).
+cudaError_t batch_stage(BatchCache *cache, const Par &par, const phx_block *blocks, const BView *views, int n,
+                        const double *const *base, double *const *out, double beta, double dt, DevStats *stats,
+                        unsigned int *err, cudaStream_t s, const char **why) {
+  *why = nullptr;
+  BatchPlan *pl = nullptr;
+  for (auto &q : cache->plans)
+    if (same_plan(*q, blocks, n, base, out, par)) pl = q.get();
+  cudaError_t e = cudaSuccess;
+  if (!pl) {
+    auto np = std::make_unique<BatchPlan>();
+    BatchPlan &P = *np;
+    P.blocks.assign(blocks, blocks + n);
+    P.base.assign(base, base + n);
+    P.out.assign(out, out + n);
+    P.par = par;
+    P.mink = !views[0].fmks;
+    P.ndim = views[0].ndim;
+    std::vector<BView> vin(views, views + n), vout(views, views + n);
+    for (int i = 0; i < n; i++) vout[i].cons = out[i];
+    const size_t bytes = 2 * sizeof(BView) * n + 2 * sizeof(double *) * n + 2 * sizeof(double) + 256 * 4;
+    if ((e = cudaMalloc(&P.mem, bytes)) != cudaSuccess) return e;
+    char *m = static_cast<char *>(P.mem);
+    auto take = [&](size_t b) {
+      char *r = m;
+      m += (b + 255) & ~size_t(255);
+      return r;
+    };
+    P.views_in = reinterpret_cast<BView *>(take(sizeof(BView) * n));
+    P.views_out = reinterpret_cast<BView *>(take(sizeof(BView) * n));
+    P.base_tab = reinterpret_cast<const double **>(take(sizeof(double *) * n));
+    P.out_tab = reinterpret_cast<double **>(take(sizeof(double *) * n));
+    P.beta_dt = reinterpret_cast<double *>(take(2 * sizeof(double)));
+    cudaMemcpy(P.views_in, vin.data(), sizeof(BView) * n, cudaMemcpyHostToDevice);
+    cudaMemcpy(P.views_out, vout.data(), sizeof(BView) * n, cudaMemcpyHostToDevice);
+    cudaMemcpy(P.base_tab, base, sizeof(double *) * n, cudaMemcpyHostToDevice);
+    cudaMemcpy(P.out_tab, out, sizeof(double *) * n, cudaMemcpyHostToDevice);
+    // work lists
+    std::vector<long long> interior, faces, all;
+    for (const BView &b : vin) {
+      interior.push_back(interior_count(b));
+      faces.push_back(fluxct_count(b));
+      all.push_back((long long)b.n1t * b.n2t * b.n3t);
+    }
+    if ((e = upload_items(P, P.sources, make_items(interior, 128))) != cudaSuccess) return e;
+    if ((e = upload_items(P, P.fluxct, make_items(faces, 256))) != cudaSuccess) return e;
+    if ((e = upload_items(P, P.update, make_items(interior, 256))) != cudaSuccess) return e;
+    if ((e = upload_items(P, P.ghost, make_items(all, 256))) != cudaSuccess) return e;
+    if ((e = upload_items(P, P.c2p, make_items(all, 128))) != cudaSuccess) return e;
+    // tile shapes
+    {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      load_tune_file();
+      const std::string key = tune_key(par, vin, P.mink);
+      auto it = g_tune.find(key);
+      if (it != g_tune.end()) {
+        P.tune = it->second;
+      } else {
+        P.tune = autotune(P, vin, err, s);
+        g_tune[key] = P.tune;
+        save_tune_file();
+      }
+    }
+    if ((e = upload_items(P, P.x1, x1_items(vin, P.tune.x1_cells, P.x1_smem))) != cudaSuccess) return e;
+    for (int dir = 1; dir <= 2; dir++) {
+      std::vector<long long> counts;
+      for (const BView &b : vin) counts.push_back(dir < P.ndim ? sweep_threads(b, dir, P.tune.seg) : 0);
+      if ((e = upload_items(P, dir == 1 ? P.x2 : P.x3, make_items(counts, 128))) != cudaSuccess) return e;
+    }
+    if ((e = cudaDeviceSynchronize()) != cudaSuccess) return e;
+    // capture the stage
+    cudaStream_t cs;
+    if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) return e;
+    e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      stage_launches(P, stats, err, cs);
+      e = cudaStreamEndCapture(cs, &P.graph);
+    }
+    cudaStreamDestroy(cs);
+    if (e != cudaSuccess) return e;
+    if ((e = cudaGraphInstantiate(&P.exec, P.graph, 0)) != cudaSuccess) return e;
+    if (cache->plans.size() >= 8) cache->plans.erase(cache->plans.begin());
+    cache->plans.push_back(std::move(np));
+    pl = cache->plans.back().get();
+  }
+  const double bd[2] = {beta, dt};
+  if ((e = cudaMemcpyAsync(pl->beta_dt, bd, sizeof(bd), cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
+  return cudaGraphLaunch(pl->exec, s);
+}
+
+// The tuned shapes of the most recent plan (for reporting).
+void batch_last_tuning(BatchCache *cache, int *x1_cells, int *seg, int *launches) {
+  if (cache->plans.empty()) {
+    *x1_cells = *seg = *launches = 0;
+    return;
+  }
+  const BatchPlan &p = *cache->plans.back();
+  *x1_cells = p.tune.x1_cells;
+  *seg = p.tune.seg;
+  size_t nn = 0;
+  cudaGraphGetNodes(p.graph, nullptr, &nn);
+  *launches = (int)nn;
+}
+
+}  // namespace phx

@@ -514,4 +514,59 @@ void launch_mlp_bracket(const Par &p, long long n, const double *cons, const dou
     launch_bracket_any<ListZones, true>(p, z, 0, n, mlp, bracket, err, s);
 }
 
+// ------------------------------------------------------------- batched
+// con2prim over the entire zones of many blocks: persistent CTAs walk
+// (block, [first, last)) items; the root find runs to completion in place
+// (no iteration cap: the retry list is per chunk of one zone list).
+template <bool MINK>
+__global__ void __launch_bounds__(C2P_THREADS) kb_c2p(Par p, const BView *views, const WorkItem *items, int nitems,
+                                                       DevStats *stats, unsigned int *err) {
+  __shared__ unsigned int s_hist[PHX_C2P_HIST];
+  __shared__ unsigned long long s_cnt[6];
+  if (stats) {
+    for (int h = threadIdx.x; h < PHX_C2P_HIST; h += blockDim.x) s_hist[h] = 0;
+    if (threadIdx.x < 6) s_cnt[threadIdx.x] = 0;
+    __syncthreads();
+  }
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const WorkItem w = items[it];
+    const BView &bv = views[w.block];
+    const BoxZones zones{bv, Range3{0, bv.n1t - 1, 0, bv.n2t - 1, 0, bv.n3t - 1}};
+    const long long q = w.first + threadIdx.x;
+    const bool valid = q < w.last;
+    long long id = 0;
+    Pt g{};
+    double U[PHX_NCONS];
+    bool setup_ok = false;
+    Residual res;
+    double rcon[3], rcov[3], bu[3], Bprim[3] = {0.0, 0.0, 0.0}, bdotr = 0.0, guess = 0.0;
+    if (valid) {
+      double x1, x2, x3;
+      zones.template load<MINK>(q, id, g, U, x1, x2, x3, guess);
+      setup_ok = c2p_setup<MINK>(p, g, U, x1, x2, x3, res, rcon, rcov, bu, Bprim, bdotr);
+    }
+    RFState st;
+    rf_start<false>(p, res, valid && setup_ok, 0.0, 1.0, guess, nullptr, st);
+    rf_iterate(p, res, valid && setup_ok, st, p.c2p_max_iter);
+    if (valid) {
+      C2POut out{0, 0, false, true, false, false};
+      const double mu = rf_result(st, guess, out);
+      c2p_complete<BoxZones, MINK>(p, zones, id, g, res, mu, rcon, bu, Bprim, bdotr, U, setup_ok, out, stats, s_hist,
+                                   s_cnt, err);
+    }
+  }
+  if (stats) c2p_flush_stats(stats, s_hist, s_cnt);
+}
+
+void launch_c2p_batched(const Par &p, bool mink, const BView *views, const WorkItem *items, int nitems, int grid,
+                        DevStats *stats, unsigned int *err, cudaStream_t s) {
+  if (nitems <= 0) return;
+  if (mink)
+    kb_c2p<true><<<persistent_grid(kb_c2p<true>, C2P_THREADS, 0, nitems, grid), C2P_THREADS, 0, s>>>(
+        p, views, items, nitems, stats, err);
+  else
+    kb_c2p<false><<<persistent_grid(kb_c2p<false>, C2P_THREADS, 0, nitems, grid), C2P_THREADS, 0, s>>>(
+        p, views, items, nitems, stats, err);
+}
+
 }  // namespace phx

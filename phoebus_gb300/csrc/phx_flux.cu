@@ -70,59 +70,80 @@ __device__ __forceinline__ void face_flux(const Par &p, const BView &b, int k, i
 constexpr int X1_WARPS = 4;    // warps per CTA
 constexpr int X1_PENCILS = 4;  // (k, j) pencils staged per CTA
 
-// A CTA stages X1_PENCILS pencils (10 primitive rows each) in shared memory
-// with TMA bulk copies completing on one mbarrier.  Its warps then walk the
-// pencils' cells as one flattened list [pencil][cell is-1 .. ie+1] in chunks
-// of 32 cells that overlap by one: lane L reconstructs its cell, takes the
+// A CTA stages np pencils (10 primitive rows each) in shared memory with TMA
+// bulk copies completing on one mbarrier.  Its warps then walk the pencils'
+// cells as one flattened list [pencil][cell is-1 .. ie+1] in chunks of 32
+// cells that overlap by one: lane L reconstructs its cell, takes the
 // upper-face state of the cell on its left from lane L-1 (__shfl_up_sync) and
 // solves the Riemann problem of its lower face; lane 0 only supplies its
 // state to lane 1 (its own face belongs to the previous chunk's lane 31).
-template <int RECON, bool MINK>
-__global__ void __launch_bounds__(32 * X1_WARPS)
-    k_flux_x1(Par p, BView b, int jlo, int nj, int klo, int npencil, int use_tma, unsigned int *err) {
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  __shared__ __align__(8) uint64_t bar;
+
+// X1 face ranges of a block: pencils (k, j) over k in [ks-dk, ke+dk],
+// j in [js-dj, je+dj]; pencil pen is (klo + pen / nj, jlo + pen % nj).
+struct X1Range {
+  int jlo, nj, klo, npencil;
+};
+__host__ __device__ __forceinline__ X1Range x1_range(const BView &b) {
+  const int dk = b.ndim == 3 ? 1 : 0, dj = b.ndim > 1 ? 1 : 0;
+  const int js = dj ? b.ng : 0, je = dj ? b.ng + b.nx2 - 1 : 0;
+  const int ks = dk ? b.ng : 0, ke = dk ? b.ng + b.nx3 - 1 : 0;
+  X1Range r;
+  r.jlo = js - dj;
+  r.nj = je - js + 1 + 2 * dj;
+  r.klo = ks - dk;
+  r.npencil = r.nj * (ke - ks + 1 + 2 * dk);
+  return r;
+}
+__host__ __device__ __forceinline__ bool x1_tma_ok(const BView &b) {
+  return (b.n1t % 2 == 0) && (b.vs % 2 == 0) && ((reinterpret_cast<uintptr_t>(b.prim) & 15) == 0);
+}
+
+// Stage pencils p0 .. p0+np-1 into rows (mbarrier phase parity `phase` when
+// use_tma).  Returns false, with ERR_TIMEOUT set, when the bounded wait gave
+// up; every thread returns the same value.
+__device__ __forceinline__ bool x1_stage(const BView &b, const X1Range &xr, int p0, int np, bool use_tma,
+                                         double *rows, uint64_t *bar, unsigned phase, unsigned int *err) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n1t = b.n1t;
-  double *rows = reinterpret_cast<double *>(smem_raw);
-  const int p0 = blockIdx.x * X1_PENCILS;
-  const int np = min(X1_PENCILS, npencil - p0);
   if (use_tma) {
-    if (threadIdx.x == 0) {
-      mbar_init(&bar, 1);
-      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
     const unsigned bytes = (unsigned)(n1t * sizeof(double));
-    if (threadIdx.x == 0) mbar_expect_tx(&bar, bytes * PHX_NRECON * np);
+    if (threadIdx.x == 0) mbar_expect_tx(bar, bytes * PHX_NRECON * np);
     __syncthreads();
     if (threadIdx.x < np * PHX_NRECON) {  // one bulk copy per (pencil, variable) row
       const int pp = threadIdx.x / PHX_NRECON, v = threadIdx.x % PHX_NRECON;
       const int pen = p0 + pp;
-      const long long base = b.idx(klo + pen / nj, jlo + pen % nj, 0);
-      bulk_g2s(rows + (long long)(pp * PHX_NRECON + v) * n1t, b.prim + v * b.vs + base, bytes, &bar);
+      const long long base = b.idx(xr.klo + pen / xr.nj, xr.jlo + pen % xr.nj, 0);
+      bulk_g2s(rows + (long long)(pp * PHX_NRECON + v) * n1t, b.prim + v * b.vs + base, bytes, bar);
     }
-    long long spins = 0;
-    while (!mbar_try_wait(&bar, 0)) {
-      if (++spins > MBAR_SPIN_LIMIT) {
-        if (threadIdx.x == 0) atomicOr(err, ERR_TIMEOUT);
-        return;  // every thread gives up on the same bounded wait
-      }
-    }
-  } else {
-    for (int r = warp; r < np * PHX_NRECON; r += X1_WARPS) {
-      const int pp = r / PHX_NRECON, v = r % PHX_NRECON;
-      const int pen = p0 + pp;
-      const long long base = b.idx(klo + pen / nj, jlo + pen % nj, 0);
-      for (int i = lane; i < n1t; i += 32) rows[(long long)r * n1t + i] = b.prim[v * b.vs + base + i];
-    }
+    bool done = false;
+    for (long long spins = 0; spins < MBAR_SPIN_LIMIT && !done; spins++) done = mbar_try_wait(bar, phase);
+    if (__syncthreads_and(done)) return true;
+    for (long long spins = 0; spins < MBAR_SPIN_LIMIT && !done; spins++) done = mbar_try_wait(bar, phase);
+    if (threadIdx.x == 0) atomicOr(err, ERR_TIMEOUT);
     __syncthreads();
+    return false;
   }
+  for (int r = warp; r < np * PHX_NRECON; r += (int)(blockDim.x >> 5)) {
+    const int pp = r / PHX_NRECON, v = r % PHX_NRECON;
+    const int pen = p0 + pp;
+    const long long base = b.idx(xr.klo + pen / xr.nj, xr.jlo + pen % xr.nj, 0);
+    for (int i = lane; i < n1t; i += 32) rows[(long long)r * n1t + i] = b.prim[v * b.vs + base + i];
+  }
+  __syncthreads();
+  return true;
+}
+
+template <int RECON, bool MINK>
+__device__ __forceinline__ void x1_compute(const Par &p, const BView &b, const X1Range &xr, int p0, int np,
+                                           const double *rows) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nwarps = (int)(blockDim.x >> 5);
+  const int n1t = b.n1t;
   const int c0 = b.is() - 1;
   const int ncell = b.ie() + 1 - c0 + 1;  // cells is-1 .. ie+1 per pencil
   const int nslot = np * ncell;
   const int nchunk = (nslot - 1 + 30) / 31;
-  for (int ch = warp; ch < nchunk; ch += X1_WARPS) {
+  for (int ch = warp; ch < nchunk; ch += nwarps) {
     const int slot = ch * 31 + lane;
     const bool have = slot < nslot;
     const int pp = have ? slot / ncell : 0;
@@ -149,8 +170,51 @@ __global__ void __launch_bounds__(32 * X1_WARPS)
     // face of cell c: left state from cell c-1 (same pencil when c > is-1)
     if (have && lane > 0 && c > c0) {
       const int pen = p0 + pp;
-      face_flux<MINK, 0>(p, b, klo + pen / nj, jlo + pen % nj, c, left, qr);
+      face_flux<MINK, 0>(p, b, xr.klo + pen / xr.nj, xr.jlo + pen % xr.nj, c, left, qr);
     }
+  }
+}
+
+template <int RECON, bool MINK>
+__global__ void __launch_bounds__(32 * X1_WARPS) k_flux_x1(Par p, BView b, int use_tma, unsigned int *err) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bar;
+  double *rows = reinterpret_cast<double *>(smem_raw);
+  const X1Range xr = x1_range(b);
+  const int p0 = blockIdx.x * X1_PENCILS;
+  const int np = min(X1_PENCILS, xr.npencil - p0);
+  if (use_tma && threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (!x1_stage(b, xr, p0, np, use_tma != 0, rows, &bar, 0u, err)) return;
+  x1_compute<RECON, MINK>(p, b, xr, p0, np, rows);
+}
+
+// Batched X1: a persistent CTA walks the work list; item = (block, first
+// pencil, pencil count).  The mbarrier is reused with alternating phase.
+template <int RECON, bool MINK>
+__global__ void __launch_bounds__(32 * X1_WARPS) kb_flux_x1(Par p, const BView *views, const WorkItem *items,
+                                                            int nitems, unsigned int *err) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bar;
+  double *rows = reinterpret_cast<double *>(smem_raw);
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  unsigned phase = 0;
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const WorkItem w = items[it];
+    const BView &b = views[w.block];
+    const X1Range xr = x1_range(b);
+    const bool tma = x1_tma_ok(b);
+    if (!x1_stage(b, xr, (int)w.first, (int)(w.last - w.first), tma, rows, &bar, phase, err)) return;
+    if (tma) phase ^= 1u;
+    x1_compute<RECON, MINK>(p, b, xr, (int)w.first, (int)(w.last - w.first), rows);
+    __syncthreads();  // rows are rewritten by the next item
   }
 }
 
@@ -158,12 +222,8 @@ __global__ void __launch_bounds__(32 * X1_WARPS)
 // Thread = (transverse a, transverse c, segment).  DIR 1: a = i, c = k;
 // DIR 2: a = i, c = j; DIR 0 (fallback for X1): a = j, c = k.
 template <int RECON, bool MINK, int DIR>
-__global__ void __launch_bounds__(128)
-    k_flux_sweep(Par p, BView b, int alo, int na, int clo, int nc, int f0, int nface, int seg,
-                 int nseg) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long total = (long long)na * nc * nseg;
-  if (t >= total) return;
+__device__ __forceinline__ void sweep_at(const Par &p, const BView &b, int alo, int na, int clo, int nc, int f0,
+                                         int nface, int seg, int nseg, long long t) {
   const int a = alo + (int)(t % na);
   const long long q = t / na;
   const int s = (int)(q % nseg);
@@ -225,6 +285,57 @@ __global__ void __launch_bounds__(128)
 }
 
 template <int RECON, bool MINK, int DIR>
+__global__ void __launch_bounds__(128)
+    k_flux_sweep(Par p, BView b, int alo, int na, int clo, int nc, int f0, int nface, int seg, int nseg) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < (long long)na * nc * nseg) sweep_at<RECON, MINK, DIR>(p, b, alo, na, clo, nc, f0, nface, seg, nseg, t);
+}
+
+// Sweep geometry of a block for DIR 1 (X2 faces: j in [js, je+1], i in
+// [is-1, ie+1], k in [ks-dk, ke+dk]) and DIR 2 (X3 faces: k in [ks, ke+1],
+// i in [is-1, ie+1], j in [js-1, je+1]); threads per block na * nc * nseg.
+struct SweepRange {
+  int alo, na, clo, nc, f0, nface, seg, nseg;
+};
+__host__ __device__ __forceinline__ SweepRange sweep_range(const BView &b, int dir, int seg_target) {
+  const int dk = b.ndim == 3 ? 1 : 0;
+  const int is = b.ng, ie = b.ng + b.nx1 - 1;
+  const int js = b.ng, je = b.ng + b.nx2 - 1;
+  const int ks = dk ? b.ng : 0, ke = dk ? b.ng + b.nx3 - 1 : 0;
+  SweepRange r;
+  r.alo = is - 1;
+  r.na = ie - is + 3;
+  if (dir == 1) {
+    r.clo = ks - dk;
+    r.nc = ke - ks + 1 + 2 * dk;
+    r.f0 = js;
+    r.nface = je - js + 2;
+  } else {
+    r.clo = js - 1;
+    r.nc = je - js + 3;
+    r.f0 = ks;
+    r.nface = ke - ks + 2;
+  }
+  r.nseg = (r.nface + seg_target - 1) / seg_target;
+  r.seg = (r.nface + r.nseg - 1) / r.nseg;
+  return r;
+}
+
+template <int RECON, bool MINK, int DIR>
+__global__ void __launch_bounds__(128) kb_flux_sweep(Par p, const BView *views, const WorkItem *items, int nitems,
+                                                     int seg_target) {
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const WorkItem w = items[it];
+    const long long t = w.first + threadIdx.x;
+    if (t < w.last) {
+      const BView &b = views[w.block];
+      const SweepRange r = sweep_range(b, DIR, seg_target);
+      sweep_at<RECON, MINK, DIR>(p, b, r.alo, r.na, r.clo, r.nc, r.f0, r.nface, r.seg, r.nseg, t);
+    }
+  }
+}
+
+template <int RECON, bool MINK, int DIR>
 static void launch_sweep(const Par &p, const BView &b, int alo, int na, int clo, int nc, int f0,
                          int nface, cudaStream_t s) {
   const int target = 32;
@@ -245,17 +356,14 @@ static void launch_fluxes_t(const Par &p, const BView &b, unsigned int *err, cud
   const int ks = dk ? b.ng : 0, ke = dk ? b.ng + b.nx3 - 1 : 0;
   // X1 faces: i in [is, ie+1]; j in [js-dj, je+dj]; k in [ks-dk, ke+dk]
   {
-    const int jlo = js - dj, nj = je - js + 1 + 2 * dj;
-    const int klo = ks - dk, nk = ke - ks + 1 + 2 * dk;
-    const int npencil = nj * nk;
+    const X1Range xr = x1_range(b);
+    const int jlo = xr.jlo, nj = xr.nj, klo = xr.klo, nk = xr.npencil / xr.nj;
     const size_t smem = (size_t)X1_PENCILS * PHX_NRECON * b.n1t * sizeof(double);
-    const bool aligned = (b.n1t % 2 == 0) && (b.vs % 2 == 0) &&
-                         ((reinterpret_cast<uintptr_t>(b.prim) & 15) == 0);
     if (smem <= 200 * 1024) {
       auto kern = k_flux_x1<RECON, MINK>;
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      kern<<<(npencil + X1_PENCILS - 1) / X1_PENCILS, 32 * X1_WARPS, smem, s>>>(p, b, jlo, nj, klo, npencil,
-                                                                              aligned ? 1 : 0, err);
+      kern<<<(xr.npencil + X1_PENCILS - 1) / X1_PENCILS, 32 * X1_WARPS, smem, s>>>(p, b, x1_tma_ok(b) ? 1 : 0,
+                                                                                   err);
     } else {
       launch_sweep<RECON, MINK, 0>(p, b, jlo, nj, klo, nk, is, ie - is + 2, s);
     }
@@ -288,6 +396,62 @@ void launch_fluxes_err(const Par &p, const BView &b, unsigned int *err, cudaStre
          : launch_fluxes_t<PHX_RECON_CONSTANT, false>(p, b, err, s);
     break;
   }
+}
+
+// ------------------------------------------------------------- batched
+int x1_npencil(const BView &b) { return x1_range(b).npencil; }
+bool x1_tma_ok_host(const BView &b) { return x1_tma_ok(b); }
+long long sweep_threads(const BView &b, int dir, int seg_target) {
+  const SweepRange r = sweep_range(b, dir, seg_target);
+  return (long long)r.na * r.nc * r.nseg;
+}
+
+template <int RECON, bool MINK>
+static void x1_batched_t(const Par &p, const BView *views, const WorkItem *items, int nitems, int grid, size_t smem,
+                         unsigned int *err, cudaStream_t s) {
+  auto kern = kb_flux_x1<RECON, MINK>;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  kern<<<persistent_grid(kern, 32 * X1_WARPS, smem, nitems, grid), 32 * X1_WARPS, smem, s>>>(p, views, items,
+                                                                                             nitems, err);
+}
+
+template <int RECON, bool MINK>
+static void sweep_batched_t(const Par &p, int dir, const BView *views, const WorkItem *items, int nitems, int grid,
+                            int seg_target, cudaStream_t s) {
+  if (dir == 1)
+    kb_flux_sweep<RECON, MINK, 1><<<persistent_grid(kb_flux_sweep<RECON, MINK, 1>, 128, 0, nitems, grid), 128, 0, s>>>(
+        p, views, items, nitems, seg_target);
+  else
+    kb_flux_sweep<RECON, MINK, 2><<<persistent_grid(kb_flux_sweep<RECON, MINK, 2>, 128, 0, nitems, grid), 128, 0, s>>>(
+        p, views, items, nitems, seg_target);
+}
+
+#define PHX_RECON_DISPATCH(FN, ...)                                                         \
+  switch (p.recon) {                                                                        \
+  case PHX_RECON_WENO5Z:                                                                    \
+    mink ? FN<PHX_RECON_WENO5Z, true>(__VA_ARGS__) : FN<PHX_RECON_WENO5Z, false>(__VA_ARGS__); \
+    break;                                                                                  \
+  case PHX_RECON_MP5:                                                                       \
+    mink ? FN<PHX_RECON_MP5, true>(__VA_ARGS__) : FN<PHX_RECON_MP5, false>(__VA_ARGS__);     \
+    break;                                                                                  \
+  case PHX_RECON_LINEAR:                                                                    \
+    mink ? FN<PHX_RECON_LINEAR, true>(__VA_ARGS__) : FN<PHX_RECON_LINEAR, false>(__VA_ARGS__); \
+    break;                                                                                  \
+  default:                                                                                  \
+    mink ? FN<PHX_RECON_CONSTANT, true>(__VA_ARGS__) : FN<PHX_RECON_CONSTANT, false>(__VA_ARGS__); \
+    break;                                                                                  \
+  }
+
+void launch_flux_x1_batched(const Par &p, bool mink, const BView *views, const WorkItem *items, int nitems, int grid,
+                            size_t smem, unsigned int *err, cudaStream_t s) {
+  if (nitems <= 0) return;
+  PHX_RECON_DISPATCH(x1_batched_t, p, views, items, nitems, grid, smem, err, s)
+}
+
+void launch_flux_sweep_batched(const Par &p, bool mink, int dir, const BView *views, const WorkItem *items,
+                               int nitems, int grid, int seg_target, cudaStream_t s) {
+  if (nitems <= 0) return;
+  PHX_RECON_DISPATCH(sweep_batched_t, p, dir, views, items, nitems, grid, seg_target, s)
 }
 
 }  // namespace phx

@@ -21,6 +21,14 @@ struct Range3 {
   int is, ie, js, je, ks, ke;
 };
 
+// One CTA's share of a batched launch: indices [first, last) of one block's
+// index space for that phase (zones, faces, pencils or sweep threads).
+struct WorkItem {
+  int block;
+  int pad;
+  long long first, last;
+};
+
 void launch_p2c(const Par &p, const BView &b, Range3 r, cudaStream_t s);
 struct MlpPacked;
 // con2prim works in chunks of C2P_CHUNK zones; per chunk the context holds
@@ -68,5 +76,43 @@ void launch_mlp_grad(const float *theta, const float *x, const float *y, long lo
 void launch_mlp_adamw(float *theta, float *grad, float *m, float *v, float lr, float b1, float b2, float eps,
                       float wd, float c1, float c2, cudaStream_t s);
 void launch_fp64_probe(double *out, int iters, cudaStream_t s, int *nthreads_out);
+
+// ---- batched (many blocks, one persistent launch per phase; phx_batch.cu)
+// Grid of a persistent launch: as many CTAs as fit on the GPU at once (or
+// fewer when there are fewer items); grid > 0 is taken as given.
+template <class K>
+inline int persistent_grid(K kernel, int threads, size_t smem, int nitems, int grid) {
+  if (grid > 0) return grid < nitems ? grid : nitems;
+  int dev = 0, nsm = 0, occ = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, smem);
+  const long long g = (long long)(nsm > 0 ? nsm : 1) * (occ > 0 ? occ : 1);
+  return (int)(g < nitems ? g : nitems);
+}
+struct BatchCache;
+BatchCache *batch_cache_create();
+void batch_cache_destroy(BatchCache *c);
+cudaError_t batch_stage(BatchCache *cache, const Par &par, const phx_block *blocks, const BView *views, int n,
+                        const double *const *base, double *const *out, double beta, double dt, DevStats *stats,
+                        unsigned int *err, cudaStream_t s, const char **why);
+void batch_last_tuning(BatchCache *cache, int *x1_cells, int *seg, int *launches);
+long long interior_count(const BView &b);
+long long fluxct_count(const BView &b);
+void launch_sources_batched(const Par &p, bool mink, const BView *views, const WorkItem *items, int nitems, int grid,
+                            cudaStream_t s);
+void launch_fluxct_batched(int ndim, const BView *views, const WorkItem *items, int nitems, int grid, cudaStream_t s);
+void launch_update_batched(const Par &p, const BView *views, const double *const *base, double *const *out,
+                           const double *beta_dt, const WorkItem *items, int nitems, int grid, cudaStream_t s);
+void launch_ghost_batched(const BView *views, int nvar, const WorkItem *items, int nitems, int grid, cudaStream_t s);
+void launch_c2p_batched(const Par &p, bool mink, const BView *views, const WorkItem *items, int nitems, int grid,
+                        DevStats *stats, unsigned int *err, cudaStream_t s);
+void launch_flux_x1_batched(const Par &p, bool mink, const BView *views, const WorkItem *items, int nitems, int grid,
+                            size_t smem, unsigned int *err, cudaStream_t s);
+void launch_flux_sweep_batched(const Par &p, bool mink, int dir, const BView *views, const WorkItem *items,
+                               int nitems, int grid, int seg_target, cudaStream_t s);
+int x1_npencil(const BView &b);
+long long sweep_threads(const BView &b, int dir, int seg_target);
+bool x1_tma_ok_host(const BView &b);
 
 }  // namespace phx

@@ -12,12 +12,13 @@ __device__ __forceinline__ double &FX(const BView &b, int d, int m, long long id
 }
 
 // ---------------------------------------------------------------- FluxCT
-__global__ void k_emf3d(BView b, int is, int js, int ks, int ni, int nj, long long n) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  const int i = is + (int)(t % ni);
-  const int j = js + (int)((t / ni) % nj);
-  const int k = ks + (int)(t / ((long long)ni * nj));
+// Bodies take the face index t over the (nx1+1)(nx2+1)(nx3+1) interior
+// corners (3D) or (nx1+1)(nx2+1) (2D), starting at (ng, ng, ng).
+__device__ __forceinline__ void emf3d_at(const BView &b, long long t) {
+  const int ni = b.nx1 + 1, nj = b.nx2 + 1;
+  const int i = b.ng + (int)(t % ni);
+  const int j = b.ng + (int)((t / ni) % nj);
+  const int k = b.ng + (int)(t / ((long long)ni * nj));
   const long long id = b.idx(k, j, i);
   const long long dk = (long long)b.n1t * b.n2t, dj = b.n1t;
   const int B1 = PHX_CB, B2 = PHX_CB + 1, B3 = PHX_CB + 2;
@@ -25,12 +26,11 @@ __global__ void k_emf3d(BView b, int is, int js, int ks, int ni, int nj, long lo
   b.emf[b.vs + id] = -0.25 * (FX(b, 0, B3, id) + FX(b, 0, B3, id - dk) - FX(b, 2, B1, id) - FX(b, 2, B1, id - 1));
   b.emf[2 * b.vs + id] = 0.25 * (FX(b, 0, B2, id) + FX(b, 0, B2, id - dj) - FX(b, 1, B1, id) - FX(b, 1, B1, id - 1));
 }
-__global__ void k_ctflux3d(BView b, int is, int js, int ks, int ni, int nj, long long n) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  const int i = is + (int)(t % ni);
-  const int j = js + (int)((t / ni) % nj);
-  const int k = ks + (int)(t / ((long long)ni * nj));
+__device__ __forceinline__ void ctflux3d_at(const BView &b, long long t) {
+  const int ni = b.nx1 + 1, nj = b.nx2 + 1;
+  const int i = b.ng + (int)(t % ni);
+  const int j = b.ng + (int)((t / ni) % nj);
+  const int k = b.ng + (int)(t / ((long long)ni * nj));
   const long long id = b.idx(k, j, i);
   const long long dk = (long long)b.n1t * b.n2t, dj = b.n1t;
   const double *e0 = b.emf, *e1 = b.emf + b.vs, *e2 = b.emf + 2 * b.vs;
@@ -45,20 +45,18 @@ __global__ void k_ctflux3d(BView b, int is, int js, int ks, int ni, int nj, long
   FX(b, 2, B2, id) = -0.5 * (e0[id] + e0[id + dj]);
   FX(b, 2, B3, id) = 0.0;
 }
-__global__ void k_emf2d(BView b, int is, int js, int ni, long long n) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  const int i = is + (int)(t % ni);
-  const int j = js + (int)(t / ni);
+__device__ __forceinline__ void emf2d_at(const BView &b, long long t) {
+  const int ni = b.nx1 + 1;
+  const int i = b.ng + (int)(t % ni);
+  const int j = b.ng + (int)(t / ni);
   const long long id = b.idx(0, j, i), dj = b.n1t;
   const int B1 = PHX_CB, B2 = PHX_CB + 1;
   b.emf[id] = 0.25 * (FX(b, 0, B2, id) + FX(b, 0, B2, id - dj) - FX(b, 1, B1, id) - FX(b, 1, B1, id - 1));
 }
-__global__ void k_ctflux2d(BView b, int is, int js, int ni, long long n) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  const int i = is + (int)(t % ni);
-  const int j = js + (int)(t / ni);
+__device__ __forceinline__ void ctflux2d_at(const BView &b, long long t) {
+  const int ni = b.nx1 + 1;
+  const int i = b.ng + (int)(t % ni);
+  const int j = b.ng + (int)(t / ni);
   const long long id = b.idx(0, j, i), dj = b.n1t;
   const int B1 = PHX_CB, B2 = PHX_CB + 1;
   FX(b, 0, B1, id) = 0.0;
@@ -67,31 +65,51 @@ __global__ void k_ctflux2d(BView b, int is, int js, int ni, long long n) {
   FX(b, 1, B2, id) = 0.0;
 }
 
+__global__ void k_emf3d(BView b, long long n) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) emf3d_at(b, t);
+}
+__global__ void k_ctflux3d(BView b, long long n) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) ctflux3d_at(b, t);
+}
+__global__ void k_emf2d(BView b, long long n) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) emf2d_at(b, t);
+}
+__global__ void k_ctflux2d(BView b, long long n) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) ctflux2d_at(b, t);
+}
+
+long long fluxct_count(const BView &b) {
+  if (b.ndim == 3) return (long long)(b.nx1 + 1) * (b.nx2 + 1) * (b.nx3 + 1);
+  if (b.ndim == 2) return (long long)(b.nx1 + 1) * (b.nx2 + 1);
+  return 0;
+}
+
 void launch_fluxct(const BView &b, cudaStream_t s) {
   const int T = 256;
+  const long long n = fluxct_count(b);
+  if (n == 0) return;
+  const unsigned g = (unsigned)((n + T - 1) / T);
   if (b.ndim == 3) {
-    const int ni = b.nx1 + 1, nj = b.nx2 + 1, nk = b.nx3 + 1;
-    const long long n = (long long)ni * nj * nk;
-    const unsigned g = (unsigned)((n + T - 1) / T);
-    k_emf3d<<<g, T, 0, s>>>(b, b.ng, b.ng, b.ng, ni, nj, n);
-    k_ctflux3d<<<g, T, 0, s>>>(b, b.ng, b.ng, b.ng, ni, nj, n);
-  } else if (b.ndim == 2) {
-    const int ni = b.nx1 + 1, nj = b.nx2 + 1;
-    const long long n = (long long)ni * nj;
-    const unsigned g = (unsigned)((n + T - 1) / T);
-    k_emf2d<<<g, T, 0, s>>>(b, b.ng, b.ng, ni, n);
-    k_ctflux2d<<<g, T, 0, s>>>(b, b.ng, b.ng, ni, n);
+    k_emf3d<<<g, T, 0, s>>>(b, n);
+    k_ctflux3d<<<g, T, 0, s>>>(b, n);
+  } else {
+    k_emf2d<<<g, T, 0, s>>>(b, n);
+    k_ctflux2d<<<g, T, 0, s>>>(b, n);
   }
 }
 
 // -------------------------------------- FluxDivergence + RK2 stage update
 // dudt = -(A1 dF1 + A2 dF2 + A3 dF3) / V (+ src for S_i, tau);
 // u0 = beta u0 + (1 - beta) base; out = u0 + (beta dt) dudt.
-__global__ void __launch_bounds__(256) k_update(BView b, const double *base, double *out, double beta,
-                                                double bdt, double A1, double A2, double A3,
-                                                double V, int ncons, long long n) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
+// t runs over the interior zones.
+__device__ __forceinline__ void update_at(const BView &b, const double *base, double *out, double beta, double bdt,
+                                          int ncons, long long t) {
+  const double dx1 = b.dx[0], dx2 = b.dx[1], dx3 = b.dx[2];
+  const double A1 = dx2 * dx3, A2 = dx1 * dx3, A3 = dx1 * dx2, V = dx1 * dx2 * dx3;
   const int ni = b.nx1, nj = b.ndim >= 2 ? b.nx2 : 1;
   const int i = b.ng + (int)(t % ni);
   const int j = (b.ndim >= 2 ? b.ng : 0) + (int)((t / ni) % nj);
@@ -115,14 +133,21 @@ __global__ void __launch_bounds__(256) k_update(BView b, const double *base, dou
   }
 }
 
+__global__ void __launch_bounds__(256) k_update(BView b, const double *base, double *out, double beta,
+                                                double bdt, int ncons, long long n) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) update_at(b, base, out, beta, bdt, ncons, t);
+}
+
+long long interior_count(const BView &b) {
+  return (long long)b.nx1 * (b.ndim >= 2 ? b.nx2 : 1) * (b.ndim >= 3 ? b.nx3 : 1);
+}
+
 void launch_update(const Par &p, const BView &b, const double *base, double *out, double beta,
                    double dt, cudaStream_t s) {
-  const double dx1 = b.dx[0], dx2 = b.dx[1], dx3 = b.dx[2];
-  const double A1 = dx2 * dx3, A2 = dx1 * dx3, A3 = dx1 * dx2, V = dx1 * dx2 * dx3;
-  const long long n = (long long)b.nx1 * (b.ndim >= 2 ? b.nx2 : 1) * (b.ndim >= 3 ? b.nx3 : 1);
+  const long long n = interior_count(b);
   const int T = 256;
-  k_update<<<(unsigned)((n + T - 1) / T), T, 0, s>>>(b, base, out, beta, beta * dt, A1, A2, A3, V,
-                                                    p.mhd ? PHX_NCONS : 5, n);
+  k_update<<<(unsigned)((n + T - 1) / T), T, 0, s>>>(b, base, out, beta, beta * dt, p.mhd ? PHX_NCONS : 5, n);
 }
 
 // ------------------------------------------------ periodic ghost exchange
@@ -131,9 +156,7 @@ __device__ __forceinline__ int wrap(int x, int ng, int n) {
   if (x >= ng + n) return x - n;
   return x;
 }
-__global__ void __launch_bounds__(256) k_ghost(BView b, double *field, int nvar, long long n) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
+__device__ __forceinline__ void ghost_at(const BView &b, double *field, int nvar, long long t) {
   const int i = (int)(t % b.n1t);
   const int j = (int)((t / b.n1t) % b.n2t);
   const int k = (int)(t / ((long long)b.n1t * b.n2t));
@@ -143,6 +166,10 @@ __global__ void __launch_bounds__(256) k_ghost(BView b, double *field, int nvar,
   if (si == i && sj == j && sk == k) return;
   const long long d = b.idx(k, j, i), src = b.idx(sk, sj, si);
   for (int v = 0; v < nvar; v++) field[v * b.vs + d] = field[v * b.vs + src];
+}
+__global__ void __launch_bounds__(256) k_ghost(BView b, double *field, int nvar, long long n) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) ghost_at(b, field, nvar, t);
 }
 
 void launch_ghost_periodic(const BView &b, double *field, int nvar, cudaStream_t s) {
@@ -199,9 +226,7 @@ void launch_dt(const Par &p, const BView &b, int use_face, unsigned long long *s
 
 // ------------------------------------------------------------- sources
 template <bool MINK>
-__global__ void __launch_bounds__(128) k_sources(Par p, BView b, long long n) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
+__device__ __forceinline__ void sources_at(const Par &p, const BView &b, long long t) {
   const int ni = b.nx1, nj = b.ndim >= 2 ? b.nx2 : 1;
   const int i = b.ng + (int)(t % ni);
   const int j = (b.ndim >= 2 ? b.ng : 0) + (int)((t / ni) % nj);
@@ -296,13 +321,99 @@ __global__ void __launch_bounds__(128) k_sources(Par p, BView b, long long n) {
   }
 }
 
+template <bool MINK>
+__global__ void __launch_bounds__(128) k_sources(Par p, BView b, long long n) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) sources_at<MINK>(p, b, t);
+}
+
 void launch_sources(const Par &p, const BView &b, cudaStream_t s) {
-  const long long n = (long long)b.nx1 * (b.ndim >= 2 ? b.nx2 : 1) * (b.ndim >= 3 ? b.nx3 : 1);
+  const long long n = interior_count(b);
   const int T = 128;
   if (b.fmks)
     k_sources<false><<<(unsigned)((n + T - 1) / T), T, 0, s>>>(p, b, n);
   else
     k_sources<true><<<(unsigned)((n + T - 1) / T), T, 0, s>>>(p, b, n);
+}
+
+// ------------------------------------------------------------- batched
+// Persistent CTAs walk a work list of (block, [first, last)) items; each
+// thread handles index first + threadIdx.x of its item's block.
+template <bool MINK>
+__global__ void __launch_bounds__(128) kb_sources(Par p, const BView *views, const WorkItem *items, int nitems) {
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const WorkItem w = items[it];
+    const long long t = w.first + threadIdx.x;
+    if (t < w.last) sources_at<MINK>(p, views[w.block], t);
+  }
+}
+template <int NDIM, bool EMF>
+__global__ void __launch_bounds__(256) kb_fluxct(const BView *views, const WorkItem *items, int nitems) {
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const WorkItem w = items[it];
+    const long long t = w.first + threadIdx.x;
+    if (t < w.last) {
+      const BView &b = views[w.block];
+      if constexpr (NDIM == 3) {
+        if constexpr (EMF) emf3d_at(b, t); else ctflux3d_at(b, t);
+      } else {
+        if constexpr (EMF) emf2d_at(b, t); else ctflux2d_at(b, t);
+      }
+    }
+  }
+}
+// beta_dt (device): beta and dt of the stage, read at run time so that a
+// captured graph serves every step.
+__global__ void __launch_bounds__(256) kb_update(const BView *views, const double *const *base, double *const *out,
+                                                 const double *beta_dt, int ncons, const WorkItem *items,
+                                                 int nitems) {
+  const double beta = beta_dt[0], bdt = beta_dt[0] * beta_dt[1];
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const WorkItem w = items[it];
+    const long long t = w.first + threadIdx.x;
+    if (t < w.last) update_at(views[w.block], base[w.block], out[w.block], beta, bdt, ncons, t);
+  }
+}
+__global__ void __launch_bounds__(256) kb_ghost(const BView *views, int nvar, const WorkItem *items, int nitems) {
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const WorkItem w = items[it];
+    const long long t = w.first + threadIdx.x;
+    if (t < w.last) {
+      const BView &b = views[w.block];
+      ghost_at(b, b.cons, nvar, t);
+    }
+  }
+}
+
+void launch_sources_batched(const Par &p, bool mink, const BView *views, const WorkItem *items, int nitems, int grid,
+                            cudaStream_t s) {
+  if (nitems <= 0) return;
+  if (mink)
+    kb_sources<true><<<persistent_grid(kb_sources<true>, 128, 0, nitems, grid), 128, 0, s>>>(p, views, items, nitems);
+  else
+    kb_sources<false><<<persistent_grid(kb_sources<false>, 128, 0, nitems, grid), 128, 0, s>>>(p, views, items,
+                                                                                              nitems);
+}
+void launch_fluxct_batched(int ndim, const BView *views, const WorkItem *items, int nitems, int grid, cudaStream_t s) {
+  if (nitems <= 0) return;
+  const int g = persistent_grid(kb_fluxct<3, true>, 256, 0, nitems, grid);
+  if (ndim == 3) {
+    kb_fluxct<3, true><<<g, 256, 0, s>>>(views, items, nitems);
+    kb_fluxct<3, false><<<g, 256, 0, s>>>(views, items, nitems);
+  } else if (ndim == 2) {
+    kb_fluxct<2, true><<<g, 256, 0, s>>>(views, items, nitems);
+    kb_fluxct<2, false><<<g, 256, 0, s>>>(views, items, nitems);
+  }
+}
+void launch_update_batched(const Par &p, const BView *views, const double *const *base, double *const *out,
+                           const double *beta_dt, const WorkItem *items, int nitems, int grid, cudaStream_t s) {
+  if (nitems <= 0) return;
+  kb_update<<<persistent_grid(kb_update, 256, 0, nitems, grid), 256, 0, s>>>(views, base, out, beta_dt,
+                                                                           p.mhd ? PHX_NCONS : 5, items, nitems);
+}
+void launch_ghost_batched(const BView *views, int nvar, const WorkItem *items, int nitems, int grid, cudaStream_t s) {
+  if (nitems <= 0) return;
+  kb_ghost<<<persistent_grid(kb_ghost, 256, 0, nitems, grid), 256, 0, s>>>(views, nvar, items, nitems);
 }
 
 // ------------------------------------------------------- FP64 peak probe

@@ -257,6 +257,25 @@ class FluidContext:
         self._ok(self.lib.phx_stage(self.h, C.byref(p), C.byref(s), _ptr(cons_base), _ptr(cons_out), beta, dt,
                                     int(learned), _stream(stream)))
 
+    def StageBatched(self, p: abi.Params, blocks, cons_base, cons_out, beta: float, dt: float, learned=False,
+                     stream=None):
+        """One RK stage over many independent blocks (phx_stage_batched):
+        blocks[n]['cons'] is block n's stage input, cons_base[n] / cons_out[n]
+        its step-start state and stage output."""
+        from .block import _ptr
+
+        n = len(blocks)
+        arr = (abi.BlockS * n)(*[b.struct() for b in blocks])
+        base = (C.c_void_p * n)(*[_ptr(x) for x in cons_base])
+        out = (C.c_void_p * n)(*[_ptr(x) for x in cons_out])
+        self._ok(self.lib.phx_stage_batched(self.h, C.byref(p), arr, n, base, out, beta, dt, int(learned),
+                                            _stream(stream)))
+
+    def batch_info(self) -> dict:
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        self._ok(self.lib.phx_batch_info(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return {"x1_cells": a.value, "sweep_seg": b.value, "graph_nodes": c.value}
+
     def probe_fp64_peak(self) -> float:
         v = C.c_double()
         self._ok(self.lib.phx_probe_fp64_peak(self.h, C.byref(v)))

@@ -47,21 +47,35 @@ def normal(seed: int, stream: int, n: int) -> np.ndarray:
     return np.sqrt(-2.0 * np.log1p(-u1)) * np.cos(2.0 * np.pi * u2)
 
 
-def isotropic(seed: int, stream: int, n: int) -> np.ndarray:
+def _uni(seed: int, stream: int, n: int, device=None):
+    """uniform() on the host (device None) or uniform_torch() on a device."""
+    return uniform(seed, stream, n) if device is None else uniform_torch(seed, stream, n, device)
+
+
+def _xp(a):
+    if isinstance(a, np.ndarray):
+        return np
+    import torch
+
+    return torch
+
+
+def isotropic(seed: int, stream: int, n: int, device=None):
     """Unit vectors uniform on the sphere, shape (3, n)."""
-    cz = 2.0 * uniform(seed, stream, n) - 1.0
-    ph = 2.0 * np.pi * uniform(seed, stream + 1, n)
-    s = np.sqrt(np.maximum(0.0, 1.0 - cz * cz))
-    return np.stack([s * np.cos(ph), s * np.sin(ph), cz])
+    cz = 2.0 * _uni(seed, stream, n, device) - 1.0
+    ph = 2.0 * np.pi * _uni(seed, stream + 1, n, device)
+    xp = _xp(cz)
+    s = (1.0 - cz * cz).clip(min=0.0) ** 0.5
+    return xp.stack([s * xp.cos(ph), s * xp.sin(ph), cz])
 
 
 def eos_prims(rho, P, gm1, Cv=1.0):
     """u, T, gamma1 from (rho, P) for the ideal gas (singularity-eos IdealGas)."""
     u = P / gm1
     sie = u / rho
-    T = np.maximum(0.0, sie / Cv)
-    Pt = np.maximum(0.0, gm1 * rho * Cv * T)
-    bmod = np.maximum(0.0, (gm1 + 1) * gm1 * rho * Cv * T)
+    T = (sie / Cv).clip(min=0.0)
+    Pt = (gm1 * rho * Cv * T).clip(min=0.0)
+    bmod = ((gm1 + 1) * gm1 * rho * Cv * T).clip(min=0.0)
     return u, T, bmod / Pt
 
 
@@ -144,30 +158,42 @@ def kelvin_helmholtz(n: int = 256, seed: int = SEED + 2, ng: int = 4) -> tuple[B
 
 
 def random_zones_prims(N: int, seed: int, logrho=(-4.0, 0.0), logT=(-3.0, 0.0), W=(1.0, 5.0),
-                       sigma=(1.0e-3, 10.0)):
+                       sigma=(1.0e-3, 10.0), device=None):
     """Per-zone random primitives: log10 rho ~ U, log10 P/rho ~ U, Lorentz
     factor ~ U with isotropic direction, |B|^2/rho log-uniform with isotropic
-    direction."""
-    rho = 10.0 ** (logrho[0] + (logrho[1] - logrho[0]) * uniform(seed, 0, N))
-    P = rho * 10.0 ** (logT[0] + (logT[1] - logT[0]) * uniform(seed, 1, N))
-    Wl = W[0] + (W[1] - W[0]) * uniform(seed, 2, N)
-    nv = isotropic(seed, 3, N)
-    wv = np.sqrt(Wl * Wl - 1.0) * nv
-    ls = np.log10(sigma[0]) + (np.log10(sigma[1]) - np.log10(sigma[0])) * uniform(seed, 5, N)
-    Bm = np.sqrt(10.0 ** ls * rho)
-    nb = isotropic(seed, 6, N)
+    direction.  device None draws with numpy, else on that torch device."""
+    rho = 10.0 ** (logrho[0] + (logrho[1] - logrho[0]) * _uni(seed, 0, N, device))
+    P = rho * 10.0 ** (logT[0] + (logT[1] - logT[0]) * _uni(seed, 1, N, device))
+    Wl = W[0] + (W[1] - W[0]) * _uni(seed, 2, N, device)
+    nv = isotropic(seed, 3, N, device)
+    wv = (Wl * Wl - 1.0) ** 0.5 * nv
+    ls = np.log10(sigma[0]) + (np.log10(sigma[1]) - np.log10(sigma[0])) * _uni(seed, 5, N, device)
+    Bm = (10.0 ** ls * rho) ** 0.5
+    nb = isotropic(seed, 6, N, device)
     return rho, wv, P, Bm * nb
 
 
-def random_block(n: int, seed: int, ng: int = 4, Gamma: float = 4.0 / 3.0) -> Block:
-    """One periodic n^3 block of per-zone random primitives."""
+def random_block(n: int, seed: int, ng: int = 4, Gamma: float = 4.0 / 3.0, device=None) -> Block:
+    """One periodic n^3 block of per-zone random primitives (host arrays, or
+    arrays on a torch device drawn there)."""
     dx = 1.0 / n
-    b = Block((n, n, n), ng, 3, (0.0, 0.0, 0.0), (dx, dx, dx)).alloc()
-    rho, wv, P, B = random_zones_prims(n ** 3, seed)
+    if device is None:
+        b = Block((n, n, n), ng, 3, (0.0, 0.0, 0.0), (dx, dx, dx)).alloc()
+    else:
+        b = Block((n, n, n), ng, 3, (0.0, 0.0, 0.0), (dx, dx, dx), backend="torch", device=device).alloc()
+    rho, wv, P, B = random_zones_prims(n ** 3, seed, device=device)
     shp = (n, n, n)
     _set_interior(b, rho.reshape(shp), [w.reshape(shp) for w in wv], P.reshape(shp), [x.reshape(shp) for x in B],
                   Gamma - 1.0)
     return b
+
+
+def uneven_blocks(nblocks: int = 1024, seed: int = SEED + 3, device="cuda", Gamma: float = 4.0 / 3.0):
+    """The batched-meshblock state: nblocks periodic blocks with edges drawn
+    by uneven_block_sizes and per-zone random primitives (block b seeded
+    seed + 1000 + b), generated on the device."""
+    return [random_block(n, seed + 1000 + b, Gamma=Gamma, device=device)
+            for b, n in enumerate(uneven_block_sizes(nblocks, seed))]
 
 
 def uneven_block_sizes(nblocks: int = 1024, seed: int = SEED + 3, sizes=(16, 32, 64), probs=(0.5, 0.35, 0.15)):

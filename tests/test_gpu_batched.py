@@ -1,0 +1,101 @@
+"""Batched uneven meshblocks (phx_stage_batched): one persistent launch per
+phase over all blocks, the stage replayed as a CUDA graph.  The exact build
+equals the single-block stage (itself bitwise equal to the oracle) bit for
+bit on every block, over several RK2 steps that reuse the captured graph."""
+import numpy as np
+import pytest
+
+from phoebus_gb300 import abi, states
+from phoebus_gb300.abi import PhxError
+from tests.util import assert_bitwise, assert_close, host
+
+pytestmark = pytest.mark.gpu
+SIZES = [8, 12, 8, 16, 12, 10]
+
+
+def params():
+    return abi.default_params(Gamma=4.0 / 3.0, recon="mp5", riemann="hll", c2p_tol=1e-10, c2p_max_iter=100)
+
+
+def make_blocks(ctx, p):
+    blocks = []
+    for b, n in enumerate(SIZES):
+        db = states.random_block(n, states.SEED + 3000 + b).to_device("cuda")
+        ctx.Initialize(p, db)
+        blocks.append(db)
+    ctx.check()
+    return blocks
+
+
+def copy_blocks(blocks):
+    out = []
+    for b in blocks:
+        c = states.Block(b.nx, b.ng, b.ndim, b.xmin, b.dx, backend="torch", device="cuda",
+                         arrays={k: v.clone() for k, v in b.arrays.items()})
+        out.append(c)
+    return out
+
+
+def rk2_single(ctx, p, blocks, seconds, dt):
+    from phoebus_gb300.fluid import rk2_step
+
+    for b, s in zip(blocks, seconds):
+        rk2_step(ctx, p, b, s, dt)
+
+
+def rk2_batched(ctx, p, blocks, seconds, dt):
+    import torch  # noqa: F401
+
+    bases = [b["cons"] for b in blocks]
+    ctx.StageBatched(p, blocks, bases, seconds, 1.0, dt)
+    stage2 = []
+    for b, s in zip(blocks, seconds):
+        c = states.Block(b.nx, b.ng, b.ndim, b.xmin, b.dx, backend="torch", device="cuda",
+                         arrays=dict(b.arrays))
+        c.arrays["cons"] = s
+        stage2.append(c)
+    ctx.StageBatched(p, stage2, bases, bases, 0.5, dt)
+
+
+@pytest.mark.parametrize("exact", [True, False])
+def test_batched_equals_single_block(request, exact):
+    import torch
+
+    ctx = request.getfixturevalue("ctx_exact" if exact else "ctx_fast")
+    p = params()
+    a = make_blocks(ctx, p)
+    b = copy_blocks(a)
+    sa = [torch.zeros_like(x["cons"]) for x in a]
+    sb = [torch.zeros_like(x["cons"]) for x in b]
+    dt = 0.2 * min(ctx.EstimateTimestepBlock(p, x, False).item() for x in a)
+    for step in range(3):  # the second and third steps replay the captured graphs
+        rk2_single(ctx, p, a, sa, dt)
+        rk2_batched(ctx, p, b, sb, dt)
+        ctx.check()
+    info = ctx.batch_info()
+    assert info["graph_nodes"] >= 9 and info["x1_cells"] > 0 and info["sweep_seg"] > 0
+    for x, y in zip(a, b):
+        for name in ("prim", "cons", "fail"):
+            if exact:
+                assert_bitwise(y[name], x[name], name)
+            else:
+                g, r = host(y[name]), host(x[name])
+                for v in range(g.shape[0] if g.ndim == 4 else 1):
+                    assert_close(g[v] if g.ndim == 4 else g, r[v] if r.ndim == 4 else r, 1e-12, name)
+
+
+def test_batched_refuses_unsupported(ctx_fast):
+    import torch
+
+    p = params()
+    blocks = make_blocks(ctx_fast, p)[:2]
+    bases = [b["cons"] for b in blocks]
+    outs = [torch.zeros_like(x) for x in bases]
+    with pytest.raises(PhxError) as e:
+        ctx_fast.StageBatched(p, blocks, bases, outs, 1.0, 1e-3, learned=True)
+    assert e.value.status == 8
+    pf = params()
+    pf.enable_floors = 1
+    with pytest.raises(PhxError) as e:
+        ctx_fast.StageBatched(pf, blocks, bases, outs, 1.0, 1e-3)
+    assert e.value.status == 8
