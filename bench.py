@@ -18,6 +18,9 @@ RK2 timestep per second.
   cpu_baseline  the oracle (CPU restatement of the reference path) timed on
              a 64^3 sample of the same state with all host threads
 
+  batched    1024 uneven periodic blocks (edges 16/32/64, MP5 + HLL): RK2
+             steps through phx_stage_batched (persistent work-list launches
+             replayed as CUDA graphs) against the same steps block by block
   c2p        con2prim over 5e7 independent FMKS Kerr-Schild zones at tolerance
              1e-10: zones/s and root-find iterations with the reference's
              start (plain) and with the learned start (network trained on
@@ -79,6 +82,8 @@ def parse():
     a.add_argument("--c2p-zones", type=float, default=5e7)
     a.add_argument("--train-pairs", type=float, default=1e7)
     a.add_argument("--train-epochs", type=int, default=10)
+    a.add_argument("--no-batched", action="store_true", help="skip the uneven-meshblock section")
+    a.add_argument("--batched-blocks", type=int, default=1024)
     return a.parse_args()
 
 
@@ -260,6 +265,86 @@ def bench_c2p(ctx, args, dev):
     return out
 
 
+def batched_params():
+    """Uneven-block workload: MP5 + HLL, Gamma 4/3, MHD; ConstantRhoSie
+    floors, c2p fixup and ceilings on (the per-zone random state develops
+    failed inversions within a few steps without them)."""
+    from phoebus_gb300 import abi
+
+    p = abi.default_params(Gamma=4.0 / 3.0, recon="mp5", riemann="hll", c2p_tol=1e-10, c2p_max_iter=100)
+    p.enable_floors, p.enable_c2p_fixup, p.enable_ceilings = 1, 1, 1
+    p.rho0_floor, p.sie0_floor = 1e-8, 1e-8
+    return p
+
+
+def bench_batched(ctx, args, dev):
+    """1024 periodic blocks with edges from {16, 32, 64} (p = 0.5, 0.35,
+    0.15), per-zone random primitives; one RK2 step = two batched stages
+    (each a captured CUDA graph of persistent work-list launches).  Compared
+    with the same steps issued block by block through phx_stage."""
+    import torch
+
+    from phoebus_gb300 import states
+    from phoebus_gb300.block import Block
+
+    p = batched_params()
+    blocks = states.uneven_blocks(args.batched_blocks, device=dev)
+    for b in blocks:
+        ctx.Initialize(p, b)
+    ctx.check()
+    zones = sum(b.nx[0] * b.nx[1] * b.nx[2] for b in blocks)
+    dt = 0.2 * min(ctx.EstimateTimestepBlock(p, b, False).item() for b in blocks)
+    seconds = [torch.zeros_like(b["cons"]) for b in blocks]
+    bases = [b["cons"] for b in blocks]
+    stage2 = []
+    for b, s2 in zip(blocks, seconds):
+        c = Block(b.nx, b.ng, b.ndim, b.xmin, b.dx, backend="torch", device=dev, arrays=dict(b.arrays))
+        c.arrays["cons"] = s2
+        stage2.append(c)
+
+    def step_batched():
+        ctx.StageBatched(p, blocks, bases, seconds, 1.0, dt)
+        ctx.StageBatched(p, stage2, bases, bases, 0.5, dt)
+
+    def step_blocks():
+        for b, b2, s2 in zip(blocks, stage2, seconds):
+            ctx.Stage(p, b, b["cons"], s2, 1.0, dt)
+            ctx.Stage(p, b2, b["cons"], b["cons"], 0.5, dt)
+
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    step_batched()  # builds both plans: work lists, autotune, graph capture
+    torch.cuda.synchronize()
+    t_plan = time.perf_counter() - t0
+    info = ctx.batch_info()
+    stream = torch.cuda.current_stream()
+    res = {}
+    for name, fn, k in (("batched", step_batched, args.steps), ("per_block", step_blocks, 2)):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / k
+        res[name] = {"zone_updates_per_s": zones / (ms * 1e-3), "ms_per_step": ms, "steps": k}
+    ctx.check()
+    nan = sum(int(torch.isnan(b["prim"][0]).sum()) for b in blocks)
+    del blocks, seconds, bases, stage2
+    torch.cuda.empty_cache()
+    from collections import Counter
+
+    sizes = Counter(states.uneven_block_sizes(args.batched_blocks))
+    return {"workload": f"{args.batched_blocks} periodic blocks, edges {dict(sorted(sizes.items()))}, Minkowski, "
+                        "MP5 + HLL, MHD, Gamma 4/3, per-zone random state, floors + c2p fixup on",
+            "interior_zones": zones, **res, "batched_over_per_block":
+                res["batched"]["zone_updates_per_s"] / res["per_block"]["zone_updates_per_s"],
+            "plan_seconds": t_plan, "tuning": info, "nan_rho_zones": nan,
+            "graph": "one CUDA graph per stage kind; nodes per graph as in tuning.graph_nodes"}
+
+
 def cpu_baseline(args, threads):
     """Oracle RK2 timestep on a cpu_n^3 sample of the workload."""
     import numpy as np
@@ -430,6 +515,7 @@ def main():
                "ms_per_step": ems}
     ctx.check()
     c2p = None if args.no_c2p else bench_c2p(ctx, args, dev)
+    batched = None if args.no_batched else bench_batched(ctx, args, dev)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
@@ -454,6 +540,7 @@ def main():
                          "note": "FP64-pipe bound on GB300; see fp64"},
             "fp64": fp64,
             "c2p": c2p,
+            "batched": batched,
             "cpu_baseline": cpu,
             "clocks": clocks,
             "e2e": e2e,

@@ -592,8 +592,6 @@ phx_status phx_stage_batched(phx_ctx *ctx, const phx_params *p, const phx_block 
   if (!blocks || nblocks <= 0 || !cons_base || !cons_out) return fail(PHX_ERR_INVALID_ARG, "no blocks");
   if (use_learned_guess)
     return fail(PHX_ERR_UNSUPPORTED, "phx_stage_batched: the learned start runs on single blocks and zone lists");
-  if (p->enable_c2p_fixup || p->enable_floors || (p->enable_mhd_floors && p->mhd))
-    return fail(PHX_ERR_UNSUPPORTED, "phx_stage_batched: c2p fixup and floors run on single blocks (phx_stage)");
   std::vector<phx::BView> views(nblocks);
   for (int n = 0; n < nblocks; n++) {
     const phx_block *b = &blocks[n];

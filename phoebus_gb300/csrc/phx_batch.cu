@@ -224,9 +224,12 @@ static void stage_launches(BatchPlan &pl, DevStats *stats, unsigned int *err, cu
   if (pl.ndim >= 3) launch_flux_sweep_batched(p, pl.mink, 2, pl.views_in, pl.x3.d_items, pl.x3.n, 0, pl.tune.seg, s);
   if (p.mhd && pl.ndim > 1) launch_fluxct_batched(pl.ndim, pl.views_in, pl.fluxct.d_items, pl.fluxct.n, 0, s);
   launch_update_batched(p, pl.views_in, pl.base_tab, pl.out_tab, pl.beta_dt, pl.update.d_items, pl.update.n, 0, s);
-  launch_c2p_batched(p, pl.mink, pl.views_out, pl.c2p.d_items, pl.c2p.n, 0, stats, err, s);
-  launch_ghost_batched(pl.views_out, p.mhd ? PHX_NCONS : 5, pl.ghost.d_items, pl.ghost.n, 0, s);
-  launch_c2p_batched(p, pl.mink, pl.views_out, pl.c2p.d_items, pl.c2p.n, 0, stats, err, s);
+  for (int pass = 0; pass < 2; pass++) {  // FillDerived over MeshData, then per block after the exchange
+    if (pass == 1) launch_ghost_batched(pl.views_out, p.mhd ? PHX_NCONS : 5, pl.ghost.d_items, pl.ghost.n, 0, s);
+    launch_c2p_batched(p, pl.mink, pl.views_out, pl.c2p.d_items, pl.c2p.n, 0, stats, err, s);
+    launch_c2p_fixup_batched(p, pl.mink, pl.views_out, pl.update.d_items, pl.update.n, s);  // interior zones
+    launch_floors_batched(p, pl.mink, pl.views_out, pl.c2p.d_items, pl.c2p.n, stats, err, s);  // entire blocks
+  }
 }
 
 // Field-wise (phx_block has padding bytes the caller need not initialise).
@@ -279,7 +282,7 @@ cudaError_t batch_stage(BatchCache *cache, const Par &par, const phx_block *bloc
     P.ndim = views[0].ndim;
     std::vector<BView> vin(views, views + n), vout(views, views + n);
     for (int i = 0; i < n; i++) vout[i].cons = out[i];
-    const size_t bytes = 2 * sizeof(BView) * n + 2 * sizeof(double *) * n + 2 * sizeof(double) + 256 * 4;
+    const size_t bytes = 2 * sizeof(BView) * n + 2 * sizeof(double *) * n + 2 * sizeof(double) + 256 * 8;
     if ((e = cudaMalloc(&P.mem, bytes)) != cudaSuccess) return e;
     char *m = static_cast<char *>(P.mem);
     auto take = [&](size_t b) {
@@ -328,6 +331,7 @@ cudaError_t batch_stage(BatchCache *cache, const Par &par, const phx_block *bloc
       for (const BView &b : vin) counts.push_back(dir < P.ndim ? sweep_threads(b, dir, P.tune.seg) : 0);
       if ((e = upload_items(P, dir == 1 ? P.x2 : P.x3, make_items(counts, 128))) != cudaSuccess) return e;
     }
+    prepare_flux_x1_batched(par, P.mink, P.x1_smem);  // kernel attributes are set outside the capture
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return e;
     // capture the stage
     cudaStream_t cs;

@@ -34,7 +34,9 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned by
       : "memory");
 }
 
-// Upper bound on mbarrier polls before a kernel reports ERR_TIMEOUT.
-constexpr long long MBAR_SPIN_LIMIT = 1ll << 26;
+// Upper bound on mbarrier polls before a kernel reports ERR_TIMEOUT.  Each
+// try_wait may itself suspend for a while, so the bound is kept at ~1e6
+// polls (a bulk copy completes within microseconds).
+constexpr long long MBAR_SPIN_LIMIT = 1ll << 20;
 
 }  // namespace phx

@@ -19,10 +19,9 @@
 
 namespace phx {
 
+// t runs over the interior zones.
 template <bool MINK>
-__global__ void __launch_bounds__(128) k_c2p_fixup(Par p, BView b, long long n) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
+__device__ __forceinline__ void c2p_fixup_at(const Par &p, const BView &b, long long t) {
   const int ni = b.nx1, nj = b.ndim >= 2 ? b.nx2 : 1;
   const int i = b.ng + (int)(t % ni);
   const int j = (b.ndim >= 2 ? b.ng : 0) + (int)((t / ni) % nj);
@@ -87,6 +86,12 @@ __global__ void __launch_bounds__(128) k_c2p_fixup(Par p, BView b, long long n) 
   for (int d = 0; d < b.ndim; d++) b.cell_sig[d * vs + id] = sig[d];
 }
 
+template <bool MINK>
+__global__ void __launch_bounds__(128) k_c2p_fixup(Par p, BView b, long long n) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) c2p_fixup_at<MINK>(p, b, t);
+}
+
 void launch_c2p_fixup(const Par &p, const BView &b, cudaStream_t s) {
   if (!p.c2p_fixup) return;
   const long long n = (long long)b.nx1 * (b.ndim >= 2 ? b.nx2 : 1) * (b.ndim >= 3 ? b.nx3 : 1);
@@ -98,11 +103,11 @@ void launch_c2p_fixup(const Par &p, const BView &b, cudaStream_t s) {
 }
 
 // ------------------------------------------------------------ floors
+// Zone t of the index box r (valid: this lane owns a zone).  Every lane of a
+// warp must call it together (the re-inversion's root find votes).
 template <bool MINK>
-__global__ void __launch_bounds__(128) k_floors(Par p, BView b, Range3 r, long long ntot, DevStats *stats,
-                                                unsigned int *err) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool valid = t < ntot;
+__device__ __forceinline__ void floors_at(const Par &p, const BView &b, const Range3 &r, long long t, bool valid,
+                                          DevStats *stats, unsigned int *err) {
   int k = 0, j = 0, i = 0;
   if (valid) {
     const int ni = r.ie - r.is + 1, nj = r.je - r.js + 1;
@@ -246,6 +251,13 @@ __global__ void __launch_bounds__(128) k_floors(Par p, BView b, Range3 r, long l
   }
 }
 
+template <bool MINK>
+__global__ void __launch_bounds__(128) k_floors(Par p, BView b, Range3 r, long long ntot, DevStats *stats,
+                                                unsigned int *err) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  floors_at<MINK>(p, b, r, t, t < ntot, stats, err);
+}
+
 void launch_floors(const Par &p, const BView &b, Range3 r, DevStats *stats, unsigned int *err, cudaStream_t s) {
   if (!p.enable_floors) return;
   const long long n = (long long)(r.ie - r.is + 1) * (r.je - r.js + 1) * (r.ke - r.ks + 1);
@@ -255,6 +267,47 @@ void launch_floors(const Par &p, const BView &b, Range3 r, DevStats *stats, unsi
     k_floors<false><<<(unsigned)((n + T - 1) / T), T, 0, s>>>(p, b, r, n, stats, err);
   else
     k_floors<true><<<(unsigned)((n + T - 1) / T), T, 0, s>>>(p, b, r, n, stats, err);
+}
+
+// ------------------------------------------------------------- batched
+template <bool MINK>
+__global__ void __launch_bounds__(128) kb_c2p_fixup(Par p, const BView *views, const WorkItem *items, int nitems) {
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const WorkItem w = items[it];
+    const long long t = w.first + threadIdx.x;
+    if (t < w.last) c2p_fixup_at<MINK>(p, views[w.block], t);
+  }
+}
+template <bool MINK>
+__global__ void __launch_bounds__(128) kb_floors(Par p, const BView *views, const WorkItem *items, int nitems,
+                                                 DevStats *stats, unsigned int *err) {
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const WorkItem w = items[it];
+    const BView &b = views[w.block];
+    const Range3 r{0, b.n1t - 1, 0, b.n2t - 1, 0, b.n3t - 1};
+    const long long t = w.first + threadIdx.x;
+    floors_at<MINK>(p, b, r, t, t < w.last, stats, err);
+  }
+}
+
+void launch_c2p_fixup_batched(const Par &p, bool mink, const BView *views, const WorkItem *items, int nitems,
+                              cudaStream_t s) {
+  if (!p.c2p_fixup || nitems <= 0) return;
+  if (mink)
+    kb_c2p_fixup<true><<<persistent_grid(kb_c2p_fixup<true>, 128, 0, nitems, 0), 128, 0, s>>>(p, views, items, nitems);
+  else
+    kb_c2p_fixup<false><<<persistent_grid(kb_c2p_fixup<false>, 128, 0, nitems, 0), 128, 0, s>>>(p, views, items,
+                                                                                                 nitems);
+}
+void launch_floors_batched(const Par &p, bool mink, const BView *views, const WorkItem *items, int nitems,
+                           DevStats *stats, unsigned int *err, cudaStream_t s) {
+  if (!p.enable_floors || nitems <= 0) return;
+  if (mink)
+    kb_floors<true><<<persistent_grid(kb_floors<true>, 128, 0, nitems, 0), 128, 0, s>>>(p, views, items, nitems,
+                                                                                         stats, err);
+  else
+    kb_floors<false><<<persistent_grid(kb_floors<false>, 128, 0, nitems, 0), 128, 0, s>>>(p, views, items, nitems,
+                                                                                           stats, err);
 }
 
 }  // namespace phx

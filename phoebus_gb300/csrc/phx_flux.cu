@@ -109,11 +109,13 @@ __device__ __forceinline__ bool x1_stage(const BView &b, const X1Range &xr, int 
     const unsigned bytes = (unsigned)(n1t * sizeof(double));
     if (threadIdx.x == 0) mbar_expect_tx(bar, bytes * PHX_NRECON * np);
     __syncthreads();
-    if (threadIdx.x < np * PHX_NRECON) {  // one bulk copy per (pencil, variable) row
-      const int pp = threadIdx.x / PHX_NRECON, v = threadIdx.x % PHX_NRECON;
+    // one bulk copy per (pencil, variable) row; a CTA may stage more rows
+    // than it has threads
+    for (int r = threadIdx.x; r < np * PHX_NRECON; r += blockDim.x) {
+      const int pp = r / PHX_NRECON, v = r % PHX_NRECON;
       const int pen = p0 + pp;
       const long long base = b.idx(xr.klo + pen / xr.nj, xr.jlo + pen % xr.nj, 0);
-      bulk_g2s(rows + (long long)(pp * PHX_NRECON + v) * n1t, b.prim + v * b.vs + base, bytes, bar);
+      bulk_g2s(rows + (long long)r * n1t, b.prim + v * b.vs + base, bytes, bar);
     }
     bool done = false;
     for (long long spins = 0; spins < MBAR_SPIN_LIMIT && !done; spins++) done = mbar_try_wait(bar, phase);
@@ -407,10 +409,19 @@ long long sweep_threads(const BView &b, int dir, int seg_target) {
 }
 
 template <int RECON, bool MINK>
+static void x1_prepare_t(size_t smem) {
+  static size_t set = 0;  // largest dynamic shared memory already allowed
+  if (smem > set) {
+    cudaFuncSetAttribute(kb_flux_x1<RECON, MINK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    set = smem;
+  }
+}
+
+template <int RECON, bool MINK>
 static void x1_batched_t(const Par &p, const BView *views, const WorkItem *items, int nitems, int grid, size_t smem,
                          unsigned int *err, cudaStream_t s) {
   auto kern = kb_flux_x1<RECON, MINK>;
-  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  x1_prepare_t<RECON, MINK>(smem);
   kern<<<persistent_grid(kern, 32 * X1_WARPS, smem, nitems, grid), 32 * X1_WARPS, smem, s>>>(p, views, items,
                                                                                              nitems, err);
 }
@@ -446,6 +457,10 @@ void launch_flux_x1_batched(const Par &p, bool mink, const BView *views, const W
                             size_t smem, unsigned int *err, cudaStream_t s) {
   if (nitems <= 0) return;
   PHX_RECON_DISPATCH(x1_batched_t, p, views, items, nitems, grid, smem, err, s)
+}
+
+void prepare_flux_x1_batched(const Par &p, bool mink, size_t smem) {
+  PHX_RECON_DISPATCH(x1_prepare_t, smem)
 }
 
 void launch_flux_sweep_batched(const Par &p, bool mink, int dir, const BView *views, const WorkItem *items,

@@ -109,8 +109,13 @@ void launch_c2p_batched(const Par &p, bool mink, const BView *views, const WorkI
                         DevStats *stats, unsigned int *err, cudaStream_t s);
 void launch_flux_x1_batched(const Par &p, bool mink, const BView *views, const WorkItem *items, int nitems, int grid,
                             size_t smem, unsigned int *err, cudaStream_t s);
+void prepare_flux_x1_batched(const Par &p, bool mink, size_t smem);
 void launch_flux_sweep_batched(const Par &p, bool mink, int dir, const BView *views, const WorkItem *items,
                                int nitems, int grid, int seg_target, cudaStream_t s);
+void launch_c2p_fixup_batched(const Par &p, bool mink, const BView *views, const WorkItem *items, int nitems,
+                              cudaStream_t s);
+void launch_floors_batched(const Par &p, bool mink, const BView *views, const WorkItem *items, int nitems,
+                           DevStats *stats, unsigned int *err, cudaStream_t s);
 int x1_npencil(const BView &b);
 long long sweep_threads(const BView &b, int dir, int seg_target);
 bool x1_tma_ok_host(const BView &b);

@@ -190,10 +190,24 @@ def random_block(n: int, seed: int, ng: int = 4, Gamma: float = 4.0 / 3.0, devic
 
 def uneven_blocks(nblocks: int = 1024, seed: int = SEED + 3, device="cuda", Gamma: float = 4.0 / 3.0):
     """The batched-meshblock state: nblocks periodic blocks with edges drawn
-    by uneven_block_sizes and per-zone random primitives (block b seeded
-    seed + 1000 + b), generated on the device."""
-    return [random_block(n, seed + 1000 + b, Gamma=Gamma, device=device)
-            for b, n in enumerate(uneven_block_sizes(nblocks, seed))]
+    by uneven_block_sizes and per-zone random primitives, drawn in one pass
+    over all interior zones (block b's zones follow block b-1's in the
+    counter order) on the device (or the host for device None)."""
+    sizes = uneven_block_sizes(nblocks, seed)
+    total = sum(n ** 3 for n in sizes)
+    rho, wv, P, B = random_zones_prims(total, seed + 7, device=device)
+    blocks, off = [], 0
+    for n in sizes:
+        dx = 1.0 / n
+        kw = {} if device is None else dict(backend="torch", device=device)
+        b = Block((n, n, n), 4, 3, (0.0, 0.0, 0.0), (dx, dx, dx), **kw).alloc()
+        sl = slice(off, off + n ** 3)
+        shp = (n, n, n)
+        _set_interior(b, rho[sl].reshape(shp), [w[sl].reshape(shp) for w in wv], P[sl].reshape(shp),
+                      [x[sl].reshape(shp) for x in B], Gamma - 1.0)
+        blocks.append(b)
+        off += n ** 3
+    return blocks
 
 
 def uneven_block_sizes(nblocks: int = 1024, seed: int = SEED + 3, sizes=(16, 32, 64), probs=(0.5, 0.35, 0.15)):

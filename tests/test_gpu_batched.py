@@ -13,8 +13,12 @@ pytestmark = pytest.mark.gpu
 SIZES = [8, 12, 8, 16, 12, 10]
 
 
-def params():
-    return abi.default_params(Gamma=4.0 / 3.0, recon="mp5", riemann="hll", c2p_tol=1e-10, c2p_max_iter=100)
+def params(floors=False):
+    p = abi.default_params(Gamma=4.0 / 3.0, recon="mp5", riemann="hll", c2p_tol=1e-10, c2p_max_iter=100)
+    if floors:  # fixup.cpp defaults: ConstantRhoSie floors, c2p fixup, ceilings
+        p.enable_floors, p.enable_c2p_fixup, p.enable_ceilings = 1, 1, 1
+        p.rho0_floor, p.sie0_floor = 1e-8, 1e-8
+    return p
 
 
 def make_blocks(ctx, p):
@@ -57,12 +61,12 @@ def rk2_batched(ctx, p, blocks, seconds, dt):
     ctx.StageBatched(p, stage2, bases, bases, 0.5, dt)
 
 
-@pytest.mark.parametrize("exact", [True, False])
-def test_batched_equals_single_block(request, exact):
+@pytest.mark.parametrize("exact,floors", [(True, False), (False, False), (True, True)])
+def test_batched_equals_single_block(request, exact, floors):
     import torch
 
     ctx = request.getfixturevalue("ctx_exact" if exact else "ctx_fast")
-    p = params()
+    p = params(floors)
     a = make_blocks(ctx, p)
     b = copy_blocks(a)
     sa = [torch.zeros_like(x["cons"]) for x in a]
@@ -80,8 +84,13 @@ def test_batched_equals_single_block(request, exact):
                 assert_bitwise(y[name], x[name], name)
             else:
                 g, r = host(y[name]), host(x[name])
-                for v in range(g.shape[0] if g.ndim == 4 else 1):
-                    assert_close(g[v] if g.ndim == 4 else g, r[v] if r.ndim == 4 else r, 1e-12, name)
+                g, r = (g, r) if g.ndim == 4 else (g[None], r[None])
+                for v in range(g.shape[0]):
+                    # zones whose inversion failed (NaN) must fail in both
+                    assert np.array_equal(np.isnan(g[v]), np.isnan(r[v])), name
+                    ok = ~np.isnan(r[v])
+                    if ok.any():
+                        assert_close(g[v][ok], r[v][ok], 1e-12, f"{name}[{v}]")
 
 
 def test_batched_refuses_unsupported(ctx_fast):
@@ -94,8 +103,9 @@ def test_batched_refuses_unsupported(ctx_fast):
     with pytest.raises(PhxError) as e:
         ctx_fast.StageBatched(p, blocks, bases, outs, 1.0, 1e-3, learned=True)
     assert e.value.status == 8
-    pf = params()
-    pf.enable_floors = 1
+    mixed = blocks[:1] + [states.Block((8, 8, 1), 4, 2, (0, 0, 0), (0.1, 0.1, 1.0), backend="torch",
+                                       device="cuda").alloc()]
     with pytest.raises(PhxError) as e:
-        ctx_fast.StageBatched(pf, blocks, bases, outs, 1.0, 1e-3)
-    assert e.value.status == 8
+        ctx_fast.StageBatched(p, mixed, [b["cons"] for b in mixed], [torch.zeros_like(b["cons"]) for b in mixed],
+                              1.0, 1e-3)
+    assert e.value.status == 1 and "share ndim" in str(e.value)
