@@ -184,7 +184,7 @@ static float time_launch(cudaStream_t s, const std::function<void()> &fn, int re
 static Tuning autotune(BatchPlan &pl, const std::vector<BView> &v, unsigned int *err, cudaStream_t s) {
   Tuning best;
   float best_ms = 1e30f;
-  for (int cells : {96, 192, 288, 384, 576}) {
+  for (int cells : {96, 192, 288, 384, 576, 768, 1152}) {
     size_t smem;
     std::vector<WorkItem> items = x1_items(v, cells, smem);
     PhaseList ph;
@@ -197,7 +197,7 @@ static Tuning autotune(BatchPlan &pl, const std::vector<BView> &v, unsigned int 
     }
   }
   best_ms = 1e30f;
-  for (int seg : {16, 32, 64}) {
+  for (int seg : {8, 16, 32, 64}) {
     float ms = 0.f;
     for (int dir = 1; dir <= pl.ndim - 1; dir++) {
       std::vector<long long> counts;
