@@ -277,7 +277,7 @@ def batched_params():
     return p
 
 
-def bench_batched(ctx, args, dev):
+def bench_batched(ctx, args, dev, learned_ready=False):
     """1024 periodic blocks with edges from {16, 32, 64} (p = 0.5, 0.35,
     0.15), per-zone random primitives; one RK2 step = two batched stages
     (each a captured CUDA graph of persistent work-list launches).  Compared
@@ -302,9 +302,12 @@ def bench_batched(ctx, args, dev):
         c.arrays["cons"] = s2
         stage2.append(c)
 
-    def step_batched():
-        ctx.StageBatched(p, blocks, bases, seconds, 1.0, dt)
-        ctx.StageBatched(p, stage2, bases, bases, 0.5, dt)
+    def step_batched(learned=False):
+        ctx.StageBatched(p, blocks, bases, seconds, 1.0, dt, learned=learned)
+        ctx.StageBatched(p, stage2, bases, bases, 0.5, dt, learned=learned)
+
+    def step_batched_learned():
+        step_batched(True)
 
     def step_blocks():
         for b, b2, s2 in zip(blocks, stage2, seconds):
@@ -319,7 +322,12 @@ def bench_batched(ctx, args, dev):
     info = ctx.batch_info()
     stream = torch.cuda.current_stream()
     res = {}
-    for name, fn, k in (("batched", step_batched, args.steps), ("per_block", step_blocks, 2)):
+    ctx.c2p_stats(reset=True)
+    runs = [("batched", step_batched, args.steps), ("per_block", step_blocks, 2)]
+    if learned_ready:
+        step_batched_learned()  # builds the learned plans
+        runs.append(("batched_learned", step_batched_learned, args.steps))
+    for name, fn, k in runs:
         fn()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -330,6 +338,10 @@ def bench_batched(ctx, args, dev):
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / k
         res[name] = {"zone_updates_per_s": zones / (ms * 1e-3), "ms_per_step": ms, "steps": k}
+        st = ctx.c2p_stats(reset=True)
+        if st["zones"]:
+            res[name]["c2p_iterations_per_zone"] = st["iterations"] / st["zones"]
+            res[name]["c2p_learned_accepted_frac"] = st["learned_accepted"] / st["zones"]
     ctx.check()
     nan = sum(int(torch.isnan(b["prim"][0]).sum()) for b in blocks)
     del blocks, seconds, bases, stage2
@@ -515,7 +527,7 @@ def main():
                "ms_per_step": ems}
     ctx.check()
     c2p = None if args.no_c2p else bench_c2p(ctx, args, dev)
-    batched = None if args.no_batched else bench_batched(ctx, args, dev)
+    batched = None if args.no_batched else bench_batched(ctx, args, dev, learned_ready=c2p is not None)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:

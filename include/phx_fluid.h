@@ -353,9 +353,10 @@ phx_status phx_stage(phx_ctx *ctx, const phx_params *p, const phx_block *b,
  * and in the JSON file PHX_AUTOTUNE_CACHE names, if set) and the captured
  * graph; later calls with the same blocks, buffers and params only update
  * beta and dt in device memory and launch the graph.  Blocks must share ndim
- * and geometry kind; c2p fixup and floors run as in phx_stage; the learned
- * start is not supported here (PHX_ERR_UNSUPPORTED).  No counterpart in the
- * reference, which launches every block's tasks separately. */
+ * and geometry kind; c2p fixup and floors run as in phx_stage; with
+ * use_learned_guess each con2prim pass is a tensor-core bracket launch and a
+ * root-find launch over all blocks.  No counterpart in the reference, which
+ * launches every block's tasks separately. */
 phx_status phx_stage_batched(phx_ctx *ctx, const phx_params *p, const phx_block *blocks,
                              int nblocks, const double *const *cons_base,
                              double *const *cons_out, double beta, double dt,

@@ -590,8 +590,7 @@ phx_status phx_stage_batched(phx_ctx *ctx, const phx_params *p, const phx_block 
   phx_status s;
   if ((s = ctx_device(ctx)) || (s = check_params(p))) return s;
   if (!blocks || nblocks <= 0 || !cons_base || !cons_out) return fail(PHX_ERR_INVALID_ARG, "no blocks");
-  if (use_learned_guess)
-    return fail(PHX_ERR_UNSUPPORTED, "phx_stage_batched: the learned start runs on single blocks and zone lists");
+  if (use_learned_guess && !ctx->mlp_loaded) return fail(PHX_ERR_INVALID_ARG, "no learned-guess weights loaded");
   std::vector<phx::BView> views(nblocks);
   for (int n = 0; n < nblocks; n++) {
     const phx_block *b = &blocks[n];
@@ -607,7 +606,8 @@ phx_status phx_stage_batched(phx_ctx *ctx, const phx_params *p, const phx_block 
   }
   const char *why = nullptr;
   cudaError_t e = phx::batch_stage(ctx->batch, make_par(*p), blocks, views.data(), nblocks, cons_base, cons_out, beta,
-                                   dt, ctx->stats, ctx->err, S(stream), &why);
+                                   dt, use_learned_guess ? ctx->mlp_packed : nullptr, ctx->stats, ctx->err, S(stream),
+                                   &why);
   if (e != cudaSuccess) return fail(PHX_ERR_CUDA, "phx_stage_batched: %s", cudaGetErrorString(e));
   return cuda_status("phx_stage_batched");
 }

@@ -102,12 +102,15 @@ struct BatchPlan {
   Tuning tune;
   bool mink = true;
   int ndim = 3;
+  const MlpPacked *mlp = nullptr;  // learned start (packed weights in the context) or null
+  double *brk = nullptr;           // learned brackets, 3 x c2p items x 128
   cudaGraphExec_t exec = nullptr;
   cudaGraph_t graph = nullptr;
   ~BatchPlan() {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     for (void *m : item_mem) cudaFree(m);
+    cudaFree(brk);
     cudaFree(mem);
   }
 };
@@ -226,7 +229,7 @@ static void stage_launches(BatchPlan &pl, DevStats *stats, unsigned int *err, cu
   launch_update_batched(p, pl.views_in, pl.base_tab, pl.out_tab, pl.beta_dt, pl.update.d_items, pl.update.n, 0, s);
   for (int pass = 0; pass < 2; pass++) {  // FillDerived over MeshData, then per block after the exchange
     if (pass == 1) launch_ghost_batched(pl.views_out, p.mhd ? PHX_NCONS : 5, pl.ghost.d_items, pl.ghost.n, 0, s);
-    launch_c2p_batched(p, pl.mink, pl.views_out, pl.c2p.d_items, pl.c2p.n, 0, stats, err, s);
+    launch_c2p_batched(p, pl.mink, pl.views_out, pl.c2p.d_items, pl.c2p.n, 0, pl.mlp, pl.brk, stats, err, s);
     launch_c2p_fixup_batched(p, pl.mink, pl.views_out, pl.update.d_items, pl.update.n, s);  // interior zones
     launch_floors_batched(p, pl.mink, pl.views_out, pl.c2p.d_items, pl.c2p.n, stats, err, s);  // entire blocks
   }
@@ -251,8 +254,8 @@ static bool same_block(const phx_block &a, const phx_block &b) {
 }
 
 static bool same_plan(const BatchPlan &pl, const phx_block *blocks, int n, const double *const *base,
-                      double *const *out, const Par &par) {
-  if ((int)pl.blocks.size() != n) return false;
+                      double *const *out, const Par &par, const MlpPacked *mlp) {
+  if ((int)pl.blocks.size() != n || pl.mlp != mlp) return false;
   if (memcmp(&pl.par, &par, sizeof(Par)) != 0) return false;  // Par is zero-filled before assignment
   for (int i = 0; i < n; i++) {
     if (!same_block(pl.blocks[i], blocks[i])) return false;
@@ -264,12 +267,12 @@ static bool same_plan(const BatchPlan &pl, const phx_block *blocks, int n, const
 // Build (or find) the plan of this block set and launch its graph.
 // views: validated views of the blocks (cons = stage input).
 cudaError_t batch_stage(BatchCache *cache, const Par &par, const phx_block *blocks, const BView *views, int n,
-                        const double *const *base, double *const *out, double beta, double dt, DevStats *stats,
-                        unsigned int *err, cudaStream_t s, const char **why) {
+                        const double *const *base, double *const *out, double beta, double dt,
+                        const MlpPacked *mlp, DevStats *stats, unsigned int *err, cudaStream_t s, const char **why) {
   *why = nullptr;
   BatchPlan *pl = nullptr;
   for (auto &q : cache->plans)
-    if (same_plan(*q, blocks, n, base, out, par)) pl = q.get();
+    if (same_plan(*q, blocks, n, base, out, par, mlp)) pl = q.get();
   cudaError_t e = cudaSuccess;
   if (!pl) {
     auto np = std::make_unique<BatchPlan>();
@@ -278,6 +281,7 @@ cudaError_t batch_stage(BatchCache *cache, const Par &par, const phx_block *bloc
     P.base.assign(base, base + n);
     P.out.assign(out, out + n);
     P.par = par;
+    P.mlp = mlp;
     P.mink = !views[0].fmks;
     P.ndim = views[0].ndim;
     std::vector<BView> vin(views, views + n), vout(views, views + n);
@@ -311,6 +315,7 @@ cudaError_t batch_stage(BatchCache *cache, const Par &par, const phx_block *bloc
     if ((e = upload_items(P, P.update, make_items(interior, 256))) != cudaSuccess) return e;
     if ((e = upload_items(P, P.ghost, make_items(all, 256))) != cudaSuccess) return e;
     if ((e = upload_items(P, P.c2p, make_items(all, 128))) != cudaSuccess) return e;
+    if (mlp && (e = cudaMalloc(&P.brk, sizeof(double) * 3 * (size_t)P.c2p.n * 128)) != cudaSuccess) return e;
     // tile shapes
     {
       std::lock_guard<std::mutex> lk(g_tune_mu);

@@ -518,9 +518,48 @@ void launch_mlp_bracket(const Par &p, long long n, const double *cons, const dou
 // con2prim over the entire zones of many blocks: persistent CTAs walk
 // (block, [first, last)) items; the root find runs to completion in place
 // (no iteration cap: the retry list is per chunk of one zone list).
+// Learned start of the batched con2prim: item it's zone first + tid gets
+// its bracket at brk[c * (nitems * C2P_THREADS) + it * C2P_THREADS + tid].
 template <bool MINK>
+__global__ void __launch_bounds__(C2P_THREADS) kb_mlp_bracket(Par p, const BView *views, const WorkItem *items,
+                                                              int nitems, const MlpPacked *mlp, double *brk,
+                                                              unsigned int *err) {
+  extern __shared__ __align__(16) unsigned char kbb_dyn[];
+  __shared__ __align__(8) uint64_t bar;
+  BracketSmem *S = reinterpret_cast<BracketSmem *>(kbb_dyn);
+  if (!mlp_stage_weights(&S->w, mlp, &bar, err)) return;
+  const int warp = threadIdx.x >> 5;
+  const long long stride = (long long)nitems * C2P_THREADS;
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const WorkItem w = items[it];
+    const BView &bv = views[w.block];
+    const BoxZones zones{bv, Range3{0, bv.n1t - 1, 0, bv.n2t - 1, 0, bv.n3t - 1}};
+    const long long q = w.first + threadIdx.x;
+    float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    bool ok = false;
+    if (q < w.last) {
+      long long id;
+      Pt g{};
+      double U[PHX_NCONS], x1, x2, x3, guess;
+      zones.template load<MINK>(q, id, g, U, x1, x2, x3, guess);
+      Residual res;
+      double rcon[3], rcov[3], bu[3], Bprim[3] = {0.0, 0.0, 0.0}, bdotr = 0.0;
+      ok = c2p_setup<MINK>(p, g, U, x1, x2, x3, res, rcon, rcov, bu, Bprim, bdotr);
+      if (ok) c2p_features(res, f);
+    }
+    float o0, o1;
+    mlp_warp_forward(S->w, f, S->xs[warp], S->os[warp], o0, o1);
+    double lb[3];
+    mlp_bracket(o0, o1, lb);
+    const double nan = __longlong_as_double(0x7ff8000000000000ll);
+    const long long o = (long long)it * C2P_THREADS + threadIdx.x;
+    for (int c = 0; c < 3; c++) brk[c * stride + o] = ok ? lb[c] : nan;
+  }
+}
+
+template <bool MINK, bool LEARNED>
 __global__ void __launch_bounds__(C2P_THREADS) kb_c2p(Par p, const BView *views, const WorkItem *items, int nitems,
-                                                       DevStats *stats, unsigned int *err) {
+                                                       const double *brk, DevStats *stats, unsigned int *err) {
   __shared__ unsigned int s_hist[PHX_C2P_HIST];
   __shared__ unsigned long long s_cnt[6];
   if (stats) {
@@ -546,7 +585,13 @@ __global__ void __launch_bounds__(C2P_THREADS) kb_c2p(Par p, const BView *views,
       setup_ok = c2p_setup<MINK>(p, g, U, x1, x2, x3, res, rcon, rcov, bu, Bprim, bdotr);
     }
     RFState st;
-    rf_start<false>(p, res, valid && setup_ok, 0.0, 1.0, guess, nullptr, st);
+    if constexpr (LEARNED) {
+      const long long stride = (long long)nitems * C2P_THREADS, o = (long long)it * C2P_THREADS + threadIdx.x;
+      const double lb[3] = {brk[o], brk[stride + o], brk[2 * stride + o]};
+      rf_start<true>(p, res, valid && setup_ok, 0.0, 1.0, guess, lb, st);
+    } else {
+      rf_start<false>(p, res, valid && setup_ok, 0.0, 1.0, guess, nullptr, st);
+    }
     rf_iterate(p, res, valid && setup_ok, st, p.c2p_max_iter);
     if (valid) {
       C2POut out{0, 0, false, true, false, false};
@@ -558,15 +603,28 @@ __global__ void __launch_bounds__(C2P_THREADS) kb_c2p(Par p, const BView *views,
   if (stats) c2p_flush_stats(stats, s_hist, s_cnt);
 }
 
+template <bool MINK>
+static void c2p_batched_t(const Par &p, const BView *views, const WorkItem *items, int nitems, int grid,
+                          const MlpPacked *mlp, double *brk, DevStats *stats, unsigned int *err, cudaStream_t s) {
+  if (mlp) {
+    static_assert(sizeof(BracketSmem) <= 48 * 1024, "no opt-in attribute needed (launches may be captured)");
+    kb_mlp_bracket<MINK><<<persistent_grid(kb_mlp_bracket<MINK>, C2P_THREADS, sizeof(BracketSmem), nitems, 0),
+                           C2P_THREADS, sizeof(BracketSmem), s>>>(p, views, items, nitems, mlp, brk, err);
+    kb_c2p<MINK, true><<<persistent_grid(kb_c2p<MINK, true>, C2P_THREADS, 0, nitems, grid), C2P_THREADS, 0, s>>>(
+        p, views, items, nitems, brk, stats, err);
+  } else {
+    kb_c2p<MINK, false><<<persistent_grid(kb_c2p<MINK, false>, C2P_THREADS, 0, nitems, grid), C2P_THREADS, 0, s>>>(
+        p, views, items, nitems, nullptr, stats, err);
+  }
+}
+
 void launch_c2p_batched(const Par &p, bool mink, const BView *views, const WorkItem *items, int nitems, int grid,
-                        DevStats *stats, unsigned int *err, cudaStream_t s) {
+                        const MlpPacked *mlp, double *brk, DevStats *stats, unsigned int *err, cudaStream_t s) {
   if (nitems <= 0) return;
   if (mink)
-    kb_c2p<true><<<persistent_grid(kb_c2p<true>, C2P_THREADS, 0, nitems, grid), C2P_THREADS, 0, s>>>(
-        p, views, items, nitems, stats, err);
+    c2p_batched_t<true>(p, views, items, nitems, grid, mlp, brk, stats, err, s);
   else
-    kb_c2p<false><<<persistent_grid(kb_c2p<false>, C2P_THREADS, 0, nitems, grid), C2P_THREADS, 0, s>>>(
-        p, views, items, nitems, stats, err);
+    c2p_batched_t<false>(p, views, items, nitems, grid, mlp, brk, stats, err, s);
 }
 
 }  // namespace phx

@@ -94,8 +94,8 @@ struct BatchCache;
 BatchCache *batch_cache_create();
 void batch_cache_destroy(BatchCache *c);
 cudaError_t batch_stage(BatchCache *cache, const Par &par, const phx_block *blocks, const BView *views, int n,
-                        const double *const *base, double *const *out, double beta, double dt, DevStats *stats,
-                        unsigned int *err, cudaStream_t s, const char **why);
+                        const double *const *base, double *const *out, double beta, double dt,
+                        const MlpPacked *mlp, DevStats *stats, unsigned int *err, cudaStream_t s, const char **why);
 void batch_last_tuning(BatchCache *cache, int *x1_cells, int *seg, int *launches);
 long long interior_count(const BView &b);
 long long fluxct_count(const BView &b);
@@ -105,8 +105,9 @@ void launch_fluxct_batched(int ndim, const BView *views, const WorkItem *items, 
 void launch_update_batched(const Par &p, const BView *views, const double *const *base, double *const *out,
                            const double *beta_dt, const WorkItem *items, int nitems, int grid, cudaStream_t s);
 void launch_ghost_batched(const BView *views, int nvar, const WorkItem *items, int nitems, int grid, cudaStream_t s);
+// mlp non-null: the learned start; brk holds 3 x nitems x 128 doubles.
 void launch_c2p_batched(const Par &p, bool mink, const BView *views, const WorkItem *items, int nitems, int grid,
-                        DevStats *stats, unsigned int *err, cudaStream_t s);
+                        const MlpPacked *mlp, double *brk, DevStats *stats, unsigned int *err, cudaStream_t s);
 void launch_flux_x1_batched(const Par &p, bool mink, const BView *views, const WorkItem *items, int nitems, int grid,
                             size_t smem, unsigned int *err, cudaStream_t s);
 void prepare_flux_x1_batched(const Par &p, bool mink, size_t smem);

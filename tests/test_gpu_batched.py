@@ -93,18 +93,58 @@ def test_batched_equals_single_block(request, exact, floors):
                         assert_close(g[v][ok], r[v][ok], 1e-12, f"{name}[{v}]")
 
 
-def test_batched_refuses_unsupported(ctx_fast):
+def test_batched_learned_equals_single_block(ctx_exact):
+    """The learned start in the batched stage (bracket launch + root-find
+    launch over all blocks) equals the single-block learned stage bit for
+    bit (exact build), with the same learned-accepted count."""
+    import torch
+
+    from phoebus_gb300 import learned
+
+    theta = learned.init_weights(5)
+    theta[-2:] = [-0.3, -1.0]  # brackets [0.25 m, m e^1.1]: a mix of accepted and rejected starts
+    ctx_exact.mlp_set_weights(theta)
+    p = params()
+    a = make_blocks(ctx_exact, p)
+    b = copy_blocks(a)
+    sa = [torch.zeros_like(x["cons"]) for x in a]
+    sb = [torch.zeros_like(x["cons"]) for x in b]
+    dt = 0.2 * min(ctx_exact.EstimateTimestepBlock(p, x, False).item() for x in a)
+    from phoebus_gb300.fluid import rk2_step
+
+    acc = []
+    for run in ("single", "batched"):
+        ctx_exact.c2p_stats(reset=True)
+        for step in range(2):
+            if run == "single":
+                for x, s in zip(a, sa):
+                    rk2_step(ctx_exact, p, x, s, dt, learned=True)
+            else:
+                bases = [x["cons"] for x in b]
+                ctx_exact.StageBatched(p, b, bases, sb, 1.0, dt, learned=True)
+                st2 = []
+                for x, s in zip(b, sb):
+                    c = states.Block(x.nx, x.ng, x.ndim, x.xmin, x.dx, backend="torch", device="cuda",
+                                     arrays=dict(x.arrays))
+                    c.arrays["cons"] = s
+                    st2.append(c)
+                ctx_exact.StageBatched(p, st2, bases, bases, 0.5, dt, learned=True)
+        ctx_exact.check()
+        acc.append(ctx_exact.c2p_stats(reset=True))
+    for x, y in zip(a, b):
+        for name in ("prim", "cons", "fail"):
+            assert_bitwise(y[name], x[name], name)
+    assert acc[0]["learned_accepted"] == acc[1]["learned_accepted"] > 0
+    assert acc[0]["iterations"] == acc[1]["iterations"]
+
+
+def test_batched_refuses_mixed_blocks(ctx_fast):
     import torch
 
     p = params()
-    blocks = make_blocks(ctx_fast, p)[:2]
-    bases = [b["cons"] for b in blocks]
-    outs = [torch.zeros_like(x) for x in bases]
-    with pytest.raises(PhxError) as e:
-        ctx_fast.StageBatched(p, blocks, bases, outs, 1.0, 1e-3, learned=True)
-    assert e.value.status == 8
-    mixed = blocks[:1] + [states.Block((8, 8, 1), 4, 2, (0, 0, 0), (0.1, 0.1, 1.0), backend="torch",
-                                       device="cuda").alloc()]
+    blocks = make_blocks(ctx_fast, p)[:1]
+    mixed = blocks + [states.Block((8, 8, 1), 4, 2, (0, 0, 0), (0.1, 0.1, 1.0), backend="torch",
+                                   device="cuda").alloc()]
     with pytest.raises(PhxError) as e:
         ctx_fast.StageBatched(p, mixed, [b["cons"] for b in mixed], [torch.zeros_like(b["cons"]) for b in mixed],
                               1.0, 1e-3)
