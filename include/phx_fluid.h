@@ -362,6 +362,38 @@ phx_status phx_stage_batched(phx_ctx *ctx, const phx_params *p, const phx_block 
                              double *const *cons_out, double beta, double dt,
                              int use_learned_guess, void *stream);
 
+/* A domain tiled by blocks as a tensor product of per-axis segments, for
+ * phx_stage_mesh.  Block (s1, s2, s3) (segment indices) is blocks[(s3 *
+ * nseg[1] + s2) * nseg[0] + s1]; its interior covers global cells
+ * seg_start[d][s_d] .. seg_start[d][s_d + 1] - 1 on axis d. */
+#define PHX_BC_PERIODIC 0
+#define PHX_BC_OUTFLOW 1 /* gr_outflow: copy the boundary cell's primitives,
+                            the normal velocity set to 0 where it points in */
+typedef struct {
+  int n[3];                  /* global interior cells per axis            */
+  int nseg[3];               /* segments (blocks) per axis                */
+  const int *seg_start[3];   /* host arrays of nseg[d] + 1 entries         */
+  int bc_lo[3], bc_hi[3];    /* PHX_BC_* of each face                      */
+} phx_mesh;
+
+/* The stage of phx_stage over a tiled mesh: the ghost exchange copies the
+ * primitives of the owning block's cell (bc_vars = primitive, as the torus
+ * deck) or applies the physical boundary, then rebuilds the ghost's conserved
+ * variables with its own metric (prim2con).  batched = 1: one persistent
+ * launch per phase replayed as a CUDA graph (as phx_stage_batched);
+ * batched = 0: the same kernels launched block by block (the launch
+ * structure of per-block tasks).  Plans are built and cached as in
+ * phx_stage_batched. */
+phx_status phx_stage_mesh(phx_ctx *ctx, const phx_params *p, const phx_mesh *mesh, const phx_block *blocks,
+                          int nblocks, const double *const *cons_base, double *const *cons_out, double beta,
+                          double dt, int use_learned_guess, int batched, void *stream);
+
+/* Fill every ghost zone of a tiled mesh (primitives from the owners or the
+ * physical boundaries, conserved variables by prim2con) -- the mesh's
+ * boundary exchange on its own, e.g. after initialisation. */
+phx_status phx_mesh_exchange(phx_ctx *ctx, const phx_params *p, const phx_mesh *mesh, const phx_block *blocks,
+                             int nblocks, void *stream);
+
 /* Tile shapes and graph size of the most recent batched plan (0 if none). */
 phx_status phx_batch_info(phx_ctx *ctx, int *x1_cells, int *sweep_seg, int *graph_nodes);
 

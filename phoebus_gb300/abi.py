@@ -80,6 +80,14 @@ class C2PStats(C.Structure):
                 ("learned_accepted", C.c_ulonglong), ("hist", C.c_ulonglong * C2P_HIST)]
 
 
+class Mesh(C.Structure):
+    _fields_ = [("n", C.c_int * 3), ("nseg", C.c_int * 3), ("seg_start", C.c_void_p * 3), ("bc_lo", C.c_int * 3),
+                ("bc_hi", C.c_int * 3)]
+
+
+BC_PERIODIC, BC_OUTFLOW = 0, 1
+
+
 class MlpTrainOpts(C.Structure):
     _fields_ = [("batch", C.c_int), ("epochs", C.c_int), ("lr", C.c_float), ("lr_min", C.c_float),
                 ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float), ("weight_decay", C.c_float)]
@@ -142,6 +150,9 @@ _SIGS = {
                             C.c_int, _P]),
     "phx_stage_batched": (C.c_int, [_P, C.POINTER(Params), C.POINTER(BlockS), C.c_int, _P, _P, C.c_double,
                                     C.c_double, C.c_int, _P]),
+    "phx_stage_mesh": (C.c_int, [_P, C.POINTER(Params), C.POINTER(Mesh), C.POINTER(BlockS), C.c_int, _P, _P,
+                                 C.c_double, C.c_double, C.c_int, C.c_int, _P]),
+    "phx_mesh_exchange": (C.c_int, [_P, C.POINTER(Params), C.POINTER(Mesh), C.POINTER(BlockS), C.c_int, _P]),
     "phx_batch_info": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "phx_mlp_set_weights": (C.c_int, [_P, C.POINTER(C.c_float)]),
     "phx_mlp_get_weights": (C.c_int, [_P, C.POINTER(C.c_float)]),

@@ -606,10 +606,91 @@ phx_status phx_stage_batched(phx_ctx *ctx, const phx_params *p, const phx_block 
   }
   const char *why = nullptr;
   cudaError_t e = phx::batch_stage(ctx->batch, make_par(*p), blocks, views.data(), nblocks, cons_base, cons_out, beta,
-                                   dt, use_learned_guess ? ctx->mlp_packed : nullptr, ctx->stats, ctx->err, S(stream),
-                                   &why);
+                                   dt, use_learned_guess ? ctx->mlp_packed : nullptr, nullptr, true, false,
+                                   ctx->stats, ctx->err, S(stream), &why);
   if (e != cudaSuccess) return fail(PHX_ERR_CUDA, "phx_stage_batched: %s", cudaGetErrorString(e));
   return cuda_status("phx_stage_batched");
+}
+
+// Validate a tiled mesh against its blocks (3D, ng equal, block extents =
+// segment lengths, blocks ordered by segment triple).
+static phx_status check_mesh(const phx_mesh *m, const phx_block *blocks, int nblocks, std::vector<phx::BView> &views) {
+  if (!m || !blocks) return fail(PHX_ERR_INVALID_ARG, "mesh/blocks is NULL");
+  long long nb = 1;
+  for (int d = 0; d < 3; d++) {
+    if (m->nseg[d] < 1 || m->n[d] < 1 || !m->seg_start[d]) return fail(PHX_ERR_INVALID_ARG, "bad mesh axis %d", d);
+    if (m->seg_start[d][0] != 0 || m->seg_start[d][m->nseg[d]] != m->n[d])
+      return fail(PHX_ERR_INVALID_ARG, "mesh axis %d: segments must cover [0, n)", d);
+    for (int k = 0; k < m->nseg[d]; k++)
+      if (m->seg_start[d][k + 1] <= m->seg_start[d][k]) return fail(PHX_ERR_INVALID_ARG, "empty segment");
+    if ((m->bc_lo[d] != PHX_BC_PERIODIC && m->bc_lo[d] != PHX_BC_OUTFLOW) ||
+        (m->bc_hi[d] != PHX_BC_PERIODIC && m->bc_hi[d] != PHX_BC_OUTFLOW))
+      return fail(PHX_ERR_INVALID_ARG, "unknown boundary condition");
+    nb *= m->nseg[d];
+  }
+  if (nb != nblocks) return fail(PHX_ERR_INVALID_ARG, "mesh has %lld blocks, %d given", nb, nblocks);
+  views.resize(nblocks);
+  phx_status s;
+  for (int s3 = 0, b = 0; s3 < m->nseg[2]; s3++)
+    for (int s2 = 0; s2 < m->nseg[1]; s2++)
+      for (int s1 = 0; s1 < m->nseg[0]; s1++, b++) {
+        if ((s = make_view(&blocks[b], views[b]))) return fail(s, "block %d: %s", b, g_last_error.c_str());
+        const phx_block &B = blocks[b];
+        if (B.ndim != 3 || B.ng != blocks[0].ng) return fail(PHX_ERR_INVALID_ARG, "mesh blocks must be 3D, same ng");
+        if (B.nx1 != m->seg_start[0][s1 + 1] - m->seg_start[0][s1] ||
+            B.nx2 != m->seg_start[1][s2 + 1] - m->seg_start[1][s2] ||
+            B.nx3 != m->seg_start[2][s3 + 1] - m->seg_start[2][s3])
+          return fail(PHX_ERR_INVALID_ARG, "block %d extents differ from its mesh segments", b);
+        if (B.nx1 < B.ng || B.nx2 < B.ng || B.nx3 < B.ng)
+          return fail(PHX_ERR_INVALID_ARG, "block %d: ghost exchange needs nx >= ng", b);
+        if (views[b].fmks != views[0].fmks) return fail(PHX_ERR_INVALID_ARG, "blocks must share the geometry kind");
+      }
+  return PHX_OK;
+}
+
+phx_status phx_stage_mesh(phx_ctx *ctx, const phx_params *p, const phx_mesh *mesh, const phx_block *blocks,
+                          int nblocks, const double *const *cons_base, double *const *cons_out, double beta,
+                          double dt, int use_learned_guess, int batched, void *stream) {
+  phx_status s;
+  if ((s = ctx_device(ctx)) || (s = check_params(p))) return s;
+  if (!cons_base || !cons_out) return fail(PHX_ERR_INVALID_ARG, "cons_base/cons_out is NULL");
+  if (use_learned_guess && !ctx->mlp_loaded) return fail(PHX_ERR_INVALID_ARG, "no learned-guess weights loaded");
+  std::vector<phx::BView> views;
+  if ((s = check_mesh(mesh, blocks, nblocks, views))) return s;
+  for (int n = 0; n < nblocks; n++) {
+    const phx_block *b = &blocks[n];
+    if (!b->flux || !b->face_sig || !b->cell_sig || !b->fail || !b->src || !cons_base[n] || !cons_out[n])
+      return fail(PHX_ERR_INVALID_ARG, "block %d: stage needs flux, face_sig, cell_sig, fail, src, cons_base, "
+                                       "cons_out", n);
+    if (p->mhd && !b->emf) return fail(PHX_ERR_INVALID_ARG, "block %d: emf is NULL", n);
+  }
+  const char *why = nullptr;
+  cudaError_t e = phx::batch_stage(ctx->batch, make_par(*p), blocks, views.data(), nblocks, cons_base, cons_out, beta,
+                                   dt, use_learned_guess ? ctx->mlp_packed : nullptr, mesh, batched != 0, false,
+                                   ctx->stats, ctx->err, S(stream), &why);
+  if (e != cudaSuccess) return fail(PHX_ERR_CUDA, "phx_stage_mesh: %s", cudaGetErrorString(e));
+  return cuda_status("phx_stage_mesh");
+}
+
+phx_status phx_mesh_exchange(phx_ctx *ctx, const phx_params *p, const phx_mesh *mesh, const phx_block *blocks,
+                             int nblocks, void *stream) {
+  phx_status s;
+  if ((s = ctx_device(ctx)) || (s = check_params(p))) return s;
+  std::vector<phx::BView> views;
+  if ((s = check_mesh(mesh, blocks, nblocks, views))) return s;
+  for (int n = 0; n < nblocks; n++)
+    if (!blocks[n].cell_sig) return fail(PHX_ERR_INVALID_ARG, "block %d: cell_sig is NULL", n);
+  std::vector<const double *> base(nblocks);
+  std::vector<double *> out(nblocks);
+  for (int n = 0; n < nblocks; n++) {
+    base[n] = blocks[n].cons;
+    out[n] = blocks[n].cons;
+  }
+  const char *why = nullptr;
+  cudaError_t e = phx::batch_stage(ctx->batch, make_par(*p), blocks, views.data(), nblocks, base.data(), out.data(),
+                                   0.0, 0.0, nullptr, mesh, true, true, ctx->stats, ctx->err, S(stream), &why);
+  if (e != cudaSuccess) return fail(PHX_ERR_CUDA, "phx_mesh_exchange: %s", cudaGetErrorString(e));
+  return cuda_status("phx_mesh_exchange");
 }
 
 phx_status phx_batch_info(phx_ctx *ctx, int *x1_cells, int *sweep_seg, int *graph_nodes) {

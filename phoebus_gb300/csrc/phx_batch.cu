@@ -37,6 +37,7 @@ namespace {
 struct PhaseList {
   WorkItem *d_items = nullptr;
   int n = 0;
+  std::vector<int> boff;  // items of block b: [boff[b], boff[b + 1])
 };
 
 struct Tuning {
@@ -86,7 +87,8 @@ void save_tune_file() {
 
 struct BatchPlan {
   // identity
-  std::vector<phx_block> blocks;
+  std::vector<phx_block> blocks;   // geom pointers re-pointed into geoms
+  std::vector<phx_geometry> geoms;
   std::vector<const double *> base;
   std::vector<double *> out;
   Par par;
@@ -104,6 +106,12 @@ struct BatchPlan {
   int ndim = 3;
   const MlpPacked *mlp = nullptr;  // learned start (packed weights in the context) or null
   double *brk = nullptr;           // learned brackets, 3 x c2p items x 128
+  bool batched = true;             // one persistent launch per phase in a graph; else block by block
+  bool has_mesh = false;           // tiled mesh exchange instead of per-block periodic ghosts
+  int mesh_n[3] = {0, 0, 0}, mesh_nseg[3] = {0, 0, 0}, mesh_bc[6] = {0, 0, 0, 0, 0, 0};
+  std::vector<int> mesh_seg[3];    // host copy of the segment starts
+  MeshDev md{};
+  void *mesh_mem = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaGraph_t graph = nullptr;
   ~BatchPlan() {
@@ -111,6 +119,7 @@ struct BatchPlan {
     if (graph) cudaGraphDestroy(graph);
     for (void *m : item_mem) cudaFree(m);
     cudaFree(brk);
+    cudaFree(mesh_mem);
     cudaFree(mem);
   }
 };
@@ -132,6 +141,9 @@ static std::vector<WorkItem> make_items(const std::vector<long long> &counts, lo
 
 static cudaError_t upload_items(BatchPlan &pl, PhaseList &ph, const std::vector<WorkItem> &items) {
   ph.n = (int)items.size();
+  ph.boff.assign(pl.blocks.size() + 1, 0);
+  for (const WorkItem &w : items) ph.boff[w.block + 1]++;
+  for (size_t b = 0; b < pl.blocks.size(); b++) ph.boff[b + 1] += ph.boff[b];
   if (items.empty()) return cudaSuccess;
   void *m = nullptr;
   cudaError_t e = cudaMalloc(&m, sizeof(WorkItem) * items.size());
@@ -218,21 +230,129 @@ static Tuning autotune(BatchPlan &pl, const std::vector<BView> &v, unsigned int 
   return best;
 }
 
-// The stage's launches, in order (captured into the plan's graph).
-static void stage_launches(BatchPlan &pl, DevStats *stats, unsigned int *err, cudaStream_t s) {
+// The stage's launches, in order.  Batched: one persistent launch per phase
+// over all items (captured into the plan's graph).  Per block: phase by phase,
+// each block's items in a launch of its own (one item per CTA).
+static void stage_launches(BatchPlan &pl, DevStats *stats, unsigned int *err, cudaStream_t s,
+                           bool exchange_only = false) {
   const Par &p = pl.par;
-  launch_sources_batched(p, pl.mink, pl.views_in, pl.sources.d_items, pl.sources.n, 0, s);
-  launch_flux_x1_batched(p, pl.mink, pl.views_in, pl.x1.d_items, pl.x1.n, 0, pl.x1_smem, err, s);
-  if (pl.ndim >= 2) launch_flux_sweep_batched(p, pl.mink, 1, pl.views_in, pl.x2.d_items, pl.x2.n, 0, pl.tune.seg, s);
-  if (pl.ndim >= 3) launch_flux_sweep_batched(p, pl.mink, 2, pl.views_in, pl.x3.d_items, pl.x3.n, 0, pl.tune.seg, s);
-  if (p.mhd && pl.ndim > 1) launch_fluxct_batched(pl.ndim, pl.views_in, pl.fluxct.d_items, pl.fluxct.n, 0, s);
-  launch_update_batched(p, pl.views_in, pl.base_tab, pl.out_tab, pl.beta_dt, pl.update.d_items, pl.update.n, 0, s);
-  for (int pass = 0; pass < 2; pass++) {  // FillDerived over MeshData, then per block after the exchange
-    if (pass == 1) launch_ghost_batched(pl.views_out, p.mhd ? PHX_NCONS : 5, pl.ghost.d_items, pl.ghost.n, 0, s);
-    launch_c2p_batched(p, pl.mink, pl.views_out, pl.c2p.d_items, pl.c2p.n, 0, pl.mlp, pl.brk, stats, err, s);
-    launch_c2p_fixup_batched(p, pl.mink, pl.views_out, pl.update.d_items, pl.update.n, s);  // interior zones
-    launch_floors_batched(p, pl.mink, pl.views_out, pl.c2p.d_items, pl.c2p.n, stats, err, s);  // entire blocks
+  const int nb = (int)pl.blocks.size();
+  // run fn(items, count, grid) for all items, or block by block
+  auto each = [&](const PhaseList &ph, const std::function<void(const WorkItem *, int, int)> &fn) {
+    if (pl.batched) {
+      fn(ph.d_items, ph.n, 0);
+      return;
+    }
+    for (int b = 0; b < nb; b++) {
+      const int c = ph.boff[b + 1] - ph.boff[b];
+      if (c > 0) fn(ph.d_items + ph.boff[b], c, c);
+    }
+  };
+  auto exchange = [&] {
+    if (pl.has_mesh)
+      each(pl.c2p, [&](const WorkItem *it, int n, int g) {
+        launch_mesh_exchange(p, pl.mink, pl.views_out, pl.md, it, n, g, s);
+      });
+    else
+      each(pl.ghost, [&](const WorkItem *it, int n, int g) {
+        launch_ghost_batched(pl.views_out, p.mhd ? PHX_NCONS : 5, it, n, g, s);
+      });
+  };
+  if (exchange_only) {
+    exchange();
+    return;
   }
+  each(pl.sources, [&](const WorkItem *it, int n, int g) { launch_sources_batched(p, pl.mink, pl.views_in, it, n, g, s); });
+  each(pl.x1, [&](const WorkItem *it, int n, int g) {
+    launch_flux_x1_batched(p, pl.mink, pl.views_in, it, n, g, pl.x1_smem, err, s);
+  });
+  if (pl.ndim >= 2)
+    each(pl.x2, [&](const WorkItem *it, int n, int g) {
+      launch_flux_sweep_batched(p, pl.mink, 1, pl.views_in, it, n, g, pl.tune.seg, s);
+    });
+  if (pl.ndim >= 3)
+    each(pl.x3, [&](const WorkItem *it, int n, int g) {
+      launch_flux_sweep_batched(p, pl.mink, 2, pl.views_in, it, n, g, pl.tune.seg, s);
+    });
+  if (p.mhd && pl.ndim > 1)
+    each(pl.fluxct, [&](const WorkItem *it, int n, int g) { launch_fluxct_batched(pl.ndim, pl.views_in, it, n, g, s); });
+  each(pl.update, [&](const WorkItem *it, int n, int g) {
+    launch_update_batched(p, pl.views_in, pl.base_tab, pl.out_tab, pl.beta_dt, it, n, g, s);
+  });
+  for (int pass = 0; pass < 2; pass++) {  // FillDerived over MeshData, then per block after the exchange
+    if (pass == 1) exchange();
+    each(pl.c2p, [&](const WorkItem *it, int n, int g) {
+      launch_c2p_batched(p, pl.mink, pl.views_out, it, n, g, pl.mlp, pl.brk, stats, err, s);
+    });
+    each(pl.update, [&](const WorkItem *it, int n, int g) {  // interior zones
+      launch_c2p_fixup_batched(p, pl.mink, pl.views_out, it, n, s);
+    });
+    each(pl.c2p, [&](const WorkItem *it, int n, int g) {  // entire blocks
+      launch_floors_batched(p, pl.mink, pl.views_out, it, n, stats, err, s);
+    });
+  }
+}
+
+static bool same_mesh(const BatchPlan &pl, const phx_mesh *m) {
+  if (!m) return !pl.has_mesh;
+  if (!pl.has_mesh) return false;
+  for (int d = 0; d < 3; d++) {
+    if (pl.mesh_n[d] != m->n[d] || pl.mesh_nseg[d] != m->nseg[d] || pl.mesh_bc[2 * d] != m->bc_lo[d] ||
+        pl.mesh_bc[2 * d + 1] != m->bc_hi[d])
+      return false;
+    for (int k = 0; k <= m->nseg[d]; k++)
+      if (pl.mesh_seg[d][k] != m->seg_start[d][k]) return false;
+  }
+  return true;
+}
+
+// Upload the mesh maps: per-axis cell -> segment, segment triple -> block,
+// block -> origin.
+static cudaError_t upload_mesh(BatchPlan &P, const phx_mesh *m, int nblocks) {
+  P.has_mesh = true;
+  size_t ints = 0;
+  for (int d = 0; d < 3; d++) {
+    P.mesh_n[d] = m->n[d];
+    P.mesh_nseg[d] = m->nseg[d];
+    P.mesh_bc[2 * d] = m->bc_lo[d];
+    P.mesh_bc[2 * d + 1] = m->bc_hi[d];
+    P.mesh_seg[d].assign(m->seg_start[d], m->seg_start[d] + m->nseg[d] + 1);
+    ints += m->n[d];
+  }
+  ints += (size_t)nblocks + 3 * (size_t)nblocks;
+  std::vector<int> host;
+  host.reserve(ints);
+  size_t off_seg[3], off_owner, off_origin;
+  for (int d = 0; d < 3; d++) {
+    off_seg[d] = host.size();
+    for (int s = 0; s < m->nseg[d]; s++)
+      for (int c = m->seg_start[d][s]; c < m->seg_start[d][s + 1]; c++) host.push_back(s);
+  }
+  off_owner = host.size();
+  for (int b = 0; b < nblocks; b++) host.push_back(b);  // blocks are ordered by segment triple
+  off_origin = host.size();
+  for (int s3 = 0; s3 < m->nseg[2]; s3++)
+    for (int s2 = 0; s2 < m->nseg[1]; s2++)
+      for (int s1 = 0; s1 < m->nseg[0]; s1++) {
+        host.push_back(m->seg_start[0][s1]);
+        host.push_back(m->seg_start[1][s2]);
+        host.push_back(m->seg_start[2][s3]);
+      }
+  cudaError_t e = cudaMalloc(&P.mesh_mem, sizeof(int) * host.size());
+  if (e != cudaSuccess) return e;
+  if ((e = cudaMemcpy(P.mesh_mem, host.data(), sizeof(int) * host.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+    return e;
+  const int *base = static_cast<const int *>(P.mesh_mem);
+  for (int d = 0; d < 3; d++) {
+    P.md.n[d] = m->n[d];
+    P.md.nseg[d] = m->nseg[d];
+    P.md.bc_lo[d] = m->bc_lo[d];
+    P.md.bc_hi[d] = m->bc_hi[d];
+    P.md.seg_of[d] = base + off_seg[d];
+  }
+  P.md.owner = base + off_owner;
+  P.md.origin = base + off_origin;
+  return cudaSuccess;
 }
 
 // Field-wise (phx_block has padding bytes the caller need not initialise).
@@ -244,18 +364,21 @@ static bool same_block(const phx_block &a, const phx_block &b) {
       a.dx3 != b.dx3)
     return false;
   if (a.prim != b.prim || a.cons != b.cons || a.flux != b.flux || a.face_sig != b.face_sig ||
-      a.cell_sig != b.cell_sig || a.fail != b.fail || a.src != b.src || a.emf != b.emf || a.dudt != b.dudt ||
-      a.geom != b.geom)
+      a.cell_sig != b.cell_sig || a.fail != b.fail || a.src != b.src || a.emf != b.emf || a.dudt != b.dudt)
     return false;
-  if (a.geom && (a.geom->kind != b.geom->kind || a.geom->cent != b.geom->cent || a.geom->face1 != b.geom->face1 ||
-                 a.geom->face2 != b.geom->face2 || a.geom->deriv != b.geom->deriv))
+  // geometry by content: the caller may pass a fresh phx_geometry each call
+  const bool fa = a.geom && a.geom->kind == PHX_GEOM_FMKS, fb = b.geom && b.geom->kind == PHX_GEOM_FMKS;
+  if (fa != fb) return false;
+  if (fa && (a.geom->cent != b.geom->cent || a.geom->face1 != b.geom->face1 || a.geom->face2 != b.geom->face2 ||
+             a.geom->deriv != b.geom->deriv))
     return false;
   return true;
 }
 
 static bool same_plan(const BatchPlan &pl, const phx_block *blocks, int n, const double *const *base,
-                      double *const *out, const Par &par, const MlpPacked *mlp) {
-  if ((int)pl.blocks.size() != n || pl.mlp != mlp) return false;
+                      double *const *out, const Par &par, const MlpPacked *mlp, const phx_mesh *mesh,
+                      bool batched) {
+  if ((int)pl.blocks.size() != n || pl.mlp != mlp || pl.batched != batched || !same_mesh(pl, mesh)) return false;
   if (memcmp(&pl.par, &par, sizeof(Par)) != 0) return false;  // Par is zero-filled before assignment
   for (int i = 0; i < n; i++) {
     if (!same_block(pl.blocks[i], blocks[i])) return false;
@@ -268,20 +391,28 @@ static bool same_plan(const BatchPlan &pl, const phx_block *blocks, int n, const
 // views: validated views of the blocks (cons = stage input).
 cudaError_t batch_stage(BatchCache *cache, const Par &par, const phx_block *blocks, const BView *views, int n,
                         const double *const *base, double *const *out, double beta, double dt,
-                        const MlpPacked *mlp, DevStats *stats, unsigned int *err, cudaStream_t s, const char **why) {
+                        const MlpPacked *mlp, const phx_mesh *mesh, bool batched, bool exchange_only,
+                        DevStats *stats, unsigned int *err, cudaStream_t s, const char **why) {
   *why = nullptr;
   BatchPlan *pl = nullptr;
   for (auto &q : cache->plans)
-    if (same_plan(*q, blocks, n, base, out, par, mlp)) pl = q.get();
+    if (same_plan(*q, blocks, n, base, out, par, mlp, mesh, batched)) pl = q.get();
   cudaError_t e = cudaSuccess;
   if (!pl) {
     auto np = std::make_unique<BatchPlan>();
     BatchPlan &P = *np;
     P.blocks.assign(blocks, blocks + n);
+    P.geoms.resize(n);
+    for (int i = 0; i < n; i++)
+      if (blocks[i].geom) {
+        P.geoms[i] = *blocks[i].geom;
+        P.blocks[i].geom = &P.geoms[i];
+      }
     P.base.assign(base, base + n);
     P.out.assign(out, out + n);
     P.par = par;
     P.mlp = mlp;
+    P.batched = batched;
     P.mink = !views[0].fmks;
     P.ndim = views[0].ndim;
     std::vector<BView> vin(views, views + n), vout(views, views + n);
@@ -316,6 +447,7 @@ cudaError_t batch_stage(BatchCache *cache, const Par &par, const phx_block *bloc
     if ((e = upload_items(P, P.ghost, make_items(all, 256))) != cudaSuccess) return e;
     if ((e = upload_items(P, P.c2p, make_items(all, 128))) != cudaSuccess) return e;
     if (mlp && (e = cudaMalloc(&P.brk, sizeof(double) * 3 * (size_t)P.c2p.n * 128)) != cudaSuccess) return e;
+    if (mesh && (e = upload_mesh(P, mesh, n)) != cudaSuccess) return e;
     // tile shapes
     {
       std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -338,24 +470,31 @@ cudaError_t batch_stage(BatchCache *cache, const Par &par, const phx_block *bloc
     }
     prepare_flux_x1_batched(par, P.mink, P.x1_smem);  // kernel attributes are set outside the capture
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return e;
-    // capture the stage
-    cudaStream_t cs;
-    if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) return e;
-    e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-    if (e == cudaSuccess) {
-      stage_launches(P, stats, err, cs);
-      e = cudaStreamEndCapture(cs, &P.graph);
+    if (batched) {  // capture the stage
+      cudaStream_t cs;
+      if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) return e;
+      e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+      if (e == cudaSuccess) {
+        stage_launches(P, stats, err, cs);
+        e = cudaStreamEndCapture(cs, &P.graph);
+      }
+      cudaStreamDestroy(cs);
+      if (e != cudaSuccess) return e;
+      if ((e = cudaGraphInstantiate(&P.exec, P.graph, 0)) != cudaSuccess) return e;
     }
-    cudaStreamDestroy(cs);
-    if (e != cudaSuccess) return e;
-    if ((e = cudaGraphInstantiate(&P.exec, P.graph, 0)) != cudaSuccess) return e;
     if (cache->plans.size() >= 8) cache->plans.erase(cache->plans.begin());
     cache->plans.push_back(std::move(np));
     pl = cache->plans.back().get();
   }
+  if (exchange_only) {
+    stage_launches(*pl, stats, err, s, true);
+    return cudaGetLastError();
+  }
   const double bd[2] = {beta, dt};
   if ((e = cudaMemcpyAsync(pl->beta_dt, bd, sizeof(bd), cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
-  return cudaGraphLaunch(pl->exec, s);
+  if (pl->batched) return cudaGraphLaunch(pl->exec, s);
+  stage_launches(*pl, stats, err, s);
+  return cudaGetLastError();
 }
 
 // The tuned shapes of the most recent plan (for reporting).
@@ -368,7 +507,7 @@ void batch_last_tuning(BatchCache *cache, int *x1_cells, int *seg, int *launches
   *x1_cells = p.tune.x1_cells;
   *seg = p.tune.seg;
   size_t nn = 0;
-  cudaGraphGetNodes(p.graph, nullptr, &nn);
+  if (p.graph) cudaGraphGetNodes(p.graph, nullptr, &nn);
   *launches = (int)nn;
 }
 

@@ -90,12 +90,25 @@ inline int persistent_grid(K kernel, int threads, size_t smem, int nitems, int g
   const long long g = (long long)(nsm > 0 ? nsm : 1) * (occ > 0 ? occ : 1);
   return (int)(g < nitems ? g : nitems);
 }
+// A tiled mesh on the device (phx_mesh): per-axis global cell -> segment
+// maps, the owner block of each segment triple, each block's origin.
+struct MeshDev {
+  int n[3], nseg[3], bc_lo[3], bc_hi[3];
+  const int *seg_of[3];  // [n[d]]
+  const int *owner;      // [nseg[2]][nseg[1]][nseg[0]]
+  const int *origin;     // [nblocks][3] global index of the first interior cell
+};
+void launch_mesh_exchange(const Par &p, bool mink, const BView *views, const MeshDev &m, const WorkItem *items,
+                          int nitems, int grid, cudaStream_t s);
 struct BatchCache;
 BatchCache *batch_cache_create();
 void batch_cache_destroy(BatchCache *c);
+// mesh: null for independent periodic blocks.  batched = false launches each
+// phase block by block (no graph).  exchange_only: fill the mesh ghosts only.
 cudaError_t batch_stage(BatchCache *cache, const Par &par, const phx_block *blocks, const BView *views, int n,
                         const double *const *base, double *const *out, double beta, double dt,
-                        const MlpPacked *mlp, DevStats *stats, unsigned int *err, cudaStream_t s, const char **why);
+                        const MlpPacked *mlp, const phx_mesh *mesh, bool batched, bool exchange_only,
+                        DevStats *stats, unsigned int *err, cudaStream_t s, const char **why);
 void batch_last_tuning(BatchCache *cache, int *x1_cells, int *seg, int *launches);
 long long interior_count(const BView &b);
 long long fluxct_count(const BView &b);

@@ -385,6 +385,93 @@ __global__ void __launch_bounds__(256) kb_ghost(const BView *views, int nvar, co
   }
 }
 
+// Ghost zone t of block blk on a tiled mesh (phx_mesh; 3D).  The source cell
+// is the global cell of the ghost, wrapped on periodic axes and clamped to
+// the boundary cell on outflow axes, in its owner block; its primitives are
+// copied (the normal velocity zeroed where it points into the domain across
+// an outflow face) and prim2con gives the ghost's conserved variables with
+// the ghost's own metric.
+template <bool MINK>
+__device__ __forceinline__ void mesh_ghost_at(const Par &p, const BView *views, const MeshDev &m, int blk,
+                                              long long t) {
+  const BView &b = views[blk];
+  const int loc[3] = {(int)(t % b.n1t), (int)((t / b.n1t) % b.n2t), (int)(t / ((long long)b.n1t * b.n2t))};
+  const int nx[3] = {b.nx1, b.nx2, b.nx3};
+  bool ghost = false;
+  int g[3], side[3];
+  for (int d = 0; d < 3; d++) {
+    if (loc[d] < b.ng || loc[d] >= b.ng + nx[d]) ghost = true;
+    int gg = m.origin[blk * 3 + d] + loc[d] - b.ng;
+    side[d] = 0;
+    if (gg < 0) {
+      if (m.bc_lo[d] == PHX_BC_PERIODIC) {
+        gg += m.n[d];
+      } else {
+        gg = 0;
+        side[d] = -1;
+      }
+    } else if (gg >= m.n[d]) {
+      if (m.bc_hi[d] == PHX_BC_PERIODIC) {
+        gg -= m.n[d];
+      } else {
+        gg = m.n[d] - 1;
+        side[d] = 1;
+      }
+    }
+    g[d] = gg;
+  }
+  if (!ghost) return;
+  const int src = m.owner[(m.seg_of[2][g[2]] * m.nseg[1] + m.seg_of[1][g[1]]) * m.nseg[0] + m.seg_of[0][g[0]]];
+  const BView &sb = views[src];
+  const long long sid = sb.idx(g[2] - m.origin[src * 3 + 2] + sb.ng, g[1] - m.origin[src * 3 + 1] + sb.ng,
+                               g[0] - m.origin[src * 3 + 0] + sb.ng);
+  double P[PHX_NPRIM];
+  for (int v = 0; v < PHX_NPRIM; v++) P[v] = sb.prim[v * sb.vs + sid];
+  for (int d = 0; d < 3; d++)
+    if ((side[d] < 0 && P[PHX_PVEL + d] > 0.0) || (side[d] > 0 && P[PHX_PVEL + d] < 0.0)) P[PHX_PVEL + d] = 0.0;
+  const long long id = b.idx(loc[2], loc[1], loc[0]);
+  Pt gm{};
+  if constexpr (!MINK) load_pt(b, 0, loc[1], loc[0], gm);
+  const double vel[3] = {P[PHX_PVEL], P[PHX_PVEL + 1], P[PHX_PVEL + 2]};
+  double bp[3] = {0.0, 0.0, 0.0};
+  if (p.mhd)
+    for (int d = 0; d < 3; d++) bp[d] = P[PHX_PB + d];
+  double D, tau, S[3], bc[3], sig[3];
+  p2c<MINK>(P[PHX_PRHO], vel, bp, P[PHX_PENG], P[PHX_PPRS], P[PHX_PGM1], gm, MINK ? 1.0 : gm.detgam, D, S, bc, tau,
+            sig);
+  for (int v = 0; v < PHX_NPRIM; v++) {
+    if (v >= PHX_PB && v < PHX_PB + 3 && !p.mhd) continue;
+    b.prim[v * b.vs + id] = P[v];
+  }
+  b.cons[PHX_CRHO * b.vs + id] = D;
+  b.cons[PHX_CENG * b.vs + id] = tau;
+  for (int d = 0; d < 3; d++) b.cons[(PHX_CMOM + d) * b.vs + id] = S[d];
+  if (p.mhd)
+    for (int d = 0; d < 3; d++) b.cons[(PHX_CB + d) * b.vs + id] = bc[d];
+  for (int d = 0; d < b.ndim; d++) b.cell_sig[d * b.vs + id] = sig[d];
+}
+
+template <bool MINK>
+__global__ void __launch_bounds__(128) kb_mesh_exchange(Par p, const BView *views, MeshDev m, const WorkItem *items,
+                                                        int nitems) {
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const WorkItem w = items[it];
+    const long long t = w.first + threadIdx.x;
+    if (t < w.last) mesh_ghost_at<MINK>(p, views, m, w.block, t);
+  }
+}
+
+void launch_mesh_exchange(const Par &p, bool mink, const BView *views, const MeshDev &m, const WorkItem *items,
+                          int nitems, int grid, cudaStream_t s) {
+  if (nitems <= 0) return;
+  if (mink)
+    kb_mesh_exchange<true><<<persistent_grid(kb_mesh_exchange<true>, 128, 0, nitems, grid), 128, 0, s>>>(
+        p, views, m, items, nitems);
+  else
+    kb_mesh_exchange<false><<<persistent_grid(kb_mesh_exchange<false>, 128, 0, nitems, grid), 128, 0, s>>>(
+        p, views, m, items, nitems);
+}
+
 void launch_sources_batched(const Par &p, bool mink, const BView *views, const WorkItem *items, int nitems, int grid,
                             cudaStream_t s) {
   if (nitems <= 0) return;

@@ -271,6 +271,26 @@ class FluidContext:
         self._ok(self.lib.phx_stage_batched(self.h, C.byref(p), arr, n, base, out, beta, dt, int(learned),
                                             _stream(stream)))
 
+    def StageMesh(self, p: abi.Params, mesh, blocks, cons_base, cons_out, beta: float, dt: float, learned=False,
+                  batched=True, stream=None):
+        """One RK stage over a tiled mesh (phx_stage_mesh); mesh: a
+        phoebus_gb300.mesh.TiledMesh, blocks in its block order."""
+        from .block import _ptr
+
+        n = len(blocks)
+        arr = (abi.BlockS * n)(*[b.struct() for b in blocks])
+        base = (C.c_void_p * n)(*[_ptr(x) for x in cons_base])
+        out = (C.c_void_p * n)(*[_ptr(x) for x in cons_out])
+        m = mesh.struct()
+        self._ok(self.lib.phx_stage_mesh(self.h, C.byref(p), C.byref(m), arr, n, base, out, beta, dt, int(learned),
+                                         int(batched), _stream(stream)))
+
+    def MeshExchange(self, p: abi.Params, mesh, blocks, stream=None):
+        n = len(blocks)
+        arr = (abi.BlockS * n)(*[b.struct() for b in blocks])
+        m = mesh.struct()
+        self._ok(self.lib.phx_mesh_exchange(self.h, C.byref(p), C.byref(m), arr, n, _stream(stream)))
+
     def batch_info(self) -> dict:
         a, b, c = C.c_int(), C.c_int(), C.c_int()
         self._ok(self.lib.phx_batch_info(self.h, C.byref(a), C.byref(b), C.byref(c)))

@@ -64,7 +64,7 @@ def test_struct_sizes_match_header(built, tmp_path):
 
     src = tmp_path / "sz.c"
     fields = {"phx_params": abi.Params, "phx_block": abi.BlockS, "phx_geometry": abi.Geometry,
-              "phx_c2p_stats": abi.C2PStats, "phx_mlp_train_opts": abi.MlpTrainOpts}
+              "phx_c2p_stats": abi.C2PStats, "phx_mlp_train_opts": abi.MlpTrainOpts, "phx_mesh": abi.Mesh}
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void){"]
     for cname, cls in fields.items():
         lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
