@@ -21,6 +21,9 @@ RK2 timestep per second.
   batched    1024 uneven periodic blocks (edges 16/32/64, MP5 + HLL): RK2
              steps through phx_stage_batched (persistent work-list launches
              replayed as CUDA graphs) against the same steps block by block
+  torus      magnetised torus on a 384^3 FMKS mesh of uneven blocks: the plain
+             GPU step (block-by-block launches, reference con2prim start)
+             against the learned start + batched graphs
   c2p        con2prim over 5e7 independent FMKS Kerr-Schild zones at tolerance
              1e-10: zones/s and root-find iterations with the reference's
              start (plain) and with the learned start (network trained on
@@ -84,6 +87,9 @@ def parse():
     a.add_argument("--train-epochs", type=int, default=10)
     a.add_argument("--no-batched", action="store_true", help="skip the uneven-meshblock section")
     a.add_argument("--batched-blocks", type=int, default=1024)
+    a.add_argument("--no-torus", action="store_true", help="skip the torus section")
+    a.add_argument("--torus-n", type=int, default=384)
+    a.add_argument("--torus-steps", type=int, default=2)
     return a.parse_args()
 
 
@@ -357,6 +363,86 @@ def bench_batched(ctx, args, dev, learned_ready=False):
             "graph": "one CUDA graph per stage kind; nodes per graph as in tuning.graph_nodes"}
 
 
+def bench_torus(ctx, args, dev, learned_ready=False):
+    """Magnetised FM torus (r_in 6, r_max 12, Gamma 13/9, beta 100, 4%
+    pressure noise) on an n^3 FMKS Kerr-Schild mesh (a = 0.9375, X1 in
+    [ln 1.2, ln 250]) split into uneven blocks (edges 32..96 per axis),
+    WENO5-Z + HLL, ExpX1RhoSie floors, MHD floors, ceilings, c2p fixup,
+    outflow X1/X2, periodic X3.  RK2 steps: the plain GPU step (every phase
+    launched block by block, the reference's con2prim start) against the
+    learned start + batched persistent launches replayed as CUDA graphs."""
+    import torch
+
+    from phoebus_gb300 import learned, torus
+
+    p = torus.torus_params()
+    mesh = torus.torus_mesh(n=args.torus_n)
+    geo = torus.torus_geometry()
+    blocks = mesh.make_blocks(dev, geo)
+    info = torus.fill_torus(ctx, p, mesh, blocks)
+    ctx.check()
+    train_s = None
+    if learned_ready:  # a network for this equation of state (Gamma 13/9)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        learned.train(ctx, p, n=int(args.train_pairs), opts=__import__("phoebus_gb300").abi.default_train_opts(
+            epochs=args.train_epochs), device=dev)
+        torch.cuda.synchronize()
+        train_s = time.perf_counter() - t0
+    dt = 0.5 * min(ctx.EstimateTimestepBlock(p, b, False).item() for b in blocks)
+    seconds = [torch.zeros_like(b["cons"]) for b in blocks]
+    bases = [b["cons"] for b in blocks]
+    stage2 = []
+    from phoebus_gb300.block import Block
+
+    for b, s2 in zip(blocks, seconds):
+        c = Block(b.nx, b.ng, b.ndim, b.xmin, b.dx, backend="torch", device=dev, arrays=dict(b.arrays), geom=b.geom)
+        c.arrays["cons"] = s2
+        stage2.append(c)
+
+    def step(batched, lrn):
+        ctx.StageMesh(p, mesh, blocks, bases, seconds, 1.0, dt, learned=lrn, batched=batched)
+        ctx.StageMesh(p, mesh, stage2, bases, bases, 0.5, dt, learned=lrn, batched=batched)
+
+    zones = mesh.n[0] * mesh.n[1] * mesh.n[2]
+    runs = [("plain_per_block", False, False), ("batched", True, False)]
+    if learned_ready:
+        runs.append(("learned_batched", True, True))
+    stream = torch.cuda.current_stream()
+    res = {}
+    for name, batched, lrn in runs:
+        step(batched, lrn)  # plan build (work lists, autotune, capture) + warm-up
+        torch.cuda.synchronize()
+        ctx.c2p_stats(reset=True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.torus_steps):
+            step(batched, lrn)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.torus_steps
+        st = ctx.c2p_stats(reset=True)
+        res[name] = {"zone_updates_per_s": zones / (ms * 1e-3), "ms_per_step": ms, "steps": args.torus_steps,
+                     "c2p_iterations_per_zone": st["iterations"] / max(st["zones"], 1),
+                     "c2p_residual_evals_per_zone": st["residual_evals"] / max(st["zones"], 1),
+                     "c2p_failures": st["failures"]}
+        if lrn:
+            res[name]["c2p_learned_accepted_frac"] = st["learned_accepted"] / max(st["zones"], 1)
+    ctx.check()
+    nan = sum(int(torch.isnan(b["prim"][0][b.isl()]).sum()) for b in blocks)
+    out = {"workload": f"FM torus on a {args.torus_n}^3 FMKS Kerr-Schild mesh (a 0.9375), "
+                       f"{mesh.nblocks} uneven blocks, edges {mesh.lens}, WENO5-Z + HLL, Gamma 13/9, floors, "
+                       "outflow X1/X2, periodic X3", "interior_zones": zones, **res,
+           "nan_interior_rho": nan, "field_factor": info["field_factor"], "training_seconds": train_s}
+    if "learned_batched" in res:
+        out["learned_batched_over_plain"] = (res["learned_batched"]["zone_updates_per_s"] /
+                                             res["plain_per_block"]["zone_updates_per_s"])
+    out["batched_over_plain"] = res["batched"]["zone_updates_per_s"] / res["plain_per_block"]["zone_updates_per_s"]
+    del blocks, seconds, bases, stage2
+    torch.cuda.empty_cache()
+    return out
+
+
 def cpu_baseline(args, threads):
     """Oracle RK2 timestep on a cpu_n^3 sample of the workload."""
     import numpy as np
@@ -528,6 +614,7 @@ def main():
     ctx.check()
     c2p = None if args.no_c2p else bench_c2p(ctx, args, dev)
     batched = None if args.no_batched else bench_batched(ctx, args, dev, learned_ready=c2p is not None)
+    torus_res = None if args.no_torus else bench_torus(ctx, args, dev, learned_ready=not args.no_c2p)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
@@ -553,6 +640,7 @@ def main():
             "fp64": fp64,
             "c2p": c2p,
             "batched": batched,
+            "torus": torus_res,
             "cpu_baseline": cpu,
             "clocks": clocks,
             "e2e": e2e,
