@@ -672,12 +672,12 @@ struct RootFind {
   // root (f < 0 below the root, > 0 above it); one more evaluation at that
   // half's outer end checks the sign change.  Accepted: the same Illinois
   // iterations from that half.  Rejected: the reference's own start from
-  // [0, 1] refined by guess.
+  // [0, 1] refined by guess.  Only cold zones (guess = 0) try it.
   template <typename F>
   Real regula_falsi_learned(F &func, Real m, Real lo, Real hi, Real tol, Real guess, bool &bracketed,
                             bool &accepted) {
     accepted = false;
-    if (!(lo >= 0.0 && lo <= m && m <= hi && hi <= 1.0))  // not a usable bracket (e.g. NaN)
+    if (guess > 0.0 || !(lo >= 0.0 && lo <= m && m <= hi && hi <= 1.0))  // warm zone, or no usable bracket
       return regula_falsi(func, 0.0, 1.0, tol, guess, bracketed);
     Real a, b, ya, yb;
     const Real ym = func(m);

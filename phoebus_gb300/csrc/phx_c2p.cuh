@@ -211,8 +211,10 @@ struct RFState {
 // in [0, 1]; f(m) picks the half that should hold the root (f < 0 below it,
 // > 0 above), one more evaluation checks that half's sign change; when it
 // holds, the iterations start from that half, otherwise from the reference's
-// own start.  A bracket that is not ordered inside [0, 1] (e.g. NaN) is not
-// tried.
+// own start.  The learned start is only tried for a cold zone (guess = 0, no
+// previous solution): a previous mu is the better start (measured: about 1.5
+// iterations from it).  A bracket that is not ordered inside [0, 1] (e.g.
+// NaN) is not tried.
 template <bool LEARNED>
 __device__ __forceinline__ void rf_start(const Par &p, Residual &res, bool valid, double a, double b, double guess,
                                          const double *lb, RFState &s) {
@@ -222,7 +224,7 @@ __device__ __forceinline__ void rf_start(const Par &p, Residual &res, bool valid
   bool started = false;
   s.learned = false;
   if constexpr (LEARNED) {
-    if (valid && lb[1] >= 0.0 && lb[1] <= lb[0] && lb[0] <= lb[2] && lb[2] <= 1.0) {
+    if (valid && !(guess > 0.0) && lb[1] >= 0.0 && lb[1] <= lb[0] && lb[0] <= lb[2] && lb[2] <= 1.0) {
       double la, lbb, lya, lyb;
       const double ym = res(p, lb[0]);
       if (ym > 0.0) {

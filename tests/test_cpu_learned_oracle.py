@@ -104,3 +104,19 @@ def test_learned_root_find_good_and_bad_brackets(oracle, zones):
     nan = np.full((3, N), np.nan)
     pr3, _, _, evals3, acc3 = solve(oracle, zones, nan)
     assert acc3 == 0 and evals3 == pytest.approx(plain_evals) and np.array_equal(pr3, ref)
+
+
+def test_learned_start_only_for_cold_zones(oracle, zones):
+    """A zone with a previous solution (guess > 0) keeps the reference's
+    warm start even when a learned bracket is given."""
+    mu = zones["mu"]
+    good = np.ascontiguousarray(np.stack([mu, mu * np.exp(-1e-3), np.minimum(mu * np.exp(1e-3), 1.0)]))
+    guess = np.ascontiguousarray(mu * (1.0 + 1e-6))
+    pr = zones["prim"].copy()
+    fail = np.zeros(N)
+    oracle.ConservedToPrimitiveZones(params(), zones["cons"].copy(), pr, zones["geom"], fail=fail, guess=guess,
+                                     bracket=good)
+    assert oracle.last_accepted == 0
+    pr2 = zones["prim"].copy()
+    oracle.ConservedToPrimitiveZones(params(), zones["cons"].copy(), pr2, zones["geom"], fail=fail, guess=guess)
+    assert np.array_equal(pr, pr2)
