@@ -95,6 +95,7 @@ phx::Par make_par(const phx_params &p) {
   d.cfl = p.cfl;
   d.c2p_fixup = p.enable_c2p_fixup;
   d.strategy_floors = p.c2p_failure_strategy_floors;
+  d.vsq_max = 1.0 - 1.0 / (d.g0 * d.g0);
   return d;
 }
 

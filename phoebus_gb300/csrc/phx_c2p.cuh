@@ -72,15 +72,43 @@ struct Residual {
     }
     return ehat_trial;
   }
+  // ehat_mu with the density from a known 1/W (production build)
+  __device__ __forceinline__ double ehat_mu_iw(const Par &p, double mu, double qbar, double rbarsq, double vhatsq,
+                                               double What, double iWhat) {
+    double rho = rhohat_mu(iWhat);
+    double e_floor;
+    get_floors(p, x1, x2, x3, rho, e_floor);
+    e_floor *= p.fsf;
+    const double ehat_trial = What * (qbar - mu * rbarsq) + vhatsq * What * ratio_p(What, 1.0 + What);
+    used_energy_floor = false;
+    used_energy_max = false;
+    if (ehat_trial <= e_floor) {
+      used_energy_floor = true;
+      return e_floor;
+    } else if (ehat_trial > e_max) {
+      used_energy_max = true;
+      return e_max;
+    }
+    return ehat_trial;
+  }
   __device__ __forceinline__ double operator()(const Par &p, double mu) {
     const double x = x_mu(mu);
     const double rbarsq = rbarsq_mu(mu, x);
     const double qbar = qbar_mu(mu, x);
     const double vhatsq = vhatsq_mu(mu, rbarsq);
+#ifdef PHX_EXACT
     const double iWhat = iWhat_mu(vhatsq);
     const double What = ratio_p(1.0, iWhat);
     const double rhohat = rhohat_mu(iWhat);
     const double ehat = ehat_mu(p, mu, qbar, rbarsq, vhatsq, What);
+#else
+    // production build: W and 1/W from one rsqrt; the density inside ehat
+    // reuses 1/W instead of inverting W again
+    const double What = rsqrt_p(1.0 - vhatsq);
+    const double iWhat = (1.0 - vhatsq) * What;
+    const double rhohat = rhohat_mu(iWhat);
+    const double ehat = ehat_mu_iw(p, mu, qbar, rbarsq, vhatsq, What, iWhat);
+#endif
     const double Phat = eos_P_rho_sie(p, rhohat, ehat);
     const double hhat = rhohat * (1.0 + ehat) + Phat;
     const double ahat = div_p(Phat, make_positive(hhat - Phat));

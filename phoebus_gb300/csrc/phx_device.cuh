@@ -62,6 +62,25 @@ __device__ __forceinline__ double div_p(double a, double b) {
   return a * rcp_p(b);
 #endif
 }
+// 1/sqrt(x) from the hardware seed and two Newton steps y <- y (3 - x y^2)/2
+// (normal, finite x > 0); the production build's replacement for
+// 1 / sqrt(x), the exact build divides.
+__device__ __forceinline__ double rsqrt_nr(double x) {
+  double y;
+  asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  double h = x * y * y;
+  y = y * fma(-0.5, h, 1.5);
+  h = x * y * y;
+  return y * fma(-0.5, h, 1.5);
+}
+__device__ __forceinline__ double rsqrt_p(double x) {
+#ifdef PHX_EXACT
+  return 1.0 / sqrt(x);
+#else
+  const int e = dexp(x);
+  return (e >= 16 && e <= 2030) ? rsqrt_nr(x) : 1.0 / sqrt(x);
+#endif
+}
 // robust::ratio with the production-build reciprocal
 __device__ __forceinline__ double ratio_p(double a, double b) {
 #ifdef PHX_EXACT
@@ -90,6 +109,7 @@ struct Par {
   int recon, riemann;
   double cfl;
   int c2p_fixup, strategy_floors, enable_floors, enable_mhd_floors;
+  double vsq_max;  // 1 - 1 / g0^2 (the gamma ceiling as a v^2 bound)
 };
 
 // ------------------------------------------------ singularity-eos IdealGas
@@ -542,7 +562,13 @@ __device__ __forceinline__ void prim_to_flux(const Par &par, const Face &f, cons
   get_floors(par, f.X1, f.X2, f.X3, rho_floor, sie_floor);
   const double rho = fmax(q[PHX_PRHO], rho_floor);
   double vpcon[3] = {q[PHX_PVEL], q[PHX_PVEL + 1], q[PHX_PVEL + 2]};
+#ifdef PHX_EXACT
   double W = lorentz<MINK>(g, vpcon);
+#else
+  const double Wsq0 = 1. + dot_sp<MINK>(g, vpcon, vpcon);
+  const double iW0 = rsqrt_p(Wsq0);
+  double W = Wsq0 * iW0;
+#endif
   if (W > gam_max) {
     const double rescale = sqrt((gam_max * gam_max - 1.) / (W * W - 1.));
 #pragma unroll
@@ -550,13 +576,14 @@ __device__ __forceinline__ void prim_to_flux(const Par &par, const Face &f, cons
   }
 #ifdef PHX_EXACT
   double vcon[3] = {vpcon[0] / W, vpcon[1] / W, vpcon[2] / W};
+  const double sie_q = q[PHX_PENG] / rho;
 #else
-  const double iW0 = 1.0 / W;
   double vcon[3] = {vpcon[0] * iW0, vpcon[1] * iW0, vpcon[2] * iW0};
+  const double sie_q = q[PHX_PENG] * rcp_p(rho);
 #endif
   double Bcon[3] = {0.0, 0.0, 0.0};
   const double qe = q[PHX_PENG];
-  const double u = (qe / rho > sie_floor ? (qe / rho > sie_max ? rho * sie_max : qe) : rho * sie_floor);
+  const double u = (sie_q > sie_floor ? (sie_q > sie_max ? rho * sie_max : qe) : rho * sie_floor);
   const double P = fmax(q[PHX_PPRS], 0.0);
   const double gamma1 = q[PHX_PGM1];
   if (par.mhd) {
@@ -582,7 +609,11 @@ __device__ __forceinline__ void prim_to_flux(const Par &par, const Face &f, cons
         BdotB += g.gcov[m + 1][n + 1] * Bcon[m] * Bcon[n];
       }
   }
+#ifdef PHX_EXACT
   const double vsq_max = 1.0 - 1.0 / (gam_max * gam_max);
+#else
+  const double vsq_max = par.vsq_max;  // 1 - 1 / gam_max^2, formed on the host
+#endif
   if (vsq > vsq_max) {
     double scale = vsq_max / vsq;
     vsq *= scale;
@@ -596,16 +627,22 @@ __device__ __forceinline__ void prim_to_flux(const Par &par, const Face &f, cons
 #else
   // production build: W = 1/s with s = sqrt(1 - v^2); divisions by W and W^2
   // become products with s and s^2
-  const double sW = sqrt(1 - vsq);
-  W = 1.0 / sW;
+  W = rsqrt_p(1 - vsq);
+  const double sW = (1 - vsq) * W;
 #endif
   const double vel = vcon[DIR];
   const double alpha = MINK ? 1.0 : g.alpha;
+#ifdef PHX_EXACT
+#define PHX_BOA(m) (g.beta[m] / alpha)
+#else
+  const double ialpha = MINK ? 1.0 : rcp_p(alpha);
+#define PHX_BOA(m) (g.beta[m] * ialpha)
+#endif
   double vtil;
   if constexpr (MINK)
     vtil = vel;
   else
-    vtil = vel - g.beta[DIR] / alpha;
+    vtil = vel - PHX_BOA(DIR);
   U[PHX_CRHO] = rho * W;
   F[PHX_CRHO] = U[PHX_CRHO] * vtil;
   const double b0 = W * Bdotv;
@@ -630,11 +667,15 @@ __device__ __forceinline__ void prim_to_flux(const Par &par, const Face &f, cons
       bcovm = PHX_DIV_W(Bcon[m]) + b0 * vcon[m];
       vcovm = vcon[m];
     } else {
+#ifdef PHX_EXACT
       bcovm = g.gcov[m + 1][0] * b0 / alpha;
+#else
+      bcovm = g.gcov[m + 1][0] * b0 * ialpha;
+#endif
       vcovm = 0.0;
 #pragma unroll
       for (int n = 1; n < 4; n++) {
-        bcovm += g.gcov[m + 1][n] * (PHX_DIV_W(Bcon[n - 1]) + b0 * (vcon[n - 1] - g.beta[n - 1] / alpha));
+        bcovm += g.gcov[m + 1][n] * (PHX_DIV_W(Bcon[n - 1]) + b0 * (vcon[n - 1] - PHX_BOA(n - 1)));
         vcovm += g.gcov[m + 1][n] * vcon[n - 1];
       }
     }
@@ -650,12 +691,18 @@ __device__ __forceinline__ void prim_to_flux(const Par &par, const Face &f, cons
     if constexpr (MINK)
       F[PHX_CB + m] = U[PHX_CB + m] * vtil - Bcon[DIR] * vcon[m];
     else
-      F[PHX_CB + m] = U[PHX_CB + m] * vtil - Bcon[DIR] * (vcon[m] - g.beta[m] / alpha);
+      F[PHX_CB + m] = U[PHX_CB + m] * vtil - Bcon[DIR] * (vcon[m] - PHX_BOA(m));
   }
+#undef PHX_BOA
+#ifdef PHX_EXACT
   const double vasq = bsqWsq / make_positive(rhohWsq + bsqWsq);
   const double cssq = make_bounded(gamma1 * P * W * W / make_positive(rhohWsq), 0.0, 1.0);
+#else
+  const double vasq = bsqWsq * rcp_p(make_positive(rhohWsq + bsqWsq));
+  const double cssq = make_bounded(gamma1 * P * W * W * rcp_p(make_positive(rhohWsq)), 0.0, 1.0);
+#endif
   const double cmsq = make_bounded(cssq + vasq * (1.0 - cssq), 0.0, 1.0);
-  const double vcoff = alpha / (1.0 - vsq * cmsq);
+  const double vcoff = div_p(alpha, 1.0 - vsq * cmsq);
   const double v0 = vel * (1.0 - cmsq);
   const double gdd = MINK ? 1.0 : f.gdd;
   const double vpm = sqrt(make_positive(cmsq * (1.0 - vsq) * (gdd * (1.0 - vsq * cmsq) - vel * v0)));
