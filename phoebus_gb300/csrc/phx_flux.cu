@@ -67,6 +67,12 @@ __device__ __forceinline__ void face_flux(const Par &p, const BView &b, int k, i
 }
 
 // ------------------------------------------------------------------ X1
+// Resident CTAs per SM the register allocation of the sweep kernels is
+// bounded for (launch bounds); 1 leaves the compiler free (no spills).
+#ifndef PHX_SWEEP_MINB
+#define PHX_SWEEP_MINB 1
+#endif
+
 constexpr int X1_WARPS = 4;    // warps per CTA
 constexpr int X1_PENCILS = 4;  // (k, j) pencils staged per CTA
 
@@ -287,7 +293,7 @@ __device__ __forceinline__ void sweep_at(const Par &p, const BView &b, int alo, 
 }
 
 template <int RECON, bool MINK, int DIR>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, PHX_SWEEP_MINB)
     k_flux_sweep(Par p, BView b, int alo, int na, int clo, int nc, int f0, int nface, int seg, int nseg) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < (long long)na * nc * nseg) sweep_at<RECON, MINK, DIR>(p, b, alo, na, clo, nc, f0, nface, seg, nseg, t);
@@ -324,7 +330,7 @@ __host__ __device__ __forceinline__ SweepRange sweep_range(const BView &b, int d
 }
 
 template <int RECON, bool MINK, int DIR>
-__global__ void __launch_bounds__(128) kb_flux_sweep(Par p, const BView *views, const WorkItem *items, int nitems,
+__global__ void __launch_bounds__(128, PHX_SWEEP_MINB) kb_flux_sweep(Par p, const BView *views, const WorkItem *items, int nitems,
                                                      int seg_target) {
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const WorkItem w = items[it];
