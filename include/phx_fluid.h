@@ -123,6 +123,10 @@ typedef struct {
   double rho0_floor, sie0_floor, rho_exp_floor, sie_exp_floor;
   double gam0_ceiling, sie0_ceiling;         /* ConstantGamSie ceilings */
   double bsqorho0_ceiling, bsqou0_ceiling;   /* ConstantBsqRat ceilings */
+  /* physical-boundary fixups of a tiled mesh (fixup.cpp:56-60; both off by
+   * default, both on in the torus deck) */
+  int enable_flux_fixup;            /* FixFluxes after FluxCT                 */
+  int enable_ox1_fmks_inflow_check; /* u^1 >= 0 in outer-X1 ghosts (FMKS)     */
 } phx_params;
 
 /* Geometry.  Minkowski is constant-folded into the kernels.  FMKS
@@ -365,10 +369,19 @@ phx_status phx_stage_batched(phx_ctx *ctx, const phx_params *p, const phx_block 
 /* A domain tiled by blocks as a tensor product of per-axis segments, for
  * phx_stage_mesh.  Block (s1, s2, s3) (segment indices) is blocks[(s3 *
  * nseg[1] + s2) * nseg[0] + s1]; its interior covers global cells
- * seg_start[d][s_d] .. seg_start[d][s_d + 1] - 1 on axis d. */
+ * seg_start[d][s_d] .. seg_start[d][s_d + 1] - 1 on axis d.
+ * Physical boundaries (phoebus_boundaries.cpp; bc_vars = primitive, the
+ * torus deck's choice) fill a ghost from the cell that the rule maps it to:
+ *   PHX_BC_OUTFLOW  gr_outflow: the boundary cell (OutflowInnerX1 & co.)
+ *   PHX_BC_REFLECT  the mirror cell, vector components along the axis
+ *                   negated (GenericBC<..., Reflect>)
+ *   PHX_BC_POLAR    X2 faces only: the mirror cell, v^2 and B^2 negated
+ *                   (PolarInnerX2 / PolarOuterX2)
+ * Periodic axes must be periodic on both faces (Parthenon's rule). */
 #define PHX_BC_PERIODIC 0
-#define PHX_BC_OUTFLOW 1 /* gr_outflow: copy the boundary cell's primitives,
-                            the normal velocity set to 0 where it points in */
+#define PHX_BC_OUTFLOW 1
+#define PHX_BC_REFLECT 2
+#define PHX_BC_POLAR 3
 typedef struct {
   int n[3];                  /* global interior cells per axis            */
   int nseg[3];               /* segments (blocks) per axis                */
@@ -376,23 +389,51 @@ typedef struct {
   int bc_lo[3], bc_hi[3];    /* PHX_BC_* of each face                      */
 } phx_mesh;
 
-/* The stage of phx_stage over a tiled mesh: the ghost exchange copies the
- * primitives of the owning block's cell (bc_vars = primitive, as the torus
- * deck) or applies the physical boundary, then rebuilds the ghost's conserved
- * variables with its own metric (prim2con).  batched = 1: one persistent
- * launch per phase replayed as a CUDA graph (as phx_stage_batched);
- * batched = 0: the same kernels launched block by block (the launch
- * structure of per-block tasks).  Plans are built and cached as in
- * phx_stage_batched. */
+/* The stage of phx_stage over a tiled mesh, in the reference's task order:
+ * sources, fluxes, FluxCT, FixFluxes (p->enable_flux_fixup), update, then
+ * twice con2prim + c2p fixup + floors with the boundary exchange between the
+ * two passes.  The exchange is phx_mesh_exchange's.  batched = 1: one
+ * persistent launch per phase replayed as a CUDA graph (as
+ * phx_stage_batched); batched = 0: the same kernels launched block by block
+ * (the launch structure of per-block tasks).  Plans are built and cached as
+ * in phx_stage_batched. */
 phx_status phx_stage_mesh(phx_ctx *ctx, const phx_params *p, const phx_mesh *mesh, const phx_block *blocks,
                           int nblocks, const double *const *cons_base, double *const *cons_out, double beta,
                           double dt, int use_learned_guess, int batched, void *stream);
 
-/* Fill every ghost zone of a tiled mesh (primitives from the owners or the
- * physical boundaries, conserved variables by prim2con) -- the mesh's
- * boundary exchange on its own, e.g. after initialisation. */
+/* The boundary exchange of a tiled mesh with bc_vars = primitive
+ * (phoebus_driver.cpp:646-668: AddBoundaryExchangeTasks,
+ * ApplyBoundaryConditions, ConvertBoundaryConditions).  A ghost whose cell
+ * lies inside the domain, across a block face or a periodic wrap, receives the
+ * owning block's primitives and conserved variables.  A ghost in a physical
+ * boundary slab receives the primitives of the cell its boundary rule maps it
+ * to (the rules of all axes composed, as the face-by-face application in
+ * X1, X2, X3 order leaves them), then, with p->enable_ox1_fmks_inflow_check
+ * on an FMKS mesh, the outer-X1 inflow check
+ * (phoebus_boundaries.cpp:366-397), then prim2con with its own metric
+ * (PrimitiveToConservedRegion, conserved variables and cell signal speeds). */
 phx_status phx_mesh_exchange(phx_ctx *ctx, const phx_params *p, const phx_mesh *mesh, const phx_block *blocks,
                              int nblocks, void *stream);
+
+/* fixup::FixFluxes (fixup.cpp:728-1078) on every block of a tiled mesh
+ * that touches a physical boundary, in place on the blocks' flux arrays; a
+ * no-op unless p->enable_flux_fixup.  Boundary faces only:
+ *   gr_outflow  the density flux may only leave: min(F, 0) on lower faces,
+ *               max(F, 0) on upper faces;
+ *   reflect     density and energy fluxes 0 (X2 faces also S_1 and S_3);
+ *   polar       X2 fluxes of density, energy, momentum and B set to 0, and the
+ *               X1 and X3 fluxes of B^2 in the ghost row outside the pole
+ *               set to minus those of the row inside. */
+phx_status phx_fix_fluxes(phx_ctx *ctx, const phx_params *p, const phx_mesh *mesh, const phx_block *blocks,
+                          int nblocks, void *stream);
+
+/* FixFluxes as the reference's per-block task: bc_lo[d] / bc_hi[d] give the
+ * boundary kind of the block's lower / upper face on axis d
+ * (PHX_BC_OUTFLOW, PHX_BC_REFLECT, PHX_BC_POLAR on a physical boundary;
+ * PHX_BC_PERIODIC for a face with a neighbouring block or a periodic wrap).
+ * A no-op unless p->enable_flux_fixup. */
+phx_status phx_fix_fluxes_block(phx_ctx *ctx, const phx_params *p, const phx_block *b, const int bc_lo[3],
+                                const int bc_hi[3], void *stream);
 
 /* Tile shapes and graph size of the most recent batched plan (0 if none). */
 phx_status phx_batch_info(phx_ctx *ctx, int *x1_cells, int *sweep_seg, int *graph_nodes);

@@ -14,6 +14,7 @@
 //                                              MeshData<Real> *)        fluid.cpp:566
 //   TaskStatus fluid::CalculateFluxes(MeshBlockData<Real> *)             fluid.cpp:659
 //   TaskStatus fluid::FluxCT(MeshBlockData<Real> *)                      fluid.cpp:775
+//   TaskStatus fixup::FixFluxes(MeshBlockData<Real> *)                   fixup.cpp:728
 //   Real fluid::EstimateTimestepBlock(MeshBlockData<Real> *)             fluid.cpp:899
 //   template <T> using fluid::c2p_type = TaskStatus (*)(T *, ...)        fluid.hpp:65
 //
@@ -84,10 +85,23 @@ class MeshBlockData<Real> {
     if (b_.ndim < 3) return IndexRange{0, 0};
     return d == IndexDomain::entire ? IndexRange{0, b_.nx3 + 2 * b_.ng - 1} : IndexRange{b_.ng, b_.ng + b_.nx3 - 1};
   }
+  // pmb->boundary_flag with the phoebus BC name of each face folded in:
+  // PHX_BC_OUTFLOW / REFLECT / POLAR on a physical ("user") boundary,
+  // PHX_BC_PERIODIC where the block has a neighbour.
+  void SetBoundaries(const int lo[3], const int hi[3]) {
+    for (int d = 0; d < 3; d++) {
+      bc_lo_[d] = lo[d];
+      bc_hi_[d] = hi[d];
+    }
+  }
+  const int *BoundaryLo() const { return bc_lo_; }
+  const int *BoundaryHi() const { return bc_hi_; }
 
  private:
   Mesh *mesh_;
   phx_block b_;
+  int bc_lo_[3] = {PHX_BC_PERIODIC, PHX_BC_PERIODIC, PHX_BC_PERIODIC};
+  int bc_hi_[3] = {PHX_BC_PERIODIC, PHX_BC_PERIODIC, PHX_BC_PERIODIC};
 };
 
 // A pack of blocks (a MeshData partition).
@@ -246,5 +260,22 @@ inline Real EstimateTimestepBlock(MeshBlockData<Real> *rc) {
 }
 
 }  // namespace fluid
+
+namespace fixup {
+using parthenon::MeshBlockData;
+using parthenon::Real;
+using parthenon::TaskStatus;
+
+// fixup::FixFluxes (fixup.cpp:728): returns at once unless
+// fixup/enable_flux_fixup (Mesh::params.enable_flux_fixup).
+inline TaskStatus FixFluxes(MeshBlockData<Real> *rc) {
+  parthenon::Mesh *m = rc->GetMeshPointer();
+  if (!m->params.enable_flux_fixup) return TaskStatus::complete;
+  fluid::detail::check(
+      phx_fix_fluxes_block(m->ctx, &m->params, &rc->Block(), rc->BoundaryLo(), rc->BoundaryHi(), m->stream),
+      "FixFluxes");
+  return TaskStatus::complete;
+}
+}  // namespace fixup
 
 #endif  // PHX_PARTHENON_SHIM_HPP_

@@ -50,6 +50,7 @@ class Params(C.Structure):
         ("rho0_floor", C.c_double), ("sie0_floor", C.c_double), ("rho_exp_floor", C.c_double),
         ("sie_exp_floor", C.c_double), ("gam0_ceiling", C.c_double), ("sie0_ceiling", C.c_double),
         ("bsqorho0_ceiling", C.c_double), ("bsqou0_ceiling", C.c_double),
+        ("enable_flux_fixup", C.c_int), ("enable_ox1_fmks_inflow_check", C.c_int),
     ]
 
 
@@ -85,7 +86,7 @@ class Mesh(C.Structure):
                 ("bc_hi", C.c_int * 3)]
 
 
-BC_PERIODIC, BC_OUTFLOW = 0, 1
+BC_PERIODIC, BC_OUTFLOW, BC_REFLECT, BC_POLAR = 0, 1, 2, 3
 
 
 class MlpTrainOpts(C.Structure):
@@ -153,6 +154,9 @@ _SIGS = {
     "phx_stage_mesh": (C.c_int, [_P, C.POINTER(Params), C.POINTER(Mesh), C.POINTER(BlockS), C.c_int, _P, _P,
                                  C.c_double, C.c_double, C.c_int, C.c_int, _P]),
     "phx_mesh_exchange": (C.c_int, [_P, C.POINTER(Params), C.POINTER(Mesh), C.POINTER(BlockS), C.c_int, _P]),
+    "phx_fix_fluxes": (C.c_int, [_P, C.POINTER(Params), C.POINTER(Mesh), C.POINTER(BlockS), C.c_int, _P]),
+    "phx_fix_fluxes_block": (C.c_int, [_P, C.POINTER(Params), C.POINTER(BlockS), C.POINTER(C.c_int),
+                                       C.POINTER(C.c_int), _P]),
     "phx_batch_info": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "phx_mlp_set_weights": (C.c_int, [_P, C.POINTER(C.c_float)]),
     "phx_mlp_get_weights": (C.c_int, [_P, C.POINTER(C.c_float)]),

@@ -96,6 +96,8 @@ phx::Par make_par(const phx_params &p) {
   d.c2p_fixup = p.enable_c2p_fixup;
   d.strategy_floors = p.c2p_failure_strategy_floors;
   d.vsq_max = 1.0 - 1.0 / (d.g0 * d.g0);
+  d.fix_flux = p.enable_flux_fixup ? 1 : 0;
+  d.inflow_check = p.enable_ox1_fmks_inflow_check ? 1 : 0;
   return d;
 }
 
@@ -607,7 +609,7 @@ phx_status phx_stage_batched(phx_ctx *ctx, const phx_params *p, const phx_block 
   }
   const char *why = nullptr;
   cudaError_t e = phx::batch_stage(ctx->batch, make_par(*p), blocks, views.data(), nblocks, cons_base, cons_out, beta,
-                                   dt, use_learned_guess ? ctx->mlp_packed : nullptr, nullptr, true, false,
+                                   dt, use_learned_guess ? ctx->mlp_packed : nullptr, nullptr, true, phx::BATCH_STAGE,
                                    ctx->stats, ctx->err, S(stream), &why);
   if (e != cudaSuccess) return fail(PHX_ERR_CUDA, "phx_stage_batched: %s", cudaGetErrorString(e));
   return cuda_status("phx_stage_batched");
@@ -624,9 +626,12 @@ static phx_status check_mesh(const phx_mesh *m, const phx_block *blocks, int nbl
       return fail(PHX_ERR_INVALID_ARG, "mesh axis %d: segments must cover [0, n)", d);
     for (int k = 0; k < m->nseg[d]; k++)
       if (m->seg_start[d][k + 1] <= m->seg_start[d][k]) return fail(PHX_ERR_INVALID_ARG, "empty segment");
-    if ((m->bc_lo[d] != PHX_BC_PERIODIC && m->bc_lo[d] != PHX_BC_OUTFLOW) ||
-        (m->bc_hi[d] != PHX_BC_PERIODIC && m->bc_hi[d] != PHX_BC_OUTFLOW))
-      return fail(PHX_ERR_INVALID_ARG, "unknown boundary condition");
+    for (int bc : {m->bc_lo[d], m->bc_hi[d]}) {
+      if (bc < PHX_BC_PERIODIC || bc > PHX_BC_POLAR) return fail(PHX_ERR_INVALID_ARG, "unknown boundary condition");
+      if (bc == PHX_BC_POLAR && d != 1) return fail(PHX_ERR_INVALID_ARG, "polar boundaries are X2 faces only");
+    }
+    if ((m->bc_lo[d] == PHX_BC_PERIODIC) != (m->bc_hi[d] == PHX_BC_PERIODIC))
+      return fail(PHX_ERR_INVALID_ARG, "mesh axis %d: periodic on one face only", d);
     nb *= m->nseg[d];
   }
   if (nb != nblocks) return fail(PHX_ERR_INVALID_ARG, "mesh has %lld blocks, %d given", nb, nblocks);
@@ -644,6 +649,9 @@ static phx_status check_mesh(const phx_mesh *m, const phx_block *blocks, int nbl
           return fail(PHX_ERR_INVALID_ARG, "block %d extents differ from its mesh segments", b);
         if (B.nx1 < B.ng || B.nx2 < B.ng || B.nx3 < B.ng)
           return fail(PHX_ERR_INVALID_ARG, "block %d: ghost exchange needs nx >= ng", b);
+        for (int d = 0; d < 3; d++)  // a mirror maps ng ghosts onto ng cells of the domain
+          if ((m->bc_lo[d] >= PHX_BC_REFLECT || m->bc_hi[d] >= PHX_BC_REFLECT) && m->n[d] < B.ng)
+            return fail(PHX_ERR_INVALID_ARG, "mesh axis %d: a mirror boundary needs n >= ng", d);
         if (views[b].fmks != views[0].fmks) return fail(PHX_ERR_INVALID_ARG, "blocks must share the geometry kind");
       }
   return PHX_OK;
@@ -667,7 +675,7 @@ phx_status phx_stage_mesh(phx_ctx *ctx, const phx_params *p, const phx_mesh *mes
   }
   const char *why = nullptr;
   cudaError_t e = phx::batch_stage(ctx->batch, make_par(*p), blocks, views.data(), nblocks, cons_base, cons_out, beta,
-                                   dt, use_learned_guess ? ctx->mlp_packed : nullptr, mesh, batched != 0, false,
+                                   dt, use_learned_guess ? ctx->mlp_packed : nullptr, mesh, batched != 0, phx::BATCH_STAGE,
                                    ctx->stats, ctx->err, S(stream), &why);
   if (e != cudaSuccess) return fail(PHX_ERR_CUDA, "phx_stage_mesh: %s", cudaGetErrorString(e));
   return cuda_status("phx_stage_mesh");
@@ -689,9 +697,50 @@ phx_status phx_mesh_exchange(phx_ctx *ctx, const phx_params *p, const phx_mesh *
   }
   const char *why = nullptr;
   cudaError_t e = phx::batch_stage(ctx->batch, make_par(*p), blocks, views.data(), nblocks, base.data(), out.data(),
-                                   0.0, 0.0, nullptr, mesh, true, true, ctx->stats, ctx->err, S(stream), &why);
+                                   0.0, 0.0, nullptr, mesh, true, phx::BATCH_EXCHANGE, ctx->stats, ctx->err,
+                                   S(stream), &why);
   if (e != cudaSuccess) return fail(PHX_ERR_CUDA, "phx_mesh_exchange: %s", cudaGetErrorString(e));
   return cuda_status("phx_mesh_exchange");
+}
+
+phx_status phx_fix_fluxes(phx_ctx *ctx, const phx_params *p, const phx_mesh *mesh, const phx_block *blocks,
+                          int nblocks, void *stream) {
+  phx_status s;
+  if ((s = ctx_device(ctx)) || (s = check_params(p))) return s;
+  std::vector<phx::BView> views;
+  if ((s = check_mesh(mesh, blocks, nblocks, views))) return s;
+  for (int n = 0; n < nblocks; n++)
+    if (!blocks[n].flux) return fail(PHX_ERR_INVALID_ARG, "block %d: flux is NULL", n);
+  if (!p->enable_flux_fixup) return PHX_OK;
+  std::vector<const double *> base(nblocks);
+  std::vector<double *> out(nblocks);
+  for (int n = 0; n < nblocks; n++) {
+    base[n] = blocks[n].cons;
+    out[n] = blocks[n].cons;
+  }
+  const char *why = nullptr;
+  cudaError_t e = phx::batch_stage(ctx->batch, make_par(*p), blocks, views.data(), nblocks, base.data(), out.data(),
+                                   0.0, 0.0, nullptr, mesh, true, phx::BATCH_FIXFLUX, ctx->stats, ctx->err,
+                                   S(stream), &why);
+  if (e != cudaSuccess) return fail(PHX_ERR_CUDA, "phx_fix_fluxes: %s", cudaGetErrorString(e));
+  return cuda_status("phx_fix_fluxes");
+}
+
+phx_status phx_fix_fluxes_block(phx_ctx *ctx, const phx_params *p, const phx_block *b, const int bc_lo[3],
+                                const int bc_hi[3], void *stream) {
+  phx_status s;
+  if ((s = ctx_device(ctx)) || (s = check_params(p))) return s;
+  phx::BView v;
+  if ((s = make_view(b, v))) return s;
+  if (!b->flux || !bc_lo || !bc_hi) return fail(PHX_ERR_INVALID_ARG, "flux/bc_lo/bc_hi is NULL");
+  for (int d = 0; d < 3; d++)
+    for (int bc : {bc_lo[d], bc_hi[d]}) {
+      if (bc < PHX_BC_PERIODIC || bc > PHX_BC_POLAR) return fail(PHX_ERR_INVALID_ARG, "unknown boundary condition");
+      if (bc == PHX_BC_POLAR && d != 1) return fail(PHX_ERR_INVALID_ARG, "polar boundaries are X2 faces only");
+    }
+  if (!p->enable_flux_fixup) return PHX_OK;
+  phx::launch_fix_fluxes_block(make_par(*p), v, bc_lo, bc_hi, S(stream));
+  return cuda_status("phx_fix_fluxes_block");
 }
 
 phx_status phx_batch_info(phx_ctx *ctx, int *x1_cells, int *sweep_seg, int *graph_nodes) {

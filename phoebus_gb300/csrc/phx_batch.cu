@@ -99,7 +99,7 @@ struct BatchPlan {
   double **out_tab = nullptr;
   double *beta_dt = nullptr;
   std::vector<void *> item_mem;  // work-list allocations
-  PhaseList sources, x1, x2, x3, fluxct, update, ghost, c2p;
+  PhaseList sources, x1, x2, x3, fluxct, fixflux, update, ghost, c2p;
   size_t x1_smem = 0;
   Tuning tune;
   bool mink = true;
@@ -112,6 +112,8 @@ struct BatchPlan {
   std::vector<int> mesh_seg[3];    // host copy of the segment starts
   MeshDev md{};
   void *mesh_mem = nullptr;
+  std::vector<BView> vin;          // host copy of views_in
+  bool staged = false;             // tuned, flux lists built, graph captured
   cudaGraphExec_t exec = nullptr;
   cudaGraph_t graph = nullptr;
   ~BatchPlan() {
@@ -234,7 +236,7 @@ static Tuning autotune(BatchPlan &pl, const std::vector<BView> &v, unsigned int 
 // over all items (captured into the plan's graph).  Per block: phase by phase,
 // each block's items in a launch of its own (one item per CTA).
 static void stage_launches(BatchPlan &pl, DevStats *stats, unsigned int *err, cudaStream_t s,
-                           bool exchange_only = false) {
+                           int only = BATCH_STAGE) {
   const Par &p = pl.par;
   const int nb = (int)pl.blocks.size();
   // run fn(items, count, grid) for all items, or block by block
@@ -258,8 +260,18 @@ static void stage_launches(BatchPlan &pl, DevStats *stats, unsigned int *err, cu
         launch_ghost_batched(pl.views_out, p.mhd ? PHX_NCONS : 5, it, n, g, s);
       });
   };
-  if (exchange_only) {
+  auto fix_fluxes = [&] {
+    if (pl.has_mesh && p.fix_flux)
+      each(pl.fixflux, [&](const WorkItem *it, int n, int g) {
+        launch_fix_fluxes(p, pl.views_in, pl.md, it, n, g, s);
+      });
+  };
+  if (only == BATCH_EXCHANGE) {
     exchange();
+    return;
+  }
+  if (only == BATCH_FIXFLUX) {
+    fix_fluxes();
     return;
   }
   each(pl.sources, [&](const WorkItem *it, int n, int g) { launch_sources_batched(p, pl.mink, pl.views_in, it, n, g, s); });
@@ -276,6 +288,7 @@ static void stage_launches(BatchPlan &pl, DevStats *stats, unsigned int *err, cu
     });
   if (p.mhd && pl.ndim > 1)
     each(pl.fluxct, [&](const WorkItem *it, int n, int g) { launch_fluxct_batched(pl.ndim, pl.views_in, it, n, g, s); });
+  fix_fluxes();
   each(pl.update, [&](const WorkItem *it, int n, int g) {
     launch_update_batched(p, pl.views_in, pl.base_tab, pl.out_tab, pl.beta_dt, it, n, g, s);
   });
@@ -387,11 +400,56 @@ static bool same_plan(const BatchPlan &pl, const phx_block *blocks, int n, const
   return true;
 }
 
+// Tile shapes (tuned on the plan's own blocks: the flux arrays are
+// overwritten), flux work lists and the captured graph of the stage.  A plan
+// first built for the exchange or FixFluxes alone gets these at its first
+// stage.
+static cudaError_t prepare_stage(BatchPlan &P, DevStats *stats, unsigned int *err, cudaStream_t s) {
+  cudaError_t e;
+  const Par &par = P.par;
+  const std::vector<BView> &vin = P.vin;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    load_tune_file();
+    const std::string key = tune_key(par, vin, P.mink);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      P.tune = it->second;
+    } else {
+      P.tune = autotune(P, vin, err, s);
+      g_tune[key] = P.tune;
+      save_tune_file();
+    }
+  }
+  if ((e = upload_items(P, P.x1, x1_items(vin, P.tune.x1_cells, P.x1_smem))) != cudaSuccess) return e;
+  for (int dir = 1; dir <= 2; dir++) {
+    std::vector<long long> counts;
+    for (const BView &b : vin) counts.push_back(dir < P.ndim ? sweep_threads(b, dir, P.tune.seg) : 0);
+    if ((e = upload_items(P, dir == 1 ? P.x2 : P.x3, make_items(counts, 128))) != cudaSuccess) return e;
+  }
+  prepare_flux_x1_batched(par, P.mink, P.x1_smem);  // kernel attributes are set outside the capture
+  if ((e = cudaDeviceSynchronize()) != cudaSuccess) return e;
+  if (P.batched) {  // capture the stage
+    cudaStream_t cs;
+    if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) return e;
+    e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      stage_launches(P, stats, err, cs);
+      e = cudaStreamEndCapture(cs, &P.graph);
+    }
+    cudaStreamDestroy(cs);
+    if (e != cudaSuccess) return e;
+    if ((e = cudaGraphInstantiate(&P.exec, P.graph, 0)) != cudaSuccess) return e;
+  }
+  P.staged = true;
+  return cudaSuccess;
+}
+
 // Build (or find) the plan of this block set and launch its graph.
 // views: validated views of the blocks (cons = stage input).
 cudaError_t batch_stage(BatchCache *cache, const Par &par, const phx_block *blocks, const BView *views, int n,
                         const double *const *base, double *const *out, double beta, double dt,
-                        const MlpPacked *mlp, const phx_mesh *mesh, bool batched, bool exchange_only,
+                        const MlpPacked *mlp, const phx_mesh *mesh, bool batched, int only,
                         DevStats *stats, unsigned int *err, cudaStream_t s, const char **why) {
   *why = nullptr;
   BatchPlan *pl = nullptr;
@@ -447,49 +505,32 @@ cudaError_t batch_stage(BatchCache *cache, const Par &par, const phx_block *bloc
     if ((e = upload_items(P, P.ghost, make_items(all, 256))) != cudaSuccess) return e;
     if ((e = upload_items(P, P.c2p, make_items(all, 128))) != cudaSuccess) return e;
     if (mlp && (e = cudaMalloc(&P.brk, sizeof(double) * 3 * (size_t)P.c2p.n * 128)) != cudaSuccess) return e;
-    if (mesh && (e = upload_mesh(P, mesh, n)) != cudaSuccess) return e;
-    // tile shapes
-    {
-      std::lock_guard<std::mutex> lk(g_tune_mu);
-      load_tune_file();
-      const std::string key = tune_key(par, vin, P.mink);
-      auto it = g_tune.find(key);
-      if (it != g_tune.end()) {
-        P.tune = it->second;
-      } else {
-        P.tune = autotune(P, vin, err, s);
-        g_tune[key] = P.tune;
-        save_tune_file();
-      }
+    if (mesh) {
+      if ((e = upload_mesh(P, mesh, n)) != cudaSuccess) return e;
+      std::vector<long long> fix;
+      for (int s3 = 0, b = 0; s3 < mesh->nseg[2]; s3++)
+        for (int s2 = 0; s2 < mesh->nseg[1]; s2++)
+          for (int s1 = 0; s1 < mesh->nseg[0]; s1++, b++) {
+            const int nx[3] = {vin[b].nx1, vin[b].nx2, vin[b].nx3};
+            const int org[3] = {mesh->seg_start[0][s1], mesh->seg_start[1][s2], mesh->seg_start[2][s3]};
+            long long cnt[6], tot = 0;
+            fix_face_counts(vin[b].ndim, nx, org, mesh->n, mesh->bc_lo, mesh->bc_hi, cnt);
+            for (long long c : cnt) tot += c;
+            fix.push_back(tot);
+          }
+      if ((e = upload_items(P, P.fixflux, make_items(fix, 128))) != cudaSuccess) return e;
     }
-    if ((e = upload_items(P, P.x1, x1_items(vin, P.tune.x1_cells, P.x1_smem))) != cudaSuccess) return e;
-    for (int dir = 1; dir <= 2; dir++) {
-      std::vector<long long> counts;
-      for (const BView &b : vin) counts.push_back(dir < P.ndim ? sweep_threads(b, dir, P.tune.seg) : 0);
-      if ((e = upload_items(P, dir == 1 ? P.x2 : P.x3, make_items(counts, 128))) != cudaSuccess) return e;
-    }
-    prepare_flux_x1_batched(par, P.mink, P.x1_smem);  // kernel attributes are set outside the capture
-    if ((e = cudaDeviceSynchronize()) != cudaSuccess) return e;
-    if (batched) {  // capture the stage
-      cudaStream_t cs;
-      if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) return e;
-      e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-      if (e == cudaSuccess) {
-        stage_launches(P, stats, err, cs);
-        e = cudaStreamEndCapture(cs, &P.graph);
-      }
-      cudaStreamDestroy(cs);
-      if (e != cudaSuccess) return e;
-      if ((e = cudaGraphInstantiate(&P.exec, P.graph, 0)) != cudaSuccess) return e;
-    }
+    P.vin = vin;
+    if (only == BATCH_STAGE && (e = prepare_stage(P, stats, err, s)) != cudaSuccess) return e;
     if (cache->plans.size() >= 8) cache->plans.erase(cache->plans.begin());
     cache->plans.push_back(std::move(np));
     pl = cache->plans.back().get();
   }
-  if (exchange_only) {
-    stage_launches(*pl, stats, err, s, true);
+  if (only != BATCH_STAGE) {
+    stage_launches(*pl, stats, err, s, only);
     return cudaGetLastError();
   }
+  if (!pl->staged && (e = prepare_stage(*pl, stats, err, s)) != cudaSuccess) return e;
   const double bd[2] = {beta, dt};
   if ((e = cudaMemcpyAsync(pl->beta_dt, bd, sizeof(bd), cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
   if (pl->batched) return cudaGraphLaunch(pl->exec, s);

@@ -110,6 +110,8 @@ struct Par {
   double cfl;
   int c2p_fixup, strategy_floors, enable_floors, enable_mhd_floors;
   double vsq_max;  // 1 - 1 / g0^2 (the gamma ceiling as a v^2 bound)
+  int fix_flux;      // fixup/enable_flux_fixup
+  int inflow_check;  // fixup/enable_ox1_fmks_inflow_check
 };
 
 // ------------------------------------------------ singularity-eos IdealGas

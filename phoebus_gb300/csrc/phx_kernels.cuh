@@ -100,14 +100,31 @@ struct MeshDev {
 };
 void launch_mesh_exchange(const Par &p, bool mink, const BView *views, const MeshDev &m, const WorkItem *items,
                           int nitems, int grid, cudaStream_t s);
+// FixFluxes: the physical-boundary faces of a block, per face (X1 lo, X1 hi,
+// X2 lo, X2 hi, X3 lo, X3 hi; 0 where the face is not physical).
+__host__ __device__ inline void fix_face_counts(int ndim, const int nx[3], const int origin[3], const int n[3],
+                                                const int bc_lo[3], const int bc_hi[3], long long cnt[6]) {
+  const long long e1 = nx[0], e2 = ndim >= 2 ? nx[1] : 1, e3 = ndim >= 3 ? nx[2] : 1;
+  const long long area[3] = {e2 * e3, e1 * e3, e1 * e2};
+  for (int d = 0; d < 3; d++) {
+    const bool on = d < ndim;
+    cnt[2 * d] = (on && origin[d] == 0 && bc_lo[d] != PHX_BC_PERIODIC) ? area[d] : 0;
+    cnt[2 * d + 1] = (on && origin[d] + nx[d] == n[d] && bc_hi[d] != PHX_BC_PERIODIC) ? area[d] : 0;
+  }
+}
+void launch_fix_fluxes(const Par &p, const BView *views, const MeshDev &m, const WorkItem *items, int nitems,
+                       int grid, cudaStream_t s);
+void launch_fix_fluxes_block(const Par &p, const BView &b, const int bc_lo[3], const int bc_hi[3], cudaStream_t s);
 struct BatchCache;
 BatchCache *batch_cache_create();
 void batch_cache_destroy(BatchCache *c);
 // mesh: null for independent periodic blocks.  batched = false launches each
-// phase block by block (no graph).  exchange_only: fill the mesh ghosts only.
+// phase block by block (no graph).  only: BATCH_STAGE the whole stage,
+// BATCH_EXCHANGE the mesh ghost fill alone, BATCH_FIXFLUX FixFluxes alone.
+enum { BATCH_STAGE = 0, BATCH_EXCHANGE = 1, BATCH_FIXFLUX = 2 };
 cudaError_t batch_stage(BatchCache *cache, const Par &par, const phx_block *blocks, const BView *views, int n,
                         const double *const *base, double *const *out, double beta, double dt,
-                        const MlpPacked *mlp, const phx_mesh *mesh, bool batched, bool exchange_only,
+                        const MlpPacked *mlp, const phx_mesh *mesh, bool batched, int only,
                         DevStats *stats, unsigned int *err, cudaStream_t s, const char **why);
 void batch_last_tuning(BatchCache *cache, int *x1_cells, int *seg, int *launches);
 long long interior_count(const BView &b);

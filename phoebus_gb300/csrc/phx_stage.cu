@@ -385,37 +385,48 @@ __global__ void __launch_bounds__(256) kb_ghost(const BView *views, int nvar, co
   }
 }
 
-// Ghost zone t of block blk on a tiled mesh (phx_mesh; 3D).  The source cell
-// is the global cell of the ghost, wrapped on periodic axes and clamped to
-// the boundary cell on outflow axes, in its owner block; its primitives are
-// copied (the normal velocity zeroed where it points into the domain across
-// an outflow face) and prim2con gives the ghost's conserved variables with
-// the ghost's own metric.
+// Ghost zone t of block blk on a tiled mesh (phx_mesh; 3D), bc_vars =
+// primitive.  Each axis maps the ghost's global cell: periodic axes wrap,
+// gr_outflow clamps to the boundary cell (OutflowInnerX1 & co.,
+// phoebus_boundaries.cpp:126-150, 215-254, GenericBC Outflow), reflect and
+// polar mirror it about the face (GenericBC Reflect :70-82, PolarInnerX2
+// :153-184, PolarOuterX2 :186-213).  Parthenon applies the faces one after
+// the other (X1, X2, X3; each over the whole extent of the other axes), so a
+// ghost in several boundary slabs ends up with the source cell of all axes'
+// maps and the product of their signs.
+//   Inside the domain (block faces, periodic wraps): the owner's primitives
+//   and conserved variables are copied (both carry FillGhost).
+//   In a physical slab: primitives from the source with the rule's signs (the
+//   velocity and B components along a reflect axis, v^2 and B^2 across a polar
+//   face), the outer-X1 inflow check (ConvertBoundaryConditions,
+//   phoebus_boundaries.cpp:366-397), then prim2con with the ghost's own metric
+//   (PrimitiveToConservedRegion, fluid.cpp:368-449: cons and cell speeds).
 template <bool MINK>
 __device__ __forceinline__ void mesh_ghost_at(const Par &p, const BView *views, const MeshDev &m, int blk,
                                               long long t) {
   const BView &b = views[blk];
   const int loc[3] = {(int)(t % b.n1t), (int)((t / b.n1t) % b.n2t), (int)(t / ((long long)b.n1t * b.n2t))};
   const int nx[3] = {b.nx1, b.nx2, b.nx3};
-  bool ghost = false;
-  int g[3], side[3];
+  bool ghost = false, physical = false, outer_x1 = false;
+  int g[3];
+  double sgn_v[3] = {1.0, 1.0, 1.0};  // sign of (v^d, B^d) from the mirrors
   for (int d = 0; d < 3; d++) {
     if (loc[d] < b.ng || loc[d] >= b.ng + nx[d]) ghost = true;
     int gg = m.origin[blk * 3 + d] + loc[d] - b.ng;
-    side[d] = 0;
-    if (gg < 0) {
-      if (m.bc_lo[d] == PHX_BC_PERIODIC) {
-        gg += m.n[d];
+    if (gg < 0 || gg >= m.n[d]) {
+      const bool lo = gg < 0;
+      const int bc = lo ? m.bc_lo[d] : m.bc_hi[d];
+      if (bc == PHX_BC_PERIODIC) {
+        gg += lo ? m.n[d] : -m.n[d];
       } else {
-        gg = 0;
-        side[d] = -1;
-      }
-    } else if (gg >= m.n[d]) {
-      if (m.bc_hi[d] == PHX_BC_PERIODIC) {
-        gg -= m.n[d];
-      } else {
-        gg = m.n[d] - 1;
-        side[d] = 1;
+        physical = true;
+        if (d == 0 && !lo) outer_x1 = true;
+        if (bc == PHX_BC_OUTFLOW) {
+          gg = lo ? 0 : m.n[d] - 1;
+        } else {  // reflect / polar: mirror about the face
+          gg = lo ? -1 - gg : 2 * m.n[d] - 1 - gg;
+          sgn_v[d] = -1.0;
+        }
       }
     }
     g[d] = gg;
@@ -425,13 +436,38 @@ __device__ __forceinline__ void mesh_ghost_at(const Par &p, const BView *views, 
   const BView &sb = views[src];
   const long long sid = sb.idx(g[2] - m.origin[src * 3 + 2] + sb.ng, g[1] - m.origin[src * 3 + 1] + sb.ng,
                                g[0] - m.origin[src * 3 + 0] + sb.ng);
+  const long long id = b.idx(loc[2], loc[1], loc[0]);
+  const int ncons = p.mhd ? PHX_NCONS : PHX_CB;
+  if (!physical) {
+    for (int v = 0; v < PHX_NPRIM; v++) {
+      if (v >= PHX_PB && v < PHX_PB + 3 && !p.mhd) continue;
+      b.prim[v * b.vs + id] = sb.prim[v * sb.vs + sid];
+    }
+    for (int v = 0; v < ncons; v++) b.cons[v * b.vs + id] = sb.cons[v * sb.vs + sid];
+    return;
+  }
   double P[PHX_NPRIM];
   for (int v = 0; v < PHX_NPRIM; v++) P[v] = sb.prim[v * sb.vs + sid];
-  for (int d = 0; d < 3; d++)
-    if ((side[d] < 0 && P[PHX_PVEL + d] > 0.0) || (side[d] > 0 && P[PHX_PVEL + d] < 0.0)) P[PHX_PVEL + d] = 0.0;
-  const long long id = b.idx(loc[2], loc[1], loc[0]);
+  for (int d = 0; d < 3; d++) {
+    P[PHX_PVEL + d] = sgn_v[d] * P[PHX_PVEL + d];
+    P[PHX_PB + d] = sgn_v[d] * P[PHX_PB + d];
+  }
   Pt gm{};
-  if constexpr (!MINK) load_pt(b, 0, loc[1], loc[0], gm);
+  if constexpr (!MINK) {
+    load_pt(b, 0, loc[1], loc[0], gm);
+    if (outer_x1 && p.inflow_check) {  // enforce u^1 >= 0 (phoebus_boundaries.cpp:366-397)
+      double vcon[3] = {P[PHX_PVEL], P[PHX_PVEL + 1], P[PHX_PVEL + 2]};
+      double W = lorentz<false>(gm, vcon);
+      const double ucon1 = vcon[0] - W * gm.beta[0] / gm.alpha;
+      if (ucon1 < 0) {
+        for (int d = 0; d < 3; d++) vcon[d] /= W;
+        vcon[0] = gm.beta[0] / gm.alpha;
+        const double vsq = dot_sp<false>(gm, vcon, vcon);
+        W = 1. / sqrt(1. - vsq);
+        for (int d = 0; d < 3; d++) P[PHX_PVEL + d] = W * vcon[d];
+      }
+    }
+  }
   const double vel[3] = {P[PHX_PVEL], P[PHX_PVEL + 1], P[PHX_PVEL + 2]};
   double bp[3] = {0.0, 0.0, 0.0};
   if (p.mhd)
@@ -470,6 +506,102 @@ void launch_mesh_exchange(const Par &p, bool mink, const BView *views, const Mes
   else
     kb_mesh_exchange<false><<<persistent_grid(kb_mesh_exchange<false>, 128, 0, nitems, grid), 128, 0, s>>>(
         p, views, m, items, nitems);
+}
+
+// FixFluxes (fixup.cpp:728-1078) at face t of block blk's physical-boundary
+// faces (fix_face_counts order).  The density-flux clamps keep the
+// reference's std::min / std::max operand order (a NaN flux stays NaN).
+__device__ __forceinline__ void fixflux_at(const Par &p, const BView &b, const int origin[3], const int n[3],
+                                           const int bc_lo[3], const int bc_hi[3], long long t) {
+  const int nx[3] = {b.nx1, b.nx2, b.nx3};
+  long long cnt[6];
+  fix_face_counts(b.ndim, nx, origin, n, bc_lo, bc_hi, cnt);
+  int f = 0;
+  while (f < 6 && t >= cnt[f]) t -= cnt[f++];
+  if (f == 6) return;
+  const int dir = f >> 1;
+  const bool hi = f & 1;
+  const int bc = hi ? bc_hi[dir] : bc_lo[dir];
+  int i, j, k;
+  if (dir == 0) {
+    const int ny = b.ndim >= 2 ? b.nx2 : 1;
+    i = hi ? b.ie() + 1 : b.is();
+    j = b.js() + (int)(t % ny);
+    k = b.ks() + (int)(t / ny);
+  } else if (dir == 1) {
+    i = b.is() + (int)(t % b.nx1);
+    j = hi ? b.je() + 1 : b.js();
+    k = b.ks() + (int)(t / b.nx1);
+  } else {
+    i = b.is() + (int)(t % b.nx1);
+    j = b.js() + (int)(t / b.nx1);
+    k = hi ? b.ke() + 1 : b.ks();
+  }
+  const long long id = b.idx(k, j, i);
+  auto F = [&](int d, int v) -> double * { return b.flux + ((long long)d * PHX_NCONS + v) * b.vs; };
+  double *fr = F(dir, PHX_CRHO);
+  if (bc == PHX_BC_OUTFLOW) {  // gr_outflow: no mass inflow
+    const double x = fr[id];
+    fr[id] = hi ? ((x < 0.0) ? 0.0 : x) : ((0.0 < x) ? 0.0 : x);
+  } else if (bc == PHX_BC_REFLECT) {
+    fr[id] = 0.0;
+    F(dir, PHX_CENG)[id] = 0.0;
+    if (dir == 1) {
+      F(dir, PHX_CMOM + 0)[id] = 0.0;
+      F(dir, PHX_CMOM + 2)[id] = 0.0;
+    }
+  } else if (bc == PHX_BC_POLAR && dir == 1) {
+    fr[id] = 0.0;
+    F(1, PHX_CENG)[id] = 0.0;
+    for (int d = 0; d < 3; d++) F(1, PHX_CMOM + d)[id] = 0.0;
+    if (p.mhd) {
+      for (int d = 0; d < 3; d++) F(1, PHX_CB + d)[id] = 0.0;
+      // the B^2 fluxes of the ghost row mirror those of the interior row
+      const long long in = hi ? b.idx(k, j - 1, i) : id, out = hi ? id : b.idx(k, j - 1, i);
+      F(0, PHX_CB + 1)[out] = -F(0, PHX_CB + 1)[in];
+      if (b.ndim == 3) F(2, PHX_CB + 1)[out] = -F(2, PHX_CB + 1)[in];
+    }
+  }
+}
+
+__global__ void __launch_bounds__(128) kb_fix_fluxes(Par p, const BView *views, MeshDev m, const WorkItem *items,
+                                                     int nitems) {
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const WorkItem w = items[it];
+    const long long t = w.first + threadIdx.x;
+    if (t < w.last) fixflux_at(p, views[w.block], m.origin + 3 * w.block, m.n, m.bc_lo, m.bc_hi, t);
+  }
+}
+
+void launch_fix_fluxes(const Par &p, const BView *views, const MeshDev &m, const WorkItem *items, int nitems,
+                       int grid, cudaStream_t s) {
+  if (nitems <= 0) return;
+  kb_fix_fluxes<<<persistent_grid(kb_fix_fluxes, 128, 0, nitems, grid), 128, 0, s>>>(p, views, m, items, nitems);
+}
+
+// One block whose faces' boundary kinds are given (PHX_BC_PERIODIC for a
+// face with a neighbour): the block is its own mesh.
+struct FaceBC {
+  int lo[3], hi[3];
+};
+__global__ void __launch_bounds__(128) k_fix_fluxes(Par p, BView b, FaceBC bc, long long count) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int origin[3] = {0, 0, 0}, n[3] = {b.nx1, b.nx2, b.nx3};
+  if (t < count) fixflux_at(p, b, origin, n, bc.lo, bc.hi, t);
+}
+
+void launch_fix_fluxes_block(const Par &p, const BView &b, const int bc_lo[3], const int bc_hi[3], cudaStream_t s) {
+  FaceBC bc;
+  const int origin[3] = {0, 0, 0}, nx[3] = {b.nx1, b.nx2, b.nx3};
+  for (int d = 0; d < 3; d++) {
+    bc.lo[d] = bc_lo[d];
+    bc.hi[d] = bc_hi[d];
+  }
+  long long cnt[6], tot = 0;
+  fix_face_counts(b.ndim, nx, origin, nx, bc.lo, bc.hi, cnt);
+  for (long long c : cnt) tot += c;
+  if (tot == 0) return;
+  k_fix_fluxes<<<(unsigned)((tot + 127) / 128), 128, 0, s>>>(p, b, bc, tot);
 }
 
 void launch_sources_batched(const Par &p, bool mink, const BView *views, const WorkItem *items, int nitems, int grid,

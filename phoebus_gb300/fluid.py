@@ -286,10 +286,27 @@ class FluidContext:
                                          int(batched), _stream(stream)))
 
     def MeshExchange(self, p: abi.Params, mesh, blocks, stream=None):
+        """The boundary exchange of a tiled mesh (phx_mesh_exchange)."""
         n = len(blocks)
         arr = (abi.BlockS * n)(*[b.struct() for b in blocks])
         m = mesh.struct()
         self._ok(self.lib.phx_mesh_exchange(self.h, C.byref(p), C.byref(m), arr, n, _stream(stream)))
+
+    def FixFluxes(self, p: abi.Params, mesh, blocks, stream=None):
+        """fixup::FixFluxes on the blocks' flux arrays at the mesh's physical
+        boundaries (phx_fix_fluxes; a no-op unless p.enable_flux_fixup)."""
+        n = len(blocks)
+        arr = (abi.BlockS * n)(*[b.struct() for b in blocks])
+        m = mesh.struct()
+        self._ok(self.lib.phx_fix_fluxes(self.h, C.byref(p), C.byref(m), arr, n, _stream(stream)))
+
+    def FixFluxesBlock(self, p: abi.Params, b: Block, bc_lo, bc_hi, stream=None):
+        """fixup::FixFluxes(MeshBlockData*) (phx_fix_fluxes_block): bc_lo /
+        bc_hi the boundary kind of each face, abi.BC_PERIODIC where the block
+        has a neighbour."""
+        lo, hi = (C.c_int * 3)(*bc_lo), (C.c_int * 3)(*bc_hi)
+        s = b.struct()
+        self._ok(self.lib.phx_fix_fluxes_block(self.h, C.byref(p), C.byref(s), lo, hi, _stream(stream)))
 
     def batch_info(self) -> dict:
         a, b, c = C.c_int(), C.c_int(), C.c_int()

@@ -92,9 +92,10 @@ def torus_params(Gamma: float = 13.0 / 9.0):
     """Fluid/fixup settings of the torus run: WENO5-Z + HLL, tolerance 1e-10,
     ExpX1RhoSie floors (rho0 1e-6, rho exponent -1.5, sie0 1e-3, sie
     exponent -1), MHD floors, ceilings gamma 10 / sie 1 (torus.pin), c2p
-    fixup."""
+    fixup, FixFluxes and the outer-X1 inflow check (torus.pin:141, 151)."""
     p = abi.default_params(Gamma=Gamma, recon="weno5z", riemann="hll", c2p_tol=1e-10, c2p_max_iter=100)
     p.enable_floors, p.enable_mhd_floors, p.enable_ceilings, p.enable_c2p_fixup = 1, 1, 1, 1
+    p.enable_flux_fixup, p.enable_ox1_fmks_inflow_check = 1, 1
     p.floor_type = abi.FLOOR["ExpX1RhoSie"]
     p.rho0_floor, p.rho_exp_floor, p.sie0_floor, p.sie_exp_floor = 1e-6, -1.5, 1e-3, -1.0
     p.gam0_ceiling, p.sie0_ceiling = 10.0, 1.0

@@ -1,7 +1,8 @@
-"""Tiled meshes (phx_stage_mesh, phx_mesh_exchange): the primitive ghost
-exchange with physical boundaries, its agreement with a single periodic
-block, batched against block-by-block launches, and the magnetised torus
-state on an FMKS mesh."""
+"""Tiled meshes (phx_stage_mesh, phx_mesh_exchange, phx_fix_fluxes): the
+boundary exchange with physical boundaries and FixFluxes against the
+oracle's restatement, agreement with a single periodic block, batched
+against block-by-block launches, and the magnetised torus state on an FMKS
+mesh."""
 import math
 
 import numpy as np
@@ -119,29 +120,123 @@ def torch_isfinite(t):
     return torch.isfinite(t).all()
 
 
-def test_outflow_and_periodic_ghosts(ctx_fast):
-    """Right after an exchange, ghost primitives are exact copies of their
-    source cells (normal velocity pointing in through an outflow face set to
-    0)."""
-    p, mesh, blocks, _ = small_torus(ctx_fast)
-    ctx_fast.MeshExchange(p, mesh, blocks)
+def random_interior(ctx, p, mesh, blocks, seed):
+    """Random primitives in every block's interior (velocities and fields of
+    both signs, so mirrors and the inflow check have work), conserved
+    variables by prim2con."""
+    import torch
+
+    rng = np.random.default_rng(seed)
+    gam = p.gm1 + 1.0
+    for b in blocks:
+        ks, js, is_ = b.isl()
+        shp = b["prim"][0][ks, js, is_].shape
+        rho = 10.0 ** rng.uniform(-3.0, 0.0, shp)
+        u = rho * 10.0 ** rng.uniform(-2.0, 0.0, shp)
+        pr = np.zeros((abi.NPRIM,) + shp)
+        pr[abi.PRHO], pr[abi.PENG], pr[abi.PPRS] = rho, u, p.gm1 * u
+        pr[abi.PVEL:abi.PVEL + 3] = rng.uniform(-0.5, 0.5, (3,) + shp)
+        pr[abi.PB:abi.PB + 3] = rng.uniform(-0.2, 0.2, (3,) + shp)
+        pr[abi.PGM1], pr[abi.PTMP], pr[abi.PMU] = gam, u / rho, rng.uniform(0.1, 0.9, shp)
+        b["prim"][:, ks, js, is_] = torch.from_numpy(pr).to(b["prim"].device)
+        ctx.PrimitiveToConserved(p, b, *b.interior())
+    ctx.check()
+
+
+# (bc_lo, bc_hi) per axis; the first is the torus deck's
+MESH_BCS = {
+    "deck": ((abi.BC_OUTFLOW, abi.BC_OUTFLOW, abi.BC_PERIODIC), (abi.BC_OUTFLOW, abi.BC_OUTFLOW, abi.BC_PERIODIC)),
+    "reflect_polar": ((abi.BC_REFLECT, abi.BC_POLAR, abi.BC_PERIODIC), (abi.BC_OUTFLOW, abi.BC_POLAR, abi.BC_PERIODIC)),
+    "reflect_x2_x3": ((abi.BC_OUTFLOW, abi.BC_REFLECT, abi.BC_REFLECT), (abi.BC_REFLECT, abi.BC_OUTFLOW, abi.BC_OUTFLOW)),
+}
+
+
+def small_fmks_mesh(bcs, n=24, lo=8, hi=12):
+    from phoebus_gb300.mesh import TiledMesh, split_axis
+
+    segs = [split_axis(n, lo, hi, torus.TORUS_SEED, 40 + d) for d in range(3)]
+    return TiledMesh((n, n, n), segs, (math.log(1.2), 0.0, 0.0), (math.log(250.0), 1.0, 2.0 * math.pi), *bcs)
+
+
+@pytest.mark.parametrize("name", list(MESH_BCS))
+@pytest.mark.parametrize("geometry", ["fmks", "minkowski"])
+def test_mesh_exchange_matches_oracle(ctx_exact, name, geometry):
+    """Exact build: the exchange (neighbour copies, physical boundaries,
+    outer-X1 inflow check, prim2con in the boundary slabs) equals the
+    oracle's literal face-by-face restatement bit for bit -- prims, cons and
+    cell signal speeds in every ghost zone."""
+    from oracle.mesh_oracle import mesh_exchange
+    from oracle.oracle import Oracle
+
+    p = torus.torus_params()
+    mesh = small_fmks_mesh(MESH_BCS[name])
+    geom = torus.torus_geometry() if geometry == "fmks" else None
+    blocks = mesh.make_blocks("cuda", geom)
+    for b in blocks:
+        if geom is not None:
+            ctx_exact.GeometryFillFMKS(b)
+    random_interior(ctx_exact, p, mesh, blocks, seed=100 + 2 * list(MESH_BCS).index(name) + (geom is not None))
+    before = [b.to_host() for b in blocks]
+    ctx_exact.MeshExchange(p, mesh, blocks)
+    ctx_exact.check()
+    mesh_exchange(Oracle(), p, mesh, before)
+    for n, (g, r) in enumerate(zip(blocks, before)):
+        assert not np.isnan(r["prim"]).any(), f"block {n}: a ghost no rule filled"
+        assert_bitwise(g["prim"], r["prim"], f"block {n} prim")
+        assert_bitwise(g["cons"], r["cons"], f"block {n} cons")
+        assert_bitwise(g["cell_sig"], r["cell_sig"], f"block {n} cell_sig")
+
+
+@pytest.mark.parametrize("name", list(MESH_BCS))
+def test_fix_fluxes_matches_oracle(ctx_fast, name):
+    """FixFluxes on random fluxes of both signs, through the mesh entry point
+    and the per-block task, against the oracle bit for bit; without
+    enable_flux_fixup nothing changes."""
+    import torch
+
+    from oracle.mesh_oracle import block_faces, fix_fluxes, fix_fluxes_block
+
+    p = torus.torus_params()
+    mesh = small_fmks_mesh(MESH_BCS[name])
+    blocks = mesh.make_blocks("cuda", None)
+    g = torch.Generator(device="cuda").manual_seed(7)
+    for b in blocks:
+        b["flux"].copy_(torch.randn(b["flux"].shape, generator=g, device="cuda", dtype=torch.float64))
+    start = [b["flux"].clone() for b in blocks]
+    p.enable_flux_fixup = 0
+    ctx_fast.FixFluxes(p, mesh, blocks)
     ctx_fast.check()
-    ng = blocks[0].ng
-    b0 = blocks[mesh.block_index(0, 0, 0)]
-    pr = host(b0["prim"])
-    n1, n2, n3 = b0.nx
-    ks, js = slice(ng, ng + n3), slice(ng, ng + n2)
-    # X1 inner outflow: every ghost layer copies the first interior cell, v^1 > 0 zeroed
-    edge = pr[:, ks, js, ng].copy()
-    edge[abi.PVEL] = np.minimum(edge[abi.PVEL], 0.0)
-    for g in range(ng):
-        assert_bitwise(pr[:abi.PMU + 1, ks, js, g], edge[:abi.PMU + 1], f"X1 ghost {g}")
-    # X3 periodic: the lower ghosts of the first k-block are the last k-block's top interior layers
-    top = blocks[mesh.block_index(0, 0, mesh.nseg[2] - 1)]
-    tp = host(top["prim"])
-    m3 = top.nx[2]
-    i_s = slice(ng, ng + n1)
-    assert_bitwise(pr[:, 0:ng, js, i_s], tp[:, m3:m3 + ng, js, i_s], "X3 periodic ghosts")
+    for b, f0 in zip(blocks, start):
+        assert_bitwise(b["flux"], f0, "flux fixup off")
+    p.enable_flux_fixup = 1
+    ref = [b.to_host() for b in blocks]
+    fix_fluxes(p, mesh, ref)
+    ctx_fast.FixFluxes(p, mesh, blocks)
+    ctx_fast.check()
+    for n, (b, r) in enumerate(zip(blocks, ref)):
+        assert_bitwise(b["flux"], r["flux"], f"block {n} flux (mesh)")
+    # per-block task on the untouched fluxes
+    for b, f0, seg in zip(blocks, start, mesh.segments()):
+        b["flux"].copy_(f0)
+        lo, hi = block_faces(mesh, seg, b)
+        ctx_fast.FixFluxesBlock(p, b, lo, hi)
+        r = b.to_host()
+        r["flux"][...] = host(f0)
+        fix_fluxes_block(p, r, lo, hi)
+        ctx_fast.check()
+        assert_bitwise(b["flux"], r["flux"], "flux (block task)")
+
+
+def test_mesh_rejects_bad_boundaries(ctx_fast):
+    p = torus.torus_params()
+    bad = [((abi.BC_POLAR, abi.BC_OUTFLOW, abi.BC_PERIODIC), (abi.BC_OUTFLOW, abi.BC_OUTFLOW, abi.BC_PERIODIC)),
+           ((abi.BC_OUTFLOW, abi.BC_OUTFLOW, abi.BC_PERIODIC), (abi.BC_OUTFLOW, abi.BC_OUTFLOW, abi.BC_OUTFLOW)),
+           ((abi.BC_OUTFLOW, 7, abi.BC_PERIODIC), (abi.BC_OUTFLOW, abi.BC_OUTFLOW, abi.BC_PERIODIC))]
+    for bcs in bad:
+        mesh = small_fmks_mesh(bcs)
+        blocks = mesh.make_blocks("cuda", None)
+        with pytest.raises(RuntimeError, match="boundar|periodic"):
+            ctx_fast.MeshExchange(p, mesh, blocks)
 
 
 def test_torus_batched_equals_per_block(ctx_exact):
