@@ -16,9 +16,13 @@ from .block import Block, GeomTables
 
 def split_axis(n: int, lo: int, hi: int, seed: int, stream: int, step: int = 2) -> list[int]:
     """Segment lengths in [lo, hi] (multiples of step) that sum to n, drawn
-    from the SplitMix64 stream; the last two segments are rebalanced so that
-    every length stays in range."""
+    from the SplitMix64 stream.  A draw whose remainder could not be split
+    into lengths in range is replaced by the nearest length whose remainder
+    can."""
     from .states import uniform
+
+    def splittable(r):  # r = 0, or some m lengths in [lo, hi] sum to r
+        return r == 0 or -(-r // hi) <= r // lo
 
     u = uniform(seed, stream, 4 * n // lo + 8)
     lens, left, k = [], n, 0
@@ -26,8 +30,9 @@ def split_axis(n: int, lo: int, hi: int, seed: int, stream: int, step: int = 2) 
     while left > hi:
         L = choices[min(int(u[k] * len(choices)), len(choices) - 1)]
         k += 1
-        if left - L < lo:  # the rest would be too short: take what keeps it in range
-            L = left - lo if left - lo <= hi else hi
+        if not splittable(left - L):
+            ok = [c for c in choices if c < left and splittable(left - c)]
+            L = min(ok, key=lambda c: (abs(c - L), c))
         lens.append(L)
         left -= L
     lens.append(left)

@@ -151,7 +151,7 @@ MESH_BCS = {
 }
 
 
-def small_fmks_mesh(bcs, n=24, lo=8, hi=12):
+def small_fmks_mesh(bcs, n=26, lo=6, hi=12):
     from phoebus_gb300.mesh import TiledMesh, split_axis
 
     segs = [split_axis(n, lo, hi, torus.TORUS_SEED, 40 + d) for d in range(3)]
