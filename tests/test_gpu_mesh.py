@@ -137,6 +137,12 @@ def random_interior(ctx, p, mesh, blocks, seed):
         pr[abi.PRHO], pr[abi.PENG], pr[abi.PPRS] = rho, u, p.gm1 * u
         pr[abi.PVEL:abi.PVEL + 3] = rng.uniform(-0.5, 0.5, (3,) + shp)
         pr[abi.PB:abi.PB + 3] = rng.uniform(-0.2, 0.2, (3,) + shp)
+        if b.geom is not None:  # components of proper size: divide by sqrt(gamma_dd)
+            cent = host(b.geom.arrays["cent"])[:, js, is_]
+            for d in range(3):
+                scale = 1.0 / np.sqrt(cent[abi.G_GCOV + (d + 1) * (d + 2) // 2 + d + 1])
+                pr[abi.PVEL + d] *= scale
+                pr[abi.PB + d] *= scale
         pr[abi.PGM1], pr[abi.PTMP], pr[abi.PMU] = gam, u / rho, rng.uniform(0.1, 0.9, shp)
         b["prim"][:, ks, js, is_] = torch.from_numpy(pr).to(b["prim"].device)
         ctx.PrimitiveToConserved(p, b, *b.interior())
