@@ -369,24 +369,34 @@ phx_status phx_stage_batched(phx_ctx *ctx, const phx_params *p, const phx_block 
 /* A domain tiled by blocks as a tensor product of per-axis segments, for
  * phx_stage_mesh.  Block (s1, s2, s3) (segment indices) is blocks[(s3 *
  * nseg[1] + s2) * nseg[0] + s1]; its interior covers global cells
- * seg_start[d][s_d] .. seg_start[d][s_d + 1] - 1 on axis d.
- * Physical boundaries (phoebus_boundaries.cpp; bc_vars = primitive, the
- * torus deck's choice) fill a ghost from the cell that the rule maps it to:
+ * seg_start[d][s_d] .. seg_start[d][s_d + 1] - 1 on axis d.  All blocks share
+ * ndim; an inactive axis has n = 1 and one segment.
+ * Physical boundaries (phoebus_boundaries.cpp) fill a ghost from the cell
+ * that the rule maps it to:
  *   PHX_BC_OUTFLOW  gr_outflow: the boundary cell (OutflowInnerX1 & co.)
  *   PHX_BC_REFLECT  the mirror cell, vector components along the axis
  *                   negated (GenericBC<..., Reflect>)
- *   PHX_BC_POLAR    X2 faces only: the mirror cell, v^2 and B^2 negated
- *                   (PolarInnerX2 / PolarOuterX2)
+ *   PHX_BC_POLAR    X2 faces only, bc_vars = primitive only: the mirror
+ *                   cell, v^2 and B^2 negated (PolarInnerX2 / PolarOuterX2)
+ * with bc_vars (fluid.cpp:153-165):
+ *   PHX_BC_VARS_CONSERVED  the conserved variables are exchanged and copied,
+ *                   each copy scaled by robust::ratio(DetGamma(ghost),
+ *                   DetGamma(source)) (the reference's default);
+ *   PHX_BC_VARS_PRIMITIVE  primitives and conserved variables are exchanged,
+ *                   physical ghosts take the primitives and prim2con.
  * Periodic axes must be periodic on both faces (Parthenon's rule). */
 #define PHX_BC_PERIODIC 0
 #define PHX_BC_OUTFLOW 1
 #define PHX_BC_REFLECT 2
 #define PHX_BC_POLAR 3
+#define PHX_BC_VARS_CONSERVED 0
+#define PHX_BC_VARS_PRIMITIVE 1
 typedef struct {
   int n[3];                  /* global interior cells per axis            */
   int nseg[3];               /* segments (blocks) per axis                */
   const int *seg_start[3];   /* host arrays of nseg[d] + 1 entries         */
   int bc_lo[3], bc_hi[3];    /* PHX_BC_* of each face                      */
+  int bc_vars;               /* PHX_BC_VARS_*                              */
 } phx_mesh;
 
 /* The stage of phx_stage over a tiled mesh, in the reference's task order:
@@ -401,17 +411,20 @@ phx_status phx_stage_mesh(phx_ctx *ctx, const phx_params *p, const phx_mesh *mes
                           int nblocks, const double *const *cons_base, double *const *cons_out, double beta,
                           double dt, int use_learned_guess, int batched, void *stream);
 
-/* The boundary exchange of a tiled mesh with bc_vars = primitive
- * (phoebus_driver.cpp:646-668: AddBoundaryExchangeTasks,
- * ApplyBoundaryConditions, ConvertBoundaryConditions).  A ghost whose cell
- * lies inside the domain, across a block face or a periodic wrap, receives the
- * owning block's primitives and conserved variables.  A ghost in a physical
- * boundary slab receives the primitives of the cell its boundary rule maps it
- * to (the rules of all axes composed, as the face-by-face application in
- * X1, X2, X3 order leaves them), then, with p->enable_ox1_fmks_inflow_check
- * on an FMKS mesh, the outer-X1 inflow check
- * (phoebus_boundaries.cpp:366-397), then prim2con with its own metric
- * (PrimitiveToConservedRegion, conserved variables and cell signal speeds). */
+/* The boundary exchange of a tiled mesh (phoebus_driver.cpp:646-668:
+ * AddBoundaryExchangeTasks, ApplyBoundaryConditions,
+ * ConvertBoundaryConditions).  A ghost whose cell lies inside the domain,
+ * across a block face or a periodic wrap, receives the owning block's
+ * exchanged variables (bc_vars).  A ghost in a physical boundary slab
+ * receives the values of the cell its boundary rule maps it to, the rules of
+ * all axes composed as the face-by-face application in X1, X2, X3 order
+ * leaves them (with bc_vars = conserved, the product of the DetGamma ratios
+ * along that path).  With bc_vars = primitive it then gets, with
+ * p->enable_ox1_fmks_inflow_check on an FMKS mesh, the outer-X1 inflow check
+ * (phoebus_boundaries.cpp:366-397), and prim2con with its own metric
+ * (PrimitiveToConservedRegion: conserved variables and cell signal speeds).
+ * The inflow check with bc_vars = conserved (a con2prim of the slab first)
+ * is not built: PHX_ERR_UNSUPPORTED. */
 phx_status phx_mesh_exchange(phx_ctx *ctx, const phx_params *p, const phx_mesh *mesh, const phx_block *blocks,
                              int nblocks, void *stream);
 

@@ -17,13 +17,14 @@ host Blocks (numpy arrays shaped (nvar, k, j, i)):
 2. ApplyBoundaryConditions: the block's physical faces in the order inner_x1,
    outer_x1, inner_x2, outer_x2, inner_x3, outer_x3, each over its ghost slab
    spanning the entire range of the other two axes, on every FillGhost
-   variable: gr_outflow copies the boundary cell (OutflowInnerX1,
+   variable (scaled by robust::ratio(DetGamma(ghost), DetGamma(source)) when
+   bc_vars = conserved): gr_outflow copies the boundary cell (OutflowInnerX1,
    OutflowOuterX1 phoebus_boundaries.cpp:115-150, 215-254; GenericBC Outflow
    :42-113), reflect copies the mirror cell with the components of vector
    variables along the axis negated (GenericBC Reflect), polar copies the
    mirror cell with v^2 and B^2 negated (PolarInnerX2, PolarOuterX2
    :153-213).
-3. ConvertBoundaryConditions (:303-472): on an FMKS mesh with
+3. ConvertBoundaryConditions (:303-472), bc_vars = primitive: on an FMKS mesh with
    enable_ox1_fmks_inflow_check, u^1 >= 0 is enforced in the outer-X1 slab of
    a block on the outer X1 boundary (:366-397); then prim2con over every
    physical slab (PrimitiveToConservedRegion, through the C oracle).
@@ -58,7 +59,7 @@ def _pvars(mhd):
 
 def _exchange_neighbours(mesh, blocks, mhd):
     ncons = abi.NCONS if mhd else 5
-    pv = _pvars(mhd)
+    pv = _pvars(mhd) if mesh.bc_vars == abi.BC_VARS_PRIMITIVE else []
     segs = list(mesh.segments())
     src = [(b["prim"].copy(), b["cons"].copy()) for b in blocks]  # owners' values before this exchange
     for b, seg in zip(blocks, segs):
@@ -67,6 +68,10 @@ def _exchange_neighbours(mesh, blocks, mhd):
         shape_t = (b.n1t, b.n2t, b.n3t)
         gg, inside, interior, owner_seg, local = [], [], [], [], []
         for d in range(3):
+            if d >= b.ndim:  # inactive axis: one cell, no ghosts
+                for lst, val in ((gg, [0]), (inside, [True]), (interior, [True]), (owner_seg, [0]), (local, [0])):
+                    lst.append(np.array(val))
+                continue
             loc = np.arange(shape_t[d])
             g = org[d] + loc - ng
             lo, hi = g < 0, g >= mesh.n[d]
@@ -113,7 +118,7 @@ def _physical_faces(mesh, b, seg):
     the order Parthenon applies them."""
     org = _origin(mesh, seg)
     out = []
-    for d in range(3):
+    for d in range(b.ndim):
         for outer in (False, True):
             bc = mesh.bc_hi[d] if outer else mesh.bc_lo[d]
             edge = org[d] + b.nx[d] == mesh.n[d] if outer else org[d] == 0
@@ -122,7 +127,21 @@ def _physical_faces(mesh, b, seg):
     return out
 
 
-def _apply_face(b, d, outer, bc, mhd):
+def _detg(b):
+    """DetGamma at cell centres, shaped (k, j, i) by broadcasting (1 in
+    Minkowski)."""
+    if b.geom is None:
+        return np.ones((1, b.n2t, b.n1t))
+    return b.geom.arrays["cent"][abi.G_DETGAM][None, :, :]
+
+
+def _ratio(a, b):
+    """robust::ratio (robust.hpp:35-39)."""
+    small = 10 * np.finfo(np.float64).tiny
+    return a / (b + np.where(b >= 0, 1.0, -1.0) * small)
+
+
+def _apply_face(b, d, outer, bc, mhd, bc_vars):
     """One boundary function on one block (all FillGhost variables)."""
     ng, nd = b.ng, b.nx[d]
     lo_i, hi_i = ng, ng + nd - 1  # interior range on axis d (local)
@@ -131,7 +150,9 @@ def _apply_face(b, d, outer, bc, mhd):
     axis = 3 - d  # array axis of dimension d in (var, k, j, i)
     P, U = b["prim"], b["cons"]
     ncons = abi.NCONS if mhd else 5
-    pvars = _pvars(mhd)
+    conserved = bc_vars == abi.BC_VARS_CONSERVED
+    pvars = [] if conserved else _pvars(mhd)
+    detg = np.broadcast_to(_detg(b), (b.n3t, b.n2t, b.n1t))
     for g in ghosts:
         if bc == OUTFLOW:
             r = ref
@@ -142,18 +163,21 @@ def _apply_face(b, d, outer, bc, mhd):
         dst[axis], src[axis] = g, r
         pv = P[tuple(src)].copy()
         uv = U[tuple(src)].copy()
+        sp, su = np.ones(abi.NPRIM), np.ones(abi.NCONS)
         if bc == REFLECT:  # VectorComponent(l) == DIR: velocity, B (prims); S, B (cons)
-            pv[abi.PVEL + d] *= -1
-            pv[abi.PB + d] *= -1
-            uv[CMOM + d] *= -1
-            uv[CB + d] *= -1
+            sp[abi.PVEL + d] = sp[abi.PB + d] = -1.0
+            su[CMOM + d] = su[CB + d] = -1.0
         elif bc == POLAR:  # idx_pvel(1), idx_pb(1) only
-            pv[abi.PVEL + 1] *= -1
-            pv[abi.PB + 1] *= -1
-        for v in pvars:
-            P[(v,) + tuple(dst[1:])] = pv[v]
-        for v in range(ncons):
-            U[(v,) + tuple(dst[1:])] = uv[v]
+            sp[abi.PVEL + 1] = sp[abi.PB + 1] = -1.0
+        if conserved:  # q = sgn * gratio * q(ref)
+            gratio = _ratio(detg[tuple(dst[1:])], detg[tuple(src[1:])])
+            for v in range(ncons):
+                U[(v,) + tuple(dst[1:])] = su[v] * gratio * uv[v]
+        else:
+            for v in pvars:
+                P[(v,) + tuple(dst[1:])] = sp[v] * pv[v]
+            for v in range(ncons):
+                U[(v,) + tuple(dst[1:])] = su[v] * uv[v]
 
 
 def _slab(b, d, outer):
@@ -204,7 +228,11 @@ def mesh_exchange(orc, p, mesh, blocks):
     segs = list(mesh.segments())
     for b, seg in zip(blocks, segs):
         for d, outer, bc in _physical_faces(mesh, b, seg):
-            _apply_face(b, d, outer, bc, mhd)
+            _apply_face(b, d, outer, bc, mhd, mesh.bc_vars)
+    if mesh.bc_vars == abi.BC_VARS_CONSERVED:
+        if p.enable_ox1_fmks_inflow_check and blocks[0].geom is not None and mesh.bc_hi[0] != PERIODIC:
+            raise NotImplementedError("inflow check with bc_vars = conserved")
+        return
     for b, seg in zip(blocks, segs):
         faces = _physical_faces(mesh, b, seg)
         fmks = b.geom is not None

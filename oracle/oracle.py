@@ -213,15 +213,23 @@ class Oracle:
         return out
 
     # ---- composite sequences (same order as the GPU host API)
-    def Initialize(self, p, b: Block):
+    def _exchange(self, p, b: Block, exchange):
+        if exchange is None:
+            self.FillGhostsPeriodic(b, b["cons"], abi.NCONS if p.mhd else 5)
+        else:
+            exchange(b)
+
+    def Initialize(self, p, b: Block, exchange=None):
+        """exchange(b): the ghost exchange of b's current arrays; None = the
+        periodic exchange of the conserved variables."""
         self.PrimitiveToConserved(p, b)
-        self.FillGhostsPeriodic(b, b["cons"], abi.NCONS if p.mhd else 5)
+        self._exchange(p, b, exchange)
         return self.ConservedToPrimitive(p, b)
 
-    def Stage(self, p, b: Block, base, out, beta, dt):
-        """PhoebusDriver::RungeKuttaStage for one periodic block: sources,
-        fluxes, FluxCT, divergence + update, con2prim (entire), ghost
-        exchange, con2prim (entire).  b['cons'] is the stage input."""
+    def Stage(self, p, b: Block, base, out, beta, dt, exchange=None):
+        """PhoebusDriver::RungeKuttaStage for one block: sources, fluxes,
+        FluxCT, divergence + update, con2prim (entire), ghost exchange,
+        con2prim (entire).  b['cons'] is the stage input."""
         self.CalculateFluidSourceTerms(p, b)
         self.CalculateFluxes(p, b)
         self.FluxCT(p, b)
@@ -232,16 +240,16 @@ class Oracle:
         unbr = self.ConservedToPrimitive(p, b)
         self.ConservedToPrimitiveFixup(p, b)
         self.ApplyFloors(p, b)
-        self.FillGhostsPeriodic(b, out, abi.NCONS if p.mhd else 5)
+        self._exchange(p, b, exchange)
         unbr += self.ConservedToPrimitive(p, b)
         self.ConservedToPrimitiveFixup(p, b)
         self.ApplyFloors(p, b)
         b.arrays["cons"] = cons_in
         return unbr
 
-    def rk2_step(self, p, b: Block, cons_stage, dt):
+    def rk2_step(self, p, b: Block, cons_stage, dt, exchange=None):
         base = b.arrays["cons"]
-        self.Stage(p, b, base, cons_stage, 1.0, dt)
+        self.Stage(p, b, base, cons_stage, 1.0, dt, exchange)
         b.arrays["cons"] = cons_stage
-        self.Stage(p, b, base, base, 0.5, dt)
+        self.Stage(p, b, base, base, 0.5, dt, exchange)
         b.arrays["cons"] = base

@@ -83,10 +83,11 @@ class C2PStats(C.Structure):
 
 class Mesh(C.Structure):
     _fields_ = [("n", C.c_int * 3), ("nseg", C.c_int * 3), ("seg_start", C.c_void_p * 3), ("bc_lo", C.c_int * 3),
-                ("bc_hi", C.c_int * 3)]
+                ("bc_hi", C.c_int * 3), ("bc_vars", C.c_int)]
 
 
 BC_PERIODIC, BC_OUTFLOW, BC_REFLECT, BC_POLAR = 0, 1, 2, 3
+BC_VARS_CONSERVED, BC_VARS_PRIMITIVE = 0, 1
 
 
 class MlpTrainOpts(C.Structure):

@@ -617,8 +617,13 @@ phx_status phx_stage_batched(phx_ctx *ctx, const phx_params *p, const phx_block 
 
 // Validate a tiled mesh against its blocks (3D, ng equal, block extents =
 // segment lengths, blocks ordered by segment triple).
-static phx_status check_mesh(const phx_mesh *m, const phx_block *blocks, int nblocks, std::vector<phx::BView> &views) {
-  if (!m || !blocks) return fail(PHX_ERR_INVALID_ARG, "mesh/blocks is NULL");
+static phx_status check_mesh(const phx_mesh *m, const phx_params *p, const phx_block *blocks, int nblocks,
+                             std::vector<phx::BView> &views) {
+  if (!m || !blocks || nblocks < 1) return fail(PHX_ERR_INVALID_ARG, "mesh/blocks is NULL");
+  const int ndim = blocks[0].ndim;
+  if (ndim < 1 || ndim > 3) return fail(PHX_ERR_INVALID_ARG, "bad ndim %d", ndim);
+  if (m->bc_vars != PHX_BC_VARS_CONSERVED && m->bc_vars != PHX_BC_VARS_PRIMITIVE)
+    return fail(PHX_ERR_INVALID_ARG, "\"bc_vars\" must be either \"conserved\" or \"primitive\"!");
   long long nb = 1;
   for (int d = 0; d < 3; d++) {
     if (m->nseg[d] < 1 || m->n[d] < 1 || !m->seg_start[d]) return fail(PHX_ERR_INVALID_ARG, "bad mesh axis %d", d);
@@ -626,9 +631,13 @@ static phx_status check_mesh(const phx_mesh *m, const phx_block *blocks, int nbl
       return fail(PHX_ERR_INVALID_ARG, "mesh axis %d: segments must cover [0, n)", d);
     for (int k = 0; k < m->nseg[d]; k++)
       if (m->seg_start[d][k + 1] <= m->seg_start[d][k]) return fail(PHX_ERR_INVALID_ARG, "empty segment");
+    if (d >= ndim && (m->n[d] != 1 || m->nseg[d] != 1))
+      return fail(PHX_ERR_INVALID_ARG, "mesh axis %d is inactive in %dD: n and nseg must be 1", d, ndim);
     for (int bc : {m->bc_lo[d], m->bc_hi[d]}) {
       if (bc < PHX_BC_PERIODIC || bc > PHX_BC_POLAR) return fail(PHX_ERR_INVALID_ARG, "unknown boundary condition");
       if (bc == PHX_BC_POLAR && d != 1) return fail(PHX_ERR_INVALID_ARG, "polar boundaries are X2 faces only");
+      if (bc == PHX_BC_POLAR && m->bc_vars != PHX_BC_VARS_PRIMITIVE)
+        return fail(PHX_ERR_INVALID_ARG, "Polar X2 reflecting BCs not supported");  // phoebus_boundaries.cpp:167
     }
     if ((m->bc_lo[d] == PHX_BC_PERIODIC) != (m->bc_hi[d] == PHX_BC_PERIODIC))
       return fail(PHX_ERR_INVALID_ARG, "mesh axis %d: periodic on one face only", d);
@@ -642,18 +651,20 @@ static phx_status check_mesh(const phx_mesh *m, const phx_block *blocks, int nbl
       for (int s1 = 0; s1 < m->nseg[0]; s1++, b++) {
         if ((s = make_view(&blocks[b], views[b]))) return fail(s, "block %d: %s", b, g_last_error.c_str());
         const phx_block &B = blocks[b];
-        if (B.ndim != 3 || B.ng != blocks[0].ng) return fail(PHX_ERR_INVALID_ARG, "mesh blocks must be 3D, same ng");
+        if (B.ndim != ndim || B.ng != blocks[0].ng)
+          return fail(PHX_ERR_INVALID_ARG, "mesh blocks must share ndim and ng");
         if (B.nx1 != m->seg_start[0][s1 + 1] - m->seg_start[0][s1] ||
             B.nx2 != m->seg_start[1][s2 + 1] - m->seg_start[1][s2] ||
             B.nx3 != m->seg_start[2][s3 + 1] - m->seg_start[2][s3])
           return fail(PHX_ERR_INVALID_ARG, "block %d extents differ from its mesh segments", b);
-        if (B.nx1 < B.ng || B.nx2 < B.ng || B.nx3 < B.ng)
-          return fail(PHX_ERR_INVALID_ARG, "block %d: ghost exchange needs nx >= ng", b);
-        for (int d = 0; d < 3; d++)  // a mirror maps ng ghosts onto ng cells of the domain
-          if ((m->bc_lo[d] >= PHX_BC_REFLECT || m->bc_hi[d] >= PHX_BC_REFLECT) && m->n[d] < B.ng)
-            return fail(PHX_ERR_INVALID_ARG, "mesh axis %d: a mirror boundary needs n >= ng", d);
+        const int nx[3] = {B.nx1, B.nx2, B.nx3};
+        for (int d = 0; d < ndim; d++)  // one neighbour per side; a mirror maps ng ghosts onto ng cells
+          if (nx[d] < B.ng) return fail(PHX_ERR_INVALID_ARG, "block %d: ghost exchange needs nx >= ng", b);
         if (views[b].fmks != views[0].fmks) return fail(PHX_ERR_INVALID_ARG, "blocks must share the geometry kind");
       }
+  if (p->enable_ox1_fmks_inflow_check && views[0].fmks && m->bc_vars == PHX_BC_VARS_CONSERVED &&
+      m->bc_hi[0] != PHX_BC_PERIODIC)
+    return fail(PHX_ERR_UNSUPPORTED, "the outer-X1 inflow check with bc_vars = conserved is not built");
   return PHX_OK;
 }
 
@@ -665,7 +676,7 @@ phx_status phx_stage_mesh(phx_ctx *ctx, const phx_params *p, const phx_mesh *mes
   if (!cons_base || !cons_out) return fail(PHX_ERR_INVALID_ARG, "cons_base/cons_out is NULL");
   if (use_learned_guess && !ctx->mlp_loaded) return fail(PHX_ERR_INVALID_ARG, "no learned-guess weights loaded");
   std::vector<phx::BView> views;
-  if ((s = check_mesh(mesh, blocks, nblocks, views))) return s;
+  if ((s = check_mesh(mesh, p, blocks, nblocks, views))) return s;
   for (int n = 0; n < nblocks; n++) {
     const phx_block *b = &blocks[n];
     if (!b->flux || !b->face_sig || !b->cell_sig || !b->fail || !b->src || !cons_base[n] || !cons_out[n])
@@ -686,7 +697,7 @@ phx_status phx_mesh_exchange(phx_ctx *ctx, const phx_params *p, const phx_mesh *
   phx_status s;
   if ((s = ctx_device(ctx)) || (s = check_params(p))) return s;
   std::vector<phx::BView> views;
-  if ((s = check_mesh(mesh, blocks, nblocks, views))) return s;
+  if ((s = check_mesh(mesh, p, blocks, nblocks, views))) return s;
   for (int n = 0; n < nblocks; n++)
     if (!blocks[n].cell_sig) return fail(PHX_ERR_INVALID_ARG, "block %d: cell_sig is NULL", n);
   std::vector<const double *> base(nblocks);
@@ -708,7 +719,7 @@ phx_status phx_fix_fluxes(phx_ctx *ctx, const phx_params *p, const phx_mesh *mes
   phx_status s;
   if ((s = ctx_device(ctx)) || (s = check_params(p))) return s;
   std::vector<phx::BView> views;
-  if ((s = check_mesh(mesh, blocks, nblocks, views))) return s;
+  if ((s = check_mesh(mesh, p, blocks, nblocks, views))) return s;
   for (int n = 0; n < nblocks; n++)
     if (!blocks[n].flux) return fail(PHX_ERR_INVALID_ARG, "block %d: flux is NULL", n);
   if (!p->enable_flux_fixup) return PHX_OK;

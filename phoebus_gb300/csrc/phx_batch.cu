@@ -108,7 +108,7 @@ struct BatchPlan {
   double *brk = nullptr;           // learned brackets, 3 x c2p items x 128
   bool batched = true;             // one persistent launch per phase in a graph; else block by block
   bool has_mesh = false;           // tiled mesh exchange instead of per-block periodic ghosts
-  int mesh_n[3] = {0, 0, 0}, mesh_nseg[3] = {0, 0, 0}, mesh_bc[6] = {0, 0, 0, 0, 0, 0};
+  int mesh_n[3] = {0, 0, 0}, mesh_nseg[3] = {0, 0, 0}, mesh_bc[6] = {0, 0, 0, 0, 0, 0}, mesh_bc_vars = 0;
   std::vector<int> mesh_seg[3];    // host copy of the segment starts
   MeshDev md{};
   void *mesh_mem = nullptr;
@@ -308,7 +308,7 @@ static void stage_launches(BatchPlan &pl, DevStats *stats, unsigned int *err, cu
 
 static bool same_mesh(const BatchPlan &pl, const phx_mesh *m) {
   if (!m) return !pl.has_mesh;
-  if (!pl.has_mesh) return false;
+  if (!pl.has_mesh || pl.mesh_bc_vars != m->bc_vars) return false;
   for (int d = 0; d < 3; d++) {
     if (pl.mesh_n[d] != m->n[d] || pl.mesh_nseg[d] != m->nseg[d] || pl.mesh_bc[2 * d] != m->bc_lo[d] ||
         pl.mesh_bc[2 * d + 1] != m->bc_hi[d])
@@ -323,6 +323,8 @@ static bool same_mesh(const BatchPlan &pl, const phx_mesh *m) {
 // block -> origin.
 static cudaError_t upload_mesh(BatchPlan &P, const phx_mesh *m, int nblocks) {
   P.has_mesh = true;
+  P.mesh_bc_vars = m->bc_vars;
+  P.md.bc_vars = m->bc_vars;
   size_t ints = 0;
   for (int d = 0; d < 3; d++) {
     P.mesh_n[d] = m->n[d];

@@ -94,6 +94,7 @@ inline int persistent_grid(K kernel, int threads, size_t smem, int nitems, int g
 // maps, the owner block of each segment triple, each block's origin.
 struct MeshDev {
   int n[3], nseg[3], bc_lo[3], bc_hi[3];
+  int bc_vars;           // PHX_BC_VARS_*
   const int *seg_of[3];  // [n[d]]
   const int *owner;      // [nseg[2]][nseg[1]][nseg[0]]
   const int *origin;     // [nblocks][3] global index of the first interior cell

@@ -385,32 +385,43 @@ __global__ void __launch_bounds__(256) kb_ghost(const BView *views, int nvar, co
   }
 }
 
-// Ghost zone t of block blk on a tiled mesh (phx_mesh; 3D), bc_vars =
-// primitive.  Each axis maps the ghost's global cell: periodic axes wrap,
-// gr_outflow clamps to the boundary cell (OutflowInnerX1 & co.,
-// phoebus_boundaries.cpp:126-150, 215-254, GenericBC Outflow), reflect and
-// polar mirror it about the face (GenericBC Reflect :70-82, PolarInnerX2
-// :153-184, PolarOuterX2 :186-213).  Parthenon applies the faces one after
-// the other (X1, X2, X3; each over the whole extent of the other axes), so a
-// ghost in several boundary slabs ends up with the source cell of all axes'
-// maps and the product of their signs.
-//   Inside the domain (block faces, periodic wraps): the owner's primitives
-//   and conserved variables are copied (both carry FillGhost).
-//   In a physical slab: primitives from the source with the rule's signs (the
-//   velocity and B components along a reflect axis, v^2 and B^2 across a polar
-//   face), the outer-X1 inflow check (ConvertBoundaryConditions,
-//   phoebus_boundaries.cpp:366-397), then prim2con with the ghost's own metric
-//   (PrimitiveToConservedRegion, fluid.cpp:368-449: cons and cell speeds).
+// Ghost zone t of block blk on a tiled mesh (phx_mesh).  Each active axis
+// maps the ghost's global cell: periodic axes wrap, gr_outflow clamps to the
+// boundary cell (OutflowInnerX1 & co., phoebus_boundaries.cpp:115-150,
+// 215-254, GenericBC Outflow), reflect and polar mirror it about the face
+// (GenericBC Reflect :42-113, PolarInnerX2 :153-184, PolarOuterX2 :186-213).
+// Parthenon applies the faces one after the other (X1, X2, X3; each over the
+// whole extent of the other axes), so a ghost in several boundary slabs ends
+// up with the source cell of all axes' maps; its value passes through the
+// faces in that order.
+//   Inside the domain (block faces, periodic wraps): the owner's exchanged
+//   variables are copied (conserved; with bc_vars = primitive also the
+//   primitives).
+//   bc_vars = conserved, physical slab: the source's conserved variables,
+//   scaled at each face by sgn * robust::ratio(DetGamma(cell), DetGamma(its
+//   mapped cell)) where the cell is the one that face's loop sets (axes before
+//   it at the ghost's own index, axes after it already mapped); sgn negates
+//   the vector components along a reflect axis.
+//   bc_vars = primitive, physical slab: primitives from the source with the
+//   rule's signs (the velocity and B components along a reflect axis, v^2 and
+//   B^2 across a polar face), the outer-X1 inflow check
+//   (ConvertBoundaryConditions, phoebus_boundaries.cpp:366-397), then
+//   prim2con with the ghost's own metric (PrimitiveToConservedRegion,
+//   fluid.cpp:368-449: cons and cell speeds).
 template <bool MINK>
 __device__ __forceinline__ void mesh_ghost_at(const Par &p, const BView *views, const MeshDev &m, int blk,
                                               long long t) {
   const BView &b = views[blk];
   const int loc[3] = {(int)(t % b.n1t), (int)((t / b.n1t) % b.n2t), (int)(t / ((long long)b.n1t * b.n2t))};
   const int nx[3] = {b.nx1, b.nx2, b.nx3};
+  const int nd = b.ndim;
   bool ghost = false, physical = false, outer_x1 = false;
-  int g[3];
-  double sgn_v[3] = {1.0, 1.0, 1.0};  // sign of (v^d, B^d) from the mirrors
+  bool phys[3] = {false, false, false};
+  int g[3], mloc[3] = {loc[0], loc[1], loc[2]};  // source cell (global); mapped local index per axis
+  double sgn_v[3] = {1.0, 1.0, 1.0};             // sign of the axis-d vector components from a mirror
   for (int d = 0; d < 3; d++) {
+    g[d] = 0;
+    if (d >= nd) continue;  // inactive axis: one cell, no ghosts
     if (loc[d] < b.ng || loc[d] >= b.ng + nx[d]) ghost = true;
     int gg = m.origin[blk * 3 + d] + loc[d] - b.ng;
     if (gg < 0 || gg >= m.n[d]) {
@@ -419,12 +430,15 @@ __device__ __forceinline__ void mesh_ghost_at(const Par &p, const BView *views, 
       if (bc == PHX_BC_PERIODIC) {
         gg += lo ? m.n[d] : -m.n[d];
       } else {
-        physical = true;
+        physical = phys[d] = true;
         if (d == 0 && !lo) outer_x1 = true;
+        const int ref = lo ? b.ng : b.ng + nx[d] - 1;  // interior cell next to the face (local)
         if (bc == PHX_BC_OUTFLOW) {
           gg = lo ? 0 : m.n[d] - 1;
+          mloc[d] = ref;
         } else {  // reflect / polar: mirror about the face
           gg = lo ? -1 - gg : 2 * m.n[d] - 1 - gg;
+          mloc[d] = 2 * ref + (lo ? -1 : 1) - loc[d];
           sgn_v[d] = -1.0;
         }
       }
@@ -434,16 +448,40 @@ __device__ __forceinline__ void mesh_ghost_at(const Par &p, const BView *views, 
   if (!ghost) return;
   const int src = m.owner[(m.seg_of[2][g[2]] * m.nseg[1] + m.seg_of[1][g[1]]) * m.nseg[0] + m.seg_of[0][g[0]]];
   const BView &sb = views[src];
-  const long long sid = sb.idx(g[2] - m.origin[src * 3 + 2] + sb.ng, g[1] - m.origin[src * 3 + 1] + sb.ng,
-                               g[0] - m.origin[src * 3 + 0] + sb.ng);
+  int sl[3];
+  for (int d = 0; d < 3; d++) sl[d] = d < nd ? g[d] - m.origin[src * 3 + d] + sb.ng : 0;
+  const long long sid = sb.idx(sl[2], sl[1], sl[0]);
   const long long id = b.idx(loc[2], loc[1], loc[0]);
   const int ncons = p.mhd ? PHX_NCONS : PHX_CB;
+  const bool prim_vars = m.bc_vars == PHX_BC_VARS_PRIMITIVE;
   if (!physical) {
-    for (int v = 0; v < PHX_NPRIM; v++) {
-      if (v >= PHX_PB && v < PHX_PB + 3 && !p.mhd) continue;
-      b.prim[v * b.vs + id] = sb.prim[v * sb.vs + sid];
-    }
+    if (prim_vars)
+      for (int v = 0; v < PHX_NPRIM; v++) {
+        if (v >= PHX_PB && v < PHX_PB + 3 && !p.mhd) continue;
+        b.prim[v * b.vs + id] = sb.prim[v * sb.vs + sid];
+      }
     for (int v = 0; v < ncons; v++) b.cons[v * b.vs + id] = sb.cons[v * sb.vs + sid];
+    return;
+  }
+  if (!prim_vars) {
+    double U[PHX_NCONS];
+    for (int v = 0; v < ncons; v++) U[v] = sb.cons[v * sb.vs + sid];
+    for (int d = 0; d < nd; d++) {
+      if (!phys[d]) continue;
+      double gr = 1.0;  // DetGamma = 1 in Minkowski: ratio(1, 1) = 1
+      if constexpr (!MINK) {
+        int c[3], r[3];
+        for (int e = 0; e < 3; e++) c[e] = e < d ? loc[e] : (e == d ? loc[d] : mloc[e]);
+        for (int e = 0; e < 3; e++) r[e] = e == d ? mloc[d] : c[e];
+        const double *detg = b.gcent + (long long)PHX_G_DETGAM * b.n2t * b.n1t;
+        gr = ratio_p(detg[(long long)c[1] * b.n1t + c[0]], detg[(long long)r[1] * b.n1t + r[0]]);
+      }
+      for (int v = 0; v < ncons; v++) {
+        const double sg = (v == PHX_CMOM + d || v == PHX_CB + d) ? sgn_v[d] : 1.0;
+        U[v] = sg * gr * U[v];
+      }
+    }
+    for (int v = 0; v < ncons; v++) b.cons[v * b.vs + id] = U[v];
     return;
   }
   double P[PHX_NPRIM];

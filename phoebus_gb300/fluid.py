@@ -337,3 +337,40 @@ def rk2_step(ctx: FluidContext, p: abi.Params, b: Block, cons_stage, dt: float, 
                geom=b.geom)
     b2.arrays["cons"] = cons_stage
     ctx.Stage(p, b2, base, base, 0.5, dt, learned, stream)
+
+
+class MeshRK2:
+    """Heun RK2 steps of a tiled mesh through phx_stage_mesh (the rk2
+    LowStorageIntegrator: beta = 1, 1/2).  The blocks' 'cons' hold U^n on
+    entry and U^{n+1} on exit; the second-stage buffers are allocated once,
+    so every step replays the same two cached stage plans."""
+
+    def __init__(self, ctx: FluidContext, p: abi.Params, mesh, blocks):
+        import torch
+
+        self.ctx, self.p, self.mesh, self.blocks = ctx, p, mesh, blocks
+        self.bases = [b["cons"] for b in blocks]
+        self.seconds = [torch.zeros_like(b["cons"]) for b in blocks]
+        self.stage2 = []
+        for b, s2 in zip(blocks, self.seconds):
+            c = Block(b.nx, b.ng, b.ndim, b.xmin, b.dx, backend=b.backend, device=b.device, arrays=dict(b.arrays),
+                      geom=b.geom)
+            c.arrays["cons"] = s2
+            self.stage2.append(c)
+
+    def step(self, dt: float, learned=False, batched=True, stream=None):
+        self.ctx.StageMesh(self.p, self.mesh, self.blocks, self.bases, self.seconds, 1.0, dt, learned, batched,
+                           stream)
+        self.ctx.StageMesh(self.p, self.mesh, self.stage2, self.bases, self.bases, 0.5, dt, learned, batched, stream)
+
+    def initialize(self, stream=None):
+        """After a problem generator wrote the primitives (entire blocks):
+        PrimitiveToConserved, the mesh's boundary exchange, FillDerived."""
+        for b in self.blocks:
+            self.ctx.PrimitiveToConserved(self.p, b, stream=stream)
+        self.ctx.MeshExchange(self.p, self.mesh, self.blocks, stream)
+        for b in self.blocks:
+            self.ctx.ConservedToPrimitive(self.p, b, stream=stream)
+
+    def estimate_dt(self, use_face_speeds: bool) -> float:
+        return min(self.ctx.EstimateTimestepBlock(self.p, b, use_face_speeds).item() for b in self.blocks)

@@ -42,9 +42,14 @@ def split_axis(n: int, lo: int, hi: int, seed: int, stream: int, step: int = 2) 
 
 class TiledMesh:
     """Global interior cells n = (n1, n2, n3) over [xmin, xmax] per axis,
-    split into segments; boundary conditions per face (abi.BC_*)."""
+    split into segments; boundary conditions per face (abi.BC_*), the
+    exchanged variables (abi.BC_VARS_*; conserved is the reference's
+    default), ndim active axes (an inactive axis has n = 1)."""
 
-    def __init__(self, n, segs, xmin, xmax, bc_lo, bc_hi, ng: int = 4):
+    def __init__(self, n, segs, xmin, xmax, bc_lo, bc_hi, ng: int = 4, bc_vars: int = abi.BC_VARS_CONSERVED,
+                 ndim: int = 3):
+        self.ndim = ndim
+        self.bc_vars = bc_vars
         self.n = tuple(int(x) for x in n)
         self.lens = [list(map(int, s)) for s in segs]
         self.starts = [np.concatenate([[0], np.cumsum(s)]).astype(np.int32) for s in self.lens]
@@ -70,17 +75,17 @@ class TiledMesh:
                 for s1 in range(self.nseg[0]):
                     yield s1, s2, s3
 
-    def make_blocks(self, device="cuda", geometry: abi.Geometry | None = None):
-        """Allocated blocks (torch on device) in block order, with FMKS table
-        storage when geometry is FMKS."""
+    def make_blocks(self, device="cuda", geometry: abi.Geometry | None = None, backend: str = "torch"):
+        """Allocated blocks (torch on device, or numpy with backend="numpy")
+        in block order, with FMKS table storage when geometry is FMKS."""
         blocks = []
         for s1, s2, s3 in self.segments():
             s = (s1, s2, s3)
             nx = tuple(self.lens[d][s[d]] for d in range(3))
             xmin = tuple(self.xmin[d] + self.starts[d][s[d]] * self.dx[d] for d in range(3))
-            b = Block(nx, self.ng, 3, xmin, self.dx, backend="torch", device=device).alloc()
+            b = Block(nx, self.ng, self.ndim, xmin, self.dx, backend=backend, device=device).alloc()
             if geometry is not None and geometry.kind == abi.GEOM_FMKS:
-                b.geom = GeomTables(geometry, b.n1t, b.n2t, "torch", device).alloc()
+                b.geom = GeomTables(geometry, b.n1t, b.n2t, backend, device).alloc()
             blocks.append(b)
         return blocks
 
@@ -93,4 +98,5 @@ class TiledMesh:
             m.seg_start[d] = self._keep[d].ctypes.data_as(C.c_void_p)
             m.bc_lo[d] = self.bc_lo[d]
             m.bc_hi[d] = self.bc_hi[d]
+        m.bc_vars = self.bc_vars
         return m

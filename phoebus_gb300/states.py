@@ -336,6 +336,126 @@ def p2c2p_fmks(n: int = 512, ng: int = 4):
     return b, par, f, x
 
 
+def bondi_1d(n: int = 128, ng: int = 4):
+    """The Bondi regression deck (inputs/bondi.pin with tst/regression/bondi.py's
+    nx1 = 128): one 1D FMKS block, X1 in [0.59, 5], one X2 zone on [0, 1]
+    (theta = pi/2), a = 0, derefine_poles = false, x0 from fmks.cpp:72-81,
+    hydro only, Gamma 1.4, Cv 2.5, PLM + LLF, cfl 0.8, c2p_tol 1e-8, 100
+    iterations, gr_outflow in X1 with bc_vars = conserved, t_lim 100,
+    dt_init_fact 1e-6.  Returns (host block with FMKS parameters and table
+    storage, params, t_lim); fill the tables, then call bondi_fill."""
+    from .block import GeomTables
+
+    x1min, x1max = 0.59, 5.0
+    dx = (x1max - x1min) / n
+    b = Block((n, 1, 1), ng, 1, (x1min, 0.0, 0.0), (dx, 1.0, 6.28318530718)).alloc()
+    g = abi.default_geometry(abi.GEOM_FMKS, a=0.0, derefine_poles=0, x0=min(x1min, max(0.0, x1min - ng * dx)))
+    b.geom = GeomTables(g, b.n1t, b.n2t).alloc()
+    par = dict(Gamma=1.4, Cv=2.5, recon="linear", riemann="llf", cfl=0.8, c2p_tol=1.0e-8, c2p_max_iter=100, mhd=0)
+    return b, par, 100.0
+
+
+def bondi_mesh(n: int = 128):
+    """The Bondi deck's one-block 1D mesh: gr_outflow on both X1 faces
+    (reflect in X2 and periodic in X3 are inactive in 1D), bc_vars =
+    conserved (the default; bondi.pin sets none)."""
+    from .mesh import TiledMesh
+
+    return TiledMesh((n, 1, 1), [[n], [1], [1]], (0.59, 0.0, 0.0), (5.0, 1.0, 6.28318530718),
+                     (abi.BC_OUTFLOW, abi.BC_REFLECT, abi.BC_PERIODIC), (abi.BC_OUTFLOW, abi.BC_REFLECT, abi.BC_PERIODIC),
+                     bc_vars=abi.BC_VARS_CONSERVED, ndim=1)
+
+
+def _bondi_temp(r, n, C1, C2, Tc, rc):
+    """pgen/bondi.cpp:24-69: bisection for T(r) between the two roots."""
+    rtol, ftol = 1.0e-12, 1.0e-14
+    Tguess = Tc * (rc / r) ** 0.8
+    T0, T1 = (0.1 * Tguess, Tguess) if r < rc else (Tguess, 10.0 * Tguess)
+
+    def f(T):
+        return (1.0 + (1.0 + n) * T) ** 2.0 * (1.0 - 2.0 / r + (C1 / (r * r * T ** n)) ** 2.0) - C2
+
+    f0, f1 = f(T0), f(T1)
+    if f0 * f1 > 0.0:
+        raise RuntimeError(f"Bondi setup failed at r = {r}")
+    Th = 0.5 * (T0 + T1)
+    fh = f(Th)
+    while (T1 - T0) / Th > rtol and abs(fh) > ftol:
+        if fh * f0 < 0.0:
+            T1, f1 = Th, fh
+        else:
+            T0, f0 = Th, fh
+        Th = 0.5 * (T0 + T1)
+        fh = f(Th)
+    return Th
+
+
+def bondi_fill(b: Block, mdot: float = 1.0, rs: float = 8.0, Rhor: float = 2.0, gam: float = 1.4):
+    """Problem generator bondi (pgen/bondi.cpp:97-228) on the entire block:
+    Michel's accretion solution in Boyer-Lindquist, moved to FMKS and
+    renormalised with the block's own metric tables (which must be filled).
+    Sets the primitives; conserved variables come from PrimitiveToConserved."""
+    geo = b.geom.params
+    tab = b.geom.arrays["cent"]
+    tab = tab if isinstance(tab, np.ndarray) else tab.detach().cpu().numpy()
+    n = 1.0 / (gam - 1.0)
+    Cv = n
+    uc = math.sqrt(1.0 / (2.0 * rs))
+    Vc = -math.sqrt(uc ** 2 / (1.0 - 3.0 * uc ** 2))
+    Tc = -n * Vc ** 2 / ((n + 1.0) * (n * Vc ** 2 - 1.0))
+    C1 = uc * rs ** 2 * Tc ** n
+    C2 = (1.0 + (1.0 + n) * Tc) ** 2 * (1.0 - 2.0 / rs + C1 ** 2 / (rs ** 4 * Tc ** (2 * n)))
+    h = geo.hslope
+    pr = b.arrays["prim"]
+    x0 = b.xmin[0] - b.ng * b.dx[0]
+    x2 = b.xmin[1] + 0.5 * b.dx[1]
+    for i in range(b.n1t):
+        x1 = x0 + (i + 0.5) * b.dx[0]
+        r = math.exp(x1)
+        while r < Rhor:
+            x1 += b.dx[0]
+            r = math.exp(x1)
+        T = _bondi_temp(r, n, C1, C2, Tc, rs)
+        rho = T ** n
+        u = rho * T / (gam - 1.0)
+        P = (gam - 1.0) * rho * (u / rho)
+        bmod = gam * (gam - 1.0) * rho * Cv * T
+        ucon_bl = [0.0, -C1 / (T ** n * r ** 2), 0.0, 0.0]
+        th = math.pi * x2 + ((1.0 - h) / 2.0) * math.sin(2.0 * math.pi * x2)  # derefine_poles = false
+        # Schwarzschild (a = 0) Boyer-Lindquist metric at (r, th)
+        gtt, grr = -(1.0 - 2.0 / r), 1.0 / (1.0 - 2.0 / r)
+        AA, BB = gtt, 0.0
+        CC = 1.0 + grr * ucon_bl[1] * ucon_bl[1]
+        ucon_bl[0] = (-BB - math.sqrt(BB * BB - 4.0 * AA * CC)) / (2.0 * AA)
+        # BL -> KS (a = 0), then KS -> FMKS: dX1/dr = 1/r, dX2/dth = 1/(dth/dX2), phi unchanged
+        idenom = 1.0 / (r * r - 2.0 * r)
+        uks = [ucon_bl[0] + 2.0 * r * idenom * ucon_bl[1], ucon_bl[1], ucon_bl[2], ucon_bl[3]]
+        dth = math.pi * (1.0 + (1.0 - h) * math.cos(2.0 * math.pi * x2))
+        ucon = [uks[0], uks[1] / r, uks[2] / dth, uks[3]]
+        # renormalise with the cell's own metric
+        t = tab[:, 0, i]
+        def gc(m, q):
+            hi, lo = max(m, q), min(m, q)
+            return t[abi.G_GCOV + hi * (hi + 1) // 2 + lo]
+        AA = gc(0, 0)
+        BB = 2.0 * (gc(0, 1) * ucon[1] + gc(0, 2) * ucon[2] + gc(0, 3) * ucon[3])
+        CC = (1.0 + gc(1, 1) * ucon[1] * ucon[1] + gc(2, 2) * ucon[2] * ucon[2] + gc(3, 3) * ucon[3] * ucon[3] +
+              2.0 * (gc(1, 2) * ucon[1] * ucon[2] + gc(1, 3) * ucon[1] * ucon[3] + gc(2, 3) * ucon[2] * ucon[3]))
+        discr = BB * BB - 4.0 * AA * CC
+        assert discr > 0, "discr < 0"
+        ucon[0] = (-BB - math.sqrt(discr)) / (2.0 * AA)
+        lapse = t[abi.G_ALPHA]
+        W = lapse * ucon[0]
+        pr[abi.PRHO, 0, 0, i] = rho
+        pr[abi.PENG, 0, 0, i] = u
+        pr[abi.PPRS, 0, 0, i] = P
+        pr[abi.PTMP, 0, 0, i] = T
+        pr[abi.PGM1, 0, 0, i] = bmod / P
+        for d in range(3):
+            pr[abi.PVEL + d, 0, 0, i] = ucon[d + 1] + W * t[abi.G_BETA + d] / lapse
+        pr[abi.PMU, 0, 0, i] = 0.0
+
+
 def fmks_random_block(nx=(12, 10, 4), seed: int = SEED + 5, ng: int = 4, r=(2.0, 20.0), x2=(0.1, 0.9),
                       a: float = 0.9375, derefine_poles: int = 1, Gamma: float = 4.0 / 3.0):
     """A block of FMKS coordinates (X1 = ln r, X2 in (0, 1), X3 = phi) holding

@@ -110,10 +110,12 @@ def torus_mesh(n: int = 384, seed: int = TORUS_SEED, lo: int = 32, hi: int = 96,
                r_out: float = 250.0) -> TiledMesh:
     """n^3 FMKS cells, X1 = ln r in [ln 1.2, ln 250], X2 in [0, 1],
     X3 in [0, 2 pi), each axis split into segments of lo..hi (even) cells;
-    outflow in X1 and X2 (the deck's gr_outflow), periodic in X3."""
+    outflow in X1 and X2 (the deck's gr_outflow), periodic in X3, bc_vars =
+    primitive (torus.pin:17)."""
     segs = [split_axis(n, lo, hi, seed, 10 + d) for d in range(3)]
     return TiledMesh((n, n, n), segs, (math.log(r_in_domain), 0.0, 0.0), (math.log(r_out), 1.0, 2.0 * math.pi),
-                     (abi.BC_OUTFLOW, abi.BC_OUTFLOW, abi.BC_PERIODIC), (abi.BC_OUTFLOW, abi.BC_OUTFLOW, abi.BC_PERIODIC))
+                     (abi.BC_OUTFLOW, abi.BC_OUTFLOW, abi.BC_PERIODIC), (abi.BC_OUTFLOW, abi.BC_OUTFLOW, abi.BC_PERIODIC),
+                     bc_vars=abi.BC_VARS_PRIMITIVE)
 
 
 def fill_torus(ctx, p: abi.Params, mesh: TiledMesh, blocks, a: float = 0.9375, rin: float = 6.0, rmax: float = 12.0,

@@ -2,8 +2,9 @@
 exchange, then the physical faces X1, X2, X3 in turn, each over the entire
 range of the other axes) against the closed form the CUDA exchange
 implements: every axis maps the ghost's global cell on its own (periodic
-wrap, clamp, mirror) and the signs of the mirrored vector components
-multiply.  Host only."""
+wrap, clamp, mirror), the signs of the mirrored vector components multiply,
+and with bc_vars = conserved the DetGamma ratios of the cells each face sets
+multiply in face order.  Host only."""
 import numpy as np
 import pytest
 
@@ -19,69 +20,95 @@ CASES = {
 }
 
 
-def host_mesh(bcs, seed):
-    mesh = TiledMesh((14, 12, 10), [[6, 8], [4, 8], [5, 5]], (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), *bcs)
+def host_mesh(bcs, seed, bc_vars, ndim=3):
+    n = [(14, 12, 10), (14, 12, 1), (14, 1, 1)][3 - ndim]
+    segs = [[[6, 8], [4, 8], [5, 5]][d] if d < ndim else [1] for d in range(3)]
+    mesh = TiledMesh(n, segs, (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), *bcs, bc_vars=bc_vars, ndim=ndim)
     rng = np.random.default_rng(seed)
-    blocks = []
-    for s1, s2, s3 in mesh.segments():
-        nx = (mesh.lens[0][s1], mesh.lens[1][s2], mesh.lens[2][s3])
-        b = Block(nx, 4, 3).alloc(["prim", "cons"])
+    blocks = mesh.make_blocks(geometry=abi.default_geometry(abi.GEOM_FMKS), backend="numpy")
+    for b in blocks:
         b["prim"][...] = rng.standard_normal(b["prim"].shape)
         b["cons"][...] = rng.standard_normal(b["cons"].shape)
-        blocks.append(b)
+        b.geom.arrays["cent"][abi.G_DETGAM] = rng.uniform(0.5, 2.0, b.geom.arrays["cent"][0].shape)
     return mesh, blocks
 
 
 def closed_form(mesh, blocks, mhd=True):
-    """Per ghost: the source cell of all axes' maps, signs multiplied."""
+    """Per ghost: the source cell of all axes' maps, signs multiplied, the
+    DetGamma ratios (bc_vars = conserved) multiplied in face order."""
     out = [(b["prim"].copy(), b["cons"].copy()) for b in blocks]
+    conserved = mesh.bc_vars == abi.BC_VARS_CONSERVED
     for (P, U), b, seg in zip(out, blocks, mesh.segments()):
         org = [int(mesh.starts[d][seg[d]]) for d in range(3)]
+        detg = b.geom.arrays["cent"][abi.G_DETGAM]
         for k in range(b.n3t):
             for j in range(b.n2t):
                 for i in range(b.n1t):
-                    loc = (i, j, k)
-                    g, sp, su, ghost, physical = [], np.ones(abi.NPRIM), np.ones(abi.NCONS), False, False
+                    loc = [i, j, k]
+                    mloc = list(loc)
+                    g, ghost, phys = [], False, [False] * 3
+                    sp, su = [np.ones(abi.NPRIM) for _ in range(3)], [np.ones(abi.NCONS) for _ in range(3)]
                     for d in range(3):
+                        if d >= b.ndim:
+                            g.append(0)
+                            continue
                         if not b.ng <= loc[d] < b.ng + b.nx[d]:
                             ghost = True
                         gg = org[d] + loc[d] - b.ng
                         if gg < 0 or gg >= mesh.n[d]:
                             lo = gg < 0
                             bc = mesh.bc_lo[d] if lo else mesh.bc_hi[d]
+                            ref = b.ng if lo else b.ng + b.nx[d] - 1
                             if bc == abi.BC_PERIODIC:
                                 gg += mesh.n[d] if lo else -mesh.n[d]
                             elif bc == abi.BC_OUTFLOW:
-                                physical = True
+                                phys[d] = True
                                 gg = 0 if lo else mesh.n[d] - 1
+                                mloc[d] = ref
                             else:
-                                physical = True
+                                phys[d] = True
                                 gg = -1 - gg if lo else 2 * mesh.n[d] - 1 - gg
+                                mloc[d] = 2 * ref + (-1 if lo else 1) - loc[d]
                                 c = 1 if bc == abi.BC_POLAR else d
-                                sp[abi.PVEL + c] *= -1
-                                sp[abi.PB + c] *= -1
+                                sp[d][abi.PVEL + c] = sp[d][abi.PB + c] = -1.0
                                 if bc == abi.BC_REFLECT:
-                                    su[mo.CMOM + d] *= -1
-                                    su[mo.CB + d] *= -1
+                                    su[d][mo.CMOM + d] = su[d][mo.CB + d] = -1.0
                         g.append(gg)
                     if not ghost:
                         continue
                     o, (li, lj, lk) = mo._owner_cell(mesh, g)
                     src = blocks[o]
-                    P[:, k, j, i] = sp * src["prim"][:, lk + b.ng, lj + b.ng, li + b.ng]
-                    U[:, k, j, i] = (su if physical else 1.0) * src["cons"][:, lk + b.ng, lj + b.ng, li + b.ng]
+                    sl = tuple(x + b.ng if d < b.ndim else 0 for d, x in enumerate((li, lj, lk)))
+                    q_p = src["prim"][:, sl[2], sl[1], sl[0]].copy()
+                    q_u = src["cons"][:, sl[2], sl[1], sl[0]].copy()
+                    for d in range(3):
+                        if not phys[d]:
+                            continue
+                        cc = [loc[e] if e <= d else mloc[e] for e in range(3)]
+                        rr = [mloc[e] if e == d else cc[e] for e in range(3)]
+                        gr = mo._ratio(detg[cc[1], cc[0]], detg[rr[1], rr[0]]) if conserved else 1.0
+                        q_u = su[d] * gr * q_u if conserved else su[d] * q_u
+                        q_p = sp[d] * q_p
+                    if not conserved:
+                        P[:, k, j, i] = q_p
+                    U[:, k, j, i] = q_u
     return out
 
 
+@pytest.mark.parametrize("ndim", [3, 2, 1])
+@pytest.mark.parametrize("bc_vars", [abi.BC_VARS_PRIMITIVE, abi.BC_VARS_CONSERVED])
 @pytest.mark.parametrize("name", list(CASES))
-def test_face_by_face_equals_composed_maps(name):
-    mesh, blocks = host_mesh(CASES[name], seed=11 + list(CASES).index(name))
+def test_face_by_face_equals_composed_maps(name, bc_vars, ndim):
+    bcs = CASES[name]
+    if bc_vars == abi.BC_VARS_CONSERVED and abi.BC_POLAR in bcs[0] + bcs[1]:
+        pytest.skip("polar boundaries need bc_vars = primitive")
+    mesh, blocks = host_mesh(bcs, 11 + list(CASES).index(name), bc_vars, ndim)
     want = closed_form(mesh, blocks)
     mo._exchange_neighbours(mesh, blocks, True)
     for b, seg in zip(blocks, mesh.segments()):
         for d, outer, bc in mo._physical_faces(mesh, b, seg):
-            mo._apply_face(b, d, outer, bc, True)
+            mo._apply_face(b, d, outer, bc, True, bc_vars)
     for n, (b, (P, U)) in enumerate(zip(blocks, want)):
-        assert not np.isnan(b["prim"]).any(), f"block {n}: a ghost no rule filled"
+        assert not np.isnan(b["cons"]).any(), f"block {n}: a ghost no rule filled"
         np.testing.assert_array_equal(b["prim"], P, err_msg=f"block {n} prim")
         np.testing.assert_array_equal(b["cons"], U, err_msg=f"block {n} cons")

@@ -51,6 +51,58 @@ def test_linear_modes_gold(oracle):
     assert np.max(np.abs(comp[:410] - gold[:410]) / np.abs(gold[:410])) < 1e-7
 
 
+def run_bondi(o, b=None):
+    """The Bondi regression run on the oracle: pgen, initialisation, RK2 steps
+    to t = 100 with the gr_outflow (bc_vars = conserved) exchange of the
+    mesh oracle.  b: a host block from states.bondi_1d with tables filled
+    (default: tables from the oracle)."""
+    from oracle.mesh_oracle import mesh_exchange
+
+    if b is None:
+        b, _, _ = states.bondi_1d()
+        o.GeometryFillFMKS(b)
+    _, par, tlim = states.bondi_1d()
+    states.bondi_fill(b)
+    p = abi.default_params(**par)
+    mesh = states.bondi_mesh()
+
+    def ex(blk):
+        mesh_exchange(o, p, mesh, [blk])
+
+    o.Initialize(p, b, ex)
+    tc = states.TimeControl(tlim, o.EstimateTimestepBlock(p, b, False), dt_init_fact=1.0e-6)
+    cs = np.zeros_like(b["cons"])
+    dts = []
+    while tc.keep_going():
+        dt = tc.begin_step()
+        dts.append(dt)
+        o.rk2_step(p, b, cs, dt, ex)
+        tc.end_step(o.EstimateTimestepBlock(p, b, True))
+    return b, tc, dts
+
+
+def bondi_values(b):
+    ks, js, is_ = b.isl()
+    pr = b["prim"]
+    return np.concatenate([pr[abi.PRHO][ks, js, is_].ravel()] + [pr[abi.PVEL + d][ks, js, is_].ravel() for d in range(3)])
+
+
+def test_bondi_gold(oracle):
+    """tst/regression/bondi.gold: the 128-zone FMKS hydro Bondi run (PLM +
+    LLF, geometric sources, gr_outflow with densitised conserved copies) at
+    t = 100 agrees with the reference's final state far inside its 1e-5
+    tolerance."""
+    gold = np.loadtxt(GOLD / "bondi.gold")
+    b, tc, _ = run_bondi(oracle)
+    comp = bondi_values(b)
+    assert len(comp) == len(gold) == 512
+    assert tc.time == 100.0
+    ok = soft_equiv(comp, gold, 1.0e-5)
+    assert ok.all(), f"{(~ok).sum()} values outside the gold tolerance"
+    assert np.max(np.abs(comp[:128] - gold[:128]) / gold[:128]) < 1e-7  # density
+    assert np.max(np.abs(comp[128:256] - gold[128:256]) / np.abs(gold[128:256])) < 1e-5  # v^1
+
+
 def test_p2c2p_known_answer(oracle):
     b, par, f, x = states.p2c2p_fmks()
     p = abi.default_params(**par)

@@ -157,37 +157,46 @@ MESH_BCS = {
 }
 
 
-def small_fmks_mesh(bcs, n=26, lo=6, hi=12):
+def small_fmks_mesh(bcs, n=26, lo=6, hi=12, bc_vars=abi.BC_VARS_PRIMITIVE):
     from phoebus_gb300.mesh import TiledMesh, split_axis
 
     segs = [split_axis(n, lo, hi, torus.TORUS_SEED, 40 + d) for d in range(3)]
-    return TiledMesh((n, n, n), segs, (math.log(1.2), 0.0, 0.0), (math.log(250.0), 1.0, 2.0 * math.pi), *bcs)
+    return TiledMesh((n, n, n), segs, (math.log(1.2), 0.0, 0.0), (math.log(250.0), 1.0, 2.0 * math.pi), *bcs,
+                     bc_vars=bc_vars)
 
 
+@pytest.mark.parametrize("bc_vars", [abi.BC_VARS_PRIMITIVE, abi.BC_VARS_CONSERVED])
 @pytest.mark.parametrize("name", list(MESH_BCS))
 @pytest.mark.parametrize("geometry", ["fmks", "minkowski"])
-def test_mesh_exchange_matches_oracle(ctx_exact, name, geometry):
-    """Exact build: the exchange (neighbour copies, physical boundaries,
-    outer-X1 inflow check, prim2con in the boundary slabs) equals the
+def test_mesh_exchange_matches_oracle(ctx_exact, name, geometry, bc_vars):
+    """Exact build: the exchange (neighbour copies, physical boundaries; with
+    bc_vars = primitive the outer-X1 inflow check and prim2con in the boundary
+    slabs, with bc_vars = conserved the DetGamma-scaled copies) equals the
     oracle's literal face-by-face restatement bit for bit -- prims, cons and
     cell signal speeds in every ghost zone."""
     from oracle.mesh_oracle import mesh_exchange
     from oracle.oracle import Oracle
 
+    bcs = MESH_BCS[name]
+    if bc_vars == abi.BC_VARS_CONSERVED and abi.BC_POLAR in bcs[0] + bcs[1]:
+        pytest.skip("polar boundaries need bc_vars = primitive")
     p = torus.torus_params()
-    mesh = small_fmks_mesh(MESH_BCS[name])
+    if bc_vars == abi.BC_VARS_CONSERVED:
+        p.enable_ox1_fmks_inflow_check = 0
+    mesh = small_fmks_mesh(bcs, bc_vars=bc_vars)
     geom = torus.torus_geometry() if geometry == "fmks" else None
     blocks = mesh.make_blocks("cuda", geom)
     for b in blocks:
         if geom is not None:
             ctx_exact.GeometryFillFMKS(b)
-    random_interior(ctx_exact, p, mesh, blocks, seed=100 + 2 * list(MESH_BCS).index(name) + (geom is not None))
+    random_interior(ctx_exact, p, mesh, blocks, seed=100 + 4 * list(MESH_BCS).index(name) + 2 * bc_vars +
+                    (geom is not None))
     before = [b.to_host() for b in blocks]
     ctx_exact.MeshExchange(p, mesh, blocks)
     ctx_exact.check()
     mesh_exchange(Oracle(), p, mesh, before)
     for n, (g, r) in enumerate(zip(blocks, before)):
-        assert not np.isnan(r["prim"]).any(), f"block {n}: a ghost no rule filled"
+        assert not np.isnan(r["cons"]).any(), f"block {n}: a ghost no rule filled"
         assert_bitwise(g["prim"], r["prim"], f"block {n} prim")
         assert_bitwise(g["cons"], r["cons"], f"block {n} cons")
         assert_bitwise(g["cell_sig"], r["cell_sig"], f"block {n} cell_sig")
@@ -235,14 +244,22 @@ def test_fix_fluxes_matches_oracle(ctx_fast, name):
 
 def test_mesh_rejects_bad_boundaries(ctx_fast):
     p = torus.torus_params()
-    bad = [((abi.BC_POLAR, abi.BC_OUTFLOW, abi.BC_PERIODIC), (abi.BC_OUTFLOW, abi.BC_OUTFLOW, abi.BC_PERIODIC)),
-           ((abi.BC_OUTFLOW, abi.BC_OUTFLOW, abi.BC_PERIODIC), (abi.BC_OUTFLOW, abi.BC_OUTFLOW, abi.BC_OUTFLOW)),
-           ((abi.BC_OUTFLOW, 7, abi.BC_PERIODIC), (abi.BC_OUTFLOW, abi.BC_OUTFLOW, abi.BC_PERIODIC))]
-    for bcs in bad:
-        mesh = small_fmks_mesh(bcs)
+    deck = MESH_BCS["deck"]
+    bad = [(((abi.BC_POLAR, abi.BC_OUTFLOW, abi.BC_PERIODIC), deck[1]), abi.BC_VARS_PRIMITIVE, "X2 faces"),
+           ((deck[0], (abi.BC_OUTFLOW, abi.BC_OUTFLOW, abi.BC_OUTFLOW)), abi.BC_VARS_PRIMITIVE, "periodic"),
+           (((abi.BC_OUTFLOW, 7, abi.BC_PERIODIC), deck[1]), abi.BC_VARS_PRIMITIVE, "unknown boundary"),
+           (MESH_BCS["reflect_polar"], abi.BC_VARS_CONSERVED, "Polar X2"),
+           (deck, 5, "bc_vars")]
+    for bcs, bc_vars, msg in bad:
+        mesh = small_fmks_mesh(bcs, bc_vars=bc_vars)
         blocks = mesh.make_blocks("cuda", None)
-        with pytest.raises(RuntimeError, match="boundar|periodic"):
+        with pytest.raises(RuntimeError, match=msg):
             ctx_fast.MeshExchange(p, mesh, blocks)
+    # the inflow check after a conserved exchange (a con2prim of the slab) is not built
+    mesh = small_fmks_mesh(deck, bc_vars=abi.BC_VARS_CONSERVED)
+    blocks = mesh.make_blocks("cuda", torus.torus_geometry())
+    with pytest.raises(RuntimeError, match="inflow check"):
+        ctx_fast.MeshExchange(p, mesh, blocks)
 
 
 def test_torus_batched_equals_per_block(ctx_exact):
