@@ -316,3 +316,44 @@ def fix_fluxes(p, mesh, blocks):
     for b, seg in zip(blocks, mesh.segments()):
         lo, hi = block_faces(mesh, seg, b)
         fix_fluxes_block(p, b, lo, hi)
+
+
+def mesh_stage(orc, p, mesh, blocks, bases, outs, beta, dt):
+    """PhoebusDriver::RungeKuttaStage over a tiled mesh on host blocks, in
+    the reference's task order: per block sources, fluxes, FluxCT, FixFluxes
+    (p.enable_flux_fixup), flux divergence and update into outs; FillDerived
+    over the mesh (con2prim, c2p fixup, floors); the boundary exchange of all
+    blocks; FillDerived per block again.  blocks[n]['cons'] is the stage
+    input."""
+    for b, seg, base, out in zip(blocks, mesh.segments(), bases, outs):
+        orc.CalculateFluidSourceTerms(p, b)
+        orc.CalculateFluxes(p, b)
+        orc.FluxCT(p, b)
+        lo, hi = block_faces(mesh, seg, b)
+        fix_fluxes_block(p, b, lo, hi)
+        orc.FluxDivergence(p, b)
+        orc.Update(p, b, base, out, beta, dt)
+    ins = [b.arrays["cons"] for b in blocks]
+    for b, out in zip(blocks, outs):
+        b.arrays["cons"] = out
+    for _ in range(2):
+        if _ == 1:
+            mesh_exchange(orc, p, mesh, blocks)
+        for b in blocks:
+            orc.ConservedToPrimitive(p, b)
+            orc.ConservedToPrimitiveFixup(p, b)
+            orc.ApplyFloors(p, b)
+    for b, c in zip(blocks, ins):
+        b.arrays["cons"] = c
+
+
+def mesh_rk2_step(orc, p, mesh, blocks, seconds, dt):
+    """One Heun RK2 step (beta = 1, 1/2) of the mesh on host blocks;
+    blocks[n]['cons'] holds U^n on entry and U^{n+1} on exit."""
+    bases = [b.arrays["cons"] for b in blocks]
+    mesh_stage(orc, p, mesh, blocks, bases, seconds, 1.0, dt)
+    for b, s in zip(blocks, seconds):
+        b.arrays["cons"] = s
+    mesh_stage(orc, p, mesh, blocks, bases, bases, 0.5, dt)
+    for b, c in zip(blocks, bases):
+        b.arrays["cons"] = c

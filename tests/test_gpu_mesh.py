@@ -282,3 +282,38 @@ def test_torus_batched_equals_per_block(ctx_exact):
             assert_bitwise(x[name], y[name], name)
         ks, js, is_ = x.isl()
         assert bool(torch.isfinite(x["prim"][:, ks, js, is_]).all())
+
+
+@pytest.mark.parametrize("floors", ["ConstantRhoSie", "ExpX1RhoSie"])
+def test_torus_rk2_matches_oracle(oracle, ctx_exact, floors):
+    """Config 5 end to end on a small mesh: one batched RK2 step of the
+    magnetised torus (FMKS, WENO5-Z + HLL, gr_outflow with bc_vars =
+    primitive, the outer-X1 inflow check, FixFluxes, floors, ceilings, c2p
+    fixup) against the oracle's mesh stage from the same tables and state.
+    Bit for bit with constant floors; ExpX1RhoSie floors evaluate exp (CUDA's
+    and glibc's are ulps apart), so there the bar is 1e-8 of each variable's
+    scale."""
+    from oracle.mesh_oracle import mesh_rk2_step
+    from phoebus_gb300.fluid import MeshRK2
+    from tests.util import assert_close
+
+    p = torus.torus_params()
+    if floors == "ConstantRhoSie":
+        p.floor_type = abi.FLOOR["ConstantRhoSie"]
+        p.rho0_floor, p.sie0_floor = 1e-6, 1e-3
+    mesh = torus.torus_mesh(n=48, lo=16, hi=32)
+    blocks = mesh.make_blocks("cuda", torus.torus_geometry())
+    torus.fill_torus(ctx_exact, p, mesh, blocks)
+    ctx_exact.check()
+    hosts = [b.to_host() for b in blocks]
+    rk = MeshRK2(ctx_exact, p, mesh, blocks)
+    dt = 0.3 * rk.estimate_dt(False)
+    rk.step(dt)
+    ctx_exact.check()
+    mesh_rk2_step(oracle, p, mesh, hosts, [np.zeros_like(h["cons"]) for h in hosts], dt)
+    for n, (g, h) in enumerate(zip(blocks, hosts)):
+        for name in ("prim", "cons", "fail"):
+            if floors == "ConstantRhoSie":
+                assert_bitwise(g[name], h[name], f"block {n} {name}")
+            else:
+                assert_close(g[name], h[name], 1e-8, f"block {n} {name}")
