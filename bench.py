@@ -581,6 +581,13 @@ def main():
         fp64 = {"achieved_tflops": flops / (flux_ms * 1e-3) / 1e12, "peak_tflops": fp64_peak / 1e12,
                 "frac": flops / (flux_ms * 1e-3) / fp64_peak, "flops_source": d["source"],
                 "peak_source": "measured in-process (phx_probe_fp64_peak)"}
+        if "fp64_instructions_per_call_per_zone" in d:
+            # the probe issues DFMAs only (2 flops each): its instruction rate is peak / 2.  A kernel
+            # with DADD/DMUL in its mix reaches frac < 1 at the full issue rate; issue_frac is the
+            # FP64 instruction rate against the probe's.
+            inst = d["fp64_instructions_per_call_per_zone"] * zones
+            fp64["issue_frac"] = inst / (flux_ms * 1e-3) / (fp64_peak / 2.0)
+            fp64["instructions_source"] = d["instructions_source"]
     traffic = None
     tf = ROOT / "profiles" / "flux_dram_traffic.json"
     if tf.exists():
