@@ -196,7 +196,11 @@ __device__ __forceinline__ bool c2p_setup(const Par &p, const Pt &g, const doubl
     bsq_rpsq = bsq * rsq - rbsq;
   }
   const double zsq = rsq / 1.0;  // h0sq_ = 1
+#ifdef PHX_EXACT
   const double v0sq = fmin(div_p(zsq, 1.0 + zsq), 1.0 - rcp_p(gam_max * gam_max));
+#else
+  const double v0sq = fmin(div_p(zsq, 1.0 + zsq), p.vsq_max);  // 1 - 1 / gam_max^2, formed on the host
+#endif
   res.D = D;
   res.q = q;
   res.bsq = bsq;
@@ -399,10 +403,16 @@ __device__ __forceinline__ void c2p_finish(const Par &p, const Pt &g, Residual &
   const double x = res.x_mu(mu);
   const double rbarsq = res.rbarsq_mu(mu, x);
   const double vsq = res.vhatsq_mu(mu, rbarsq);
+#ifdef PHX_EXACT
   const double iW = res.iWhat_mu(vsq);
+  const double W = rcp_p(iW);
+#else
+  // W and 1/W from one reciprocal square root, as in the residual
+  const double W = rsqrt_p(1.0 - vsq);
+  const double iW = (1.0 - vsq) * W;
+#endif
   prim[PHX_PRHO] = res.rhohat_mu(iW);
   const double qbar = res.qbar_mu(mu, x);
-  const double W = rcp_p(iW);
   double eng = res.ehat_mu(p, mu, qbar, rbarsq, vsq, W);
   prim[PHX_PTMP] = eos_T_rho_sie(p, prim[PHX_PRHO], eng);
   eng *= prim[PHX_PRHO];
