@@ -223,12 +223,8 @@ __global__ void __launch_bounds__(C2P_THREADS) k_mlp_bracket(Par p, Z zones, lon
       Pt g{};
       double U[PHX_NCONS], x1, x2, x3, guess;
       zones.template load<MINK>(t0 + q, id, g, U, x1, x2, x3, guess);
-      if (!(guess > 0.0)) {  // warm zones keep the reference's start: no bracket needed
-        Residual res;
-        double rcon[3], rcov[3], bu[3], Bprim[3] = {0.0, 0.0, 0.0}, bdotr = 0.0;
-        ok = c2p_setup<MINK>(p, g, U, x1, x2, x3, res, rcon, rcov, bu, Bprim, bdotr);
-        if (ok) c2p_features(res, f);
-      }
+      if (!(guess > 0.0))  // warm zones keep the reference's start: no bracket needed
+        ok = c2p_features_fp32<MINK>(p, g, U, x1, x2, x3, f);
     }
     float o0, o1;
     mlp_warp_forward(S->w, f, S->xs[warp], S->os[warp], o0, o1);
@@ -544,12 +540,8 @@ __global__ void __launch_bounds__(C2P_THREADS) kb_mlp_bracket(Par p, const BView
       Pt g{};
       double U[PHX_NCONS], x1, x2, x3, guess;
       zones.template load<MINK>(q, id, g, U, x1, x2, x3, guess);
-      if (!(guess > 0.0)) {  // warm zones keep the reference's start: no bracket needed
-        Residual res;
-        double rcon[3], rcov[3], bu[3], Bprim[3] = {0.0, 0.0, 0.0}, bdotr = 0.0;
-        ok = c2p_setup<MINK>(p, g, U, x1, x2, x3, res, rcon, rcov, bu, Bprim, bdotr);
-        if (ok) c2p_features(res, f);
-      }
+      if (!(guess > 0.0))  // warm zones keep the reference's start: no bracket needed
+        ok = c2p_features_fp32<MINK>(p, g, U, x1, x2, x3, f);
     }
     float o0, o1;
     mlp_warp_forward(S->w, f, S->xs[warp], S->os[warp], o0, o1);

@@ -228,6 +228,63 @@ __device__ __forceinline__ void c2p_features(const Residual &r, float f[6]) {
   f[5] = log10f((float)fmax(r.D, 1e-30)) * 0.125f;
 }
 
+// The same six invariants for inference, in FP32 arithmetic from the
+// conserved variables and the metric (GB300 issues FP32 at 64x its FP64 rate;
+// the invariants agree with c2p_setup's FP64 ones to FP32 rounding, far
+// below the network's own error).  Returns false for NaN input, as
+// c2p_setup does.
+template <bool MINK>
+__device__ __forceinline__ bool c2p_features_fp32(const Par &p, const Pt &g, const double U[PHX_NCONS], double x1,
+                                                  double x2, double x3, float f[6]) {
+  if (isnan(U[PHX_CRHO]) || isnan(U[PHX_CMOM]) || isnan(U[PHX_CENG])) return false;
+  double rhoflr_d = 0.0, epsflr;
+  get_floors(p, x1, x2, x3, rhoflr_d, epsflr);
+  const float rhoflr = (float)(rhoflr_d * p.fsf);
+  const float igdet = MINK ? 1.0f : 1.0f / (float)g.detgam;
+  const float D = (float)U[PHX_CRHO] * igdet;
+  const float q = (float)U[PHX_CENG] * igdet / D;
+  const float ic = 1.0f / (float)U[PHX_CRHO];
+  float rcov[3], rcon[3];
+#pragma unroll
+  for (int ii = 0; ii < 3; ii++) rcov[ii] = (float)U[PHX_CMOM + ii] * ic;
+  float rsq = 0.0f;
+#pragma unroll
+  for (int ii = 0; ii < 3; ii++) {
+    if constexpr (MINK) {
+      rcon[ii] = rcov[ii];
+    } else {
+      rcon[ii] = 0.0f;
+#pragma unroll
+      for (int jj = 0; jj < 3; jj++) rcon[ii] += (float)g.gamcon[ii][jj] * rcov[jj];
+    }
+    rsq += rcon[ii] * rcov[ii];
+  }
+  float bsq = 0.0f, rbsq = 0.0f;
+  if (p.mhd) {
+    const float sD = rsqrtf(fmaxf(D, rhoflr));
+    float bu[3], bdotr = 0.0f;
+#pragma unroll
+    for (int ii = 0; ii < 3; ii++) {
+      bu[ii] = (float)U[PHX_CB + ii] * igdet * sD;
+      bdotr += bu[ii] * rcov[ii];
+    }
+#pragma unroll
+    for (int m = 0; m < 3; m++)
+#pragma unroll
+      for (int n = 0; n < 3; n++) bsq += (MINK ? (m == n ? 1.0f : 0.0f) : (float)g.gcov[m + 1][n + 1]) * bu[m] * bu[n];
+    bsq = fmaxf(0.0f, bsq);
+    rbsq = bdotr * bdotr;
+  }
+  const float v0sq = fminf(rsq / (1.0f + rsq), (float)p.vsq_max);
+  f[0] = log10f(fmaxf(q, 1e-12f)) * 0.25f;
+  f[1] = log10f(fmaxf(rsq, 1e-12f)) * 0.25f;
+  f[2] = log10f(fmaxf(bsq, 1e-12f)) * 0.25f;
+  f[3] = rbsq / fmaxf(bsq * rsq, 1e-30f);
+  f[4] = v0sq;
+  f[5] = log10f(fmaxf(D, 1e-30f)) * 0.125f;
+  return true;
+}
+
 // State of one zone's regula falsi (root_find.hpp:110-167) between
 // iterations: the bracket [a, b] with sign-normalised end values, the Illinois
 // counters, and the tallies.  Saving and restoring it resumes the same
