@@ -14,14 +14,14 @@ namespace phx {
 
 struct Residual {
   double D, q, bsq, bsq_rpsq, rsq, rbsq, v0sq;
-  double x1, x2, x3;
+  FloorPt fl;  // floor_point of the zone: every evaluation's floors come from it
   double rho_floor, gam_max, e_max;
   bool used_density_floor, used_energy_floor, used_energy_max, used_gamma_max;
 
   __device__ __forceinline__ void init(const Par &p) {
     double garbage = 0.0;
     rho_floor = 0.0;
-    get_floors(p, x1, x2, x3, rho_floor, garbage);
+    floors_from(p, fl, rho_floor, garbage);
     gam_max = p.g0;
     e_max = p.smax0;
     rho_floor *= p.fsf;
@@ -58,7 +58,7 @@ struct Residual {
                                             double vhatsq, double What) {
     double rho = rhohat_mu(ratio_p(1.0, What));
     double e_floor;
-    get_floors(p, x1, x2, x3, rho, e_floor);
+    floors_from(p, fl, rho, e_floor);
     e_floor *= p.fsf;
     const double ehat_trial = What * (qbar - mu * rbarsq) + vhatsq * What * ratio_p(What, 1.0 + What);
     used_energy_floor = false;
@@ -77,7 +77,7 @@ struct Residual {
                                                double What, double iWhat) {
     double rho = rhohat_mu(iWhat);
     double e_floor;
-    get_floors(p, x1, x2, x3, rho, e_floor);
+    floors_from(p, fl, rho, e_floor);
     e_floor *= p.fsf;
     const double ehat_trial = What * (qbar - mu * rbarsq) + vhatsq * What * ratio_p(What, 1.0 + What);
     used_energy_floor = false;
@@ -145,7 +145,8 @@ __device__ __forceinline__ bool c2p_setup(const Par &p, const Pt &g, const doubl
   const double gdet = MINK ? 1.0 : g.detgam;
   const double igdet = rcp_p(gdet);
   double rhoflr = 0.0, epsflr;
-  get_floors(p, x1, x2, x3, rhoflr, epsflr);
+  const FloorPt fl = floor_point(p, x1, x2, x3);
+  floors_from(p, fl, rhoflr, epsflr);
   rhoflr *= p.fsf;
   const double gam_max = p.g0;
   const double D = U[PHX_CRHO] * igdet;
@@ -208,9 +209,7 @@ __device__ __forceinline__ bool c2p_setup(const Par &p, const Pt &g, const doubl
   res.rsq = rsq;
   res.rbsq = rbsq;
   res.v0sq = v0sq;
-  res.x1 = x1;
-  res.x2 = x2;
-  res.x3 = x3;
+  res.fl = fl;
   res.init(p);
   return true;
 }

@@ -129,34 +129,54 @@ __device__ __forceinline__ double eos_bmod_rho_T(const Par &p, double rho, doubl
 }
 
 // ------------------------------------------------------- fixup.hpp Bounds
-__device__ __forceinline__ void get_floors(const Par &p, double x1, double x2, double x3,
-                                           double &rflr, double &sflr) {
+// Bounds::GetFloors in two parts.  floor_point holds what depends on the
+// position only (for ExpX1RhoSie two exponentials); floors_from finishes
+// the floors from it and the density passed in (only ExpX1RhoU's sie floor
+// depends on that density).  A zone's con2prim evaluates its floors at every
+// residual and both states of a face at the face's position, so they compute
+// floor_point once and reuse it: the same values as get_floors, bit for bit.
+struct FloorPt {
+  double r, s;
+};
+__device__ __forceinline__ FloorPt floor_point(const Par &p, double x1, double x2, double x3) {
+  FloorPt f;
   switch (p.floor_type) {
   case PHX_FLOOR_CONSTANT_RHO_SIE:
-    rflr = p.r0;
-    sflr = p.s0;
+    f.r = p.r0;
+    f.s = p.s0;
     break;
   case PHX_FLOOR_EXPX1_RHO_SIE:
-    rflr = p.r0 * exp(p.ralpha * x1);
-    sflr = p.s0 * exp(p.salpha * x1);
+  case PHX_FLOOR_EXPX1_RHO_U:  // s: the sie floor's numerator
+    f.r = p.r0 * exp(p.ralpha * x1);
+    f.s = p.s0 * exp(p.salpha * x1);
     break;
-  case PHX_FLOOR_EXPX1_RHO_U: {
-    double scratch = p.r0 * exp(p.ralpha * x1);
-    sflr = p.s0 * exp(p.salpha * x1) / fmax(rflr, scratch);
-    rflr = scratch;
-  } break;
   case PHX_FLOOR_X1_RHO_SIE:
-    rflr = p.r0 * fmin(1.0, pow(x1, p.ralpha));
-    sflr = p.s0 * fmin(1.0, pow(x1, p.salpha));
+    f.r = p.r0 * fmin(1.0, pow(x1, p.ralpha));
+    f.s = p.s0 * fmin(1.0, pow(x1, p.salpha));
     break;
   default: {
     double r = sqrt(x1 * x1 + x2 * x2 + x3 * x3);
-    rflr = p.r0 * fmin(1.0, pow(r, p.ralpha));
-    sflr = p.s0 * fmin(1.0, pow(r, p.salpha));
+    f.r = p.r0 * fmin(1.0, pow(r, p.ralpha));
+    f.s = p.s0 * fmin(1.0, pow(r, p.salpha));
   } break;
   }
+  return f;
+}
+// True when the floors depend on X1 alone (all types but RRhoSie).
+__device__ __forceinline__ bool floors_x1_only(const Par &p) { return p.floor_type != PHX_FLOOR_R_RHO_SIE; }
+__device__ __forceinline__ void floors_from(const Par &p, const FloorPt &f, double &rflr, double &sflr) {
+  if (p.floor_type == PHX_FLOOR_EXPX1_RHO_U) {
+    sflr = f.s / fmax(rflr, f.r);
+  } else {
+    sflr = f.s;
+  }
+  rflr = f.r;
   rflr = fmax(rflr, p.rho_min_eos);
   sflr = fmax(sflr, p.sie_min_eos);
+}
+__device__ __forceinline__ void get_floors(const Par &p, double x1, double x2, double x3,
+                                           double &rflr, double &sflr) {
+  floors_from(p, floor_point(p, x1, x2, x3), rflr, sflr);
 }
 
 // ------------------------------------------------------------ block view
@@ -559,7 +579,7 @@ struct Face {
   double gdet;   // DetG: 1 for Minkowski, alpha * detgam from the cache
   double gammadet;
   double gdd;
-  double X1, X2, X3;
+  FloorPt fl;    // floor_point at the face, shared by its two states
 };
 
 // prim_to_flux (riemann.hpp:88-209) for face direction DIR (0-based).
@@ -570,7 +590,7 @@ __device__ __forceinline__ void prim_to_flux(const Par &par, const Face &f, cons
   const Pt &g = f.g;
   double rho_floor = q[PHX_PRHO];
   double sie_floor;
-  get_floors(par, f.X1, f.X2, f.X3, rho_floor, sie_floor);
+  floors_from(par, f.fl, rho_floor, sie_floor);
   const double rho = fmax(q[PHX_PRHO], rho_floor);
   double vpcon[3] = {q[PHX_PVEL], q[PHX_PVEL + 1], q[PHX_PVEL + 2]};
 #ifdef PHX_EXACT

@@ -22,9 +22,12 @@ namespace phx {
 constexpr unsigned FULL = 0xffffffffu;
 
 // Riemann solve + store for one face (riemann.hpp:256-301).
+// col: the face's floor_point when the caller holds it (a sweep across X1
+// faces' constant X1 when the floors depend on X1 alone), else null.
 template <bool MINK, int DIR>
 __device__ __forceinline__ void face_flux(const Par &p, const BView &b, int k, int j, int i,
-                                          const double ql[PHX_NRECON], const double qr[PHX_NRECON]) {
+                                          const double ql[PHX_NRECON], const double qr[PHX_NRECON],
+                                          const FloorPt *col = nullptr) {
   Face f;
   if constexpr (!MINK) {
     load_pt(b, DIR == 0 ? 1 : (DIR == 1 ? 2 : 0), j, i, f.g);
@@ -32,9 +35,12 @@ __device__ __forceinline__ void face_flux(const Par &p, const BView &b, int k, i
     f.gammadet = f.g.detgam;
     f.gdd = f.g.gamcon[DIR][DIR];
   }
-  f.X1 = DIR == 0 ? b.Xf(0, i) : b.Xc(0, i);
-  f.X2 = DIR == 1 ? b.Xf(1, j) : b.Xc(1, j);
-  f.X3 = DIR == 2 ? b.Xf(2, k) : b.Xc(2, k);
+  if (col) {
+    f.fl = *col;
+  } else {
+    f.fl = floor_point(p, DIR == 0 ? b.Xf(0, i) : b.Xc(0, i), DIR == 1 ? b.Xf(1, j) : b.Xc(1, j),
+                       DIR == 2 ? b.Xf(2, k) : b.Xc(2, k));
+  }
   const double gam_max = p.g0, sie_max = p.smax0;
   double Ul[PHX_NCONS], Fl[PHX_NCONS], Ur[PHX_NCONS], Fr[PHX_NCONS];
   double vml, vpl, vmr, vpr;
@@ -272,6 +278,10 @@ __device__ __forceinline__ void sweep_at(const Par &p, const BView &b, int alo, 
 #pragma unroll
     for (int o = 0; o < 4; o++) w[v][o + 1] = pc[v * vs + (o - 2) * stride];  // cells x-2..x+1
   double prev_ql[PHX_NRECON];
+  // X2 and X3 faces of this column share X1 (= the cell centre of column a)
+  FloorPt col{};
+  const bool use_col = DIR != 0 && floors_x1_only(p);
+  if (use_col) col = floor_point(p, b.Xc(0, a), 0.0, 0.0);
   for (int x = fbeg - 1; x <= fend; x++) {
     const double *pn = pc + (long long)(x - (fbeg - 1)) * stride;
     double ql[PHX_NRECON], qr[PHX_NRECON];
@@ -285,7 +295,7 @@ __device__ __forceinline__ void sweep_at(const Par &p, const BView &b, int alo, 
     if (x >= fbeg) {
       int k, j, i;
       kji(x, k, j, i);
-      face_flux<MINK, DIR>(p, b, k, j, i, prev_ql, qr);
+      face_flux<MINK, DIR>(p, b, k, j, i, prev_ql, qr, use_col ? &col : nullptr);
     }
 #pragma unroll
     for (int v = 0; v < PHX_NRECON; v++) prev_ql[v] = ql[v];
