@@ -351,7 +351,7 @@ def bench_batched(ctx, args, dev, learned_ready=False):
             res[name]["c2p_learned_accepted_frac"] = st["learned_accepted"] / st["zones"]
     ctx.check()
     nan = sum(int(torch.isnan(b["prim"][0]).sum()) for b in blocks)
-    del blocks, rk
+    del blocks, seconds, bases, stage2
     torch.cuda.empty_cache()
     from collections import Counter
 
