@@ -522,7 +522,11 @@ __device__ __forceinline__ double mp5_subcalc(double Fjm2, double Fjm1, double F
                                               double Fjp2) {
   constexpr double alpha = 4.0, epsm = 1.e-12;
   double f = 2.0 * Fjm2 - 13.0 * Fjm1 + 47.0 * Fj + 27.0 * Fjp1 - 3.0 * Fjp2;
+#ifdef PHX_EXACT
   f /= 60.0;
+#else
+  f *= 1.0 / 60.0;  // a product instead of the IEEE division (an ulp apart)
+#endif
   const double fMP = Fj + minmod(Fjp1 - Fj, alpha * (Fj - Fjm1));
   if ((f - Fj) * (f - fMP) <= epsm) return f;
   const double d2m = Fjm2 + Fj - 2.0 * Fjm1;

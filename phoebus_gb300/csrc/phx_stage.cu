@@ -116,11 +116,18 @@ __device__ __forceinline__ void update_at(const BView &b, const double *base, do
   const int k = (b.ndim >= 3 ? b.ng : 0) + (int)(t / ((long long)ni * nj));
   const long long id = b.idx(k, j, i);
   const long long dk = (long long)b.n1t * b.n2t, dj = b.n1t;
+#ifndef PHX_EXACT
+  const double iV = rcp_p(V);  // one reciprocal for the ncons divisions by the volume
+#endif
   for (int m = 0; m < ncons; m++) {
     double du = (A1 * FX(b, 0, m, id + 1) - A1 * FX(b, 0, m, id));
     if (b.ndim >= 2) du += A2 * FX(b, 1, m, id + dj) - A2 * FX(b, 1, m, id);
     if (b.ndim == 3) du += A3 * FX(b, 2, m, id + dk) - A3 * FX(b, 2, m, id);
+#ifdef PHX_EXACT
     double r = -du / V;
+#else
+    double r = -du * iV;
+#endif
     if (m >= 1 && m <= 4 && b.src != nullptr) r = r + b.src[(m - 1) * b.vs + id];
     const long long vid = m * b.vs + id;
     if (b.dudt != nullptr) b.dudt[vid] = r;
