@@ -141,7 +141,7 @@ __device__ __forceinline__ void floors_at(const Par &p, const BView &b, const Ra
       const double vp[3] = {pr[PHX_PVEL], pr[PHX_PVEL + 1], pr[PHX_PVEL + 2]};
       const double bb[3] = {pr[PHX_PB], pr[PHX_PB + 1], pr[PHX_PB + 2]};
       const double W = lorentz<MINK>(g, vp);
-      const double iW = 1.0 / W;
+      const double iW = rcp_p(W);
       double Bsq, Bdotv;
       if constexpr (MINK) {
         Bsq = bb[0] * bb[0] + bb[1] * bb[1] + bb[2] * bb[2];
@@ -156,11 +156,11 @@ __device__ __forceinline__ void floors_at(const Par &p, const BView &b, const Ra
           }
       }
       const double alpha = MINK ? 1.0 : g.alpha;
-      const double bcon0 = W * Bdotv / alpha;
+      const double bcon0 = div_p(W * Bdotv, alpha);
       const double bsq = (Bsq + alpha * alpha * bcon0 * bcon0) * iW * iW;
-      rho_floor_max = fmax(rho_floor_max, bsq / p.bsqorho0);
-      u_floor_max = fmax(u_floor_max, bsq / p.bsqou0);
-      rho_floor_max = fmax(rho_floor_max, fmax(pr[PHX_PENG], u_floor_max) / e_max);
+      rho_floor_max = fmax(rho_floor_max, div_p(bsq, p.bsqorho0));
+      u_floor_max = fmax(u_floor_max, div_p(bsq, p.bsqou0));
+      rho_floor_max = fmax(rho_floor_max, div_p(fmax(pr[PHX_PENG], u_floor_max), e_max));
     }
     drho = rho_floor_max - pr[PHX_PRHO];
     du = u_floor_max - pr[PHX_PENG];
@@ -225,7 +225,7 @@ __device__ __forceinline__ void floors_at(const Par &p, const BView &b, const Ra
   const double gamma_max = p.g0, e_max = p.smax0;
   double vpcon[3] = {pr[PHX_PVEL], pr[PHX_PVEL + 1], pr[PHX_PVEL + 2]};
   const double W = lorentz<MINK>(g, vpcon);
-  const bool ceiling_applied = (W > gamma_max || pr[PHX_PENG] / pr[PHX_PRHO] > e_max);
+  const bool ceiling_applied = (W > gamma_max || div_p(pr[PHX_PENG], pr[PHX_PRHO]) > e_max);
   if (ceiling_applied) {
     const double rescale = sqrt(gamma_max * gamma_max - 1.) / (W * W - 1.);
     for (int d = 0; d < 3; d++) {
