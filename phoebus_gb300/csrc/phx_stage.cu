@@ -265,13 +265,13 @@ __device__ __forceinline__ void sources_at(const Par &p, const BView &b, long lo
     double Bdotv = 0.0, Bsq = 0.0;
     for (int ii = 0; ii < 3; ii++)
       for (int jj = 0; jj < 3; jj++) {
-        Bdotv += bf[ii] * (vp[jj] / W) * g.gcov[ii + 1][jj + 1];
+        Bdotv += bf[ii] * div_p(vp[jj], W) * g.gcov[ii + 1][jj + 1];
         Bsq += bf[ii] * bf[jj] * g.gcov[ii + 1][jj + 1];
       }
-    const double iW = ratio(1., W);
+    const double iW = ratio_p(1., W);
     const double alpha = g.alpha;
     double u[4], bb[4];
-    u[0] = ratio(W, fabs(alpha));
+    u[0] = ratio_p(W, fabs(alpha));
     bb[0] = u[0] * Bdotv;
     for (int l = 1; l < 4; ++l) {
       u[l] = vp[l - 1] - u[0] * g.beta[l - 1];
@@ -282,8 +282,8 @@ __device__ __forceinline__ void sources_at(const Par &p, const BView &b, long lo
     {
       double alpha2 = g.alpha;
       alpha2 *= alpha2;
-      gi[0][0] = -ratio(1, alpha2);
-      for (int mu = 0; mu < 3; mu++) gi[mu + 1][0] = gi[0][mu + 1] = ratio(g.beta[mu], alpha2);
+      gi[0][0] = -ratio_p(1, alpha2);
+      for (int mu = 0; mu < 3; mu++) gi[mu + 1][0] = gi[0][mu + 1] = ratio_p(g.beta[mu], alpha2);
       for (int mu = 0; mu < 3; mu++)
         for (int nu = 0; nu < 3; nu++) {
           gi[mu + 1][nu + 1] = g.gamcon[mu][nu];
@@ -312,7 +312,7 @@ __device__ __forceinline__ void sources_at(const Par &p, const BView &b, long lo
       b.src[l * vs + id] = gdet * src_mom;
     }
     double TGam = 0.0;
-    const double inv_alpha2 = ratio(1, alpha * alpha);
+    const double inv_alpha2 = ratio_p(1, alpha * alpha);
     const double gcon0[4] = {-inv_alpha2, inv_alpha2 * g.beta[0], inv_alpha2 * g.beta[1], inv_alpha2 * g.beta[2]};
     for (int m = 0; m < 4; m++)
       for (int nn = 0; nn < 4; nn++) {
