@@ -509,6 +509,7 @@ __device__ __forceinline__ void c2p_finish(const Par &p, const Pt &g, Residual &
         bsq = bu[0] * bu[0] + bu[1] * bu[1] + bu[2] * bu[2];
         bdotv = bu[0] * vel[0] + bu[1] * vel[1] + bu[2] * vel[2];
       } else {
+#ifdef PHX_EXACT
         bdotv = 0.0;
 #pragma unroll
         for (int m = 0; m < 3; m++)
@@ -517,6 +518,12 @@ __device__ __forceinline__ void c2p_finish(const Par &p, const Pt &g, Residual &
             bsq += bu[m] * bu[n] * g.gcov[m + 1][n + 1];
             bdotv += bu[m] * vel[n] * g.gcov[m + 1][n + 1];
           }
+#else
+        double blo[3];  // lowered B serves both contractions
+        lower_sp(g, bu, blo);
+        bsq = dot3(bu, blo);
+        bdotv = dot3(vel, blo);
+#endif
       }
       bsq = iW * iW * bsq + bdotv * bdotv;
     }

@@ -259,18 +259,35 @@ __device__ __forceinline__ void load_pt_flat(const double *t, long long pitch, l
   p.detgam = __ldg(t + PHX_G_DETGAM * pitch + q);
 }
 
-// sum_{m,n} gcov[m+1][n+1] a[m] b[n], in the reference's loop order.
+// a_m = gamma_mn a^n (the spatial metric lowers a vector).
+__device__ __forceinline__ void lower_sp(const Pt &g, const double a[3], double out[3]) {
+#pragma unroll
+  for (int m = 0; m < 3; m++) out[m] = g.gcov[m + 1][1] * a[0] + g.gcov[m + 1][2] * a[1] + g.gcov[m + 1][3] * a[2];
+}
+__device__ __forceinline__ double dot3(const double a[3], const double b[3]) {
+  return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+
+// sum_{m,n} gcov[m+1][n+1] a[m] b[n]: the reference's nine-term loop in the
+// exact build; a . (gamma b) in the production build (12 FP64 instructions
+// instead of 18).
 template <bool MINK>
 __device__ __forceinline__ double dot_sp(const Pt &g, const double a[3], const double b[3]) {
   if constexpr (MINK) {
     return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
   } else {
+#ifdef PHX_EXACT
     double s = 0.0;
 #pragma unroll
     for (int m = 0; m < 3; m++)
 #pragma unroll
       for (int n = 0; n < 3; n++) s += g.gcov[m + 1][n + 1] * a[m] * b[n];
     return s;
+#else
+    double bl[3];
+    lower_sp(g, b, bl);
+    return dot3(a, bl);
+#endif
   }
 }
 
@@ -635,6 +652,7 @@ __device__ __forceinline__ void prim_to_flux(const Par &par, const Face &f, cons
     vsq = 0.0;
     Bdotv = 0.0;
     BdotB = 0.0;
+#ifdef PHX_EXACT
 #pragma unroll
     for (int m = 0; m < 3; m++)
 #pragma unroll
@@ -643,7 +661,20 @@ __device__ __forceinline__ void prim_to_flux(const Par &par, const Face &f, cons
         Bdotv += g.gcov[m + 1][n + 1] * Bcon[m] * vcon[n];
         BdotB += g.gcov[m + 1][n + 1] * Bcon[m] * Bcon[n];
       }
+#endif
   }
+#ifndef PHX_EXACT
+  // production build: the lowered v and B serve the three contractions here
+  // and the covariant momentum / field terms below
+  double vlo[3], Blo[3];
+  if constexpr (!MINK) {
+    lower_sp(g, vcon, vlo);
+    lower_sp(g, Bcon, Blo);
+    vsq = dot3(vcon, vlo);
+    Bdotv = dot3(Bcon, vlo);
+    BdotB = dot3(Bcon, Blo);
+  }
+#endif
 #ifdef PHX_EXACT
   const double vsq_max = 1.0 - 1.0 / (gam_max * gam_max);
 #else
@@ -656,6 +687,11 @@ __device__ __forceinline__ void prim_to_flux(const Par &par, const Face &f, cons
     Bdotv *= scale;
 #pragma unroll
     for (int m = 0; m < 3; m++) vcon[m] *= scale;
+#ifndef PHX_EXACT
+    if constexpr (!MINK)
+#pragma unroll
+      for (int m = 0; m < 3; m++) vlo[m] *= scale;
+#endif
   }
 #ifdef PHX_EXACT
   W = 1.0 / sqrt(1 - vsq);
@@ -704,15 +740,17 @@ __device__ __forceinline__ void prim_to_flux(const Par &par, const Face &f, cons
     } else {
 #ifdef PHX_EXACT
       bcovm = g.gcov[m + 1][0] * b0 / alpha;
-#else
-      bcovm = g.gcov[m + 1][0] * b0 * ialpha;
-#endif
       vcovm = 0.0;
 #pragma unroll
       for (int n = 1; n < 4; n++) {
         bcovm += g.gcov[m + 1][n] * (PHX_DIV_W(Bcon[n - 1]) + b0 * (vcon[n - 1] - PHX_BOA(n - 1)));
         vcovm += g.gcov[m + 1][n] * vcon[n - 1];
       }
+#else
+      // g_{m0} = gamma_mn beta^n: the shift terms cancel, b_m = B_m / W + b0 v_m
+      bcovm = Blo[m] * sW + b0 * vlo[m];
+      vcovm = vlo[m];
+#endif
     }
     U[PHX_CMOM + m] = (rhohWsq + bsqWsq) * vcovm - b0 * bcovm;
     F[PHX_CMOM + m] = U[PHX_CMOM + m] * vtil + ptot * (double)(DIR == m) - PHX_DIV_W(bcovm * Bcon[DIR]);
