@@ -258,6 +258,7 @@ __device__ __forceinline__ void sources_at(const Par &p, const BView &b, long lo
   } else {
     Pt g;
     load_pt(b, 0, j, i, g);
+#ifdef PHX_EXACT
     double vsqw = 0.;
     for (int ii = 0; ii < 3; ii++)
       for (int jj = 0; jj < 3; jj++) vsqw += g.gcov[ii + 1][jj + 1] * vp[ii] * vp[jj];
@@ -265,9 +266,17 @@ __device__ __forceinline__ void sources_at(const Par &p, const BView &b, long lo
     double Bdotv = 0.0, Bsq = 0.0;
     for (int ii = 0; ii < 3; ii++)
       for (int jj = 0; jj < 3; jj++) {
-        Bdotv += bf[ii] * div_p(vp[jj], W) * g.gcov[ii + 1][jj + 1];
+        Bdotv += bf[ii] * (vp[jj] / W) * g.gcov[ii + 1][jj + 1];
         Bsq += bf[ii] * bf[jj] * g.gcov[ii + 1][jj + 1];
       }
+#else
+    double vlo[3], blo[3];  // the lowered vectors serve the three contractions
+    lower_sp(g, vp, vlo);
+    lower_sp(g, bf, blo);
+    const double W = sqrt(1. + dot3(vp, vlo));
+    const double Bdotv = div_p(dot3(bf, vlo), W);
+    const double Bsq = dot3(bf, blo);
+#endif
     const double iW = ratio_p(1., W);
     const double alpha = g.alpha;
     double u[4], bb[4];
