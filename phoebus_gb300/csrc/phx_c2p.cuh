@@ -143,7 +143,7 @@ __device__ __forceinline__ bool c2p_setup(const Par &p, const Pt &g, const doubl
   const int num_nans = isnan(U[PHX_CRHO]) + isnan(U[PHX_CMOM]) + isnan(U[PHX_CENG]);
   if (num_nans > 0) return false;
   const double gdet = MINK ? 1.0 : g.detgam;
-  const double igdet = rcp_p(gdet);
+  const double igdet = MINK ? 1.0 : rcp_p(gdet);  // 1 / 1 = 1 in both builds
   double rhoflr = 0.0, epsflr;
   const FloorPt fl = floor_point(p, x1, x2, x3);
   floors_from(p, fl, rhoflr, epsflr);
@@ -151,20 +151,20 @@ __device__ __forceinline__ bool c2p_setup(const Par &p, const Pt &g, const doubl
   const double gam_max = p.g0;
   const double D = U[PHX_CRHO] * igdet;
   const double tau = U[PHX_CENG] * igdet;
-  const double q = ratio_p(tau, D);
   double bsq = 0.0, bsq_rpsq = 0.0, rbsq = 0.0, rsq;
   bdotr = 0.0;
 #ifdef PHX_EXACT
+  const double q = ratio_p(tau, D);
   rcov[0] = ratio(U[PHX_CMOM], U[PHX_CRHO]);
   rcov[1] = ratio(U[PHX_CMOM + 1], U[PHX_CRHO]);
   rcov[2] = ratio(U[PHX_CMOM + 2], U[PHX_CRHO]);
 #else
-  {
-    const double ic = ratio_p(1.0, U[PHX_CRHO]);
-    rcov[0] = U[PHX_CMOM] * ic;
-    rcov[1] = U[PHX_CMOM + 1] * ic;
-    rcov[2] = U[PHX_CMOM + 2] * ic;
-  }
+  // tau / D = U_tau / U_D: one reciprocal serves q and the three r_i
+  const double ic = ratio_p(1.0, U[PHX_CRHO]);
+  const double q = U[PHX_CENG] * ic;
+  rcov[0] = U[PHX_CMOM] * ic;
+  rcov[1] = U[PHX_CMOM + 1] * ic;
+  rcov[2] = U[PHX_CMOM + 2] * ic;
 #endif
   if constexpr (MINK) {
     rcon[0] = rcov[0];
@@ -185,7 +185,11 @@ __device__ __forceinline__ bool c2p_setup(const Par &p, const Pt &g, const doubl
   if (p.mhd) {
 #pragma unroll
     for (int ii = 0; ii < 3; ii++) Bprim[ii] = U[PHX_CB + ii] * igdet;
+#ifdef PHX_EXACT
     const double sD = rcp_p(sqrt(fmax(D, rhoflr)));
+#else
+    const double sD = rsqrt_p(fmax(D, rhoflr));
+#endif
 #pragma unroll
     for (int ii = 0; ii < 3; ii++) {
       bu[ii] = Bprim[ii] * sD;
