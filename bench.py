@@ -28,7 +28,7 @@ RK2 timestep per second.
   c2p        con2prim over 5e7 independent FMKS Kerr-Schild zones at tolerance
              1e-10: zones/s and root-find iterations with the reference's
              start (plain) and with the learned start (network trained on
-             the GPU on 1e7 separately seeded pairs before timing)
+             the GPU on 3e7 separately seeded pairs, 20 epochs, before timing)
 
 --impl reference runs the reference's CPU path (the oracle port) on the host
 cores: each step is one RK2 timestep of a 64^3 sample of the same state.
@@ -84,8 +84,8 @@ def parse():
     a.add_argument("--no-cpu", action="store_true")
     a.add_argument("--no-c2p", action="store_true", help="skip the con2prim learned-vs-plain section")
     a.add_argument("--c2p-zones", type=float, default=5e7)
-    a.add_argument("--train-pairs", type=float, default=1e7)
-    a.add_argument("--train-epochs", type=int, default=10)
+    a.add_argument("--train-pairs", type=float, default=3e7)
+    a.add_argument("--train-epochs", type=int, default=20)
     a.add_argument("--no-batched", action="store_true", help="skip the uneven-meshblock section")
     a.add_argument("--batched-blocks", type=int, default=1024)
     a.add_argument("--no-torus", action="store_true", help="skip the torus section")
