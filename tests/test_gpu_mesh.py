@@ -157,18 +157,19 @@ MESH_BCS = {
 }
 
 
-def small_fmks_mesh(bcs, n=26, lo=6, hi=12, bc_vars=abi.BC_VARS_PRIMITIVE):
+def small_fmks_mesh(bcs, n=26, lo=6, hi=12, bc_vars=abi.BC_VARS_PRIMITIVE, ndim=3):
     from phoebus_gb300.mesh import TiledMesh, split_axis
 
-    segs = [split_axis(n, lo, hi, torus.TORUS_SEED, 40 + d) for d in range(3)]
-    return TiledMesh((n, n, n), segs, (math.log(1.2), 0.0, 0.0), (math.log(250.0), 1.0, 2.0 * math.pi), *bcs,
-                     bc_vars=bc_vars)
+    segs = [split_axis(n, lo, hi, torus.TORUS_SEED, 40 + d) if d < ndim else [1] for d in range(3)]
+    return TiledMesh(tuple(n if d < ndim else 1 for d in range(3)), segs, (math.log(1.2), 0.0, 0.0),
+                     (math.log(250.0), 1.0, 2.0 * math.pi), *bcs, bc_vars=bc_vars, ndim=ndim)
 
 
+@pytest.mark.parametrize("ndim", [3, 2])
 @pytest.mark.parametrize("bc_vars", [abi.BC_VARS_PRIMITIVE, abi.BC_VARS_CONSERVED])
 @pytest.mark.parametrize("name", list(MESH_BCS))
 @pytest.mark.parametrize("geometry", ["fmks", "minkowski"])
-def test_mesh_exchange_matches_oracle(ctx_exact, name, geometry, bc_vars):
+def test_mesh_exchange_matches_oracle(ctx_exact, name, geometry, bc_vars, ndim):
     """Exact build: the exchange (neighbour copies, physical boundaries; with
     bc_vars = primitive the outer-X1 inflow check and prim2con in the boundary
     slabs, with bc_vars = conserved the DetGamma-scaled copies) equals the
@@ -183,7 +184,7 @@ def test_mesh_exchange_matches_oracle(ctx_exact, name, geometry, bc_vars):
     p = torus.torus_params()
     if bc_vars == abi.BC_VARS_CONSERVED:
         p.enable_ox1_fmks_inflow_check = 0
-    mesh = small_fmks_mesh(bcs, bc_vars=bc_vars)
+    mesh = small_fmks_mesh(bcs, bc_vars=bc_vars, ndim=ndim)
     geom = torus.torus_geometry() if geometry == "fmks" else None
     blocks = mesh.make_blocks("cuda", geom)
     for b in blocks:
