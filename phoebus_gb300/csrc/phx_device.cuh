@@ -464,22 +464,17 @@ __device__ __forceinline__ void recon_weno5z(double q0, double q1, double q2, do
 // on the exponents) the reference sequence is used.
 __device__ __forceinline__ void recon_weno5z_fast(double q0, double q1, double q2, double q3, double q4,
                                                   double &ql, double &qr) {
-  constexpr double a00 = 1.0 / 3.0, a01 = -7.0 / 6.0, a02 = 11.0 / 6.0;
-  constexpr double a10 = -1.0 / 6.0, a11 = 5.0 / 6.0, a12 = 1.0 / 3.0;
-  constexpr double a20 = 1.0 / 3.0, a21 = 5.0 / 6.0, a22 = -1.0 / 6.0;
   constexpr double g0 = 0.1, g1 = 0.6, g2 = 0.3;
   constexpr double eps = 1e-100;
   constexpr double t13 = 13.0 / 3.0;
-  // beta = 13/3 a^2 + b^2 + eps with eps folded into the b^2 product
-  double a = q0 - 2 * q1 + q2;
-  double b = q0 - 4.0 * q1 + 3.0 * q2;
-  const double beta0 = fma(t13 * a, a, fma(b, b, eps));
-  a = q1 - 2.0 * q2 + q3;
-  b = q3 - q1;
-  const double beta1 = fma(t13 * a, a, fma(b, b, eps));
-  a = q2 - 2.0 * q3 + q4;
-  b = q4 - 4.0 * q3 + 3.0 * q2;
-  const double beta2 = fma(t13 * a, a, fma(b, b, eps));
+  // second differences a_k and one-sided slopes b_k of the three stencils;
+  // beta_k = 13/3 a_k^2 + b_k^2 + eps with eps folded into the b^2 product
+  const double a0 = q0 - 2 * q1 + q2, b0 = q0 - 4.0 * q1 + 3.0 * q2;
+  const double a1 = q1 - 2.0 * q2 + q3, b1 = q3 - q1;
+  const double a2 = q2 - 2.0 * q3 + q4, b2 = q4 - 4.0 * q3 + 3.0 * q2;
+  const double beta0 = fma(t13 * a0, a0, fma(b0, b0, eps));
+  const double beta1 = fma(t13 * a1, a1, fma(b1, b1, eps));
+  const double beta2 = fma(t13 * a2, a2, fma(b2, b2, eps));
   const double tau5 = fabs(beta2 - beta0);
   const double b01 = beta0 * beta1;
   const double prod = b01 * beta2;
@@ -509,20 +504,23 @@ __device__ __forceinline__ void recon_weno5z_fast(double q0, double q1, double q
   wr0 *= isr;
   const double wm_r = wl1 * isr;
   wr2 *= isr;
-  ql = wl0 * (a00 * q0 + a01 * q1 + a02 * q2) + wm_l * (a10 * q1 + a11 * q2 + a12 * q3) +
-       wl2 * (a20 * q2 + a21 * q3 + a22 * q4);
-  qr = wr0 * (a00 * q4 + a01 * q3 + a02 * q2) + wm_r * (a10 * q3 + a11 * q2 + a12 * q1) +
-       wr2 * (a20 * q2 + a21 * q1 + a22 * q0);
-  const double Dl = g2 * wl0 * wm_l + g1 * wl0 * wl2 + g0 * wm_l * wl2;
-  const double Dr = g2 * wr0 * wm_r + g1 * wr0 * wr2 + g0 * wm_r * wr2;
+  // candidate values as q2 plus a twelfth of a_k +- 3 b_k: for ql (upper
+  // face) (a0 + 3 b0), (a1 + 3 b1), (a2 - 3 b2); for qr (lower face, the
+  // mirrored stencils) (a2 + 3 b2), (a1 - 3 b1), (a0 - 3 b0); the weights sum
+  // to one, so sum_k w_k c_k = q2 + sum_k w_k (c_k - q2)
+  ql = fma(wl0 * fma(3.0, b0, a0) + wm_l * fma(3.0, b1, a1) + wl2 * fma(-3.0, b2, a2), 1.0 / 12.0, q2);
+  qr = fma(wr0 * fma(3.0, b2, a2) + wm_r * fma(-3.0, b1, a1) + wr2 * fma(-3.0, b0, a0), 1.0 / 12.0, q2);
+  const double tl = wm_l * wl2, tr = wm_r * wr2;
+  const double Dl = fma(wl0, fma(g1, wl2, g2 * wm_l), g0 * tl);
+  const double Dr = fma(wr0, fma(g1, wr2, g2 * wm_r), g0 * tr);
   const double DD = Dl * Dr;
   if (dexp(DD) < 16) {
     recon_weno5z(q0, q1, q2, q3, q4, ql, qr);
     return;
   }
   const double rD = rcp_nr(DD);
-  const double alpha_l = 3.0 * wl0 * wm_l * wl2 * (Dr * rD) + eps;
-  const double alpha_r = 3.0 * wr0 * wm_r * wr2 * (Dl * rD) + eps;
+  const double alpha_l = fma(3.0 * wl0 * tl, Dr * rD, eps);
+  const double alpha_r = fma(3.0 * wr0 * tr, Dl * rD, eps);
   double dq = q3 - q2;
   dq = mc(q2 - q1, dq, 2.0);
   const double alpha_lin = 2.0 * alpha_l * alpha_r * rcp_nr(alpha_l + alpha_r);
