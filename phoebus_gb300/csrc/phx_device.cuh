@@ -624,16 +624,27 @@ __device__ __forceinline__ void prim_to_flux(const Par &par, const Face &f, cons
 #pragma unroll
     for (int ii = 0; ii < 3; ii++) vpcon[ii] *= rescale;
   }
+  const double qe = q[PHX_PENG];
 #ifdef PHX_EXACT
   double vcon[3] = {vpcon[0] / W, vpcon[1] / W, vpcon[2] / W};
   const double sie_q = q[PHX_PENG] / rho;
+  const bool above_floor = sie_q > sie_floor, above_max = sie_q > sie_max;
 #else
   double vcon[3] = {vpcon[0] * iW0, vpcon[1] * iW0, vpcon[2] * iW0};
-  const double sie_q = q[PHX_PENG] * rcp_p(rho);
+  // u / rho > s as u > rho s for rho > 0 (no reciprocal; the products are the
+  // bounded energies anyway); the quotient only where rho <= 0
+  bool above_floor, above_max;
+  if (rho > 0.0) {
+    above_floor = qe > rho * sie_floor;
+    above_max = qe > rho * sie_max;
+  } else {
+    const double sie_q = qe * rcp_p(rho);
+    above_floor = sie_q > sie_floor;
+    above_max = sie_q > sie_max;
+  }
 #endif
   double Bcon[3] = {0.0, 0.0, 0.0};
-  const double qe = q[PHX_PENG];
-  const double u = (sie_q > sie_floor ? (sie_q > sie_max ? rho * sie_max : qe) : rho * sie_floor);
+  const double u = (above_floor ? (above_max ? rho * sie_max : qe) : rho * sie_floor);
   const double P = fmax(q[PHX_PPRS], 0.0);
   const double gamma1 = q[PHX_PGM1];
   if (par.mhd) {
@@ -769,8 +780,20 @@ __device__ __forceinline__ void prim_to_flux(const Par &par, const Face &f, cons
   const double vasq = bsqWsq / make_positive(rhohWsq + bsqWsq);
   const double cssq = make_bounded(gamma1 * P * W * W / make_positive(rhohWsq), 0.0, 1.0);
 #else
-  const double vasq = bsqWsq * rcp_p(make_positive(rhohWsq + bsqWsq));
-  const double cssq = make_bounded(gamma1 * P * W * W * rcp_p(make_positive(rhohWsq)), 0.0, 1.0);
+  // one reciprocal of the product of the two denominators when it is normal
+  const double dA = make_positive(rhohWsq + bsqWsq), dB = make_positive(rhohWsq);
+  const double dAB = dA * dB;
+  const int eAB = dexp(dAB);
+  double vasq, cs_raw;
+  if (eAB >= 16 && eAB <= 2030) {
+    const double rAB = rcp_nr(dAB);
+    vasq = bsqWsq * (dB * rAB);
+    cs_raw = gamma1 * P * W * W * (dA * rAB);
+  } else {
+    vasq = bsqWsq * rcp_p(dA);
+    cs_raw = gamma1 * P * W * W * rcp_p(dB);
+  }
+  const double cssq = make_bounded(cs_raw, 0.0, 1.0);
 #endif
   const double cmsq = make_bounded(cssq + vasq * (1.0 - cssq), 0.0, 1.0);
   const double vcoff = div_p(alpha, 1.0 - vsq * cmsq);

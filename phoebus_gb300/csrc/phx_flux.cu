@@ -62,7 +62,7 @@ __device__ __forceinline__ void face_flux(const Par &p, const BView &b, int k, i
     const double cl = fmin(fmin(vml, vmr), 0.0);
     const double cr = fmax(fmax(vpl, vpr), 0.0);
     const double crcl = cr * cl;
-    const double inv_cr_cl = ratio(1.0, cr - cl);
+    const double inv_cr_cl = ratio_p(1.0, cr - cl);
 #pragma unroll
     for (int m = 0; m < PHX_NCONS; m++)
       if (m < ncons)
