@@ -79,7 +79,8 @@ struct Residual {
     double e_floor;
     floors_from(p, fl, rho, e_floor);
     e_floor *= p.fsf;
-    const double ehat_trial = What * (qbar - mu * rbarsq) + vhatsq * What * ratio_p(What, 1.0 + What);
+    // What = 1 / sqrt(1 - vhatsq): vhatsq What^2 / (1 + What) = What - 1
+    const double ehat_trial = fma(What, qbar - mu * rbarsq, What - 1.0);
     used_energy_floor = false;
     used_energy_max = false;
     if (ehat_trial <= e_floor) {
