@@ -112,20 +112,11 @@ struct Residual {
 #endif
     const double Phat = eos_P_rho_sie(p, rhohat, ehat);
     const double hhat = rhohat * (1.0 + ehat) + Phat;
-#ifdef PHX_EXACT
     const double ahat = div_p(Phat, make_positive(hhat - Phat));
     const double nua = (1.0 + ahat) * (1.0 + ehat) * iWhat;
     const double nub = (1.0 + ahat) * (1.0 + qbar - mu * rbarsq);
     const double nuhat = fmax(nua, nub);
     const double muhat = rcp_p(nuhat + mu * rbarsq);
-#else
-    // 1 + ahat = (d + P) / d > 0 factors out of the max, and its reciprocal
-    // joins the final one: muhat = d / ((d + P) max(..) + mu rbar^2 d)
-    const double d = make_positive(hhat - Phat);
-    const double mr = mu * rbarsq;
-    const double M = fmax((1.0 + ehat) * iWhat, 1.0 + qbar - mr);
-    const double muhat = d * rcp_p(fma(d + Phat, M, mr * d));
-#endif
     return mu - muhat;
   }
   __device__ __forceinline__ bool used_bounds() const {
