@@ -474,7 +474,11 @@ __device__ __forceinline__ void c2p_finish(const Par &p, const Pt &g, Residual &
 #endif
   prim[PHX_PRHO] = res.rhohat_mu(iW);
   const double qbar = res.qbar_mu(mu, x);
+#ifdef PHX_EXACT
   double eng = res.ehat_mu(p, mu, qbar, rbarsq, vsq, W);
+#else
+  double eng = res.ehat_mu_iw(p, mu, qbar, rbarsq, vsq, W, iW);  // 1/W known
+#endif
   prim[PHX_PTMP] = eos_T_rho_sie(p, prim[PHX_PRHO], eng);
   eng *= prim[PHX_PRHO];
   prim[PHX_PENG] = eng;

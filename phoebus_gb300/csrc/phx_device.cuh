@@ -799,7 +799,12 @@ __device__ __forceinline__ void prim_to_flux(const Par &par, const Face &f, cons
   const double vcoff = div_p(alpha, 1.0 - vsq * cmsq);
   const double v0 = vel * (1.0 - cmsq);
   const double gdd = MINK ? 1.0 : f.gdd;
+#ifdef PHX_EXACT
   const double vpm = sqrt(make_positive(cmsq * (1.0 - vsq) * (gdd * (1.0 - vsq * cmsq) - vel * v0)));
+#else
+  const double vpm_sq = make_positive(cmsq * (1.0 - vsq) * (gdd * (1.0 - vsq * cmsq) - vel * v0));
+  const double vpm = vpm_sq * rsqrt_p(vpm_sq);  // vpm_sq >= 10 DBL_EPSILON > 0
+#endif
   vp = vcoff * (v0 + vpm);
   vm = vcoff * (v0 - vpm);
   if constexpr (!MINK) {
