@@ -63,10 +63,18 @@ __device__ __forceinline__ void face_flux(const Par &p, const BView &b, int k, i
     const double cr = fmax(fmax(vpl, vpr), 0.0);
     const double crcl = cr * cl;
     const double inv_cr_cl = ratio_p(1.0, cr - cl);
+#ifdef PHX_EXACT
 #pragma unroll
     for (int m = 0; m < PHX_NCONS; m++)
       if (m < ncons)
         fx[m * b.vs] = ((cr * Fl[m] - cl * Fr[m]) * gdet + crcl * (Ur[m] - Ul[m]) * gammadet) * inv_cr_cl;
+#else
+    // the per-face factors formed once: F_l cr' - F_r cl' + (U_r - U_l) c'
+    const double crg = cr * gdet * inv_cr_cl, clg = cl * gdet * inv_cr_cl, cc = crcl * gammadet * inv_cr_cl;
+#pragma unroll
+    for (int m = 0; m < PHX_NCONS; m++)
+      if (m < ncons) fx[m * b.vs] = fma(crg, Fl[m], fma(-clg, Fr[m], cc * (Ur[m] - Ul[m])));
+#endif
     sig = fmax(-cl, cr);
   }
   b.face_sig[(long long)DIR * b.vs + id] = sig;
