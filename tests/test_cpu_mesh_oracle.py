@@ -112,3 +112,21 @@ def test_face_by_face_equals_composed_maps(name, bc_vars, ndim):
         assert not np.isnan(b["cons"]).any(), f"block {n}: a ghost no rule filled"
         np.testing.assert_array_equal(b["prim"], P, err_msg=f"block {n} prim")
         np.testing.assert_array_equal(b["cons"], U, err_msg=f"block {n} cons")
+
+
+def test_split_axis_covers_the_axis_in_range():
+    """Segment draws cover n exactly with lengths in [lo, hi] whenever such a
+    split exists (a draw that would leave an unsplittable remainder is
+    replaced)."""
+    from phoebus_gb300.mesh import split_axis
+
+    for lo, hi in [(6, 12), (8, 12), (16, 32), (32, 96)]:
+        for n in range(lo, 6 * hi + 2, 2):
+            possible = -(-n // hi) <= n // lo
+            for stream in range(4):
+                if possible:
+                    lens = split_axis(n, lo, hi, 1234, stream)
+                    assert sum(lens) == n and all(lo <= x <= hi and x % 2 == 0 for x in lens), (n, lo, hi, lens)
+                else:
+                    with pytest.raises((AssertionError, ValueError)):
+                        split_axis(n, lo, hi, 1234, stream)
