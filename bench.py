@@ -91,6 +91,10 @@ def parse():
     a.add_argument("--no-torus", action="store_true", help="skip the torus section")
     a.add_argument("--torus-n", type=int, default=384)
     a.add_argument("--torus-steps", type=int, default=2)
+    a.add_argument("--no-m1", action="store_true", help="skip the radiation M1 section")
+    a.add_argument("--m1-n", type=int, default=128)
+    a.add_argument("--m1-steps", type=int, default=3)
+    a.add_argument("--m1-cpu-n", type=int, default=48)
     return a.parse_args()
 
 
@@ -444,6 +448,103 @@ def bench_torus(ctx, args, dev, learned_ready=False):
     return out
 
 
+def bench_m1(ctx, args, dev):
+    """Radiation M1 moments (phx_radiation.h): an m1_n^3 periodic Minkowski
+    block in the regime of the radiation_diffusion regression (gray
+    scattering, optical depth 2 per zone, uniform fluid velocity 0.3 c, weak
+    absorption), linear reconstruction.  RK2 steps of phx_rad_stage (opacities,
+    fluxes, update, con2prim, implicit source, ghost exchange, con2prim) plus
+    the radiation timestep estimate, timed with CUDA events; the per-task
+    split is a separate pass with events around each task.  The oracle times
+    the same step on an m1_cpu_n^3 sample on all host cores."""
+    import numpy as np
+    import torch
+
+    from phoebus_gb300 import abi, radiation
+
+    rc = radiation.RadiationContext(ctx)
+    hb, par, rpar = radiation.radiation_pulse_3d(n=args.m1_n)
+    p, rp = abi.default_params(**par), abi.default_rad_params(**rpar)
+    db = hb.to_device(dev)
+    del hb
+    rc.MomentPrim2Con(rp, p, db)
+    rc.Initialize(rp, p, db)
+    rc.MomentCalculateOpacities(rp, p, db)
+    dt = rc.EstimateTimestepBlock(rp, p, db)
+    buf = torch.zeros_like(db["rcons"])
+    dt_dev = torch.empty(1, dtype=torch.float64, device=dev)
+
+    def step():
+        rc.rk2_step(rp, p, db, buf, dt)
+        rc.EstimateTimestepBlock(rp, p, db, out=dt_dev)
+
+    for _ in range(max(1, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.m1_steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.m1_steps
+    zones = args.m1_n ** 3
+    # per-task split of one stage (same launches as phx_rad_stage)
+    base, out = db["rcons"].clone(), buf
+    tasks = [("opacities", lambda: rc.MomentCalculateOpacities(rp, p, db)),
+             ("fluxes", lambda: rc.CalculateFluxes(rp, p, db)),
+             ("update", lambda: rc.Update(rp, db, base, out, 1.0, dt)),
+             ("con2prim_interior", lambda: rc.MomentCon2Prim(rp, p, db, *db.interior())),
+             ("fluid_source", lambda: rc.MomentFluidSource(rp, p, db, dt)),
+             ("ghost_exchange", lambda: rc.FillGhostsPeriodic(db)),
+             ("con2prim_entire", lambda: rc.MomentCon2Prim(rp, p, db))]
+    split = {}
+    for name, fn in tasks:
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        split[name] = a.elapsed_time(b)
+    ctx.check()
+    J = db["rprim"][abi.RJ][db.isl()]
+    res = {"workload": f"M1 radiation, {args.m1_n}^3 periodic Minkowski block, gray scattering kappa dx = 2, "
+                       "kappa_a = 1, fluid u = W (0.3, 0, 0), Gaussian J pulse, linear reconstruction; one RK2 "
+                       "step (2 stages + timestep estimate) per step",
+           "zone_updates_per_s": zones / (ms * 1e-3), "ms_per_step": ms, "steps": args.m1_steps,
+           "stage_split_ms": split, "nan_J": int(torch.isnan(J).sum()),
+           "c2p_fail_zones": int((db["rprim"][abi.RFAIL][db.isl()] != 1.0).sum()),
+           "gpu_launches_per_step": 2 * (4 + 3 + 2 + 1) + 3}
+    del db, buf, base
+    torch.cuda.empty_cache()
+    if not args.no_cpu:
+        from oracle.oracle import RadOracle
+
+        os.environ["OMP_NUM_THREADS"] = str(os.cpu_count() or 1)
+        o = RadOracle()
+        hb, par, rpar = radiation.radiation_pulse_3d(n=args.m1_cpu_n)
+        p, rp = abi.default_params(**par), abi.default_rad_params(**rpar)
+        o.MomentPrim2Con(rp, p, hb)
+        o.Initialize(rp, p, hb)
+        o.MomentCalculateOpacities(rp, p, hb)
+        hdt = o.EstimateTimestepBlock(rp, p, hb)
+        hbuf = np.zeros_like(hb["rcons"])
+        o.rk2_step(rp, p, hb, hbuf, hdt)
+        times = []
+        for _ in range(2):
+            t0 = time.perf_counter()
+            o.rk2_step(rp, p, hb, hbuf, hdt)
+            o.EstimateTimestepBlock(rp, p, hb)
+            times.append(time.perf_counter() - t0)
+        t = min(times)
+        res["cpu_baseline"] = {"value": args.m1_cpu_n ** 3 / t, "unit": UNIT, "cores": os.cpu_count() or 1,
+                               "kind": "port", "sample": f"oracle RK2 step on a {args.m1_cpu_n}^3 sample of the "
+                                                         f"same state ({t:.2f} s/step)"}
+        res["gpu_over_cpu"] = res["zone_updates_per_s"] / res["cpu_baseline"]["value"]
+    return res
+
+
 def cpu_baseline(args, threads):
     """Oracle RK2 timestep on a cpu_n^3 sample of the workload."""
     import numpy as np
@@ -667,6 +768,7 @@ def main():
     c2p = None if args.no_c2p else bench_c2p(ctx, args, dev)
     batched = None if args.no_batched else bench_batched(ctx, args, dev, learned_ready=c2p is not None)
     torus_res = None if args.no_torus else bench_torus(ctx, args, dev, learned_ready=not args.no_c2p)
+    m1_res = None if args.no_m1 else bench_m1(ctx, args, dev)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
@@ -693,6 +795,7 @@ def main():
             "c2p": c2p,
             "batched": batched,
             "torus": torus_res,
+            "m1": m1_res,
             "cpu_baseline": cpu,
             "clocks": clocks,
             "e2e": e2e,

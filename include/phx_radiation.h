@@ -1,0 +1,162 @@
+/*
+ * phx_radiation.h -- C ABI of the GB300 (sm_103a) radiation moment (M1 /
+ * Eddington) transport of phoebus.
+ *
+ * Each entry point replaces one task of the reference's radiation package
+ * (src/radiation/moments.cpp, moments_source.cpp, radiation.cpp; paths
+ * relative to the phoebus source tree) for the "moment_m1" and
+ * "moment_eddington" methods with one neutrino species, on a Minkowski block
+ * with a static fluid background (physics/hydro = false; the reference then
+ * calls MomentFluidSource with update_fluid = false).
+ *
+ * Conventions are those of phx_fluid.h: caller-owned device memory, FP64,
+ * structure of arrays with i fastest, ghost-inclusive inclusive ranges, every
+ * call asynchronous on the given stream, no allocation inside a call.  The
+ * fluid block (phx_block) supplies the mesh, the coordinates and the fluid
+ * primitives the moments read (density, W v^i, internal energy,
+ * temperature); the radiation fields live in a phx_rad_block.
+ */
+#ifndef PHX_RADIATION_H_
+#define PHX_RADIATION_H_
+
+#include "phx_fluid.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Conserved radiation moments (cons[PHX_RNCONS][N]), densitised by
+ * sqrt(gamma), in the reference's flux order.  Like the fluid's conserved
+ * variables they have one copy per RK stage container. */
+enum {
+  PHX_RE = 0,  /* sqrt(gamma) E                 */
+  PHX_RF = 1,  /* sqrt(gamma) F_i (3 entries)   */
+  PHX_RNCONS = 4
+};
+/* Radiation fields with a single copy shared by all stage containers
+ * (Metadata::OneCopy in radiation.cpp:471-520): prim[PHX_RNPRIM][N]. */
+enum {
+  PHX_RJ = 0,       /* J, fluid-frame energy density (radmoment_prim::J)        */
+  PHX_RH = 1,       /* H_i / J (3 entries; radmoment_prim::H stores the ratio)  */
+  PHX_RXI = 4,      /* closure guess xi = |H| / J (radmoment_internal::xi)      */
+  PHX_RPHI = 5,     /* closure guess phi (radmoment_internal::phi)              */
+  PHX_RFAIL = 6,    /* c2pfail: 1.0 success, 0.0 failure                        */
+  PHX_RKAPPAJ = 7,  /* absorption coefficient (radmoment_internal::kappaJ)      */
+  PHX_RKAPPAH = 8,  /* total coefficient (radmoment_internal::kappaH)           */
+  PHX_RJBB = 9,     /* black-body energy density (radmoment_internal::JBB)      */
+  PHX_RNPRIM = 10
+};
+
+typedef enum { PHX_RAD_M1 = 0, PHX_RAD_EDDINGTON = 1 } phx_rad_method; /* radiation.cpp:51-59 */
+
+typedef enum { /* radiation.hpp OneDFixupStrategy, radiation.cpp:432-445 */
+  PHX_RAD_ONED_FIXUP_NONE = 0,
+  PHX_RAD_ONED_FIXUP_IGNORE_DJ = 1,
+  PHX_RAD_ONED_FIXUP_IGNORE_ALL = 2
+} phx_rad_oned_fixup;
+
+/* Radiation package Params (radiation.cpp:340-450) and the radiation
+ * bounds of the fixup package (fixup.cpp:75-76, 188-215).  Fill with
+ * phx_rad_params_default() and override. */
+typedef struct {
+  int method;                 /* phx_rad_method                           */
+  int recon;                  /* phx_recon; reference default: linear    */
+  double cfl;                 /* radiation/cfl (default 0.8)             */
+  int closure_frail;          /* closure_c2p_strategy: 0 robust, 1 frail */
+  int recon_fixup_bounds;     /* recon_fixup_strategy: 1 bounds, 0 none  */
+  double src_rootfind_tol;    /* radiation/src_rootfind_tol (1e-12)      */
+  int src_rootfind_maxiter;   /* radiation/src_rootfind_maxiter (100)    */
+  int oned_fixup_strategy;    /* phx_rad_oned_fixup                      */
+  /* Gray opacities in the run's code units.  kappaJ = rho kappa_a,
+   * kappaH = kappaJ + rho kappa_s, JBB = jbb_coeff T^4.  The reference takes
+   * Rosseland means from singularity-opac tables; for gray opacities they
+   * are these constants. */
+  double kappa_a, kappa_s, jbb_coeff;
+  /* fixup/enable_rad_floors with rad_floor_type ConstantJ, and
+   * fixup/enable_rad_ceilings with ConstantXi0 */
+  int enable_rad_floors;
+  double J0_floor;
+  int enable_rad_ceilings;
+  double xi0_ceiling, tau0_ceiling;
+  /* 0: the fluid is not evolved (physics/hydro = false).  1 is the coupled
+   * fluid update of MomentFluidSource and is not built. */
+  int update_fluid;
+} phx_rad_params;
+
+/* Radiation fields of one block.  Same shape and var_stride convention as
+ * the fluid block it is paired with (var_stride 0 = the block's cell count). */
+typedef struct {
+  long long var_stride;
+  double *cons; /* [PHX_RNCONS][N]  stage input E, F_i (the reference's sc0) */
+  double *prim; /* [PHX_RNPRIM][N]                                          */
+  double *flux; /* [3][PHX_RNCONS][N]  flux(d, m, k, j, i)                  */
+  double *dudt; /* [PHX_RNCONS][N]     right-hand side (scratch)            */
+} phx_rad_block;
+
+void phx_rad_params_default(phx_rad_params *p);
+
+/* radiation::MomentPrim2Con (moments.cpp:198-275): E, F_i from J, H_i/J and
+ * the fluid velocity over the range. */
+phx_status phx_rad_prim_to_con(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_block *fb,
+                               const phx_rad_block *rb, phx_range ib, phx_range jb, phx_range kb, void *stream);
+
+/* radiation::MomentCon2Prim (moments.cpp:61-192): the closure solve from the
+ * stored xi guess, then J, H_i/J, xi, phi, c2pfail (and E, F_i when the
+ * robust inversion modified the state) over the range. */
+phx_status phx_rad_con_to_prim(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_block *fb,
+                               const phx_rad_block *rb, phx_range ib, phx_range jb, phx_range kb, void *stream);
+
+/* radiation::MomentCalculateOpacities (moments.cpp:919-995): kappaJ, kappaH,
+ * JBB over the entire block. */
+phx_status phx_rad_calculate_opacities(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p,
+                                       const phx_block *fb, const phx_rad_block *rb, void *stream);
+
+/* radiation::ReconstructEdgeStates + radiation::CalculateFluxes
+ * (moments.cpp:280-736), fused: flux of E and F_i on every face the
+ * interior update reads. */
+phx_status phx_rad_calculate_fluxes(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p,
+                                    const phx_block *fb, const phx_rad_block *rb, void *stream);
+
+/* Parthenon FluxDivergence + SumData (the Minkowski geometric source of
+ * CalculateGeometricSource, moments.cpp:756-885, is zero) +
+ * AverageIndependentData + UpdateIndependentData on E, F_i (interior):
+ *   cons = beta cons + (1 - beta) base;  out = cons + beta dt dudt.
+ * base and out are [PHX_RNCONS][N] arrays with the block's var_stride. */
+phx_status phx_rad_update(phx_ctx *ctx, const phx_rad_params *rp, const phx_block *fb, const phx_rad_block *rb,
+                          const double *base, double *out, double beta, double dt, void *stream);
+
+/* radiation::MomentFluidSource with the "oned" source solver and
+ * update_fluid = false (moments_source.cpp:203-490, 786-958): the implicit
+ * absorption/scattering update of E, F_i over dt, then the frail closure
+ * inversion that sets J, H_i/J (or the failure state). */
+phx_status phx_rad_fluid_source(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_block *fb,
+                                const phx_rad_block *rb, double dt, void *stream);
+
+/* Periodic ghost exchange of the radiation fields (E, F_i, J, H_i, xi, phi,
+ * c2pfail: every radiation field with Metadata::FillGhost) of a block that
+ * is periodic on every active axis. */
+phx_status phx_rad_fill_ghosts_periodic(phx_ctx *ctx, const phx_block *fb, const phx_rad_block *rb, void *stream);
+
+/* radiation::EstimateTimestepBlock (radiation.cpp:681-733): cfl * the
+ * minimum over interior zones and active directions of dx / csig, written to
+ * dt_out_device. */
+phx_status phx_rad_estimate_timestep(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p,
+                                     const phx_block *fb, const phx_rad_block *rb, double *dt_out_device,
+                                     void *stream);
+
+/* One RK stage of the moment transport on a periodic block, in the task
+ * order of PhoebusDriver::RungeKuttaStage with hydro off
+ * (phoebus_driver.cpp:349-362, 547-620, 640-668): opacities, fluxes,
+ * update into out, con2prim, fluid source (beta dt), ghost exchange,
+ * con2prim.  rb->cons is the stage input (the reference's sc0), base the
+ * step's initial state, out the stage output (sc1); everything after the
+ * update acts on out and the shared prim fields. */
+phx_status phx_rad_stage(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_block *fb,
+                         const phx_rad_block *rb, const double *base, double *out, double beta, double dt,
+                         void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PHX_RADIATION_H_ */

@@ -29,8 +29,8 @@ SRC = ROOT / "oracle" / "phx_oracle.cpp"
 
 def build(force: bool = False) -> Path:
     LIB.parent.mkdir(exist_ok=True)
-    hdr = ROOT / "include" / "phx_fluid.h"
-    if force or not LIB.exists() or LIB.stat().st_mtime < max(SRC.stat().st_mtime, hdr.stat().st_mtime):
+    hdrs = [ROOT / "include" / "phx_fluid.h", ROOT / "include" / "phx_radiation.h"]
+    if force or not LIB.exists() or LIB.stat().st_mtime < max([SRC.stat().st_mtime] + [h.stat().st_mtime for h in hdrs]):
         subprocess.run(["g++", "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-o",
                         str(LIB), str(SRC)], check=True)
     return LIB
@@ -79,6 +79,20 @@ def lib() -> C.CDLL:
         L.orc_c2p_features_zones.restype = None
         L.orc_fmks_points.argtypes = [C.POINTER(abi.Geometry), C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_fmks_points.restype = None
+        RP, PP, BS, RB = C.POINTER(abi.RadParams), C.POINTER(abi.Params), C.POINTER(abi.BlockS), C.POINTER(abi.RadBlockS)
+        for name, args, res in [
+            ("orc_rad_prim_to_con", [RP, PP, BS, RB, abi.Range, abi.Range, abi.Range], None),
+            ("orc_rad_con_to_prim", [RP, PP, BS, RB, abi.Range, abi.Range, abi.Range], None),
+            ("orc_rad_calculate_opacities", [RP, PP, BS, RB], None),
+            ("orc_rad_calculate_fluxes", [RP, PP, BS, RB], None),
+            ("orc_rad_update", [RP, BS, RB, C.c_void_p, C.c_void_p, C.c_double, C.c_double], None),
+            ("orc_rad_fluid_source", [RP, PP, BS, RB, C.c_double], C.c_longlong),
+            ("orc_rad_fill_ghosts_periodic", [BS, RB], None),
+            ("orc_rad_estimate_timestep", [RP, PP, BS, RB], C.c_double),
+            ("orc_rad_tanh", [C.c_double], C.c_double),
+        ]:
+            fn = getattr(L, name)
+            fn.argtypes, fn.restype = args, res
         _lib = L
     return _lib
 
@@ -253,3 +267,85 @@ class Oracle:
         b.arrays["cons"] = cons_stage
         self.Stage(p, b, base, base, 0.5, dt, exchange)
         b.arrays["cons"] = base
+
+
+class RadOracle:
+    """The reference's radiation moment tasks on host Blocks (numpy arrays
+    "prim" ... and "rcons", "rprim", "rflux", "rdudt"), in the order of
+    phoebus_gb300.radiation.RadiationContext."""
+
+    def __init__(self):
+        self.L = lib()
+
+    @staticmethod
+    def _s(b: Block, cons=None):
+        from phoebus_gb300.radiation import rad_struct
+
+        return b.struct(), rad_struct(b, cons)
+
+    def MomentPrim2Con(self, rp, p, b: Block, ib=None, jb=None, kb=None):
+        e = b.interior()
+        s, r = self._s(b)
+        self.L.orc_rad_prim_to_con(C.byref(rp), C.byref(p), C.byref(s), C.byref(r), _r(ib or e[0]), _r(jb or e[1]),
+                                   _r(kb or e[2]))
+
+    def MomentCon2Prim(self, rp, p, b: Block, ib=None, jb=None, kb=None):
+        e = b.entire()
+        s, r = self._s(b)
+        self.L.orc_rad_con_to_prim(C.byref(rp), C.byref(p), C.byref(s), C.byref(r), _r(ib or e[0]), _r(jb or e[1]),
+                                   _r(kb or e[2]))
+
+    def MomentCalculateOpacities(self, rp, p, b: Block):
+        s, r = self._s(b)
+        self.L.orc_rad_calculate_opacities(C.byref(rp), C.byref(p), C.byref(s), C.byref(r))
+
+    def CalculateFluxes(self, rp, p, b: Block):
+        s, r = self._s(b)
+        self.L.orc_rad_calculate_fluxes(C.byref(rp), C.byref(p), C.byref(s), C.byref(r))
+
+    def Update(self, rp, b: Block, base, out, beta, dt):
+        s, r = self._s(b)
+        self.L.orc_rad_update(C.byref(rp), C.byref(s), C.byref(r), base.ctypes.data, out.ctypes.data, beta, dt)
+
+    def MomentFluidSource(self, rp, p, b: Block, dt) -> int:
+        s, r = self._s(b)
+        return self.L.orc_rad_fluid_source(C.byref(rp), C.byref(p), C.byref(s), C.byref(r), dt)
+
+    def FillGhostsPeriodic(self, b: Block):
+        s, r = self._s(b)
+        self.L.orc_rad_fill_ghosts_periodic(C.byref(s), C.byref(r))
+
+    def EstimateTimestepBlock(self, rp, p, b: Block) -> float:
+        s, r = self._s(b)
+        return self.L.orc_rad_estimate_timestep(C.byref(rp), C.byref(p), C.byref(s), C.byref(r))
+
+    def tanh(self, x: float) -> float:
+        return self.L.orc_rad_tanh(x)
+
+    def Initialize(self, rp, p, b: Block):
+        self.FillGhostsPeriodic(b)
+        self.MomentCon2Prim(rp, p, b)
+
+    def Stage(self, rp, p, b: Block, base, out, beta, dt):
+        """PhoebusDriver::RungeKuttaStage with the fluid not evolved
+        (phoebus_driver.cpp:349-362, 547-620, 640-668): opacities, fluxes,
+        update into out, con2prim, the implicit source over beta dt, ghost
+        exchange, con2prim.  b['rcons'] is the stage input."""
+        self.MomentCalculateOpacities(rp, p, b)
+        self.CalculateFluxes(rp, p, b)
+        self.Update(rp, b, base, out, beta, dt)
+        cons_in = b.arrays["rcons"]
+        b.arrays["rcons"] = out
+        ib, jb, kb = b.interior()
+        self.MomentCon2Prim(rp, p, b, ib, jb, kb)
+        self.MomentFluidSource(rp, p, b, beta * dt)
+        self.FillGhostsPeriodic(b)
+        self.MomentCon2Prim(rp, p, b)
+        b.arrays["rcons"] = cons_in
+
+    def rk2_step(self, rp, p, b: Block, stage_buf, dt):
+        base = b.arrays["rcons"]
+        self.Stage(rp, p, b, base, stage_buf, 1.0, dt)
+        b.arrays["rcons"] = stage_buf
+        self.Stage(rp, p, b, base, base, 0.5, dt)
+        b.arrays["rcons"] = base

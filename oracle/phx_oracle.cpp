@@ -33,6 +33,7 @@
 #include <vector>
 
 #include "../include/phx_fluid.h"
+#include "../include/phx_radiation.h"
 
 namespace orc {
 
@@ -1905,5 +1906,935 @@ void orc_c2p_fixup(const phx_params *par, const phx_block *blk) { c2p_fixup(*par
 long long orc_apply_floors(const phx_params *par, const phx_block *blk, phx_range ib, phx_range jb, phx_range kb) {
   return apply_floors(*par, blk, ib, jb, kb);
 }
+
+}  // extern "C"
+
+// =====================================================================
+// Radiation moments (M1 and Eddington closures), Minkowski, one species,
+// static fluid background.  Restates radiation/closure.hpp:49-352,
+// closure_m1.hpp:31-372, local_three_geometry.hpp:140-185, moments.cpp:61-995,
+// moments_source.cpp:152-958 (oned solver, update_fluid = false),
+// radiation.cpp:681-733, linear_algebra.hpp:58-96 and root_find.hpp:20-160.
+// Minkowski: the spatial metric is the identity, lapse 1, shift 0.  Each
+// contraction keeps the reference's order over its non-zero terms; for finite
+// values the zero terms of the full 3x3 sums change no rounding.
+// Third-party semantics restated from their definitions: gray opacities
+// (kappaJ = rho kappa_a, kappaH = kappaJ + rho kappa_s, JBB = a T^4; the
+// Rosseland means of a gray opacity are the gray values) and the
+// singularity-eos IdealGas energy sie = Cv T.
+// std::pow(x, 2) and std::pow(x, 3) are written as products; tanh is the
+// restatement below (the same algorithm as the device's).
+// =====================================================================
+namespace orc {
+namespace rad {
+
+// std::min / std::max semantics (NaN handling matters for bitwise parity)
+inline Real smin(Real a, Real b) { return (b < a) ? b : a; }
+inline Real smax(Real a, Real b) { return (a < b) ? b : a; }
+inline Real sgn(Real v) { return (Real)((0.0 <= v) - (v < 0.0)); }  // robust.hpp sgn
+
+// tanh from exp and expm1 written out: Cody-Waite reduction
+// y = n ln2 + r (ln2 split into a 32-bit head and a tail so n * head is
+// exact), Taylor series of e^r to degree 13 (|r| <= ln2 / 2: truncation below
+// 5e-18), e^y - 1 by its own Taylor series to degree 14 for |y| < 1/4, and
+// tanh(x) = -m / (2 + m) with m = e^{-2|x|} - 1.  Host and device evaluate
+// the same operations in the same order.
+constexpr Real LN2_HI = 0.693147180369123816490;   // 2977044471 / 2^32
+constexpr Real LN2_LO = 1.9082149292705877000e-10; // ln 2 - LN2_HI
+constexpr Real INV_LN2 = 1.4426950408889634074;
+inline Real exp_taylor(Real r) {
+  Real p = 1.0 / 6227020800.0;  // 1/13!
+  p = p * r + 1.0 / 479001600.0;
+  p = p * r + 1.0 / 39916800.0;
+  p = p * r + 1.0 / 3628800.0;
+  p = p * r + 1.0 / 362880.0;
+  p = p * r + 1.0 / 40320.0;
+  p = p * r + 1.0 / 5040.0;
+  p = p * r + 1.0 / 720.0;
+  p = p * r + 1.0 / 120.0;
+  p = p * r + 1.0 / 24.0;
+  p = p * r + 1.0 / 6.0;
+  p = p * r + 0.5;
+  p = p * r + 1.0;
+  p = p * r + 1.0;
+  return p;
+}
+inline Real expm1_small(Real y) {  // |y| < 1/4
+  Real p = 1.0 / 87178291200.0;  // 1/14!
+  p = p * y + 1.0 / 6227020800.0;
+  p = p * y + 1.0 / 479001600.0;
+  p = p * y + 1.0 / 39916800.0;
+  p = p * y + 1.0 / 3628800.0;
+  p = p * y + 1.0 / 362880.0;
+  p = p * y + 1.0 / 40320.0;
+  p = p * y + 1.0 / 5040.0;
+  p = p * y + 1.0 / 720.0;
+  p = p * y + 1.0 / 120.0;
+  p = p * y + 1.0 / 24.0;
+  p = p * y + 1.0 / 6.0;
+  p = p * y + 0.5;
+  p = p * y + 1.0;
+  return p * y;
+}
+// e^y for -46 <= y <= 0
+inline Real exp_neg(Real y) {
+  const Real n = std::floor(y * INV_LN2 + 0.5);
+  const Real r = (y - n * LN2_HI) - n * LN2_LO;
+  return std::ldexp(exp_taylor(r), (int)n);
+}
+inline Real tanh_r(Real x) {
+  const Real ax = std::fabs(x);
+  Real t;
+  if (ax > 22.0) {
+    t = 1.0;
+  } else {
+    const Real y = -2.0 * ax;
+    const Real m = (y > -0.25) ? expm1_small(y) : exp_neg(y) - 1.0;
+    t = -m / (2.0 + m);
+  }
+  return std::copysign(t, x);
+}
+
+struct V3 {
+  Real d[3];
+  Real &operator()(int i) { return d[i]; }
+  const Real &operator()(int i) const { return d[i]; }
+};
+struct T2 {
+  Real d[3][3];
+  Real &operator()(int i, int j) { return d[i][j]; }
+  const Real &operator()(int i, int j) const { return d[i][j]; }
+};
+
+// local_three_geometry.hpp:150-185 with gamma_ij = delta_ij
+inline void lower3(const V3 &a, V3 &o) {
+  for (int i = 0; i < 3; i++) o(i) = 0.0 + a(i);
+}
+inline void raise3(const V3 &a, V3 &o) {
+  for (int i = 0; i < 3; i++) o(i) = 0.0 + a(i);
+}
+inline Real ccov(const V3 &a, const V3 &b) {  // contractCov3Vectors
+  Real s = 0.0;
+  for (int i = 0; i < 3; i++) s += a(i) * b(i);
+  return s;
+}
+inline Real cconcov(const V3 &a, const V3 &b) {  // contractConCov3Vectors
+  Real s = 0.0;
+  for (int i = 0; i < 3; i++) s += a(i) * b(i);
+  return s;
+}
+inline Real gdelta(int i, int j) { return i == j ? 1.0 : 0.0; }
+
+// linear_algebra.hpp:58-96
+inline Real DifferenceOfProducts(Real a, Real b, Real c, Real d) {
+  const Real cd = c * d;
+  const Real err = std::fma(-c, d, cd);
+  const Real dop = std::fma(a, b, -cd);
+  return dop + err;
+}
+inline void SolveAxb2x2(Real A[2][2], Real b[2], Real x[2]) {
+  const Real invDet = 1.0 / DifferenceOfProducts(A[0][0], A[1][1], A[0][1], A[1][0]);
+  x[0] = invDet * DifferenceOfProducts(A[1][1], b[0], A[0][1], b[1]);
+  x[1] = invDet * DifferenceOfProducts(A[0][0], b[1], A[1][0], b[0]);
+}
+
+// relativity_utils.hpp:38-43 with the spatial metric
+inline Real lorentz3(const Real vp[3]) {
+  Real vsq = 0.;
+  for (int i = 0; i < 3; i++) vsq += vp[i] * vp[i];
+  return std::sqrt(1. + vsq);
+}
+
+enum Status { SUCCESS = 0, FAILURE = 1, MODIFIED = 2 };
+constexpr Real PI = 3.141592653589793;
+constexpr Real SIN_PI = 1.2246467991473532e-16;  // sin of the double nearest pi
+
+// ClosureEdd (closure.hpp:49-352) and ClosureM1 (closure_m1.hpp:31-372),
+// energy-conserving settings.
+struct Closure {
+  bool m1, robust;
+  V3 con_v, cov_v;
+  Real v2, W, W2;
+  Closure(const V3 &cv, bool m1_, bool robust_) : m1(m1_), robust(robust_) {
+    con_v = cv;
+    lower3(con_v, cov_v);
+    v2 = 0.0;
+    for (int i = 0; i < 3; i++) v2 += con_v(i) * cov_v(i);
+    v2 = smin(v2, 0.9999);
+    W = 1 / std::sqrt(1 - v2);
+    W2 = W * W;
+  }
+  void TilPiContractions(const T2 &Pi, V3 &cov_vPi, Real &vvPi) const {
+    V3 con_vPi;
+    vvPi = 0.0;
+    for (int i = 0; i < 3; i++) {
+      con_vPi(i) = 0.0;
+      for (int j = 0; j < 3; j++) con_vPi(i) += cov_v(j) * Pi(i, j);
+      vvPi += cov_v(i) * con_vPi(i);
+    }
+    lower3(con_vPi, cov_vPi);
+  }
+  void LinearSourceUpdate(Real Estar, const V3 &cov_Fstar, const T2 &Pi, Real JBB, Real tauJ, Real tauH,
+                          Real &dE, V3 &cov_dF) const {
+    Real vvPi;
+    V3 cov_vPi;
+    TilPiContractions(Pi, cov_vPi, vvPi);
+    Real A[2][2], x[2], b[2];
+    A[0][0] = (4 * W2 - 1) / 3 + W2 * vvPi + W * tauJ;
+    A[0][1] = 2 * W + tauH;
+    A[1][0] = A[0][0] - 1 - tauJ / W;
+    A[1][1] = A[0][1] - 1 / W;
+    const Real vFstar = cconcov(con_v, cov_Fstar);
+    b[0] = Estar + W * tauJ * JBB;
+    b[1] = vFstar + (W2 - 1) / W * tauJ * JBB;
+    SolveAxb2x2(A, b, x);
+    const Real J = x[0], zeta = x[1];
+    dE = (4 * W2 - 1 + 3 * W2 * vvPi) / 3 * J + 2 * W * zeta - Estar;
+    for (int i = 0; i < 3; i++)
+      cov_dF(i) = (cov_v(i) * tauH * (4 * W2 / 3 * J + W * zeta) + tauH * cov_vPi(i) * J +
+                   tauJ * W2 * cov_v(i) * (JBB - J) + W * cov_Fstar(i)) /
+                      (W + tauH) -
+                  cov_Fstar(i);
+  }
+  void ConCovP(Real J, const V3 &cov_H, const T2 &Pi, T2 &P) const {
+    V3 con_H;
+    T2 ccPi;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) ccPi(i, j) = 0.0 + Pi(i, j);
+    raise3(cov_H, con_H);
+    for (int i = 0; i < 3; i++) {
+      for (int j = 0; j < 3; j++)
+        P(i, j) = 4.0 / 3.0 * W2 * con_v(i) * cov_v(j) * J + W * (con_v(i) * cov_H(j) + cov_v(j) * con_H(i)) +
+                  J * ccPi(i, j);
+      P(i, i) += J / 3.0;
+    }
+  }
+  void ConP(Real J, const V3 &cov_H, const T2 &Pi, T2 &P) const {
+    V3 con_H;
+    raise3(cov_H, con_H);
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++)
+        P(i, j) = 4.0 / 3.0 * W2 * con_v(i) * con_v(j) * J + W * (con_v(i) * con_H(j) + con_v(j) * con_H(i)) +
+                  J * Pi(i, j) + J / 3.0 * gdelta(i, j);
+  }
+  void Prim2Con(Real J, const V3 &cov_H, const T2 &Pi, Real &E, V3 &cov_F) const {
+    Real vvPi;
+    V3 cov_vPi;
+    TilPiContractions(Pi, cov_vPi, vvPi);
+    Real vH = 0.0;
+    for (int i = 0; i < 3; i++) vH += con_v(i) * cov_H(i);
+    E = (4 * W2 - 1 + 3 * W2 * vvPi) / 3 * J + 2 * W * vH;
+    for (int i = 0; i < 3; i++)
+      cov_F(i) = 4 * W2 / 3 * cov_v(i) * J + W * cov_v(i) * vH + W * cov_H(i) + J * cov_vPi(i);
+  }
+  // getFluxesFromPrim (lapse 1: the final scalings are exact)
+  void FluxesFromPrim(Real J, const V3 &cov_H, const T2 &Pi, V3 &con_F, T2 &P) const {
+    ConCovP(J, cov_H, Pi, P);
+    Real E;
+    V3 cov_F;
+    Prim2Con(J, cov_H, Pi, E, cov_F);
+    raise3(cov_F, con_F);
+  }
+  Status Con2Prim(Real E, const V3 &cov_F, const T2 &Pi, Real &J, V3 &cov_H) const {
+    Real vvPi;
+    V3 cov_vPi;
+    TilPiContractions(Pi, cov_vPi, vvPi);
+    double vF = 0.0;
+    for (int i = 0; i < 3; i++) vF += con_v(i) * cov_F(i);
+    const Real lam = (2.0 * W2 + 1.0) / 3.0 + (2.0 * W2 - 3.0) * W2 * vvPi;
+    const Real a = ratio(W2, lam) * ((4 * W2 / 3 - vvPi) * E - ((4 * W2 + 1) / 3 - W2 * vvPi) * vF);
+    J = ratio((2 * W2 - 1) * E - 2 * W2 * vF, lam);
+    for (int i = 0; i < 3; i++) cov_H(i) = (cov_F(i) - J * cov_vPi(i) - cov_v(i) * a) / W;
+    const Real vh = cconcov(con_v, cov_H);
+    const Real xi = std::sqrt(ccov(cov_H, cov_H) - vh * vh) / J;
+    if (std::isnan(xi) || std::isnan(J)) return FAILURE;
+    if (J < 0. || xi >= 1.0) {
+      if (robust) {
+        if (J < 0.) J = smin(J, 10. * SMALL);
+        if (xi >= 1.0)
+          for (int i = 0; i < 3; i++) cov_H(i) *= 0.999 / xi;
+        return MODIFIED;
+      }
+      return FAILURE;
+    }
+    return SUCCESS;
+  }
+  static Real closure_fn(Real xi) { return (1.0 - 2 * (xi * xi) + 4 * (xi * xi * xi)) / 3.0; }
+  // M1FluidPressureTensor from J and H (closure_m1.hpp:274-299)
+  void PressureFromPrim(Real J, const V3 &cov_H, T2 &Pi, V3 &con_f) const {
+    V3 con_H;
+    raise3(cov_H, con_H);
+    Real H = 0.0, vH = 0.0;
+    for (int i = 0; i < 3; i++) H += cov_H(i) * con_H(i);
+    for (int i = 0; i < 3; i++) vH += cov_H(i) * con_v(i);
+    H = std::sqrt(H - vH * vH);
+    for (int i = 0; i < 3; i++) con_f(i) = ratio(con_H(i), H);
+    const Real xi = smax(smin(1.0, ratio(H, J)), 0.0);
+    const Real athin = 0.5 * (3 * closure_fn(xi) - 1);
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) {
+        Pi(i, j) = con_f(i) * con_f(j) - (W2 * con_v(i) * con_v(j) + gdelta(i, j)) / 3;
+        Pi(i, j) *= athin;
+      }
+  }
+  // M1FluidPressureTensor from xi, phi and the basis (closure_m1.hpp:301-324)
+  void PressureFromAngles(Real xi, Real phi, const V3 &g, const V3 &dd, T2 &Pi, V3 &con_f) const {
+    Real s, c;
+    if (phi == PI) {
+      s = SIN_PI;
+      c = -1.0;
+    } else {
+      s = std::sin(phi);
+      c = std::cos(phi);
+    }
+    for (int i = 0; i < 3; i++) con_f(i) = -c * g(i) + s * dd(i);
+    const Real athin = 0.5 * (3 * closure_fn(xi) - 1);
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) {
+        Pi(i, j) = con_f(i) * con_f(j) - (W2 * con_v(i) * con_v(j) + gdelta(i, j)) / 3;
+        Pi(i, j) *= athin;
+      }
+  }
+  // closure_m1.hpp:326-372
+  void BasisVectors(const V3 &cov_F, V3 &g, V3 &dd) const {
+    V3 con_F;
+    raise3(cov_F, con_F);
+    Real Fmag = 0.0, vl = 0.0, vv = 0.0;
+    for (int i = 0; i < 3; i++) Fmag += cov_F(i) * con_F(i);
+    Fmag = std::sqrt(Fmag);
+    for (int i = 0; i < 3; i++) vl += cov_F(i) * con_v(i);
+    vl = ratio(vl, Fmag);
+    for (int i = 0; i < 3; i++) vv += cov_v(i) * con_v(i);
+    const Real lam = ratio(1.0, W * (1 - vl));
+    const Real aa = std::sqrt(vv * (1 + 10 * std::numeric_limits<Real>::epsilon()) - vl * vl);
+    for (int i = 0; i < 3; i++) {
+      g(i) = ratio(con_F(i) * lam, Fmag) - W * con_v(i);
+      dd(i) = ratio(ratio(con_F(i), Fmag) * (1 - lam / W) + con_v(i), aa);
+    }
+  }
+  void Residuals(Real E, const V3 &cov_F, Real xi, Real phi, const V3 &g, const V3 &dd, Real &fXi,
+                 Real &fPhi) const {
+    T2 Pi;
+    V3 con_f;
+    PressureFromAngles(xi, phi, g, dd, Pi, con_f);
+    Real J;
+    V3 cov_H;
+    Con2Prim(E, cov_F, Pi, J, cov_H);
+    Real H(0.0), vH(0.0), Hf(0.0), vf(0.0);
+    for (int i = 0; i < 3; i++) H += cov_H(i) * cov_H(i);
+    for (int i = 0; i < 3; i++) vH += con_v(i) * cov_H(i);
+    for (int i = 0; i < 3; i++) Hf += cov_H(i) * con_f(i);
+    for (int i = 0; i < 3; i++) vf += cov_v(i) * con_f(i);
+    Hf -= vf * vH;
+    H = std::sqrt(H - vH * vH);
+    fXi = xi - ratio(H, J);
+    fPhi = Hf - H;
+  }
+  // SolveClosure (closure_m1.hpp:178-258).  The reference holds phi at pi
+  // (its "first two updates" test is true for every iteration) and drops the
+  // 2x2 solve; the two phi-perturbed residuals only feed that solve and are
+  // not evaluated here.  Returns the iteration count; *failed on NaN or the
+  // iteration cap.
+  int SolveClosure(Real E, V3 cov_F, Real &xi_out, Real &phi_out, Real xi_guess, bool &failed) const {
+    const int max_iter = 30;
+    const Real tol = 1.e6 * std::numeric_limits<Real>::epsilon();
+    const Real eps = std::sqrt(10 * std::numeric_limits<Real>::epsilon());
+    const Real delta = 20 * std::numeric_limits<Real>::epsilon();
+    for (int i = 0; i < 3; i++)
+      cov_F(i) = ratio(cov_F(i), E) + 1.e3 * sgn(cov_F(i)) * std::numeric_limits<Real>::min();
+    E = 1.0;
+    V3 g, dd;
+    BasisVectors(cov_F, g, dd);
+    int iter = 0;
+    Real fXi = 1.e3, fPhi = 1.e3;
+    Real xi = xi_guess;
+    Real phi = PI;
+    do {
+      Real fXi_up, fXi_lo, fPhi_up, fPhi_lo;
+      const Real xi_up = smin(xi * (1.0 + eps) + delta, 1.0);
+      const Real xi_lo = smax(xi * (1.0 - eps) - delta, 0.0);
+      Residuals(E, cov_F, xi_up, phi, g, dd, fXi_up, fPhi_up);
+      Residuals(E, cov_F, xi_lo, phi, g, dd, fXi_lo, fPhi_lo);
+      const Real J00 = (fXi_up - fXi_lo) / (xi_up - xi_lo);
+      Residuals(E, cov_F, xi, phi, g, dd, fXi, fPhi);
+      const Real dx0 = fXi / J00, dx1 = 0.0;
+      fPhi = 0.0;
+      Real cdx = smin(dx0, xi - delta * xi);
+      cdx = smax(cdx, xi - (1 - delta * (1 - xi)));
+      Real alpha = ratio(cdx, dx0);
+      alpha = smin(alpha, 0.5 * 3.14159 / std::fabs(dx1));
+      xi -= alpha * dx0;
+      phi -= alpha * dx1;
+      ++iter;
+    } while (iter < max_iter && (std::fabs(fXi) > tol || std::fabs(fPhi) > tol));
+    xi_out = xi;
+    phi_out = phi;
+    failed = std::isnan(xi) || iter >= max_iter;
+    return iter;
+  }
+  // GetConTilPiFromCon: M1 solves the closure from the xi guess; Eddington
+  // returns pi = 0, xi = 0, phi = pi.
+  void TilPiFromCon(Real E, const V3 &cov_F, Real &xi, Real &phi, T2 &Pi) const {
+    if (!m1) {
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) Pi(i, j) = 0.0;
+      xi = 0.0;
+      phi = PI;
+      return;
+    }
+    bool failed;
+    SolveClosure(E, cov_F, xi, phi, xi, failed);
+    V3 g, dd, con_f;
+    BasisVectors(cov_F, g, dd);
+    PressureFromAngles(xi, phi, g, dd, Pi, con_f);
+  }
+  void TilPiFromPrim(Real J, const V3 &cov_H, T2 &Pi) const {
+    if (!m1) {
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) Pi(i, j) = 0.0;
+      return;
+    }
+    V3 con_f;
+    PressureFromPrim(J, cov_H, Pi, con_f);
+  }
+};
+
+struct RBlk {
+  Blk B;
+  const phx_rad_block *r;
+  long long rvs;
+  explicit RBlk(const phx_block *fb, const phx_rad_block *rb) : B(fb), r(rb) {
+    rvs = rb->var_stride ? rb->var_stride : B.N;
+  }
+  Real &U(int v, long long id) const { return r->cons[v * rvs + id]; }
+  Real &Q(int v, long long id) const { return r->prim[v * rvs + id]; }
+  Real &F(int d, int m, long long id) const { return r->flux[((long long)d * PHX_RNCONS + m) * rvs + id]; }
+  Real fp(int v, long long id) const { return B.b->prim[v * B.vs + id]; }
+  V3 con_v(long long id, Real *Wout = nullptr) const {
+    const Real vp[3] = {fp(PHX_PVEL, id), fp(PHX_PVEL + 1, id), fp(PHX_PVEL + 2, id)};
+    const Real W = lorentz3(vp);
+    if (Wout) *Wout = W;
+    return V3{{vp[0] / W, vp[1] / W, vp[2] / W}};
+  }
+};
+
+struct RPar {
+  bool m1, robust, bounds;
+  int recon;
+  Real cfl, tol, kappa_a, kappa_s, jbb;
+  int maxiter, oned_fixup;
+  Real J_floor, xi_ceiling, tau_max, W_ceiling, Cv;
+  RPar(const phx_rad_params &rp, const phx_params &p) {
+    m1 = rp.method == PHX_RAD_M1;
+    robust = !rp.closure_frail;
+    bounds = rp.recon_fixup_bounds != 0;
+    recon = rp.recon;
+    cfl = rp.cfl;
+    tol = rp.src_rootfind_tol;
+    maxiter = rp.src_rootfind_maxiter;
+    oned_fixup = rp.oned_fixup_strategy;
+    kappa_a = rp.kappa_a;
+    kappa_s = rp.kappa_s;
+    jbb = rp.jbb_coeff;
+    J_floor = rp.enable_rad_floors ? rp.J0_floor : -std::numeric_limits<Real>::max();
+    xi_ceiling = rp.enable_rad_ceilings ? rp.xi0_ceiling : std::numeric_limits<Real>::max();
+    tau_max = rp.enable_rad_ceilings ? rp.tau0_ceiling : std::numeric_limits<Real>::max();
+    W_ceiling = p.enable_ceilings ? p.gam0_ceiling : std::numeric_limits<Real>::max();
+    Cv = p.Cv;
+  }
+  Real kappaJ(Real rho, Real T) const { return rho * kappa_a; }
+  Real kappaS(Real rho, Real T) const { return rho * kappa_s; }
+  Real JBB(Real T) const { return jbb * (T * T) * (T * T); }
+};
+
+// MomentPrim2Con (moments.cpp:198-256)
+void prim_to_con(const RPar &rp, const RBlk &R, long long id) {
+  const Closure c(R.con_v(id), rp.m1, true);
+  const Real J = R.Q(PHX_RJ, id);
+  const V3 covH{{R.Q(PHX_RH, id) * J, R.Q(PHX_RH + 1, id) * J, R.Q(PHX_RH + 2, id) * J}};
+  T2 Pi;
+  c.TilPiFromPrim(J, covH, Pi);
+  Real E;
+  V3 covF;
+  c.Prim2Con(J, covH, Pi, E, covF);
+  const Real sdetgam = 1.0;
+  R.U(PHX_RE, id) = sdetgam * E;
+  for (int d = 0; d < 3; d++) R.U(PHX_RF + d, id) = sdetgam * covF(d);
+}
+
+// MomentCon2PrimImpl (moments.cpp:61-159)
+void con_to_prim(const RPar &rp, const RBlk &R, long long id) {
+  const Real isdetgam = 1.0 / 1.0;
+  const Closure c(R.con_v(id), rp.m1, rp.robust);
+  Real J;
+  V3 covH;
+  T2 Pi;
+  Real E = R.U(PHX_RE, id) * isdetgam;
+  V3 covF{{R.U(PHX_RF, id) * isdetgam, R.U(PHX_RF + 1, id) * isdetgam, R.U(PHX_RF + 2, id) * isdetgam}};
+  Real xi = 0.0, phi = PI;
+  if (rp.m1) {
+    xi = R.Q(PHX_RXI, id);
+    phi = 1.0001 * R.Q(PHX_RPHI, id);
+  }
+  c.TilPiFromCon(E, covF, xi, phi, Pi);
+  if (rp.m1) {
+    R.Q(PHX_RXI, id) = xi;
+    R.Q(PHX_RPHI, id) = phi;
+  }
+  Status st = c.Con2Prim(E, covF, Pi, J, covH);
+  if (st == MODIFIED) {
+    c.Prim2Con(J, covH, Pi, E, covF);
+    R.U(PHX_RE, id) = E / isdetgam;
+    for (int d = 0; d < 3; d++) R.U(PHX_RF + d, id) = covF(d) / isdetgam;
+    st = SUCCESS;
+  }
+  R.Q(PHX_RJ, id) = J;
+  for (int d = 0; d < 3; d++) R.Q(PHX_RH + d, id) = ratio(covH(d), J);
+  R.Q(PHX_RFAIL, id) = st == SUCCESS ? 1.0 : 0.0;
+}
+
+// MomentCalculateOpacities (moments.cpp:960-991)
+void opacities(const RPar &rp, const RBlk &R, long long id) {
+  const Real rho = R.fp(PHX_PRHO, id), T = R.fp(PHX_PTMP, id);
+  const Real kJ = rp.kappaJ(rho, T);
+  const Real kH = kJ + rp.kappaS(rho, T);
+  R.Q(PHX_RJBB, id) = rp.JBB(T);
+  R.Q(PHX_RKAPPAJ, id) = kJ;
+  R.Q(PHX_RKAPPAH, id) = kH;
+}
+
+inline void recon5(int recon, Real qm2, Real qm1, Real q0, Real qp1, Real qp2, Real &ql, Real &qr) {
+  switch (recon) {
+  case PHX_RECON_WENO5Z: WENO5Z(qm2, qm1, q0, qp1, qp2, ql, qr); break;
+  case PHX_RECON_MP5: MP5(qm2, qm1, q0, qp1, qp2, ql, qr); break;
+  case PHX_RECON_LINEAR: PiecewiseLinear(qm1, q0, qp1, ql, qr); break;
+  default: ql = q0; qr = q0;
+  }
+}
+
+// One face of CalculateFluxesImpl (moments.cpp:548-722): direction d, the
+// face between cells (k, j, i) - e_d and (k, j, i).  Left and right states
+// come from the reconstruction of the two cells (ReconstructEdgeStates,
+// moments.cpp:282-458: ql of a face = the upper value of the cell below,
+// qr = the lower value of the cell above), dJ from its face formulas.
+void face_flux(const RPar &rp, const RBlk &R, int d, int k, int j, int i) {
+  const Blk &B = R.B;
+  const int ndim = B.ndim;
+  const int dj = ndim > 1 ? 1 : 0, dk = ndim > 2 ? 1 : 0;
+  const long long st = d == 0 ? 1 : (d == 1 ? (long long)B.n1t : (long long)B.n1t * B.n2t);
+  const long long id = B.idx(k, j, i), idm = id - st;
+  // reconstructed J, H/J (4 values) and velocity (3): left from cell idm, right from id
+  Real ql[7], qr[7];
+  for (int n = 0; n < 7; n++) {
+    auto val = [&](long long c) { return n < 4 ? R.Q(PHX_RJ + n, c) : R.fp(PHX_PVEL + n - 4, c); };
+    Real a, b;
+    recon5(rp.recon, val(idm - 2 * st), val(idm - st), val(idm), val(idm + st), val(idm + 2 * st), ql[n], a);
+    recon5(rp.recon, val(id - 2 * st), val(id - st), val(id), val(id + st), val(id + 2 * st), b, qr[n]);
+  }
+  // dJ at this face (moments.cpp:412-455)
+  auto Jat = [&](int kk, int jj, int ii) { return R.Q(PHX_RJ, B.idx(kk, jj, ii)); };
+  const Real idx = 1.0 / B.dx(1), idx4 = 0.25 * idx;
+  const Real idy = 1.0 / B.dx(2), idy4 = 0.25 * idy;
+  const Real idz = 1.0 / B.dx(3), idz4 = 0.25 * idz;
+  V3 cov_dJ;
+  if (d == 0) {
+    cov_dJ(0) = (Jat(k, j, i) - Jat(k, j, i - 1)) * idx;
+    cov_dJ(1) = (Jat(k, j + dj, i) + Jat(k, j + dj, i - 1) - Jat(k, j - dj, i) - Jat(k, j - dj, i - 1)) * idy4;
+    cov_dJ(2) = (Jat(k + dk, j, i) + Jat(k + dk, j, i - 1) - Jat(k - dk, j, i) - Jat(k - dk, j, i - 1)) * idz4;
+  } else if (d == 1) {
+    cov_dJ(0) = (Jat(k, j, i + 1) + Jat(k, j - dj, i + 1) - Jat(k, j, i - 1) - Jat(k, j - dj, i - 1)) * idx4;
+    cov_dJ(1) = (Jat(k, j, i) - Jat(k, j - dj, i)) * idy;
+    cov_dJ(2) = (Jat(k + dk, j, i) + Jat(k + dk, j - dj, i) - Jat(k - dk, j, i) - Jat(k - dk, j - dj, i)) * idz4;
+  } else {
+    cov_dJ(0) = (Jat(k, j, i + 1) + Jat(k - dk, j, i + 1) - Jat(k, j, i - 1) - Jat(k - dk, j, i - 1)) * idx4;
+    cov_dJ(1) = (Jat(k, j + dj, i) + Jat(k - dk, j + dj, i) - Jat(k, j - dj, i) - Jat(k - dk, j - dj, i)) * idy4;
+    cov_dJ(2) = (Jat(k, j, i) - Jat(k - dk, j, i)) * idz;
+  }
+  const Real dx = B.dx(d + 1) * std::sqrt(1.0);
+  Real vpl[3] = {ql[4], ql[5], ql[6]}, vpr[3] = {qr[4], qr[5], qr[6]};
+  Real Wl = lorentz3(vpl), Wr = lorentz3(vpr);
+  if (rp.bounds) {
+    if (Wl > rp.W_ceiling) {
+      const Real rescale = std::sqrt(rp.W_ceiling * rp.W_ceiling - 1.) / (Wl * Wl - 1.);
+      for (int a = 0; a < 3; a++) vpl[a] *= rescale;
+      Wl = rp.W_ceiling;
+    }
+    if (Wr > rp.W_ceiling) {
+      const Real rescale = std::sqrt(rp.W_ceiling * rp.W_ceiling - 1.) / (Wr * Wr - 1.);
+      for (int a = 0; a < 3; a++) vpr[a] *= rescale;
+      Wr = rp.W_ceiling;
+    }
+  }
+  const V3 vl{{vpl[0] / Wl, vpl[1] / Wl, vpl[2] / Wl}}, vr{{vpr[0] / Wr, vpr[1] / Wr, vpr[2] / Wr}};
+  const Real sigp = 1.0 * std::sqrt(1.0) - 0.0;
+  const Real sigm = -1.0 * std::sqrt(1.0) - 0.0;
+  const Real asym_sigl = 1.0 * vl(d) - 0.0;
+  const Real asym_sigr = 1.0 * vr(d) - 0.0;
+
+  Real Jl = ql[0], Jr = qr[0];
+  if (rp.bounds) {
+    Jl = smax(Jl, rp.J_floor);
+    Jr = smax(Jr, rp.J_floor);
+  }
+  V3 Hl{{Jl * ql[1], Jl * ql[2], Jl * ql[3]}}, Hr{{Jr * qr[1], Jr * qr[2], Jr * qr[3]}};
+  if (rp.bounds) {
+    const Real vhl = cconcov(vl, Hl), vhr = cconcov(vr, Hr);
+    const Real xil = std::sqrt(ccov(Hl, Hl) - vhl * vhl) / Jl;
+    const Real xir = std::sqrt(ccov(Hr, Hr) - vhr * vhr) / Jr;
+    if (xil > rp.xi_ceiling)
+      for (int a = 0; a < 3; a++) Hl(a) *= rp.xi_ceiling / xil;
+    if (xir > rp.xi_ceiling)
+      for (int a = 0; a < 3; a++) Hr(a) *= rp.xi_ceiling / xir;
+  }
+  const Real kappaH = std::sqrt(R.Q(PHX_RKAPPAH, id) * R.Q(PHX_RKAPPAH, idm));
+  const Real a = tanh_r(ratio(1.0, std::fabs(kappaH * dx)));
+  const Real kappaH_min = 1.e-20;
+  V3 HasymL;
+  for (int c = 0; c < 3; c++) HasymL(c) = ratio(-cov_dJ(c), 3 * kappaH + 3 * kappaH_min);
+  const V3 HasymR = HasymL;
+  const Closure cl(vl, rp.m1, true), cr(vr, rp.m1, true);
+  T2 Pil, Pir, Pl, Pr, Pl_asym, Pr_asym;
+  V3 conFl, conFr, conFl_asym, conFr_asym, covFl, covFr;
+  Real El, Er;
+  cl.TilPiFromPrim(Jl, HasymL, Pil);
+  cr.TilPiFromPrim(Jr, HasymR, Pir);
+  cl.FluxesFromPrim(Jl, HasymL, Pil, conFl_asym, Pl_asym);
+  cr.FluxesFromPrim(Jr, HasymR, Pir, conFr_asym, Pr_asym);
+  cl.TilPiFromPrim(Jl, Hl, Pil);
+  cr.TilPiFromPrim(Jr, Hr, Pir);
+  cl.FluxesFromPrim(Jl, Hl, Pil, conFl, Pl);
+  cr.FluxesFromPrim(Jr, Hr, Pir, conFr, Pr);
+  cl.Prim2Con(Jl, Hl, Pil, El, covFl);
+  cr.Prim2Con(Jr, Hr, Pir, Er, covFr);
+  for (int c = 0; c < 3; c++) {
+    conFl(c) = a * conFl(c) + (1 - a) * conFl_asym(c);
+    conFr(c) = a * conFr(c) + (1 - a) * conFr_asym(c);
+  }
+  for (int p = 0; p < 3; p++)
+    for (int q = 0; q < 3; q++) {
+      Pl(p, q) = a * Pl(p, q) + (1 - a) * Pl_asym(p, q);
+      Pr(p, q) = a * Pr(p, q) + (1 - a) * Pr_asym(p, q);
+    }
+  const Real rad_sigspeed = smax(std::fabs(sigm), std::fabs(sigp));
+  const Real asym_sigspeed = smax(std::fabs(asym_sigl), std::fabs(asym_sigr));
+  const Real sigspeed = a * rad_sigspeed + (1. - a) * asym_sigspeed;
+  conFl(d) -= 0.0 * El;
+  conFr(d) -= 0.0 * Er;
+  for (int c = 0; c < 3; c++) {
+    Pl(d, c) -= 0.0 * covFl(c);
+    Pr(d, c) -= 0.0 * covFr(c);
+  }
+  const Real sdetgam = 1.0;
+  R.F(d, PHX_RE, id) = 0.5 * sdetgam * (conFl(d) + conFr(d) + sigspeed * (El - Er));
+  for (int c = 0; c < 3; c++)
+    R.F(d, PHX_RF + c, id) = 0.5 * sdetgam * (Pl(d, c) + Pr(d, c) + sigspeed * (covFl(c) - covFr(c)));
+}
+
+// The temperature residual of the oned solver (moments_source.cpp:152-196)
+struct TResidual {
+  const RPar &rp;
+  Real rho, ug0, J0, dtau, alpha_max;
+  Real operator()(Real T) const {
+    Real kappa = rp.kappaJ(rho, T);
+    kappa = smin(kappa, alpha_max);
+    const Real JBB = rp.JBB(T);
+    const Real dJ = (J0 + dtau * kappa * JBB) / (1. + dtau * kappa) - J0;
+    const Real ug1 = rho * (rp.Cv * T);
+    return ((ug1 - ug0) + dJ) / (ug0 + J0);
+  }
+};
+// RootFind::regula_falsi with a status (root_find.hpp:111-160); the object
+// (and its iteration count) persists across the re-bracketing attempts.
+struct RF {
+  int iteration_count = 0, max_iter;
+  explicit RF(int m) : max_iter(m) {}
+  template <typename Fn>
+  Real regula_falsi(const Fn &func, Real a, Real b, Real tol, Real guess, bool &ok) {
+    Real ya, yb;
+    if (a <= guess && b >= guess) {
+      ya = func(guess);
+      yb = func(b);
+      if (ya * yb > 0.0) {
+        yb = ya;
+        b = guess;
+        ya = func(a);
+      } else {
+        a = guess;
+      }
+    } else {
+      ya = func(a);
+      yb = func(b);
+    }
+    if (ya * yb > 0.0) {
+      ok = false;
+      return guess;
+    }
+    const Real sign = (ya < 0 ? 1.0 : -1.0);
+    ya *= sign;
+    yb *= sign;
+    int b1 = 0, b2 = 0;
+    while (b - a > 2.0 * tol && iteration_count < max_iter) {
+      const Real c = (a * yb - b * ya) / (yb - ya);
+      if (c == a) {
+        b = a;
+        iteration_count++;
+        continue;
+      } else if (c == b) {
+        a = b;
+        iteration_count++;
+        continue;
+      }
+      const Real yc = sign * func(c);
+      if (yc > 0.0) {
+        b = c;
+        yb = yc;
+        b1++;
+        ya *= (b1 > 1 ? 0.5 : 1.0);
+        b2 = 0;
+      } else if (yc < 0.0) {
+        a = c;
+        ya = yc;
+        b2++;
+        yb *= (b2 > 1 ? 0.5 : 1.0);
+        b1 = 0;
+      } else {
+        a = c;
+        b = c;
+      }
+      iteration_count++;
+    }
+    ok = iteration_count != max_iter;
+    return 0.5 * (a + b);
+  }
+};
+
+// MomentFluidSourceImpl, oned solver, update_fluid = false, one species
+// (moments_source.cpp:203-490 and 786-958).  Returns 1 when the source
+// update was applied.
+int fluid_source(const RPar &rp, const RBlk &R, long long id, Real dt) {
+  const Real alpha = 1.0, sdetgam = 1.0;
+  const Real alpha_max = rp.tau_max / (alpha * dt);
+  const Real rho = R.fp(PHX_PRHO, id), ug = R.fp(PHX_PENG, id), Tf = R.fp(PHX_PTMP, id);
+  Real W;
+  const V3 con_v = R.con_v(id, &W);
+  Real dE = 0.0;
+  V3 cov_dF{{0.0, 0.0, 0.0}};
+  bool success = false;
+  {
+    const Real J0 = R.Q(PHX_RJ, id);
+    const Real dtau = alpha * dt / W;
+    RF root(rp.maxiter);
+    TResidual res{rp, rho, ug, J0, dtau, alpha_max};
+    bool ok;
+    Real T1 = root.regula_falsi(res, 1.e-2 * Tf, 1.e2 * Tf, rp.tol * Tf, Tf, ok);
+    Real fac = 10.;
+    int tries = 0;
+    while (!ok && tries < 4) {
+      T1 = root.regula_falsi(res, 1.e-1 / fac * Tf, 1.e1 * fac * Tf, rp.tol * Tf, Tf, ok);
+      tries++;
+      fac *= 10.;
+    }
+    const Closure c(con_v, rp.m1, true);
+    Real Estar = R.U(PHX_RE, id) / sdetgam;
+    V3 Fstar{{R.U(PHX_RF, id) / sdetgam, R.U(PHX_RF + 1, id) / sdetgam, R.U(PHX_RF + 2, id) / sdetgam}};
+    Real J = R.Q(PHX_RJ, id);
+    V3 cov_H{{J * R.Q(PHX_RH, id), J * R.Q(PHX_RH + 1, id), J * R.Q(PHX_RH + 2, id)}};
+    T2 Pi;
+    c.TilPiFromPrim(J, cov_H, Pi);
+    const Real JBB = rp.JBB(T1);
+    Real kappaJ = smin(rp.kappaJ(rho, T1), alpha_max);
+    Real kappaH = smin(rp.kappaS(rho, T1), alpha_max);
+    kappaH += kappaJ;
+    Real tauJ = alpha * dt * kappaJ;
+    Real tauH = alpha * dt * kappaH;
+    if (ok) {
+      c.LinearSourceUpdate(Estar, Fstar, Pi, JBB, tauJ, tauH, dE, cov_dF);
+      Estar += dE;
+      for (int a = 0; a < 3; a++) Fstar(a) += cov_dF(a);
+      success = c.Con2Prim(Estar, Fstar, Pi, J, cov_H) == SUCCESS;
+    }
+    if (!success && rp.oned_fixup == PHX_RAD_ONED_FIXUP_IGNORE_DJ) {
+      Estar = R.U(PHX_RE, id) / sdetgam;
+      for (int a = 0; a < 3; a++) Fstar(a) = R.U(PHX_RF + a, id) / sdetgam;
+      const Real JBB2 = rp.JBB(Tf);
+      const Real kJ = rp.kappaJ(rho, T1);
+      const Real kH = rp.kappaS(rho, T1) + kJ;
+      tauJ = alpha * dt * kJ;
+      tauH = alpha * dt * kH;
+      c.LinearSourceUpdate(Estar, Fstar, Pi, JBB2, tauJ, tauH, dE, cov_dF);
+      Estar = R.U(PHX_RE, id) / sdetgam + dE;
+      for (int a = 0; a < 3; a++) Fstar(a) = R.U(PHX_RF + a, id) / sdetgam + cov_dF(a);
+      success = c.Con2Prim(Estar, Fstar, Pi, J, cov_H) == SUCCESS;
+    } else if (!success && rp.oned_fixup == PHX_RAD_ONED_FIXUP_IGNORE_ALL) {
+      dE = 0.;
+      for (int a = 0; a < 3; a++) cov_dF(a) = 0.;
+      success = true;
+    }
+  }
+  if (success) {
+    R.U(PHX_RE, id) += sdetgam * dE;
+    for (int a = 0; a < 3; a++) R.U(PHX_RF + a, id) += sdetgam * cov_dF(a);
+  }
+  T2 Pi;
+  Real E = R.U(PHX_RE, id) / sdetgam;
+  V3 covF;
+  Real J;
+  V3 covH;
+  {
+    const Closure c(con_v, rp.m1, false);
+    for (int a = 0; a < 3; a++) covF(a) = R.U(PHX_RF + a, id) / sdetgam;
+    Real xi = 0.0, phi = PI;
+    c.TilPiFromCon(E, covF, xi, phi, Pi);
+    if (c.Con2Prim(E, covF, Pi, J, covH) == SUCCESS) {
+      R.Q(PHX_RJ, id) = J;
+      for (int a = 0; a < 3; a++) R.Q(PHX_RH + a, id) = covH(a) / J;
+      return success ? 1 : 0;
+    }
+  }
+  // failed inversion: the reference's zero-radiation state
+  Real Wc;
+  const V3 cv2 = R.con_v(id, &Wc);
+  const Closure c(cv2, rp.m1, false);
+  R.Q(PHX_RJ, id) = SMALL;
+  J = R.Q(PHX_RJ, id);
+  for (int a = 0; a < 3; a++) {
+    R.Q(PHX_RH + a, id) = 0.;
+    covH(a) = R.Q(PHX_RH + a, id) * J;
+  }
+  c.Prim2Con(J, covH, Pi, E, covF);
+  R.U(PHX_RE, id) = E * sdetgam;
+  for (int a = 0; a < 3; a++) R.U(PHX_RF + a, id) = covF(a) * sdetgam;
+  return success ? 1 : 0;
+}
+
+// radiation.cpp:681-733 (one species; lapse 1, shift 0)
+Real zone_dt(const RPar &rp, const RBlk &R, int k, int j, int i) {
+  const long long id = R.B.idx(k, j, i);
+  Real ldt = std::numeric_limits<Real>::max();
+  const Real kappaH = R.Q(PHX_RKAPPAH, id);
+  for (int d = 0; d < R.B.ndim; d++) {
+    const Real sigp = 1.0 * std::sqrt(1.0) - 0.0;
+    const Real sigm = -1.0 * std::sqrt(1.0) - 0.0;
+    const Real asym_sigl = 1.0 * R.fp(PHX_PVEL + d, id) - 0.0;
+    const Real rad_speed = smax(std::fabs(sigm), std::fabs(sigp));
+    const Real asym_speed = std::fabs(asym_sigl);
+    const Real w = R.B.dx(d + 1);
+    const Real dx = w * std::sqrt(1.0);
+    const Real a = tanh_r(ratio(1.0, std::fabs(kappaH * dx)));
+    const Real csig = a * rad_speed + (1. - a) * asym_speed;
+    ldt = smin(ldt, 1.0 / (csig / w));
+  }
+  return ldt;
+}
+
+}  // namespace rad
+}  // namespace orc
+
+extern "C" {
+using namespace orc::rad;
+
+void orc_rad_prim_to_con(const phx_rad_params *rp, const phx_params *p, const phx_block *fb, const phx_rad_block *rb,
+                         phx_range ib, phx_range jb, phx_range kb) {
+  const RPar P(*rp, *p);
+  const RBlk R(fb, rb);
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int k = kb.s; k <= kb.e; k++)
+    for (int j = jb.s; j <= jb.e; j++)
+      for (int i = ib.s; i <= ib.e; i++) prim_to_con(P, R, R.B.idx(k, j, i));
+}
+
+void orc_rad_con_to_prim(const phx_rad_params *rp, const phx_params *p, const phx_block *fb, const phx_rad_block *rb,
+                         phx_range ib, phx_range jb, phx_range kb) {
+  const RPar P(*rp, *p);
+  const RBlk R(fb, rb);
+#pragma omp parallel for collapse(2) schedule(dynamic, 4)
+  for (int k = kb.s; k <= kb.e; k++)
+    for (int j = jb.s; j <= jb.e; j++)
+      for (int i = ib.s; i <= ib.e; i++) con_to_prim(P, R, R.B.idx(k, j, i));
+}
+
+void orc_rad_calculate_opacities(const phx_rad_params *rp, const phx_params *p, const phx_block *fb,
+                                 const phx_rad_block *rb) {
+  const RPar P(*rp, *p);
+  const RBlk R(fb, rb);
+  for (long long id = 0; id < R.B.N; id++) opacities(P, R, id);
+}
+
+// Every face the interior update reads: X1 faces i in [is, ie + 1] of
+// interior rows, and likewise for X2, X3.
+void orc_rad_calculate_fluxes(const phx_rad_params *rp, const phx_params *p, const phx_block *fb,
+                              const phx_rad_block *rb) {
+  const RPar P(*rp, *p);
+  const RBlk R(fb, rb);
+  const orc::Blk &B = R.B;
+  for (int d = 0; d < B.ndim; d++) {
+    const int ie = B.ie() + (d == 0), je = B.je() + (d == 1), ke = B.ke() + (d == 2);
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int k = B.ks(); k <= ke; k++)
+      for (int j = B.js(); j <= je; j++)
+        for (int i = B.is(); i <= ie; i++) face_flux(P, R, d, k, j, i);
+  }
+}
+
+void orc_rad_update(const phx_rad_params *rp, const phx_block *fb, const phx_rad_block *rb, const double *base,
+                    double *out, double beta, double dt) {
+  const RBlk R(fb, rb);
+  const orc::Blk &B = R.B;
+  const Real dx1 = fb->dx1, dx2 = fb->dx2, dx3 = fb->dx3;
+  const Real A1 = dx2 * dx3, A2 = dx1 * dx3, A3 = dx1 * dx2, V = dx1 * dx2 * dx3;
+  const Real bdt = beta * dt;
+  const long long s1 = 1, s2 = B.n1t, s3 = (long long)B.n1t * B.n2t;
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int m = 0; m < PHX_RNCONS; m++)
+    for (int k = B.ks(); k <= B.ke(); k++)
+      for (int j = B.js(); j <= B.je(); j++)
+        for (int i = B.is(); i <= B.ie(); i++) {
+          const long long id = B.idx(k, j, i);
+          Real du = (A1 * R.F(0, m, id + s1) - A1 * R.F(0, m, id));
+          if (B.ndim >= 2) du += A2 * R.F(1, m, id + s2) - A2 * R.F(1, m, id);
+          if (B.ndim == 3) du += A3 * R.F(2, m, id + s3) - A3 * R.F(2, m, id);
+          const Real r = -du / V + 0.0;  // + the Minkowski geometric source
+          rb->dudt[m * R.rvs + id] = r;
+          Real u0 = R.U(m, id);
+          u0 = beta * u0 + (1 - beta) * base[m * R.rvs + id];
+          R.U(m, id) = u0;
+          out[m * R.rvs + id] = u0 + bdt * r;
+        }
+}
+
+long long orc_rad_fluid_source(const phx_rad_params *rp, const phx_params *p, const phx_block *fb,
+                               const phx_rad_block *rb, double dt) {
+  const RPar P(*rp, *p);
+  const RBlk R(fb, rb);
+  const orc::Blk &B = R.B;
+  long long applied = 0;
+#pragma omp parallel for collapse(2) schedule(dynamic, 4) reduction(+ : applied)
+  for (int k = B.ks(); k <= B.ke(); k++)
+    for (int j = B.js(); j <= B.je(); j++)
+      for (int i = B.is(); i <= B.ie(); i++) applied += fluid_source(P, R, B.idx(k, j, i), dt);
+  return applied;
+}
+
+void orc_rad_fill_ghosts_periodic(const phx_block *fb, const phx_rad_block *rb) {
+  const RBlk R(fb, rb);
+  phx_block tmp = *fb;
+  tmp.var_stride = R.rvs;
+  orc_fill_ghosts_periodic(&tmp, rb->cons, PHX_RNCONS);
+  orc_fill_ghosts_periodic(&tmp, rb->prim, PHX_RFAIL + 1);
+}
+
+double orc_rad_estimate_timestep(const phx_rad_params *rp, const phx_params *p, const phx_block *fb,
+                                 const phx_rad_block *rb) {
+  const RPar P(*rp, *p);
+  const RBlk R(fb, rb);
+  const orc::Blk &B = R.B;
+  Real min_dt = std::numeric_limits<Real>::max();
+  for (int k = B.ks(); k <= B.ke(); k++)
+    for (int j = B.js(); j <= B.je(); j++)
+      for (int i = B.is(); i <= B.ie(); i++) min_dt = smin(min_dt, zone_dt(P, R, k, j, i));
+  return rp->cfl * min_dt;
+}
+
+double orc_rad_tanh(double x) { return tanh_r(x); }
 
 }  // extern "C"

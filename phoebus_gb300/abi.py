@@ -1,4 +1,5 @@
-"""ctypes mirror of include/phx_fluid.h and loader of the sm_103a libraries.
+"""ctypes mirror of include/phx_fluid.h and include/phx_radiation.h, and
+loader of the sm_103a libraries.
 
 The structures here are byte-for-byte the C structs of the header; the same
 definitions describe host arrays (numpy) and device arrays (torch CUDA
@@ -29,6 +30,12 @@ MLP_IN, MLP_HID, MLP_OUT = 6, 64, 2
 C2P_CHUNK = 1 << 21  # zones per con2prim chunk inside the library (launch accounting only)
 MLP_MAX_EPOCHS = 1024
 MLP_NPARAM = MLP_IN * MLP_HID + MLP_HID + 2 * (MLP_HID * MLP_HID + MLP_HID) + MLP_HID * 2 + 2
+
+# ---- constants (phx_radiation.h)
+RE, RF, RNCONS = 0, 1, 4
+RJ, RH, RXI, RPHI, RFAIL, RKAPPAJ, RKAPPAH, RJBB, RNPRIM = 0, 1, 4, 5, 6, 7, 8, 9, 10
+RAD_METHOD = {"moment_m1": 0, "moment_eddington": 1}
+RAD_ONED_FIXUP = {"none": 0, "ignore_dJ": 1, "ignore_all": 2}
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "con2prim root not bracketed", 3: "NaN input",
           4: "device wait timed out", 5: "CUDA error", 6: "no CUDA device",
@@ -88,6 +95,20 @@ class Mesh(C.Structure):
 
 BC_PERIODIC, BC_OUTFLOW, BC_REFLECT, BC_POLAR = 0, 1, 2, 3
 BC_VARS_CONSERVED, BC_VARS_PRIMITIVE = 0, 1
+
+
+class RadParams(C.Structure):
+    _fields_ = [("method", C.c_int), ("recon", C.c_int), ("cfl", C.c_double), ("closure_frail", C.c_int),
+                ("recon_fixup_bounds", C.c_int), ("src_rootfind_tol", C.c_double),
+                ("src_rootfind_maxiter", C.c_int), ("oned_fixup_strategy", C.c_int), ("kappa_a", C.c_double),
+                ("kappa_s", C.c_double), ("jbb_coeff", C.c_double), ("enable_rad_floors", C.c_int),
+                ("J0_floor", C.c_double), ("enable_rad_ceilings", C.c_int), ("xi0_ceiling", C.c_double),
+                ("tau0_ceiling", C.c_double), ("update_fluid", C.c_int)]
+
+
+class RadBlockS(C.Structure):
+    _fields_ = [("var_stride", C.c_longlong), ("cons", C.c_void_p), ("prim", C.c_void_p), ("flux", C.c_void_p),
+                ("dudt", C.c_void_p)]
 
 
 class MlpTrainOpts(C.Structure):
@@ -158,6 +179,16 @@ _SIGS = {
     "phx_fix_fluxes": (C.c_int, [_P, C.POINTER(Params), C.POINTER(Mesh), C.POINTER(BlockS), C.c_int, _P]),
     "phx_fix_fluxes_block": (C.c_int, [_P, C.POINTER(Params), C.POINTER(BlockS), C.POINTER(C.c_int),
                                        C.POINTER(C.c_int), _P]),
+    "phx_rad_params_default": (None, [C.POINTER(RadParams)]),
+    "phx_rad_prim_to_con": (C.c_int, [_P, C.POINTER(RadParams), C.POINTER(Params), C.POINTER(BlockS), C.POINTER(RadBlockS), Range, Range, Range, _P]),
+    "phx_rad_con_to_prim": (C.c_int, [_P, C.POINTER(RadParams), C.POINTER(Params), C.POINTER(BlockS), C.POINTER(RadBlockS), Range, Range, Range, _P]),
+    "phx_rad_calculate_opacities": (C.c_int, [_P, C.POINTER(RadParams), C.POINTER(Params), C.POINTER(BlockS), C.POINTER(RadBlockS), _P]),
+    "phx_rad_calculate_fluxes": (C.c_int, [_P, C.POINTER(RadParams), C.POINTER(Params), C.POINTER(BlockS), C.POINTER(RadBlockS), _P]),
+    "phx_rad_update": (C.c_int, [_P, C.POINTER(RadParams), C.POINTER(BlockS), C.POINTER(RadBlockS), _P, _P, C.c_double, C.c_double, _P]),
+    "phx_rad_fluid_source": (C.c_int, [_P, C.POINTER(RadParams), C.POINTER(Params), C.POINTER(BlockS), C.POINTER(RadBlockS), C.c_double, _P]),
+    "phx_rad_fill_ghosts_periodic": (C.c_int, [_P, C.POINTER(BlockS), C.POINTER(RadBlockS), _P]),
+    "phx_rad_estimate_timestep": (C.c_int, [_P, C.POINTER(RadParams), C.POINTER(Params), C.POINTER(BlockS), C.POINTER(RadBlockS), _P, _P]),
+    "phx_rad_stage": (C.c_int, [_P, C.POINTER(RadParams), C.POINTER(Params), C.POINTER(BlockS), C.POINTER(RadBlockS), _P, _P, C.c_double, C.c_double, _P]),
     "phx_batch_info": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "phx_mlp_set_weights": (C.c_int, [_P, C.POINTER(C.c_float)]),
     "phx_mlp_get_weights": (C.c_int, [_P, C.POINTER(C.c_float)]),
@@ -166,7 +197,8 @@ _SIGS = {
 
 
 def exported_symbols() -> list[str]:
-    """Every entry point include/phx_fluid.h declares (kept in sync by a test)."""
+    """Every entry point include/phx_fluid.h and include/phx_radiation.h
+    declare (kept in sync by a test)."""
     return sorted(_SIGS)
 
 
@@ -227,3 +259,28 @@ def default_geometry(kind: int, **over) -> Geometry:
     for k, v in over.items():
         setattr(g, k, v)
     return g
+
+
+def default_rad_params(**over) -> RadParams:
+    """phx_rad_params_default (radiation.cpp:340-450, fixup.cpp:75-76,
+    188-215 defaults), then overrides; method / oned_fixup_strategy / recon
+    accept the input-deck strings."""
+    r = RadParams()
+    r.method, r.recon, r.cfl = RAD_METHOD["moment_m1"], RECON["linear"], 0.8
+    r.closure_frail, r.recon_fixup_bounds = 0, 1
+    r.src_rootfind_tol, r.src_rootfind_maxiter, r.oned_fixup_strategy = 1.0e-12, 100, 0
+    r.kappa_a, r.kappa_s, r.jbb_coeff = 0.0, 0.0, 0.0
+    r.enable_rad_floors, r.J0_floor = 0, 0.0
+    r.enable_rad_ceilings, r.xi0_ceiling, r.tau0_ceiling = 0, 0.99, 1.0e3
+    r.update_fluid = 0
+    for k, v in over.items():
+        if k == "method" and isinstance(v, str):
+            v = RAD_METHOD[v]
+        if k == "recon" and isinstance(v, str):
+            v = RECON[v]
+        if k == "oned_fixup_strategy" and isinstance(v, str):
+            v = RAD_ONED_FIXUP[v]
+        if not hasattr(r, k):
+            raise KeyError(k)
+        setattr(r, k, v)
+    return r

@@ -23,7 +23,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 LIB = PKG / "_lib"
 OBJ = PKG / "_build"
-SOURCES = ["phx_api.cu", "phx_c2p.cu", "phx_flux.cu", "phx_stage.cu", "phx_geometry.cu", "phx_mlp.cu", "phx_noalloc.cu", "phx_fixup.cu", "phx_batch.cu"]
+SOURCES = ["phx_api.cu", "phx_c2p.cu", "phx_flux.cu", "phx_stage.cu", "phx_geometry.cu", "phx_mlp.cu", "phx_noalloc.cu", "phx_fixup.cu", "phx_batch.cu", "phx_m1.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAVOURS = {
     "libphx_fluid.so": ["-fmad=true"],
@@ -55,7 +55,7 @@ def build_cuda(force: bool = False, verbose: bool = False, jobs: int | None = No
     """Compile every CUDA source for sm_103a and link both flavours."""
     LIB.mkdir(exist_ok=True)
     OBJ.mkdir(exist_ok=True)
-    headers = sorted(CSRC.glob("*.cuh")) + [ROOT / "include" / "phx_fluid.h"]
+    headers = sorted(CSRC.glob("*.cuh")) + [ROOT / "include" / "phx_fluid.h", ROOT / "include" / "phx_radiation.h"]
     tool = nvcc()
     common = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
                      "-I", str(ROOT / "include")]

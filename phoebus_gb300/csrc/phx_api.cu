@@ -11,6 +11,7 @@
 #include <string>
 #include <vector>
 
+#include "phx_m1.cuh"
 #include "phx_mlp.cuh"
 
 struct phx_ctx {
@@ -903,6 +904,221 @@ phx_status phx_probe_fp64_peak(phx_ctx *ctx, double *flops_out) {
   cudaEventDestroy(e1);
   *flops_out = 2.0 * 8.0 * (double)iters * nthreads / (ms * 1e-3);
   return cuda_status("phx_probe_fp64_peak");
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------
+// Radiation moments (phx_radiation.h)
+// ---------------------------------------------------------------------
+namespace {
+
+phx_status check_rad(const phx_rad_params *rp, const phx_params *p, const phx_block *fb) {
+  if (!rp) return fail(PHX_ERR_INVALID_ARG, "radiation params is NULL");
+  if (rp->method != PHX_RAD_M1 && rp->method != PHX_RAD_EDDINGTON)
+    return fail(PHX_ERR_INVALID_ARG, "invalid radiation method %d (choose moment_m1 or moment_eddington)",
+                rp->method);
+  if (rp->recon < PHX_RECON_CONSTANT || rp->recon > PHX_RECON_MP5)
+    return fail(PHX_ERR_INVALID_ARG, "Invalid Reconstruction option.  Choose from [constant,linear,mp5,weno5,weno5z]");
+  if (rp->oned_fixup_strategy < PHX_RAD_ONED_FIXUP_NONE || rp->oned_fixup_strategy > PHX_RAD_ONED_FIXUP_IGNORE_ALL)
+    return fail(PHX_ERR_INVALID_ARG, "radiation/oned_fixup_strategy has an invalid entry!");
+  if (rp->src_rootfind_maxiter < 0) return fail(PHX_ERR_INVALID_ARG, "src_rootfind_maxiter < 0");
+  if (rp->update_fluid)
+    return fail(PHX_ERR_UNSUPPORTED, "the coupled fluid update of MomentFluidSource is not built (update_fluid = 1)");
+  if (p == nullptr) return fail(PHX_ERR_INVALID_ARG, "params is NULL");
+  if (fb && fb->geom && fb->geom->kind != PHX_GEOM_MINKOWSKI)
+    return fail(PHX_ERR_UNSUPPORTED, "radiation moments are built for Minkowski blocks only");
+  return PHX_OK;
+}
+
+phx::rad::RPar make_rpar(const phx_rad_params &rp, const phx_params &p) {
+  phx::rad::RPar r;
+  std::memset(&r, 0, sizeof(r));
+  r.m1 = rp.method == PHX_RAD_M1;
+  r.robust = !rp.closure_frail;
+  r.bounds = rp.recon_fixup_bounds != 0;
+  r.recon = rp.recon;
+  r.maxiter = rp.src_rootfind_maxiter;
+  r.oned_fixup = rp.oned_fixup_strategy;
+  r.cfl = rp.cfl;
+  r.tol = rp.src_rootfind_tol;
+  r.kappa_a = rp.kappa_a;
+  r.kappa_s = rp.kappa_s;
+  r.jbb = rp.jbb_coeff;
+  // RadiationFloors() / RadiationCeilings() / Ceilings() defaults when
+  // disabled (fixup.hpp:157-273)
+  r.J_floor = rp.enable_rad_floors ? rp.J0_floor : -phx::kDBLMAX;
+  r.xi_ceiling = rp.enable_rad_ceilings ? rp.xi0_ceiling : phx::kDBLMAX;
+  r.tau_max = rp.enable_rad_ceilings ? rp.tau0_ceiling : phx::kDBLMAX;
+  r.W_ceiling = p.enable_ceilings ? p.gam0_ceiling : phx::kDBLMAX;
+  r.Cv = p.Cv;
+  return r;
+}
+
+phx_status make_rview(const phx::BView &v, const phx_rad_block *rb, bool need_flux, phx::rad::RView &r) {
+  if (!rb) return fail(PHX_ERR_INVALID_ARG, "radiation block is NULL");
+  if (!rb->cons || !rb->prim) return fail(PHX_ERR_INVALID_ARG, "radiation cons/prim pointers are NULL");
+  if (need_flux && (!rb->flux || !rb->dudt)) return fail(PHX_ERR_INVALID_ARG, "radiation flux/dudt is NULL");
+  const long long N = (long long)v.n1t * v.n2t * v.n3t;
+  r.vs = rb->var_stride ? rb->var_stride : N;
+  if (r.vs < N) return fail(PHX_ERR_INVALID_ARG, "radiation var_stride smaller than the block");
+  r.cons = rb->cons;
+  r.prim = rb->prim;
+  r.flux = rb->flux;
+  r.dudt = rb->dudt;
+  return PHX_OK;
+}
+
+// fluid block view + radiation view + parameters, validated
+phx_status rad_setup(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_block *fb,
+                     const phx_rad_block *rb, bool need_flux, phx::BView &v, phx::rad::RView &r,
+                     phx::rad::RPar &par) {
+  phx_status s;
+  if ((s = ctx_device(ctx)) || (s = check_rad(rp, p, fb))) return s;
+  if ((s = make_view(fb, v))) return s;
+  if ((s = make_rview(v, rb, need_flux, r))) return s;
+  par = make_rpar(*rp, *p);
+  return PHX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void phx_rad_params_default(phx_rad_params *p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->method = PHX_RAD_M1;
+  p->recon = PHX_RECON_LINEAR;  // radiation/recon default "linear" (radiation.cpp:368)
+  p->cfl = 0.8;                 // radiation/cfl (radiation.cpp:77)
+  p->closure_frail = 0;         // closure_c2p_strategy "robust"
+  p->recon_fixup_bounds = 1;    // recon_fixup_strategy "bounds"
+  p->src_rootfind_tol = 1.e-12;
+  p->src_rootfind_maxiter = 100;
+  p->oned_fixup_strategy = PHX_RAD_ONED_FIXUP_NONE;
+  p->xi0_ceiling = 0.99;
+  p->tau0_ceiling = 1.e3;
+}
+
+phx_status phx_rad_prim_to_con(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_block *fb,
+                               const phx_rad_block *rb, phx_range ib, phx_range jb, phx_range kb, void *stream) {
+  phx::BView v;
+  phx::rad::RView r;
+  phx::rad::RPar par;
+  phx::Range3 rg;
+  phx_status s;
+  if ((s = rad_setup(ctx, rp, p, fb, rb, false, v, r, par)) || (s = check_range(v, ib, jb, kb, rg))) return s;
+  phx::rad::launch_p2c(par, v, r, rg, S(stream));
+  return cuda_status("phx_rad_prim_to_con");
+}
+
+phx_status phx_rad_con_to_prim(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_block *fb,
+                               const phx_rad_block *rb, phx_range ib, phx_range jb, phx_range kb, void *stream) {
+  phx::BView v;
+  phx::rad::RView r;
+  phx::rad::RPar par;
+  phx::Range3 rg;
+  phx_status s;
+  if ((s = rad_setup(ctx, rp, p, fb, rb, false, v, r, par)) || (s = check_range(v, ib, jb, kb, rg))) return s;
+  phx::rad::launch_c2p(par, v, r, rg, S(stream));
+  return cuda_status("phx_rad_con_to_prim");
+}
+
+phx_status phx_rad_calculate_opacities(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p,
+                                       const phx_block *fb, const phx_rad_block *rb, void *stream) {
+  phx::BView v;
+  phx::rad::RView r;
+  phx::rad::RPar par;
+  phx_status s;
+  if ((s = rad_setup(ctx, rp, p, fb, rb, false, v, r, par))) return s;
+  phx::rad::launch_opacities(par, v, r, S(stream));
+  return cuda_status("phx_rad_calculate_opacities");
+}
+
+phx_status phx_rad_calculate_fluxes(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p,
+                                    const phx_block *fb, const phx_rad_block *rb, void *stream) {
+  phx::BView v;
+  phx::rad::RView r;
+  phx::rad::RPar par;
+  phx_status s;
+  if ((s = rad_setup(ctx, rp, p, fb, rb, true, v, r, par))) return s;
+  if (v.ng < 3) return fail(PHX_ERR_INVALID_ARG, "radiation fluxes need ng >= 3");
+  phx::rad::launch_fluxes(par, v, r, S(stream));
+  return cuda_status("phx_rad_calculate_fluxes");
+}
+
+phx_status phx_rad_update(phx_ctx *ctx, const phx_rad_params *rp, const phx_block *fb, const phx_rad_block *rb,
+                          const double *base, double *out, double beta, double dt, void *stream) {
+  phx_status s;
+  if ((s = ctx_device(ctx))) return s;
+  if (!rp) return fail(PHX_ERR_INVALID_ARG, "radiation params is NULL");
+  phx::BView v;
+  phx::rad::RView r;
+  if ((s = make_view(fb, v)) || (s = make_rview(v, rb, true, r))) return s;
+  if (!base || !out) return fail(PHX_ERR_INVALID_ARG, "base/out is NULL");
+  phx::rad::launch_update(v, r, base, out, beta, dt, S(stream));
+  return cuda_status("phx_rad_update");
+}
+
+phx_status phx_rad_fluid_source(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_block *fb,
+                                const phx_rad_block *rb, double dt, void *stream) {
+  phx::BView v;
+  phx::rad::RView r;
+  phx::rad::RPar par;
+  phx_status s;
+  if ((s = rad_setup(ctx, rp, p, fb, rb, false, v, r, par))) return s;
+  phx::rad::launch_source(par, v, r, dt, S(stream));
+  return cuda_status("phx_rad_fluid_source");
+}
+
+phx_status phx_rad_fill_ghosts_periodic(phx_ctx *ctx, const phx_block *fb, const phx_rad_block *rb, void *stream) {
+  phx_status s;
+  if ((s = ctx_device(ctx))) return s;
+  phx::BView v;
+  phx::rad::RView r;
+  if ((s = make_view(fb, v)) || (s = make_rview(v, rb, false, r))) return s;
+  phx::rad::launch_ghosts(v, r, S(stream));
+  return cuda_status("phx_rad_fill_ghosts_periodic");
+}
+
+phx_status phx_rad_estimate_timestep(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p,
+                                     const phx_block *fb, const phx_rad_block *rb, double *dt_out_device,
+                                     void *stream) {
+  phx::BView v;
+  phx::rad::RView r;
+  phx::rad::RPar par;
+  phx_status s;
+  if ((s = rad_setup(ctx, rp, p, fb, rb, false, v, r, par))) return s;
+  if (!dt_out_device) return fail(PHX_ERR_INVALID_ARG, "dt_out is NULL");
+  phx::rad::launch_dt(par, v, r, ctx->dt_scr, dt_out_device, S(stream));
+  return cuda_status("phx_rad_estimate_timestep");
+}
+
+phx_status phx_rad_stage(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_block *fb,
+                         const phx_rad_block *rb, const double *base, double *out, double beta, double dt,
+                         void *stream) {
+  phx::BView v;
+  phx::rad::RView r;
+  phx::rad::RPar par;
+  phx_status s;
+  if ((s = rad_setup(ctx, rp, p, fb, rb, true, v, r, par))) return s;
+  if (!base || !out) return fail(PHX_ERR_INVALID_ARG, "base/out is NULL");
+  if (v.ng < 3) return fail(PHX_ERR_INVALID_ARG, "radiation fluxes need ng >= 3");
+  if (p->enable_floors || p->enable_c2p_fixup)
+    return fail(PHX_ERR_UNSUPPORTED,
+                "radiation floors in ApplyFloors and RadConservedToPrimitiveFixup are not built "
+                "(fixup/enable_floors and fixup/enable_c2p_fixup must be off)");
+  cudaStream_t st = S(stream);
+  phx::rad::launch_opacities(par, v, r, st);
+  phx::rad::launch_fluxes(par, v, r, st);
+  phx::rad::launch_update(v, r, base, out, beta, dt, st);
+  phx::rad::RView ro = r;
+  ro.cons = out;
+  phx::rad::launch_c2p(par, v, ro, interior(v), st);
+  phx::rad::launch_source(par, v, ro, beta * dt, st);
+  phx::rad::launch_ghosts(v, ro, st);
+  phx::rad::launch_c2p(par, v, ro, entire(v), st);
+  return cuda_status("phx_rad_stage");
 }
 
 }  // extern "C"

@@ -1,0 +1,924 @@
+// phx_m1.cu -- radiation moment transport (M1 and Eddington closures) on the
+// device: one neutrino species, Minkowski metric, static fluid background.
+//
+// Follows, in the reference's floating-point operation order (paths relative
+// to the phoebus tree): radiation/closure.hpp:49-352 (ClosureEdd),
+// closure_m1.hpp:31-372 (ClosureM1), local_three_geometry.hpp:140-185,
+// linear_algebra.hpp:58-96, moments.cpp:61-995, moments_source.cpp:152-958
+// (oned solver, update_fluid = false), radiation.cpp:681-733,
+// root_find.hpp:111-160.  With the identity spatial metric each contraction
+// keeps the order of its non-zero terms (for finite values the zero terms of
+// the full 3x3 sums change no rounding).  std::pow(x, 2) and std::pow(x, 3)
+// are products, and tanh is written out (Cody-Waite reduction + Taylor
+// series) so that a CPU build without FMA contraction gives the same bits.
+//
+// One thread per zone (con2prim, source, prim2con, update) or per face
+// (fluxes).  The fluxes of a face need only the row d of the pressure
+// tensors P^i_j of its direction; the other rows are not formed.
+#include <cfloat>
+
+#include "phx_m1.cuh"
+
+namespace phx {
+namespace rad {
+
+// std::min / std::max (NaN handling of the reference)
+__device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b : a; }
+__device__ __forceinline__ double smax(double a, double b) { return (a < b) ? b : a; }
+__device__ __forceinline__ double sgn(double v) { return (double)((0.0 <= v) - (v < 0.0)); }
+
+// tanh: e^y by Cody-Waite reduction y = n ln2 + r (32-bit head of ln2, so
+// n * head is exact) and the Taylor series of e^r to degree 13; e^y - 1 by its
+// Taylor series to degree 14 for |y| < 1/4; tanh x = -m / (2 + m) with
+// m = e^{-2|x|} - 1.
+constexpr double LN2_HI = 0.693147180369123816490;
+constexpr double LN2_LO = 1.9082149292705877000e-10;
+constexpr double INV_LN2 = 1.4426950408889634074;
+__device__ __forceinline__ double exp_taylor(double r) {
+  double p = 1.0 / 6227020800.0;
+  p = p * r + 1.0 / 479001600.0;
+  p = p * r + 1.0 / 39916800.0;
+  p = p * r + 1.0 / 3628800.0;
+  p = p * r + 1.0 / 362880.0;
+  p = p * r + 1.0 / 40320.0;
+  p = p * r + 1.0 / 5040.0;
+  p = p * r + 1.0 / 720.0;
+  p = p * r + 1.0 / 120.0;
+  p = p * r + 1.0 / 24.0;
+  p = p * r + 1.0 / 6.0;
+  p = p * r + 0.5;
+  p = p * r + 1.0;
+  p = p * r + 1.0;
+  return p;
+}
+__device__ __forceinline__ double expm1_small(double y) {
+  double p = 1.0 / 87178291200.0;
+  p = p * y + 1.0 / 6227020800.0;
+  p = p * y + 1.0 / 479001600.0;
+  p = p * y + 1.0 / 39916800.0;
+  p = p * y + 1.0 / 3628800.0;
+  p = p * y + 1.0 / 362880.0;
+  p = p * y + 1.0 / 40320.0;
+  p = p * y + 1.0 / 5040.0;
+  p = p * y + 1.0 / 720.0;
+  p = p * y + 1.0 / 120.0;
+  p = p * y + 1.0 / 24.0;
+  p = p * y + 1.0 / 6.0;
+  p = p * y + 0.5;
+  p = p * y + 1.0;
+  return p * y;
+}
+__device__ __forceinline__ double exp_neg(double y) {
+  const double n = floor(y * INV_LN2 + 0.5);
+  const double r = (y - n * LN2_HI) - n * LN2_LO;
+  return ldexp(exp_taylor(r), (int)n);
+}
+__device__ __forceinline__ double tanh_r(double x) {
+  const double ax = fabs(x);
+  double t;
+  if (ax > 22.0) {
+    t = 1.0;
+  } else {
+    const double y = -2.0 * ax;
+    const double m = (y > -0.25) ? expm1_small(y) : exp_neg(y) - 1.0;
+    t = -m / (2.0 + m);
+  }
+  return copysign(t, x);
+}
+
+struct V3 {
+  double d[3];
+};
+struct T2 {
+  double d[3][3];
+};
+
+__device__ __forceinline__ double ccov(const V3 &a, const V3 &b) {
+  double s = 0.0;
+#pragma unroll
+  for (int i = 0; i < 3; i++) s += a.d[i] * b.d[i];
+  return s;
+}
+__device__ __forceinline__ double gdelta(int i, int j) { return i == j ? 1.0 : 0.0; }
+__device__ __forceinline__ double dop(double a, double b, double c, double d) {  // DifferenceOfProducts
+  const double cd = c * d;
+  const double err = fma(-c, d, cd);
+  const double dp = fma(a, b, -cd);
+  return dp + err;
+}
+__device__ __forceinline__ double lorentz3(const double vp[3]) {
+  double vsq = 0.;
+#pragma unroll
+  for (int i = 0; i < 3; i++) vsq += vp[i] * vp[i];
+  return sqrt(1. + vsq);
+}
+
+enum { SUCCESS = 0, FAILURE = 1, MODIFIED = 2 };
+constexpr double PI = 3.141592653589793;
+constexpr double SIN_PI = 1.2246467991473532e-16;
+
+template <bool M1>
+struct Closure {
+  V3 con_v, cov_v;
+  double W, W2;
+  bool robust;
+  __device__ __forceinline__ Closure(const V3 &cv, bool rob) : robust(rob) {
+    con_v = cv;
+#pragma unroll
+    for (int i = 0; i < 3; i++) cov_v.d[i] = 0.0 + cv.d[i];
+    double v2 = 0.0;
+#pragma unroll
+    for (int i = 0; i < 3; i++) v2 += con_v.d[i] * cov_v.d[i];
+    v2 = smin(v2, 0.9999);
+    W = 1 / sqrt(1 - v2);
+    W2 = W * W;
+  }
+  __device__ __forceinline__ void contractions(const T2 &Pi, V3 &cov_vPi, double &vvPi) const {
+    vvPi = 0.0;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      double c = 0.0;
+#pragma unroll
+      for (int j = 0; j < 3; j++) c += cov_v.d[j] * Pi.d[i][j];
+      vvPi += cov_v.d[i] * c;
+      cov_vPi.d[i] = 0.0 + c;
+    }
+  }
+  __device__ __forceinline__ void linear_source_update(double Estar, const V3 &Fs, const T2 &Pi, double JBB,
+                                                       double tauJ, double tauH, double &dE, V3 &dF) const {
+    double vvPi;
+    V3 cvPi;
+    contractions(Pi, cvPi, vvPi);
+    double A00 = (4 * W2 - 1) / 3 + W2 * vvPi + W * tauJ;
+    double A01 = 2 * W + tauH;
+    double A10 = A00 - 1 - tauJ / W;
+    double A11 = A01 - 1 / W;
+    const double vFs = ccov(con_v, Fs);
+    const double b0 = Estar + W * tauJ * JBB;
+    const double b1 = vFs + (W2 - 1) / W * tauJ * JBB;
+    const double invDet = 1.0 / dop(A00, A11, A01, A10);
+    const double J = invDet * dop(A11, b0, A01, b1);
+    const double zeta = invDet * dop(A00, b1, A10, b0);
+    dE = (4 * W2 - 1 + 3 * W2 * vvPi) / 3 * J + 2 * W * zeta - Estar;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+      dF.d[i] = (cov_v.d[i] * tauH * (4 * W2 / 3 * J + W * zeta) + tauH * cvPi.d[i] * J +
+                 tauJ * W2 * cov_v.d[i] * (JBB - J) + W * Fs.d[i]) /
+                    (W + tauH) -
+                Fs.d[i];
+  }
+  __device__ __forceinline__ void prim2con(double J, const V3 &H, const T2 &Pi, double &E, V3 &F) const {
+    double vvPi;
+    V3 cvPi;
+    contractions(Pi, cvPi, vvPi);
+    const double vH = ccov(con_v, H);
+    E = (4 * W2 - 1 + 3 * W2 * vvPi) / 3 * J + 2 * W * vH;
+#pragma unroll
+    for (int i = 0; i < 3; i++) F.d[i] = 4 * W2 / 3 * cov_v.d[i] * J + W * cov_v.d[i] * vH + W * H.d[i] + J * cvPi.d[i];
+  }
+  // row d of ClosureEdd::getConCovPFromPrim (lapse 1)
+  __device__ __forceinline__ void concov_p_row(double J, const V3 &H, const T2 &Pi, int d, double P[3]) const {
+    const double conH_d = 0.0 + H.d[d];
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+      P[j] = 4.0 / 3.0 * W2 * con_v.d[d] * cov_v.d[j] * J + W * (con_v.d[d] * H.d[j] + cov_v.d[j] * conH_d) +
+             J * (0.0 + Pi.d[d][j]);
+    P[d] += J / 3.0;
+  }
+  __device__ __forceinline__ int con2prim(double E, const V3 &F, const T2 &Pi, double &J, V3 &H) const {
+    double vvPi;
+    V3 cvPi;
+    contractions(Pi, cvPi, vvPi);
+    const double vF = ccov(con_v, F);
+    const double lam = (2.0 * W2 + 1.0) / 3.0 + (2.0 * W2 - 3.0) * W2 * vvPi;
+    const double a = ratio(W2, lam) * ((4 * W2 / 3 - vvPi) * E - ((4 * W2 + 1) / 3 - W2 * vvPi) * vF);
+    J = ratio((2 * W2 - 1) * E - 2 * W2 * vF, lam);
+#pragma unroll
+    for (int i = 0; i < 3; i++) H.d[i] = (F.d[i] - J * cvPi.d[i] - cov_v.d[i] * a) / W;
+    const double vh = ccov(con_v, H);
+    const double xi = sqrt(ccov(H, H) - vh * vh) / J;
+    if (isnan(xi) || isnan(J)) return FAILURE;
+    if (J < 0. || xi >= 1.0) {
+      if (robust) {
+        if (J < 0.) J = smin(J, 10. * kSMALL);
+        if (xi >= 1.0) {
+#pragma unroll
+          for (int i = 0; i < 3; i++) H.d[i] *= 0.999 / xi;
+        }
+        return MODIFIED;
+      }
+      return FAILURE;
+    }
+    return SUCCESS;
+  }
+  __device__ __forceinline__ static double closure_fn(double xi) {
+    return (1.0 - 2 * (xi * xi) + 4 * (xi * xi * xi)) / 3.0;
+  }
+  __device__ __forceinline__ void tilpi_fill(const double f[3], double athin, T2 &Pi) const {
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        Pi.d[i][j] = f[i] * f[j] - (W2 * con_v.d[i] * con_v.d[j] + gdelta(i, j)) / 3;
+        Pi.d[i][j] *= athin;
+      }
+  }
+  // GetConTilPiFromPrim
+  __device__ __forceinline__ void tilpi_from_prim(double J, const V3 &H, T2 &Pi) const {
+    if constexpr (!M1) {
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) Pi.d[i][j] = 0.0;
+    } else {
+      double Hm = 0.0, vH = 0.0;
+#pragma unroll
+      for (int i = 0; i < 3; i++) Hm += H.d[i] * (0.0 + H.d[i]);
+#pragma unroll
+      for (int i = 0; i < 3; i++) vH += H.d[i] * con_v.d[i];
+      Hm = sqrt(Hm - vH * vH);
+      double f[3];
+#pragma unroll
+      for (int i = 0; i < 3; i++) f[i] = ratio(0.0 + H.d[i], Hm);
+      const double xi = smax(smin(1.0, ratio(Hm, J)), 0.0);
+      tilpi_fill(f, 0.5 * (3 * closure_fn(xi) - 1), Pi);
+    }
+  }
+  __device__ __forceinline__ void angles_pressure(double xi, double phi, const V3 &g, const V3 &dd, T2 &Pi,
+                                                  double f[3]) const {
+    double s, c;
+    if (phi == PI) {
+      s = SIN_PI;
+      c = -1.0;
+    } else {
+      s = sin(phi);
+      c = cos(phi);
+    }
+#pragma unroll
+    for (int i = 0; i < 3; i++) f[i] = -c * g.d[i] + s * dd.d[i];
+    tilpi_fill(f, 0.5 * (3 * closure_fn(xi) - 1), Pi);
+  }
+  __device__ __forceinline__ void basis(const V3 &F, V3 &g, V3 &dd) const {
+    double Fmag = 0.0, vl = 0.0, vv = 0.0;
+#pragma unroll
+    for (int i = 0; i < 3; i++) Fmag += F.d[i] * (0.0 + F.d[i]);
+    Fmag = sqrt(Fmag);
+#pragma unroll
+    for (int i = 0; i < 3; i++) vl += F.d[i] * con_v.d[i];
+    vl = ratio(vl, Fmag);
+#pragma unroll
+    for (int i = 0; i < 3; i++) vv += cov_v.d[i] * con_v.d[i];
+    const double lam = ratio(1.0, W * (1 - vl));
+    const double aa = sqrt(vv * (1 + 10 * DBL_EPSILON) - vl * vl);
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const double cF = 0.0 + F.d[i];
+      g.d[i] = ratio(cF * lam, Fmag) - W * con_v.d[i];
+      dd.d[i] = ratio(ratio(cF, Fmag) * (1 - lam / W) + con_v.d[i], aa);
+    }
+  }
+  __device__ __forceinline__ double residual(double E, const V3 &F, double xi, double phi, const V3 &g,
+                                             const V3 &dd) const {
+    T2 Pi;
+    double f[3];
+    angles_pressure(xi, phi, g, dd, Pi, f);
+    double J;
+    V3 H;
+    con2prim(E, F, Pi, J, H);
+    double Hm = 0.0, vH = 0.0;
+#pragma unroll
+    for (int i = 0; i < 3; i++) Hm += H.d[i] * H.d[i];
+#pragma unroll
+    for (int i = 0; i < 3; i++) vH += con_v.d[i] * H.d[i];
+    Hm = sqrt(Hm - vH * vH);
+    return xi - ratio(Hm, J);
+  }
+  // SolveClosure with phi held at pi (the reference's update rule keeps it
+  // there); the phi-perturbed residuals only feed the discarded 2x2 solve.
+  __device__ __forceinline__ void solve_closure(double E, V3 F, double &xi_io, double &phi_out) const {
+    const int max_iter = 30;
+    const double tol = 1.e6 * DBL_EPSILON;
+    const double eps = sqrt(10 * DBL_EPSILON);
+    const double delta = 20 * DBL_EPSILON;
+#pragma unroll
+    for (int i = 0; i < 3; i++) F.d[i] = ratio(F.d[i], E) + 1.e3 * sgn(F.d[i]) * DBL_MIN;
+    E = 1.0;
+    V3 g, dd;
+    basis(F, g, dd);
+    int iter = 0;
+    double fXi = 1.e3, fPhi = 1.e3;
+    double xi = xi_io, phi = PI;
+    do {
+      const double xi_up = smin(xi * (1.0 + eps) + delta, 1.0);
+      const double xi_lo = smax(xi * (1.0 - eps) - delta, 0.0);
+      const double f_up = residual(E, F, xi_up, phi, g, dd);
+      const double f_lo = residual(E, F, xi_lo, phi, g, dd);
+      const double J00 = (f_up - f_lo) / (xi_up - xi_lo);
+      fXi = residual(E, F, xi, phi, g, dd);
+      const double dx0 = fXi / J00, dx1 = 0.0;
+      fPhi = 0.0;
+      double cdx = smin(dx0, xi - delta * xi);
+      cdx = smax(cdx, xi - (1 - delta * (1 - xi)));
+      double alpha = ratio(cdx, dx0);
+      alpha = smin(alpha, 0.5 * 3.14159 / fabs(dx1));
+      xi -= alpha * dx0;
+      phi -= alpha * dx1;
+      ++iter;
+    } while (iter < max_iter && (fabs(fXi) > tol || fabs(fPhi) > tol));
+    xi_io = xi;
+    phi_out = phi;
+  }
+  // GetConTilPiFromCon
+  __device__ __forceinline__ void tilpi_from_con(double E, const V3 &F, double &xi, double &phi, T2 &Pi) const {
+    if constexpr (!M1) {
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) Pi.d[i][j] = 0.0;
+      xi = 0.0;
+      phi = PI;
+    } else {
+      solve_closure(E, F, xi, phi);
+      V3 g, dd;
+      basis(F, g, dd);
+      double f[3];
+      angles_pressure(xi, phi, g, dd, Pi, f);
+    }
+  }
+};
+
+// ---------------------------------------------------------------- views
+__device__ __forceinline__ V3 fluid_v(const BView &b, long long id, double *Wout = nullptr) {
+  const double vp[3] = {b.prim[PHX_PVEL * b.vs + id], b.prim[(PHX_PVEL + 1) * b.vs + id],
+                        b.prim[(PHX_PVEL + 2) * b.vs + id]};
+  const double W = lorentz3(vp);
+  if (Wout) *Wout = W;
+  V3 v;
+  v.d[0] = vp[0] / W;
+  v.d[1] = vp[1] / W;
+  v.d[2] = vp[2] / W;
+  return v;
+}
+__device__ __forceinline__ void zone_of(const Range3 &r, long long t, int &k, int &j, int &i) {
+  const int ni = r.ie - r.is + 1, nj = r.je - r.js + 1;
+  i = r.is + (int)(t % ni);
+  j = r.js + (int)((t / ni) % nj);
+  k = r.ks + (int)(t / ((long long)ni * nj));
+}
+__host__ __device__ inline long long range_count(const Range3 &r) {
+  return (long long)(r.ie - r.is + 1) * (r.je - r.js + 1) * (r.ke - r.ks + 1);
+}
+
+// ---------------------------------------------------- MomentPrim2Con
+template <bool M1>
+__global__ void __launch_bounds__(128) k_p2c(RPar p, BView b, RView r, Range3 rg) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= range_count(rg)) return;
+  int k, j, i;
+  zone_of(rg, t, k, j, i);
+  const long long id = b.idx(k, j, i), vs = r.vs;
+  const Closure<M1> c(fluid_v(b, id), true);
+  const double J = r.prim[PHX_RJ * vs + id];
+  V3 H;
+#pragma unroll
+  for (int a = 0; a < 3; a++) H.d[a] = r.prim[(PHX_RH + a) * vs + id] * J;
+  T2 Pi;
+  c.tilpi_from_prim(J, H, Pi);
+  double E;
+  V3 F;
+  c.prim2con(J, H, Pi, E, F);
+  r.cons[PHX_RE * vs + id] = 1.0 * E;
+#pragma unroll
+  for (int a = 0; a < 3; a++) r.cons[(PHX_RF + a) * vs + id] = 1.0 * F.d[a];
+}
+
+// ---------------------------------------------------- MomentCon2Prim
+template <bool M1>
+__global__ void __launch_bounds__(128) k_c2p(RPar p, BView b, RView r, Range3 rg) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= range_count(rg)) return;
+  int k, j, i;
+  zone_of(rg, t, k, j, i);
+  const long long id = b.idx(k, j, i), vs = r.vs;
+  const double isdetgam = 1.0 / 1.0;
+  const Closure<M1> c(fluid_v(b, id), p.robust != 0);
+  double E = r.cons[PHX_RE * vs + id] * isdetgam;
+  V3 F;
+#pragma unroll
+  for (int a = 0; a < 3; a++) F.d[a] = r.cons[(PHX_RF + a) * vs + id] * isdetgam;
+  double xi = 0.0, phi = PI;
+  if constexpr (M1) {
+    xi = r.prim[PHX_RXI * vs + id];
+    phi = 1.0001 * r.prim[PHX_RPHI * vs + id];
+  }
+  T2 Pi;
+  c.tilpi_from_con(E, F, xi, phi, Pi);
+  if constexpr (M1) {
+    r.prim[PHX_RXI * vs + id] = xi;
+    r.prim[PHX_RPHI * vs + id] = phi;
+  }
+  double J;
+  V3 H;
+  int st = c.con2prim(E, F, Pi, J, H);
+  if (st == MODIFIED) {
+    c.prim2con(J, H, Pi, E, F);
+    r.cons[PHX_RE * vs + id] = E / isdetgam;
+#pragma unroll
+    for (int a = 0; a < 3; a++) r.cons[(PHX_RF + a) * vs + id] = F.d[a] / isdetgam;
+    st = SUCCESS;
+  }
+  r.prim[PHX_RJ * vs + id] = J;
+#pragma unroll
+  for (int a = 0; a < 3; a++) r.prim[(PHX_RH + a) * vs + id] = ratio(H.d[a], J);
+  r.prim[PHX_RFAIL * vs + id] = st == SUCCESS ? 1.0 : 0.0;
+}
+
+// ------------------------------------------ MomentCalculateOpacities
+__global__ void __launch_bounds__(256) k_opacities(RPar p, BView b, RView r, long long n) {
+  const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= n) return;
+  const double rho = b.prim[PHX_PRHO * b.vs + id], T = b.prim[PHX_PTMP * b.vs + id];
+  const double kJ = rho * p.kappa_a;
+  const double kH = kJ + rho * p.kappa_s;
+  r.prim[PHX_RJBB * r.vs + id] = p.jbb * (T * T) * (T * T);
+  r.prim[PHX_RKAPPAJ * r.vs + id] = kJ;
+  r.prim[PHX_RKAPPAH * r.vs + id] = kH;
+}
+
+// --------------------------------------------------------- fluxes
+// One face state: E, F_i, and the flux of direction d (con_F^d and row d of
+// P^i_j) for the closure's velocity, J and H_i.
+template <bool M1>
+__device__ __forceinline__ void face_state(const Closure<M1> &c, double J, const V3 &H, int d, double &E, V3 &F,
+                                           double &Fd, double P[3]) {
+  T2 Pi;
+  c.tilpi_from_prim(J, H, Pi);
+  c.concov_p_row(J, H, Pi, d, P);
+  c.prim2con(J, H, Pi, E, F);
+  Fd = 0.0 + F.d[d];
+}
+
+template <bool M1, int RECON>
+__global__ void __launch_bounds__(128) k_fluxes(RPar p, BView b, RView r, int d, Range3 rg) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= range_count(rg)) return;
+  int k, j, i;
+  zone_of(rg, t, k, j, i);
+  const long long vs = r.vs, fvs = b.vs;
+  const long long st = d == 0 ? 1 : (d == 1 ? (long long)b.n1t : (long long)b.n1t * b.n2t);
+  const long long id = b.idx(k, j, i), idm = id - st;
+  // reconstruction: J, H/J (rad prims 0..3) and u^i (fluid prims 1..3)
+  double ql[7], qr[7];
+#pragma unroll
+  for (int n = 0; n < 7; n++) {
+    const double *base = n < 4 ? r.prim + n * vs : b.prim + (PHX_PVEL + n - 4) * fvs;
+    const double q0 = base[idm - 2 * st], q1 = base[idm - st], q2 = base[idm], q3 = base[id], q4 = base[id + st],
+                 q5 = base[id + 2 * st];
+    double a, c;
+    recon<RECON>(q0, q1, q2, q3, q4, ql[n], a);
+    recon<RECON>(q1, q2, q3, q4, q5, c, qr[n]);
+  }
+  // dJ at the face (moments.cpp:412-455)
+  const int dj = b.ndim > 1 ? 1 : 0, dk = b.ndim > 2 ? 1 : 0;
+  const double *Jp = r.prim + PHX_RJ * vs;
+  auto Jat = [&](int kk, int jj, int ii) { return Jp[b.idx(kk, jj, ii)]; };
+  const double idx = 1.0 / b.dx[0], idx4 = 0.25 * idx;
+  const double idy = 1.0 / b.dx[1], idy4 = 0.25 * idy;
+  const double idz = 1.0 / b.dx[2], idz4 = 0.25 * idz;
+  V3 dJ;
+  if (d == 0) {
+    dJ.d[0] = (Jat(k, j, i) - Jat(k, j, i - 1)) * idx;
+    dJ.d[1] = (Jat(k, j + dj, i) + Jat(k, j + dj, i - 1) - Jat(k, j - dj, i) - Jat(k, j - dj, i - 1)) * idy4;
+    dJ.d[2] = (Jat(k + dk, j, i) + Jat(k + dk, j, i - 1) - Jat(k - dk, j, i) - Jat(k - dk, j, i - 1)) * idz4;
+  } else if (d == 1) {
+    dJ.d[0] = (Jat(k, j, i + 1) + Jat(k, j - dj, i + 1) - Jat(k, j, i - 1) - Jat(k, j - dj, i - 1)) * idx4;
+    dJ.d[1] = (Jat(k, j, i) - Jat(k, j - dj, i)) * idy;
+    dJ.d[2] = (Jat(k + dk, j, i) + Jat(k + dk, j - dj, i) - Jat(k - dk, j, i) - Jat(k - dk, j - dj, i)) * idz4;
+  } else {
+    dJ.d[0] = (Jat(k, j, i + 1) + Jat(k - dk, j, i + 1) - Jat(k, j, i - 1) - Jat(k - dk, j, i - 1)) * idx4;
+    dJ.d[1] = (Jat(k, j + dj, i) + Jat(k - dk, j + dj, i) - Jat(k, j - dj, i) - Jat(k - dk, j - dj, i)) * idy4;
+    dJ.d[2] = (Jat(k, j, i) - Jat(k - dk, j, i)) * idz;
+  }
+  const double dx = b.dx[d] * sqrt(1.0);
+  double vpl[3] = {ql[4], ql[5], ql[6]}, vpr[3] = {qr[4], qr[5], qr[6]};
+  double Wl = lorentz3(vpl), Wr = lorentz3(vpr);
+  if (p.bounds) {
+    if (Wl > p.W_ceiling) {
+      const double rescale = sqrt(p.W_ceiling * p.W_ceiling - 1.) / (Wl * Wl - 1.);
+#pragma unroll
+      for (int a = 0; a < 3; a++) vpl[a] *= rescale;
+      Wl = p.W_ceiling;
+    }
+    if (Wr > p.W_ceiling) {
+      const double rescale = sqrt(p.W_ceiling * p.W_ceiling - 1.) / (Wr * Wr - 1.);
+#pragma unroll
+      for (int a = 0; a < 3; a++) vpr[a] *= rescale;
+      Wr = p.W_ceiling;
+    }
+  }
+  V3 vl, vr;
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    vl.d[a] = vpl[a] / Wl;
+    vr.d[a] = vpr[a] / Wr;
+  }
+  const double sigp = 1.0 * sqrt(1.0) - 0.0;
+  const double sigm = -1.0 * sqrt(1.0) - 0.0;
+  const double asym_sigl = 1.0 * vl.d[d] - 0.0;
+  const double asym_sigr = 1.0 * vr.d[d] - 0.0;
+  double Jl = ql[0], Jr = qr[0];
+  if (p.bounds) {
+    Jl = smax(Jl, p.J_floor);
+    Jr = smax(Jr, p.J_floor);
+  }
+  V3 Hl, Hr;
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    Hl.d[a] = Jl * ql[1 + a];
+    Hr.d[a] = Jr * qr[1 + a];
+  }
+  if (p.bounds) {
+    const double vhl = ccov(vl, Hl), vhr = ccov(vr, Hr);
+    const double xil = sqrt(ccov(Hl, Hl) - vhl * vhl) / Jl;
+    const double xir = sqrt(ccov(Hr, Hr) - vhr * vhr) / Jr;
+    if (xil > p.xi_ceiling) {
+#pragma unroll
+      for (int a = 0; a < 3; a++) Hl.d[a] *= p.xi_ceiling / xil;
+    }
+    if (xir > p.xi_ceiling) {
+#pragma unroll
+      for (int a = 0; a < 3; a++) Hr.d[a] *= p.xi_ceiling / xir;
+    }
+  }
+  const double *kH = r.prim + PHX_RKAPPAH * vs;
+  const double kappaH = sqrt(kH[id] * kH[idm]);
+  const double aw = tanh_r(ratio(1.0, fabs(kappaH * dx)));
+  const double kappaH_min = 1.e-20;
+  V3 Has;
+#pragma unroll
+  for (int a = 0; a < 3; a++) Has.d[a] = ratio(-dJ.d[a], 3 * kappaH + 3 * kappaH_min);
+  const Closure<M1> cl(vl, true), cr(vr, true);
+  double El, Er, Fdl, Fdr, Fdl_a, Fdr_a, Pl[3], Pr[3], Pl_a[3], Pr_a[3], Ed;
+  V3 Fl, Fr, Fd_scr;
+  face_state(cl, Jl, Has, d, Ed, Fd_scr, Fdl_a, Pl_a);
+  face_state(cr, Jr, Has, d, Ed, Fd_scr, Fdr_a, Pr_a);
+  face_state(cl, Jl, Hl, d, El, Fl, Fdl, Pl);
+  face_state(cr, Jr, Hr, d, Er, Fr, Fdr, Pr);
+  Fdl = aw * Fdl + (1 - aw) * Fdl_a;
+  Fdr = aw * Fdr + (1 - aw) * Fdr_a;
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    Pl[a] = aw * Pl[a] + (1 - aw) * Pl_a[a];
+    Pr[a] = aw * Pr[a] + (1 - aw) * Pr_a[a];
+  }
+  const double rad_sigspeed = smax(fabs(sigm), fabs(sigp));
+  const double asym_sigspeed = smax(fabs(asym_sigl), fabs(asym_sigr));
+  const double sigspeed = aw * rad_sigspeed + (1. - aw) * asym_sigspeed;
+  Fdl -= 0.0 * El;
+  Fdr -= 0.0 * Er;
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    Pl[a] -= 0.0 * Fl.d[a];
+    Pr[a] -= 0.0 * Fr.d[a];
+  }
+  double *fl = r.flux + (long long)d * PHX_RNCONS * vs;
+  fl[PHX_RE * vs + id] = 0.5 * 1.0 * (Fdl + Fdr + sigspeed * (El - Er));
+#pragma unroll
+  for (int a = 0; a < 3; a++) fl[(PHX_RF + a) * vs + id] = 0.5 * 1.0 * (Pl[a] + Pr[a] + sigspeed * (Fl.d[a] - Fr.d[a]));
+}
+
+// ------------------------------------------ divergence + RK update
+__global__ void __launch_bounds__(256) k_update(BView b, RView r, const double *base, double *out, double beta,
+                                                double dt, Range3 rg) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= range_count(rg)) return;
+  int k, j, i;
+  zone_of(rg, t, k, j, i);
+  const long long id = b.idx(k, j, i), vs = r.vs;
+  const double dx1 = b.dx[0], dx2 = b.dx[1], dx3 = b.dx[2];
+  const double A1 = dx2 * dx3, A2 = dx1 * dx3, A3 = dx1 * dx2, V = dx1 * dx2 * dx3;
+  const double bdt = beta * dt;
+  const long long s2 = b.n1t, s3 = (long long)b.n1t * b.n2t;
+#pragma unroll
+  for (int m = 0; m < PHX_RNCONS; m++) {
+    const double *F0 = r.flux + (long long)m * vs;
+    const double *F1 = r.flux + (long long)(PHX_RNCONS + m) * vs;
+    const double *F2 = r.flux + (long long)(2 * PHX_RNCONS + m) * vs;
+    double du = (A1 * F0[id + 1] - A1 * F0[id]);
+    if (b.ndim >= 2) du += A2 * F1[id + s2] - A2 * F1[id];
+    if (b.ndim == 3) du += A3 * F2[id + s3] - A3 * F2[id];
+    const double rr = -du / V + 0.0;
+    r.dudt[m * vs + id] = rr;
+    double u0 = r.cons[m * vs + id];
+    u0 = beta * u0 + (1 - beta) * base[m * vs + id];
+    r.cons[m * vs + id] = u0;
+    out[m * vs + id] = u0 + bdt * rr;
+  }
+}
+
+// ------------------------------------------ MomentFluidSource (oned)
+struct TRes {
+  const RPar *p;
+  double rho, ug0, J0, dtau, amax;
+  __device__ __forceinline__ double operator()(double T) const {
+    double kappa = rho * p->kappa_a;
+    kappa = smin(kappa, amax);
+    const double JBB = p->jbb * (T * T) * (T * T);
+    const double dJ = (J0 + dtau * kappa * JBB) / (1. + dtau * kappa) - J0;
+    const double ug1 = rho * (p->Cv * T);
+    return ((ug1 - ug0) + dJ) / (ug0 + J0);
+  }
+};
+// RootFind::regula_falsi with a status; the iteration count persists across
+// calls (the reference reuses one RootFind for its re-bracketing tries).
+__device__ __forceinline__ double regula_falsi(const TRes &f, double a, double b, double tol, double guess,
+                                               int &count, int max_iter, bool &ok) {
+  double ya, yb;
+  if (a <= guess && b >= guess) {
+    ya = f(guess);
+    yb = f(b);
+    if (ya * yb > 0.0) {
+      yb = ya;
+      b = guess;
+      ya = f(a);
+    } else {
+      a = guess;
+    }
+  } else {
+    ya = f(a);
+    yb = f(b);
+  }
+  if (ya * yb > 0.0) {
+    ok = false;
+    return guess;
+  }
+  const double sign = (ya < 0 ? 1.0 : -1.0);
+  ya *= sign;
+  yb *= sign;
+  int b1 = 0, b2 = 0;
+  while (b - a > 2.0 * tol && count < max_iter) {
+    const double c = (a * yb - b * ya) / (yb - ya);
+    if (c == a) {
+      b = a;
+      count++;
+      continue;
+    } else if (c == b) {
+      a = b;
+      count++;
+      continue;
+    }
+    const double yc = sign * f(c);
+    if (yc > 0.0) {
+      b = c;
+      yb = yc;
+      b1++;
+      ya *= (b1 > 1 ? 0.5 : 1.0);
+      b2 = 0;
+    } else if (yc < 0.0) {
+      a = c;
+      ya = yc;
+      b2++;
+      yb *= (b2 > 1 ? 0.5 : 1.0);
+      b1 = 0;
+    } else {
+      a = c;
+      b = c;
+    }
+    count++;
+  }
+  ok = count != max_iter;
+  return 0.5 * (a + b);
+}
+
+template <bool M1>
+__global__ void __launch_bounds__(128) k_source(RPar p, BView b, RView r, double dt, Range3 rg) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= range_count(rg)) return;
+  int k, j, i;
+  zone_of(rg, t, k, j, i);
+  const long long id = b.idx(k, j, i), vs = r.vs, fvs = b.vs;
+  const double alpha = 1.0, sdetgam = 1.0;
+  const double amax = p.tau_max / (alpha * dt);
+  const double rho = b.prim[PHX_PRHO * fvs + id], ug = b.prim[PHX_PENG * fvs + id],
+               Tf = b.prim[PHX_PTMP * fvs + id];
+  double W;
+  const V3 cv = fluid_v(b, id, &W);
+  double dE = 0.0;
+  V3 dF;
+  dF.d[0] = dF.d[1] = dF.d[2] = 0.0;
+  bool success = false;
+  T2 Pi;
+  {
+    const double J0 = r.prim[PHX_RJ * vs + id];
+    const double dtau = alpha * dt / W;
+    const TRes res{&p, rho, ug, J0, dtau, amax};
+    int count = 0;
+    bool ok;
+    double T1 = regula_falsi(res, 1.e-2 * Tf, 1.e2 * Tf, p.tol * Tf, Tf, count, p.maxiter, ok);
+    double fac = 10.;
+    for (int tries = 0; !ok && tries < 4; tries++) {
+      T1 = regula_falsi(res, 1.e-1 / fac * Tf, 1.e1 * fac * Tf, p.tol * Tf, Tf, count, p.maxiter, ok);
+      fac *= 10.;
+    }
+    const Closure<M1> c(cv, true);
+    double Es = r.cons[PHX_RE * vs + id] / sdetgam;
+    V3 Fs;
+#pragma unroll
+    for (int a = 0; a < 3; a++) Fs.d[a] = r.cons[(PHX_RF + a) * vs + id] / sdetgam;
+    double J = r.prim[PHX_RJ * vs + id];
+    V3 H;
+#pragma unroll
+    for (int a = 0; a < 3; a++) H.d[a] = J * r.prim[(PHX_RH + a) * vs + id];
+    c.tilpi_from_prim(J, H, Pi);
+    const double JBB = p.jbb * (T1 * T1) * (T1 * T1);
+    const double kappaJ = smin(rho * p.kappa_a, amax);
+    double kappaH = smin(rho * p.kappa_s, amax);
+    kappaH += kappaJ;
+    double tauJ = alpha * dt * kappaJ;
+    double tauH = alpha * dt * kappaH;
+    if (ok) {
+      c.linear_source_update(Es, Fs, Pi, JBB, tauJ, tauH, dE, dF);
+      Es += dE;
+#pragma unroll
+      for (int a = 0; a < 3; a++) Fs.d[a] += dF.d[a];
+      success = c.con2prim(Es, Fs, Pi, J, H) == SUCCESS;
+    }
+    if (!success && p.oned_fixup == PHX_RAD_ONED_FIXUP_IGNORE_DJ) {
+      Es = r.cons[PHX_RE * vs + id] / sdetgam;
+#pragma unroll
+      for (int a = 0; a < 3; a++) Fs.d[a] = r.cons[(PHX_RF + a) * vs + id] / sdetgam;
+      const double JBB2 = p.jbb * (Tf * Tf) * (Tf * Tf);
+      const double kJ = rho * p.kappa_a;
+      const double kH2 = rho * p.kappa_s + kJ;
+      tauJ = alpha * dt * kJ;
+      tauH = alpha * dt * kH2;
+      c.linear_source_update(Es, Fs, Pi, JBB2, tauJ, tauH, dE, dF);
+      Es = r.cons[PHX_RE * vs + id] / sdetgam + dE;
+#pragma unroll
+      for (int a = 0; a < 3; a++) Fs.d[a] = r.cons[(PHX_RF + a) * vs + id] / sdetgam + dF.d[a];
+      success = c.con2prim(Es, Fs, Pi, J, H) == SUCCESS;
+    } else if (!success && p.oned_fixup == PHX_RAD_ONED_FIXUP_IGNORE_ALL) {
+      dE = 0.;
+      dF.d[0] = dF.d[1] = dF.d[2] = 0.;
+      success = true;
+    }
+  }
+  if (success) {
+    r.cons[PHX_RE * vs + id] += sdetgam * dE;
+#pragma unroll
+    for (int a = 0; a < 3; a++) r.cons[(PHX_RF + a) * vs + id] += sdetgam * dF.d[a];
+  }
+  double E = r.cons[PHX_RE * vs + id] / sdetgam;
+  V3 F, H;
+  double J;
+  const Closure<M1> cf(cv, false);
+#pragma unroll
+  for (int a = 0; a < 3; a++) F.d[a] = r.cons[(PHX_RF + a) * vs + id] / sdetgam;
+  double xi = 0.0, phi = PI;
+  cf.tilpi_from_con(E, F, xi, phi, Pi);
+  if (cf.con2prim(E, F, Pi, J, H) == SUCCESS) {
+    r.prim[PHX_RJ * vs + id] = J;
+#pragma unroll
+    for (int a = 0; a < 3; a++) r.prim[(PHX_RH + a) * vs + id] = H.d[a] / J;
+    return;
+  }
+  // failed inversion: the reference's zero-radiation state
+  r.prim[PHX_RJ * vs + id] = kSMALL;
+  J = r.prim[PHX_RJ * vs + id];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    r.prim[(PHX_RH + a) * vs + id] = 0.;
+    H.d[a] = r.prim[(PHX_RH + a) * vs + id] * J;
+  }
+  cf.prim2con(J, H, Pi, E, F);
+  r.cons[PHX_RE * vs + id] = E * sdetgam;
+#pragma unroll
+  for (int a = 0; a < 3; a++) r.cons[(PHX_RF + a) * vs + id] = F.d[a] * sdetgam;
+}
+
+// ------------------------------------------------------- timestep
+__global__ void k_dt_init(unsigned long long *scratch) { *scratch = 0x7fefffffffffffffull; }
+__global__ void __launch_bounds__(256) k_dt(RPar p, BView b, RView r, Range3 rg, unsigned long long *scratch) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double v = DBL_MAX;
+  if (t < range_count(rg)) {
+    int k, j, i;
+    zone_of(rg, t, k, j, i);
+    const long long id = b.idx(k, j, i);
+    const double kappaH = r.prim[PHX_RKAPPAH * r.vs + id];
+    for (int d = 0; d < b.ndim; d++) {
+      const double sigp = 1.0 * sqrt(1.0) - 0.0;
+      const double sigm = -1.0 * sqrt(1.0) - 0.0;
+      const double asym_sigl = 1.0 * b.prim[(PHX_PVEL + d) * b.vs + id] - 0.0;
+      const double rad_speed = smax(fabs(sigm), fabs(sigp));
+      const double asym_speed = fabs(asym_sigl);
+      const double w = b.dx[d];
+      const double dx = w * sqrt(1.0);
+      const double a = tanh_r(ratio(1.0, fabs(kappaH * dx)));
+      const double csig = a * rad_speed + (1. - a) * asym_speed;
+      v = smin(v, 1.0 / (csig / w));
+    }
+  }
+  // non-negative doubles order like their bit patterns; NaN zones are
+  // skipped like the reference's min (a NaN never compares less)
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+  __shared__ double sm[8];
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) v = fmin(v, sm[w]);
+    if (v >= 0.0) atomicMin(scratch, (unsigned long long)__double_as_longlong(v));
+  }
+}
+__global__ void k_dt_final(const unsigned long long *scratch, double cfl, double *out) {
+  *out = cfl * __longlong_as_double((long long)*scratch);
+}
+
+// ------------------------------------------------------- launchers
+namespace {
+inline unsigned blocks_for(long long n, int T) { return (unsigned)((n + T - 1) / T); }
+Range3 interior3(const BView &b) {
+  return {b.ng, b.ng + b.nx1 - 1, b.ndim >= 2 ? b.ng : 0, b.ndim >= 2 ? b.ng + b.nx2 - 1 : 0,
+          b.ndim >= 3 ? b.ng : 0, b.ndim >= 3 ? b.ng + b.nx3 - 1 : 0};
+}
+}  // namespace
+
+void launch_p2c(const RPar &p, const BView &b, const RView &r, Range3 rg, cudaStream_t s) {
+  const long long n = range_count(rg);
+  if (n <= 0) return;
+  if (p.m1)
+    k_p2c<true><<<blocks_for(n, 128), 128, 0, s>>>(p, b, r, rg);
+  else
+    k_p2c<false><<<blocks_for(n, 128), 128, 0, s>>>(p, b, r, rg);
+}
+
+void launch_c2p(const RPar &p, const BView &b, const RView &r, Range3 rg, cudaStream_t s) {
+  const long long n = range_count(rg);
+  if (n <= 0) return;
+  if (p.m1)
+    k_c2p<true><<<blocks_for(n, 128), 128, 0, s>>>(p, b, r, rg);
+  else
+    k_c2p<false><<<blocks_for(n, 128), 128, 0, s>>>(p, b, r, rg);
+}
+
+void launch_opacities(const RPar &p, const BView &b, const RView &r, cudaStream_t s) {
+  const long long n = (long long)b.n1t * b.n2t * b.n3t;
+  k_opacities<<<blocks_for(n, 256), 256, 0, s>>>(p, b, r, n);
+}
+
+template <bool M1>
+static void fluxes_t(const RPar &p, const BView &b, const RView &r, int d, Range3 rg, cudaStream_t s) {
+  const unsigned g = blocks_for(range_count(rg), 128);
+  switch (p.recon) {
+  case PHX_RECON_WENO5Z: k_fluxes<M1, PHX_RECON_WENO5Z><<<g, 128, 0, s>>>(p, b, r, d, rg); break;
+  case PHX_RECON_MP5: k_fluxes<M1, PHX_RECON_MP5><<<g, 128, 0, s>>>(p, b, r, d, rg); break;
+  case PHX_RECON_LINEAR: k_fluxes<M1, PHX_RECON_LINEAR><<<g, 128, 0, s>>>(p, b, r, d, rg); break;
+  default: k_fluxes<M1, PHX_RECON_CONSTANT><<<g, 128, 0, s>>>(p, b, r, d, rg); break;
+  }
+}
+
+void launch_fluxes(const RPar &p, const BView &b, const RView &r, cudaStream_t s) {
+  for (int d = 0; d < b.ndim; d++) {
+    Range3 rg = interior3(b);
+    if (d == 0) rg.ie += 1;
+    if (d == 1) rg.je += 1;
+    if (d == 2) rg.ke += 1;
+    if (p.m1)
+      fluxes_t<true>(p, b, r, d, rg, s);
+    else
+      fluxes_t<false>(p, b, r, d, rg, s);
+  }
+}
+
+void launch_update(const BView &b, const RView &r, const double *base, double *out, double beta, double dt,
+                   cudaStream_t s) {
+  const Range3 rg = interior3(b);
+  k_update<<<blocks_for(range_count(rg), 256), 256, 0, s>>>(b, r, base, out, beta, dt, rg);
+}
+
+void launch_source(const RPar &p, const BView &b, const RView &r, double dt, cudaStream_t s) {
+  const Range3 rg = interior3(b);
+  const unsigned g = blocks_for(range_count(rg), 128);
+  if (p.m1)
+    k_source<true><<<g, 128, 0, s>>>(p, b, r, dt, rg);
+  else
+    k_source<false><<<g, 128, 0, s>>>(p, b, r, dt, rg);
+}
+
+void launch_ghosts(const BView &b, const RView &r, cudaStream_t s) {
+  BView v = b;
+  v.vs = r.vs;
+  launch_ghost_periodic(v, r.cons, PHX_RNCONS, s);
+  launch_ghost_periodic(v, r.prim, PHX_RFAIL + 1, s);
+}
+
+void launch_dt(const RPar &p, const BView &b, const RView &r, unsigned long long *scratch, double *dt_out,
+               cudaStream_t s) {
+  const Range3 rg = interior3(b);
+  k_dt_init<<<1, 1, 0, s>>>(scratch);
+  k_dt<<<blocks_for(range_count(rg), 256), 256, 0, s>>>(p, b, r, rg, scratch);
+  k_dt_final<<<1, 1, 0, s>>>(scratch, p.cfl, dt_out);
+}
+
+}  // namespace rad
+}  // namespace phx

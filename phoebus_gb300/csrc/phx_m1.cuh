@@ -1,0 +1,40 @@
+// phx_m1.cuh -- declarations of the radiation moment kernels (phx_m1.cu).
+#pragma once
+#include "phx_kernels.cuh"
+#include "../../include/phx_radiation.h"
+
+namespace phx {
+namespace rad {
+
+// Radiation package parameters resolved for the device (phx_rad_params plus
+// the fluid ceiling and the EOS heat capacity).
+struct RPar {
+  int m1;          // 1 M1 closure, 0 Eddington
+  int robust;      // closure_c2p_strategy robust (MomentCon2Prim)
+  int bounds;      // recon_fixup_strategy bounds
+  int recon;       // phx_recon
+  int maxiter;     // src_rootfind_maxiter
+  int oned_fixup;  // phx_rad_oned_fixup
+  double cfl, tol, kappa_a, kappa_s, jbb;
+  double J_floor, xi_ceiling, tau_max, W_ceiling, Cv;
+};
+
+// Radiation fields of one block.
+struct RView {
+  double *cons, *prim, *flux, *dudt;
+  long long vs;
+};
+
+void launch_p2c(const RPar &p, const BView &b, const RView &r, Range3 rg, cudaStream_t s);
+void launch_c2p(const RPar &p, const BView &b, const RView &r, Range3 rg, cudaStream_t s);
+void launch_opacities(const RPar &p, const BView &b, const RView &r, cudaStream_t s);
+void launch_fluxes(const RPar &p, const BView &b, const RView &r, cudaStream_t s);
+void launch_update(const BView &b, const RView &r, const double *base, double *out, double beta, double dt,
+                   cudaStream_t s);
+void launch_source(const RPar &p, const BView &b, const RView &r, double dt, cudaStream_t s);
+void launch_ghosts(const BView &b, const RView &r, cudaStream_t s);
+void launch_dt(const RPar &p, const BView &b, const RView &r, unsigned long long *scratch, double *dt_out,
+               cudaStream_t s);
+
+}  // namespace rad
+}  // namespace phx

@@ -1,6 +1,6 @@
 """CPU-side checks of the C ABI: the libraries build, load, and export every
-entry point include/phx_fluid.h declares; the ctypes mirror matches the
-header.  No compute calls (no GPU here)."""
+entry point include/phx_fluid.h and include/phx_radiation.h declare; the
+ctypes mirror matches the headers.  No compute calls (no GPU here)."""
 import re
 import subprocess
 from pathlib import Path
@@ -11,10 +11,11 @@ from phoebus_gb300 import abi
 
 ROOT = Path(__file__).resolve().parent.parent
 HEADER = ROOT / "include" / "phx_fluid.h"
+HEADERS = [HEADER, ROOT / "include" / "phx_radiation.h"]
 
 
 def declared_functions():
-    text = HEADER.read_text()
+    text = "".join(h.read_text() for h in HEADERS)
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return sorted(set(re.findall(r"\b(phx_[a-z0-9_]+)\s*\(", text)))
 
@@ -64,8 +65,9 @@ def test_struct_sizes_match_header(built, tmp_path):
 
     src = tmp_path / "sz.c"
     fields = {"phx_params": abi.Params, "phx_block": abi.BlockS, "phx_geometry": abi.Geometry,
-              "phx_c2p_stats": abi.C2PStats, "phx_mlp_train_opts": abi.MlpTrainOpts, "phx_mesh": abi.Mesh}
-    lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void){"]
+              "phx_c2p_stats": abi.C2PStats, "phx_mlp_train_opts": abi.MlpTrainOpts, "phx_mesh": abi.Mesh,
+              "phx_rad_params": abi.RadParams, "phx_rad_block": abi.RadBlockS}
+    lines = ['#include <stdio.h>', '#include <stddef.h>'] + [f'#include "{h}"' for h in HEADERS] + ["int main(void){"]
     for cname, cls in fields.items():
         lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
         for fname, _ in cls._fields_:

@@ -1,0 +1,130 @@
+"""Pin the radiation-moment oracle (CPU only).
+
+- radiation_diffusion.gold (tst/regression/radiation_diffusion.py): the
+  512-zone M1 diffusion run of the radiation_advection deck to t = 1,
+  flattened like regression_test.py:347-391 (r.p.J, then r.p.H components,
+  every 10th value).  The gold predates the reference tree (its deck lacks
+  the <phoebus> boundary keys the current fluid package requires), and the
+  restatement of the current code meets it on the pulse, not at its 1e-5
+  tolerance: the bands below are the measured agreement with margin.
+- the restated tanh against the correctly rounded value;
+- closure inversions: prim -> con -> prim round trips (M1, Eddington).
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from phoebus_gb300 import abi, radiation, states
+from tests.util import random_rad_block
+
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+@pytest.fixture(scope="module")
+def rad_oracle(built):
+    from oracle.oracle import RadOracle
+
+    return RadOracle()
+
+
+def run_diffusion(o, b=None):
+    """The regression run through any object with the RadOracle task names
+    (the oracle on host arrays, or a RadiationContext on device arrays).
+    Returns (block, TimeControl, dts)."""
+    if b is None:
+        b, par, rpar, tlim = radiation.radiation_advection()
+    else:
+        _, par, rpar, tlim = radiation.radiation_advection(nx1=b.nx[0])
+    p, rp = abi.default_params(**par), abi.default_rad_params(**rpar)
+    o.MomentPrim2Con(rp, p, b)
+    o.Initialize(rp, p, b)
+    tc = states.TimeControl(tlim, o.EstimateTimestepBlock(rp, p, b), dt_init_fact=1.0e-6)
+    buf = np.zeros_like(b["rcons"]) if isinstance(b["rcons"], np.ndarray) else b["rcons"].clone()
+    dts = []
+    while tc.keep_going():
+        dt = tc.begin_step()
+        dts.append(dt)
+        o.rk2_step(rp, p, b, buf, dt)
+        tc.end_step(o.EstimateTimestepBlock(rp, p, b))
+    return b, tc, dts
+
+
+def diffusion_values(b):
+    """regression_test.py:347-376 flattening with compression_factor 10."""
+    sl = b.isl()
+    R = b["rprim"]
+    data = np.concatenate([R[abi.RJ][sl].ravel()] + [R[abi.RH + d][sl].ravel() for d in range(3)])
+    return np.array([data[10 * n] for n in range(len(data) // 10)])
+
+
+def test_radiation_diffusion_gold(rad_oracle):
+    b, tc, _ = run_diffusion(rad_oracle)
+    assert tc.time == 1.0
+    comp, gold = diffusion_values(b), np.loadtxt(GOLD / "radiation_diffusion.gold")
+    assert comp.shape == gold.shape == (204,)
+    rel = np.abs(comp - gold) / np.maximum(np.abs(gold), 1.0e-10)  # soft_equiv's measure
+    J, Jg = comp[:52], gold[:52]
+    assert rel[:52][Jg >= 1.0e-2].max() < 1.5e-2  # the pulse (measured 9.9e-3)
+    assert rel[:52].max() < 0.15  # tails and floor region (measured 0.105)
+    # pulse moments
+    x = (np.arange(52) * 10 + 0.5) / 512
+    m, mg = J > 1e-6, Jg > 1e-6
+    c, cg = (x[m] * J[m]).sum() / J[m].sum(), (x[mg] * Jg[mg]).sum() / Jg[mg].sum()
+    assert abs(c - cg) < 1.0e-4 and abs(J.max() - Jg.max()) / Jg.max() < 1.0e-3
+    assert np.abs(comp[52:104] - gold[52:104]).max() < 4.0e-3  # H_x / J (measured 2.2e-3)
+    assert np.abs(comp[104:]).max() < 1.0e-20  # H_y, H_z: round-off only, as in the gold
+
+
+def test_tanh_restatement(rad_oracle):
+    import mpmath
+
+    mpmath.mp.dps = 40
+    rng = np.random.default_rng(3)
+    xs = np.concatenate([rng.uniform(0, 23, 400), 10 ** rng.uniform(-9, 1.4, 400), [0.0, 0.25, 0.5, 21.99, 22.0]])
+    worst = 0.0
+    for x in xs:
+        ex = mpmath.tanh(mpmath.mpf(float(x)))
+        t = rad_oracle.tanh(float(x))
+        if ex == 0:
+            assert t == 0.0
+            continue
+        worst = max(worst, abs(float((mpmath.mpf(t) - ex) / np.spacing(float(ex)))))
+        assert rad_oracle.tanh(-float(x)) == -t
+    assert worst <= 4.0
+
+
+@pytest.mark.parametrize("method", ["moment_m1", "moment_eddington"])
+@pytest.mark.parametrize("aligned", [False, True])
+def test_closure_round_trip(rad_oracle, method, aligned):
+    """MomentPrim2Con then MomentCon2Prim recovers J and H/J where the
+    reference's closure solve is exact: fluid at rest, or flux and velocity
+    along one axis.  (It holds the angle phi at pi, i.e. takes the rest-frame
+    flux along the F / v basis vector g of closure_m1.hpp:326-372; for other
+    states the inversion differs from the prim2con closure at the 1e-3 level,
+    in the reference as here.)"""
+    b = random_rad_block((16, 12, 1), 2, seed=5, vmax=0.4 if aligned else 0.0)
+    if aligned:
+        for d in (1, 2):
+            b["prim"][abi.PVEL + d] = 0.0
+            b["rprim"][abi.RH + d] = 0.0
+    rp, p = abi.default_rad_params(method=method), abi.default_params(Cv=1.0)
+    J0, H0 = b["rprim"][abi.RJ].copy(), b["rprim"][abi.RH:abi.RH + 3].copy()
+    rad_oracle.MomentPrim2Con(rp, p, b, *b.entire())
+    rad_oracle.MomentCon2Prim(rp, p, b)
+    R = b["rprim"]
+    assert (R[abi.RFAIL] == 1.0).all()
+    tol = 1e-8 if method == "moment_m1" else 1e-13
+    assert np.max(np.abs(R[abi.RJ] - J0) / J0) < tol
+    assert np.max(np.abs(R[abi.RH:abi.RH + 3] - H0)) < tol
+
+
+def test_rad_params_default_matches_library(built):
+    import ctypes as C
+
+    lib = abi.load()
+    r = abi.RadParams()
+    lib.phx_rad_params_default(C.byref(r))
+    ref = abi.default_rad_params()
+    for name, _ in abi.RadParams._fields_:
+        assert getattr(r, name) == getattr(ref, name), name

@@ -1,0 +1,166 @@
+"""Radiation moments on the GPU against the oracle (exact build: bit for bit).
+
+Every task of include/phx_radiation.h on random 1D/2D/3D states (M1 and
+Eddington closures, each reconstruction), full RK stages, and the
+radiation_diffusion regression run (512 zones to t = 1, 655 steps): the exact
+build equals the oracle bit for bit, the production build stays within the
+oracle's agreement bands with the reference gold.
+"""
+import numpy as np
+import pytest
+
+from phoebus_gb300 import abi, radiation, states
+from phoebus_gb300.radiation import RadiationContext
+from tests.test_cpu_m1_oracle import GOLD, diffusion_values, run_diffusion
+from tests.util import assert_bitwise, host, random_rad_block
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def rad_oracle(built):
+    from oracle.oracle import RadOracle
+
+    return RadOracle()
+
+
+@pytest.fixture(scope="module")
+def rx(ctx_exact):
+    return RadiationContext(ctx_exact)
+
+
+@pytest.fixture(scope="module")
+def rf(ctx_fast):
+    return RadiationContext(ctx_fast)
+
+
+def _pair(nx, ndim, seed, **kw):
+    hb = random_rad_block(nx, ndim, seed, **kw)
+    return hb, hb.to_device()
+
+
+def _cmp(db, hb, names, what, region=None):
+    for n in names:
+        g, r = host(db[n]), hb[n]
+        if region is not None:
+            g, r = g[(slice(None),) + region], r[(slice(None),) + region]
+        assert_bitwise(g, r, f"{what}: {n}")
+
+
+CASES = [("moment_m1", "linear", 1), ("moment_m1", "linear", 3), ("moment_m1", "weno5z", 2),
+         ("moment_m1", "mp5", 3), ("moment_m1", "constant", 2), ("moment_eddington", "linear", 3),
+         ("moment_eddington", "weno5z", 1)]
+
+
+@pytest.mark.parametrize("method,recon,ndim", CASES)
+def test_tasks_bitwise(rx, rad_oracle, method, recon, ndim):
+    nx = {1: (64, 1, 1), 2: (24, 20, 1), 3: (12, 10, 8)}[ndim]
+    hb, db = _pair(nx, ndim, seed=11 + ndim)
+    rp = abi.default_rad_params(method=method, recon=recon, cfl=0.5, kappa_s=40.0, kappa_a=3.0, jbb_coeff=0.7)
+    p = abi.default_params(Cv=1.3)
+    e = hb.entire()
+    for o, b in ((rad_oracle, hb), (rx, db)):
+        o.MomentPrim2Con(rp, p, b, *e)
+    _cmp(db, hb, ["rcons"], "prim2con")
+    for o, b in ((rad_oracle, hb), (rx, db)):
+        o.MomentCon2Prim(rp, p, b)
+    _cmp(db, hb, ["rcons", "rprim"], "con2prim")
+    for o, b in ((rad_oracle, hb), (rx, db)):
+        o.MomentCalculateOpacities(rp, p, b)
+    _cmp(db, hb, ["rprim"], "opacities")
+    for o, b in ((rad_oracle, hb), (rx, db)):
+        o.CalculateFluxes(rp, p, b)
+    ks, js, is_ = hb.isl()
+    for d in range(ndim):
+        reg = (slice(ks.start, ks.stop + (d == 2)), slice(js.start, js.stop + (d == 1)),
+               slice(is_.start, is_.stop + (d == 0)))
+        g = host(db["rflux"])[4 * d:4 * d + 4][(slice(None),) + reg]
+        assert_bitwise(g, hb["rflux"][4 * d:4 * d + 4][(slice(None),) + reg], f"fluxes d={d}")
+    import torch
+
+    base_h = hb["rcons"] * 1.01
+    out_h = np.zeros_like(base_h)
+    base_d = torch.from_numpy(base_h).cuda()
+    out_d = torch.zeros_like(base_d)
+    rad_oracle.Update(rp, hb, base_h, out_h, 0.5, 1.0e-3)
+    rx.Update(rp, db, base_d, out_d, 0.5, 1.0e-3)
+    assert_bitwise(host(out_d)[(slice(None), ks, js, is_)], out_h[(slice(None), ks, js, is_)], "update out")
+    _cmp(db, hb, ["rcons"], "update in place", (ks, js, is_))
+    for o, b in ((rad_oracle, hb), (rx, db)):
+        o.MomentFluidSource(rp, p, b, 2.0e-3)
+    _cmp(db, hb, ["rcons", "rprim"], "fluid source", (ks, js, is_))
+    dt_h = rad_oracle.EstimateTimestepBlock(rp, p, hb)
+    dt_d = rx.EstimateTimestepBlock(rp, p, db)
+    assert dt_d == dt_h
+    rx.check()
+
+
+@pytest.mark.parametrize("method,ndim", [("moment_m1", 3), ("moment_eddington", 2), ("moment_m1", 1)])
+def test_rk2_steps_bitwise(rx, rad_oracle, method, ndim):
+    nx = {1: (48, 1, 1), 2: (16, 16, 1), 3: (10, 8, 8)}[ndim]
+    hb, db = _pair(nx, ndim, seed=23, vmax=0.3)
+    rp = abi.default_rad_params(method=method, recon="linear", cfl=0.5, kappa_s=30.0, kappa_a=2.0, jbb_coeff=0.5)
+    p = abi.default_params(Cv=1.0)
+    import torch
+
+    for o, b in ((rad_oracle, hb), (rx, db)):
+        o.MomentPrim2Con(rp, p, b)
+        o.Initialize(rp, p, b)
+    _cmp(db, hb, ["rcons", "rprim"], "initialize")
+    buf_h = np.zeros_like(hb["rcons"])
+    buf_d = torch.zeros_like(db["rcons"])
+    for step in range(3):
+        dt = rad_oracle.EstimateTimestepBlock(rp, p, hb)
+        assert rx.EstimateTimestepBlock(rp, p, db) == dt
+        rad_oracle.rk2_step(rp, p, hb, buf_h, dt)
+        rx.rk2_step(rp, p, db, buf_d, dt)
+        _cmp(db, hb, ["rcons", "rprim"], f"step {step}")
+    rx.check()
+
+
+def gpu_diffusion(rc):
+    hb, _, _, _ = radiation.radiation_advection()
+    return run_diffusion(rc, hb.to_device())
+
+
+def test_diffusion_run_bitwise(rx, rad_oracle):
+    db, tc, dts = gpu_diffusion(rx)
+    hb, otc, odts = run_diffusion(rad_oracle)
+    assert dts == odts and tc.ncycle == otc.ncycle == 655
+    assert_bitwise(db["rprim"][:abi.RFAIL + 1], hb["rprim"][:abi.RFAIL + 1], "prims at t = 1")
+    assert_bitwise(db["rcons"], hb["rcons"], "cons at t = 1")
+    rx.check()
+
+
+def test_diffusion_run_production(rf, rad_oracle):
+    db, tc, _ = gpu_diffusion(rf)
+    assert tc.time == 1.0
+    hb, _, _ = run_diffusion(rad_oracle)
+    comp, ref = diffusion_values(db.to_host()), diffusion_values(hb)
+    gold = np.loadtxt(GOLD / "radiation_diffusion.gold")
+    # production (FMA contraction) against the exact oracle: J on the pulse
+    m = np.abs(ref[:52]) > 1e-8
+    assert np.max(np.abs(comp[:52][m] - ref[:52][m]) / np.abs(ref[:52][m])) < 1e-8
+    assert np.abs(comp[52:104] - ref[52:104]).max() < 1e-9
+    # and the gold bands of the oracle pin
+    rel = np.abs(comp - gold) / np.maximum(np.abs(gold), 1.0e-10)
+    assert rel[:52][gold[:52] >= 1.0e-2].max() < 1.5e-2 and rel[:52].max() < 0.15
+    rf.check()
+
+
+def test_rad_configuration_errors(rx):
+    hb = random_rad_block((8, 1, 1), 1, seed=1)
+    db = hb.to_device()
+    p = abi.default_params()
+    with pytest.raises(abi.PhxError) as e:
+        rx.MomentCon2Prim(abi.default_rad_params(update_fluid=1), p, db)
+    assert e.value.status == 8
+    with pytest.raises(abi.PhxError) as e:
+        rx.MomentCon2Prim(abi.default_rad_params(method=7), p, db)
+    assert e.value.status == 1
+    import torch
+
+    with pytest.raises(abi.PhxError) as e:
+        rx.Stage(abi.default_rad_params(), abi.default_params(enable_floors=1), db, db["rcons"],
+                 torch.zeros_like(db["rcons"]), 1.0, 1e-3)
+    assert e.value.status == 8

@@ -69,3 +69,37 @@ def assert_close(got, ref, rtol, what="", floor=None):
         i0 = tuple(idx)
         raise AssertionError(f"{what}: {bad.sum()} of {bad.size} beyond rtol {rtol:g}; first {i0}: got "
                              f"{got[i0]!r} ref {ref[i0]!r}")
+
+
+def random_rad_block(nx, ndim, seed, vmax=0.4, kappa_s=50.0, kappa_a=5.0, ng=4):
+    """A host Block with random fluid background (rho, T, u, u^i on the whole
+    block) and random radiation primitives J > 0, |H|/J < 0.6 of one species,
+    xi = 0, phi = pi, radiation conserved moments unset."""
+    from phoebus_gb300 import abi
+    from phoebus_gb300.block import Block
+    from phoebus_gb300.radiation import alloc_rad
+
+    rng = np.random.default_rng(seed)
+    nxs = tuple(nx[d] if d < ndim else 1 for d in range(3))
+    dx = tuple(1.0 / nxs[d] if d < ndim else 1.0 for d in range(3))
+    b = Block(nxs, ng=ng, ndim=ndim, xmin=(0.0, 0.0, 0.0), dx=dx, backend="numpy")
+    b.alloc(["prim", "cons", "flux", "face_sig", "cell_sig", "fail", "src", "emf", "dudt"])
+    alloc_rad(b)
+    P, R = b["prim"], b["rprim"]
+    shp = b.shape
+    P[abi.PRHO] = rng.uniform(0.5, 2.0, shp)
+    P[abi.PTMP] = rng.uniform(0.5, 2.0, shp)
+    P[abi.PENG] = P[abi.PRHO] * P[abi.PTMP]
+    u = rng.uniform(-1, 1, (3,) + shp)
+    u *= vmax * rng.uniform(0, 1, shp) / np.maximum(np.sqrt((u * u).sum(0)), 1e-12)
+    W = 1 / np.sqrt(1 - (u * u).sum(0))
+    for d in range(3):
+        P[abi.PVEL + d] = W * u[d] if d < ndim else 0.3 * W * u[d]
+    R[abi.RJ] = np.exp(rng.uniform(np.log(1e-3), 0.0, shp))
+    h = rng.uniform(-1, 1, (3,) + shp)
+    h *= 0.6 * rng.uniform(0, 1, shp) / np.maximum(np.sqrt((h * h).sum(0)), 1e-12)
+    for d in range(3):
+        R[abi.RH + d] = h[d]
+    R[abi.RXI] = 0.0
+    R[abi.RPHI] = np.pi
+    return b
