@@ -92,6 +92,8 @@ def parse():
     a.add_argument("--torus-n", type=int, default=384)
     a.add_argument("--torus-steps", type=int, default=2)
     a.add_argument("--no-m1", action="store_true", help="skip the radiation M1 section")
+    a.add_argument("--m1-only", action="store_true",
+                   help="run only the radiation M1 section and print its JSON (profiling)")
     a.add_argument("--m1-n", type=int, default=128)
     a.add_argument("--m1-steps", type=int, default=3)
     a.add_argument("--m1-cpu-n", type=int, default=48)
@@ -619,6 +621,12 @@ def main():
 
     dev = f"cuda:{local}"
     torch.cuda.set_device(local)
+    if args.m1_only:
+        ctx = FluidContext(local, exact=args.exact)
+        if rank == 0:
+            print(json.dumps({"m1": bench_m1(ctx, args, dev)}), flush=True)
+        ctx.close()
+        return
     n = args.n
     hb, par = states.kelvin_helmholtz(n=n)
     p = abi.default_params(**par)

@@ -295,6 +295,11 @@ struct Closure {
   }
   // SolveClosure with phi held at pi (the reference's update rule keeps it
   // there); the phi-perturbed residuals only feed the discarded 2x2 solve.
+  // Production build: with phi fixed the rest-frame flux direction f is
+  // fixed, so pi^ij(xi) = athin(xi) pi0^ij and the contractions con2prim
+  // needs scale by athin; they are formed once per solve and each residual
+  // is scalar work (the exact build keeps the reference's per-residual
+  // tensor arithmetic).
   __device__ __forceinline__ void solve_closure(double E, V3 F, double &xi_io, double &phi_out) const {
     const int max_iter = 30;
     const double tol = 1.e6 * DBL_EPSILON;
@@ -308,13 +313,55 @@ struct Closure {
     int iter = 0;
     double fXi = 1.e3, fPhi = 1.e3;
     double xi = xi_io, phi = PI;
+#ifndef PHX_EXACT
+    // pi0 contractions for phi = pi
+    double f[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) f[i] = g.d[i] + SIN_PI * dd.d[i];
+    T2 Pi0;
+    tilpi_fill(f, 1.0, Pi0);
+    V3 cvPi0;
+    double vvPi0;
+    contractions(Pi0, cvPi0, vvPi0);
+    const double vF = ccov(con_v, F);
+    auto res = [&](double x) {
+      const double athin = 0.5 * (3 * closure_fn(x) - 1);
+      const double vvPi = athin * vvPi0;
+      const double lam = (2.0 * W2 + 1.0) / 3.0 + (2.0 * W2 - 3.0) * W2 * vvPi;
+      const double ilam = 1.0 / (lam + (lam >= 0 ? kSMALL : -kSMALL));
+      const double a = W2 * ilam * ((4 * W2 / 3 - vvPi) * E - ((4 * W2 + 1) / 3 - W2 * vvPi) * vF);
+      double J = ((2 * W2 - 1) * E - 2 * W2 * vF) * ilam;
+      const double iW = 1.0 / W;
+      V3 H;
+#pragma unroll
+      for (int i = 0; i < 3; i++) H.d[i] = (F.d[i] - J * athin * cvPi0.d[i] - cov_v.d[i] * a) * iW;
+      double vh = ccov(con_v, H);
+      double hh = ccov(H, H);
+      const double xc = sqrt(hh - vh * vh) / J;
+      if (robust && !isnan(xc) && !isnan(J) && (J < 0. || xc >= 1.0)) {
+        if (J < 0.) J = smin(J, 10. * kSMALL);
+        if (xc >= 1.0) {
+          const double sc = 0.999 / xc;
+          vh *= sc;
+          hh *= sc * sc;
+        }
+      }
+      return x - ratio(sqrt(hh - vh * vh), J);
+    };
+#endif
     do {
       const double xi_up = smin(xi * (1.0 + eps) + delta, 1.0);
       const double xi_lo = smax(xi * (1.0 - eps) - delta, 0.0);
+#ifdef PHX_EXACT
       const double f_up = residual(E, F, xi_up, phi, g, dd);
       const double f_lo = residual(E, F, xi_lo, phi, g, dd);
-      const double J00 = (f_up - f_lo) / (xi_up - xi_lo);
       fXi = residual(E, F, xi, phi, g, dd);
+#else
+      const double f_up = res(xi_up);
+      const double f_lo = res(xi_lo);
+      fXi = res(xi);
+#endif
+      const double J00 = (f_up - f_lo) / (xi_up - xi_lo);
       const double dx0 = fXi / J00, dx1 = 0.0;
       fPhi = 0.0;
       double cdx = smin(dx0, xi - delta * xi);
@@ -448,8 +495,8 @@ __global__ void __launch_bounds__(256) k_opacities(RPar p, BView b, RView r, lon
 // --------------------------------------------------------- fluxes
 // One face state: E, F_i, and the flux of direction d (con_F^d and row d of
 // P^i_j) for the closure's velocity, J and H_i.
-template <bool M1>
-__device__ __forceinline__ void face_state(const Closure<M1> &c, double J, const V3 &H, int d, double &E, V3 &F,
+template <bool M1, int d>
+__device__ __forceinline__ void face_state(const Closure<M1> &c, double J, const V3 &H, double &E, V3 &F,
                                            double &Fd, double P[3]) {
   T2 Pi;
   c.tilpi_from_prim(J, H, Pi);
@@ -458,8 +505,8 @@ __device__ __forceinline__ void face_state(const Closure<M1> &c, double J, const
   Fd = 0.0 + F.d[d];
 }
 
-template <bool M1, int RECON>
-__global__ void __launch_bounds__(128) k_fluxes(RPar p, BView b, RView r, int d, Range3 rg) {
+template <bool M1, int RECON, int d>
+__global__ void __launch_bounds__(128) k_fluxes(RPar p, BView b, RView r, Range3 rg) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= range_count(rg)) return;
   int k, j, i;
@@ -486,11 +533,11 @@ __global__ void __launch_bounds__(128) k_fluxes(RPar p, BView b, RView r, int d,
   const double idy = 1.0 / b.dx[1], idy4 = 0.25 * idy;
   const double idz = 1.0 / b.dx[2], idz4 = 0.25 * idz;
   V3 dJ;
-  if (d == 0) {
+  if constexpr (d == 0) {
     dJ.d[0] = (Jat(k, j, i) - Jat(k, j, i - 1)) * idx;
     dJ.d[1] = (Jat(k, j + dj, i) + Jat(k, j + dj, i - 1) - Jat(k, j - dj, i) - Jat(k, j - dj, i - 1)) * idy4;
     dJ.d[2] = (Jat(k + dk, j, i) + Jat(k + dk, j, i - 1) - Jat(k - dk, j, i) - Jat(k - dk, j, i - 1)) * idz4;
-  } else if (d == 1) {
+  } else if constexpr (d == 1) {
     dJ.d[0] = (Jat(k, j, i + 1) + Jat(k, j - dj, i + 1) - Jat(k, j, i - 1) - Jat(k, j - dj, i - 1)) * idx4;
     dJ.d[1] = (Jat(k, j, i) - Jat(k, j - dj, i)) * idy;
     dJ.d[2] = (Jat(k + dk, j, i) + Jat(k + dk, j - dj, i) - Jat(k - dk, j, i) - Jat(k - dk, j - dj, i)) * idz4;
@@ -560,10 +607,10 @@ __global__ void __launch_bounds__(128) k_fluxes(RPar p, BView b, RView r, int d,
   const Closure<M1> cl(vl, true), cr(vr, true);
   double El, Er, Fdl, Fdr, Fdl_a, Fdr_a, Pl[3], Pr[3], Pl_a[3], Pr_a[3], Ed;
   V3 Fl, Fr, Fd_scr;
-  face_state(cl, Jl, Has, d, Ed, Fd_scr, Fdl_a, Pl_a);
-  face_state(cr, Jr, Has, d, Ed, Fd_scr, Fdr_a, Pr_a);
-  face_state(cl, Jl, Hl, d, El, Fl, Fdl, Pl);
-  face_state(cr, Jr, Hr, d, Er, Fr, Fdr, Pr);
+  face_state<M1, d>(cl, Jl, Has, Ed, Fd_scr, Fdl_a, Pl_a);
+  face_state<M1, d>(cr, Jr, Has, Ed, Fd_scr, Fdr_a, Pr_a);
+  face_state<M1, d>(cl, Jl, Hl, El, Fl, Fdl, Pl);
+  face_state<M1, d>(cr, Jr, Hr, Er, Fr, Fdr, Pr);
   Fdl = aw * Fdl + (1 - aw) * Fdl_a;
   Fdr = aw * Fdr + (1 - aw) * Fdr_a;
 #pragma unroll
@@ -866,14 +913,24 @@ void launch_opacities(const RPar &p, const BView &b, const RView &r, cudaStream_
   k_opacities<<<blocks_for(n, 256), 256, 0, s>>>(p, b, r, n);
 }
 
+template <bool M1, int RECON>
+static void fluxes_r(const BView &b, const RPar &p, const RView &r, int d, Range3 rg, unsigned g, cudaStream_t s) {
+  if (d == 0)
+    k_fluxes<M1, RECON, 0><<<g, 128, 0, s>>>(p, b, r, rg);
+  else if (d == 1)
+    k_fluxes<M1, RECON, 1><<<g, 128, 0, s>>>(p, b, r, rg);
+  else
+    k_fluxes<M1, RECON, 2><<<g, 128, 0, s>>>(p, b, r, rg);
+}
+
 template <bool M1>
 static void fluxes_t(const RPar &p, const BView &b, const RView &r, int d, Range3 rg, cudaStream_t s) {
   const unsigned g = blocks_for(range_count(rg), 128);
   switch (p.recon) {
-  case PHX_RECON_WENO5Z: k_fluxes<M1, PHX_RECON_WENO5Z><<<g, 128, 0, s>>>(p, b, r, d, rg); break;
-  case PHX_RECON_MP5: k_fluxes<M1, PHX_RECON_MP5><<<g, 128, 0, s>>>(p, b, r, d, rg); break;
-  case PHX_RECON_LINEAR: k_fluxes<M1, PHX_RECON_LINEAR><<<g, 128, 0, s>>>(p, b, r, d, rg); break;
-  default: k_fluxes<M1, PHX_RECON_CONSTANT><<<g, 128, 0, s>>>(p, b, r, d, rg); break;
+  case PHX_RECON_WENO5Z: fluxes_r<M1, PHX_RECON_WENO5Z>(b, p, r, d, rg, g, s); break;
+  case PHX_RECON_MP5: fluxes_r<M1, PHX_RECON_MP5>(b, p, r, d, rg, g, s); break;
+  case PHX_RECON_LINEAR: fluxes_r<M1, PHX_RECON_LINEAR>(b, p, r, d, rg, g, s); break;
+  default: fluxes_r<M1, PHX_RECON_CONSTANT>(b, p, r, d, rg, g, s); break;
   }
 }
 
