@@ -22,6 +22,17 @@
 namespace phx {
 namespace rad {
 
+// Production-build arithmetic (the exact build keeps the reference's IEEE
+// divisions): x / 3 as a product with 1/3, divisions by W as products with
+// 1/W, shared reciprocals for repeated denominators.
+#ifdef PHX_EXACT
+#define D3(x) ((x) / 3)
+#define DW(x) ((x) / W)
+#else
+#define D3(x) ((x) * (1.0 / 3.0))
+#define DW(x) ((x) * iW)
+#endif
+
 // std::min / std::max (NaN handling of the reference)
 __device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b : a; }
 __device__ __forceinline__ double smax(double a, double b) { return (a < b) ? b : a; }
@@ -120,7 +131,7 @@ constexpr double SIN_PI = 1.2246467991473532e-16;
 template <bool M1>
 struct Closure {
   V3 con_v, cov_v;
-  double W, W2;
+  double W, W2, iW;
   bool robust;
   __device__ __forceinline__ Closure(const V3 &cv, bool rob) : robust(rob) {
     con_v = cv;
@@ -130,8 +141,9 @@ struct Closure {
 #pragma unroll
     for (int i = 0; i < 3; i++) v2 += con_v.d[i] * cov_v.d[i];
     v2 = smin(v2, 0.9999);
-    W = 1 / sqrt(1 - v2);
+    W = rsqrt_p(1 - v2);
     W2 = W * W;
+    iW = rcp_p(W);
   }
   __device__ __forceinline__ void contractions(const T2 &Pi, V3 &cov_vPi, double &vvPi) const {
     vvPi = 0.0;
@@ -149,32 +161,39 @@ struct Closure {
     double vvPi;
     V3 cvPi;
     contractions(Pi, cvPi, vvPi);
-    double A00 = (4 * W2 - 1) / 3 + W2 * vvPi + W * tauJ;
+    double A00 = D3(4 * W2 - 1) + W2 * vvPi + W * tauJ;
     double A01 = 2 * W + tauH;
-    double A10 = A00 - 1 - tauJ / W;
-    double A11 = A01 - 1 / W;
+    double A10 = A00 - 1 - DW(tauJ);
+    double A11 = A01 - DW(1.0);
     const double vFs = ccov(con_v, Fs);
     const double b0 = Estar + W * tauJ * JBB;
-    const double b1 = vFs + (W2 - 1) / W * tauJ * JBB;
-    const double invDet = 1.0 / dop(A00, A11, A01, A10);
+    const double b1 = vFs + DW(W2 - 1) * tauJ * JBB;
+    const double invDet = rcp_p(dop(A00, A11, A01, A10));
     const double J = invDet * dop(A11, b0, A01, b1);
     const double zeta = invDet * dop(A00, b1, A10, b0);
-    dE = (4 * W2 - 1 + 3 * W2 * vvPi) / 3 * J + 2 * W * zeta - Estar;
+    dE = D3(4 * W2 - 1 + 3 * W2 * vvPi) * J + 2 * W * zeta - Estar;
+#ifndef PHX_EXACT
+    const double iWt = rcp_p(W + tauH);
+#endif
 #pragma unroll
-    for (int i = 0; i < 3; i++)
-      dF.d[i] = (cov_v.d[i] * tauH * (4 * W2 / 3 * J + W * zeta) + tauH * cvPi.d[i] * J +
-                 tauJ * W2 * cov_v.d[i] * (JBB - J) + W * Fs.d[i]) /
-                    (W + tauH) -
-                Fs.d[i];
+    for (int i = 0; i < 3; i++) {
+      const double num = cov_v.d[i] * tauH * (D3(4 * W2) * J + W * zeta) + tauH * cvPi.d[i] * J +
+                         tauJ * W2 * cov_v.d[i] * (JBB - J) + W * Fs.d[i];
+#ifdef PHX_EXACT
+      dF.d[i] = num / (W + tauH) - Fs.d[i];
+#else
+      dF.d[i] = num * iWt - Fs.d[i];
+#endif
+    }
   }
   __device__ __forceinline__ void prim2con(double J, const V3 &H, const T2 &Pi, double &E, V3 &F) const {
     double vvPi;
     V3 cvPi;
     contractions(Pi, cvPi, vvPi);
     const double vH = ccov(con_v, H);
-    E = (4 * W2 - 1 + 3 * W2 * vvPi) / 3 * J + 2 * W * vH;
+    E = D3(4 * W2 - 1 + 3 * W2 * vvPi) * J + 2 * W * vH;
 #pragma unroll
-    for (int i = 0; i < 3; i++) F.d[i] = 4 * W2 / 3 * cov_v.d[i] * J + W * cov_v.d[i] * vH + W * H.d[i] + J * cvPi.d[i];
+    for (int i = 0; i < 3; i++) F.d[i] = D3(4 * W2) * cov_v.d[i] * J + W * cov_v.d[i] * vH + W * H.d[i] + J * cvPi.d[i];
   }
   // row d of ClosureEdd::getConCovPFromPrim (lapse 1)
   __device__ __forceinline__ void concov_p_row(double J, const V3 &H, const T2 &Pi, int d, double P[3]) const {
@@ -183,27 +202,34 @@ struct Closure {
     for (int j = 0; j < 3; j++)
       P[j] = 4.0 / 3.0 * W2 * con_v.d[d] * cov_v.d[j] * J + W * (con_v.d[d] * H.d[j] + cov_v.d[j] * conH_d) +
              J * (0.0 + Pi.d[d][j]);
-    P[d] += J / 3.0;
+    P[d] += D3(J);
   }
   __device__ __forceinline__ int con2prim(double E, const V3 &F, const T2 &Pi, double &J, V3 &H) const {
     double vvPi;
     V3 cvPi;
     contractions(Pi, cvPi, vvPi);
     const double vF = ccov(con_v, F);
-    const double lam = (2.0 * W2 + 1.0) / 3.0 + (2.0 * W2 - 3.0) * W2 * vvPi;
+    const double lam = D3(2.0 * W2 + 1.0) + (2.0 * W2 - 3.0) * W2 * vvPi;
+#ifdef PHX_EXACT
     const double a = ratio(W2, lam) * ((4 * W2 / 3 - vvPi) * E - ((4 * W2 + 1) / 3 - W2 * vvPi) * vF);
     J = ratio((2 * W2 - 1) * E - 2 * W2 * vF, lam);
+#else
+    const double ilam = rcp_p(lam + (lam >= 0 ? kSMALL : -kSMALL));
+    const double a = W2 * ilam * ((D3(4 * W2) - vvPi) * E - (D3(4 * W2 + 1) - W2 * vvPi) * vF);
+    J = ((2 * W2 - 1) * E - 2 * W2 * vF) * ilam;
+#endif
 #pragma unroll
-    for (int i = 0; i < 3; i++) H.d[i] = (F.d[i] - J * cvPi.d[i] - cov_v.d[i] * a) / W;
+    for (int i = 0; i < 3; i++) H.d[i] = DW(F.d[i] - J * cvPi.d[i] - cov_v.d[i] * a);
     const double vh = ccov(con_v, H);
-    const double xi = sqrt(ccov(H, H) - vh * vh) / J;
+    const double xi = div_p(sqrt(ccov(H, H) - vh * vh), J);
     if (isnan(xi) || isnan(J)) return FAILURE;
     if (J < 0. || xi >= 1.0) {
       if (robust) {
         if (J < 0.) J = smin(J, 10. * kSMALL);
         if (xi >= 1.0) {
+          const double sc = div_p(0.999, xi);
 #pragma unroll
-          for (int i = 0; i < 3; i++) H.d[i] *= 0.999 / xi;
+          for (int i = 0; i < 3; i++) H.d[i] *= sc;
         }
         return MODIFIED;
       }
@@ -212,9 +238,10 @@ struct Closure {
     return SUCCESS;
   }
   __device__ __forceinline__ static double closure_fn(double xi) {
-    return (1.0 - 2 * (xi * xi) + 4 * (xi * xi * xi)) / 3.0;
+    return D3(1.0 - 2 * (xi * xi) + 4 * (xi * xi * xi));
   }
   __device__ __forceinline__ void tilpi_fill(const double f[3], double athin, T2 &Pi) const {
+#ifdef PHX_EXACT
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -222,6 +249,17 @@ struct Closure {
         Pi.d[i][j] = f[i] * f[j] - (W2 * con_v.d[i] * con_v.d[j] + gdelta(i, j)) / 3;
         Pi.d[i][j] *= athin;
       }
+#else
+    // symmetric: the upper triangle, mirrored
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = i; j < 3; j++) {
+        const double v = (f[i] * f[j] - D3(W2 * con_v.d[i] * con_v.d[j] + gdelta(i, j))) * athin;
+        Pi.d[i][j] = v;
+        Pi.d[j][i] = v;
+      }
+#endif
   }
   // GetConTilPiFromPrim
   __device__ __forceinline__ void tilpi_from_prim(double J, const V3 &H, T2 &Pi) const {
@@ -238,9 +276,15 @@ struct Closure {
       for (int i = 0; i < 3; i++) vH += H.d[i] * con_v.d[i];
       Hm = sqrt(Hm - vH * vH);
       double f[3];
+#ifdef PHX_EXACT
 #pragma unroll
       for (int i = 0; i < 3; i++) f[i] = ratio(0.0 + H.d[i], Hm);
-      const double xi = smax(smin(1.0, ratio(Hm, J)), 0.0);
+#else
+      const double iHm = rcp_p(Hm + (Hm >= 0 ? kSMALL : -kSMALL));
+#pragma unroll
+      for (int i = 0; i < 3; i++) f[i] = H.d[i] * iHm;
+#endif
+      const double xi = smax(smin(1.0, ratio_p(Hm, J)), 0.0);
       tilpi_fill(f, 0.5 * (3 * closure_fn(xi) - 1), Pi);
     }
   }
@@ -265,16 +309,27 @@ struct Closure {
     Fmag = sqrt(Fmag);
 #pragma unroll
     for (int i = 0; i < 3; i++) vl += F.d[i] * con_v.d[i];
-    vl = ratio(vl, Fmag);
+#ifndef PHX_EXACT
+    const double iF = rcp_p(Fmag + kSMALL);
+#endif
+    vl = ratio_p(vl, Fmag);
 #pragma unroll
     for (int i = 0; i < 3; i++) vv += cov_v.d[i] * con_v.d[i];
-    const double lam = ratio(1.0, W * (1 - vl));
+    const double lam = ratio_p(1.0, W * (1 - vl));
     const double aa = sqrt(vv * (1 + 10 * DBL_EPSILON) - vl * vl);
+#ifndef PHX_EXACT
+    const double iaa = rcp_p(aa + kSMALL);
+#endif
 #pragma unroll
     for (int i = 0; i < 3; i++) {
       const double cF = 0.0 + F.d[i];
+#ifdef PHX_EXACT
       g.d[i] = ratio(cF * lam, Fmag) - W * con_v.d[i];
       dd.d[i] = ratio(ratio(cF, Fmag) * (1 - lam / W) + con_v.d[i], aa);
+#else
+      g.d[i] = cF * lam * iF - W * con_v.d[i];
+      dd.d[i] = (cF * iF * (1 - DW(lam)) + con_v.d[i]) * iaa;
+#endif
     }
   }
   __device__ __forceinline__ double residual(double E, const V3 &F, double xi, double phi, const V3 &g,
@@ -327,26 +382,22 @@ struct Closure {
     auto res = [&](double x) {
       const double athin = 0.5 * (3 * closure_fn(x) - 1);
       const double vvPi = athin * vvPi0;
-      const double lam = (2.0 * W2 + 1.0) / 3.0 + (2.0 * W2 - 3.0) * W2 * vvPi;
-      const double ilam = 1.0 / (lam + (lam >= 0 ? kSMALL : -kSMALL));
-      const double a = W2 * ilam * ((4 * W2 / 3 - vvPi) * E - ((4 * W2 + 1) / 3 - W2 * vvPi) * vF);
+      const double lam = D3(2.0 * W2 + 1.0) + (2.0 * W2 - 3.0) * W2 * vvPi;
+      const double ilam = rcp_p(lam + (lam >= 0 ? kSMALL : -kSMALL));
+      const double a = W2 * ilam * ((D3(4 * W2) - vvPi) * E - (D3(4 * W2 + 1) - W2 * vvPi) * vF);
       double J = ((2 * W2 - 1) * E - 2 * W2 * vF) * ilam;
-      const double iW = 1.0 / W;
       V3 H;
 #pragma unroll
       for (int i = 0; i < 3; i++) H.d[i] = (F.d[i] - J * athin * cvPi0.d[i] - cov_v.d[i] * a) * iW;
-      double vh = ccov(con_v, H);
-      double hh = ccov(H, H);
-      const double xc = sqrt(hh - vh * vh) / J;
+      const double vh = ccov(con_v, H);
+      const double s0 = sqrt(ccov(H, H) - vh * vh);
+      const double iJ = rcp_p(J + (J >= 0 ? kSMALL : -kSMALL));
+      const double xc = s0 * iJ;
+      double sH = s0;
       if (robust && !isnan(xc) && !isnan(J) && (J < 0. || xc >= 1.0)) {
-        if (J < 0.) J = smin(J, 10. * kSMALL);
-        if (xc >= 1.0) {
-          const double sc = 0.999 / xc;
-          vh *= sc;
-          hh *= sc * sc;
-        }
+        if (xc >= 1.0) sH = s0 * (0.999 * rcp_p(xc));
       }
-      return x - ratio(sqrt(hh - vh * vh), J);
+      return x - sH * iJ;
     };
 #endif
     do {
@@ -475,8 +526,14 @@ __global__ void __launch_bounds__(128) k_c2p(RPar p, BView b, RView r, Range3 rg
     st = SUCCESS;
   }
   r.prim[PHX_RJ * vs + id] = J;
+#ifdef PHX_EXACT
 #pragma unroll
   for (int a = 0; a < 3; a++) r.prim[(PHX_RH + a) * vs + id] = ratio(H.d[a], J);
+#else
+  const double iJ = rcp_p(J + (J >= 0 ? kSMALL : -kSMALL));
+#pragma unroll
+  for (int a = 0; a < 3; a++) r.prim[(PHX_RH + a) * vs + id] = H.d[a] * iJ;
+#endif
   r.prim[PHX_RFAIL * vs + id] = st == SUCCESS ? 1.0 : 0.0;
 }
 
@@ -564,10 +621,16 @@ __global__ void __launch_bounds__(128) k_fluxes(RPar p, BView b, RView r, Range3
     }
   }
   V3 vl, vr;
+  const double iWl = rcp_p(Wl), iWr = rcp_p(Wr);
 #pragma unroll
   for (int a = 0; a < 3; a++) {
+#ifdef PHX_EXACT
     vl.d[a] = vpl[a] / Wl;
     vr.d[a] = vpr[a] / Wr;
+#else
+    vl.d[a] = vpl[a] * iWl;
+    vr.d[a] = vpr[a] * iWr;
+#endif
   }
   const double sigp = 1.0 * sqrt(1.0) - 0.0;
   const double sigm = -1.0 * sqrt(1.0) - 0.0;
@@ -586,8 +649,8 @@ __global__ void __launch_bounds__(128) k_fluxes(RPar p, BView b, RView r, Range3
   }
   if (p.bounds) {
     const double vhl = ccov(vl, Hl), vhr = ccov(vr, Hr);
-    const double xil = sqrt(ccov(Hl, Hl) - vhl * vhl) / Jl;
-    const double xir = sqrt(ccov(Hr, Hr) - vhr * vhr) / Jr;
+    const double xil = div_p(sqrt(ccov(Hl, Hl) - vhl * vhl), Jl);
+    const double xir = div_p(sqrt(ccov(Hr, Hr) - vhr * vhr), Jr);
     if (xil > p.xi_ceiling) {
 #pragma unroll
       for (int a = 0; a < 3; a++) Hl.d[a] *= p.xi_ceiling / xil;
@@ -602,8 +665,14 @@ __global__ void __launch_bounds__(128) k_fluxes(RPar p, BView b, RView r, Range3
   const double aw = tanh_r(ratio(1.0, fabs(kappaH * dx)));
   const double kappaH_min = 1.e-20;
   V3 Has;
+#ifdef PHX_EXACT
 #pragma unroll
   for (int a = 0; a < 3; a++) Has.d[a] = ratio(-dJ.d[a], 3 * kappaH + 3 * kappaH_min);
+#else
+  const double ik = rcp_p(3 * kappaH + 3 * kappaH_min + kSMALL);
+#pragma unroll
+  for (int a = 0; a < 3; a++) Has.d[a] = -dJ.d[a] * ik;
+#endif
   const Closure<M1> cl(vl, true), cr(vr, true);
   double El, Er, Fdl, Fdr, Fdl_a, Fdr_a, Pl[3], Pr[3], Pl_a[3], Pr_a[3], Ed;
   V3 Fl, Fr, Fd_scr;
@@ -826,7 +895,7 @@ __global__ void __launch_bounds__(128) k_source(RPar p, BView b, RView r, double
   if (cf.con2prim(E, F, Pi, J, H) == SUCCESS) {
     r.prim[PHX_RJ * vs + id] = J;
 #pragma unroll
-    for (int a = 0; a < 3; a++) r.prim[(PHX_RH + a) * vs + id] = H.d[a] / J;
+    for (int a = 0; a < 3; a++) r.prim[(PHX_RH + a) * vs + id] = div_p(H.d[a], J);
     return;
   }
   // failed inversion: the reference's zero-radiation state
