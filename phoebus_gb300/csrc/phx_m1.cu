@@ -350,12 +350,16 @@ struct Closure {
   }
   // SolveClosure with phi held at pi (the reference's update rule keeps it
   // there); the phi-perturbed residuals only feed the discarded 2x2 solve.
-  // Production build: with phi fixed the rest-frame flux direction f is
-  // fixed, so pi^ij(xi) = athin(xi) pi0^ij and the contractions con2prim
-  // needs scale by athin; they are formed once per solve and each residual
-  // is scalar work (the exact build keeps the reference's per-residual
-  // tensor arithmetic).
-  __device__ __forceinline__ void solve_closure(double E, V3 F, double &xi_io, double &phi_out) const {
+  // Exact build: the reference's central-difference Newton, tensor
+  // arithmetic per residual.  Production build: with phi fixed the
+  // rest-frame flux direction f is fixed, so pi^ij(xi) = athin(xi) pi0^ij
+  // with athin = xi^2 (2 xi - 1), and every quantity con2prim forms is a
+  // rational function of athin: the residual and its exact derivative are
+  // scalar work (the difference quotient is kept for the robust-rewrite
+  // branch and degenerate states).  Pi_out (production, phi = pi) receives
+  // athin(xi) pi0 for the caller's pressure tensor.
+  __device__ __forceinline__ void solve_closure(double E, V3 F, double &xi_io, double &phi_out,
+                                                T2 *Pi_out = nullptr, bool *pi_done = nullptr) const {
     const int max_iter = 30;
     const double tol = 1.e6 * DBL_EPSILON;
     const double eps = sqrt(10 * DBL_EPSILON);
@@ -369,33 +373,58 @@ struct Closure {
     double fXi = 1.e3, fPhi = 1.e3;
     double xi = xi_io, phi = PI;
 #ifndef PHX_EXACT
-    // pi0 contractions for phi = pi
     double f[3];
 #pragma unroll
     for (int i = 0; i < 3; i++) f[i] = g.d[i] + SIN_PI * dd.d[i];
     T2 Pi0;
     tilpi_fill(f, 1.0, Pi0);
-    V3 cvPi0;
-    double vvPi0;
-    contractions(Pi0, cvPi0, vvPi0);
+    V3 C0;
+    double V0;
+    contractions(Pi0, C0, V0);
     const double vF = ccov(con_v, F);
-    auto res = [&](double x) {
-      const double athin = 0.5 * (3 * closure_fn(x) - 1);
-      const double vvPi = athin * vvPi0;
-      const double lam = D3(2.0 * W2 + 1.0) + (2.0 * W2 - 3.0) * W2 * vvPi;
+    const double L0 = D3(2.0 * W2 + 1.0), c1 = (2.0 * W2 - 3.0) * W2;
+    const double NJ = (2 * W2 - 1) * E - 2 * W2 * vF;
+    const double K0 = D3(4 * W2) * E - D3(4 * W2 + 1) * vF, Kv = -E + W2 * vF;
+    // residual at x; *df its derivative, NaN where the difference quotient is needed
+    auto res = [&](double x, double *df) {
+      const double at = x * x * (2 * x - 1);
+      const double V = at * V0;
+      const double lam = L0 + c1 * V;
       const double ilam = rcp_p(lam + (lam >= 0 ? kSMALL : -kSMALL));
-      const double a = W2 * ilam * ((D3(4 * W2) - vvPi) * E - (D3(4 * W2 + 1) - W2 * vvPi) * vF);
-      double J = ((2 * W2 - 1) * E - 2 * W2 * vF) * ilam;
+      const double K = K0 + V * Kv;
+      const double A = W2 * ilam * K;
+      const double J = NJ * ilam;
+      const double Ja = J * at;
       V3 H;
 #pragma unroll
-      for (int i = 0; i < 3; i++) H.d[i] = (F.d[i] - J * athin * cvPi0.d[i] - cov_v.d[i] * a) * iW;
+      for (int i = 0; i < 3; i++) H.d[i] = (F.d[i] - Ja * C0.d[i] - cov_v.d[i] * A) * iW;
       const double vh = ccov(con_v, H);
       const double s0 = sqrt(ccov(H, H) - vh * vh);
       const double iJ = rcp_p(J + (J >= 0 ? kSMALL : -kSMALL));
       const double xc = s0 * iJ;
       double sH = s0;
-      if (robust && !isnan(xc) && !isnan(J) && (J < 0. || xc >= 1.0)) {
-        if (xc >= 1.0) sH = s0 * (0.999 * rcp_p(xc));
+      const bool modified = robust && !isnan(xc) && !isnan(J) && (J < 0. || xc >= 1.0);
+      if (modified && xc >= 1.0) sH = s0 * (0.999 * rcp_p(xc));
+      if (df) {
+        if (modified || !(s0 > 0.0)) {
+          *df = __longlong_as_double(0x7ff8000000000000ll);
+        } else {
+          const double dat = x * (6 * x - 2);
+          const double dV = dat * V0;
+          const double dilam = -(c1 * dV) * ilam * ilam;
+          const double dJ = NJ * dilam;
+          const double dA = W2 * (dilam * K + ilam * (Kv * dV));
+          const double dJa = dJ * at + J * dat;
+          double hdh = 0.0, vdh = 0.0;
+#pragma unroll
+          for (int i = 0; i < 3; i++) {
+            const double dH = (-dJa * C0.d[i] - cov_v.d[i] * dA) * iW;
+            hdh += H.d[i] * dH;
+            vdh += con_v.d[i] * dH;
+          }
+          const double ds0 = (hdh - vh * vdh) * rcp_p(s0);
+          *df = 1.0 - (ds0 - s0 * dJ * iJ) * iJ;
+        }
       }
       return x - sH * iJ;
     };
@@ -407,12 +436,12 @@ struct Closure {
       const double f_up = residual(E, F, xi_up, phi, g, dd);
       const double f_lo = residual(E, F, xi_lo, phi, g, dd);
       fXi = residual(E, F, xi, phi, g, dd);
-#else
-      const double f_up = res(xi_up);
-      const double f_lo = res(xi_lo);
-      fXi = res(xi);
-#endif
       const double J00 = (f_up - f_lo) / (xi_up - xi_lo);
+#else
+      double J00;
+      fXi = res(xi, &J00);
+      if (!isfinite(J00)) J00 = (res(xi_up, nullptr) - res(xi_lo, nullptr)) / (xi_up - xi_lo);
+#endif
       const double dx0 = fXi / J00, dx1 = 0.0;
       fPhi = 0.0;
       double cdx = smin(dx0, xi - delta * xi);
@@ -425,6 +454,16 @@ struct Closure {
     } while (iter < max_iter && (fabs(fXi) > tol || fabs(fPhi) > tol));
     xi_io = xi;
     phi_out = phi;
+#ifndef PHX_EXACT
+    if (Pi_out && phi == PI) {
+      const double at = 0.5 * (3 * closure_fn(xi) - 1);
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) Pi_out->d[i][j] = Pi0.d[i][j] * at;
+      *pi_done = true;
+    }
+#endif
   }
   // GetConTilPiFromCon
   __device__ __forceinline__ void tilpi_from_con(double E, const V3 &F, double &xi, double &phi, T2 &Pi) const {
@@ -436,11 +475,14 @@ struct Closure {
       xi = 0.0;
       phi = PI;
     } else {
-      solve_closure(E, F, xi, phi);
-      V3 g, dd;
-      basis(F, g, dd);
-      double f[3];
-      angles_pressure(xi, phi, g, dd, Pi, f);
+      bool done = false;
+      solve_closure(E, F, xi, phi, &Pi, &done);
+      if (!done) {
+        V3 g, dd;
+        basis(F, g, dd);
+        double f[3];
+        angles_pressure(xi, phi, g, dd, Pi, f);
+      }
     }
   }
 };
@@ -647,7 +689,13 @@ __global__ void __launch_bounds__(128) k_fluxes(RPar p, BView b, RView r, Range3
     Hl.d[a] = Jl * ql[1 + a];
     Hr.d[a] = Jr * qr[1 + a];
   }
+#ifdef PHX_EXACT
   if (p.bounds) {
+#else
+  // with the ceiling at DBL_MAX (radiation ceilings off) no finite xi
+  // exceeds it, and an infinite xi needs J = 0, where H = J q is already 0
+  if (p.bounds && p.xi_ceiling < kDBLMAX) {
+#endif
     const double vhl = ccov(vl, Hl), vhr = ccov(vr, Hr);
     const double xil = div_p(sqrt(ccov(Hl, Hl) - vhl * vhl), Jl);
     const double xir = div_p(sqrt(ccov(Hr, Hr) - vhr * vhr), Jr);
