@@ -510,12 +510,26 @@ def bench_m1(ctx, args, dev):
         torch.cuda.synchronize()
         split[name] = a.elapsed_time(b)
     ctx.check()
+    # FP64 rate of the flux kernel: ncu's FP64 operation count per face (the
+    # production build, profiles/m1_fp64_per_unit.json) over the event time
+    fp64 = None
+    prof = ROOT / "profiles" / "m1_fp64_per_unit.json"
+    if prof.exists():
+        cnt = json.loads(prof.read_text())
+        faces = 3 * args.m1_n * args.m1_n * (args.m1_n + 1)
+        peak = ctx.probe_fp64_peak()
+        ach = faces * cnt["flux_flops_per_face"] / (split["fluxes"] * 1e-3)
+        inst = faces * cnt["flux_fp64_instructions_per_face"] / (split["fluxes"] * 1e-3)
+        fp64 = {"kernel": "rad::k_fluxes (x1/x2/x3)", "achieved_tflops": ach / 1e12, "peak_tflops": peak / 1e12,
+                "frac": ach / peak, "issue_frac": inst / (peak / 2.0),
+                "flops_source": "ncu dadd + dmul + 2 dfma per face, 96^3 capture (profiles/m1_fp64_per_unit.json)",
+                "peak_source": "measured in-process (phx_probe_fp64_peak)"}
     J = db["rprim"][abi.RJ][db.isl()]
     res = {"workload": f"M1 radiation, {args.m1_n}^3 periodic Minkowski block, gray scattering kappa dx = 2, "
                        "kappa_a = 1, fluid u = W (0.3, 0, 0), Gaussian J pulse, linear reconstruction; one RK2 "
                        "step (2 stages + timestep estimate) per step",
            "zone_updates_per_s": zones / (ms * 1e-3), "ms_per_step": ms, "steps": args.m1_steps,
-           "stage_split_ms": split, "nan_J": int(torch.isnan(J).sum()),
+           "stage_split_ms": split, "fp64": fp64, "nan_J": int(torch.isnan(J).sum()),
            "c2p_fail_zones": int((db["rprim"][abi.RFAIL][db.isl()] != 1.0).sum()),
            "gpu_launches_per_step": 2 * (4 + 3 + 2 + 1) + 3}
     del db, buf, base
