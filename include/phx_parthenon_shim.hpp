@@ -15,6 +15,14 @@
 //   TaskStatus fluid::CalculateFluxes(MeshBlockData<Real> *)             fluid.cpp:659
 //   TaskStatus fluid::FluxCT(MeshBlockData<Real> *)                      fluid.cpp:775
 //   TaskStatus fixup::FixFluxes(MeshBlockData<Real> *)                   fixup.cpp:728
+//   template <T> TaskStatus radiation::MomentPrim2Con(T *, IndexDomain)  moments.cpp:258
+//   template <T> TaskStatus radiation::MomentCon2Prim(T *)               moments.cpp:162
+//   template <T> TaskStatus radiation::MomentCalculateOpacities(T *)     moments.cpp:919
+//   template <T> TaskStatus radiation::ReconstructEdgeStates(T *)        moments.cpp:280
+//   template <T> TaskStatus radiation::CalculateFluxes(T *)              moments.cpp:724
+//   template <T> TaskStatus radiation::CalculateGeometricSource(T *, T *) moments.cpp:886
+//   template <T> TaskStatus radiation::MomentFluidSource(T *, Real, bool) moments_source.cpp:960
+//   Real radiation::EstimateTimestepBlock(MeshBlockData<Real> *)         radiation.cpp:681
 //   Real fluid::EstimateTimestepBlock(MeshBlockData<Real> *)             fluid.cpp:899
 //   template <T> using fluid::c2p_type = TaskStatus (*)(T *, ...)        fluid.hpp:65
 //
@@ -40,6 +48,7 @@
 #include <vector>
 
 #include "phx_fluid.h"
+#include "phx_radiation.h"
 
 namespace parthenon {
 using Real = double;
@@ -59,6 +68,7 @@ struct Mesh {
   double *dt_device = nullptr;  // one device double for EstimateTimestepBlock
   bool has_face_speeds = false; // fluid.cpp:911-941 switch
   int ndim = 3;
+  phx_rad_params rad_params{};  // "radiation" (+ opacity, fixup) package Params
 };
 
 template <typename T>
@@ -96,10 +106,15 @@ class MeshBlockData<Real> {
   }
   const int *BoundaryLo() const { return bc_lo_; }
   const int *BoundaryHi() const { return bc_hi_; }
+  // the radiation fields of the block (E, F_i of this stage container; the
+  // OneCopy J, H, xi, phi, c2pfail, kappaJ, kappaH, JBB)
+  void SetRadiation(const phx_rad_block &r) { rad_ = r; }
+  phx_rad_block &RadBlock() { return rad_; }
 
  private:
   Mesh *mesh_;
   phx_block b_;
+  phx_rad_block rad_{};
   int bc_lo_[3] = {PHX_BC_PERIODIC, PHX_BC_PERIODIC, PHX_BC_PERIODIC};
   int bc_hi_[3] = {PHX_BC_PERIODIC, PHX_BC_PERIODIC, PHX_BC_PERIODIC};
 };
@@ -277,5 +292,107 @@ inline TaskStatus FixFluxes(MeshBlockData<Real> *rc) {
   return TaskStatus::complete;
 }
 }  // namespace fixup
+
+namespace radiation {
+using parthenon::IndexDomain;
+using parthenon::IndexRange;
+using parthenon::MeshBlockData;
+using parthenon::Real;
+using parthenon::TaskStatus;
+
+namespace detail {
+inline void check(phx_status s, const char *where) {
+  if (s != PHX_OK) throw std::runtime_error(std::string(where) + ": " + phx_last_error());
+}
+inline phx_range R(const IndexRange &r) { return phx_range{r.s, r.e}; }
+}  // namespace detail
+
+template <typename T>
+TaskStatus MomentPrim2Con(T *rc, IndexDomain domain);
+template <>
+inline TaskStatus MomentPrim2Con<MeshBlockData<Real>>(MeshBlockData<Real> *rc, IndexDomain domain) {
+  parthenon::Mesh *m = rc->GetMeshPointer();
+  detail::check(phx_rad_prim_to_con(m->ctx, &m->rad_params, &m->params, &rc->Block(), &rc->RadBlock(),
+                                    detail::R(rc->GetBoundsI(domain)), detail::R(rc->GetBoundsJ(domain)),
+                                    detail::R(rc->GetBoundsK(domain)), m->stream),
+                "MomentPrim2Con");
+  return TaskStatus::complete;
+}
+
+// the package's PostFillDerivedBlock: the entire block
+template <typename T>
+TaskStatus MomentCon2Prim(T *rc);
+template <>
+inline TaskStatus MomentCon2Prim<MeshBlockData<Real>>(MeshBlockData<Real> *rc) {
+  parthenon::Mesh *m = rc->GetMeshPointer();
+  const IndexDomain e = IndexDomain::entire;
+  detail::check(phx_rad_con_to_prim(m->ctx, &m->rad_params, &m->params, &rc->Block(), &rc->RadBlock(),
+                                    detail::R(rc->GetBoundsI(e)), detail::R(rc->GetBoundsJ(e)),
+                                    detail::R(rc->GetBoundsK(e)), m->stream),
+                "MomentCon2Prim");
+  return TaskStatus::complete;
+}
+
+template <typename T>
+TaskStatus MomentCalculateOpacities(T *rc);
+template <>
+inline TaskStatus MomentCalculateOpacities<MeshBlockData<Real>>(MeshBlockData<Real> *rc) {
+  parthenon::Mesh *m = rc->GetMeshPointer();
+  detail::check(phx_rad_calculate_opacities(m->ctx, &m->rad_params, &m->params, &rc->Block(), &rc->RadBlock(),
+                                            m->stream),
+                "MomentCalculateOpacities");
+  return TaskStatus::complete;
+}
+
+// The reconstruction is fused into CalculateFluxes (no ql/qr/dJ fields).
+template <typename T>
+TaskStatus ReconstructEdgeStates(T *rc) {
+  return TaskStatus::complete;
+}
+
+template <typename T>
+TaskStatus CalculateFluxes(T *rc);
+template <>
+inline TaskStatus CalculateFluxes<MeshBlockData<Real>>(MeshBlockData<Real> *rc) {
+  parthenon::Mesh *m = rc->GetMeshPointer();
+  detail::check(phx_rad_calculate_fluxes(m->ctx, &m->rad_params, &m->params, &rc->Block(), &rc->RadBlock(),
+                                         m->stream),
+                "radiation::CalculateFluxes");
+  return TaskStatus::complete;
+}
+
+// Minkowski: every source term is zero (moments.cpp:820-870 with vanishing
+// metric derivatives); phx_rad_update adds it.
+template <typename T>
+TaskStatus CalculateGeometricSource(T *rc, T *rc_src) {
+  return TaskStatus::complete;
+}
+
+template <typename T>
+TaskStatus MomentFluidSource(T *rc, Real dt, bool update_fluid);
+template <>
+inline TaskStatus MomentFluidSource<MeshBlockData<Real>>(MeshBlockData<Real> *rc, Real dt, bool update_fluid) {
+  parthenon::Mesh *m = rc->GetMeshPointer();
+  phx_rad_params rp = m->rad_params;
+  rp.update_fluid = update_fluid ? 1 : 0;
+  detail::check(phx_rad_fluid_source(m->ctx, &rp, &m->params, &rc->Block(), &rc->RadBlock(), dt, m->stream),
+                "MomentFluidSource");
+  return TaskStatus::complete;
+}
+
+inline Real EstimateTimestepBlock(MeshBlockData<Real> *rc) {
+  parthenon::Mesh *m = rc->GetMeshPointer();
+  if (!m->dt_device) throw std::runtime_error("EstimateTimestepBlock: Mesh::dt_device is not set");
+  detail::check(phx_rad_estimate_timestep(m->ctx, &m->rad_params, &m->params, &rc->Block(), &rc->RadBlock(),
+                                          m->dt_device, m->stream),
+                "radiation::EstimateTimestepBlock");
+  Real dt = 0.0;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(m->stream);
+  if (cudaMemcpyAsync(&dt, m->dt_device, sizeof(Real), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    throw std::runtime_error("radiation::EstimateTimestepBlock: copy of dt failed");
+  return dt;
+}
+}  // namespace radiation
 
 #endif  // PHX_PARTHENON_SHIM_HPP_

@@ -118,6 +118,48 @@ def test_rk2_steps_bitwise(rx, rad_oracle, method, ndim):
     rx.check()
 
 
+BRANCHES = [
+    dict(rad=dict(enable_rad_floors=1, J0_floor=0.05, enable_rad_ceilings=1, xi0_ceiling=0.3, tau0_ceiling=0.5),
+         fluid=dict(enable_ceilings=1, gam0_ceiling=1.05)),
+    dict(rad=dict(closure_frail=1, oned_fixup_strategy="ignore_all"), fluid={}),
+    dict(rad=dict(oned_fixup_strategy="ignore_dJ", recon_fixup_bounds=0), fluid={}),
+    dict(rad=dict(method="moment_eddington", oned_fixup_strategy="ignore_dJ", enable_rad_ceilings=1,
+                  xi0_ceiling=0.5, tau0_ceiling=2.0), fluid={}),
+]
+
+
+@pytest.mark.parametrize("case", range(len(BRANCHES)))
+def test_branches_bitwise(rx, rad_oracle, case):
+    """Bounds, ceilings, the W ceiling, the frail closure and the oned fixup
+    strategies on states with |H|/J up to 0.999 (inversions that fail or are
+    rewritten), every task and a full stage, bit for bit."""
+    import torch
+
+    cfg = BRANCHES[case]
+    hb, db = _pair((14, 12, 10), 3, seed=70 + case, vmax=0.45, hmax=0.999)
+    rp = abi.default_rad_params(cfl=0.5, kappa_s=60.0, kappa_a=4.0, jbb_coeff=0.8, **cfg["rad"])
+    p = abi.default_params(Cv=1.0, **cfg["fluid"])
+    for o, b in ((rad_oracle, hb), (rx, db)):
+        o.MomentPrim2Con(rp, p, b, *b.entire())
+    # every 7th zone gets a flux beyond the free-streaming limit: inversions
+    # that the robust strategy rewrites and the frail one fails
+    bad = (np.arange(hb.N) % 7 == 3).reshape(hb.shape)
+    hb["rcons"][abi.RF:abi.RF + 3][:, bad] *= 1.8
+    db["rcons"].copy_(torch.from_numpy(hb["rcons"]))
+    for o, b in ((rad_oracle, hb), (rx, db)):
+        o.MomentCon2Prim(rp, p, b)
+    _cmp(db, hb, ["rcons", "rprim"], "con2prim")
+    dt = 3.0e-3
+    out_h = np.zeros_like(hb["rcons"])
+    out_d = torch.zeros_like(db["rcons"])
+    rad_oracle.Stage(rp, p, hb, hb["rcons"].copy(), out_h, 1.0, dt)
+    rx.Stage(rp, p, db, db["rcons"].clone(), out_d, 1.0, dt)
+    assert_bitwise(out_d, out_h, "stage output")
+    _cmp(db, hb, ["rprim"], "stage prims")
+    assert rx.EstimateTimestepBlock(rp, p, db) == rad_oracle.EstimateTimestepBlock(rp, p, hb)
+    rx.check()
+
+
 def gpu_diffusion(rc):
     hb, _, _, _ = radiation.radiation_advection()
     return run_diffusion(rc, hb.to_device())

@@ -71,10 +71,10 @@ def assert_close(got, ref, rtol, what="", floor=None):
                              f"{got[i0]!r} ref {ref[i0]!r}")
 
 
-def random_rad_block(nx, ndim, seed, vmax=0.4, kappa_s=50.0, kappa_a=5.0, ng=4):
+def random_rad_block(nx, ndim, seed, vmax=0.4, kappa_s=50.0, kappa_a=5.0, ng=4, hmax=0.6):
     """A host Block with random fluid background (rho, T, u, u^i on the whole
-    block) and random radiation primitives J > 0, |H|/J < 0.6 of one species,
-    xi = 0, phi = pi, radiation conserved moments unset."""
+    block) and random radiation primitives J > 0, |H|/J < hmax of one
+    species, xi = 0, phi = pi, radiation conserved moments unset."""
     from phoebus_gb300 import abi
     from phoebus_gb300.block import Block
     from phoebus_gb300.radiation import alloc_rad
@@ -97,7 +97,7 @@ def random_rad_block(nx, ndim, seed, vmax=0.4, kappa_s=50.0, kappa_a=5.0, ng=4):
         P[abi.PVEL + d] = W * u[d] if d < ndim else 0.3 * W * u[d]
     R[abi.RJ] = np.exp(rng.uniform(np.log(1e-3), 0.0, shp))
     h = rng.uniform(-1, 1, (3,) + shp)
-    h *= 0.6 * rng.uniform(0, 1, shp) / np.maximum(np.sqrt((h * h).sum(0)), 1e-12)
+    h *= hmax * rng.uniform(0, 1, shp) ** 0.25 / np.maximum(np.sqrt((h * h).sum(0)), 1e-12)
     for d in range(3):
         R[abi.RH + d] = h[d]
     R[abi.RXI] = 0.0
