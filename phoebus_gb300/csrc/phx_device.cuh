@@ -401,7 +401,14 @@ __device__ __forceinline__ double mc(double dm, double dp, double alpha) {
   // FP64 instructions; only the sign of a zero slope can differ
   const double dc = dm * dp > 0.0 ? 0.5 * (dm + dp) : 0.0;
 #endif
+#ifdef PHX_EXACT
+  // std::min (reconstruction.hpp:106): a NaN slope propagates, as fmin would not
+  const double m1 = (fabs(dp) < fabs(dm)) ? fabs(dp) : fabs(dm);
+  const double m2 = alpha * m1;
+  return copysign((m2 < fabs(dc)) ? m2 : fabs(dc), dc);
+#else
   return copysign(fmin(fabs(dc), alpha * fmin(fabs(dm), fabs(dp))), dc);
+#endif
 }
 __device__ __forceinline__ void recon_plm(double qm, double q0, double qp, double &ql, double &qr) {
   double dq = qp - q0;
