@@ -784,6 +784,24 @@ __global__ void __launch_bounds__(256) k_update(BView b, RView r, const double *
 struct TRes {
   const RPar *p;
   double rho, ug0, J0, dtau, amax;
+#ifndef PHX_EXACT
+  // gray opacity: kappa does not depend on T, so both denominators are fixed
+  // per zone (production build: two reciprocals instead of a division per
+  // evaluation)
+  double dk, i1, i2;
+  __device__ __forceinline__ void prepare() {
+    dk = dtau * smin(rho * p->kappa_a, amax);
+    i1 = rcp_p(1. + dk);
+    i2 = rcp_p(ug0 + J0);
+  }
+  __device__ __forceinline__ double operator()(double T) const {
+    const double JBB = p->jbb * (T * T) * (T * T);
+    const double dJ = (J0 + dk * JBB) * i1 - J0;
+    const double ug1 = rho * (p->Cv * T);
+    return ((ug1 - ug0) + dJ) * i2;
+  }
+#else
+  __device__ __forceinline__ void prepare() {}
   __device__ __forceinline__ double operator()(double T) const {
     double kappa = rho * p->kappa_a;
     kappa = smin(kappa, amax);
@@ -792,6 +810,7 @@ struct TRes {
     const double ug1 = rho * (p->Cv * T);
     return ((ug1 - ug0) + dJ) / (ug0 + J0);
   }
+#endif
 };
 // RootFind::regula_falsi with a status; the iteration count persists across
 // calls (the reference reuses one RootFind for its re-bracketing tries).
@@ -875,7 +894,8 @@ __global__ void __launch_bounds__(128) k_source(RPar p, BView b, RView r, double
   {
     const double J0 = r.prim[PHX_RJ * vs + id];
     const double dtau = alpha * dt / W;
-    const TRes res{&p, rho, ug, J0, dtau, amax};
+    TRes res{&p, rho, ug, J0, dtau, amax};
+    res.prepare();
     int count = 0;
     bool ok;
     double T1 = regula_falsi(res, 1.e-2 * Tf, 1.e2 * Tf, p.tol * Tf, Tf, count, p.maxiter, ok);
