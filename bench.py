@@ -96,7 +96,7 @@ def parse():
                    help="run only the radiation M1 section and print its JSON (profiling)")
     a.add_argument("--m1-n", type=int, default=128)
     a.add_argument("--m1-steps", type=int, default=3)
-    a.add_argument("--m1-cpu-n", type=int, default=48)
+    a.add_argument("--m1-cpu-n", type=int, default=64)
     return a.parse_args()
 
 
@@ -548,7 +548,7 @@ def bench_m1(ctx, args, dev):
         hbuf = np.zeros_like(hb["rcons"])
         o.rk2_step(rp, p, hb, hbuf, hdt)
         times = []
-        for _ in range(2):
+        for _ in range(3):
             t0 = time.perf_counter()
             o.rk2_step(rp, p, hb, hbuf, hdt)
             o.EstimateTimestepBlock(rp, p, hb)
