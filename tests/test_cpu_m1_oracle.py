@@ -6,7 +6,9 @@
   every 10th value).  The gold predates the reference tree (its deck lacks
   the <phoebus> boundary keys the current fluid package requires), and the
   restatement of the current code meets it on the pulse, not at its 1e-5
-  tolerance: the bands below are the measured agreement with margin.
+  tolerance: the bands below are the measured agreement with margin.  With
+  the timestep of the free-streaming signal speed (the estimate before its
+  diffusion-limit mixing) the agreement is about three times closer.
 - the restated tanh against the correctly rounded value;
 - closure inversions: prim -> con -> prim round trips (M1, Eddington).
 """
@@ -28,10 +30,12 @@ def rad_oracle(built):
     return RadOracle()
 
 
-def run_diffusion(o, b=None):
+def run_diffusion(o, b=None, free_streaming_dt=False):
     """The regression run through any object with the RadOracle task names
     (the oracle on host arrays, or a RadiationContext on device arrays).
-    Returns (block, TimeControl, dts)."""
+    free_streaming_dt: the timestep cfl dx / 1 of the signal speed cs_rad = 1
+    (the estimate before its diffusion-limit mixing) instead of the current
+    EstimateTimestepBlock.  Returns (block, TimeControl, dts)."""
     if b is None:
         b, par, rpar, tlim = radiation.radiation_advection()
     else:
@@ -39,14 +43,15 @@ def run_diffusion(o, b=None):
     p, rp = abi.default_params(**par), abi.default_rad_params(**rpar)
     o.MomentPrim2Con(rp, p, b)
     o.Initialize(rp, p, b)
-    tc = states.TimeControl(tlim, o.EstimateTimestepBlock(rp, p, b), dt_init_fact=1.0e-6)
+    est = (lambda: rp.cfl * b.dx[0]) if free_streaming_dt else (lambda: o.EstimateTimestepBlock(rp, p, b))
+    tc = states.TimeControl(tlim, est(), dt_init_fact=1.0e-6)
     buf = np.zeros_like(b["rcons"]) if isinstance(b["rcons"], np.ndarray) else b["rcons"].clone()
     dts = []
     while tc.keep_going():
         dt = tc.begin_step()
         dts.append(dt)
         o.rk2_step(rp, p, b, buf, dt)
-        tc.end_step(o.EstimateTimestepBlock(rp, p, b))
+        tc.end_step(est())
     return b, tc, dts
 
 
@@ -74,6 +79,21 @@ def test_radiation_diffusion_gold(rad_oracle):
     assert abs(c - cg) < 1.0e-4 and abs(J.max() - Jg.max()) / Jg.max() < 1.0e-3
     assert np.abs(comp[52:104] - gold[52:104]).max() < 4.0e-3  # H_x / J (measured 2.2e-3)
     assert np.abs(comp[104:]).max() < 1.0e-20  # H_y, H_z: round-off only, as in the gold
+
+
+def test_radiation_diffusion_gold_free_streaming_dt(rad_oracle):
+    """The same run with the timestep of the free-streaming signal speed
+    (cs_rad = 1, dt = cfl dx: 1025 steps) meets the gold about three times
+    closer on every measure: the gold's dt sequence is the earlier estimate's,
+    and the time-discretisation error of the operator-split stiff scattering
+    source is most of the remaining difference."""
+    b, tc, dts = run_diffusion(rad_oracle, free_streaming_dt=True)
+    assert tc.time == 1.0 and tc.ncycle == 1025
+    comp, gold = diffusion_values(b), np.loadtxt(GOLD / "radiation_diffusion.gold")
+    rel = np.abs(comp - gold) / np.maximum(np.abs(gold), 1.0e-10)
+    assert rel[:52][gold[:52] >= 1.0e-2].max() < 5.0e-3  # measured 3.7e-3
+    assert rel[:52].max() < 3.0e-2  # measured 2.2e-2
+    assert np.abs(comp[52:104] - gold[52:104]).max() < 1.0e-3  # measured 7.6e-4
 
 
 def test_tanh_restatement(rad_oracle):
