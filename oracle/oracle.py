@@ -90,6 +90,7 @@ def lib() -> C.CDLL:
             ("orc_rad_fill_ghosts_periodic", [BS, RB], None),
             ("orc_rad_estimate_timestep", [RP, PP, BS, RB], C.c_double),
             ("orc_rad_tanh", [C.c_double], C.c_double),
+            ("orc_rad_m1_guess", [C.c_void_p] * 3 + [C.c_longlong] + [C.c_void_p] * 2, None),
         ]:
             fn = getattr(L, name)
             fn.argtypes, fn.restype = args, res
@@ -321,6 +322,15 @@ class RadOracle:
 
     def tanh(self, x: float) -> float:
         return self.L.orc_rad_tanh(x)
+
+    def M1GuessesFromEddington(self, E, F, v):
+        """ClosureM1::GetM1GuessesFromEddington for arrays E [n], F [3][n],
+        coordinate velocity v [3][n]; returns (xi [n], phi [n])."""
+        E, F, v = (np.ascontiguousarray(a, dtype=np.float64) for a in (E, F, v))
+        n = E.shape[0]
+        xi, phi = np.zeros(n), np.zeros(n)
+        self.L.orc_rad_m1_guess(E.ctypes.data, F.ctypes.data, v.ctypes.data, n, xi.ctypes.data, phi.ctypes.data)
+        return xi, phi
 
     def Initialize(self, rp, p, b: Block):
         self.FillGhostsPeriodic(b)

@@ -2837,4 +2837,26 @@ double orc_rad_estimate_timestep(const phx_rad_params *rp, const phx_params *p, 
 
 double orc_rad_tanh(double x) { return tanh_r(x); }
 
+// ClosureM1::GetM1GuessesFromEddington (closure_m1.hpp:146-168) for n zones:
+// the Eddington inversion's xi = |H| / J (capped at 0.99) and phi = 1.000001 pi,
+// from E, F_i [3][n] and the fluid's coordinate velocity v^i [3][n].
+void orc_rad_m1_guess(const double *E, const double *F, const double *v, long long n, double *xi_out,
+                      double *phi_out) {
+  for (long long z = 0; z < n; z++) {
+    const V3 cv{{v[z], v[n + z], v[2 * n + z]}};
+    const Closure c(cv, true, true);
+    const V3 cF{{F[z], F[n + z], F[2 * n + z]}};
+    T2 Pi;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) Pi(i, j) = 0.0;
+    Real JEdd;
+    V3 HEdd;
+    c.Con2Prim(E[z], cF, Pi, JEdd, HEdd);
+    const Real vH = cconcov(cv, HEdd);
+    const Real Hm = std::sqrt(ccov(HEdd, HEdd) - vH * vH);
+    xi_out[z] = smin(ratio(Hm, JEdd), 0.99);
+    phi_out[z] = 1.000001 * PI;
+  }
+}
+
 }  // extern "C"

@@ -182,3 +182,59 @@ def test_pulse_workload_steps_cleanly(rad_oracle):
         rad_oracle.rk2_step(rp2, p2, b2, buf2, dt2)
     E1 = b2["rcons"][abi.RE][sl].sum()
     assert abs(E1 - E0) / E0 < 1e-12
+
+
+def closure_unit_block():
+    """tst/unit/radiation/test_closure.cpp's grid as a 1D block: phi_v = 0,
+    |v| in [0, 0.6) step 0.01, xi in [1e-10, 1] step 0.01; J = 1 and
+    tilde H_1 = xi J / sqrt(gamma^11 - v_1^2) (the reference's loop bounds and
+    accumulation, restated)."""
+    from phoebus_gb300.block import Block
+    from phoebus_gb300.radiation import alloc_rad
+
+    pts = []
+    vmag = 0.0
+    while vmag < 0.6:
+        xi = 1.0e-10
+        while xi <= 1.0:
+            pts.append((vmag, xi))
+            xi += 1.0e-2
+        vmag += 1.0e-2
+    n = len(pts)
+    b = Block((n, 1, 1), ng=4, ndim=1, xmin=(0.0, 0.0, 0.0), dx=(1.0 / n, 1.0, 1.0), backend="numpy")
+    b.alloc(["prim", "cons", "flux", "face_sig", "cell_sig", "fail", "src", "emf", "dudt"])
+    alloc_rad(b)
+    sl = b.isl()
+    v = np.array([q[0] for q in pts])
+    x = np.array([q[1] for q in pts])
+    W = 1 / np.sqrt(1 - v * v)
+    P, R = b["prim"], b["rprim"]
+    P[abi.PRHO][sl] = 1.0
+    P[abi.PTMP][sl] = 1.0
+    P[abi.PVEL][sl] = W * v
+    R[abi.RJ][sl] = 1.0
+    R[abi.RH][sl] = x * 1.0 / np.sqrt(1.0 - v * v)  # H_1 / J
+    return b, v, x
+
+
+def test_closure_unit_known_answer(rad_oracle):
+    """tst/unit/radiation/test_closure.cpp ("M1 Closure"): prim2con, the M1
+    guesses from the Eddington inversion, the closure solve and con2prim
+    recover J and tilde H_1 within 1e-5 at every one of the 6000 points
+    (REQUIRE(n_wrong == 0))."""
+    b, v, x = closure_unit_block()
+    rp, p = abi.default_rad_params(method="moment_m1"), abi.default_params()
+    rad_oracle.MomentPrim2Con(rp, p, b)
+    sl = b.isl()
+    E = b["rcons"][abi.RE][sl].ravel()
+    F = np.stack([b["rcons"][abi.RF + d][sl].ravel() for d in range(3)])
+    con_v = np.stack([v, 0 * v, 0 * v])
+    xig, phig = rad_oracle.M1GuessesFromEddington(E, F, con_v)
+    b["rprim"][abi.RXI][sl] = xig
+    b["rprim"][abi.RPHI][sl] = phig / 1.0001  # MomentCon2Prim scales the stored phi by 1.0001
+    rad_oracle.MomentCon2Prim(rp, p, b, *b.interior())
+    J_out = b["rprim"][abi.RJ][sl].ravel()
+    H_out = b["rprim"][abi.RH][sl].ravel() * J_out
+    H_in = x / np.sqrt(1.0 - v * v)
+    wrong = ~((np.abs(1.0 - J_out) / 1.0 < 1.0e-5) & (np.abs(H_in - H_out) / 1.0 < 1.0e-5))
+    assert len(x) == 6000 and wrong.sum() == 0, f"{wrong.sum()} of {len(x)} points wrong"
