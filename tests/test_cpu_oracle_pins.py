@@ -139,3 +139,60 @@ def test_uniform_state_is_stationary(oracle, recon):
     ks, js, is_ = b.isl()
     assert np.all(b["dudt"][:, ks, js, is_] == 0.0)
     assert np.all(b["src"][:, ks, js, is_] == 0.0)
+
+
+def test_fmks_geometry_known_answer(oracle):
+    """tst/unit/geometry/test_geometry.cpp "Modified Kerr-Schild": FMKS with
+    a = 0.8, pole derefinement, hslope 0.3, poly_xt 0.82, poly_alpha 14,
+    smooth 0.5, x0 = -0.4409148982097008 at X = (1.13248983, 0.26388889,
+    3.27249235): lapse, det g, g_mu nu and g^mu nu within the test's
+    GetDifference < 1e-5 (and |value| < 1e-5 where it requires zero)."""
+    g = abi.default_geometry(abi.GEOM_FMKS, a=0.8, derefine_poles=1, hslope=0.3, poly_xt=0.82, poly_alpha=14.0,
+                             smooth=0.5, x0=-0.4409148982097008)
+    out = oracle.fmks_point(g, 1.1324898310315077, 0.2638888888888889, 3.2724923474893677)
+    ind = [[0, 1, 3, 6], [1, 2, 4, 7], [3, 4, 5, 8], [6, 7, 8, 9]]
+    ind3 = [[0, 1, 3], [1, 2, 4], [3, 4, 5]]
+    gc = np.array([[out[abi.G_GCOV + ind[m][n]] for n in range(4)] for m in range(4)])
+    alpha = out[abi.G_ALPHA]
+    beta = out[abi.G_BETA:abi.G_BETA + 3]
+    gam = np.array([[out[abi.G_GAMCON + ind3[a][b]] for b in range(3)] for a in range(3)])
+    gi = np.zeros((4, 4))  # spacetime inverse from lapse, shift, gamma^ij
+    gi[0, 0] = -1 / alpha**2
+    gi[0, 1:] = gi[1:, 0] = beta / alpha**2
+    gi[1:, 1:] = gam - np.outer(beta, beta) / alpha**2
+
+    def diff(a, b):  # test_geometry.cpp GetDifference
+        return 2 * abs(b - a) / (abs(b) + abs(a) + 1e-300)
+
+    assert diff(alpha, 0.7811769941965497) < 1e-5
+    assert diff(alpha * out[abi.G_DETGAM], 64.40965903079623) < 1e-5
+    for (m, n), ref in {(0, 0): -0.3612937485396168, (0, 1): 1.9821442243860723, (1, 1): 15.78288823,
+                        (1, 2): -0.17903916, (1, 3): -3.51690001, (2, 2): 51.27859056, (3, 3): 9.18405881}.items():
+        assert diff(gc[m, n], ref) < 1e-5 and diff(gc[n, m], ref) < 1e-5, (m, n)
+    assert abs(gc[0, 2]) < 1e-5 and abs(gc[2, 3]) < 1e-5
+    for (m, n), ref in {(0, 0): -1.63870625, (0, 1): 2.05810289e-01, (1, 1): 4.34252153e-02,
+                        (1, 2): 0.00015161910494636605, (1, 3): 2.65272964e-02, (2, 2): 1.95018454e-02,
+                        (3, 3): 1.19042557e-01}.items():
+        assert diff(gi[m, n], ref) < 1e-5, (m, n)
+    assert abs(gi[0, 3]) < 1e-5
+    assert np.allclose(gc @ gi, np.eye(4), atol=1e-12)
+
+
+def test_lorentz_factor_known_answer(oracle):
+    """tst/unit/phoebus_utils/test_relativity_utils.cpp "RELATIVITY": for the
+    primitive velocity W (0.7, 0.2, 0.1) on Minkowski, W = 1.474419561548971247
+    (SoftEquiv at 1e-8); through prim2con, D = rho W and S_i = (rho h + b^2)
+    W^2 v_i."""
+    W_ref = 1.474419561548971247e+00
+    prim = np.zeros((abi.NPRIM, 1))
+    prim[abi.PRHO] = 1.0
+    prim[abi.PENG] = 1.0e-3
+    prim[abi.PPRS] = (5.0 / 3.0 - 1.0) * 1.0e-3
+    prim[abi.PGM1] = 5.0 / 3.0
+    prim[abi.PVEL:abi.PVEL + 3, 0] = np.array([0.7, 0.2, 0.1]) * W_ref
+    p = abi.default_params(Gamma=5.0 / 3.0, mhd=0)
+    cons = oracle.PrimitiveToConservedZones(p, prim)
+    assert abs(cons[abi.CRHO, 0] - W_ref) < 1e-8 * W_ref / 2
+    h = 1.0 + (1.0e-3 + prim[abi.PPRS, 0]) / 1.0
+    for d, vd in enumerate((0.7, 0.2, 0.1)):
+        assert abs(cons[abi.CMOM + d, 0] - h * W_ref**2 * vd) < 1e-8 * abs(h * W_ref**2 * vd)
