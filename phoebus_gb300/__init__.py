@@ -3,8 +3,10 @@
 Hand-written FP64 CUDA kernels behind the C ABI of include/phx_fluid.h:
 reconstruction (PLM, WENO5-Z, MP5) + LLF/HLL Riemann fluxes, the robust
 con2prim root find, geometric source terms and the RK stage glue, for
-Minkowski and FMKS (cached, axisymmetric) geometry.  `fluid` is the host API
-mirroring the reference task names; `states` makes seeded initial states.
+Minkowski and FMKS (cached, axisymmetric) geometry; and the radiation M1 /
+Eddington moment transport behind include/phx_radiation.h.  `fluid` and
+`radiation` are the host APIs mirroring the reference task names; `states`,
+`torus` and `radiation` make seeded initial states.
 """
 from . import abi  # noqa: F401
 from .block import Block, GeomTables  # noqa: F401
