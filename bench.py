@@ -16,8 +16,9 @@ RK2 timestep per second.
   roofline   CalculateFluxes (the dominant kernels): algorithmic bytes per
              launch / measured launch time vs the measured HBM copy peak; an
              FP64 section relates the same launches to the measured FP64 peak
-  cpu_baseline  the oracle (CPU restatement of the reference path) timed on
-             a 64^3 sample of the same state with all host threads
+  cpu_baseline  the oracle (CPU restatement of the reference path, its -O3
+             timing build) timed on a 128^3 sample of the same state with all
+             host threads
 
   batched    1024 uneven periodic blocks (edges 16/32/64, MP5 + HLL): RK2
              steps through phx_stage_batched (persistent work-list launches
@@ -28,10 +29,14 @@ RK2 timestep per second.
   c2p        con2prim over 5e7 independent FMKS Kerr-Schild zones at tolerance
              1e-10: zones/s and root-find iterations with the reference's
              start (plain) and with the learned start (network trained on
-             the GPU on 3e7 separately seeded pairs, 20 epochs, before timing)
+             the GPU on 1e7 separately seeded pairs, 20 epochs, before timing)
 
---impl reference runs the reference's CPU path (the oracle port) on the host
-cores: each step is one RK2 timestep of a 64^3 sample of the same state.
+The sections' full results are printed as one {"detail": ...} line before the
+result line, which carries their headline numbers under "sections".
+
+--impl reference runs the reference's CPU path (the oracle port, its timing
+build) on all host cores: each step is one RK2 timestep of the same 256^3
+block.
 Multi-GPU: independent replicas (one block per rank, weak scaling); the only
 cross-rank operations are the timing barriers.
 """
@@ -78,19 +83,25 @@ def parse():
     a.add_argument("--warmup", type=int, default=3)
     a.add_argument("--impl", default="ours", choices=["ours", "reference"])
     a.add_argument("--n", type=int, default=256)
-    a.add_argument("--cpu-n", type=int, default=64)
+    a.add_argument("--cpu-n", type=int, default=128,
+                   help="edge of the block the cpu_baseline leg of this arm times (a sample of the workload)")
+    a.add_argument("--ref-n", type=int, default=0,
+                   help="--impl reference: block edge (0 = the workload's own --n)")
     a.add_argument("--exact", action="store_true", help="time the parity (no-FMA) build")
     a.add_argument("--no-e2e", action="store_true")
     a.add_argument("--no-cpu", action="store_true")
     a.add_argument("--no-c2p", action="store_true", help="skip the con2prim learned-vs-plain section")
     a.add_argument("--c2p-zones", type=float, default=5e7)
-    a.add_argument("--train-pairs", type=float, default=3e7)
+    a.add_argument("--train-pairs", type=float, default=1e7)
     a.add_argument("--train-epochs", type=int, default=20)
     a.add_argument("--no-batched", action="store_true", help="skip the uneven-meshblock section")
     a.add_argument("--batched-blocks", type=int, default=1024)
     a.add_argument("--no-torus", action="store_true", help="skip the torus section")
     a.add_argument("--torus-n", type=int, default=384)
     a.add_argument("--torus-steps", type=int, default=2)
+    a.add_argument("--section-steps", type=int, default=3, help="RK2 steps per timed round (batched section)")
+    a.add_argument("--section-rounds", type=int, default=2,
+                   help="interleaved timed rounds per arm (batched and torus sections)")
     a.add_argument("--no-m1", action="store_true", help="skip the radiation M1 section")
     a.add_argument("--m1-only", action="store_true",
                    help="run only the radiation M1 section and print its JSON (profiling)")
@@ -290,11 +301,40 @@ def batched_params():
     return p
 
 
+def _timed_rounds(arms, restore, rounds, stream):
+    """Run every arm (name, step function, steps per round) from the same
+    restored state, interleaved over rounds; per arm the median over rounds
+    of the mean ms per step.  Each arm's first call (plan build, autotune,
+    graph capture) happens before its timed rounds."""
+    import statistics
+
+    import torch
+
+    for _, fn, _ in arms:
+        restore()
+        fn()
+    ms = {name: [] for name, _, _ in arms}
+    for _ in range(rounds):
+        for name, fn, k in arms:
+            restore()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(k):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms[name].append(e0.elapsed_time(e1) / k)
+    return {name: statistics.median(v) for name, v in ms.items()}, ms
+
+
 def bench_batched(ctx, args, dev, learned_ready=False):
     """1024 periodic blocks with edges from {16, 32, 64} (p = 0.5, 0.35,
     0.15), per-zone random primitives; one RK2 step = two batched stages
     (each a captured CUDA graph of persistent work-list launches).  Compared
-    with the same steps issued block by block through phx_stage."""
+    with the same steps issued block by block through phx_stage.  Every arm
+    starts from the same snapshot of the initialised state; the batched arms
+    are interleaved over rounds and reported as the median round."""
     import torch
 
     from phoebus_gb300 import states
@@ -307,6 +347,13 @@ def bench_batched(ctx, args, dev, learned_ready=False):
     ctx.check()
     zones = sum(b.nx[0] * b.nx[1] * b.nx[2] for b in blocks)
     dt = 0.2 * min(ctx.EstimateTimestepBlock(p, b, False).item() for b in blocks)
+    snap = [(b["prim"].clone(), b["cons"].clone()) for b in blocks]
+
+    def restore():
+        for b, (pr, co) in zip(blocks, snap):
+            b["prim"].copy_(pr)
+            b["cons"].copy_(co)
+
     seconds = [torch.zeros_like(b["cons"]) for b in blocks]
     bases = [b["cons"] for b in blocks]
     stage2 = []
@@ -334,40 +381,46 @@ def bench_batched(ctx, args, dev, learned_ready=False):
     t_plan = time.perf_counter() - t0
     info = ctx.batch_info()
     stream = torch.cuda.current_stream()
-    res = {}
-    ctx.c2p_stats(reset=True)
-    runs = [("batched", step_batched, args.steps), ("per_block", step_blocks, 2)]
+    k = args.section_steps
+    arms = [("batched", step_batched, k)]
     if learned_ready:
-        step_batched_learned()  # builds the learned plans
-        runs.append(("batched_learned", step_batched_learned, args.steps))
-    for name, fn, k in runs:
+        arms.append(("batched_learned", step_batched_learned, k))
+    med, per_round = _timed_rounds(arms, restore, args.section_rounds, stream)
+    res = {}
+    for name, _, _ in arms:
+        res[name] = {"zone_updates_per_s": zones / (med[name] * 1e-3), "ms_per_step": med[name], "steps": k,
+                     "rounds_ms": per_round[name]}
+    # statistics of one step of each arm from the snapshot
+    for name, fn, _ in arms:
+        restore()
+        ctx.c2p_stats(reset=True)
         fn()
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(k):
-            fn()
-        e1.record(stream)
-        torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / k
-        res[name] = {"zone_updates_per_s": zones / (ms * 1e-3), "ms_per_step": ms, "steps": k}
         st = ctx.c2p_stats(reset=True)
         if st["zones"]:
             res[name]["c2p_iterations_per_zone"] = st["iterations"] / st["zones"]
             res[name]["c2p_learned_accepted_frac"] = st["learned_accepted"] / st["zones"]
+    pb, _ = _timed_rounds([("per_block", step_blocks, 1)], restore, 1, stream)
+    res["per_block"] = {"zone_updates_per_s": zones / (pb["per_block"] * 1e-3), "ms_per_step": pb["per_block"],
+                        "steps": 1}
     ctx.check()
     nan = sum(int(torch.isnan(b["prim"][0]).sum()) for b in blocks)
-    del blocks, seconds, bases, stage2
+    del blocks, seconds, bases, stage2, snap
     torch.cuda.empty_cache()
     from collections import Counter
 
     sizes = Counter(states.uneven_block_sizes(args.batched_blocks))
-    return {"workload": f"{args.batched_blocks} periodic blocks, edges {dict(sorted(sizes.items()))}, Minkowski, "
-                        "MP5 + HLL, MHD, Gamma 4/3, per-zone random state, floors + c2p fixup on",
-            "interior_zones": zones, **res, "batched_over_per_block":
-                res["batched"]["zone_updates_per_s"] / res["per_block"]["zone_updates_per_s"],
-            "plan_seconds": t_plan, "tuning": info, "nan_rho_zones": nan,
-            "graph": "one CUDA graph per stage kind; nodes per graph as in tuning.graph_nodes"}
+    out = {"workload": f"{args.batched_blocks} periodic blocks, edges {dict(sorted(sizes.items()))}, Minkowski, "
+                       "MP5 + HLL, MHD, Gamma 4/3, per-zone random state, floors + c2p fixup on",
+           "interior_zones": zones, **res, "batched_over_per_block":
+               res["batched"]["zone_updates_per_s"] / res["per_block"]["zone_updates_per_s"],
+           "plan_seconds": t_plan, "tuning": info, "nan_rho_zones": nan,
+           "inputs": "every arm from the same snapshot of the initialised state; batched arms interleaved over "
+                     f"{args.section_rounds} rounds of {k} steps, median round",
+           "graph": "one CUDA graph per stage kind; nodes per graph as in tuning.graph_nodes"}
+    if "batched_learned" in res:
+        out["learned_over_batched"] = (res["batched_learned"]["zone_updates_per_s"] /
+                                       res["batched"]["zone_updates_per_s"])
+    return out
 
 
 def bench_torus(ctx, args, dev, learned_ready=False):
@@ -410,28 +463,36 @@ def bench_torus(ctx, args, dev, learned_ready=False):
         rk.step(dt, learned=lrn, batched=batched)
 
     zones = mesh.n[0] * mesh.n[1] * mesh.n[2]
-    runs = [("plain_per_block", False, False), ("batched", True, False)]
+    snap = [(b["prim"].clone(), b["cons"].clone()) for b in blocks]
+
+    def restore():
+        for b, (pr, co) in zip(blocks, snap):
+            b["prim"].copy_(pr)
+            b["cons"].copy_(co)
+
+    k = args.torus_steps
+    arms = [("batched", lambda: step(True, False), k)]
     if learned_ready:
-        runs.append(("learned_batched", True, True))
+        arms.append(("learned_batched", lambda: step(True, True), k))
     stream = torch.cuda.current_stream()
+    med, per_round = _timed_rounds(arms, restore, args.section_rounds, stream)
+    plain, _ = _timed_rounds([("plain_per_block", lambda: step(False, False), k)], restore, 1, stream)
+    med.update(plain)
+    per_round.update({"plain_per_block": [plain["plain_per_block"]]})
     res = {}
-    for name, batched, lrn in runs:
-        step(batched, lrn)  # plan build (work lists, autotune, capture) + warm-up
-        torch.cuda.synchronize()
+    for name in ["plain_per_block"] + [a[0] for a in arms]:
+        res[name] = {"zone_updates_per_s": zones / (med[name] * 1e-3), "ms_per_step": med[name], "steps": k,
+                     "rounds_ms": per_round[name]}
+    fns = {"plain_per_block": (False, False), "batched": (True, False), "learned_batched": (True, True)}
+    for name in res:
+        restore()
         ctx.c2p_stats(reset=True)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(args.torus_steps):
-            step(batched, lrn)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / args.torus_steps
+        step(*fns[name])
         st = ctx.c2p_stats(reset=True)
-        res[name] = {"zone_updates_per_s": zones / (ms * 1e-3), "ms_per_step": ms, "steps": args.torus_steps,
-                     "c2p_iterations_per_zone": st["iterations"] / max(st["zones"], 1),
-                     "c2p_residual_evals_per_zone": st["residual_evals"] / max(st["zones"], 1),
-                     "c2p_failures": st["failures"]}
-        if lrn:
+        res[name].update({"c2p_iterations_per_zone": st["iterations"] / max(st["zones"], 1),
+                          "c2p_residual_evals_per_zone": st["residual_evals"] / max(st["zones"], 1),
+                          "c2p_failures": st["failures"]})
+        if fns[name][1]:
             res[name]["c2p_learned_accepted_frac"] = st["learned_accepted"] / max(st["zones"], 1)
     ctx.check()
     nan = sum(int(torch.isnan(b["prim"][0][b.isl()]).sum()) for b in blocks)
@@ -439,13 +500,17 @@ def bench_torus(ctx, args, dev, learned_ready=False):
                        f"{mesh.nblocks} uneven blocks, edges {mesh.lens}, WENO5-Z + HLL, Gamma 13/9, floors, "
                        "gr_outflow X1/X2 (bc_vars primitive, outer-X1 inflow check, FixFluxes), periodic X3",
            "interior_zones": zones, **res,
+           "inputs": "every arm from the same snapshot of the initialised state; batched arms interleaved over "
+                     f"{args.section_rounds} rounds of {k} steps, median round",
            "nan_interior_rho": nan, "field_factor": info["field_factor"], "training_seconds": train_s,
            "setup_seconds": setup_s[1], "setup_seconds_first_call": setup_s[0]}
     if "learned_batched" in res:
         out["learned_batched_over_plain"] = (res["learned_batched"]["zone_updates_per_s"] /
                                              res["plain_per_block"]["zone_updates_per_s"])
+        out["learned_over_batched"] = (res["learned_batched"]["zone_updates_per_s"] /
+                                       res["batched"]["zone_updates_per_s"])
     out["batched_over_plain"] = res["batched"]["zone_updates_per_s"] / res["plain_per_block"]["zone_updates_per_s"]
-    del blocks, rk
+    del blocks, rk, snap
     torch.cuda.empty_cache()
     return out
 
@@ -538,7 +603,7 @@ def bench_m1(ctx, args, dev):
         from oracle.oracle import RadOracle
 
         os.environ["OMP_NUM_THREADS"] = str(os.cpu_count() or 1)
-        o = RadOracle()
+        o = RadOracle(tuned=True)
         hb, par, rpar = radiation.radiation_pulse_3d(n=args.m1_cpu_n)
         p, rp = abi.default_params(**par), abi.default_rad_params(**rpar)
         o.MomentPrim2Con(rp, p, hb)
@@ -555,70 +620,145 @@ def bench_m1(ctx, args, dev):
             times.append(time.perf_counter() - t0)
         t = min(times)
         res["cpu_baseline"] = {"value": args.m1_cpu_n ** 3 / t, "unit": UNIT, "cores": os.cpu_count() or 1,
-                               "kind": "port", "sample": f"oracle RK2 step on a {args.m1_cpu_n}^3 sample of the "
+                               "kind": "port", "sample": f"oracle timing build, RK2 step on a {args.m1_cpu_n}^3 sample of the "
                                                          f"same state ({t:.2f} s/step)"}
         res["gpu_over_cpu"] = res["zone_updates_per_s"] / res["cpu_baseline"]["value"]
     return res
 
 
-def cpu_baseline(args, threads):
-    """Oracle RK2 timestep on a cpu_n^3 sample of the workload."""
+def cpu_model():
+    """The host CPU's model name and logical core count."""
+    name = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.split(":")[0].strip() in ("Model name", "Vendor ID") and ":" in line:
+                name = line.split(":", 1)[1].strip()
+                if line.startswith("Model name"):
+                    break
+    except Exception:
+        pass
+    import platform
+
+    return {"model": name or platform.processor() or "unknown", "arch": platform.machine(),
+            "logical_cores": os.cpu_count() or 1}
+
+
+def workload_config(args, ws):
+    """The config object both arms print (same workload, same keys)."""
+    n = args.n
+    return {"workload": f"shear layer {n}^3 single block, Minkowski, Gamma 5/3, WENO5-Z + HLL, MHD, periodic; one "
+                        "RK2 timestep (2 stages + timestep estimate) per step",
+            "n": n, "ng": 4, "rk_stages_per_step": 2,
+            "l2": "inputs larger than L2 (state ~%.1f GB)" % ((n + 8) ** 3 * 60 * 8 / 1e9),
+            "parallelism": f"replicas x{ws}"}
+
+
+def cpu_step_timer(n, threads, steps, warmup):
+    """The oracle's timing build (-O3, contraction on) advancing an n^3 block
+    of the shear layer by RK2 steps with the face-speed timestep estimate, on
+    threads host threads; returns (seconds per step over `steps` timed steps,
+    the per-step times)."""
     import numpy as np
 
     from oracle.oracle import Oracle
     from phoebus_gb300 import abi, states
 
     os.environ["OMP_NUM_THREADS"] = str(threads)
-    o = Oracle()
-    hb, par = states.kelvin_helmholtz(n=args.cpu_n)
+    o = Oracle(tuned=True)
+    hb, par = states.kelvin_helmholtz(n=n)
     p = abi.default_params(**par)
     o.Initialize(p, hb)
     dt = 0.5 * o.EstimateTimestepBlock(p, hb, False)
     cs = np.zeros_like(hb["cons"])
-    o.rk2_step(p, hb, cs, dt)  # warm-up
+    for _ in range(warmup):
+        o.rk2_step(p, hb, cs, dt)
+        o.EstimateTimestepBlock(p, hb, True)
     times = []
-    for _ in range(max(1, min(args.steps, 3))):
+    for _ in range(steps):
         t0 = time.perf_counter()
         o.rk2_step(p, hb, cs, dt)
         o.EstimateTimestepBlock(p, hb, True)
         times.append(time.perf_counter() - t0)
-    t = min(times)
-    return args.cpu_n ** 3 / t, t
+    return sum(times) / len(times), times
 
 
 def run_reference(args, ws, rank):
+    """The reference's CPU path (the oracle port, timing build) on all host
+    cores, on the same workload: the n^3 block itself (--ref-n 0), one RK2
+    step + timestep estimate per bench step."""
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    import numpy as np
-
-    from oracle.oracle import Oracle
-    from phoebus_gb300 import abi, states
-
-    os.environ["OMP_NUM_THREADS"] = str(threads)
-    o = Oracle()
-    hb, par = states.kelvin_helmholtz(n=args.cpu_n)
-    p = abi.default_params(**par)
-    o.Initialize(p, hb)
-    dt = 0.5 * o.EstimateTimestepBlock(p, hb, False)
-    cs = np.zeros_like(hb["cons"])
-    for _ in range(args.warmup):
-        o.rk2_step(p, hb, cs, dt)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        o.rk2_step(p, hb, cs, dt)
-        o.EstimateTimestepBlock(p, hb, True)
-    el = time.perf_counter() - t0
-    v = args.cpu_n ** 3 * args.steps / el
-    sample = f"{args.cpu_n}^3 sample of the {args.n}^3 shear layer, one RK2 step per bench step"
+    n = args.ref_n or args.n
+    t_step, _ = cpu_step_timer(n, threads, args.steps, args.warmup)
+    v = n ** 3 / t_step
+    cfg = workload_config(args, ws)
+    sample = (f"the {n}^3 block itself" if n == args.n else f"{n}^3 sample of the {args.n}^3 shear layer") + \
+             ", one RK2 step per bench step"
+    if n != args.n:
+        cfg["workload"] += f" (reference CPU path on a {n}^3 sample)"
+        cfg["sample_n"] = n
     out = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_step,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": f"shear layer {args.n}^3 WENO5-Z+HLL MHD RK2 (reference CPU path on a "
-                                  f"{args.cpu_n}^3 sample)", "n": args.n, "sample_n": args.cpu_n},
-           "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+           "config": cfg,
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                            "build": "oracle timing build: g++ -O3 -ffp-contract=fast -fno-math-errno "
+                                     "-funroll-loops -fopenmp", "cpu": cpu_model()},
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
+
+
+def _sig(x, d=4):
+    """x rounded to d significant digits (compact summary numbers)."""
+    if x is None or not isinstance(x, (int, float)):
+        return x
+    if x == 0 or x != x:
+        return x
+    import math
+
+    return round(x, -int(math.floor(math.log10(abs(x)))) + d - 1)
+
+
+def section_summary(fp64, c2p, batched, torus_res, m1):
+    """The sections' headline numbers, short enough for the last line."""
+    g = lambda d, *k: _sig(_dig(d, *k))  # noqa: E731
+    out = {}
+    if fp64:
+        out["flux_fp64"] = {"tflops": g(fp64, "achieved_tflops"), "frac_of_probe": g(fp64, "frac"),
+                            "issue_frac": g(fp64, "issue_frac")}
+    if c2p:
+        out["c2p_zones_per_s"] = {"plain": g(c2p, "plain", "zones_per_s"), "learned": g(c2p, "learned", "zones_per_s"),
+                                  "ratio": g(c2p, "learned_over_plain"),
+                                  "iters": [g(c2p, "plain", "iterations_per_zone"),
+                                            g(c2p, "learned", "iterations_per_zone")],
+                                  "accepted": g(c2p, "learned", "learned_accepted_frac"),
+                                  "train_pairs": g(c2p, "training", "pairs")}
+    if batched:
+        out["batched_zone_updates_per_s"] = {
+            "per_block": g(batched, "per_block", "zone_updates_per_s"),
+            "batched": g(batched, "batched", "zone_updates_per_s"),
+            "learned_batched": g(batched, "batched_learned", "zone_updates_per_s"),
+            "learned_over_batched": g(batched, "learned_over_batched")}
+    if torus_res:
+        out["torus_zone_updates_per_s"] = {
+            "plain": g(torus_res, "plain_per_block", "zone_updates_per_s"),
+            "batched": g(torus_res, "batched", "zone_updates_per_s"),
+            "learned_batched": g(torus_res, "learned_batched", "zone_updates_per_s"),
+            "learned_over_batched": g(torus_res, "learned_over_batched")}
+    if m1:
+        out["m1_zone_updates_per_s"] = {"gpu": g(m1, "zone_updates_per_s"), "cpu": g(m1, "cpu_baseline", "value"),
+                                        "flux_fp64_frac": g(m1, "fp64", "frac")}
+    return out
+
+
+def _dig(d, *keys):
+    for k in keys:
+        if not isinstance(d, dict) or k not in d:
+            return None
+        d = d[k]
+    return d
 
 
 def main():
@@ -783,8 +923,7 @@ def main():
         ems = max_over_ranks(ws, g0.elapsed_time(g1) / args.steps, dev)
         nb = (h_prim.numel() + h_cons.numel()) * 8
         e2e = {"value": ws * zones / (ems * 1e-3), "unit": UNIT, "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb,
-               "ms_per_step": ems, "pipelining": "double-buffered device state; H2D of step k+1 and D2H of step "
-                                                 "k-1 on two copy streams overlap step k"}
+               "ms_per_step": ems, "pipelining": "double-buffered; H2D of step k+1 and D2H of k-1 overlap step k"}
         del db2, second2
     ctx.check()
     c2p = None if args.no_c2p else bench_c2p(ctx, args, dev)
@@ -795,29 +934,25 @@ def main():
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        v, t = cpu_baseline(args, threads)
-        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"oracle RK2 step on a {args.cpu_n}^3 sample of the same state ({t:.2f} s/step)"}
+        t, _ = cpu_step_timer(args.cpu_n, threads, 3, 1)
+        cpu = {"value": args.cpu_n ** 3 / t, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"oracle timing build, RK2 step on a {args.cpu_n}^3 sample of the same state "
+                         f"({t:.2f} s/step, 3 steps after 1 warm-up)", "cpu": cpu_model()}
 
     if rank == 0:
+        detail = {"fp64": fp64, "c2p": c2p, "batched": batched, "torus": torus_res, "m1": m1_res}
+        print(json.dumps({"detail": detail}), flush=True)  # full sections, one line before the result
+        cfg = workload_config(args, ws)
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic",
-            "config": {"workload": f"shear layer {n}^3 single block, Minkowski, Gamma 5/3, WENO5-Z + HLL, MHD, "
-                                   "periodic; one RK2 timestep (2 stages + timestep estimate) per step",
-                       "n": n, "ng": 4, "rk_stages_per_step": 2, "zone_stages_per_s": 2 * value,
-                       "l2": "inputs larger than L2 (state ~%.1f GB)" % (db.N * 60 * 8 / 1e9),
-                       "parallelism": f"replicas x{ws}", "build": "exact" if args.exact else "production"},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": achieved / hbm_peak, "traffic": traffic, "kernel": "CalculateFluxes (x1/x2/x3)",
-                         "peak_source": peak_src, "algorithmic_bytes": fb, "launch_ms": flux_ms,
-                         "note": "FP64-pipe bound on GB300; see fp64"},
-            "fp64": fp64,
-            "c2p": c2p,
-            "batched": batched,
-            "torus": torus_res,
-            "m1": m1_res,
+            "data": "synthetic", "config": cfg, "build": "exact" if args.exact else "production",
+            "zone_stages_per_s": 2 * value,
+            "roofline": {"bound": "hbm", "achieved": _sig(achieved, 6), "peak": hbm_peak, "unit": "GB/s",
+                         "frac": _sig(achieved / hbm_peak, 6), "traffic": traffic, "kernel": "CalculateFluxes x1-x3",
+                         "peak_source": peak_src, "algorithmic_bytes": fb, "launch_ms": _sig(flux_ms, 6),
+                         "note": "FP64-bound; see sections.flux_fp64"},
+            "sections": section_summary(fp64, c2p, batched, torus_res, m1_res),
             "cpu_baseline": cpu,
             "clocks": clocks,
             "e2e": e2e,

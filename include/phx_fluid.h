@@ -311,10 +311,15 @@ phx_status phx_estimate_timestep(phx_ctx *ctx, const phx_params *p, const phx_bl
  * Its scratch is a file-scope __device__ array of PHX_DT_STATIC_MAX_PARTIALS
  * doubles (512 KiB) that every device loading the library keeps until exit,
  * so blocks with more than PHX_DT_STATIC_MAX_ZONES interior zones are
- * rejected with PHX_ERR_CAPACITY.  The first call on each device looks up the
- * array's device address (cudaGetSymbolAddress); make that first call before
- * any stream capture.  All calls share the array: calls that overlap on the
- * GPU (different streams, concurrent host threads) race on it. */
+ * rejected with PHX_ERR_CAPACITY.  The block checks are those of
+ * phx_estimate_timestep that do not involve prim/cons (ng >= 3, var_stride 0
+ * or at least the block's size); errors are described by phx_last_error().
+ * The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * The address is kept with the id of the CUDA context it was found in and
+ * looked up again when another context is current (after cudaDeviceReset).
+ * All calls share the array: calls that overlap on the GPU (different
+ * streams, concurrent host threads) race on it. */
 #define PHX_DT_STATIC_MAX_PARTIALS 65536
 #define PHX_DT_STATIC_MAX_ZONES (65536LL * 256LL)
 phx_status phx_estimate_timestep_static(const phx_params *p, const phx_block *b,
@@ -471,9 +476,18 @@ phx_status phx_batch_info(phx_ctx *ctx, int *x1_cells, int *sweep_seg, int *grap
  * the tensor cores with FP32 accumulation. */
 
 /* Load FP32 master parameters (host memory, PHX_MLP_NPARAM floats); resets
- * the optimiser state. */
+ * the optimiser state and the input box (unbounded). */
 phx_status phx_mlp_set_weights(phx_ctx *ctx, const float *params_host);
 phx_status phx_mlp_get_weights(phx_ctx *ctx, float *params_host);
+
+/* Input box of the learned start (6 floats each, host): a cold zone whose
+ * features (phx_mlp_features_zones) fall outside [lo, hi] gets no learned
+ * bracket and keeps the reference's start, so the network is not consulted
+ * outside the states it was trained on.  phx_mlp_train sets the box to the
+ * training features' range widened by 2% of it on each side; NULL lo or hi
+ * leaves that side unbounded. */
+phx_status phx_mlp_set_input_box(phx_ctx *ctx, const float *lo_host, const float *hi_host);
+phx_status phx_mlp_get_input_box(phx_ctx *ctx, float *lo_host, float *hi_host);
 
 /* The 6 FP32 network inputs of independent zones, x[6][n] (device), from the
  * con2prim setup invariants of cons/geom/coords as in
@@ -514,10 +528,21 @@ void phx_mlp_train_opts_default(phx_mlp_train_opts *o);
 
 /* Train the loaded parameters on n samples (x[6][n], y[n], device) with
  * AdamW, floor(n / batch) steps per epoch, on the GPU; then pack the
- * parameters for inference.  epoch_loss (host, may be NULL) receives the mean
+ * parameters for inference and set the input box from x (phx_mlp_set_input_box).
+ * epoch_loss (host, may be NULL) receives the mean
  * training loss of each epoch.  Synchronises the stream. */
 phx_status phx_mlp_train(phx_ctx *ctx, long long n, const float *x, const float *y, const phx_mlp_train_opts *o,
                          float *epoch_loss, void *stream);
+
+/* ---- the library's transcendental functions ----------------------------- */
+/* The FMKS geometry tables and the exponential floors evaluate exp, sin, cos
+ * and pow written out from their series with IEEE operations only (no
+ * counterpart in the reference, which calls the C library's): the oracle
+ * evaluates the same operations, so tables and floors compare bit for bit.
+ * out[q] = f(x[q]) (pow: x[q]^y[q]) for device arrays of n doubles, for
+ * validating them against other implementations. */
+enum { PHX_MATH_EXP = 0, PHX_MATH_LOG = 1, PHX_MATH_SIN = 2, PHX_MATH_COS = 3, PHX_MATH_POW = 4 };
+phx_status phx_math_eval(int fn, long long n, const double *x, const double *y, double *out, void *stream);
 
 /* ---- measurement probe -------------------------------------------------- */
 /* Time a dependent-chain-free FP64 FMA loop and report FLOP/s (2 per FMA).

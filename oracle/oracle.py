@@ -10,7 +10,6 @@ from __future__ import annotations
 
 import ctypes as C
 import os
-import subprocess
 from pathlib import Path
 
 import numpy as np
@@ -27,23 +26,26 @@ LIB = ROOT / "oracle" / "_build" / "libphx_oracle.so"
 SRC = ROOT / "oracle" / "phx_oracle.cpp"
 
 
+LIB_TUNED = ROOT / "oracle" / "_build" / "libphx_oracle_tuned.so"
+
+
 def build(force: bool = False) -> Path:
-    LIB.parent.mkdir(exist_ok=True)
-    hdrs = [ROOT / "include" / "phx_fluid.h", ROOT / "include" / "phx_radiation.h"]
-    if force or not LIB.exists() or LIB.stat().st_mtime < max([SRC.stat().st_mtime] + [h.stat().st_mtime for h in hdrs]):
-        subprocess.run(["g++", "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-o",
-                        str(LIB), str(SRC)], check=True)
-    return LIB
+    """Both oracle builds (phoebus_gb300/build.py: the parity build with
+    contraction off, and the -O3 timing build)."""
+    from phoebus_gb300.build import build_oracle
+
+    return build_oracle(force)
 
 
-_lib = None
+_libs = {}
 
 
-def lib() -> C.CDLL:
-    global _lib
-    if _lib is None:
+def lib(tuned: bool = False) -> C.CDLL:
+    """The parity build, or with tuned the timing build (CPU baseline only:
+    its contracted arithmetic rounds differently)."""
+    if tuned not in _libs:
         build()
-        L = C.CDLL(str(LIB))
+        L = C.CDLL(str(LIB_TUNED if tuned else LIB))
         P, B, R = C.POINTER(abi.Params), C.POINTER(abi.BlockS), abi.Range
         L.orc_prim_to_con.argtypes = [P, B, R, R, R]
         L.orc_prim_to_con.restype = None
@@ -90,12 +92,13 @@ def lib() -> C.CDLL:
             ("orc_rad_fill_ghosts_periodic", [BS, RB], None),
             ("orc_rad_estimate_timestep", [RP, PP, BS, RB], C.c_double),
             ("orc_rad_tanh", [C.c_double], C.c_double),
+            ("orc_math_eval", [C.c_int, C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p], None),
             ("orc_rad_m1_guess", [C.c_void_p] * 3 + [C.c_longlong] + [C.c_void_p] * 2, None),
         ]:
             fn = getattr(L, name)
             fn.argtypes, fn.restype = args, res
-        _lib = L
-    return _lib
+        _libs[tuned] = L
+    return _libs[tuned]
 
 
 def _r(r):
@@ -108,10 +111,11 @@ def set_threads(n: int | None):
 
 
 class Oracle:
-    """The reference tasks on host Blocks (numpy arrays)."""
+    """The reference tasks on host Blocks (numpy arrays).  tuned selects the
+    -O3 timing build (for the CPU baseline; the tests use the parity build)."""
 
-    def __init__(self):
-        self.L = lib()
+    def __init__(self, tuned: bool = False):
+        self.L = lib(tuned)
 
     def PrimitiveToConserved(self, p, b: Block, ib=None, jb=None, kb=None):
         e = b.entire()
@@ -220,6 +224,15 @@ class Oracle:
         self.L.orc_c2p_features_zones(C.byref(p), n, self._p(cons), self._p(geom), self._p(coords), x.ctypes.data)
         return x
 
+    def math_eval(self, fn: str, x, y=None):
+        """phx_math.h's exp / log / sin / cos / pow over a float64 array."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        yy = None if y is None else np.ascontiguousarray(y, dtype=np.float64)
+        out = np.empty_like(x)
+        self.L.orc_math_eval(abi.MATH[fn], x.size, x.ctypes.data, None if yy is None else yy.ctypes.data,
+                             out.ctypes.data)
+        return out
+
     def fmks_points(self, g, x1, x2):
         n = x1.shape[0]
         out = np.zeros((abi.GEOM_NLOC, n))
@@ -275,8 +288,8 @@ class RadOracle:
     "prim" ... and "rcons", "rprim", "rflux", "rdudt"), in the order of
     phoebus_gb300.radiation.RadiationContext."""
 
-    def __init__(self):
-        self.L = lib()
+    def __init__(self, tuned: bool = False):
+        self.L = lib(tuned)
 
     @staticmethod
     def _s(b: Block, cons=None):

@@ -23,6 +23,14 @@
 // Build: g++ -O2 -std=c++17 -fopenmp -ffp-contract=off -fPIC -shared.
 // -ffp-contract=off keeps every multiply and add separately rounded, so the
 // CUDA exact build (nvcc -fmad=false) can be compared bit for bit.
+//
+// Transcendentals: the reference calls std::exp, std::sin, std::cos and
+// std::pow in the FMKS geometry and the floors.  Those calls go to the
+// library's written-out exp, sin, cos and pow (phoebus_gb300/csrc/phx_math.h,
+// series restated from the mathematics and measured within 2 ulp of the C
+// library's), which the CUDA kernels also evaluate: a libm choice, like
+// glibc's, that makes the geometry tables and the exponential floors
+// comparable bit for bit.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -34,6 +42,7 @@
 
 #include "../include/phx_fluid.h"
 #include "../include/phx_radiation.h"
+#include "../phoebus_gb300/csrc/phx_math.h"
 
 namespace orc {
 
@@ -115,22 +124,22 @@ struct Bounds {
       sflr = s0;
       break;
     case PHX_FLOOR_EXPX1_RHO_SIE:
-      rflr = r0 * std::exp(ralpha * x1);
-      sflr = s0 * std::exp(salpha * x1);
+      rflr = r0 * phx_math::exp(ralpha * x1);
+      sflr = s0 * phx_math::exp(salpha * x1);
       break;
     case PHX_FLOOR_EXPX1_RHO_U: {
-      Real scratch = r0 * std::exp(ralpha * x1);
-      sflr = s0 * std::exp(salpha * x1) / std::max(rflr, scratch);
+      Real scratch = r0 * phx_math::exp(ralpha * x1);
+      sflr = s0 * phx_math::exp(salpha * x1) / std::max(rflr, scratch);
       rflr = scratch;
     } break;
     case PHX_FLOOR_X1_RHO_SIE:
-      rflr = r0 * std::min(1.0, std::pow(x1, ralpha));
-      sflr = s0 * std::min(1.0, std::pow(x1, salpha));
+      rflr = r0 * std::min(1.0, phx_math::pow(x1, ralpha));
+      sflr = s0 * std::min(1.0, phx_math::pow(x1, salpha));
       break;
     default: {  // PHX_FLOOR_R_RHO_SIE
       Real r = std::sqrt(x1 * x1 + x2 * x2 + x3 * x3);
-      rflr = r0 * std::min(1.0, std::pow(r, ralpha));
-      sflr = s0 * std::min(1.0, std::pow(r, salpha));
+      rflr = r0 * std::min(1.0, phx_math::pow(r, ralpha));
+      sflr = s0 * std::min(1.0, phx_math::pow(r, salpha));
     } break;
     }
     rflr = std::max(rflr, rho_min_eos);
@@ -207,17 +216,17 @@ struct FMKS {
         xt(g.poly_xt), alpha(g.poly_alpha), x0(g.x0), smooth(g.smooth),
         hexp_br(g.hexp_br), hexp_nsq(g.hexp_nsq), hexp_csq(g.hexp_csq), dxfd(1e-8) {
     // mckinney_gammie_ryan.hpp:188-190 GetNorm_
-    norm = 0.5 * M_PI * 1. / (1. + 1. / (alpha + 1.) * 1. / std::pow(xt, alpha));
+    norm = 0.5 * M_PI * 1. / (1. + 1. / (alpha + 1.) * 1. / phx_math::pow(xt, alpha));
   }
   // ---- McKinneyGammieRyan (mckinney_gammie_ryan.hpp:64-198)
   Real r_(Real X1) const {
     const Real hexp_dr = X1 - hexp_br;
-    return std::exp(X1 + (hexp_dr > 0.) * hexp_csq * std::pow(hexp_dr, hexp_nsq));
+    return phx_math::exp(X1 + (hexp_dr > 0.) * hexp_csq * phx_math::pow(hexp_dr, hexp_nsq));
   }
-  Real thG_(Real X2) const { return M_PI * X2 + ((1. - h) / 2.) * std::sin(2. * M_PI * X2); }
+  Real thG_(Real X2) const { return M_PI * X2 + ((1. - h) / 2.) * phx_math::sin(2. * M_PI * X2); }
   void thJ_(Real X2, Real &y, Real &thJ) const {
     y = 2. * X2 - 1.;
-    thJ = norm * y * (1. + std::pow(y / xt, alpha) / (alpha + 1.)) + 0.5 * M_PI;
+    thJ = norm * y * (1. + phx_math::pow(y / xt, alpha) / (alpha + 1.)) + 0.5 * M_PI;
   }
   void th_(Real X1, Real X2, Real &y, Real &th) const {
     Real thG = thG_(X2);
@@ -225,7 +234,7 @@ struct FMKS {
       Real thJ;
       thJ_(X2, y, thJ);
       const Real fac = x0 - X1;
-      th = thG + std::exp(smooth * fac) * (thJ - thG);
+      th = thG + phx_math::exp(smooth * fac) * (thJ - thG);
     } else {
       y = 0;
       th = thG;
@@ -254,19 +263,19 @@ struct FMKS {
     C[2] = X3;
     const Real hexp_dr = X1 - hexp_br;
     const Real drdX1 =
-        std::exp(X1 + (hexp_dr > 0.) * hexp_csq * std::pow(hexp_dr, hexp_nsq)) *
-        (1. + (hexp_dr > 0.) * hexp_csq * hexp_nsq * std::pow(hexp_dr, hexp_nsq - 1.));
-    const Real dthGdX2 = M_PI + M_PI * (1 - h) * std::cos(2 * M_PI * X2);
+        phx_math::exp(X1 + (hexp_dr > 0.) * hexp_csq * phx_math::pow(hexp_dr, hexp_nsq)) *
+        (1. + (hexp_dr > 0.) * hexp_csq * hexp_nsq * phx_math::pow(hexp_dr, hexp_nsq - 1.));
+    const Real dthGdX2 = M_PI + M_PI * (1 - h) * phx_math::cos(2 * M_PI * X2);
     Real dthdX1, dthdX2;
     if (derefine_poles) {
       thJ_(X2, y, thJ);
       const Real thG = thG_(X2);
       const Real dydX2 = 2.;
-      const Real dthJdy = norm * (1 + std::pow(y / xt, alpha));
+      const Real dthJdy = norm * (1 + phx_math::pow(y / xt, alpha));
       const Real dthJdX2 = dthJdy * dydX2;
       const Real fac = x0 - X1;
-      dthdX1 = -smooth * (thJ - thG) * std::exp(smooth * fac);
-      dthdX2 = dthGdX2 + std::exp(smooth * fac) * (dthJdX2 - dthGdX2);
+      dthdX1 = -smooth * (thJ - thG) * phx_math::exp(smooth * fac);
+      dthdX2 = dthGdX2 + phx_math::exp(smooth * fac) * (dthJdX2 - dthGdX2);
     } else {
       dthdX1 = 0.0;
       dthdX2 = dthGdX2;
@@ -288,20 +297,20 @@ struct FMKS {
              Real &rho2) const {
     r = std::abs(X1);
     th = X2;
-    cth = std::cos(th);
-    sth = std::sin(th);
+    cth = phx_math::cos(th);
+    sth = phx_math::sin(th);
     sth2 = sth * sth;
     rho2 = rho2_(r, cth);
   }
   Real ks_lapse(Real X1, Real X2) const {
     const Real r = std::abs(X1);
-    const Real cth = std::cos(X2);
+    const Real cth = phx_math::cos(X2);
     const Real rho2 = rho2_(r, cth);
     return std::sqrt(ratio(rho2, 2 * r + rho2));
   }
   void ks_shift(Real X1, Real X2, Real beta[3]) const {
     Real r = std::abs(X1);
-    Real cth = std::cos(X2);
+    Real cth = phx_math::cos(X2);
     const Real rho2 = rho2_(r, cth);
     beta[0] = ratio(2 * r, 2 * r + rho2);
     beta[1] = 0;
@@ -390,7 +399,7 @@ struct FMKS {
   }
   // geometry_utils.hpp:149-178 SetMetricGradientByFD (dx argument unused)
   void MetricDerivative(Real X1, Real X2, Real X3, Real dg[4][4][4]) const {
-    Real EPSFD = std::pow(std::numeric_limits<Real>::epsilon(), 1.0 / 3.0);
+    Real EPSFD = phx_math::pow(2.220446049250313e-16, 1.0 / 3.0);
     for (int a = 0; a < 4; a++)
       for (int b = 0; b < 4; b++)
         for (int c = 0; c < 4; c++) dg[a][b][c] = 0;
@@ -422,7 +431,7 @@ struct FMKS {
   }
   // geometry_utils.hpp:89-119 SetGradLnAlphaByFD
   void GradLnAlpha(Real X1, Real X2, Real X3, Real da[4]) const {
-    Real EPSFD = std::pow(std::numeric_limits<Real>::epsilon(), 1.0 / 3.0);
+    Real EPSFD = phx_math::pow(2.220446049250313e-16, 1.0 / 3.0);
     for (int m = 0; m < 4; m++) da[m] = 0;
     Real dx = dxfd;
     for (int d = 1; d < 4; ++d) {
@@ -2836,6 +2845,19 @@ double orc_rad_estimate_timestep(const phx_rad_params *rp, const phx_params *p, 
 }
 
 double orc_rad_tanh(double x) { return tanh_r(x); }
+
+// phx_math.h's functions over an array (fn as PHX_MATH_*), for their tests.
+void orc_math_eval(int fn, long long n, const double *x, const double *y, double *out) {
+  for (long long q = 0; q < n; q++) {
+    switch (fn) {
+    case PHX_MATH_EXP: out[q] = phx_math::exp(x[q]); break;
+    case PHX_MATH_LOG: out[q] = phx_math::log(x[q]); break;
+    case PHX_MATH_SIN: out[q] = phx_math::sin(x[q]); break;
+    case PHX_MATH_COS: out[q] = phx_math::cos(x[q]); break;
+    default: out[q] = phx_math::pow(x[q], y[q]); break;
+    }
+  }
+}
 
 // ClosureM1::GetM1GuessesFromEddington (closure_m1.hpp:146-168) for n zones:
 // the Eddington inversion's xi = |H| / J (capped at 0.99) and phi = 1.000001 pi,

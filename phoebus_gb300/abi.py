@@ -37,6 +37,9 @@ RJ, RH, RXI, RPHI, RFAIL, RKAPPAJ, RKAPPAH, RJBB, RNPRIM = 0, 1, 4, 5, 6, 7, 8, 
 RAD_METHOD = {"moment_m1": 0, "moment_eddington": 1}
 RAD_ONED_FIXUP = {"none": 0, "ignore_dJ": 1, "ignore_all": 2}
 
+MATH = {"exp": 0, "log": 1, "sin": 2, "cos": 3, "pow": 4}
+PHX_OK, PHX_ERR_INVALID_ARG, PHX_ERR_UNBRACKETED, PHX_ERR_NAN_INPUT, PHX_ERR_TIMEOUT = 0, 1, 2, 3, 4
+PHX_ERR_CUDA, PHX_ERR_NO_DEVICE, PHX_ERR_CAPACITY, PHX_ERR_UNSUPPORTED = 5, 6, 7, 8
 STATUS = {0: "ok", 1: "invalid argument", 2: "con2prim root not bracketed", 3: "NaN input",
           4: "device wait timed out", 5: "CUDA error", 6: "no CUDA device",
           7: "request exceeds a fixed capacity", 8: "unsupported"}
@@ -192,6 +195,9 @@ _SIGS = {
     "phx_batch_info": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "phx_mlp_set_weights": (C.c_int, [_P, C.POINTER(C.c_float)]),
     "phx_mlp_get_weights": (C.c_int, [_P, C.POINTER(C.c_float)]),
+    "phx_mlp_set_input_box": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "phx_mlp_get_input_box": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "phx_math_eval": (C.c_int, [C.c_int, C.c_longlong, _P, _P, _P, _P]),
     "phx_probe_fp64_peak": (C.c_int, [_P, C.POINTER(C.c_double)]),
 }
 

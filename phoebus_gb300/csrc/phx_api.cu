@@ -5,6 +5,7 @@
 // asynchronous on the caller's stream; nothing is allocated per call.
 #include <cmath>
 #include <cstdarg>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -22,7 +23,8 @@ struct phx_ctx {
   float *mlp_w;                // device FP32 master parameters of the learned start
   float *mlp_grad, *mlp_m, *mlp_v;  // device gradient and AdamW moments
   float *mlp_loss;             // device per-epoch loss sums [PHX_MLP_MAX_EPOCHS]
-  phx::MlpPacked *mlp_packed;  // device BF16 fragments for inference
+  phx::MlpPacked *mlp_packed;  // device BF16 fragments for inference (and the input box)
+  int *mlp_boxkeys;            // device scratch of the input-box reduction [12]
   phx::C2PScratch c2p;         // device con2prim chunk scratch (brackets, retry list)
   void *c2p_mem;               // its single allocation
   long long mlp_step;          // AdamW step count
@@ -43,6 +45,15 @@ phx_status fail(phx_status s, const char *fmt, ...) {
   return s;
 }
 
+}  // namespace
+
+namespace phx {
+// Records msg as phx_last_error()'s text for entry points defined in other
+// translation units (phx_noalloc.cu).
+void set_last_error(const char *msg) { g_last_error = msg ? msg : ""; }
+}  // namespace phx
+
+namespace {
 phx_status cuda_status(const char *where) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(PHX_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
@@ -306,6 +317,7 @@ phx_status phx_ctx_create(int device, phx_ctx **out) {
       cudaMalloc(&c->mlp_v, sizeof(float) * PHX_MLP_NPARAM) != cudaSuccess ||
       cudaMalloc(&c->mlp_loss, sizeof(float) * PHX_MLP_MAX_EPOCHS) != cudaSuccess ||
       cudaMalloc(&c->mlp_packed, sizeof(phx::MlpPacked)) != cudaSuccess ||
+      cudaMalloc(&c->mlp_boxkeys, sizeof(int) * 2 * PHX_MLP_IN) != cudaSuccess ||
       cudaMalloc(&c->c2p_mem, c2p_scratch_bytes()) != cudaSuccess) {
     phx_status s = cuda_status("cudaMalloc");
     phx_ctx_destroy(c);
@@ -318,6 +330,7 @@ phx_status phx_ctx_create(int device, phx_ctx **out) {
   cudaMemset(c->mlp_m, 0, sizeof(float) * PHX_MLP_NPARAM);
   cudaMemset(c->mlp_v, 0, sizeof(float) * PHX_MLP_NPARAM);
   cudaMemset(c->mlp_packed, 0, sizeof(phx::MlpPacked));
+  phx::launch_mlp_box_reset(c->mlp_packed, 0);
   c->c2p = c2p_scratch_carve(c->c2p_mem);
   c->batch = phx::batch_cache_create();
   phx_status s = cuda_status("ctx init");
@@ -341,6 +354,7 @@ phx_status phx_ctx_destroy(phx_ctx *ctx) {
   cudaFree(ctx->mlp_v);
   cudaFree(ctx->mlp_loss);
   cudaFree(ctx->mlp_packed);
+  cudaFree(ctx->mlp_boxkeys);
   cudaFree(ctx->c2p_mem);
   if (ctx->batch) phx::batch_cache_destroy(ctx->batch);
   delete ctx;
@@ -772,9 +786,42 @@ phx_status phx_mlp_set_weights(phx_ctx *ctx, const float *params_host) {
   cudaMemset(ctx->mlp_v, 0, sizeof(float) * PHX_MLP_NPARAM);
   ctx->mlp_step = 0;
   phx::launch_mlp_pack(ctx->mlp_w, ctx->mlp_packed, 0);
+  phx::launch_mlp_box_reset(ctx->mlp_packed, 0);  // weights from elsewhere: no input box until one is set
   if ((s = cuda_status("mlp pack"))) return s;
   if (cudaDeviceSynchronize() != cudaSuccess) return cuda_status("mlp pack");
   ctx->mlp_loaded = 1;
+  return PHX_OK;
+}
+
+phx_status phx_mlp_set_input_box(phx_ctx *ctx, const float *lo_host, const float *hi_host) {
+  phx_status s;
+  if ((s = ctx_device(ctx))) return s;
+  float lo[8], hi[8];
+  for (int c = 0; c < 8; c++) {
+    lo[c] = (lo_host && c < PHX_MLP_IN) ? lo_host[c] : -INFINITY;
+    hi[c] = (hi_host && c < PHX_MLP_IN) ? hi_host[c] : INFINITY;
+    if (!(lo[c] <= hi[c])) return fail(PHX_ERR_INVALID_ARG, "input box: lo > hi (or NaN) in feature %d", c);
+  }
+  char *base = reinterpret_cast<char *>(ctx->mlp_packed);
+  if (cudaMemcpy(base + offsetof(phx::MlpPacked, xlo), lo, sizeof(lo), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(base + offsetof(phx::MlpPacked, xhi), hi, sizeof(hi), cudaMemcpyHostToDevice) != cudaSuccess)
+    return cuda_status("phx_mlp_set_input_box");
+  return PHX_OK;
+}
+
+phx_status phx_mlp_get_input_box(phx_ctx *ctx, float *lo_host, float *hi_host) {
+  phx_status s;
+  if ((s = ctx_device(ctx))) return s;
+  if (!lo_host || !hi_host) return fail(PHX_ERR_INVALID_ARG, "lo/hi is NULL");
+  float lo[8], hi[8];
+  const char *base = reinterpret_cast<const char *>(ctx->mlp_packed);
+  if (cudaMemcpy(lo, base + offsetof(phx::MlpPacked, xlo), sizeof(lo), cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemcpy(hi, base + offsetof(phx::MlpPacked, xhi), sizeof(hi), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return cuda_status("phx_mlp_get_input_box");
+  for (int c = 0; c < PHX_MLP_IN; c++) {
+    lo_host[c] = lo[c];
+    hi_host[c] = hi[c];
+  }
   return PHX_OK;
 }
 
@@ -861,6 +908,9 @@ phx_status phx_mlp_train(phx_ctx *ctx, long long n, const float *x, const float 
                             o->weight_decay, (float)c1, (float)c2, st);
     }
   phx::launch_mlp_pack(ctx->mlp_w, ctx->mlp_packed, st);
+  // the learned start only serves zones inside the training set's feature
+  // range, widened by 2% of the range on each side
+  phx::launch_mlp_box_from(x, n, 0.02f, ctx->mlp_boxkeys, ctx->mlp_packed, st);
   if ((s = cuda_status("phx_mlp_train"))) return s;
   if (cudaStreamSynchronize(st) != cudaSuccess) return cuda_status("phx_mlp_train");
   if (epoch_loss) {
@@ -879,6 +929,15 @@ phx_status phx_mlp_get_weights(phx_ctx *ctx, float *params_host) {
   if (cudaMemcpy(params_host, ctx->mlp_w, sizeof(float) * PHX_MLP_NPARAM, cudaMemcpyDeviceToHost) != cudaSuccess)
     return cuda_status("mlp weights");
   return PHX_OK;
+}
+
+phx_status phx_math_eval(int fn, long long n, const double *x, const double *y, double *out, void *stream) {
+  if (fn < PHX_MATH_EXP || fn > PHX_MATH_POW) return fail(PHX_ERR_INVALID_ARG, "phx_math_eval: unknown function %d", fn);
+  if (n < 0) return fail(PHX_ERR_INVALID_ARG, "n < 0");
+  if (n == 0) return PHX_OK;
+  if (!x || !out || (fn == PHX_MATH_POW && !y)) return fail(PHX_ERR_INVALID_ARG, "x/y/out is NULL");
+  phx::launch_math_eval(fn, n, x, y, out, S(stream));
+  return cuda_status("phx_math_eval");
 }
 
 phx_status phx_probe_fp64_peak(phx_ctx *ctx, double *flops_out) {

@@ -163,8 +163,8 @@ static std::vector<WorkItem> x1_items(const std::vector<BView> &v, int x1_cells,
   for (size_t b = 0; b < v.size(); b++) {
     int pen = (x1_cells + v[b].n1t / 2) / v[b].n1t;
     pen = std::max(1, std::min(32, pen));
-    while (pen > 1 && (size_t)pen * PHX_NRECON * v[b].n1t * sizeof(double) > 200 * 1024) pen--;
-    smem = std::max(smem, (size_t)pen * PHX_NRECON * v[b].n1t * sizeof(double));
+    while (pen > 1 && (size_t)pen * kReconLoad * v[b].n1t * sizeof(double) > 200 * 1024) pen--;
+    smem = std::max(smem, (size_t)pen * kReconLoad * v[b].n1t * sizeof(double));
     const int np = x1_npencil(v[b]);
     for (int f = 0; f < np; f += pen) items.push_back(WorkItem{(int)b, 0, f, std::min(f + pen, np)});
   }

@@ -139,6 +139,11 @@ struct BoxZones {
     x3 = b.Xc(2, k);
     guess = b.prim[PHX_PMU * b.vs + id];
   }
+  // the stored mu of zone t alone (the learned start's cold-zone test)
+  __device__ __forceinline__ double guess_of(long long t) const {
+    int k, j, i;
+    return b.prim[PHX_PMU * b.vs + id(t, k, j, i)];
+  }
   __device__ __forceinline__ void store(long long id, const Par &p, const double prim[PHX_NPRIM],
                                         const double U[PHX_NCONS], bool used_bounds, const double sig[3]) const {
     double *P = b.prim + id;
@@ -176,6 +181,7 @@ struct ListZones {
     x3 = coords ? coords[2 * n + t] : 0.0;
     guess = prim ? prim[PHX_PMU * n + t] : 0.0;
   }
+  __device__ __forceinline__ double guess_of(long long t) const { return prim ? prim[PHX_PMU * n + t] : 0.0; }
   __device__ __forceinline__ void store(long long id, const Par &p, const double pr[PHX_NPRIM],
                                         const double U[PHX_NCONS], bool used_bounds, const double sig[3]) const {
 #pragma unroll
@@ -218,17 +224,20 @@ __global__ void __launch_bounds__(C2P_THREADS) k_mlp_bracket(Par p, Z zones, lon
     const long long q = base + threadIdx.x;
     float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     bool ok = false;
-    if (q < count) {
+    // warm zones (a stored mu > 0) keep the reference's start: their stored
+    // mu is the only value read, and the root find reads no bracket for them
+    const bool cold = q < count && !(zones.guess_of(t0 + q) > 0.0);
+    if (cold) {
       long long id;
       Pt g{};
       double U[PHX_NCONS], x1, x2, x3, guess;
       zones.template load<MINK>(t0 + q, id, g, U, x1, x2, x3, guess);
-      if (!(guess > 0.0))  // warm zones keep the reference's start: no bracket needed
-        ok = c2p_features_fp32<MINK>(p, g, U, x1, x2, x3, f);
+      ok = c2p_features_fp32<MINK>(p, g, U, x1, x2, x3, f) && mlp_in_box(S->w, f);
     }
+    if (!__any_sync(0xffffffffu, cold)) continue;  // whole warp warm: no network
     float o0, o1;
     mlp_warp_forward(S->w, f, S->xs[warp], S->os[warp], o0, o1);
-    if (q < count) {
+    if (cold) {
       double lb[3];
       mlp_bracket(o0, o1, lb);
       const double nan = __longlong_as_double(0x7ff8000000000000ll);
@@ -346,7 +355,7 @@ __global__ void __launch_bounds__(C2P_THREADS) k_c2p(Par p, Z zones, long long t
   RFState st;
   if constexpr (LEARNED) {
     double lb[3] = {0.0, 0.0, 0.0};
-    if (valid) {
+    if (valid && !(guess > 0.0)) {  // brackets exist for cold zones only
       lb[0] = brk[q];
       lb[1] = brk[count + q];
       lb[2] = brk[2 * count + q];
@@ -535,21 +544,24 @@ __global__ void __launch_bounds__(C2P_THREADS) kb_mlp_bracket(Par p, const BView
     const long long q = w.first + threadIdx.x;
     float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     bool ok = false;
-    if (q < w.last) {
+    const bool cold = q < w.last && !(zones.guess_of(q) > 0.0);  // warm zones: stored mu only
+    if (cold) {
       long long id;
       Pt g{};
       double U[PHX_NCONS], x1, x2, x3, guess;
       zones.template load<MINK>(q, id, g, U, x1, x2, x3, guess);
-      if (!(guess > 0.0))  // warm zones keep the reference's start: no bracket needed
-        ok = c2p_features_fp32<MINK>(p, g, U, x1, x2, x3, f);
+      ok = c2p_features_fp32<MINK>(p, g, U, x1, x2, x3, f) && mlp_in_box(S->w, f);
     }
+    if (!__any_sync(0xffffffffu, cold)) continue;  // whole warp warm: no network
     float o0, o1;
     mlp_warp_forward(S->w, f, S->xs[warp], S->os[warp], o0, o1);
-    double lb[3];
-    mlp_bracket(o0, o1, lb);
-    const double nan = __longlong_as_double(0x7ff8000000000000ll);
-    const long long o = (long long)it * C2P_THREADS + threadIdx.x;
-    for (int c = 0; c < 3; c++) brk[c * stride + o] = ok ? lb[c] : nan;
+    if (cold) {
+      double lb[3];
+      mlp_bracket(o0, o1, lb);
+      const double nan = __longlong_as_double(0x7ff8000000000000ll);
+      const long long o = (long long)it * C2P_THREADS + threadIdx.x;
+      for (int c = 0; c < 3; c++) brk[c * stride + o] = ok ? lb[c] : nan;
+    }
   }
 }
 
@@ -583,7 +595,12 @@ __global__ void __launch_bounds__(C2P_THREADS) kb_c2p(Par p, const BView *views,
     RFState st;
     if constexpr (LEARNED) {
       const long long stride = (long long)nitems * C2P_THREADS, o = (long long)it * C2P_THREADS + threadIdx.x;
-      const double lb[3] = {brk[o], brk[stride + o], brk[2 * stride + o]};
+      double lb[3] = {0.0, 0.0, 0.0};
+      if (valid && !(guess > 0.0)) {  // brackets exist for cold zones only
+        lb[0] = brk[o];
+        lb[1] = brk[stride + o];
+        lb[2] = brk[2 * stride + o];
+      }
       rf_start<true>(p, res, valid && setup_ok, 0.0, 1.0, guess, lb, st);
     } else {
       rf_start<false>(p, res, valid && setup_ok, 0.0, 1.0, guess, nullptr, st);

@@ -14,6 +14,7 @@
 #include <stdint.h>
 
 #include "../../include/phx_fluid.h"
+#include "phx_math.h"
 
 namespace phx {
 
@@ -94,6 +95,20 @@ __device__ __forceinline__ double ratio_p(double a, double b) {
 // ---------------------------------------------------------- parameters
 // Device copy of the fluid / fixup / eos params (phx_params), with the
 // fixup package's defaults already resolved (fixup.cpp:120-180).
+// Reconstructed variables the flux kernels read from memory.  The exact
+// build reconstructs all PHX_NRECON, as the reference does
+// (fluid.cpp:272-286).  Under the ideal gas gamma1 = bulk modulus / P is the
+// constant Gamma (every zone's stored value is Gamma to a few ulps), so the
+// production build reconstructs the first PHX_NRECON - 1 and gives both face
+// states gamma1 = Gamma (recon_gamma1): one variable fewer staged, held in
+// registers and reconstructed per cell and direction.
+#ifdef PHX_EXACT
+constexpr int kReconLoad = PHX_NRECON;
+#else
+constexpr int kReconLoad = PHX_NRECON - 1;
+static_assert(PHX_PGM1 == PHX_NRECON - 1, "gamma1 is the last reconstructed variable");
+#endif
+
 struct Par {
   double gm1, Cv;
   double rho_min_eos, sie_min_eos;
@@ -113,6 +128,14 @@ struct Par {
   int fix_flux;      // fixup/enable_flux_fixup
   int inflow_check;  // fixup/enable_ox1_fmks_inflow_check
 };
+
+// Face states of gamma1 where the production build does not reconstruct it.
+__device__ __forceinline__ void recon_gamma1(const Par &p, double *ql, double *qr) {
+  if constexpr (kReconLoad < PHX_NRECON) {
+    ql[PHX_PGM1] = p.gm1 + 1.0;
+    qr[PHX_PGM1] = p.gm1 + 1.0;
+  }
+}
 
 // ------------------------------------------------ singularity-eos IdealGas
 __device__ __forceinline__ double eos_P_rho_sie(const Par &p, double rho, double sie) {
@@ -147,17 +170,17 @@ __device__ __forceinline__ FloorPt floor_point(const Par &p, double x1, double x
     break;
   case PHX_FLOOR_EXPX1_RHO_SIE:
   case PHX_FLOOR_EXPX1_RHO_U:  // s: the sie floor's numerator
-    f.r = p.r0 * exp(p.ralpha * x1);
-    f.s = p.s0 * exp(p.salpha * x1);
+    f.r = p.r0 * phx_math::exp(p.ralpha * x1);
+    f.s = p.s0 * phx_math::exp(p.salpha * x1);
     break;
   case PHX_FLOOR_X1_RHO_SIE:
-    f.r = p.r0 * fmin(1.0, pow(x1, p.ralpha));
-    f.s = p.s0 * fmin(1.0, pow(x1, p.salpha));
+    f.r = p.r0 * fmin(1.0, phx_math::pow(x1, p.ralpha));
+    f.s = p.s0 * fmin(1.0, phx_math::pow(x1, p.salpha));
     break;
   default: {
     double r = sqrt(x1 * x1 + x2 * x2 + x3 * x3);
-    f.r = p.r0 * fmin(1.0, pow(r, p.ralpha));
-    f.s = p.s0 * fmin(1.0, pow(r, p.salpha));
+    f.r = p.r0 * fmin(1.0, phx_math::pow(r, p.ralpha));
+    f.s = p.s0 * fmin(1.0, phx_math::pow(r, p.salpha));
   } break;
   }
   return f;

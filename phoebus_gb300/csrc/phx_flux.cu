@@ -127,12 +127,12 @@ __device__ __forceinline__ bool x1_stage(const BView &b, const X1Range &xr, int 
   const int n1t = b.n1t;
   if (use_tma) {
     const unsigned bytes = (unsigned)(n1t * sizeof(double));
-    if (threadIdx.x == 0) mbar_expect_tx(bar, bytes * PHX_NRECON * np);
+    if (threadIdx.x == 0) mbar_expect_tx(bar, bytes * kReconLoad * np);
     __syncthreads();
     // one bulk copy per (pencil, variable) row; a CTA may stage more rows
     // than it has threads
-    for (int r = threadIdx.x; r < np * PHX_NRECON; r += blockDim.x) {
-      const int pp = r / PHX_NRECON, v = r % PHX_NRECON;
+    for (int r = threadIdx.x; r < np * kReconLoad; r += blockDim.x) {
+      const int pp = r / kReconLoad, v = r % kReconLoad;
       const int pen = p0 + pp;
       const long long base = b.idx(xr.klo + pen / xr.nj, xr.jlo + pen % xr.nj, 0);
       bulk_g2s(rows + (long long)r * n1t, b.prim + v * b.vs + base, bytes, bar);
@@ -145,8 +145,8 @@ __device__ __forceinline__ bool x1_stage(const BView &b, const X1Range &xr, int 
     __syncthreads();
     return false;
   }
-  for (int r = warp; r < np * PHX_NRECON; r += (int)(blockDim.x >> 5)) {
-    const int pp = r / PHX_NRECON, v = r % PHX_NRECON;
+  for (int r = warp; r < np * kReconLoad; r += (int)(blockDim.x >> 5)) {
+    const int pp = r / kReconLoad, v = r % kReconLoad;
     const int pen = p0 + pp;
     const long long base = b.idx(xr.klo + pen / xr.nj, xr.jlo + pen % xr.nj, 0);
     for (int i = lane; i < n1t; i += 32) rows[(long long)r * n1t + i] = b.prim[v * b.vs + base + i];
@@ -170,10 +170,10 @@ __device__ __forceinline__ void x1_compute(const Par &p, const BView &b, const X
     const bool have = slot < nslot;
     const int pp = have ? slot / ncell : 0;
     const int c = c0 + (have ? slot % ncell : 0);
-    const double *prow = rows + (long long)pp * PHX_NRECON * n1t;
+    const double *prow = rows + (long long)pp * kReconLoad * n1t;
     double ql[PHX_NRECON], qr[PHX_NRECON];
 #pragma unroll
-    for (int v = 0; v < PHX_NRECON; v++) {
+    for (int v = 0; v < kReconLoad; v++) {
       const double *r = prow + v * n1t;
       if (have) {
         if constexpr (RECON == PHX_RECON_WENO5Z || RECON == PHX_RECON_MP5)
@@ -188,7 +188,8 @@ __device__ __forceinline__ void x1_compute(const Par &p, const BView &b, const X
     }
     double left[PHX_NRECON];
 #pragma unroll
-    for (int v = 0; v < PHX_NRECON; v++) left[v] = __shfl_up_sync(FULL, ql[v], 1);
+    for (int v = 0; v < kReconLoad; v++) left[v] = __shfl_up_sync(FULL, ql[v], 1);
+    recon_gamma1(p, left, qr);
     // face of cell c: left state from cell c-1 (same pencil when c > is-1)
     if (have && lane > 0 && c > c0) {
       const int pen = p0 + pp;
@@ -280,9 +281,9 @@ __device__ __forceinline__ void sweep_at(const Par &p, const BView &b, int alo, 
   kji(fbeg - 1, k0, j0, i0);
   const double *pc = b.prim + b.idx(k0, j0, i0);  // cell fbeg-1
   const long long vs = b.vs;
-  double w[PHX_NRECON][5];
+  double w[kReconLoad][5];
 #pragma unroll
-  for (int v = 0; v < PHX_NRECON; v++)
+  for (int v = 0; v < kReconLoad; v++)
 #pragma unroll
     for (int o = 0; o < 4; o++) w[v][o + 1] = pc[v * vs + (o - 2) * stride];  // cells x-2..x+1
   double prev_ql[PHX_NRECON];
@@ -294,7 +295,7 @@ __device__ __forceinline__ void sweep_at(const Par &p, const BView &b, int alo, 
     const double *pn = pc + (long long)(x - (fbeg - 1)) * stride;
     double ql[PHX_NRECON], qr[PHX_NRECON];
 #pragma unroll
-    for (int v = 0; v < PHX_NRECON; v++) {
+    for (int v = 0; v < kReconLoad; v++) {
 #pragma unroll
       for (int o = 0; o < 4; o++) w[v][o] = w[v][o + 1];
       w[v][4] = pn[v * vs + 2 * stride];
@@ -303,10 +304,11 @@ __device__ __forceinline__ void sweep_at(const Par &p, const BView &b, int alo, 
     if (x >= fbeg) {
       int k, j, i;
       kji(x, k, j, i);
+      recon_gamma1(p, prev_ql, qr);
       face_flux<MINK, DIR>(p, b, k, j, i, prev_ql, qr, use_col ? &col : nullptr);
     }
 #pragma unroll
-    for (int v = 0; v < PHX_NRECON; v++) prev_ql[v] = ql[v];
+    for (int v = 0; v < kReconLoad; v++) prev_ql[v] = ql[v];
   }
 }
 
@@ -384,7 +386,7 @@ static void launch_fluxes_t(const Par &p, const BView &b, unsigned int *err, cud
   {
     const X1Range xr = x1_range(b);
     const int jlo = xr.jlo, nj = xr.nj, klo = xr.klo, nk = xr.npencil / xr.nj;
-    const size_t smem = (size_t)X1_PENCILS * PHX_NRECON * b.n1t * sizeof(double);
+    const size_t smem = (size_t)X1_PENCILS * kReconLoad * b.n1t * sizeof(double);
     if (smem <= 200 * 1024) {
       auto kern = k_flux_x1<RECON, MINK>;
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

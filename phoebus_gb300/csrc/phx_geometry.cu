@@ -7,25 +7,31 @@
 // sqrt(gamma); at cell centres the finite-difference derivatives of ln alpha
 // and g_{mu nu} (geometry_utils.hpp:89-178).  The metric does not depend on
 // X3, so X3 faces share the centre table.
+//
+// exp, sin, cos and pow are phx_math.h's (the oracle evaluates the same
+// operations), and this file is compiled without contraction in both library
+// builds, so the tables equal the oracle's bit for bit.
 #include "phx_kernels.cuh"
+#include "phx_math.h"
 
 namespace phx {
 
 struct FmksDev {
   double a, a2, h, xt, alpha, x0, smooth, norm, hexp_br, hexp_nsq, hexp_csq;
+  double epsfd;  // finite-difference step scale eps^(1/3) (geometry_utils.hpp:153)
   int derefine_poles;
 
   // ---- McKinneyGammieRyan (mckinney_gammie_ryan.hpp:64-198)
   __device__ double r_(double X1) const {
     const double hexp_dr = X1 - hexp_br;
-    return exp(X1 + (hexp_dr > 0.) * hexp_csq * pow(hexp_dr, hexp_nsq));
+    return phx_math::exp(X1 + (hexp_dr > 0.) * hexp_csq * phx_math::pow(hexp_dr, hexp_nsq));
   }
   __device__ double thG_(double X2) const {
-    return M_PI * X2 + ((1. - h) / 2.) * sin(2. * M_PI * X2);
+    return M_PI * X2 + ((1. - h) / 2.) * phx_math::sin(2. * M_PI * X2);
   }
   __device__ void thJ_(double X2, double &y, double &thJ) const {
     y = 2. * X2 - 1.;
-    thJ = norm * y * (1. + pow(y / xt, alpha) / (alpha + 1.)) + 0.5 * M_PI;
+    thJ = norm * y * (1. + phx_math::pow(y / xt, alpha) / (alpha + 1.)) + 0.5 * M_PI;
   }
   __device__ void th_(double X1, double X2, double &y, double &th) const {
     const double thG = thG_(X2);
@@ -33,7 +39,7 @@ struct FmksDev {
       double thJ;
       thJ_(X2, y, thJ);
       const double fac = x0 - X1;
-      th = thG + exp(smooth * fac) * (thJ - thG);
+      th = thG + phx_math::exp(smooth * fac) * (thJ - thG);
     } else {
       y = 0;
       th = thG;
@@ -50,19 +56,19 @@ struct FmksDev {
     C[1] = th;
     C[2] = 0.0;
     const double hexp_dr = X1 - hexp_br;
-    const double drdX1 = exp(X1 + (hexp_dr > 0.) * hexp_csq * pow(hexp_dr, hexp_nsq)) *
-                         (1. + (hexp_dr > 0.) * hexp_csq * hexp_nsq * pow(hexp_dr, hexp_nsq - 1.));
-    const double dthGdX2 = M_PI + M_PI * (1 - h) * cos(2 * M_PI * X2);
+    const double drdX1 = phx_math::exp(X1 + (hexp_dr > 0.) * hexp_csq * phx_math::pow(hexp_dr, hexp_nsq)) *
+                         (1. + (hexp_dr > 0.) * hexp_csq * hexp_nsq * phx_math::pow(hexp_dr, hexp_nsq - 1.));
+    const double dthGdX2 = M_PI + M_PI * (1 - h) * phx_math::cos(2 * M_PI * X2);
     double dthdX1, dthdX2;
     if (derefine_poles) {
       thJ_(X2, y, thJ);
       const double thG = thG_(X2);
       const double dydX2 = 2.;
-      const double dthJdy = norm * (1 + pow(y / xt, alpha));
+      const double dthJdy = norm * (1 + phx_math::pow(y / xt, alpha));
       const double dthJdX2 = dthJdy * dydX2;
       const double fac = x0 - X1;
-      dthdX1 = -smooth * (thJ - thG) * exp(smooth * fac);
-      dthdX2 = dthGdX2 + exp(smooth * fac) * (dthJdX2 - dthGdX2);
+      dthdX1 = -smooth * (thJ - thG) * phx_math::exp(smooth * fac);
+      dthdX2 = dthGdX2 + phx_math::exp(smooth * fac) * (dthJdX2 - dthGdX2);
     } else {
       dthdX1 = 0.0;
       dthdX2 = dthGdX2;
@@ -81,11 +87,11 @@ struct FmksDev {
   // ---- SphericalKerrSchild (spherical_kerr_schild.hpp:48-243)
   __device__ double rho2_(double r, double cth) const { return r * r + a2 * cth * cth; }
   __device__ double ks_lapse(double X1, double X2) const {
-    const double r = fabs(X1), cth = cos(X2), rho2 = rho2_(r, cth);
+    const double r = fabs(X1), cth = phx_math::cos(X2), rho2 = rho2_(r, cth);
     return sqrt(ratio(rho2, 2 * r + rho2));
   }
   __device__ void ks_gcov(double X1, double X2, double g[4][4]) const {
-    const double r = fabs(X1), th = X2, cth = cos(th), sth = sin(th), sth2 = sth * sth;
+    const double r = fabs(X1), th = X2, cth = phx_math::cos(th), sth = phx_math::sin(th), sth2 = sth * sth;
     const double rho2 = rho2_(r, cth);
     for (int m = 0; m < 4; m++)
       for (int n = 0; n < 4; n++) g[m][n] = 0;
@@ -98,7 +104,7 @@ struct FmksDev {
     g[3][3] = (rho2 + a2 * (1 + g[0][1]) * sth2) * sth2;
   }
   __device__ void ks_gamcon(double X1, double X2, double g[3][3]) const {
-    const double r = fabs(X1), th = X2, cth = cos(th), sth = sin(th), sth2 = sth * sth;
+    const double r = fabs(X1), th = X2, cth = phx_math::cos(th), sth = phx_math::sin(th), sth2 = sth * sth;
     const double rho2 = rho2_(r, cth);
     for (int m = 0; m < 3; m++)
       for (int n = 0; n < 3; n++) g[m][n] = 0;
@@ -108,7 +114,7 @@ struct FmksDev {
     g[2][2] = ratio(1, rho2 * sth2);
   }
   __device__ double ks_detgam(double X1, double X2) const {
-    const double r = fabs(X1), th = X2, cth = cos(th), sth = sin(th), sth2 = sth * sth;
+    const double r = fabs(X1), th = X2, cth = phx_math::cos(th), sth = phx_math::sin(th), sth2 = sth * sth;
     const double rho2 = rho2_(r, cth);
     return sqrt(fabs(rho2 * (2 * r + rho2) * sth2));
   }
@@ -144,7 +150,7 @@ struct FmksDev {
                          Jcov[0][1] * Jcov[1][0] * Jcov[2][2] - Jcov[0][0] * Jcov[1][2] * Jcov[2][1]);
     out[PHX_G_DETGAM * pitch] = fabs(ks_detgam(C[0], C[1]) * detJ);
     {  // shift: beta^i = Jcon^i_j beta0^j
-      const double r = fabs(C[0]), cth = cos(C[1]), rho2 = rho2_(r, cth);
+      const double r = fabs(C[0]), cth = phx_math::cos(C[1]), rho2 = rho2_(r, cth);
       const double beta0[3] = {ratio(2 * r, 2 * r + rho2), 0, 0};
       for (int i = 0; i < 3; i++) {
         double s = 0;
@@ -196,7 +202,7 @@ __global__ void k_geom_deriv(FmksDev f, double x01, double dx1, double x02, doub
   const int i = (int)(q % ni), j = (int)(q / ni);
   const double X1 = x01 + (i + 0.5) * dx1;
   const double X2 = x02 + (j + 0.5) * dx2;
-  const double EPSFD = pow(2.220446049250313e-16, 1.0 / 3.0);
+  const double EPSFD = f.epsfd;
   // GradLnAlpha (geometry_utils.hpp:89-119); the X3 derivative is 0 exactly
   // (identical lapse at X3 +- dx) and is stored as the reference computes it.
   for (int d = 1; d < 4; d++) {
@@ -255,7 +261,8 @@ static FmksDev make_fmks(const phx_geometry &g) {
   f.hexp_nsq = g.hexp_nsq;
   f.hexp_csq = g.hexp_csq;
   f.derefine_poles = g.derefine_poles;
-  f.norm = 0.5 * M_PI * 1. / (1. + 1. / (f.alpha + 1.) * 1. / pow(f.xt, f.alpha));
+  f.norm = 0.5 * M_PI * 1. / (1. + 1. / (f.alpha + 1.) * 1. / phx_math::pow(f.xt, f.alpha));
+  f.epsfd = phx_math::pow(2.220446049250313e-16, 1.0 / 3.0);
   return f;
 }
 
@@ -265,6 +272,27 @@ void launch_geom_points(const phx_geometry &g, long long n, const double *x1, co
   const FmksDev f = make_fmks(g);
   const int T = 128;
   k_geom_points<<<(unsigned)((n + T - 1) / T), T, 0, s>>>(f, n, x1, x2, geom);
+}
+
+// The library's exp / log / sin / cos / pow over an array (their validation).
+__global__ void k_math_eval(int fn, long long n, const double *x, const double *y, double *out) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const double a = x[q];
+  double r;
+  switch (fn) {
+  case PHX_MATH_EXP: r = phx_math::exp(a); break;
+  case PHX_MATH_LOG: r = phx_math::log(a); break;
+  case PHX_MATH_SIN: r = phx_math::sin(a); break;
+  case PHX_MATH_COS: r = phx_math::cos(a); break;
+  default: r = phx_math::pow(a, y[q]); break;
+  }
+  out[q] = r;
+}
+
+void launch_math_eval(int fn, long long n, const double *x, const double *y, double *out, cudaStream_t s) {
+  if (n <= 0) return;
+  k_math_eval<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(fn, n, x, y, out);
 }
 
 void launch_geom_fmks(const phx_geometry &g, const BView &b, cudaStream_t s) {

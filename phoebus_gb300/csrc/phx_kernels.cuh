@@ -29,6 +29,9 @@ struct WorkItem {
   long long first, last;
 };
 
+// Sets the text phx_last_error() returns on this host thread.
+void set_last_error(const char *msg);
+
 void launch_p2c(const Par &p, const BView &b, Range3 r, cudaStream_t s);
 struct MlpPacked;
 // con2prim works in chunks of C2P_CHUNK zones; per chunk the context holds
@@ -58,6 +61,7 @@ void launch_floors(const Par &p, const BView &b, Range3 r, DevStats *stats, unsi
 void launch_geom_fmks(const phx_geometry &g, const BView &b, cudaStream_t s);
 void launch_geom_points(const phx_geometry &g, long long n, const double *x1, const double *x2, double *geom,
                         cudaStream_t s);
+void launch_math_eval(int fn, long long n, const double *x, const double *y, double *out, cudaStream_t s);
 void launch_p2c_zones(const Par &p, long long n, const double *prim, const double *geom, double *cons,
                       double *cell_sig, cudaStream_t s);
 void launch_c2p_zones(const Par &p, long long n, double *cons, double *prim, const double *geom, double *fail,
@@ -67,6 +71,11 @@ void launch_mlp_bracket(const Par &p, long long n, const double *cons, const dou
                         const MlpPacked *mlp, double *bracket, unsigned int *err, cudaStream_t s);
 // learned-start network (phx_mlp.cu)
 void launch_mlp_pack(const float *theta, MlpPacked *out, cudaStream_t s);
+// The input box: reset to (-inf, inf), or the range of the features x[6][n]
+// widened by `margin` of the range on each side (keys: 12 ints of device
+// scratch).
+void launch_mlp_box_reset(MlpPacked *out, cudaStream_t s);
+void launch_mlp_box_from(const float *x, long long n, float margin, int *keys, MlpPacked *out, cudaStream_t s);
 void launch_mlp_features(const Par &p, long long n, const double *cons, const double *geom, const double *coords,
                          float *x, cudaStream_t s);
 void launch_mlp_forward(const MlpPacked *mlp, long long n, const float *x, float *out, unsigned int *err,

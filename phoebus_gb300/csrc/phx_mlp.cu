@@ -60,6 +60,93 @@ void launch_mlp_pack(const float *theta, MlpPacked *out, cudaStream_t s) {
   k_mlp_pack<<<(n + 255) / 256, 256, 0, s>>>(theta, out);
 }
 
+// ------------------------------------------------------------- input box
+// Floats ordered as ints: non-negative floats keep their bits, negative ones
+// flip the magnitude bits, so int order equals float order (NaN excluded).
+__device__ __forceinline__ int mlp_fkey(float f) {
+  const int b = __float_as_int(f);
+  return b >= 0 ? b : b ^ 0x7fffffff;
+}
+__device__ __forceinline__ float mlp_funkey(int k) { return __int_as_float(k >= 0 ? k : k ^ 0x7fffffff); }
+
+__global__ void k_mlp_box_reset(MlpPacked *out) {
+  const int c = threadIdx.x;
+  if (c < 8) {
+    out->xlo[c] = -INFINITY;
+    out->xhi[c] = INFINITY;
+  }
+}
+
+__global__ void k_mlp_box_init(int *keys) {
+  const int c = threadIdx.x;
+  if (c < PHX_MLP_IN) {
+    keys[c] = 0x7fffffff;                // running min
+    keys[PHX_MLP_IN + c] = (int)0x80000000;  // running max
+  }
+}
+
+__global__ void __launch_bounds__(256) k_mlp_box_reduce(const float *x, long long n, int *keys) {
+  __shared__ int smin[PHX_MLP_IN], smax[PHX_MLP_IN];
+  if (threadIdx.x < PHX_MLP_IN) {
+    smin[threadIdx.x] = 0x7fffffff;
+    smax[threadIdx.x] = (int)0x80000000;
+  }
+  __syncthreads();
+  for (int c = 0; c < PHX_MLP_IN; c++) {
+    int lo = 0x7fffffff, hi = (int)0x80000000;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+      const float f = x[c * n + q];
+      if (isfinite(f)) {
+        lo = min(lo, mlp_fkey(f));
+        hi = max(hi, mlp_fkey(f));
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+      hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicMin(&smin[c], lo);
+      atomicMax(&smax[c], hi);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < PHX_MLP_IN) {
+    atomicMin(&keys[threadIdx.x], smin[threadIdx.x]);
+    atomicMax(&keys[PHX_MLP_IN + threadIdx.x], smax[threadIdx.x]);
+  }
+}
+
+__global__ void k_mlp_box_finish(const int *keys, float margin, MlpPacked *out) {
+  const int c = threadIdx.x;
+  if (c < PHX_MLP_IN) {
+    const int klo = keys[c], khi = keys[PHX_MLP_IN + c];
+    if (klo > khi) {  // no finite sample: leave the input unbounded
+      out->xlo[c] = -INFINITY;
+      out->xhi[c] = INFINITY;
+      return;
+    }
+    const float lo = mlp_funkey(klo), hi = mlp_funkey(khi), w = margin * (hi - lo);
+    out->xlo[c] = lo - w;
+    out->xhi[c] = hi + w;
+  } else if (c < 8) {
+    out->xlo[c] = -INFINITY;
+    out->xhi[c] = INFINITY;
+  }
+}
+
+void launch_mlp_box_reset(MlpPacked *out, cudaStream_t s) { k_mlp_box_reset<<<1, 32, 0, s>>>(out); }
+
+void launch_mlp_box_from(const float *x, long long n, float margin, int *keys, MlpPacked *out, cudaStream_t s) {
+  k_mlp_box_init<<<1, 32, 0, s>>>(keys);
+  if (n > 0) {
+    long long grid = (n + 255) / 256;
+    if (grid > 152 * 4) grid = 152 * 4;
+    k_mlp_box_reduce<<<(unsigned)grid, 256, 0, s>>>(x, n, keys);
+  }
+  k_mlp_box_finish<<<1, 32, 0, s>>>(keys, margin, out);
+}
+
 // ----------------------------------------------------------------- features
 template <bool MINK>
 __global__ void __launch_bounds__(128) k_mlp_features(Par p, long long n, const double *cons, const double *geom,

@@ -39,6 +39,10 @@ struct MlpPacked {
   uint2 w3[8 * 4 * 32];
   uint2 w4[1 * 4 * 32];
   float b1[64], b2[64], b3[64], b4[8];
+  // input box of the learned start: a cold zone whose features fall outside
+  // [xlo, xhi] (the training set's range, widened) gets no bracket and keeps
+  // the reference's start; (-inf, inf) when no box is set
+  float xlo[8], xhi[8];
 };
 static_assert(sizeof(MlpPacked) % 16 == 0, "bulk copies move multiples of 16 bytes");
 
@@ -174,6 +178,14 @@ __device__ __forceinline__ void mlp_warp_forward(const MlpPacked &S, const float
   o0 = os[lane * 2];
   o1 = os[lane * 2 + 1];
   __syncwarp();
+}
+
+// True when all six features lie inside the network's input box (NaN: no).
+__device__ __forceinline__ bool mlp_in_box(const MlpPacked &S, const float f[6]) {
+  bool in = true;
+#pragma unroll
+  for (int c = 0; c < 6; c++) in = in && f[c] >= S.xlo[c] && f[c] <= S.xhi[c];
+  return in;
 }
 
 // (m, lo, hi) in [0, 1] from the outputs: m = e^{o0}, half-width

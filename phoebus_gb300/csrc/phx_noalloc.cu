@@ -18,6 +18,8 @@
 // PHX_DT_STATIC_MAX_ZONES interior zones are rejected.  Every call shares the
 // array: calls whose kernels overlap on the GPU (e.g. on two streams) race on
 // it.  Nothing needs clearing: each call writes every partial it reads.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "phx_kernels.cuh"
@@ -30,12 +32,21 @@ static_assert((long long)kMaxPartials * kThreads == PHX_DT_STATIC_MAX_ZONES, "ca
 
 static __device__ __align__(256) double g_dt_partials[kMaxPartials];
 
-// Device address of g_dt_partials per device, looked up once per device.
+// Device address of g_dt_partials per device, looked up on the first call
+// with that device current.  The address belongs to the context the module
+// was loaded into: it is kept with that context's unique id and looked up
+// again when the current context differs (after cudaDeviceReset the primary
+// context is a new one, and the module may sit at another address).
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 double *g_addr[kMaxDevices] = {};
+unsigned long long g_ctx_id[kMaxDevices] = {};
 
-phx_status reject(phx_status s, const char *) { return s; }
+// Errors go to phx_last_error() like every other entry point's.
+phx_status reject(phx_status s, const char *msg) {
+  phx::set_last_error(msg);
+  return s;
+}
 
 // Same per-zone estimate as fluid.cpp:913-939: 1 / (sum_d max signal speed /
 // dx_d + 1e-50); one partial minimum per thread block.
@@ -84,15 +95,43 @@ __global__ void __launch_bounds__(1024) k_dt_finish(const double *partials, int 
   }
 }
 
-// Set-up, once per device, with that device current: the host-side name of a
-// __device__ array is not a device address, so look the address up.
+// Set-up, once per device (and again after the device's context was
+// replaced), with that device current: the host-side name of a __device__
+// array is not a device address, so look the address up.
 phx_status scratch_address(double **out) {
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0)
     return reject(PHX_ERR_NO_DEVICE, "phx_estimate_timestep_static: no current CUDA device");
   if (dev >= kMaxDevices) return reject(PHX_ERR_CAPACITY, "phx_estimate_timestep_static: device index >= 64");
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_addr[dev]) {
+  // The driver calls are resolved through the runtime, so the library keeps
+  // loading on hosts without a driver (the CPU test suite).
+  using GetCurrentFn = CUresult (*)(CUcontext *);
+  using GetIdFn = CUresult (*)(CUcontext, unsigned long long *);
+  static GetCurrentFn get_current = nullptr;
+  static GetIdFn get_id = nullptr;
+  if (!get_current || !get_id) {
+    void *f0 = nullptr, *f1 = nullptr;
+    cudaDriverEntryPointQueryResult q0, q1;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f0, 4000, cudaEnableDefault, &q0) != cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+        q0 != cudaDriverEntryPointSuccess || q1 != cudaDriverEntryPointSuccess || !f0 || !f1) {
+      cudaGetLastError();
+      return reject(PHX_ERR_CUDA, "phx_estimate_timestep_static: driver entry points not found");
+    }
+    get_current = reinterpret_cast<GetCurrentFn>(f0);
+    get_id = reinterpret_cast<GetIdFn>(f1);
+  }
+  // The id of the current context (0 when the runtime has not made one current
+  // yet; the lookup below does, and the id is read again after it).
+  auto ctx_id = [&]() -> unsigned long long {
+    CUcontext cu = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&cu) != CUDA_SUCCESS || cu == nullptr || get_id(cu, &id) != CUDA_SUCCESS) return 0;
+    return id;
+  };
+  const unsigned long long id = ctx_id();
+  if (!g_addr[dev] || id == 0 || g_ctx_id[dev] != id) {
     void *p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_dt_partials);
     if (e != cudaSuccess || p == nullptr) {
@@ -100,6 +139,7 @@ phx_status scratch_address(double **out) {
       return reject(PHX_ERR_CUDA, "phx_estimate_timestep_static: cudaGetSymbolAddress failed");
     }
     g_addr[dev] = static_cast<double *>(p);
+    g_ctx_id[dev] = ctx_id();
   }
   *out = g_addr[dev];
   return PHX_OK;
@@ -111,12 +151,22 @@ extern "C" {
 
 phx_status phx_estimate_timestep_static(const phx_params *p, const phx_block *blk, int use_face_speeds,
                                         double *dt_out_device, void *stream) {
-  if (!p || !blk || !dt_out_device) return reject(PHX_ERR_INVALID_ARG, "params, block and dt_out are required");
-  if (blk->ndim < 1 || blk->ndim > 3 || blk->ng < 1 || blk->nx1 < 1 || blk->nx2 < 1 || blk->nx3 < 1 ||
+  if (!p || !blk || !dt_out_device)
+    return reject(PHX_ERR_INVALID_ARG, "phx_estimate_timestep_static: params, block and dt_out are required");
+  // the block checks of phx_estimate_timestep that do not involve prim/cons
+  if (blk->ndim < 1 || blk->ndim > 3 || blk->nx1 < 1 || blk->nx2 < 1 || blk->nx3 < 1 ||
       (blk->ndim < 2 && blk->nx2 != 1) || (blk->ndim < 3 && blk->nx3 != 1))
-    return reject(PHX_ERR_INVALID_ARG, "invalid block shape");
+    return reject(PHX_ERR_INVALID_ARG, "phx_estimate_timestep_static: invalid block shape");
+  if (blk->ng < 3) return reject(PHX_ERR_INVALID_ARG, "phx_estimate_timestep_static: ng must be >= 3");
   if (!blk->cell_sig || (use_face_speeds && !blk->face_sig))
-    return reject(PHX_ERR_INVALID_ARG, "cell_sig (and face_sig with use_face_speeds) are required");
+    return reject(PHX_ERR_INVALID_ARG,
+                  "phx_estimate_timestep_static: cell_sig (and face_sig with use_face_speeds) are required");
+  {
+    const long long N = (long long)(blk->nx1 + 2 * blk->ng) * (blk->ndim >= 2 ? blk->nx2 + 2 * blk->ng : 1) *
+                        (blk->ndim >= 3 ? blk->nx3 + 2 * blk->ng : 1);
+    if (blk->var_stride != 0 && blk->var_stride < N)
+      return reject(PHX_ERR_INVALID_ARG, "phx_estimate_timestep_static: var_stride smaller than the block");
+  }
   const long long n = (long long)blk->nx1 * (blk->ndim >= 2 ? blk->nx2 : 1) * (blk->ndim >= 3 ? blk->nx3 : 1);
   if (n > PHX_DT_STATIC_MAX_ZONES)
     return reject(PHX_ERR_CAPACITY,

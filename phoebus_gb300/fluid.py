@@ -140,6 +140,19 @@ class FluidContext:
         self._ok(self.lib.phx_mlp_get_weights(self.h, t.ctypes.data_as(C.POINTER(C.c_float))))
         return t
 
+    def mlp_input_box(self):
+        """(lo[6], hi[6]) of the learned start's input box."""
+        import numpy as np
+
+        lo, hi = (C.c_float * abi.MLP_IN)(), (C.c_float * abi.MLP_IN)()
+        self._ok(self.lib.phx_mlp_get_input_box(self.h, lo, hi))
+        return np.array(lo[:], dtype=np.float32), np.array(hi[:], dtype=np.float32)
+
+    def mlp_set_input_box(self, lo=None, hi=None):
+        """Set the box (None: that side unbounded)."""
+        f = lambda a: None if a is None else (C.c_float * abi.MLP_IN)(*[float(x) for x in a])  # noqa: E731
+        self._ok(self.lib.phx_mlp_set_input_box(self.h, f(lo), f(hi)))
+
     def MLPFeaturesZones(self, p: abi.Params, cons, geom=None, coords=None, x=None, stream=None):
         import torch
 

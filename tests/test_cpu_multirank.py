@@ -58,7 +58,7 @@ def test_reference_arm_under_torchrun(built):
     port = _free_port()
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2", "--master-addr",
            "127.0.0.1", "--master-port", str(port), str(ROOT / "bench.py"), "--impl", "reference", "--gpus", "2",
-           "--steps", "1", "--warmup", "1", "--cpu-n", "16"]
+           "--steps", "1", "--warmup", "1", "--ref-n", "16"]
     r = subprocess.run(cmd, capture_output=True, text=True, cwd=ROOT, env={**os.environ, "OMP_NUM_THREADS": "2"},
                        timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]

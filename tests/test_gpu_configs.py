@@ -1,0 +1,335 @@
+"""Parity of the benchmarked (production) build at the workload sizes, per zone.
+
+The kernel-level parity tests run small blocks.  These run the production
+library (libphx_fluid.so: FMA contraction, Newton-refined reciprocals, the
+build the bench times) and the exact library against the oracle on the
+workloads themselves:
+
+  config 1  64^3 SR-MHD blast wave, PLM (MC) + LLF, 10 RK2 steps
+  config 2  one 256^3 shear-layer block, WENO5-Z + HLL: fluxes, dU/dt and one
+            full RK stage (the bench's block)
+  config 3  64 periodic blocks drawn from the {16^3, 32^3, 64^3} mix
+            (p = 0.5, 0.35, 0.15), per-zone random states, MP5 + HLL, floors,
+            ceilings and c2p fixup on, one RK2 step through phx_stage_batched
+            against the oracle's per-block Stage
+
+Bars (per zone / per face, never against a block-wide maximum):
+  fluxes, dU/dt, conserved updates: |d| <= 1e-12 (|ref| + local scale), the
+      local scale being the magnitude of the terms that form the value at that
+      face or zone (tests/util.py: cell_flux_magnitudes, face_flux_scale);
+  signal speeds: 1e-12 relative;
+  primitives after con2prim: the root mu within 2 tol of the oracle's (both
+      are within tol of the root); each primitive within 2.5 delta + 1e-11,
+      delta being the largest per-zone deviation the tolerance itself allows
+      (the oracle at tol against the oracle at a tighter tolerance on the
+      same inputs), plus the 1e-12-level difference of the conserved inputs;
+      per-zone deviations are |d| / (|ref| + floor), the floors of
+      tests/util.py:prim_floors (velocities against |W v| plus the zone's
+      signal speed, fields against |B|, rho, u, P against themselves);
+  fail flags: bit for bit.
+The printed maxima ([per-zone] lines, pytest -s) are the measured agreement.
+"""
+import numpy as np
+import pytest
+
+from phoebus_gb300 import abi, states
+from tests.util import (assert_bitwise, cell_flux_magnitudes, face_flux_scale, face_region, flux_view, host,
+                        max_rel_floor, prim_floors, report_close, _shift)
+
+pytestmark = pytest.mark.gpu
+
+PRIM_VARS = {"rho": abi.PRHO, "v1": abi.PVEL, "v2": abi.PVEL + 1, "v3": abi.PVEL + 2, "u": abi.PENG,
+             "P": abi.PPRS, "B1": abi.PB, "B2": abi.PB + 1, "B3": abi.PB + 2}
+
+
+def _mem_available_gb():
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    return int(line.split()[1]) / 1e6
+    except OSError:
+        pass
+    return 0.0
+
+
+def _dudt_scale(hb, mags=None):
+    """Local scale [8][...] of dU/dt per zone: the face scales of both faces
+    in every direction over dx; the B rows after FluxCT mix the B fluxes of
+    the transverse neighbours (corner EMFs), so they take the largest over
+    the 3^3 neighbourhood."""
+    m = cell_flux_magnitudes(hb) if mags is None else mags
+    tot = np.zeros_like(m)
+    for d in range(hb.ndim):
+        fs = face_flux_scale(hb, d, m)
+        tot += (fs + _shift(fs, d, -1)) / hb.dx[d]
+        del fs
+    B = tot[5:8]
+    for d in range(hb.ndim):
+        B = np.maximum(B, np.maximum(_shift(B, d, 1), _shift(B, d, -1)))
+    tot[5:8] = B
+    return tot
+
+
+def _tight_delta(oracle, p, prim, cons, floors, tol_tight=1e-15):
+    """Largest per-zone deviation of each primitive, |d| / (|ref| + floor),
+    between the oracle's result at p.c2p_tol (prim [12][...]) and its result
+    at tol_tight on the same conserved state (cons [8][...]), Minkowski zones
+    inverted independently."""
+    pt = abi.default_params()
+    for f, _ in pt._fields_:
+        setattr(pt, f, getattr(p, f))
+    pt.c2p_tol, pt.c2p_max_iter = tol_tight, 400
+    pz = np.ascontiguousarray(prim.reshape(prim.shape[0], -1))
+    cz = np.ascontiguousarray(cons.reshape(cons.shape[0], -1))
+    tp, tc = pz.copy(), cz.copy()
+    oracle.ConservedToPrimitiveZones(pt, tc, tp)
+    return {n: max_rel_floor(pz[v], tp[v], floors[v].reshape(-1)) for n, v in PRIM_VARS.items()}
+
+
+def _check_prims(got_b, ref_b, delta, tol, what, check_mu=True):
+    """mu within 2 tol; every primitive within 2.5 delta + 1e-11 per zone
+    (floors of prim_floors); fail flags bitwise."""
+    g, r = host(got_b["prim"]), ref_b["prim"]
+    fl = prim_floors(ref_b)
+    if check_mu:
+        dmu = np.nanmax(np.abs(g[abi.PMU] - r[abi.PMU]))
+        print(f"[per-zone] {what}: max |mu - mu_ref| = {dmu:.3e} (bar {2 * tol:g})")
+        assert dmu <= 2 * tol, (what, dmu)
+    for n, v in PRIM_VARS.items():
+        e = max_rel_floor(g[v], r[v], fl[v])
+        bar = 2.5 * delta[n] + 1e-11
+        print(f"[per-zone] {what} {n}: max {e:.3e} (delta {delta[n]:.3e}, bar {bar:.3e})")
+        assert e <= bar, (what, n, e, delta[n])
+    assert_bitwise(got_b["fail"], ref_b["fail"], f"{what} fail")
+
+
+def test_config2_shear256_production(oracle, ctx_fast):
+    """Config 2 at its own size, 256^3 (the bench's block): fluxes of all
+    three directions and both signal speeds per face, dU/dt per zone, then
+    one full RK stage (sources, fluxes, FluxCT, update, con2prim, periodic
+    exchange, con2prim): conserved per zone, primitives and fail flags."""
+    import torch
+
+    if _mem_available_gb() < 40:
+        pytest.skip("needs about 40 GB of host memory for the 256^3 oracle block")
+    hb, par = states.kelvin_helmholtz(256)
+    p = abi.default_params(**par)
+    oracle.Initialize(p, hb)
+    db = hb.to_device()
+    oracle.CalculateFluxes(p, hb)
+    ctx_fast.CalculateFluxes(p, db)
+    ctx_fast.check()
+    mags = cell_flux_magnitudes(hb)
+    for d in range(3):
+        r = face_region(hb, d)
+        fs = face_flux_scale(hb, d, mags)
+        g = flux_view(db["flux"], d).cpu().numpy()
+        f = flux_view(hb["flux"], d)
+        for m in range(8):
+            report_close(g[m][r], f[m][r], fs[m][r], 1e-12, f"config2 flux d={d} m={m}")
+        report_close(db["face_sig"][d].cpu().numpy()[r], hb["face_sig"][d][r], 0.0, 1e-12, f"config2 face_sig d={d}")
+        del fs, g
+    # dU/dt (sources + fluxes + FluxCT + divergence), interior zones
+    oracle.CalculateFluidSourceTerms(p, hb)
+    oracle.FluxCT(p, hb)
+    oracle.FluxDivergence(p, hb)
+    ctx_fast.CalculateFluidSourceTerms(p, db)
+    ctx_fast.FluxCT(p, db)
+    ctx_fast.UpdateStage(db, None, None, 1.0, 0.0)
+    sd = _dudt_scale(hb, mags)
+    isl = (slice(None),) + hb.isl()
+    report_close(db["dudt"].cpu().numpy()[isl], hb["dudt"][isl], sd[isl], 1e-12, "config2 dU/dt")
+    # one full stage from the same initial state
+    dt = 0.5 * oracle.EstimateTimestepBlock(p, hb, False)
+    base_h = hb["cons"].copy()
+    out_h = np.zeros_like(base_h)
+    oracle.Stage(p, hb, base_h, out_h, 1.0, dt)
+    out_d = torch.zeros_like(db["cons"])
+    ctx_fast.Stage(p, db, db["cons"], out_d, 1.0, dt)
+    ctx_fast.check()
+    scale = np.abs(base_h) + dt * sd
+    del sd
+    report_close(out_d.cpu().numpy()[isl], out_h[isl], scale[isl], 1e-12, "config2 stage cons")
+    del scale
+    hb.arrays["cons"] = out_h
+    sl = (slice(None), slice(100, 108))
+    fl = {v: f[slice(100, 108)] for v, f in prim_floors(hb).items()}
+    delta = _tight_delta(oracle, p, hb["prim"][sl], out_h[sl], fl)
+    _check_prims(db, hb, delta, p.c2p_tol, "config2 stage prims")
+
+
+def _blast_run(oracle, p, hb, nsteps, dts=None):
+    """nsteps RK2 steps of the oracle; returns the dt sequence (the
+    reference's control: first estimate from cell speeds, then face speeds,
+    growth at most 2x) or replays dts."""
+    hs = np.zeros_like(hb["cons"])
+    out = []
+    dt = oracle.EstimateTimestepBlock(p, hb, False) if dts is None else dts[0]
+    for s in range(nsteps):
+        if dts is not None:
+            dt = dts[s]
+        out.append(dt)
+        oracle.rk2_step(p, hb, hs, dt)
+        if dts is None:
+            dt = min(2 * dt, oracle.EstimateTimestepBlock(p, hb, True))
+    return out
+
+
+@pytest.mark.parametrize("exact", [True, False])
+def test_config1_blast64_ten_steps(oracle, ctx_exact, ctx_fast, exact):
+    """Config 1 at its own size: the 64^3 blast wave, PLM + LLF, CFL 0.3,
+    10 RK2 steps on the oracle's timestep sequence.  Exact build: bit for
+    bit.  Production build: the primitives per zone within the spread the
+    con2prim tolerance itself allows over the same 10 steps (the oracle at
+    tolerance 1e-10 against the oracle at 1e-13), fail flags bit for bit."""
+    import torch
+
+    from phoebus_gb300.fluid import rk2_step
+
+    ctx = ctx_exact if exact else ctx_fast
+    hb, par = states.blast_wave(64)
+    p = abi.default_params(**par)
+    oracle.Initialize(p, hb)
+    db = hb.to_device()
+    h0 = hb.to_host()
+    dts = _blast_run(oracle, p, hb, 10)
+    ds = torch.zeros_like(db["cons"])
+    for dt in dts:
+        rk2_step(ctx, p, db, ds, dt)
+    ctx.check()
+    if exact:
+        for name in ("cons", "prim", "fail"):
+            assert_bitwise(db[name], hb[name], f"config1 {name} after 10 steps")
+        return
+    pt = abi.default_params(**par)
+    pt.c2p_tol, pt.c2p_max_iter = 1e-13, 200
+    _blast_run(oracle, pt, h0, 10, dts)
+    fl = prim_floors(hb)
+    delta = {n: max_rel_floor(h0["prim"][v], hb["prim"][v], fl[v]) for n, v in PRIM_VARS.items()}
+    g = db["prim"].cpu().numpy()
+    # mu: each run is within tol of its own root, but the conserved states
+    # drift apart over 10 steps, so mu is held to the same spread
+    dmu = np.max(np.abs(g[abi.PMU] - hb["prim"][abi.PMU]))
+    dmu_tol = np.max(np.abs(h0["prim"][abi.PMU] - hb["prim"][abi.PMU]))
+    print(f"[per-zone] config1 10 steps mu: max abs {dmu:.3e} (spread {dmu_tol:.3e})")
+    assert dmu <= 2.5 * dmu_tol + 2 * p.c2p_tol
+    for n, v in PRIM_VARS.items():
+        e = max_rel_floor(g[v], hb["prim"][v], fl[v])
+        bar = 2.5 * delta[n] + 1e-11
+        print(f"[per-zone] config1 10 steps {n}: max {e:.3e} (delta {delta[n]:.3e}, bar {bar:.3e})")
+        assert e <= bar, (n, e, delta[n])
+    assert_bitwise(db["fail"], hb["fail"], "config1 fail")
+
+
+def _config3_blocks(oracle, p, nblocks=64):
+    hosts = states.uneven_blocks(nblocks, device=None)
+    for b in hosts:
+        oracle.Initialize(p, b)
+    return hosts
+
+
+@pytest.mark.parametrize("exact", [True, False])
+def test_config3_batched_vs_oracle(oracle, ctx_exact, ctx_fast, exact):
+    """Config 3's form against the oracle: 64 blocks of the {16, 32, 64}
+    mix with per-zone random states (log rho in [-4, 0], log P/rho in
+    [-3, 0], W in [1, 5], |B|^2/rho in [1e-3, 10]), MP5 + HLL, floors,
+    ceilings and c2p fixup on; one RK2 step as two phx_stage_batched calls
+    (persistent work-list launches replayed as CUDA graphs) against the
+    oracle's Stage block by block.  Exact build: bit for bit.  Production:
+    dU/dt per zone at 1e-12 of the local scale (before any con2prim); after
+    the first batched stage the primitives and conserved variables (which
+    floors and fixups rewrite from the primitives) within the spread the
+    con2prim tolerance allows, fail flags bit for bit."""
+    import torch
+
+    from tests.test_gpu_batched import params
+
+    ctx = ctx_exact if exact else ctx_fast
+    p = params(floors=True)
+    hosts = _config3_blocks(oracle, p)
+    sizes = sorted({b.nx[0] for b in hosts})
+    assert sizes == [16, 32, 64], sizes
+    devs = [h.to_device() for h in hosts]
+    dt = 0.2 * min(oracle.EstimateTimestepBlock(p, h, False) for h in hosts)
+    if not exact:
+        # the kernels' arithmetic before any con2prim: fluxes + FluxCT +
+        # divergence per zone at 1e-12 of the local scale
+        worst = 0.0
+        for n, (h, d) in enumerate(zip(hosts, devs)):
+            hh = h.to_host()
+            oracle.CalculateFluidSourceTerms(p, hh)
+            oracle.CalculateFluxes(p, hh)
+            oracle.FluxCT(p, hh)
+            oracle.FluxDivergence(p, hh)
+            dd = h.to_device()
+            ctx.CalculateFluidSourceTerms(p, dd)
+            ctx.CalculateFluxes(p, dd)
+            ctx.FluxCT(p, dd)
+            ctx.UpdateStage(dd, None, None, 1.0, 0.0)
+            isl = (slice(None),) + hh.isl()
+            sd = _dudt_scale(hh)
+            worst = max(worst, report_close(dd["dudt"].cpu().numpy()[isl], hh["dudt"][isl], sd[isl], 1e-12,
+                                            f"config3 block {n} ({h.nx[0]}^3) dU/dt"))
+        print(f"[per-zone] config3 dU/dt over 64 blocks: {worst:.3e}")
+    # stage 1 on both sides
+    h_base = [h["cons"].copy() for h in hosts]
+    h_out = [np.zeros_like(h["cons"]) for h in hosts]
+    tight = [h.to_host() for h in hosts] if not exact else None
+    d_out = [torch.zeros_like(d["cons"]) for d in devs]
+    ctx.StageBatched(p, devs, [d["cons"] for d in devs], d_out, 1.0, dt)
+    ctx.check()
+    for h, hb0, ho in zip(hosts, h_base, h_out):
+        oracle.Stage(p, h, hb0, ho, 1.0, dt)
+    if not exact:
+        # the spread the con2prim tolerance allows: the oracle's stage at
+        # tolerance 1e-14 from the same state (floors and fixups act on
+        # primitives, so the conserved outputs carry it too)
+        pt = params(floors=True)
+        pt.c2p_tol, pt.c2p_max_iter = 1e-14, 400
+        t_out = [np.zeros_like(h["cons"]) for h in hosts]
+        for t, tb, to in zip(tight, h_base, t_out):
+            oracle.Stage(pt, t, tb.copy(), to, 1.0, dt)
+        names = list(PRIM_VARS.items())
+        dmax = {n: 0.0 for n, _ in names}
+        emax = {n: 0.0 for n, _ in names}
+        cmax_d = cmax_e = 0.0
+        for h, t, d, ho, to, dd, hb0 in zip(hosts, tight, devs, h_out, t_out, d_out, h_base):
+            fl = prim_floors(h)
+            g = d["prim"].cpu().numpy()
+            for n, v in names:
+                dmax[n] = max(dmax[n], max_rel_floor(t["prim"][v], h["prim"][v], fl[v]))
+                emax[n] = max(emax[n], max_rel_floor(g[v], h["prim"][v], fl[v]))
+            cfl = np.abs(hb0) + dt * _dudt_scale(h)
+            cmax_d = max(cmax_d, max_rel_floor(to, ho, cfl))
+            cmax_e = max(cmax_e, max_rel_floor(dd.cpu().numpy(), ho, cfl))
+            assert_bitwise(d["fail"], h["fail"], "config3 fail after stage 1")
+        for n, _ in names:
+            bar = 2.5 * dmax[n] + 1e-11
+            print(f"[per-zone] config3 stage 1 {n}: max {emax[n]:.3e} (delta {dmax[n]:.3e}, bar {bar:.3e})")
+            assert emax[n] <= bar, (n, emax[n], dmax[n])
+        bar = 2.5 * cmax_d + 1e-11
+        print(f"[per-zone] config3 stage 1 cons: max {cmax_e:.3e} (delta {cmax_d:.3e}, bar {bar:.3e})")
+        assert cmax_e <= bar
+        return
+    for n, (h, d, ho, dd) in enumerate(zip(hosts, devs, h_out, d_out)):
+        assert_bitwise(dd, ho, f"block {n} cons after stage 1")
+        assert_bitwise(d["prim"], h["prim"], f"block {n} prim after stage 1")
+        assert_bitwise(d["fail"], h["fail"], f"block {n} fail after stage 1")
+    # stage 2 (exact build): the second batched call, then the whole step
+    d2 = []
+    from phoebus_gb300.block import Block
+
+    for d, dd in zip(devs, d_out):
+        c = Block(d.nx, d.ng, d.ndim, d.xmin, d.dx, backend="torch", device=dd.device, arrays=dict(d.arrays))
+        c.arrays["cons"] = dd
+        d2.append(c)
+    ctx.StageBatched(p, d2, [d["cons"] for d in devs], [d["cons"] for d in devs], 0.5, dt)
+    ctx.check()
+    for h, hb0, ho in zip(hosts, h_base, h_out):
+        h.arrays["cons"] = ho
+        oracle.Stage(p, h, hb0, hb0, 0.5, dt)
+        h.arrays["cons"] = hb0
+    for n, (h, d) in enumerate(zip(hosts, devs)):
+        for name in ("cons", "prim", "fail"):
+            assert_bitwise(d[name], h[name], f"block {n} {name} after the RK2 step")
