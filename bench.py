@@ -347,14 +347,18 @@ def bench_batched(ctx, args, dev, learned_ready=False):
     ctx.check()
     zones = sum(b.nx[0] * b.nx[1] * b.nx[2] for b in blocks)
     dt = 0.2 * min(ctx.EstimateTimestepBlock(p, b, False).item() for b in blocks)
-    snap = [(b["prim"].clone(), b["cons"].clone()) for b in blocks]
+    seconds = [torch.zeros_like(b["cons"]) for b in blocks]
+    # the stage inputs: prims, cons, and the second-stage buffers, whose ghost
+    # zones (from the previous step's exchange) the first con2prim of a stage
+    # reads, as the reference's does
+    snap = [(b["prim"].clone(), b["cons"].clone(), s2.clone()) for b, s2 in zip(blocks, seconds)]
 
     def restore():
-        for b, (pr, co) in zip(blocks, snap):
+        for b, s2, (pr, co, sc) in zip(blocks, seconds, snap):
             b["prim"].copy_(pr)
             b["cons"].copy_(co)
+            s2.copy_(sc)
 
-    seconds = [torch.zeros_like(b["cons"]) for b in blocks]
     bases = [b["cons"] for b in blocks]
     stage2 = []
     for b, s2 in zip(blocks, seconds):
@@ -463,12 +467,15 @@ def bench_torus(ctx, args, dev, learned_ready=False):
         rk.step(dt, learned=lrn, batched=batched)
 
     zones = mesh.n[0] * mesh.n[1] * mesh.n[2]
-    snap = [(b["prim"].clone(), b["cons"].clone()) for b in blocks]
+    # prims, cons and the second-stage buffers (their ghosts feed the first
+    # con2prim of a stage)
+    snap = [(b["prim"].clone(), b["cons"].clone(), s2.clone()) for b, s2 in zip(blocks, rk.seconds)]
 
     def restore():
-        for b, (pr, co) in zip(blocks, snap):
+        for b, s2, (pr, co, sc) in zip(blocks, rk.seconds, snap):
             b["prim"].copy_(pr)
             b["cons"].copy_(co)
+            s2.copy_(sc)
 
     k = args.torus_steps
     arms = [("batched", lambda: step(True, False), k)]

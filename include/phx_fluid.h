@@ -534,6 +534,39 @@ void phx_mlp_train_opts_default(phx_mlp_train_opts *o);
 phx_status phx_mlp_train(phx_ctx *ctx, long long n, const float *x, const float *y, const phx_mlp_train_opts *o,
                          float *epoch_loss, void *stream);
 
+/* ---- problem generator: the magnetised Fishbone-Moncrief torus --------- */
+typedef struct phx_torus_params {
+  double rin;               /* inner edge of the torus (torus/rin, 6)                */
+  double rmax;              /* radius of the pressure maximum (torus/rmax, 12)       */
+  double kappa;             /* polytropic constant (torus/kappa, 1e-2)               */
+  double u_jitter;          /* u *= 1 + u_jitter (U - 0.5) (torus/u_jitter, 1e-2)    */
+  double target_beta;       /* max P / max (b^2 / 2) after normalisation (100)       */
+  int magnetized;           /* torus/magnetized (1): 0 leaves B = 0                  */
+  unsigned long long seed;  /* counter seed of the noise draws U                     */
+} phx_torus_params;
+
+void phx_torus_params_default(phx_torus_params *tp);
+
+/* torus::ProblemGenerator (pgen/torus.cpp:130-474) on every block, then
+ * torus::PostInitializationModifier's HARM-style field normalisation
+ * (torus.cpp:525-740, ComputeBetas :844-924), for the ideal gas with
+ * nsub = 1 and no radiation or tracers.  Per block, over its entire index
+ * range: the Fishbone-Moncrief solution (torus.cpp:743-843) at the cell
+ * centres in FMKS coordinates, u^phi transformed BL -> FMKS, the pressure
+ * noise, the floors, T, P, gamma1; A_phi at the corners from the floored
+ * density and the poloidal field from it; PrimitiveToConserved and
+ * ApplyFloors.  Then the maxima of P and b^2 over all blocks' interiors give
+ * the field factor sqrt(beta_pmax / target_beta) (written to *field_factor,
+ * host, may be NULL), the interior field is scaled and PrimitiveToConserved
+ * runs again.  The blocks need FMKS geometry tables (phx_geometry_fill_fmks)
+ * and share one geometry.  U is a counter-based uniform (SplitMix64 of
+ * (seed, zone)), zones numbered block after block over the entire ranges (the
+ * reference's Kokkos pool is seeded by the clock).  Synchronises the stream
+ * once, for the maxima.  Blocks wider than 3 x 2^21 / 7 cells per (j, i)
+ * plane return PHX_ERR_CAPACITY. */
+phx_status phx_torus_init(phx_ctx *ctx, const phx_params *p, const phx_torus_params *tp,
+                          const phx_block *blocks, int nblocks, double *field_factor, void *stream);
+
 /* ---- the library's transcendental functions ----------------------------- */
 /* The FMKS geometry tables and the exponential floors evaluate exp, sin, cos
  * and pow written out from their series with IEEE operations only (no

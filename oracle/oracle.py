@@ -93,6 +93,8 @@ def lib(tuned: bool = False) -> C.CDLL:
             ("orc_rad_estimate_timestep", [RP, PP, BS, RB], C.c_double),
             ("orc_rad_tanh", [C.c_double], C.c_double),
             ("orc_math_eval", [C.c_int, C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p], None),
+            ("orc_torus_init", [PP, C.POINTER(abi.TorusParams), C.POINTER(abi.BlockS), C.c_int,
+                                C.POINTER(C.c_double)], None),
             ("orc_rad_m1_guess", [C.c_void_p] * 3 + [C.c_longlong] + [C.c_void_p] * 2, None),
         ]:
             fn = getattr(L, name)
@@ -232,6 +234,17 @@ class Oracle:
         self.L.orc_math_eval(abi.MATH[fn], x.size, x.ctypes.data, None if yy is None else yy.ctypes.data,
                              out.ctypes.data)
         return out
+
+    def TorusInit(self, p, tp, blocks) -> float:
+        """pgen/torus.cpp's ProblemGenerator on every block and the field
+        normalisation of PostInitializationModifier; returns the factor."""
+        arr = (abi.BlockS * len(blocks))(*[b.struct() for b in blocks])
+        # the structs point at each block's geometry struct: keep them alive
+        keep = [b._gstruct for b in blocks]
+        fac = C.c_double()
+        self.L.orc_torus_init(C.byref(p), C.byref(tp), arr, len(blocks), C.byref(fac))
+        del keep
+        return fac.value
 
     def fmks_points(self, g, x1, x2):
         n = x1.shape[0]

@@ -1918,6 +1918,300 @@ long long orc_apply_floors(const phx_params *par, const phx_block *blk, phx_rang
 
 }  // extern "C"
 
+// ---------------------------------------------------------------------
+// The magnetised Fishbone-Moncrief torus (pgen/torus.cpp, ideal gas, nsub =
+// 1, no radiation, no tracers), restated from the reference's loops.
+namespace torus {
+
+// torus.cpp:743-754
+Real lfish_calc(Real r, Real a) {
+  using phx_math::pow;
+  return (((pow(a, 2) - 2. * a * std::sqrt(r) + pow(r, 2)) *
+           ((-2. * a * r * (pow(a, 2) - 2. * a * std::sqrt(r) + pow(r, 2))) /
+                std::sqrt(2. * a * std::sqrt(r) + (-3. + r) * r) +
+            ((a + (-2. + r) * std::sqrt(r)) * (pow(r, 3) + pow(a, 2) * (2. + r))) /
+                std::sqrt(1 + (2. * a) / pow(r, 1.5) - 3. / r))) /
+          (pow(r, 3) * std::sqrt(2. * a * std::sqrt(r) + (-3. + r) * r) * (pow(a, 2) + (-2. + r) * r)));
+}
+
+// torus.cpp:756-793
+Real log_enthalpy(Real r, Real th, Real a, Real rin, Real l, Real &uphi) {
+  const Real sth = phx_math::sin(th);
+  const Real cth = phx_math::cos(th);
+  const Real DD = r * r - 2. * r + a * a;
+  const Real AA = (r * r + a * a) * (r * r + a * a) - DD * a * a * sth * sth;
+  const Real SS = r * r + a * a * cth * cth;
+  const Real thin = M_PI / 2.;
+  const Real sthin = phx_math::sin(thin);
+  const Real cthin = phx_math::cos(thin);
+  const Real DDin = rin * rin - 2. * rin + a * a;
+  const Real AAin = (rin * rin + a * a) * (rin * rin + a * a) - DDin * a * a * sthin * sthin;
+  const Real SSin = rin * rin + a * a * cthin * cthin;
+  uphi = 0.0;
+  const Real lnh =
+      0.5 * phx_math::log((1. + std::sqrt(1. + 4. * (l * l * SS * SS) * DD / (AA * AA * sth * sth))) /
+                          (SS * DD / AA)) -
+      0.5 * std::sqrt(1. + 4. * (l * l * SS * SS) * DD / (AA * AA * sth * sth)) - 2. * a * r * l / AA -
+      (0.5 * phx_math::log((1. + std::sqrt(1. + 4. * (l * l * SSin * SSin) * DDin /
+                                                (AAin * AAin * sthin * sthin))) /
+                           (SSin * DDin / AAin)) -
+       0.5 * std::sqrt(1. + 4. * (l * l * SSin * SSin) * DDin / (AAin * AAin * sthin * sthin)) -
+       2. * a * rin * l / AAin);
+  if (lnh > 0.0) {
+    Real expm2chi = SS * SS * DD / (AA * AA * sth * sth);
+    Real up1 = std::sqrt((-1. + std::sqrt(1. + 4. * l * l * expm2chi)) / 2.);
+    uphi = 2. * a * r * std::sqrt(1. + up1 * up1) / std::sqrt(AA * SS * DD) + std::sqrt(SS / AA) * up1 / sth;
+  }
+  return lnh;
+}
+
+// torus.cpp:799-829, the IdealGas branch
+void GetStateFromEnthalpy(Real hm1, Real kappa, Real gam, Real rho_rmax, Real &rho_out, Real &u_out) {
+  rho_out = phx_math::pow(hm1 * (gam - 1.) / (kappa * gam), 1. / (gam - 1.));
+  u_out = kappa * phx_math::pow(rho_out, gam) / (gam - 1.) / rho_rmax;
+  rho_out /= rho_rmax;
+}
+
+// torus.cpp:831-843
+Real ucon_norm(Real ucon[4], Real gcov[4][4]) {
+  Real AA = gcov[0][0];
+  Real BB = 2. * (gcov[0][1] * ucon[1] + gcov[0][2] * ucon[2] + gcov[0][3] * ucon[3]);
+  Real CC = 1. + gcov[1][1] * ucon[1] * ucon[1] + gcov[2][2] * ucon[2] * ucon[2] +
+            gcov[3][3] * ucon[3] * ucon[3] +
+            2. * (gcov[1][2] * ucon[1] * ucon[2] + gcov[1][3] * ucon[1] * ucon[3] + gcov[2][3] * ucon[2] * ucon[3]);
+  Real discr = BB * BB - 4. * AA * CC;
+  return (-BB - std::sqrt(discr)) / (2. * AA);
+}
+
+// Geometry::BoyerLindquist::SpacetimeMetric (boyer_lindquist.hpp:77-95, 262-280)
+void bl_spacetime_metric(Real a_, Real X1, Real X2, Real g[4][4]) {
+  const Real a2_ = a_ * a_;
+  const Real r = std::abs(X1);
+  const Real th = X2;
+  const Real sth = phx_math::sin(th);
+  const Real cth = phx_math::cos(th);
+  const Real r2 = r * r;
+  const Real r3 = r2 * r;
+  const Real DD = 1. - ratio(2., r) + ratio(a2_, r2);
+  const Real mu = 1. + ratio(a2_ * cth * cth, r2);
+  const Real sth2 = sth * sth;
+  for (int m = 0; m < 4; m++)
+    for (int n = 0; n < 4; n++) g[m][n] = 0;
+  g[0][0] = -(1.0 - ratio(2.0, r * mu));
+  g[0][3] = g[3][0] = -ratio(2.0 * a_ * sth2, r * mu);
+  g[1][1] = mu / DD;
+  g[2][2] = r2 * mu;
+  g[3][3] = r2 * sth2 * (1.0 + ratio(a2_, r2) + ratio(2.0 * a2_ * sth2, r3 * mu));
+}
+
+// McKinneyGammieRyan::bl_to_ks, bl_to_fmks (mckinney_gammie_ryan.hpp:119-151)
+void bl_to_fmks(const FMKS &f, Real x1, Real x2, Real x3, Real a, Real *ucon_bl, Real *ucon_fmks) {
+  Real trans[4][4];
+  for (int m = 0; m < 4; m++)
+    for (int n = 0; n < 4; n++) trans[m][n] = 0;
+  const Real r = f.r_(x1);
+  const Real idenom = 1.0 / (r * r - 2.0 * r + a * a);
+  trans[0][0] = 1.0;
+  trans[0][1] = 2.0 * r * idenom;
+  trans[1][1] = 1.0;
+  trans[2][2] = 1.0;
+  trans[3][1] = a * idenom;
+  trans[3][3] = 1.0;
+  Real ucon_ks[4] = {0, 0, 0, 0};
+  for (int mu = 0; mu < 4; mu++)
+    for (int nu = 0; nu < 4; nu++) ucon_ks[mu] += trans[mu][nu] * ucon_bl[nu];
+  Real c[3], Jcov[3][3], Jcon[3][3];
+  f.transform(x1, x2, x3, c, Jcov, Jcon);
+  for (int m = 0; m < 4; m++)
+    for (int n = 0; n < 4; n++) trans[m][n] = 0;
+  trans[0][0] = 1.0;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) trans[i + 1][j + 1] = Jcon[i][j];
+  for (int mu = 0; mu < 4; mu++) ucon_fmks[mu] = 0;
+  for (int mu = 0; mu < 4; mu++)
+    for (int nu = 0; nu < 4; nu++) ucon_fmks[mu] += trans[mu][nu] * ucon_ks[nu];
+}
+
+// The noise U: SplitMix64 of the counter (seed, stream 0, idx), 53 bits
+Real uniform(unsigned long long seed, unsigned long long idx) {
+  uint64_t z = (uint64_t)seed * 0x100000001B3ull;
+  z += (uint64_t)(idx + 1ull) * 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z = z ^ (z >> 31);
+  return (Real)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+// ProblemGenerator (torus.cpp:130-474) for one block; noise0 = the counter of
+// its first zone
+void ProblemGenerator(const phx_params &par, const phx_torus_params &tp, const phx_block *blk,
+                      unsigned long long noise0) {
+  Blk B(blk);
+  Geom G(blk->geom, &B);
+  FMKS tr(*blk->geom);
+  EOS eos{par.gm1, par.Cv};
+  Bounds floor(par);
+  const Real gam = par.gm1 + 1.0, Cv = par.Cv;
+  const Real rin = tp.rin, rmax = tp.rmax, kappa = tp.kappa, u_jitter = tp.u_jitter;
+  const Real a = blk->geom->a;
+  const int nsub = 1;
+  const Real angular_mom = lfish_calc(rmax, a);
+  Real uphi_rmax;
+  const Real hm1_rmax = phx_math::exp(log_enthalpy(rmax, 0.5 * M_PI, a, rin, angular_mom, uphi_rmax)) - 1.0;
+  Real rho_rmax, u_rmax;
+  GetStateFromEnthalpy(hm1_rmax, kappa, gam, 1.0, rho_rmax, u_rmax);
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int k = 0; k < B.n3t; k++)
+    for (int j = 0; j < B.n2t; j++)
+      for (int i = 0; i < B.n1t; i++) {
+        const Real dx_sub = B.dx(1) / nsub;
+        const Real dy_sub = B.dx(2) / nsub;
+        B.P(PHX_PRHO, k, j, i) = 0.0;
+        B.P(PHX_PENG, k, j, i) = 0.0;
+        for (int d = 0; d < 3; d++) B.P(PHX_PVEL + d, k, j, i) = 0.0;
+        const Real x3 = B.Xc(3, k);
+        for (int m = 0; m < nsub; m++) {
+          for (int n = 0; n < nsub; n++) {
+            const Real x1 = B.Xf(1, i) + (m + 0.5) * dx_sub;
+            const Real x2 = B.Xf(2, j) + (n + 0.5) * dy_sub;
+            Real r = tr.r_(x1);
+            Real yy, th;
+            tr.th_(x1, x2, yy, th);
+            Real lnh = -1.0;
+            Real uphi;
+            if (r > rin) lnh = log_enthalpy(r, th, a, rin, angular_mom, uphi);
+            if (lnh > 0.0) {
+              Real hm1 = phx_math::exp(lnh) - 1.;
+              Real rho, u;
+              GetStateFromEnthalpy(hm1, kappa, gam, rho_rmax, rho, u);
+              Real ucon_bl[] = {0.0, 0.0, 0.0, uphi};
+              Real gcov[4][4];
+              bl_spacetime_metric(a, r, th, gcov);
+              ucon_bl[0] = ucon_norm(ucon_bl, gcov);
+              Real ucon[4];
+              bl_to_fmks(tr, x1, x2, x3, a, ucon_bl, ucon);
+              const Real lapse = tr.Lapse(x1, x2, x3);
+              Real beta[3];
+              tr.Shift(x1, x2, x3, beta);
+              tr.SpacetimeMetric(x1, x2, x3, gcov);
+              ucon[0] = ucon_norm(ucon, gcov);
+              const Real W = lapse * ucon[0];
+              Real vcon[] = {ucon[1] / W + beta[0] / lapse, ucon[2] / W + beta[1] / lapse,
+                             ucon[3] / W + beta[2] / lapse};
+              B.P(PHX_PRHO, k, j, i) += rho / (nsub * nsub);
+              B.P(PHX_PENG, k, j, i) += u / (nsub * nsub);
+              for (int d = 0; d < 3; d++) B.P(PHX_PVEL + d, k, j, i) += W * vcon[d] / (nsub * nsub);
+            }
+          }
+        }
+        const Real x1v = B.Xc(1, i);
+        const Real x2v = B.Xc(2, j);
+        B.P(PHX_PENG, k, j, i) *= (1. + u_jitter * (uniform(tp.seed, noise0 + (unsigned long long)B.idx(k, j, i)) - 0.5));
+        Real rhoflr = 0;
+        Real epsflr;
+        floor.GetFloors(x1v, x2v, x3, rhoflr, epsflr);
+        B.P(PHX_PRHO, k, j, i) = B.P(PHX_PRHO, k, j, i) < rhoflr ? rhoflr : B.P(PHX_PRHO, k, j, i);
+        B.P(PHX_PENG, k, j, i) = B.P(PHX_PENG, k, j, i) / B.P(PHX_PRHO, k, j, i) < epsflr
+                                     ? B.P(PHX_PRHO, k, j, i) * epsflr
+                                     : B.P(PHX_PENG, k, j, i);
+        B.P(PHX_PTMP, k, j, i) =
+            eos.TemperatureFromDensityInternalEnergy(B.P(PHX_PRHO, k, j, i), B.P(PHX_PENG, k, j, i) / B.P(PHX_PRHO, k, j, i));
+        B.P(PHX_PPRS, k, j, i) = eos.PressureFromDensityTemperature(B.P(PHX_PRHO, k, j, i), B.P(PHX_PTMP, k, j, i));
+        B.P(PHX_PGM1, k, j, i) =
+            eos.BulkModulusFromDensityTemperature(B.P(PHX_PRHO, k, j, i), B.P(PHX_PTMP, k, j, i)) /
+            B.P(PHX_PPRS, k, j, i);
+        for (int d = 0; d < 3; d++) B.P(PHX_PB + d, k, j, i) = 0.0;  // Parthenon's zero-initialised field
+        B.P(PHX_PMU, k, j, i) = 0.0;
+      }
+  (void)Cv;
+  // the vector potential at the corners (torus.cpp:452-470), from the k = kb.s plane
+  std::vector<Real> A((size_t)B.n2t * B.n1t, 0.0);
+  for (int j = 1; j <= B.n2t - 1; j++)
+    for (int i = 1; i <= B.n1t - 1; i++) {
+      const Real rho_av = 0.25 * (B.P(PHX_PRHO, 0, j, i) + B.P(PHX_PRHO, 0, j, i - 1) + B.P(PHX_PRHO, 0, j - 1, i) +
+                                  B.P(PHX_PRHO, 0, j - 1, i - 1));
+      const Real q = rho_av - 0.2;
+      A[(size_t)j * B.n1t + i] = (q > 0 ? q : 0.0);
+    }
+  auto Aij = [&](int j, int i) { return A[(size_t)j * B.n1t + i]; };
+  // the poloidal field (torus.cpp:472-488)
+  for (int k = 0; k < B.n3t; k++)
+    for (int j = 0; j <= B.n2t - 2; j++)
+      for (int i = 0; i <= B.n1t - 2; i++) {
+        GeomPt g;
+        G.at(CENT, k, j, i, g);
+        const Real gamdet = g.detgam;
+        B.P(PHX_PB, k, j, i) =
+            -(Aij(j, i) - Aij(j + 1, i) + Aij(j, i + 1) - Aij(j + 1, i + 1)) / (2.0 * B.dx(2) * gamdet);
+        B.P(PHX_PB + 1, k, j, i) =
+            (Aij(j, i) + Aij(j + 1, i) - Aij(j, i + 1) - Aij(j + 1, i + 1)) / (2.0 * B.dx(1) * gamdet);
+        B.P(PHX_PB + 2, k, j, i) = 0.0;
+      }
+}
+
+}  // namespace torus
+
+extern "C" {
+
+// ProblemGenerator on every block, then PostInitializationModifier's
+// HARM-style normalisation (torus.cpp:525-740, ComputeBetas :844-924).
+void orc_torus_init(const phx_params *par, const phx_torus_params *tp, phx_block *blocks, int nblocks,
+                    double *field_factor) {
+  unsigned long long noise0 = 0;
+  for (int q = 0; q < nblocks; q++) {
+    Blk B(&blocks[q]);
+    torus::ProblemGenerator(*par, *tp, &blocks[q], noise0);
+    const phx_range ib{0, B.n1t - 1}, jb{0, B.n2t - 1}, kb{0, B.n3t - 1};
+    orc_prim_to_con(par, &blocks[q], ib, jb, kb);
+    apply_floors(*par, &blocks[q], ib, jb, kb);
+    noise0 += (unsigned long long)B.N;
+  }
+  Real bsq_max = -std::numeric_limits<Real>::infinity();
+  Real press_max = -std::numeric_limits<Real>::infinity();
+  for (int q = 0; q < nblocks; q++) {
+    Blk B(&blocks[q]);
+    Geom G(blocks[q].geom, &B);
+    for (int k = B.ks(); k <= B.ke(); k++)
+      for (int j = B.js(); j <= B.je(); j++)
+        for (int i = B.is(); i <= B.ie(); i++) {
+          GeomPt g;
+          G.at(CENT, k, j, i, g);
+          Real gcov[3][3];
+          for (int m = 0; m < 3; m++)
+            for (int n = 0; n < 3; n++) gcov[m][n] = g.gcov[m + 1][n + 1];
+          const Real vp[] = {B.P(PHX_PVEL, k, j, i), B.P(PHX_PVEL + 1, k, j, i), B.P(PHX_PVEL + 2, k, j, i)};
+          const Real Bp[] = {B.P(PHX_PB, k, j, i), B.P(PHX_PB + 1, k, j, i), B.P(PHX_PB + 2, k, j, i)};
+          // GetLorentzFactor and GetMagneticFieldSquared (relativity_utils.hpp:38-43, 131-164)
+          Real vsq = 0.;
+          for (int m = 0; m < 3; m++)
+            for (int n = 0; n < 3; n++) vsq += gcov[m][n] * vp[m] * vp[n];
+          const Real W = std::sqrt(1. + vsq);
+          Real Bsq = 0, Bdotv = 0;
+          for (int m = 0; m < 3; m++)
+            for (int n = 0; n < 3; n++) {
+              Bdotv += gcov[m][n] * ratio(vp[m], W) * Bp[n];
+              Bsq += gcov[m][n] * Bp[m] * Bp[n];
+            }
+          const Real bsq = ratio(Bsq, W * W) + Bdotv * Bdotv;
+          bsq_max = std::max(bsq, bsq_max);
+          press_max = std::max(B.P(PHX_PPRS, k, j, i), press_max);
+        }
+  }
+  const Real beta_pmax = ratio(press_max, 0.5 * bsq_max);
+  const Real B_field_fac = tp->magnetized ? std::sqrt(beta_pmax / tp->target_beta) : 0;
+  for (int q = 0; q < nblocks; q++) {
+    Blk B(&blocks[q]);
+    for (int k = B.ks(); k <= B.ke(); k++)
+      for (int j = B.js(); j <= B.je(); j++)
+        for (int i = B.is(); i <= B.ie(); i++)
+          for (int d = 0; d < 3; d++) B.P(PHX_PB + d, k, j, i) *= B_field_fac;
+    orc_prim_to_con(par, &blocks[q], phx_range{0, B.n1t - 1}, phx_range{0, B.n2t - 1}, phx_range{0, B.n3t - 1});
+  }
+  if (field_factor) *field_factor = B_field_fac;
+}
+
+}  // extern "C"
+
 // =====================================================================
 // Radiation moments (M1 and Eddington closures), Minkowski, one species,
 // static fluid background.  Restates radiation/closure.hpp:49-352,

@@ -45,6 +45,11 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "con2prim root not bracketed", 3: "
           7: "request exceeds a fixed capacity", 8: "unsupported"}
 
 
+class TorusParams(C.Structure):
+    _fields_ = [("rin", C.c_double), ("rmax", C.c_double), ("kappa", C.c_double), ("u_jitter", C.c_double),
+                ("target_beta", C.c_double), ("magnetized", C.c_int), ("seed", C.c_ulonglong)]
+
+
 class Range(C.Structure):
     _fields_ = [("s", C.c_int), ("e", C.c_int)]
 
@@ -198,6 +203,9 @@ _SIGS = {
     "phx_mlp_set_input_box": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "phx_mlp_get_input_box": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "phx_math_eval": (C.c_int, [C.c_int, C.c_longlong, _P, _P, _P, _P]),
+    "phx_torus_params_default": (None, [C.POINTER(TorusParams)]),
+    "phx_torus_init": (C.c_int, [_P, C.POINTER(Params), C.POINTER(TorusParams), C.POINTER(BlockS), C.c_int,
+                                 C.POINTER(C.c_double), _P]),
     "phx_probe_fp64_peak": (C.c_int, [_P, C.POINTER(C.c_double)]),
 }
 
@@ -265,6 +273,16 @@ def default_geometry(kind: int, **over) -> Geometry:
     for k, v in over.items():
         setattr(g, k, v)
     return g
+
+
+def default_torus_params(**over) -> TorusParams:
+    """phx_torus_params_default (torus.cpp:174-181, 525-530 defaults), then
+    overrides."""
+    t = TorusParams()
+    t.rin, t.rmax, t.kappa, t.u_jitter, t.target_beta, t.magnetized, t.seed = 6.0, 12.0, 1e-2, 1e-2, 100.0, 1, 0
+    for k, v in over.items():
+        setattr(t, k, v)
+    return t
 
 
 def default_rad_params(**over) -> RadParams:

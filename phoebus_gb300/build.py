@@ -23,15 +23,17 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 LIB = PKG / "_lib"
 OBJ = PKG / "_build"
-SOURCES = ["phx_api.cu", "phx_c2p.cu", "phx_flux.cu", "phx_stage.cu", "phx_geometry.cu", "phx_mlp.cu", "phx_noalloc.cu", "phx_fixup.cu", "phx_batch.cu", "phx_m1.cu"]
+SOURCES = ["phx_api.cu", "phx_c2p.cu", "phx_flux.cu", "phx_stage.cu", "phx_geometry.cu", "phx_mlp.cu", "phx_noalloc.cu",
+           "phx_fixup.cu", "phx_batch.cu", "phx_m1.cu", "phx_torus.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAVOURS = {
     "libphx_fluid.so": ["-fmad=true"],
     "libphx_fluid_exact.so": ["-fmad=false", "-DPHX_EXACT"],
 }
 # Sources compiled without contraction in both flavours: the FMKS geometry
-# tables (built once per block) equal the oracle's bit for bit in both.
-NO_CONTRACT = {"phx_geometry.cu"}
+# tables (built once per block) and the torus initial state equal the
+# oracle's bit for bit in both.
+NO_CONTRACT = {"phx_geometry.cu", "phx_torus.cu"}
 
 
 def nvcc() -> str:
@@ -61,8 +63,11 @@ def build_cuda(force: bool = False, verbose: bool = False, jobs: int | None = No
     headers = sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + [ROOT / "include" / "phx_fluid.h",
                                                                        ROOT / "include" / "phx_radiation.h"]
     tool = nvcc()
-    common = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-                     "-I", str(ROOT / "include")]
+    # host code without contraction too: host-side constants (FMKS norm and
+    # step, the torus' density scale) then equal the oracle's on aarch64,
+    # where the host compiler would otherwise fuse multiply-adds
+    common = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+                     "--expt-relaxed-constexpr", "-I", str(ROOT / "include")]
     jobs_list = []
     for lib, extra in FLAVOURS.items():
         tag = "exact" if "exact" in lib else "fast"

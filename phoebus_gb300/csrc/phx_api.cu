@@ -25,6 +25,7 @@ struct phx_ctx {
   float *mlp_loss;             // device per-epoch loss sums [PHX_MLP_MAX_EPOCHS]
   phx::MlpPacked *mlp_packed;  // device BF16 fragments for inference (and the input box)
   int *mlp_boxkeys;            // device scratch of the input-box reduction [12]
+  unsigned long long *red;     // device scratch of mesh-wide maxima [2]
   phx::C2PScratch c2p;         // device con2prim chunk scratch (brackets, retry list)
   void *c2p_mem;               // its single allocation
   long long mlp_step;          // AdamW step count
@@ -318,6 +319,7 @@ phx_status phx_ctx_create(int device, phx_ctx **out) {
       cudaMalloc(&c->mlp_loss, sizeof(float) * PHX_MLP_MAX_EPOCHS) != cudaSuccess ||
       cudaMalloc(&c->mlp_packed, sizeof(phx::MlpPacked)) != cudaSuccess ||
       cudaMalloc(&c->mlp_boxkeys, sizeof(int) * 2 * PHX_MLP_IN) != cudaSuccess ||
+      cudaMalloc(&c->red, sizeof(unsigned long long) * 2) != cudaSuccess ||
       cudaMalloc(&c->c2p_mem, c2p_scratch_bytes()) != cudaSuccess) {
     phx_status s = cuda_status("cudaMalloc");
     phx_ctx_destroy(c);
@@ -355,6 +357,7 @@ phx_status phx_ctx_destroy(phx_ctx *ctx) {
   cudaFree(ctx->mlp_loss);
   cudaFree(ctx->mlp_packed);
   cudaFree(ctx->mlp_boxkeys);
+  cudaFree(ctx->red);
   cudaFree(ctx->c2p_mem);
   if (ctx->batch) phx::batch_cache_destroy(ctx->batch);
   delete ctx;
@@ -928,6 +931,46 @@ phx_status phx_mlp_get_weights(phx_ctx *ctx, float *params_host) {
   if (!params_host) return fail(PHX_ERR_INVALID_ARG, "params is NULL");
   if (cudaMemcpy(params_host, ctx->mlp_w, sizeof(float) * PHX_MLP_NPARAM, cudaMemcpyDeviceToHost) != cudaSuccess)
     return cuda_status("mlp weights");
+  return PHX_OK;
+}
+
+void phx_torus_params_default(phx_torus_params *tp) {
+  if (!tp) return;
+  tp->rin = 6.0;
+  tp->rmax = 12.0;
+  tp->kappa = 1.e-2;
+  tp->u_jitter = 1.e-2;
+  tp->target_beta = 100.;
+  tp->magnetized = 1;
+  tp->seed = 0;
+}
+
+phx_status phx_torus_init(phx_ctx *ctx, const phx_params *p, const phx_torus_params *tp, const phx_block *blocks,
+                          int nblocks, double *field_factor, void *stream) {
+  phx_status s;
+  if ((s = ctx_device(ctx)) || (s = check_params(p))) return s;
+  if (!tp || !blocks || nblocks <= 0) return fail(PHX_ERR_INVALID_ARG, "phx_torus_init: params and blocks required");
+  if (!(tp->rmax > tp->rin) || !(tp->kappa > 0) || !(tp->target_beta > 0))
+    return fail(PHX_ERR_INVALID_ARG, "phx_torus_init: need rmax > rin, kappa > 0, target_beta > 0");
+  std::vector<phx::BView> v(nblocks);
+  const phx_geometry *g0 = blocks[0].geom;
+  for (int q = 0; q < nblocks; q++) {
+    if ((s = make_view(&blocks[q], v[q]))) return s;
+    const phx_geometry *g = blocks[q].geom;
+    if (!v[q].fmks || !g) return fail(PHX_ERR_INVALID_ARG, "phx_torus_init: block %d has no FMKS tables", q);
+    if (g->a != g0->a || g->hslope != g0->hslope || g->poly_xt != g0->poly_xt || g->poly_alpha != g0->poly_alpha ||
+        g->x0 != g0->x0 || g->smooth != g0->smooth || g->hexp_br != g0->hexp_br || g->hexp_nsq != g0->hexp_nsq ||
+        g->hexp_csq != g0->hexp_csq || g->derefine_poles != g0->derefine_poles)
+      return fail(PHX_ERR_INVALID_ARG, "phx_torus_init: blocks must share one geometry");
+    if ((long long)phx::TORUS_PLANE_VARS * v[q].n1t * v[q].n2t > 3 * phx::C2P_CHUNK)
+      return fail(PHX_ERR_CAPACITY, "phx_torus_init: block %d's (j, i) plane is too large for the scratch", q);
+    if (!blocks[q].fail) return fail(PHX_ERR_INVALID_ARG, "phx_torus_init: fail field required (ApplyFloors)");
+  }
+  double fac = 0.0;
+  cudaError_t e = phx::torus_init(make_par(*p), *g0, *tp, v.data(), nblocks, ctx->c2p.brk, ctx->red, ctx->stats,
+                                  ctx->err, &fac, S(stream));
+  if (e != cudaSuccess) return fail(PHX_ERR_CUDA, "phx_torus_init: %s", cudaGetErrorString(e));
+  if (field_factor) *field_factor = fac;
   return PHX_OK;
 }
 

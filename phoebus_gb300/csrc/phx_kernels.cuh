@@ -62,6 +62,13 @@ void launch_geom_fmks(const phx_geometry &g, const BView &b, cudaStream_t s);
 void launch_geom_points(const phx_geometry &g, long long n, const double *x1, const double *x2, double *geom,
                         cudaStream_t s);
 void launch_math_eval(int fn, long long n, const double *x, const double *y, double *out, cudaStream_t s);
+// The torus problem generator and its field normalisation (phx_torus.cu) over
+// the blocks of a mesh: scratch holds 7 x n1t x n2t doubles of the largest
+// block, red 2 words; synchronises s once (the mesh-wide maxima).
+constexpr int TORUS_PLANE_VARS = 7;
+cudaError_t torus_init(const Par &p, const phx_geometry &g, const phx_torus_params &tp, const BView *views, int n,
+                       double *scratch, unsigned long long *red, DevStats *stats, unsigned int *err, double *fac_out,
+                       cudaStream_t s);
 void launch_p2c_zones(const Par &p, long long n, const double *prim, const double *geom, double *cons,
                       double *cell_sig, cudaStream_t s);
 void launch_c2p_zones(const Par &p, long long n, double *cons, double *prim, const double *geom, double *fail,

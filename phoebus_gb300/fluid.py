@@ -256,6 +256,15 @@ class FluidContext:
         self._ok(self.lib.phx_apply_floors(self.h, C.byref(p), C.byref(s), _rng(ib), _rng(jb), _rng(kb),
                                            _stream(stream)))
 
+    def TorusInit(self, p: abi.Params, tp: abi.TorusParams, blocks, stream=None) -> float:
+        """The torus problem generator on every block and the field
+        normalisation (phx_torus_init); returns the field factor."""
+        arr = (abi.BlockS * len(blocks))(*[b.struct() for b in blocks])
+        fac = C.c_double()
+        self._ok(self.lib.phx_torus_init(self.h, C.byref(p), C.byref(tp), arr, len(blocks), C.byref(fac),
+                                         _stream(stream)))
+        return fac.value
+
     def GeometryFillFMKS(self, b: Block, stream=None):
         assert b.geom is not None
         g = b.geom.struct()

@@ -87,16 +87,12 @@ def test_stage_with_fixup_and_floors(oracle, ctx_exact):
     assert_bitwise(db["fail"], hb["fail"], "stage fail")
 
 
-def test_apply_floors_expx1_tolerance(oracle, ctx_exact):
-    """Each side runs prim2con, con2prim and ApplyFloors from the same
-    primitives, so its con2prim floor clamp and its ApplyFloors use the same
-    exp(); the two sides' floors differ by an ulp at most.  Floored zones are
-    re-inverted by con2prim (tolerance 1e-10 on mu), where an ulp-level
-    change of the floor can change the root finder's path, so their
-    primitives agree to the con2prim tolerance (1e-8 after conditioning),
-    as in the production-build con2prim test."""
-    from tests.util import assert_close
-
+def test_apply_floors_expx1_exact(oracle, ctx_exact):
+    """ExpX1RhoSie floors (rho0 e^{-2 x1}-type exponentials): each side runs
+    prim2con, con2prim and ApplyFloors from the same primitives.  The floors'
+    exp is the library's written-out one, which the oracle evaluates too, so
+    the floored state is bit for bit the oracle's (more than a fifth of the
+    zones are floored)."""
     p = _params(floor_type="ExpX1RhoSie", rho0_floor=2e-3, sie0_floor=1e-2)
     hb = states.random_block(10, 64)
     hb.xmin = (-1.0, -1.0, -1.0)
@@ -109,9 +105,5 @@ def test_apply_floors_expx1_tolerance(oracle, ctx_exact):
         side.ApplyFloors(p, blk)
     ctx_exact.check()
     assert (~np.all(before["prim"] == hb["prim"], axis=0)).mean() > 0.2
-    assert_bitwise(db["fail"], hb["fail"], "fail")
-    got = db["prim"].cpu().numpy()
-    for v in (abi.PRHO, abi.PENG, abi.PPRS, abi.PVEL, abi.PVEL + 1, abi.PVEL + 2):
-        assert_close(got[v], hb["prim"][v], 1e-8, f"prim {v}", floor=0.0)
-    for m in range(5):
-        assert_close(db["cons"][m].cpu().numpy(), hb["cons"][m], 1e-8, f"cons {m}")
+    for name in ("fail", "prim", "cons"):
+        assert_bitwise(db[name], hb[name], name)

@@ -1,37 +1,35 @@
 """GPU parity on the FMKS (Kerr-Schild) path and on the 2D linear-modes run.
 
 FMKS geometry is read from tables (the reference's cached, axisymmetric
-geometry).  The tables built on the GPU use CUDA's libm for exp/sin/cos/pow
-and so agree with the oracle's glibc tables to rounding (and the
-finite-difference derivatives to rounding / step size); given the SAME tables
-the hot path is bit-identical in the exact build.
+geometry).  The tables call exp, sin, cos and pow, which the GPU and the
+oracle both evaluate through phoebus_gb300/csrc/phx_math.h with the same IEEE
+operations, and the table kernels are compiled without contraction in both
+library builds: the tables built on the GPU equal the oracle's bit for bit,
+finite-difference derivatives included, and so do the hot-path tasks that
+read them.
 """
 import numpy as np
 import pytest
 
 from phoebus_gb300 import abi, states
-from tests.util import assert_bitwise, assert_close, face_region, flux_view
+from tests.util import assert_bitwise, face_region, flux_view, report_close
 
 pytestmark = pytest.mark.gpu
 
 
+@pytest.mark.parametrize("exact", [True, False])
 @pytest.mark.parametrize("derefine", [0, 1])
-def test_fmks_tables(oracle, ctx_exact, derefine):
-    """GPU tables vs the oracle's: libm differences of an ulp, amplified where
-    theta = thG + e (thJ - thG) cancels near the pole (derefined poles, ghost
-    zones at X2 < 0), stay below 1e-10 of each variable's scale; the
-    finite-difference derivatives (step eps^(1/3) max(|X|, 1)) below 1e-9."""
+def test_fmks_tables(oracle, ctx_exact, ctx_fast, derefine, exact):
+    """GPU tables (both builds) equal the oracle's bit for bit: centre and
+    face tables and the finite-difference derivatives, pole derefinement on
+    and off (ghost zones at X2 < 0 and > 1 included)."""
+    ctx = ctx_exact if exact else ctx_fast
     hb = states.fmks_random_block(derefine_poles=derefine)
     db = hb.to_device()
     oracle.GeometryFillFMKS(hb)
-    ctx_exact.GeometryFillFMKS(db)
-    for name in ("cent", "face1", "face2"):
-        g, r = db.geom.arrays[name].cpu().numpy(), hb.geom.arrays[name]
-        for v in range(abi.GEOM_NLOC):
-            assert_close(g[v], r[v], 1e-10, f"{name}[{v}]")
-    g, r = db.geom.arrays["deriv"].cpu().numpy(), hb.geom.arrays["deriv"]
-    for v in range(abi.GEOM_NDER):
-        assert_close(g[v], r[v], 1e-9, f"deriv[{v}]")
+    ctx.GeometryFillFMKS(db)
+    for name in ("cent", "face1", "face2", "deriv"):
+        assert_bitwise(db.geom.arrays[name], hb.geom.arrays[name], f"{name} table")
 
 
 def _shared_tables(oracle, hb):
@@ -66,20 +64,23 @@ def test_fmks_hot_path_exact(oracle, ctx_exact):
 
 
 def test_fmks_sources_fast(oracle, ctx_fast):
-    """Production build: sources within 1e-12 relative (per-variable floor)."""
+    """Production build on tables it built itself: sources per zone within
+    1e-12 of the zone's source scale (|S_t| + |S_r| + |S_theta| + |tau|
+    source magnitudes; S_phi vanishes analytically in axisymmetric Kerr and
+    both builds give rounding residuals on that scale)."""
     p = abi.default_params(Gamma=4.0 / 3.0, c2p_tol=1e-10, c2p_max_iter=100)
     hb = states.fmks_random_block(seed=78)
-    db = _shared_tables(oracle, hb)
+    db = hb.to_device()
+    oracle.GeometryFillFMKS(hb)
+    ctx_fast.GeometryFillFMKS(db)
+    assert_bitwise(db.geom.arrays["deriv"], hb.geom.arrays["deriv"], "deriv table (production build)")
     oracle.CalculateFluidSourceTerms(p, hb)
     ctx_fast.CalculateFluidSourceTerms(p, db)
     ks, js, is_ = hb.isl()
     got, ref = db["src"][:, ks, js, is_].cpu().numpy(), hb["src"][:, ks, js, is_]
-    for v in (0, 1, 3):
-        assert_close(got[v], ref[v], 1e-12, f"src {v}")
-    # S_phi is zero analytically in axisymmetric Kerr (T symmetric, d_phi g = 0):
-    # both builds give rounding residuals, compared on the zone's source scale
     scale = np.abs(ref[0]) + np.abs(ref[1]) + np.abs(ref[3])
-    assert np.all(np.abs(got[2] - ref[2]) <= 1e-12 * scale)
+    for v in range(4):
+        report_close(got[v], ref[v], scale, 1e-12, f"FMKS src {v}")
 
 
 def test_p2c2p_known_answer_gpu(oracle, ctx_exact):

@@ -1,0 +1,71 @@
+"""The library's written-out exp, log, sin, cos and pow on the GPU
+(phx_math_eval, both library builds) against the oracle's evaluation of the
+same header on the CPU -- bit for bit -- and against CUDA's own libm (through
+torch) within the bounds the CPU test holds against the C library plus one
+ulp for CUDA's own error."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from phoebus_gb300 import abi
+
+pytestmark = pytest.mark.gpu
+
+
+def _args(fn, n=200000, seed=5):
+    rng = np.random.default_rng(seed)
+    if fn == "exp":
+        x = np.concatenate([rng.uniform(-700, 700, n // 2), rng.uniform(-2, 2, n // 2), [800.0, -800.0, np.nan]])
+    elif fn == "log":
+        x = np.concatenate([10.0 ** rng.uniform(-300, 300, n // 2), rng.uniform(0.5, 2, n // 2),
+                            [0.0, -1.0, np.inf, np.nan, 5e-324]])
+    elif fn in ("sin", "cos"):
+        x = np.concatenate([rng.uniform(-10, 10, n // 2), rng.uniform(-1e5, 1e5, n // 2), [np.inf, np.nan]])
+    else:
+        x = np.concatenate([rng.uniform(-1.3, 1.3, n // 2), rng.uniform(1e-3, 300, n // 2)])
+    y = None
+    if fn == "pow":
+        y = np.concatenate([np.full(n // 2, 14.0), rng.uniform(-3, 3, n // 2)])
+    return x, y
+
+
+def _gpu_eval(lib, fn, x, y):
+    import torch
+
+    xd = torch.from_numpy(x).cuda()
+    yd = torch.from_numpy(y).cuda() if y is not None else None
+    out = torch.empty_like(xd)
+    st = lib.phx_math_eval(abi.MATH[fn], x.size, xd.data_ptr(), yd.data_ptr() if yd is not None else None,
+                           out.data_ptr(), None)
+    assert st == 0
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+@pytest.mark.parametrize("exact", [True, False])
+@pytest.mark.parametrize("fn", ["exp", "log", "sin", "cos", "pow"])
+def test_gpu_math_equals_oracle(oracle, fn, exact):
+    lib = abi.load(exact)
+    x, y = _args(fn)
+    got = _gpu_eval(lib, fn, x, y)
+    ref = oracle.math_eval(fn, x, y)
+    same = (got == ref) | (np.isnan(got) & np.isnan(ref))
+    assert same.all(), f"{fn}: {int((~same).sum())} values differ, first x = {x[~same][0]!r}"
+
+
+@pytest.mark.parametrize("fn", ["exp", "log", "sin", "cos"])
+def test_gpu_math_against_cuda_libm(built, fn):
+    import torch
+
+    lib = abi.load(False)
+    x, _ = _args(fn, seed=6)
+    fin = np.isfinite(x) & ((x > 0) if fn == "log" else True)
+    x = x[fin]
+    got = _gpu_eval(lib, fn, x, None)
+    ref = getattr(torch, fn)(torch.from_numpy(x).cuda()).cpu().numpy()
+    ok = np.isfinite(ref) & (np.abs(ref) > 1e-3)
+    sp = np.spacing(np.abs(ref[ok]))
+    e = np.abs(got[ok] - ref[ok]) / np.where(sp > 0, sp, 5e-324)
+    print(f"{fn}: max {e.max():.2f} ulp against CUDA's libm")
+    assert e.max() <= 3.0

@@ -291,13 +291,11 @@ def test_torus_rk2_matches_oracle(oracle, ctx_exact, floors):
     magnetised torus (FMKS, WENO5-Z + HLL, gr_outflow with bc_vars =
     primitive, the outer-X1 inflow check, FixFluxes, floors, ceilings, c2p
     fixup) against the oracle's mesh stage from the same tables and state.
-    Bit for bit with constant floors; ExpX1RhoSie floors evaluate exp (CUDA's
-    and glibc's are ulps apart), so there the bar is 1e-8 of each variable's
-    scale."""
+    Bit for bit with both floor models: the ExpX1RhoSie floors' exp is the
+    library's written-out one (phoebus_gb300/csrc/phx_math.h), which the
+    oracle evaluates too."""
     from oracle.mesh_oracle import mesh_rk2_step
     from phoebus_gb300.fluid import MeshRK2
-    from tests.util import assert_close
-
     p = torus.torus_params()
     if floors == "ConstantRhoSie":
         p.floor_type = abi.FLOOR["ConstantRhoSie"]
@@ -314,7 +312,4 @@ def test_torus_rk2_matches_oracle(oracle, ctx_exact, floors):
     mesh_rk2_step(oracle, p, mesh, hosts, [np.zeros_like(h["cons"]) for h in hosts], dt)
     for n, (g, h) in enumerate(zip(blocks, hosts)):
         for name in ("prim", "cons", "fail"):
-            if floors == "ConstantRhoSie":
-                assert_bitwise(g[name], h[name], f"block {n} {name}")
-            else:
-                assert_close(g[name], h[name], 1e-8, f"block {n} {name}")
+            assert_bitwise(g[name], h[name], f"block {n} {name}")

@@ -1,0 +1,112 @@
+"""The torus initial state and one step of the torus run against the oracle,
+each side from its own FMKS tables.
+
+phx_torus_init restates pgen/torus.cpp's ProblemGenerator and the field
+normalisation of PostInitializationModifier on the GPU; the oracle restates
+the same loops on the CPU (orc_torus_init).  The generator's kernels and the
+FMKS tables are compiled without contraction and call phx_math.h's
+transcendentals, so the state is bit for bit the oracle's in the exact
+build; in the production build the prim2con and floors that close the
+generator are contracted, and the state is compared per zone.
+
+The run's step (config 5's form: FMKS a = 0.9375, WENO5-Z + HLL, Gamma 13/9,
+ExpX1RhoSie floors, MHD floors, ceilings, c2p fixup, gr_outflow X1/X2 with
+the inflow check and FixFluxes, periodic X3) runs on a 96^3 mesh of uneven
+blocks through phx_stage_mesh (batched, CUDA graphs) against the oracle's
+mesh stage: bit for bit in the exact build.
+"""
+import numpy as np
+import pytest
+
+from phoebus_gb300 import abi, torus
+from tests.util import assert_bitwise, host, max_rel_floor, prim_floors
+
+pytestmark = pytest.mark.gpu
+
+PRIMS = {"rho": abi.PRHO, "v1": abi.PVEL, "v2": abi.PVEL + 1, "v3": abi.PVEL + 2, "u": abi.PENG, "P": abi.PPRS,
+         "B1": abi.PB, "B2": abi.PB + 1, "B3": abi.PB + 2, "T": abi.PTMP, "gamma1": abi.PGM1}
+
+
+def _two_sides(oracle, ctx, n, lo, hi):
+    """GPU blocks with GPU tables, host blocks with the oracle's own tables
+    (checked equal), both states from their own torus generators."""
+    p = torus.torus_params()
+    mesh = torus.torus_mesh(n=n, lo=lo, hi=hi)
+    blocks = mesh.make_blocks("cuda", torus.torus_geometry())
+    for b in blocks:
+        ctx.GeometryFillFMKS(b)
+    hosts = [b.to_host() for b in blocks]
+    for h in hosts:
+        for t in h.geom.arrays.values():
+            t[...] = np.nan
+        oracle.GeometryFillFMKS(h)
+    for b, h in zip(blocks, hosts):
+        for name in ("cent", "face1", "face2", "deriv"):
+            assert_bitwise(b.geom.arrays[name], h.geom.arrays[name], f"{name} table")
+    tp = torus.torus_problem()
+    fac_d = ctx.TorusInit(p, tp, blocks)
+    fac_h = oracle.TorusInit(p, tp, hosts)
+    ctx.check()
+    return p, mesh, blocks, hosts, fac_d, fac_h
+
+
+@pytest.mark.parametrize("exact", [True, False])
+def test_torus_problem_generator_matches_oracle(oracle, ctx_exact, ctx_fast, exact):
+    """48^3 torus mesh in uneven blocks (edges 16..32): the field factor and
+    every block's primitives and conserved variables over the entire index
+    range (ghosts included) against pgen/torus.cpp restated in the oracle."""
+    ctx = ctx_exact if exact else ctx_fast
+    p, mesh, blocks, hosts, fac_d, fac_h = _two_sides(oracle, ctx, 48, 16, 32)
+    assert fac_d == fac_h and fac_d > 0
+    inside = 0
+    for n, (b, h) in enumerate(zip(blocks, hosts)):
+        inside += int((h["prim"][abi.PRHO] > 2e-6).sum())
+        if exact:
+            assert_bitwise(b["prim"], h["prim"], f"block {n} prim")
+            assert_bitwise(b["cons"], h["cons"], f"block {n} cons")
+            assert_bitwise(b["fail"], h["fail"], f"block {n} fail")
+        else:
+            g = b["prim"].cpu().numpy()
+            fl = prim_floors(h)
+            for name, v in PRIMS.items():
+                e = max_rel_floor(g[v], h["prim"][v], fl.get(v, np.zeros_like(g[v])))
+                assert e <= 1e-12, (n, name, e)
+            gc = b["cons"].cpu().numpy()
+            sc = np.abs(h["cons"]).sum(axis=0)
+            for m in range(abi.NCONS):
+                e = max_rel_floor(gc[m], h["cons"][m], 1e-12 * sc)
+                assert e <= 1e-12, (n, m, e)
+    assert inside > 1000  # the torus is on the mesh
+
+
+def test_torus_step_96_matches_oracle(oracle, ctx_exact):
+    """Config 5's step at 96^3: from each side's own tables and own torus
+    state, the start of the run (mesh exchange, con2prim, floors) and one
+    batched RK2 step equal the oracle's bit for bit."""
+    import torch
+
+    from oracle.mesh_oracle import mesh_exchange, mesh_rk2_step
+    from phoebus_gb300.fluid import MeshRK2
+
+    p, mesh, blocks, hosts, fac_d, fac_h = _two_sides(oracle, ctx_exact, 96, 32, 48)
+    assert fac_d == fac_h
+    assert mesh.nblocks >= 8
+    ctx_exact.MeshExchange(p, mesh, blocks)
+    for b in blocks:
+        ctx_exact.ConservedToPrimitive(p, b)
+        ctx_exact.ApplyFloors(p, b)
+    mesh_exchange(oracle, p, mesh, hosts)
+    for h in hosts:
+        oracle.ConservedToPrimitive(p, h)
+        oracle.ApplyFloors(p, h)
+    for n, (b, h) in enumerate(zip(blocks, hosts)):
+        assert_bitwise(b["prim"], h["prim"], f"block {n} prim at the start of the run")
+    rk = MeshRK2(ctx_exact, p, mesh, blocks)
+    dt = 0.3 * rk.estimate_dt(False)
+    rk.step(dt)
+    ctx_exact.check()
+    mesh_rk2_step(oracle, p, mesh, hosts, [np.zeros_like(h["cons"]) for h in hosts], dt)
+    for n, (b, h) in enumerate(zip(blocks, hosts)):
+        for name in ("prim", "cons", "fail"):
+            assert_bitwise(b[name], h[name], f"block {n} {name} after the RK2 step")
+    torch.cuda.synchronize()
