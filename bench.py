@@ -204,16 +204,18 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def flux_bytes(n, ng=4):
+def flux_bytes(n, ng=4, exact=False):
     """Algorithmic HBM bytes of one CalculateFluxes call (three launches) on
-    an n^3 block: each direction reads the 10 reconstructed primitives of
-    every cell its stencils touch and writes 8 fluxes + 1 signal speed per
-    face it computes."""
+    an n^3 block: each direction reads the reconstructed primitives of every
+    cell its stencils touch (9 in the production build, which takes gamma1 as
+    the ideal gas's constant Gamma; the exact build reads all 10) and writes
+    8 fluxes + 1 signal speed per face it computes."""
     n1t = n + 2 * ng
     t = n + 2  # transverse face range [s-1, e+1]
     cells = n1t * t * t  # stencil cells per direction (full pencil, +-1 layer)
     faces = (n + 1) * t * t
-    return 3 * (10 * cells + 9 * faces) * 8
+    nrec = 10 if exact else 9
+    return 3 * (nrec * cells + 9 * faces) * 8
 
 
 def bench_c2p(ctx, args, dev):
@@ -840,7 +842,7 @@ def main():
     torch.cuda.synchronize()
     flux_ms = f0.elapsed_time(f1) / reps
     hbm_peak, peak_src = measured_peaks()
-    fb = flux_bytes(n)
+    fb = flux_bytes(n, exact=args.exact)
     achieved = fb / (flux_ms * 1e-3) / 1e9
     fp64_peak = ctx.probe_fp64_peak()
     prof = ROOT / "profiles" / "flux_fp64_per_zone.json"

@@ -582,6 +582,15 @@ phx_status phx_math_eval(int fn, long long n, const double *x, const double *y, 
  * Used to measure the FP64 roofline of the device the library runs on. */
 phx_status phx_probe_fp64_peak(phx_ctx *ctx, double *flops_out);
 
+/* Drive the failure path of the library's bounded device waits (no
+ * counterpart in the reference): one thread block arms an mbarrier for 16
+ * bytes and issues no copy, so the wait can never complete and nothing is in
+ * flight; after `polls` polls (1 .. 2^20) the block gives up exactly as the
+ * bulk-copy staging of the flux and learned-start kernels does, sets the
+ * context's timeout bit and returns.  The next phx_ctx_check on ctx returns
+ * PHX_ERR_TIMEOUT (and clears the bit); the context stays usable. */
+phx_status phx_probe_bounded_wait(phx_ctx *ctx, long long polls, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -93,6 +93,7 @@ def lib(tuned: bool = False) -> C.CDLL:
             ("orc_rad_estimate_timestep", [RP, PP, BS, RB], C.c_double),
             ("orc_rad_tanh", [C.c_double], C.c_double),
             ("orc_math_eval", [C.c_int, C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p], None),
+            ("orc_con_to_prim_zones_at_mu", [PP, C.c_longlong] + [C.c_void_p] * 5, None),
             ("orc_torus_init", [PP, C.POINTER(abi.TorusParams), C.POINTER(abi.BlockS), C.c_int,
                                 C.POINTER(C.c_double)], None),
             ("orc_rad_m1_guess", [C.c_void_p] * 3 + [C.c_longlong] + [C.c_void_p] * 2, None),
@@ -218,6 +219,16 @@ class Oracle:
         self.last_evals = ev.value
         self.last_accepted = acc.value
         return r
+
+    def ConservedToPrimitiveZonesAtMu(self, p, cons, prim, mu, geom=None):
+        """The reference's con2prim finish at the given roots (no root find),
+        in place on prim (and cons where bounds applied); returns the fail
+        flags."""
+        n = cons.shape[1]
+        fail = np.zeros(n)
+        self.L.orc_con_to_prim_zones_at_mu(C.byref(p), n, self._p(cons), self._p(prim), self._p(geom),
+                                           self._p(np.ascontiguousarray(mu, dtype=np.float64)), fail.ctypes.data)
+        return fail
 
     def C2PFeaturesZones(self, p, cons, geom=None, coords=None):
         """The learned start's FP32 inputs [6][n]."""

@@ -825,9 +825,11 @@ struct ZoneRef {
 // cell-centre coordinates x1..x3 (used by the floors).  guess: the starting
 // value of the regula-falsi (the stored c2p_mu in the reference).  sig gets
 // the three cell signal speeds.
+// fixed_mu (not the reference's): skip the root find and finish at *fixed_mu
+// (the tests use it to evaluate the reference's finish at another build's root).
 C2PResult con2prim_core(const GeomPt &g, const EOS &eos, const Bounds &bounds, const phx_params &par,
                         Real x1, Real x2, Real x3, const ZoneRef &z, Real guess, Real sig[3],
-                        const Real *learned = nullptr) {
+                        const Real *learned = nullptr, const Real *fixed_mu = nullptr) {
   C2PResult res{false, true, 0, 0, false};
   auto P = [&](int v) -> Real & { return z.P(v); };
   auto U = [&](int v) -> Real & { return z.U(v); };
@@ -876,14 +878,22 @@ C2PResult con2prim_core(const GeomPt &g, const EOS &eos, const Bounds &bounds, c
   Real v0sq = std::min(zsq / (1.0 + zsq), 1.0 - 1.0 / (gam_max * gam_max));
   Residual resid(D, q, bsq, bsq_rpsq, rsq, rbsq, v0sq, eos, bounds, x1, x2, x3,
                  par.c2p_floor_scale_fac);
-  RootFind root(par.c2p_max_iter);
-  bool bracketed = true;
-  const Real mu = learned ? root.regula_falsi_learned(resid, learned[0], learned[1], learned[2], par.c2p_tol,
-                                                      guess, bracketed, res.learned_accepted)
-                          : root.regula_falsi(resid, 0.0, 1.0, par.c2p_tol, guess, bracketed);
-  res.bracketed = bracketed;
-  res.iterations = root.iteration_count;
-  res.evals = root.evals;
+  Real mu;
+  if (fixed_mu) {
+    mu = *fixed_mu;
+    res.bracketed = true;
+    res.iterations = 0;
+    res.evals = 1;
+  } else {
+    RootFind root(par.c2p_max_iter);
+    bool bracketed = true;
+    mu = learned ? root.regula_falsi_learned(resid, learned[0], learned[1], learned[2], par.c2p_tol, guess,
+                                             bracketed, res.learned_accepted)
+                 : root.regula_falsi(resid, 0.0, 1.0, par.c2p_tol, guess, bracketed);
+    res.bracketed = bracketed;
+    res.iterations = root.iteration_count;
+    res.evals = root.evals;
+  }
   P(PHX_PMU) = mu;
 
   const Real x = resid.x_mu(mu);
@@ -931,7 +941,7 @@ C2PResult con2prim_core(const GeomPt &g, const EOS &eos, const Bounds &bounds, c
                   g.beta, g.gamcon, sig);
   }
   num_nans = std::isnan(U(PHX_CRHO)) + std::isnan(U(PHX_CMOM)) + std::isnan(U(PHX_CENG));
-  if (!bracketed) return res;
+  if (!res.bracketed) return res;
   if (num_nans > 0) return res;
   if (par.c2p_fail_on_floors && (resid.used_density_floor_ || resid.used_energy_floor_))
     return res;
@@ -1646,6 +1656,24 @@ void orc_prim_to_con_zones(const phx_params *par, long long n, const double *pri
 // fail [n], cell_sig [3][n] (null = not written).  The same per-zone
 // inversion as a block zone.  bracket [3][n] (optional): a learned start
 // (m, lo, hi) per zone for RootFind::regula_falsi_learned.
+// con2prim of independent zones finished at the given roots mu[n] (no root
+// find): the reference's finish arithmetic at another build's roots.
+void orc_con_to_prim_zones_at_mu(const phx_params *par, long long n, double *cons, double *prim,
+                                 const double *geom, const double *mu, double *fail) {
+  Bounds bounds(*par);
+  EOS eos{par->gm1, par->Cv};
+#pragma omp parallel for schedule(static)
+  for (long long q = 0; q < n; q++) {
+    GeomPt g;
+    zone_geom(geom, n, q, g);
+    const ZoneRef z{prim + q, cons + q, n};
+    Real sig[3];
+    const Real m = mu[q];
+    C2PResult r = con2prim_core(g, eos, bounds, *par, 0.0, 0.0, 0.0, z, m, sig, nullptr, &m);
+    if (fail) fail[q] = r.success ? 1.0 : 0.0;
+  }
+}
+
 long long orc_con_to_prim_zones(const phx_params *par, long long n, double *cons, double *prim,
                                 const double *geom, double *fail, double *cell_sig,
                                 const double *coords, int *iters, const double *guess,

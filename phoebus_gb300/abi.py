@@ -207,6 +207,7 @@ _SIGS = {
     "phx_torus_init": (C.c_int, [_P, C.POINTER(Params), C.POINTER(TorusParams), C.POINTER(BlockS), C.c_int,
                                  C.POINTER(C.c_double), _P]),
     "phx_probe_fp64_peak": (C.c_int, [_P, C.POINTER(C.c_double)]),
+    "phx_probe_bounded_wait": (C.c_int, [_P, C.c_longlong, _P]),
 }
 
 

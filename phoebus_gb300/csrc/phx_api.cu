@@ -983,6 +983,15 @@ phx_status phx_math_eval(int fn, long long n, const double *x, const double *y, 
   return cuda_status("phx_math_eval");
 }
 
+phx_status phx_probe_bounded_wait(phx_ctx *ctx, long long polls, void *stream) {
+  phx_status s;
+  if ((s = ctx_device(ctx))) return s;
+  if (polls < 1 || polls > phx::MBAR_SPIN_LIMIT)
+    return fail(PHX_ERR_INVALID_ARG, "phx_probe_bounded_wait: polls must be in [1, 2^20]");
+  phx::launch_wait_probe(polls, ctx->err, S(stream));
+  return cuda_status("phx_probe_bounded_wait");
+}
+
 phx_status phx_probe_fp64_peak(phx_ctx *ctx, double *flops_out) {
   phx_status s;
   if ((s = ctx_device(ctx))) return s;

@@ -565,9 +565,14 @@ __global__ void __launch_bounds__(C2P_THREADS) kb_mlp_bracket(Par p, const BView
   }
 }
 
+// only: 0 every zone; 1 the warm zones alone (a stored mu > 0); 2 the cold
+// zones alone.  With the learned start the plan runs the plain kernel over
+// the warm zones and the learned one over the cold zones, so warm zones (all
+// of them once a run is under way) go through exactly the plain kernel's code.
 template <bool MINK, bool LEARNED>
 __global__ void __launch_bounds__(C2P_THREADS) kb_c2p(Par p, const BView *views, const WorkItem *items, int nitems,
-                                                       const double *brk, DevStats *stats, unsigned int *err) {
+                                                       const double *brk, DevStats *stats, unsigned int *err,
+                                                       int only) {
   __shared__ unsigned int s_hist[PHX_C2P_HIST];
   __shared__ unsigned long long s_cnt[6];
   if (stats) {
@@ -580,7 +585,9 @@ __global__ void __launch_bounds__(C2P_THREADS) kb_c2p(Par p, const BView *views,
     const BView &bv = views[w.block];
     const BoxZones zones{bv, Range3{0, bv.n1t - 1, 0, bv.n2t - 1, 0, bv.n3t - 1}};
     const long long q = w.first + threadIdx.x;
-    const bool valid = q < w.last;
+    bool valid = q < w.last;
+    if (only && valid) valid = (zones.guess_of(q) > 0.0) == (only == 1);
+    if (!__any_sync(0xffffffffu, valid)) continue;  // nothing for this warp in this pass
     long long id = 0;
     Pt g{};
     double U[PHX_NCONS];
@@ -623,11 +630,13 @@ static void c2p_batched_t(const Par &p, const BView *views, const WorkItem *item
     static_assert(sizeof(BracketSmem) <= 48 * 1024, "no opt-in attribute needed (launches may be captured)");
     kb_mlp_bracket<MINK><<<persistent_grid(kb_mlp_bracket<MINK>, C2P_THREADS, sizeof(BracketSmem), nitems, 0),
                            C2P_THREADS, sizeof(BracketSmem), s>>>(p, views, items, nitems, mlp, brk, err);
+    kb_c2p<MINK, false><<<persistent_grid(kb_c2p<MINK, false>, C2P_THREADS, 0, nitems, grid), C2P_THREADS, 0, s>>>(
+        p, views, items, nitems, nullptr, stats, err, 1);
     kb_c2p<MINK, true><<<persistent_grid(kb_c2p<MINK, true>, C2P_THREADS, 0, nitems, grid), C2P_THREADS, 0, s>>>(
-        p, views, items, nitems, brk, stats, err);
+        p, views, items, nitems, brk, stats, err, 2);
   } else {
     kb_c2p<MINK, false><<<persistent_grid(kb_c2p<MINK, false>, C2P_THREADS, 0, nitems, grid), C2P_THREADS, 0, s>>>(
-        p, views, items, nitems, nullptr, stats, err);
+        p, views, items, nitems, nullptr, stats, err, 0);
   }
 }
 

@@ -563,41 +563,37 @@ __device__ __forceinline__ void recon_weno5z_fast(double q0, double q1, double q
 __device__ __forceinline__ double minmod(double a, double b) {
   return a * b > 0.0 ? (fabs(a) < fabs(b) ? a : b) : 0.0;
 }
-__device__ __forceinline__ double mp5_subcalc(double Fjm2, double Fjm1, double Fj, double Fjp1,
-                                              double Fjp2) {
-  constexpr double alpha = 4.0, epsm = 1.e-12;
-  double f = 2.0 * Fjm2 - 13.0 * Fjm1 + 47.0 * Fj + 27.0 * Fjp1 - 3.0 * Fjp2;
+// MP5 value at the face j+1/2 from f_{j-2} .. f_{j+2}: the monotonicity-
+// preserving fifth-order scheme of Suresh & Huynh (1997, J. Comput. Phys.
+// 136, 83-99; alpha = 4, eps = 1e-12).  The fifth-order interface value is
+// kept when it lies between f_j and the monotonicity bound f_MP; otherwise
+// it is clipped to [f_min, f_max], built from the minmod4-limited
+// curvatures at j+1/2 and j-1/2 and the upper-limit (UL), average (AV),
+// median (MD) and large-curvature (LC) values.  The operations are in the
+// order of the reference (reconstruction.hpp:186-244), which bitwise parity
+// needs; minmod4(a, b, c, d) is minmod(minmod(a, b), minmod(c, d)).
+__device__ __forceinline__ double mp5_face(double fm2, double fm1, double f0, double fp1, double fp2) {
+  constexpr double alpha = 4.0, eps = 1.e-12;
+  double f = 2.0 * fm2 - 13.0 * fm1 + 47.0 * f0 + 27.0 * fp1 - 3.0 * fp2;
 #ifdef PHX_EXACT
   f /= 60.0;
 #else
   f *= 1.0 / 60.0;  // a product instead of the IEEE division (an ulp apart)
 #endif
-  const double fMP = Fj + minmod(Fjp1 - Fj, alpha * (Fj - Fjm1));
-  if ((f - Fj) * (f - fMP) <= epsm) return f;
-  const double d2m = Fjm2 + Fj - 2.0 * Fjm1;
-  const double d2 = Fjm1 + Fjp1 - 2.0 * Fj;
-  const double d2p = Fj + Fjp2 - 2.0 * Fjp1;
-  double scrh1 = minmod(4.0 * d2 - d2p, 4.0 * d2p - d2);
-  double scrh2 = minmod(d2, d2p);
-  const double dMMp = minmod(scrh1, scrh2);
-  scrh1 = minmod(4.0 * d2m - d2, 4.0 * d2 - d2m);
-  scrh2 = minmod(d2, d2m);
-  const double dMMm = minmod(scrh1, scrh2);
-  const double fUL = Fj + alpha * (Fj - Fjm1);
-  const double fAV = 0.5 * (Fj + Fjp1);
-  const double fMD = fAV - 0.5 * dMMp;
-  const double fLC = 0.5 * (3.0 * Fj - Fjm1) + 4.0 / 3.0 * dMMm;
-  scrh1 = fmin(Fj, Fjp1);
-  scrh1 = fmin(scrh1, fMD);
-  scrh2 = fmin(Fj, fUL);
-  scrh2 = fmin(scrh2, fLC);
-  const double Fmin = fmax(scrh1, scrh2);
-  scrh1 = fmax(Fj, Fjp1);
-  scrh1 = fmax(scrh1, fMD);
-  scrh2 = fmax(Fj, fUL);
-  scrh2 = fmax(scrh2, fLC);
-  const double Fmax = fmin(scrh1, scrh2);
-  return f + minmod(Fmin - f, Fmax - f);  // Median(f, Fmin, Fmax)
+  const double f_mp = f0 + minmod(fp1 - f0, alpha * (f0 - fm1));
+  if ((f - f0) * (f - f_mp) <= eps) return f;
+  const double curv_m = fm2 + f0 - 2.0 * fm1;  // second differences at j-1, j, j+1
+  const double curv_0 = fm1 + fp1 - 2.0 * f0;
+  const double curv_p = f0 + fp2 - 2.0 * fp1;
+  const double m4_plus = minmod(minmod(4.0 * curv_0 - curv_p, 4.0 * curv_p - curv_0), minmod(curv_0, curv_p));
+  const double m4_minus = minmod(minmod(4.0 * curv_m - curv_0, 4.0 * curv_0 - curv_m), minmod(curv_0, curv_m));
+  const double f_ul = f0 + alpha * (f0 - fm1);
+  const double f_av = 0.5 * (f0 + fp1);
+  const double f_md = f_av - 0.5 * m4_plus;
+  const double f_lc = 0.5 * (3.0 * f0 - fm1) + 4.0 / 3.0 * m4_minus;
+  const double f_min = fmax(fmin(fmin(f0, fp1), f_md), fmin(fmin(f0, f_ul), f_lc));
+  const double f_max = fmin(fmax(fmax(f0, fp1), f_md), fmax(fmax(f0, f_ul), f_lc));
+  return f + minmod(f_min - f, f_max - f);  // the median of f, f_min, f_max
 }
 
 // 5-point (or 3-point) reconstruction of one variable.  ql = value at the
@@ -612,8 +608,8 @@ __device__ __forceinline__ void recon(double qm2, double qm1, double q0, double 
     recon_weno5z_fast(qm2, qm1, q0, qp1, qp2, ql, qr);
 #endif
   } else if constexpr (RECON == PHX_RECON_MP5) {
-    ql = mp5_subcalc(qm2, qm1, q0, qp1, qp2);
-    qr = mp5_subcalc(qp2, qp1, q0, qm1, qm2);
+    ql = mp5_face(qm2, qm1, q0, qp1, qp2);
+    qr = mp5_face(qp2, qp1, q0, qm1, qm2);
   } else if constexpr (RECON == PHX_RECON_LINEAR) {
     recon_plm(qm1, q0, qp1, ql, qr);
   } else {

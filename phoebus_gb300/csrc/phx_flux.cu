@@ -137,13 +137,7 @@ __device__ __forceinline__ bool x1_stage(const BView &b, const X1Range &xr, int 
       const long long base = b.idx(xr.klo + pen / xr.nj, xr.jlo + pen % xr.nj, 0);
       bulk_g2s(rows + (long long)r * n1t, b.prim + v * b.vs + base, bytes, bar);
     }
-    bool done = false;
-    for (long long spins = 0; spins < MBAR_SPIN_LIMIT && !done; spins++) done = mbar_try_wait(bar, phase);
-    if (__syncthreads_and(done)) return true;
-    for (long long spins = 0; spins < MBAR_SPIN_LIMIT && !done; spins++) done = mbar_try_wait(bar, phase);
-    if (threadIdx.x == 0) atomicOr(err, ERR_TIMEOUT);
-    __syncthreads();
-    return false;
+    return mbar_wait_block(bar, phase, MBAR_SPIN_LIMIT, err);
   }
   for (int r = warp; r < np * kReconLoad; r += (int)(blockDim.x >> 5)) {
     const int pp = r / kReconLoad, v = r % kReconLoad;
@@ -239,6 +233,27 @@ __global__ void __launch_bounds__(32 * X1_WARPS) kb_flux_x1(Par p, const BView *
     x1_compute<RECON, MINK>(p, b, xr, (int)w.first, (int)(w.last - w.first), rows);
     __syncthreads();  // rows are rewritten by the next item
   }
+}
+
+// The failure path of the bounded waits above, driven on purpose: one CTA
+// arms an mbarrier for 16 bytes and issues no copy, so the phase never
+// completes and nothing is in flight; mbar_wait_block gives up after `limit`
+// polls, sets ERR_TIMEOUT and the CTA returns.
+__global__ void __launch_bounds__(128) k_wait_probe(long long limit, unsigned int *err) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) mbar_expect_tx(&bar, 16u);
+  mbar_wait_block(&bar, 0u, limit, err);
+  __syncthreads();
+  if (threadIdx.x == 0) mbar_inval(&bar);
+}
+
+void launch_wait_probe(long long limit, unsigned int *err, cudaStream_t s) {
+  k_wait_probe<<<1, 128, 0, s>>>(limit, err);
 }
 
 // ------------------------------------------------------------- sweeps

@@ -8,7 +8,7 @@ namespace phx {
 enum : unsigned int {
   ERR_UNBRACKETED = 1u,
   ERR_NAN_INPUT = 2u,
-  ERR_TIMEOUT = 4u,
+  ERR_TIMEOUT = 4u,  // MBAR_ERR_TIMEOUT of phx_bulk.cuh
   ERR_BOUNDS = 8u,
 };
 
@@ -62,6 +62,7 @@ void launch_geom_fmks(const phx_geometry &g, const BView &b, cudaStream_t s);
 void launch_geom_points(const phx_geometry &g, long long n, const double *x1, const double *x2, double *geom,
                         cudaStream_t s);
 void launch_math_eval(int fn, long long n, const double *x, const double *y, double *out, cudaStream_t s);
+void launch_wait_probe(long long limit, unsigned int *err, cudaStream_t s);
 // The torus problem generator and its field normalisation (phx_torus.cu) over
 // the blocks of a mesh: scratch holds 7 x n1t x n2t doubles of the largest
 // block, red 2 words; synchronises s once (the mesh-wide maxima).

@@ -218,13 +218,7 @@ __device__ __forceinline__ bool mlp_stage_weights(MlpPacked *dst, const MlpPacke
     mbar_expect_tx(bar, (unsigned)sizeof(MlpPacked));
     bulk_g2s(dst, src, (unsigned)sizeof(MlpPacked), bar);
   }
-  bool done = false;
-  for (long long spins = 0; spins < MBAR_SPIN_LIMIT && !done; spins++) done = mbar_try_wait(bar, 0);
-  if (__syncthreads_and(done)) return true;
-  for (long long spins = 0; spins < MBAR_SPIN_LIMIT && !done; spins++) done = mbar_try_wait(bar, 0);
-  if (threadIdx.x == 0) atomicOr(err, ERR_TIMEOUT);
-  __syncthreads();
-  return false;
+  return mbar_wait_block(bar, 0u, MBAR_SPIN_LIMIT, err);
 }
 
 }  // namespace phx

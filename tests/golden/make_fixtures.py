@@ -9,15 +9,16 @@ Sources in phoebus's tst/regression/:
 - radiation_diffusion.gold: 204 values, r.p.J then r.p.H components of the
   final state (t = 1) of the 512-zone M1 diffusion run (radiation_advection
   pgen, gray scattering tau = 1e3, u^1 = W 0.3), every 10th value, tol 1e-5.
-Run from the repo
-root with the reference mounted; the copy is committed so the tests do not
-need the reference at run time.
+Usage: python tests/golden/make_fixtures.py <phoebus source tree>.  The
+copy is committed, so the tests do not need the reference at run time.
 """
 import shutil
 import sys
 from pathlib import Path
 
-REF = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+if len(sys.argv) != 2:
+    sys.exit("usage: make_fixtures.py <phoebus source tree>")
+REF = Path(sys.argv[1])
 HERE = Path(__file__).resolve().parent
 for name in ("linear_modes.gold", "bondi.gold", "radiation_diffusion.gold"):
     shutil.copyfile(REF / "tst" / "regression" / name, HERE / name)

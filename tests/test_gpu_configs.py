@@ -292,18 +292,18 @@ def test_config3_batched_vs_oracle(oracle, ctx_exact, ctx_fast, exact):
         t_out = [np.zeros_like(h["cons"]) for h in hosts]
         for t, tb, to in zip(tight, h_base, t_out):
             oracle.Stage(pt, t, tb.copy(), to, 1.0, dt)
-        # Each side's result against the oracle's stage at tolerance 1e-14
+        # (1) Each side's result against the oracle's stage at tolerance 1e-14
         # from the same state ("tight"): the production build must be about
         # as close to it as the oracle at the run's tolerance is.  Per zone
-        # the deviation is |x - tight| / (|tight| + floor).  In this random
-        # state u is ill-conditioned where the magnetic or kinetic energy
-        # dwarfs it (tau - ... cancels), and floors, ceilings and the fixup
-        # act on thresholds of the primitives, so both sides scatter around
-        # the tight result; the bars compare the scatter: the 99.9th
-        # percentile and the count of zones beyond 1e-6, each within 3x the
-        # oracle's own (the conserved inputs of the two sides also differ at
-        # 1e-15, amplified by the same conditioning).
-        names = list(PRIM_VARS.items())
+        # the deviation is |x - tight| / (|tight| + floor); the bars compare
+        # the scatter: the 99.9th percentile and the count of zones beyond
+        # 1e-6, each within 3x the oracle's own (the conserved inputs of the
+        # two sides also differ at 1e-15).  u and P are left to (2): in this
+        # random state they are ill-conditioned where the magnetic or kinetic
+        # energy dwarfs them (tau - ... cancels), up to a sensitivity of 1e6 to
+        # the root mu, so any two roots within the tolerance give u apart by
+        # up to 1e-4 there.
+        names = [(n, v) for n, v in PRIM_VARS.items() if n not in ("u", "P")]
         dev_o = {n: [] for n, _ in names}
         dev_g = {n: [] for n, _ in names}
         cd_o, cd_g = [], []
@@ -320,7 +320,7 @@ def test_config3_batched_vs_oracle(oracle, ctx_exact, ctx_fast, exact):
             cd_g.append((np.abs(dd.cpu().numpy() - to) / cfl).ravel())
             assert_bitwise(d["fail"], h["fail"], "config3 fail after stage 1")
         dev_o["cons"], dev_g["cons"] = cd_o, cd_g
-        for n in list(PRIM_VARS) + ["cons"]:
+        for n in [n for n, _ in names] + ["cons"]:
             eo, eg = np.nan_to_num(np.concatenate(dev_o[n])), np.nan_to_num(np.concatenate(dev_g[n]))
             po, pg = np.quantile(eo, 0.999), np.quantile(eg, 0.999)
             co, cg = int((eo > 1e-6).sum()), int((eg > 1e-6).sum())
@@ -328,6 +328,35 @@ def test_config3_batched_vs_oracle(oracle, ctx_exact, ctx_fast, exact):
                   f"zones beyond 1e-6: GPU {cg}, oracle {co} of {eg.size}")
             assert pg <= 3 * po + 1e-11, (n, pg, po)
             assert cg <= 3 * co + 10, (n, cg, co)
+        # (2) The con2prim arithmetic alone, per zone: in every zone the
+        # inversion succeeded, the GPU's root against the oracle's, and the
+        # GPU's primitives against the reference's finish (oracle) evaluated
+        # at the GPU's own root on the GPU's own conserved state.
+        dmu, fin = [], {n: [] for n in PRIM_VARS}
+        for h, d, dd in zip(hosts, devs, d_out):
+            ok = h["fail"][0].ravel() == 1.0
+            g = d["prim"].cpu().numpy().reshape(abi.NPRIM, -1)
+            pz = np.ascontiguousarray(g.copy())
+            cz = np.ascontiguousarray(dd.cpu().numpy().reshape(abi.NCONS, -1).copy())
+            oracle.ConservedToPrimitiveZonesAtMu(p, cz, pz, g[abi.PMU].copy())
+            dmu.append(np.abs(g[abi.PMU] - h["prim"][abi.PMU].ravel())[ok])
+            fl = prim_floors(h)
+            for n, v in PRIM_VARS.items():
+                den = np.abs(pz[v]) + fl[v].ravel()
+                sel = ok & (den > 0)
+                fin[n].append(np.abs(g[v] - pz[v])[sel] / den[sel])
+        dmu = np.concatenate(dmu)
+        nbig = int((dmu > 2 * p.c2p_tol).sum())
+        print(f"[per-zone] config3 stage 1 mu: max |mu - mu_oracle| {dmu.max():.3e}, zones beyond 2 tol: {nbig} "
+              f"of {dmu.size}")
+        for n in PRIM_VARS:
+            e = np.nan_to_num(np.concatenate(fin[n]))
+            print(f"[per-zone] config3 stage 1 {n} against the reference finish at the GPU's root: max {e.max():.3e}, "
+                  f"99.99th pct {np.quantile(e, 0.9999):.3e}")
+        assert nbig <= 1e-4 * dmu.size, nbig
+        for n in PRIM_VARS:
+            e = np.nan_to_num(np.concatenate(fin[n]))
+            assert np.quantile(e, 0.9999) <= 1e-9, (n, np.quantile(e, 0.9999))
         return
     for n, (h, d, ho, dd) in enumerate(zip(hosts, devs, h_out, d_out)):
         assert_bitwise(dd, ho, f"block {n} cons after stage 1")

@@ -67,3 +67,35 @@ def test_zone_calls_refuse_bad_sizes_and_missing_weights(built):
         ctx.check()
     finally:
         ctx.close()
+
+
+def test_bounded_wait_times_out_and_context_recovers(built):
+    """The bounded-wait failure path, driven in the allowed form: a thread
+    block arms an mbarrier for bytes that no copy will deliver (nothing in
+    flight), gives up after 1000 polls, sets the timeout bit and returns.
+    phx_ctx_check reports PHX_ERR_TIMEOUT once; afterwards the same context
+    runs the bulk-copy flux kernel (the same wait) and checks clean, and
+    another context was never affected."""
+    from phoebus_gb300.fluid import FluidContext
+
+    ctx, other = FluidContext(0, exact=False), FluidContext(0, exact=False)
+    try:
+        assert ctx.lib.phx_probe_bounded_wait(ctx.h, 0, None) == abi.PHX_ERR_INVALID_ARG
+        assert ctx.lib.phx_probe_bounded_wait(ctx.h, 1000, None) == abi.PHX_OK
+        with pytest.raises(PhxError) as e:
+            ctx.check()
+        assert e.value.status == abi.PHX_ERR_TIMEOUT and "bounded device wait" in str(e.value)
+        ctx.check()  # the bit was cleared
+        other.check()
+        p = abi.default_params(Gamma=5.0 / 3.0, recon="weno5z", riemann="hll")
+        hb, _ = states.kelvin_helmholtz(n=12, seed=11)
+        b = hb.to_device("cuda")
+        ctx.Initialize(p, b)
+        ctx.CalculateFluxes(p, b)
+        ctx.check()
+        import torch
+
+        assert bool(torch.isfinite(b["flux"][:, 4:17, 4:17, 4:17]).all())
+    finally:
+        ctx.close()
+        other.close()
