@@ -428,8 +428,10 @@ phx_status phx_stage_mesh(phx_ctx *ctx, const phx_params *p, const phx_mesh *mes
  * p->enable_ox1_fmks_inflow_check on an FMKS mesh, the outer-X1 inflow check
  * (phoebus_boundaries.cpp:366-397), and prim2con with its own metric
  * (PrimitiveToConservedRegion: conserved variables and cell signal speeds).
- * The inflow check with bc_vars = conserved (a con2prim of the slab first)
- * is not built: PHX_ERR_UNSUPPORTED. */
+ * With bc_vars = conserved and the inflow check on an FMKS mesh, the
+ * outer-X1 slab of a block on the physical outer X1 face is first inverted
+ * (ConservedToPrimitiveRegion, phoebus_boundaries.cpp:333-340: primitives,
+ * floors, fail flags), then checked and prim2con'd the same way. */
 phx_status phx_mesh_exchange(phx_ctx *ctx, const phx_params *p, const phx_mesh *mesh, const phx_block *blocks,
                              int nblocks, void *stream);
 

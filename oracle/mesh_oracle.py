@@ -1,5 +1,5 @@
-"""NumPy restatement of a tiled mesh's boundary exchange with bc_vars =
-primitive, and of fixup::FixFluxes.
+"""NumPy restatement of a tiled mesh's boundary exchange (both bc_vars) and
+of fixup::FixFluxes.
 
 TEST INFRASTRUCTURE ONLY: imported by tests/ as the checker.  The product
 never loads it.
@@ -24,10 +24,13 @@ host Blocks (numpy arrays shaped (nvar, k, j, i)):
    variables along the axis negated (GenericBC Reflect), polar copies the
    mirror cell with v^2 and B^2 negated (PolarInnerX2, PolarOuterX2
    :153-213).
-3. ConvertBoundaryConditions (:303-472), bc_vars = primitive: on an FMKS mesh with
+3. ConvertBoundaryConditions (:303-472): on an FMKS mesh with
    enable_ox1_fmks_inflow_check, u^1 >= 0 is enforced in the outer-X1 slab of
-   a block on the outer X1 boundary (:366-397); then prim2con over every
-   physical slab (PrimitiveToConservedRegion, through the C oracle).
+   a block on the outer X1 boundary (:366-397) and the slab is prim2con'd
+   (:416); with bc_vars = conserved the slab goes through con2prim first
+   (ConservedToPrimitiveRegion, :333-340).  With bc_vars = primitive, prim2con
+   then runs over every physical slab (PrimitiveToConservedRegion, through
+   the C oracle).
 
 FixFluxes follows fixup.cpp:728-1078 on the blocks' flux arrays.
 """
@@ -229,19 +232,19 @@ def mesh_exchange(orc, p, mesh, blocks):
     for b, seg in zip(blocks, segs):
         for d, outer, bc in _physical_faces(mesh, b, seg):
             _apply_face(b, d, outer, bc, mhd, mesh.bc_vars)
-    if mesh.bc_vars == abi.BC_VARS_CONSERVED:
-        if p.enable_ox1_fmks_inflow_check and blocks[0].geom is not None and mesh.bc_hi[0] != PERIODIC:
-            raise NotImplementedError("inflow check with bc_vars = conserved")
-        return
+    conserved = mesh.bc_vars == abi.BC_VARS_CONSERVED
     for b, seg in zip(blocks, segs):
         faces = _physical_faces(mesh, b, seg)
         fmks = b.geom is not None
         if fmks and p.enable_ox1_fmks_inflow_check and any(d == 0 and outer for d, outer, _ in faces):
             ib, jb, kb = _slab(b, 0, True)
+            if conserved:  # ConservedToPrimitiveRegion over the slab first (:333-340)
+                orc.ConservedToPrimitive(p, b, ib, jb, kb)
             _inflow_check(b, ib, jb, kb)
             orc.PrimitiveToConserved(p, b, ib, jb, kb)
-        for d, outer, _ in faces:
-            orc.PrimitiveToConserved(p, b, *_slab(b, d, outer))
+        if not conserved:
+            for d, outer, _ in faces:
+                orc.PrimitiveToConserved(p, b, *_slab(b, d, outer))
 
 
 def fix_fluxes_block(p, b, bc_lo, bc_hi):

@@ -680,9 +680,6 @@ static phx_status check_mesh(const phx_mesh *m, const phx_params *p, const phx_b
           if (nx[d] < B.ng) return fail(PHX_ERR_INVALID_ARG, "block %d: ghost exchange needs nx >= ng", b);
         if (views[b].fmks != views[0].fmks) return fail(PHX_ERR_INVALID_ARG, "blocks must share the geometry kind");
       }
-  if (p->enable_ox1_fmks_inflow_check && views[0].fmks && m->bc_vars == PHX_BC_VARS_CONSERVED &&
-      m->bc_hi[0] != PHX_BC_PERIODIC)
-    return fail(PHX_ERR_UNSUPPORTED, "the outer-X1 inflow check with bc_vars = conserved is not built");
   return PHX_OK;
 }
 

@@ -99,7 +99,7 @@ struct BatchPlan {
   double **out_tab = nullptr;
   double *beta_dt = nullptr;
   std::vector<void *> item_mem;  // work-list allocations
-  PhaseList sources, x1, x2, x3, fluxct, fixflux, update, ghost, c2p;
+  PhaseList sources, x1, x2, x3, fluxct, fixflux, update, ghost, c2p, inflow;
   size_t x1_smem = 0;
   Tuning tune;
   bool mink = true;
@@ -251,11 +251,14 @@ static void stage_launches(BatchPlan &pl, DevStats *stats, unsigned int *err, cu
     }
   };
   auto exchange = [&] {
-    if (pl.has_mesh)
+    if (pl.has_mesh) {
       each(pl.c2p, [&](const WorkItem *it, int n, int g) {
         launch_mesh_exchange(p, pl.mink, pl.views_out, pl.md, it, n, g, s);
       });
-    else
+      each(pl.inflow, [&](const WorkItem *it, int n, int g) {
+        launch_ox1_inflow(p, pl.views_out, it, n, g, err, s);
+      });
+    } else
       each(pl.ghost, [&](const WorkItem *it, int n, int g) {
         launch_ghost_batched(pl.views_out, p.mhd ? PHX_NCONS : 5, it, n, g, s);
       });
@@ -521,6 +524,15 @@ cudaError_t batch_stage(BatchCache *cache, const Par &par, const phx_block *bloc
             fix.push_back(tot);
           }
       if ((e = upload_items(P, P.fixflux, make_items(fix, 128))) != cudaSuccess) return e;
+      // bc_vars = conserved: the inflow check's slabs (blocks on the physical outer X1 face)
+      std::vector<long long> slab(n, 0);
+      if (mesh->bc_vars == PHX_BC_VARS_CONSERVED && par.inflow_check && !P.mink &&
+          mesh->bc_hi[0] != PHX_BC_PERIODIC)
+        for (int s3 = 0, b = 0; s3 < mesh->nseg[2]; s3++)
+          for (int s2 = 0; s2 < mesh->nseg[1]; s2++)
+            for (int s1 = 0; s1 < mesh->nseg[0]; s1++, b++)
+              if (s1 == mesh->nseg[0] - 1) slab[b] = (long long)vin[b].ng * vin[b].n2t * vin[b].n3t;
+      if ((e = upload_items(P, P.inflow, make_items(slab, 128))) != cudaSuccess) return e;
     }
     P.vin = vin;
     if (only == BATCH_STAGE && (e = prepare_stage(P, stats, err, s)) != cudaSuccess) return e;

@@ -640,6 +640,70 @@ static void c2p_batched_t(const Par &p, const BView *views, const WorkItem *item
   }
 }
 
+// bc_vars = conserved with the outer-X1 inflow check on an FMKS mesh
+// (ConvertBoundaryConditions, phoebus_boundaries.cpp:333-340, 366-397, 416):
+// after the exchange, the outer-X1 ghost slab of each block on the physical
+// outer X1 face goes through con2prim (ConservedToPrimitiveRegion: the plain
+// start from the stored mu, floors, the fail flag), the inflow check on the
+// primitives it left, and prim2con with the zone's own metric (conserved
+// variables and cell speeds).  Item zone t of a block is the slab zone
+// i = n1t - ng + t % ng, j = (t / ng) % n2t, k = t / (ng n2t).
+__global__ void __launch_bounds__(C2P_THREADS) kb_ox1_inflow(Par p, const BView *views, const WorkItem *items,
+                                                              int nitems, unsigned int *err) {
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const WorkItem w = items[it];
+    const BView &bv = views[w.block];
+    const BoxZones zones{bv, Range3{bv.n1t - bv.ng, bv.n1t - 1, 0, bv.n2t - 1, 0, bv.n3t - 1}};
+    const long long q = w.first + threadIdx.x;
+    const bool valid = q < w.last;
+    if (!__any_sync(0xffffffffu, valid)) continue;
+    long long id = 0;
+    Pt g{};
+    double U[PHX_NCONS];
+    bool setup_ok = false;
+    Residual res;
+    double rcon[3], rcov[3], bu[3], Bprim[3] = {0.0, 0.0, 0.0}, bdotr = 0.0, guess = 0.0;
+    if (valid) {
+      double x1, x2, x3;
+      zones.template load<false>(q, id, g, U, x1, x2, x3, guess);
+      setup_ok = c2p_setup<false>(p, g, U, x1, x2, x3, res, rcon, rcov, bu, Bprim, bdotr);
+    }
+    RFState st;
+    rf_start<false>(p, res, valid && setup_ok, 0.0, 1.0, guess, nullptr, st);
+    rf_iterate(p, res, valid && setup_ok, st, p.c2p_max_iter);
+    if (!valid) continue;
+    C2POut out{0, 0, false, true, false, false};
+    const double mu = rf_result(st, guess, out);
+    c2p_complete<BoxZones, false>(p, zones, id, g, res, mu, rcon, bu, Bprim, bdotr, U, setup_ok, out, nullptr,
+                                  nullptr, nullptr, err);
+    double *P = bv.prim + id;
+    const long long vs = bv.vs;
+    double vel[3] = {P[PHX_PVEL * vs], P[(PHX_PVEL + 1) * vs], P[(PHX_PVEL + 2) * vs]};
+    ox1_inflow_fix(g, vel);
+    for (int d = 0; d < 3; d++) P[(PHX_PVEL + d) * vs] = vel[d];
+    double bp[3] = {0.0, 0.0, 0.0};
+    if (p.mhd)
+      for (int d = 0; d < 3; d++) bp[d] = P[(PHX_PB + d) * vs];
+    double D, tau, S[3], bc[3], sig[3];
+    p2c<false>(P[PHX_PRHO * vs], vel, bp, P[PHX_PENG * vs], P[PHX_PPRS * vs], P[PHX_PGM1 * vs], g, g.detgam, D, S,
+               bc, tau, sig);
+    double *C = bv.cons + id;
+    C[PHX_CRHO * vs] = D;
+    C[PHX_CENG * vs] = tau;
+    for (int d = 0; d < 3; d++) C[(PHX_CMOM + d) * vs] = S[d];
+    if (p.mhd)
+      for (int d = 0; d < 3; d++) C[(PHX_CB + d) * vs] = bc[d];
+    for (int d = 0; d < bv.ndim; d++) bv.cell_sig[d * vs + id] = sig[d];
+  }
+}
+
+void launch_ox1_inflow(const Par &p, const BView *views, const WorkItem *items, int nitems, int grid,
+                       unsigned int *err, cudaStream_t s) {
+  if (nitems <= 0) return;
+  kb_ox1_inflow<<<persistent_grid(kb_ox1_inflow, C2P_THREADS, 0, nitems, grid), C2P_THREADS, 0, s>>>(
+      p, views, items, nitems, err);
+}
+
 void launch_c2p_batched(const Par &p, bool mink, const BView *views, const WorkItem *items, int nitems, int grid,
                         const MlpPacked *mlp, double *brk, DevStats *stats, unsigned int *err, cudaStream_t s) {
   if (nitems <= 0) return;

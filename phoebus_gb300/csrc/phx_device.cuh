@@ -320,6 +320,22 @@ __device__ __forceinline__ double lorentz(const Pt &g, const double v[3]) {
   return sqrt(1. + dot_sp<MINK>(g, v, v));
 }
 
+// The outer-X1 inflow check of one ghost zone (ConvertBoundaryConditions,
+// phoebus_boundaries.cpp:366-397): where u^1 = v^1 - W beta^1 / alpha < 0,
+// the three-velocity v / W keeps its X2 and X3 components, takes
+// beta^1 / alpha along X1, and is turned back into W v.  v: W v^i in place.
+__device__ __forceinline__ void ox1_inflow_fix(const Pt &gm, double v[3]) {
+  double W = lorentz<false>(gm, v);
+  const double ucon1 = v[0] - W * gm.beta[0] / gm.alpha;
+  if (ucon1 < 0) {
+    double vcon[3] = {v[0] / W, v[1] / W, v[2] / W};
+    vcon[0] = gm.beta[0] / gm.alpha;
+    const double vsq = dot_sp<false>(gm, vcon, vcon);
+    W = 1. / sqrt(1. - vsq);
+    for (int d = 0; d < 3; d++) v[d] = W * vcon[d];
+  }
+}
+
 // ---------------------------------------------------------- prim2con.hpp
 // signal_speeds (prim2con.hpp:24-46); ndim entries written.
 template <bool MINK>

@@ -156,6 +156,10 @@ void launch_ghost_batched(const BView *views, int nvar, const WorkItem *items, i
 // mlp non-null: the learned start; brk holds 3 x nitems x 128 doubles.
 void launch_c2p_batched(const Par &p, bool mink, const BView *views, const WorkItem *items, int nitems, int grid,
                         const MlpPacked *mlp, double *brk, DevStats *stats, unsigned int *err, cudaStream_t s);
+// bc_vars = conserved, outer-X1 inflow check (FMKS): con2prim, u^1 >= 0 and
+// prim2con over the outer-X1 ghost slabs; items over ng * n2t * n3t zones.
+void launch_ox1_inflow(const Par &p, const BView *views, const WorkItem *items, int nitems, int grid,
+                       unsigned int *err, cudaStream_t s);
 void launch_flux_x1_batched(const Par &p, bool mink, const BView *views, const WorkItem *items, int nitems, int grid,
                             size_t smem, unsigned int *err, cudaStream_t s);
 void prepare_flux_x1_batched(const Par &p, bool mink, size_t smem);

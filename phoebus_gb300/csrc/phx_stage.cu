@@ -417,7 +417,9 @@ __global__ void __launch_bounds__(256) kb_ghost(const BView *views, int nvar, co
 //   scaled at each face by sgn * robust::ratio(DetGamma(cell), DetGamma(its
 //   mapped cell)) where the cell is the one that face's loop sets (axes before
 //   it at the ghost's own index, axes after it already mapped); sgn negates
-//   the vector components along a reflect axis.
+//   the vector components along a reflect axis.  With the outer-X1 inflow
+//   check on an FMKS mesh, launch_ox1_inflow (phx_c2p.cu) then takes the
+//   outer-X1 slab through con2prim, the check and prim2con.
 //   bc_vars = primitive, physical slab: primitives from the source with the
 //   rule's signs (the velocity and B components along a reflect axis, v^2 and
 //   B^2 across a polar face), the outer-X1 inflow check
@@ -509,17 +511,10 @@ __device__ __forceinline__ void mesh_ghost_at(const Par &p, const BView *views, 
   Pt gm{};
   if constexpr (!MINK) {
     load_pt(b, 0, loc[1], loc[0], gm);
-    if (outer_x1 && p.inflow_check) {  // enforce u^1 >= 0 (phoebus_boundaries.cpp:366-397)
-      double vcon[3] = {P[PHX_PVEL], P[PHX_PVEL + 1], P[PHX_PVEL + 2]};
-      double W = lorentz<false>(gm, vcon);
-      const double ucon1 = vcon[0] - W * gm.beta[0] / gm.alpha;
-      if (ucon1 < 0) {
-        for (int d = 0; d < 3; d++) vcon[d] /= W;
-        vcon[0] = gm.beta[0] / gm.alpha;
-        const double vsq = dot_sp<false>(gm, vcon, vcon);
-        W = 1. / sqrt(1. - vsq);
-        for (int d = 0; d < 3; d++) P[PHX_PVEL + d] = W * vcon[d];
-      }
+    if (outer_x1 && p.inflow_check) {  // enforce u^1 >= 0
+      double v[3] = {P[PHX_PVEL], P[PHX_PVEL + 1], P[PHX_PVEL + 2]};
+      ox1_inflow_fix(gm, v);
+      for (int d = 0; d < 3; d++) P[PHX_PVEL + d] = v[d];
     }
   }
   const double vel[3] = {P[PHX_PVEL], P[PHX_PVEL + 1], P[PHX_PVEL + 2]};

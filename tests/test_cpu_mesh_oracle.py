@@ -130,3 +130,76 @@ def test_split_axis_covers_the_axis_in_range():
                 else:
                     with pytest.raises((AssertionError, ValueError)):
                         split_axis(n, lo, hi, 1234, stream)
+
+
+def test_conserved_exchange_inflow_check(built):
+    """bc_vars = conserved with the outer-X1 inflow check on an FMKS mesh
+    (ConvertBoundaryConditions, phoebus_boundaries.cpp:333-340, 366-397):
+    the outer-X1 ghosts of the blocks on the outer X1 face leave the
+    exchange with u^1 >= 0 although their interior neighbours flow inward,
+    with primitives that con2prim of the copied conserved variables gives
+    where u^1 was already >= 0, and with conserved variables that are
+    prim2con of their primitives."""
+    import math
+
+    from oracle.oracle import Oracle
+    from phoebus_gb300 import torus
+
+    orc = Oracle()
+    p = torus.torus_params()
+    bcs = CASES["deck"]
+    mesh = TiledMesh((12, 10, 1), [[6, 6], [4, 6], [1]], (math.log(1.2), 0.0, 0.0), (math.log(250.0), 1.0, 1.0),
+                     *bcs, bc_vars=abi.BC_VARS_CONSERVED, ndim=2)
+    blocks = mesh.make_blocks(geometry=torus.torus_geometry(), backend="numpy")
+    rng = np.random.default_rng(5)
+    for b, seg in zip(blocks, mesh.segments()):
+        orc.GeometryFillFMKS(b)
+        ks, js, is_ = b.isl()
+        shp = b["prim"][0][ks, js, is_].shape
+        cent = b.geom.arrays["cent"][:, js, is_][:, None]
+        pr = b["prim"]
+        rho = 10.0 ** rng.uniform(-3.0, 0.0, shp)
+        u = rho * 10.0 ** rng.uniform(-2.0, 0.0, shp)
+        pr[abi.PRHO][ks, js, is_], pr[abi.PENG][ks, js, is_], pr[abi.PPRS][ks, js, is_] = rho, u, p.gm1 * u
+        for d in range(3):
+            g_dd = cent[abi.G_GCOV + (d + 1) * (d + 2) // 2 + d + 1]
+            pr[abi.PVEL + d][ks, js, is_] = rng.uniform(-0.5, 0.5, shp) / np.sqrt(g_dd)
+            pr[abi.PB + d][ks, js, is_] = rng.uniform(-0.2, 0.2, shp) / np.sqrt(g_dd)
+            if d == 0 and seg[0] == mesh.nseg[0] - 1:  # inflow at the outer X1 face
+                last = pr[abi.PVEL][ks, js, is_.stop - 1]
+                pr[abi.PVEL][ks, js, is_.stop - 1] = -np.abs(last) - 0.1 / np.sqrt(g_dd[..., -1])
+        pr[abi.PGM1][ks, js, is_], pr[abi.PTMP][ks, js, is_] = p.gm1 + 1.0, u / rho
+        pr[abi.PMU][ks, js, is_] = rng.uniform(0.1, 0.9, shp)
+        orc.PrimitiveToConserved(p, b, *b.interior())
+    plain = [b.to_host() for b in blocks]
+    p_off = torus.torus_params()
+    p_off.enable_ox1_fmks_inflow_check = 0
+    mo.mesh_exchange(orc, p_off, mesh, plain)
+    mo.mesh_exchange(orc, p, mesh, blocks)
+    for b, q, seg in zip(blocks, plain, mesh.segments()):
+        if seg[0] != mesh.nseg[0] - 1:
+            continue
+        ib, jb, kb = mo._slab(b, 0, True)
+        sl = (slice(kb[0], kb[1] + 1), slice(jb[0], jb[1] + 1), slice(ib[0], ib[1] + 1))
+        orc.ConservedToPrimitive(p, q, ib, jb, kb)  # the copied state, inverted
+        cent = b.geom.arrays["cent"][:, sl[1], sl[2]][:, None]
+
+        def gam(a, c):  # gamma_{a+1, c+1} from the packed symmetric 4-metric
+            hi, lo = max(a, c) + 1, min(a, c) + 1
+            return cent[abi.G_GCOV + hi * (hi + 1) // 2 + lo]
+
+        def ucon1(P):
+            v = [P[abi.PVEL + a][sl] for a in range(3)]
+            vsq = sum(gam(a, c) * v[a] * v[c] for a in range(3) for c in range(3))
+            return v[0] - np.sqrt(1.0 + vsq) * cent[abi.G_BETA] / cent[abi.G_ALPHA]
+
+        before, after = ucon1(q["prim"]), ucon1(b["prim"])
+        assert (before < 0).sum() > 0, "no inflow to fix"
+        scale = np.abs(cent[abi.G_BETA] / cent[abi.G_ALPHA])
+        assert np.all(after >= -1e-12 * scale), after.min()
+        keep = before >= 0
+        for v in range(abi.NPRIM):
+            np.testing.assert_array_equal(b["prim"][v][sl][keep], q["prim"][v][sl][keep])
+        cons = b["cons"].copy()
+        orc.PrimitiveToConserved(p, b, ib, jb, kb)
+        np.testing.assert_array_equal(b["cons"][(slice(None),) + sl], cons[(slice(None),) + sl])

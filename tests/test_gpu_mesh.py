@@ -172,9 +172,10 @@ def small_fmks_mesh(bcs, n=26, lo=6, hi=12, bc_vars=abi.BC_VARS_PRIMITIVE, ndim=
 def test_mesh_exchange_matches_oracle(ctx_exact, name, geometry, bc_vars, ndim):
     """Exact build: the exchange (neighbour copies, physical boundaries; with
     bc_vars = primitive the outer-X1 inflow check and prim2con in the boundary
-    slabs, with bc_vars = conserved the DetGamma-scaled copies) equals the
-    oracle's literal face-by-face restatement bit for bit -- prims, cons and
-    cell signal speeds in every ghost zone."""
+    slabs, with bc_vars = conserved the DetGamma-scaled copies and, on FMKS,
+    con2prim + the inflow check + prim2con in the outer-X1 slab) equals the
+    oracle's literal face-by-face restatement bit for bit -- prims, cons, fail
+    flags and cell signal speeds in every ghost zone."""
     from oracle.mesh_oracle import mesh_exchange
     from oracle.oracle import Oracle
 
@@ -182,8 +183,6 @@ def test_mesh_exchange_matches_oracle(ctx_exact, name, geometry, bc_vars, ndim):
     if bc_vars == abi.BC_VARS_CONSERVED and abi.BC_POLAR in bcs[0] + bcs[1]:
         pytest.skip("polar boundaries need bc_vars = primitive")
     p = torus.torus_params()
-    if bc_vars == abi.BC_VARS_CONSERVED:
-        p.enable_ox1_fmks_inflow_check = 0
     mesh = small_fmks_mesh(bcs, bc_vars=bc_vars, ndim=ndim)
     geom = torus.torus_geometry() if geometry == "fmks" else None
     blocks = mesh.make_blocks("cuda", geom)
@@ -201,6 +200,65 @@ def test_mesh_exchange_matches_oracle(ctx_exact, name, geometry, bc_vars, ndim):
         assert_bitwise(g["prim"], r["prim"], f"block {n} prim")
         assert_bitwise(g["cons"], r["cons"], f"block {n} cons")
         assert_bitwise(g["cell_sig"], r["cell_sig"], f"block {n} cell_sig")
+        assert_bitwise(g["fail"], r["fail"], f"block {n} fail")
+
+
+def test_conserved_exchange_inflow_fixes_ghosts(ctx_exact):
+    """bc_vars = conserved on an FMKS mesh with X1 outflow: interior zones
+    next to the outer X1 face given an inward velocity (u^1 < 0) leave
+    u^1 >= 0 in the outer-X1 ghosts once the slab has gone through
+    con2prim, the inflow check and prim2con; without the check the ghosts
+    keep the copied inflow.  The cons of the fixed ghosts are prim2con of
+    their prims (a con2prim of the ghost gives the prims back)."""
+    import torch
+
+    bcs = MESH_BCS["deck"]
+    p = torus.torus_params()
+    mesh = small_fmks_mesh(bcs, bc_vars=abi.BC_VARS_CONSERVED, ndim=2)
+    blocks = mesh.make_blocks("cuda", torus.torus_geometry())
+    for b in blocks:
+        ctx_exact.GeometryFillFMKS(b)
+    random_interior(ctx_exact, p, mesh, blocks, seed=77)
+    outer = [b for b, seg in zip(blocks, mesh.segments()) if seg[0] == mesh.nseg[0] - 1]
+    for b in outer:  # inward radial velocity in the last interior column
+        ks, js, is_ = b.isl()
+        last = is_.stop - 1
+        g11 = b.geom.arrays["cent"][abi.G_GCOV + 2][js, last]
+        v1 = b["prim"][abi.PVEL, ks, js, last]
+        b["prim"][abi.PVEL, ks, js, last] = -v1.abs() - 0.1 / torch.sqrt(g11)
+        ctx_exact.PrimitiveToConserved(p, b, *b.interior())
+    saved = [{k: v.clone() for k, v in b.arrays.items()} for b in blocks]
+
+    def ucon1(b):
+        cent = b.geom.arrays["cent"]
+        pr = b["prim"]
+        g = lambda m, n: cent[abi.G_GCOV + (max(m, n) * (max(m, n) + 1)) // 2 + min(m, n)][None]  # noqa: E731
+        W = torch.sqrt(1 + sum(g(m + 1, n + 1) * pr[abi.PVEL + m] * pr[abi.PVEL + n]
+                               for m in range(3) for n in range(3)))
+        return pr[abi.PVEL] - W * cent[abi.G_BETA][None] / cent[abi.G_ALPHA][None]
+
+    def ghosts(b, a):  # the outer-X1 ghosts beside the interior rows
+        return a[..., b.ng:b.ng + b.nx[1], b.n1t - b.ng:]
+
+    p.enable_ox1_fmks_inflow_check = 0
+    ctx_exact.MeshExchange(p, mesh, blocks)
+    for b in outer:
+        ctx_exact.ConservedToPrimitive(p, b)
+    ctx_exact.check()
+    assert any(bool((ghosts(b, ucon1(b)) < 0).any()) for b in outer), "no inflow to fix"
+    for b, a in zip(blocks, saved):
+        for k, v in a.items():
+            b.arrays[k].copy_(v)
+    p.enable_ox1_fmks_inflow_check = 1
+    ctx_exact.MeshExchange(p, mesh, blocks)
+    ctx_exact.check()
+    for b in outer:
+        u1 = ghosts(b, ucon1(b))
+        scale = ghosts(b, (b.geom.arrays["cent"][abi.G_BETA] / b.geom.arrays["cent"][abi.G_ALPHA])[None]).abs()
+        assert bool((u1 >= -1e-12 * scale).all()), float(u1.min())
+        cons = b["cons"].clone()
+        ctx_exact.PrimitiveToConserved(p, b, *b.entire())
+        assert_bitwise(ghosts(b, b["cons"]), ghosts(b, cons), "ghost cons = prim2con(prims)")
 
 
 @pytest.mark.parametrize("name", list(MESH_BCS))
@@ -256,11 +314,6 @@ def test_mesh_rejects_bad_boundaries(ctx_fast):
         blocks = mesh.make_blocks("cuda", None)
         with pytest.raises(RuntimeError, match=msg):
             ctx_fast.MeshExchange(p, mesh, blocks)
-    # the inflow check after a conserved exchange (a con2prim of the slab) is not built
-    mesh = small_fmks_mesh(deck, bc_vars=abi.BC_VARS_CONSERVED)
-    blocks = mesh.make_blocks("cuda", torus.torus_geometry())
-    with pytest.raises(RuntimeError, match="inflow check"):
-        ctx_fast.MeshExchange(p, mesh, blocks)
 
 
 def test_torus_batched_equals_per_block(ctx_exact):
@@ -285,15 +338,18 @@ def test_torus_batched_equals_per_block(ctx_exact):
         assert bool(torch.isfinite(x["prim"][:, ks, js, is_]).all())
 
 
-@pytest.mark.parametrize("floors", ["ConstantRhoSie", "ExpX1RhoSie"])
-def test_torus_rk2_matches_oracle(oracle, ctx_exact, floors):
+@pytest.mark.parametrize("floors,bc_vars", [("ConstantRhoSie", abi.BC_VARS_PRIMITIVE),
+                                            ("ExpX1RhoSie", abi.BC_VARS_PRIMITIVE),
+                                            ("ExpX1RhoSie", abi.BC_VARS_CONSERVED)])
+def test_torus_rk2_matches_oracle(oracle, ctx_exact, floors, bc_vars):
     """Config 5 end to end on a small mesh: one batched RK2 step of the
     magnetised torus (FMKS, WENO5-Z + HLL, gr_outflow with bc_vars =
-    primitive, the outer-X1 inflow check, FixFluxes, floors, ceilings, c2p
-    fixup) against the oracle's mesh stage from the same tables and state.
-    Bit for bit with both floor models: the ExpX1RhoSie floors' exp is the
-    library's written-out one (phoebus_gb300/csrc/phx_math.h), which the
-    oracle evaluates too."""
+    primitive as in the deck, or conserved with the slab's con2prim before
+    the inflow check, the outer-X1 inflow check, FixFluxes, floors,
+    ceilings, c2p fixup) against the oracle's mesh stage from the same
+    tables and state.  Bit for bit with both floor models: the ExpX1RhoSie
+    floors' exp is the library's written-out one
+    (phoebus_gb300/csrc/phx_math.h), which the oracle evaluates too."""
     from oracle.mesh_oracle import mesh_rk2_step
     from phoebus_gb300.fluid import MeshRK2
     p = torus.torus_params()
@@ -301,6 +357,7 @@ def test_torus_rk2_matches_oracle(oracle, ctx_exact, floors):
         p.floor_type = abi.FLOOR["ConstantRhoSie"]
         p.rho0_floor, p.sie0_floor = 1e-6, 1e-3
     mesh = torus.torus_mesh(n=48, lo=16, hi=32)
+    mesh.bc_vars = bc_vars
     blocks = mesh.make_blocks("cuda", torus.torus_geometry())
     torus.fill_torus(ctx_exact, p, mesh, blocks)
     ctx_exact.check()
