@@ -5,9 +5,10 @@
  * Each entry point replaces one task of the reference's radiation package
  * (src/radiation/moments.cpp, moments_source.cpp, radiation.cpp; paths
  * relative to the phoebus source tree) for the "moment_m1" and
- * "moment_eddington" methods with one neutrino species, on a Minkowski block
+ * "moment_eddington" methods with one neutrino species, on a Minkowski block:
  * with a static fluid background (physics/hydro = false; the reference then
- * calls MomentFluidSource with update_fluid = false).
+ * calls MomentFluidSource with update_fluid = false), or coupled to the
+ * evolved fluid (update_fluid = true: phx_rad_fluid_stage).
  *
  * Conventions are those of phx_fluid.h: caller-owned device memory, FP64,
  * structure of arrays with i fastest, ghost-inclusive inclusive ranges, every
@@ -125,10 +126,17 @@ phx_status phx_rad_calculate_fluxes(phx_ctx *ctx, const phx_rad_params *rp, cons
 phx_status phx_rad_update(phx_ctx *ctx, const phx_rad_params *rp, const phx_block *fb, const phx_rad_block *rb,
                           const double *base, double *out, double beta, double dt, void *stream);
 
-/* radiation::MomentFluidSource with the "oned" source solver and
- * update_fluid = false (moments_source.cpp:203-490, 786-958): the implicit
- * absorption/scattering update of E, F_i over dt, then the frail closure
- * inversion that sets J, H_i/J (or the failure state). */
+/* radiation::MomentFluidSource with the "oned" source solver
+ * (moments_source.cpp:203-490, 786-965): the implicit absorption/scattering
+ * update of E, F_i over dt, then the frail closure inversion that sets
+ * J, H_i/J (or the failure state).  With rp->update_fluid the fluid's tau
+ * and S_i lose what the radiation gained, the fluid is inverted (robust
+ * con2prim with p's tolerance, iteration cap and floor scale, failing on
+ * floors and ceilings: prims, cell speeds, cons where bounds were used), and
+ * the closure inversion uses the new fluid velocity; when either inversion
+ * fails the fluid becomes rho = u = 10 SMALL at rest (with the bulk modulus
+ * stored in the gamma1 slot, as the reference stores it) with its D, S_i,
+ * tau from prim2con, and the radiation the J = SMALL, H = 0 state. */
 phx_status phx_rad_fluid_source(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_block *fb,
                                 const phx_rad_block *rb, double dt, void *stream);
 
@@ -154,6 +162,20 @@ phx_status phx_rad_estimate_timestep(phx_ctx *ctx, const phx_rad_params *rp, con
 phx_status phx_rad_stage(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_block *fb,
                          const phx_rad_block *rb, const double *base, double *out, double beta, double dt,
                          void *stream);
+
+/* One RK stage of the fluid and the moments together on a periodic
+ * Minkowski block (physics/hydro = true, phoebus_driver.cpp:318-362,
+ * 547-620, 640-680): fluid source terms, fluid fluxes, FluxCT, opacities,
+ * radiation fluxes; both updates (fluid_base/fluid_out and rad_base/rad_out,
+ * each [nvar][N] like its block's cons); FillDerived (the fluid's con2prim
+ * over the entire block, then MomentCon2Prim); MomentFluidSource over
+ * beta dt with update_fluid; the periodic exchange of the fluid's conserved
+ * variables and the radiation fields; FillDerived again.  fb->cons and
+ * rb->cons are the stage inputs.  Fluid floors and the c2p fixup must be off
+ * (their radiation parts are not built); rp->update_fluid is implied. */
+phx_status phx_rad_fluid_stage(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_block *fb,
+                               const phx_rad_block *rb, const double *fluid_base, double *fluid_out,
+                               const double *rad_base, double *rad_out, double beta, double dt, void *stream);
 
 #ifdef __cplusplus
 }

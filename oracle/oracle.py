@@ -396,3 +396,45 @@ class RadOracle:
         b.arrays["rcons"] = stage_buf
         self.Stage(rp, p, b, base, base, 0.5, dt)
         b.arrays["rcons"] = base
+
+    def FluidStage(self, rp, p, b: Block, fbase, fout, rbase, rout, beta, dt):
+        """PhoebusDriver::RungeKuttaStage with the fluid and the moments
+        active on one periodic block (phoebus_driver.cpp:318-362, 547-620,
+        640-680): fluid source terms, fluxes, FluxCT, opacities, moment
+        fluxes; both updates; FillDerived (fluid con2prim over the entire
+        block, then MomentCon2Prim); MomentFluidSource(update_fluid = true)
+        over beta dt; the periodic exchange of the fluid's conserved
+        variables and the radiation fields; FillDerived again.  b['cons'] and
+        b['rcons'] are the stage inputs."""
+        import copy
+
+        orc = Oracle()
+        orc.L = self.L
+        orc.CalculateFluidSourceTerms(p, b)
+        orc.CalculateFluxes(p, b)
+        orc.FluxCT(p, b)
+        self.MomentCalculateOpacities(rp, p, b)
+        self.CalculateFluxes(rp, p, b)
+        orc.FluxDivergence(p, b)
+        orc.Update(p, b, fbase, fout, beta, dt)
+        self.Update(rp, b, rbase, rout, beta, dt)
+        fin, rin = b.arrays["cons"], b.arrays["rcons"]
+        b.arrays["cons"], b.arrays["rcons"] = fout, rout
+        orc.ConservedToPrimitive(p, b)
+        ib, jb, kb = b.interior()
+        self.MomentCon2Prim(rp, p, b, ib, jb, kb)
+        rpu = copy.copy(rp)
+        rpu.update_fluid = 1
+        self.MomentFluidSource(rpu, p, b, beta * dt)
+        orc.FillGhostsPeriodic(b, b["cons"], abi.NCONS if p.mhd else 5)
+        self.FillGhostsPeriodic(b)
+        orc.ConservedToPrimitive(p, b)
+        self.MomentCon2Prim(rp, p, b)
+        b.arrays["cons"], b.arrays["rcons"] = fin, rin
+
+    def rk2_fluid_step(self, rp, p, b: Block, fluid_buf, rad_buf, dt):
+        fb, rb = b.arrays["cons"], b.arrays["rcons"]
+        self.FluidStage(rp, p, b, fb, fluid_buf, rb, rad_buf, 1.0, dt)
+        b.arrays["cons"], b.arrays["rcons"] = fluid_buf, rad_buf
+        self.FluidStage(rp, p, b, fb, fb, rb, rb, 0.5, dt)
+        b.arrays["cons"], b.arrays["rcons"] = fb, rb

@@ -2244,7 +2244,7 @@ void orc_torus_init(const phx_params *par, const phx_torus_params *tp, phx_block
 // Radiation moments (M1 and Eddington closures), Minkowski, one species,
 // static fluid background.  Restates radiation/closure.hpp:49-352,
 // closure_m1.hpp:31-372, local_three_geometry.hpp:140-185, moments.cpp:61-995,
-// moments_source.cpp:152-958 (oned solver, update_fluid = false),
+// moments_source.cpp:152-965 (oned solver, both update_fluid settings),
 // radiation.cpp:681-733, linear_algebra.hpp:58-96 and root_find.hpp:20-160.
 // Minkowski: the spatial metric is the identity, lapse 1, shift 0.  Each
 // contraction keeps the reference's order over its non-zero terms; for finite
@@ -2654,8 +2654,10 @@ struct RPar {
   int recon;
   Real cfl, tol, kappa_a, kappa_s, jbb;
   int maxiter, oned_fixup;
+  bool update_fluid;
   Real J_floor, xi_ceiling, tau_max, W_ceiling, Cv;
   RPar(const phx_rad_params &rp, const phx_params &p) {
+    update_fluid = rp.update_fluid != 0;
     m1 = rp.method == PHX_RAD_M1;
     robust = !rp.closure_frail;
     bounds = rp.recon_fixup_bounds != 0;
@@ -2939,10 +2941,99 @@ struct RF {
   }
 };
 
-// MomentFluidSourceImpl, oned solver, update_fluid = false, one species
-// (moments_source.cpp:203-490 and 786-958).  Returns 1 when the source
-// update was applied.
-int fluid_source(const RPar &rp, const RBlk &R, long long id, Real dt) {
+// The fluid inversion of MomentFluidSourceImpl (ConToPrimSetup with
+// c2p_fail_on_floors and c2p_fail_on_ceilings true, moments_source.cpp:286-295):
+// con2prim_robust's solve of zone (k, j, i) from its stored mu, writing
+// prims, cell speeds and (bounds used) conserved variables.  fp carries the
+// two failure flags set.  True on success.
+bool fluid_invert(const phx_params &fp, const Blk &B, int k, int j, int i) {
+  GeomPt g;
+  Geom(nullptr, nullptr).at(CENT, 0, 0, 0, g);
+  const EOS eos{fp.gm1, fp.Cv};
+  const Bounds bounds(fp);
+  const long long id = B.idx(k, j, i);
+  const ZoneRef z{B.b->prim + id, B.b->cons + id, B.vs};
+  Real sig[3];
+  const C2PResult r = con2prim_core(g, eos, bounds, fp, B.Xc(1, i), B.Xc(2, j), B.Xc(3, k), z, z.P(PHX_PMU), sig);
+  if (r.evals == 0) return false;  // NaN input: nothing written
+  for (int d = 0; d < B.ndim; d++) B.b->cell_sig[d * B.vs + id] = sig[d];
+  return r.success;
+}
+
+// update_fluid = true (moments_source.cpp:807-965): the fluid loses what the
+// radiation gained (dE, cov_dF: the solve's last values, whether or not the
+// radiation kept them), is inverted, and the closure inversion runs with the
+// new fluid velocity (frail strategy).  On failure of either inversion the
+// fluid is reset to rho = u = 10 SMALL at rest (P, T and the bulk modulus in
+// the gamma1 slot, prim2con into D, S, tau) and the radiation to J = SMALL,
+// H = 0 through the closure of the reset fluid, with the tilde-pressure
+// tensor as the failed inversion left it (zero if the fluid failed).  B
+// primitives enter that prim2con as stored (zero without MHD).
+void update_fluid_zone(const RPar &rp, const phx_params &fp, const RBlk &R, int k, int j, int i, long long id,
+                       Real dE, const V3 &cov_dF) {
+  const Real sdetgam = 1.0;
+  const Blk &B = R.B;
+  auto FU = [&](int v) -> Real & { return B.b->cons[v * B.vs + id]; };
+  auto FP = [&](int v) -> Real & { return B.b->prim[v * B.vs + id]; };
+  FU(PHX_CENG) -= sdetgam * dE;
+  for (int a = 0; a < 3; a++) FU(PHX_CMOM + a) -= sdetgam * cov_dF(a);
+  T2 Pi;
+  for (int a = 0; a < 3; a++)
+    for (int c = 0; c < 3; c++) Pi(a, c) = 0.0;
+  Real E = R.U(PHX_RE, id) / sdetgam;
+  V3 covF, covH;
+  Real J;
+  if (fluid_invert(fp, B, k, j, i)) {
+    Real W;
+    const V3 cv = R.con_v(id, &W);
+    const Closure c(cv, rp.m1, false);
+    for (int a = 0; a < 3; a++) covF(a) = R.U(PHX_RF + a, id) / sdetgam;
+    Real xi = 0.0, phi = PI;
+    c.TilPiFromCon(E, covF, xi, phi, Pi);
+    if (c.Con2Prim(E, covF, Pi, J, covH) == SUCCESS) {
+      R.Q(PHX_RJ, id) = J;
+      for (int a = 0; a < 3; a++) R.Q(PHX_RH + a, id) = covH(a) / J;
+      return;
+    }
+  }
+  const EOS eos{fp.gm1, fp.Cv};
+  FP(PHX_PRHO) = 10. * SMALL;
+  FP(PHX_PENG) = 10. * SMALL;
+  for (int a = 0; a < 3; a++) FP(PHX_PVEL + a) = 0.;
+  FP(PHX_PPRS) = eos.PressureFromDensityInternalEnergy(FP(PHX_PRHO), ratio(FP(PHX_PENG), FP(PHX_PRHO)));
+  FP(PHX_PTMP) = eos.TemperatureFromDensityInternalEnergy(FP(PHX_PRHO), ratio(FP(PHX_PENG), FP(PHX_PRHO)));
+  FP(PHX_PGM1) = eos.BulkModulusFromDensityTemperature(FP(PHX_PRHO), FP(PHX_PTMP));
+  const Real vp[3] = {FP(PHX_PVEL), FP(PHX_PVEL + 1), FP(PHX_PVEL + 2)};
+  Real bp[3] = {0.0, 0.0, 0.0};
+  if (fp.mhd)
+    for (int a = 0; a < 3; a++) bp[a] = FP(PHX_PB + a);
+  GeomPt g;
+  Geom(nullptr, nullptr).at(CENT, 0, 0, 0, g);
+  Real D, tau, S[3], bcons[3], sig[3];
+  p2c(FP(PHX_PRHO), vp, bp, FP(PHX_PENG), FP(PHX_PPRS), FP(PHX_PGM1), g.gcov, g.gamcon, g.beta, g.alpha, sdetgam, D,
+      S, bcons, tau, sig);
+  FU(PHX_CRHO) = D;
+  for (int a = 0; a < 3; a++) FU(PHX_CMOM + a) = S[a];
+  FU(PHX_CENG) = tau;
+  Real Wc;
+  const V3 cv2 = R.con_v(id, &Wc);
+  const Closure c(cv2, rp.m1, false);
+  R.Q(PHX_RJ, id) = SMALL;
+  J = R.Q(PHX_RJ, id);
+  for (int a = 0; a < 3; a++) {
+    R.Q(PHX_RH + a, id) = 0.;
+    covH(a) = R.Q(PHX_RH + a, id) * J;
+  }
+  c.Prim2Con(J, covH, Pi, E, covF);
+  R.U(PHX_RE, id) = E * sdetgam;
+  for (int a = 0; a < 3; a++) R.U(PHX_RF + a, id) = covF(a) * sdetgam;
+}
+
+// MomentFluidSourceImpl, oned solver, one species (moments_source.cpp:203-490
+// and 786-965); fp: the fluid inversion's settings (update_fluid).  Returns 1
+// when the source update was applied.
+int fluid_source(const RPar &rp, const phx_params &fp, const RBlk &R, int k, int j, int i, Real dt) {
+  const long long id = R.B.idx(k, j, i);
   const Real alpha = 1.0, sdetgam = 1.0;
   const Real alpha_max = rp.tau_max / (alpha * dt);
   const Real rho = R.fp(PHX_PRHO, id), ug = R.fp(PHX_PENG, id), Tf = R.fp(PHX_PTMP, id);
@@ -3005,6 +3096,10 @@ int fluid_source(const RPar &rp, const RBlk &R, long long id, Real dt) {
   if (success) {
     R.U(PHX_RE, id) += sdetgam * dE;
     for (int a = 0; a < 3; a++) R.U(PHX_RF + a, id) += sdetgam * cov_dF(a);
+  }
+  if (rp.update_fluid) {
+    update_fluid_zone(rp, fp, R, k, j, i, id, dE, cov_dF);
+    return success ? 1 : 0;
   }
   T2 Pi;
   Real E = R.U(PHX_RE, id) / sdetgam;
@@ -3138,11 +3233,14 @@ long long orc_rad_fluid_source(const phx_rad_params *rp, const phx_params *p, co
   const RPar P(*rp, *p);
   const RBlk R(fb, rb);
   const orc::Blk &B = R.B;
+  phx_params fp = *p;  // the inversion MomentFluidSourceImpl sets up
+  fp.c2p_fail_on_floors = 1;
+  fp.c2p_fail_on_ceilings = 1;
   long long applied = 0;
 #pragma omp parallel for collapse(2) schedule(dynamic, 4) reduction(+ : applied)
   for (int k = B.ks(); k <= B.ke(); k++)
     for (int j = B.js(); j <= B.je(); j++)
-      for (int i = B.is(); i <= B.ie(); i++) applied += fluid_source(P, R, B.idx(k, j, i), dt);
+      for (int i = B.is(); i <= B.ie(); i++) applied += fluid_source(P, fp, R, k, j, i, dt);
   return applied;
 }
 

@@ -197,6 +197,7 @@ _SIGS = {
     "phx_rad_fill_ghosts_periodic": (C.c_int, [_P, C.POINTER(BlockS), C.POINTER(RadBlockS), _P]),
     "phx_rad_estimate_timestep": (C.c_int, [_P, C.POINTER(RadParams), C.POINTER(Params), C.POINTER(BlockS), C.POINTER(RadBlockS), _P, _P]),
     "phx_rad_stage": (C.c_int, [_P, C.POINTER(RadParams), C.POINTER(Params), C.POINTER(BlockS), C.POINTER(RadBlockS), _P, _P, C.c_double, C.c_double, _P]),
+    "phx_rad_fluid_stage": (C.c_int, [_P, C.POINTER(RadParams), C.POINTER(Params), C.POINTER(BlockS), C.POINTER(RadBlockS), _P, _P, _P, _P, C.c_double, C.c_double, _P]),
     "phx_batch_info": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "phx_mlp_set_weights": (C.c_int, [_P, C.POINTER(C.c_float)]),
     "phx_mlp_get_weights": (C.c_int, [_P, C.POINTER(C.c_float)]),

@@ -1031,8 +1031,6 @@ phx_status check_rad(const phx_rad_params *rp, const phx_params *p, const phx_bl
   if (rp->oned_fixup_strategy < PHX_RAD_ONED_FIXUP_NONE || rp->oned_fixup_strategy > PHX_RAD_ONED_FIXUP_IGNORE_ALL)
     return fail(PHX_ERR_INVALID_ARG, "radiation/oned_fixup_strategy has an invalid entry!");
   if (rp->src_rootfind_maxiter < 0) return fail(PHX_ERR_INVALID_ARG, "src_rootfind_maxiter < 0");
-  if (rp->update_fluid)
-    return fail(PHX_ERR_UNSUPPORTED, "the coupled fluid update of MomentFluidSource is not built (update_fluid = 1)");
   if (p == nullptr) return fail(PHX_ERR_INVALID_ARG, "params is NULL");
   if (fb && fb->geom && fb->geom->kind != PHX_GEOM_MINKOWSKI)
     return fail(PHX_ERR_UNSUPPORTED, "radiation moments are built for Minkowski blocks only");
@@ -1048,6 +1046,7 @@ phx::rad::RPar make_rpar(const phx_rad_params &rp, const phx_params &p) {
   r.recon = rp.recon;
   r.maxiter = rp.src_rootfind_maxiter;
   r.oned_fixup = rp.oned_fixup_strategy;
+  r.update_fluid = rp.update_fluid != 0;
   r.cfl = rp.cfl;
   r.tol = rp.src_rootfind_tol;
   r.kappa_a = rp.kappa_a;
@@ -1078,6 +1077,16 @@ phx_status make_rview(const phx::BView &v, const phx_rad_block *rb, bool need_fl
 }
 
 // fluid block view + radiation view + parameters, validated
+// The fluid inversion MomentFluidSourceImpl sets up for update_fluid
+// (moments_source.cpp:286-295): the fluid's tolerance, iteration cap and
+// floor scale, failing on floors and on ceilings.
+phx::Par source_inversion_par(const phx_params &p) {
+  phx::Par fp = make_par(p);
+  fp.fail_on_floors = 1;
+  fp.fail_on_ceilings = 1;
+  return fp;
+}
+
 phx_status rad_setup(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_block *fb,
                      const phx_rad_block *rb, bool need_flux, phx::BView &v, phx::rad::RView &r,
                      phx::rad::RPar &par) {
@@ -1175,7 +1184,11 @@ phx_status phx_rad_fluid_source(phx_ctx *ctx, const phx_rad_params *rp, const ph
   phx::rad::RPar par;
   phx_status s;
   if ((s = rad_setup(ctx, rp, p, fb, rb, false, v, r, par))) return s;
-  phx::rad::launch_source(par, v, r, dt, S(stream));
+  if (par.update_fluid) {
+    if ((s = check_params(p))) return s;
+    if (!fb->cell_sig) return fail(PHX_ERR_INVALID_ARG, "update_fluid needs the fluid block's cell_sig");
+  }
+  phx::rad::launch_source(par, source_inversion_par(*p), v, r, dt, S(stream));
   return cuda_status("phx_rad_fluid_source");
 }
 
@@ -1216,6 +1229,8 @@ phx_status phx_rad_stage(phx_ctx *ctx, const phx_rad_params *rp, const phx_param
     return fail(PHX_ERR_UNSUPPORTED,
                 "radiation floors in ApplyFloors and RadConservedToPrimitiveFixup are not built "
                 "(fixup/enable_floors and fixup/enable_c2p_fixup must be off)");
+  if (par.update_fluid)
+    return fail(PHX_ERR_INVALID_ARG, "update_fluid = 1 evolves the fluid too: use phx_rad_fluid_stage");
   cudaStream_t st = S(stream);
   phx::rad::launch_opacities(par, v, r, st);
   phx::rad::launch_fluxes(par, v, r, st);
@@ -1223,10 +1238,56 @@ phx_status phx_rad_stage(phx_ctx *ctx, const phx_rad_params *rp, const phx_param
   phx::rad::RView ro = r;
   ro.cons = out;
   phx::rad::launch_c2p(par, v, ro, interior(v), st);
-  phx::rad::launch_source(par, v, ro, beta * dt, st);
+  phx::rad::launch_source(par, source_inversion_par(*p), v, ro, beta * dt, st);
   phx::rad::launch_ghosts(v, ro, st);
   phx::rad::launch_c2p(par, v, ro, entire(v), st);
   return cuda_status("phx_rad_stage");
+}
+
+phx_status phx_rad_fluid_stage(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_block *fb,
+                               const phx_rad_block *rb, const double *fluid_base, double *fluid_out,
+                               const double *rad_base, double *rad_out, double beta, double dt, void *stream) {
+  phx::BView v;
+  phx::rad::RView r;
+  phx::rad::RPar par;
+  phx_status s;
+  if ((s = rad_setup(ctx, rp, p, fb, rb, true, v, r, par)) || (s = check_params(p))) return s;
+  if (!fluid_base || !fluid_out || !rad_base || !rad_out)
+    return fail(PHX_ERR_INVALID_ARG, "fluid_base/fluid_out/rad_base/rad_out is NULL");
+  if (!fb->flux || !fb->face_sig || !fb->cell_sig || !fb->fail || !fb->src)
+    return fail(PHX_ERR_INVALID_ARG, "stage needs flux, face_sig, cell_sig, fail, src");
+  if (p->mhd && fb->ndim > 1 && !fb->emf) return fail(PHX_ERR_INVALID_ARG, "emf is NULL");
+  if (v.ng < 3) return fail(PHX_ERR_INVALID_ARG, "radiation fluxes need ng >= 3");
+  if (fb->nx1 < fb->ng || (fb->ndim >= 2 && fb->nx2 < fb->ng) || (fb->ndim >= 3 && fb->nx3 < fb->ng))
+    return fail(PHX_ERR_INVALID_ARG, "periodic exchange needs nx >= ng");
+  if (p->enable_floors || p->enable_c2p_fixup)
+    return fail(PHX_ERR_UNSUPPORTED,
+                "radiation floors in ApplyFloors and RadConservedToPrimitiveFixup are not built "
+                "(fixup/enable_floors and fixup/enable_c2p_fixup must be off)");
+  par.update_fluid = 1;  // MomentFluidSource(update_fluid = fluid active)
+  const phx::Par fpar = make_par(*p);
+  cudaStream_t st = S(stream);
+  phx::launch_sources(fpar, v, st);                      // CalculateFluidSourceTerms
+  phx::launch_fluxes_err(fpar, v, ctx->err, st);         // fluid CalculateFluxes
+  if (p->mhd && fb->ndim > 1) phx::launch_fluxct(v, st);  // FluxCT
+  phx::rad::launch_opacities(par, v, r, st);              // MomentCalculateOpacities
+  phx::rad::launch_fluxes(par, v, r, st);                 // radiation CalculateFluxes
+  phx::launch_update(fpar, v, fluid_base, fluid_out, beta, dt, st);
+  phx::rad::launch_update(v, r, rad_base, rad_out, beta, dt, st);
+  phx::BView vo = v;
+  vo.cons = fluid_out;
+  phx::rad::RView ro = r;
+  ro.cons = rad_out;
+  // FillDerived over the mesh: the fluid's con2prim, then MomentCon2Prim
+  // (PostFillDerived, with the new fluid velocity)
+  phx::launch_c2p(fpar, vo, entire(vo), ctx->stats, ctx->err, nullptr, ctx->c2p, st);
+  phx::rad::launch_c2p(par, vo, ro, interior(vo), st);
+  phx::rad::launch_source(par, source_inversion_par(*p), vo, ro, beta * dt, st);  // MomentFluidSource
+  phx::launch_ghost_periodic(vo, fluid_out, p->mhd ? PHX_NCONS : 5, st);         // boundary exchange
+  phx::rad::launch_ghosts(vo, ro, st);
+  phx::launch_c2p(fpar, vo, entire(vo), ctx->stats, ctx->err, nullptr, ctx->c2p, st);  // FillDerived (block)
+  phx::rad::launch_c2p(par, vo, ro, entire(vo), st);
+  return cuda_status("phx_rad_fluid_stage");
 }
 
 }  // extern "C"

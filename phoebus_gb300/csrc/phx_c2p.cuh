@@ -381,7 +381,10 @@ __device__ __forceinline__ bool rf_running(const Par &p, const RFState &s) {
 // The Illinois iterations (root_find.hpp:120-166), warp-synchronous: every
 // lane stays in the loop until the warp's vote says none is still
 // iterating.  A lane stops after cap iterations in total even if it has not
-// converged (rf_running stays true: the caller resumes it later).
+// converged (rf_running stays true: the caller resumes it later).  WARP =
+// false: the lane loops on its own (for callers whose lanes may have left;
+// the arithmetic is the same).
+template <bool WARP = true>
 __device__ __forceinline__ void rf_iterate(const Par &p, Residual &res, bool valid, RFState &s, int cap) {
   const double tol = p.c2p_tol;
   const int max_iter = p.c2p_max_iter;
@@ -389,7 +392,7 @@ __device__ __forceinline__ void rf_iterate(const Par &p, Residual &res, bool val
   const double sign = s.sign;
   int it = s.it, b1 = s.b1, b2 = s.b2, evals = s.evals;
   bool active = valid && s.bracketed && (b - a > 2.0 * tol) && (it < max_iter) && (it < cap);
-  while (__any_sync(0xffffffffu, active)) {
+  while (WARP ? __any_sync(0xffffffffu, active) : active) {
     if (active) {
       const double c = div_p(a * yb - b * ya, yb - ya);
       if (c == a) {

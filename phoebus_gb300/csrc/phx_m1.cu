@@ -1,11 +1,13 @@
 // phx_m1.cu -- radiation moment transport (M1 and Eddington closures) on the
-// device: one neutrino species, Minkowski metric, static fluid background.
+// device: one neutrino species, Minkowski metric, a static fluid background
+// or (update_fluid) a fluid that exchanges energy and momentum with the
+// radiation in the source step.
 //
 // Follows, in the reference's floating-point operation order (paths relative
 // to the phoebus tree): radiation/closure.hpp:49-352 (ClosureEdd),
 // closure_m1.hpp:31-372 (ClosureM1), local_three_geometry.hpp:140-185,
 // linear_algebra.hpp:58-96, moments.cpp:61-995, moments_source.cpp:152-958
-// (oned solver, update_fluid = false), radiation.cpp:681-733,
+// (oned solver; update_fluid with the fluid's con2prim), radiation.cpp:681-733,
 // root_find.hpp:111-160.  With the identity spatial metric each contraction
 // keeps the order of its non-zero terms (for finite values the zero terms of
 // the full 3x3 sums change no rounding).  std::pow(x, 2) and std::pow(x, 3)
@@ -873,8 +875,122 @@ __device__ __forceinline__ double regula_falsi(const TRes &f, double a, double b
   return 0.5 * (a + b);
 }
 
+// con2prim_robust's solve (con2prim_robust.hpp:299-453) of one zone of the
+// Minkowski fluid block with MomentFluidSourceImpl's settings (fp fails on
+// floors and ceilings), from the stored mu.  The lane iterates on its own.
+// Writes the primitives, the cell speeds and, when bounds were used, the
+// conserved variables.  True on success; an unbracketed root is a failure.
+__device__ bool fluid_invert(const Par &fp, const BView &b, int k, int j, int i, long long id) {
+  const long long vs = b.vs;
+  Pt g{};
+  double U[PHX_NCONS];
+#pragma unroll
+  for (int m = 0; m < PHX_NCONS; m++) U[m] = b.cons[m * vs + id];
+  Residual res;
+  double rcon[3], rcov[3], bu[3], Bprim[3] = {0.0, 0.0, 0.0}, bdotr = 0.0;
+  if (!c2p_setup<true>(fp, g, U, b.Xc(0, i), b.Xc(1, j), b.Xc(2, k), res, rcon, rcov, bu, Bprim, bdotr))
+    return false;
+  const double guess = b.prim[PHX_PMU * vs + id];
+  RFState st;
+  rf_start<false>(fp, res, true, 0.0, 1.0, guess, nullptr, st);
+  rf_iterate<false>(fp, res, true, st, fp.c2p_max_iter);
+  C2POut out{0, 0, false, true, false, false};
+  const double mu = rf_result(st, guess, out);
+  double prim[PHX_NPRIM], sig[3];
+  bool used_bounds;
+  c2p_finish<true>(fp, g, res, mu, rcon, bu, Bprim, bdotr, prim, U, sig, used_bounds);
+  for (int v = 0; v < PHX_NPRIM; v++) {
+    if (v >= PHX_PB && v < PHX_PB + 3 && !fp.mhd) continue;
+    b.prim[v * vs + id] = prim[v];
+  }
+  if (used_bounds) {
+    b.cons[PHX_CRHO * vs + id] = U[PHX_CRHO];
+    b.cons[PHX_CENG * vs + id] = U[PHX_CENG];
+    for (int m = 0; m < 3; m++) b.cons[(PHX_CMOM + m) * vs + id] = U[PHX_CMOM + m];
+  }
+  for (int d = 0; d < b.ndim; d++) b.cell_sig[d * vs + id] = sig[d];
+  const int num_nans = isnan(U[PHX_CRHO]) + isnan(U[PHX_CMOM]) + isnan(U[PHX_CENG]);
+  bool ok = out.bracketed && num_nans == 0;
+  if (fp.fail_on_floors && (res.used_density_floor || res.used_energy_floor)) ok = false;
+  if (fp.fail_on_ceilings && res.used_gamma_max) ok = false;
+  return ok;
+}
+
+// update_fluid (moments_source.cpp:807-965): the fluid gives up the energy
+// and momentum the radiation took (dE, dF: the source solve's last values,
+// applied to the fluid whether or not the radiation kept them), is inverted,
+// and the closure inversion runs with the new fluid velocity.  When either
+// inversion fails, the fluid becomes a near-vacuum at rest (rho = u =
+// 10 SMALL, P, T and -- as the reference stores it -- the bulk modulus in
+// the gamma1 slot, then prim2con of D, S, tau) and the radiation the
+// J = SMALL, H = 0 state of that fluid's closure, with the tilde-pressure
+// tensor of the inversion that failed (zero when the fluid inversion failed).
 template <bool M1>
-__global__ void __launch_bounds__(128) k_source(RPar p, BView b, RView r, double dt, Range3 rg) {
+__device__ void source_update_fluid(const Par &fp, const BView &b, const RView &r, int k, int j, int i,
+                                    long long id, double dE, const V3 &dF) {
+  const long long vs = r.vs, fvs = b.vs;
+  const double sdetgam = 1.0;
+  b.cons[PHX_CENG * fvs + id] -= sdetgam * dE;
+#pragma unroll
+  for (int a = 0; a < 3; a++) b.cons[(PHX_CMOM + a) * fvs + id] -= sdetgam * dF.d[a];
+  T2 Pi;
+#pragma unroll
+  for (int a = 0; a < 3; a++)
+#pragma unroll
+    for (int c = 0; c < 3; c++) Pi.d[a][c] = 0.0;
+  double E = r.cons[PHX_RE * vs + id] / sdetgam;
+  V3 F, H;
+  double J;
+#pragma unroll
+  for (int a = 0; a < 3; a++) F.d[a] = r.cons[(PHX_RF + a) * vs + id] / sdetgam;
+  if (fluid_invert(fp, b, k, j, i, id)) {
+    const Closure<M1> c(fluid_v(b, id), false);
+    double xi = 0.0, phi = PI;
+    c.tilpi_from_con(E, F, xi, phi, Pi);
+    if (c.con2prim(E, F, Pi, J, H) == SUCCESS) {
+      r.prim[PHX_RJ * vs + id] = J;
+#pragma unroll
+      for (int a = 0; a < 3; a++) r.prim[(PHX_RH + a) * vs + id] = div_p(H.d[a], J);
+      return;
+    }
+  }
+  double *P = b.prim + id;
+  P[PHX_PRHO * fvs] = 10. * kSMALL;
+  P[PHX_PENG * fvs] = 10. * kSMALL;
+#pragma unroll
+  for (int a = 0; a < 3; a++) P[(PHX_PVEL + a) * fvs] = 0.;
+  P[PHX_PPRS * fvs] = eos_P_rho_sie(fp, P[PHX_PRHO * fvs], ratio(P[PHX_PENG * fvs], P[PHX_PRHO * fvs]));
+  P[PHX_PTMP * fvs] = eos_T_rho_sie(fp, P[PHX_PRHO * fvs], ratio(P[PHX_PENG * fvs], P[PHX_PRHO * fvs]));
+  P[PHX_PGM1 * fvs] = eos_bmod_rho_T(fp, P[PHX_PRHO * fvs], P[PHX_PTMP * fvs]);
+  const double vp[3] = {P[PHX_PVEL * fvs], P[(PHX_PVEL + 1) * fvs], P[(PHX_PVEL + 2) * fvs]};
+  double bp[3] = {0.0, 0.0, 0.0};
+  if (fp.mhd)
+#pragma unroll
+    for (int a = 0; a < 3; a++) bp[a] = P[(PHX_PB + a) * fvs];
+  Pt g{};
+  double D, tau, S[3], bc[3], sig[3];
+  p2c<true>(P[PHX_PRHO * fvs], vp, bp, P[PHX_PENG * fvs], P[PHX_PPRS * fvs], P[PHX_PGM1 * fvs], g, sdetgam, D, S,
+            bc, tau, sig);
+  b.cons[PHX_CRHO * fvs + id] = D;
+#pragma unroll
+  for (int a = 0; a < 3; a++) b.cons[(PHX_CMOM + a) * fvs + id] = S[a];
+  b.cons[PHX_CENG * fvs + id] = tau;
+  const Closure<M1> c(fluid_v(b, id), false);
+  r.prim[PHX_RJ * vs + id] = kSMALL;
+  J = r.prim[PHX_RJ * vs + id];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    r.prim[(PHX_RH + a) * vs + id] = 0.;
+    H.d[a] = r.prim[(PHX_RH + a) * vs + id] * J;
+  }
+  c.prim2con(J, H, Pi, E, F);
+  r.cons[PHX_RE * vs + id] = E * sdetgam;
+#pragma unroll
+  for (int a = 0; a < 3; a++) r.cons[(PHX_RF + a) * vs + id] = F.d[a] * sdetgam;
+}
+
+template <bool M1, bool UPD>
+__global__ void __launch_bounds__(128) k_source(RPar p, Par fp, BView b, RView r, double dt, Range3 rg) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= range_count(rg)) return;
   int k, j, i;
@@ -951,6 +1067,10 @@ __global__ void __launch_bounds__(128) k_source(RPar p, BView b, RView r, double
     r.cons[PHX_RE * vs + id] += sdetgam * dE;
 #pragma unroll
     for (int a = 0; a < 3; a++) r.cons[(PHX_RF + a) * vs + id] += sdetgam * dF.d[a];
+  }
+  if constexpr (UPD) {
+    source_update_fluid<M1>(fp, b, r, k, j, i, id, dE, dF);
+    return;
   }
   double E = r.cons[PHX_RE * vs + id] / sdetgam;
   V3 F, H;
@@ -1090,13 +1210,20 @@ void launch_update(const BView &b, const RView &r, const double *base, double *o
   k_update<<<blocks_for(range_count(rg), 256), 256, 0, s>>>(b, r, base, out, beta, dt, rg);
 }
 
-void launch_source(const RPar &p, const BView &b, const RView &r, double dt, cudaStream_t s) {
+void launch_source(const RPar &p, const Par &fp, const BView &b, const RView &r, double dt, cudaStream_t s) {
   const Range3 rg = interior3(b);
   const unsigned g = blocks_for(range_count(rg), 128);
-  if (p.m1)
-    k_source<true><<<g, 128, 0, s>>>(p, b, r, dt, rg);
-  else
-    k_source<false><<<g, 128, 0, s>>>(p, b, r, dt, rg);
+  if (p.m1) {
+    if (p.update_fluid)
+      k_source<true, true><<<g, 128, 0, s>>>(p, fp, b, r, dt, rg);
+    else
+      k_source<true, false><<<g, 128, 0, s>>>(p, fp, b, r, dt, rg);
+  } else {
+    if (p.update_fluid)
+      k_source<false, true><<<g, 128, 0, s>>>(p, fp, b, r, dt, rg);
+    else
+      k_source<false, false><<<g, 128, 0, s>>>(p, fp, b, r, dt, rg);
+  }
 }
 
 void launch_ghosts(const BView &b, const RView &r, cudaStream_t s) {

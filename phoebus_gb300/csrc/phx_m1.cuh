@@ -15,6 +15,7 @@ struct RPar {
   int recon;       // phx_recon
   int maxiter;     // src_rootfind_maxiter
   int oned_fixup;  // phx_rad_oned_fixup
+  int update_fluid;  // MomentFluidSource also updates and inverts the fluid
   double cfl, tol, kappa_a, kappa_s, jbb;
   double J_floor, xi_ceiling, tau_max, W_ceiling, Cv;
 };
@@ -31,7 +32,9 @@ void launch_opacities(const RPar &p, const BView &b, const RView &r, cudaStream_
 void launch_fluxes(const RPar &p, const BView &b, const RView &r, cudaStream_t s);
 void launch_update(const BView &b, const RView &r, const double *base, double *out, double beta, double dt,
                    cudaStream_t s);
-void launch_source(const RPar &p, const BView &b, const RView &r, double dt, cudaStream_t s);
+// fp: the fluid's con2prim settings for update_fluid (failure on floors and
+// ceilings, as MomentFluidSourceImpl sets them up)
+void launch_source(const RPar &p, const Par &fp, const BView &b, const RView &r, double dt, cudaStream_t s);
 void launch_ghosts(const BView &b, const RView &r, cudaStream_t s);
 void launch_dt(const RPar &p, const BView &b, const RView &r, unsigned long long *scratch, double *dt_out,
                cudaStream_t s);

@@ -7,11 +7,13 @@ radiation.cpp) for the moment_m1 / moment_eddington methods:
     MomentCalculateOpacities   moments.cpp:919-995
     ReconstructEdgeStates +
     CalculateFluxes            moments.cpp:280-736 (fused on the device)
-    MomentFluidSource          moments_source.cpp:203-958 (oned, update_fluid = false)
+    MomentFluidSource          moments_source.cpp:203-965 (oned; update_fluid either way)
     EstimateTimestepBlock      radiation.cpp:681-733
 plus the RK stage glue of PhoebusDriver::RungeKuttaStage with the fluid not
-evolved, and the problem generator radiation_advection
-(pgen/radiation_advection.cpp) that the radiation_diffusion regression runs.
+evolved (Stage) or evolved with the moments (FluidStage), and the problem
+generators radiation_advection (pgen/radiation_advection.cpp, which the
+radiation_diffusion regression runs) and radiation_equilibration
+(pgen/radiation_equilibration.cpp).
 All work runs on the GPU through include/phx_radiation.h; there is no CPU
 fallback.
 """
@@ -135,6 +137,25 @@ class RadiationContext:
         self.Stage(rp, p, b, base, base, 0.5, dt)
         b.arrays["rcons"] = base
 
+    def FluidStage(self, rp, p, b: Block, fbase, fout, rbase, rout, beta, dt, stream=None):
+        """One RK stage of the fluid and the moments together
+        (phx_rad_fluid_stage): b['cons'] and b['rcons'] are the stage inputs."""
+        s, r = b.struct(), rad_struct(b)
+        self._ok(self.lib.phx_rad_fluid_stage(self.h, C.byref(rp), C.byref(p), C.byref(s), C.byref(r), _ptr(fbase),
+                                              _ptr(fout), _ptr(rbase), _ptr(rout), float(beta), float(dt),
+                                              _stream(stream)))
+
+    def rk2_fluid_step(self, rp, p, b: Block, fluid_buf, rad_buf, dt):
+        """rk2 of the coupled system; U^{n+1} is left in b['cons'] and
+        b['rcons']."""
+        fb, rb = b.arrays["cons"], b.arrays["rcons"]
+        self.FluidStage(rp, p, b, fb, fluid_buf, rb, rad_buf, 1.0, dt)
+        b.arrays["cons"], b.arrays["rcons"] = fluid_buf, rad_buf
+        b._struct = None
+        self.FluidStage(rp, p, b, fb, fb, rb, rb, 0.5, dt)
+        b.arrays["cons"], b.arrays["rcons"] = fb, rb
+        b._struct = None
+
 
 # ---------------------------------------------------------------- problem
 def radiation_advection(nx1: int = 512, ng: int = 4, J0: float = 1.0, H=(0.0, 0.0, 0.0), vx: float = 0.3,
@@ -216,3 +237,33 @@ def radiation_pulse_3d(n: int = 128, ng: int = 4, v=(0.3, 0.0, 0.0), kappa_dx: f
     rpar = dict(method="moment_m1", recon="linear", cfl=0.5, kappa_s=kappa_dx / dx, kappa_a=kappa_a,
                 jbb_coeff=jbb_coeff)
     return b, par, rpar
+
+
+def radiation_equilibration(nx1: int = 4, ng: int = 4, rho0: float = 1.0, Tg0: float = 1.0, Tr0: float = 1.0e-2,
+                            kappa: float = 0.2, Cv: float = 1.0, Gamma: float = 1.6666666666666666667,
+                            jbb_coeff: float = 1.0):
+    """pgen/radiation_equilibration.cpp on inputs/radiation_equilibration.pin:
+    a 1D periodic Minkowski block of nx1 zones on [0, 1] (X2, X3 inactive on
+    [-1, 1]), gas at rest with rho = rho0, T = Tg0 (ideal gas, Gamma 5/3,
+    Cv 1), radiation J = JBB(Tr0), H = 0, over the entire block; gray
+    absorption kappa (the deck's gray_kappa 0.2, no scattering) with
+    JBB = jbb_coeff T^4 in the run's units.  The pgen sets every zone, ghosts
+    included, and prim2cons the fluid over the entire block
+    (fluid::PrimitiveToConserved) and the moments over the entire block;
+    the stored c2p guesses (mu, xi, phi) stay zero.  Returns (host Block,
+    fluid params, radiation params, tlim)."""
+    b = Block((nx1, 1, 1), ng=ng, ndim=1, xmin=(0.0, -1.0, -1.0), dx=(1.0 / nx1, 2.0, 2.0), backend="numpy")
+    b.alloc(["prim", "cons", "flux", "face_sig", "cell_sig", "fail", "src", "emf", "dudt"])
+    alloc_rad(b)
+    gm1 = Gamma - 1.0
+    P, R = b["prim"], b["rprim"]
+    P[abi.PRHO] = rho0
+    P[abi.PTMP] = Tg0
+    P[abi.PPRS] = max(0.0, gm1 * rho0 * Cv * Tg0)                      # PressureFromDensityTemperature
+    P[abi.PENG] = rho0 * max(0.0, Cv * Tg0)                            # rho * InternalEnergyFromDensityTemperature
+    P[abi.PGM1] = max(0.0, Gamma * gm1 * rho0 * Cv * Tg0) / P[abi.PPRS]  # BulkModulus / P
+    R[abi.RJ] = jbb_coeff * (Tr0 * Tr0) * (Tr0 * Tr0)
+    par = dict(Gamma=Gamma, Cv=Cv, recon="weno5", riemann="hll", cfl=0.8, mhd=0, c2p_max_iter=100)
+    rpar = dict(method="moment_eddington", recon="linear", cfl=0.8, kappa_s=0.0, kappa_a=kappa,
+                jbb_coeff=jbb_coeff)
+    return b, par, rpar, 1.0

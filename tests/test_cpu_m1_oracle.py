@@ -238,3 +238,98 @@ def test_closure_unit_known_answer(rad_oracle):
     H_in = x / np.sqrt(1.0 - v * v)
     wrong = ~((np.abs(1.0 - J_out) / 1.0 < 1.0e-5) & (np.abs(H_in - H_out) / 1.0 < 1.0e-5))
     assert len(x) == 6000 and wrong.sum() == 0, f"{wrong.sum()} of {len(x)} points wrong"
+
+
+# ---- coupled fluid update (MomentFluidSource with update_fluid = true)
+def equilibration_run(o, fo=None, steps=120, dt=0.01, kappa=5.0, nx1=4, b=None):
+    """The radiation_equilibration problem (gas at T = 1, radiation at
+    T = 0.01, gray absorption kappa) through any object with the RadOracle /
+    RadiationContext task names: fo (an Oracle or a FluidContext) initialises
+    the fluid, o the moments; fixed dt.  Returns (block, par, radiation par,
+    total energy tau + E per interior zone at the start)."""
+    hb, par, rpar, _ = radiation.radiation_equilibration(nx1=nx1, kappa=kappa)
+    b = hb if b is None else b(hb)
+    p, rp = abi.default_params(**par), abi.default_rad_params(**rpar)
+    fo.PrimitiveToConserved(p, b, *b.entire())
+    o.MomentPrim2Con(rp, p, b, *b.entire())
+    fo.FillGhostsPeriodic(b, b["cons"], 5)
+    o.FillGhostsPeriodic(b)
+    fo.ConservedToPrimitive(p, b)
+    o.MomentCon2Prim(rp, p, b)
+    ks, js, is_ = b.isl()
+    e0 = b["cons"][abi.CENG][ks, js, is_] + b["rcons"][abi.RE][ks, js, is_]
+    fbuf = b["cons"] * 0
+    rbuf = b["rcons"] * 0
+    for _ in range(steps):
+        o.rk2_fluid_step(rp, p, b, fbuf, rbuf, dt)
+    return b, p, rp, e0
+
+
+def test_equilibration_conserves_energy_and_equilibrates(rad_oracle):
+    """Gas and radiation at rest exchange energy only through the source:
+    tau + E per zone stays at its initial value to rounding, the gas cools
+    monotonically towards the temperature T_eq with Cv T_eq + JBB(T_eq) =
+    the initial total, and J approaches JBB(T_eq)."""
+    from oracle.oracle import Oracle
+
+    fo = Oracle()
+    b, p, rp, e0 = equilibration_run(rad_oracle, fo, steps=1)
+    T1 = b["prim"][abi.PTMP][b.isl()].copy()
+    assert np.all(T1 < 1.0) and np.all(T1 > 0.9)
+    b, p, rp, e0 = equilibration_run(rad_oracle, fo, steps=200)
+    ks, js, is_ = b.isl()
+    tot = b["cons"][abi.CENG][ks, js, is_] + b["rcons"][abi.RE][ks, js, is_]
+    assert np.max(np.abs(tot - e0) / e0) < 1e-13
+    T = b["prim"][abi.PTMP][ks, js, is_]
+    J = b["rprim"][abi.RJ][ks, js, is_]
+    e = float(e0.ravel()[0])
+    # T_eq from Cv T + T^4 = e (Cv = jbb = 1) by Newton
+    Teq = 0.7
+    for _ in range(50):
+        Teq -= (Teq + Teq ** 4 - e) / (1 + 4 * Teq ** 3)
+    assert np.allclose(T, Teq, rtol=1e-9, atol=0), (T.ravel(), Teq)
+    assert np.allclose(J, Teq ** 4, rtol=1e-8, atol=0)
+    assert np.all(b["fail"][0][ks, js, is_] == 1.0) and np.all(b["rprim"][abi.RFAIL][ks, js, is_] == 1.0)
+    assert np.all(b["prim"][abi.PVEL:abi.PVEL + 3][:, ks, js, is_] == 0.0)
+
+
+def test_update_fluid_failure_state(rad_oracle):
+    """A zone whose fluid cannot be inverted (NaN conserved density) leaves
+    MomentFluidSource with the reference's failure state: the fluid at
+    rho = u = 10 SMALL at rest with P = (Gamma - 1) rho u / rho,
+    T = (u / rho) / Cv, the bulk modulus Gamma (Gamma - 1) rho Cv T in the
+    gamma1 slot and D, S, tau from prim2con; the radiation at J = SMALL,
+    H = 0.  Other zones keep tau + E."""
+    from oracle.oracle import Oracle
+
+    fo = Oracle()
+    hb = random_rad_block((12, 1, 1), 1, seed=41, vmax=0.2)
+    p = abi.default_params(Gamma=5.0 / 3.0, Cv=1.0)
+    rp = abi.default_rad_params(method="moment_m1", kappa_a=3.0, kappa_s=5.0, jbb_coeff=0.5, update_fluid=1)
+    P = hb["prim"]
+    P[abi.PPRS] = p.gm1 * P[abi.PENG]
+    P[abi.PGM1] = p.gm1 + 1.0
+    fo.PrimitiveToConserved(p, hb, *hb.entire())
+    rad_oracle.MomentPrim2Con(rp, p, hb, *hb.entire())
+    rad_oracle.MomentCon2Prim(rp, p, hb)
+    rad_oracle.MomentCalculateOpacities(rp, p, hb)
+    bad = hb.ng + 5
+    hb["cons"][abi.CRHO][0, 0, bad] = np.nan
+    ks, js, is_ = hb.isl()
+    e0 = hb["cons"][abi.CENG][ks, js, is_] + hb["rcons"][abi.RE][ks, js, is_]
+    rad_oracle.MomentFluidSource(rp, p, hb, 0.05)
+    small = 10 * np.finfo(np.float64).tiny
+    z = (slice(None), 0, 0, bad)
+    Pz, Uz, Rz = hb["prim"][z], hb["cons"][z], hb["rprim"][z]
+    assert Pz[abi.PRHO] == 10 * small and Pz[abi.PENG] == 10 * small
+    assert np.all(Pz[abi.PVEL:abi.PVEL + 3] == 0.0)
+    sie = (10 * small) / (10 * small + small)
+    assert Pz[abi.PPRS] == p.gm1 * (10 * small) * sie
+    assert Pz[abi.PTMP] == sie / p.Cv
+    assert Pz[abi.PGM1] == (p.gm1 + 1) * p.gm1 * (10 * small) * p.Cv * Pz[abi.PTMP]
+    assert Uz[abi.CRHO] == Pz[abi.PRHO] and np.all(Uz[abi.CMOM:abi.CMOM + 3] == 0.0)
+    assert Rz[abi.RJ] == small and np.all(Rz[abi.RH:abi.RH + 3] == 0.0)
+    tot = hb["cons"][abi.CENG][ks, js, is_] + hb["rcons"][abi.RE][ks, js, is_]
+    keep = np.ones(tot.shape, bool)
+    keep[..., bad - hb.ng] = False
+    assert np.max(np.abs(tot - e0)[keep] / np.abs(e0)[keep]) < 1e-12

@@ -1,8 +1,10 @@
 """Radiation moments on the GPU against the oracle (exact build: bit for bit).
 
 Every task of include/phx_radiation.h on random 1D/2D/3D states (M1 and
-Eddington closures, each reconstruction), full RK stages, and the
-radiation_diffusion regression run (512 zones to t = 1, 655 steps): the exact
+Eddington closures, each reconstruction), full RK stages, the source with
+the coupled fluid update and the coupled fluid + moment stage
+(radiation_equilibration and a moving fluid), and the radiation_diffusion
+regression run (512 zones to t = 1, 655 steps): the exact
 build equals the oracle bit for bit, the production build stays within the
 oracle's agreement bands with the reference gold.
 """
@@ -197,17 +199,23 @@ def test_rad_configuration_errors(rx):
     db = hb.to_device()
     p = abi.default_params()
     with pytest.raises(abi.PhxError) as e:
-        rx.MomentCon2Prim(abi.default_rad_params(update_fluid=1), p, db)
-    assert e.value.status == 8
-    with pytest.raises(abi.PhxError) as e:
         rx.MomentCon2Prim(abi.default_rad_params(method=7), p, db)
-    assert e.value.status == 1
+    assert e.value.status == abi.PHX_ERR_INVALID_ARG
     import torch
 
     with pytest.raises(abi.PhxError) as e:
         rx.Stage(abi.default_rad_params(), abi.default_params(enable_floors=1), db, db["rcons"],
                  torch.zeros_like(db["rcons"]), 1.0, 1e-3)
-    assert e.value.status == 8
+    assert e.value.status == abi.PHX_ERR_UNSUPPORTED
+    # the radiation-only stage refuses update_fluid (the fluid stage carries it)
+    with pytest.raises(abi.PhxError, match="phx_rad_fluid_stage") as e:
+        rx.Stage(abi.default_rad_params(update_fluid=1), p, db, db["rcons"], torch.zeros_like(db["rcons"]), 1.0,
+                 1e-3)
+    assert e.value.status == abi.PHX_ERR_INVALID_ARG
+    with pytest.raises(abi.PhxError) as e:
+        rx.FluidStage(abi.default_rad_params(), abi.default_params(enable_c2p_fixup=1), db, db["cons"],
+                      torch.zeros_like(db["cons"]), db["rcons"], torch.zeros_like(db["rcons"]), 1.0, 1e-3)
+    assert e.value.status == abi.PHX_ERR_UNSUPPORTED
 
 
 @pytest.mark.parametrize("exact", [True, False])
@@ -248,3 +256,96 @@ def test_closure_unit_known_answer_gpu(rx, rf, rad_oracle, exact):
     H_in = x / np.sqrt(1.0 - v * v)
     wrong = ~((np.abs(1.0 - J_out) < 1.0e-5) & (np.abs(H_in - H_out) < 1.0e-5))
     assert wrong.sum() == 0
+
+
+def _coupled_pair(nx, ndim, seed, p, vmax=0.3):
+    """Host/device blocks with a random moving fluid whose conserved
+    variables are its prim2con (entire block) and random moments."""
+    from oracle.oracle import Oracle
+
+    hb = random_rad_block(nx, ndim, seed, vmax=vmax)
+    P = hb["prim"]
+    P[abi.PPRS] = p.gm1 * P[abi.PENG]
+    P[abi.PGM1] = p.gm1 + 1.0
+    Oracle().PrimitiveToConserved(p, hb, *hb.entire())
+    return hb, hb.to_device()
+
+
+@pytest.mark.parametrize("method,ndim", [("moment_m1", 1), ("moment_m1", 3), ("moment_eddington", 2)])
+def test_fluid_source_update_fluid_bitwise(rx, rad_oracle, method, ndim):
+    """MomentFluidSource with update_fluid = 1 (exact build): the fluid's tau
+    and S_i, its con2prim (prims, cell speeds, cons where bounds were used),
+    the closure inversion with the new velocity, and the failure state of a
+    zone whose fluid cannot be inverted (NaN D) equal the oracle bit for bit
+    in every fluid and radiation field of the interior."""
+    nx = {1: (64, 1, 1), 2: (20, 16, 1), 3: (10, 8, 8)}[ndim]
+    p = abi.default_params(Gamma=5.0 / 3.0, Cv=1.0)
+    rp = abi.default_rad_params(method=method, kappa_a=4.0, kappa_s=20.0, jbb_coeff=0.6, update_fluid=1)
+    hb, db = _coupled_pair(nx, ndim, 61 + ndim, p)
+    for o, b in ((rad_oracle, hb), (rx, db)):
+        o.MomentPrim2Con(rp, p, b, *b.entire())
+        o.MomentCon2Prim(rp, p, b)
+        o.MomentCalculateOpacities(rp, p, b)
+    ks, js, is_ = hb.isl()
+    bad = (ks.start, js.start, is_.start + 3)
+    hb["cons"][(abi.CRHO,) + bad] = np.nan
+    db["cons"][(abi.CRHO,) + bad] = float("nan")
+    for o, b in ((rad_oracle, hb), (rx, db)):
+        o.MomentFluidSource(rp, p, b, 0.05)
+    rx.check()
+    _cmp(db, hb, ["prim", "cons", "cell_sig", "rcons", "rprim"], "update_fluid source", (ks, js, is_))
+    assert host(db["rprim"])[(abi.RJ,) + bad] == 10 * np.finfo(np.float64).tiny
+
+
+@pytest.mark.parametrize("method,ndim", [("moment_m1", 1), ("moment_eddington", 2), ("moment_m1", 3)])
+def test_fluid_stage_rk2_bitwise(rx, rad_oracle, method, ndim):
+    """phx_rad_fluid_stage (exact build): three rk2 steps of a moving fluid
+    coupled to the moments (both packages' fluxes and updates, FillDerived,
+    MomentFluidSource with update_fluid, exchange, FillDerived) equal the
+    oracle's composed reference stage bit for bit in every field."""
+    import torch
+
+    nx = {1: (48, 1, 1), 2: (16, 16, 1), 3: (10, 8, 8)}[ndim]
+    p = abi.default_params(Gamma=5.0 / 3.0, Cv=1.0, recon="linear", riemann="hll", c2p_tol=1e-10,
+                           c2p_max_iter=100)
+    rp = abi.default_rad_params(method=method, recon="linear", cfl=0.5, kappa_a=2.0, kappa_s=10.0, jbb_coeff=0.4)
+    hb, db = _coupled_pair(nx, ndim, 71 + ndim, p, vmax=0.2)
+    for o, b in ((rad_oracle, hb), (rx, db)):
+        o.MomentPrim2Con(rp, p, b, *b.entire())
+        o.MomentCon2Prim(rp, p, b)
+    fh, rh = np.zeros_like(hb["cons"]), np.zeros_like(hb["rcons"])
+    fd, rd = torch.zeros_like(db["cons"]), torch.zeros_like(db["rcons"])
+    dt = 0.2 * min(hb.dx[d] for d in range(ndim))
+    for step in range(3):
+        rad_oracle.rk2_fluid_step(rp, p, hb, fh, rh, dt)
+        rx.rk2_fluid_step(rp, p, db, fd, rd, dt)
+        _cmp(db, hb, ["prim", "cons", "fail", "rcons", "rprim"], f"coupled step {step}")
+    rx.check()
+
+
+def test_equilibration_exact_and_production(rx, rf, rad_oracle):
+    """radiation_equilibration through phx_rad_fluid_stage: the exact build
+    equals the oracle bit for bit after 60 rk2 steps; the production build
+    conserves tau + E per zone to 1e-13 and reaches the oracle's gas
+    temperature and J within the con2prim tolerance (c2p_tol 1e-8, the
+    deck's default: the fluid inversion stops anywhere inside a bracket of
+    that relative width, and both builds take their own path to it)."""
+    from oracle.oracle import Oracle
+
+    from tests.test_cpu_m1_oracle import equilibration_run
+
+    hb, _, _, e0 = equilibration_run(rad_oracle, Oracle(), steps=60, nx1=16)
+    ctx_e, ctx_f = rx.fc, rf.fc
+    db, _, _, _ = equilibration_run(rx, ctx_e, steps=60, nx1=16, b=lambda h: h.to_device())
+    _cmp(db, hb, ["prim", "cons", "fail", "rcons", "rprim"], "equilibration (exact)")
+    fb, _, _, _ = equilibration_run(rf, ctx_f, steps=60, nx1=16, b=lambda h: h.to_device())
+    ks, js, is_ = hb.isl()
+    tot = host(fb["cons"])[abi.CENG][ks, js, is_] + host(fb["rcons"])[abi.RE][ks, js, is_]
+    assert np.max(np.abs(tot - e0) / e0) < 1e-13
+    for name, v in (("prim", abi.PTMP), ("rprim", abi.RJ)):
+        g, r = host(fb[name])[v][ks, js, is_], hb[name][v][ks, js, is_]
+        err = float(np.max(np.abs(g - r) / np.abs(r)))
+        print(f"[per-zone] equilibration production {name}[{v}] max rel {err:.2e}")
+        assert err < 1e-8
+    rx.check()
+    rf.check()
