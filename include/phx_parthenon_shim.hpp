@@ -22,7 +22,7 @@
 //   template <T> TaskStatus radiation::CalculateFluxes(T *)              moments.cpp:724
 //   template <T> TaskStatus radiation::CalculateGeometricSource(T *, T *) moments.cpp:886
 //   template <T> TaskStatus radiation::MomentFluidSource(T *, Real, bool) moments_source.cpp:960
-//   Real radiation::EstimateTimestepBlock(MeshBlockData<Real> *)         radiation.cpp:681
+//   Real radiation::EstimateTimestepBlock(MeshBlockData<Real> *)         radiation.cpp:585
 //   Real fluid::EstimateTimestepBlock(MeshBlockData<Real> *)             fluid.cpp:899
 //   template <T> using fluid::c2p_type = TaskStatus (*)(T *, ...)        fluid.hpp:65
 //
@@ -361,8 +361,9 @@ inline TaskStatus CalculateFluxes<MeshBlockData<Real>>(MeshBlockData<Real> *rc) 
   return TaskStatus::complete;
 }
 
-// Minkowski: every source term is zero (moments.cpp:820-870 with vanishing
-// metric derivatives); phx_rad_update adds it.
+// The geometric source is computed inside phx_rad_update (zero on
+// Minkowski; on FMKS per zone from the stage input), so the task itself has
+// nothing left to do.
 template <typename T>
 TaskStatus CalculateGeometricSource(T *rc, T *rc_src) {
   return TaskStatus::complete;

@@ -79,9 +79,12 @@ typedef struct {
   double J0_floor;
   int enable_rad_ceilings;
   double xi0_ceiling, tau0_ceiling;
-  /* 0: the fluid is not evolved (physics/hydro = false).  1 is the coupled
-   * fluid update of MomentFluidSource and is not built. */
+  /* MomentFluidSource's update_fluid: 0, the fluid is not evolved
+   * (physics/hydro = false); 1, the source hands the exchanged energy and
+   * momentum to the fluid and inverts it (phx_rad_fluid_stage sets it). */
   int update_fluid;
+  /* fixup/rad_c2p_failure_strategy: 0 interpolate (default), 1 floors */
+  int rad_c2p_failure_floors;
 } phx_rad_params;
 
 /* Radiation fields of one block.  Same shape and var_stride convention as
@@ -118,9 +121,11 @@ phx_status phx_rad_calculate_opacities(phx_ctx *ctx, const phx_rad_params *rp, c
 phx_status phx_rad_calculate_fluxes(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p,
                                     const phx_block *fb, const phx_rad_block *rb, void *stream);
 
-/* Parthenon FluxDivergence + SumData (the Minkowski geometric source of
- * CalculateGeometricSource, moments.cpp:756-885, is zero) +
- * AverageIndependentData + UpdateIndependentData on E, F_i (interior):
+/* Parthenon FluxDivergence + SumData with CalculateGeometricSource
+ * (moments.cpp:764-885: zero on Minkowski; on an FMKS block computed per
+ * zone from the stage input E, F_i, the stored J, H_i and the derivative
+ * table) + AverageIndependentData + UpdateIndependentData on E, F_i
+ * (interior):
  *   cons = beta cons + (1 - beta) base;  out = cons + beta dt dudt.
  * base and out are [PHX_RNCONS][N] arrays with the block's var_stride. */
 phx_status phx_rad_update(phx_ctx *ctx, const phx_rad_params *rp, const phx_block *fb, const phx_rad_block *rb,
@@ -145,34 +150,54 @@ phx_status phx_rad_fluid_source(phx_ctx *ctx, const phx_rad_params *rp, const ph
  * is periodic on every active axis. */
 phx_status phx_rad_fill_ghosts_periodic(phx_ctx *ctx, const phx_block *fb, const phx_rad_block *rb, void *stream);
 
-/* radiation::EstimateTimestepBlock (radiation.cpp:681-733): cfl * the
+/* radiation::EstimateTimestepBlock (radiation.cpp:585-648): cfl * the
  * minimum over interior zones and active directions of dx / csig, written to
  * dt_out_device. */
 phx_status phx_rad_estimate_timestep(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p,
                                      const phx_block *fb, const phx_rad_block *rb, double *dt_out_device,
                                      void *stream);
 
+/* fixup::RadConservedToPrimitiveFixup (fixup_radc2p.cpp:45-225), with
+ * p->enable_c2p_fixup: interior zones whose closure inversion failed take the
+ * c2pfail-weighted average of their face neighbours' J and H_i / J (or, with
+ * rp->rad_c2p_failure_floors or no valid neighbour, J = 10 SMALL, H = 0),
+ * H / J held to the xi ceiling, and E, F_i from prim2con. */
+phx_status phx_rad_c2p_fixup(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_block *fb,
+                             const phx_rad_block *rb, void *stream);
+
+/* fixup::ApplyFloors with the radiation active (fixup.cpp:285-678) over the
+ * range: the fluid part (as phx_apply_floors), then, with
+ * rp->enable_rad_floors (which needs p->enable_floors), the radiation part:
+ * the closure inversion again where the fluid floors or ceilings acted, the
+ * J floor as an added isotropic normal-observer field, the xi ceiling.
+ * rb->dudt is used as scratch. */
+phx_status phx_rad_apply_floors(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_block *fb,
+                                const phx_rad_block *rb, phx_range ib, phx_range jb, phx_range kb, void *stream);
+
 /* One RK stage of the moment transport on a periodic block, in the task
  * order of PhoebusDriver::RungeKuttaStage with hydro off
  * (phoebus_driver.cpp:349-362, 547-620, 640-668): opacities, fluxes,
- * update into out, con2prim, fluid source (beta dt), ghost exchange,
- * con2prim.  rb->cons is the stage input (the reference's sc0), base the
+ * update into out, FillDerived (con2prim over the entire block),
+ * RadConservedToPrimitiveFixup, ApplyFloors, fluid source (beta dt),
+ * ApplyFloors, ghost exchange, FillDerived, the fixup and the floors
+ * again (the fixups and floors as p / rp enable them).  rb->cons is the stage input (the reference's sc0), base the
  * step's initial state, out the stage output (sc1); everything after the
  * update acts on out and the shared prim fields. */
 phx_status phx_rad_stage(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_block *fb,
                          const phx_rad_block *rb, const double *base, double *out, double beta, double dt,
                          void *stream);
 
-/* One RK stage of the fluid and the moments together on a periodic
- * Minkowski block (physics/hydro = true, phoebus_driver.cpp:318-362,
- * 547-620, 640-680): fluid source terms, fluid fluxes, FluxCT, opacities,
- * radiation fluxes; both updates (fluid_base/fluid_out and rad_base/rad_out,
- * each [nvar][N] like its block's cons); FillDerived (the fluid's con2prim
- * over the entire block, then MomentCon2Prim); MomentFluidSource over
- * beta dt with update_fluid; the periodic exchange of the fluid's conserved
- * variables and the radiation fields; FillDerived again.  fb->cons and
- * rb->cons are the stage inputs.  Fluid floors and the c2p fixup must be off
- * (their radiation parts are not built); rp->update_fluid is implied. */
+/* One RK stage of the fluid and the moments together on a periodic block
+ * (physics/hydro = true, phoebus_driver.cpp:318-362, 547-620, 640-680):
+ * fluid source terms, fluid fluxes, FluxCT, opacities, radiation fluxes;
+ * both updates (fluid_base/fluid_out and rad_base/rad_out, each [nvar][N]
+ * like its block's cons); FillDerived (the fluid's con2prim over the entire
+ * block, then MomentCon2Prim), ConservedToPrimitiveFixup,
+ * RadConservedToPrimitiveFixup, ApplyFloors; MomentFluidSource over beta dt
+ * with update_fluid; ApplyFloors; the periodic exchange of the fluid's
+ * conserved variables and the radiation fields; FillDerived, the fixups and
+ * the floors again.  fb->cons and rb->cons are the stage inputs;
+ * rp->update_fluid is implied. */
 phx_status phx_rad_fluid_stage(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_block *fb,
                                const phx_rad_block *rb, const double *fluid_base, double *fluid_out,
                                const double *rad_base, double *rad_out, double beta, double dt, void *stream);

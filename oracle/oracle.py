@@ -88,6 +88,9 @@ def lib(tuned: bool = False) -> C.CDLL:
             ("orc_rad_calculate_opacities", [RP, PP, BS, RB], None),
             ("orc_rad_calculate_fluxes", [RP, PP, BS, RB], None),
             ("orc_rad_update", [RP, BS, RB, C.c_void_p, C.c_void_p, C.c_double, C.c_double], None),
+            ("orc_rad_geometric_source", [RP, BS, RB, C.c_void_p], None),
+            ("orc_rad_c2p_fixup", [RP, PP, BS, RB], None),
+            ("orc_rad_apply_floors", [RP, PP, BS, RB, abi.Range, abi.Range, abi.Range], None),
             ("orc_rad_fluid_source", [RP, PP, BS, RB, C.c_double], C.c_longlong),
             ("orc_rad_fill_ghosts_periodic", [BS, RB], None),
             ("orc_rad_estimate_timestep", [RP, PP, BS, RB], C.c_double),
@@ -345,6 +348,26 @@ class RadOracle:
         s, r = self._s(b)
         self.L.orc_rad_update(C.byref(rp), C.byref(s), C.byref(r), base.ctypes.data, out.ctypes.data, beta, dt)
 
+    def GeometricSource(self, rp, b: Block):
+        """CalculateGeometricSource over the interior: [4][k][j][i] (zero on
+        Minkowski blocks)."""
+        s, r = self._s(b)
+        out = np.zeros((abi.RNCONS,) + b.shape)
+        self.L.orc_rad_geometric_source(C.byref(rp), C.byref(s), C.byref(r), out.ctypes.data)
+        return out
+
+    def RadConservedToPrimitiveFixup(self, rp, p, b: Block):
+        s, r = self._s(b)
+        self.L.orc_rad_c2p_fixup(C.byref(rp), C.byref(p), C.byref(s), C.byref(r))
+
+    def ApplyFloors(self, rp, p, b: Block, ib=None, jb=None, kb=None):
+        """fixup::ApplyFloors with radiation active: the fluid part, then
+        (rp.enable_rad_floors) the radiation part."""
+        e = b.entire()
+        s, r = self._s(b)
+        self.L.orc_rad_apply_floors(C.byref(rp), C.byref(p), C.byref(s), C.byref(r), _r(ib or e[0]), _r(jb or e[1]),
+                                    _r(kb or e[2]))
+
     def MomentFluidSource(self, rp, p, b: Block, dt) -> int:
         s, r = self._s(b)
         return self.L.orc_rad_fluid_source(C.byref(rp), C.byref(p), C.byref(s), C.byref(r), dt)
@@ -376,18 +399,26 @@ class RadOracle:
     def Stage(self, rp, p, b: Block, base, out, beta, dt):
         """PhoebusDriver::RungeKuttaStage with the fluid not evolved
         (phoebus_driver.cpp:349-362, 547-620, 640-668): opacities, fluxes,
-        update into out, con2prim, the implicit source over beta dt, ghost
-        exchange, con2prim.  b['rcons'] is the stage input."""
+        update into out, con2prim, RadConservedToPrimitiveFixup, ApplyFloors,
+        the implicit source over beta dt, ApplyFloors, ghost exchange,
+        con2prim, fixup and floors again (each fixup and floor as p / rp
+        enable it).  b['rcons'] is the stage input."""
         self.MomentCalculateOpacities(rp, p, b)
         self.CalculateFluxes(rp, p, b)
         self.Update(rp, b, base, out, beta, dt)
         cons_in = b.arrays["rcons"]
         b.arrays["rcons"] = out
-        ib, jb, kb = b.interior()
-        self.MomentCon2Prim(rp, p, b, ib, jb, kb)
+
+        def derived():  # FillDerived (hydro off: the moments alone), the fixup, the floors
+            self.MomentCon2Prim(rp, p, b)
+            self.RadConservedToPrimitiveFixup(rp, p, b)
+            self.ApplyFloors(rp, p, b)
+
+        derived()
         self.MomentFluidSource(rp, p, b, beta * dt)
+        self.ApplyFloors(rp, p, b)
         self.FillGhostsPeriodic(b)
-        self.MomentCon2Prim(rp, p, b)
+        derived()
         b.arrays["rcons"] = cons_in
 
     def rk2_step(self, rp, p, b: Block, stage_buf, dt):
@@ -402,10 +433,11 @@ class RadOracle:
         active on one periodic block (phoebus_driver.cpp:318-362, 547-620,
         640-680): fluid source terms, fluxes, FluxCT, opacities, moment
         fluxes; both updates; FillDerived (fluid con2prim over the entire
-        block, then MomentCon2Prim); MomentFluidSource(update_fluid = true)
-        over beta dt; the periodic exchange of the fluid's conserved
-        variables and the radiation fields; FillDerived again.  b['cons'] and
-        b['rcons'] are the stage inputs."""
+        block, then MomentCon2Prim), the fluid and radiation c2p fixups,
+        ApplyFloors; MomentFluidSource(update_fluid = true) over beta dt;
+        ApplyFloors; the periodic exchange of the fluid's conserved variables
+        and the radiation fields; FillDerived, fixups and floors again.
+        b['cons'] and b['rcons'] are the stage inputs."""
         import copy
 
         orc = Oracle()
@@ -420,16 +452,22 @@ class RadOracle:
         self.Update(rp, b, rbase, rout, beta, dt)
         fin, rin = b.arrays["cons"], b.arrays["rcons"]
         b.arrays["cons"], b.arrays["rcons"] = fout, rout
-        orc.ConservedToPrimitive(p, b)
-        ib, jb, kb = b.interior()
-        self.MomentCon2Prim(rp, p, b, ib, jb, kb)
+
+        def derived():  # FillDerived, ConservedToPrimitiveFixup, RadConservedToPrimitiveFixup, ApplyFloors
+            orc.ConservedToPrimitive(p, b)
+            self.MomentCon2Prim(rp, p, b)
+            orc.ConservedToPrimitiveFixup(p, b)
+            self.RadConservedToPrimitiveFixup(rp, p, b)
+            self.ApplyFloors(rp, p, b)
+
+        derived()
         rpu = copy.copy(rp)
         rpu.update_fluid = 1
         self.MomentFluidSource(rpu, p, b, beta * dt)
+        self.ApplyFloors(rp, p, b)
         orc.FillGhostsPeriodic(b, b["cons"], abi.NCONS if p.mhd else 5)
         self.FillGhostsPeriodic(b)
-        orc.ConservedToPrimitive(p, b)
-        self.MomentCon2Prim(rp, p, b)
+        derived()
         b.arrays["cons"], b.arrays["rcons"] = fin, rin
 
     def rk2_fluid_step(self, rp, p, b: Block, fluid_buf, rad_buf, dt):

@@ -1442,7 +1442,9 @@ void c2p_fixup(const phx_params &par, const phx_block *blk) {
 
 // fixup.cpp:370-540 (ApplyFloorsImpl, fluid part) over the given range.
 // Returns the number of zones whose re-inversion failed (set to floors).
-long long apply_floors(const phx_params &par, const phx_block *blk, phx_range ib, phx_range jb, phx_range kb) {
+// flag (optional, [N]): 1 where floors or ceilings acted, else 0.
+long long apply_floors(const phx_params &par, const phx_block *blk, phx_range ib, phx_range jb, phx_range kb,
+                       double *flag = nullptr) {
   Blk B(blk);
   Geom G(blk->geom, &B);
   Bounds bounds(par);
@@ -1536,6 +1538,7 @@ long long apply_floors(const phx_params &par, const phx_block *blk, phx_range ib
           U(PHX_CENG) = taun;
           for (int ii = 0; ii < 3; ii++) U(PHX_CMOM + ii) = dS[ii];
         }
+        if (flag) flag[B.idx(k, j, i)] = (floor_applied || ceiling_applied) ? 1.0 : 0.0;
         if (floor_applied || ceiling_applied) {
           P(PHX_PTMP) = eos.TemperatureFromDensityInternalEnergy(P(PHX_PRHO), ratio(P(PHX_PENG), P(PHX_PRHO)));
           P(PHX_PPRS) = eos.PressureFromDensityTemperature(P(PHX_PRHO), P(PHX_PTMP));
@@ -2241,14 +2244,17 @@ void orc_torus_init(const phx_params *par, const phx_torus_params *tp, phx_block
 }  // extern "C"
 
 // =====================================================================
-// Radiation moments (M1 and Eddington closures), Minkowski, one species,
-// static fluid background.  Restates radiation/closure.hpp:49-352,
-// closure_m1.hpp:31-372, local_three_geometry.hpp:140-185, moments.cpp:61-995,
+// Radiation moments (M1 and Eddington closures), one species, on Minkowski
+// or FMKS blocks.  Restates radiation/closure.hpp:49-352,
+// closure_m1.hpp:31-372, local_three_geometry.hpp:123-185, moments.cpp:61-995
+// (with CalculateGeometricSourceImpl, moments.cpp:764-885),
 // moments_source.cpp:152-965 (oned solver, both update_fluid settings),
-// radiation.cpp:681-733, linear_algebra.hpp:58-96 and root_find.hpp:20-160.
+// radiation.cpp:585-648, linear_algebra.hpp:58-96 and root_find.hpp:20-160.
 // Minkowski: the spatial metric is the identity, lapse 1, shift 0.  Each
 // contraction keeps the reference's order over its non-zero terms; for finite
-// values the zero terms of the full 3x3 sums change no rounding.
+// values the zero terms of the full 3x3 sums change no rounding.  FMKS: the
+// cached tables' values at the cell centre or face, and the closures'
+// LocalThreeGeometry (gamma^ij from matrixInverse3x3, full 3x3 sums).
 // Third-party semantics restated from their definitions: gray opacities
 // (kappaJ = rho kappa_a, kappaH = kappaJ + rho kappa_s, JBB = a T^4; the
 // Rosseland means of a gray opacity are the gray values) and the
@@ -2368,6 +2374,62 @@ inline void SolveAxb2x2(Real A[2][2], Real b[2], Real x[2]) {
   x[0] = invDet * DifferenceOfProducts(A[1][1], b[0], A[0][1], b[1]);
   x[1] = invDet * DifferenceOfProducts(A[0][0], b[1], A[1][0], b[0]);
 }
+// linear_algebra.hpp:67-89: the adjugate over the determinant, each entry
+// a DifferenceOfProducts, the determinant expanded along the first column.
+inline Real matrixInverse3x3(const Real A[3][3], Real Ainv[3][3]) {
+  Ainv[0][0] = DifferenceOfProducts(A[1][1], A[2][2], A[1][2], A[2][1]);
+  Ainv[1][0] = -DifferenceOfProducts(A[1][0], A[2][2], A[1][2], A[2][0]);
+  Ainv[2][0] = DifferenceOfProducts(A[1][0], A[2][1], A[1][1], A[2][0]);
+  Ainv[0][1] = -DifferenceOfProducts(A[0][1], A[2][2], A[0][2], A[2][1]);
+  Ainv[1][1] = DifferenceOfProducts(A[0][0], A[2][2], A[0][2], A[2][0]);
+  Ainv[2][1] = -DifferenceOfProducts(A[0][0], A[2][1], A[0][1], A[2][0]);
+  Ainv[0][2] = DifferenceOfProducts(A[0][1], A[1][2], A[0][2], A[1][1]);
+  Ainv[1][2] = -DifferenceOfProducts(A[0][0], A[1][2], A[0][2], A[1][0]);
+  Ainv[2][2] = DifferenceOfProducts(A[0][0], A[1][1], A[0][1], A[1][0]);
+  const Real det = std::fma(A[0][0], Ainv[0][0], DifferenceOfProducts(A[2][0], Ainv[2][0], A[1][0], -Ainv[1][0]));
+  const Real invDet = 1.0 / det;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) Ainv[i][j] *= invDet;
+  return det;
+}
+
+// LocalThreeGeometry (local_three_geometry.hpp:123-185) off Minkowski:
+// gamma_ij of the location, gamma^ij from matrixInverse3x3 of it (not the
+// table's inverse), the lapse.  Contractions keep the reference's loop order.
+struct G3 {
+  Real cov[3][3], con[3][3], alpha;
+  G3() = default;
+  explicit G3(const GeomPt &p) {
+    for (int a = 0; a < 3; a++)
+      for (int b = 0; b < 3; b++) cov[a][b] = p.gcov[a + 1][b + 1];
+    matrixInverse3x3(cov, con);
+    alpha = p.alpha;
+  }
+  void lower(const V3 &a, V3 &o) const {
+    for (int i = 0; i < 3; i++) o(i) = 0.0;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) o(i) += a(j) * cov[i][j];
+  }
+  void raise(const V3 &a, V3 &o) const {
+    for (int i = 0; i < 3; i++) o(i) = 0.0;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) o(i) += a(j) * con[i][j];
+  }
+  Real contract_cov(const V3 &a, const V3 &b) const {  // contractCov3Vectors
+    Real s(0.0);
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) s += con[i][j] * a(i) * b(j);
+    return s;
+  }
+};
+
+// relativity_utils.hpp:38-43 (GetLorentzFactor with gamma_ij)
+inline Real lorentz_g(const Real vp[3], const G3 &g) {
+  Real vsq = 0.;
+  for (int ii = 0; ii < 3; ii++)
+    for (int jj = 0; jj < 3; jj++) vsq += g.cov[ii][jj] * vp[ii] * vp[jj];
+  return std::sqrt(1. + vsq);
+}
 
 // relativity_utils.hpp:38-43 with the spatial metric
 inline Real lorentz3(const Real vp[3]) {
@@ -2384,11 +2446,26 @@ constexpr Real SIN_PI = 1.2246467991473532e-16;  // sin of the double nearest pi
 // energy-conserving settings.
 struct Closure {
   bool m1, robust;
+  const G3 *geo;  // null: Minkowski (gamma_ij = delta_ij)
   V3 con_v, cov_v;
   Real v2, W, W2;
-  Closure(const V3 &cv, bool m1_, bool robust_) : m1(m1_), robust(robust_) {
+  void lower(const V3 &a, V3 &o) const {
+    if (geo)
+      geo->lower(a, o);
+    else
+      lower3(a, o);
+  }
+  void raise(const V3 &a, V3 &o) const {
+    if (geo)
+      geo->raise(a, o);
+    else
+      raise3(a, o);
+  }
+  Real ccv(const V3 &a, const V3 &b) const { return geo ? geo->contract_cov(a, b) : ccov(a, b); }
+  Real gcon(int i, int j) const { return geo ? geo->con[i][j] : gdelta(i, j); }
+  Closure(const V3 &cv, bool m1_, bool robust_, const G3 *g_ = nullptr) : m1(m1_), robust(robust_), geo(g_) {
     con_v = cv;
-    lower3(con_v, cov_v);
+    lower(con_v, cov_v);
     v2 = 0.0;
     for (int i = 0; i < 3; i++) v2 += con_v(i) * cov_v(i);
     v2 = smin(v2, 0.9999);
@@ -2403,7 +2480,7 @@ struct Closure {
       for (int j = 0; j < 3; j++) con_vPi(i) += cov_v(j) * Pi(i, j);
       vvPi += cov_v(i) * con_vPi(i);
     }
-    lower3(con_vPi, cov_vPi);
+    lower(con_vPi, cov_vPi);
   }
   void LinearSourceUpdate(Real Estar, const V3 &cov_Fstar, const T2 &Pi, Real JBB, Real tauJ, Real tauH,
                           Real &dE, V3 &cov_dF) const {
@@ -2431,8 +2508,15 @@ struct Closure {
     V3 con_H;
     T2 ccPi;
     for (int i = 0; i < 3; i++)
-      for (int j = 0; j < 3; j++) ccPi(i, j) = 0.0 + Pi(i, j);
-    raise3(cov_H, con_H);
+      for (int j = 0; j < 3; j++) {
+        if (geo) {
+          ccPi(i, j) = 0.0;
+          for (int k = 0; k < 3; k++) ccPi(i, j) += Pi(i, k) * geo->cov[k][j];
+        } else {
+          ccPi(i, j) = 0.0 + Pi(i, j);
+        }
+      }
+    raise(cov_H, con_H);
     for (int i = 0; i < 3; i++) {
       for (int j = 0; j < 3; j++)
         P(i, j) = 4.0 / 3.0 * W2 * con_v(i) * cov_v(j) * J + W * (con_v(i) * cov_H(j) + cov_v(j) * con_H(i)) +
@@ -2442,11 +2526,11 @@ struct Closure {
   }
   void ConP(Real J, const V3 &cov_H, const T2 &Pi, T2 &P) const {
     V3 con_H;
-    raise3(cov_H, con_H);
+    raise(cov_H, con_H);
     for (int i = 0; i < 3; i++)
       for (int j = 0; j < 3; j++)
         P(i, j) = 4.0 / 3.0 * W2 * con_v(i) * con_v(j) * J + W * (con_v(i) * con_H(j) + con_v(j) * con_H(i)) +
-                  J * Pi(i, j) + J / 3.0 * gdelta(i, j);
+                  J * Pi(i, j) + J / 3.0 * gcon(i, j);
   }
   void Prim2Con(Real J, const V3 &cov_H, const T2 &Pi, Real &E, V3 &cov_F) const {
     Real vvPi;
@@ -2458,13 +2542,18 @@ struct Closure {
     for (int i = 0; i < 3; i++)
       cov_F(i) = 4 * W2 / 3 * cov_v(i) * J + W * cov_v(i) * vH + W * cov_H(i) + J * cov_vPi(i);
   }
-  // getFluxesFromPrim (lapse 1: the final scalings are exact)
+  // getFluxesFromPrim (on Minkowski the lapse scalings by 1 are exact)
   void FluxesFromPrim(Real J, const V3 &cov_H, const T2 &Pi, V3 &con_F, T2 &P) const {
     ConCovP(J, cov_H, Pi, P);
     Real E;
     V3 cov_F;
     Prim2Con(J, cov_H, Pi, E, cov_F);
-    raise3(cov_F, con_F);
+    raise(cov_F, con_F);
+    if (geo) {
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) P(i, j) *= geo->alpha;
+      for (int i = 0; i < 3; i++) con_F(i) *= geo->alpha;
+    }
   }
   Status Con2Prim(Real E, const V3 &cov_F, const T2 &Pi, Real &J, V3 &cov_H) const {
     Real vvPi;
@@ -2477,7 +2566,7 @@ struct Closure {
     J = ratio((2 * W2 - 1) * E - 2 * W2 * vF, lam);
     for (int i = 0; i < 3; i++) cov_H(i) = (cov_F(i) - J * cov_vPi(i) - cov_v(i) * a) / W;
     const Real vh = cconcov(con_v, cov_H);
-    const Real xi = std::sqrt(ccov(cov_H, cov_H) - vh * vh) / J;
+    const Real xi = std::sqrt(ccv(cov_H, cov_H) - vh * vh) / J;
     if (std::isnan(xi) || std::isnan(J)) return FAILURE;
     if (J < 0. || xi >= 1.0) {
       if (robust) {
@@ -2494,7 +2583,7 @@ struct Closure {
   // M1FluidPressureTensor from J and H (closure_m1.hpp:274-299)
   void PressureFromPrim(Real J, const V3 &cov_H, T2 &Pi, V3 &con_f) const {
     V3 con_H;
-    raise3(cov_H, con_H);
+    raise(cov_H, con_H);
     Real H = 0.0, vH = 0.0;
     for (int i = 0; i < 3; i++) H += cov_H(i) * con_H(i);
     for (int i = 0; i < 3; i++) vH += cov_H(i) * con_v(i);
@@ -2504,7 +2593,7 @@ struct Closure {
     const Real athin = 0.5 * (3 * closure_fn(xi) - 1);
     for (int i = 0; i < 3; i++)
       for (int j = 0; j < 3; j++) {
-        Pi(i, j) = con_f(i) * con_f(j) - (W2 * con_v(i) * con_v(j) + gdelta(i, j)) / 3;
+        Pi(i, j) = con_f(i) * con_f(j) - (W2 * con_v(i) * con_v(j) + gcon(i, j)) / 3;
         Pi(i, j) *= athin;
       }
   }
@@ -2522,14 +2611,14 @@ struct Closure {
     const Real athin = 0.5 * (3 * closure_fn(xi) - 1);
     for (int i = 0; i < 3; i++)
       for (int j = 0; j < 3; j++) {
-        Pi(i, j) = con_f(i) * con_f(j) - (W2 * con_v(i) * con_v(j) + gdelta(i, j)) / 3;
+        Pi(i, j) = con_f(i) * con_f(j) - (W2 * con_v(i) * con_v(j) + gcon(i, j)) / 3;
         Pi(i, j) *= athin;
       }
   }
   // closure_m1.hpp:326-372
   void BasisVectors(const V3 &cov_F, V3 &g, V3 &dd) const {
     V3 con_F;
-    raise3(cov_F, con_F);
+    raise(cov_F, con_F);
     Real Fmag = 0.0, vl = 0.0, vv = 0.0;
     for (int i = 0; i < 3; i++) Fmag += cov_F(i) * con_F(i);
     Fmag = std::sqrt(Fmag);
@@ -2552,7 +2641,12 @@ struct Closure {
     V3 cov_H;
     Con2Prim(E, cov_F, Pi, J, cov_H);
     Real H(0.0), vH(0.0), Hf(0.0), vf(0.0);
-    for (int i = 0; i < 3; i++) H += cov_H(i) * cov_H(i);
+    if (geo) {
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) H += cov_H(i) * cov_H(j) * geo->con[i][j];
+    } else {
+      for (int i = 0; i < 3; i++) H += cov_H(i) * cov_H(i);
+    }
     for (int i = 0; i < 3; i++) vH += con_v(i) * cov_H(i);
     for (int i = 0; i < 3; i++) Hf += cov_H(i) * con_f(i);
     for (int i = 0; i < 3; i++) vf += cov_v(i) * con_f(i);
@@ -2654,10 +2748,11 @@ struct RPar {
   int recon;
   Real cfl, tol, kappa_a, kappa_s, jbb;
   int maxiter, oned_fixup;
-  bool update_fluid;
+  bool update_fluid, fixup_floors;
   Real J_floor, xi_ceiling, tau_max, W_ceiling, Cv;
   RPar(const phx_rad_params &rp, const phx_params &p) {
     update_fluid = rp.update_fluid != 0;
+    fixup_floors = rp.rad_c2p_failure_floors != 0;
     m1 = rp.method == PHX_RAD_M1;
     robust = !rp.closure_frail;
     bounds = rp.recon_fixup_bounds != 0;
@@ -2680,9 +2775,37 @@ struct RPar {
   Real JBB(Real T) const { return jbb * (T * T) * (T * T); }
 };
 
+// The geometry a moment task reads at one location (loc at k, j, i): the
+// tables' lapse, shift, gamma_ij, gamma^ij (MetricInverse) and sqrt(gamma),
+// and off Minkowski the LocalThreeGeometry built from them.
+struct RGeo {
+  GeomPt p;
+  G3 g3;
+  bool mink;
+  RGeo(const RBlk &R, Loc loc, int k, int j, int i) {
+    const Geom G(R.B.b->geom, &R.B);
+    G.at(loc, k, j, i, p);
+    mink = G.mink();
+    if (!mink) g3 = G3(p);
+  }
+  const G3 *g() const { return mink ? nullptr : &g3; }
+  Real cov(int a, int b) const { return p.gcov[a + 1][b + 1]; }
+  Real con(int a, int b) const { return p.gamcon[a][b]; }
+};
+// con_v = (W v^i) / W, W from gamma_ij (relativity_utils.hpp:38-43)
+inline V3 con_v_at(const RBlk &R, long long id, const RGeo &G, Real *Wout = nullptr) {
+  if (G.mink) return R.con_v(id, Wout);
+  const Real vp[3] = {R.fp(PHX_PVEL, id), R.fp(PHX_PVEL + 1, id), R.fp(PHX_PVEL + 2, id)};
+  const Real W = lorentz_g(vp, G.g3);
+  if (Wout) *Wout = W;
+  return V3{{vp[0] / W, vp[1] / W, vp[2] / W}};
+}
+
 // MomentPrim2Con (moments.cpp:198-256)
-void prim_to_con(const RPar &rp, const RBlk &R, long long id) {
-  const Closure c(R.con_v(id), rp.m1, true);
+void prim_to_con(const RPar &rp, const RBlk &R, int k, int j, int i) {
+  const long long id = R.B.idx(k, j, i);
+  const RGeo G(R, CENT, k, j, i);
+  const Closure c(con_v_at(R, id, G), rp.m1, true, G.g());
   const Real J = R.Q(PHX_RJ, id);
   const V3 covH{{R.Q(PHX_RH, id) * J, R.Q(PHX_RH + 1, id) * J, R.Q(PHX_RH + 2, id) * J}};
   T2 Pi;
@@ -2690,15 +2813,17 @@ void prim_to_con(const RPar &rp, const RBlk &R, long long id) {
   Real E;
   V3 covF;
   c.Prim2Con(J, covH, Pi, E, covF);
-  const Real sdetgam = 1.0;
+  const Real sdetgam = G.p.detgam;
   R.U(PHX_RE, id) = sdetgam * E;
   for (int d = 0; d < 3; d++) R.U(PHX_RF + d, id) = sdetgam * covF(d);
 }
 
 // MomentCon2PrimImpl (moments.cpp:61-159)
-void con_to_prim(const RPar &rp, const RBlk &R, long long id) {
-  const Real isdetgam = 1.0 / 1.0;
-  const Closure c(R.con_v(id), rp.m1, rp.robust);
+void con_to_prim(const RPar &rp, const RBlk &R, int k, int j, int i) {
+  const long long id = R.B.idx(k, j, i);
+  const RGeo G(R, CENT, k, j, i);
+  const Real isdetgam = 1.0 / G.p.detgam;
+  const Closure c(con_v_at(R, id, G), rp.m1, rp.robust, G.g());
   Real J;
   V3 covH;
   T2 Pi;
@@ -2783,9 +2908,10 @@ void face_flux(const RPar &rp, const RBlk &R, int d, int k, int j, int i) {
     cov_dJ(1) = (Jat(k, j + dj, i) + Jat(k - dk, j + dj, i) - Jat(k, j - dj, i) - Jat(k - dk, j - dj, i)) * idy4;
     cov_dJ(2) = (Jat(k, j, i) - Jat(k - dk, j, i)) * idz;
   }
-  const Real dx = B.dx(d + 1) * std::sqrt(1.0);
+  const RGeo G(R, d == 0 ? FACE1 : (d == 1 ? FACE2 : CENT), k, j, i);  // X3 faces: the centre table
+  const Real dx = B.dx(d + 1) * std::sqrt(G.cov(d, d));
   Real vpl[3] = {ql[4], ql[5], ql[6]}, vpr[3] = {qr[4], qr[5], qr[6]};
-  Real Wl = lorentz3(vpl), Wr = lorentz3(vpr);
+  Real Wl = G.mink ? lorentz3(vpl) : lorentz_g(vpl, G.g3), Wr = G.mink ? lorentz3(vpr) : lorentz_g(vpr, G.g3);
   if (rp.bounds) {
     if (Wl > rp.W_ceiling) {
       const Real rescale = std::sqrt(rp.W_ceiling * rp.W_ceiling - 1.) / (Wl * Wl - 1.);
@@ -2799,10 +2925,11 @@ void face_flux(const RPar &rp, const RBlk &R, int d, int k, int j, int i) {
     }
   }
   const V3 vl{{vpl[0] / Wl, vpl[1] / Wl, vpl[2] / Wl}}, vr{{vpr[0] / Wr, vpr[1] / Wr, vpr[2] / Wr}};
-  const Real sigp = 1.0 * std::sqrt(1.0) - 0.0;
-  const Real sigm = -1.0 * std::sqrt(1.0) - 0.0;
-  const Real asym_sigl = 1.0 * vl(d) - 0.0;
-  const Real asym_sigr = 1.0 * vr(d) - 0.0;
+  const Real alpha = G.p.alpha, beta_d = G.p.beta[d];
+  const Real sigp = alpha * std::sqrt(G.con(d, d)) - beta_d;
+  const Real sigm = -alpha * std::sqrt(G.con(d, d)) - beta_d;
+  const Real asym_sigl = alpha * vl(d) - beta_d;
+  const Real asym_sigr = alpha * vr(d) - beta_d;
 
   Real Jl = ql[0], Jr = qr[0];
   if (rp.bounds) {
@@ -2812,8 +2939,10 @@ void face_flux(const RPar &rp, const RBlk &R, int d, int k, int j, int i) {
   V3 Hl{{Jl * ql[1], Jl * ql[2], Jl * ql[3]}}, Hr{{Jr * qr[1], Jr * qr[2], Jr * qr[3]}};
   if (rp.bounds) {
     const Real vhl = cconcov(vl, Hl), vhr = cconcov(vr, Hr);
-    const Real xil = std::sqrt(ccov(Hl, Hl) - vhl * vhl) / Jl;
-    const Real xir = std::sqrt(ccov(Hr, Hr) - vhr * vhr) / Jr;
+    const Real hhl = G.mink ? ccov(Hl, Hl) : G.g3.contract_cov(Hl, Hl);
+    const Real hhr = G.mink ? ccov(Hr, Hr) : G.g3.contract_cov(Hr, Hr);
+    const Real xil = std::sqrt(hhl - vhl * vhl) / Jl;
+    const Real xir = std::sqrt(hhr - vhr * vhr) / Jr;
     if (xil > rp.xi_ceiling)
       for (int a = 0; a < 3; a++) Hl(a) *= rp.xi_ceiling / xil;
     if (xir > rp.xi_ceiling)
@@ -2825,7 +2954,7 @@ void face_flux(const RPar &rp, const RBlk &R, int d, int k, int j, int i) {
   V3 HasymL;
   for (int c = 0; c < 3; c++) HasymL(c) = ratio(-cov_dJ(c), 3 * kappaH + 3 * kappaH_min);
   const V3 HasymR = HasymL;
-  const Closure cl(vl, rp.m1, true), cr(vr, rp.m1, true);
+  const Closure cl(vl, rp.m1, true, G.g()), cr(vr, rp.m1, true, G.g());
   T2 Pil, Pir, Pl, Pr, Pl_asym, Pr_asym;
   V3 conFl, conFr, conFl_asym, conFr_asym, covFl, covFr;
   Real El, Er;
@@ -2851,16 +2980,81 @@ void face_flux(const RPar &rp, const RBlk &R, int d, int k, int j, int i) {
   const Real rad_sigspeed = smax(std::fabs(sigm), std::fabs(sigp));
   const Real asym_sigspeed = smax(std::fabs(asym_sigl), std::fabs(asym_sigr));
   const Real sigspeed = a * rad_sigspeed + (1. - a) * asym_sigspeed;
-  conFl(d) -= 0.0 * El;
-  conFr(d) -= 0.0 * Er;
+  conFl(d) -= beta_d * El;
+  conFr(d) -= beta_d * Er;
   for (int c = 0; c < 3; c++) {
-    Pl(d, c) -= 0.0 * covFl(c);
-    Pr(d, c) -= 0.0 * covFr(c);
+    Pl(d, c) -= beta_d * covFl(c);
+    Pr(d, c) -= beta_d * covFr(c);
   }
-  const Real sdetgam = 1.0;
+  const Real sdetgam = G.p.detgam;
   R.F(d, PHX_RE, id) = 0.5 * sdetgam * (conFl(d) + conFr(d) + sigspeed * (El - Er));
   for (int c = 0; c < 3; c++)
     R.F(d, PHX_RF + c, id) = 0.5 * sdetgam * (Pl(d, c) + Pr(d, c) + sigspeed * (covFl(c) - covFr(c)));
+  if (sdetgam < SMALL) {
+    R.F(d, PHX_RE, id) = 0.0;
+    for (int c = 0; c < 3; c++) R.F(d, PHX_RF + c, id) = 0.0;
+  }
+}
+
+// CalculateGeometricSourceImpl (moments.cpp:764-885) of one zone off
+// Minkowski: the radiation stress tensor T^{mu nu} from E, F^i (stage input)
+// and P^{ij} of J, H_i (the stored primitives), contracted with the
+// connection coefficients 0.5 (dg_{b a, c} + dg_{c a, b} - dg_{b c, a}) of the
+// derivative table, g^{0 r} and d ln(alpha).  src: E, F_1..3 (densitised).
+void geometric_source(bool m1, const RBlk &R, int k, int j, int i, Real src[4]) {
+  const long long id = R.B.idx(k, j, i);
+  const Geom Gm(R.B.b->geom, &R.B);
+  const RGeo G(R, CENT, k, j, i);
+  const V3 con_v = con_v_at(R, id, G);
+  const Closure c(con_v, m1, true, G.g());
+  const Real alp = G.p.alpha, sdetgam = G.p.detgam;
+  const Real *con_beta = G.p.beta;
+  Real con_g[4][4];
+  Gm.SpacetimeMetricInverse(G.p, con_g);
+  Real dlnalp[4], dg[4][4][4], Gamma[4][4][4];
+  Gm.GradLnAlpha(k, j, i, dlnalp);
+  Gm.MetricDerivative(k, j, i, dg);
+  for (int a = 0; a < 4; a++)
+    for (int b = 0; b < 4; b++)
+      for (int cc = 0; cc < 4; cc++) Gamma[a][b][cc] = 0.5 * (dg[b][a][cc] + dg[cc][a][b] - dg[b][cc][a]);
+  const Real con_n[4] = {1. / alp, -con_beta[0] / alp, -con_beta[1] / alp, -con_beta[2] / alp};
+  const Real E = R.U(PHX_RE, id) / sdetgam;
+  const Real J = R.Q(PHX_RJ, id);
+  const V3 covF{{R.U(PHX_RF, id) / sdetgam, R.U(PHX_RF + 1, id) / sdetgam, R.U(PHX_RF + 2, id) / sdetgam}};
+  const V3 covH{{J * R.Q(PHX_RH, id), J * R.Q(PHX_RH + 1, id), J * R.Q(PHX_RH + 2, id)}};
+  T2 conTilPi, conP;
+  c.TilPiFromPrim(J, covH, conTilPi);
+  c.ConP(J, covH, conTilPi, conP);
+  V3 conF;
+  G.g3.raise(covF, conF);
+  Real con_T[4][4];
+  for (int mu = 0; mu < 4; mu++)
+    for (int nu = 0; nu < 4; nu++) con_T[mu][nu] = 0;
+  for (int mu = 0; mu < 4; mu++)
+    for (int nu = 0; nu < 4; nu++) con_T[mu][nu] += con_n[mu] * con_n[nu] * E;
+  for (int mu = 0; mu < 4; mu++)
+    for (int ii = 0; ii < 3; ii++) {
+      con_T[mu][ii + 1] += con_n[mu] * conF(ii);
+      con_T[ii + 1][mu] += con_n[mu] * conF(ii);
+    }
+  for (int ii = 0; ii < 3; ii++)
+    for (int jj = 0; jj < 3; jj++) con_T[ii + 1][jj + 1] += conP(ii, jj);
+  Real TGam = 0.0;
+  for (int m = 0; m < 4; m++)
+    for (int n = 0; n < 4; n++) {
+      Real gam0 = 0.;
+      for (int r = 0; r < 4; r++) gam0 += con_g[0][r] * Gamma[r][m][n];
+      TGam += con_T[m][n] * gam0;
+    }
+  Real Ta = 0.0;
+  for (int m = 0; m < 4; m++) Ta += con_T[m][0] * dlnalp[m];
+  src[0] = sdetgam * alp * alp * (Ta - TGam);
+  for (int l = 0; l < 3; l++) {
+    Real src_mom = 0.0;
+    for (int m = 0; m < 4; m++)
+      for (int n = 0; n < 4; n++) src_mom += con_T[m][n] * (dg[n][l + 1][m] - Gamma[l + 1][n][m]);
+    src[1 + l] = alp * sdetgam * src_mom;
+  }
 }
 
 // The temperature residual of the oned solver (moments_source.cpp:152-196)
@@ -2948,7 +3142,7 @@ struct RF {
 // two failure flags set.  True on success.
 bool fluid_invert(const phx_params &fp, const Blk &B, int k, int j, int i) {
   GeomPt g;
-  Geom(nullptr, nullptr).at(CENT, 0, 0, 0, g);
+  Geom(B.b->geom, &B).at(CENT, k, j, i, g);
   const EOS eos{fp.gm1, fp.Cv};
   const Bounds bounds(fp);
   const long long id = B.idx(k, j, i);
@@ -2969,9 +3163,9 @@ bool fluid_invert(const phx_params &fp, const Blk &B, int k, int j, int i) {
 // H = 0 through the closure of the reset fluid, with the tilde-pressure
 // tensor as the failed inversion left it (zero if the fluid failed).  B
 // primitives enter that prim2con as stored (zero without MHD).
-void update_fluid_zone(const RPar &rp, const phx_params &fp, const RBlk &R, int k, int j, int i, long long id,
-                       Real dE, const V3 &cov_dF) {
-  const Real sdetgam = 1.0;
+void update_fluid_zone(const RPar &rp, const phx_params &fp, const RBlk &R, const RGeo &G, int k, int j, int i,
+                       long long id, Real dE, const V3 &cov_dF) {
+  const Real sdetgam = G.p.detgam;
   const Blk &B = R.B;
   auto FU = [&](int v) -> Real & { return B.b->cons[v * B.vs + id]; };
   auto FP = [&](int v) -> Real & { return B.b->prim[v * B.vs + id]; };
@@ -2985,8 +3179,8 @@ void update_fluid_zone(const RPar &rp, const phx_params &fp, const RBlk &R, int 
   Real J;
   if (fluid_invert(fp, B, k, j, i)) {
     Real W;
-    const V3 cv = R.con_v(id, &W);
-    const Closure c(cv, rp.m1, false);
+    const V3 cv = con_v_at(R, id, G, &W);
+    const Closure c(cv, rp.m1, false, G.g());
     for (int a = 0; a < 3; a++) covF(a) = R.U(PHX_RF + a, id) / sdetgam;
     Real xi = 0.0, phi = PI;
     c.TilPiFromCon(E, covF, xi, phi, Pi);
@@ -3007,8 +3201,7 @@ void update_fluid_zone(const RPar &rp, const phx_params &fp, const RBlk &R, int 
   Real bp[3] = {0.0, 0.0, 0.0};
   if (fp.mhd)
     for (int a = 0; a < 3; a++) bp[a] = FP(PHX_PB + a);
-  GeomPt g;
-  Geom(nullptr, nullptr).at(CENT, 0, 0, 0, g);
+  const GeomPt &g = G.p;
   Real D, tau, S[3], bcons[3], sig[3];
   p2c(FP(PHX_PRHO), vp, bp, FP(PHX_PENG), FP(PHX_PPRS), FP(PHX_PGM1), g.gcov, g.gamcon, g.beta, g.alpha, sdetgam, D,
       S, bcons, tau, sig);
@@ -3016,8 +3209,8 @@ void update_fluid_zone(const RPar &rp, const phx_params &fp, const RBlk &R, int 
   for (int a = 0; a < 3; a++) FU(PHX_CMOM + a) = S[a];
   FU(PHX_CENG) = tau;
   Real Wc;
-  const V3 cv2 = R.con_v(id, &Wc);
-  const Closure c(cv2, rp.m1, false);
+  const V3 cv2 = con_v_at(R, id, G, &Wc);
+  const Closure c(cv2, rp.m1, false, G.g());
   R.Q(PHX_RJ, id) = SMALL;
   J = R.Q(PHX_RJ, id);
   for (int a = 0; a < 3; a++) {
@@ -3034,11 +3227,12 @@ void update_fluid_zone(const RPar &rp, const phx_params &fp, const RBlk &R, int 
 // when the source update was applied.
 int fluid_source(const RPar &rp, const phx_params &fp, const RBlk &R, int k, int j, int i, Real dt) {
   const long long id = R.B.idx(k, j, i);
-  const Real alpha = 1.0, sdetgam = 1.0;
+  const RGeo G(R, CENT, k, j, i);
+  const Real alpha = G.p.alpha, sdetgam = G.p.detgam;
   const Real alpha_max = rp.tau_max / (alpha * dt);
   const Real rho = R.fp(PHX_PRHO, id), ug = R.fp(PHX_PENG, id), Tf = R.fp(PHX_PTMP, id);
   Real W;
-  const V3 con_v = R.con_v(id, &W);
+  const V3 con_v = con_v_at(R, id, G, &W);
   Real dE = 0.0;
   V3 cov_dF{{0.0, 0.0, 0.0}};
   bool success = false;
@@ -3056,7 +3250,7 @@ int fluid_source(const RPar &rp, const phx_params &fp, const RBlk &R, int k, int
       tries++;
       fac *= 10.;
     }
-    const Closure c(con_v, rp.m1, true);
+    const Closure c(con_v, rp.m1, true, G.g());
     Real Estar = R.U(PHX_RE, id) / sdetgam;
     V3 Fstar{{R.U(PHX_RF, id) / sdetgam, R.U(PHX_RF + 1, id) / sdetgam, R.U(PHX_RF + 2, id) / sdetgam}};
     Real J = R.Q(PHX_RJ, id);
@@ -3098,7 +3292,7 @@ int fluid_source(const RPar &rp, const phx_params &fp, const RBlk &R, int k, int
     for (int a = 0; a < 3; a++) R.U(PHX_RF + a, id) += sdetgam * cov_dF(a);
   }
   if (rp.update_fluid) {
-    update_fluid_zone(rp, fp, R, k, j, i, id, dE, cov_dF);
+    update_fluid_zone(rp, fp, R, G, k, j, i, id, dE, cov_dF);
     return success ? 1 : 0;
   }
   T2 Pi;
@@ -3107,7 +3301,7 @@ int fluid_source(const RPar &rp, const phx_params &fp, const RBlk &R, int k, int
   Real J;
   V3 covH;
   {
-    const Closure c(con_v, rp.m1, false);
+    const Closure c(con_v, rp.m1, false, G.g());
     for (int a = 0; a < 3; a++) covF(a) = R.U(PHX_RF + a, id) / sdetgam;
     Real xi = 0.0, phi = PI;
     c.TilPiFromCon(E, covF, xi, phi, Pi);
@@ -3119,8 +3313,8 @@ int fluid_source(const RPar &rp, const phx_params &fp, const RBlk &R, int k, int
   }
   // failed inversion: the reference's zero-radiation state
   Real Wc;
-  const V3 cv2 = R.con_v(id, &Wc);
-  const Closure c(cv2, rp.m1, false);
+  const V3 cv2 = con_v_at(R, id, G, &Wc);
+  const Closure c(cv2, rp.m1, false, G.g());
   R.Q(PHX_RJ, id) = SMALL;
   J = R.Q(PHX_RJ, id);
   for (int a = 0; a < 3; a++) {
@@ -3133,19 +3327,128 @@ int fluid_source(const RPar &rp, const phx_params &fp, const RBlk &R, int k, int
   return success ? 1 : 0;
 }
 
-// radiation.cpp:681-733 (one species; lapse 1, shift 0)
+// RadConservedToPrimitiveFixupImpl (fixup_radc2p.cpp:45-225) at an interior
+// zone whose closure inversion failed: the c2pfail-weighted neighbour average
+// of J and H_i / J (a failed neighbour contributes nothing), or J = 10 SMALL,
+// H = 0; the xi ceiling on H / J; E, F_i from prim2con.
+void rad_c2p_fixup_zone(const RPar &rp, const RBlk &R, int k, int j, int i) {
+  const Blk &B = R.B;
+  const long long id = B.idx(k, j, i);
+  if (R.Q(PHX_RFAIL, id) != 0.0) return;
+  const RGeo G(R, CENT, k, j, i);
+  const V3 con_v = con_v_at(R, id, G);
+  const long long di = 1, dj = B.n1t, dk = (long long)B.n1t * B.n2t;
+  auto F = [&](long long o) { return R.Q(PHX_RFAIL, o); };
+  auto nb = [&](int iv, long long o) { return F(o) != 0.0 ? F(o) * R.Q(iv, o) : 0.0; };
+  auto fixv = [&](int iv, Real norm) {
+    Real sum = nb(iv, id - di) + nb(iv, id + di);
+    if (B.ndim > 1) {
+      sum += nb(iv, id - dj) + nb(iv, id + dj);
+      if (B.ndim == 3) sum += nb(iv, id - dk) + nb(iv, id + dk);
+    }
+    return norm * sum;
+  };
+  Real num_valid = F(id - di) + F(id + di);
+  if (B.ndim > 1) num_valid += F(id - dj) + F(id + dj);
+  if (B.ndim == 3) num_valid += F(id - dk) + F(id + dk);
+  Real J;
+  V3 Hr;
+  if (num_valid > 0.5 && !rp.fixup_floors) {
+    const Real norm = 1.0 / num_valid;
+    J = fixv(PHX_RJ, norm);
+    for (int a = 0; a < 3; a++) Hr(a) = fixv(PHX_RH + a, norm);
+  } else {
+    J = 10. * SMALL;
+    for (int a = 0; a < 3; a++) Hr(a) = 0.;
+  }
+  const Real hh = G.mink ? ccov(Hr, Hr) : G.g3.contract_cov(Hr, Hr);
+  const Real vh = cconcov(con_v, Hr);
+  const Real xi = std::sqrt(hh - vh * vh);
+  if (xi > rp.xi_ceiling)
+    for (int a = 0; a < 3; a++) Hr(a) *= rp.xi_ceiling / xi;
+  R.Q(PHX_RJ, id) = J;
+  for (int a = 0; a < 3; a++) R.Q(PHX_RH + a, id) = Hr(a);
+  const Closure c(con_v, rp.m1, true, G.g());
+  V3 H{{Hr(0) * J, Hr(1) * J, Hr(2) * J}};
+  T2 Pi;
+  c.TilPiFromPrim(J, H, Pi);
+  Real E;
+  V3 Fc;
+  c.Prim2Con(J, H, Pi, E, Fc);
+  const Real sdetgam = G.p.detgam;
+  R.U(PHX_RE, id) = sdetgam * E;
+  for (int a = 0; a < 3; a++) R.U(PHX_RF + a, id) = sdetgam * Fc(a);
+}
+
+// ApplyFloorsImpl's radiation part (fixup.cpp:542-678, enable_rad_floors,
+// one species) after the fluid part of the zone; flag: the fluid part acted.
+void rad_floors_zone(const RPar &rp, const RBlk &R, int k, int j, int i, bool flag) {
+  const long long id = R.B.idx(k, j, i);
+  const RGeo G(R, CENT, k, j, i);
+  const Real sdetgam = G.p.detgam;
+  const V3 con_v = con_v_at(R, id, G);
+  const Closure c(con_v, rp.m1, true, G.g());
+  Real E, J;
+  V3 F, H;
+  T2 Pi;
+  auto invert = [&]() {
+    Real xi = 0.0, phi = std::acos(-1.0) * 1.000001;
+    c.TilPiFromCon(E, F, xi, phi, Pi);
+    c.Con2Prim(E, F, Pi, J, H);
+    R.Q(PHX_RJ, id) = J;
+    for (int a = 0; a < 3; a++) R.Q(PHX_RH + a, id) = H(a) / J;
+  };
+  if (flag) {
+    E = R.U(PHX_RE, id) / sdetgam;
+    for (int a = 0; a < 3; a++) F(a) = R.U(PHX_RF + a, id) / sdetgam;
+    invert();
+  }
+  const Real dJ = rp.J_floor - R.Q(PHX_RJ, id);
+  if (dJ > 0.) {
+    const V3 zero{{0.0, 0.0, 0.0}};
+    T2 Pz;
+    for (int a = 0; a < 3; a++)
+      for (int q = 0; q < 3; q++) Pz(a, q) = 0.0;
+    const Closure c_iso(zero, rp.m1, true, G.g());
+    c_iso.Prim2Con(dJ, zero, Pz, E, F);
+    E += R.U(PHX_RE, id) / sdetgam;
+    for (int a = 0; a < 3; a++) F(a) += R.U(PHX_RF + a, id) / sdetgam;
+    R.U(PHX_RE, id) = E * sdetgam;
+    for (int a = 0; a < 3; a++) R.U(PHX_RF + a, id) = F(a) * sdetgam;
+    invert();
+  }
+  const V3 Hr{{R.Q(PHX_RH, id), R.Q(PHX_RH + 1, id), R.Q(PHX_RH + 2, id)}};
+  const Real hh = G.mink ? ccov(Hr, Hr) : G.g3.contract_cov(Hr, Hr);
+  const Real vh = cconcov(con_v, Hr);
+  const Real xi = std::sqrt(hh - vh * vh);
+  if (xi > rp.xi_ceiling) {
+    J = R.Q(PHX_RJ, id);
+    for (int a = 0; a < 3; a++) {
+      H(a) = (rp.xi_ceiling / xi) * Hr(a) * J;
+      R.Q(PHX_RH + a, id) = H(a) / J;
+    }
+    c.TilPiFromPrim(J, H, Pi);
+    c.Prim2Con(J, H, Pi, E, F);
+    R.U(PHX_RE, id) = E * sdetgam;
+    for (int a = 0; a < 3; a++) R.U(PHX_RF + a, id) = F(a) * sdetgam;
+  }
+}
+
+// radiation.cpp:585-648 (one species)
 Real zone_dt(const RPar &rp, const RBlk &R, int k, int j, int i) {
   const long long id = R.B.idx(k, j, i);
+  const RGeo G(R, CENT, k, j, i);
+  const Real alpha = G.p.alpha;
   Real ldt = std::numeric_limits<Real>::max();
   const Real kappaH = R.Q(PHX_RKAPPAH, id);
   for (int d = 0; d < R.B.ndim; d++) {
-    const Real sigp = 1.0 * std::sqrt(1.0) - 0.0;
-    const Real sigm = -1.0 * std::sqrt(1.0) - 0.0;
-    const Real asym_sigl = 1.0 * R.fp(PHX_PVEL + d, id) - 0.0;
+    const Real sigp = alpha * std::sqrt(G.con(d, d)) - G.p.beta[d];
+    const Real sigm = -alpha * std::sqrt(G.con(d, d)) - G.p.beta[d];
+    const Real asym_sigl = alpha * R.fp(PHX_PVEL + d, id) - G.p.beta[d];
     const Real rad_speed = smax(std::fabs(sigm), std::fabs(sigp));
     const Real asym_speed = std::fabs(asym_sigl);
     const Real w = R.B.dx(d + 1);
-    const Real dx = w * std::sqrt(1.0);
+    const Real dx = w * std::sqrt(G.cov(d, d));
     const Real a = tanh_r(ratio(1.0, std::fabs(kappaH * dx)));
     const Real csig = a * rad_speed + (1. - a) * asym_speed;
     ldt = smin(ldt, 1.0 / (csig / w));
@@ -3166,7 +3469,7 @@ void orc_rad_prim_to_con(const phx_rad_params *rp, const phx_params *p, const ph
 #pragma omp parallel for collapse(2) schedule(static)
   for (int k = kb.s; k <= kb.e; k++)
     for (int j = jb.s; j <= jb.e; j++)
-      for (int i = ib.s; i <= ib.e; i++) prim_to_con(P, R, R.B.idx(k, j, i));
+      for (int i = ib.s; i <= ib.e; i++) prim_to_con(P, R, k, j, i);
 }
 
 void orc_rad_con_to_prim(const phx_rad_params *rp, const phx_params *p, const phx_block *fb, const phx_rad_block *rb,
@@ -3176,7 +3479,7 @@ void orc_rad_con_to_prim(const phx_rad_params *rp, const phx_params *p, const ph
 #pragma omp parallel for collapse(2) schedule(dynamic, 4)
   for (int k = kb.s; k <= kb.e; k++)
     for (int j = jb.s; j <= jb.e; j++)
-      for (int i = ib.s; i <= ib.e; i++) con_to_prim(P, R, R.B.idx(k, j, i));
+      for (int i = ib.s; i <= ib.e; i++) con_to_prim(P, R, k, j, i);
 }
 
 void orc_rad_calculate_opacities(const phx_rad_params *rp, const phx_params *p, const phx_block *fb,
@@ -3204,7 +3507,22 @@ void orc_rad_calculate_fluxes(const phx_rad_params *rp, const phx_params *p, con
 
 void orc_rad_update(const phx_rad_params *rp, const phx_block *fb, const phx_rad_block *rb, const double *base,
                     double *out, double beta, double dt) {
+  const bool m1 = rp->method == PHX_RAD_M1;
   const RBlk R(fb, rb);
+  // the geometric source reads the stage input: every zone's before the
+  // in-place averaging below touches any
+  std::vector<Real> gsrc;
+  if (fb->geom && fb->geom->kind != PHX_GEOM_MINKOWSKI) {
+    gsrc.assign(4 * (size_t)R.rvs, 0.0);
+    const orc::Blk &Bk = R.B;
+    for (int k = Bk.ks(); k <= Bk.ke(); k++)
+      for (int j = Bk.js(); j <= Bk.je(); j++)
+        for (int i = Bk.is(); i <= Bk.ie(); i++) {
+          Real src[4];
+          geometric_source(m1, R, k, j, i, src);
+          for (int m = 0; m < 4; m++) gsrc[m * R.rvs + Bk.idx(k, j, i)] = src[m];
+        }
+  }
   const orc::Blk &B = R.B;
   const Real dx1 = fb->dx1, dx2 = fb->dx2, dx3 = fb->dx3;
   const Real A1 = dx2 * dx3, A2 = dx1 * dx3, A3 = dx1 * dx2, V = dx1 * dx2 * dx3;
@@ -3219,7 +3537,7 @@ void orc_rad_update(const phx_rad_params *rp, const phx_block *fb, const phx_rad
           Real du = (A1 * R.F(0, m, id + s1) - A1 * R.F(0, m, id));
           if (B.ndim >= 2) du += A2 * R.F(1, m, id + s2) - A2 * R.F(1, m, id);
           if (B.ndim == 3) du += A3 * R.F(2, m, id + s3) - A3 * R.F(2, m, id);
-          const Real r = -du / V + 0.0;  // + the Minkowski geometric source
+          const Real r = -du / V + (gsrc.empty() ? 0.0 : gsrc[m * R.rvs + id]);  // + the geometric source
           rb->dudt[m * R.rvs + id] = r;
           Real u0 = R.U(m, id);
           u0 = beta * u0 + (1 - beta) * base[m * R.rvs + id];
@@ -3242,6 +3560,45 @@ long long orc_rad_fluid_source(const phx_rad_params *rp, const phx_params *p, co
     for (int j = B.js(); j <= B.je(); j++)
       for (int i = B.is(); i <= B.ie(); i++) applied += fluid_source(P, fp, R, k, j, i, dt);
   return applied;
+}
+
+// CalculateGeometricSource into out[4][N] over the interior (FMKS blocks;
+// zero on Minkowski), for tests of the source alone.
+void orc_rad_geometric_source(const phx_rad_params *rp, const phx_block *fb, const phx_rad_block *rb, double *out) {
+  const RBlk R(fb, rb);
+  const orc::Blk &B = R.B;
+  const bool curved = fb->geom && fb->geom->kind != PHX_GEOM_MINKOWSKI;
+  for (int k = B.ks(); k <= B.ke(); k++)
+    for (int j = B.js(); j <= B.je(); j++)
+      for (int i = B.is(); i <= B.ie(); i++) {
+        Real src[4] = {0.0, 0.0, 0.0, 0.0};
+        if (curved) geometric_source(rp->method == PHX_RAD_M1, R, k, j, i, src);
+        for (int m = 0; m < 4; m++) out[m * R.rvs + B.idx(k, j, i)] = src[m];
+      }
+}
+
+void orc_rad_c2p_fixup(const phx_rad_params *rp, const phx_params *p, const phx_block *fb, const phx_rad_block *rb) {
+  if (!p->enable_c2p_fixup) return;
+  const RPar P(*rp, *p);
+  const RBlk R(fb, rb);
+  const orc::Blk &B = R.B;
+  for (int k = B.ks(); k <= B.ke(); k++)
+    for (int j = B.js(); j <= B.je(); j++)
+      for (int i = B.is(); i <= B.ie(); i++) rad_c2p_fixup_zone(P, R, k, j, i);
+}
+
+// ApplyFloors with radiation active: the fluid part, then (enable_rad_floors)
+// the radiation part, zone by zone over the range.
+void orc_rad_apply_floors(const phx_rad_params *rp, const phx_params *p, const phx_block *fb, const phx_rad_block *rb,
+                          phx_range ib, phx_range jb, phx_range kb) {
+  const RPar P(*rp, *p);
+  const RBlk R(fb, rb);
+  std::vector<double> flag((size_t)R.B.N, 0.0);
+  orc::apply_floors(*p, fb, ib, jb, kb, flag.data());
+  if (!rp->enable_rad_floors || !p->enable_floors) return;
+  for (int k = kb.s; k <= kb.e; k++)
+    for (int j = jb.s; j <= jb.e; j++)
+      for (int i = ib.s; i <= ib.e; i++) rad_floors_zone(P, R, k, j, i, flag[R.B.idx(k, j, i)] != 0.0);
 }
 
 void orc_rad_fill_ghosts_periodic(const phx_block *fb, const phx_rad_block *rb) {

@@ -111,7 +111,7 @@ class RadParams(C.Structure):
                 ("src_rootfind_maxiter", C.c_int), ("oned_fixup_strategy", C.c_int), ("kappa_a", C.c_double),
                 ("kappa_s", C.c_double), ("jbb_coeff", C.c_double), ("enable_rad_floors", C.c_int),
                 ("J0_floor", C.c_double), ("enable_rad_ceilings", C.c_int), ("xi0_ceiling", C.c_double),
-                ("tau0_ceiling", C.c_double), ("update_fluid", C.c_int)]
+                ("tau0_ceiling", C.c_double), ("update_fluid", C.c_int), ("rad_c2p_failure_floors", C.c_int)]
 
 
 class RadBlockS(C.Structure):
@@ -198,6 +198,8 @@ _SIGS = {
     "phx_rad_estimate_timestep": (C.c_int, [_P, C.POINTER(RadParams), C.POINTER(Params), C.POINTER(BlockS), C.POINTER(RadBlockS), _P, _P]),
     "phx_rad_stage": (C.c_int, [_P, C.POINTER(RadParams), C.POINTER(Params), C.POINTER(BlockS), C.POINTER(RadBlockS), _P, _P, C.c_double, C.c_double, _P]),
     "phx_rad_fluid_stage": (C.c_int, [_P, C.POINTER(RadParams), C.POINTER(Params), C.POINTER(BlockS), C.POINTER(RadBlockS), _P, _P, _P, _P, C.c_double, C.c_double, _P]),
+    "phx_rad_c2p_fixup": (C.c_int, [_P, C.POINTER(RadParams), C.POINTER(Params), C.POINTER(BlockS), C.POINTER(RadBlockS), _P]),
+    "phx_rad_apply_floors": (C.c_int, [_P, C.POINTER(RadParams), C.POINTER(Params), C.POINTER(BlockS), C.POINTER(RadBlockS), Range, Range, Range, _P]),
     "phx_batch_info": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "phx_mlp_set_weights": (C.c_int, [_P, C.POINTER(C.c_float)]),
     "phx_mlp_get_weights": (C.c_int, [_P, C.POINTER(C.c_float)]),
@@ -298,7 +300,7 @@ def default_rad_params(**over) -> RadParams:
     r.kappa_a, r.kappa_s, r.jbb_coeff = 0.0, 0.0, 0.0
     r.enable_rad_floors, r.J0_floor = 0, 0.0
     r.enable_rad_ceilings, r.xi0_ceiling, r.tau0_ceiling = 0, 0.99, 1.0e3
-    r.update_fluid = 0
+    r.update_fluid, r.rad_c2p_failure_floors = 0, 0
     for k, v in over.items():
         if k == "method" and isinstance(v, str):
             v = RAD_METHOD[v]

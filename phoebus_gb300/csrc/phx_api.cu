@@ -1032,8 +1032,6 @@ phx_status check_rad(const phx_rad_params *rp, const phx_params *p, const phx_bl
     return fail(PHX_ERR_INVALID_ARG, "radiation/oned_fixup_strategy has an invalid entry!");
   if (rp->src_rootfind_maxiter < 0) return fail(PHX_ERR_INVALID_ARG, "src_rootfind_maxiter < 0");
   if (p == nullptr) return fail(PHX_ERR_INVALID_ARG, "params is NULL");
-  if (fb && fb->geom && fb->geom->kind != PHX_GEOM_MINKOWSKI)
-    return fail(PHX_ERR_UNSUPPORTED, "radiation moments are built for Minkowski blocks only");
   return PHX_OK;
 }
 
@@ -1047,6 +1045,7 @@ phx::rad::RPar make_rpar(const phx_rad_params &rp, const phx_params &p) {
   r.maxiter = rp.src_rootfind_maxiter;
   r.oned_fixup = rp.oned_fixup_strategy;
   r.update_fluid = rp.update_fluid != 0;
+  r.rad_fixup_floors = rp.rad_c2p_failure_floors != 0;
   r.cfl = rp.cfl;
   r.tol = rp.src_rootfind_tol;
   r.kappa_a = rp.kappa_a;
@@ -1085,6 +1084,25 @@ phx::Par source_inversion_par(const phx_params &p) {
   fp.fail_on_floors = 1;
   fp.fail_on_ceilings = 1;
   return fp;
+}
+
+// fixup::ApplyFloors with radiation active (fixup.cpp:285-678): the fluid
+// part over the range, recording where floors or ceilings acted in the
+// radiation scratch dudt, then, with fixup/enable_rad_floors, the radiation
+// part (the reference loops over no species otherwise).
+void rad_apply_floors(phx_ctx *ctx, const phx::Par &fpar, const phx::rad::RPar &par, const phx_rad_params &rp,
+                      const phx::BView &v, const phx::rad::RView &r, phx::Range3 rg, cudaStream_t st) {
+  double *flag = rp.enable_rad_floors ? r.dudt : nullptr;
+  phx::launch_floors(fpar, v, rg, ctx->stats, ctx->err, st, flag);
+  if (rp.enable_rad_floors && fpar.enable_floors) phx::rad::launch_rad_floors(par, v, r, flag, rg, st);
+}
+
+phx_status check_rad_fixups(const phx_rad_params *rp, const phx_params *p, const phx_rad_block *rb) {
+  if (rp->enable_rad_floors && !p->enable_floors)
+    return fail(PHX_ERR_INVALID_ARG, "enable_rad_floors needs fixup/enable_floors (the fixup package forces it on)");
+  if (rp->enable_rad_floors && !rb->dudt)
+    return fail(PHX_ERR_INVALID_ARG, "the radiation floors use the radiation block's dudt as scratch: it is NULL");
+  return PHX_OK;
 }
 
 phx_status rad_setup(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_block *fb,
@@ -1173,7 +1191,10 @@ phx_status phx_rad_update(phx_ctx *ctx, const phx_rad_params *rp, const phx_bloc
   phx::rad::RView r;
   if ((s = make_view(fb, v)) || (s = make_rview(v, rb, true, r))) return s;
   if (!base || !out) return fail(PHX_ERR_INVALID_ARG, "base/out is NULL");
-  phx::rad::launch_update(v, r, base, out, beta, dt, S(stream));
+  phx::rad::RPar par;
+  std::memset(&par, 0, sizeof(par));
+  par.m1 = rp->method == PHX_RAD_M1;  // the geometric source's closure (FMKS blocks)
+  phx::rad::launch_update(par, v, r, base, out, beta, dt, S(stream));
   return cuda_status("phx_rad_update");
 }
 
@@ -1225,23 +1246,54 @@ phx_status phx_rad_stage(phx_ctx *ctx, const phx_rad_params *rp, const phx_param
   if ((s = rad_setup(ctx, rp, p, fb, rb, true, v, r, par))) return s;
   if (!base || !out) return fail(PHX_ERR_INVALID_ARG, "base/out is NULL");
   if (v.ng < 3) return fail(PHX_ERR_INVALID_ARG, "radiation fluxes need ng >= 3");
-  if (p->enable_floors || p->enable_c2p_fixup)
-    return fail(PHX_ERR_UNSUPPORTED,
-                "radiation floors in ApplyFloors and RadConservedToPrimitiveFixup are not built "
-                "(fixup/enable_floors and fixup/enable_c2p_fixup must be off)");
+  if ((s = check_rad_fixups(rp, p, rb))) return s;
   if (par.update_fluid)
     return fail(PHX_ERR_INVALID_ARG, "update_fluid = 1 evolves the fluid too: use phx_rad_fluid_stage");
+  const phx::Par fpar = make_par(*p);
   cudaStream_t st = S(stream);
   phx::rad::launch_opacities(par, v, r, st);
   phx::rad::launch_fluxes(par, v, r, st);
-  phx::rad::launch_update(v, r, base, out, beta, dt, st);
+  phx::rad::launch_update(par, v, r, base, out, beta, dt, st);
   phx::rad::RView ro = r;
   ro.cons = out;
-  phx::rad::launch_c2p(par, v, ro, interior(v), st);
+  // hydro off: the fluid's con2prim and its c2p fixup do not run
+  auto derived = [&] {
+    phx::rad::launch_c2p(par, v, ro, entire(v), st);                      // FillDerived
+    if (p->enable_c2p_fixup) phx::rad::launch_rad_c2p_fixup(par, v, ro, st);  // RadConservedToPrimitiveFixup
+    rad_apply_floors(ctx, fpar, par, *rp, v, ro, entire(v), st);           // ApplyFloors
+  };
+  derived();
   phx::rad::launch_source(par, source_inversion_par(*p), v, ro, beta * dt, st);
+  rad_apply_floors(ctx, fpar, par, *rp, v, ro, entire(v), st);
   phx::rad::launch_ghosts(v, ro, st);
-  phx::rad::launch_c2p(par, v, ro, entire(v), st);
+  derived();
   return cuda_status("phx_rad_stage");
+}
+
+phx_status phx_rad_c2p_fixup(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_block *fb,
+                             const phx_rad_block *rb, void *stream) {
+  phx::BView v;
+  phx::rad::RView r;
+  phx::rad::RPar par;
+  phx_status s;
+  if ((s = rad_setup(ctx, rp, p, fb, rb, false, v, r, par))) return s;
+  if (p->enable_c2p_fixup) phx::rad::launch_rad_c2p_fixup(par, v, r, S(stream));
+  return cuda_status("phx_rad_c2p_fixup");
+}
+
+phx_status phx_rad_apply_floors(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_block *fb,
+                                const phx_rad_block *rb, phx_range ib, phx_range jb, phx_range kb, void *stream) {
+  phx::BView v;
+  phx::rad::RView r;
+  phx::rad::RPar par;
+  phx::Range3 rg;
+  phx_status s;
+  if ((s = rad_setup(ctx, rp, p, fb, rb, false, v, r, par)) || (s = check_range(v, ib, jb, kb, rg)) ||
+      (s = check_params(p)) || (s = check_rad_fixups(rp, p, rb)))
+    return s;
+  r.dudt = rb->dudt;
+  rad_apply_floors(ctx, make_par(*p), par, *rp, v, r, rg, S(stream));
+  return cuda_status("phx_rad_apply_floors");
 }
 
 phx_status phx_rad_fluid_stage(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_block *fb,
@@ -1260,10 +1312,7 @@ phx_status phx_rad_fluid_stage(phx_ctx *ctx, const phx_rad_params *rp, const phx
   if (v.ng < 3) return fail(PHX_ERR_INVALID_ARG, "radiation fluxes need ng >= 3");
   if (fb->nx1 < fb->ng || (fb->ndim >= 2 && fb->nx2 < fb->ng) || (fb->ndim >= 3 && fb->nx3 < fb->ng))
     return fail(PHX_ERR_INVALID_ARG, "periodic exchange needs nx >= ng");
-  if (p->enable_floors || p->enable_c2p_fixup)
-    return fail(PHX_ERR_UNSUPPORTED,
-                "radiation floors in ApplyFloors and RadConservedToPrimitiveFixup are not built "
-                "(fixup/enable_floors and fixup/enable_c2p_fixup must be off)");
+  if ((s = check_rad_fixups(rp, p, rb))) return s;
   par.update_fluid = 1;  // MomentFluidSource(update_fluid = fluid active)
   const phx::Par fpar = make_par(*p);
   cudaStream_t st = S(stream);
@@ -1273,20 +1322,27 @@ phx_status phx_rad_fluid_stage(phx_ctx *ctx, const phx_rad_params *rp, const phx
   phx::rad::launch_opacities(par, v, r, st);              // MomentCalculateOpacities
   phx::rad::launch_fluxes(par, v, r, st);                 // radiation CalculateFluxes
   phx::launch_update(fpar, v, fluid_base, fluid_out, beta, dt, st);
-  phx::rad::launch_update(v, r, rad_base, rad_out, beta, dt, st);
+  phx::rad::launch_update(par, v, r, rad_base, rad_out, beta, dt, st);
   phx::BView vo = v;
   vo.cons = fluid_out;
   phx::rad::RView ro = r;
   ro.cons = rad_out;
-  // FillDerived over the mesh: the fluid's con2prim, then MomentCon2Prim
-  // (PostFillDerived, with the new fluid velocity)
-  phx::launch_c2p(fpar, vo, entire(vo), ctx->stats, ctx->err, nullptr, ctx->c2p, st);
-  phx::rad::launch_c2p(par, vo, ro, interior(vo), st);
+  // FillDerived (the fluid's con2prim, then MomentCon2Prim with the new
+  // fluid velocity as PostFillDerived), ConservedToPrimitiveFixup,
+  // RadConservedToPrimitiveFixup, ApplyFloors
+  auto derived = [&] {
+    phx::launch_c2p(fpar, vo, entire(vo), ctx->stats, ctx->err, nullptr, ctx->c2p, st);
+    phx::rad::launch_c2p(par, vo, ro, entire(vo), st);
+    phx::launch_c2p_fixup(fpar, vo, st);
+    if (p->enable_c2p_fixup) phx::rad::launch_rad_c2p_fixup(par, vo, ro, st);
+    rad_apply_floors(ctx, fpar, par, *rp, vo, ro, entire(vo), st);
+  };
+  derived();
   phx::rad::launch_source(par, source_inversion_par(*p), vo, ro, beta * dt, st);  // MomentFluidSource
+  rad_apply_floors(ctx, fpar, par, *rp, vo, ro, entire(vo), st);                 // ApplyFloors
   phx::launch_ghost_periodic(vo, fluid_out, p->mhd ? PHX_NCONS : 5, st);         // boundary exchange
   phx::rad::launch_ghosts(vo, ro, st);
-  phx::launch_c2p(fpar, vo, entire(vo), ctx->stats, ctx->err, nullptr, ctx->c2p, st);  // FillDerived (block)
-  phx::rad::launch_c2p(par, vo, ro, entire(vo), st);
+  derived();
   return cuda_status("phx_rad_fluid_stage");
 }
 

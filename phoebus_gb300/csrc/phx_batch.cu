@@ -105,7 +105,7 @@ struct BatchPlan {
   bool mink = true;
   int ndim = 3;
   const MlpPacked *mlp = nullptr;  // learned start (packed weights in the context) or null
-  double *brk = nullptr;           // learned brackets, 3 x c2p items x 128
+  double *brk = nullptr;           // learned brackets + pass marker, 4 x c2p items x 128
   bool batched = true;             // one persistent launch per phase in a graph; else block by block
   bool has_mesh = false;           // tiled mesh exchange instead of per-block periodic ghosts
   int mesh_n[3] = {0, 0, 0}, mesh_nseg[3] = {0, 0, 0}, mesh_bc[6] = {0, 0, 0, 0, 0, 0}, mesh_bc_vars = 0;
@@ -509,7 +509,8 @@ cudaError_t batch_stage(BatchCache *cache, const Par &par, const phx_block *bloc
     if ((e = upload_items(P, P.update, make_items(interior, 256))) != cudaSuccess) return e;
     if ((e = upload_items(P, P.ghost, make_items(all, 256))) != cudaSuccess) return e;
     if ((e = upload_items(P, P.c2p, make_items(all, 128))) != cudaSuccess) return e;
-    if (mlp && (e = cudaMalloc(&P.brk, sizeof(double) * 3 * (size_t)P.c2p.n * 128)) != cudaSuccess) return e;
+    // learned brackets (3 planes) and each zone's warm / cold pass (plane 3)
+    if (mlp && (e = cudaMalloc(&P.brk, sizeof(double) * 4 * (size_t)P.c2p.n * 128)) != cudaSuccess) return e;
     if (mesh) {
       if ((e = upload_mesh(P, mesh, n)) != cudaSuccess) return e;
       std::vector<long long> fix;

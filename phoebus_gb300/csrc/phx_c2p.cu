@@ -526,7 +526,12 @@ void launch_mlp_bracket(const Par &p, long long n, const double *cons, const dou
 // (block, [first, last)) items; the root find runs to completion in place
 // (no iteration cap: the retry list is per chunk of one zone list).
 // Learned start of the batched con2prim: item it's zone first + tid gets
-// its bracket at brk[c * (nitems * C2P_THREADS) + it * C2P_THREADS + tid].
+// its bracket at brk[c * (nitems * C2P_THREADS) + it * C2P_THREADS + tid]
+// (c = 0, 1, 2) and in plane 3 its pass: 1.0 cold (no stored mu > 0: the
+// learned start), 0.0 warm (the plain start from the stored mu).  The passes
+// read plane 3, so each zone is inverted exactly once even when a warm
+// zone's new mu is not positive.  A warp none of whose cold zones has
+// features inside the network's input box skips the network.
 template <bool MINK>
 __global__ void __launch_bounds__(C2P_THREADS) kb_mlp_bracket(Par p, const BView *views, const WorkItem *items,
                                                               int nitems, const MlpPacked *mlp, double *brk,
@@ -542,9 +547,12 @@ __global__ void __launch_bounds__(C2P_THREADS) kb_mlp_bracket(Par p, const BView
     const BView &bv = views[w.block];
     const BoxZones zones{bv, Range3{0, bv.n1t - 1, 0, bv.n2t - 1, 0, bv.n3t - 1}};
     const long long q = w.first + threadIdx.x;
+    const long long o = (long long)it * C2P_THREADS + threadIdx.x;
     float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     bool ok = false;
-    const bool cold = q < w.last && !(zones.guess_of(q) > 0.0);  // warm zones: stored mu only
+    const bool valid = q < w.last;
+    const bool cold = valid && !(zones.guess_of(q) > 0.0);  // warm zones: stored mu only
+    if (valid) brk[3 * stride + o] = cold ? 1.0 : 0.0;
     if (cold) {
       long long id;
       Pt g{};
@@ -552,23 +560,27 @@ __global__ void __launch_bounds__(C2P_THREADS) kb_mlp_bracket(Par p, const BView
       zones.template load<MINK>(q, id, g, U, x1, x2, x3, guess);
       ok = c2p_features_fp32<MINK>(p, g, U, x1, x2, x3, f) && mlp_in_box(S->w, f);
     }
-    if (!__any_sync(0xffffffffu, cold)) continue;  // whole warp warm: no network
+    const double nan = __longlong_as_double(0x7ff8000000000000ll);
+    if (!__any_sync(0xffffffffu, ok)) {  // no usable start in this warp: no network
+      if (cold)
+        for (int c = 0; c < 3; c++) brk[c * stride + o] = nan;
+      continue;
+    }
     float o0, o1;
     mlp_warp_forward(S->w, f, S->xs[warp], S->os[warp], o0, o1);
     if (cold) {
       double lb[3];
       mlp_bracket(o0, o1, lb);
-      const double nan = __longlong_as_double(0x7ff8000000000000ll);
-      const long long o = (long long)it * C2P_THREADS + threadIdx.x;
       for (int c = 0; c < 3; c++) brk[c * stride + o] = ok ? lb[c] : nan;
     }
   }
 }
 
-// only: 0 every zone; 1 the warm zones alone (a stored mu > 0); 2 the cold
-// zones alone.  With the learned start the plan runs the plain kernel over
-// the warm zones and the learned one over the cold zones, so warm zones (all
-// of them once a run is under way) go through exactly the plain kernel's code.
+// only: 0 every zone; 1 the warm zones alone; 2 the cold zones alone, as
+// kb_mlp_bracket classified them before either pass ran (plane 3 of brk).
+// With the learned start the plan runs the plain kernel over the warm zones
+// and the learned one over the cold zones, so warm zones (all of them once a
+// run is under way) go through exactly the plain kernel's code.
 template <bool MINK, bool LEARNED>
 __global__ void __launch_bounds__(C2P_THREADS) kb_c2p(Par p, const BView *views, const WorkItem *items, int nitems,
                                                        const double *brk, DevStats *stats, unsigned int *err,
@@ -586,7 +598,9 @@ __global__ void __launch_bounds__(C2P_THREADS) kb_c2p(Par p, const BView *views,
     const BoxZones zones{bv, Range3{0, bv.n1t - 1, 0, bv.n2t - 1, 0, bv.n3t - 1}};
     const long long q = w.first + threadIdx.x;
     bool valid = q < w.last;
-    if (only && valid) valid = (zones.guess_of(q) > 0.0) == (only == 1);
+    if (only && valid)
+      valid = (brk[3 * (long long)nitems * C2P_THREADS + (long long)it * C2P_THREADS + threadIdx.x] == 1.0) ==
+              (only == 2);
     if (!__any_sync(0xffffffffu, valid)) continue;  // nothing for this warp in this pass
     long long id = 0;
     Pt g{};
@@ -631,7 +645,7 @@ static void c2p_batched_t(const Par &p, const BView *views, const WorkItem *item
     kb_mlp_bracket<MINK><<<persistent_grid(kb_mlp_bracket<MINK>, C2P_THREADS, sizeof(BracketSmem), nitems, 0),
                            C2P_THREADS, sizeof(BracketSmem), s>>>(p, views, items, nitems, mlp, brk, err);
     kb_c2p<MINK, false><<<persistent_grid(kb_c2p<MINK, false>, C2P_THREADS, 0, nitems, grid), C2P_THREADS, 0, s>>>(
-        p, views, items, nitems, nullptr, stats, err, 1);
+        p, views, items, nitems, brk, stats, err, 1);
     kb_c2p<MINK, true><<<persistent_grid(kb_c2p<MINK, true>, C2P_THREADS, 0, nitems, grid), C2P_THREADS, 0, s>>>(
         p, views, items, nitems, brk, stats, err, 2);
   } else {

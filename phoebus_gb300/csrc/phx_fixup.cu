@@ -104,10 +104,12 @@ void launch_c2p_fixup(const Par &p, const BView &b, cudaStream_t s) {
 
 // ------------------------------------------------------------ floors
 // Zone t of the index box r (valid: this lane owns a zone).  Every lane of a
-// warp must call it together (the re-inversion's root find votes).
+// warp must call it together (the re-inversion's root find votes).  flag
+// (optional, [N]): 1 where floors or ceilings acted, else 0 (the radiation
+// part of ApplyFloors redoes the closure inversion there).
 template <bool MINK>
 __device__ __forceinline__ void floors_at(const Par &p, const BView &b, const Range3 &r, long long t, bool valid,
-                                          DevStats *stats, unsigned int *err) {
+                                          DevStats *stats, unsigned int *err, double *flag = nullptr) {
   int k = 0, j = 0, i = 0;
   if (valid) {
     const int ni = r.ie - r.is + 1, nj = r.je - r.js + 1;
@@ -239,6 +241,7 @@ __device__ __forceinline__ void floors_at(const Par &p, const BView &b, const Ra
     U[PHX_CENG] = taun;
     for (int d = 0; d < 3; d++) U[PHX_CMOM + d] = dS[d];
   }
+  if (flag) flag[id] = (floor_applied || ceiling_applied) ? 1.0 : 0.0;
   if (floor_applied || ceiling_applied) {
     pr[PHX_PTMP] = eos_T_rho_sie(p, pr[PHX_PRHO], ratio(pr[PHX_PENG], pr[PHX_PRHO]));
     pr[PHX_PPRS] = eos_P_rho_T(p, pr[PHX_PRHO], pr[PHX_PTMP]);
@@ -253,20 +256,21 @@ __device__ __forceinline__ void floors_at(const Par &p, const BView &b, const Ra
 
 template <bool MINK>
 __global__ void __launch_bounds__(128) k_floors(Par p, BView b, Range3 r, long long ntot, DevStats *stats,
-                                                unsigned int *err) {
+                                                unsigned int *err, double *flag) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  floors_at<MINK>(p, b, r, t, t < ntot, stats, err);
+  floors_at<MINK>(p, b, r, t, t < ntot, stats, err, flag);
 }
 
-void launch_floors(const Par &p, const BView &b, Range3 r, DevStats *stats, unsigned int *err, cudaStream_t s) {
+void launch_floors(const Par &p, const BView &b, Range3 r, DevStats *stats, unsigned int *err, cudaStream_t s,
+                   double *flag) {
   if (!p.enable_floors) return;
   const long long n = (long long)(r.ie - r.is + 1) * (r.je - r.js + 1) * (r.ke - r.ks + 1);
   if (n <= 0) return;
   const int T = 128;
   if (b.fmks)
-    k_floors<false><<<(unsigned)((n + T - 1) / T), T, 0, s>>>(p, b, r, n, stats, err);
+    k_floors<false><<<(unsigned)((n + T - 1) / T), T, 0, s>>>(p, b, r, n, stats, err, flag);
   else
-    k_floors<true><<<(unsigned)((n + T - 1) / T), T, 0, s>>>(p, b, r, n, stats, err);
+    k_floors<true><<<(unsigned)((n + T - 1) / T), T, 0, s>>>(p, b, r, n, stats, err, flag);
 }
 
 // ------------------------------------------------------------- batched

@@ -56,8 +56,9 @@ void launch_ghost_periodic(const BView &b, double *field, int nvar, cudaStream_t
 void launch_dt(const Par &p, const BView &b, int use_face, unsigned long long *scratch,
                double *dt_out, cudaStream_t s);
 void launch_c2p_fixup(const Par &p, const BView &b, cudaStream_t s);
+// flag (optional, [N]): 1 where floors or ceilings acted, else 0
 void launch_floors(const Par &p, const BView &b, Range3 r, DevStats *stats, unsigned int *err,
-                   cudaStream_t s);
+                   cudaStream_t s, double *flag = nullptr);
 void launch_geom_fmks(const phx_geometry &g, const BView &b, cudaStream_t s);
 void launch_geom_points(const phx_geometry &g, long long n, const double *x1, const double *x2, double *geom,
                         cudaStream_t s);
@@ -153,7 +154,8 @@ void launch_fluxct_batched(int ndim, const BView *views, const WorkItem *items, 
 void launch_update_batched(const Par &p, const BView *views, const double *const *base, double *const *out,
                            const double *beta_dt, const WorkItem *items, int nitems, int grid, cudaStream_t s);
 void launch_ghost_batched(const BView *views, int nvar, const WorkItem *items, int nitems, int grid, cudaStream_t s);
-// mlp non-null: the learned start; brk holds 3 x nitems x 128 doubles.
+// mlp non-null: the learned start; brk holds 4 x nitems x 128 doubles (the
+// brackets and each zone's warm / cold pass).
 void launch_c2p_batched(const Par &p, bool mink, const BView *views, const WorkItem *items, int nitems, int grid,
                         const MlpPacked *mlp, double *brk, DevStats *stats, unsigned int *err, cudaStream_t s);
 // bc_vars = conserved, outer-X1 inflow check (FMKS): con2prim, u^1 >= 0 and

@@ -7,7 +7,7 @@
 // to the phoebus tree): radiation/closure.hpp:49-352 (ClosureEdd),
 // closure_m1.hpp:31-372 (ClosureM1), local_three_geometry.hpp:140-185,
 // linear_algebra.hpp:58-96, moments.cpp:61-995, moments_source.cpp:152-958
-// (oned solver; update_fluid with the fluid's con2prim), radiation.cpp:681-733,
+// (oned solver; update_fluid with the fluid's con2prim), radiation.cpp:585-648,
 // root_find.hpp:111-160.  With the identity spatial metric each contraction
 // keeps the order of its non-zero terms (for finite values the zero terms of
 // the full 3x3 sums change no rounding).  std::pow(x, 2) and std::pow(x, 3)
@@ -130,15 +130,99 @@ enum { SUCCESS = 0, FAILURE = 1, MODIFIED = 2 };
 constexpr double PI = 3.141592653589793;
 constexpr double SIN_PI = 1.2246467991473532e-16;
 
-template <bool M1>
+// LocalThreeGeometry (local_three_geometry.hpp:123-185) off Minkowski:
+// gamma_ij of the location, gamma^ij from matrixInverse3x3 (the closure's
+// own inverse, not the table's), the lapse.  Contractions in the
+// reference's loop order.
+struct G3 {
+  double cov[3][3], con[3][3], alpha;
+  __device__ __forceinline__ void lower(const V3 &a, V3 &o) const {
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      double s = 0.0;
+#pragma unroll
+      for (int j = 0; j < 3; j++) s += a.d[j] * cov[i][j];
+      o.d[i] = s;
+    }
+  }
+  __device__ __forceinline__ void raise(const V3 &a, V3 &o) const {
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      double s = 0.0;
+#pragma unroll
+      for (int j = 0; j < 3; j++) s += a.d[j] * con[i][j];
+      o.d[i] = s;
+    }
+  }
+  __device__ __forceinline__ double contract_cov(const V3 &a, const V3 &b) const {  // contractCov3Vectors
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) s += con[i][j] * a.d[i] * b.d[j];
+    return s;
+  }
+};
+// linear_algebra.hpp:67-89: adjugate over determinant (first-column expansion)
+__device__ __forceinline__ G3 make_g3(const Pt &p) {
+  G3 g;
+#pragma unroll
+  for (int a = 0; a < 3; a++)
+#pragma unroll
+    for (int b = 0; b < 3; b++) g.cov[a][b] = p.gcov[a + 1][b + 1];
+  const double(&A)[3][3] = g.cov;
+  double(&I)[3][3] = g.con;
+  I[0][0] = dop(A[1][1], A[2][2], A[1][2], A[2][1]);
+  I[1][0] = -dop(A[1][0], A[2][2], A[1][2], A[2][0]);
+  I[2][0] = dop(A[1][0], A[2][1], A[1][1], A[2][0]);
+  I[0][1] = -dop(A[0][1], A[2][2], A[0][2], A[2][1]);
+  I[1][1] = dop(A[0][0], A[2][2], A[0][2], A[2][0]);
+  I[2][1] = -dop(A[0][0], A[2][1], A[0][1], A[2][0]);
+  I[0][2] = dop(A[0][1], A[1][2], A[0][2], A[1][1]);
+  I[1][2] = -dop(A[0][0], A[1][2], A[0][2], A[1][0]);
+  I[2][2] = dop(A[0][0], A[1][1], A[0][1], A[1][0]);
+  const double det = fma(A[0][0], I[0][0], dop(A[2][0], I[2][0], A[1][0], -I[1][0]));
+  const double invDet = 1.0 / det;
+#pragma unroll
+  for (int a = 0; a < 3; a++)
+#pragma unroll
+    for (int b = 0; b < 3; b++) I[a][b] *= invDet;
+  g.alpha = p.alpha;
+  return g;
+}
+// GetLorentzFactor with gamma_ij (relativity_utils.hpp:38-43)
+__device__ __forceinline__ double lorentz_g(const double vp[3], const G3 &g) {
+  double vsq = 0.;
+#pragma unroll
+  for (int ii = 0; ii < 3; ii++)
+#pragma unroll
+    for (int jj = 0; jj < 3; jj++) vsq += g.cov[ii][jj] * vp[ii] * vp[jj];
+  return sqrt(1. + vsq);
+}
+
+#ifdef PHX_EXACT
+constexpr bool kExactBuild = true;
+#else
+constexpr bool kExactBuild = false;
+#endif
+
+// ClosureEdd / ClosureM1 (M1).  MINK: the identity spatial metric, each
+// contraction over its non-zero terms; otherwise geo (the LocalThreeGeometry
+// of the zone or face) with the full 3x3 sums.
+template <bool M1, bool MINK = true>
 struct Closure {
   V3 con_v, cov_v;
   double W, W2, iW;
   bool robust;
-  __device__ __forceinline__ Closure(const V3 &cv, bool rob) : robust(rob) {
+  const G3 *geo;
+  __device__ __forceinline__ Closure(const V3 &cv, bool rob, const G3 *g = nullptr) : robust(rob), geo(g) {
     con_v = cv;
+    if constexpr (MINK) {
 #pragma unroll
-    for (int i = 0; i < 3; i++) cov_v.d[i] = 0.0 + cv.d[i];
+      for (int i = 0; i < 3; i++) cov_v.d[i] = 0.0 + cv.d[i];
+    } else {
+      geo->lower(cv, cov_v);
+    }
     double v2 = 0.0;
 #pragma unroll
     for (int i = 0; i < 3; i++) v2 += con_v.d[i] * cov_v.d[i];
@@ -147,16 +231,40 @@ struct Closure {
     W2 = W * W;
     iW = rcp_p(W);
   }
+  __device__ __forceinline__ void raise(const V3 &a, V3 &o) const {
+    if constexpr (MINK) {
+#pragma unroll
+      for (int i = 0; i < 3; i++) o.d[i] = 0.0 + a.d[i];
+    } else {
+      geo->raise(a, o);
+    }
+  }
+  // contractCov3Vectors
+  __device__ __forceinline__ double ccv(const V3 &a, const V3 &b) const {
+    if constexpr (MINK)
+      return ccov(a, b);
+    else
+      return geo->contract_cov(a, b);
+  }
+  __device__ __forceinline__ double gcon(int i, int j) const {
+    if constexpr (MINK)
+      return gdelta(i, j);
+    else
+      return geo->con[i][j];
+  }
   __device__ __forceinline__ void contractions(const T2 &Pi, V3 &cov_vPi, double &vvPi) const {
     vvPi = 0.0;
+    V3 con_vPi;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
       double c = 0.0;
 #pragma unroll
       for (int j = 0; j < 3; j++) c += cov_v.d[j] * Pi.d[i][j];
       vvPi += cov_v.d[i] * c;
-      cov_vPi.d[i] = 0.0 + c;
+      con_vPi.d[i] = c;
+      if constexpr (MINK) cov_vPi.d[i] = 0.0 + c;
     }
+    if constexpr (!MINK) geo->lower(con_vPi, cov_vPi);
   }
   __device__ __forceinline__ void linear_source_update(double Estar, const V3 &Fs, const T2 &Pi, double JBB,
                                                        double tauJ, double tauH, double &dE, V3 &dF) const {
@@ -197,14 +305,38 @@ struct Closure {
 #pragma unroll
     for (int i = 0; i < 3; i++) F.d[i] = D3(4 * W2) * cov_v.d[i] * J + W * cov_v.d[i] * vH + W * H.d[i] + J * cvPi.d[i];
   }
-  // row d of ClosureEdd::getConCovPFromPrim (lapse 1)
+  // row d of ClosureEdd::getConCovPFromPrim, before the lapse scaling
   __device__ __forceinline__ void concov_p_row(double J, const V3 &H, const T2 &Pi, int d, double P[3]) const {
-    const double conH_d = 0.0 + H.d[d];
+    if constexpr (MINK) {
+      const double conH_d = 0.0 + H.d[d];
 #pragma unroll
-    for (int j = 0; j < 3; j++)
-      P[j] = 4.0 / 3.0 * W2 * con_v.d[d] * cov_v.d[j] * J + W * (con_v.d[d] * H.d[j] + cov_v.d[j] * conH_d) +
-             J * (0.0 + Pi.d[d][j]);
+      for (int j = 0; j < 3; j++)
+        P[j] = 4.0 / 3.0 * W2 * con_v.d[d] * cov_v.d[j] * J + W * (con_v.d[d] * H.d[j] + cov_v.d[j] * conH_d) +
+               J * (0.0 + Pi.d[d][j]);
+    } else {
+      V3 conH;
+      geo->raise(H, conH);
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        double cc = 0.0;
+#pragma unroll
+        for (int k = 0; k < 3; k++) cc += Pi.d[d][k] * geo->cov[k][j];
+        P[j] = 4.0 / 3.0 * W2 * con_v.d[d] * cov_v.d[j] * J + W * (con_v.d[d] * H.d[j] + cov_v.d[j] * conH.d[d]) +
+               J * cc;
+      }
+    }
     P[d] += D3(J);
+  }
+  // ClosureEdd::getConPFromPrim
+  __device__ __forceinline__ void con_p(double J, const V3 &H, const T2 &Pi, T2 &P) const {
+    V3 conH;
+    raise(H, conH);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++)
+        P.d[i][j] = 4.0 / 3.0 * W2 * con_v.d[i] * con_v.d[j] * J + W * (con_v.d[i] * conH.d[j] + con_v.d[j] * conH.d[i]) +
+                    J * Pi.d[i][j] + J / 3.0 * gcon(i, j);
   }
   __device__ __forceinline__ int con2prim(double E, const V3 &F, const T2 &Pi, double &J, V3 &H) const {
     double vvPi;
@@ -223,7 +355,7 @@ struct Closure {
 #pragma unroll
     for (int i = 0; i < 3; i++) H.d[i] = DW(F.d[i] - J * cvPi.d[i] - cov_v.d[i] * a);
     const double vh = ccov(con_v, H);
-    const double xi = div_p(sqrt(ccov(H, H) - vh * vh), J);
+    const double xi = div_p(sqrt(ccv(H, H) - vh * vh), J);
     if (isnan(xi) || isnan(J)) return FAILURE;
     if (J < 0. || xi >= 1.0) {
       if (robust) {
@@ -248,19 +380,27 @@ struct Closure {
     for (int i = 0; i < 3; i++)
 #pragma unroll
       for (int j = 0; j < 3; j++) {
-        Pi.d[i][j] = f[i] * f[j] - (W2 * con_v.d[i] * con_v.d[j] + gdelta(i, j)) / 3;
+        Pi.d[i][j] = f[i] * f[j] - (W2 * con_v.d[i] * con_v.d[j] + gcon(i, j)) / 3;
         Pi.d[i][j] *= athin;
       }
 #else
-    // symmetric: the upper triangle, mirrored
+    // Minkowski: symmetric, the upper triangle mirrored (gamma^ij from
+    // matrixInverse3x3 need not be exactly symmetric: all nine otherwise)
+    if constexpr (MINK) {
 #pragma unroll
-    for (int i = 0; i < 3; i++)
+      for (int i = 0; i < 3; i++)
 #pragma unroll
-      for (int j = i; j < 3; j++) {
-        const double v = (f[i] * f[j] - D3(W2 * con_v.d[i] * con_v.d[j] + gdelta(i, j))) * athin;
-        Pi.d[i][j] = v;
-        Pi.d[j][i] = v;
-      }
+        for (int j = i; j < 3; j++) {
+          const double v = (f[i] * f[j] - D3(W2 * con_v.d[i] * con_v.d[j] + gdelta(i, j))) * athin;
+          Pi.d[i][j] = v;
+          Pi.d[j][i] = v;
+        }
+    } else {
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) Pi.d[i][j] = (f[i] * f[j] - D3(W2 * con_v.d[i] * con_v.d[j] + geo->con[i][j])) * athin;
+    }
 #endif
   }
   // GetConTilPiFromPrim
@@ -271,20 +411,22 @@ struct Closure {
 #pragma unroll
         for (int j = 0; j < 3; j++) Pi.d[i][j] = 0.0;
     } else {
+      V3 conH;
+      raise(H, conH);
       double Hm = 0.0, vH = 0.0;
 #pragma unroll
-      for (int i = 0; i < 3; i++) Hm += H.d[i] * (0.0 + H.d[i]);
+      for (int i = 0; i < 3; i++) Hm += H.d[i] * conH.d[i];
 #pragma unroll
       for (int i = 0; i < 3; i++) vH += H.d[i] * con_v.d[i];
       Hm = sqrt(Hm - vH * vH);
       double f[3];
 #ifdef PHX_EXACT
 #pragma unroll
-      for (int i = 0; i < 3; i++) f[i] = ratio(0.0 + H.d[i], Hm);
+      for (int i = 0; i < 3; i++) f[i] = ratio(conH.d[i], Hm);
 #else
       const double iHm = rcp_p(Hm + (Hm >= 0 ? kSMALL : -kSMALL));
 #pragma unroll
-      for (int i = 0; i < 3; i++) f[i] = H.d[i] * iHm;
+      for (int i = 0; i < 3; i++) f[i] = (MINK ? H.d[i] : conH.d[i]) * iHm;
 #endif
       const double xi = smax(smin(1.0, ratio_p(Hm, J)), 0.0);
       tilpi_fill(f, 0.5 * (3 * closure_fn(xi) - 1), Pi);
@@ -305,9 +447,11 @@ struct Closure {
     tilpi_fill(f, 0.5 * (3 * closure_fn(xi) - 1), Pi);
   }
   __device__ __forceinline__ void basis(const V3 &F, V3 &g, V3 &dd) const {
+    V3 conF;
+    raise(F, conF);
     double Fmag = 0.0, vl = 0.0, vv = 0.0;
 #pragma unroll
-    for (int i = 0; i < 3; i++) Fmag += F.d[i] * (0.0 + F.d[i]);
+    for (int i = 0; i < 3; i++) Fmag += F.d[i] * conF.d[i];
     Fmag = sqrt(Fmag);
 #pragma unroll
     for (int i = 0; i < 3; i++) vl += F.d[i] * con_v.d[i];
@@ -324,7 +468,7 @@ struct Closure {
 #endif
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-      const double cF = 0.0 + F.d[i];
+      const double cF = conF.d[i];
 #ifdef PHX_EXACT
       g.d[i] = ratio(cF * lam, Fmag) - W * con_v.d[i];
       dd.d[i] = ratio(ratio(cF, Fmag) * (1 - lam / W) + con_v.d[i], aa);
@@ -343,8 +487,15 @@ struct Closure {
     V3 H;
     con2prim(E, F, Pi, J, H);
     double Hm = 0.0, vH = 0.0;
+    if constexpr (MINK) {
 #pragma unroll
-    for (int i = 0; i < 3; i++) Hm += H.d[i] * H.d[i];
+      for (int i = 0; i < 3; i++) Hm += H.d[i] * H.d[i];
+    } else {
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) Hm += H.d[i] * H.d[j] * geo->con[i][j];
+    }
 #pragma unroll
     for (int i = 0; i < 3; i++) vH += con_v.d[i] * H.d[i];
     Hm = sqrt(Hm - vH * vH);
@@ -352,16 +503,18 @@ struct Closure {
   }
   // SolveClosure with phi held at pi (the reference's update rule keeps it
   // there); the phi-perturbed residuals only feed the discarded 2x2 solve.
-  // Exact build: the reference's central-difference Newton, tensor
-  // arithmetic per residual.  Production build: with phi fixed the
-  // rest-frame flux direction f is fixed, so pi^ij(xi) = athin(xi) pi0^ij
-  // with athin = xi^2 (2 xi - 1), and every quantity con2prim forms is a
-  // rational function of athin: the residual and its exact derivative are
-  // scalar work (the difference quotient is kept for the robust-rewrite
-  // branch and degenerate states).  Pi_out (production, phi = pi) receives
-  // athin(xi) pi0 for the caller's pressure tensor.
+  // Exact build and curved metrics: the reference's central-difference
+  // Newton, tensor arithmetic per residual.  Production build on Minkowski:
+  // with phi fixed the rest-frame flux direction f is fixed, so
+  // pi^ij(xi) = athin(xi) pi0^ij with athin = xi^2 (2 xi - 1), and every
+  // quantity con2prim forms is a rational function of athin: the residual
+  // and its exact derivative are scalar work (the difference quotient is
+  // kept for the robust-rewrite branch and degenerate states).  Pi_out
+  // (that path, phi = pi) receives athin(xi) pi0 for the caller's pressure
+  // tensor.
   __device__ __forceinline__ void solve_closure(double E, V3 F, double &xi_io, double &phi_out,
                                                 T2 *Pi_out = nullptr, bool *pi_done = nullptr) const {
+    constexpr bool FD = kExactBuild || !MINK;
     const int max_iter = 30;
     const double tol = 1.e6 * DBL_EPSILON;
     const double eps = sqrt(10 * DBL_EPSILON);
@@ -374,98 +527,107 @@ struct Closure {
     int iter = 0;
     double fXi = 1.e3, fPhi = 1.e3;
     double xi = xi_io, phi = PI;
-#ifndef PHX_EXACT
-    double f[3];
+    if constexpr (FD) {
+      do {
+        const double xi_up = smin(xi * (1.0 + eps) + delta, 1.0);
+        const double xi_lo = smax(xi * (1.0 - eps) - delta, 0.0);
+        const double f_up = residual(E, F, xi_up, phi, g, dd);
+        const double f_lo = residual(E, F, xi_lo, phi, g, dd);
+        fXi = residual(E, F, xi, phi, g, dd);
+        const double J00 = (f_up - f_lo) / (xi_up - xi_lo);
+        const double dx0 = fXi / J00, dx1 = 0.0;
+        fPhi = 0.0;
+        double cdx = smin(dx0, xi - delta * xi);
+        cdx = smax(cdx, xi - (1 - delta * (1 - xi)));
+        double alpha = ratio(cdx, dx0);
+        alpha = smin(alpha, 0.5 * 3.14159 / fabs(dx1));
+        xi -= alpha * dx0;
+        phi -= alpha * dx1;
+        ++iter;
+      } while (iter < max_iter && (fabs(fXi) > tol || fabs(fPhi) > tol));
+    } else {
+      double f[3];
 #pragma unroll
-    for (int i = 0; i < 3; i++) f[i] = g.d[i] + SIN_PI * dd.d[i];
-    T2 Pi0;
-    tilpi_fill(f, 1.0, Pi0);
-    V3 C0;
-    double V0;
-    contractions(Pi0, C0, V0);
-    const double vF = ccov(con_v, F);
-    const double L0 = D3(2.0 * W2 + 1.0), c1 = (2.0 * W2 - 3.0) * W2;
-    const double NJ = (2 * W2 - 1) * E - 2 * W2 * vF;
-    const double K0 = D3(4 * W2) * E - D3(4 * W2 + 1) * vF, Kv = -E + W2 * vF;
-    // residual at x; *df its derivative, NaN where the difference quotient is needed
-    auto res = [&](double x, double *df) {
-      const double at = x * x * (2 * x - 1);
-      const double V = at * V0;
-      const double lam = L0 + c1 * V;
-      const double ilam = rcp_p(lam + (lam >= 0 ? kSMALL : -kSMALL));
-      const double K = K0 + V * Kv;
-      const double A = W2 * ilam * K;
-      const double J = NJ * ilam;
-      const double Ja = J * at;
-      V3 H;
+      for (int i = 0; i < 3; i++) f[i] = g.d[i] + SIN_PI * dd.d[i];
+      T2 Pi0;
+      tilpi_fill(f, 1.0, Pi0);
+      V3 C0;
+      double V0;
+      contractions(Pi0, C0, V0);
+      const double vF = ccov(con_v, F);
+      const double L0 = D3(2.0 * W2 + 1.0), c1 = (2.0 * W2 - 3.0) * W2;
+      const double NJ = (2 * W2 - 1) * E - 2 * W2 * vF;
+      const double K0 = D3(4 * W2) * E - D3(4 * W2 + 1) * vF, Kv = -E + W2 * vF;
+      // residual at x; *df its derivative, NaN where the difference quotient is needed
+      auto res = [&](double x, double *df) {
+        const double at = x * x * (2 * x - 1);
+        const double V = at * V0;
+        const double lam = L0 + c1 * V;
+        const double ilam = rcp_p(lam + (lam >= 0 ? kSMALL : -kSMALL));
+        const double K = K0 + V * Kv;
+        const double A = W2 * ilam * K;
+        const double J = NJ * ilam;
+        const double Ja = J * at;
+        V3 H;
 #pragma unroll
-      for (int i = 0; i < 3; i++) H.d[i] = (F.d[i] - Ja * C0.d[i] - cov_v.d[i] * A) * iW;
-      const double vh = ccov(con_v, H);
-      const double s0 = sqrt(ccov(H, H) - vh * vh);
-      const double iJ = rcp_p(J + (J >= 0 ? kSMALL : -kSMALL));
-      const double xc = s0 * iJ;
-      double sH = s0;
-      const bool modified = robust && !isnan(xc) && !isnan(J) && (J < 0. || xc >= 1.0);
-      if (modified && xc >= 1.0) sH = s0 * (0.999 * rcp_p(xc));
-      if (df) {
-        if (modified || !(s0 > 0.0)) {
-          *df = __longlong_as_double(0x7ff8000000000000ll);
-        } else {
-          const double dat = x * (6 * x - 2);
-          const double dV = dat * V0;
-          const double dilam = -(c1 * dV) * ilam * ilam;
-          const double dJ = NJ * dilam;
-          const double dA = W2 * (dilam * K + ilam * (Kv * dV));
-          const double dJa = dJ * at + J * dat;
-          double hdh = 0.0, vdh = 0.0;
+        for (int i = 0; i < 3; i++) H.d[i] = (F.d[i] - Ja * C0.d[i] - cov_v.d[i] * A) * iW;
+        const double vh = ccov(con_v, H);
+        const double s0 = sqrt(ccov(H, H) - vh * vh);
+        const double iJ = rcp_p(J + (J >= 0 ? kSMALL : -kSMALL));
+        const double xc = s0 * iJ;
+        double sH = s0;
+        const bool modified = robust && !isnan(xc) && !isnan(J) && (J < 0. || xc >= 1.0);
+        if (modified && xc >= 1.0) sH = s0 * (0.999 * rcp_p(xc));
+        if (df) {
+          if (modified || !(s0 > 0.0)) {
+            *df = __longlong_as_double(0x7ff8000000000000ll);
+          } else {
+            const double dat = x * (6 * x - 2);
+            const double dV = dat * V0;
+            const double dilam = -(c1 * dV) * ilam * ilam;
+            const double dJ = NJ * dilam;
+            const double dA = W2 * (dilam * K + ilam * (Kv * dV));
+            const double dJa = dJ * at + J * dat;
+            double hdh = 0.0, vdh = 0.0;
 #pragma unroll
-          for (int i = 0; i < 3; i++) {
-            const double dH = (-dJa * C0.d[i] - cov_v.d[i] * dA) * iW;
-            hdh += H.d[i] * dH;
-            vdh += con_v.d[i] * dH;
+            for (int i = 0; i < 3; i++) {
+              const double dH = (-dJa * C0.d[i] - cov_v.d[i] * dA) * iW;
+              hdh += H.d[i] * dH;
+              vdh += con_v.d[i] * dH;
+            }
+            const double ds0 = (hdh - vh * vdh) * rcp_p(s0);
+            *df = 1.0 - (ds0 - s0 * dJ * iJ) * iJ;
           }
-          const double ds0 = (hdh - vh * vdh) * rcp_p(s0);
-          *df = 1.0 - (ds0 - s0 * dJ * iJ) * iJ;
         }
+        return x - sH * iJ;
+      };
+      do {
+        const double xi_up = smin(xi * (1.0 + eps) + delta, 1.0);
+        const double xi_lo = smax(xi * (1.0 - eps) - delta, 0.0);
+        double J00;
+        fXi = res(xi, &J00);
+        if (!isfinite(J00)) J00 = (res(xi_up, nullptr) - res(xi_lo, nullptr)) / (xi_up - xi_lo);
+        const double dx0 = fXi / J00, dx1 = 0.0;
+        fPhi = 0.0;
+        double cdx = smin(dx0, xi - delta * xi);
+        cdx = smax(cdx, xi - (1 - delta * (1 - xi)));
+        double alpha = ratio(cdx, dx0);
+        alpha = smin(alpha, 0.5 * 3.14159 / fabs(dx1));
+        xi -= alpha * dx0;
+        phi -= alpha * dx1;
+        ++iter;
+      } while (iter < max_iter && (fabs(fXi) > tol || fabs(fPhi) > tol));
+      if (Pi_out && phi == PI) {
+        const double at = 0.5 * (3 * closure_fn(xi) - 1);
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int j = 0; j < 3; j++) Pi_out->d[i][j] = Pi0.d[i][j] * at;
+        *pi_done = true;
       }
-      return x - sH * iJ;
-    };
-#endif
-    do {
-      const double xi_up = smin(xi * (1.0 + eps) + delta, 1.0);
-      const double xi_lo = smax(xi * (1.0 - eps) - delta, 0.0);
-#ifdef PHX_EXACT
-      const double f_up = residual(E, F, xi_up, phi, g, dd);
-      const double f_lo = residual(E, F, xi_lo, phi, g, dd);
-      fXi = residual(E, F, xi, phi, g, dd);
-      const double J00 = (f_up - f_lo) / (xi_up - xi_lo);
-#else
-      double J00;
-      fXi = res(xi, &J00);
-      if (!isfinite(J00)) J00 = (res(xi_up, nullptr) - res(xi_lo, nullptr)) / (xi_up - xi_lo);
-#endif
-      const double dx0 = fXi / J00, dx1 = 0.0;
-      fPhi = 0.0;
-      double cdx = smin(dx0, xi - delta * xi);
-      cdx = smax(cdx, xi - (1 - delta * (1 - xi)));
-      double alpha = ratio(cdx, dx0);
-      alpha = smin(alpha, 0.5 * 3.14159 / fabs(dx1));
-      xi -= alpha * dx0;
-      phi -= alpha * dx1;
-      ++iter;
-    } while (iter < max_iter && (fabs(fXi) > tol || fabs(fPhi) > tol));
+    }
     xi_io = xi;
     phi_out = phi;
-#ifndef PHX_EXACT
-    if (Pi_out && phi == PI) {
-      const double at = 0.5 * (3 * closure_fn(xi) - 1);
-#pragma unroll
-      for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) Pi_out->d[i][j] = Pi0.d[i][j] * at;
-      *pi_done = true;
-    }
-#endif
   }
   // GetConTilPiFromCon
   __device__ __forceinline__ void tilpi_from_con(double E, const V3 &F, double &xi, double &phi, T2 &Pi) const {
@@ -490,10 +652,37 @@ struct Closure {
 };
 
 // ---------------------------------------------------------------- views
-__device__ __forceinline__ V3 fluid_v(const BView &b, long long id, double *Wout = nullptr) {
+// The geometry a moment task reads at one location (loc 0 centre and X3
+// faces, 1 X1 face, 2 X2 face): the table values and, off Minkowski, the
+// LocalThreeGeometry built from them.  Minkowski: lapse 1, shift 0, identity.
+template <bool MINK>
+struct RGeo {
+  Pt p;
+  G3 g;
+  __device__ __forceinline__ RGeo(const BView &b, int loc, int j, int i) {
+    if constexpr (!MINK) {
+      load_pt(b, loc, j, i, p);
+      g = make_g3(p);
+    }
+  }
+  __device__ __forceinline__ const G3 *geo() const { return MINK ? nullptr : &g; }
+  __device__ __forceinline__ double alpha() const { return MINK ? 1.0 : p.alpha; }
+  __device__ __forceinline__ double beta(int d) const { return MINK ? 0.0 : p.beta[d]; }
+  __device__ __forceinline__ double sdetgam() const { return MINK ? 1.0 : p.detgam; }
+  __device__ __forceinline__ double cov(int a, int c) const { return MINK ? gdelta(a, c) : p.gcov[a + 1][c + 1]; }
+  __device__ __forceinline__ double con(int a, int c) const { return MINK ? gdelta(a, c) : p.gamcon[a][c]; }
+};
+
+// The fluid three-velocity (W v^i) / W, W of gamma_ij.
+template <bool MINK = true>
+__device__ __forceinline__ V3 fluid_v(const BView &b, long long id, const G3 *g = nullptr, double *Wout = nullptr) {
   const double vp[3] = {b.prim[PHX_PVEL * b.vs + id], b.prim[(PHX_PVEL + 1) * b.vs + id],
                         b.prim[(PHX_PVEL + 2) * b.vs + id]};
-  const double W = lorentz3(vp);
+  double W;
+  if constexpr (MINK)
+    W = lorentz3(vp);
+  else
+    W = lorentz_g(vp, *g);
   if (Wout) *Wout = W;
   V3 v;
   v.d[0] = vp[0] / W;
@@ -512,14 +701,15 @@ __host__ __device__ inline long long range_count(const Range3 &r) {
 }
 
 // ---------------------------------------------------- MomentPrim2Con
-template <bool M1>
+template <bool M1, bool MINK>
 __global__ void __launch_bounds__(128) k_p2c(RPar p, BView b, RView r, Range3 rg) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= range_count(rg)) return;
   int k, j, i;
   zone_of(rg, t, k, j, i);
   const long long id = b.idx(k, j, i), vs = r.vs;
-  const Closure<M1> c(fluid_v(b, id), true);
+  const RGeo<MINK> G(b, 0, j, i);
+  const Closure<M1, MINK> c(fluid_v<MINK>(b, id, G.geo()), true, G.geo());
   const double J = r.prim[PHX_RJ * vs + id];
   V3 H;
 #pragma unroll
@@ -529,21 +719,23 @@ __global__ void __launch_bounds__(128) k_p2c(RPar p, BView b, RView r, Range3 rg
   double E;
   V3 F;
   c.prim2con(J, H, Pi, E, F);
-  r.cons[PHX_RE * vs + id] = 1.0 * E;
+  const double sdetgam = G.sdetgam();
+  r.cons[PHX_RE * vs + id] = sdetgam * E;
 #pragma unroll
-  for (int a = 0; a < 3; a++) r.cons[(PHX_RF + a) * vs + id] = 1.0 * F.d[a];
+  for (int a = 0; a < 3; a++) r.cons[(PHX_RF + a) * vs + id] = sdetgam * F.d[a];
 }
 
 // ---------------------------------------------------- MomentCon2Prim
-template <bool M1>
+template <bool M1, bool MINK>
 __global__ void __launch_bounds__(128) k_c2p(RPar p, BView b, RView r, Range3 rg) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= range_count(rg)) return;
   int k, j, i;
   zone_of(rg, t, k, j, i);
   const long long id = b.idx(k, j, i), vs = r.vs;
-  const double isdetgam = 1.0 / 1.0;
-  const Closure<M1> c(fluid_v(b, id), p.robust != 0);
+  const RGeo<MINK> G(b, 0, j, i);
+  const double isdetgam = 1.0 / G.sdetgam();
+  const Closure<M1, MINK> c(fluid_v<MINK>(b, id, G.geo()), p.robust != 0, G.geo());
   double E = r.cons[PHX_RE * vs + id] * isdetgam;
   V3 F;
 #pragma unroll
@@ -596,17 +788,27 @@ __global__ void __launch_bounds__(256) k_opacities(RPar p, BView b, RView r, lon
 // --------------------------------------------------------- fluxes
 // One face state: E, F_i, and the flux of direction d (con_F^d and row d of
 // P^i_j) for the closure's velocity, J and H_i.
-template <bool M1, int d>
-__device__ __forceinline__ void face_state(const Closure<M1> &c, double J, const V3 &H, double &E, V3 &F,
+// ClosureEdd::getFluxesFromPrim: con_F^d = alpha gamma^{dj} F_j and
+// alpha P^d_j (on Minkowski the lapse scalings by 1 are exact and skipped).
+template <bool M1, int d, bool MINK>
+__device__ __forceinline__ void face_state(const Closure<M1, MINK> &c, double J, const V3 &H, double &E, V3 &F,
                                            double &Fd, double P[3]) {
   T2 Pi;
   c.tilpi_from_prim(J, H, Pi);
   c.concov_p_row(J, H, Pi, d, P);
   c.prim2con(J, H, Pi, E, F);
-  Fd = 0.0 + F.d[d];
+  if constexpr (MINK) {
+    Fd = 0.0 + F.d[d];
+  } else {
+    V3 conF;
+    c.geo->raise(F, conF);
+#pragma unroll
+    for (int a = 0; a < 3; a++) P[a] *= c.geo->alpha;
+    Fd = conF.d[d] * c.geo->alpha;
+  }
 }
 
-template <bool M1, int RECON, int d>
+template <bool M1, int RECON, int d, bool MINK>
 __global__ void __launch_bounds__(128) k_fluxes(RPar p, BView b, RView r, Range3 rg) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= range_count(rg)) return;
@@ -647,9 +849,17 @@ __global__ void __launch_bounds__(128) k_fluxes(RPar p, BView b, RView r, Range3
     dJ.d[1] = (Jat(k, j + dj, i) + Jat(k - dk, j + dj, i) - Jat(k, j - dj, i) - Jat(k - dk, j - dj, i)) * idy4;
     dJ.d[2] = (Jat(k, j, i) - Jat(k - dk, j, i)) * idz;
   }
-  const double dx = b.dx[d] * sqrt(1.0);
+  const RGeo<MINK> G(b, d == 0 ? 1 : (d == 1 ? 2 : 0), j, i);  // X3 faces: the centre table
+  const double dx = b.dx[d] * sqrt(G.cov(d, d));
   double vpl[3] = {ql[4], ql[5], ql[6]}, vpr[3] = {qr[4], qr[5], qr[6]};
-  double Wl = lorentz3(vpl), Wr = lorentz3(vpr);
+  double Wl, Wr;
+  if constexpr (MINK) {
+    Wl = lorentz3(vpl);
+    Wr = lorentz3(vpr);
+  } else {
+    Wl = lorentz_g(vpl, G.g);
+    Wr = lorentz_g(vpr, G.g);
+  }
   if (p.bounds) {
     if (Wl > p.W_ceiling) {
       const double rescale = sqrt(p.W_ceiling * p.W_ceiling - 1.) / (Wl * Wl - 1.);
@@ -676,10 +886,11 @@ __global__ void __launch_bounds__(128) k_fluxes(RPar p, BView b, RView r, Range3
     vr.d[a] = vpr[a] * iWr;
 #endif
   }
-  const double sigp = 1.0 * sqrt(1.0) - 0.0;
-  const double sigm = -1.0 * sqrt(1.0) - 0.0;
-  const double asym_sigl = 1.0 * vl.d[d] - 0.0;
-  const double asym_sigr = 1.0 * vr.d[d] - 0.0;
+  const double alpha = G.alpha(), beta_d = G.beta(d);
+  const double sigp = alpha * sqrt(G.con(d, d)) - beta_d;
+  const double sigm = -alpha * sqrt(G.con(d, d)) - beta_d;
+  const double asym_sigl = alpha * vl.d[d] - beta_d;
+  const double asym_sigr = alpha * vr.d[d] - beta_d;
   double Jl = ql[0], Jr = qr[0];
   if (p.bounds) {
     Jl = smax(Jl, p.J_floor);
@@ -699,8 +910,10 @@ __global__ void __launch_bounds__(128) k_fluxes(RPar p, BView b, RView r, Range3
   if (p.bounds && p.xi_ceiling < kDBLMAX) {
 #endif
     const double vhl = ccov(vl, Hl), vhr = ccov(vr, Hr);
-    const double xil = div_p(sqrt(ccov(Hl, Hl) - vhl * vhl), Jl);
-    const double xir = div_p(sqrt(ccov(Hr, Hr) - vhr * vhr), Jr);
+    const double hhl = MINK ? ccov(Hl, Hl) : G.g.contract_cov(Hl, Hl);
+    const double hhr = MINK ? ccov(Hr, Hr) : G.g.contract_cov(Hr, Hr);
+    const double xil = div_p(sqrt(hhl - vhl * vhl), Jl);
+    const double xir = div_p(sqrt(hhr - vhr * vhr), Jr);
     if (xil > p.xi_ceiling) {
 #pragma unroll
       for (int a = 0; a < 3; a++) Hl.d[a] *= p.xi_ceiling / xil;
@@ -723,13 +936,13 @@ __global__ void __launch_bounds__(128) k_fluxes(RPar p, BView b, RView r, Range3
 #pragma unroll
   for (int a = 0; a < 3; a++) Has.d[a] = -dJ.d[a] * ik;
 #endif
-  const Closure<M1> cl(vl, true), cr(vr, true);
+  const Closure<M1, MINK> cl(vl, true, G.geo()), cr(vr, true, G.geo());
   double El, Er, Fdl, Fdr, Fdl_a, Fdr_a, Pl[3], Pr[3], Pl_a[3], Pr_a[3], Ed;
   V3 Fl, Fr, Fd_scr;
-  face_state<M1, d>(cl, Jl, Has, Ed, Fd_scr, Fdl_a, Pl_a);
-  face_state<M1, d>(cr, Jr, Has, Ed, Fd_scr, Fdr_a, Pr_a);
-  face_state<M1, d>(cl, Jl, Hl, El, Fl, Fdl, Pl);
-  face_state<M1, d>(cr, Jr, Hr, Er, Fr, Fdr, Pr);
+  face_state<M1, d, MINK>(cl, Jl, Has, Ed, Fd_scr, Fdl_a, Pl_a);
+  face_state<M1, d, MINK>(cr, Jr, Has, Ed, Fd_scr, Fdr_a, Pr_a);
+  face_state<M1, d, MINK>(cl, Jl, Hl, El, Fl, Fdl, Pl);
+  face_state<M1, d, MINK>(cr, Jr, Hr, Er, Fr, Fdr, Pr);
   Fdl = aw * Fdl + (1 - aw) * Fdl_a;
   Fdr = aw * Fdr + (1 - aw) * Fdr_a;
 #pragma unroll
@@ -740,20 +953,108 @@ __global__ void __launch_bounds__(128) k_fluxes(RPar p, BView b, RView r, Range3
   const double rad_sigspeed = smax(fabs(sigm), fabs(sigp));
   const double asym_sigspeed = smax(fabs(asym_sigl), fabs(asym_sigr));
   const double sigspeed = aw * rad_sigspeed + (1. - aw) * asym_sigspeed;
-  Fdl -= 0.0 * El;
-  Fdr -= 0.0 * Er;
+  Fdl -= beta_d * El;
+  Fdr -= beta_d * Er;
 #pragma unroll
   for (int a = 0; a < 3; a++) {
-    Pl[a] -= 0.0 * Fl.d[a];
-    Pr[a] -= 0.0 * Fr.d[a];
+    Pl[a] -= beta_d * Fl.d[a];
+    Pr[a] -= beta_d * Fr.d[a];
   }
+  const double sdetgam = G.sdetgam();
   double *fl = r.flux + (long long)d * PHX_RNCONS * vs;
-  fl[PHX_RE * vs + id] = 0.5 * 1.0 * (Fdl + Fdr + sigspeed * (El - Er));
+  const bool zero = !MINK && sdetgam < kSMALL;
+  fl[PHX_RE * vs + id] = zero ? 0.0 : 0.5 * sdetgam * (Fdl + Fdr + sigspeed * (El - Er));
 #pragma unroll
-  for (int a = 0; a < 3; a++) fl[(PHX_RF + a) * vs + id] = 0.5 * 1.0 * (Pl[a] + Pr[a] + sigspeed * (Fl.d[a] - Fr.d[a]));
+  for (int a = 0; a < 3; a++)
+    fl[(PHX_RF + a) * vs + id] = zero ? 0.0 : 0.5 * sdetgam * (Pl[a] + Pr[a] + sigspeed * (Fl.d[a] - Fr.d[a]));
+}
+
+// CalculateGeometricSourceImpl (moments.cpp:764-885) of one zone off
+// Minkowski, from the stage input E, F_i and the stored J, H_i: the
+// radiation stress tensor T^{mu nu} (E n n + F n + n F + P), the connection
+// coefficients 0.5 (dg_{b a, c} + dg_{c a, b} - dg_{b c, a}) of the derivative
+// table, row 0 of g^{mu nu} (cached_system.hpp:281-299) and d ln(alpha).
+// src: the densitised sources of E and F_1..3.
+template <bool M1>
+__device__ void geometric_source(const BView &b, const RView &r, int k, int j, int i, double src[4]) {
+  const long long id = b.idx(k, j, i), vs = r.vs;
+  const RGeo<false> G(b, 0, j, i);
+  const Closure<M1, false> c(fluid_v<false>(b, id, &G.g), true, &G.g);
+  const double alp = G.p.alpha, sdetgam = G.p.detgam;
+  double alpha2 = alp;
+  alpha2 *= alpha2;
+  const double g0[4] = {-ratio_p(1, alpha2), ratio_p(G.p.beta[0], alpha2), ratio_p(G.p.beta[1], alpha2),
+                        ratio_p(G.p.beta[2], alpha2)};
+  const long long pitch = (long long)b.n2t * b.n1t, off = (long long)j * b.n1t + i;
+  double dg[4][4][4];
+#pragma unroll
+  for (int mu = 0; mu < 4; mu++)
+#pragma unroll
+    for (int nu = 0; nu < 4; nu++) {
+      dg[mu][nu][0] = 0.0;
+#pragma unroll
+      for (int s = 1; s < 4; s++) dg[mu][nu][s] = __ldg(b.gderiv + (PHX_GD_DG + 3 * flat2(mu, nu) + s - 1) * pitch + off);
+    }
+  auto gam = [&](int a, int bb, int cc) { return 0.5 * (dg[bb][a][cc] + dg[cc][a][bb] - dg[bb][cc][a]); };
+  double dlnalp[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+  for (int s = 1; s < 4; s++) dlnalp[s] = __ldg(b.gderiv + (PHX_GD_DALPHA + s - 1) * pitch + off);
+  const double con_n[4] = {1. / alp, -G.p.beta[0] / alp, -G.p.beta[1] / alp, -G.p.beta[2] / alp};
+  const double E = r.cons[PHX_RE * vs + id] / sdetgam;
+  const double J = r.prim[PHX_RJ * vs + id];
+  V3 covF, covH, conF;
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    covF.d[a] = r.cons[(PHX_RF + a) * vs + id] / sdetgam;
+    covH.d[a] = J * r.prim[(PHX_RH + a) * vs + id];
+  }
+  T2 Pi, P;
+  c.tilpi_from_prim(J, covH, Pi);
+  c.con_p(J, covH, Pi, P);
+  G.g.raise(covF, conF);
+  double T[4][4];
+#pragma unroll
+  for (int mu = 0; mu < 4; mu++)
+#pragma unroll
+    for (int nu = 0; nu < 4; nu++) T[mu][nu] = 0.0 + con_n[mu] * con_n[nu] * E;
+#pragma unroll
+  for (int mu = 0; mu < 4; mu++)
+#pragma unroll
+    for (int ii = 0; ii < 3; ii++) {
+      T[mu][ii + 1] += con_n[mu] * conF.d[ii];
+      T[ii + 1][mu] += con_n[mu] * conF.d[ii];
+    }
+#pragma unroll
+  for (int ii = 0; ii < 3; ii++)
+#pragma unroll
+    for (int jj = 0; jj < 3; jj++) T[ii + 1][jj + 1] += P.d[ii][jj];
+  double TGam = 0.0;
+#pragma unroll
+  for (int m = 0; m < 4; m++)
+#pragma unroll
+    for (int n = 0; n < 4; n++) {
+      double gam0 = 0.;
+#pragma unroll
+      for (int q = 0; q < 4; q++) gam0 += g0[q] * gam(q, m, n);
+      TGam += T[m][n] * gam0;
+    }
+  double Ta = 0.0;
+#pragma unroll
+  for (int m = 0; m < 4; m++) Ta += T[m][0] * dlnalp[m];
+  src[0] = sdetgam * alp * alp * (Ta - TGam);
+#pragma unroll
+  for (int l = 0; l < 3; l++) {
+    double sm = 0.0;
+#pragma unroll
+    for (int m = 0; m < 4; m++)
+#pragma unroll
+      for (int n = 0; n < 4; n++) sm += T[m][n] * (dg[n][l + 1][m] - gam(l + 1, n, m));
+    src[1 + l] = alp * sdetgam * sm;
+  }
 }
 
 // ------------------------------------------ divergence + RK update
+template <bool M1, bool MINK>
 __global__ void __launch_bounds__(256) k_update(BView b, RView r, const double *base, double *out, double beta,
                                                 double dt, Range3 rg) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -761,6 +1062,9 @@ __global__ void __launch_bounds__(256) k_update(BView b, RView r, const double *
   int k, j, i;
   zone_of(rg, t, k, j, i);
   const long long id = b.idx(k, j, i), vs = r.vs;
+  // SumData: the geometric source (zero on Minkowski), from the stage input
+  double src[4] = {0.0, 0.0, 0.0, 0.0};
+  if constexpr (!MINK) geometric_source<M1>(b, r, k, j, i, src);
   const double dx1 = b.dx[0], dx2 = b.dx[1], dx3 = b.dx[2];
   const double A1 = dx2 * dx3, A2 = dx1 * dx3, A3 = dx1 * dx2, V = dx1 * dx2 * dx3;
   const double bdt = beta * dt;
@@ -773,7 +1077,7 @@ __global__ void __launch_bounds__(256) k_update(BView b, RView r, const double *
     double du = (A1 * F0[id + 1] - A1 * F0[id]);
     if (b.ndim >= 2) du += A2 * F1[id + s2] - A2 * F1[id];
     if (b.ndim == 3) du += A3 * F2[id + s3] - A3 * F2[id];
-    const double rr = -du / V + 0.0;
+    const double rr = -du / V + src[m];
     r.dudt[m * vs + id] = rr;
     double u0 = r.cons[m * vs + id];
     u0 = beta * u0 + (1 - beta) * base[m * vs + id];
@@ -876,19 +1180,20 @@ __device__ __forceinline__ double regula_falsi(const TRes &f, double a, double b
 }
 
 // con2prim_robust's solve (con2prim_robust.hpp:299-453) of one zone of the
-// Minkowski fluid block with MomentFluidSourceImpl's settings (fp fails on
-// floors and ceilings), from the stored mu.  The lane iterates on its own.
-// Writes the primitives, the cell speeds and, when bounds were used, the
-// conserved variables.  True on success; an unbracketed root is a failure.
-__device__ bool fluid_invert(const Par &fp, const BView &b, int k, int j, int i, long long id) {
+// fluid block (g: its centre geometry; unused on Minkowski) with
+// MomentFluidSourceImpl's settings (fp fails on floors and ceilings), from
+// the stored mu.  The lane iterates on its own.  Writes the primitives, the
+// cell speeds and, when bounds were used, the conserved variables.  True on
+// success; an unbracketed root is a failure.
+template <bool MINK>
+__device__ bool fluid_invert(const Par &fp, const BView &b, const Pt &g, int k, int j, int i, long long id) {
   const long long vs = b.vs;
-  Pt g{};
   double U[PHX_NCONS];
 #pragma unroll
   for (int m = 0; m < PHX_NCONS; m++) U[m] = b.cons[m * vs + id];
   Residual res;
   double rcon[3], rcov[3], bu[3], Bprim[3] = {0.0, 0.0, 0.0}, bdotr = 0.0;
-  if (!c2p_setup<true>(fp, g, U, b.Xc(0, i), b.Xc(1, j), b.Xc(2, k), res, rcon, rcov, bu, Bprim, bdotr))
+  if (!c2p_setup<MINK>(fp, g, U, b.Xc(0, i), b.Xc(1, j), b.Xc(2, k), res, rcon, rcov, bu, Bprim, bdotr))
     return false;
   const double guess = b.prim[PHX_PMU * vs + id];
   RFState st;
@@ -898,7 +1203,7 @@ __device__ bool fluid_invert(const Par &fp, const BView &b, int k, int j, int i,
   const double mu = rf_result(st, guess, out);
   double prim[PHX_NPRIM], sig[3];
   bool used_bounds;
-  c2p_finish<true>(fp, g, res, mu, rcon, bu, Bprim, bdotr, prim, U, sig, used_bounds);
+  c2p_finish<MINK>(fp, g, res, mu, rcon, bu, Bprim, bdotr, prim, U, sig, used_bounds);
   for (int v = 0; v < PHX_NPRIM; v++) {
     if (v >= PHX_PB && v < PHX_PB + 3 && !fp.mhd) continue;
     b.prim[v * vs + id] = prim[v];
@@ -925,11 +1230,11 @@ __device__ bool fluid_invert(const Par &fp, const BView &b, int k, int j, int i,
 // the gamma1 slot, then prim2con of D, S, tau) and the radiation the
 // J = SMALL, H = 0 state of that fluid's closure, with the tilde-pressure
 // tensor of the inversion that failed (zero when the fluid inversion failed).
-template <bool M1>
-__device__ void source_update_fluid(const Par &fp, const BView &b, const RView &r, int k, int j, int i,
-                                    long long id, double dE, const V3 &dF) {
+template <bool M1, bool MINK>
+__device__ void source_update_fluid(const Par &fp, const BView &b, const RView &r, const RGeo<MINK> &G, int k, int j,
+                                    int i, long long id, double dE, const V3 &dF) {
   const long long vs = r.vs, fvs = b.vs;
-  const double sdetgam = 1.0;
+  const double sdetgam = G.sdetgam();
   b.cons[PHX_CENG * fvs + id] -= sdetgam * dE;
 #pragma unroll
   for (int a = 0; a < 3; a++) b.cons[(PHX_CMOM + a) * fvs + id] -= sdetgam * dF.d[a];
@@ -943,8 +1248,8 @@ __device__ void source_update_fluid(const Par &fp, const BView &b, const RView &
   double J;
 #pragma unroll
   for (int a = 0; a < 3; a++) F.d[a] = r.cons[(PHX_RF + a) * vs + id] / sdetgam;
-  if (fluid_invert(fp, b, k, j, i, id)) {
-    const Closure<M1> c(fluid_v(b, id), false);
+  if (fluid_invert<MINK>(fp, b, G.p, k, j, i, id)) {
+    const Closure<M1, MINK> c(fluid_v<MINK>(b, id, G.geo()), false, G.geo());
     double xi = 0.0, phi = PI;
     c.tilpi_from_con(E, F, xi, phi, Pi);
     if (c.con2prim(E, F, Pi, J, H) == SUCCESS) {
@@ -967,15 +1272,14 @@ __device__ void source_update_fluid(const Par &fp, const BView &b, const RView &
   if (fp.mhd)
 #pragma unroll
     for (int a = 0; a < 3; a++) bp[a] = P[(PHX_PB + a) * fvs];
-  Pt g{};
   double D, tau, S[3], bc[3], sig[3];
-  p2c<true>(P[PHX_PRHO * fvs], vp, bp, P[PHX_PENG * fvs], P[PHX_PPRS * fvs], P[PHX_PGM1 * fvs], g, sdetgam, D, S,
+  p2c<MINK>(P[PHX_PRHO * fvs], vp, bp, P[PHX_PENG * fvs], P[PHX_PPRS * fvs], P[PHX_PGM1 * fvs], G.p, sdetgam, D, S,
             bc, tau, sig);
   b.cons[PHX_CRHO * fvs + id] = D;
 #pragma unroll
   for (int a = 0; a < 3; a++) b.cons[(PHX_CMOM + a) * fvs + id] = S[a];
   b.cons[PHX_CENG * fvs + id] = tau;
-  const Closure<M1> c(fluid_v(b, id), false);
+  const Closure<M1, MINK> c(fluid_v<MINK>(b, id, G.geo()), false, G.geo());
   r.prim[PHX_RJ * vs + id] = kSMALL;
   J = r.prim[PHX_RJ * vs + id];
 #pragma unroll
@@ -989,19 +1293,20 @@ __device__ void source_update_fluid(const Par &fp, const BView &b, const RView &
   for (int a = 0; a < 3; a++) r.cons[(PHX_RF + a) * vs + id] = F.d[a] * sdetgam;
 }
 
-template <bool M1, bool UPD>
+template <bool M1, bool UPD, bool MINK>
 __global__ void __launch_bounds__(128) k_source(RPar p, Par fp, BView b, RView r, double dt, Range3 rg) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= range_count(rg)) return;
   int k, j, i;
   zone_of(rg, t, k, j, i);
   const long long id = b.idx(k, j, i), vs = r.vs, fvs = b.vs;
-  const double alpha = 1.0, sdetgam = 1.0;
+  const RGeo<MINK> G(b, 0, j, i);
+  const double alpha = G.alpha(), sdetgam = G.sdetgam();
   const double amax = p.tau_max / (alpha * dt);
   const double rho = b.prim[PHX_PRHO * fvs + id], ug = b.prim[PHX_PENG * fvs + id],
                Tf = b.prim[PHX_PTMP * fvs + id];
   double W;
-  const V3 cv = fluid_v(b, id, &W);
+  const V3 cv = fluid_v<MINK>(b, id, G.geo(), &W);
   double dE = 0.0;
   V3 dF;
   dF.d[0] = dF.d[1] = dF.d[2] = 0.0;
@@ -1020,7 +1325,7 @@ __global__ void __launch_bounds__(128) k_source(RPar p, Par fp, BView b, RView r
       T1 = regula_falsi(res, 1.e-1 / fac * Tf, 1.e1 * fac * Tf, p.tol * Tf, Tf, count, p.maxiter, ok);
       fac *= 10.;
     }
-    const Closure<M1> c(cv, true);
+    const Closure<M1, MINK> c(cv, true, G.geo());
     double Es = r.cons[PHX_RE * vs + id] / sdetgam;
     V3 Fs;
 #pragma unroll
@@ -1069,13 +1374,13 @@ __global__ void __launch_bounds__(128) k_source(RPar p, Par fp, BView b, RView r
     for (int a = 0; a < 3; a++) r.cons[(PHX_RF + a) * vs + id] += sdetgam * dF.d[a];
   }
   if constexpr (UPD) {
-    source_update_fluid<M1>(fp, b, r, k, j, i, id, dE, dF);
+    source_update_fluid<M1, MINK>(fp, b, r, G, k, j, i, id, dE, dF);
     return;
   }
   double E = r.cons[PHX_RE * vs + id] / sdetgam;
   V3 F, H;
   double J;
-  const Closure<M1> cf(cv, false);
+  const Closure<M1, MINK> cf(cv, false, G.geo());
 #pragma unroll
   for (int a = 0; a < 3; a++) F.d[a] = r.cons[(PHX_RF + a) * vs + id] / sdetgam;
   double xi = 0.0, phi = PI;
@@ -1100,8 +1405,157 @@ __global__ void __launch_bounds__(128) k_source(RPar p, Par fp, BView b, RView r
   for (int a = 0; a < 3; a++) r.cons[(PHX_RF + a) * vs + id] = F.d[a] * sdetgam;
 }
 
+// ------------------------------------- RadConservedToPrimitiveFixup
+// fixup_radc2p.cpp:45-225 over the interior: a zone whose closure inversion
+// failed (c2pfail = 0) takes the average of J and H_i / J over its face
+// neighbours weighted by their c2pfail flags (strategy interpolate, at least
+// one valid neighbour), else J = 10 SMALL, H = 0; H / J is then held to the
+// xi ceiling and E, F_i follow from prim2con with the zone's fluid velocity.
+// A failed neighbour contributes nothing; the reference multiplies it by its
+// zero flag in place while other zones are rewritten, which is the same
+// whenever the failed zones hold finite values.
+template <bool M1, bool MINK>
+__global__ void __launch_bounds__(128) k_rad_c2p_fixup(RPar p, BView b, RView r, Range3 rg) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= range_count(rg)) return;
+  int k, j, i;
+  zone_of(rg, t, k, j, i);
+  const long long id = b.idx(k, j, i), vs = r.vs;
+  const double *F = r.prim + PHX_RFAIL * vs;
+  if (F[id] != 0.0) return;
+  const long long di = 1, dj = b.n1t, dk = (long long)b.n1t * b.n2t;
+  const RGeo<MINK> G(b, 0, j, i);
+  const V3 cv = fluid_v<MINK>(b, id, G.geo());
+  auto nb = [&](int iv, long long o) { return F[o] != 0.0 ? F[o] * r.prim[iv * vs + o] : 0.0; };
+  auto fixv = [&](int iv, double inv_mask_sum) {
+    double s = nb(iv, id - di) + nb(iv, id + di);
+    if (b.ndim > 1) {
+      s += nb(iv, id - dj) + nb(iv, id + dj);
+      if (b.ndim == 3) s += nb(iv, id - dk) + nb(iv, id + dk);
+    }
+    return inv_mask_sum * s;
+  };
+  double num_valid = F[id - di] + F[id + di];
+  if (b.ndim > 1) num_valid += F[id - dj] + F[id + dj];
+  if (b.ndim == 3) num_valid += F[id - dk] + F[id + dk];
+  double J;
+  V3 Hr;
+  if (num_valid > 0.5 && !p.rad_fixup_floors) {
+    const double norm = 1.0 / num_valid;
+    J = fixv(PHX_RJ, norm);
+#pragma unroll
+    for (int a = 0; a < 3; a++) Hr.d[a] = fixv(PHX_RH + a, norm);
+  } else {
+    J = 10. * kSMALL;
+    Hr.d[0] = Hr.d[1] = Hr.d[2] = 0.;
+  }
+  {
+    const double hh = MINK ? ccov(Hr, Hr) : G.g.contract_cov(Hr, Hr);
+    const double vh = ccov(cv, Hr);
+    const double xi = sqrt(hh - vh * vh);
+    if (xi > p.xi_ceiling) {
+#pragma unroll
+      for (int a = 0; a < 3; a++) Hr.d[a] *= p.xi_ceiling / xi;
+    }
+  }
+  r.prim[PHX_RJ * vs + id] = J;
+#pragma unroll
+  for (int a = 0; a < 3; a++) r.prim[(PHX_RH + a) * vs + id] = Hr.d[a];
+  const Closure<M1, MINK> c(cv, true, G.geo());
+  V3 H;
+#pragma unroll
+  for (int a = 0; a < 3; a++) H.d[a] = Hr.d[a] * J;
+  T2 Pi;
+  c.tilpi_from_prim(J, H, Pi);
+  double E;
+  V3 Fc;
+  c.prim2con(J, H, Pi, E, Fc);
+  const double sdetgam = G.sdetgam();
+  r.cons[PHX_RE * vs + id] = sdetgam * E;
+#pragma unroll
+  for (int a = 0; a < 3; a++) r.cons[(PHX_RF + a) * vs + id] = sdetgam * Fc.d[a];
+}
+
+// ------------------------------------- ApplyFloors, radiation part
+// fixup.cpp:542-678 (enable_rad_floors, one species), after the fluid part
+// of the same zone: with the fluid's velocity as the floors left it, the
+// closure inversion is redone where the fluid floors or ceilings acted
+// (flag != 0), from xi = 0; a J below the floor gains an isotropic
+// normal-observer radiation field of the missing J (added to E, F_i, then
+// inverted again); H / J above the xi ceiling is scaled down and E, F_i
+// recomputed.
+template <bool M1, bool MINK>
+__global__ void __launch_bounds__(128) k_rad_floors(RPar p, BView b, RView r, const double *flag, Range3 rg) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= range_count(rg)) return;
+  int k, j, i;
+  zone_of(rg, t, k, j, i);
+  const long long id = b.idx(k, j, i), vs = r.vs;
+  const RGeo<MINK> G(b, 0, j, i);
+  const double sdetgam = G.sdetgam();
+  const V3 cv = fluid_v<MINK>(b, id, G.geo());
+  const Closure<M1, MINK> c(cv, true, G.geo());
+  double E, J;
+  V3 F, H;
+  T2 Pi;
+  auto invert = [&]() {  // GetConTilPiFromCon from xi = 0, then Con2Prim; J, H / J stored
+    double xi = 0.0, phi = PI * 1.000001;
+    c.tilpi_from_con(E, F, xi, phi, Pi);
+    c.con2prim(E, F, Pi, J, H);
+    r.prim[PHX_RJ * vs + id] = J;
+#pragma unroll
+    for (int a = 0; a < 3; a++) r.prim[(PHX_RH + a) * vs + id] = H.d[a] / J;
+  };
+  if (flag[id] != 0.0) {
+    E = r.cons[PHX_RE * vs + id] / sdetgam;
+#pragma unroll
+    for (int a = 0; a < 3; a++) F.d[a] = r.cons[(PHX_RF + a) * vs + id] / sdetgam;
+    invert();
+  }
+  const double dJ = p.J_floor - r.prim[PHX_RJ * vs + id];
+  if (dJ > 0.) {
+    V3 zero, Hz;
+    zero.d[0] = zero.d[1] = zero.d[2] = 0.0;
+    Hz = zero;
+    T2 Pz;
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int q = 0; q < 3; q++) Pz.d[a][q] = 0.0;
+    const Closure<M1, MINK> c_iso(zero, true, G.geo());
+    c_iso.prim2con(dJ, Hz, Pz, E, F);
+    E += r.cons[PHX_RE * vs + id] / sdetgam;
+#pragma unroll
+    for (int a = 0; a < 3; a++) F.d[a] += r.cons[(PHX_RF + a) * vs + id] / sdetgam;
+    r.cons[PHX_RE * vs + id] = E * sdetgam;
+#pragma unroll
+    for (int a = 0; a < 3; a++) r.cons[(PHX_RF + a) * vs + id] = F.d[a] * sdetgam;
+    invert();
+  }
+  V3 Hr;
+#pragma unroll
+  for (int a = 0; a < 3; a++) Hr.d[a] = r.prim[(PHX_RH + a) * vs + id];
+  const double hh = MINK ? ccov(Hr, Hr) : G.g.contract_cov(Hr, Hr);
+  const double vh = ccov(cv, Hr);
+  const double xi = sqrt(hh - vh * vh);
+  if (xi > p.xi_ceiling) {
+    J = r.prim[PHX_RJ * vs + id];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      H.d[a] = (p.xi_ceiling / xi) * Hr.d[a] * J;
+      r.prim[(PHX_RH + a) * vs + id] = H.d[a] / J;
+    }
+    c.tilpi_from_prim(J, H, Pi);
+    c.prim2con(J, H, Pi, E, F);
+    r.cons[PHX_RE * vs + id] = E * sdetgam;
+#pragma unroll
+    for (int a = 0; a < 3; a++) r.cons[(PHX_RF + a) * vs + id] = F.d[a] * sdetgam;
+  }
+}
+
 // ------------------------------------------------------- timestep
 __global__ void k_dt_init(unsigned long long *scratch) { *scratch = 0x7fefffffffffffffull; }
+template <bool MINK>
 __global__ void __launch_bounds__(256) k_dt(RPar p, BView b, RView r, Range3 rg, unsigned long long *scratch) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   double v = DBL_MAX;
@@ -1109,15 +1563,17 @@ __global__ void __launch_bounds__(256) k_dt(RPar p, BView b, RView r, Range3 rg,
     int k, j, i;
     zone_of(rg, t, k, j, i);
     const long long id = b.idx(k, j, i);
+    const RGeo<MINK> G(b, 0, j, i);
+    const double alpha = G.alpha();
     const double kappaH = r.prim[PHX_RKAPPAH * r.vs + id];
     for (int d = 0; d < b.ndim; d++) {
-      const double sigp = 1.0 * sqrt(1.0) - 0.0;
-      const double sigm = -1.0 * sqrt(1.0) - 0.0;
-      const double asym_sigl = 1.0 * b.prim[(PHX_PVEL + d) * b.vs + id] - 0.0;
+      const double sigp = alpha * sqrt(G.con(d, d)) - G.beta(d);
+      const double sigm = -alpha * sqrt(G.con(d, d)) - G.beta(d);
+      const double asym_sigl = alpha * b.prim[(PHX_PVEL + d) * b.vs + id] - G.beta(d);
       const double rad_speed = smax(fabs(sigm), fabs(sigp));
       const double asym_speed = fabs(asym_sigl);
       const double w = b.dx[d];
-      const double dx = w * sqrt(1.0);
+      const double dx = w * sqrt(G.cov(d, d));
       const double a = tanh_r(ratio(1.0, fabs(kappaH * dx)));
       const double csig = a * rad_speed + (1. - a) * asym_speed;
       v = smin(v, 1.0 / (csig / w));
@@ -1147,22 +1603,40 @@ Range3 interior3(const BView &b) {
 }
 }  // namespace
 
+// Every launcher picks the closure (M1 or Eddington) and the metric
+// (Minkowski, or the block's FMKS tables) at run time.
 void launch_p2c(const RPar &p, const BView &b, const RView &r, Range3 rg, cudaStream_t s) {
   const long long n = range_count(rg);
   if (n <= 0) return;
-  if (p.m1)
-    k_p2c<true><<<blocks_for(n, 128), 128, 0, s>>>(p, b, r, rg);
-  else
-    k_p2c<false><<<blocks_for(n, 128), 128, 0, s>>>(p, b, r, rg);
+  const unsigned g = blocks_for(n, 128);
+  if (b.fmks) {
+    if (p.m1)
+      k_p2c<true, false><<<g, 128, 0, s>>>(p, b, r, rg);
+    else
+      k_p2c<false, false><<<g, 128, 0, s>>>(p, b, r, rg);
+  } else {
+    if (p.m1)
+      k_p2c<true, true><<<g, 128, 0, s>>>(p, b, r, rg);
+    else
+      k_p2c<false, true><<<g, 128, 0, s>>>(p, b, r, rg);
+  }
 }
 
 void launch_c2p(const RPar &p, const BView &b, const RView &r, Range3 rg, cudaStream_t s) {
   const long long n = range_count(rg);
   if (n <= 0) return;
-  if (p.m1)
-    k_c2p<true><<<blocks_for(n, 128), 128, 0, s>>>(p, b, r, rg);
-  else
-    k_c2p<false><<<blocks_for(n, 128), 128, 0, s>>>(p, b, r, rg);
+  const unsigned g = blocks_for(n, 128);
+  if (b.fmks) {
+    if (p.m1)
+      k_c2p<true, false><<<g, 128, 0, s>>>(p, b, r, rg);
+    else
+      k_c2p<false, false><<<g, 128, 0, s>>>(p, b, r, rg);
+  } else {
+    if (p.m1)
+      k_c2p<true, true><<<g, 128, 0, s>>>(p, b, r, rg);
+    else
+      k_c2p<false, true><<<g, 128, 0, s>>>(p, b, r, rg);
+  }
 }
 
 void launch_opacities(const RPar &p, const BView &b, const RView &r, cudaStream_t s) {
@@ -1170,24 +1644,24 @@ void launch_opacities(const RPar &p, const BView &b, const RView &r, cudaStream_
   k_opacities<<<blocks_for(n, 256), 256, 0, s>>>(p, b, r, n);
 }
 
-template <bool M1, int RECON>
+template <bool M1, int RECON, bool MINK>
 static void fluxes_r(const BView &b, const RPar &p, const RView &r, int d, Range3 rg, unsigned g, cudaStream_t s) {
   if (d == 0)
-    k_fluxes<M1, RECON, 0><<<g, 128, 0, s>>>(p, b, r, rg);
+    k_fluxes<M1, RECON, 0, MINK><<<g, 128, 0, s>>>(p, b, r, rg);
   else if (d == 1)
-    k_fluxes<M1, RECON, 1><<<g, 128, 0, s>>>(p, b, r, rg);
+    k_fluxes<M1, RECON, 1, MINK><<<g, 128, 0, s>>>(p, b, r, rg);
   else
-    k_fluxes<M1, RECON, 2><<<g, 128, 0, s>>>(p, b, r, rg);
+    k_fluxes<M1, RECON, 2, MINK><<<g, 128, 0, s>>>(p, b, r, rg);
 }
 
-template <bool M1>
+template <bool M1, bool MINK>
 static void fluxes_t(const RPar &p, const BView &b, const RView &r, int d, Range3 rg, cudaStream_t s) {
   const unsigned g = blocks_for(range_count(rg), 128);
   switch (p.recon) {
-  case PHX_RECON_WENO5Z: fluxes_r<M1, PHX_RECON_WENO5Z>(b, p, r, d, rg, g, s); break;
-  case PHX_RECON_MP5: fluxes_r<M1, PHX_RECON_MP5>(b, p, r, d, rg, g, s); break;
-  case PHX_RECON_LINEAR: fluxes_r<M1, PHX_RECON_LINEAR>(b, p, r, d, rg, g, s); break;
-  default: fluxes_r<M1, PHX_RECON_CONSTANT>(b, p, r, d, rg, g, s); break;
+  case PHX_RECON_WENO5Z: fluxes_r<M1, PHX_RECON_WENO5Z, MINK>(b, p, r, d, rg, g, s); break;
+  case PHX_RECON_MP5: fluxes_r<M1, PHX_RECON_MP5, MINK>(b, p, r, d, rg, g, s); break;
+  case PHX_RECON_LINEAR: fluxes_r<M1, PHX_RECON_LINEAR, MINK>(b, p, r, d, rg, g, s); break;
+  default: fluxes_r<M1, PHX_RECON_CONSTANT, MINK>(b, p, r, d, rg, g, s); break;
   }
 }
 
@@ -1197,33 +1671,55 @@ void launch_fluxes(const RPar &p, const BView &b, const RView &r, cudaStream_t s
     if (d == 0) rg.ie += 1;
     if (d == 1) rg.je += 1;
     if (d == 2) rg.ke += 1;
-    if (p.m1)
-      fluxes_t<true>(p, b, r, d, rg, s);
-    else
-      fluxes_t<false>(p, b, r, d, rg, s);
+    if (b.fmks) {
+      if (p.m1)
+        fluxes_t<true, false>(p, b, r, d, rg, s);
+      else
+        fluxes_t<false, false>(p, b, r, d, rg, s);
+    } else {
+      if (p.m1)
+        fluxes_t<true, true>(p, b, r, d, rg, s);
+      else
+        fluxes_t<false, true>(p, b, r, d, rg, s);
+    }
   }
 }
 
-void launch_update(const BView &b, const RView &r, const double *base, double *out, double beta, double dt,
-                   cudaStream_t s) {
+void launch_update(const RPar &p, const BView &b, const RView &r, const double *base, double *out, double beta,
+                   double dt, cudaStream_t s) {
   const Range3 rg = interior3(b);
-  k_update<<<blocks_for(range_count(rg), 256), 256, 0, s>>>(b, r, base, out, beta, dt, rg);
+  const unsigned g = blocks_for(range_count(rg), 256);
+  if (!b.fmks)
+    k_update<true, true><<<g, 256, 0, s>>>(b, r, base, out, beta, dt, rg);
+  else if (p.m1)
+    k_update<true, false><<<g, 256, 0, s>>>(b, r, base, out, beta, dt, rg);
+  else
+    k_update<false, false><<<g, 256, 0, s>>>(b, r, base, out, beta, dt, rg);
+}
+
+template <bool MINK>
+static void source_t(const RPar &p, const Par &fp, const BView &b, const RView &r, double dt, Range3 rg, unsigned g,
+                     cudaStream_t s) {
+  if (p.m1) {
+    if (p.update_fluid)
+      k_source<true, true, MINK><<<g, 128, 0, s>>>(p, fp, b, r, dt, rg);
+    else
+      k_source<true, false, MINK><<<g, 128, 0, s>>>(p, fp, b, r, dt, rg);
+  } else {
+    if (p.update_fluid)
+      k_source<false, true, MINK><<<g, 128, 0, s>>>(p, fp, b, r, dt, rg);
+    else
+      k_source<false, false, MINK><<<g, 128, 0, s>>>(p, fp, b, r, dt, rg);
+  }
 }
 
 void launch_source(const RPar &p, const Par &fp, const BView &b, const RView &r, double dt, cudaStream_t s) {
   const Range3 rg = interior3(b);
   const unsigned g = blocks_for(range_count(rg), 128);
-  if (p.m1) {
-    if (p.update_fluid)
-      k_source<true, true><<<g, 128, 0, s>>>(p, fp, b, r, dt, rg);
-    else
-      k_source<true, false><<<g, 128, 0, s>>>(p, fp, b, r, dt, rg);
-  } else {
-    if (p.update_fluid)
-      k_source<false, true><<<g, 128, 0, s>>>(p, fp, b, r, dt, rg);
-    else
-      k_source<false, false><<<g, 128, 0, s>>>(p, fp, b, r, dt, rg);
-  }
+  if (b.fmks)
+    source_t<false>(p, fp, b, r, dt, rg, g, s);
+  else
+    source_t<true>(p, fp, b, r, dt, rg, g, s);
 }
 
 void launch_ghosts(const BView &b, const RView &r, cudaStream_t s) {
@@ -1233,11 +1729,48 @@ void launch_ghosts(const BView &b, const RView &r, cudaStream_t s) {
   launch_ghost_periodic(v, r.prim, PHX_RFAIL + 1, s);
 }
 
+void launch_rad_c2p_fixup(const RPar &p, const BView &b, const RView &r, cudaStream_t s) {
+  const Range3 rg = interior3(b);
+  const unsigned g = blocks_for(range_count(rg), 128);
+  if (b.fmks) {
+    if (p.m1)
+      k_rad_c2p_fixup<true, false><<<g, 128, 0, s>>>(p, b, r, rg);
+    else
+      k_rad_c2p_fixup<false, false><<<g, 128, 0, s>>>(p, b, r, rg);
+  } else {
+    if (p.m1)
+      k_rad_c2p_fixup<true, true><<<g, 128, 0, s>>>(p, b, r, rg);
+    else
+      k_rad_c2p_fixup<false, true><<<g, 128, 0, s>>>(p, b, r, rg);
+  }
+}
+
+void launch_rad_floors(const RPar &p, const BView &b, const RView &r, const double *flag, Range3 rg,
+                       cudaStream_t s) {
+  const long long n = range_count(rg);
+  if (n <= 0) return;
+  const unsigned g = blocks_for(n, 128);
+  if (b.fmks) {
+    if (p.m1)
+      k_rad_floors<true, false><<<g, 128, 0, s>>>(p, b, r, flag, rg);
+    else
+      k_rad_floors<false, false><<<g, 128, 0, s>>>(p, b, r, flag, rg);
+  } else {
+    if (p.m1)
+      k_rad_floors<true, true><<<g, 128, 0, s>>>(p, b, r, flag, rg);
+    else
+      k_rad_floors<false, true><<<g, 128, 0, s>>>(p, b, r, flag, rg);
+  }
+}
+
 void launch_dt(const RPar &p, const BView &b, const RView &r, unsigned long long *scratch, double *dt_out,
                cudaStream_t s) {
   const Range3 rg = interior3(b);
   k_dt_init<<<1, 1, 0, s>>>(scratch);
-  k_dt<<<blocks_for(range_count(rg), 256), 256, 0, s>>>(p, b, r, rg, scratch);
+  if (b.fmks)
+    k_dt<false><<<blocks_for(range_count(rg), 256), 256, 0, s>>>(p, b, r, rg, scratch);
+  else
+    k_dt<true><<<blocks_for(range_count(rg), 256), 256, 0, s>>>(p, b, r, rg, scratch);
   k_dt_final<<<1, 1, 0, s>>>(scratch, p.cfl, dt_out);
 }
 

@@ -16,6 +16,7 @@ struct RPar {
   int maxiter;     // src_rootfind_maxiter
   int oned_fixup;  // phx_rad_oned_fixup
   int update_fluid;  // MomentFluidSource also updates and inverts the fluid
+  int rad_fixup_floors;  // rad_c2p_failure_strategy floors (else interpolate)
   double cfl, tol, kappa_a, kappa_s, jbb;
   double J_floor, xi_ceiling, tau_max, W_ceiling, Cv;
 };
@@ -30,12 +31,20 @@ void launch_p2c(const RPar &p, const BView &b, const RView &r, Range3 rg, cudaSt
 void launch_c2p(const RPar &p, const BView &b, const RView &r, Range3 rg, cudaStream_t s);
 void launch_opacities(const RPar &p, const BView &b, const RView &r, cudaStream_t s);
 void launch_fluxes(const RPar &p, const BView &b, const RView &r, cudaStream_t s);
-void launch_update(const BView &b, const RView &r, const double *base, double *out, double beta, double dt,
-                   cudaStream_t s);
+// FluxDivergence + SumData (the geometric source on FMKS blocks) + the RK
+// update of the interior
+void launch_update(const RPar &p, const BView &b, const RView &r, const double *base, double *out, double beta,
+                   double dt, cudaStream_t s);
 // fp: the fluid's con2prim settings for update_fluid (failure on floors and
 // ceilings, as MomentFluidSourceImpl sets them up)
 void launch_source(const RPar &p, const Par &fp, const BView &b, const RView &r, double dt, cudaStream_t s);
 void launch_ghosts(const BView &b, const RView &r, cudaStream_t s);
+// RadConservedToPrimitiveFixup over the interior
+void launch_rad_c2p_fixup(const RPar &p, const BView &b, const RView &r, cudaStream_t s);
+// the radiation part of ApplyFloors over rg; flag[N]: nonzero where the fluid
+// part floored or ceilinged the zone (launch_floors' flag output)
+void launch_rad_floors(const RPar &p, const BView &b, const RView &r, const double *flag, Range3 rg,
+                       cudaStream_t s);
 void launch_dt(const RPar &p, const BView &b, const RView &r, unsigned long long *scratch, double *dt_out,
                cudaStream_t s);
 

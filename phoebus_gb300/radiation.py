@@ -8,7 +8,9 @@ radiation.cpp) for the moment_m1 / moment_eddington methods:
     ReconstructEdgeStates +
     CalculateFluxes            moments.cpp:280-736 (fused on the device)
     MomentFluidSource          moments_source.cpp:203-965 (oned; update_fluid either way)
-    EstimateTimestepBlock      radiation.cpp:681-733
+    RadConservedToPrimitiveFixup fixup_radc2p.cpp:45-225
+    ApplyFloors (radiation on) fixup.cpp:285-678
+    EstimateTimestepBlock      radiation.cpp:585-648
 plus the RK stage glue of PhoebusDriver::RungeKuttaStage with the fluid not
 evolved (Stage) or evolved with the moments (FluidStage), and the problem
 generators radiation_advection (pgen/radiation_advection.cpp, which the
@@ -99,6 +101,17 @@ class RadiationContext:
         s, r = b.struct(), rad_struct(b)
         self._ok(self.lib.phx_rad_fluid_source(self.h, C.byref(rp), C.byref(p), C.byref(s), C.byref(r),
                                                float(dt), _stream(stream)))
+
+    def RadConservedToPrimitiveFixup(self, rp, p, b: Block, stream=None):
+        s, r = b.struct(), rad_struct(b)
+        self._ok(self.lib.phx_rad_c2p_fixup(self.h, C.byref(rp), C.byref(p), C.byref(s), C.byref(r), _stream(stream)))
+
+    def ApplyFloors(self, rp, p, b: Block, ib=None, jb=None, kb=None, stream=None):
+        """fixup::ApplyFloors with radiation active (phx_rad_apply_floors)."""
+        e = b.entire()
+        s, r = b.struct(), rad_struct(b)
+        self._ok(self.lib.phx_rad_apply_floors(self.h, C.byref(rp), C.byref(p), C.byref(s), C.byref(r),
+                                               _rng(ib or e[0]), _rng(jb or e[1]), _rng(kb or e[2]), _stream(stream)))
 
     def FillGhostsPeriodic(self, b: Block, stream=None):
         s, r = b.struct(), rad_struct(b)

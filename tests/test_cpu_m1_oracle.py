@@ -333,3 +333,151 @@ def test_update_fluid_failure_state(rad_oracle):
     keep = np.ones(tot.shape, bool)
     keep[..., bad - hb.ng] = False
     assert np.max(np.abs(tot - e0)[keep] / np.abs(e0)[keep]) < 1e-12
+
+
+# ---- curved geometry (FMKS tables)
+@pytest.mark.parametrize("method", ["moment_m1", "moment_eddington"])
+def test_fmks_closure_round_trip(rad_oracle, method):
+    """On an FMKS block, MomentPrim2Con then MomentCon2Prim returns J and
+    H_i / J (LocalThreeGeometry with gamma^ij from matrixInverse3x3, the
+    tables' sqrt(gamma)) where the reference's closure solve is exact: the
+    Eddington closure for a moving fluid (a linear inversion), M1 for a fluid
+    at rest (the rest-frame flux then lies along the basis vector g the solve
+    holds it to); the second prim2con returns E and F_i."""
+    from tests.util import random_rad_block_fmks
+
+    m1 = method == "moment_m1"
+    hb = random_rad_block_fmks((12, 10, 1), 2, seed=31, vmax=0.0 if m1 else 0.3)
+    rp = abi.default_rad_params(method=method)
+    p = abi.default_params()
+    J0, H0 = hb["rprim"][abi.RJ].copy(), hb["rprim"][abi.RH:abi.RH + 3].copy()
+    rad_oracle.MomentPrim2Con(rp, p, hb, *hb.entire())
+    E0 = hb["rcons"].copy()
+    rad_oracle.MomentCon2Prim(rp, p, hb)
+    tol = 1e-8 if m1 else 1e-12
+    assert np.all(hb["rprim"][abi.RFAIL] == 1.0)
+    assert np.max(np.abs(hb["rprim"][abi.RJ] - J0) / J0) < tol
+    assert np.max(np.abs(hb["rprim"][abi.RH:abi.RH + 3] - H0) / np.abs(H0).max()) < tol
+    rad_oracle.MomentPrim2Con(rp, p, hb, *hb.entire())
+    assert np.max(np.abs(hb["rcons"] - E0) / np.abs(E0[0])) < tol
+
+
+def test_fmks_geometric_source_equals_fluid_source(rad_oracle):
+    """Isotropic radiation at rest (Eddington closure, H = 0, v = 0) has
+    T^{mu nu} = (4/3) J u^mu u^nu + (1/3) J g^{mu nu}: the stress tensor of a
+    perfect fluid with u = J, P = J / 3, rho = 0.  Its geometric source
+    (moments.cpp:764-885) therefore equals the fluid's
+    (CalculateFluidSourceTerms, fluid.cpp:566-657) on the same FMKS tables, to
+    rounding of the two operation orders."""
+    from oracle.oracle import Oracle
+    from tests.util import random_rad_block_fmks
+
+    hb = random_rad_block_fmks((10, 8, 1), 2, seed=5, vmax=0.0, hmax=0.0)
+    rp = abi.default_rad_params(method="moment_eddington")
+    p = abi.default_params(Gamma=4.0 / 3.0)
+    J = hb["rprim"][abi.RJ]
+    hb["rprim"][abi.RH:abi.RH + 3] = 0.0
+    hb["prim"][abi.PVEL:abi.PVEL + 3] = 0.0
+    rad_oracle.MomentPrim2Con(rp, p, hb, *hb.entire())
+    src_r = rad_oracle.GeometricSource(rp, hb)
+    P = hb["prim"]
+    P[abi.PRHO] = 0.0
+    P[abi.PENG] = J
+    P[abi.PPRS] = J / 3.0
+    P[abi.PB:abi.PB + 3] = 0.0
+    Oracle().CalculateFluidSourceTerms(p, hb)
+    src_f = hb["src"]  # S_1..3, tau
+    ks, js, is_ = hb.isl()
+    big = np.max(np.abs(src_f[:4][:, ks, js, is_]))
+    for m_r, m_f, name in ((0, 3, "E / tau"), (1, 0, "F_1"), (2, 1, "F_2")):
+        a, b = src_r[m_r][ks, js, is_], src_f[m_f][ks, js, is_]
+        err = np.max(np.abs(a - b) / (np.abs(b) + 1e-14 * big))
+        print(f"geometric source {name}: max rel {err:.2e}")
+        assert err < 1e-10, name
+    # d/dphi is a Killing vector of the axisymmetric metric: both F_3 sources
+    # vanish, each to the rounding of its own sum
+    a, b = src_r[3][ks, js, is_], src_f[2][ks, js, is_]
+    print(f"geometric source F_3: max |rad| {np.abs(a).max():.2e}, max |fluid| {np.abs(b).max():.2e} of {big:.2e}")
+    assert np.abs(a).max() <= 1e-12 * big and np.abs(b).max() <= 1e-12 * big
+
+
+# ---- radiation parts of the fixups and floors
+def _rad_state(rad_oracle, method, seed=13):
+    hb = random_rad_block((16, 12, 1), 2, seed=seed, vmax=0.3)
+    p = abi.default_params(Gamma=5.0 / 3.0, Cv=1.0)
+    P = hb["prim"]
+    P[abi.PPRS] = p.gm1 * P[abi.PENG]
+    P[abi.PGM1] = p.gm1 + 1.0
+    rp = abi.default_rad_params(method=method)
+    rad_oracle.MomentPrim2Con(rp, p, hb, *hb.entire())
+    rad_oracle.MomentCon2Prim(rp, p, hb)
+    return hb, p, rp
+
+
+@pytest.mark.parametrize("method", ["moment_m1", "moment_eddington"])
+def test_rad_c2p_fixup(rad_oracle, method):
+    """RadConservedToPrimitiveFixup (fixup_radc2p.cpp:45-225): a zone marked
+    failed takes the mean of its valid face neighbours' J and H / J, and its
+    E, F_i become prim2con of those; with no valid neighbour (or the floors
+    strategy) J = 10 SMALL, H = 0; valid zones are untouched."""
+    hb, p, rp = _rad_state(rad_oracle, method)
+    p.enable_c2p_fixup = 1
+    R = hb["rprim"]
+    k, j0 = 0, hb.ng + 3
+    i0 = hb.ng + 4
+    R[abi.RFAIL][k, j0, i0] = 0.0             # isolated failure
+    R[abi.RFAIL][k, j0 + 5, i0:i0 + 2] = 0.0  # two adjacent failures
+    before = {n: hb[n].copy() for n in ("rprim", "rcons")}
+    nbrs = [(k, j0, i0 - 1), (k, j0, i0 + 1), (k, j0 - 1, i0), (k, j0 + 1, i0)]
+    want_J = np.mean([R[abi.RJ][z] for z in nbrs])
+    want_H = [np.mean([R[abi.RH + a][z] for z in nbrs]) for a in range(3)]
+    rad_oracle.RadConservedToPrimitiveFixup(rp, p, hb)
+    assert hb["rprim"][abi.RJ][k, j0, i0] == pytest.approx(want_J, rel=1e-14)
+    for a in range(3):
+        assert hb["rprim"][abi.RH + a][k, j0, i0] == pytest.approx(want_H[a], rel=1e-12, abs=1e-15)
+    # the pair: each sees three valid neighbours and one failed (contributing nothing)
+    z = (k, j0 + 5, i0)
+    n3 = [(k, j0 + 5, i0 - 1), (k, j0 + 4, i0), (k, j0 + 6, i0)]
+    assert hb["rprim"][abi.RJ][z] == pytest.approx(np.mean([before["rprim"][abi.RJ][q] for q in n3]), rel=1e-14)
+    changed = np.any(hb["rprim"] != before["rprim"], axis=0) | np.any(hb["rcons"] != before["rcons"], axis=0)
+    assert set(map(tuple, np.argwhere(changed))) <= {(k, j0, i0), (k, j0 + 5, i0), (k, j0 + 5, i0 + 1)}
+    # E, F from the fixed primitives
+    fresh = hb.to_host()
+    rad_oracle.MomentPrim2Con(rp, p, fresh, *fresh.entire())
+    np.testing.assert_array_equal(hb["rcons"][:, k, j0, i0], fresh["rcons"][:, k, j0, i0])
+    # floors strategy
+    hb, p, rp = _rad_state(rad_oracle, method)
+    p.enable_c2p_fixup, rp.rad_c2p_failure_floors = 1, 1
+    hb["rprim"][abi.RFAIL][k, j0, i0] = 0.0
+    rad_oracle.RadConservedToPrimitiveFixup(rp, p, hb)
+    assert hb["rprim"][abi.RJ][k, j0, i0] == 10 * 10 * np.finfo(np.float64).tiny
+    assert np.all(hb["rprim"][abi.RH:abi.RH + 3, k, j0, i0] == 0.0)
+
+
+def test_rad_floors_and_ceiling(rad_oracle):
+    """The radiation part of ApplyFloors (fixup.cpp:542-678): after it every
+    zone has J at or above the J floor (an isotropic normal-observer field
+    of the missing J added to E), xi = |H| / J at or below the xi ceiling,
+    and zones the floors do not touch keep their state."""
+    hb, p, rp = _rad_state(rad_oracle, "moment_m1", seed=17)
+    p.enable_floors = 1
+    p.rho0_floor, p.sie0_floor = 1e-12, 1e-12  # the fluid floors stay inactive
+    J = hb["rprim"][abi.RJ]
+    rp.enable_rad_floors, rp.J0_floor = 1, float(np.quantile(J, 0.3))
+    rp.enable_rad_ceilings, rp.xi0_ceiling = 1, 0.5
+    before = {n: hb[n].copy() for n in ("rprim", "rcons")}
+    rad_oracle.ApplyFloors(rp, p, hb)
+    R = hb["rprim"]
+    assert np.all(R[abi.RJ] >= rp.J0_floor * (1 - 1e-9))
+    raised = before["rprim"][abi.RJ] < rp.J0_floor
+    assert raised.sum() > 10
+    Hr = R[abi.RH:abi.RH + 3]
+    P = hb["prim"]
+    W = np.sqrt(1 + (P[abi.PVEL:abi.PVEL + 3] ** 2).sum(0))
+    v = P[abi.PVEL:abi.PVEL + 3] / W
+    xi = np.sqrt((Hr * Hr).sum(0) - (v * Hr).sum(0) ** 2)
+    assert np.all(xi <= 0.5 * (1 + 1e-9))
+    xb = before["rprim"][abi.RH:abi.RH + 3]
+    xi0 = np.sqrt((xb * xb).sum(0) - (v * xb).sum(0) ** 2)
+    keep = ~raised & (xi0 <= 0.5)
+    np.testing.assert_array_equal(hb["rcons"][:, keep], before["rcons"][:, keep])

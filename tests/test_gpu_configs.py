@@ -328,31 +328,46 @@ def test_config3_batched_vs_oracle(oracle, ctx_exact, ctx_fast, exact):
                   f"zones beyond 1e-6: GPU {cg}, oracle {co} of {eg.size}")
             assert pg <= 3 * po + 1e-11, (n, pg, po)
             assert cg <= 3 * co + 10, (n, cg, co)
-        # (2) The con2prim arithmetic alone, per zone: in every zone the
-        # inversion succeeded, the GPU's root against the oracle's, and the
-        # GPU's primitives against the reference's finish (oracle) evaluated
-        # at the GPU's own root on the GPU's own conserved state.
+        # (2) The con2prim arithmetic alone, per zone, on the GPU's stage-1
+        # output: the production zone con2prim and the oracle's from the same
+        # conserved variables and the same stored mu (the stage's floors,
+        # ceilings and c2p fixup rewrite primitives after the inversion, so
+        # the stage's own primitives are left to (1)).  Where both succeed:
+        # the GPU's root against the oracle's, and the GPU's primitives
+        # against the reference's finish at the GPU's own root.
         dmu, fin = [], {n: [] for n in PRIM_VARS}
-        for h, d, dd in zip(hosts, devs, d_out):
-            ok = h["fail"][0].ravel() == 1.0
-            g = d["prim"].cpu().numpy().reshape(abi.NPRIM, -1)
-            pz = np.ascontiguousarray(g.copy())
-            cz = np.ascontiguousarray(dd.cpu().numpy().reshape(abi.NCONS, -1).copy())
-            oracle.ConservedToPrimitiveZonesAtMu(p, cz, pz, g[abi.PMU].copy())
-            dmu.append(np.abs(g[abi.PMU] - h["prim"][abi.PMU].ravel())[ok])
-            fl = prim_floors(h)
+        for d, dd in zip(devs, d_out):
+            cz = dd.reshape(abi.NCONS, -1).clone()
+            pz = d["prim"].reshape(abi.NPRIM, -1).clone()
+            fail_g = ctx.ConservedToPrimitiveZones(p, cz, pz)
+            ctx.check()
+            ch = np.ascontiguousarray(dd.cpu().numpy().reshape(abi.NCONS, -1))
+            ph = np.ascontiguousarray(d["prim"].cpu().numpy().reshape(abi.NPRIM, -1))
+            fail_o = np.zeros(ch.shape[1])
+            oracle.ConservedToPrimitiveZones(p, ch.copy(), ph, fail=fail_o)
+            g = pz.cpu().numpy()
+            at = np.ascontiguousarray(g.copy())
+            oracle.ConservedToPrimitiveZonesAtMu(p, np.ascontiguousarray(dd.cpu().numpy().reshape(abi.NCONS, -1)),
+                                                 at, g[abi.PMU].copy())
+            ok = (fail_g.cpu().numpy() == 1.0) & (fail_o == 1.0)
+            dmu.append(np.abs(g[abi.PMU] - ph[abi.PMU])[ok])
+            cs = d["cell_sig"].cpu().numpy().reshape(3, -1)
+            av = np.abs(at[1]) + np.abs(at[2]) + np.abs(at[3])
+            c = np.maximum(np.maximum(np.abs(cs[0]), np.abs(cs[1])), np.abs(cs[2]))
+            aB = np.abs(at[5]) + np.abs(at[6]) + np.abs(at[7])
+            fl = {0: 0.0, 1: av + c, 2: av + c, 3: av + c, 4: 0.0, 8: 0.0, 5: aB, 6: aB, 7: aB}
             for n, v in PRIM_VARS.items():
-                den = np.abs(pz[v]) + fl[v].ravel()
+                den = np.abs(at[v]) + fl[v]
                 sel = ok & (den > 0)
-                fin[n].append(np.abs(g[v] - pz[v])[sel] / den[sel])
+                fin[n].append(np.abs(g[v] - at[v])[sel] / den[sel])
         dmu = np.concatenate(dmu)
         nbig = int((dmu > 2 * p.c2p_tol).sum())
-        print(f"[per-zone] config3 stage 1 mu: max |mu - mu_oracle| {dmu.max():.3e}, zones beyond 2 tol: {nbig} "
-              f"of {dmu.size}")
+        print(f"[per-zone] config3 stage-1 state, zone con2prim: max |mu - mu_oracle| {dmu.max():.3e}, zones beyond "
+              f"2 tol: {nbig} of {dmu.size}")
         for n in PRIM_VARS:
             e = np.nan_to_num(np.concatenate(fin[n]))
-            print(f"[per-zone] config3 stage 1 {n} against the reference finish at the GPU's root: max {e.max():.3e}, "
-                  f"99.99th pct {np.quantile(e, 0.9999):.3e}")
+            print(f"[per-zone] config3 stage-1 state {n} against the reference finish at the GPU's root: max "
+                  f"{e.max():.3e}, 99.99th pct {np.quantile(e, 0.9999):.3e}")
         assert nbig <= 1e-4 * dmu.size, nbig
         for n in PRIM_VARS:
             e = np.nan_to_num(np.concatenate(fin[n]))

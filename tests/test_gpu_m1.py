@@ -203,19 +203,20 @@ def test_rad_configuration_errors(rx):
     assert e.value.status == abi.PHX_ERR_INVALID_ARG
     import torch
 
-    with pytest.raises(abi.PhxError) as e:
-        rx.Stage(abi.default_rad_params(), abi.default_params(enable_floors=1), db, db["rcons"],
+    # the radiation floors need the fluid floors (the fixup package forces them on)
+    with pytest.raises(abi.PhxError, match="enable_rad_floors") as e:
+        rx.Stage(abi.default_rad_params(enable_rad_floors=1), abi.default_params(), db, db["rcons"],
                  torch.zeros_like(db["rcons"]), 1.0, 1e-3)
-    assert e.value.status == abi.PHX_ERR_UNSUPPORTED
+    assert e.value.status == abi.PHX_ERR_INVALID_ARG
     # the radiation-only stage refuses update_fluid (the fluid stage carries it)
     with pytest.raises(abi.PhxError, match="phx_rad_fluid_stage") as e:
         rx.Stage(abi.default_rad_params(update_fluid=1), p, db, db["rcons"], torch.zeros_like(db["rcons"]), 1.0,
                  1e-3)
     assert e.value.status == abi.PHX_ERR_INVALID_ARG
-    with pytest.raises(abi.PhxError) as e:
-        rx.FluidStage(abi.default_rad_params(), abi.default_params(enable_c2p_fixup=1), db, db["cons"],
+    with pytest.raises(abi.PhxError, match="enable_rad_floors") as e:
+        rx.FluidStage(abi.default_rad_params(enable_rad_floors=1), abi.default_params(), db, db["cons"],
                       torch.zeros_like(db["cons"]), db["rcons"], torch.zeros_like(db["rcons"]), 1.0, 1e-3)
-    assert e.value.status == abi.PHX_ERR_UNSUPPORTED
+    assert e.value.status == abi.PHX_ERR_INVALID_ARG
 
 
 @pytest.mark.parametrize("exact", [True, False])
@@ -349,3 +350,183 @@ def test_equilibration_exact_and_production(rx, rf, rad_oracle):
         assert err < 1e-8
     rx.check()
     rf.check()
+
+
+# ---- curved geometry: FMKS tables (the torus' Kerr-Schild metric, a = 0.9375)
+@pytest.mark.parametrize("method,recon,ndim", [("moment_m1", "linear", 2), ("moment_eddington", "weno5z", 2),
+                                               ("moment_m1", "mp5", 3), ("moment_eddington", "constant", 3)])
+def test_fmks_tasks_bitwise(rx, rad_oracle, method, recon, ndim):
+    """Every radiation task on an FMKS block (exact build) equals the oracle
+    bit for bit: prim2con and con2prim with the LocalThreeGeometry and
+    sqrt(gamma), fluxes with the face metric, lapse and shift, the update
+    with the geometric source (moments.cpp:764-885), the source step with
+    the lapse in the optical depths (both update_fluid settings), and the
+    timestep with the metric's signal speeds."""
+    import torch
+
+    from tests.util import random_rad_block_fmks
+
+    nx = {2: (20, 16, 1), 3: (12, 10, 8)}[ndim]
+    hb = random_rad_block_fmks(nx, ndim, seed=91 + ndim)
+    p = abi.default_params(Gamma=5.0 / 3.0, Cv=1.3)
+    P = hb["prim"]
+    P[abi.PPRS] = p.gm1 * P[abi.PENG]
+    P[abi.PGM1] = p.gm1 + 1.0
+    from oracle.oracle import Oracle
+
+    Oracle().PrimitiveToConserved(p, hb, *hb.entire())
+    db = hb.to_device()
+    rp = abi.default_rad_params(method=method, recon=recon, cfl=0.5, kappa_s=40.0, kappa_a=3.0, jbb_coeff=0.7)
+    for o, b in ((rad_oracle, hb), (rx, db)):
+        o.MomentPrim2Con(rp, p, b, *b.entire())
+    _cmp(db, hb, ["rcons"], "fmks prim2con")
+    for o, b in ((rad_oracle, hb), (rx, db)):
+        o.MomentCon2Prim(rp, p, b)
+    _cmp(db, hb, ["rcons", "rprim"], "fmks con2prim")
+    for o, b in ((rad_oracle, hb), (rx, db)):
+        o.MomentCalculateOpacities(rp, p, b)
+        o.CalculateFluxes(rp, p, b)
+    ks, js, is_ = hb.isl()
+    for d in range(ndim):
+        reg = (slice(ks.start, ks.stop + (d == 2)), slice(js.start, js.stop + (d == 1)),
+               slice(is_.start, is_.stop + (d == 0)))
+        g = host(db["rflux"])[4 * d:4 * d + 4][(slice(None),) + reg]
+        assert_bitwise(g, hb["rflux"][4 * d:4 * d + 4][(slice(None),) + reg], f"fmks fluxes d={d}")
+    base_h = hb["rcons"] * 1.01
+    out_h = np.zeros_like(base_h)
+    base_d = torch.from_numpy(base_h).cuda()
+    out_d = torch.zeros_like(base_d)
+    rad_oracle.Update(rp, hb, base_h, out_h, 0.5, 1.0e-3)
+    rx.Update(rp, db, base_d, out_d, 0.5, 1.0e-3)
+    assert_bitwise(host(out_d)[(slice(None), ks, js, is_)], out_h[(slice(None), ks, js, is_)], "fmks update out")
+    _cmp(db, hb, ["rcons", "rdudt"], "fmks update (geometric source)", (ks, js, is_))
+    src = rad_oracle.GeometricSource(rp, hb)
+    assert np.abs(src[0][ks, js, is_]).max() > 0  # the curved source is at work
+    for upd in (0, 1):
+        rpu = abi.default_rad_params(method=method, recon=recon, cfl=0.5, kappa_s=40.0, kappa_a=3.0,
+                                     jbb_coeff=0.7, update_fluid=upd)
+        for o, b in ((rad_oracle, hb), (rx, db)):
+            o.MomentFluidSource(rpu, p, b, 2.0e-3)
+        _cmp(db, hb, ["rcons", "rprim", "cons", "prim"], f"fmks fluid source update_fluid={upd}", (ks, js, is_))
+    assert rx.EstimateTimestepBlock(rp, p, db) == rad_oracle.EstimateTimestepBlock(rp, p, hb)
+    rx.check()
+
+
+@pytest.mark.parametrize("method", ["moment_m1", "moment_eddington"])
+def test_fmks_stages_bitwise(rx, rad_oracle, method):
+    """Two rk2 steps on an FMKS block (periodic ghosts), exact build, bit
+    for bit: the moment-only stage, then the coupled fluid + moment stage."""
+    import torch
+
+    from oracle.oracle import Oracle
+    from tests.util import random_rad_block_fmks
+
+    hb = random_rad_block_fmks((16, 12, 1), 2, seed=7, vmax=0.2)
+    p = abi.default_params(Gamma=5.0 / 3.0, Cv=1.0, recon="linear", riemann="hll", c2p_tol=1e-10, c2p_max_iter=100)
+    P = hb["prim"]
+    P[abi.PPRS] = p.gm1 * P[abi.PENG]
+    P[abi.PGM1] = p.gm1 + 1.0
+    Oracle().PrimitiveToConserved(p, hb, *hb.entire())
+    db = hb.to_device()
+    rp = abi.default_rad_params(method=method, recon="linear", cfl=0.5, kappa_s=10.0, kappa_a=2.0, jbb_coeff=0.4)
+    for o, b in ((rad_oracle, hb), (rx, db)):
+        o.MomentPrim2Con(rp, p, b, *b.entire())
+        o.Initialize(rp, p, b)
+    dt = 0.2 * min(hb.dx[d] for d in range(2))
+    rh, rd = np.zeros_like(hb["rcons"]), torch.zeros_like(db["rcons"])
+    fh, fd = np.zeros_like(hb["cons"]), torch.zeros_like(db["cons"])
+    rad_oracle.rk2_step(rp, p, hb, rh, dt)
+    rx.rk2_step(rp, p, db, rd, dt)
+    _cmp(db, hb, ["rcons", "rprim"], "fmks moment stage")
+    rad_oracle.rk2_fluid_step(rp, p, hb, fh, rh, dt)
+    rx.rk2_fluid_step(rp, p, db, fd, rd, dt)
+    _cmp(db, hb, ["prim", "cons", "rcons", "rprim"], "fmks coupled stage")
+    rx.check()
+
+
+# ---- the radiation parts of the fixups and floors
+@pytest.mark.parametrize("geometry", ["minkowski", "fmks"])
+@pytest.mark.parametrize("method", ["moment_m1", "moment_eddington"])
+def test_rad_fixup_and_floors_bitwise(rx, rad_oracle, method, geometry):
+    """RadConservedToPrimitiveFixup (zones marked failed, isolated and
+    adjacent, both strategies) and ApplyFloors with the radiation on (fluid
+    floors acting in some zones, the J floor and the xi ceiling acting in
+    others) equal the oracle bit for bit (exact build)."""
+    from oracle.oracle import Oracle
+    from tests.util import random_rad_block_fmks
+
+    nx = (16, 12, 1)
+    hb = random_rad_block(nx, 2, seed=29, vmax=0.3) if geometry == "minkowski" else \
+        random_rad_block_fmks(nx, 2, seed=29, vmax=0.3)
+    p = abi.default_params(Gamma=5.0 / 3.0, Cv=1.0)
+    P = hb["prim"]
+    P[abi.PPRS] = p.gm1 * P[abi.PENG]
+    P[abi.PGM1] = p.gm1 + 1.0
+    Oracle().PrimitiveToConserved(p, hb, *hb.entire())
+    rp = abi.default_rad_params(method=method)
+    rad_oracle.MomentPrim2Con(rp, p, hb, *hb.entire())
+    rad_oracle.MomentCon2Prim(rp, p, hb)
+    ks, js, is_ = hb.isl()
+    F = hb["rprim"][abi.RFAIL]
+    F[0, js.start + 2, is_.start + 3] = 0.0
+    F[0, js.start + 6, is_.start + 5:is_.start + 7] = 0.0
+    F[0, js.start, is_.start] = 0.0  # next to the ghosts
+    db = hb.to_device()
+    p.enable_c2p_fixup = 1
+    for strategy in (0, 1):
+        rp.rad_c2p_failure_floors = strategy
+        h2, d2 = hb.to_host(), hb.to_device()
+        rad_oracle.RadConservedToPrimitiveFixup(rp, p, h2)
+        rx.RadConservedToPrimitiveFixup(rp, p, d2)
+        _cmp(d2, h2, ["rprim", "rcons"], f"rad c2p fixup strategy {strategy}")
+    rp.rad_c2p_failure_floors = 0
+    p.enable_floors = 1
+    rho = hb["prim"][abi.PRHO]
+    p.rho0_floor, p.sie0_floor = float(np.quantile(rho, 0.1)), 1e-6  # some fluid floors act
+    rp.enable_rad_floors, rp.J0_floor = 1, float(np.quantile(hb["rprim"][abi.RJ], 0.3))
+    rp.enable_rad_ceilings, rp.xi0_ceiling = 1, 0.5
+    rad_oracle.ApplyFloors(rp, p, hb)
+    rx.ApplyFloors(rp, p, db)
+    _cmp(db, hb, ["prim", "cons", "rprim", "rcons"], "apply floors with radiation")
+    rx.check()
+
+
+@pytest.mark.parametrize("geometry", ["minkowski", "fmks"])
+def test_stages_with_fixups_and_floors_bitwise(rx, rad_oracle, geometry):
+    """The moment stage and the coupled fluid + moment stage with the c2p
+    fixups, the fluid floors and the radiation floors and ceilings on: two
+    rk2 steps of each equal the oracle bit for bit (exact build)."""
+    import torch
+
+    from oracle.oracle import Oracle
+    from tests.util import random_rad_block_fmks
+
+    nx = (16, 12, 1)
+    hb = random_rad_block(nx, 2, seed=37, vmax=0.2) if geometry == "minkowski" else \
+        random_rad_block_fmks(nx, 2, seed=37, vmax=0.2)
+    p = abi.default_params(Gamma=5.0 / 3.0, Cv=1.0, recon="linear", riemann="hll", c2p_tol=1e-10, c2p_max_iter=100)
+    P = hb["prim"]
+    P[abi.PPRS] = p.gm1 * P[abi.PENG]
+    P[abi.PGM1] = p.gm1 + 1.0
+    Oracle().PrimitiveToConserved(p, hb, *hb.entire())
+    p.enable_floors, p.enable_c2p_fixup, p.enable_ceilings = 1, 1, 1
+    p.rho0_floor, p.sie0_floor = float(np.quantile(P[abi.PRHO], 0.05)), 1e-6
+    rp = abi.default_rad_params(method="moment_m1", recon="linear", cfl=0.5, kappa_s=10.0, kappa_a=2.0, jbb_coeff=0.4)
+    rp.enable_rad_floors, rp.J0_floor = 1, float(np.quantile(hb["rprim"][abi.RJ], 0.1))
+    rp.enable_rad_ceilings, rp.xi0_ceiling, rp.tau0_ceiling = 1, 0.9, 1e3
+    db = hb.to_device()
+    for o, b in ((rad_oracle, hb), (rx, db)):
+        o.MomentPrim2Con(rp, p, b, *b.entire())
+        o.Initialize(rp, p, b)
+    dt = 0.2 * min(hb.dx[d] for d in range(2))
+    rh, rd = np.zeros_like(hb["rcons"]), torch.zeros_like(db["rcons"])
+    fh, fd = np.zeros_like(hb["cons"]), torch.zeros_like(db["cons"])
+    for step in range(2):
+        rad_oracle.rk2_step(rp, p, hb, rh, dt)
+        rx.rk2_step(rp, p, db, rd, dt)
+        _cmp(db, hb, ["prim", "cons", "rprim", "rcons"], f"moment stage with fixups, step {step}")
+    for step in range(2):
+        rad_oracle.rk2_fluid_step(rp, p, hb, fh, rh, dt)
+        rx.rk2_fluid_step(rp, p, db, fd, rd, dt)
+        _cmp(db, hb, ["prim", "cons", "fail", "rprim", "rcons"], f"coupled stage with fixups, step {step}")
+    rx.check()

@@ -1,6 +1,8 @@
 """Comparison helpers shared by the parity tests."""
 from __future__ import annotations
 
+import math
+
 import numpy as np
 
 
@@ -210,3 +212,30 @@ def max_rel_floor(got, ref, floor):
     if not ok.any():
         return 0.0
     return float(np.nanmax(np.abs(got[ok] - ref[ok]) / den[ok]))
+
+
+def random_rad_block_fmks(nx, ndim, seed, vmax=0.3, hmax=0.6, ng=4, x1=(math.log(4.0), math.log(40.0)),
+                          x2=(0.15, 0.85)):
+    """random_rad_block on an FMKS block (the torus geometry, a = 0.9375) of
+    X1 = ln r in x1, X2 in x2, X3 in [0, 2 pi) with the oracle's tables: the
+    fluid's W v^i scaled by 1 / sqrt(gamma_ii) and the radiation's covariant
+    H_i / J by sqrt(gamma_ii), so that |v| and xi keep the ranges of the
+    Minkowski helper."""
+    from oracle.oracle import Oracle
+    from phoebus_gb300 import abi, torus
+    from phoebus_gb300.block import Block, GeomTables
+
+    b = random_rad_block(nx, ndim, seed, vmax=vmax, hmax=hmax, ng=ng)
+    nxs = b.nx
+    lo = (x1[0], x2[0], 0.0)
+    hi = (x1[1], x2[1], 2 * math.pi)
+    dx = tuple((hi[d] - lo[d]) / nxs[d] if d < ndim else (1.0 if d == 1 else 2 * math.pi) for d in range(3))
+    fb = Block(b.nx, ng=ng, ndim=ndim, xmin=lo, dx=dx, backend="numpy", arrays=b.arrays)
+    fb.geom = GeomTables(torus.torus_geometry(), fb.n1t, fb.n2t, "numpy").alloc()
+    Oracle().GeometryFillFMKS(fb)
+    cent = fb.geom.arrays["cent"]
+    for d in range(3):
+        g_dd = cent[abi.G_GCOV + (d + 1) * (d + 2) // 2 + d + 1][None]
+        fb["prim"][abi.PVEL + d] /= np.sqrt(g_dd)
+        fb["rprim"][abi.RH + d] *= np.sqrt(g_dd)
+    return fb
