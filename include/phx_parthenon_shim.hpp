@@ -22,6 +22,8 @@
 //   template <T> TaskStatus radiation::CalculateFluxes(T *)              moments.cpp:724
 //   template <T> TaskStatus radiation::CalculateGeometricSource(T *, T *) moments.cpp:886
 //   template <T> TaskStatus radiation::MomentFluidSource(T *, Real, bool) moments_source.cpp:960
+//   TaskStatus fixup::RadConservedToPrimitiveFixup(MeshBlockData<Real> *) fixup_radc2p.cpp:227
+//   TaskStatus fixup::ApplyFloors(MeshBlockData<Real> *), radiation on    fixup.cpp:680
 //   Real radiation::EstimateTimestepBlock(MeshBlockData<Real> *)         radiation.cpp:585
 //   Real fluid::EstimateTimestepBlock(MeshBlockData<Real> *)             fluid.cpp:899
 //   template <T> using fluid::c2p_type = TaskStatus (*)(T *, ...)        fluid.hpp:65
@@ -395,5 +397,30 @@ inline Real EstimateTimestepBlock(MeshBlockData<Real> *rc) {
   return dt;
 }
 }  // namespace radiation
+
+namespace fixup {
+// fixup::RadConservedToPrimitiveFixup (fixup_radc2p.cpp:227): a no-op unless
+// fixup/enable_c2p_fixup.
+inline TaskStatus RadConservedToPrimitiveFixup(MeshBlockData<Real> *rc) {
+  parthenon::Mesh *m = rc->GetMeshPointer();
+  radiation::detail::check(
+      phx_rad_c2p_fixup(m->ctx, &m->rad_params, &m->params, &rc->Block(), &rc->RadBlock(), m->stream),
+      "RadConservedToPrimitiveFixup");
+  return TaskStatus::complete;
+}
+
+// fixup::ApplyFloors (fixup.cpp:680) with the radiation package active, over
+// the entire block: the fluid floors, then the radiation floors and ceilings.
+inline TaskStatus ApplyFloorsWithRadiation(MeshBlockData<Real> *rc) {
+  parthenon::Mesh *m = rc->GetMeshPointer();
+  const parthenon::IndexDomain e = parthenon::IndexDomain::entire;
+  radiation::detail::check(
+      phx_rad_apply_floors(m->ctx, &m->rad_params, &m->params, &rc->Block(), &rc->RadBlock(),
+                           radiation::detail::R(rc->GetBoundsI(e)), radiation::detail::R(rc->GetBoundsJ(e)),
+                           radiation::detail::R(rc->GetBoundsK(e)), m->stream),
+      "ApplyFloors");
+  return TaskStatus::complete;
+}
+}  // namespace fixup
 
 #endif  // PHX_PARTHENON_SHIM_HPP_

@@ -509,8 +509,9 @@ cudaError_t batch_stage(BatchCache *cache, const Par &par, const phx_block *bloc
     if ((e = upload_items(P, P.update, make_items(interior, 256))) != cudaSuccess) return e;
     if ((e = upload_items(P, P.ghost, make_items(all, 256))) != cudaSuccess) return e;
     if ((e = upload_items(P, P.c2p, make_items(all, 128))) != cudaSuccess) return e;
-    // learned brackets (3 planes) and each zone's warm / cold pass (plane 3)
-    if (mlp && (e = cudaMalloc(&P.brk, sizeof(double) * 4 * (size_t)P.c2p.n * 128)) != cudaSuccess) return e;
+    // learned brackets (3 planes), each zone's warm / cold pass (plane 3) and
+    // the count of cold zones (one word after)
+    if (mlp && (e = cudaMalloc(&P.brk, sizeof(double) * (4 * (size_t)P.c2p.n * 128 + 1))) != cudaSuccess) return e;
     if (mesh) {
       if ((e = upload_mesh(P, mesh, n)) != cudaSuccess) return e;
       std::vector<long long> fix;

@@ -527,11 +527,14 @@ void launch_mlp_bracket(const Par &p, long long n, const double *cons, const dou
 // (no iteration cap: the retry list is per chunk of one zone list).
 // Learned start of the batched con2prim: item it's zone first + tid gets
 // its bracket at brk[c * (nitems * C2P_THREADS) + it * C2P_THREADS + tid]
-// (c = 0, 1, 2) and in plane 3 its pass: 1.0 cold (no stored mu > 0: the
-// learned start), 0.0 warm (the plain start from the stored mu).  The passes
-// read plane 3, so each zone is inverted exactly once even when a warm
-// zone's new mu is not positive.  A warp none of whose cold zones has
-// features inside the network's input box skips the network.
+// (c = 0, 1, 2); plane 3 holds its pass (1.0 cold: no stored mu > 0, the
+// learned start; 0.0 warm: the plain start from the stored mu), written by
+// the warm pass, which runs first and counts the cold zones in the word after
+// plane 3.  This kernel and the cold pass return at once when that count is
+// zero (a running simulation has no cold zones), and each zone is inverted
+// exactly once even when a warm zone's new mu is not positive.  A warp none
+// of whose cold zones has features inside the network's input box skips the
+// network.
 template <bool MINK>
 __global__ void __launch_bounds__(C2P_THREADS) kb_mlp_bracket(Par p, const BView *views, const WorkItem *items,
                                                               int nitems, const MlpPacked *mlp, double *brk,
@@ -539,9 +542,10 @@ __global__ void __launch_bounds__(C2P_THREADS) kb_mlp_bracket(Par p, const BView
   extern __shared__ __align__(16) unsigned char kbb_dyn[];
   __shared__ __align__(8) uint64_t bar;
   BracketSmem *S = reinterpret_cast<BracketSmem *>(kbb_dyn);
+  const long long stride = (long long)nitems * C2P_THREADS;
+  if (*reinterpret_cast<const unsigned long long *>(brk + 4 * stride) == 0) return;  // no cold zone
   if (!mlp_stage_weights(&S->w, mlp, &bar, err)) return;
   const int warp = threadIdx.x >> 5;
-  const long long stride = (long long)nitems * C2P_THREADS;
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const WorkItem w = items[it];
     const BView &bv = views[w.block];
@@ -550,9 +554,7 @@ __global__ void __launch_bounds__(C2P_THREADS) kb_mlp_bracket(Par p, const BView
     const long long o = (long long)it * C2P_THREADS + threadIdx.x;
     float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     bool ok = false;
-    const bool valid = q < w.last;
-    const bool cold = valid && !(zones.guess_of(q) > 0.0);  // warm zones: stored mu only
-    if (valid) brk[3 * stride + o] = cold ? 1.0 : 0.0;
+    const bool cold = q < w.last && brk[3 * stride + o] == 1.0;
     if (cold) {
       long long id;
       Pt g{};
@@ -576,15 +578,17 @@ __global__ void __launch_bounds__(C2P_THREADS) kb_mlp_bracket(Par p, const BView
   }
 }
 
-// only: 0 every zone; 1 the warm zones alone; 2 the cold zones alone, as
-// kb_mlp_bracket classified them before either pass ran (plane 3 of brk).
-// With the learned start the plan runs the plain kernel over the warm zones
-// and the learned one over the cold zones, so warm zones (all of them once a
-// run is under way) go through exactly the plain kernel's code.
+// only: 0 every zone; 1 the warm zones alone (this pass classifies every
+// zone into plane 3 of brk and counts the cold ones); 2 the cold zones alone,
+// as the warm pass classified them.  With the learned start the plan runs the
+// plain kernel over the warm zones and the learned one over the cold zones,
+// so warm zones (all of them once a run is under way) go through exactly the
+// plain kernel's code.
 template <bool MINK, bool LEARNED>
 __global__ void __launch_bounds__(C2P_THREADS) kb_c2p(Par p, const BView *views, const WorkItem *items, int nitems,
-                                                       const double *brk, DevStats *stats, unsigned int *err,
-                                                       int only) {
+                                                       double *brk, DevStats *stats, unsigned int *err, int only) {
+  if (only == 2 && *reinterpret_cast<const unsigned long long *>(brk + 4 * (long long)nitems * C2P_THREADS) == 0)
+    return;  // no cold zone
   __shared__ unsigned int s_hist[PHX_C2P_HIST];
   __shared__ unsigned long long s_cnt[6];
   if (stats) {
@@ -598,9 +602,19 @@ __global__ void __launch_bounds__(C2P_THREADS) kb_c2p(Par p, const BView *views,
     const BoxZones zones{bv, Range3{0, bv.n1t - 1, 0, bv.n2t - 1, 0, bv.n3t - 1}};
     const long long q = w.first + threadIdx.x;
     bool valid = q < w.last;
-    if (only && valid)
-      valid = (brk[3 * (long long)nitems * C2P_THREADS + (long long)it * C2P_THREADS + threadIdx.x] == 1.0) ==
-              (only == 2);
+    if (only) {
+      const long long stride = (long long)nitems * C2P_THREADS, o = (long long)it * C2P_THREADS + threadIdx.x;
+      if (only == 1) {
+        const bool cold = valid && !(zones.guess_of(q) > 0.0);
+        if (valid) brk[3 * stride + o] = cold ? 1.0 : 0.0;
+        const unsigned m = __ballot_sync(0xffffffffu, cold);
+        if (m && (threadIdx.x & 31) == 0)
+          atomicAdd(reinterpret_cast<unsigned long long *>(brk + 4 * stride), (unsigned long long)__popc(m));
+        valid = valid && !cold;
+      } else {
+        valid = valid && brk[3 * stride + o] == 1.0;
+      }
+    }
     if (!__any_sync(0xffffffffu, valid)) continue;  // nothing for this warp in this pass
     long long id = 0;
     Pt g{};
@@ -642,10 +656,12 @@ static void c2p_batched_t(const Par &p, const BView *views, const WorkItem *item
                           const MlpPacked *mlp, double *brk, DevStats *stats, unsigned int *err, cudaStream_t s) {
   if (mlp) {
     static_assert(sizeof(BracketSmem) <= 48 * 1024, "no opt-in attribute needed (launches may be captured)");
-    kb_mlp_bracket<MINK><<<persistent_grid(kb_mlp_bracket<MINK>, C2P_THREADS, sizeof(BracketSmem), nitems, 0),
-                           C2P_THREADS, sizeof(BracketSmem), s>>>(p, views, items, nitems, mlp, brk, err);
+    // warm pass (classifies and counts), bracket kernel, cold pass
+    cudaMemsetAsync(brk + 4 * (long long)nitems * C2P_THREADS, 0, sizeof(unsigned long long), s);
     kb_c2p<MINK, false><<<persistent_grid(kb_c2p<MINK, false>, C2P_THREADS, 0, nitems, grid), C2P_THREADS, 0, s>>>(
         p, views, items, nitems, brk, stats, err, 1);
+    kb_mlp_bracket<MINK><<<persistent_grid(kb_mlp_bracket<MINK>, C2P_THREADS, sizeof(BracketSmem), nitems, 0),
+                           C2P_THREADS, sizeof(BracketSmem), s>>>(p, views, items, nitems, mlp, brk, err);
     kb_c2p<MINK, true><<<persistent_grid(kb_c2p<MINK, true>, C2P_THREADS, 0, nitems, grid), C2P_THREADS, 0, s>>>(
         p, views, items, nitems, brk, stats, err, 2);
   } else {

@@ -154,8 +154,8 @@ void launch_fluxct_batched(int ndim, const BView *views, const WorkItem *items, 
 void launch_update_batched(const Par &p, const BView *views, const double *const *base, double *const *out,
                            const double *beta_dt, const WorkItem *items, int nitems, int grid, cudaStream_t s);
 void launch_ghost_batched(const BView *views, int nvar, const WorkItem *items, int nitems, int grid, cudaStream_t s);
-// mlp non-null: the learned start; brk holds 4 x nitems x 128 doubles (the
-// brackets and each zone's warm / cold pass).
+// mlp non-null: the learned start; brk holds 4 x nitems x 128 + 1 doubles
+// (the brackets, each zone's warm / cold pass, the cold-zone count).
 void launch_c2p_batched(const Par &p, bool mink, const BView *views, const WorkItem *items, int nitems, int grid,
                         const MlpPacked *mlp, double *brk, DevStats *stats, unsigned int *err, cudaStream_t s);
 // bc_vars = conserved, outer-X1 inflow check (FMKS): con2prim, u^1 >= 0 and

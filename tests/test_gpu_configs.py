@@ -355,7 +355,14 @@ def test_config3_batched_vs_oracle(oracle, ctx_exact, ctx_fast, exact):
             av = np.abs(at[1]) + np.abs(at[2]) + np.abs(at[3])
             c = np.maximum(np.maximum(np.abs(cs[0]), np.abs(cs[1])), np.abs(cs[2]))
             aB = np.abs(at[5]) + np.abs(at[6]) + np.abs(at[7])
-            fl = {0: 0.0, 1: av + c, 2: av + c, 3: av + c, 4: 0.0, 8: 0.0, 5: aB, 6: aB, 7: aB}
+            # u (and P = (Gamma - 1) u) comes out of the finish as the
+            # difference of the zone's energy terms: its rounding is relative
+            # to rho times the specific energy scale of the conserved state
+            # (|tau| + |S| + B^2) / D, not to u itself
+            U = np.ascontiguousarray(dd.cpu().numpy().reshape(abi.NCONS, -1))
+            escale = np.abs(at[0]) * (np.abs(U[4]) + np.abs(U[1]) + np.abs(U[2]) + np.abs(U[3]) +
+                                      U[5] ** 2 + U[6] ** 2 + U[7] ** 2) / np.abs(U[0])
+            fl = {0: 0.0, 1: av + c, 2: av + c, 3: av + c, 4: escale, 8: p.gm1 * escale, 5: aB, 6: aB, 7: aB}
             for n, v in PRIM_VARS.items():
                 den = np.abs(at[v]) + fl[v]
                 sel = ok & (den > 0)
