@@ -115,7 +115,7 @@ struct Residual {
     const double ahat = div_p(Phat, make_positive(hhat - Phat));
     const double nua = (1.0 + ahat) * (1.0 + ehat) * iWhat;
     const double nub = (1.0 + ahat) * (1.0 + qbar - mu * rbarsq);
-    const double nuhat = fmax(nua, nub);
+    const double nuhat = rmax(nua, nub);
     const double muhat = rcp_p(nuhat + mu * rbarsq);
     return mu - muhat;
   }
@@ -187,9 +187,9 @@ __device__ __forceinline__ bool c2p_setup(const Par &p, const Pt &g, const doubl
 #pragma unroll
     for (int ii = 0; ii < 3; ii++) Bprim[ii] = U[PHX_CB + ii] * igdet;
 #ifdef PHX_EXACT
-    const double sD = rcp_p(sqrt(fmax(D, rhoflr)));
+    const double sD = rcp_p(sqrt(rmax(D, rhoflr)));
 #else
-    const double sD = rsqrt_p(fmax(D, rhoflr));
+    const double sD = rsqrt_p(rmax(D, rhoflr));
 #endif
 #pragma unroll
     for (int ii = 0; ii < 3; ii++) {
@@ -203,9 +203,9 @@ __device__ __forceinline__ bool c2p_setup(const Par &p, const Pt &g, const doubl
   }
   const double zsq = rsq / 1.0;  // h0sq_ = 1
 #ifdef PHX_EXACT
-  const double v0sq = fmin(div_p(zsq, 1.0 + zsq), 1.0 - rcp_p(gam_max * gam_max));
+  const double v0sq = rmin(div_p(zsq, 1.0 + zsq), 1.0 - rcp_p(gam_max * gam_max));
 #else
-  const double v0sq = fmin(div_p(zsq, 1.0 + zsq), p.vsq_max);  // 1 - 1 / gam_max^2, formed on the host
+  const double v0sq = rmin(div_p(zsq, 1.0 + zsq), p.vsq_max);  // 1 - 1 / gam_max^2, formed on the host
 #endif
   res.D = D;
   res.q = q;

@@ -23,9 +23,28 @@ constexpr double kSMALL = 10 * 2.2250738585072014e-308;  // 10 * DBL_MIN
 constexpr double kEPS = 10 * 2.220446049250313e-16;      // 10 * DBL_EPSILON
 constexpr double kDBLMAX = 1.7976931348623157e308;
 
-__device__ __forceinline__ double make_positive(double v) { return fmax(v, kEPS); }
+// std::max / std::min as the reference calls them: the first argument comes
+// back when the comparison is false, so a NaN there propagates (fmax / fmin
+// would drop it).  The exact build keeps that for bit-for-bit parity on
+// every input, NaN states included; the production build uses the one-
+// instruction fmax / fmin (the two differ only where an argument is NaN).
+__device__ __forceinline__ double rmax(double a, double b) {
+#ifdef PHX_EXACT
+  return (a < b) ? b : a;
+#else
+  return fmax(a, b);
+#endif
+}
+__device__ __forceinline__ double rmin(double a, double b) {
+#ifdef PHX_EXACT
+  return (b < a) ? b : a;
+#else
+  return fmin(a, b);
+#endif
+}
+__device__ __forceinline__ double make_positive(double v) { return rmax(v, kEPS); }
 __device__ __forceinline__ double make_bounded(double v, double vmin, double vmax) {
-  return fmin(fmax(v, vmin + kEPS), vmax * (1.0 - kEPS));
+  return rmin(rmax(v, vmin + kEPS), vmax * (1.0 - kEPS));
 }
 __device__ __forceinline__ double ratio(double a, double b) {
   const double sgn = b >= 0 ? 1.0 : -1.0;
@@ -189,13 +208,13 @@ __device__ __forceinline__ FloorPt floor_point(const Par &p, double x1, double x
 __device__ __forceinline__ bool floors_x1_only(const Par &p) { return p.floor_type != PHX_FLOOR_R_RHO_SIE; }
 __device__ __forceinline__ void floors_from(const Par &p, const FloorPt &f, double &rflr, double &sflr) {
   if (p.floor_type == PHX_FLOOR_EXPX1_RHO_U) {
-    sflr = f.s / fmax(rflr, f.r);
+    sflr = f.s / rmax(rflr, f.r);
   } else {
     sflr = f.s;
   }
   rflr = f.r;
-  rflr = fmax(rflr, p.rho_min_eos);
-  sflr = fmax(sflr, p.sie_min_eos);
+  rflr = rmax(rflr, p.rho_min_eos);
+  sflr = rmax(sflr, p.sie_min_eos);
 }
 __device__ __forceinline__ void get_floors(const Par &p, double x1, double x2, double x3,
                                            double &rflr, double &sflr) {
@@ -358,7 +377,7 @@ __device__ __forceinline__ void signal_speeds(double rho, double u, double p, do
       vp -= g.beta[m];
       vm -= g.beta[m];
     }
-    sig[m] = fmax(fabs(vp), fabs(vm));
+    sig[m] = rmax(fabs(vp), fabs(vm));
   }
 }
 
@@ -652,7 +671,7 @@ __device__ __forceinline__ void prim_to_flux(const Par &par, const Face &f, cons
   double rho_floor = q[PHX_PRHO];
   double sie_floor;
   floors_from(par, f.fl, rho_floor, sie_floor);
-  const double rho = fmax(q[PHX_PRHO], rho_floor);
+  const double rho = rmax(q[PHX_PRHO], rho_floor);
   double vpcon[3] = {q[PHX_PVEL], q[PHX_PVEL + 1], q[PHX_PVEL + 2]};
 #ifdef PHX_EXACT
   double W = lorentz<MINK>(g, vpcon);
@@ -687,7 +706,7 @@ __device__ __forceinline__ void prim_to_flux(const Par &par, const Face &f, cons
 #endif
   double Bcon[3] = {0.0, 0.0, 0.0};
   const double u = (above_floor ? (above_max ? rho * sie_max : qe) : rho * sie_floor);
-  const double P = fmax(q[PHX_PPRS], 0.0);
+  const double P = rmax(q[PHX_PPRS], 0.0);
   const double gamma1 = q[PHX_PGM1];
   if (par.mhd) {
     Bcon[0] = q[PHX_PB];

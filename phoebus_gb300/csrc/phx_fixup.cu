@@ -50,8 +50,8 @@ __device__ __forceinline__ void c2p_fixup_at(const Par &p, const BView &b, long 
     rho = fixv(PHX_PRHO, norm);
     for (int d = 0; d < 3; d++) vp[d] = fixv(PHX_PVEL + d, norm);
     u = fixv(PHX_PENG, norm);
-    rho = fmax(rho, 100. * kSMALL);
-    u = fmax(u, 100. * kSMALL);
+    rho = rmax(rho, 100. * kSMALL);
+    u = rmax(u, 100. * kSMALL);
   } else {
     rho = 100. * kSMALL;
     u = 100. * kSMALL;
@@ -160,16 +160,16 @@ __device__ __forceinline__ void floors_at(const Par &p, const BView &b, const Ra
       const double alpha = MINK ? 1.0 : g.alpha;
       const double bcon0 = div_p(W * Bdotv, alpha);
       const double bsq = (Bsq + alpha * alpha * bcon0 * bcon0) * iW * iW;
-      rho_floor_max = fmax(rho_floor_max, div_p(bsq, p.bsqorho0));
-      u_floor_max = fmax(u_floor_max, div_p(bsq, p.bsqou0));
-      rho_floor_max = fmax(rho_floor_max, div_p(fmax(pr[PHX_PENG], u_floor_max), e_max));
+      rho_floor_max = rmax(rho_floor_max, div_p(bsq, p.bsqorho0));
+      u_floor_max = rmax(u_floor_max, div_p(bsq, p.bsqou0));
+      rho_floor_max = rmax(rho_floor_max, div_p(rmax(pr[PHX_PENG], u_floor_max), e_max));
     }
     drho = rho_floor_max - pr[PHX_PRHO];
     du = u_floor_max - pr[PHX_PENG];
     if (drho > 0. || du > 0.) {
       floor_applied = true;
-      drho = fmax(drho, du / sie_floor);
-      du = fmax(du, sie_floor * drho);
+      drho = rmax(drho, du / sie_floor);
+      du = rmax(du, sie_floor * drho);
     }
     if (p.mhd)
       for (int d = 0; d < 3; d++) bp[d] = pr[PHX_PB + d];

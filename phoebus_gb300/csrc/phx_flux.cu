@@ -53,14 +53,14 @@ __device__ __forceinline__ void face_flux(const Par &p, const BView &b, int k, i
   const int ncons = p.mhd ? PHX_NCONS : 5;
   double sig;
   if (p.riemann == PHX_RIEMANN_LLF) {
-    const double cmax = fmax(fmax(-vml, vpl), fmax(-vmr, vpr));
+    const double cmax = rmax(rmax(-vml, vpl), rmax(-vmr, vpr));
 #pragma unroll
     for (int m = 0; m < PHX_NCONS; m++)
       if (m < ncons) fx[m * b.vs] = 0.5 * ((Fl[m] + Fr[m]) * gdet - cmax * ((Ur[m] - Ul[m]) * gammadet));
     sig = cmax;
   } else {
-    const double cl = fmin(fmin(vml, vmr), 0.0);
-    const double cr = fmax(fmax(vpl, vpr), 0.0);
+    const double cl = rmin(rmin(vml, vmr), 0.0);
+    const double cr = rmax(rmax(vpl, vpr), 0.0);
     const double crcl = cr * cl;
     const double inv_cr_cl = ratio_p(1.0, cr - cl);
 #ifdef PHX_EXACT
@@ -75,7 +75,7 @@ __device__ __forceinline__ void face_flux(const Par &p, const BView &b, int k, i
     for (int m = 0; m < PHX_NCONS; m++)
       if (m < ncons) fx[m * b.vs] = fma(crg, Fl[m], fma(-clg, Fr[m], cc * (Ur[m] - Ul[m])));
 #endif
-    sig = fmax(-cl, cr);
+    sig = rmax(-cl, cr);
   }
   b.face_sig[(long long)DIR * b.vs + id] = sig;
 }

@@ -121,8 +121,10 @@ def test_rk2_steps_bitwise(rx, rad_oracle, method, ndim):
 
 
 BRANCHES = [
+    # the radiation floors force the fluid floors on (fixup.cpp:130-134), so
+    # ApplyFloors runs with its radiation part
     dict(rad=dict(enable_rad_floors=1, J0_floor=0.05, enable_rad_ceilings=1, xi0_ceiling=0.3, tau0_ceiling=0.5),
-         fluid=dict(enable_ceilings=1, gam0_ceiling=1.05)),
+         fluid=dict(enable_ceilings=1, gam0_ceiling=1.05, enable_floors=1)),
     dict(rad=dict(closure_frail=1, oned_fixup_strategy="ignore_all"), fluid={}),
     dict(rad=dict(oned_fixup_strategy="ignore_dJ", recon_fixup_bounds=0), fluid={}),
     dict(rad=dict(method="moment_eddington", oned_fixup_strategy="ignore_dJ", enable_rad_ceilings=1,
