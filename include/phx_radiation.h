@@ -177,10 +177,12 @@ phx_status phx_rad_apply_floors(phx_ctx *ctx, const phx_rad_params *rp, const ph
 /* One RK stage of the moment transport on a periodic block, in the task
  * order of PhoebusDriver::RungeKuttaStage with hydro off
  * (phoebus_driver.cpp:349-362, 547-620, 640-668): opacities, fluxes,
- * update into out, FillDerived (con2prim over the entire block),
- * RadConservedToPrimitiveFixup, ApplyFloors, fluid source (beta dt),
- * ApplyFloors, ghost exchange, FillDerived, the fixup and the floors
- * again (the fixups and floors as p / rp enable them).  rb->cons is the stage input (the reference's sc0), base the
+ * update into out, FillDerived (con2prim over the entire block; over the
+ * interior when the c2p fixup is off, since nothing reads the ghosts'
+ * inversion before the exchange rewrites them), RadConservedToPrimitiveFixup,
+ * ApplyFloors, fluid source (beta dt), ApplyFloors, ghost exchange,
+ * FillDerived, the fixup and the floors again (the fixups and floors as
+ * p / rp enable them).  rb->cons is the stage input (the reference's sc0), base the
  * step's initial state, out the stage output (sc1); everything after the
  * update acts on out and the shared prim fields. */
 phx_status phx_rad_stage(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_block *fb,

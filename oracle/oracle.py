@@ -409,16 +409,19 @@ class RadOracle:
         cons_in = b.arrays["rcons"]
         b.arrays["rcons"] = out
 
-        def derived():  # FillDerived (hydro off: the moments alone), the fixup, the floors
-            self.MomentCon2Prim(rp, p, b)
+        def derived(first):  # FillDerived (hydro off: the moments alone), the fixup, the floors
+            if first and not p.enable_c2p_fixup:  # the ghosts' inversion is overwritten unread
+                self.MomentCon2Prim(rp, p, b, *b.interior())
+            else:
+                self.MomentCon2Prim(rp, p, b)
             self.RadConservedToPrimitiveFixup(rp, p, b)
             self.ApplyFloors(rp, p, b)
 
-        derived()
+        derived(True)
         self.MomentFluidSource(rp, p, b, beta * dt)
         self.ApplyFloors(rp, p, b)
         self.FillGhostsPeriodic(b)
-        derived()
+        derived(False)
         b.arrays["rcons"] = cons_in
 
     def rk2_step(self, rp, p, b: Block, stage_buf, dt):

@@ -1256,17 +1256,20 @@ phx_status phx_rad_stage(phx_ctx *ctx, const phx_rad_params *rp, const phx_param
   phx::rad::launch_update(par, v, r, base, out, beta, dt, st);
   phx::rad::RView ro = r;
   ro.cons = out;
-  // hydro off: the fluid's con2prim and its c2p fixup do not run
-  auto derived = [&] {
-    phx::rad::launch_c2p(par, v, ro, entire(v), st);                      // FillDerived
+  // hydro off: the fluid's con2prim and its c2p fixup do not run.  Before
+  // the exchange only the c2p fixup reads the ghosts' inversion (the
+  // exchange overwrites every radiation field there), so without the fixup
+  // the first inversion covers the interior alone.
+  auto derived = [&](bool first) {
+    phx::rad::launch_c2p(par, v, ro, first && !p->enable_c2p_fixup ? interior(v) : entire(v), st);  // FillDerived
     if (p->enable_c2p_fixup) phx::rad::launch_rad_c2p_fixup(par, v, ro, st);  // RadConservedToPrimitiveFixup
-    rad_apply_floors(ctx, fpar, par, *rp, v, ro, entire(v), st);           // ApplyFloors
+    rad_apply_floors(ctx, fpar, par, *rp, v, ro, entire(v), st);               // ApplyFloors
   };
-  derived();
+  derived(true);
   phx::rad::launch_source(par, source_inversion_par(*p), v, ro, beta * dt, st);
   rad_apply_floors(ctx, fpar, par, *rp, v, ro, entire(v), st);
   phx::rad::launch_ghosts(v, ro, st);
-  derived();
+  derived(false);
   return cuda_status("phx_rad_stage");
 }
 
