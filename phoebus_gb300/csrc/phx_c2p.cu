@@ -204,21 +204,25 @@ struct ListZones {
 
 // The learned start of zones t0 .. t0 + count - 1 into brk[3][count]
 // (NaN where the setup rejects the zone).  CTAs stage the packed weights
-// once and walk chunks of 128 zones; each warp runs the network for its 32.
+// once and walk chunks of 128 zones, one tensor-core tile per chunk.
 struct BracketSmem {
   MlpPacked w;
-  uint32_t xs[C2P_WARPS][128];
-  float os[C2P_WARPS][64];
+  MlpTile tile;
 };
+static_assert(C2P_THREADS == 128, "one network tile row per thread");
+// more than 1/9 of an SM's shared memory: at most 8 CTAs resident, whose TMEM
+// columns (8 x 64) fit the SM's 512, so tcgen05.alloc never waits on another CTA
+static_assert(sizeof(BracketSmem) * 9 > 228 * 1024, "TMEM columns of the resident CTAs");
 
 template <class Z, bool MINK>
 __global__ void __launch_bounds__(C2P_THREADS) k_mlp_bracket(Par p, Z zones, long long t0, long long count,
                                                              const MlpPacked *mlp, double *brk, unsigned int *err) {
-  extern __shared__ __align__(16) unsigned char brk_dyn[];
+  extern __shared__ __align__(128) unsigned char brk_dyn[];
   __shared__ __align__(8) uint64_t bar;
   BracketSmem *S = reinterpret_cast<BracketSmem *>(brk_dyn);
   if (!mlp_stage_weights(&S->w, mlp, &bar, err)) return;
-  const int warp = threadIdx.x >> 5;
+  mlp_tc_init(&S->tile);
+  unsigned phase = 0;
   for (long long base = (long long)blockIdx.x * C2P_THREADS; base < count;
        base += (long long)gridDim.x * C2P_THREADS) {
     const long long q = base + threadIdx.x;
@@ -234,9 +238,9 @@ __global__ void __launch_bounds__(C2P_THREADS) k_mlp_bracket(Par p, Z zones, lon
       zones.template load<MINK>(t0 + q, id, g, U, x1, x2, x3, guess);
       ok = c2p_features_fp32<MINK>(p, g, U, x1, x2, x3, f) && mlp_in_box(S->w, f);
     }
-    if (!__any_sync(0xffffffffu, cold)) continue;  // whole warp warm: no network
+    if (!__syncthreads_or(cold)) continue;  // whole chunk warm: no network
     float o0, o1;
-    mlp_warp_forward(S->w, f, S->xs[warp], S->os[warp], o0, o1);
+    if (!mlp_cta_forward(S->w, &S->tile, f, phase, err, o0, o1)) break;
     if (cold) {
       double lb[3];
       mlp_bracket(o0, o1, lb);
@@ -244,6 +248,7 @@ __global__ void __launch_bounds__(C2P_THREADS) k_mlp_bracket(Par p, Z zones, lon
       for (int c = 0; c < 3; c++) brk[c * count + q] = ok ? lb[c] : nan;
     }
   }
+  mlp_tc_finish(&S->tile);
 }
 
 // Per-zone statistics into the block's shared counters.
@@ -532,20 +537,21 @@ void launch_mlp_bracket(const Par &p, long long n, const double *cons, const dou
 // the warm pass, which runs first and counts the cold zones in the word after
 // plane 3.  This kernel and the cold pass return at once when that count is
 // zero (a running simulation has no cold zones), and each zone is inverted
-// exactly once even when a warm zone's new mu is not positive.  A warp none
-// of whose cold zones has features inside the network's input box skips the
-// network.
+// exactly once even when a warm zone's new mu is not positive.  A 128-zone
+// tile none of whose cold zones has features inside the network's input box
+// skips the network.
 template <bool MINK>
 __global__ void __launch_bounds__(C2P_THREADS) kb_mlp_bracket(Par p, const BView *views, const WorkItem *items,
                                                               int nitems, const MlpPacked *mlp, double *brk,
                                                               unsigned int *err) {
-  extern __shared__ __align__(16) unsigned char kbb_dyn[];
+  extern __shared__ __align__(128) unsigned char kbb_dyn[];
   __shared__ __align__(8) uint64_t bar;
   BracketSmem *S = reinterpret_cast<BracketSmem *>(kbb_dyn);
   const long long stride = (long long)nitems * C2P_THREADS;
   if (*reinterpret_cast<const unsigned long long *>(brk + 4 * stride) == 0) return;  // no cold zone
   if (!mlp_stage_weights(&S->w, mlp, &bar, err)) return;
-  const int warp = threadIdx.x >> 5;
+  mlp_tc_init(&S->tile);
+  unsigned phase = 0;
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const WorkItem w = items[it];
     const BView &bv = views[w.block];
@@ -563,19 +569,20 @@ __global__ void __launch_bounds__(C2P_THREADS) kb_mlp_bracket(Par p, const BView
       ok = c2p_features_fp32<MINK>(p, g, U, x1, x2, x3, f) && mlp_in_box(S->w, f);
     }
     const double nan = __longlong_as_double(0x7ff8000000000000ll);
-    if (!__any_sync(0xffffffffu, ok)) {  // no usable start in this warp: no network
+    if (!__syncthreads_or(ok)) {  // no usable start in this tile: no network
       if (cold)
         for (int c = 0; c < 3; c++) brk[c * stride + o] = nan;
       continue;
     }
     float o0, o1;
-    mlp_warp_forward(S->w, f, S->xs[warp], S->os[warp], o0, o1);
+    if (!mlp_cta_forward(S->w, &S->tile, f, phase, err, o0, o1)) break;
     if (cold) {
       double lb[3];
       mlp_bracket(o0, o1, lb);
       for (int c = 0; c < 3; c++) brk[c * stride + o] = ok ? lb[c] : nan;
     }
   }
+  mlp_tc_finish(&S->tile);
 }
 
 // only: 0 every zone; 1 the warm zones alone (this pass classifies every

@@ -112,6 +112,10 @@ struct Residual {
 #endif
     const double Phat = eos_P_rho_sie(p, rhohat, ehat);
     const double hhat = rhohat * (1.0 + ehat) + Phat;
+    // Both builds keep the reference's two reciprocals: muhat = 1 / (nuhat +
+    // mu rbarsq) with nuhat >= 1 stays <= 1 under rounding, so f(1) >= 0 holds
+    // where the root sits at the end of [0, 1] (cold gas); a single merged
+    // reciprocal den / (c M + ...) loses that and can leave the root unbracketed.
     const double ahat = div_p(Phat, make_positive(hhat - Phat));
     const double nua = (1.0 + ahat) * (1.0 + ehat) * iWhat;
     const double nub = (1.0 + ahat) * (1.0 + qbar - mu * rbarsq);

@@ -51,15 +51,17 @@ __device__ __forceinline__ double ratio(double a, double b) {
   return a / (b + sgn * kSMALL);
 }
 
-// 1/x from the hardware reciprocal seed and two Newton steps (accurate to an
-// ulp or two for normal x; callers guarantee a normal, finite argument).
+// 1/x from the hardware reciprocal seed r and one third-order step
+// r (1 + e + e^2), e = 1 - x r: the relative error goes from e to e^3 (the
+// seed's e is below 2^-19.9 over the normal range, so e^3 is below 2^-59),
+// three FP64 instructions where two Newton steps take four.  Within an ulp of
+// the correctly rounded 1/x (2^28 random normal x: 0.03% one ulp off, none
+// more); callers guarantee a normal, finite argument.
 __device__ __forceinline__ double rcp_nr(double x) {
   double r;
   asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
-  double e = fma(-x, r, 1.0);
-  r = fma(r, e, r);
-  e = fma(-x, r, 1.0);
-  return fma(r, e, r);
+  const double e = fma(-x, r, 1.0);
+  return fma(r, fma(e, e, e), r);
 }
 // biased exponent of a double, on the integer pipe
 __device__ __forceinline__ int dexp(double x) { return (__double2hiint(x) >> 20) & 0x7ff; }
@@ -82,16 +84,18 @@ __device__ __forceinline__ double div_p(double a, double b) {
   return a * rcp_p(b);
 #endif
 }
-// 1/sqrt(x) from the hardware seed and two Newton steps y <- y (3 - x y^2)/2
-// (normal, finite x > 0); the production build's replacement for
-// 1 / sqrt(x), the exact build divides.
+// 1/sqrt(x) from the hardware seed y and one third-order step: with
+// h = 1 - x y^2, (1 - h)^(-1/2) = 1 + h/2 + 3h^2/8 + O(h^3), so
+// y (1 + h (1/2 + 3h/8)) cuts the relative error from h/2 (the seed's, below
+// 2^-20) to about 5h^3/16 (normal, finite x > 0); five FP64 instructions where
+// two Newton steps take eight.  Within two ulps of 1.0 / sqrt(x) over 2^28
+// random normal x.  The production build's replacement for 1 / sqrt(x); the
+// exact build divides.
 __device__ __forceinline__ double rsqrt_nr(double x) {
   double y;
   asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-  double h = x * y * y;
-  y = y * fma(-0.5, h, 1.5);
-  h = x * y * y;
-  return y * fma(-0.5, h, 1.5);
+  const double h = fma(-(x * y), y, 1.0);
+  return fma(y * h, fma(0.375, h, 0.5), y);
 }
 __device__ __forceinline__ double rsqrt_p(double x) {
 #ifdef PHX_EXACT
@@ -520,13 +524,28 @@ __device__ __forceinline__ void recon_weno5z(double q0, double q1, double q2, do
   qr = alpha_lin * qr + (1.0 - alpha_lin) * (q2 - 0.5 * dq);
 }
 // ---- production-build WENO5-Z: same mathematics, fewer FP64 instructions.
-// WENO5-Z as reconstruction.hpp:127-183, rearranged: the nonlinear weights
-// are gamma_k (1 + tau5 / beta_k), normalised by their sum; the three 1/beta_k
-// come from one reciprocal of beta0 beta1 beta2, the two weight sums and the
-// two denominators of alpha_l, alpha_r (on normalised weights) from one
-// reciprocal each.  Four reciprocals instead of eight divisions.  Every
-// intermediate stays in the normal range for |q| < 1e50; outside it (checked
-// on the exponents) the reference sequence is used.
+// WENO5-Z as reconstruction.hpp:127-183, rearranged.
+//  - The nonlinear weights are gamma_k bp_k, bp_k = 1 + tau5 / beta_k,
+//    normalised by their sums S_l, S_r; the three 1/beta_k come from one
+//    reciprocal of beta0 beta1 beta2.  (The reference's + eps on a weight is
+//    below half an ulp of gamma_k bp_k >= 0.1 and drops out.)
+//  - The blend factor: with normalised weights w_k = gamma_k bp_k / S,
+//    alpha = 3 w0 w1 w2 / (g2 w0 w1 + g1 w0 w2 + g0 w1 w2) = 3 / (S R) with
+//    R = sum_k 1/bp_k, the same for both faces, so the harmonic mean
+//    alpha_lin = 2 alpha_l alpha_r / (alpha_l + alpha_r) = 6 / (R (S_l + S_r)).
+//    1/bp_k = beta_k / (beta_k + tau5): with M the larger of beta0, beta2 and
+//    m the smaller, beta_m + tau5 = beta_M, so 1/bp_m = beta_m / beta_M from
+//    the reciprocal above, and 1/bp_M, 1/bp_1 share one reciprocal of
+//    (2 beta_M - beta_m)(beta1 + tau5).  (The reference's + eps on alpha_l,
+//    alpha_r moves alpha_lin only where alpha_lin < 1e-90.)
+//  - The MC slope of the blend, mc(q2 - q1, q3 - q2, 2), doubled, on the
+//    integer pipe: the sign test, the minima of magnitudes and the power-of-two
+//    scale act on the bit patterns; the sum dm + dp is the slope b1 = q3 - q1
+//    the smoothness indicator already forms.
+// Four reciprocals (three FP64 instructions each) and about 90 FP64
+// instructions for both face states.  Every intermediate stays in the normal
+// range for |q| < 1e50; outside it (checked on the exponents) the reference
+// sequence is used.
 __device__ __forceinline__ void recon_weno5z_fast(double q0, double q1, double q2, double q3, double q4,
                                                   double &ql, double &qr) {
   constexpr double g0 = 0.1, g1 = 0.6, g2 = 0.3;
@@ -540,7 +559,8 @@ __device__ __forceinline__ void recon_weno5z_fast(double q0, double q1, double q
   const double beta0 = fma(t13 * a0, a0, fma(b0, b0, eps));
   const double beta1 = fma(t13 * a1, a1, fma(b1, b1, eps));
   const double beta2 = fma(t13 * a2, a2, fma(b2, b2, eps));
-  const double tau5 = fabs(beta2 - beta0);
+  const double d20 = beta2 - beta0;
+  const double tau5 = fabs(d20);
   const double b01 = beta0 * beta1;
   const double prod = b01 * beta2;
   const int ep = dexp(prod);
@@ -550,49 +570,46 @@ __device__ __forceinline__ void recon_weno5z_fast(double q0, double q1, double q
   }
   const double rp = rcp_nr(prod);
   const double t = beta2 * rp;
-  const double bp0 = fma(tau5, beta1 * t, 1.0);
+  const double ib0 = beta1 * t, ib2 = b01 * rp;  // 1/beta0, 1/beta2
+  const double bp0 = fma(tau5, ib0, 1.0);
   const double bp1 = fma(tau5, beta0 * t, 1.0);
-  const double bp2 = fma(tau5, b01 * rp, 1.0);
-  double wl0 = fma(g0, bp0, eps), wl1 = fma(g1, bp1, eps), wl2 = fma(g2, bp2, eps);
-  double wr0 = fma(g0, bp2, eps), wr2 = fma(g2, bp0, eps);
+  const double bp2 = fma(tau5, ib2, 1.0);
+  const bool big2 = __double2hiint(d20) >= 0;  // beta2 >= beta0
+  const double bM = big2 ? beta2 : beta0, bm = big2 ? beta0 : beta2;
+  const double X1 = fma(2.0, bM, -bm), Y1 = beta1 + tau5;
+  const double X = X1 * Y1;
+  const double wl0 = g0 * bp0, wl1 = g1 * bp1, wl2 = g2 * bp2;
+  const double wr0 = g0 * bp2, wr2 = g2 * bp0;
   const double Sl = wl0 + wl1 + wl2, Sr = wr0 + wl1 + wr2;
-  const double SS = Sl * Sr;
-  if (dexp(SS) > 2030) {
+  const double SS = Sl * Sr, S2 = Sl + Sr;
+  const int ex = dexp(X);
+  if (ex < 16 || ex > 2030 || dexp(SS) > 2030 || dexp(S2) > 2027) {
     recon_weno5z(q0, q1, q2, q3, q4, ql, qr);
     return;
   }
-  const double rS = rcp_nr(SS);
-  const double isl = Sr * rS, isr = Sl * rS;
-  wl0 *= isl;
-  const double wm_l = wl1 * isl;
-  wl2 *= isl;
-  wr0 *= isr;
-  const double wm_r = wl1 * isr;
-  wr2 *= isr;
+  const double rx = rcp_nr(X);
+  const double R = fma(bm, big2 ? ib2 : ib0, fma(bM, Y1 * rx, beta1 * (X1 * rx)));
+  const double alpha_lin = rcp_nr(R * S2 * (1.0 / 6.0));
+  const double rS = rcp_nr(SS) * (1.0 / 12.0);
+  const double isl = Sr * rS, isr = Sl * rS;  // 1 / (12 S_l), 1 / (12 S_r)
+  // 2 mc(q2 - q1, q3 - q2, 2) = copysign(min(|dm + dp|, 4 min(|dm|, |dp|)),
+  // dm + dp) where dm dp > 0, else 0 (finite dm, dp: |q| < 1e50 here)
+  const long long MAG = 0x7fffffffffffffffLL;
+  const long long idm = __double_as_longlong(q2 - q1), idp = __double_as_longlong(q3 - q2);
+  const long long isum = __double_as_longlong(b1);
+  const long long adm = idm & MAG, adp = idp & MAG, asum = isum & MAG;
+  const bool same = ((idm ^ idp) >= 0) && adm != 0 && adp != 0;
+  const long long a4 = (adm < adp ? adm : adp) + (2LL << 52);
+  const double dq2 = same ? __longlong_as_double((asum < a4 ? asum : a4) | (isum & ~MAG)) : 0.0;
   // candidate values as q2 plus a twelfth of a_k +- 3 b_k: for ql (upper
   // face) (a0 + 3 b0), (a1 + 3 b1), (a2 - 3 b2); for qr (lower face, the
   // mirrored stencils) (a2 + 3 b2), (a1 - 3 b1), (a0 - 3 b0); the weights sum
-  // to one, so sum_k w_k c_k = q2 + sum_k w_k (c_k - q2)
-  ql = fma(wl0 * fma(3.0, b0, a0) + wm_l * fma(3.0, b1, a1) + wl2 * fma(-3.0, b2, a2), 1.0 / 12.0, q2);
-  qr = fma(wr0 * fma(3.0, b2, a2) + wm_r * fma(-3.0, b1, a1) + wr2 * fma(-3.0, b0, a0), 1.0 / 12.0, q2);
-  const double tl = wm_l * wl2, tr = wm_r * wr2;
-  const double Dl = fma(wl0, fma(g1, wl2, g2 * wm_l), g0 * tl);
-  const double Dr = fma(wr0, fma(g1, wr2, g2 * wm_r), g0 * tr);
-  const double DD = Dl * Dr;
-  if (dexp(DD) < 16) {
-    recon_weno5z(q0, q1, q2, q3, q4, ql, qr);
-    return;
-  }
-  const double rD = rcp_nr(DD);
-  const double alpha_l = fma(3.0 * wl0 * tl, Dr * rD, eps);
-  const double alpha_r = fma(3.0 * wr0 * tr, Dl * rD, eps);
-  double dq = q3 - q2;
-  dq = mc(q2 - q1, dq, 2.0);
-  const double alpha_lin = 2.0 * alpha_l * alpha_r * rcp_nr(alpha_l + alpha_r);
-  // alpha q + (1 - alpha) p as p + alpha (q - p)
-  const double pl = fma(0.5, dq, q2), pr = fma(-0.5, dq, q2);
-  ql = fma(alpha_lin, ql - pl, pl);
-  qr = fma(alpha_lin, qr - pr, pr);
+  // to one, so sum_k w_k c_k = q2 + sum_k w_k (c_k - q2).  Then the blend
+  // alpha q + (1 - alpha) p with p = q2 +- dq2 / 4 as p + alpha (q - p).
+  const double xl = (wl0 * fma(3.0, b0, a0) + wl1 * fma(3.0, b1, a1) + wl2 * fma(-3.0, b2, a2)) * isl;
+  const double xr = (wr0 * fma(3.0, b2, a2) + wl1 * fma(-3.0, b1, a1) + wr2 * fma(-3.0, b0, a0)) * isr;
+  ql = fma(alpha_lin, fma(-0.25, dq2, xl), fma(0.25, dq2, q2));
+  qr = fma(alpha_lin, fma(0.25, dq2, xr), fma(-0.25, dq2, q2));
 }
 
 __device__ __forceinline__ double minmod(double a, double b) {
@@ -680,10 +697,16 @@ __device__ __forceinline__ void prim_to_flux(const Par &par, const Face &f, cons
   const double iW0 = rsqrt_p(Wsq0);
   double W = Wsq0 * iW0;
 #endif
+#ifndef PHX_EXACT
+  bool capped = false;  // a velocity cap changed v: W is formed again below
+#endif
   if (W > gam_max) {
     const double rescale = sqrt((gam_max * gam_max - 1.) / (W * W - 1.));
 #pragma unroll
     for (int ii = 0; ii < 3; ii++) vpcon[ii] *= rescale;
+#ifndef PHX_EXACT
+    capped = true;
+#endif
   }
   const double qe = q[PHX_PENG];
 #ifdef PHX_EXACT
@@ -761,15 +784,20 @@ __device__ __forceinline__ void prim_to_flux(const Par &par, const Face &f, cons
     if constexpr (!MINK)
 #pragma unroll
       for (int m = 0; m < 3; m++) vlo[m] *= scale;
+    capped = true;
 #endif
   }
 #ifdef PHX_EXACT
   W = 1.0 / sqrt(1 - vsq);
 #else
   // production build: W = 1/s with s = sqrt(1 - v^2); divisions by W and W^2
-  // become products with s and s^2
-  W = rsqrt_p(1 - vsq);
-  const double sW = (1 - vsq) * W;
+  // become products with s and s^2.  Without a cap v^2 = 1 - 1/W0^2, so W
+  // stays W0 and s is the 1/W0 formed above (no second rsqrt)
+  double sW = iW0;
+  if (capped) {
+    W = rsqrt_p(1 - vsq);
+    sW = (1 - vsq) * W;
+  }
 #endif
   const double vel = vcon[DIR];
   const double alpha = MINK ? 1.0 : g.alpha;
@@ -789,11 +817,15 @@ __device__ __forceinline__ void prim_to_flux(const Par &par, const Face &f, cons
   const double b0 = W * Bdotv;
 #ifdef PHX_EXACT
   const double bsq = (BdotB + b0 * b0) / (W * W);
-#else
-  const double bsq = (BdotB + b0 * b0) * (sW * sW);
-#endif
   const double rhohWsq = (rho + u + P) * W * W;
   const double bsqWsq = bsq * W * W;
+#else
+  // production build: bsq W^2 = B.B + b0^2 (sW = 1/W), W^2 formed once
+  const double Wsq = W * W;
+  const double bsqWsq = fma(b0, b0, BdotB);
+  const double bsq = bsqWsq * (sW * sW);
+  const double rhohWsq = (rho + u + P) * Wsq;
+#endif
   const double ptot = P + 0.5 * bsq;
 #pragma unroll
   for (int m = 0; m < 3; m++) {
@@ -826,7 +858,11 @@ __device__ __forceinline__ void prim_to_flux(const Par &par, const Face &f, cons
     F[PHX_CMOM + m] = U[PHX_CMOM + m] * vtil + ptot * (double)(DIR == m) - PHX_DIV_W(bcovm * Bcon[DIR]);
 #undef PHX_DIV_W
   }
+#ifdef PHX_EXACT
   U[PHX_CENG] = rhohWsq + bsqWsq - ptot - b0 * b0 - U[PHX_CRHO];
+#else
+  U[PHX_CENG] = rhohWsq + BdotB - ptot - U[PHX_CRHO];  // bsq W^2 - b0^2 = B.B
+#endif
   F[PHX_CENG] = U[PHX_CENG] * vtil + ptot * vel - Bdotv * Bcon[DIR];
 #pragma unroll
   for (int m = 0; m < 3; m++) {
@@ -849,10 +885,10 @@ __device__ __forceinline__ void prim_to_flux(const Par &par, const Face &f, cons
   if (eAB >= 16 && eAB <= 2030) {
     const double rAB = rcp_nr(dAB);
     vasq = bsqWsq * (dB * rAB);
-    cs_raw = gamma1 * P * W * W * (dA * rAB);
+    cs_raw = gamma1 * P * Wsq * (dA * rAB);
   } else {
     vasq = bsqWsq * rcp_p(dA);
-    cs_raw = gamma1 * P * W * W * rcp_p(dB);
+    cs_raw = gamma1 * P * Wsq * rcp_p(dB);
   }
   const double cssq = make_bounded(cs_raw, 0.0, 1.0);
 #endif

@@ -23,26 +23,23 @@ __device__ __forceinline__ float mlp_w(const float *theta, int off, int N, int K
 
 __global__ void k_mlp_pack(const float *theta, MlpPacked *out) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
-  constexpr int E1 = 8 * 1 * 32, E2 = 8 * 4 * 32, E4 = 1 * 4 * 32;
+  constexpr int E1 = 64 * 16, E2 = 64 * 64, E4 = 16 * 64;
   if (t < E1 + 2 * E2 + E4) {
-    int e = t, off, N, K, KS;
-    uint2 *dst;
+    // element (n, k) of an N x K weight matrix, K-major core-matrix layout
+    int e = t, off, N, K, KP;
+    uint16_t *dst;
     if (e < E1) {
-      off = MLP_OFF_W1, N = 64, K = PHX_MLP_IN, KS = 1, dst = out->w1;
+      off = MLP_OFF_W1, N = 64, K = PHX_MLP_IN, KP = 16, dst = out->w1;
     } else if ((e -= E1) < E2) {
-      off = MLP_OFF_W2, N = 64, K = 64, KS = 4, dst = out->w2;
+      off = MLP_OFF_W2, N = 64, K = 64, KP = 64, dst = out->w2;
     } else if ((e -= E2) < E2) {
-      off = MLP_OFF_W3, N = 64, K = 64, KS = 4, dst = out->w3;
+      off = MLP_OFF_W3, N = 64, K = 64, KP = 64, dst = out->w3;
     } else {
       e -= E2;
-      off = MLP_OFF_W4, N = PHX_MLP_OUT, K = 64, KS = 4, dst = out->w4;
+      off = MLP_OFF_W4, N = PHX_MLP_OUT, K = 64, KP = 64, dst = out->w4;
     }
-    const int lane = e & 31, ks = (e >> 5) % KS, nt = (e >> 5) / KS;
-    const int n = nt * 8 + (lane >> 2), k0 = ks * 16 + (lane & 3) * 2;
-    uint2 v;
-    v.x = pack_bf16x2(mlp_w(theta, off, N, K, n, k0), mlp_w(theta, off, N, K, n, k0 + 1));
-    v.y = pack_bf16x2(mlp_w(theta, off, N, K, n, k0 + 8), mlp_w(theta, off, N, K, n, k0 + 9));
-    dst[e] = v;
+    const int n = e / KP, k = e % KP;
+    dst[kmaj_off(n, k, KP) / 2] = __bfloat16_as_ushort(__float2bfloat16_rn(mlp_w(theta, off, N, K, n, k)));
   } else if ((t -= E1 + 2 * E2 + E4) < 64 * 3 + 8) {
     if (t < 64)
       out->b1[t] = theta[MLP_OFF_B1 + t];
@@ -56,7 +53,7 @@ __global__ void k_mlp_pack(const float *theta, MlpPacked *out) {
 }
 
 void launch_mlp_pack(const float *theta, MlpPacked *out, cudaStream_t s) {
-  const int n = 8 * 32 + 2 * 8 * 4 * 32 + 4 * 32 + 64 * 3 + 8;
+  const int n = 64 * 16 + 2 * 64 * 64 + 16 * 64 + 64 * 3 + 8;
   k_mlp_pack<<<(n + 255) / 256, 256, 0, s>>>(theta, out);
 }
 
@@ -179,28 +176,32 @@ void launch_mlp_features(const Par &p, long long n, const double *cons, const do
 // --------------------------------------------------- inference on features
 struct MlpFwdSmem {
   MlpPacked w;
-  uint32_t xs[4][128];
-  float os[4][64];
+  MlpTile tile;
 };
+// more than 1/9 of an SM's shared memory: at most 8 CTAs resident, whose TMEM
+// columns (8 x 64) fit the SM's 512, so tcgen05.alloc never waits on another CTA
+static_assert(sizeof(MlpFwdSmem) * 9 > 228 * 1024, "TMEM columns of the resident CTAs");
 
 __global__ void __launch_bounds__(128) k_mlp_forward(const MlpPacked *mlp, long long n, const float *x, float *out,
                                                      unsigned int *err) {
-  extern __shared__ __align__(16) unsigned char fwd_dyn[];
+  extern __shared__ __align__(128) unsigned char fwd_dyn[];
   __shared__ __align__(8) uint64_t bar;
   MlpFwdSmem *S = reinterpret_cast<MlpFwdSmem *>(fwd_dyn);
   if (!mlp_stage_weights(&S->w, mlp, &bar, err)) return;
-  const int warp = threadIdx.x >> 5;
+  mlp_tc_init(&S->tile);
+  unsigned phase = 0;
   for (long long base = (long long)blockIdx.x * 128; base < n; base += (long long)gridDim.x * 128) {
     const long long q = base + threadIdx.x;
     float f[6];
     for (int c = 0; c < 6; c++) f[c] = q < n ? x[c * n + q] : 0.0f;
     float o0, o1;
-    mlp_warp_forward(S->w, f, S->xs[warp], S->os[warp], o0, o1);
+    if (!mlp_cta_forward(S->w, &S->tile, f, phase, err, o0, o1)) break;
     if (q < n) {
       out[q] = o0;
       out[n + q] = o1;
     }
   }
+  mlp_tc_finish(&S->tile);
 }
 
 void launch_mlp_forward(const MlpPacked *mlp, long long n, const float *x, float *out, unsigned int *err,

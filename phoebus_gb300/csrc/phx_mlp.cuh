@@ -1,18 +1,22 @@
 // phx_mlp.cuh -- the learned con2prim start on the device (no reference
-// counterpart): packed BF16 weights and the warp-level tensor-core forward
+// counterpart): packed BF16 weights and the CTA-level tensor-core forward
 // pass used inside the con2prim kernels.
 //
 // Network 6 -> 64 -> 64 -> 64 -> 2 with GELU (tanh form).  FP32 master
 // parameters (phx_fluid.h, PHX_MLP_NPARAM) in the order W1[64][6], b1,
 // W2[64][64], b2, W3[64][64], b3, W4[2][64], b4 (weights [out][in]).
 //
-// Inference: one warp evaluates 32 zones as two 16-row tiles with
-// mma.sync.m16n8k16 (BF16 operands, FP32 accumulate).  The weights are
-// pre-packed in the B-fragment order of that instruction (per n-tile, k-step
-// and lane one 8-byte pair), so a lane loads each fragment with one shared
-// memory load; the accumulator fragments of one layer are the A fragments of
-// the next (after GELU and BF16 rounding), so activations never leave
-// registers.
+// Inference: a CTA of 128 threads evaluates 128 zones as one M = 128 tile on
+// the fifth-generation tensor cores.  Thread t writes its zone's layer input
+// as row t of a BF16 operand tile in shared memory; one thread issues
+// tcgen05.mma (kind::f16: BF16 operands, FP32 accumulate) with the layer's
+// weights as the second operand, also in shared memory, and the accumulator
+// (128 lanes x 64 FP32 columns) lands in tensor memory; tcgen05.commit
+// arrives on an mbarrier when the products are done.  Each warp then reads
+// its 32 lanes (rows) back with tcgen05.ld, adds the bias, applies GELU and
+// writes the next layer's BF16 input tile.  Layer 1 is one K = 16 product
+// (6 features, zero padded), layers 2 and 3 four K = 16 steps each, layer 4
+// four steps with N = 16 (2 outputs, zero padded).
 #pragma once
 #include <cuda_bf16.h>
 
@@ -31,13 +35,23 @@ constexpr int MLP_OFF_W4 = MLP_OFF_B3 + PHX_MLP_HID;
 constexpr int MLP_OFF_B4 = MLP_OFF_W4 + PHX_MLP_OUT * PHX_MLP_HID;
 static_assert(MLP_OFF_B4 + PHX_MLP_OUT == PHX_MLP_NPARAM, "parameter layout");
 
-// B fragments: layer 1 (K 6 -> 16, N 64): 8 n-tiles x 1 k-step; layers 2, 3
-// (K 64, N 64): 8 x 4; layer 4 (K 64, N 2 -> 8): 1 x 4.  32 lanes each.
+// Byte offset of element (r, k) of a BF16 matrix with K columns in the
+// canonical K-major layout without swizzling that tcgen05.mma reads through
+// a shared-memory descriptor: 8-row x 16-byte core matrices, the core
+// matrices of one 8-row group adjacent along K (128 bytes apart: the
+// descriptor's leading-dimension offset), the 8-row groups K * 16 bytes apart
+// (its stride-dimension offset).
+__host__ __device__ constexpr int kmaj_off(int r, int k, int K) {
+  return (r >> 3) * (K >> 3) * 128 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2;
+}
+
+// Weights as BF16 bit patterns in that layout (rows = output features,
+// columns = input features), biases and the input box in FP32.
 struct MlpPacked {
-  uint2 w1[8 * 1 * 32];
-  uint2 w2[8 * 4 * 32];
-  uint2 w3[8 * 4 * 32];
-  uint2 w4[1 * 4 * 32];
+  alignas(128) uint16_t w1[64 * 16];  // N 64 x K 16 (6 inputs, zero padded)
+  alignas(128) uint16_t w2[64 * 64];
+  alignas(128) uint16_t w3[64 * 64];
+  alignas(128) uint16_t w4[16 * 64];  // N 16 (2 outputs, zero padded) x K 64
   float b1[64], b2[64], b3[64], b4[8];
   // input box of the learned start: a cold zone whose features fall outside
   // [xlo, xhi] (the training set's range, widened) gets no bracket and keeps
@@ -54,14 +68,6 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
   return *reinterpret_cast<uint32_t *>(&v);
 }
 
-__device__ __forceinline__ void mma_bf16_16816(float c[4], const uint32_t a[4], uint2 b) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};"
-      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b.x), "r"(b.y));
-}
-
 // GELU, tanh form, with the hardware tanh approximation.
 __device__ __forceinline__ float gelu_fast(float z) {
   const float u = 0.7978845608028654f * (z + 0.044715f * z * z * z);
@@ -70,114 +76,179 @@ __device__ __forceinline__ float gelu_fast(float z) {
   return 0.5f * z * (1.0f + t);
 }
 
-// Accumulator fragments C[mt][nt] of a 64-wide layer -> GELU -> A fragments
-// A[mt][ks] of the next layer (k-step ks spans n-tiles 2ks and 2ks+1).
-__device__ __forceinline__ void mlp_act_to_a(const float C[2][8][4], uint32_t A[2][4][4]) {
-#pragma unroll
-  for (int mt = 0; mt < 2; mt++)
-#pragma unroll
-    for (int ks = 0; ks < 4; ks++) {
-      const float *c0 = C[mt][2 * ks], *c1 = C[mt][2 * ks + 1];
-      A[mt][ks][0] = pack_bf16x2(gelu_fast(c0[0]), gelu_fast(c0[1]));
-      A[mt][ks][1] = pack_bf16x2(gelu_fast(c0[2]), gelu_fast(c0[3]));
-      A[mt][ks][2] = pack_bf16x2(gelu_fast(c1[0]), gelu_fast(c1[1]));
-      A[mt][ks][3] = pack_bf16x2(gelu_fast(c1[2]), gelu_fast(c1[3]));
-    }
+// ------------------------------------------------ tensor-core forward pass
+// TMEM columns of the accumulator: 64 FP32 columns x 128 lanes.  A CTA of the
+// inference kernels takes more than 1/8 of an SM's shared memory, so at most
+// 8 are resident and their 8 x 64 columns fit the SM's 512.
+constexpr uint32_t MLP_TMEM_COLS = 64;
+
+// Per-CTA scratch: the BF16 layer-input tile (M 128 x K 64; layer 1 uses the
+// K 16 layout in its first 4 KB), the MMA-completion mbarrier and the TMEM
+// base address tcgen05.alloc returns.
+struct MlpTile {
+  alignas(128) uint16_t a[128 * 64];
+  alignas(8) uint64_t bar;
+  uint32_t tmem;
+  uint32_t pad;
+};
+
+// Shared-memory matrix descriptor: start address >> 4 (bits 0-13), leading-
+// dimension byte offset >> 4 (bits 16-29, here 128: core matrices adjacent
+// along K), stride-dimension byte offset >> 4 (bits 32-45), the descriptor
+// version 1 in bits 46-48, base offset 0, no swizzling (bits 61-63 = 0).
+__device__ __forceinline__ uint64_t mlp_desc(const void *p, uint32_t sbo) {
+  return (uint64_t)((smem_u32(p) & 0x3FFFFu) >> 4) | ((uint64_t)(128u >> 4) << 16) |
+         ((uint64_t)(sbo >> 4) << 32) | (1ull << 46);
+}
+// Instruction descriptor of kind::f16: D FP32 (bits 4-5 = 1), A and B BF16
+// (bits 7-9 and 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 in bits
+// 17-22, M >> 4 = 8 (M = 128) in bits 24-28.
+__host__ __device__ constexpr uint32_t mlp_idesc(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
 }
 
-__device__ __forceinline__ void mlp_hidden(const uint2 *W, const float *bias, const uint32_t A[2][4][4],
-                                           float C[2][8][4], int lane) {
-  const int tig = lane & 3;
+__device__ __forceinline__ void mlp_mma(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void mlp_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 32 consecutive FP32 columns of this warp's 32 TMEM lanes (thread = lane),
+// waited for inside the same statement.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float v[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
 #pragma unroll
-  for (int nt = 0; nt < 8; nt++) {
-    const float bx = bias[nt * 8 + tig * 2], by = bias[nt * 8 + tig * 2 + 1];
+  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_ld2(uint32_t taddr, float v[2]) {
+  uint32_t r0, r1;
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0,%1}, [%2];\n"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r0), "=r"(r1)
+      : "r"(taddr)
+      : "memory");
+  v[0] = __uint_as_float(r0);
+  v[1] = __uint_as_float(r1);
+}
+
+// CTA entry: thread 0 initialises the mbarrier, warp 0 allocates the TMEM
+// columns; every thread then reads the base address.
+__device__ __forceinline__ void mlp_tc_init(MlpTile *T) {
+  if (threadIdx.x == 0) {
+    mbar_init(&T->bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (threadIdx.x < 32) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&T->tmem)),
+                 "r"(MLP_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+}
+// CTA exit (every thread, after its last tcgen05.ld): warp 0 frees the columns.
+__device__ __forceinline__ void mlp_tc_finish(MlpTile *T) {
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (threadIdx.x < 32)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(T->tmem), "r"(MLP_TMEM_COLS)
+                 : "memory");
+}
+
+// The layer input written by every thread becomes visible to the tensor
+// cores (async proxy) and every thread's TMEM reads are complete; then thread
+// 0 issues `nk` K = 16 steps of [A | a_sbo] x [W | w_sbo] into the TMEM
+// columns and commits them to the mbarrier; every thread waits (bounded) for
+// that phase.  False, with ERR_TIMEOUT set, when the wait gave up.
+__device__ __forceinline__ bool mlp_tc_layer(MlpTile *T, const uint16_t *W, int nk, uint32_t a_sbo, uint32_t w_sbo,
+                                             uint32_t idesc, unsigned &phase, unsigned int *err) {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    tc_fence_after();
+    for (int s = 0; s < nk; s++)
+      mlp_mma(T->tmem, mlp_desc(T->a + s * 128, a_sbo), mlp_desc(W + s * 128, w_sbo), idesc, s > 0 ? 1u : 0u);
+    mlp_commit(&T->bar);
+  }
+  const bool ok = mbar_wait_block(&T->bar, phase, MBAR_SPIN_LIMIT, err);
+  phase ^= 1u;
+  tc_fence_after();
+  return ok;
+}
+
+// This thread's 64 accumulator columns + bias -> GELU -> BF16 row `row` of
+// the next layer's K 64 input tile.
+__device__ __forceinline__ void mlp_tc_activate(MlpTile *T, const float *bias, int row) {
+  const uint32_t lane_base = (uint32_t)((threadIdx.x >> 5) * 32) << 16;
 #pragma unroll
-    for (int mt = 0; mt < 2; mt++) {
-      C[mt][nt][0] = bx;
-      C[mt][nt][1] = by;
-      C[mt][nt][2] = bx;
-      C[mt][nt][3] = by;
-    }
+  for (int h = 0; h < 2; h++) {
+    float v[32];
+    tmem_ld32(T->tmem + lane_base + (uint32_t)(32 * h), v);
 #pragma unroll
-    for (int ks = 0; ks < 4; ks++) {
-      const uint2 bf = W[(nt * 4 + ks) * 32 + lane];
-      mma_bf16_16816(C[0][nt], A[0][ks], bf);
-      mma_bf16_16816(C[1][nt], A[1][ks], bf);
+    for (int g = 0; g < 4; g++) {
+      uint4 q;
+      const float *c = v + 8 * g;
+      const float *b = bias + 32 * h + 8 * g;
+      q.x = pack_bf16x2(gelu_fast(c[0] + b[0]), gelu_fast(c[1] + b[1]));
+      q.y = pack_bf16x2(gelu_fast(c[2] + b[2]), gelu_fast(c[3] + b[3]));
+      q.z = pack_bf16x2(gelu_fast(c[4] + b[4]), gelu_fast(c[5] + b[5]));
+      q.w = pack_bf16x2(gelu_fast(c[6] + b[6]), gelu_fast(c[7] + b[7]));
+      *reinterpret_cast<uint4 *>(reinterpret_cast<unsigned char *>(T->a) + kmaj_off(row, 32 * h + 8 * g, 64)) = q;
     }
   }
 }
 
-// Forward pass for the 32 zones of a warp (lane L owns zone L).  f: this
-// lane's 6 features.  xs: 128 words and os: 64 floats of per-warp shared
-// scratch.  Returns this lane's outputs (o0 = ln mu, o1 = ln sigma).
-__device__ __forceinline__ void mlp_warp_forward(const MlpPacked &S, const float f[6], uint32_t *xs, float *os,
-                                                 float &o0, float &o1) {
-  const int lane = threadIdx.x & 31, r = lane >> 2, tig = lane & 3;
-  xs[lane * 4 + 0] = pack_bf16x2(f[0], f[1]);
-  xs[lane * 4 + 1] = pack_bf16x2(f[2], f[3]);
-  xs[lane * 4 + 2] = pack_bf16x2(f[4], f[5]);
-  xs[lane * 4 + 3] = 0u;
-  __syncwarp();
-  uint32_t A[2][4][4];
-  float C[2][8][4];
-  {  // layer 1: K = 16 (6 features, zero padded), one k-step
-    uint32_t A1[2][4];
-#pragma unroll
-    for (int mt = 0; mt < 2; mt++) {
-      A1[mt][0] = xs[(mt * 16 + r) * 4 + tig];
-      A1[mt][1] = xs[(mt * 16 + r + 8) * 4 + tig];
-      A1[mt][2] = 0u;
-      A1[mt][3] = 0u;
-    }
-#pragma unroll
-    for (int nt = 0; nt < 8; nt++) {
-      const float bx = S.b1[nt * 8 + tig * 2], by = S.b1[nt * 8 + tig * 2 + 1];
-      const uint2 bf = S.w1[nt * 32 + lane];
-#pragma unroll
-      for (int mt = 0; mt < 2; mt++) {
-        C[mt][nt][0] = bx;
-        C[mt][nt][1] = by;
-        C[mt][nt][2] = bx;
-        C[mt][nt][3] = by;
-        mma_bf16_16816(C[mt][nt], A1[mt], bf);
-      }
-    }
-  }
-  mlp_act_to_a(C, A);
-  mlp_hidden(S.w2, S.b2, A, C, lane);
-  mlp_act_to_a(C, A);
-  mlp_hidden(S.w3, S.b3, A, C, lane);
-  mlp_act_to_a(C, A);
-  float C4[2][4];
-  {
-    const float bx = S.b4[tig * 2], by = S.b4[tig * 2 + 1];
-#pragma unroll
-    for (int mt = 0; mt < 2; mt++) {
-      C4[mt][0] = bx;
-      C4[mt][1] = by;
-      C4[mt][2] = bx;
-      C4[mt][3] = by;
-    }
-#pragma unroll
-    for (int ks = 0; ks < 4; ks++) {
-      const uint2 bf = S.w4[ks * 32 + lane];
-      mma_bf16_16816(C4[0], A[0][ks], bf);
-      mma_bf16_16816(C4[1], A[1][ks], bf);
-    }
-  }
-  if (tig == 0) {  // columns 0, 1 of rows r and r + 8 of each tile
-#pragma unroll
-    for (int mt = 0; mt < 2; mt++) {
-      os[(mt * 16 + r) * 2 + 0] = C4[mt][0];
-      os[(mt * 16 + r) * 2 + 1] = C4[mt][1];
-      os[(mt * 16 + r + 8) * 2 + 0] = C4[mt][2];
-      os[(mt * 16 + r + 8) * 2 + 1] = C4[mt][3];
-    }
-  }
-  __syncwarp();
-  o0 = os[lane * 2];
-  o1 = os[lane * 2 + 1];
-  __syncwarp();
+// Forward pass of the CTA's 128 zones (thread t owns zone t: f its six
+// features).  Every thread of the CTA calls it.  Returns this thread's
+// outputs (o0 = ln mu, o1 = ln sigma); false, with ERR_TIMEOUT set, when a
+// product did not complete within the bounded wait (every thread returns the
+// same value; the caller stops using the network).
+__device__ __forceinline__ bool mlp_cta_forward(const MlpPacked &S, MlpTile *T, const float f[6], unsigned &phase,
+                                                unsigned int *err, float &o0, float &o1) {
+  const int t = threadIdx.x;
+  unsigned char *a = reinterpret_cast<unsigned char *>(T->a);
+  uint4 x0, x1 = make_uint4(0u, 0u, 0u, 0u);
+  x0.x = pack_bf16x2(f[0], f[1]);
+  x0.y = pack_bf16x2(f[2], f[3]);
+  x0.z = pack_bf16x2(f[4], f[5]);
+  x0.w = 0u;
+  *reinterpret_cast<uint4 *>(a + kmaj_off(t, 0, 16)) = x0;
+  *reinterpret_cast<uint4 *>(a + kmaj_off(t, 8, 16)) = x1;
+  if (!mlp_tc_layer(T, S.w1, 1, 16 * 16, 16 * 16, mlp_idesc(64), phase, err)) return false;
+  mlp_tc_activate(T, S.b1, t);
+  if (!mlp_tc_layer(T, S.w2, 4, 64 * 16, 64 * 16, mlp_idesc(64), phase, err)) return false;
+  mlp_tc_activate(T, S.b2, t);
+  if (!mlp_tc_layer(T, S.w3, 4, 64 * 16, 64 * 16, mlp_idesc(64), phase, err)) return false;
+  mlp_tc_activate(T, S.b3, t);
+  if (!mlp_tc_layer(T, S.w4, 4, 64 * 16, 64 * 16, mlp_idesc(16), phase, err)) return false;
+  float o[2];
+  tmem_ld2(T->tmem + ((uint32_t)((t >> 5) * 32) << 16), o);
+  o0 = o[0] + S.b4[0];
+  o1 = o[1] + S.b4[1];
+  return true;
 }
 
 // True when all six features lie inside the network's input box (NaN: no).
