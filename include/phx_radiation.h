@@ -50,6 +50,11 @@ enum {
 
 typedef enum { PHX_RAD_M1 = 0, PHX_RAD_EDDINGTON = 1 } phx_rad_method; /* radiation.cpp:51-59 */
 
+typedef enum { /* radiation.hpp SourceSolver, radiation.cpp:403-415 (zerod is disabled there) */
+  PHX_RAD_SRC_ONED = 0,
+  PHX_RAD_SRC_FOURD = 1
+} phx_rad_src_solver;
+
 typedef enum { /* radiation.hpp OneDFixupStrategy, radiation.cpp:432-445 */
   PHX_RAD_ONED_FIXUP_NONE = 0,
   PHX_RAD_ONED_FIXUP_IGNORE_DJ = 1,
@@ -85,6 +90,13 @@ typedef struct {
   int update_fluid;
   /* fixup/rad_c2p_failure_strategy: 0 interpolate (default), 1 floors */
   int rad_c2p_failure_floors;
+  /* radiation/src_solver (phx_rad_src_solver, default oned), and for fourd
+   * radiation/src_rootfind_eps (finite-difference step, 1e-8) and
+   * radiation/src_use_oned_backup (0).  fourd iterates to src_rootfind_tol
+   * within src_rootfind_maxiter Newton steps. */
+  int src_solver;
+  double src_rootfind_eps;
+  int src_use_oned_backup;
 } phx_rad_params;
 
 /* Radiation fields of one block.  Same shape and var_stride convention as

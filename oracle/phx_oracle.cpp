@@ -77,6 +77,9 @@ struct EOS {
   Real BulkModulusFromDensityTemperature(Real rho, Real T) const {
     return std::max(0.0, (gm1 + 1) * gm1 * rho * Cv * T);
   }
+  Real BulkModulusFromDensityInternalEnergy(Real rho, Real sie) const {
+    return std::max(0.0, gm1 * (gm1 + 1) * rho * sie);
+  }
 };
 
 // ------------------------------------------------------------- fixup.hpp
@@ -2749,10 +2752,15 @@ struct RPar {
   Real cfl, tol, kappa_a, kappa_s, jbb;
   int maxiter, oned_fixup;
   bool update_fluid, fixup_floors;
+  bool fourd, oned_backup;  // src_solver fourd; src_use_oned_backup
+  Real fd_eps;              // src_rootfind_eps
   Real J_floor, xi_ceiling, tau_max, W_ceiling, Cv;
   RPar(const phx_rad_params &rp, const phx_params &p) {
     update_fluid = rp.update_fluid != 0;
     fixup_floors = rp.rad_c2p_failure_floors != 0;
+    fourd = rp.src_solver == PHX_RAD_SRC_FOURD;
+    oned_backup = rp.src_use_oned_backup != 0;
+    fd_eps = rp.src_rootfind_eps;
     m1 = rp.method == PHX_RAD_M1;
     robust = !rp.closure_frail;
     bounds = rp.recon_fixup_bounds != 0;
@@ -3222,9 +3230,234 @@ void update_fluid_zone(const RPar &rp, const phx_params &fp, const RBlk &R, cons
   for (int a = 0; a < 3; a++) R.U(PHX_RF + a, id) = covF(a) * sdetgam;
 }
 
-// MomentFluidSourceImpl, oned solver, one species (moments_source.cpp:203-490
-// and 786-965); fp: the fluid inversion's settings (update_fluid).  Returns 1
-// when the source update was applied.
+// The fourd source solver's residual pieces (moments_source.cpp:39-150) for
+// one zone.  Properties of the reference kept as they are: the fluid state
+// enters prim2con with B = 0 (MomentFluidSourceImpl declares the B array a
+// second time inside the block that reads it, moments_source.cpp:324-328, so
+// the array it hands on stays zero); kappaH is the absorption coefficient
+// added twice (:106-109), both capped at 1e5 before the source; the closure's
+// xi guess, an uninitialised local there (:94-96), is SolveClosure's
+// declared default 0.5 here.
+struct SourceResidual4 {
+  const RPar &rp;
+  const EOS &eos;
+  const RGeo &G;
+  Real rho, sdetgam, alpha;
+  Real U_mhd_0[4], U_rad_0[4];
+  void MHDConserved(const Real P_mhd[4], Real U_mhd[4]) const {
+    const Real Pg = eos.PressureFromDensityInternalEnergy(rho, P_mhd[0] / rho);
+    const Real gam1 = eos.BulkModulusFromDensityInternalEnergy(rho, P_mhd[0] / rho) / Pg;
+    const Real bprim[3] = {0.0, 0.0, 0.0};
+    Real D, bcons[3], sig[3];
+    p2c(rho, &P_mhd[1], bprim, P_mhd[0], Pg, gam1, G.p.gcov, G.p.gamcon, G.p.beta, G.p.alpha, sdetgam, D, &U_mhd[1],
+        bcons, U_mhd[0], sig);
+  }
+  void RadConserved(const Real U_mhd[4], Real U_rad[4]) const {
+    for (int n = 0; n < 4; n++) U_rad[n] = U_rad_0[n] - (U_mhd[n] - U_mhd_0[n]);
+  }
+  Real W_of(const Real P_mhd[4]) const {
+    Real W = 0.;
+    for (int ii = 0; ii < 3; ii++)
+      for (int jj = 0; jj < 3; jj++) W += G.p.gcov[ii + 1][jj + 1] * P_mhd[ii + 1] * P_mhd[jj + 1];
+    return std::sqrt(1. + W);
+  }
+  Status RadPrimitive(const Real P_mhd[4], const Real U_rad[4], Real P_rad[4]) const {
+    const Real E = U_rad[0] / sdetgam;
+    const V3 cov_F{{U_rad[1] / sdetgam, U_rad[2] / sdetgam, U_rad[3] / sdetgam}};
+    const Real W = W_of(P_mhd);
+    const V3 con_v{{P_mhd[1] / W, P_mhd[2] / W, P_mhd[3] / W}};
+    const Closure c(con_v, rp.m1, true, G.g());
+    Real xi = 0.5, phi = PI;
+    T2 Pi;
+    c.TilPiFromCon(E, cov_F, xi, phi, Pi);
+    V3 cov_H;
+    const Status st = c.Con2Prim(E, cov_F, Pi, P_rad[0], cov_H);
+    for (int ii = 0; ii < 3; ii++) P_rad[ii + 1] = cov_H(ii);
+    return st;
+  }
+  void Source(const Real P_mhd[4], const Real P_rad[4], Real S[4]) const {
+    const Real Tg = eos.TemperatureFromDensityInternalEnergy(rho, P_mhd[0] / rho);
+    const Real JBB = rp.JBB(Tg);
+    Real kappaJ = rp.kappaJ(rho, Tg);
+    Real kappaH = kappaJ + rp.kappaJ(rho, Tg);
+    kappaH = smin(kappaH, 1.e5);
+    kappaJ = smin(kappaJ, 1.e5);
+    const Real W = W_of(P_mhd);
+    Real cov_v[3] = {0.0, 0.0, 0.0};
+    for (int ii = 0; ii < 3; ii++)
+      for (int jj = 0; jj < 3; jj++) cov_v[ii] += G.p.gcov[ii + 1][jj + 1] * P_mhd[jj + 1] / W;
+    Real vdH = 0.;
+    for (int ii = 0; ii < 3; ii++) vdH += P_mhd[ii + 1] / W * P_rad[ii + 1];
+    S[0] = alpha * sdetgam * (kappaJ * W * (JBB - P_rad[0]) - kappaH * vdH);
+    for (int ii = 0; ii < 3; ii++)
+      S[ii + 1] = alpha * sdetgam * (kappaJ * W * cov_v[ii] * (JBB - P_rad[0]) - kappaH * P_rad[1 + ii]);
+  }
+  // U_mhd, U_rad, P_rad and the source at P_mhd; the closure inversion's status
+  Status eval(const Real P_mhd[4], Real U_mhd[4], Real U_rad[4], Real P_rad[4], Real S[4]) const {
+    MHDConserved(P_mhd, U_mhd);
+    RadConserved(U_mhd, U_rad);
+    const Status st = RadPrimitive(P_mhd, U_rad, P_rad);
+    Source(P_mhd, P_rad, S);
+    return st;
+  }
+};
+
+// LinearAlgebra::matrixInverse4x4 (linear_algebra.hpp:90-147): the adjugate
+// from 3x3 minors (cofactor expansion), divided by the determinant expanded
+// along the first row.
+inline Real minor3(const Real m[16], int r0, int r1, int r2, int c0, int c1, int c2) {
+  return m[4 * r0 + c0] * (m[4 * r1 + c1] * m[4 * r2 + c2] - m[4 * r2 + c1] * m[4 * r1 + c2]) -
+         m[4 * r0 + c1] * (m[4 * r1 + c0] * m[4 * r2 + c2] - m[4 * r2 + c0] * m[4 * r1 + c2]) +
+         m[4 * r0 + c2] * (m[4 * r1 + c0] * m[4 * r2 + c1] - m[4 * r2 + c0] * m[4 * r1 + c1]);
+}
+void inverse4x4(const Real a[4][4], Real inv[4][4]) {
+  const Real *m = &a[0][0];
+  Real *o = &inv[0][0];
+  // column c of the adjugate holds the cofactors of row c
+  static const int R[4][3] = {{1, 2, 3}, {0, 2, 3}, {0, 1, 3}, {0, 1, 2}};
+  for (int col = 0; col < 4; col++)      // adjugate column = matrix row left out
+    for (int row = 0; row < 4; row++) {  // adjugate row = matrix column left out
+      const Real mn = minor3(m, R[col][0], R[col][1], R[col][2], R[row][0], R[row][1], R[row][2]);
+      o[4 * row + col] = ((row + col) % 2 == 0) ? mn : -mn;
+    }
+  const Real det = m[0] * minor3(m, 1, 2, 3, 1, 2, 3) - m[1] * minor3(m, 1, 2, 3, 0, 2, 3) +
+                   m[2] * minor3(m, 1, 2, 3, 0, 1, 3) - m[3] * minor3(m, 1, 2, 3, 0, 1, 2);
+  for (int i = 0; i < 16; i++) o[i] /= det;
+}
+
+// The fourd solver (moments_source.cpp:489-786): Newton's method over
+// P_mhd = (u, W v^i) for U_mhd(P) - U_mhd_0 + dt S = 0.  Each step: the
+// Jacobian from centred differences of step eps max(min_m |P_m| over the
+// nonzero P_m, |P_m|) (one-sided from the current guess when the closure
+// inversion fails at one support point, failure at both), the update
+// P -= J^-1 r, and after a failed inversion at the new guess the reference's
+// step rescaling (its factor test admits only factors >= 1).  Converged when
+// max_n |r_n| / max_n(|U_mhd_n| + |U_mhd_0,n| + |dt S_n|) <= tol; success
+// also needs finite U_rad and fewer than maxiter iterations.  dE, cov_dF (the
+// radiation's change, per sdetgam) are written only on success.
+bool fourd_zone(const RPar &rp, const phx_params &fp, const RBlk &R, const RGeo &G, long long id, Real dt, Real &dE,
+                V3 &cov_dF) {
+  const EOS eos{fp.gm1, fp.Cv};
+  const Real sdetgam = G.p.detgam;
+  const Real rho = R.fp(PHX_PRHO, id), ug = R.fp(PHX_PENG, id);
+  Real P[4] = {ug, R.fp(PHX_PVEL, id), R.fp(PHX_PVEL + 1, id), R.fp(PHX_PVEL + 2, id)};
+  SourceResidual4 srm{rp, eos, G, rho, sdetgam, G.p.alpha, {}, {}};
+  srm.MHDConserved(P, srm.U_mhd_0);
+  for (int n = 0; n < 4; n++) srm.U_rad_0[n] = R.U(PHX_RE + n, id);
+  const Real eps = rp.fd_eps, xi_max = rp.xi_ceiling;
+  Real U_mhd[4], U_rad[4], P_rad[4], dS[4], resid[4];
+  Status status = srm.eval(P, U_mhd, U_rad, P_rad, dS);
+  for (int n = 0; n < 4; n++) resid[n] = U_mhd[n] - srm.U_mhd_0[n] + dt * dS[n];
+  Real err = 1.e100;
+  int niter = 0;
+  bool bad_guess = false;
+  do {
+    Real jac[4][4] = {{0}};
+    Real mag_min = std::numeric_limits<Real>::max();
+    for (int m = 0; m < 4; m++)
+      if (std::fabs(P[m]) > 0.) mag_min = smin(mag_min, std::fabs(P[m]));
+    bool bad_m = false, bad_p = false;
+    for (int m = 0; m < 4; m++) {
+      Real Pm[4] = {P[0], P[1], P[2], P[3]}, Pp[4] = {P[0], P[1], P[2], P[3]};
+      const Real step = smax(eps * mag_min, eps * std::fabs(P[m]));
+      Pm[m] -= step;
+      Pp[m] += step;
+      Real Um[4], Urm[4], Prm[4], dSm[4], Up[4], Urp[4], Prp[4], dSp[4];
+      if (srm.eval(Pm, Um, Urm, Prm, dSm) == FAILURE) bad_m = true;
+      if (srm.eval(Pp, Up, Urp, Prp, dSp) == FAILURE) bad_p = true;
+      for (int n = 0; n < 4; n++) {
+        const Real fpl = Up[n] - srm.U_mhd_0[n] + dt * dSp[n];
+        const Real fmi = Um[n] - srm.U_mhd_0[n] + dt * dSm[n];
+        jac[n][m] = (fpl - fmi) / (Pp[m] - Pm[m]);
+      }
+    }
+    if (bad_m && bad_p) {
+      bad_guess = true;
+      break;
+    } else if (bad_m || bad_p) {  // one-sided from the guess, on the good side
+      const Real side = bad_m ? 1.0 : -1.0;
+      for (int m = 0; m < 4; m++) {
+        Real Ps[4] = {P[0], P[1], P[2], P[3]};
+        Ps[m] += side * smax(eps * mag_min, eps * std::fabs(Ps[m]));
+        Real Us[4], Urs[4], Prs[4], dSs[4];
+        srm.eval(Ps, Us, Urs, Prs, dSs);
+        for (int n = 0; n < 4; n++) {
+          const Real fs = Us[n] - srm.U_mhd_0[n] + dt * dSs[n];
+          const Real fg = U_mhd[n] - srm.U_mhd_0[n] + dt * dS[n];
+          jac[n][m] = bad_m ? (fs - fg) / (Ps[m] - P[m]) : (fg - fs) / (P[m] - Ps[m]);
+        }
+      }
+    }
+    Real jinv[4][4];
+    inverse4x4(jac, jinv);
+    if (!bad_guess) {
+      const Real ug0 = P[0], ur0 = P_rad[0];
+      for (int m = 0; m < 4; m++)
+        for (int n = 0; n < 4; n++) P[m] -= jinv[m][n] * resid[n];
+      status = srm.eval(P, U_mhd, U_rad, P_rad, dS);
+      if (status == FAILURE) bad_guess = true;
+      if (bad_guess) {
+        const V3 cov_H{{P_rad[1] / P_rad[0], P_rad[2] / P_rad[0], P_rad[3] / P_rad[0]}};
+        const V3 con_v{{P[1], P[2], P[3]}};
+        const Real J = P_rad[0];
+        Real hh, vh;
+        if (G.mink) {
+          hh = 0.0;
+          for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) hh += (a == b ? 1.0 : 0.0) * cov_H(a) * cov_H(b);
+        } else {
+          hh = G.g3.contract_cov(cov_H, cov_H);
+        }
+        vh = 0.0;
+        for (int a = 0; a < 3; a++) vh += con_v(a) * cov_H(a);
+        const Real xi = std::sqrt(hh - vh * vh) / J;  // std::pow(vh, 2) there
+        constexpr Real umin = 100. * SMALL, Jmin = 100. * SMALL;
+        Real scale = 0.;
+        if (xi > xi_max) scale = smax(scale, xi_max / xi);
+        if (P[0] < umin) scale = smax(scale, (ug0 - umin) / (ug0 - P[0]));
+        if (P_rad[0] < Jmin) scale = smax(scale, (ur0 - Jmin) / (ur0 - P_rad[0]));
+        if (!(scale > SMALL && scale >= 1.)) {  // the reference prints and gives up
+          bad_guess = true;
+          break;
+        }
+        scale *= 0.5;
+        for (int m = 0; m < 4; m++)
+          for (int n = 0; n < 4; n++) P[m] += (1. - scale) * jinv[m][n] * resid[n];
+        status = srm.eval(P, U_mhd, U_rad, P_rad, dS);
+        if (status == SUCCESS) bad_guess = false;
+      }
+    }
+    if (bad_guess) break;
+    for (int n = 0; n < 4; n++) {
+      resid[n] = U_mhd[n] - srm.U_mhd_0[n] + dt * dS[n];
+      if (std::isnan(resid[n])) {
+        bad_guess = true;
+        break;
+      }
+    }
+    if (bad_guess) break;
+    err = SMALL;
+    Real max_div = SMALL;
+    for (int n = 0; n < 4; n++)
+      max_div = smax(max_div, std::fabs(U_mhd[n]) + std::fabs(srm.U_mhd_0[n]) + std::fabs(dt * dS[n]));
+    for (int n = 0; n < 4; n++) {
+      const Real sub = std::fabs(resid[n]) / max_div;
+      if (sub > err) err = sub;
+    }
+    niter++;
+    if (niter == rp.maxiter) break;
+  } while (err > rp.tol);
+  if (niter == rp.maxiter || err > rp.tol || std::isnan(U_rad[0]) || std::isnan(U_rad[1]) ||
+      std::isnan(U_rad[2]) || std::isnan(U_rad[3]) || bad_guess)
+    return false;
+  dE = (U_rad[0] - R.U(PHX_RE, id)) / sdetgam;
+  for (int a = 0; a < 3; a++) cov_dF(a) = (U_rad[a + 1] - R.U(PHX_RF + a, id)) / sdetgam;
+  return true;
+}
+
+// MomentFluidSourceImpl, oned or fourd solver, one species
+// (moments_source.cpp:203-965); fp: the fluid inversion's settings
+// (update_fluid).  Returns 1 when the source update was applied.
 int fluid_source(const RPar &rp, const phx_params &fp, const RBlk &R, int k, int j, int i, Real dt) {
   const long long id = R.B.idx(k, j, i);
   const RGeo G(R, CENT, k, j, i);
@@ -3236,7 +3469,16 @@ int fluid_source(const RPar &rp, const phx_params &fp, const RBlk &R, int k, int
   Real dE = 0.0;
   V3 cov_dF{{0.0, 0.0, 0.0}};
   bool success = false;
-  {
+  bool oned = !rp.fourd;
+  if (rp.fourd) {
+    // fourd, falling back to the oned solver when it fails and
+    // src_use_oned_backup is set (the reference's goto, :781-785); without
+    // the fallback a failed zone keeps dE = cov_dF = 0 (left uninitialised
+    // there) for the fluid update
+    success = fourd_zone(rp, fp, R, G, id, dt, dE, cov_dF);
+    oned = !success && rp.oned_backup;
+  }
+  if (oned) {
     const Real J0 = R.Q(PHX_RJ, id);
     const Real dtau = alpha * dt / W;
     RF root(rp.maxiter);

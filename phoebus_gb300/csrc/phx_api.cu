@@ -109,6 +109,7 @@ phx::Par make_par(const phx_params &p) {
   d.c2p_fixup = p.enable_c2p_fixup;
   d.strategy_floors = p.c2p_failure_strategy_floors;
   d.vsq_max = 1.0 - 1.0 / (d.g0 * d.g0);
+  d.iCv = 1.0 / p.Cv;
   d.fix_flux = p.enable_flux_fixup ? 1 : 0;
   d.inflow_check = p.enable_ox1_fmks_inflow_check ? 1 : 0;
   return d;
@@ -1031,6 +1032,8 @@ phx_status check_rad(const phx_rad_params *rp, const phx_params *p, const phx_bl
   if (rp->oned_fixup_strategy < PHX_RAD_ONED_FIXUP_NONE || rp->oned_fixup_strategy > PHX_RAD_ONED_FIXUP_IGNORE_ALL)
     return fail(PHX_ERR_INVALID_ARG, "radiation/oned_fixup_strategy has an invalid entry!");
   if (rp->src_rootfind_maxiter < 0) return fail(PHX_ERR_INVALID_ARG, "src_rootfind_maxiter < 0");
+  if (rp->src_solver != PHX_RAD_SRC_ONED && rp->src_solver != PHX_RAD_SRC_FOURD)
+    return fail(PHX_ERR_INVALID_ARG, "\"radiation/src_solver\" option unrecognized!");
   if (p == nullptr) return fail(PHX_ERR_INVALID_ARG, "params is NULL");
   return PHX_OK;
 }
@@ -1046,6 +1049,9 @@ phx::rad::RPar make_rpar(const phx_rad_params &rp, const phx_params &p) {
   r.oned_fixup = rp.oned_fixup_strategy;
   r.update_fluid = rp.update_fluid != 0;
   r.rad_fixup_floors = rp.rad_c2p_failure_floors != 0;
+  r.fourd = rp.src_solver == PHX_RAD_SRC_FOURD;
+  r.oned_backup = rp.src_use_oned_backup != 0;
+  r.fd_eps = rp.src_rootfind_eps;
   r.cfl = rp.cfl;
   r.tol = rp.src_rootfind_tol;
   r.kappa_a = rp.kappa_a;
@@ -1133,6 +1139,9 @@ void phx_rad_params_default(phx_rad_params *p) {
   p->oned_fixup_strategy = PHX_RAD_ONED_FIXUP_NONE;
   p->xi0_ceiling = 0.99;
   p->tau0_ceiling = 1.e3;
+  p->src_solver = PHX_RAD_SRC_ONED;  // radiation/src_solver "oned" (radiation.cpp:403-404)
+  p->src_rootfind_eps = 1.e-8;       // radiation/src_rootfind_eps (radiation.cpp:421)
+  p->src_use_oned_backup = 0;        // radiation/src_use_oned_backup (radiation.cpp:417-418)
 }
 
 phx_status phx_rad_prim_to_con(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_block *fb,

@@ -95,6 +95,8 @@ struct BatchPlan {
   // device state (one allocation for the tables)
   void *mem = nullptr;
   BView *views_in = nullptr, *views_out = nullptr;
+  CUtensorMap *x1_maps = nullptr;  // per block: X1 tensor map (64-byte aligned) and staging mode
+  int *x1_modes = nullptr;
   const double **base_tab = nullptr;
   double **out_tab = nullptr;
   double *beta_dt = nullptr;
@@ -163,8 +165,9 @@ static std::vector<WorkItem> x1_items(const std::vector<BView> &v, int x1_cells,
   for (size_t b = 0; b < v.size(); b++) {
     int pen = (x1_cells + v[b].n1t / 2) / v[b].n1t;
     pen = std::max(1, std::min(32, pen));
-    while (pen > 1 && (size_t)pen * kReconLoad * v[b].n1t * sizeof(double) > 200 * 1024) pen--;
-    smem = std::max(smem, (size_t)pen * kReconLoad * v[b].n1t * sizeof(double));
+    const size_t pst = (size_t)x1_pencil_stride_host(v[b]) * sizeof(double);
+    while (pen > 1 && (size_t)pen * pst > 200 * 1024) pen--;
+    smem = std::max(smem, (size_t)pen * pst);
     const int np = x1_npencil(v[b]);
     for (int f = 0; f < np; f += pen) items.push_back(WorkItem{(int)b, 0, f, std::min(f + pen, np)});
   }
@@ -207,7 +210,12 @@ static Tuning autotune(BatchPlan &pl, const std::vector<BView> &v, unsigned int 
     PhaseList ph;
     if (upload_items(pl, ph, items) != cudaSuccess) break;
     const float ms = time_launch(
-        s, [&] { launch_flux_x1_batched(pl.par, pl.mink, pl.views_in, ph.d_items, ph.n, 0, smem, err, s); }, 3);
+        s,
+        [&] {
+          launch_flux_x1_batched(pl.par, pl.mink, pl.views_in, ph.d_items, ph.n, 0, smem, pl.x1_maps, pl.x1_modes,
+                                 err, s);
+        },
+        3);
     if (ms < best_ms) {
       best_ms = ms;
       best.x1_cells = cells;
@@ -279,7 +287,7 @@ static void stage_launches(BatchPlan &pl, DevStats *stats, unsigned int *err, cu
   }
   each(pl.sources, [&](const WorkItem *it, int n, int g) { launch_sources_batched(p, pl.mink, pl.views_in, it, n, g, s); });
   each(pl.x1, [&](const WorkItem *it, int n, int g) {
-    launch_flux_x1_batched(p, pl.mink, pl.views_in, it, n, g, pl.x1_smem, err, s);
+    launch_flux_x1_batched(p, pl.mink, pl.views_in, it, n, g, pl.x1_smem, pl.x1_maps, pl.x1_modes, err, s);
   });
   if (pl.ndim >= 2)
     each(pl.x2, [&](const WorkItem *it, int n, int g) {
@@ -480,7 +488,8 @@ cudaError_t batch_stage(BatchCache *cache, const Par &par, const phx_block *bloc
     P.ndim = views[0].ndim;
     std::vector<BView> vin(views, views + n), vout(views, views + n);
     for (int i = 0; i < n; i++) vout[i].cons = out[i];
-    const size_t bytes = 2 * sizeof(BView) * n + 2 * sizeof(double *) * n + 2 * sizeof(double) + 256 * 8;
+    const size_t bytes = 2 * sizeof(BView) * n + 2 * sizeof(double *) * n + 2 * sizeof(double) +
+                         sizeof(CUtensorMap) * n + sizeof(int) * n + 256 * 10;
     if ((e = cudaMalloc(&P.mem, bytes)) != cudaSuccess) return e;
     char *m = static_cast<char *>(P.mem);
     auto take = [&](size_t b) {
@@ -493,6 +502,18 @@ cudaError_t batch_stage(BatchCache *cache, const Par &par, const phx_block *bloc
     P.base_tab = reinterpret_cast<const double **>(take(sizeof(double *) * n));
     P.out_tab = reinterpret_cast<double **>(take(sizeof(double *) * n));
     P.beta_dt = reinterpret_cast<double *>(take(2 * sizeof(double)));
+    P.x1_maps = reinterpret_cast<CUtensorMap *>(take(sizeof(CUtensorMap) * n));
+    P.x1_modes = reinterpret_cast<int *>(take(sizeof(int) * n));
+    {
+      std::vector<CUtensorMap> maps(n);
+      std::vector<int> modes(n);
+      for (int i = 0; i < n; i++) {
+        memset(&maps[i], 0, sizeof(CUtensorMap));
+        modes[i] = x1_mode(vin[i], &maps[i]);
+      }
+      cudaMemcpy(P.x1_maps, maps.data(), sizeof(CUtensorMap) * n, cudaMemcpyHostToDevice);
+      cudaMemcpy(P.x1_modes, modes.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
+    }
     cudaMemcpy(P.views_in, vin.data(), sizeof(BView) * n, cudaMemcpyHostToDevice);
     cudaMemcpy(P.views_out, vout.data(), sizeof(BView) * n, cudaMemcpyHostToDevice);
     cudaMemcpy(P.base_tab, base, sizeof(double *) * n, cudaMemcpyHostToDevice);

@@ -490,7 +490,15 @@ __device__ __forceinline__ void c2p_finish(const Par &p, const Pt &g, Residual &
   eng *= prim[PHX_PRHO];
   prim[PHX_PENG] = eng;
   prim[PHX_PPRS] = eos_P_rho_T(p, prim[PHX_PRHO], prim[PHX_PTMP]);
+#ifdef PHX_EXACT
   prim[PHX_PGM1] = div_p(eos_bmod_rho_T(p, prim[PHX_PRHO], prim[PHX_PTMP]), prim[PHX_PPRS]);
+#else
+  // production build: bmod / P of the ideal gas is Gamma wherever P > 0 (the
+  // quotient, NaN for P = 0, elsewhere)
+  prim[PHX_PGM1] = prim[PHX_PPRS] > 0.0
+                       ? p.gm1 + 1.0
+                       : div_p(eos_bmod_rho_T(p, prim[PHX_PRHO], prim[PHX_PTMP]), prim[PHX_PPRS]);
+#endif
   double vel[3];
 #pragma unroll
   for (int ii = 0; ii < 3; ii++) {

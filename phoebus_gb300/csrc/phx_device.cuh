@@ -148,6 +148,7 @@ struct Par {
   double cfl;
   int c2p_fixup, strategy_floors, enable_floors, enable_mhd_floors;
   double vsq_max;  // 1 - 1 / g0^2 (the gamma ceiling as a v^2 bound)
+  double iCv;      // 1 / Cv, formed on the host (production-build temperature)
   int fix_flux;      // fixup/enable_flux_fixup
   int inflow_check;  // fixup/enable_ox1_fmks_inflow_check
 };
@@ -165,13 +166,20 @@ __device__ __forceinline__ double eos_P_rho_sie(const Par &p, double rho, double
   return fmax(0.0, p.gm1 * rho * sie);
 }
 __device__ __forceinline__ double eos_T_rho_sie(const Par &p, double rho, double sie) {
+#ifdef PHX_EXACT
   return fmax(0.0, div_p(sie, p.Cv));
+#else
+  return fmax(0.0, sie * p.iCv);  // production build: the host's 1/Cv
+#endif
 }
 __device__ __forceinline__ double eos_P_rho_T(const Par &p, double rho, double T) {
   return fmax(0.0, p.gm1 * rho * p.Cv * T);
 }
 __device__ __forceinline__ double eos_bmod_rho_T(const Par &p, double rho, double T) {
   return fmax(0.0, (p.gm1 + 1) * p.gm1 * rho * p.Cv * T);
+}
+__device__ __forceinline__ double eos_bmod_rho_sie(const Par &p, double rho, double sie) {
+  return fmax(0.0, p.gm1 * (p.gm1 + 1) * rho * sie);
 }
 
 // ------------------------------------------------------- fixup.hpp Bounds
@@ -366,15 +374,39 @@ __device__ __forceinline__ void signal_speeds(double rho, double u, double p, do
                                               const double v[3], double vsq, double gam1,
                                               const Pt &g, double *sig) {
   const double rho_rel = rho + u + p;
+#ifdef PHX_EXACT
   const double vasq = div_p(bsq, rho_rel + bsq);
   double cssq = div_p(gam1 * p, rho_rel);
+#else
+  // production build: one reciprocal of the product of the two denominators
+  // where it is normal
+  double vasq, cssq;
+  const double dAB = (rho_rel + bsq) * rho_rel;
+  const int eAB = dexp(dAB);
+  if (eAB >= 16 && eAB <= 2030) {
+    const double rAB = rcp_nr(dAB);
+    vasq = bsq * (rho_rel * rAB);
+    cssq = gam1 * p * ((rho_rel + bsq) * rAB);
+  } else {
+    vasq = div_p(bsq, rho_rel + bsq);
+    cssq = div_p(gam1 * p, rho_rel);
+  }
+#endif
   cssq += vasq - cssq * vasq;
   const double alpha = MINK ? 1.0 : g.alpha;
   const double vcoff = div_p(alpha, 1.0 - vsq * cssq);
 #pragma unroll
   for (int m = 0; m < 3; m++) {
     const double gmm = MINK ? 1.0 : g.gamcon[m][m];
+#ifdef PHX_EXACT
     const double vpm = sqrt(cssq * (1.0 - vsq) * (gmm * (1.0 - vsq * cssq) - v[m] * v[m] * (1.0 - cssq)));
+#else
+    // production build: sqrt(x) as x rsqrt(x) for normal x > 0 (zero, negative
+    // and extreme arguments take the IEEE square root)
+    const double vpm_sq = cssq * (1.0 - vsq) * (gmm * (1.0 - vsq * cssq) - v[m] * v[m] * (1.0 - cssq));
+    const int ev = dexp(vpm_sq);
+    const double vpm = (vpm_sq > 0.0 && ev >= 16 && ev <= 2030) ? vpm_sq * rsqrt_nr(vpm_sq) : sqrt(vpm_sq);
+#endif
     double vp = vcoff * (v[m] * (1.0 - cssq) + vpm);
     double vm = vcoff * (v[m] * (1.0 - cssq) - vpm);
     if constexpr (!MINK) {

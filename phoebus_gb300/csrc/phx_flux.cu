@@ -4,16 +4,26 @@
 // The reference reconstructs every variable into ql/qr arrays (K1) and then
 // solves one Riemann problem per face (K2).  Here each face's two states are
 // produced and consumed in registers:
-//   X1: a CTA stages four (k, j) pencils' 10 primitive rows in shared memory
-//       with cp.async.bulk (TMA bulk copies completing on an mbarrier); lanes
-//       reconstruct consecutive cells and the left state of face i (the
-//       upper-face value of cell i-1) moves to lane i with __shfl_up_sync.
+//   X1: a CTA stages four (k, j) pencils' reconstructed primitive rows in
+//       shared memory with one tiled TMA copy per pencil
+//       (cp.async.bulk.tensor through a 5-D tensor map of the primitive
+//       array: i split in S rows of n1t/S, j, k, variable), completing on an
+//       mbarrier (1-D cp.async.bulk per row, or plain loads, where the block
+//       shape does not admit the map); lanes reconstruct consecutive cells and
+//       the left state of face i (the upper-face value of cell i-1) moves to
+//       lane i with __shfl_up_sync.
 //   X2, X3: a thread sweeps a segment of faces along the direction with the
 //       5-point stencil window and the previous cell's upper-face state held
 //       in registers; consecutive lanes are consecutive i (coalesced).
 // Faces computed, per direction d: along d [s, e+1]; transverse active
 // directions [s-1, e+1].  These are all the faces FluxDivergence, FluxCT and
 // EstimateTimestep read.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <cstdlib>
+#include <cstring>
+
 #include "phx_kernels.cuh"
 #include "phx_bulk.cuh"
 
@@ -117,15 +127,47 @@ __host__ __device__ __forceinline__ X1Range x1_range(const BView &b) {
 __host__ __device__ __forceinline__ bool x1_tma_ok(const BView &b) {
   return (b.n1t % 2 == 0) && (b.vs % 2 == 0) && ((reinterpret_cast<uintptr_t>(b.prim) & 15) == 0);
 }
+// Staging modes of the X1 kernels.
+enum X1Mode { X1_LOADS = 0, X1_BULK = 1, X1_TENSOR = 2 };
 
-// Stage pencils p0 .. p0+np-1 into rows (mbarrier phase parity `phase` when
-// use_tma).  Returns false, with ERR_TIMEOUT set, when the bounded wait gave
-// up; every thread returns the same value.
-__device__ __forceinline__ bool x1_stage(const BView &b, const X1Range &xr, int p0, int np, bool use_tma,
-                                         double *rows, uint64_t *bar, unsigned phase, unsigned int *err) {
+// Shared-memory doubles per staged pencil: its kReconLoad rows of n1t,
+// rounded up to 128 bytes (the alignment of a tiled TMA destination).
+__host__ __device__ __forceinline__ long long x1_pencil_stride(const BView &b) {
+  return ((long long)kReconLoad * b.n1t + 15) / 16 * 16;
+}
+
+// One tiled TMA copy: box {n1t/S, S, 1, 1, kReconLoad} of the 5-D map at
+// (0, 0, j, k, 0) -> a pencil's kReconLoad rows, contiguous in shared memory.
+__device__ __forceinline__ void tensor_g2s_5d(void *dst, const CUtensorMap *map, int j, int k, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+      "%5, %6}], [%7];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(0), "r"(j), "r"(k), "r"(0), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Stage pencils p0 .. p0+np-1 into rows (pencil pp at rows + pp * pencil
+// stride; mbarrier phase parity `phase` for the TMA modes).  Returns false,
+// with ERR_TIMEOUT set, when the bounded wait gave up; every thread returns
+// the same value.
+__device__ __forceinline__ bool x1_stage(const BView &b, const X1Range &xr, int p0, int np, int mode,
+                                         const CUtensorMap *map, double *rows, uint64_t *bar, unsigned phase,
+                                         unsigned int *err) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n1t = b.n1t;
-  if (use_tma) {
+  const long long pst = x1_pencil_stride(b);
+  if (mode == X1_TENSOR && (smem_u32(rows) & 127u) != 0) mode = X1_BULK;  // tiled TMA wants 128-byte rows
+  if (mode == X1_TENSOR) {
+    if (threadIdx.x == 0) {
+      mbar_expect_tx(bar, (unsigned)(n1t * sizeof(double)) * kReconLoad * np);
+      for (int pp = 0; pp < np; pp++) {
+        const int pen = p0 + pp;
+        tensor_g2s_5d(rows + pp * pst, map, xr.jlo + pen % xr.nj, xr.klo + pen / xr.nj, bar);
+      }
+    }
+    return mbar_wait_block(bar, phase, MBAR_SPIN_LIMIT, err);
+  }
+  if (mode == X1_BULK) {
     const unsigned bytes = (unsigned)(n1t * sizeof(double));
     if (threadIdx.x == 0) mbar_expect_tx(bar, bytes * kReconLoad * np);
     __syncthreads();
@@ -135,7 +177,7 @@ __device__ __forceinline__ bool x1_stage(const BView &b, const X1Range &xr, int 
       const int pp = r / kReconLoad, v = r % kReconLoad;
       const int pen = p0 + pp;
       const long long base = b.idx(xr.klo + pen / xr.nj, xr.jlo + pen % xr.nj, 0);
-      bulk_g2s(rows + (long long)r * n1t, b.prim + v * b.vs + base, bytes, bar);
+      bulk_g2s(rows + pp * pst + (long long)v * n1t, b.prim + v * b.vs + base, bytes, bar);
     }
     return mbar_wait_block(bar, phase, MBAR_SPIN_LIMIT, err);
   }
@@ -143,7 +185,7 @@ __device__ __forceinline__ bool x1_stage(const BView &b, const X1Range &xr, int 
     const int pp = r / kReconLoad, v = r % kReconLoad;
     const int pen = p0 + pp;
     const long long base = b.idx(xr.klo + pen / xr.nj, xr.jlo + pen % xr.nj, 0);
-    for (int i = lane; i < n1t; i += 32) rows[(long long)r * n1t + i] = b.prim[v * b.vs + base + i];
+    for (int i = lane; i < n1t; i += 32) rows[pp * pst + (long long)v * n1t + i] = b.prim[v * b.vs + base + i];
   }
   __syncthreads();
   return true;
@@ -164,7 +206,7 @@ __device__ __forceinline__ void x1_compute(const Par &p, const BView &b, const X
     const bool have = slot < nslot;
     const int pp = have ? slot / ncell : 0;
     const int c = c0 + (have ? slot % ncell : 0);
-    const double *prow = rows + (long long)pp * kReconLoad * n1t;
+    const double *prow = rows + pp * x1_pencil_stride(b);
     double ql[PHX_NRECON], qr[PHX_NRECON];
 #pragma unroll
     for (int v = 0; v < kReconLoad; v++) {
@@ -193,27 +235,30 @@ __device__ __forceinline__ void x1_compute(const Par &p, const BView &b, const X
 }
 
 template <int RECON, bool MINK>
-__global__ void __launch_bounds__(32 * X1_WARPS) k_flux_x1(Par p, BView b, int use_tma, unsigned int *err) {
+__global__ void __launch_bounds__(32 * X1_WARPS)
+    k_flux_x1(Par p, BView b, int mode, const __grid_constant__ CUtensorMap map, unsigned int *err) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar;
   double *rows = reinterpret_cast<double *>(smem_raw);
   const X1Range xr = x1_range(b);
   const int p0 = blockIdx.x * X1_PENCILS;
   const int np = min(X1_PENCILS, xr.npencil - p0);
-  if (use_tma && threadIdx.x == 0) {
+  if (mode != X1_LOADS && threadIdx.x == 0) {
     mbar_init(&bar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  if (!x1_stage(b, xr, p0, np, use_tma != 0, rows, &bar, 0u, err)) return;
+  if (!x1_stage(b, xr, p0, np, mode, &map, rows, &bar, 0u, err)) return;
   x1_compute<RECON, MINK>(p, b, xr, p0, np, rows);
 }
 
 // Batched X1: a persistent CTA walks the work list; item = (block, first
 // pencil, pencil count).  The mbarrier is reused with alternating phase.
+// maps[b] / modes[b]: block b's tensor map and staging mode.
 template <int RECON, bool MINK>
 __global__ void __launch_bounds__(32 * X1_WARPS) kb_flux_x1(Par p, const BView *views, const WorkItem *items,
-                                                            int nitems, unsigned int *err) {
+                                                            int nitems, const CUtensorMap *maps, const int *modes,
+                                                            unsigned int *err) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar;
   double *rows = reinterpret_cast<double *>(smem_raw);
@@ -227,12 +272,64 @@ __global__ void __launch_bounds__(32 * X1_WARPS) kb_flux_x1(Par p, const BView *
     const WorkItem w = items[it];
     const BView &b = views[w.block];
     const X1Range xr = x1_range(b);
-    const bool tma = x1_tma_ok(b);
-    if (!x1_stage(b, xr, (int)w.first, (int)(w.last - w.first), tma, rows, &bar, phase, err)) return;
-    if (tma) phase ^= 1u;
+    const int mode = modes[w.block];
+    if (!x1_stage(b, xr, (int)w.first, (int)(w.last - w.first), mode, maps + w.block, rows, &bar, phase, err))
+      return;
+    if (mode != X1_LOADS) phase ^= 1u;
     x1_compute<RECON, MINK>(p, b, xr, (int)w.first, (int)(w.last - w.first), rows);
     __syncthreads();  // rows are rewritten by the next item
   }
+}
+
+// ------------------------------------------------------ X1 tensor maps
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library).
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  }
+  return fn;
+}
+
+// The 5-D map of a block's reconstructed primitive planes: dimensions
+// (n1t / S, S, n2t, n3t, kReconLoad) with byte strides (8, 8 n1t / S, 8 n1t,
+// 8 n1t n2t, 8 vs), box (n1t / S, S, 1, 1, kReconLoad): one copy moves one
+// (k, j) pencil's rows.  S is the smallest split with n1t / S <= 256 (the
+// box limit) and n1t / S even (16-byte rows).  False (mode falls back) when
+// no split fits, the strides are not multiples of 16 bytes, the base is not
+// 16-byte aligned, or the encode is refused.
+bool x1_encode_map(const BView &b, CUtensorMap *map) {
+  if (!x1_tma_ok(b)) return false;
+  int S = 0;
+  for (int s = 1; s <= 8 && !S; s++)
+    if (b.n1t % s == 0 && (b.n1t / s) % 2 == 0 && b.n1t / s <= 256) S = s;
+  if (!S) return false;
+  PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
+  if (!fn) return false;
+  const cuuint64_t h = (cuuint64_t)(b.n1t / S);
+  const cuuint64_t dim[5] = {h, (cuuint64_t)S, (cuuint64_t)b.n2t, (cuuint64_t)b.n3t, (cuuint64_t)kReconLoad};
+  const cuuint64_t stride[4] = {h * 8, (cuuint64_t)b.n1t * 8, (cuuint64_t)b.n1t * b.n2t * 8, (cuuint64_t)b.vs * 8};
+  const cuuint32_t box[5] = {(cuuint32_t)h, (cuuint32_t)S, 1, 1, (cuuint32_t)kReconLoad};
+  const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 5, b.prim, dim, stride, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+// PHX_X1_STAGING=loads or =bulk in the environment forces a simpler mode
+// (read at every call; the three modes give identical fluxes).
+int x1_mode(const BView &b, CUtensorMap *map) {
+  const char *force = getenv("PHX_X1_STAGING");
+  if (force && strcmp(force, "loads") == 0) return X1_LOADS;
+  if (!(force && strcmp(force, "bulk") == 0) && x1_encode_map(b, map)) return X1_TENSOR;
+  return x1_tma_ok(b) ? X1_BULK : X1_LOADS;
 }
 
 // The failure path of the bounded waits above, driven on purpose: one CTA
@@ -401,12 +498,14 @@ static void launch_fluxes_t(const Par &p, const BView &b, unsigned int *err, cud
   {
     const X1Range xr = x1_range(b);
     const int jlo = xr.jlo, nj = xr.nj, klo = xr.klo, nk = xr.npencil / xr.nj;
-    const size_t smem = (size_t)X1_PENCILS * kReconLoad * b.n1t * sizeof(double);
+    const size_t smem = (size_t)X1_PENCILS * x1_pencil_stride(b) * sizeof(double);
     if (smem <= 200 * 1024) {
       auto kern = k_flux_x1<RECON, MINK>;
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      kern<<<(xr.npencil + X1_PENCILS - 1) / X1_PENCILS, 32 * X1_WARPS, smem, s>>>(p, b, x1_tma_ok(b) ? 1 : 0,
-                                                                                   err);
+      CUtensorMap map;
+      memset(&map, 0, sizeof(map));
+      const int mode = x1_mode(b, &map);
+      kern<<<(xr.npencil + X1_PENCILS - 1) / X1_PENCILS, 32 * X1_WARPS, smem, s>>>(p, b, mode, map, err);
     } else {
       launch_sweep<RECON, MINK, 0>(p, b, jlo, nj, klo, nk, is, ie - is + 2, s);
     }
@@ -444,6 +543,7 @@ void launch_fluxes_err(const Par &p, const BView &b, unsigned int *err, cudaStre
 // ------------------------------------------------------------- batched
 int x1_npencil(const BView &b) { return x1_range(b).npencil; }
 bool x1_tma_ok_host(const BView &b) { return x1_tma_ok(b); }
+long long x1_pencil_stride_host(const BView &b) { return x1_pencil_stride(b); }
 long long sweep_threads(const BView &b, int dir, int seg_target) {
   const SweepRange r = sweep_range(b, dir, seg_target);
   return (long long)r.na * r.nc * r.nseg;
@@ -460,11 +560,11 @@ static void x1_prepare_t(size_t smem) {
 
 template <int RECON, bool MINK>
 static void x1_batched_t(const Par &p, const BView *views, const WorkItem *items, int nitems, int grid, size_t smem,
-                         unsigned int *err, cudaStream_t s) {
+                         const CUtensorMap *maps, const int *modes, unsigned int *err, cudaStream_t s) {
   auto kern = kb_flux_x1<RECON, MINK>;
   x1_prepare_t<RECON, MINK>(smem);
-  kern<<<persistent_grid(kern, 32 * X1_WARPS, smem, nitems, grid), 32 * X1_WARPS, smem, s>>>(p, views, items,
-                                                                                             nitems, err);
+  kern<<<persistent_grid(kern, 32 * X1_WARPS, smem, nitems, grid), 32 * X1_WARPS, smem, s>>>(
+      p, views, items, nitems, maps, modes, err);
 }
 
 template <int RECON, bool MINK>
@@ -495,9 +595,10 @@ static void sweep_batched_t(const Par &p, int dir, const BView *views, const Wor
   }
 
 void launch_flux_x1_batched(const Par &p, bool mink, const BView *views, const WorkItem *items, int nitems, int grid,
-                            size_t smem, unsigned int *err, cudaStream_t s) {
+                            size_t smem, const CUtensorMap *maps, const int *modes, unsigned int *err,
+                            cudaStream_t s) {
   if (nitems <= 0) return;
-  PHX_RECON_DISPATCH(x1_batched_t, p, views, items, nitems, grid, smem, err, s)
+  PHX_RECON_DISPATCH(x1_batched_t, p, views, items, nitems, grid, smem, maps, modes, err, s)
 }
 
 void prepare_flux_x1_batched(const Par &p, bool mink, size_t smem) {

@@ -1,5 +1,7 @@
 // phx_kernels.cuh -- kernel declarations shared by the translation units.
 #pragma once
+#include <cuda.h>  // CUtensorMap (the type only; the encode goes through the runtime)
+
 #include "phx_c2p.cuh"
 
 namespace phx {
@@ -162,8 +164,10 @@ void launch_c2p_batched(const Par &p, bool mink, const BView *views, const WorkI
 // prim2con over the outer-X1 ghost slabs; items over ng * n2t * n3t zones.
 void launch_ox1_inflow(const Par &p, const BView *views, const WorkItem *items, int nitems, int grid,
                        unsigned int *err, cudaStream_t s);
+// maps / modes: per block, the X1 tensor map and staging mode from x1_mode
 void launch_flux_x1_batched(const Par &p, bool mink, const BView *views, const WorkItem *items, int nitems, int grid,
-                            size_t smem, unsigned int *err, cudaStream_t s);
+                            size_t smem, const CUtensorMap *maps, const int *modes, unsigned int *err,
+                            cudaStream_t s);
 void prepare_flux_x1_batched(const Par &p, bool mink, size_t smem);
 void launch_flux_sweep_batched(const Par &p, bool mink, int dir, const BView *views, const WorkItem *items,
                                int nitems, int grid, int seg_target, cudaStream_t s);
@@ -174,5 +178,10 @@ void launch_floors_batched(const Par &p, bool mink, const BView *views, const Wo
 int x1_npencil(const BView &b);
 long long sweep_threads(const BView &b, int dir, int seg_target);
 bool x1_tma_ok_host(const BView &b);
+// Shared-memory doubles per staged X1 pencil (rows rounded up to 128 bytes).
+long long x1_pencil_stride_host(const BView &b);
+// X1 staging mode of a block: 2 tiled TMA through *map (encoded here), 1
+// 1-D bulk copies, 0 plain loads.
+int x1_mode(const BView &b, CUtensorMap *map);
 
 }  // namespace phx

@@ -1293,6 +1293,240 @@ __device__ void source_update_fluid(const Par &fp, const BView &b, const RView &
   for (int a = 0; a < 3; a++) r.cons[(PHX_RF + a) * vs + id] = F.d[a] * sdetgam;
 }
 
+// ------------------------------------------------------ fourd solver
+// moments_source.cpp:39-150 (SourceResidual4) and :489-786 for one zone:
+// Newton's method over the fluid's P = (u, W v^i) for
+// U_mhd(P) - U_mhd_0 + dt S(P, P_rad) = 0, where the radiation takes up what
+// the fluid loses (U_rad = U_rad_0 - (U_mhd - U_mhd_0)) and P_rad = (J, H_i)
+// is its closure inversion with the guess's velocity.  As in the reference:
+// the fluid enters prim2con with B = 0 (the B primitives are declared a
+// second time in an inner block there and never reach the solver); kappaH is
+// the absorption coefficient taken twice, both capped at 1e5; the closure
+// solve starts from xi = 0.5 (SolveClosure's default; the reference passes
+// an uninitialised local).
+template <bool M1, bool MINK>
+struct SrcRes4 {
+  const RPar &p;
+  const Par &fp;
+  const RGeo<MINK> &G;
+  double rho, sdetgam, alpha;
+  double U0[4], R0[4];  // U_mhd_0, U_rad_0
+  __device__ __forceinline__ void mhd_cons(const double P[4], double U[4]) const {
+    const double Pg = eos_P_rho_sie(fp, rho, div_p(P[0], rho));
+    const double gam1 = div_p(eos_bmod_rho_sie(fp, rho, div_p(P[0], rho)), Pg);
+    const double bp[3] = {0.0, 0.0, 0.0};
+    double D, bc[3];
+    p2c<MINK>(rho, &P[1], bp, P[0], Pg, gam1, G.p, sdetgam, D, &U[1], bc, U[0], nullptr);
+  }
+  __device__ __forceinline__ double W_of(const double P[4]) const {
+    double W = 0.;
+#pragma unroll
+    for (int ii = 0; ii < 3; ii++)
+#pragma unroll
+      for (int jj = 0; jj < 3; jj++) W += G.cov(ii, jj) * P[ii + 1] * P[jj + 1];
+    return sqrt(1. + W);
+  }
+  // U_mhd, U_rad, P_rad and the source at P; the closure inversion's status
+  __device__ __forceinline__ int eval(const double P[4], double U[4], double Ur[4], double Pr[4], double S[4]) const {
+    mhd_cons(P, U);
+#pragma unroll
+    for (int n = 0; n < 4; n++) Ur[n] = R0[n] - (U[n] - U0[n]);
+    const double E = div_p(Ur[0], sdetgam);
+    V3 F;
+#pragma unroll
+    for (int a = 0; a < 3; a++) F.d[a] = div_p(Ur[a + 1], sdetgam);
+    const double W = W_of(P);
+    V3 cv;
+#pragma unroll
+    for (int a = 0; a < 3; a++) cv.d[a] = div_p(P[a + 1], W);
+    const Closure<M1, MINK> c(cv, true, G.geo());
+    double xi = 0.5, phi = PI;
+    T2 Pi;
+    c.tilpi_from_con(E, F, xi, phi, Pi);
+    V3 H;
+    const int st = c.con2prim(E, F, Pi, Pr[0], H);
+#pragma unroll
+    for (int a = 0; a < 3; a++) Pr[a + 1] = H.d[a];
+    // CalculateSource
+    const double Tg = eos_T_rho_sie(fp, rho, div_p(P[0], rho));
+    const double JBB = p.jbb * (Tg * Tg) * (Tg * Tg);
+    double kappaJ = rho * p.kappa_a;
+    double kappaH = kappaJ + rho * p.kappa_a;
+    kappaH = smin(kappaH, 1.e5);
+    kappaJ = smin(kappaJ, 1.e5);
+    double cov_v[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int ii = 0; ii < 3; ii++)
+#pragma unroll
+      for (int jj = 0; jj < 3; jj++) cov_v[ii] += div_p(G.cov(ii, jj) * P[jj + 1], W);
+    double vdH = 0.;
+#pragma unroll
+    for (int ii = 0; ii < 3; ii++) vdH += div_p(P[ii + 1], W) * Pr[ii + 1];
+    S[0] = alpha * sdetgam * (kappaJ * W * (JBB - Pr[0]) - kappaH * vdH);
+#pragma unroll
+    for (int ii = 0; ii < 3; ii++)
+      S[ii + 1] = alpha * sdetgam * (kappaJ * W * cov_v[ii] * (JBB - Pr[0]) - kappaH * Pr[1 + ii]);
+    return st;
+  }
+};
+
+// LinearAlgebra::matrixInverse4x4 (linear_algebra.hpp:90-147): the adjugate
+// from 3x3 minors over the determinant expanded along the first row.
+__device__ __forceinline__ double minor3(const double m[16], int r0, int r1, int r2, int c0, int c1, int c2) {
+  return m[4 * r0 + c0] * (m[4 * r1 + c1] * m[4 * r2 + c2] - m[4 * r2 + c1] * m[4 * r1 + c2]) -
+         m[4 * r0 + c1] * (m[4 * r1 + c0] * m[4 * r2 + c2] - m[4 * r2 + c0] * m[4 * r1 + c2]) +
+         m[4 * r0 + c2] * (m[4 * r1 + c0] * m[4 * r2 + c1] - m[4 * r2 + c0] * m[4 * r1 + c1]);
+}
+__device__ __forceinline__ void inverse4x4(const double a[4][4], double inv[4][4]) {
+  const double *m = &a[0][0];
+  double *o = &inv[0][0];
+  const int R[4][3] = {{1, 2, 3}, {0, 2, 3}, {0, 1, 3}, {0, 1, 2}};
+#pragma unroll
+  for (int col = 0; col < 4; col++)
+#pragma unroll
+    for (int row = 0; row < 4; row++) {
+      const double mn = minor3(m, R[col][0], R[col][1], R[col][2], R[row][0], R[row][1], R[row][2]);
+      o[4 * row + col] = ((row + col) % 2 == 0) ? mn : -mn;
+    }
+  const double det = m[0] * minor3(m, 1, 2, 3, 1, 2, 3) - m[1] * minor3(m, 1, 2, 3, 0, 2, 3) +
+                     m[2] * minor3(m, 1, 2, 3, 0, 1, 3) - m[3] * minor3(m, 1, 2, 3, 0, 1, 2);
+#pragma unroll
+  for (int i = 0; i < 16; i++) o[i] = o[i] / det;
+}
+
+// The Newton iterations (see the oracle's fourd_zone for the steps).  True
+// on success, with dE, dF the radiation's change per sqrt(gamma).
+template <bool M1, bool MINK>
+__device__ bool fourd_zone(const RPar &p, const Par &fp, const BView &b, const RView &r, const RGeo<MINK> &G,
+                           long long id, double dt, double &dE, V3 &dF) {
+  const long long vs = r.vs, fvs = b.vs;
+  const double rho = b.prim[PHX_PRHO * fvs + id];
+  double P[4] = {b.prim[PHX_PENG * fvs + id], b.prim[PHX_PVEL * fvs + id], b.prim[(PHX_PVEL + 1) * fvs + id],
+                 b.prim[(PHX_PVEL + 2) * fvs + id]};
+  SrcRes4<M1, MINK> srm{p, fp, G, rho, G.sdetgam(), G.alpha(), {}, {}};
+  srm.mhd_cons(P, srm.U0);
+#pragma unroll
+  for (int n = 0; n < 4; n++) srm.R0[n] = r.cons[(PHX_RE + n) * vs + id];
+  const double eps = p.fd_eps, xi_max = p.xi_ceiling;
+  double U[4], Ur[4], Pr[4], dS[4], res[4];
+  int status = srm.eval(P, U, Ur, Pr, dS);
+#pragma unroll
+  for (int n = 0; n < 4; n++) res[n] = U[n] - srm.U0[n] + dt * dS[n];
+  double err = 1.e100;
+  int niter = 0;
+  bool bad = false;
+  do {
+    double jac[4][4];
+    double mag_min = DBL_MAX;
+#pragma unroll
+    for (int m = 0; m < 4; m++)
+      if (fabs(P[m]) > 0.) mag_min = smin(mag_min, fabs(P[m]));
+    bool bad_m = false, bad_p = false;
+    for (int m = 0; m < 4; m++) {
+      double Pm[4] = {P[0], P[1], P[2], P[3]}, Pp[4] = {P[0], P[1], P[2], P[3]};
+      const double step = smax(eps * mag_min, eps * fabs(P[m]));
+      Pm[m] -= step;
+      Pp[m] += step;
+      double Um[4], Urm[4], Prm[4], dSm[4], Up[4], Urp[4], Prp[4], dSp[4];
+      if (srm.eval(Pm, Um, Urm, Prm, dSm) == FAILURE) bad_m = true;
+      if (srm.eval(Pp, Up, Urp, Prp, dSp) == FAILURE) bad_p = true;
+#pragma unroll
+      for (int n = 0; n < 4; n++) {
+        const double fpl = Up[n] - srm.U0[n] + dt * dSp[n];
+        const double fmi = Um[n] - srm.U0[n] + dt * dSm[n];
+        jac[n][m] = div_p(fpl - fmi, Pp[m] - Pm[m]);
+      }
+    }
+    if (bad_m && bad_p) {
+      bad = true;
+      break;
+    } else if (bad_m || bad_p) {  // one-sided from the guess, on the good side
+      const double side = bad_m ? 1.0 : -1.0;
+      for (int m = 0; m < 4; m++) {
+        double Ps[4] = {P[0], P[1], P[2], P[3]};
+        Ps[m] += side * smax(eps * mag_min, eps * fabs(Ps[m]));
+        double Us[4], Urs[4], Prs[4], dSs[4];
+        srm.eval(Ps, Us, Urs, Prs, dSs);
+#pragma unroll
+        for (int n = 0; n < 4; n++) {
+          const double fs = Us[n] - srm.U0[n] + dt * dSs[n];
+          const double fg = U[n] - srm.U0[n] + dt * dS[n];
+          jac[n][m] = bad_m ? div_p(fs - fg, Ps[m] - P[m]) : div_p(fg - fs, P[m] - Ps[m]);
+        }
+      }
+    }
+    double jinv[4][4];
+    inverse4x4(jac, jinv);
+    if (!bad) {
+      const double ug0 = P[0], ur0 = Pr[0];
+#pragma unroll
+      for (int m = 0; m < 4; m++)
+#pragma unroll
+        for (int n = 0; n < 4; n++) P[m] -= jinv[m][n] * res[n];
+      status = srm.eval(P, U, Ur, Pr, dS);
+      if (status == FAILURE) bad = true;
+      if (bad) {
+        V3 H;
+#pragma unroll
+        for (int a = 0; a < 3; a++) H.d[a] = div_p(Pr[a + 1], Pr[0]);
+        double hh = 0.0;
+        if constexpr (MINK) {
+#pragma unroll
+          for (int a = 0; a < 3; a++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) hh += gdelta(a, c) * H.d[a] * H.d[c];
+        } else {
+          hh = G.g.contract_cov(H, H);
+        }
+        double vh = 0.0;
+#pragma unroll
+        for (int a = 0; a < 3; a++) vh += P[a + 1] * H.d[a];
+        const double xi = div_p(sqrt(hh - vh * vh), Pr[0]);
+        constexpr double umin = 100. * kSMALL, Jmin = 100. * kSMALL;
+        double scale = 0.;
+        if (xi > xi_max) scale = smax(scale, div_p(xi_max, xi));
+        if (P[0] < umin) scale = smax(scale, div_p(ug0 - umin, ug0 - P[0]));
+        if (Pr[0] < Jmin) scale = smax(scale, div_p(ur0 - Jmin, ur0 - Pr[0]));
+        if (!(scale > kSMALL && scale >= 1.)) {  // the reference prints and gives up
+          bad = true;
+          break;
+        }
+        scale *= 0.5;
+#pragma unroll
+        for (int m = 0; m < 4; m++)
+#pragma unroll
+          for (int n = 0; n < 4; n++) P[m] += (1. - scale) * jinv[m][n] * res[n];
+        status = srm.eval(P, U, Ur, Pr, dS);
+        if (status == SUCCESS) bad = false;
+      }
+    }
+    if (bad) break;
+#pragma unroll
+    for (int n = 0; n < 4; n++) res[n] = U[n] - srm.U0[n] + dt * dS[n];
+    if (isnan(res[0]) || isnan(res[1]) || isnan(res[2]) || isnan(res[3])) {
+      bad = true;
+      break;
+    }
+    err = kSMALL;
+    double max_div = kSMALL;
+#pragma unroll
+    for (int n = 0; n < 4; n++) max_div = smax(max_div, fabs(U[n]) + fabs(srm.U0[n]) + fabs(dt * dS[n]));
+#pragma unroll
+    for (int n = 0; n < 4; n++) {
+      const double sub = div_p(fabs(res[n]), max_div);
+      if (sub > err) err = sub;
+    }
+    niter++;
+    if (niter == p.maxiter) break;
+  } while (err > p.tol);
+  if (niter == p.maxiter || err > p.tol || isnan(Ur[0]) || isnan(Ur[1]) || isnan(Ur[2]) || isnan(Ur[3]) || bad)
+    return false;
+  dE = div_p(Ur[0] - r.cons[PHX_RE * vs + id], srm.sdetgam);
+#pragma unroll
+  for (int a = 0; a < 3; a++) dF.d[a] = div_p(Ur[a + 1] - r.cons[(PHX_RF + a) * vs + id], srm.sdetgam);
+  return true;
+}
+
 template <bool M1, bool UPD, bool MINK>
 __global__ void __launch_bounds__(128) k_source(RPar p, Par fp, BView b, RView r, double dt, Range3 rg) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1312,7 +1546,15 @@ __global__ void __launch_bounds__(128) k_source(RPar p, Par fp, BView b, RView r
   dF.d[0] = dF.d[1] = dF.d[2] = 0.0;
   bool success = false;
   T2 Pi;
-  {
+  bool oned = !p.fourd;
+  if (p.fourd) {
+    // fourd, falling back to oned when it fails and src_use_oned_backup is
+    // set (the reference's goto); without the fallback a failed zone keeps
+    // dE = dF = 0 for the fluid update (uninitialised in the reference)
+    success = fourd_zone<M1, MINK>(p, fp, b, r, G, id, dt, dE, dF);
+    oned = !success && p.oned_backup;
+  }
+  if (oned) {
     const double J0 = r.prim[PHX_RJ * vs + id];
     const double dtau = alpha * dt / W;
     TRes res{&p, rho, ug, J0, dtau, amax};

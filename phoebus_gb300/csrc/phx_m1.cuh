@@ -17,6 +17,9 @@ struct RPar {
   int oned_fixup;  // phx_rad_oned_fixup
   int update_fluid;  // MomentFluidSource also updates and inverts the fluid
   int rad_fixup_floors;  // rad_c2p_failure_strategy floors (else interpolate)
+  int fourd;       // src_solver fourd (else oned)
+  int oned_backup;  // src_use_oned_backup
+  double fd_eps;   // src_rootfind_eps
   double cfl, tol, kappa_a, kappa_s, jbb;
   double J_floor, xi_ceiling, tau_max, W_ceiling, Cv;
 };

@@ -293,6 +293,44 @@ def test_equilibration_conserves_energy_and_equilibrates(rad_oracle):
     assert np.all(b["prim"][abi.PVEL:abi.PVEL + 3][:, ks, js, is_] == 0.0)
 
 
+@pytest.mark.parametrize("method", ["moment_eddington", "moment_m1"])
+def test_fourd_equilibration(rad_oracle, method, monkeypatch):
+    """The fourd source solver (moments_source.cpp:489-786) on the
+    radiation_equilibration problem: at rest the 4-D Newton iteration over
+    (u, W v^i) solves the same backward-Euler energy exchange as the oned
+    temperature root find (T and J agree to 1e-10 after 20 steps); it
+    conserves tau + E per zone to rounding and reaches T_eq and
+    J = JBB(T_eq) with every zone converged."""
+    from oracle.oracle import Oracle
+
+    orig = radiation.radiation_equilibration
+
+    def run(solver, steps):
+        def patched(*a, **k):
+            hb, par, rpar, t = orig(*a, **k)
+            return hb, par, dict(rpar, src_solver=solver, method=method), t
+
+        monkeypatch.setattr(radiation, "radiation_equilibration", patched)
+        return equilibration_run(rad_oracle, Oracle(), steps=steps)
+
+    b1, _, _, _ = run("oned", 20)
+    b4, _, _, _ = run("fourd", 20)
+    ks, js, is_ = b1.isl()
+    for name, v in (("prim", abi.PTMP), ("rprim", abi.RJ)):
+        a, c = b1[name][v][ks, js, is_], b4[name][v][ks, js, is_]
+        assert np.max(np.abs(a - c) / np.abs(a)) < 1e-10
+    b, p, rp, e0 = run("fourd", 200)
+    tot = b["cons"][abi.CENG][ks, js, is_] + b["rcons"][abi.RE][ks, js, is_]
+    assert np.max(np.abs(tot - e0) / e0) < 1e-13
+    e = float(e0.ravel()[0])
+    Teq = 0.7
+    for _ in range(50):
+        Teq -= (Teq + Teq ** 4 - e) / (1 + 4 * Teq ** 3)
+    assert np.allclose(b["prim"][abi.PTMP][ks, js, is_], Teq, rtol=1e-9, atol=0)
+    assert np.allclose(b["rprim"][abi.RJ][ks, js, is_], Teq ** 4, rtol=1e-8, atol=0)
+    assert np.all(b["fail"][0][ks, js, is_] == 1.0) and np.all(b["rprim"][abi.RFAIL][ks, js, is_] == 1.0)
+
+
 def test_update_fluid_failure_state(rad_oracle):
     """A zone whose fluid cannot be inverted (NaN conserved density) leaves
     MomentFluidSource with the reference's failure state: the fluid at

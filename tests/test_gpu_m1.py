@@ -203,6 +203,10 @@ def test_rad_configuration_errors(rx):
     with pytest.raises(abi.PhxError) as e:
         rx.MomentCon2Prim(abi.default_rad_params(method=7), p, db)
     assert e.value.status == abi.PHX_ERR_INVALID_ARG
+    # radiation/src_solver other than oned / fourd (radiation.cpp:403-415)
+    with pytest.raises(abi.PhxError, match="src_solver") as e:
+        rx.MomentFluidSource(abi.default_rad_params(src_solver=7), p, db, 1e-3)
+    assert e.value.status == abi.PHX_ERR_INVALID_ARG
     import torch
 
     # the radiation floors need the fluid floors (the fixup package forces them on)
@@ -298,6 +302,53 @@ def test_fluid_source_update_fluid_bitwise(rx, rad_oracle, method, ndim):
     rx.check()
     _cmp(db, hb, ["prim", "cons", "cell_sig", "rcons", "rprim"], "update_fluid source", (ks, js, is_))
     assert host(db["rprim"])[(abi.RJ,) + bad] == 10 * np.finfo(np.float64).tiny
+
+
+@pytest.mark.parametrize("method", ["moment_m1", "moment_eddington"])
+@pytest.mark.parametrize("geom,ndim", [("mink", 1), ("mink", 3), ("fmks", 2)])
+@pytest.mark.parametrize("upd,backup,maxiter", [(0, 0, 100), (1, 0, 100), (0, 1, 2), (1, 0, 2)])
+def test_fourd_source_bitwise(rx, rad_oracle, method, geom, ndim, upd, backup, maxiter):
+    """MomentFluidSource with the fourd solver (moments_source.cpp:489-786),
+    exact build, equals the oracle bit for bit in every fluid and radiation
+    field of the interior: the Newton iterations over (u, W v^i) with the
+    finite-difference Jacobian and the 4x4 adjugate inverse, on Minkowski and
+    FMKS blocks, with and without the coupled fluid update.  Two Newton steps
+    leave most zones unconverged: with src_use_oned_backup they take the oned
+    solver, without it the radiation keeps its state (and, with update_fluid,
+    the fluid takes a zero exchange)."""
+    p = abi.default_params(Gamma=5.0 / 3.0, Cv=1.0)
+    if geom == "mink":
+        nx = {1: (48, 1, 1), 3: (8, 8, 6)}[ndim]
+        hb, db = _coupled_pair(nx, ndim, 101 + ndim, p, vmax=0.3)
+    else:
+        from oracle.oracle import Oracle
+
+        from tests.util import random_rad_block_fmks
+
+        hb = random_rad_block_fmks((16, 12, 1), 2, seed=97)
+        P = hb["prim"]
+        P[abi.PPRS] = p.gm1 * P[abi.PENG]
+        P[abi.PGM1] = p.gm1 + 1.0
+        Oracle().PrimitiveToConserved(p, hb, *hb.entire())
+        db = hb.to_device()
+    rp = abi.default_rad_params(method=method, kappa_a=4.0, kappa_s=20.0, jbb_coeff=0.6, update_fluid=upd,
+                                src_solver="fourd", src_use_oned_backup=backup, src_rootfind_maxiter=maxiter)
+    for o, b in ((rad_oracle, hb), (rx, db)):
+        o.MomentPrim2Con(rp, p, b, *b.entire())
+        o.MomentCon2Prim(rp, p, b)
+        o.MomentCalculateOpacities(rp, p, b)
+    r0 = hb["rcons"].copy()
+    applied = rad_oracle.MomentFluidSource(rp, p, hb, 0.02)
+    rx.MomentFluidSource(rp, p, db, 0.02)
+    rx.check()
+    ks, js, is_ = hb.isl()
+    _cmp(db, hb, ["prim", "cons", "rcons", "rprim"], f"fourd source ({geom}, update_fluid={upd})", (ks, js, is_))
+    n = hb["rcons"][0][ks, js, is_].size
+    if maxiter == 100:
+        assert applied == n  # every zone converged
+    elif not backup:
+        assert applied < n
+    assert np.any(hb["rcons"][:, ks, js, is_] != r0[:, ks, js, is_])
 
 
 @pytest.mark.parametrize("method,ndim", [("moment_m1", 1), ("moment_eddington", 2), ("moment_m1", 3)])

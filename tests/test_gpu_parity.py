@@ -147,6 +147,36 @@ def test_fluxes_random_state(oracle, ctx_exact, recon):
                        f"flux d={d}")
 
 
+@pytest.mark.parametrize("staging", ["tensor", "bulk", "loads"])
+@pytest.mark.parametrize("shape", [(10, 10, 10), (256, 6, 6)])
+def test_fluxes_x1_staging(oracle, ctx_exact, staging, shape, monkeypatch):
+    """The X1 kernel's three ways of staging pencils in shared memory (tiled
+    TMA through a tensor map, 1-D bulk copies, plain loads) give the oracle's
+    fluxes bit for bit; (256, 6, 6) has 264-cell pencils, which the tensor
+    map splits in two 132-cell rows (a TMA box dimension is at most 256)."""
+    from phoebus_gb300.block import Block
+
+    monkeypatch.setenv("PHX_X1_STAGING", staging)
+    p = abi.default_params(Gamma=4.0 / 3.0, recon="weno5z", riemann="hll", c2p_tol=1e-10, c2p_max_iter=100)
+    ref = states.random_block(6, 35)
+    hb = Block(shape, 4, 3, (0.0, 0.0, 0.0), tuple(1.0 / n for n in shape)).alloc()
+    rng = np.random.default_rng(36)
+    for v in range(hb["prim"].shape[0]):  # tile the random state over the larger block
+        src = ref["prim"][v]
+        reps = [int(np.ceil(t / s)) for t, s in zip(hb["prim"][v].shape, src.shape)]
+        hb["prim"][v] = np.tile(src, reps)[tuple(slice(0, t) for t in hb["prim"][v].shape)]
+    hb["prim"][abi.PRHO] *= 1.0 + 0.01 * rng.random(hb["prim"][abi.PRHO].shape)
+    oracle.Initialize(p, hb)
+    db = hb.to_device()
+    oracle.CalculateFluxes(p, hb)
+    ctx_exact.CalculateFluxes(p, db)
+    ctx_exact.check()
+    r = face_region(hb, 0)
+    assert_bitwise(flux_view(db["flux"], 0)[(slice(None),) + r], flux_view(hb["flux"], 0)[(slice(None),) + r],
+                   f"flux d=0 ({staging})")
+    assert_bitwise(db["face_sig"][0][r], hb["face_sig"][0][r], f"face_sig d=0 ({staging})")
+
+
 @pytest.mark.parametrize("recon", ["weno5z", "mp5"])
 def test_fluxes_fast_tolerance(oracle, ctx_fast, recon):
     """Production build: fluxes within 1e-12 relative (floor: 1e-12 of the
