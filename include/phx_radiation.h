@@ -55,6 +55,11 @@ typedef enum { /* radiation.hpp SourceSolver, radiation.cpp:403-415 (zerod is di
   PHX_RAD_SRC_FOURD = 1
 } phx_rad_src_solver;
 
+typedef enum { /* fixup/rad_floor_type, fixup.cpp:188-200, fixup.hpp:150-182 */
+  PHX_RAD_FLOOR_CONSTANT_J = 0, /* J_floor = J0_floor                          */
+  PHX_RAD_FLOOR_EXPX1_J = 1     /* J_floor = J0_floor exp(J_exp_floor X1)     */
+} phx_rad_floor_type;
+
 typedef enum { /* radiation.hpp OneDFixupStrategy, radiation.cpp:432-445 */
   PHX_RAD_ONED_FIXUP_NONE = 0,
   PHX_RAD_ONED_FIXUP_IGNORE_DJ = 1,
@@ -78,7 +83,7 @@ typedef struct {
    * Rosseland means from singularity-opac tables; for gray opacities they
    * are these constants. */
   double kappa_a, kappa_s, jbb_coeff;
-  /* fixup/enable_rad_floors with rad_floor_type ConstantJ, and
+  /* fixup/enable_rad_floors (rad_floor_type below), and
    * fixup/enable_rad_ceilings with ConstantXi0 */
   int enable_rad_floors;
   double J0_floor;
@@ -97,6 +102,11 @@ typedef struct {
   int src_solver;
   double src_rootfind_eps;
   int src_use_oned_backup;
+  /* fixup/rad_floor_type (phx_rad_floor_type, with enable_rad_floors) and
+   * fixup/J_exp_floor (-2) of the ExpX1J floor, evaluated at the X1 of the
+   * zone (ApplyFloors) or of the face (the flux's reconstructed J) */
+  int rad_floor_type;
+  double J_exp_floor;
 } phx_rad_params;
 
 /* Radiation fields of one block.  Same shape and var_stride convention as

@@ -2754,6 +2754,8 @@ struct RPar {
   bool update_fluid, fixup_floors;
   bool fourd, oned_backup;  // src_solver fourd; src_use_oned_backup
   Real fd_eps;              // src_rootfind_eps
+  bool floor_expx1;         // rad_floor_type ExpX1J
+  Real J_alpha;             // J_exp_floor
   Real J_floor, xi_ceiling, tau_max, W_ceiling, Cv;
   RPar(const phx_rad_params &rp, const phx_params &p) {
     update_fluid = rp.update_fluid != 0;
@@ -2773,11 +2775,15 @@ struct RPar {
     kappa_s = rp.kappa_s;
     jbb = rp.jbb_coeff;
     J_floor = rp.enable_rad_floors ? rp.J0_floor : -std::numeric_limits<Real>::max();
+    floor_expx1 = rp.enable_rad_floors && rp.rad_floor_type == PHX_RAD_FLOOR_EXPX1_J;
+    J_alpha = rp.J_exp_floor;
     xi_ceiling = rp.enable_rad_ceilings ? rp.xi0_ceiling : std::numeric_limits<Real>::max();
     tau_max = rp.enable_rad_ceilings ? rp.tau0_ceiling : std::numeric_limits<Real>::max();
     W_ceiling = p.enable_ceilings ? p.gam0_ceiling : std::numeric_limits<Real>::max();
     Cv = p.Cv;
   }
+  // RadiationFloors::GetRadiationFloors (fixup.hpp:166-177) at X1 = x1
+  Real JFloor(Real x1) const { return floor_expx1 ? J_floor * phx_math::exp(J_alpha * x1) : J_floor; }
   Real kappaJ(Real rho, Real T) const { return rho * kappa_a; }
   Real kappaS(Real rho, Real T) const { return rho * kappa_s; }
   Real JBB(Real T) const { return jbb * (T * T) * (T * T); }
@@ -2941,8 +2947,10 @@ void face_flux(const RPar &rp, const RBlk &R, int d, int k, int j, int i) {
 
   Real Jl = ql[0], Jr = qr[0];
   if (rp.bounds) {
-    Jl = smax(Jl, rp.J_floor);
-    Jr = smax(Jr, rp.J_floor);
+    // at the face's X1 (moments.cpp:562-575)
+    const Real Jf = rp.JFloor(d == 0 ? R.B.Xf(1, i) : R.B.Xc(1, i));
+    Jl = smax(Jl, Jf);
+    Jr = smax(Jr, Jf);
   }
   V3 Hl{{Jl * ql[1], Jl * ql[2], Jl * ql[3]}}, Hr{{Jr * qr[1], Jr * qr[2], Jr * qr[3]}};
   if (rp.bounds) {
@@ -3645,7 +3653,7 @@ void rad_floors_zone(const RPar &rp, const RBlk &R, int k, int j, int i, bool fl
     for (int a = 0; a < 3; a++) F(a) = R.U(PHX_RF + a, id) / sdetgam;
     invert();
   }
-  const Real dJ = rp.J_floor - R.Q(PHX_RJ, id);
+  const Real dJ = rp.JFloor(R.B.Xc(1, i)) - R.Q(PHX_RJ, id);
   if (dJ > 0.) {
     const V3 zero{{0.0, 0.0, 0.0}};
     T2 Pz;

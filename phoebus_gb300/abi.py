@@ -37,6 +37,7 @@ RJ, RH, RXI, RPHI, RFAIL, RKAPPAJ, RKAPPAH, RJBB, RNPRIM = 0, 1, 4, 5, 6, 7, 8, 
 RAD_METHOD = {"moment_m1": 0, "moment_eddington": 1}
 RAD_ONED_FIXUP = {"none": 0, "ignore_dJ": 1, "ignore_all": 2}
 RAD_SRC_SOLVER = {"oned": 0, "fourd": 1}  # radiation/src_solver (radiation.cpp:403-415)
+RAD_FLOOR = {"ConstantJ": 0, "ExpX1J": 1}  # fixup/rad_floor_type (fixup.cpp:188-200)
 
 MATH = {"exp": 0, "log": 1, "sin": 2, "cos": 3, "pow": 4}
 PHX_OK, PHX_ERR_INVALID_ARG, PHX_ERR_UNBRACKETED, PHX_ERR_NAN_INPUT, PHX_ERR_TIMEOUT = 0, 1, 2, 3, 4
@@ -113,7 +114,8 @@ class RadParams(C.Structure):
                 ("kappa_s", C.c_double), ("jbb_coeff", C.c_double), ("enable_rad_floors", C.c_int),
                 ("J0_floor", C.c_double), ("enable_rad_ceilings", C.c_int), ("xi0_ceiling", C.c_double),
                 ("tau0_ceiling", C.c_double), ("update_fluid", C.c_int), ("rad_c2p_failure_floors", C.c_int),
-                ("src_solver", C.c_int), ("src_rootfind_eps", C.c_double), ("src_use_oned_backup", C.c_int)]
+                ("src_solver", C.c_int), ("src_rootfind_eps", C.c_double), ("src_use_oned_backup", C.c_int),
+                ("rad_floor_type", C.c_int), ("J_exp_floor", C.c_double)]
 
 
 class RadBlockS(C.Structure):
@@ -304,6 +306,7 @@ def default_rad_params(**over) -> RadParams:
     r.enable_rad_ceilings, r.xi0_ceiling, r.tau0_ceiling = 0, 0.99, 1.0e3
     r.update_fluid, r.rad_c2p_failure_floors = 0, 0
     r.src_solver, r.src_rootfind_eps, r.src_use_oned_backup = RAD_SRC_SOLVER["oned"], 1.0e-8, 0
+    r.rad_floor_type, r.J_exp_floor = RAD_FLOOR["ConstantJ"], -2.0
     for k, v in over.items():
         if k == "method" and isinstance(v, str):
             v = RAD_METHOD[v]
@@ -313,6 +316,8 @@ def default_rad_params(**over) -> RadParams:
             v = RAD_ONED_FIXUP[v]
         if k == "src_solver" and isinstance(v, str):
             v = RAD_SRC_SOLVER[v]
+        if k == "rad_floor_type" and isinstance(v, str):
+            v = RAD_FLOOR[v]
         if not hasattr(r, k):
             raise KeyError(k)
         setattr(r, k, v)

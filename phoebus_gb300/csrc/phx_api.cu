@@ -1034,6 +1034,9 @@ phx_status check_rad(const phx_rad_params *rp, const phx_params *p, const phx_bl
   if (rp->src_rootfind_maxiter < 0) return fail(PHX_ERR_INVALID_ARG, "src_rootfind_maxiter < 0");
   if (rp->src_solver != PHX_RAD_SRC_ONED && rp->src_solver != PHX_RAD_SRC_FOURD)
     return fail(PHX_ERR_INVALID_ARG, "\"radiation/src_solver\" option unrecognized!");
+  if (rp->enable_rad_floors && rp->rad_floor_type != PHX_RAD_FLOOR_CONSTANT_J &&
+      rp->rad_floor_type != PHX_RAD_FLOOR_EXPX1_J)
+    return fail(PHX_ERR_INVALID_ARG, "invalid <fixup>/rad_floor_type input");
   if (p == nullptr) return fail(PHX_ERR_INVALID_ARG, "params is NULL");
   return PHX_OK;
 }
@@ -1060,6 +1063,8 @@ phx::rad::RPar make_rpar(const phx_rad_params &rp, const phx_params &p) {
   // RadiationFloors() / RadiationCeilings() / Ceilings() defaults when
   // disabled (fixup.hpp:157-273)
   r.J_floor = rp.enable_rad_floors ? rp.J0_floor : -phx::kDBLMAX;
+  r.floor_expx1 = rp.enable_rad_floors && rp.rad_floor_type == PHX_RAD_FLOOR_EXPX1_J;
+  r.J_alpha = rp.J_exp_floor;
   r.xi_ceiling = rp.enable_rad_ceilings ? rp.xi0_ceiling : phx::kDBLMAX;
   r.tau_max = rp.enable_rad_ceilings ? rp.tau0_ceiling : phx::kDBLMAX;
   r.W_ceiling = p.enable_ceilings ? p.gam0_ceiling : phx::kDBLMAX;
@@ -1142,6 +1147,8 @@ void phx_rad_params_default(phx_rad_params *p) {
   p->src_solver = PHX_RAD_SRC_ONED;  // radiation/src_solver "oned" (radiation.cpp:403-404)
   p->src_rootfind_eps = 1.e-8;       // radiation/src_rootfind_eps (radiation.cpp:421)
   p->src_use_oned_backup = 0;        // radiation/src_use_oned_backup (radiation.cpp:417-418)
+  p->rad_floor_type = PHX_RAD_FLOOR_CONSTANT_J;
+  p->J_exp_floor = -2.0;             // fixup/J_exp_floor (fixup.cpp:194-195)
 }
 
 phx_status phx_rad_prim_to_con(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_block *fb,

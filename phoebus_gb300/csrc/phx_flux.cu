@@ -100,8 +100,8 @@ __device__ __forceinline__ void face_flux(const Par &p, const BView &b, int k, i
 constexpr int X1_WARPS = 4;    // warps per CTA
 constexpr int X1_PENCILS = 4;  // (k, j) pencils staged per CTA
 
-// A CTA stages np pencils (10 primitive rows each) in shared memory with TMA
-// bulk copies completing on one mbarrier.  Its warps then walk the pencils'
+// A CTA stages np pencils (kReconLoad primitive rows each) in shared memory
+// with TMA copies completing on one mbarrier.  Its warps then walk the pencils'
 // cells as one flattened list [pencil][cell is-1 .. ie+1] in chunks of 32
 // cells that overlap by one: lane L reconstructs its cell, takes the
 // upper-face state of the cell on its left from lane L-1 (__shfl_up_sync) and

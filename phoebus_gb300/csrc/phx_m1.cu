@@ -651,6 +651,13 @@ struct Closure {
   }
 };
 
+// RadiationFloors::GetRadiationFloors (fixup.hpp:166-177) at X1 = x1:
+// ConstantJ, or ExpX1J J0 exp(J_alpha x1) with the project's exp (the one the
+// oracle uses, so both agree bit for bit)
+__device__ __forceinline__ double j_floor_at(const RPar &p, double x1) {
+  return p.floor_expx1 ? p.J_floor * phx_math::exp(p.J_alpha * x1) : p.J_floor;
+}
+
 // ---------------------------------------------------------------- views
 // The geometry a moment task reads at one location (loc 0 centre and X3
 // faces, 1 X1 face, 2 X2 face): the table values and, off Minkowski, the
@@ -893,8 +900,9 @@ __global__ void __launch_bounds__(128) k_fluxes(RPar p, BView b, RView r, Range3
   const double asym_sigr = alpha * vr.d[d] - beta_d;
   double Jl = ql[0], Jr = qr[0];
   if (p.bounds) {
-    Jl = smax(Jl, p.J_floor);
-    Jr = smax(Jr, p.J_floor);
+    const double Jf = j_floor_at(p, d == 0 ? b.Xf(0, i) : b.Xc(0, i));  // at the face (moments.cpp:562-575)
+    Jl = smax(Jl, Jf);
+    Jr = smax(Jr, Jf);
   }
   V3 Hl, Hr;
 #pragma unroll
@@ -1754,7 +1762,7 @@ __global__ void __launch_bounds__(128) k_rad_floors(RPar p, BView b, RView r, co
     for (int a = 0; a < 3; a++) F.d[a] = r.cons[(PHX_RF + a) * vs + id] / sdetgam;
     invert();
   }
-  const double dJ = p.J_floor - r.prim[PHX_RJ * vs + id];
+  const double dJ = j_floor_at(p, b.Xc(0, i)) - r.prim[PHX_RJ * vs + id];
   if (dJ > 0.) {
     V3 zero, Hz;
     zero.d[0] = zero.d[1] = zero.d[2] = 0.0;

@@ -22,6 +22,8 @@ struct RPar {
   double fd_eps;   // src_rootfind_eps
   double cfl, tol, kappa_a, kappa_s, jbb;
   double J_floor, xi_ceiling, tau_max, W_ceiling, Cv;
+  int floor_expx1;  // rad_floor_type ExpX1J: J_floor exp(J_alpha X1)
+  double J_alpha;
 };
 
 // Radiation fields of one block.
