@@ -23,6 +23,7 @@
 
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 
 #include "phx_kernels.cuh"
 #include "phx_bulk.cuh"
@@ -286,16 +287,15 @@ __global__ void __launch_bounds__(32 * X1_WARPS) kb_flux_x1(Par p, const BView *
 // against the driver library).
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  static bool tried = false;
-  if (!tried) {
-    tried = true;
+  static std::once_flag once;  // callers on several host threads look it up once
+  std::call_once(once, [] {
     void *f = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
             cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
       fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
-  }
+  });
   return fn;
 }
 
