@@ -177,21 +177,29 @@ def test_fluxes_x1_staging(oracle, ctx_exact, staging, shape, monkeypatch):
     assert_bitwise(db["face_sig"][0][r], hb["face_sig"][0][r], f"face_sig d=0 ({staging})")
 
 
-@pytest.mark.parametrize("recon", ["weno5z", "mp5"])
-def test_fluxes_fast_tolerance(oracle, ctx_fast, recon):
-    """Production build: fluxes within 1e-12 relative (floor: 1e-12 of the
-    variable's largest flux magnitude)."""
-    p = abi.default_params(Gamma=5.0 / 3.0, recon=recon, riemann="hll", c2p_tol=1e-10, c2p_max_iter=100)
-    hb, _ = _smooth_state(12)
+@pytest.mark.parametrize("recon,solver,state", [("weno5z", "hll", "smooth"), ("mp5", "hll", "smooth"),
+                                                ("linear", "llf", "smooth"), ("weno5z", "hll", "random"),
+                                                ("mp5", "hll", "random"), ("linear", "llf", "random")])
+def test_fluxes_fast_tolerance(oracle, ctx_fast, recon, solver, state):
+    """Production build: every face flux within 1e-12 of the oracle's relative
+    to the face's own scale (the magnitudes of the terms that form it there,
+    tests/util.py face_flux_scale), on the smooth shear state and on the
+    per-zone random discontinuous state (limiters, MP5 branches, WENO5-Z
+    weights far from linear)."""
+    from tests.util import face_flux_scale, report_close
+
+    p = abi.default_params(Gamma=5.0 / 3.0, recon=recon, riemann=solver, c2p_tol=1e-10, c2p_max_iter=100)
+    hb = _smooth_state(12)[0] if state == "smooth" else states.random_block(10, 33)
     oracle.Initialize(p, hb)
     db = hb.to_device()
     oracle.CalculateFluxes(p, hb)
     ctx_fast.CalculateFluxes(p, db)
     for d in range(3):
         r = face_region(hb, d)
-        g, f = flux_view(db["flux"], d)[(slice(None),) + r], flux_view(hb["flux"], d)[(slice(None),) + r]
-        for m in range(8):
-            assert_close(g[m], f[m], 1e-12, f"flux d={d} m={m}")
+        sl = (slice(None),) + r
+        scale = face_flux_scale(hb, d)
+        report_close(flux_view(db["flux"], d)[sl], flux_view(hb["flux"], d)[sl], scale[sl], 1e-12,
+                     f"{recon}/{solver} {state} flux d={d}")
 
 
 def test_flux_ct_and_update(oracle, ctx_exact):

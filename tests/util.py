@@ -157,7 +157,8 @@ def report_close(got, ref, scale, rtol, what="", sl=None):
     """Per-zone check |got - ref| <= rtol (|ref| + scale) (NaN equal NaN);
     returns the largest per-zone ratio |got - ref| / (|ref| + scale), printed
     for the test log."""
-    got, ref, scale = host(got), host(ref), host(scale)
+    got, ref = host(got), host(ref)
+    scale = np.broadcast_to(host(scale), np.shape(ref))  # a scalar floor too
     if sl is not None:
         got, ref, scale = got[sl], ref[sl], scale[sl]
     both_nan = np.isnan(got) & np.isnan(ref)
