@@ -352,6 +352,43 @@ def test_fourd_source_bitwise(rx, rad_oracle, method, geom, ndim, upd, backup, m
         assert applied < n
 
 
+@pytest.mark.parametrize("method", ["moment_m1", "moment_eddington"])
+@pytest.mark.parametrize("upd", [0, 1])
+def test_fourd_source_production(rf, rad_oracle, method, upd):
+    """The fourd solver in the production build (FMA contraction, reciprocal
+    products) against the oracle: both Newton iterations stop at a relative
+    residual of 1e-12 (src_rootfind_tol), so the conserved radiation and the
+    fluid states agree per zone to 1e-9 (the residual's tolerance times the
+    Jacobian's conditioning; measured up to 5e-10) and the radiation
+    primitives, inverted from them, to 1e-7 (measured up to 1e-8 in H_i / J)."""
+    p = abi.default_params(Gamma=5.0 / 3.0, Cv=1.0)
+    hb, db = _coupled_pair((8, 8, 6), 3, 131 + upd, p, vmax=0.3)
+    rp = abi.default_rad_params(method=method, kappa_a=4.0, kappa_s=20.0, jbb_coeff=0.6, update_fluid=upd,
+                                src_solver="fourd")
+    for o, b in ((rad_oracle, hb), (rf, db)):
+        o.MomentPrim2Con(rp, p, b, *b.entire())
+        o.MomentCon2Prim(rp, p, b)
+        o.MomentCalculateOpacities(rp, p, b)
+    applied = rad_oracle.MomentFluidSource(rp, p, hb, 0.02)
+    rf.MomentFluidSource(rp, p, db, 0.02)
+    rf.check()
+    ks, js, is_ = hb.isl()
+    assert applied == hb["rcons"][0][ks, js, is_].size
+    for name in ("rcons", "rprim", "cons", "prim"):
+        g, r = host(db[name])[(slice(None), ks, js, is_)], hb[name][(slice(None), ks, js, is_)]
+        n = abi.RFAIL + 1 if name == "rprim" else g.shape[0]
+        for v in range(n):
+            # per zone, with a floor of 1e-6 of the variable's magnitude for
+            # components that pass through zero (velocities, fluxes)
+            den = np.abs(r[v]) + 1e-6 * np.abs(r[v]).max() + 1e-300
+            err = float(np.max(np.abs(g[v] - r[v]) / den))
+            print(f"[per-zone] fourd production {name}[{v}] max rel {err:.2e}")
+            # the radiation primitives are the closure inversion of the
+            # updated E, F_i: H_i / J of a nearly isotropic field carries the
+            # cancellation of F_i - (J terms) into the ratio
+            assert err < (1e-7 if name == "rprim" else 1e-9), (name, v, err)
+
+
 @pytest.mark.parametrize("method,ndim", [("moment_m1", 1), ("moment_eddington", 2), ("moment_m1", 3)])
 def test_fluid_stage_rk2_bitwise(rx, rad_oracle, method, ndim):
     """phx_rad_fluid_stage (exact build): three rk2 steps of a moving fluid
