@@ -1535,7 +1535,7 @@ __device__ bool fourd_zone(const RPar &p, const Par &fp, const BView &b, const R
   return true;
 }
 
-template <bool M1, bool UPD, bool MINK>
+template <bool M1, bool UPD, bool MINK, bool FOURD>
 __global__ void __launch_bounds__(128) k_source(RPar p, Par fp, BView b, RView r, double dt, Range3 rg) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= range_count(rg)) return;
@@ -1554,8 +1554,8 @@ __global__ void __launch_bounds__(128) k_source(RPar p, Par fp, BView b, RView r
   dF.d[0] = dF.d[1] = dF.d[2] = 0.0;
   bool success = false;
   T2 Pi;
-  bool oned = !p.fourd;
-  if (p.fourd) {
+  bool oned = !FOURD;
+  if constexpr (FOURD) {
     // fourd, falling back to oned when it fails and src_use_oned_backup is
     // set (the reference's goto); without the fallback a failed zone keeps
     // dE = dF = 0 for the fluid update (uninitialised in the reference)
@@ -1947,20 +1947,30 @@ void launch_update(const RPar &p, const BView &b, const RView &r, const double *
     k_update<false, false><<<g, 256, 0, s>>>(b, r, base, out, beta, dt, rg);
 }
 
+// the fourd solver is its own instantiation, so the oned kernels keep the
+// registers they need
+template <bool MINK, bool FOURD>
+static void source_s(const RPar &p, const Par &fp, const BView &b, const RView &r, double dt, Range3 rg,
+                     unsigned g, cudaStream_t s) {
+  if (p.m1) {
+    if (p.update_fluid)
+      k_source<true, true, MINK, FOURD><<<g, 128, 0, s>>>(p, fp, b, r, dt, rg);
+    else
+      k_source<true, false, MINK, FOURD><<<g, 128, 0, s>>>(p, fp, b, r, dt, rg);
+  } else {
+    if (p.update_fluid)
+      k_source<false, true, MINK, FOURD><<<g, 128, 0, s>>>(p, fp, b, r, dt, rg);
+    else
+      k_source<false, false, MINK, FOURD><<<g, 128, 0, s>>>(p, fp, b, r, dt, rg);
+  }
+}
 template <bool MINK>
 static void source_t(const RPar &p, const Par &fp, const BView &b, const RView &r, double dt, Range3 rg, unsigned g,
                      cudaStream_t s) {
-  if (p.m1) {
-    if (p.update_fluid)
-      k_source<true, true, MINK><<<g, 128, 0, s>>>(p, fp, b, r, dt, rg);
-    else
-      k_source<true, false, MINK><<<g, 128, 0, s>>>(p, fp, b, r, dt, rg);
-  } else {
-    if (p.update_fluid)
-      k_source<false, true, MINK><<<g, 128, 0, s>>>(p, fp, b, r, dt, rg);
-    else
-      k_source<false, false, MINK><<<g, 128, 0, s>>>(p, fp, b, r, dt, rg);
-  }
+  if (p.fourd)
+    source_s<MINK, true>(p, fp, b, r, dt, rg, g, s);
+  else
+    source_s<MINK, false>(p, fp, b, r, dt, rg, g, s);
 }
 
 void launch_source(const RPar &p, const Par &fp, const BView &b, const RView &r, double dt, cudaStream_t s) {
