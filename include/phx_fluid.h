@@ -576,7 +576,11 @@ phx_status phx_torus_init(phx_ctx *ctx, const phx_params *p, const phx_torus_par
  * evaluates the same operations, so tables and floors compare bit for bit.
  * out[q] = f(x[q]) (pow: x[q]^y[q]) for device arrays of n doubles, for
  * validating them against other implementations. */
-enum { PHX_MATH_EXP = 0, PHX_MATH_LOG = 1, PHX_MATH_SIN = 2, PHX_MATH_COS = 3, PHX_MATH_POW = 4 };
+enum { PHX_MATH_EXP = 0, PHX_MATH_LOG = 1, PHX_MATH_SIN = 2, PHX_MATH_COS = 3, PHX_MATH_POW = 4,
+       /* the kernels' 1/x and 1/sqrt(x): IEEE division and square root in the
+        * exact build; in the production build the hardware seed with one
+        * third-order correction (normal x; others divide) */
+       PHX_MATH_RCP = 5, PHX_MATH_RSQRT = 6 };
 phx_status phx_math_eval(int fn, long long n, const double *x, const double *y, double *out, void *stream);
 
 /* ---- measurement probe -------------------------------------------------- */

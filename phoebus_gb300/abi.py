@@ -39,7 +39,7 @@ RAD_ONED_FIXUP = {"none": 0, "ignore_dJ": 1, "ignore_all": 2}
 RAD_SRC_SOLVER = {"oned": 0, "fourd": 1}  # radiation/src_solver (radiation.cpp:403-415)
 RAD_FLOOR = {"ConstantJ": 0, "ExpX1J": 1}  # fixup/rad_floor_type (fixup.cpp:188-200)
 
-MATH = {"exp": 0, "log": 1, "sin": 2, "cos": 3, "pow": 4}
+MATH = {"exp": 0, "log": 1, "sin": 2, "cos": 3, "pow": 4, "rcp": 5, "rsqrt": 6}
 PHX_OK, PHX_ERR_INVALID_ARG, PHX_ERR_UNBRACKETED, PHX_ERR_NAN_INPUT, PHX_ERR_TIMEOUT = 0, 1, 2, 3, 4
 PHX_ERR_CUDA, PHX_ERR_NO_DEVICE, PHX_ERR_CAPACITY, PHX_ERR_UNSUPPORTED = 5, 6, 7, 8
 STATUS = {0: "ok", 1: "invalid argument", 2: "con2prim root not bracketed", 3: "NaN input",

@@ -973,7 +973,8 @@ phx_status phx_torus_init(phx_ctx *ctx, const phx_params *p, const phx_torus_par
 }
 
 phx_status phx_math_eval(int fn, long long n, const double *x, const double *y, double *out, void *stream) {
-  if (fn < PHX_MATH_EXP || fn > PHX_MATH_POW) return fail(PHX_ERR_INVALID_ARG, "phx_math_eval: unknown function %d", fn);
+  if (fn < PHX_MATH_EXP || fn > PHX_MATH_RSQRT)
+    return fail(PHX_ERR_INVALID_ARG, "phx_math_eval: unknown function %d", fn);
   if (n < 0) return fail(PHX_ERR_INVALID_ARG, "n < 0");
   if (n == 0) return PHX_OK;
   if (!x || !out || (fn == PHX_MATH_POW && !y)) return fail(PHX_ERR_INVALID_ARG, "x/y/out is NULL");

@@ -89,7 +89,9 @@ void launch_geom_points(const phx_geometry &g, long long n, const double *x1, co
   k_geom_points<<<(unsigned)((n + T - 1) / T), T, 0, s>>>(f, n, x1, x2, geom);
 }
 
-// The library's exp / log / sin / cos / pow over an array (their validation).
+// The library's exp / log / sin / cos / pow over an array, and the
+// reciprocal and inverse square root of the kernels' arithmetic (their
+// validation).
 __global__ void k_math_eval(int fn, long long n, const double *x, const double *y, double *out) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
@@ -100,6 +102,8 @@ __global__ void k_math_eval(int fn, long long n, const double *x, const double *
   case PHX_MATH_LOG: r = phx_math::log(a); break;
   case PHX_MATH_SIN: r = phx_math::sin(a); break;
   case PHX_MATH_COS: r = phx_math::cos(a); break;
+  case PHX_MATH_RCP: r = rcp_p(a); break;
+  case PHX_MATH_RSQRT: r = rsqrt_p(a); break;
   default: r = phx_math::pow(a, y[q]); break;
   }
   out[q] = r;

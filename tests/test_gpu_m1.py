@@ -357,10 +357,11 @@ def test_fourd_source_bitwise(rx, rad_oracle, method, geom, ndim, upd, backup, m
 def test_fourd_source_production(rf, rad_oracle, method, upd):
     """The fourd solver in the production build (FMA contraction, reciprocal
     products) against the oracle: both Newton iterations stop at a relative
-    residual of 1e-12 (src_rootfind_tol), so the conserved radiation and the
-    fluid states agree per zone to 1e-9 (the residual's tolerance times the
-    Jacobian's conditioning; measured up to 5e-10) and the radiation
-    primitives, inverted from them, to 1e-7 (measured up to 1e-8 in H_i / J)."""
+    residual of 1e-12 (src_rootfind_tol), so the conserved radiation and
+    fluid variables agree per zone to 1e-9 (the residual's tolerance times the
+    Jacobian's conditioning; measured up to 5e-10) and the primitives inverted
+    from them to 1e-7 (measured up to 1e-8 in H_i / J and 4e-8 in a fluid
+    velocity component near zero)."""
     p = abi.default_params(Gamma=5.0 / 3.0, Cv=1.0)
     hb, db = _coupled_pair((8, 8, 6), 3, 131 + upd, p, vmax=0.3)
     rp = abi.default_rad_params(method=method, kappa_a=4.0, kappa_s=20.0, jbb_coeff=0.6, update_fluid=upd,
@@ -383,10 +384,11 @@ def test_fourd_source_production(rf, rad_oracle, method, upd):
             den = np.abs(r[v]) + 1e-6 * np.abs(r[v]).max() + 1e-300
             err = float(np.max(np.abs(g[v] - r[v]) / den))
             print(f"[per-zone] fourd production {name}[{v}] max rel {err:.2e}")
-            # the radiation primitives are the closure inversion of the
-            # updated E, F_i: H_i / J of a nearly isotropic field carries the
-            # cancellation of F_i - (J terms) into the ratio
-            assert err < (1e-7 if name == "rprim" else 1e-9), (name, v, err)
+            # primitives are inversions of the updated conserved variables:
+            # the closure's H_i / J of a nearly isotropic field carries the
+            # cancellation of F_i - (J terms) into the ratio, and the fluid's
+            # con2prim (update_fluid) stops within its 1e-10 bracket
+            assert err < (1e-7 if name in ("rprim", "prim") else 1e-9), (name, v, err)
 
 
 @pytest.mark.parametrize("method,ndim", [("moment_m1", 1), ("moment_eddington", 2), ("moment_m1", 3)])

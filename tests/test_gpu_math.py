@@ -69,3 +69,31 @@ def test_gpu_math_against_cuda_libm(built, fn):
     e = np.abs(got[ok] - ref[ok]) / np.where(sp > 0, sp, 5e-324)
     print(f"{fn}: max {e.max():.2f} ulp against CUDA's libm")
     assert e.max() <= 3.0
+
+
+def _ulps(a, b):
+    """|a - b| in units of the spacing of b (finite positive b)."""
+    return np.abs(a - b) / np.spacing(b)
+
+
+@pytest.mark.parametrize("exact", [True, False])
+def test_reciprocals_of_the_kernels(built, exact):
+    """The kernels' 1/x and 1/sqrt(x) (phx_math_eval RCP, RSQRT): the exact
+    build divides (correctly rounded); the production build's hardware seed
+    with one third-order correction is within one ulp of the correctly
+    rounded reciprocal and within two ulps of 1.0 / sqrt(x) (itself rounded
+    twice) over normal x from 1e-300 to 1e300, and takes the IEEE operation
+    at the ends of the range."""
+    lib = abi.load(exact)
+    rng = np.random.default_rng(17)
+    x = np.concatenate([10.0 ** rng.uniform(-300, 300, 400000), rng.uniform(0.5, 2.0, 100000),
+                        [1.0, 2.0, 0.5, 1e-305, 1e305]])
+    r = _gpu_eval(lib, "rcp", x, None)
+    s = _gpu_eval(lib, "rsqrt", x, None)
+    rcp_ulps = _ulps(r, 1.0 / x)
+    rsq_ulps = _ulps(s, 1.0 / np.sqrt(x))
+    print(f"[ulps] exact={exact}: rcp max {rcp_ulps.max():.2f}, rsqrt max {rsq_ulps.max():.2f}")
+    if exact:
+        assert rcp_ulps.max() == 0 and rsq_ulps.max() <= 1
+    else:
+        assert rcp_ulps.max() <= 1 and rsq_ulps.max() <= 2
