@@ -172,6 +172,33 @@ phx_status phx_rad_fluid_source(phx_ctx *ctx, const phx_rad_params *rp, const ph
  * is periodic on every active axis. */
 phx_status phx_rad_fill_ghosts_periodic(phx_ctx *ctx, const phx_block *fb, const phx_rad_block *rb, void *stream);
 
+/* The radiation fields' part of the boundary exchange of a tiled mesh
+ * (phoebus_driver.cpp:646-668; phoebus_boundaries.cpp:42-254, 303-445), on
+ * every FillGhost radiation field (E, F_i, J, H_i/J, xi, phi, c2pfail;
+ * radiation.cpp:448-474, 506-508).  rblocks[n] pairs with blocks[n]; mesh
+ * and blocks as for phx_mesh_exchange, which must have run first (the
+ * primitive rebuild reads the fluid ghosts' velocities).  Ghosts inside the
+ * domain copy the owning block's fields.  Beyond a physical face each field
+ * takes the mapped cell's value: with bc_vars = conserved scaled by the
+ * DetGamma ratios, as every FillGhost field (the radiation primitives
+ * included); F_d and H_d negated across a reflect face on axis d; polar faces
+ * negate no radiation field.  Then, in the outer-X1 slab of an FMKS mesh with
+ * p->enable_ox1_fmks_inflow_check, H^1 < 0 is set to 0 with |H| capped at
+ * 0.99 (:383-411), and with bc_vars = primitive E and F_i are rebuilt from J,
+ * H_i and the ghost's fluid velocity (MomentPrim2Con over the physical
+ * slabs, :436-445). */
+phx_status phx_rad_mesh_exchange(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_mesh *mesh,
+                                 const phx_block *blocks, const phx_rad_block *rblocks, int nblocks, void *stream);
+
+/* FixFluxes' radiation part (fixup.cpp:728-1078) on every block of a tiled
+ * mesh that touches a physical boundary, in place on the radiation flux
+ * arrays; a no-op unless p->enable_flux_fixup.  Boundary faces only, over
+ * the interior of the other axes: reflect faces set the normal flux of E to
+ * 0 (X2 faces also those of F_1 and F_3); polar X2 faces set the X2 fluxes
+ * of E, F_1 and F_3 to 0; gr_outflow leaves the radiation fluxes alone. */
+phx_status phx_rad_fix_fluxes(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_mesh *mesh,
+                              const phx_block *blocks, const phx_rad_block *rblocks, int nblocks, void *stream);
+
 /* radiation::EstimateTimestepBlock (radiation.cpp:585-648): cfl * the
  * minimum over interior zones and active directions of dx / csig, written to
  * dt_out_device. */

@@ -63,8 +63,14 @@ def _pvars(mhd):
 def _exchange_neighbours(mesh, blocks, mhd):
     ncons = abi.NCONS if mhd else 5
     pv = _pvars(mhd) if mesh.bc_vars == abi.BC_VARS_PRIMITIVE else []
+    _copy_neighbours(mesh, blocks, [("prim", pv), ("cons", range(ncons))])
+
+
+def _copy_neighbours(mesh, blocks, fields):
+    """Parthenon's exchange of the FillGhost fields: fields = [(array name,
+    variable indices)]."""
     segs = list(mesh.segments())
-    src = [(b["prim"].copy(), b["cons"].copy()) for b in blocks]  # owners' values before this exchange
+    src = [{n: b[n].copy() for n, _ in fields} for b in blocks]  # owners' values before this exchange
     for b, seg in zip(blocks, segs):
         ng = b.ng
         org = _origin(mesh, seg)
@@ -100,20 +106,17 @@ def _exchange_neighbours(mesh, blocks, mhd):
         ghost = ~(interior[0][I] & interior[1][J] & interior[2][K])
         ins = inside[0][I] & inside[1][J] & inside[2][K]
         out = ghost & ~ins
-        for v in pv:
-            b["prim"][v][out] = np.nan
-        for v in range(ncons):
-            b["cons"][v][out] = np.nan
+        for n, vs in fields:
+            for v in vs:
+                b[n][v][out] = np.nan
         take = ghost & ins
         own = np.vectorize(mesh.block_index)(owner_seg[0][I], owner_seg[1][J], owner_seg[2][K])
         li, lj, lk = local[0][I], local[1][J], local[2][K]
         for o in np.unique(own[take]):
             m = take & (own == o)
-            sp, sc = src[o]
-            for v in pv:
-                b["prim"][v][m] = sp[v][lk[m], lj[m], li[m]]
-            for v in range(ncons):
-                b["cons"][v][m] = sc[v][lk[m], lj[m], li[m]]
+            for n, vs in fields:
+                for v in vs:
+                    b[n][v][m] = src[o][n][v][lk[m], lj[m], li[m]]
 
 
 def _physical_faces(mesh, b, seg):
@@ -246,6 +249,123 @@ def mesh_exchange(orc, p, mesh, blocks):
             for d, outer, _ in faces:
                 orc.PrimitiveToConserved(p, b, *_slab(b, d, outer))
 
+
+# ------------------------------------------------------------------ radiation
+# The FillGhost radiation fields (radiation.cpp:448-474, 506-508): E, F_i and
+# the primitives J, H_i/J, xi, phi, c2pfail (the first RFAIL + 1 of rprim).
+RFILL = abi.RFAIL + 1
+
+
+def _rad_apply_face(b, d, outer, bc, bc_vars):
+    """One boundary function on the radiation fields of one block: every
+    FillGhost field, scaled by the DetGamma ratio under bc_vars = conserved
+    (GenericBC's rescale covers the radiation primitives too), F_d and H_d
+    negated across a reflect face (Metadata::Vector); the polar functions
+    negate only the fluid's v^2 and B^2."""
+    ng, nd = b.ng, b.nx[d]
+    lo_i, hi_i = ng, ng + nd - 1
+    ghosts = range(hi_i + 1, hi_i + 1 + ng) if outer else range(0, ng)
+    ref = hi_i if outer else lo_i
+    axis = 3 - d
+    conserved = bc_vars == abi.BC_VARS_CONSERVED
+    detg = np.broadcast_to(_detg(b), (b.n3t, b.n2t, b.n1t))
+    for g in ghosts:
+        r = ref if bc == OUTFLOW else (2 * ref + (1 if outer else -1)) - g
+        dst = [slice(None)] * 4
+        src = [slice(None)] * 4
+        dst[axis], src[axis] = g, r
+        for name, nv, vec in (("rcons", abi.RNCONS, abi.RF), ("rprim", RFILL, abi.RH)):
+            val = b[name][tuple(src)].copy()
+            sg = np.ones(nv)
+            if bc == REFLECT:
+                sg[vec + d] = -1.0
+            if conserved:
+                gratio = _ratio(detg[tuple(dst[1:])], detg[tuple(src[1:])])
+                for v in range(nv):
+                    b[name][(v,) + tuple(dst[1:])] = sg[v] * gratio * val[v]
+            else:
+                for v in range(nv):
+                    b[name][(v,) + tuple(dst[1:])] = sg[v] * val[v]
+
+
+def _rad_inflow_check(b, ib, jb, kb):
+    """phoebus_boundaries.cpp:383-411: no radiation flux into the domain
+    through the outer X1 face.  Where H^1 = gamma^1j H_j < 0: H^1 = 0, |H|
+    capped at 0.99, H_i = gamma_ij H^j; in the reference's operation order."""
+    ks, js, is_ = slice(kb[0], kb[1] + 1), slice(jb[0], jb[1] + 1), slice(ib[0], ib[1] + 1)
+    t = b.geom.arrays["cent"][:, js, is_][:, None, :, :]
+
+    def flat(a, c):
+        hi, lo = max(a, c), min(a, c)
+        return hi * (hi + 1) // 2 + lo
+
+    gcov = [[t[abi.G_GCOV + flat(a + 1, c + 1)] for c in range(3)] for a in range(3)]
+    gcon = [[t[abi.G_GAMCON + flat(a, c)] for c in range(3)] for a in range(3)]
+    P = b["rprim"]
+    H = [P[abi.RH + a, ks, js, is_].copy() for a in range(3)]
+    Hcon = []
+    for a in range(3):
+        acc = np.zeros_like(H[0])
+        for c in range(3):
+            acc = acc + gcon[a][c] * H[c]
+        Hcon.append(acc)
+    fix = Hcon[0] < 0.0
+    Hcon[0] = np.zeros_like(Hcon[0])
+    xi = np.zeros_like(H[0])
+    for a in range(3):
+        for c in range(3):
+            xi = xi + gcov[a][c] * Hcon[a] * Hcon[c]
+    xi = np.sqrt(xi)
+    cap = xi > 0.99
+    with np.errstate(invalid="ignore", divide="ignore"):
+        Hcon = [np.where(cap, h * (0.99 / xi), h) for h in Hcon]
+    for a in range(3):
+        acc = np.zeros_like(H[0])
+        for c in range(3):
+            acc = acc + gcov[a][c] * Hcon[c]
+        P[abi.RH + a, ks, js, is_] = np.where(fix, acc, H[a])
+
+
+def rad_mesh_exchange(rorc, rp, p, mesh, blocks):
+    """The radiation fields' exchange on host blocks, in place, after the
+    fluid's (mesh_exchange): neighbours, the boundary functions face by face,
+    then ConvertBoundaryConditions' radiation steps (rorc: oracle.RadOracle)."""
+    _copy_neighbours(mesh, blocks, [("rcons", range(abi.RNCONS)), ("rprim", range(RFILL))])
+    segs = list(mesh.segments())
+    for b, seg in zip(blocks, segs):
+        for d, outer, bc in _physical_faces(mesh, b, seg):
+            _rad_apply_face(b, d, outer, bc, mesh.bc_vars)
+    conserved = mesh.bc_vars == abi.BC_VARS_CONSERVED
+    for b, seg in zip(blocks, segs):
+        faces = _physical_faces(mesh, b, seg)
+        if b.geom is not None and p.enable_ox1_fmks_inflow_check and any(d == 0 and o for d, o, _ in faces):
+            _rad_inflow_check(b, *_slab(b, 0, True))
+        if not conserved:
+            for d, outer, _ in faces:
+                rorc.MomentPrim2Con(rp, p, b, *_slab(b, d, outer))
+
+
+def rad_fix_fluxes(p, mesh, blocks):
+    """FixFluxes' radiation part (fixup.cpp:728-1078) on the blocks'
+    radiation fluxes, in place: on each physical face, over the interior of
+    the other axes, reflect zeroes the normal flux of E (X2 faces also F_1,
+    F_3), polar the X2 fluxes of E, F_1, F_3; gr_outflow none."""
+    if not p.enable_flux_fixup:
+        return
+    for b, seg in zip(blocks, mesh.segments()):
+        (i0, i1), (j0, j1), (k0, k1) = b.interior()
+        for d, outer, bc in _physical_faces(mesh, b, seg):
+            if bc == REFLECT:
+                comps = [abi.RE] + ([abi.RF, abi.RF + 2] if d == 1 else [])
+            elif bc == POLAR:
+                comps = [abi.RE, abi.RF, abi.RF + 2]
+            else:
+                continue
+            f = b.ng + b.nx[d] if outer else b.ng
+            rng = [slice(i0, i1 + 1), slice(j0, j1 + 1), slice(k0, k1 + 1)]
+            rng[d] = f
+            for m in comps:
+                b["rflux"][d * abi.RNCONS + m, rng[2], rng[1], rng[0]] = 0.0
 
 def fix_fluxes_block(p, b, bc_lo, bc_hi):
     """fixup::FixFluxes on one host block's flux array, in place; bc_lo /

@@ -199,6 +199,10 @@ _SIGS = {
     "phx_rad_update": (C.c_int, [_P, C.POINTER(RadParams), C.POINTER(BlockS), C.POINTER(RadBlockS), _P, _P, C.c_double, C.c_double, _P]),
     "phx_rad_fluid_source": (C.c_int, [_P, C.POINTER(RadParams), C.POINTER(Params), C.POINTER(BlockS), C.POINTER(RadBlockS), C.c_double, _P]),
     "phx_rad_fill_ghosts_periodic": (C.c_int, [_P, C.POINTER(BlockS), C.POINTER(RadBlockS), _P]),
+    "phx_rad_fix_fluxes": (C.c_int, [_P, C.POINTER(RadParams), C.POINTER(Params), C.POINTER(Mesh),
+                                     C.POINTER(BlockS), C.POINTER(RadBlockS), C.c_int, _P]),
+    "phx_rad_mesh_exchange": (C.c_int, [_P, C.POINTER(RadParams), C.POINTER(Params), C.POINTER(Mesh),
+                                        C.POINTER(BlockS), C.POINTER(RadBlockS), C.c_int, _P]),
     "phx_rad_estimate_timestep": (C.c_int, [_P, C.POINTER(RadParams), C.POINTER(Params), C.POINTER(BlockS), C.POINTER(RadBlockS), _P, _P]),
     "phx_rad_stage": (C.c_int, [_P, C.POINTER(RadParams), C.POINTER(Params), C.POINTER(BlockS), C.POINTER(RadBlockS), _P, _P, C.c_double, C.c_double, _P]),
     "phx_rad_fluid_stage": (C.c_int, [_P, C.POINTER(RadParams), C.POINTER(Params), C.POINTER(BlockS), C.POINTER(RadBlockS), _P, _P, _P, _P, C.c_double, C.c_double, _P]),

@@ -1240,6 +1240,113 @@ phx_status phx_rad_fill_ghosts_periodic(phx_ctx *ctx, const phx_block *fb, const
   return cuda_status("phx_rad_fill_ghosts_periodic");
 }
 
+phx_status phx_rad_mesh_exchange(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_mesh *mesh,
+                                 const phx_block *blocks, const phx_rad_block *rblocks, int nblocks, void *stream) {
+  phx_status s;
+  if ((s = ctx_device(ctx)) || (s = check_params(p))) return s;
+  std::vector<phx::BView> views;
+  if ((s = check_mesh(mesh, p, blocks, nblocks, views))) return s;
+  if (!rblocks) return fail(PHX_ERR_INVALID_ARG, "radiation blocks is NULL");
+  std::vector<phx::rad::RView> rviews(nblocks);
+  for (int n = 0; n < nblocks; n++) {
+    if ((s = check_rad(rp, p, &blocks[n]))) return s;
+    if ((s = make_rview(views[n], &rblocks[n], false, rviews[n]))) return fail(s, "block %d: %s", n, g_last_error.c_str());
+  }
+  const phx::rad::RPar par = make_rpar(*rp, *p);
+  // One stream-ordered table: per-axis cell -> segment, block -> origin, the
+  // block and radiation views (blocks are ordered by segment triple, so the
+  // owner of segment triple s is block s).
+  std::vector<int> ints;
+  size_t off_seg[3];
+  for (int d = 0; d < 3; d++) {
+    off_seg[d] = ints.size();
+    for (int g = 0; g < mesh->nseg[d]; g++)
+      for (int c = mesh->seg_start[d][g]; c < mesh->seg_start[d][g + 1]; c++) ints.push_back(g);
+  }
+  const size_t off_owner = ints.size();
+  for (int b = 0; b < nblocks; b++) ints.push_back(b);
+  const size_t off_origin = ints.size();
+  for (int s3 = 0; s3 < mesh->nseg[2]; s3++)
+    for (int s2 = 0; s2 < mesh->nseg[1]; s2++)
+      for (int s1 = 0; s1 < mesh->nseg[0]; s1++) {
+        ints.push_back(mesh->seg_start[0][s1]);
+        ints.push_back(mesh->seg_start[1][s2]);
+        ints.push_back(mesh->seg_start[2][s3]);
+      }
+  auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t b_views = up(sizeof(phx::BView) * nblocks), b_rviews = up(sizeof(phx::rad::RView) * nblocks);
+  const size_t bytes = b_views + b_rviews + sizeof(int) * ints.size();
+  std::vector<unsigned char> host(bytes);
+  memcpy(host.data(), views.data(), sizeof(phx::BView) * nblocks);
+  memcpy(host.data() + b_views, rviews.data(), sizeof(phx::rad::RView) * nblocks);
+  memcpy(host.data() + b_views + b_rviews, ints.data(), sizeof(int) * ints.size());
+  cudaStream_t st = S(stream);
+  unsigned char *dev = nullptr;
+  cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&dev), bytes, st);
+  if (e != cudaSuccess) return fail(PHX_ERR_CUDA, "phx_rad_mesh_exchange: %s", cudaGetErrorString(e));
+  // pageable source: the call returns once the table is staged
+  e = cudaMemcpyAsync(dev, host.data(), bytes, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    const phx::BView *dviews = reinterpret_cast<const phx::BView *>(dev);
+    const phx::rad::RView *drviews = reinterpret_cast<const phx::rad::RView *>(dev + b_views);
+    const int *base = reinterpret_cast<const int *>(dev + b_views + b_rviews);
+    phx::MeshDev md{};
+    md.bc_vars = mesh->bc_vars;
+    for (int d = 0; d < 3; d++) {
+      md.n[d] = mesh->n[d];
+      md.nseg[d] = mesh->nseg[d];
+      md.bc_lo[d] = mesh->bc_lo[d];
+      md.bc_hi[d] = mesh->bc_hi[d];
+      md.seg_of[d] = base + off_seg[d];
+    }
+    md.owner = base + off_owner;
+    md.origin = base + off_origin;
+    const int inflow = p->enable_ox1_fmks_inflow_check ? 1 : 0;
+    for (int n = 0; n < nblocks; n++)
+      phx::rad::launch_mesh_ghosts(par, !views[n].fmks, views[n], dviews, drviews, md, n, inflow, st);
+  }
+  const cudaError_t e2 = cudaFreeAsync(dev, st);
+  if (e == cudaSuccess) e = e2;
+  if (e != cudaSuccess) return fail(PHX_ERR_CUDA, "phx_rad_mesh_exchange: %s", cudaGetErrorString(e));
+  return cuda_status("phx_rad_mesh_exchange");
+}
+
+phx_status phx_rad_fix_fluxes(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p, const phx_mesh *mesh,
+                              const phx_block *blocks, const phx_rad_block *rblocks, int nblocks, void *stream) {
+  phx_status s;
+  if ((s = ctx_device(ctx)) || (s = check_params(p))) return s;
+  std::vector<phx::BView> views;
+  if ((s = check_mesh(mesh, p, blocks, nblocks, views))) return s;
+  if (!rblocks) return fail(PHX_ERR_INVALID_ARG, "radiation blocks is NULL");
+  std::vector<phx::rad::RView> rviews(nblocks);
+  for (int n = 0; n < nblocks; n++) {
+    if ((s = check_rad(rp, p, &blocks[n]))) return s;
+    if ((s = make_rview(views[n], &rblocks[n], false, rviews[n]))) return fail(s, "block %d: %s", n, g_last_error.c_str());
+    if (!rblocks[n].flux) return fail(PHX_ERR_INVALID_ARG, "block %d: radiation flux is NULL", n);
+  }
+  if (!p->enable_flux_fixup) return PHX_OK;
+  cudaStream_t st = S(stream);
+  for (int s3 = 0, b = 0; s3 < mesh->nseg[2]; s3++)
+    for (int s2 = 0; s2 < mesh->nseg[1]; s2++)
+      for (int s1 = 0; s1 < mesh->nseg[0]; s1++, b++) {
+        const int seg[3] = {s1, s2, s3};
+        const phx::BView &v = views[b];
+        const int nx[3] = {v.nx1, v.nx2, v.nx3};
+        for (int d = 0; d < v.ndim; d++)
+          for (int outer = 0; outer < 2; outer++) {
+            const bool edge = outer ? seg[d] == mesh->nseg[d] - 1 : seg[d] == 0;
+            const int bc = outer ? mesh->bc_hi[d] : mesh->bc_lo[d];
+            if (!edge || bc == PHX_BC_PERIODIC) continue;
+            // reflect: E (X2 faces also F_1, F_3); polar: E, F_1, F_3; gr_outflow: none
+            unsigned mask = 0;
+            if (bc == PHX_BC_REFLECT) mask = 1u << PHX_RE | (d == 1 ? (1u << PHX_RF | 1u << (PHX_RF + 2)) : 0u);
+            if (bc == PHX_BC_POLAR) mask = 1u << PHX_RE | 1u << PHX_RF | 1u << (PHX_RF + 2);
+            if (mask) phx::rad::launch_fix_face(v, rviews[b], d, outer ? v.ng + nx[d] : v.ng, mask, st);
+          }
+      }
+  return cuda_status("phx_rad_fix_fluxes");
+}
+
 phx_status phx_rad_estimate_timestep(phx_ctx *ctx, const phx_rad_params *rp, const phx_params *p,
                                      const phx_block *fb, const phx_rad_block *rb, double *dt_out_device,
                                      void *stream) {

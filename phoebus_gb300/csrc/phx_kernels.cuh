@@ -119,6 +119,82 @@ struct MeshDev {
   const int *owner;      // [nseg[2]][nseg[1]][nseg[0]]
   const int *origin;     // [nblocks][3] global index of the first interior cell
 };
+// Where ghost cell t of block blk takes its values from.  Periodic axes
+// wrap; beyond a physical face gr_outflow clamps to the boundary cell and
+// reflect / polar mirror about the face.  src / sid: the owner block and cell
+// of the mapped global cell; mloc[d]: the mapped local index on each axis
+// (the cell Parthenon's face loop reads); phys[d]: axis d crossed a physical
+// face; reflect[d]: that face is reflect (vector components along d flip);
+// mirror[d]: reflect or polar.
+struct GhostMap {
+  bool ghost, physical, outer_x1;
+  bool phys[3], reflect[3], mirror[3];
+  int loc[3], mloc[3];
+  int src;
+  long long id, sid;
+};
+#ifdef __CUDACC__
+__device__ __forceinline__ GhostMap map_ghost(const BView *views, const MeshDev &m, int blk, long long t) {
+  const BView &b = views[blk];
+  GhostMap q;
+  q.loc[0] = (int)(t % b.n1t);
+  q.loc[1] = (int)((t / b.n1t) % b.n2t);
+  q.loc[2] = (int)(t / ((long long)b.n1t * b.n2t));
+  const int nx[3] = {b.nx1, b.nx2, b.nx3};
+  const int nd = b.ndim;
+  q.ghost = q.physical = q.outer_x1 = false;
+  int g[3];
+  for (int d = 0; d < 3; d++) {
+    q.mloc[d] = q.loc[d];
+    q.phys[d] = q.reflect[d] = q.mirror[d] = false;
+    g[d] = 0;
+    if (d >= nd) continue;  // inactive axis: one cell, no ghosts
+    if (q.loc[d] < b.ng || q.loc[d] >= b.ng + nx[d]) q.ghost = true;
+    int gg = m.origin[blk * 3 + d] + q.loc[d] - b.ng;
+    if (gg < 0 || gg >= m.n[d]) {
+      const bool lo = gg < 0;
+      const int bc = lo ? m.bc_lo[d] : m.bc_hi[d];
+      if (bc == PHX_BC_PERIODIC) {
+        gg += lo ? m.n[d] : -m.n[d];
+      } else {
+        q.physical = q.phys[d] = true;
+        if (d == 0 && !lo) q.outer_x1 = true;
+        const int ref = lo ? b.ng : b.ng + nx[d] - 1;  // interior cell next to the face (local)
+        if (bc == PHX_BC_OUTFLOW) {
+          gg = lo ? 0 : m.n[d] - 1;
+          q.mloc[d] = ref;
+        } else {  // reflect / polar: mirror about the face
+          gg = lo ? -1 - gg : 2 * m.n[d] - 1 - gg;
+          q.mloc[d] = 2 * ref + (lo ? -1 : 1) - q.loc[d];
+          q.mirror[d] = true;
+          q.reflect[d] = bc == PHX_BC_REFLECT;
+        }
+      }
+    }
+    g[d] = gg;
+  }
+  q.src = -1;
+  q.id = q.sid = 0;
+  if (!q.ghost) return q;
+  q.src = m.owner[(m.seg_of[2][g[2]] * m.nseg[1] + m.seg_of[1][g[1]]) * m.nseg[0] + m.seg_of[0][g[0]]];
+  const BView &sb = views[q.src];
+  int sl[3];
+  for (int d = 0; d < 3; d++) sl[d] = d < nd ? g[d] - m.origin[q.src * 3 + d] + sb.ng : 0;
+  q.sid = sb.idx(sl[2], sl[1], sl[0]);
+  q.id = b.idx(q.loc[2], q.loc[1], q.loc[0]);
+  return q;
+}
+// robust::ratio(DetGamma(c), DetGamma(r)) of face d's boundary loop (FMKS):
+// c is the cell that loop sets (axes before d at the ghost's own index, axes
+// after it already mapped), r the cell it reads (c mapped on axis d).
+__device__ __forceinline__ double ghost_gratio(const BView &b, const GhostMap &q, int d) {
+  int c[3], r[3];
+  for (int e = 0; e < 3; e++) c[e] = e < d ? q.loc[e] : (e == d ? q.loc[d] : q.mloc[e]);
+  for (int e = 0; e < 3; e++) r[e] = e == d ? q.mloc[d] : c[e];
+  const double *detg = b.gcent + (long long)PHX_G_DETGAM * b.n2t * b.n1t;
+  return ratio_p(detg[(long long)c[1] * b.n1t + c[0]], detg[(long long)r[1] * b.n1t + r[0]]);
+}
+#endif
 void launch_mesh_exchange(const Par &p, bool mink, const BView *views, const MeshDev &m, const WorkItem *items,
                           int nitems, int grid, cudaStream_t s);
 // FixFluxes: the physical-boundary faces of a block, per face (X1 lo, X1 hi,

@@ -1982,6 +1982,142 @@ void launch_source(const RPar &p, const Par &fp, const BView &b, const RView &r,
     source_t<true>(p, fp, b, r, dt, rg, g, s);
 }
 
+// ------------------------------------------ boundary exchange of a tiled mesh
+// The radiation half of PhoebusDriver's exchange (phoebus_driver.cpp:646-668)
+// for one ghost: every radiation field with Metadata::FillGhost (E, F_i and
+// J, H_i/J, xi, phi, c2pfail; radiation.cpp:448-474, 506-508).  Inside the
+// domain the owner's values are copied.  Beyond a physical face the boundary
+// functions act on every FillGhost field (phoebus_boundaries.cpp:42-254): the
+// mapped cell's value, with bc_vars = conserved scaled at each face by
+// robust::ratio(DetGamma(cell), DetGamma(source)) -- the radiation primitives
+// too, since they carry FillGhost under either bc_vars -- and F_d, H_d
+// negated across a reflect face along d (Metadata::Vector); the polar faces
+// negate only the fluid's v^2 and B^2 (PolarInnerX2 / PolarOuterX2).
+// ConvertBoundaryConditions (:303-445) then, in the outer-X1 slab of an FMKS
+// mesh with the inflow check, removes radiation flux entering the domain
+// (H^1 < 0: H^1 = 0, |H| capped at 0.99, H_i lowered again), and with
+// bc_vars = primitive rebuilds E, F_i from J, H_i and the fluid velocity of
+// the ghost (MomentPrim2Con over the physical slabs).
+template <bool M1, bool MINK>
+__global__ void __launch_bounds__(128) k_mesh_ghost(RPar p, const BView *views, const RView *rviews, MeshDev m,
+                                                    int blk, int inflow) {
+  const BView &b = views[blk];
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)b.n1t * b.n2t * b.n3t) return;
+  const GhostMap q = map_ghost(views, m, blk, t);
+  if (!q.ghost) return;
+  const RView &r = rviews[blk], &sr = rviews[q.src];
+  constexpr int NP = PHX_RFAIL + 1;  // the FillGhost primitives
+  double U[PHX_RNCONS], P[NP];
+#pragma unroll
+  for (int v = 0; v < PHX_RNCONS; v++) U[v] = sr.cons[v * sr.vs + q.sid];
+#pragma unroll
+  for (int v = 0; v < NP; v++) P[v] = sr.prim[v * sr.vs + q.sid];
+  if (q.physical) {
+    const bool conserved = m.bc_vars == PHX_BC_VARS_CONSERVED;
+    for (int d = 0; d < b.ndim; d++) {
+      if (!q.phys[d]) continue;
+      const double sg = q.reflect[d] ? -1.0 : 1.0;
+      double gr = 1.0;  // DetGamma = 1 in Minkowski: ratio(1, 1) = 1
+      if (!MINK && conserved) gr = ghost_gratio(b, q, d);
+#pragma unroll
+      for (int v = 0; v < PHX_RNCONS; v++) {
+        const double s = v == PHX_RF + d ? sg : 1.0;
+        U[v] = conserved ? s * gr * U[v] : s * U[v];
+      }
+#pragma unroll
+      for (int v = 0; v < NP; v++) {
+        const double s = v == PHX_RH + d ? sg : 1.0;
+        P[v] = conserved ? s * gr * P[v] : s * P[v];
+      }
+    }
+    const RGeo<MINK> G(b, 0, q.loc[1], q.loc[0]);
+    if constexpr (!MINK) {
+      if (inflow && q.outer_x1) {  // no flux of radiation into the domain (:383-411)
+        double Hcon[3] = {0.0, 0.0, 0.0};
+        for (int a = 0; a < 3; a++)
+          for (int c = 0; c < 3; c++) Hcon[a] += G.con(a, c) * P[PHX_RH + c];
+        if (Hcon[0] < 0.) {
+          Hcon[0] = 0.;
+          double xi = 0.;
+          for (int a = 0; a < 3; a++)
+            for (int c = 0; c < 3; c++) xi += G.cov(a, c) * Hcon[a] * Hcon[c];
+          xi = sqrt(xi);
+          if (xi > 0.99)
+            for (int a = 0; a < 3; a++) Hcon[a] *= 0.99 / xi;
+          for (int a = 0; a < 3; a++) {
+            P[PHX_RH + a] = 0.;
+            for (int c = 0; c < 3; c++) P[PHX_RH + a] += G.cov(a, c) * Hcon[c];
+          }
+        }
+      }
+    }
+    if (!conserved) {  // MomentPrim2Con (moments.cpp:198-275) at the ghost
+      const Closure<M1, MINK> c(fluid_v<MINK>(b, q.id, G.geo()), true, G.geo());
+      const double J = P[PHX_RJ];
+      V3 H;
+#pragma unroll
+      for (int a = 0; a < 3; a++) H.d[a] = P[PHX_RH + a] * J;
+      T2 Pi;
+      c.tilpi_from_prim(J, H, Pi);
+      double E;
+      V3 F;
+      c.prim2con(J, H, Pi, E, F);
+      const double sdetgam = G.sdetgam();
+      U[PHX_RE] = sdetgam * E;
+#pragma unroll
+      for (int a = 0; a < 3; a++) U[PHX_RF + a] = sdetgam * F.d[a];
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < PHX_RNCONS; v++) r.cons[v * r.vs + q.id] = U[v];
+#pragma unroll
+  for (int v = 0; v < NP; v++) r.prim[v * r.vs + q.id] = P[v];
+}
+
+void launch_mesh_ghosts(const RPar &p, bool mink, const BView &b, const BView *views, const RView *rviews,
+                        const MeshDev &m, int blk, int inflow, cudaStream_t s) {
+  const unsigned g = blocks_for((long long)b.n1t * b.n2t * b.n3t, 128);
+  if (p.m1) {
+    if (mink)
+      k_mesh_ghost<true, true><<<g, 128, 0, s>>>(p, views, rviews, m, blk, 0);
+    else
+      k_mesh_ghost<true, false><<<g, 128, 0, s>>>(p, views, rviews, m, blk, inflow);
+  } else {
+    if (mink)
+      k_mesh_ghost<false, true><<<g, 128, 0, s>>>(p, views, rviews, m, blk, 0);
+    else
+      k_mesh_ghost<false, false><<<g, 128, 0, s>>>(p, views, rviews, m, blk, inflow);
+  }
+}
+
+// FixFluxes' radiation part (fixup.cpp:728-1078) on one physical face of a
+// block: the direction-d fluxes of the moments in mask (bit m: conserved
+// moment m) set to 0 at local face index f, over the interior of the other
+// axes.
+__global__ void __launch_bounds__(256) k_fix_face(BView b, RView r, int d, int f, unsigned mask) {
+  const int ng = b.ng;
+  const int e1 = b.nx1, e2 = b.ndim >= 2 ? b.nx2 : 1, e3 = b.ndim >= 3 ? b.nx3 : 1;
+  const int na = d == 0 ? e2 : e1, nb = d == 2 ? e2 : e3;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)na * nb) return;
+  const int a = (int)(t % na), c = (int)(t / na);
+  const int o2 = b.ndim >= 2 ? ng : 0, o3 = b.ndim >= 3 ? ng : 0;
+  const int i = d == 0 ? f : ng + a;
+  const int j = d == 1 ? f : (d == 0 ? o2 + a : o2 + c);
+  const int k = d == 2 ? f : o3 + c;
+  const long long id = b.idx(k, j, i);
+#pragma unroll
+  for (int m = 0; m < PHX_RNCONS; m++)
+    if ((mask >> m) & 1u) r.flux[((long long)d * PHX_RNCONS + m) * r.vs + id] = 0.0;
+}
+
+void launch_fix_face(const BView &b, const RView &r, int d, int f, unsigned mask, cudaStream_t s) {
+  const long long e1 = b.nx1, e2 = b.ndim >= 2 ? b.nx2 : 1, e3 = b.ndim >= 3 ? b.nx3 : 1;
+  const long long n = d == 0 ? e2 * e3 : (d == 1 ? e1 * e3 : e1 * e2);
+  k_fix_face<<<blocks_for(n, 256), 256, 0, s>>>(b, r, d, f, mask);
+}
+
 void launch_ghosts(const BView &b, const RView &r, cudaStream_t s) {
   BView v = b;
   v.vs = r.vs;

@@ -44,6 +44,15 @@ void launch_update(const RPar &p, const BView &b, const RView &r, const double *
 // ceilings, as MomentFluidSourceImpl sets them up)
 void launch_source(const RPar &p, const Par &fp, const BView &b, const RView &r, double dt, cudaStream_t s);
 void launch_ghosts(const BView &b, const RView &r, cudaStream_t s);
+// The radiation fields' boundary exchange of block blk of a tiled mesh
+// (views / rviews: device arrays over the mesh's blocks); inflow: the FMKS
+// outer-X1 inflow check is on.  Reads the fluid ghosts' primitives, so it runs
+// after the fluid's exchange.
+void launch_mesh_ghosts(const RPar &p, bool mink, const BView &b, const BView *views, const RView *rviews,
+                        const MeshDev &m, int blk, int inflow, cudaStream_t s);
+// the direction-d radiation fluxes of the moments in mask (bit m: moment m)
+// zeroed on local face index f over the interior of the other axes
+void launch_fix_face(const BView &b, const RView &r, int d, int f, unsigned mask, cudaStream_t s);
 // RadConservedToPrimitiveFixup over the interior
 void launch_rad_c2p_fixup(const RPar &p, const BView &b, const RView &r, cudaStream_t s);
 // the radiation part of ApplyFloors over rg; flag[N]: nonzero where the fluid

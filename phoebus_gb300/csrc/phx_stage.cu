@@ -430,46 +430,15 @@ template <bool MINK>
 __device__ __forceinline__ void mesh_ghost_at(const Par &p, const BView *views, const MeshDev &m, int blk,
                                               long long t) {
   const BView &b = views[blk];
-  const int loc[3] = {(int)(t % b.n1t), (int)((t / b.n1t) % b.n2t), (int)(t / ((long long)b.n1t * b.n2t))};
-  const int nx[3] = {b.nx1, b.nx2, b.nx3};
+  const GhostMap q = map_ghost(views, m, blk, t);
+  if (!q.ghost) return;
   const int nd = b.ndim;
-  bool ghost = false, physical = false, outer_x1 = false;
-  bool phys[3] = {false, false, false};
-  int g[3], mloc[3] = {loc[0], loc[1], loc[2]};  // source cell (global); mapped local index per axis
-  double sgn_v[3] = {1.0, 1.0, 1.0};             // sign of the axis-d vector components from a mirror
-  for (int d = 0; d < 3; d++) {
-    g[d] = 0;
-    if (d >= nd) continue;  // inactive axis: one cell, no ghosts
-    if (loc[d] < b.ng || loc[d] >= b.ng + nx[d]) ghost = true;
-    int gg = m.origin[blk * 3 + d] + loc[d] - b.ng;
-    if (gg < 0 || gg >= m.n[d]) {
-      const bool lo = gg < 0;
-      const int bc = lo ? m.bc_lo[d] : m.bc_hi[d];
-      if (bc == PHX_BC_PERIODIC) {
-        gg += lo ? m.n[d] : -m.n[d];
-      } else {
-        physical = phys[d] = true;
-        if (d == 0 && !lo) outer_x1 = true;
-        const int ref = lo ? b.ng : b.ng + nx[d] - 1;  // interior cell next to the face (local)
-        if (bc == PHX_BC_OUTFLOW) {
-          gg = lo ? 0 : m.n[d] - 1;
-          mloc[d] = ref;
-        } else {  // reflect / polar: mirror about the face
-          gg = lo ? -1 - gg : 2 * m.n[d] - 1 - gg;
-          mloc[d] = 2 * ref + (lo ? -1 : 1) - loc[d];
-          sgn_v[d] = -1.0;
-        }
-      }
-    }
-    g[d] = gg;
-  }
-  if (!ghost) return;
-  const int src = m.owner[(m.seg_of[2][g[2]] * m.nseg[1] + m.seg_of[1][g[1]]) * m.nseg[0] + m.seg_of[0][g[0]]];
-  const BView &sb = views[src];
-  int sl[3];
-  for (int d = 0; d < 3; d++) sl[d] = d < nd ? g[d] - m.origin[src * 3 + d] + sb.ng : 0;
-  const long long sid = sb.idx(sl[2], sl[1], sl[0]);
-  const long long id = b.idx(loc[2], loc[1], loc[0]);
+  const bool physical = q.physical, outer_x1 = q.outer_x1;
+  double sgn_v[3];  // sign of the axis-d vector components from a mirror
+  for (int d = 0; d < 3; d++) sgn_v[d] = q.mirror[d] ? -1.0 : 1.0;
+  const BView &sb = views[q.src];
+  const long long sid = q.sid, id = q.id;
+  const int *loc = q.loc;
   const int ncons = p.mhd ? PHX_NCONS : PHX_CB;
   const bool prim_vars = m.bc_vars == PHX_BC_VARS_PRIMITIVE;
   if (!physical) {
@@ -485,15 +454,9 @@ __device__ __forceinline__ void mesh_ghost_at(const Par &p, const BView *views, 
     double U[PHX_NCONS];
     for (int v = 0; v < ncons; v++) U[v] = sb.cons[v * sb.vs + sid];
     for (int d = 0; d < nd; d++) {
-      if (!phys[d]) continue;
+      if (!q.phys[d]) continue;
       double gr = 1.0;  // DetGamma = 1 in Minkowski: ratio(1, 1) = 1
-      if constexpr (!MINK) {
-        int c[3], r[3];
-        for (int e = 0; e < 3; e++) c[e] = e < d ? loc[e] : (e == d ? loc[d] : mloc[e]);
-        for (int e = 0; e < 3; e++) r[e] = e == d ? mloc[d] : c[e];
-        const double *detg = b.gcent + (long long)PHX_G_DETGAM * b.n2t * b.n1t;
-        gr = ratio_p(detg[(long long)c[1] * b.n1t + c[0]], detg[(long long)r[1] * b.n1t + r[0]]);
-      }
+      if constexpr (!MINK) gr = ghost_gratio(b, q, d);
       for (int v = 0; v < ncons; v++) {
         const double sg = (v == PHX_CMOM + d || v == PHX_CB + d) ? sgn_v[d] : 1.0;
         U[v] = sg * gr * U[v];

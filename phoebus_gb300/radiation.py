@@ -117,6 +117,26 @@ class RadiationContext:
         s, r = b.struct(), rad_struct(b)
         self._ok(self.lib.phx_rad_fill_ghosts_periodic(self.h, C.byref(s), C.byref(r), _stream(stream)))
 
+    def MeshExchange(self, rp, p, mesh, blocks, stream=None):
+        """The radiation fields' boundary exchange of a tiled mesh
+        (phx_rad_mesh_exchange); run after the fluid's (FluidContext.MeshExchange)."""
+        n = len(blocks)
+        arr = (abi.BlockS * n)(*[b.struct() for b in blocks])
+        rarr = (abi.RadBlockS * n)(*[rad_struct(b) for b in blocks])
+        m = mesh.struct()
+        self._ok(self.lib.phx_rad_mesh_exchange(self.h, C.byref(rp), C.byref(p), C.byref(m), arr, rarr, n,
+                                                _stream(stream)))
+
+    def FixFluxes(self, rp, p, mesh, blocks, stream=None):
+        """FixFluxes' radiation part on the blocks' radiation fluxes
+        (phx_rad_fix_fluxes)."""
+        n = len(blocks)
+        arr = (abi.BlockS * n)(*[b.struct() for b in blocks])
+        rarr = (abi.RadBlockS * n)(*[rad_struct(b) for b in blocks])
+        m = mesh.struct()
+        self._ok(self.lib.phx_rad_fix_fluxes(self.h, C.byref(rp), C.byref(p), C.byref(m), arr, rarr, n,
+                                             _stream(stream)))
+
     def EstimateTimestepBlock(self, rp, p, b: Block, out=None, stream=None) -> float:
         """cfl * min dx / csig; returns a float (synchronising) unless out (a
         one-element CUDA tensor) is given."""

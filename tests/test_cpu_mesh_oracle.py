@@ -203,3 +203,89 @@ def test_conserved_exchange_inflow_check(built):
         cons = b["cons"].copy()
         orc.PrimitiveToConserved(p, b, ib, jb, kb)
         np.testing.assert_array_equal(b["cons"][(slice(None),) + sl], cons[(slice(None),) + sl])
+
+
+def rad_closed_form(mesh, blocks):
+    """The radiation fields' composed map per ghost: every FillGhost field
+    from the source cell of all axes' maps, F_d and H_d negated per reflect
+    axis (polar negates none), and under bc_vars = conserved every field
+    times the DetGamma ratios in face order."""
+    out = [(b["rcons"].copy(), b["rprim"].copy()) for b in blocks]
+    conserved = mesh.bc_vars == abi.BC_VARS_CONSERVED
+    for (U, P), b, seg in zip(out, blocks, mesh.segments()):
+        org = [int(mesh.starts[d][seg[d]]) for d in range(3)]
+        detg = b.geom.arrays["cent"][abi.G_DETGAM]
+        for k in range(b.n3t):
+            for j in range(b.n2t):
+                for i in range(b.n1t):
+                    loc = [i, j, k]
+                    mloc, g, ghost, phys, refl = list(loc), [], False, [False] * 3, [False] * 3
+                    for d in range(3):
+                        if d >= b.ndim:
+                            g.append(0)
+                            continue
+                        ghost |= not b.ng <= loc[d] < b.ng + b.nx[d]
+                        gg = org[d] + loc[d] - b.ng
+                        if gg < 0 or gg >= mesh.n[d]:
+                            lo = gg < 0
+                            bc = mesh.bc_lo[d] if lo else mesh.bc_hi[d]
+                            ref = b.ng if lo else b.ng + b.nx[d] - 1
+                            if bc == abi.BC_PERIODIC:
+                                gg += mesh.n[d] if lo else -mesh.n[d]
+                            elif bc == abi.BC_OUTFLOW:
+                                phys[d], gg, mloc[d] = True, 0 if lo else mesh.n[d] - 1, ref
+                            else:
+                                phys[d] = True
+                                gg = -1 - gg if lo else 2 * mesh.n[d] - 1 - gg
+                                mloc[d] = 2 * ref + (-1 if lo else 1) - loc[d]
+                                refl[d] = bc == abi.BC_REFLECT
+                        g.append(gg)
+                    if not ghost:
+                        continue
+                    o, (li, lj, lk) = mo._owner_cell(mesh, g)
+                    sl = tuple(x + b.ng if d < b.ndim else 0 for d, x in enumerate((li, lj, lk)))
+                    q_u = blocks[o]["rcons"][:, sl[2], sl[1], sl[0]].copy()
+                    q_p = blocks[o]["rprim"][:mo.RFILL, sl[2], sl[1], sl[0]].copy()
+                    for d in range(3):
+                        if not phys[d]:
+                            continue
+                        su, sp = np.ones(abi.RNCONS), np.ones(mo.RFILL)
+                        if refl[d]:
+                            su[abi.RF + d] = sp[abi.RH + d] = -1.0
+                        cc = [loc[e] if e <= d else mloc[e] for e in range(3)]
+                        rr = [mloc[e] if e == d else cc[e] for e in range(3)]
+                        gr = mo._ratio(detg[cc[1], cc[0]], detg[rr[1], rr[0]]) if conserved else 1.0
+                        q_u = su * gr * q_u if conserved else su * q_u
+                        q_p = sp * gr * q_p if conserved else sp * q_p
+                    U[:, k, j, i] = q_u
+                    P[:mo.RFILL, k, j, i] = q_p
+    return out
+
+
+@pytest.mark.parametrize("ndim", [3, 2])
+@pytest.mark.parametrize("bc_vars", [abi.BC_VARS_PRIMITIVE, abi.BC_VARS_CONSERVED])
+@pytest.mark.parametrize("name", list(CASES))
+def test_rad_face_by_face_equals_composed_maps(name, bc_vars, ndim):
+    """The radiation fields through the oracle's neighbour copy and
+    face-by-face boundary functions equal the composed map the CUDA exchange
+    implements (before ConvertBoundaryConditions' radiation steps)."""
+    from phoebus_gb300.radiation import alloc_rad
+
+    bcs = CASES[name]
+    if bc_vars == abi.BC_VARS_CONSERVED and abi.BC_POLAR in bcs[0] + bcs[1]:
+        pytest.skip("polar boundaries need bc_vars = primitive")
+    mesh, blocks = host_mesh(bcs, 21 + list(CASES).index(name), bc_vars, ndim)
+    rng = np.random.default_rng(5)
+    for b in blocks:
+        alloc_rad(b)
+        b["rcons"][...] = rng.standard_normal(b["rcons"].shape)
+        b["rprim"][...] = rng.standard_normal(b["rprim"].shape)
+    want = rad_closed_form(mesh, blocks)
+    mo._copy_neighbours(mesh, blocks, [("rcons", range(abi.RNCONS)), ("rprim", range(mo.RFILL))])
+    for b, seg in zip(blocks, mesh.segments()):
+        for d, outer, bc in mo._physical_faces(mesh, b, seg):
+            mo._rad_apply_face(b, d, outer, bc, bc_vars)
+    for n, (b, (U, P)) in enumerate(zip(blocks, want)):
+        assert not np.isnan(b["rcons"]).any(), f"block {n}: a ghost no rule filled"
+        np.testing.assert_array_equal(b["rcons"], U, err_msg=f"block {n} rcons")
+        np.testing.assert_array_equal(b["rprim"][:mo.RFILL], P[:mo.RFILL], err_msg=f"block {n} rprim")

@@ -203,6 +203,163 @@ def test_mesh_exchange_matches_oracle(ctx_exact, name, geometry, bc_vars, ndim):
         assert_bitwise(g["fail"], r["fail"], f"block {n} fail")
 
 
+def random_rad_interior(blocks, seed):
+    """Radiation fields on every block (ghosts NaN, so a ghost no rule fills
+    shows up): random J, H_i / J of both signs with |H| / J up to 1.2 (some
+    zones above the inflow check's 0.99 cap), xi, phi, c2pfail, and random
+    conserved moments."""
+    import torch
+
+    from phoebus_gb300.radiation import alloc_rad
+
+    rng = np.random.default_rng(seed)
+    for b in blocks:
+        alloc_rad(b, fill=float("nan"))
+        ks, js, is_ = b.isl()
+        shp = b["rprim"][0][ks, js, is_].shape
+        R = np.zeros((abi.RNPRIM,) + shp)
+        R[abi.RJ] = 10.0 ** rng.uniform(-3.0, 0.0, shp)
+        h = rng.uniform(-1.0, 1.0, (3,) + shp)
+        h *= 1.2 * rng.uniform(0.0, 1.0, shp) ** 0.25 / np.maximum(np.sqrt((h * h).sum(0)), 1e-12)
+        if b.geom is not None:  # covariant components of proper size: times sqrt(gamma_dd)
+            cent = host(b.geom.arrays["cent"])[:, js, is_]
+            for d in range(3):
+                h[d] *= np.sqrt(cent[abi.G_GCOV + (d + 1) * (d + 2) // 2 + d + 1])
+        R[abi.RH:abi.RH + 3] = h
+        R[abi.RXI] = rng.uniform(0.0, 1.0, shp)
+        R[abi.RPHI] = rng.uniform(0.0, 2.0 * np.pi, shp)
+        R[abi.RFAIL] = rng.integers(0, 2, shp).astype(np.float64)
+        U = rng.uniform(-1.0, 1.0, (abi.RNCONS,) + shp)
+        U[abi.RE] = 10.0 ** rng.uniform(-3.0, 0.0, shp)
+        b["rprim"][:, ks, js, is_] = torch.from_numpy(R).to(b["rprim"].device)
+        b["rcons"][:, ks, js, is_] = torch.from_numpy(U).to(b["rcons"].device)
+
+
+def rad_exchange_case(ctx, name, geometry, bc_vars, ndim, method, seed):
+    """A small tiled mesh with fluid and radiation interiors, the fluid
+    exchanged; returns (p, rp, mesh, blocks, host copies before the radiation
+    exchange)."""
+    bcs = MESH_BCS[name]
+    if bc_vars == abi.BC_VARS_CONSERVED and abi.BC_POLAR in bcs[0] + bcs[1]:
+        pytest.skip("polar boundaries need bc_vars = primitive")
+    p = torus.torus_params()
+    rp = abi.default_rad_params(method=method)
+    mesh = small_fmks_mesh(bcs, bc_vars=bc_vars, ndim=ndim)
+    geom = torus.torus_geometry() if geometry == "fmks" else None
+    blocks = mesh.make_blocks("cuda", geom)
+    for b in blocks:
+        if geom is not None:
+            ctx.GeometryFillFMKS(b)
+    random_interior(ctx, p, mesh, blocks, seed=seed)
+    ctx.MeshExchange(p, mesh, blocks)
+    random_rad_interior(blocks, seed + 1)
+    return p, rp, mesh, blocks, [b.to_host() for b in blocks]
+
+
+@pytest.mark.parametrize("method", ["moment_m1", "moment_eddington"])
+@pytest.mark.parametrize("ndim", [3, 2])
+@pytest.mark.parametrize("bc_vars", [abi.BC_VARS_PRIMITIVE, abi.BC_VARS_CONSERVED])
+@pytest.mark.parametrize("name", list(MESH_BCS))
+@pytest.mark.parametrize("geometry", ["fmks", "minkowski"])
+def test_rad_mesh_exchange_matches_oracle(ctx_exact, name, geometry, bc_vars, ndim, method):
+    """Exact build: the radiation fields' exchange (neighbour copies; the
+    boundary functions on every FillGhost radiation field, DetGamma-scaled
+    under bc_vars = conserved, F_d and H_d flipped across reflect faces; on
+    FMKS the outer-X1 cut of incoming radiation flux; with bc_vars = primitive
+    MomentPrim2Con in the physical slabs) equals the oracle's face-by-face
+    restatement bit for bit in every ghost zone."""
+    from oracle.mesh_oracle import RFILL, rad_mesh_exchange
+    from oracle.oracle import RadOracle
+    from phoebus_gb300.radiation import RadiationContext
+
+    seed = 300 + 8 * list(MESH_BCS).index(name) + 4 * bc_vars + 2 * (geometry == "fmks") + (ndim == 2)
+    p, rp, mesh, blocks, before = rad_exchange_case(ctx_exact, name, geometry, bc_vars, ndim, method, seed)
+    rx = RadiationContext(ctx_exact)
+    rx.MeshExchange(rp, p, mesh, blocks)
+    rx.check()
+    rad_mesh_exchange(RadOracle(), rp, p, mesh, before)
+    for n, (g, r) in enumerate(zip(blocks, before)):
+        assert not np.isnan(r["rcons"]).any(), f"block {n}: a ghost no rule filled"
+        assert not np.isnan(r["rprim"][:RFILL]).any(), f"block {n}: a ghost no rule filled"
+        assert_bitwise(g["rcons"], r["rcons"], f"block {n} rcons")
+        assert_bitwise(g["rprim"][:RFILL], r["rprim"][:RFILL], f"block {n} rprim")
+
+
+def test_rad_mesh_exchange_inflow_cut(ctx_exact):
+    """The outer-X1 cut acts: on the torus deck's FMKS mesh, outer-X1 ghosts
+    whose mapped H^1 points into the domain leave the exchange with H^1 = 0
+    (within rounding of gamma^1j H_j) and |H| <= 0.99; the others keep the
+    copied values."""
+    from phoebus_gb300.radiation import RadiationContext
+
+    p, rp, mesh, blocks, _ = rad_exchange_case(ctx_exact, "deck", "fmks", abi.BC_VARS_PRIMITIVE, 3, "moment_m1", 77)
+    rx = RadiationContext(ctx_exact)
+    rx.MeshExchange(rp, p, mesh, blocks)
+    rx.check()
+    cut = kept = 0
+    for (s1, s2, s3), b in zip(mesh.segments(), blocks):
+        if s1 != mesh.nseg[0] - 1:
+            continue
+        ng, n1 = b.ng, b.nx[0]
+        ks, js, _ = b.isl()
+        R = host(b["rprim"])
+        cent = host(b.geom.arrays["cent"])
+        for i in range(ng + n1, 2 * ng + n1):
+            H = R[abi.RH:abi.RH + 3, ks, js, i]
+            src = R[abi.RH:abi.RH + 3, ks, js, ng + n1 - 1]
+            t = cent[:, js, i][:, None, :]
+
+            def flat(a, c):
+                return max(a, c) * (max(a, c) + 1) // 2 + min(a, c)
+
+            gcon = [[t[abi.G_GAMCON + flat(a, c)] for c in range(3)] for a in range(3)]
+            gcov = [[t[abi.G_GCOV + flat(a + 1, c + 1)] for c in range(3)] for a in range(3)]
+            hsrc1 = sum(gcon[0][c] * src[c] for c in range(3))
+            into = hsrc1 < 0
+            h1 = sum(gcon[0][c] * H[c] for c in range(3))
+            hcon = [sum(gcon[a][c] * H[c] for c in range(3)) for a in range(3)]
+            xi = np.sqrt(sum(gcov[a][c] * hcon[a] * hcon[c] for a in range(3) for c in range(3)))
+            assert np.all(np.abs(h1[into]) <= 1e-12 * (1.0 + np.abs(H).max()))
+            assert np.all(xi[into] <= 0.99 * (1 + 1e-12))
+            assert_bitwise(H[:, ~into], src[:, ~into], "outer-X1 ghosts with outgoing H")
+            cut += int(into.sum())
+            kept += int((~into).sum())
+    assert cut > 0 and kept > 0
+
+
+@pytest.mark.parametrize("fixup", [1, 0])
+@pytest.mark.parametrize("ndim", [3, 2])
+@pytest.mark.parametrize("name", list(MESH_BCS))
+def test_rad_fix_fluxes_matches_oracle(ctx_fast, name, ndim, fixup):
+    """FixFluxes' radiation part equals the oracle's restatement bit for bit
+    on random radiation fluxes (every face of every block compared; a no-op
+    with enable_flux_fixup off)."""
+    import torch
+
+    from oracle.mesh_oracle import rad_fix_fluxes
+    from phoebus_gb300.radiation import RadiationContext, alloc_rad
+
+    p = torus.torus_params()
+    p.enable_flux_fixup = fixup
+    rp = abi.default_rad_params()
+    mesh = small_fmks_mesh(MESH_BCS[name], ndim=ndim)
+    blocks = mesh.make_blocks("cuda", None)
+    rng = np.random.default_rng(500 + ndim + 4 * fixup + 8 * list(MESH_BCS).index(name))
+    for b in blocks:
+        alloc_rad(b)
+        b["rflux"].copy_(torch.from_numpy(rng.standard_normal(tuple(b["rflux"].shape))))
+    before = [b.to_host() for b in blocks]
+    rx = RadiationContext(ctx_fast)
+    rx.FixFluxes(rp, p, mesh, blocks)
+    rx.check()
+    rad_fix_fluxes(p, mesh, before)
+    changed = 0
+    for n, (g, r) in enumerate(zip(blocks, before)):
+        assert_bitwise(g["rflux"], r["rflux"], f"block {n} rflux")
+        changed += int((host(g["rflux"]) == 0.0).sum())
+    assert (changed > 0) == (fixup == 1 and name != "deck")
+
+
 def test_conserved_exchange_inflow_fixes_ghosts(ctx_exact):
     """bc_vars = conserved on an FMKS mesh with X1 outflow: interior zones
     next to the outer X1 face given an inward velocity (u^1 < 0) leave
