@@ -569,13 +569,15 @@ __device__ __forceinline__ void recon_weno5z(double q0, double q1, double q2, do
 //    m the smaller, beta_m + tau5 = beta_M, so 1/bp_m = beta_m / beta_M from
 //    the reciprocal above, and 1/bp_M, 1/bp_1 share one reciprocal of
 //    (2 beta_M - beta_m)(beta1 + tau5).  (The reference's + eps on alpha_l,
-//    alpha_r moves alpha_lin only where alpha_lin < 1e-90.)
+//    alpha_r moves alpha_lin only where alpha_lin < 1e-90.)  alpha_lin and
+//    the weights' normalisations 1 / S_l, 1 / S_r come from one reciprocal of
+//    R (S_l + S_r) S_l S_r.
 //  - The MC slope of the blend, mc(q2 - q1, q3 - q2, 2), doubled, on the
 //    integer pipe: the sign test, the minima of magnitudes and the power-of-two
 //    scale act on the bit patterns; the sum dm + dp is the slope b1 = q3 - q1
 //    the smoothness indicator already forms.
-// Four reciprocals (three FP64 instructions each) and 93 FP64 instructions
-// for both face states (measured).  Every intermediate stays in the normal
+// Three reciprocals (three FP64 instructions each) and about 90 FP64
+// instructions for both face states.  Every intermediate stays in the normal
 // range for |q| < 1e50; outside it (checked on the exponents) the reference
 // sequence is used.
 __device__ __forceinline__ void recon_weno5z_fast(double q0, double q1, double q2, double q3, double q4,
@@ -618,16 +620,21 @@ __device__ __forceinline__ void recon_weno5z_fast(double q0, double q1, double q
   const double wr0 = g0 * bp2, wr2 = g2 * bp0;
   const double Sl = wl0 + wl1 + wl2, Sr = wr0 + wl1 + wr2;
   const double SS = Sl * Sr, S2 = Sl + Sr;
-  const int ex = dexp(X);
-  if (ex < 16 || ex > 2030 || dexp(SS) > 2030 || dexp(S2) > 2027) {
+  const int ex = dexp(X), eSS = dexp(SS), eS2 = dexp(S2);
+  // R in [1/2, 3] and S_l, S_r >= 1: R S2 SS lies in [1, 2^1021) below the sum bound
+  if (ex < 16 || ex > 2030 || eSS > 2030 || eS2 > 2027 || eSS + eS2 > 3060) {
     recon_weno5z(q0, q1, q2, q3, q4, ql, qr);
     return;
   }
   const double rx = rcp_nr(X);
   const double R = fma(bm, big2 ? ib2 : ib0, fma(bM, Y1 * rx, beta1 * (X1 * rx)));
-  const double alpha_lin = rcp_nr(R * S2 * (1.0 / 6.0));
-  const double rS = rcp_nr(SS) * (1.0 / 12.0);
-  const double isl = Sr * rS, isr = Sl * rS;  // 1 / (12 S_l), 1 / (12 S_r)
+  // one reciprocal Z = 1 / (R S2 S_l S_r) gives alpha_lin / 4 = 1.5 S_l S_r Z and
+  // the candidates' normalisation with the blend factor folded in:
+  // alpha_lin / (12 S_l) = S_r Z / 2, alpha_lin / (12 S_r) = S_l Z / 2
+  const double Z = rcp_nr(R * S2 * SS);
+  const double aq = (1.5 * SS) * Z;  // alpha_lin / 4
+  const double hZ = 0.5 * Z;
+  const double zl = hZ * Sr, zr = hZ * Sl;
   // 2 mc(q2 - q1, q3 - q2, 2) = copysign(min(|dm + dp|, 4 min(|dm|, |dp|)),
   // dm + dp) where dm dp > 0, else 0 (finite dm, dp: |q| < 1e50 here)
   const long long MAG = 0x7fffffffffffffffLL;
@@ -641,11 +648,12 @@ __device__ __forceinline__ void recon_weno5z_fast(double q0, double q1, double q
   // face) (a0 + 3 b0), (a1 + 3 b1), (a2 - 3 b2); for qr (lower face, the
   // mirrored stencils) (a2 + 3 b2), (a1 - 3 b1), (a0 - 3 b0); the weights sum
   // to one, so sum_k w_k c_k = q2 + sum_k w_k (c_k - q2).  Then the blend
-  // alpha q + (1 - alpha) p with p = q2 +- dq2 / 4 as p + alpha (q - p).
-  const double xl = (wl0 * fma(3.0, b0, a0) + wl1 * fma(3.0, b1, a1) + wl2 * fma(-3.0, b2, a2)) * isl;
-  const double xr = (wr0 * fma(3.0, b2, a2) + wl1 * fma(-3.0, b1, a1) + wr2 * fma(-3.0, b0, a0)) * isr;
-  ql = fma(alpha_lin, fma(-0.25, dq2, xl), fma(0.25, dq2, q2));
-  qr = fma(alpha_lin, fma(0.25, dq2, xr), fma(-0.25, dq2, q2));
+  // alpha q + (1 - alpha) p with p = q2 +- dq2 / 4 as p -+ (alpha / 4) dq2 +
+  // alpha (q - q2), alpha (q - q2) = (sum_k w_k (a_k +- 3 b_k)) alpha / (12 S).
+  const double sl = wl0 * fma(3.0, b0, a0) + wl1 * fma(3.0, b1, a1) + wl2 * fma(-3.0, b2, a2);
+  const double sr = wr0 * fma(3.0, b2, a2) + wl1 * fma(-3.0, b1, a1) + wr2 * fma(-3.0, b0, a0);
+  ql = fma(sl, zl, fma(-aq, dq2, fma(0.25, dq2, q2)));
+  qr = fma(sr, zr, fma(aq, dq2, fma(-0.25, dq2, q2)));
 }
 
 __device__ __forceinline__ double minmod(double a, double b) {
